@@ -1,0 +1,100 @@
+/*
+ * ks.h -- C ABI of the GB300-native single-level incompressible advance.
+ *
+ * One handle owns one uniform single-box grid, its device fields and one CUDA
+ * stream.  Calls on a handle are single-threaded (the handle is not
+ * re-entrant); different handles are independent.  No C++ exception crosses
+ * this boundary: every entry point returns a ks_status (0 on success).
+ *
+ * Each entry point replaces one member of the reference's incflo operator
+ * surface (paths inside the Kynema-SGF repository):
+ *   ks_create / ks_destroy     incflo::incflo(), ReadParameters, init_mesh     src/incflo.cpp:43-61, src/setup/init.cpp:48-96
+ *   ks_init_data               incflo::InitData (initial projection + pressure iterations)  src/incflo.cpp:218-228, src/setup/init.cpp:104-225
+ *   ks_compute_dt              incflo::compute_dt + SimTime::set_current_cfl  src/incflo_compute_dt.cpp:33-221, src/core/SimTime.cpp:162-291
+ *   ks_pre_advance             pre_advance_stage1 + pre_advance_stage2 (ABL, actuators)  src/incflo_advance.cpp:15-32
+ *   ks_prepare_time_step       incflo::prepare_time_step (New -> Old)          src/incflo_advance.cpp:34-44
+ *   ks_advance                 incflo::advance(fixed_point_iteration)          src/incflo_advance.cpp:63-79
+ *   ks_apply_predictor         incflo::ApplyPredictor                          src/incflo_advance.cpp:186-438
+ *   ks_apply_corrector         incflo::ApplyCorrector (MOL only)               src/incflo_advance.cpp:528-652
+ *   ks_apply_projection        incflo::ApplyProjection                         src/projection/incflo_apply_nodal_projection.cpp:149-465
+ *   ks_evolve                  incflo::Evolve time loop                        src/incflo.cpp:338-411
+ *   ks_set_field / ks_get_field  FieldRepo field access by name              src/core/FieldRepo.H:139-173
+ *   ks_last_solver_stats       io::print_mlmg_info                            src/utilities/console_io.cpp:178-186
+ *
+ * Deck: ParmParse text ("prefix.key = values" lines), the reference's keys.
+ * Field exchange: valid region only, structure of arrays, x fastest, then y,
+ * then z, then component (AMReX Array4 order, no ghost cells).  Cell fields
+ * hold nx*ny*nz points per component; the node field "p" has one more point
+ * along a wall-bounded z; face fields u_mac/v_mac/w_mac have one more point
+ * along their normal direction.
+ */
+#ifndef KS_H
+#define KS_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum ks_status {
+    KS_OK = 0,
+    KS_ERR_DECK = 1,            /* invalid or missing deck value */
+    KS_ERR_UNSUPPORTED = 2,     /* valid reference option outside this path */
+    KS_ERR_NOT_CONVERGED = 3,   /* multigrid hit maxiter (only when abort-on-fail is on) */
+    KS_ERR_NONFINITE = 4,       /* NaN/Inf detected, or dt below time.min_dt */
+    KS_ERR_OOM = 5,             /* device allocation failed */
+    KS_ERR_ARG = 6,             /* bad handle, name, pointer or size */
+    KS_DONE = 7,                /* time loop finished (max_step / stop_time) */
+    KS_ERR_CUDA = 8             /* CUDA runtime error */
+} ks_status;
+
+typedef enum ks_precision { KS_FP64 = 0, KS_MIXED = 1 } ks_precision;
+
+typedef enum ks_memory { KS_HOST = 0, KS_DEVICE = 1 } ks_memory;
+
+typedef struct ks_handle ks_handle;
+
+typedef struct ks_mg_stats {
+    int mac_iterations;
+    double mac_initial_residual;
+    double mac_final_residual;
+    int nodal_iterations;
+    double nodal_initial_residual;
+    double nodal_final_residual;
+} ks_mg_stats;
+
+typedef struct ks_layout {
+    int ncomp;
+    int nx, ny, nz;   /* points per component along x, y, z */
+} ks_layout;
+
+int ks_create(const char* deck_text, ks_handle** out);
+void ks_destroy(ks_handle* h);
+const char* ks_last_error(const ks_handle* h);
+
+int ks_init_data(ks_handle* h);
+int ks_compute_dt(ks_handle* h, double* dt);
+int ks_pre_advance(ks_handle* h);
+int ks_prepare_time_step(ks_handle* h);
+int ks_advance(ks_handle* h, int fixed_point_iteration);
+int ks_apply_predictor(ks_handle* h, int incremental_projection, int fixed_point_iteration);
+int ks_apply_corrector(ks_handle* h);
+int ks_apply_projection(ks_handle* h, double time, double scaling_factor, int incremental);
+int ks_evolve(ks_handle* h, int nsteps);
+int ks_step(ks_handle* h);
+
+int ks_field_layout(ks_handle* h, const char* name, ks_layout* layout);
+int ks_get_field(ks_handle* h, const char* name, void* dst, ks_memory where);
+int ks_set_field(ks_handle* h, const char* name, const void* src, ks_memory where);
+int ks_get_scalar(ks_handle* h, const char* name, double* value);
+int ks_last_solver_stats(const ks_handle* h, ks_mg_stats* stats);
+int ks_set_precision(ks_handle* h, int precision);
+int ks_synchronize(ks_handle* h);
+int ks_kernel_launches(const ks_handle* h, long long* count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KS_H */

@@ -1,0 +1,87 @@
+// Shared device definitions: grid descriptor, index maps with periodic wrap,
+// boundary-condition accessors and kernel declarations.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+namespace ks {
+
+enum ZBC { ZPER = 0, ZSLIP = 1, ZWALLMODEL = 2 };
+
+constexpr double kSmallVel = 1.0e-8;  // AMReX-Hydro small_vel
+
+// Uniform single-box grid.  x and y are periodic; z is periodic (zper = 1) or
+// bounded by a slip wall / wall-model wall at each end.
+struct Grid {
+    int nx, ny, nz;
+    int zper;
+    int zlo, zhi;
+    double dx, dy, dz;
+    long long N;    // cells
+    long long NFz;  // z faces stored: nx*ny*(nz+1)
+};
+
+__host__ __device__ inline long long cidx(const Grid& g, int i, int j, int k) {
+    return ((long long)k * g.ny + j) * g.nx + i;
+}
+__host__ __device__ inline int wrapn(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+__host__ __device__ inline double hd(const Grid& g, int d) { return d == 0 ? g.dx : (d == 1 ? g.dy : g.dz); }
+__host__ __device__ inline int nd(const Grid& g, int d) { return d == 0 ? g.nx : (d == 1 ? g.ny : g.nz); }
+__host__ __device__ inline int nzfaces(const Grid& g) { return g.zper ? g.nz : g.nz + 1; }
+
+// Face arrays: x and y faces use the cell index of the cell on their high
+// side (N entries, periodic); z faces use nx*ny*(nz+1) storage with layer k
+// at k-1/2 (walls) or wrap into [0,nz) (periodic).
+__host__ __device__ inline long long fidx(const Grid& g, int d, int i, int j, int k) {
+    i = wrapn(i, g.nx);
+    j = wrapn(j, g.ny);
+    if (d != 2 || g.zper) k = wrapn(k, g.nz);
+    return cidx(g, i, j, k);
+}
+
+// Cell-centred velocity (or rho*velocity) with fill-patch ghost values:
+// periodic wrap in x, y (and z); at walls the tangential components take the
+// high-order extrapolation to the face, (15 q0 - 10 q1 + 3 q2)/8, in every
+// ghost layer and the normal component is 0.
+struct VelFP {
+    const double* v;
+    Grid g;
+    double scale;
+    __device__ inline double operator()(int n, int i, int j, int k) const {
+        i = wrapn(i, g.nx);
+        j = wrapn(j, g.ny);
+        const long long N = g.N;
+        const double* c = v + n * N;
+        if (g.zper) return scale * c[cidx(g, i, j, wrapn(k, g.nz))];
+        if (k < 0) {
+            if (n == 2) return 0.0;
+            return scale * 0.125 * (15.0 * c[cidx(g, i, j, 0)] - 10.0 * c[cidx(g, i, j, 1)] + 3.0 * c[cidx(g, i, j, 2)]);
+        }
+        if (k >= g.nz) {
+            if (n == 2) return 0.0;
+            const int t = g.nz - 1;
+            return scale * 0.125 * (15.0 * c[cidx(g, i, j, t)] - 10.0 * c[cidx(g, i, j, t - 1)] + 3.0 * c[cidx(g, i, j, t - 2)]);
+        }
+        return scale * c[cidx(g, i, j, k)];
+    }
+};
+
+// Cell field with first-order extrapolation ghosts in z (forces, viscosity).
+struct CellFO {
+    const double* v;
+    Grid g;
+    __device__ inline double operator()(int n, int i, int j, int k) const {
+        i = wrapn(i, g.nx);
+        j = wrapn(j, g.ny);
+        if (g.zper) k = wrapn(k, g.nz);
+        else k = k < 0 ? 0 : (k >= g.nz ? g.nz - 1 : k);
+        return v[n * g.N + cidx(g, i, j, k)];
+    }
+};
+
+inline unsigned nblocks(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
+
+}  // namespace ks

@@ -1,0 +1,1112 @@
+// Host driver of the GB300-native advance and its C ABI (include/ks.h).
+//
+// Owns the deck, SimTime, the device fields of one single-box grid and one
+// CUDA stream; sequences the device passes in the order of the reference's
+// incflo::advance (src/incflo_advance.cpp:63-438) and ApplyProjection
+// (src/projection/incflo_apply_nodal_projection.cpp:149-465).  Every device
+// pass is a hand-written kernel in ks_kernels.cu, ks_godunov.cu or ks_mg.cu;
+// the host only computes scalars (dt, u_tau, disk forces) and launches.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/ks.h"
+#include "ks_launch.hpp"
+
+namespace ks {
+
+struct KsError : std::runtime_error {
+    int code;
+    KsError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+static void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) {
+        const int code = (e == cudaErrorMemoryAllocation) ? KS_ERR_OOM : KS_ERR_CUDA;
+        throw KsError(code, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
+static std::string lc(std::string s) {
+    for (auto& c : s) c = (char)std::tolower((unsigned char)c);
+    return s;
+}
+
+// ---------------------------------------------------------------- deck
+// ParmParse-style input: "prefix.key = v1 v2 ...", '#' starts a comment.
+class Deck {
+   public:
+    explicit Deck(const std::string& text) {
+        std::istringstream in(text);
+        std::string ln;
+        while (std::getline(in, ln)) {
+            const auto hash = ln.find('#');
+            if (hash != std::string::npos) ln.resize(hash);
+            const auto eq = ln.find('=');
+            if (eq == std::string::npos) continue;
+            std::string k = trim(ln.substr(0, eq));
+            std::istringstream vs(ln.substr(eq + 1));
+            std::vector<std::string> v;
+            for (std::string w; vs >> w;) {
+                if (w.size() >= 2 && (w[0] == '"' || w[0] == '\'')) w = w.substr(1, w.size() - 2);
+                v.push_back(w);
+            }
+            if (!k.empty()) kv_[k] = v;
+        }
+    }
+    bool has(const std::string& k) const { return kv_.count(k) > 0; }
+    std::vector<std::string> strs(const std::string& k) const {
+        auto it = kv_.find(k);
+        return it == kv_.end() ? std::vector<std::string>{} : it->second;
+    }
+    std::string str(const std::string& k, const std::string& def) const {
+        auto v = strs(k);
+        return v.empty() ? def : v[0];
+    }
+    double num(const std::string& k, double def) const {
+        auto v = strs(k);
+        return v.empty() ? def : std::stod(v[0]);
+    }
+    int flag(const std::string& k, int def) const {
+        auto v = strs(k);
+        if (v.empty()) return def;
+        if (v[0] == "true") return 1;
+        if (v[0] == "false") return 0;
+        return std::stoi(v[0]);
+    }
+    std::vector<double> nums(const std::string& k) const {
+        auto it = kv_.find(k);
+        if (it == kv_.end()) throw KsError(KS_ERR_DECK, "missing deck key " + k);
+        std::vector<double> r;
+        for (auto& s : it->second) r.push_back(std::stod(s));
+        return r;
+    }
+
+   private:
+    static std::string trim(std::string s) {
+        const auto a = s.find_first_not_of(" \t\r");
+        if (a == std::string::npos) return "";
+        const auto b = s.find_last_not_of(" \t\r");
+        return s.substr(a, b - a + 1);
+    }
+    std::map<std::string, std::vector<std::string>> kv_;
+};
+
+// ---------------------------------------------------------------- SimTime
+// src/core/SimTime.cpp:11-324 semantics for the keys on this path.
+struct Clock {
+    double cur = 0, next = 0, dt[3] = {-1, -1, -1};
+    double cfl = 1, fixed_dt = -1, init_dt = -1, max_dt = -1, min_dt = -1, shrink = 0.1, growth = 0.1, stop = -1;
+    int max_step = -1, step = 0;
+    bool adaptive = false, init = true, force_cfl = true;
+    double cur_cfl = 0, conv_cfl = 0, diff_cfl = 0, src_cfl = 0;
+
+    void set_cfl(double conv, double diff, double src) {
+        const double eps = 2.220446049250313e-16;
+        const double cd = conv + diff;
+        const double unit = cd + std::sqrt(cd * cd + 4.0 * src);
+        bool use_init = false;
+        if (adaptive && !init && unit < eps) {
+            if (cur < eps && init_dt > 0) use_init = true;
+            else throw KsError(KS_ERR_NONFINITE, "CFL is below machine epsilon and the time step is adaptive");
+        }
+        double d = use_init ? init_dt : 2.0 * cfl / std::max(unit, eps);
+        if (init) d *= shrink;
+        if (dt[0] > 0 && adaptive) d = std::min(d, (1.0 + growth) * dt[0]);
+        if (adaptive) {
+            if (max_dt > 0) d = std::min(d, max_dt);
+            if (min_dt > 0 && d < min_dt) throw KsError(KS_ERR_NONFINITE, "adaptive dt fell below time.min_dt");
+            if (stop > 0 && cur + d > stop) d = stop - cur;
+            if (init && init_dt > 0) d = std::min(d, init_dt);
+            dt[0] = d;
+        } else {
+            dt[0] = fixed_dt;
+        }
+        cur_cfl = 0.5 * unit * dt[0];
+        conv_cfl = conv * dt[0];
+        diff_cfl = diff * dt[0];
+        src_cfl = std::sqrt(src) * dt[0];
+    }
+    bool keep_going() const {
+        if (max_step >= 0 && step >= max_step) return false;
+        if (stop > 0 && next >= stop - 2.220446049250313e-12) return false;
+        return true;
+    }
+    bool new_step() {
+        const bool go = keep_going();
+        init = false;
+        if (go) {
+            dt[2] = dt[1];
+            dt[1] = dt[0];
+            ++step;
+            cur = next;
+        }
+        return go;
+    }
+};
+
+struct Disk {
+    double center[3], normal[3], cvec[3];
+    double D, eps, to_sample, dr;
+    std::vector<double> ct, ws;
+    int nr, nt;
+    bool about_center;
+    double ct_now = 0, uinf2 = 0, ref[3] = {0, 0, 0};
+};
+
+struct MGParams {
+    double rtol = 1.0e5 * 2.220446049250313e-16, atol = 1.0e2 * 2.220446049250313e-16;
+    int maxiter = 200, nu1 = 2, nu2 = 2, bottom = 100;
+    double omega = 0.9;
+};
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    void alloc(size_t count) {
+        n = count;
+        ck(cudaMalloc(&p, std::max<size_t>(1, count) * sizeof(T)), "cudaMalloc");
+        ck(cudaMemset(p, 0, std::max<size_t>(1, count) * sizeof(T)), "cudaMemset");
+    }
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+};
+
+// ---------------------------------------------------------------- simulation
+class Sim {
+   public:
+    explicit Sim(const std::string& text);
+    ~Sim();
+
+    void init_data();
+    void compute_dt();
+    void pre_advance();
+    void prepare_time_step();
+    void apply_predictor(bool incremental);
+    void apply_projection(double time, double scaling, bool incremental);
+    int step();
+
+    double scalar(const std::string& name);
+    void layout(const std::string& name, ks_layout& L);
+    void get(const std::string& name, void* dst, int where);
+    void set(const std::string& name, const void* src, int where);
+    void sync() { ck(cudaStreamSynchronize(ctx_.stream), "stream synchronize"); }
+
+    Ctx ctx_;
+    Grid g_{};
+    Clock t_;
+    int mac_it_ = 0, nod_it_ = 0;
+    double mac_r0_ = 0, mac_r_ = 0, nod_r0_ = 0, nod_r_ = 0;
+    std::string err_;
+
+   private:
+    void setup(const Deck& D);
+    void alloc();
+    void init_fields(const Deck& D);
+    void abl_update();
+    void actuator_update();
+    void mac_project();
+    double reduce(int np, int ncomp, int op_max, double* host);
+    void cc_vcycle(size_t l);
+    void nd_vcycle(size_t l, double sigma);
+    double* field(const std::string& name, int& ncomp, int& kind);
+
+    double plo_[3], phi_[3];
+    double rho_ = 1, mu_ = 0;
+    Scalars S_{};
+    bool wallmodel_ = false;
+    int shear_ = 0;
+    double kappa_ = 0.41, z0_ = 0.1, zref_ = 0, utau_ = 0, um_[2] = {0, 0}, vmag_ = 0;
+    std::vector<Disk> disks_;
+    MGParams mac_, nod_;
+    int initial_proj_ = 1, initial_iters_ = 3;
+
+    DevBuf<double> vel_, vel_old_, vel_tmp_, gp_, p_, src_, forces_, mueff_, divtau_, conv_, act_, wg_;
+    DevBuf<double> umac_[3];
+    DevBuf<double> gbuf_;
+    GodunovBufs gb_{};
+    std::vector<CCLevelDev> cc_;
+    std::vector<NDLevelDev> nd_;
+    DevBuf<double> mgbuf_;
+    DevBuf<double> parts_, red_;
+    DevBuf<double> pts_, samp_;
+    double* hred_ = nullptr;  // pinned
+};
+
+Sim::Sim(const std::string& text) {
+    Deck D(text);
+    setup(D);
+    ck(cudaStreamCreateWithFlags(&ctx_.stream, cudaStreamNonBlocking), "stream create");
+    ck(cudaMallocHost(&hred_, 64 * sizeof(double)), "pinned alloc");
+    alloc();
+    init_fields(D);
+    sync();
+}
+
+Sim::~Sim() {
+    if (ctx_.stream) cudaStreamSynchronize(ctx_.stream);
+    if (hred_) cudaFreeHost(hred_);
+    if (ctx_.stream) cudaStreamDestroy(ctx_.stream);
+}
+
+void Sim::setup(const Deck& D) {
+    std::vector<double> nc, lo, hi, per;
+    nc = D.nums("amr.n_cell");
+    lo = D.nums("geometry.prob_lo");
+    hi = D.nums("geometry.prob_hi");
+    per = D.nums("geometry.is_periodic");
+    if (nc.size() < 3 || lo.size() < 3 || hi.size() < 3 || per.size() < 3) throw KsError(KS_ERR_DECK, "geometry needs 3 values");
+    if (D.flag("amr.max_level", 0) != 0) throw KsError(KS_ERR_UNSUPPORTED, "single level only (amr.max_level = 0)");
+    for (int d = 0; d < 3; ++d) {
+        plo_[d] = lo[d];
+        phi_[d] = hi[d];
+    }
+    g_.nx = (int)nc[0];
+    g_.ny = (int)nc[1];
+    g_.nz = (int)nc[2];
+    g_.dx = (hi[0] - lo[0]) / g_.nx;
+    g_.dy = (hi[1] - lo[1]) / g_.ny;
+    g_.dz = (hi[2] - lo[2]) / g_.nz;
+    if (per[0] == 0 || per[1] == 0) throw KsError(KS_ERR_UNSUPPORTED, "x and y must be periodic");
+    g_.zper = per[2] != 0;
+    g_.zlo = g_.zhi = ZPER;
+    if (!g_.zper) {
+        auto bc = [&](const char* key) {
+            const std::string s = lc(D.str(key, ""));
+            if (s == "slip_wall") return (int)ZSLIP;
+            if (s == "wall_model") return (int)ZWALLMODEL;
+            throw KsError(KS_ERR_UNSUPPORTED, std::string(key) + " = " + s + " is outside this path");
+        };
+        g_.zlo = bc("zlo.type");
+        g_.zhi = bc("zhi.type");
+        if (g_.zhi == ZWALLMODEL) throw KsError(KS_ERR_DECK, "ABL wall models are not applicable to a zhi BC");
+        if (g_.nz < 4) throw KsError(KS_ERR_UNSUPPORTED, "wall-bounded z needs at least 4 cells");
+    }
+    if (g_.nx % 2 || g_.ny % 2 || g_.nz % 2 || g_.nx < 4 || g_.ny < 4 || g_.nz < 4)
+        throw KsError(KS_ERR_UNSUPPORTED, "cell counts must be even and at least 4");
+    g_.N = (long long)g_.nx * g_.ny * g_.nz;
+    g_.NFz = (long long)g_.nx * g_.ny * (g_.nz + 1);
+    wallmodel_ = (g_.zlo == ZWALLMODEL);
+
+    rho_ = D.num("incflo.density", 1.0);
+    mu_ = D.num("transport.viscosity", 0.0);
+    if (D.flag("incflo.use_godunov", 1) != 1) throw KsError(KS_ERR_UNSUPPORTED, "the MOL scheme is outside this path");
+    if (lc(D.str("incflo.godunov_type", "weno_z")) != "ppm") throw KsError(KS_ERR_UNSUPPORTED, "incflo.godunov_type must be ppm");
+    if (D.flag("incflo.diffusion_type", 1) != 0) throw KsError(KS_ERR_UNSUPPORTED, "only explicit diffusion (incflo.diffusion_type = 0)");
+    if (D.flag("incflo.godunov_use_forces_in_trans", 0) != 0) throw KsError(KS_ERR_UNSUPPORTED, "godunov_use_forces_in_trans");
+    if (D.flag("incflo.icns_conserv", 1) != 1) throw KsError(KS_ERR_UNSUPPORTED, "non-conservative momentum form");
+    initial_proj_ = D.flag("incflo.do_initial_proj", 1);
+    initial_iters_ = D.flag("incflo.initial_iterations", 3);
+    const std::string tm = lc(D.str("turbulence.model", "laminar"));
+    if (tm != "laminar" && tm != "smagorinsky") throw KsError(KS_ERR_UNSUPPORTED, "turbulence.model = " + tm);
+    S_.rho = rho_;
+    S_.mu = mu_;
+    S_.smag = tm == "smagorinsky";
+    const double Cs = D.num("Smagorinsky_coeffs.Cs", 0.135);
+    const double ds = std::cbrt(g_.dx * g_.dy * g_.dz);
+    S_.smag_fac = Cs * Cs * ds * ds;
+
+    for (auto& s : D.strs("ICNS.source_terms")) {
+        if (s == "GeostrophicForcing") S_.geo = 1;
+        else if (s == "CoriolisForcing") S_.cor = 1;
+        else if (s == "BodyForce") S_.body = 1;
+        else if (s == "ActuatorForcing") S_.act = 1;
+        else throw KsError(KS_ERR_UNSUPPORTED, "momentum source " + s);
+    }
+    const double pi = 3.14159265358979323846;
+    const double period = D.num("CoriolisForcing.rotational_time_period", 86164.091);
+    const double lat = (S_.geo || S_.cor) ? D.nums("CoriolisForcing.latitude").at(0) * pi / 180.0 : 0.5 * pi;
+    const double omega = 2 * pi / period;
+    S_.sinphi = std::sin(lat);
+    S_.cosphi = std::cos(lat);
+    S_.corfac = 2 * omega;
+    S_.hfac = D.flag("CoriolisForcing.is_horizontal", 0) ? 0.0 : 1.0;
+    double e[3] = {1, 0, 0}, n[3] = {0, 1, 0};
+    if (D.has("CoriolisForcing.east_vector")) { auto v = D.nums("CoriolisForcing.east_vector"); for (int d = 0; d < 3; ++d) e[d] = v.at(d); }
+    if (D.has("CoriolisForcing.north_vector")) { auto v = D.nums("CoriolisForcing.north_vector"); for (int d = 0; d < 3; ++d) n[d] = v.at(d); }
+    auto unit = [](double* v) { const double m = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); for (int d = 0; d < 3; ++d) v[d] /= m; };
+    unit(e);
+    unit(n);
+    for (int d = 0; d < 3; ++d) { S_.east[d] = e[d]; S_.north[d] = n[d]; }
+    S_.up[0] = e[1] * n[2] - e[2] * n[1];
+    S_.up[1] = e[2] * n[0] - e[0] * n[2];
+    S_.up[2] = e[0] * n[1] - e[1] * n[0];
+    if (S_.geo) {
+        auto w = D.nums("GeostrophicForcing.geostrophic_wind");
+        const double cf = 2 * omega * S_.sinphi;
+        S_.gf[0] = -cf * w.at(1);
+        S_.gf[1] = cf * w.at(0);
+        S_.gf[2] = 0.0;
+    }
+    if (S_.body) {
+        if (lc(D.str("BodyForce.type", "constant")) != "constant") throw KsError(KS_ERR_UNSUPPORTED, "BodyForce.type");
+        auto m = D.nums("BodyForce.magnitude");
+        for (int d = 0; d < 3; ++d) S_.body_force[d] = m.at(d);
+    }
+    kappa_ = D.num("ABL.kappa", 0.41);
+    z0_ = D.num("ABL.surface_roughness_z0", 0.1);
+    const std::string st = lc(D.str("ABL.wall_shear_stress_type", "moeng"));
+    if (st == "moeng") shear_ = 0;
+    else if (st == "constant") shear_ = 1;
+    else if (st == "local") shear_ = 2;
+    else if (st == "schumann") shear_ = 3;
+    else throw KsError(KS_ERR_UNSUPPORTED, "ABL.wall_shear_stress_type = " + st);
+    zref_ = D.has("ABL.log_law_height") ? D.num("ABL.log_law_height", 0) : 0.5 * g_.dz;
+    if (wallmodel_ && std::fabs(zref_ - 0.5 * g_.dz) > 1e-12 * g_.dz)
+        throw KsError(KS_ERR_UNSUPPORTED, "ABL.log_law_height other than the first cell centre");
+
+    auto mg = [&](MGParams& m, const std::string& p) {
+        m.rtol = D.num(p + ".mg_rtol", m.rtol);
+        m.atol = D.num(p + ".mg_atol", m.atol);
+        m.maxiter = D.flag(p + ".maxiter", m.maxiter);
+        m.nu1 = D.flag(p + ".num_pre_smooth", m.nu1);
+        m.nu2 = D.flag(p + ".num_post_smooth", m.nu2);
+    };
+    mg(mac_, "mac_proj");
+    mg(nod_, "nodal_proj");
+
+    t_.stop = D.num("time.stop_time", -1);
+    t_.max_step = D.flag("time.max_step", -1);
+    t_.fixed_dt = D.num("time.fixed_dt", -1);
+    t_.init_dt = D.num("time.initial_dt", -1);
+    t_.max_dt = D.num("time.max_dt", -1);
+    t_.min_dt = D.num("time.min_dt", -1);
+    t_.shrink = D.num("time.init_shrink", 0.1);
+    t_.growth = D.num("time.max_dt_growth", 0.1);
+    t_.cfl = D.num("time.cfl", 1.0);
+    t_.force_cfl = D.flag("time.use_force_cfl", 1) != 0;
+    if (t_.fixed_dt > 0) t_.dt[0] = t_.fixed_dt;
+    else t_.adaptive = true;
+    if (t_.cfl > 1.0) throw KsError(KS_ERR_DECK, "We currently require cfl <= 1.0 when using the Godunov advection scheme");
+
+    // Actuator disks (src/wind_energy/actuator/disk/disk_ops.cpp:182-276,
+    // uniform_ct_ops.cpp:53-88)
+    if (S_.act) {
+        for (auto& lab : D.strs("Actuator.labels")) {
+            const std::string type = D.str("Actuator." + lab + ".type", D.str("Actuator.type", ""));
+            if (type != "UniformCtDisk") throw KsError(KS_ERR_UNSUPPORTED, "actuator type " + type);
+            auto key = [&](const std::string& k) {
+                const std::string a = "Actuator." + lab + "." + k;
+                return D.has(a) ? a : "Actuator." + type + "." + k;
+            };
+            Disk d{};
+            d.D = D.num(key("rotor_diameter"), 0);
+            d.eps = D.num(key("epsilon"), 0);
+            if (d.D <= 0 || d.eps <= 0) throw KsError(KS_ERR_DECK, "actuator rotor_diameter and epsilon are required");
+            d.ct = D.nums(key("thrust_coeff"));
+            if (D.has(key("wind_speed"))) d.ws = D.nums(key("wind_speed"));
+            if (d.ct.size() == 1) d.ws = {1.0};
+            if (d.ws.size() != d.ct.size()) throw KsError(KS_ERR_DECK, "wind_speed and thrust_coeff must have the same number of values");
+            d.nr = D.flag(key("num_points_r"), 1);
+            d.nt = D.flag(key("num_points_t"), 1);
+            if (d.nr < 1 || d.nt < 1) throw KsError(KS_ERR_DECK, "num_points_r and num_points_t must both be >=1");
+            if (lc(D.str(key("spreading_type"), "LinearBasis")) != "uniformgaussian")
+                throw KsError(KS_ERR_UNSUPPORTED, "only spreading_type = UniformGaussian");
+            for (int m = 0; m < 3; ++m) { d.center[m] = 0; d.normal[m] = S_.north[m]; }
+            if (D.has(key("disk_center"))) {
+                auto c = D.nums(key("disk_center"));
+                for (int m = 0; m < 3; ++m) d.center[m] = c.at(m);
+            } else if (D.has(key("base_position"))) {
+                auto b = D.nums(key("base_position"));
+                for (int m = 0; m < 3; ++m) d.center[m] = b.at(m);
+                d.center[2] += D.num(key("hub_height"), 0);
+            }
+            if (D.has(key("disk_normal"))) {
+                auto v = D.nums(key("disk_normal"));
+                for (int m = 0; m < 3; ++m) d.normal[m] = v.at(m);
+            }
+            unit(d.normal);
+            if (d.normal[0] * d.normal[0] + d.normal[1] * d.normal[1] < 1e-28)
+                throw KsError(KS_ERR_DECK, "A constant Ct disk normal is too close to vertical.");
+            d.cvec[0] = -d.normal[1];
+            d.cvec[1] = d.normal[0];
+            d.cvec[2] = 0.0;
+            unit(d.cvec);
+            d.to_sample = D.num(key("diameters_to_sample"), 0.0);
+            d.about_center = D.flag(key("ks_spread_about_center"), 0) != 0;
+            d.dr = 0.5 * d.D / d.nr;
+            d.ct_now = d.ct[0];
+            disks_.push_back(d);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- allocation
+void Sim::alloc() {
+    const size_t N = (size_t)g_.N, NF = (size_t)g_.NFz;
+    vel_.alloc(3 * N);
+    vel_old_.alloc(3 * N);
+    vel_tmp_.alloc(3 * N);
+    gp_.alloc(3 * N);
+    p_.alloc((size_t)g_.nx * g_.ny * (g_.zper ? g_.nz : g_.nz + 1));
+    src_.alloc(3 * N);
+    forces_.alloc(3 * N);
+    mueff_.alloc(N);
+    divtau_.alloc(3 * N);
+    conv_.alloc(3 * N);
+    act_.alloc(S_.act ? 3 * N : 3);
+    wg_.alloc(2 * (size_t)g_.nx * g_.ny);
+    umac_[0].alloc(N);
+    umac_[1].alloc(N);
+    umac_[2].alloc(NF);
+    // Godunov scratch: ad[3], edge[3][3], tr[6 pairs][3], flux[3][3]
+    const size_t fsz[3] = {N, N, NF};
+    size_t total = 0;
+    for (int d = 0; d < 3; ++d) total += fsz[d] * (1 + 3 + 3);  // ad, edge, flux
+    for (int a = 0; a < 3; ++a) total += 2 * 3 * fsz[a];        // tr[a][b][n], b != a
+    gbuf_.alloc(total);
+    double* q = gbuf_.p;
+    for (int d = 0; d < 3; ++d) {
+        gb_.ad[d] = q; q += fsz[d];
+        for (int n = 0; n < 3; ++n) { gb_.edge[d][n] = q; q += fsz[d]; }
+        for (int n = 0; n < 3; ++n) { gb_.flux[d][n] = q; q += fsz[d]; }
+    }
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            if (a == b) continue;
+            for (int n = 0; n < 3; ++n) { gb_.tr[a][b][n] = q; q += fsz[a]; }
+        }
+    // multigrid hierarchies
+    std::vector<std::array<int, 3>> dims;
+    int n3[3] = {g_.nx, g_.ny, g_.nz};
+    while (true) {
+        dims.push_back({n3[0], n3[1], n3[2]});
+        bool can = true;
+        for (int d = 0; d < 3; ++d) can = can && (n3[d] % 4 == 0);
+        if (!can) break;
+        for (int d = 0; d < 3; ++d) n3[d] /= 2;
+    }
+    size_t mgtot = 0;
+    for (auto& dm : dims) {
+        const size_t nc = (size_t)dm[0] * dm[1] * dm[2];
+        const size_t nn = (size_t)dm[0] * dm[1] * (dm[2] + (g_.zper ? 0 : 1));
+        mgtot += 3 * nc + 4 * nn;
+    }
+    mgbuf_.alloc(mgtot);
+    q = mgbuf_.p;
+    double h[3] = {g_.dx, g_.dy, g_.dz};
+    for (auto& dm : dims) {
+        CCLevelDev C{};
+        C.nx = dm[0]; C.ny = dm[1]; C.nz = dm[2]; C.zper = g_.zper;
+        C.ix2 = 1.0 / (h[0] * h[0]); C.iy2 = 1.0 / (h[1] * h[1]); C.iz2 = 1.0 / (h[2] * h[2]);
+        const size_t nc = (size_t)dm[0] * dm[1] * dm[2];
+        C.phi = q; q += nc; C.rhs = q; q += nc; C.res = q; q += nc;
+        cc_.push_back(C);
+        NDLevelDev Nd{};
+        Nd.nx = dm[0]; Nd.ny = dm[1]; Nd.nz = dm[2] + (g_.zper ? 0 : 1); Nd.zper = g_.zper;
+        const double mu1[3] = {1.0 / 6.0, 2.0 / 3.0, 1.0 / 6.0};
+        double sg[3][3];
+        for (int d = 0; d < 3; ++d) {
+            const double i2 = 1.0 / (h[d] * h[d]);
+            sg[d][0] = -i2; sg[d][1] = 2.0 * i2; sg[d][2] = -i2;
+        }
+        for (int c = 0; c < 3; ++c)
+            for (int b = 0; b < 3; ++b)
+                for (int a = 0; a < 3; ++a)
+                    Nd.W[(c * 3 + b) * 3 + a] = -(sg[0][a] * mu1[b] * mu1[c] + mu1[a] * sg[1][b] * mu1[c] + mu1[a] * mu1[b] * sg[2][c]);
+        const size_t nn = (size_t)Nd.nx * Nd.ny * Nd.nz;
+        Nd.phi = q; q += nn; Nd.rhs = q; q += nn; Nd.res = q; q += nn; Nd.tmp = q; q += nn;
+        nd_.push_back(Nd);
+        for (int d = 0; d < 3; ++d) h[d] *= 2;
+    }
+    parts_.alloc(4 * 1216);
+    red_.alloc(8);
+    size_t maxpts = 1;
+    for (auto& d : disks_) maxpts = std::max(maxpts, (size_t)d.nr * d.nt);
+    pts_.alloc(4 * maxpts);
+    samp_.alloc(3 * maxpts);
+    launch_fill(ctx_, mueff_.p, mu_, g_.N);
+}
+
+void Sim::init_fields(const Deck& D) {
+    const std::string phys = D.str("incflo.physics", "");
+    if (phys == "TaylorGreenVortex") {
+        rho_ = D.num("TGV.density", rho_);
+        S_.rho = rho_;
+        const double L[3] = {phi_[0] - plo_[0], phi_[1] - plo_[1], phi_[2] - plo_[2]};
+        launch_init_tgv(ctx_, g_, vel_.p, plo_, L);
+    } else if (phys == "ABL" || phys == "FreeStream") {
+        const std::string prof = lc(D.str("ks_init.profile", phys == "ABL" ? "loglaw" : "uniform"));
+        double U[3] = {0, 0, 0};
+        if (D.has("incflo.velocity")) { auto u = D.nums("incflo.velocity"); for (int d = 0; d < 3; ++d) U[d] = u.at(d); }
+        const double utop = D.num("ks_init.loglaw_utop", 8.0);
+        const double H = phi_[2] - plo_[2];
+        const double ut = utop * kappa_ / std::log(H / z0_);
+        const double amp = D.num("ks_init.noise_amplitude", 0.0);
+        const double zmax = D.num("ks_init.noise_zmax", 1e300);
+        const unsigned long long seed = (unsigned long long)D.flag("ks_init.noise_seed", 0);
+        launch_init_abl(ctx_, g_, vel_.p, prof == "loglaw", U, ut / kappa_, z0_, amp, zmax - plo_[2], seed);
+    } else if (!phys.empty()) {
+        throw KsError(KS_ERR_UNSUPPORTED, "incflo.physics = " + phys);
+    }
+}
+
+// ---------------------------------------------------------------- reductions
+double Sim::reduce(int np, int ncomp, int op_max, double* host) {
+    launch_reduce(ctx_, parts_.p, np, ncomp, op_max, red_.p);
+    ck(cudaMemcpyAsync(hred_, red_.p, ncomp * sizeof(double), cudaMemcpyDeviceToHost, ctx_.stream), "D2H");
+    sync();
+    if (host)
+        for (int c = 0; c < ncomp; ++c) host[c] = hred_[c];
+    return hred_[0];
+}
+
+// ---------------------------------------------------------------- compute_dt
+void Sim::compute_dt() {
+    int np = 0;
+    launch_cfl(ctx_, g_, vel_.p, src_.p, mueff_.p, rho_, parts_.p, &np);
+    double m[3];
+    reduce(np, 3, 1, m);
+    if (!std::isfinite(m[0]) || !std::isfinite(m[1]) || !std::isfinite(m[2])) throw KsError(KS_ERR_NONFINITE, "non-finite CFL");
+    t_.set_cfl(m[0], m[1], t_.force_cfl ? m[2] : 0.0);
+}
+
+// ---------------------------------------------------------------- ABL
+void Sim::abl_update() {
+    if (!wallmodel_) return;
+    int np = 0;
+    launch_plane_sums(ctx_, g_, vel_.p, parts_.p, &np);
+    double s[3];
+    reduce(np, 3, 0, s);
+    const double M = (double)g_.nx * g_.ny;
+    um_[0] = s[0] / M;
+    um_[1] = s[1] / M;
+    vmag_ = s[2] / M;
+    utau_ = kappa_ * vmag_ / std::log(zref_ / z0_);
+}
+
+// ---------------------------------------------------------------- actuators
+static void rot(const double* a, double ang, const double* v, double* o) {
+    const double c = std::cos(ang), s = std::sin(ang);
+    const double dd = a[0] * v[0] + a[1] * v[1] + a[2] * v[2];
+    const double x[3] = {a[1] * v[2] - a[2] * v[1], a[2] * v[0] - a[0] * v[2], a[0] * v[1] - a[1] * v[0]};
+    for (int m = 0; m < 3; ++m) o[m] = v[m] * c + x[m] * s + a[m] * dd * (1 - c);
+}
+
+void Sim::actuator_update() {
+    if (!S_.act) return;
+    const double pi = 3.14159265358979323846;
+    launch_fill(ctx_, act_.p, 0.0, 3 * g_.N);
+    for (auto& d : disks_) {
+        // sample points on the sampling disk (disk_ops.cpp:378-412)
+        const double* ax = d.normal;
+        double rv[3] = {-ax[1], ax[0], 0.0};
+        const double rm = std::sqrt(rv[0] * rv[0] + rv[1] * rv[1]);
+        rv[0] /= rm;
+        rv[1] /= rm;
+        const double drs = 0.5 * d.D / d.nr;
+        const double shift = d.nr == 1 ? 0.0 : 0.5;
+        const int np = d.nr * d.nt;
+        std::vector<double> hp(3 * (size_t)np);
+        for (int ir = 0; ir < d.nr; ++ir)
+            for (int it = 0; it < d.nt; ++it) {
+                double r[3];
+                rot(ax, 2 * pi / d.nt * it, rv, r);
+                for (int m = 0; m < 3; ++m)
+                    hp[3 * (ir * d.nt + it) + m] = d.center[m] + d.to_sample * d.D * ax[m] + drs * (ir + shift) * r[m];
+            }
+        for (int p = 0; p < np; ++p) {
+            const double hh[3] = {g_.dx, g_.dy, g_.dz};
+            const int nn[3] = {g_.nx, g_.ny, g_.nz};
+            for (int m = 0; m < 3; ++m) {
+                const int c = (int)std::floor((hp[3 * p + m] - plo_[m] - 0.5 * hh[m]) / hh[m]);
+                if (c < -1 || c + 1 > nn[m]) throw KsError(KS_ERR_DECK, "actuator sample point outside the domain");
+            }
+        }
+        ck(cudaMemcpyAsync(pts_.p, hp.data(), hp.size() * sizeof(double), cudaMemcpyHostToDevice, ctx_.stream), "H2D");
+        launch_act_sample(ctx_, g_, vel_.p, pts_.p, np, plo_, samp_.p);
+        std::vector<double> sv(3 * (size_t)np);
+        ck(cudaMemcpyAsync(sv.data(), samp_.p, sv.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx_.stream), "D2H");
+        sync();
+        double ref[3] = {0, 0, 0};
+        for (int ir = 0; ir < d.nr; ++ir) {
+            const double w = ((ir + 1.0) * (ir + 1.0) - (double)ir * ir) / ((double)d.nr * d.nr * d.nt);
+            for (int it = 0; it < d.nt; ++it)
+                for (int m = 0; m < 3; ++m) ref[m] += sv[3 * (ir * d.nt + it) + m] * w;
+        }
+        for (int m = 0; m < 3; ++m) d.ref[m] = ref[m];
+        const double un = ref[0] * ax[0] + ref[1] * ax[1] + ref[2] * ax[2];
+        d.uinf2 = un * un;
+        const double umag = std::sqrt(d.uinf2);
+        if (d.ws.size() == 1 || umag <= d.ws.front()) d.ct_now = d.ct.front();
+        else if (umag >= d.ws.back()) d.ct_now = d.ct.back();
+        else {
+            size_t m = 0;
+            while (m + 1 < d.ws.size() && d.ws[m + 1] < umag) ++m;
+            d.ct_now = d.ct[m] + (d.ct[m + 1] - d.ct[m]) * (umag - d.ws[m]) / (d.ws[m + 1] - d.ws[m]);
+        }
+        const double aero = 0.5 * d.uinf2 * d.ct_now;
+        // ring points with per-point force magnitude
+        std::vector<double> ring;
+        double bmin[3] = {1e300, 1e300, 1e300}, bmax[3] = {-1e300, -1e300, -1e300};
+        for (int ip = 0; ip < d.nr; ++ip) {
+            const double r = (ip + 0.5) * d.dr, rp = r + 0.5 * d.dr, rmn = r - 0.5 * d.dr;
+            const double f = aero * pi * (rp * rp - rmn * rmn);
+            double pos[3];
+            for (int m = 0; m < 3; ++m) pos[m] = d.center[m] + (ip + 0.5) * d.dr * d.cvec[m];
+            for (int it = 0; it < d.nt; ++it) {
+                const double ang = 2 * pi / d.nt * it;
+                double o[3];
+                if (d.about_center) {
+                    const double rel[3] = {pos[0] - d.center[0], pos[1] - d.center[1], pos[2] - d.center[2]};
+                    rot(ax, ang, rel, o);
+                    for (int m = 0; m < 3; ++m) o[m] += d.center[m];
+                } else {
+                    rot(ax, ang, pos, o);  // the reference rotates the absolute position (disk_spreading.H:85-86)
+                }
+                for (int m = 0; m < 3; ++m) {
+                    ring.push_back(o[m]);
+                    bmin[m] = std::min(bmin[m], o[m]);
+                    bmax[m] = std::max(bmax[m], o[m]);
+                }
+                ring.push_back(f / d.nt);
+            }
+        }
+        const int nring = (int)ring.size() / 4;
+        ck(cudaMemcpyAsync(pts_.p, ring.data(), ring.size() * sizeof(double), cudaMemcpyHostToDevice, ctx_.stream), "H2D");
+        // cells within 4 eps of any ring point, clamped to the domain
+        int lo[3], hi[3];
+        const double h[3] = {g_.dx, g_.dy, g_.dz};
+        const int nn[3] = {g_.nx, g_.ny, g_.nz};
+        for (int m = 0; m < 3; ++m) {
+            lo[m] = std::max(0, (int)std::floor((bmin[m] - 4.0 * d.eps - plo_[m]) / h[m]) - 1);
+            hi[m] = std::min(nn[m] - 1, (int)std::floor((bmax[m] + 4.0 * d.eps - plo_[m]) / h[m]) + 1);
+        }
+        launch_act_spread(ctx_, g_, act_.p, pts_.p, nring, ax, d.eps, plo_, lo, hi);
+        sync();  // pts_ is reused by the next disk
+    }
+}
+
+// ---------------------------------------------------------------- MAC projection
+void Sim::cc_vcycle(size_t l) {
+    const double beta = 1.0 / rho_;
+    CCLevelDev& L = cc_[l];
+    if (l + 1 == cc_.size()) {
+        launch_cc_bottom(ctx_, L, beta, mac_.bottom);
+        return;
+    }
+    for (int s = 0; s < mac_.nu1; ++s) {
+        launch_cc_gsrb(ctx_, L, beta, 0);
+        launch_cc_gsrb(ctx_, L, beta, 1);
+    }
+    launch_cc_resid(ctx_, L, beta, nullptr, nullptr);
+    launch_cc_restrict(ctx_, L, cc_[l + 1]);
+    cc_vcycle(l + 1);
+    launch_cc_prolong(ctx_, L, cc_[l + 1]);
+    for (int s = 0; s < mac_.nu2; ++s) {
+        launch_cc_gsrb(ctx_, L, beta, 0);
+        launch_cc_gsrb(ctx_, L, beta, 1);
+    }
+}
+
+void Sim::mac_project() {
+    const double beta = 1.0 / rho_;
+    CCLevelDev& L = cc_[0];
+    int np = 0;
+    launch_mac_rhs(ctx_, g_, umac_[0].p, umac_[1].p, umac_[2].p, L.rhs, parts_.p, &np);
+    launch_reduce(ctx_, parts_.p, np, 1, 0, red_.p);
+    launch_sub_ratio(ctx_, L.rhs, g_.N, red_.p, (double)g_.N);
+    launch_fill(ctx_, L.phi, 0.0, g_.N);
+    launch_cc_resid(ctx_, L, beta, parts_.p, &np);
+    const double r0 = reduce(np, 1, 1, nullptr);
+    mac_r0_ = r0;
+    const double target = std::max(mac_.atol, mac_.rtol * r0);
+    int it = 0;
+    double rn = r0;
+    while (rn > target && it < mac_.maxiter) {
+        cc_vcycle(0);
+        launch_cc_resid(ctx_, L, beta, parts_.p, &np);
+        rn = reduce(np, 1, 1, nullptr);
+        ++it;
+        if (!std::isfinite(rn)) throw KsError(KS_ERR_NONFINITE, "MAC projection diverged");
+    }
+    mac_it_ = it;
+    mac_r_ = rn;
+    launch_mac_correct(ctx_, g_, L.phi, umac_[0].p, umac_[1].p, umac_[2].p, beta);
+}
+
+// ---------------------------------------------------------------- nodal projection
+void Sim::nd_vcycle(size_t l, double sigma) {
+    NDLevelDev& L = nd_[l];
+    if (l + 1 == nd_.size()) {
+        launch_nd_bottom(ctx_, L, sigma, nod_.omega, nod_.bottom);
+        return;
+    }
+    for (int s = 0; s < nod_.nu1; ++s) {
+        launch_nd_jacobi(ctx_, L, sigma, nod_.omega, L.phi, L.tmp);
+        std::swap(L.phi, L.tmp);
+    }
+    launch_nd_resid(ctx_, L, sigma, nullptr, nullptr);
+    launch_nd_restrict(ctx_, L, nd_[l + 1]);
+    nd_vcycle(l + 1, sigma);
+    launch_nd_prolong(ctx_, L, nd_[l + 1]);
+    for (int s = 0; s < nod_.nu2; ++s) {
+        launch_nd_jacobi(ctx_, L, sigma, nod_.omega, L.phi, L.tmp);
+        std::swap(L.phi, L.tmp);
+    }
+}
+
+void Sim::apply_projection(double time, double scaling, bool incremental) {
+    const bool small_dt = (time > 0.0 && t_.dt[0] < 0.1 * t_.dt[1]);
+    const bool sub_old = small_dt || incremental;
+    launch_proj_pre(ctx_, g_, vel_.p, vel_old_.p, gp_.p, scaling, rho_, incremental ? 0 : 1, sub_old ? 1 : 0);
+    NDLevelDev& L = nd_[0];
+    const long long M = (long long)L.nx * L.ny * L.nz;
+    int np = 0;
+    launch_nodal_rhs(ctx_, g_, vel_.p, L.rhs, parts_.p, &np);
+    launch_reduce(ctx_, parts_.p, np, 2, 0, red_.p);
+    launch_sub_ratio(ctx_, L.rhs, M, red_.p, 0.0);
+    launch_fill(ctx_, L.phi, 0.0, M);
+    const double sigma = scaling / rho_;
+    launch_nd_resid(ctx_, L, sigma, parts_.p, &np);
+    const double r0 = reduce(np, 1, 1, nullptr);
+    nod_r0_ = r0;
+    const double target = std::max(nod_.atol, nod_.rtol * r0);
+    int it = 0;
+    double rn = r0;
+    while (rn > target && it < nod_.maxiter) {
+        nd_vcycle(0, sigma);
+        launch_nd_resid(ctx_, L, sigma, parts_.p, &np);
+        rn = reduce(np, 1, 1, nullptr);
+        ++it;
+        if (!std::isfinite(rn)) throw KsError(KS_ERR_NONFINITE, "nodal projection diverged");
+    }
+    nod_it_ = it;
+    nod_r_ = rn;
+    launch_nodal_post(ctx_, g_, L.phi, vel_.p, vel_old_.p, gp_.p, p_.p, sigma, sub_old ? 1 : 0, incremental ? 1 : 0);
+}
+
+// ---------------------------------------------------------------- ApplyPredictor
+void Sim::apply_predictor(bool incremental) {
+    const double dt = t_.dt[0];
+    launch_smagorinsky(ctx_, g_, vel_old_.p, mueff_.p, S_);
+    launch_sources(ctx_, g_, vel_old_.p, gp_.p, act_.p, src_.p, S_);
+    if (wallmodel_) launch_wall_grad(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, shear_, utau_ * utau_, um_[0], um_[1], vmag_, rho_);
+    launch_divtau(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, divtau_.p, 1, src_.p, forces_.p, nullptr, nullptr, dt, rho_);
+    double* mac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
+    launch_premac(ctx_, g_, vel_old_.p, forces_.p, dt, gb_, mac);
+    mac_project();
+    const double* cmac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
+    launch_advection(ctx_, g_, vel_old_.p, forces_.p, cmac, dt, rho_, gb_, conv_.p);
+    // compute_source_term(NPH) and compute_diffusion_term(Old) reproduce src
+    // and divtau on this path (Coriolis reads the Old velocity, gp unchanged).
+    launch_predictor_rhs(ctx_, g_, vel_old_.p, conv_.p, src_.p, divtau_.p, vel_.p, dt, rho_);
+    launch_divtau(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, 2, nullptr, nullptr, vel_.p, divtau_.p, dt, rho_);
+    std::swap(vel_.p, vel_tmp_.p);
+    apply_projection(t_.next, dt, incremental);
+}
+
+void Sim::prepare_time_step() { launch_copy(ctx_, vel_old_.p, vel_.p, 3 * g_.N); }
+
+void Sim::pre_advance() {
+    t_.next = t_.cur + t_.dt[0];
+    abl_update();
+    actuator_update();
+}
+
+void Sim::init_data() {
+    abl_update();
+    if (initial_proj_) {
+        apply_projection(t_.cur, 1.0, false);
+        launch_fill(ctx_, p_.p, 0.0, (long long)p_.n);
+        launch_fill(ctx_, gp_.p, 0.0, 3 * g_.N);
+    }
+    if (initial_iters_ > 0) {
+        compute_dt();
+        launch_copy(ctx_, vel_old_.p, vel_.p, 3 * g_.N);
+        for (int it = 0; it < initial_iters_; ++it) {
+            apply_predictor(true);
+            launch_copy(ctx_, vel_.p, vel_old_.p, 3 * g_.N);
+        }
+    }
+    sync();
+}
+
+int Sim::step() {
+    if (!t_.new_step()) return KS_DONE;
+    compute_dt();
+    pre_advance();
+    prepare_time_step();
+    apply_predictor(false);
+    return KS_OK;
+}
+
+// ---------------------------------------------------------------- field access
+// kind: 0 cell, 1 node, 2/3/4 x/y/z face
+double* Sim::field(const std::string& name, int& nc, int& kind) {
+    kind = 0;
+    nc = 3;
+    if (name == "velocity") return vel_.p;
+    if (name == "velocity_old") return vel_old_.p;
+    if (name == "gp") return gp_.p;
+    if (name == "src_term") return src_.p;
+    if (name == "forces") return forces_.p;
+    if (name == "diff_term") return divtau_.p;
+    if (name == "conv_term") return conv_.p;
+    if (name == "actuator_src_term") { if (!S_.act) throw KsError(KS_ERR_ARG, "no actuator source"); return act_.p; }
+    nc = 1;
+    if (name == "velocity_mueff") return mueff_.p;
+    if (name == "p") { kind = 1; return p_.p; }
+    if (name == "u_mac") { kind = 2; return umac_[0].p; }
+    if (name == "v_mac") { kind = 3; return umac_[1].p; }
+    if (name == "w_mac") { kind = 4; return umac_[2].p; }
+    throw KsError(KS_ERR_ARG, "unknown field " + name);
+}
+
+void Sim::layout(const std::string& name, ks_layout& L) {
+    int nc, kind;
+    field(name, nc, kind);
+    L.ncomp = nc;
+    L.nx = g_.nx + (kind == 2);
+    L.ny = g_.ny + (kind == 3);
+    L.nz = g_.nz + (kind == 4) + ((kind == 1 && !g_.zper) ? 1 : 0);
+}
+
+void Sim::get(const std::string& name, void* dst, int where) {
+    int nc, kind;
+    double* f = field(name, nc, kind);
+    ks_layout L;
+    layout(name, L);
+    const size_t out = (size_t)L.ncomp * L.nx * L.ny * L.nz;
+    if (kind < 2) {
+        ck(cudaMemcpyAsync(dst, f, out * sizeof(double), where == KS_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx_.stream),
+           "get_field");
+        sync();
+        return;
+    }
+    // face fields: expand the periodic storage with the duplicate last face
+    const size_t stored = (kind == 4) ? (size_t)g_.NFz : (size_t)g_.N;
+    std::vector<double> h(stored), o(out);
+    ck(cudaMemcpyAsync(h.data(), f, stored * sizeof(double), cudaMemcpyDeviceToHost, ctx_.stream), "get_field");
+    sync();
+    const int d = kind - 2;
+    for (int k = 0; k < L.nz; ++k)
+        for (int j = 0; j < L.ny; ++j)
+            for (int i = 0; i < L.nx; ++i) {
+                int a = i % g_.nx, b = j % g_.ny, c = k;
+                if (d != 2 || g_.zper) c = k % g_.nz;
+                o[((size_t)k * L.ny + j) * L.nx + i] = h[((size_t)c * g_.ny + b) * g_.nx + a];
+            }
+    if (where == KS_DEVICE) {
+        ck(cudaMemcpyAsync(dst, o.data(), out * sizeof(double), cudaMemcpyHostToDevice, ctx_.stream), "get_field");
+        sync();
+    } else {
+        std::memcpy(dst, o.data(), out * sizeof(double));
+    }
+}
+
+void Sim::set(const std::string& name, const void* src, int where) {
+    int nc, kind;
+    double* f = field(name, nc, kind);
+    if (kind >= 2) throw KsError(KS_ERR_ARG, "face fields are derived and cannot be set");
+    ks_layout L;
+    layout(name, L);
+    const size_t n = (size_t)L.ncomp * L.nx * L.ny * L.nz;
+    ck(cudaMemcpyAsync(f, src, n * sizeof(double), where == KS_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx_.stream),
+       "set_field");
+    sync();
+}
+
+double Sim::scalar(const std::string& n) {
+    if (n == "time") return t_.cur;
+    if (n == "new_time") return t_.next;
+    if (n == "dt") return t_.dt[0];
+    if (n == "dt_nm1") return t_.dt[1];
+    if (n == "step") return t_.step;
+    if (n == "mac_iters") return mac_it_;
+    if (n == "nodal_iters") return nod_it_;
+    if (n == "mac_res0") return mac_r0_;
+    if (n == "mac_res") return mac_r_;
+    if (n == "nodal_res0") return nod_r0_;
+    if (n == "nodal_res") return nod_r_;
+    if (n == "utau") return utau_;
+    if (n == "cfl") return t_.cur_cfl;
+    if (n == "conv_cfl") return t_.conv_cfl;
+    if (n == "diff_cfl") return t_.diff_cfl;
+    if (n == "src_cfl") return t_.src_cfl;
+    if (n == "density") return rho_;
+    if (n == "ncells") return (double)g_.N;
+    if (n == "ke") {
+        int np = 0;
+        launch_ke(ctx_, g_, vel_.p, rho_, parts_.p, &np);
+        return reduce(np, 1, 0, nullptr) / (double)g_.N;
+    }
+    if (n.rfind("disk_ct:", 0) == 0) return disks_.at(std::stoul(n.substr(8))).ct_now;
+    if (n.rfind("disk_uinf2:", 0) == 0) return disks_.at(std::stoul(n.substr(11))).uinf2;
+    throw KsError(KS_ERR_ARG, "unknown scalar " + n);
+}
+
+}  // namespace ks
+
+// ---------------------------------------------------------------- C ABI
+struct ks_handle {
+    std::unique_ptr<ks::Sim> sim;
+    std::string err;
+};
+
+template <typename F>
+static int guarded(ks_handle* h, F&& f) {
+    if (!h || !h->sim) return KS_ERR_ARG;
+    try {
+        const int rc = f(*h->sim);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            h->err = std::string("CUDA: ") + cudaGetErrorString(e);
+            return KS_ERR_CUDA;
+        }
+        return rc;
+    } catch (const ks::KsError& e) {
+        h->err = e.what();
+        return e.code;
+    } catch (const std::exception& e) {
+        h->err = e.what();
+        return KS_ERR_DECK;
+    }
+}
+
+extern "C" {
+
+int ks_create(const char* deck_text, ks_handle** out) {
+    if (!deck_text || !out) return KS_ERR_ARG;
+    *out = nullptr;
+    auto* h = new ks_handle();
+    *out = h;
+    try {
+        h->sim = std::make_unique<ks::Sim>(deck_text);
+    } catch (const ks::KsError& e) {
+        h->err = e.what();
+        return e.code;
+    } catch (const std::exception& e) {
+        h->err = e.what();
+        return KS_ERR_DECK;
+    }
+    return KS_OK;
+}
+
+void ks_destroy(ks_handle* h) { delete h; }
+
+const char* ks_last_error(const ks_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int ks_init_data(ks_handle* h) { return guarded(h, [](ks::Sim& s) { s.init_data(); return 0; }); }
+
+int ks_compute_dt(ks_handle* h, double* dt) {
+    return guarded(h, [&](ks::Sim& s) {
+        s.compute_dt();
+        if (dt) *dt = s.t_.dt[0];
+        return 0;
+    });
+}
+
+int ks_pre_advance(ks_handle* h) { return guarded(h, [](ks::Sim& s) { s.pre_advance(); return 0; }); }
+
+int ks_prepare_time_step(ks_handle* h) { return guarded(h, [](ks::Sim& s) { s.prepare_time_step(); s.sync(); return 0; }); }
+
+int ks_advance(ks_handle* h, int fpi) {
+    return guarded(h, [&](ks::Sim& s) {
+        if (fpi != 0) throw ks::KsError(KS_ERR_UNSUPPORTED, "fixed-point iterations > 0");
+        s.prepare_time_step();
+        s.apply_predictor(false);
+        s.sync();
+        return 0;
+    });
+}
+
+int ks_apply_predictor(ks_handle* h, int incremental, int fpi) {
+    return guarded(h, [&](ks::Sim& s) {
+        if (fpi != 0) throw ks::KsError(KS_ERR_UNSUPPORTED, "fixed-point iterations > 0");
+        s.apply_predictor(incremental != 0);
+        s.sync();
+        return 0;
+    });
+}
+
+int ks_apply_corrector(ks_handle* h) {
+    if (!h || !h->sim) return KS_ERR_ARG;
+    h->err = "ApplyCorrector is the MOL corrector; the Godunov path completes in ApplyPredictor";
+    return KS_ERR_UNSUPPORTED;
+}
+
+int ks_apply_projection(ks_handle* h, double time, double scaling, int incremental) {
+    return guarded(h, [&](ks::Sim& s) {
+        s.apply_projection(time, scaling, incremental != 0);
+        s.sync();
+        return 0;
+    });
+}
+
+int ks_step(ks_handle* h) {
+    return guarded(h, [](ks::Sim& s) {
+        const int rc = s.step();
+        s.sync();
+        return rc;
+    });
+}
+
+int ks_evolve(ks_handle* h, int nsteps) {
+    return guarded(h, [&](ks::Sim& s) {
+        for (int m = 0; m < nsteps; ++m)
+            if (s.step() == KS_DONE) break;
+        s.sync();
+        return 0;
+    });
+}
+
+int ks_field_layout(ks_handle* h, const char* name, ks_layout* L) {
+    if (!name || !L) return KS_ERR_ARG;
+    return guarded(h, [&](ks::Sim& s) { s.layout(name, *L); return 0; });
+}
+
+int ks_get_field(ks_handle* h, const char* name, void* dst, ks_memory where) {
+    if (!name || !dst) return KS_ERR_ARG;
+    return guarded(h, [&](ks::Sim& s) { s.get(name, dst, (int)where); return 0; });
+}
+
+int ks_set_field(ks_handle* h, const char* name, const void* src, ks_memory where) {
+    if (!name || !src) return KS_ERR_ARG;
+    return guarded(h, [&](ks::Sim& s) { s.set(name, src, (int)where); return 0; });
+}
+
+int ks_get_scalar(ks_handle* h, const char* name, double* v) {
+    if (!name || !v) return KS_ERR_ARG;
+    return guarded(h, [&](ks::Sim& s) { *v = s.scalar(name); return 0; });
+}
+
+int ks_last_solver_stats(const ks_handle* h, ks_mg_stats* st) {
+    if (!h || !h->sim || !st) return KS_ERR_ARG;
+    const ks::Sim& s = *h->sim;
+    st->mac_iterations = s.mac_it_;
+    st->mac_initial_residual = s.mac_r0_;
+    st->mac_final_residual = s.mac_r_;
+    st->nodal_iterations = s.nod_it_;
+    st->nodal_initial_residual = s.nod_r0_;
+    st->nodal_final_residual = s.nod_r_;
+    return KS_OK;
+}
+
+int ks_set_precision(ks_handle* h, int precision) {
+    if (!h || !h->sim) return KS_ERR_ARG;
+    if (precision == KS_FP64) return KS_OK;
+    h->err = "mixed precision is not built yet";
+    return KS_ERR_UNSUPPORTED;
+}
+
+int ks_synchronize(ks_handle* h) { return guarded(h, [](ks::Sim& s) { s.sync(); return 0; }); }
+
+int ks_kernel_launches(const ks_handle* h, long long* count) {
+    if (!h || !h->sim || !count) return KS_ERR_ARG;
+    *count = h->sim->ctx_.launches;
+    return KS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,605 @@
+// Pointwise and stencil passes of the advance: initial fields, Smagorinsky,
+// momentum sources, wall model, tensor diffusion (+ RK2 correction), RHS
+// assembly, projection updates, CFL / norm reductions and the actuator-disk
+// sampling and Gaussian spreading.  One thread per output point; periodic
+// wrap and wall boundary conditions are applied inside the kernels (no ghost
+// cells are stored).
+#include <cmath>
+
+#include "ks_launch.hpp"
+
+namespace ks {
+
+namespace {
+
+constexpr int BS = 256;
+constexpr int MAXPARTS = 1216;  // 152 SMs x 8
+
+__device__ inline void cell_of(const Grid& g, long long t, int& i, int& j, int& k) {
+    i = (int)(t % g.nx);
+    long long r = t / g.nx;
+    j = (int)(r % g.ny);
+    k = (int)(r / g.ny);
+}
+
+template <int OPMAX>
+__device__ inline double block_reduce(double v) {
+    __shared__ double sh[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        const double x = __shfl_down_sync(0xffffffffu, v, o);
+        v = OPMAX ? fmax(v, x) : v + x;
+    }
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    const int nw = (blockDim.x + 31) >> 5;
+    v = (threadIdx.x < nw) ? sh[threadIdx.x] : (OPMAX ? -1.0e300 : 0.0);
+    if (w == 0)
+        for (int o = 16; o > 0; o >>= 1) {
+            const double x = __shfl_down_sync(0xffffffffu, v, o);
+            v = OPMAX ? fmax(v, x) : v + x;
+        }
+    return v;
+}
+
+inline int parts_for(long long n) {
+    long long b = (n + BS - 1) / BS;
+    return (int)(b < MAXPARTS ? (b < 1 ? 1 : b) : MAXPARTS);
+}
+
+__device__ inline uint64_t splitmix64(uint64_t x) {
+    uint64_t z = x + 0x9e3779b97f4a7c15ULL;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+
+// ---------------------------------------------------------------- init
+// TaylorGreenVortex::initialize_fields (src/physics/TaylorGreenVortex.cpp:22-54)
+__global__ void k_init_tgv(Grid g, double* vel, double x0, double y0, double z0, double Lx, double Ly, double Lz) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= g.N) return;
+    int i, j, k;
+    cell_of(g, t, i, j, k);
+    const double tp = 6.283185307179586476925;
+    const double x = x0 + (i + 0.5) * g.dx, y = y0 + (j + 0.5) * g.dy, z = z0 + (k + 0.5) * g.dz;
+    vel[t] = sin(tp * x / Lx) * cos(tp * y / Ly) * cos(tp * z / Lz);
+    vel[g.N + t] = -cos(tp * x / Lx) * sin(tp * y / Ly) * cos(tp * z / Lz);
+    vel[2 * g.N + t] = 0.0;
+}
+
+// Synthetic ABL / free-stream start: log-law or uniform mean plus uniform
+// noise of amplitude amp below zmax, SplitMix64 keyed on (seed, comp, k, j, i).
+__global__ void k_init_abl(Grid g, double* vel, int loglaw, double U0, double U1, double U2, double ut_k, double z0, double amp,
+                           double zmax_rel, unsigned long long seed) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= g.N) return;
+    int i, j, k;
+    cell_of(g, t, i, j, k);
+    const double z = (k + 0.5) * g.dz;
+    const double U[3] = {U0, U1, U2};
+    for (int n = 0; n < 3; ++n) {
+        double val = U[n];
+        if (loglaw) val = (n == 0) ? ut_k * log(z / z0) : 0.0;
+        if (amp > 0.0 && z < zmax_rel) {
+            const uint64_t idx = (uint64_t)n * (uint64_t)g.N + (uint64_t)t;
+            const uint64_t r = splitmix64(seed * 0x100000001b3ULL ^ idx);
+            const double u01 = (double)(r >> 11) * (1.0 / 9007199254740992.0);
+            val += amp * (2.0 * u01 - 1.0);
+        }
+        vel[n * g.N + t] = val;
+    }
+}
+
+__global__ void k_fill(double* p, double v, long long n) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < n) p[t] = v;
+}
+__global__ void k_copy(double* d, const double* s, long long n) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < n) d[t] = s[t];
+}
+
+// ---------------------------------------------------------------- Smagorinsky
+// mu_eff = mu + rho Cs^2 Delta^2 |S| (src/turbulence/LES/Smagorinsky.cpp:22-62,
+// strain rate src/fvm/strainrate.H:24-86, one-sided z stencils at walls
+// src/fvm/stencils.H:166-330).
+__global__ void k_smag(Grid g, const double* vel, double* mueff, double mu, double rho, double fac, int smag) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= g.N) return;
+    if (!smag) { mueff[t] = mu; return; }
+    int i, j, k;
+    cell_of(g, t, i, j, k);
+    VelFP V{vel, g, 1.0};
+    double a = 0.5, b = 0.0, c = -0.5;
+    if (!g.zper && k == 0) { a = 1.0 / 3.0; b = 1.0; c = -4.0 / 3.0; }
+    if (!g.zper && k == g.nz - 1) { a = 4.0 / 3.0; b = -1.0; c = -1.0 / 3.0; }
+    double gx[3], gy[3], gz[3];
+    for (int n = 0; n < 3; ++n) {
+        gx[n] = 0.5 * (V(n, i + 1, j, k) - V(n, i - 1, j, k)) / g.dx;
+        gy[n] = 0.5 * (V(n, i, j + 1, k) - V(n, i, j - 1, k)) / g.dy;
+        gz[n] = (a * V(n, i, j, k + 1) + b * V(n, i, j, k) + c * V(n, i, j, k - 1)) / g.dz;
+    }
+    const double s = sqrt(2.0 * gx[0] * gx[0] + 2.0 * gy[1] * gy[1] + 2.0 * gz[2] * gz[2] + (gy[0] + gx[1]) * (gy[0] + gx[1]) +
+                          (gz[1] + gy[2]) * (gz[1] + gy[2]) + (gx[2] + gz[0]) * (gx[2] + gz[0]));
+    mueff[t] = mu + rho * fac * s;
+}
+
+// ---------------------------------------------------------------- sources
+// src = rho (-gp/rho + geostrophic + Coriolis(u_old) + body + actuator)
+// (icns_ops.H:78-124, PDEOps.H:94-145, GeostrophicForcing.cpp:103-,
+// CoriolisForcing.cpp:60-108, BodyForce.cpp:117-169, ActuatorForcing.cpp:19-29)
+__global__ void k_sources(Grid g, const double* vel, const double* gp, const double* act, double* src, Scalars s) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= g.N) return;
+    const long long N = g.N;
+    double f[3];
+    for (int n = 0; n < 3; ++n) f[n] = -gp[n * N + t] / s.rho;
+    if (s.geo)
+        for (int n = 0; n < 3; ++n) f[n] += (n == 2 ? s.hfac : 1.0) * s.gf[n];
+    if (s.cor) {
+        const double u0 = vel[t], u1 = vel[N + t], u2 = vel[2 * N + t];
+        const double ue = s.east[0] * u0 + s.east[1] * u1 + s.east[2] * u2;
+        const double un = s.north[0] * u0 + s.north[1] * u1 + s.north[2] * u2;
+        const double uu = s.up[0] * u0 + s.up[1] * u1 + s.up[2] * u2;
+        const double ae = s.corfac * (un * s.sinphi - s.hfac * uu * s.cosphi);
+        const double an = -s.corfac * ue * s.sinphi;
+        const double au = s.hfac * s.corfac * ue * s.cosphi;
+        for (int n = 0; n < 3; ++n) f[n] += ae * s.east[n] + an * s.north[n] + au * s.up[n];
+    }
+    if (s.body)
+        for (int n = 0; n < 3; ++n) f[n] += s.body_force[n];
+    if (s.act)
+        for (int n = 0; n < 3; ++n) f[n] += act[n * N + t];
+    for (int n = 0; n < 3; ++n) src[n * N + t] = s.rho * f[n];
+}
+
+// ---------------------------------------------------------------- ABL wall
+// plane sums over the first cell layer: u, v, |u_h|
+__global__ void k_plane_sums(Grid g, const double* vel, double* parts, int np) {
+    double su = 0, sv = 0, sm = 0;
+    const long long M = (long long)g.nx * g.ny;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < M; t += (long long)gridDim.x * blockDim.x) {
+        const double u = vel[t], v = vel[g.N + t];
+        su += u; sv += v; sm += sqrt(u * u + v * v);
+    }
+    su = block_reduce<0>(su);
+    sv = block_reduce<0>(sv);
+    sm = block_reduce<0>(sm);
+    if (threadIdx.x == 0) { parts[blockIdx.x] = su; parts[np + blockIdx.x] = sv; parts[2 * np + blockIdx.x] = sm; }
+}
+
+// wall-normal gradient of the tangential velocity at z-lo: tau rho / mu_eff
+// (ABLWallFunction.cpp:236-347, ShearStress.H:22-167), Old velocity.
+__global__ void k_wall_grad(Grid g, const double* vel, const double* mueff, double* wg, int type, double ut2, double um0, double um1,
+                            double vm, double rho) {
+    const long long M = (long long)g.nx * g.ny;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= M) return;
+    const double u = vel[t], v = vel[g.N + t];
+    const double ws = sqrt(u * u + v * v);
+    double tx, ty;
+    if (type == 0) {  // moeng
+        tx = ((u - um0) * vm + ws * um0) / (vm * vm) * ut2;
+        ty = ((v - um1) * vm + ws * um1) / (vm * vm) * ut2;
+    } else if (type == 1) {  // constant
+        tx = um0 / vm * ut2;
+        ty = um1 / vm * ut2;
+    } else if (type == 2) {  // local
+        tx = u / fmax(ws, 1.0e-6) * ut2;
+        ty = v / fmax(ws, 1.0e-6) * ut2;
+    } else {  // schumann
+        tx = u / vm * ut2;
+        ty = v / vm * ut2;
+    }
+    const double m = mueff[t];
+    wg[t] = tx * rho / m;
+    wg[M + t] = ty * rho / m;
+}
+
+// ---------------------------------------------------------------- diffusion
+// Velocity seen by the tensor operator: periodic wrap; across a z wall the
+// normal component is odd-reflected (Dirichlet 0), the tangential ones are
+// even-reflected (Neumann) or shifted so that the face gradient equals the
+// wall-model gradient (inhomogeneous Neumann).
+struct VelDiff {
+    const double* v;
+    const double* wg;
+    Grid g;
+    __device__ inline double operator()(int n, int i, int j, int k) const {
+        i = wrapn(i, g.nx);
+        j = wrapn(j, g.ny);
+        const double* c = v + n * g.N;
+        if (g.zper) return c[cidx(g, i, j, wrapn(k, g.nz))];
+        if (k < 0) {
+            const double q0 = c[cidx(g, i, j, 0)];
+            if (n == 2) return -q0;
+            if (g.zlo == ZWALLMODEL) return q0 - wg[(long long)n * g.nx * g.ny + (long long)j * g.nx + i] * g.dz;
+            return q0;
+        }
+        if (k >= g.nz) {
+            const double q0 = c[cidx(g, i, j, g.nz - 1)];
+            return n == 2 ? -q0 : q0;
+        }
+        return c[cidx(g, i, j, k)];
+    }
+};
+
+// Flux of mu (grad u + grad u^T) - 2/3 mu div(u) I through the d-face at the
+// low side of cell (i,j,k).
+__device__ inline void tensor_flux(const Grid& g, const VelDiff& V, const double* mu, int d, int i, int j, int k, double F[3]) {
+    int e[3] = {0, 0, 0};
+    e[d] = 1;
+    const int im = i - e[0], jm = j - e[1], km = k - e[2];
+    // face viscosity
+    double mf;
+    const long long cc = cidx(g, wrapn(i, g.nx), wrapn(j, g.ny), g.zper ? wrapn(k, g.nz) : (k < g.nz ? k : g.nz - 1));
+    if (d == 2 && !g.zper && k == 0) mf = mu[cidx(g, wrapn(i, g.nx), wrapn(j, g.ny), 0)];
+    else if (d == 2 && !g.zper && k == g.nz) mf = mu[cidx(g, wrapn(i, g.nx), wrapn(j, g.ny), g.nz - 1)];
+    else {
+        const long long cm = cidx(g, wrapn(im, g.nx), wrapn(jm, g.ny), g.zper ? wrapn(km, g.nz) : km);
+        mf = 0.5 * (mu[cm] + mu[cc]);
+    }
+    const double h[3] = {g.dx, g.dy, g.dz};
+    double gr[3][3];  // gr[m][n] = d u_n / d x_m on the face
+    for (int n = 0; n < 3; ++n) {
+        for (int m = 0; m < 3; ++m) {
+            if (m == d) {
+                gr[m][n] = (V(n, i, j, k) - V(n, im, jm, km)) / h[m];
+            } else {
+                int f[3] = {0, 0, 0};
+                f[m] = 1;
+                gr[m][n] = 0.25 *
+                           (V(n, i + f[0], j + f[1], k + f[2]) + V(n, im + f[0], jm + f[1], km + f[2]) - V(n, i - f[0], j - f[1], k - f[2]) -
+                            V(n, im - f[0], jm - f[1], km - f[2])) /
+                           h[m];
+            }
+        }
+    }
+    const double dv = gr[0][0] + gr[1][1] + gr[2][2];
+    for (int n = 0; n < 3; ++n) {
+        if (n == d) F[n] = mf * (2.0 * gr[d][d] - (2.0 / 3.0) * dv);
+        else F[n] = mf * (gr[d][n] + gr[n][d]);
+    }
+}
+
+__global__ void k_divtau(Grid g, const double* vel, const double* mueff, const double* wg, double* out, int mode, const double* src,
+                         double* forces, const double* base, const double* dold, double dt, double rho) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= g.N) return;
+    int i, j, k;
+    cell_of(g, t, i, j, k);
+    VelDiff V{vel, wg, g};
+    double Fl[3], Fh[3], acc[3] = {0, 0, 0};
+    const double h[3] = {g.dx, g.dy, g.dz};
+    for (int d = 0; d < 3; ++d) {
+        tensor_flux(g, V, mueff, d, i, j, k, Fl);
+        tensor_flux(g, V, mueff, d, i + (d == 0), j + (d == 1), k + (d == 2), Fh);
+        for (int n = 0; n < 3; ++n) acc[n] += (Fh[n] - Fl[n]) / h[d];
+    }
+    const long long N = g.N;
+    if (mode == 0) {
+        for (int n = 0; n < 3; ++n) out[n * N + t] = acc[n];
+    } else if (mode == 1) {
+        for (int n = 0; n < 3; ++n) {
+            out[n * N + t] = acc[n];
+            forces[n * N + t] = (src[n * N + t] + acc[n]) / rho;
+        }
+    } else {
+        for (int n = 0; n < 3; ++n) out[n * N + t] = base[n * N + t] + 0.5 * dt * (acc[n] - dold[n * N + t]) / rho;
+    }
+}
+
+// predictor_rhs, Explicit (src/equation_systems/CompRHSOps.H:32-141)
+__global__ void k_pred_rhs(long long N3, const double* vo, const double* conv, const double* src, const double* dt_, double* vel, double dt,
+                           double rho) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= N3) return;
+    vel[t] = (rho * vo[t] + dt * (conv[t] + src[t] + dt_[t])) / rho;
+}
+
+// ---------------------------------------------------------------- projection
+__global__ void k_proj_pre(long long N3, double* vel, const double* vo, const double* gp, double scaling, double rho, int add_gp,
+                           int sub_old) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= N3) return;
+    double v = vel[t];
+    if (add_gp) v += gp[t] * scaling / rho;
+    if (sub_old) v -= vo[t];
+    vel[t] = v;
+}
+
+// Cell velocity as seen by the nodal divergence: periodic wrap, mirror images
+// across z walls (normal component odd, tangential even).
+__device__ inline double vel_mirror(const Grid& g, const double* v, int n, int i, int j, int k) {
+    i = wrapn(i, g.nx);
+    j = wrapn(j, g.ny);
+    double s = 1.0;
+    if (g.zper) k = wrapn(k, g.nz);
+    else if (k < 0) { k = -1 - k; s = (n == 2) ? -1.0 : 1.0; }
+    else if (k >= g.nz) { k = 2 * g.nz - 1 - k; s = (n == 2) ? -1.0 : 1.0; }
+    return s * v[n * g.N + cidx(g, i, j, k)];
+}
+
+// Nodal divergence (the MLNodeLaplacian right-hand side) with weighted partial
+// sums (boundary nodes carry half weight) for the solvability shift.
+__global__ void k_nodal_rhs(Grid g, const double* vel, double* rhs, double* parts, int np) {
+    const int nzn = g.zper ? g.nz : g.nz + 1;
+    const long long M = (long long)g.nx * g.ny * nzn;
+    double ws = 0, wt = 0;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < M; t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % g.nx);
+        const long long r = t / g.nx;
+        const int j = (int)(r % g.ny), k = (int)(r / g.ny);
+        double dv = 0;
+        for (int c = 0; c < 2; ++c)
+            for (int b = 0; b < 2; ++b) {
+                dv += 0.25 / g.dx * (vel_mirror(g, vel, 0, i, j - b, k - c) - vel_mirror(g, vel, 0, i - 1, j - b, k - c));
+                dv += 0.25 / g.dy * (vel_mirror(g, vel, 1, i - b, j, k - c) - vel_mirror(g, vel, 1, i - b, j - 1, k - c));
+                dv += 0.25 / g.dz * (vel_mirror(g, vel, 2, i - b, j - c, k) - vel_mirror(g, vel, 2, i - b, j - c, k - 1));
+            }
+        rhs[t] = dv;
+        const double w = (!g.zper && (k == 0 || k == nzn - 1)) ? 0.5 : 1.0;
+        ws += w * dv;
+        wt += w;
+    }
+    ws = block_reduce<0>(ws);
+    wt = block_reduce<0>(wt);
+    if (threadIdx.x == 0) { parts[blockIdx.x] = ws; parts[np + blockIdx.x] = wt; }
+}
+
+__device__ inline double node_at(const Grid& g, const double* phi, int i, int j, int k) {
+    const int nzn = g.zper ? g.nz : g.nz + 1;
+    i = wrapn(i, g.nx);
+    j = wrapn(j, g.ny);
+    if (g.zper) k = wrapn(k, g.nz);
+    return phi[((long long)k * g.ny + j) * g.nx + i];
+    (void)nzn;
+}
+
+// u -= sigma G phi ; gp = (or +=) G phi ; optional add-back of u_old.
+__global__ void k_nodal_post_cells(Grid g, const double* phi, double* vel, const double* vo, double* gp, double sigma, int add_old,
+                                   int incr) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= g.N) return;
+    int i, j, k;
+    cell_of(g, t, i, j, k);
+    double gx = 0, gy = 0, gz = 0;
+    for (int c = 0; c < 2; ++c)
+        for (int b = 0; b < 2; ++b) {
+            gx += node_at(g, phi, i + 1, j + b, k + c) - node_at(g, phi, i, j + b, k + c);
+            gy += node_at(g, phi, i + b, j + 1, k + c) - node_at(g, phi, i + b, j, k + c);
+            gz += node_at(g, phi, i + b, j + c, k + 1) - node_at(g, phi, i + b, j + c, k);
+        }
+    const double G[3] = {0.25 * gx / g.dx, 0.25 * gy / g.dy, 0.25 * gz / g.dz};
+    const long long N = g.N;
+    for (int n = 0; n < 3; ++n) {
+        double v = vel[n * N + t] - sigma * G[n];
+        if (add_old) v += vo[n * N + t];
+        vel[n * N + t] = v;
+        if (incr) gp[n * N + t] += G[n];
+        else gp[n * N + t] = G[n];
+    }
+}
+
+__global__ void k_nodal_post_nodes(long long M, const double* phi, double* p, int incr) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= M) return;
+    if (incr) p[t] += phi[t];
+    else p[t] = phi[t];
+}
+
+// MAC divergence + partial sums
+__global__ void k_mac_rhs(Grid g, const double* um, const double* vm, const double* wm, double* rhs, double* parts, int np) {
+    double s = 0;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < g.N; t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        cell_of(g, t, i, j, k);
+        const double r = (um[fidx(g, 0, i + 1, j, k)] - um[t]) / g.dx + (vm[fidx(g, 1, i, j + 1, k)] - vm[t]) / g.dy +
+                         (wm[fidx(g, 2, i, j, k + 1)] - wm[fidx(g, 2, i, j, k)]) / g.dz;
+        rhs[t] = r;
+        s += r;
+    }
+    s = block_reduce<0>(s);
+    if (threadIdx.x == 0) parts[blockIdx.x] = s;
+}
+
+__global__ void k_mac_correct(Grid g, const double* phi, double* um, double* vm, double* wm, double beta) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= g.N) return;
+    int i, j, k;
+    cell_of(g, t, i, j, k);
+    const double p0 = phi[t];
+    um[t] -= beta * (p0 - phi[cidx(g, wrapn(i - 1, g.nx), j, k)]) / g.dx;
+    vm[t] -= beta * (p0 - phi[cidx(g, i, wrapn(j - 1, g.ny), k)]) / g.dy;
+    if (g.zper) wm[t] -= beta * (p0 - phi[cidx(g, i, j, wrapn(k - 1, g.nz))]) / g.dz;
+    else if (k > 0) wm[t] -= beta * (p0 - phi[cidx(g, i, j, k - 1)]) / g.dz;
+}
+
+// ---------------------------------------------------------------- reductions
+__global__ void k_cfl(Grid g, const double* vel, const double* src, const double* mu, double rho, double* parts, int np) {
+    double c = 0, d = 0, f = 0;
+    const double dxi[3] = {1.0 / g.dx, 1.0 / g.dy, 1.0 / g.dz};
+    const double dxinv2 = 2.0 * (dxi[0] * dxi[0] + dxi[1] * dxi[1] + dxi[2] * dxi[2]);
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < g.N; t += (long long)gridDim.x * blockDim.x) {
+        for (int n = 0; n < 3; ++n) {
+            c = fmax(c, fabs(vel[n * g.N + t]) * dxi[n]);
+            f = fmax(f, fabs(src[n * g.N + t]) * dxi[n] / rho);
+        }
+        d = fmax(d, mu[t] * dxinv2 / rho);
+    }
+    c = block_reduce<1>(c);
+    d = block_reduce<1>(d);
+    f = block_reduce<1>(f);
+    if (threadIdx.x == 0) { parts[blockIdx.x] = c; parts[np + blockIdx.x] = d; parts[2 * np + blockIdx.x] = f; }
+}
+
+__global__ void k_ke(Grid g, const double* vel, double rho, double* parts) {
+    double s = 0;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < g.N; t += (long long)gridDim.x * blockDim.x)
+        for (int n = 0; n < 3; ++n) {
+            const double v = vel[n * g.N + t];
+            s += 0.5 * rho * v * v;
+        }
+    s = block_reduce<0>(s);
+    if (threadIdx.x == 0) parts[blockIdx.x] = s;
+}
+
+__global__ void k_reduce(const double* parts, int np, int op_max, double* out) {
+    const int comp = blockIdx.x;
+    double v = op_max ? -1.0e300 : 0.0;
+    for (int m = threadIdx.x; m < np; m += blockDim.x) {
+        const double x = parts[comp * np + m];
+        v = op_max ? fmax(v, x) : v + x;
+    }
+    v = op_max ? block_reduce<1>(v) : block_reduce<0>(v);
+    if (threadIdx.x == 0) out[comp] = v;
+}
+
+// a -= s[0] / den (den > 0) or a -= s[0] / s[1]
+__global__ void k_sub_ratio(double* a, long long n, const double* s, double den) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < n) a[t] -= s[0] / (den > 0.0 ? den : s[1]);
+}
+
+// ---------------------------------------------------------------- actuator
+// Trilinear sampling of the velocity at disk points
+// (ActuatorContainer.cpp:284-360); ghosts follow the fill-patch rules.
+__global__ void k_act_sample(Grid g, const double* vel, const double* pts, int npts, double x0, double y0, double z0, double* out) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npts) return;
+    VelFP V{vel, g, 1.0};
+    const double fx = (pts[3 * p] - x0 - 0.5 * g.dx) / g.dx;
+    const double fy = (pts[3 * p + 1] - y0 - 0.5 * g.dy) / g.dy;
+    const double fz = (pts[3 * p + 2] - z0 - 0.5 * g.dz) / g.dz;
+    const int i = (int)floor(fx), j = (int)floor(fy), k = (int)floor(fz);
+    const double wx = fx - i, wy = fy - j, wz = fz - k;
+    for (int n = 0; n < 3; ++n) {
+        double s = 0;
+        for (int c = 0; c < 2; ++c)
+            for (int b = 0; b < 2; ++b)
+                for (int a = 0; a < 2; ++a) {
+                    const double w = (a ? wx : 1 - wx) * (b ? wy : 1 - wy) * (c ? wz : 1 - wz);
+                    s += w * V(n, i + a, j + b, k + c);
+                }
+        out[3 * p + n] = s;
+    }
+}
+
+// Gaussian spreading of ring-point forces (disk_spreading.H:45-105,
+// actuator_utils.H:45-60) over the cells of the cut-off box of one disk.
+__global__ void k_act_spread(Grid g, double* act, const double* pts, int npts, double ax0, double ax1, double ax2, double eps,
+                             double x0, double y0, double z0, int lo0, int lo1, int lo2, int n0, int n1, int n2) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long M = (long long)n0 * n1 * n2;
+    if (t >= M) return;
+    const int a = (int)(t % n0);
+    const long long r = t / n0;
+    const int b = (int)(r % n1), c = (int)(r / n1);
+    const int i = lo0 + a, j = lo1 + b, k = lo2 + c;
+    if (k < 0 || k >= g.nz) return;
+    // cell centre of the unwrapped index; stored at the wrapped cell
+    const double x = x0 + (i + 0.5) * g.dx, y = y0 + (j + 0.5) * g.dy, z = z0 + (k + 0.5) * g.dz;
+    const double gfac = 0.17958712212516656 / (eps * eps * eps);
+    double s = 0;
+    for (int m = 0; m < npts; ++m) {
+        const double rx = (pts[4 * m] - x) / eps, ry = (pts[4 * m + 1] - y) / eps, rz = (pts[4 * m + 2] - z) / eps;
+        const double r2 = rx * rx + ry * ry + rz * rz;
+        if (r2 < 16.0) s += gfac * exp(-rx * rx - ry * ry - rz * rz) * pts[4 * m + 3];
+    }
+    if (s == 0.0) return;
+    const long long cc = cidx(g, wrapn(i, g.nx), wrapn(j, g.ny), k);
+    act[cc] += s * ax0;
+    act[g.N + cc] += s * ax1;
+    act[2 * g.N + cc] += s * ax2;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- launchers
+#define KS_LAUNCH(c, kern, grid, block, ...)                      \
+    do {                                                          \
+        kern<<<(grid), (block), 0, (c).stream>>>(__VA_ARGS__);    \
+        ++(c).launches;                                           \
+    } while (0)
+
+void launch_init_tgv(Ctx& c, const Grid& g, double* vel, const double plo[3], const double L[3]) {
+    KS_LAUNCH(c, k_init_tgv, nblocks(g.N, BS), BS, g, vel, plo[0], plo[1], plo[2], L[0], L[1], L[2]);
+}
+void launch_init_abl(Ctx& c, const Grid& g, double* vel, int loglaw, const double U[3], double ut_k, double z0, double amp,
+                     double zmax_rel, unsigned long long seed) {
+    KS_LAUNCH(c, k_init_abl, nblocks(g.N, BS), BS, g, vel, loglaw, U[0], U[1], U[2], ut_k, z0, amp, zmax_rel, seed);
+}
+void launch_fill(Ctx& c, double* p, double v, long long n) { KS_LAUNCH(c, k_fill, nblocks(n, BS), BS, p, v, n); }
+void launch_copy(Ctx& c, double* d, const double* s, long long n) { KS_LAUNCH(c, k_copy, nblocks(n, BS), BS, d, s, n); }
+void launch_smagorinsky(Ctx& c, const Grid& g, const double* vel, double* mueff, const Scalars& s) {
+    KS_LAUNCH(c, k_smag, nblocks(g.N, BS), BS, g, vel, mueff, s.mu, s.rho, s.smag_fac, s.smag);
+}
+void launch_sources(Ctx& c, const Grid& g, const double* vel_old, const double* gp, const double* act, double* src, const Scalars& s) {
+    KS_LAUNCH(c, k_sources, nblocks(g.N, BS), BS, g, vel_old, gp, act, src, s);
+}
+void launch_plane_sums(Ctx& c, const Grid& g, const double* vel, double* parts, int* np) {
+    *np = parts_for((long long)g.nx * g.ny);
+    KS_LAUNCH(c, k_plane_sums, *np, BS, g, vel, parts, *np);
+}
+void launch_wall_grad(Ctx& c, const Grid& g, const double* vel_old, const double* mueff, double* wg, int type, double ut2, double um0,
+                      double um1, double vm, double rho) {
+    KS_LAUNCH(c, k_wall_grad, nblocks((long long)g.nx * g.ny, BS), BS, g, vel_old, mueff, wg, type, ut2, um0, um1, vm, rho);
+}
+void launch_divtau(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, int mode,
+                   const double* src, double* forces, const double* base, const double* dold, double dt, double rho) {
+    KS_LAUNCH(c, k_divtau, nblocks(g.N, BS), BS, g, vel, mueff, wg, out, mode, src, forces, base, dold, dt, rho);
+}
+void launch_predictor_rhs(Ctx& c, const Grid& g, const double* vo, const double* conv, const double* src, const double* dtau, double* vel,
+                          double dt, double rho) {
+    KS_LAUNCH(c, k_pred_rhs, nblocks(3 * g.N, BS), BS, 3 * g.N, vo, conv, src, dtau, vel, dt, rho);
+}
+void launch_proj_pre(Ctx& c, const Grid& g, double* vel, const double* vo, const double* gp, double scaling, double rho, int add_gp,
+                     int sub_old) {
+    KS_LAUNCH(c, k_proj_pre, nblocks(3 * g.N, BS), BS, 3 * g.N, vel, vo, gp, scaling, rho, add_gp, sub_old);
+}
+void launch_nodal_rhs(Ctx& c, const Grid& g, const double* vel, double* rhs, double* parts, int* np) {
+    const long long M = (long long)g.nx * g.ny * (g.zper ? g.nz : g.nz + 1);
+    *np = parts_for(M);
+    KS_LAUNCH(c, k_nodal_rhs, *np, BS, g, vel, rhs, parts, *np);
+}
+void launch_nodal_post(Ctx& c, const Grid& g, const double* phi, double* vel, const double* vo, double* gp, double* p, double sigma,
+                       int add_old, int incr) {
+    KS_LAUNCH(c, k_nodal_post_cells, nblocks(g.N, BS), BS, g, phi, vel, vo, gp, sigma, add_old, incr);
+    const long long M = (long long)g.nx * g.ny * (g.zper ? g.nz : g.nz + 1);
+    KS_LAUNCH(c, k_nodal_post_nodes, nblocks(M, BS), BS, M, phi, p, incr);
+}
+void launch_mac_rhs(Ctx& c, const Grid& g, const double* um, const double* vm, const double* wm, double* rhs, double* parts, int* np) {
+    *np = parts_for(g.N);
+    KS_LAUNCH(c, k_mac_rhs, *np, BS, g, um, vm, wm, rhs, parts, *np);
+}
+void launch_mac_correct(Ctx& c, const Grid& g, const double* phi, double* um, double* vm, double* wm, double beta) {
+    KS_LAUNCH(c, k_mac_correct, nblocks(g.N, BS), BS, g, phi, um, vm, wm, beta);
+}
+void launch_cfl(Ctx& c, const Grid& g, const double* vel, const double* src, const double* mu, double rho, double* parts, int* np) {
+    *np = parts_for(g.N);
+    KS_LAUNCH(c, k_cfl, *np, BS, g, vel, src, mu, rho, parts, *np);
+}
+void launch_ke(Ctx& c, const Grid& g, const double* vel, double rho, double* parts, int* np) {
+    *np = parts_for(g.N);
+    KS_LAUNCH(c, k_ke, *np, BS, g, vel, rho, parts);
+}
+void launch_reduce(Ctx& c, const double* parts, int np, int ncomp, int op_max, double* out) {
+    KS_LAUNCH(c, k_reduce, ncomp, 256, parts, np, op_max, out);
+}
+void launch_sub_ratio(Ctx& c, double* a, long long n, const double* s, double den) {
+    KS_LAUNCH(c, k_sub_ratio, nblocks(n, BS), BS, a, n, s, den);
+}
+void launch_act_sample(Ctx& c, const Grid& g, const double* vel, const double* pts, int npts, const double plo[3], double* out) {
+    KS_LAUNCH(c, k_act_sample, nblocks(npts, 64), 64, g, vel, pts, npts, plo[0], plo[1], plo[2], out);
+}
+void launch_act_spread(Ctx& c, const Grid& g, double* act, const double* pts, int npts, const double ax[3], double eps, const double plo[3],
+                       const int lo[3], const int hi[3]) {
+    const int n0 = hi[0] - lo[0] + 1, n1 = hi[1] - lo[1] + 1, n2 = hi[2] - lo[2] + 1;
+    if (n0 <= 0 || n1 <= 0 || n2 <= 0) return;
+    KS_LAUNCH(c, k_act_spread, nblocks((long long)n0 * n1 * n2, BS), BS, g, act, pts, npts, ax[0], ax[1], ax[2], eps, plo[0], plo[1], plo[2],
+              lo[0], lo[1], lo[2], n0, n1, n2);
+}
+
+}  // namespace ks

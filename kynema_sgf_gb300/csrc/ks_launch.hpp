@@ -1,0 +1,93 @@
+// Host-side declarations of the kernel launchers (one per device pass).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ks_common.cuh"
+
+namespace ks {
+
+struct Ctx {
+    cudaStream_t stream = nullptr;
+    long long launches = 0;
+};
+
+struct Scalars {  // values fed to the pointwise kernels
+    double rho, mu, smag_fac;
+    int smag;
+    int geo, cor, body, act;
+    double gf[3];
+    double east[3], north[3], up[3];
+    double corfac, sinphi, cosphi, hfac;
+    double body_force[3];
+};
+
+// ---- pointwise / stencil passes (ks_kernels.cu)
+void launch_init_tgv(Ctx& c, const Grid& g, double* vel, const double plo[3], const double L[3]);
+void launch_init_abl(Ctx& c, const Grid& g, double* vel, int loglaw, const double U[3], double ut_over_kappa, double z0,
+                     double amp, double zmax_rel, unsigned long long seed);
+void launch_smagorinsky(Ctx& c, const Grid& g, const double* vel, double* mueff, const Scalars& s);
+void launch_fill(Ctx& c, double* p, double v, long long n);
+void launch_copy(Ctx& c, double* dst, const double* src, long long n);
+void launch_sources(Ctx& c, const Grid& g, const double* vel_old, const double* gp, const double* act, double* src, const Scalars& s);
+void launch_plane_sums(Ctx& c, const Grid& g, const double* vel, double* partials, int* nparts);
+void launch_wall_grad(Ctx& c, const Grid& g, const double* vel_old, const double* mueff, double* wg, int shear_type, double ut2,
+                      double um0, double um1, double vmag, double rho);
+// out = divtau(vel) ; mode 0: plain, mode 1: forces = (src + divtau)/rho also written,
+// mode 2: out = base + 0.5*dt*(divtau(vel) - dold)/rho (RK2 correction into out)
+void launch_divtau(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, int mode,
+                   const double* src, double* forces, const double* base, const double* dold, double dt, double rho);
+void launch_predictor_rhs(Ctx& c, const Grid& g, const double* vel_old, const double* conv, const double* src, const double* divtau,
+                          double* vel, double dt, double rho);
+void launch_proj_pre(Ctx& c, const Grid& g, double* vel, const double* vel_old, const double* gp, double scaling, double rho,
+                     int add_gp, int sub_old);
+void launch_nodal_rhs(Ctx& c, const Grid& g, const double* vel, double* rhs, double* partials, int* nparts);
+void launch_nodal_post(Ctx& c, const Grid& g, const double* phi, double* vel, const double* vel_old, double* gp, double* p,
+                       double sigma, int add_old, int incremental);
+void launch_mac_rhs(Ctx& c, const Grid& g, const double* um, const double* vm, const double* wm, double* rhs, double* partials,
+                    int* nparts);
+void launch_mac_correct(Ctx& c, const Grid& g, const double* phi, double* um, double* vm, double* wm, double beta);
+void launch_cfl(Ctx& c, const Grid& g, const double* vel, const double* src, const double* mueff, double rho, double* partials,
+                int* nparts);
+void launch_ke(Ctx& c, const Grid& g, const double* vel, double rho, double* partials, int* nparts);
+void launch_sub_ratio(Ctx& c, double* a, long long n, const double* s, double den);
+void launch_reduce(Ctx& c, const double* partials, int nparts, int ncomp, int op_max, double* out);
+void launch_act_sample(Ctx& c, const Grid& g, const double* vel, const double* pts, int npts, const double plo[3], double* out);
+void launch_act_spread(Ctx& c, const Grid& g, double* act, const double* pts, int npts, const double ax[3], double eps,
+                       const double plo[3], const int lo[3], const int hi[3]);
+
+// ---- Godunov (ks_godunov.cu)
+struct GodunovBufs {
+    double* ad[3];
+    double* edge[3][3];   // premac: edge[d][n], n != d ; postmac: all n
+    double* tr[3][3][3];  // tr[a][b][n]
+    double* flux[3][3];   // flux[d][n]
+};
+void launch_premac(Ctx& c, const Grid& g, const double* vel_old, const double* forces, double dt, GodunovBufs& B, double* mac[3]);
+void launch_advection(Ctx& c, const Grid& g, const double* vel_old, const double* forces, const double* mac[3], double dt, double rho,
+                      GodunovBufs& B, double* conv);
+
+// ---- multigrid (ks_mg.cu)
+struct CCLevelDev {
+    int nx, ny, nz, zper;
+    double ix2, iy2, iz2;
+    double *phi, *rhs, *res;
+};
+struct NDLevelDev {
+    int nx, ny, nz;  // nodes
+    int zper;
+    double W[27];
+    double *phi, *rhs, *res, *tmp;
+};
+void launch_cc_gsrb(Ctx& c, const CCLevelDev& L, double beta, int color);
+void launch_cc_resid(Ctx& c, const CCLevelDev& L, double beta, double* partials, int* nparts);
+void launch_cc_restrict(Ctx& c, const CCLevelDev& F, const CCLevelDev& C);
+void launch_cc_prolong(Ctx& c, const CCLevelDev& F, const CCLevelDev& C);
+void launch_cc_bottom(Ctx& c, const CCLevelDev& L, double beta, int sweeps);
+void launch_nd_jacobi(Ctx& c, const NDLevelDev& L, double sigma, double omega, const double* in, double* out);
+void launch_nd_resid(Ctx& c, const NDLevelDev& L, double sigma, double* partials, int* nparts);
+void launch_nd_restrict(Ctx& c, const NDLevelDev& F, const NDLevelDev& C);
+void launch_nd_prolong(Ctx& c, const NDLevelDev& F, const NDLevelDev& C);
+void launch_nd_bottom(Ctx& c, const NDLevelDev& L, double sigma, double omega, int sweeps);
+
+}  // namespace ks

@@ -1,0 +1,277 @@
+// Geometric multigrid kernels for the two Poisson problems of the step.
+//
+// MAC projection (cell-centred, 7-point, beta = 1/rho0): red-black
+// Gauss-Seidel with the exact local solve at Neumann z walls, residual with a
+// max-norm partial, 8-cell average restriction, piecewise-constant
+// prolongation, single-CTA bottom sweeps.
+//
+// Nodal projection (node-centred, 27-point Q1 finite-element Laplacian times
+// sigma = dt/rho0): weighted Jacobi, residual, full-weighting restriction
+// (the transpose of trilinear prolongation over 8), trilinear prolongation,
+// single-CTA bottom sweeps.  Wall-bounded z uses mirror images of the
+// node values about the boundary node plane.
+#include "ks_launch.hpp"
+
+namespace ks {
+
+namespace {
+
+constexpr int BS = 256;
+constexpr int MAXPARTS = 1216;
+
+template <int OPMAX>
+__device__ inline double bred(double v) {
+    __shared__ double sh[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        const double x = __shfl_down_sync(0xffffffffu, v, o);
+        v = OPMAX ? fmax(v, x) : v + x;
+    }
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    const int nw = (blockDim.x + 31) >> 5;
+    v = (threadIdx.x < nw) ? sh[threadIdx.x] : (OPMAX ? -1.0e300 : 0.0);
+    if (w == 0)
+        for (int o = 16; o > 0; o >>= 1) {
+            const double x = __shfl_down_sync(0xffffffffu, v, o);
+            v = OPMAX ? fmax(v, x) : v + x;
+        }
+    return v;
+}
+
+inline int parts_for(long long n) {
+    long long b = (n + BS - 1) / BS;
+    return (int)(b < MAXPARTS ? (b < 1 ? 1 : b) : MAXPARTS);
+}
+
+// ---------------------------------------------------------------- cell-centred
+__device__ inline long long ci3(const CCLevelDev& L, int i, int j, int k) { return ((long long)k * L.ny + j) * L.nx + i; }
+
+// beta * laplacian at (i,j,k) and its diagonal
+__device__ inline void cc_ax(const CCLevelDev& L, const double* p, double beta, int i, int j, int k, double& Ax, double& dg) {
+    const int ip = i + 1 == L.nx ? 0 : i + 1, im = i == 0 ? L.nx - 1 : i - 1;
+    const int jp = j + 1 == L.ny ? 0 : j + 1, jm = j == 0 ? L.ny - 1 : j - 1;
+    double s = L.ix2 * (p[ci3(L, ip, j, k)] + p[ci3(L, im, j, k)]) + L.iy2 * (p[ci3(L, i, jp, k)] + p[ci3(L, i, jm, k)]);
+    double d = 2.0 * L.ix2 + 2.0 * L.iy2;
+    if (L.zper) {
+        const int km = k == 0 ? L.nz - 1 : k - 1;
+        s += L.iz2 * p[ci3(L, i, j, km)];
+        d += L.iz2;
+        const int kp = k + 1 == L.nz ? 0 : k + 1;
+        s += L.iz2 * p[ci3(L, i, j, kp)];
+        d += L.iz2;
+    } else {
+        if (k > 0) { s += L.iz2 * p[ci3(L, i, j, k - 1)]; d += L.iz2; }
+        if (k < L.nz - 1) { s += L.iz2 * p[ci3(L, i, j, k + 1)]; d += L.iz2; }
+    }
+    Ax = beta * (s - d * p[ci3(L, i, j, k)]);
+    dg = -beta * d;
+}
+
+__global__ void k_cc_gsrb(CCLevelDev L, double beta, int color) {
+    const long long half = (long long)L.nx * L.ny * L.nz / 2;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= half) return;
+    const int hx = L.nx / 2;
+    const int i2 = (int)(t % hx);
+    const long long r = t / hx;
+    const int j = (int)(r % L.ny), k = (int)(r / L.ny);
+    const int i = 2 * i2 + ((j + k + color) & 1);
+    double Ax, dg;
+    cc_ax(L, L.phi, beta, i, j, k, Ax, dg);
+    const long long c = ci3(L, i, j, k);
+    L.phi[c] += (L.rhs[c] - Ax) / dg;
+}
+
+__global__ void k_cc_resid(CCLevelDev L, double beta, double* parts) {
+    const long long N = (long long)L.nx * L.ny * L.nz;
+    double mx = 0.0;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N; t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % L.nx);
+        const long long r = t / L.nx;
+        const int j = (int)(r % L.ny), k = (int)(r / L.ny);
+        double Ax, dg;
+        cc_ax(L, L.phi, beta, i, j, k, Ax, dg);
+        const double v = L.rhs[t] - Ax;
+        L.res[t] = v;
+        mx = fmax(mx, fabs(v));
+    }
+    mx = bred<1>(mx);
+    if (threadIdx.x == 0 && parts) parts[blockIdx.x] = mx;
+}
+
+__global__ void k_cc_restrict(CCLevelDev F, CCLevelDev C) {
+    const long long N = (long long)C.nx * C.ny * C.nz;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= N) return;
+    const int i = (int)(t % C.nx);
+    const long long r = t / C.nx;
+    const int j = (int)(r % C.ny), k = (int)(r / C.ny);
+    double s = 0.0;
+    for (int c = 0; c < 2; ++c)
+        for (int b = 0; b < 2; ++b)
+            for (int a = 0; a < 2; ++a) s += F.res[ci3(F, 2 * i + a, 2 * j + b, 2 * k + c)];
+    C.rhs[t] = 0.125 * s;
+    C.phi[t] = 0.0;
+}
+
+__global__ void k_cc_prolong(CCLevelDev F, CCLevelDev C) {
+    const long long N = (long long)F.nx * F.ny * F.nz;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= N) return;
+    const int i = (int)(t % F.nx);
+    const long long r = t / F.nx;
+    const int j = (int)(r % F.ny), k = (int)(r / F.ny);
+    F.phi[t] += C.phi[ci3(C, i / 2, j / 2, k / 2)];
+}
+
+__global__ void k_cc_bottom(CCLevelDev L, double beta, int sweeps) {
+    const long long N = (long long)L.nx * L.ny * L.nz;
+    for (int s = 0; s < sweeps; ++s)
+        for (int color = 0; color < 2; ++color) {
+            for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+                const int i = (int)(t % L.nx);
+                const long long r = t / L.nx;
+                const int j = (int)(r % L.ny), k = (int)(r / L.ny);
+                if (((i + j + k) & 1) != color) continue;
+                double Ax, dg;
+                cc_ax(L, L.phi, beta, i, j, k, Ax, dg);
+                L.phi[t] += (L.rhs[t] - Ax) / dg;
+            }
+            __syncthreads();
+        }
+}
+
+// ---------------------------------------------------------------- nodal
+__device__ inline double nd_at(const NDLevelDev& L, const double* p, int i, int j, int k) {
+    i = i < 0 ? i + L.nx : (i >= L.nx ? i - L.nx : i);
+    j = j < 0 ? j + L.ny : (j >= L.ny ? j - L.ny : j);
+    if (L.zper) k = k < 0 ? k + L.nz : (k >= L.nz ? k - L.nz : k);
+    else k = k < 0 ? -k : (k >= L.nz ? 2 * (L.nz - 1) - k : k);
+    return p[((long long)k * L.ny + j) * L.nx + i];
+}
+
+__device__ inline double nd_ax(const NDLevelDev& L, const double* p, double sigma, int i, int j, int k) {
+    double s = 0.0;
+    for (int c = -1; c <= 1; ++c)
+        for (int b = -1; b <= 1; ++b)
+            for (int a = -1; a <= 1; ++a) s += L.W[((c + 1) * 3 + b + 1) * 3 + a + 1] * nd_at(L, p, i + a, j + b, k + c);
+    return sigma * s;
+}
+
+__global__ void k_nd_jacobi(NDLevelDev L, double sigma, double omega, const double* in, double* out) {
+    const long long N = (long long)L.nx * L.ny * L.nz;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= N) return;
+    const int i = (int)(t % L.nx);
+    const long long r = t / L.nx;
+    const int j = (int)(r % L.ny), k = (int)(r / L.ny);
+    const double diag = sigma * L.W[13];
+    out[t] = in[t] + omega * (L.rhs[t] - nd_ax(L, in, sigma, i, j, k)) / diag;
+}
+
+__global__ void k_nd_resid(NDLevelDev L, double sigma, double* parts) {
+    const long long N = (long long)L.nx * L.ny * L.nz;
+    double mx = 0.0;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N; t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % L.nx);
+        const long long r = t / L.nx;
+        const int j = (int)(r % L.ny), k = (int)(r / L.ny);
+        const double v = L.rhs[t] - nd_ax(L, L.phi, sigma, i, j, k);
+        L.res[t] = v;
+        mx = fmax(mx, fabs(v));
+    }
+    mx = bred<1>(mx);
+    if (threadIdx.x == 0 && parts) parts[blockIdx.x] = mx;
+}
+
+__global__ void k_nd_restrict(NDLevelDev F, NDLevelDev C) {
+    const long long N = (long long)C.nx * C.ny * C.nz;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= N) return;
+    const int i = (int)(t % C.nx);
+    const long long r = t / C.nx;
+    const int j = (int)(r % C.ny), k = (int)(r / C.ny);
+    const double w1[3] = {0.25, 0.5, 0.25};
+    double s = 0.0;
+    for (int c = -1; c <= 1; ++c)
+        for (int b = -1; b <= 1; ++b)
+            for (int a = -1; a <= 1; ++a) s += w1[a + 1] * w1[b + 1] * w1[c + 1] * nd_at(F, F.res, 2 * i + a, 2 * j + b, 2 * k + c);
+    C.rhs[t] = s;
+    C.phi[t] = 0.0;
+}
+
+__global__ void k_nd_prolong(NDLevelDev F, NDLevelDev C) {
+    const long long N = (long long)F.nx * F.ny * F.nz;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= N) return;
+    const int i = (int)(t % F.nx);
+    const long long r = t / F.nx;
+    const int j = (int)(r % F.ny), k = (int)(r / F.ny);
+    const int ci = i >> 1, cj = j >> 1, ck = k >> 1, oi = i & 1, oj = j & 1, ok = k & 1;
+    double s = 0.0;
+    for (int c = 0; c <= ok; ++c)
+        for (int b = 0; b <= oj; ++b)
+            for (int a = 0; a <= oi; ++a) s += nd_at(C, C.phi, ci + a, cj + b, ck + c);
+    F.phi[t] += s / (double)((1 + oi) * (1 + oj) * (1 + ok));
+}
+
+__global__ void k_nd_bottom(NDLevelDev L, double sigma, double omega, int sweeps) {
+    const long long N = (long long)L.nx * L.ny * L.nz;
+    const double diag = sigma * L.W[13];
+    for (int s = 0; s < sweeps; ++s) {
+        for (long long t = threadIdx.x; t < N; t += blockDim.x) {
+            const int i = (int)(t % L.nx);
+            const long long r = t / L.nx;
+            const int j = (int)(r % L.ny), k = (int)(r / L.ny);
+            L.tmp[t] = L.phi[t] + omega * (L.rhs[t] - nd_ax(L, L.phi, sigma, i, j, k)) / diag;
+        }
+        __syncthreads();
+        for (long long t = threadIdx.x; t < N; t += blockDim.x) L.phi[t] = L.tmp[t];
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+#define KS_LAUNCH(c, kern, grid, block, ...)                   \
+    do {                                                       \
+        kern<<<(grid), (block), 0, (c).stream>>>(__VA_ARGS__); \
+        ++(c).launches;                                        \
+    } while (0)
+
+void launch_cc_gsrb(Ctx& c, const CCLevelDev& L, double beta, int color) {
+    KS_LAUNCH(c, k_cc_gsrb, nblocks((long long)L.nx * L.ny * L.nz / 2, BS), BS, L, beta, color);
+}
+void launch_cc_resid(Ctx& c, const CCLevelDev& L, double beta, double* parts, int* np) {
+    const int n = parts_for((long long)L.nx * L.ny * L.nz);
+    if (np) *np = n;
+    KS_LAUNCH(c, k_cc_resid, n, BS, L, beta, parts);
+}
+void launch_cc_restrict(Ctx& c, const CCLevelDev& F, const CCLevelDev& C) {
+    KS_LAUNCH(c, k_cc_restrict, nblocks((long long)C.nx * C.ny * C.nz, BS), BS, F, C);
+}
+void launch_cc_prolong(Ctx& c, const CCLevelDev& F, const CCLevelDev& C) {
+    KS_LAUNCH(c, k_cc_prolong, nblocks((long long)F.nx * F.ny * F.nz, BS), BS, F, C);
+}
+void launch_cc_bottom(Ctx& c, const CCLevelDev& L, double beta, int sweeps) { KS_LAUNCH(c, k_cc_bottom, 1, 256, L, beta, sweeps); }
+void launch_nd_jacobi(Ctx& c, const NDLevelDev& L, double sigma, double omega, const double* in, double* out) {
+    KS_LAUNCH(c, k_nd_jacobi, nblocks((long long)L.nx * L.ny * L.nz, BS), BS, L, sigma, omega, in, out);
+}
+void launch_nd_resid(Ctx& c, const NDLevelDev& L, double sigma, double* parts, int* np) {
+    const int n = parts_for((long long)L.nx * L.ny * L.nz);
+    if (np) *np = n;
+    KS_LAUNCH(c, k_nd_resid, n, BS, L, sigma, parts);
+}
+void launch_nd_restrict(Ctx& c, const NDLevelDev& F, const NDLevelDev& C) {
+    KS_LAUNCH(c, k_nd_restrict, nblocks((long long)C.nx * C.ny * C.nz, BS), BS, F, C);
+}
+void launch_nd_prolong(Ctx& c, const NDLevelDev& F, const NDLevelDev& C) {
+    KS_LAUNCH(c, k_nd_prolong, nblocks((long long)F.nx * F.ny * F.nz, BS), BS, F, C);
+}
+void launch_nd_bottom(Ctx& c, const NDLevelDev& L, double sigma, double omega, int sweeps) {
+    KS_LAUNCH(c, k_nd_bottom, 1, 256, L, sigma, omega, sweeps);
+}
+
+}  // namespace ks

@@ -1,0 +1,109 @@
+"""Input decks (ParmParse text) for the workloads used by tests and bench.
+
+Every deck uses the reference's keys; the ``ks_init.*`` keys select the
+synthetic initial fields (seeded noise) that the reference cannot produce.
+"""
+import math
+
+TWO_PI = 2.0 * math.pi
+
+
+def tgv(n=64, steps=20, cfl=0.5, rtol=1e-11):
+    """Taylor-Green vortex, Re = 1600, triply periodic cube of side 2 pi."""
+    return f"""
+geometry.prob_lo = 0 0 0
+geometry.prob_hi = {TWO_PI!r} {TWO_PI!r} {TWO_PI!r}
+geometry.is_periodic = 1 1 1
+amr.n_cell = {n} {n} {n}
+amr.max_level = 0
+incflo.physics = TaylorGreenVortex
+incflo.density = 1.0
+transport.viscosity = 0.000625
+turbulence.model = Laminar
+incflo.use_godunov = 1
+incflo.godunov_type = ppm
+incflo.diffusion_type = 0
+nodal_proj.mg_rtol = {rtol}
+time.cfl = {cfl}
+time.fixed_dt = -1
+time.max_step = {steps}
+"""
+
+
+def abl(nx=256, ny=256, nz=128, steps=100, dx=20.0, cfl=0.9, seed=42):
+    """Neutral ABL LES: periodic x/y, wall-model bottom, slip top,
+    Smagorinsky Cs = 0.135, geostrophic forcing for 8 m/s with Coriolis."""
+    return f"""
+geometry.prob_lo = 0 0 0
+geometry.prob_hi = {nx * dx} {ny * dx} {nz * dx}
+geometry.is_periodic = 1 1 0
+amr.n_cell = {nx} {ny} {nz}
+amr.max_level = 0
+zlo.type = wall_model
+zhi.type = slip_wall
+incflo.physics = ABL
+incflo.density = 1.225
+transport.viscosity = 1.8e-5
+turbulence.model = Smagorinsky
+Smagorinsky_coeffs.Cs = 0.135
+ICNS.source_terms = GeostrophicForcing CoriolisForcing
+CoriolisForcing.latitude = 45.0
+GeostrophicForcing.geostrophic_wind = 8 0 0
+ABL.kappa = 0.41
+ABL.surface_roughness_z0 = 0.1
+ABL.wall_shear_stress_type = moeng
+incflo.use_godunov = 1
+incflo.godunov_type = ppm
+incflo.diffusion_type = 0
+time.cfl = {cfl}
+time.max_step = {steps}
+ks_init.loglaw_utop = 8.0
+ks_init.noise_amplitude = 0.5
+ks_init.noise_zmax = 300
+ks_init.noise_seed = {seed}
+"""
+
+
+def disks(nx=128, ny=128, nz=64, steps=40, dcells=16, cts=(0.75, 0.8, 0.7), seed=7, about_center=1, nr=5, nt=20,
+          eps_cells=2.0, cfl=0.9):
+    """Periodic box with uniform 8 m/s inflow plus noise and uniform-Ct disks
+    spaced along x (Gaussian spreading)."""
+    dx = 10.0
+    D = dcells * dx
+    labels = " ".join("T%d" % i for i in range(len(cts)))
+    lines = []
+    for i, ct in enumerate(cts):
+        x = (0.15 + 0.2 * i) * nx * dx
+        lines.append(f"Actuator.T{i}.disk_center = {x} {0.5 * ny * dx} {0.5 * nz * dx}")
+        lines.append(f"Actuator.T{i}.thrust_coeff = {ct!r}")
+    body = "\n".join(lines)
+    return f"""
+geometry.prob_lo = 0 0 0
+geometry.prob_hi = {nx * dx} {ny * dx} {nz * dx}
+geometry.is_periodic = 1 1 1
+amr.n_cell = {nx} {ny} {nz}
+incflo.physics = FreeStream
+incflo.velocity = 8.0 0.0 0.0
+incflo.density = 1.225
+transport.viscosity = 1.8e-5
+turbulence.model = Smagorinsky
+Smagorinsky_coeffs.Cs = 0.135
+ICNS.source_terms = ActuatorForcing
+Actuator.labels = {labels}
+Actuator.type = UniformCtDisk
+Actuator.UniformCtDisk.rotor_diameter = {D}
+Actuator.UniformCtDisk.epsilon = {eps_cells * dx}
+Actuator.UniformCtDisk.num_points_r = {nr}
+Actuator.UniformCtDisk.num_points_t = {nt}
+Actuator.UniformCtDisk.spreading_type = UniformGaussian
+Actuator.UniformCtDisk.disk_normal = 1.0 0.0 0.0
+Actuator.UniformCtDisk.ks_spread_about_center = {about_center}
+{body}
+incflo.use_godunov = 1
+incflo.godunov_type = ppm
+incflo.diffusion_type = 0
+time.cfl = {cfl}
+time.max_step = {steps}
+ks_init.noise_amplitude = 0.2
+ks_init.noise_seed = {seed}
+"""

@@ -1,0 +1,203 @@
+"""ctypes binding of include/ks.h with the reference's incflo method names.
+
+``Incflo`` mirrors ``class incflo`` (src/incflo.H:51-233 in Kynema-SGF):
+``InitData``, ``Evolve``, ``advance``, ``ApplyPredictor``, ``ApplyCorrector``,
+``ApplyProjection`` and ``compute_dt`` keep their names, argument meaning and
+their failure behaviour (an invalid deck raises, ``ApplyCorrector`` on the
+Godunov path raises as unsupported).  Field access by repository name
+(``velocity``, ``p``, ``gp``, ...) replaces ``FieldRepo::get_field``.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+STATUS = {
+    0: "KS_OK", 1: "KS_ERR_DECK", 2: "KS_ERR_UNSUPPORTED", 3: "KS_ERR_NOT_CONVERGED", 4: "KS_ERR_NONFINITE",
+    5: "KS_ERR_OOM", 6: "KS_ERR_ARG", 7: "KS_DONE", 8: "KS_ERR_CUDA",
+}
+KS_DONE = 7
+KS_HOST, KS_DEVICE = 0, 1
+
+FIELDS = ["velocity", "velocity_old", "gp", "p", "src_term", "forces", "diff_term", "conv_term", "velocity_mueff",
+          "u_mac", "v_mac", "w_mac", "actuator_src_term"]
+
+# every symbol declared in include/ks.h
+SYMBOLS = ["ks_create", "ks_destroy", "ks_last_error", "ks_init_data", "ks_compute_dt", "ks_pre_advance",
+           "ks_prepare_time_step", "ks_advance", "ks_apply_predictor", "ks_apply_corrector", "ks_apply_projection",
+           "ks_evolve", "ks_step", "ks_field_layout", "ks_get_field", "ks_set_field", "ks_get_scalar",
+           "ks_last_solver_stats", "ks_set_precision", "ks_synchronize", "ks_kernel_launches"]
+
+
+class KsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (STATUS.get(code, code), msg))
+        self.code = code
+
+
+class _Layout(ctypes.Structure):
+    _fields_ = [("ncomp", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int)]
+
+
+class _Stats(ctypes.Structure):
+    _fields_ = [("mac_iterations", ctypes.c_int), ("mac_initial_residual", ctypes.c_double),
+                ("mac_final_residual", ctypes.c_double), ("nodal_iterations", ctypes.c_int),
+                ("nodal_initial_residual", ctypes.c_double), ("nodal_final_residual", ctypes.c_double)]
+
+
+def library_path():
+    return os.path.join(_HERE, "_build", "libks.so")
+
+
+def build_library(verbose=False):
+    from . import build as _b
+    return _b.build(verbose=verbose)
+
+
+def load_library(path=None):
+    """Load libks.so (raises if it was not built)."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = path or library_path()
+    if not os.path.exists(p):
+        raise KsError(8, "CUDA extension %s is missing: run kynema_sgf_gb300.build_library()" % p)
+    lib = ctypes.CDLL(p)
+    vp, ip, dp = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    lib.ks_create.argtypes = [ctypes.c_char_p, ctypes.POINTER(vp)]
+    lib.ks_destroy.argtypes = [vp]
+    lib.ks_destroy.restype = None
+    lib.ks_last_error.argtypes = [vp]
+    lib.ks_last_error.restype = ctypes.c_char_p
+    for name in ["ks_init_data", "ks_pre_advance", "ks_prepare_time_step", "ks_apply_corrector", "ks_synchronize", "ks_step"]:
+        getattr(lib, name).argtypes = [vp]
+    lib.ks_compute_dt.argtypes = [vp, ctypes.POINTER(dp)]
+    lib.ks_advance.argtypes = [vp, ip]
+    lib.ks_apply_predictor.argtypes = [vp, ip, ip]
+    lib.ks_apply_projection.argtypes = [vp, dp, dp, ip]
+    lib.ks_evolve.argtypes = [vp, ip]
+    lib.ks_field_layout.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(_Layout)]
+    lib.ks_get_field.argtypes = [vp, ctypes.c_char_p, vp, ip]
+    lib.ks_set_field.argtypes = [vp, ctypes.c_char_p, vp, ip]
+    lib.ks_get_scalar.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(dp)]
+    lib.ks_last_solver_stats.argtypes = [vp, ctypes.POINTER(_Stats)]
+    lib.ks_set_precision.argtypes = [vp, ip]
+    lib.ks_kernel_launches.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+class Incflo:
+    """One simulation on cuda:0 driven through the C ABI."""
+
+    def __init__(self, deck_text, lib=None):
+        self._lib = lib or load_library()
+        self._h = ctypes.c_void_p()
+        rc = self._lib.ks_create(deck_text.encode(), ctypes.byref(self._h))
+        if rc != 0:
+            msg = self._lib.ks_last_error(self._h).decode() if self._h else "ks_create failed"
+            self._lib.ks_destroy(self._h)
+            self._h = None
+            raise KsError(rc, msg)
+
+    def _check(self, rc, allow_done=False):
+        if rc == 0 or (allow_done and rc == KS_DONE):
+            return rc
+        raise KsError(rc, self._lib.ks_last_error(self._h).decode())
+
+    def close(self):
+        if self._h:
+            self._lib.ks_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- reference operator surface
+    def InitData(self):
+        self._check(self._lib.ks_init_data(self._h))
+
+    def compute_dt(self):
+        dt = ctypes.c_double()
+        self._check(self._lib.ks_compute_dt(self._h, ctypes.byref(dt)))
+        return dt.value
+
+    def pre_advance(self):
+        self._check(self._lib.ks_pre_advance(self._h))
+
+    def prepare_time_step(self):
+        self._check(self._lib.ks_prepare_time_step(self._h))
+
+    def advance(self, fixed_point_iteration=0):
+        self._check(self._lib.ks_advance(self._h, int(fixed_point_iteration)))
+
+    def ApplyPredictor(self, incremental_projection=False, fixed_point_iteration=0):
+        self._check(self._lib.ks_apply_predictor(self._h, int(bool(incremental_projection)), int(fixed_point_iteration)))
+
+    def ApplyCorrector(self):
+        self._check(self._lib.ks_apply_corrector(self._h))
+
+    def ApplyProjection(self, time, scaling_factor, incremental=False):
+        self._check(self._lib.ks_apply_projection(self._h, float(time), float(scaling_factor), int(bool(incremental))))
+
+    def step(self):
+        """One iteration of the Evolve loop; returns False once the run is finished."""
+        return self._check(self._lib.ks_step(self._h), allow_done=True) == 0
+
+    def Evolve(self, nsteps=1 << 30):
+        self._check(self._lib.ks_evolve(self._h, int(nsteps)))
+
+    # --- fields and scalars
+    def layout(self, name):
+        L = _Layout()
+        self._check(self._lib.ks_field_layout(self._h, name.encode(), ctypes.byref(L)))
+        return (L.ncomp, L.nz, L.ny, L.nx)
+
+    def get_field(self, name, out=None):
+        """Copy a field into a numpy array shaped (ncomp, nz, ny, nx), or into a
+        torch CUDA tensor of that size when ``out`` is one."""
+        shape = self.layout(name)
+        if out is not None and hasattr(out, "data_ptr"):
+            assert out.is_cuda and out.numel() == int(np.prod(shape)) and out.is_contiguous()
+            self._check(self._lib.ks_get_field(self._h, name.encode(), ctypes.c_void_p(out.data_ptr()), KS_DEVICE))
+            return out
+        a = np.empty(shape, dtype=np.float64) if out is None else out
+        self._check(self._lib.ks_get_field(self._h, name.encode(), a.ctypes.data_as(ctypes.c_void_p), KS_HOST))
+        return a
+
+    def set_field(self, name, value):
+        shape = self.layout(name)
+        if hasattr(value, "data_ptr") and getattr(value, "is_cuda", False):
+            assert value.numel() == int(np.prod(shape)) and value.is_contiguous()
+            self._check(self._lib.ks_set_field(self._h, name.encode(), ctypes.c_void_p(value.data_ptr()), KS_DEVICE))
+            return
+        a = np.ascontiguousarray(value, dtype=np.float64).reshape(shape)
+        self._check(self._lib.ks_set_field(self._h, name.encode(), a.ctypes.data_as(ctypes.c_void_p), KS_HOST))
+
+    def scalar(self, name):
+        v = ctypes.c_double()
+        self._check(self._lib.ks_get_scalar(self._h, name.encode(), ctypes.byref(v)))
+        return v.value
+
+    def solver_stats(self):
+        s = _Stats()
+        self._check(self._lib.ks_last_solver_stats(self._h, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in _Stats._fields_}
+
+    def set_precision(self, precision):
+        self._check(self._lib.ks_set_precision(self._h, int(precision)))
+
+    def synchronize(self):
+        self._check(self._lib.ks_synchronize(self._h))
+
+    def kernel_launches(self):
+        c = ctypes.c_longlong()
+        self._check(self._lib.ks_kernel_launches(self._h, ctypes.byref(c)))
+        return c.value
