@@ -1,0 +1,304 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the single-level incompressible advance.
+
+Workload: neutral ABL LES, 256 x 256 x 128 cells on 5120 x 5120 x 1280 m,
+FP64, Godunov PPM advection, MAC and nodal projections by geometric
+multigrid, Smagorinsky Cs = 0.135, geostrophic (8 m/s) + Coriolis forcing,
+wall-model bottom, slip top, CFL 0.9, log-law start with seeded +-0.5 m/s
+noise below 300 m (synthetic input: no dataset exists for this path).
+
+One "step" is one iteration of the Evolve loop (compute_dt, pre-advance
+work, ApplyPredictor with both projections).  The state (~6 GB) is larger
+than L2 (129 MB), so no L2 flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun each rank advances its own replica (the path is replicas-only
+on one GPU each); value = all ranks' cell-steps / max rank time.  The
+reference arm times the CPU restatement (the reference's own build cannot be
+compiled: its AMReX / AMReX-Hydro submodules are absent) on the host cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mcell-steps/s at 256^3 (FP64 vs mixed-precision at stated error) + adjoint/forward cost ratio"
+UNIT = "Mcell-steps/s"
+WORKLOAD = "ABL LES 256x256x128 FP64 (5120x5120x1280 m, Smagorinsky, geostrophic+Coriolis, wall model, CFL 0.9)"
+CPU_SAMPLE = (128, 128, 64)  # same dx, physics and deck as the workload, 1/8 of the cells
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--profile-all", action="store_true", help="print the per-kernel breakdown to stderr")
+    p.add_argument("--size", default="256,256,128")
+    p.add_argument("--cpu-worker", default="", help=argparse.SUPPRESS)
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------- CPU side
+def cpu_worker(spec):
+    """Runs in a child process: times the oracle on the bounded CPU sample."""
+    warm, steps = (int(x) for x in spec.split(","))
+    from kynema_sgf_gb300 import decks
+    from oracle.oracle import Oracle
+    nx, ny, nz = CPU_SAMPLE
+    deck = decks.abl(nx, ny, nz, steps=10 ** 6) + "\nincflo.do_initial_proj = 0\nincflo.initial_iterations = 0\n"
+    o = Oracle(deck)
+    for _ in range(warm):
+        o.step()
+    per = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        o.step()
+        per.append(time.perf_counter() - t0)
+    print(json.dumps({"per_step_s": per, "cells": nx * ny * nz}))
+
+
+def run_cpu(warm, steps):
+    from oracle import oracle as orc
+    orc.build()
+    cores = os.cpu_count() or 1
+    env = dict(os.environ, OMP_NUM_THREADS=str(cores), OMP_PROC_BIND="spread", OMP_PLACES="cores")
+    r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-worker", "%d,%d" % (warm, steps)],
+                       capture_output=True, text=True, env=env, cwd=ROOT)
+    if r.returncode != 0:
+        raise RuntimeError("CPU baseline failed: " + r.stderr[-2000:])
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    per = out["per_step_s"]
+    return out["cells"], per, cores
+
+
+def cpu_sample_text(steps):
+    nx, ny, nz = CPU_SAMPLE
+    return ("CPU restatement (oracle/ks_oracle.cpp, g++ -O3 -fopenmp) on %dx%dx%d cells of the same ABL deck "
+            "(same dx and physics, 1/8 of the cells), %d timed Evolve step(s) after 1 warm-up, init skipped" % (nx, ny, nz, steps))
+
+
+# ---------------------------------------------------------------- clocks
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ---------------------------------------------------------------- GPU side
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"], "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel):
+    try:
+        t = json.load(open(os.path.join(ROOT, "profiles", "ncu_traffic.json")))
+        return t.get(kernel, {}).get("dram_bytes_per_launch")
+    except Exception:
+        return None
+
+
+def our_arm(args, rank, world, local_rank):
+    import torch
+    import kynema_sgf_gb300 as ks
+    from kynema_sgf_gb300 import decks
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+    torch.cuda.set_device(local_rank)
+    nx, ny, nz = (int(x) for x in args.size.split(","))
+    sim = ks.Incflo(decks.abl(nx, ny, nz, steps=10 ** 9))
+    sim.InitData()
+    cells = sim.scalar("ncells")
+    # warm-up; the last warm-up step times every kernel to pick the dominant one
+    for w in range(args.warmup):
+        if w == args.warmup - 1:
+            sim.profile_kernels("*")
+        sim.step()
+    breakdown = sim.profile_report()
+    dominant = max(breakdown, key=lambda k: breakdown[k][1])
+    if args.profile_all and rank == 0:
+        tot = sum(v[1] for v in breakdown.values())
+        for k, v in sorted(breakdown.items(), key=lambda kv: -kv[1][1]):
+            sys.stderr.write("%-22s %6d launches %9.3f ms %5.1f%% %8.1f GB/s\n" % (k, v[0], v[1], 100 * v[1] / tot,
+                                                                                  v[2] / (v[1] * 1e-3) / 1e9 if v[1] else 0))
+    sim.profile_kernels(dominant)
+    stream = torch.cuda.ExternalStream(sim.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(local_rank)
+    if dist:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    l0 = sim.kernel_launches()
+    mac_it, nod_it = [], []
+    clocks.start()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        sim.step()
+        mac_it.append(sim.scalar("mac_iters"))
+        nod_it.append(sim.scalar("nodal_iters"))
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    if dist:
+        tdist.barrier()
+    launches = sim.kernel_launches() - l0
+    ms = ev0.elapsed_time(ev1)
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if dist:
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    dom = sim.profile_report().get(dominant, (0, 0.0, 0.0))
+    sim.profile_kernels("")
+    value = cells * args.steps * world / (ms_max * 1e-3) / 1e6
+
+    # end to end through the public API: host inputs in, host result out
+    e2e = None
+    if not args.no_e2e:
+        shapes = {f: sim.layout(f) for f in ("velocity", "gp", "p")}
+        host = {f: torch.empty(int(torch.tensor(s).prod()), dtype=torch.float64, pin_memory=True) for f, s in shapes.items()}
+        for f in host:
+            sim.get_field(f, out=host[f])
+        if dist:
+            tdist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            for f in ("velocity", "gp", "p"):
+                sim.set_field(f, host[f])
+            sim.step()
+            sim.get_field("velocity", out=host["velocity"])
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        te = torch.tensor([el], dtype=torch.float64, device="cuda")
+        if dist:
+            tdist.all_reduce(te, op=tdist.ReduceOp.MAX)
+        el = float(te.item())
+        hin = sum(host[f].numel() * 8 for f in host)
+        e2e = {"value": cells * args.steps * world / el / 1e6, "unit": UNIT, "h2d_bytes_per_step": hin,
+               "d2h_bytes_per_step": host["velocity"].numel() * 8}
+    return dict(value=value, ms=ms_max, cells=cells, launches=launches, dominant=dominant, dom=dom, clocks=clk, e2e=e2e,
+                mac=statistics.mean(mac_it), nodal=statistics.mean(nod_it), size=(nx, ny, nz))
+
+
+def main():
+    args = parse()
+    if args.cpu_worker:
+        cpu_worker(args.cpu_worker)
+        return
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cells, per, cores = run_cpu(args.warmup, args.steps)
+        v = cells * len(per) / sum(per) / 1e6
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * sum(per) / len(per), "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "sample": "%dx%dx%d" % CPU_SAMPLE},
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": cpu_sample_text(len(per))},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(local_rank)
+        tdist.init_process_group("nccl")
+    r = our_arm(args, rank, world, local_rank)
+    if rank != 0:
+        if world > 1:
+            import torch.distributed as tdist
+            tdist.destroy_process_group()
+        return
+    peak, peak_kind = peaks()
+    n_l, ms_l, by_l = r["dom"]
+    achieved = (by_l / n_l) / ((ms_l / n_l) * 1e-3) / 1e9 if n_l else None
+    traffic = ncu_traffic(r["dominant"])
+    nx, ny, nz = r["size"]
+    line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (log-law + seeded uniform noise, SplitMix64 seed 42)",
+            "config": {"workload": WORKLOAD, "cells": [nx, ny, nz], "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "state larger than L2 (no flush)", "mac_vcycles_per_step": r["mac"],
+                       "nodal_vcycles_per_step": r["nodal"]},
+            "roofline": {"bound": "hbm", "kernel": r["dominant"], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": (achieved / peak) if achieved else None, "traffic": traffic, "peak_kind": peak_kind,
+                         "launches": n_l, "avg_launch_us": 1e3 * ms_l / n_l if n_l else None,
+                         "algorithmic_bytes_per_launch": by_l / n_l if n_l else None},
+            "gpu_launches": r["launches"], "clocks": r["clocks"], "e2e": r["e2e"]}
+    # whole-step algorithmic traffic: 8 * (125 + 20.86 * V-cycles) bytes per cell
+    bstep = 8.0 * (125.0 + 20.86 * (r["mac"] + r["nodal"])) * r["cells"]
+    line["step_roofline"] = {"algorithmic_bytes_per_step": bstep, "achieved_GBs": bstep / (r["ms"] / args.steps * 1e-3) / 1e9,
+                             "frac": bstep / (r["ms"] / args.steps * 1e-3) / 1e9 / peak}
+    if world == 1 and not args.no_cpu_baseline:
+        try:
+            cells, per, cores = run_cpu(1, 2)
+            line["cpu_baseline"] = {"value": cells * len(per) / sum(per) / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
+                                    "sample": cpu_sample_text(len(per))}
+        except Exception as e:  # reported, never silently replaced
+            line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": "failed: %s" % e}
+    print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -93,6 +93,16 @@ int ks_set_precision(ks_handle* h, int precision);
 int ks_synchronize(ks_handle* h);
 int ks_kernel_launches(const ks_handle* h, long long* count);
 
+/* Instrumentation (no counterpart in the reference): the CUDA stream all
+ * kernels of the handle run on, and CUDA-event timing of kernels whose name
+ * matches `kernel` ("*" = every kernel, NULL or "" = off).  The report is
+ * "name launches total_ms algorithmic_bytes" lines (bytes: every distinct array
+ * each launch reads or writes, counted once); it returns the bytes needed (including the
+ * terminating zero) and clears the accumulated totals. */
+int ks_get_stream(ks_handle* h, void** stream);
+int ks_profile_kernels(ks_handle* h, const char* kernel);
+long long ks_profile_report(ks_handle* h, char* buf, long long len);
+
 #ifdef __cplusplus
 }
 #endif

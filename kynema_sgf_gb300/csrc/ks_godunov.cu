@@ -315,50 +315,54 @@ __global__ void k_adv_div_s(Grid g, FluxPtrs F, double* conv) {
 
 }  // namespace
 
-#define KS_LAUNCH(c, kern, grid, block, ...)                   \
-    do {                                                       \
-        kern<<<(grid), (block), 0, (c).stream>>>(__VA_ARGS__); \
-        ++(c).launches;                                        \
-    } while (0)
 
 void launch_premac(Ctx& c, const Grid& g, const double* vel, const double* forces, double dt, GodunovBufs& B, double* mac[3]) {
+    const double B8 = 8.0;
     for (int d = 0; d < 3; ++d) {
         const int n1 = (d + 1) % 3, n2 = (d + 2) % 3;
-        KS_LAUNCH(c, k_pm_faces, nblocks(nfaces(g, d), BS), BS, g, d, vel, dt, B.ad[d], B.edge[d][n1], B.edge[d][n2]);
+        const double nf = (double)nfaces(g, d);
+        KS_LAUNCH(c, k_pm_faces, nblocks(nfaces(g, d), BS), BS, B8 * (3.0 * g.N + 3.0 * nf), g, d, vel, dt, B.ad[d], B.edge[d][n1],
+                  B.edge[d][n2]);
     }
     // (a, b, n): states on a-faces of component n corrected along b
     const int tp[6][3] = {{1, 2, 0}, {2, 1, 0}, {0, 2, 1}, {2, 0, 1}, {0, 1, 2}, {1, 0, 2}};
     for (auto& p : tp) {
         const int a = p[0], b = p[1], n = p[2];
-        KS_LAUNCH(c, k_pm_trans, nblocks(nfaces(g, a), BS), BS, g, a, b, n, vel, dt, B.ad[a], B.ad[b], B.edge[b][n], B.tr[a][b][0]);
+        const double bytes = B8 * (2.0 * g.N + 2.0 * nfaces(g, a) + 2.0 * nfaces(g, b));
+        KS_LAUNCH(c, k_pm_trans, nblocks(nfaces(g, a), BS), BS, bytes, g, a, b, n, vel, dt, B.ad[a], B.ad[b], B.edge[b][n], B.tr[a][b][0]);
     }
     for (int d = 0; d < 3; ++d) {
         const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
-        KS_LAUNCH(c, k_pm_final, nblocks(nfaces(g, d), BS), BS, g, d, vel, forces, dt, B.ad[0], B.ad[1], B.ad[2], B.tr[b1][b2][0],
+        const double bytes = B8 * (2.0 * g.N + 2.0 * nfaces(g, d) + 2.0 * nfaces(g, b1) + 2.0 * nfaces(g, b2));
+        KS_LAUNCH(c, k_pm_final, nblocks(nfaces(g, d), BS), BS, bytes, g, d, vel, forces, dt, B.ad[0], B.ad[1], B.ad[2], B.tr[b1][b2][0],
                   B.tr[b2][b1][0], mac[d]);
     }
 }
 
 void launch_advection(Ctx& c, const Grid& g, const double* vel, const double* forces, const double* mac[3], double dt, double rho,
                       GodunovBufs& B, double* conv) {
+    const double B8 = 8.0;
     FaceVel fv{{mac[0], mac[1], mac[2]}};
     for (int a = 0; a < 3; ++a)
-        KS_LAUNCH(c, k_adv_faces, nblocks(nfaces(g, a), BS), BS, g, a, vel, rho, fv, dt, B.edge[a][0], B.edge[a][1], B.edge[a][2]);
+        KS_LAUNCH(c, k_adv_faces, nblocks(nfaces(g, a), BS), BS, B8 * (3.0 * g.N + 4.0 * nfaces(g, a)), g, a, vel, rho, fv, dt, B.edge[a][0],
+                  B.edge[a][1], B.edge[a][2]);
     for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 3; ++b) {
             if (a == b) continue;
-            KS_LAUNCH(c, k_adv_trans, nblocks(nfaces(g, a), BS), BS, g, a, b, vel, rho, fv, dt, B.edge[b][0], B.edge[b][1], B.edge[b][2],
-                      B.tr[a][b][0], B.tr[a][b][1], B.tr[a][b][2]);
+            const double bytes = B8 * (3.0 * g.N + 4.0 * nfaces(g, a) + 4.0 * nfaces(g, b));
+            KS_LAUNCH(c, k_adv_trans, nblocks(nfaces(g, a), BS), BS, bytes, g, a, b, vel, rho, fv, dt, B.edge[b][0], B.edge[b][1],
+                      B.edge[b][2], B.tr[a][b][0], B.tr[a][b][1], B.tr[a][b][2]);
         }
     for (int d = 0; d < 3; ++d) {
         const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
-        KS_LAUNCH(c, k_adv_flux, nblocks(nfaces(g, d), BS), BS, g, d, vel, forces, rho, fv, dt, B.tr[b1][b2][0], B.tr[b1][b2][1],
+        const double bytes = B8 * (6.0 * g.N + 4.0 * nfaces(g, d) + 4.0 * nfaces(g, b1) + 4.0 * nfaces(g, b2));
+        KS_LAUNCH(c, k_adv_flux, nblocks(nfaces(g, d), BS), BS, bytes, g, d, vel, forces, rho, fv, dt, B.tr[b1][b2][0], B.tr[b1][b2][1],
                   B.tr[b1][b2][2], B.tr[b2][b1][0], B.tr[b2][b1][1], B.tr[b2][b1][2], B.flux[d][0], B.flux[d][1], B.flux[d][2]);
     }
     FluxPtrs F;
     for (int d = 0; d < 3; ++d)
         for (int n = 0; n < 3; ++n) F.p[d * 3 + n] = B.flux[d][n];
-    KS_LAUNCH(c, k_adv_div_s, nblocks(g.N, BS), BS, g, F, conv);
+    KS_LAUNCH(c, k_adv_div_s, nblocks(g.N, BS), BS, B8 * (9.0 * g.N + 3.0 * g.N), g, F, conv);
 }
 
 }  // namespace ks

@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -1102,6 +1103,46 @@ int ks_set_precision(ks_handle* h, int precision) {
 }
 
 int ks_synchronize(ks_handle* h) { return guarded(h, [](ks::Sim& s) { s.sync(); return 0; }); }
+
+int ks_get_stream(ks_handle* h, void** stream) {
+    if (!h || !h->sim || !stream) return KS_ERR_ARG;
+    *stream = (void*)h->sim->ctx_.stream;
+    return KS_OK;
+}
+
+int ks_profile_kernels(ks_handle* h, const char* kernel) {
+    return guarded(h, [&](ks::Sim& s) {
+        s.sync();
+        s.ctx_.prof_collect();
+        s.ctx_.acc.clear();
+        s.ctx_.prof = kernel ? kernel : "";
+        return 0;
+    });
+}
+
+long long ks_profile_report(ks_handle* h, char* buf, long long len) {
+    if (!h || !h->sim) return -KS_ERR_ARG;
+    ks::Sim& s = *h->sim;
+    try {
+        s.sync();
+    } catch (const std::exception& e) {
+        h->err = e.what();
+        return -KS_ERR_CUDA;
+    }
+    s.ctx_.prof_collect();
+    std::string out;
+    char line[256];
+    for (auto& kv : s.ctx_.acc) {
+        std::snprintf(line, sizeof(line), "%s %lld %.6f %.0f\n", kv.first.c_str(), kv.second.launches, kv.second.ms, kv.second.bytes);
+        out += line;
+    }
+    const long long need = (long long)out.size() + 1;
+    if (buf && len >= need) {
+        std::memcpy(buf, out.c_str(), (size_t)need);
+        s.ctx_.acc.clear();
+    }
+    return need;
+}
 
 int ks_kernel_launches(const ks_handle* h, long long* count) {
     if (!h || !h->sim || !count) return KS_ERR_ARG;

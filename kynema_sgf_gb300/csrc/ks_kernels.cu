@@ -518,88 +518,90 @@ __global__ void k_act_spread(Grid g, double* act, const double* pts, int npts, d
 }  // namespace
 
 // ---------------------------------------------------------------- launchers
-#define KS_LAUNCH(c, kern, grid, block, ...)                      \
-    do {                                                          \
-        kern<<<(grid), (block), 0, (c).stream>>>(__VA_ARGS__);    \
-        ++(c).launches;                                           \
-    } while (0)
+
+constexpr double B8 = 8.0;  // bytes per FP64 value
 
 void launch_init_tgv(Ctx& c, const Grid& g, double* vel, const double plo[3], const double L[3]) {
-    KS_LAUNCH(c, k_init_tgv, nblocks(g.N, BS), BS, g, vel, plo[0], plo[1], plo[2], L[0], L[1], L[2]);
+    KS_LAUNCH(c, k_init_tgv, nblocks(g.N, BS), BS, B8 * 3 * g.N, g, vel, plo[0], plo[1], plo[2], L[0], L[1], L[2]);
 }
 void launch_init_abl(Ctx& c, const Grid& g, double* vel, int loglaw, const double U[3], double ut_k, double z0, double amp,
                      double zmax_rel, unsigned long long seed) {
-    KS_LAUNCH(c, k_init_abl, nblocks(g.N, BS), BS, g, vel, loglaw, U[0], U[1], U[2], ut_k, z0, amp, zmax_rel, seed);
+    KS_LAUNCH(c, k_init_abl, nblocks(g.N, BS), BS, B8 * 3 * g.N, g, vel, loglaw, U[0], U[1], U[2], ut_k, z0, amp, zmax_rel, seed);
 }
-void launch_fill(Ctx& c, double* p, double v, long long n) { KS_LAUNCH(c, k_fill, nblocks(n, BS), BS, p, v, n); }
-void launch_copy(Ctx& c, double* d, const double* s, long long n) { KS_LAUNCH(c, k_copy, nblocks(n, BS), BS, d, s, n); }
+void launch_fill(Ctx& c, double* p, double v, long long n) { KS_LAUNCH(c, k_fill, nblocks(n, BS), BS, B8 * n, p, v, n); }
+void launch_copy(Ctx& c, double* d, const double* s, long long n) { KS_LAUNCH(c, k_copy, nblocks(n, BS), BS, B8 * 2 * n, d, s, n); }
 void launch_smagorinsky(Ctx& c, const Grid& g, const double* vel, double* mueff, const Scalars& s) {
-    KS_LAUNCH(c, k_smag, nblocks(g.N, BS), BS, g, vel, mueff, s.mu, s.rho, s.smag_fac, s.smag);
+    KS_LAUNCH(c, k_smag, nblocks(g.N, BS), BS, B8 * (s.smag ? 4 : 1) * g.N, g, vel, mueff, s.mu, s.rho, s.smag_fac, s.smag);
 }
 void launch_sources(Ctx& c, const Grid& g, const double* vel_old, const double* gp, const double* act, double* src, const Scalars& s) {
-    KS_LAUNCH(c, k_sources, nblocks(g.N, BS), BS, g, vel_old, gp, act, src, s);
+    KS_LAUNCH(c, k_sources, nblocks(g.N, BS), BS, B8 * (6 + 3 * s.cor + 3 * s.act) * g.N, g, vel_old, gp, act, src, s);
 }
 void launch_plane_sums(Ctx& c, const Grid& g, const double* vel, double* parts, int* np) {
     *np = parts_for((long long)g.nx * g.ny);
-    KS_LAUNCH(c, k_plane_sums, *np, BS, g, vel, parts, *np);
+    KS_LAUNCH(c, k_plane_sums, *np, BS, B8 * 2 * g.nx * g.ny, g, vel, parts, *np);
 }
 void launch_wall_grad(Ctx& c, const Grid& g, const double* vel_old, const double* mueff, double* wg, int type, double ut2, double um0,
                       double um1, double vm, double rho) {
-    KS_LAUNCH(c, k_wall_grad, nblocks((long long)g.nx * g.ny, BS), BS, g, vel_old, mueff, wg, type, ut2, um0, um1, vm, rho);
+    KS_LAUNCH(c, k_wall_grad, nblocks((long long)g.nx * g.ny, BS), BS, B8 * 5 * g.nx * g.ny, g, vel_old, mueff, wg, type, ut2, um0,
+              um1, vm, rho);
 }
 void launch_divtau(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, int mode,
                    const double* src, double* forces, const double* base, const double* dold, double dt, double rho) {
-    KS_LAUNCH(c, k_divtau, nblocks(g.N, BS), BS, g, vel, mueff, wg, out, mode, src, forces, base, dold, dt, rho);
+    const double per_cell = 3 + 1 + 3 + (mode == 1 ? 6 : 0) + (mode == 2 ? 6 : 0);
+    KS_LAUNCH(c, k_divtau, nblocks(g.N, BS), BS, B8 * per_cell * g.N, g, vel, mueff, wg, out, mode, src, forces, base, dold, dt, rho);
 }
 void launch_predictor_rhs(Ctx& c, const Grid& g, const double* vo, const double* conv, const double* src, const double* dtau, double* vel,
                           double dt, double rho) {
-    KS_LAUNCH(c, k_pred_rhs, nblocks(3 * g.N, BS), BS, 3 * g.N, vo, conv, src, dtau, vel, dt, rho);
+    KS_LAUNCH(c, k_pred_rhs, nblocks(3 * g.N, BS), BS, B8 * 15 * g.N, 3 * g.N, vo, conv, src, dtau, vel, dt, rho);
 }
 void launch_proj_pre(Ctx& c, const Grid& g, double* vel, const double* vo, const double* gp, double scaling, double rho, int add_gp,
                      int sub_old) {
-    KS_LAUNCH(c, k_proj_pre, nblocks(3 * g.N, BS), BS, 3 * g.N, vel, vo, gp, scaling, rho, add_gp, sub_old);
+    KS_LAUNCH(c, k_proj_pre, nblocks(3 * g.N, BS), BS, B8 * 3 * (2 + add_gp + sub_old) * g.N, 3 * g.N, vel, vo, gp, scaling, rho, add_gp,
+              sub_old);
 }
 void launch_nodal_rhs(Ctx& c, const Grid& g, const double* vel, double* rhs, double* parts, int* np) {
     const long long M = (long long)g.nx * g.ny * (g.zper ? g.nz : g.nz + 1);
     *np = parts_for(M);
-    KS_LAUNCH(c, k_nodal_rhs, *np, BS, g, vel, rhs, parts, *np);
+    KS_LAUNCH(c, k_nodal_rhs, *np, BS, B8 * (3 * g.N + M), g, vel, rhs, parts, *np);
 }
 void launch_nodal_post(Ctx& c, const Grid& g, const double* phi, double* vel, const double* vo, double* gp, double* p, double sigma,
                        int add_old, int incr) {
-    KS_LAUNCH(c, k_nodal_post_cells, nblocks(g.N, BS), BS, g, phi, vel, vo, gp, sigma, add_old, incr);
     const long long M = (long long)g.nx * g.ny * (g.zper ? g.nz : g.nz + 1);
-    KS_LAUNCH(c, k_nodal_post_nodes, nblocks(M, BS), BS, M, phi, p, incr);
+    KS_LAUNCH(c, k_nodal_post_cells, nblocks(g.N, BS), BS, B8 * (M + (9 + 3 * add_old + 3 * incr) * g.N), g, phi, vel, vo, gp, sigma,
+              add_old, incr);
+    KS_LAUNCH(c, k_nodal_post_nodes, nblocks(M, BS), BS, B8 * (2 + incr) * M, M, phi, p, incr);
 }
 void launch_mac_rhs(Ctx& c, const Grid& g, const double* um, const double* vm, const double* wm, double* rhs, double* parts, int* np) {
     *np = parts_for(g.N);
-    KS_LAUNCH(c, k_mac_rhs, *np, BS, g, um, vm, wm, rhs, parts, *np);
+    KS_LAUNCH(c, k_mac_rhs, *np, BS, B8 * (3 * g.N + g.NFz), g, um, vm, wm, rhs, parts, *np);
 }
 void launch_mac_correct(Ctx& c, const Grid& g, const double* phi, double* um, double* vm, double* wm, double beta) {
-    KS_LAUNCH(c, k_mac_correct, nblocks(g.N, BS), BS, g, phi, um, vm, wm, beta);
+    KS_LAUNCH(c, k_mac_correct, nblocks(g.N, BS), BS, B8 * 7 * g.N, g, phi, um, vm, wm, beta);
 }
 void launch_cfl(Ctx& c, const Grid& g, const double* vel, const double* src, const double* mu, double rho, double* parts, int* np) {
     *np = parts_for(g.N);
-    KS_LAUNCH(c, k_cfl, *np, BS, g, vel, src, mu, rho, parts, *np);
+    KS_LAUNCH(c, k_cfl, *np, BS, B8 * 7 * g.N, g, vel, src, mu, rho, parts, *np);
 }
 void launch_ke(Ctx& c, const Grid& g, const double* vel, double rho, double* parts, int* np) {
     *np = parts_for(g.N);
-    KS_LAUNCH(c, k_ke, *np, BS, g, vel, rho, parts);
+    KS_LAUNCH(c, k_ke, *np, BS, B8 * 3 * g.N, g, vel, rho, parts);
 }
 void launch_reduce(Ctx& c, const double* parts, int np, int ncomp, int op_max, double* out) {
-    KS_LAUNCH(c, k_reduce, ncomp, 256, parts, np, op_max, out);
+    KS_LAUNCH(c, k_reduce, ncomp, 256, B8 * (np + 1) * ncomp, parts, np, op_max, out);
 }
 void launch_sub_ratio(Ctx& c, double* a, long long n, const double* s, double den) {
-    KS_LAUNCH(c, k_sub_ratio, nblocks(n, BS), BS, a, n, s, den);
+    KS_LAUNCH(c, k_sub_ratio, nblocks(n, BS), BS, B8 * 2 * n, a, n, s, den);
 }
 void launch_act_sample(Ctx& c, const Grid& g, const double* vel, const double* pts, int npts, const double plo[3], double* out) {
-    KS_LAUNCH(c, k_act_sample, nblocks(npts, 64), 64, g, vel, pts, npts, plo[0], plo[1], plo[2], out);
+    KS_LAUNCH(c, k_act_sample, nblocks(npts, 64), 64, B8 * 6 * npts, g, vel, pts, npts, plo[0], plo[1], plo[2], out);
 }
 void launch_act_spread(Ctx& c, const Grid& g, double* act, const double* pts, int npts, const double ax[3], double eps, const double plo[3],
                        const int lo[3], const int hi[3]) {
     const int n0 = hi[0] - lo[0] + 1, n1 = hi[1] - lo[1] + 1, n2 = hi[2] - lo[2] + 1;
     if (n0 <= 0 || n1 <= 0 || n2 <= 0) return;
-    KS_LAUNCH(c, k_act_spread, nblocks((long long)n0 * n1 * n2, BS), BS, g, act, pts, npts, ax[0], ax[1], ax[2], eps, plo[0], plo[1], plo[2],
-              lo[0], lo[1], lo[2], n0, n1, n2);
+    const long long M = (long long)n0 * n1 * n2;
+    KS_LAUNCH(c, k_act_spread, nblocks(M, BS), BS, B8 * 6 * M, g, act, pts, npts, ax[0], ax[1], ax[2], eps, plo[0], plo[1], plo[2], lo[0],
+              lo[1], lo[2], n0, n1, n2);
 }
 
 }  // namespace ks

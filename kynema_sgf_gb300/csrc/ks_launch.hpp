@@ -3,14 +3,86 @@
 
 #include <cuda_runtime.h>
 
+#include <cstring>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
 #include "ks_common.cuh"
 
 namespace ks {
 
+// Launch context: the stream every kernel of a handle runs on, a launch
+// counter, and optional CUDA-event timing of selected kernels (by kernel
+// name, or "*" for all) recorded on that same stream.
 struct Ctx {
     cudaStream_t stream = nullptr;
     long long launches = 0;
+    std::string prof;
+    struct Open {
+        std::string name;
+        cudaEvent_t a, b;
+        double bytes;
+    };
+    struct Acc {
+        long long launches = 0;
+        double ms = 0.0, bytes = 0.0;
+    };
+    std::vector<Open> open;
+    std::vector<cudaEvent_t> pool;
+    std::map<std::string, Acc> acc;  // kernel name -> totals
+
+    bool prof_match(const char* name) const { return !prof.empty() && (prof == "*" || prof == name); }
+    cudaEvent_t ev() {
+        cudaEvent_t e;
+        if (!pool.empty()) {
+            e = pool.back();
+            pool.pop_back();
+        } else {
+            cudaEventCreate(&e);
+        }
+        return e;
+    }
+    void prof_begin(const char* name, double bytes) {
+        open.push_back({name, ev(), ev(), bytes});
+        cudaEventRecord(open.back().a, stream);
+    }
+    void prof_end() { cudaEventRecord(open.back().b, stream); }
+    // fold recorded launches into acc (call after the stream is synchronised)
+    void prof_collect() {
+        for (auto& o : open) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, o.a, o.b);
+            auto& a = acc[o.name];
+            a.launches += 1;
+            a.ms += ms;
+            a.bytes += o.bytes;
+            pool.push_back(o.a);
+            pool.push_back(o.b);
+        }
+        open.clear();
+    }
+    ~Ctx() {
+        for (auto& o : open) {
+            cudaEventDestroy(o.a);
+            cudaEventDestroy(o.b);
+        }
+        for (auto e : pool) cudaEventDestroy(e);
+    }
 };
+
+// Launch on the context's stream.  `bytes` is the algorithmic HBM traffic of
+// the launch: every distinct array the kernel reads or writes, counted once,
+// times its element size (stencil neighbours are not counted again).
+#define KS_LAUNCH(c, kern, grid, block, bytes, ...)            \
+    do {                                                       \
+        const bool ks_p_ = (c).prof_match(#kern);              \
+        if (ks_p_) (c).prof_begin(#kern, (double)(bytes));     \
+        kern<<<(grid), (block), 0, (c).stream>>>(__VA_ARGS__); \
+        if (ks_p_) (c).prof_end();                             \
+        ++(c).launches;                                        \
+    } while (0)
 
 struct Scalars {  // values fed to the pointwise kernels
     double rho, mu, smag_fac;

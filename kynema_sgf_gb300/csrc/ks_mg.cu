@@ -235,43 +235,44 @@ __global__ void k_nd_bottom(NDLevelDev L, double sigma, double omega, int sweeps
 
 }  // namespace
 
-#define KS_LAUNCH(c, kern, grid, block, ...)                   \
-    do {                                                       \
-        kern<<<(grid), (block), 0, (c).stream>>>(__VA_ARGS__); \
-        ++(c).launches;                                        \
-    } while (0)
+
+inline double ncc(const CCLevelDev& L) { return (double)L.nx * L.ny * L.nz; }
+inline double nnd(const NDLevelDev& L) { return (double)L.nx * L.ny * L.nz; }
+constexpr double B8 = 8.0;
 
 void launch_cc_gsrb(Ctx& c, const CCLevelDev& L, double beta, int color) {
-    KS_LAUNCH(c, k_cc_gsrb, nblocks((long long)L.nx * L.ny * L.nz / 2, BS), BS, L, beta, color);
+    KS_LAUNCH(c, k_cc_gsrb, nblocks((long long)L.nx * L.ny * L.nz / 2, BS), BS, B8 * 2.0 * ncc(L), L, beta, color);
 }
 void launch_cc_resid(Ctx& c, const CCLevelDev& L, double beta, double* parts, int* np) {
     const int n = parts_for((long long)L.nx * L.ny * L.nz);
     if (np) *np = n;
-    KS_LAUNCH(c, k_cc_resid, n, BS, L, beta, parts);
+    KS_LAUNCH(c, k_cc_resid, n, BS, B8 * 3.0 * ncc(L), L, beta, parts);
 }
 void launch_cc_restrict(Ctx& c, const CCLevelDev& F, const CCLevelDev& C) {
-    KS_LAUNCH(c, k_cc_restrict, nblocks((long long)C.nx * C.ny * C.nz, BS), BS, F, C);
+    KS_LAUNCH(c, k_cc_restrict, nblocks((long long)C.nx * C.ny * C.nz, BS), BS, B8 * (ncc(F) + 2.0 * ncc(C)), F, C);
 }
 void launch_cc_prolong(Ctx& c, const CCLevelDev& F, const CCLevelDev& C) {
-    KS_LAUNCH(c, k_cc_prolong, nblocks((long long)F.nx * F.ny * F.nz, BS), BS, F, C);
+    KS_LAUNCH(c, k_cc_prolong, nblocks((long long)F.nx * F.ny * F.nz, BS), BS, B8 * (2.0 * ncc(F) + ncc(C)), F, C);
 }
-void launch_cc_bottom(Ctx& c, const CCLevelDev& L, double beta, int sweeps) { KS_LAUNCH(c, k_cc_bottom, 1, 256, L, beta, sweeps); }
+void launch_cc_bottom(Ctx& c, const CCLevelDev& L, double beta, int sweeps) {
+    KS_LAUNCH(c, k_cc_bottom, 1, 256, B8 * 3.0 * ncc(L), L, beta, sweeps);
+}
 void launch_nd_jacobi(Ctx& c, const NDLevelDev& L, double sigma, double omega, const double* in, double* out) {
-    KS_LAUNCH(c, k_nd_jacobi, nblocks((long long)L.nx * L.ny * L.nz, BS), BS, L, sigma, omega, in, out);
+    KS_LAUNCH(c, k_nd_jacobi, nblocks((long long)L.nx * L.ny * L.nz, BS), BS, B8 * 3.0 * nnd(L), L, sigma, omega, in, out);
 }
 void launch_nd_resid(Ctx& c, const NDLevelDev& L, double sigma, double* parts, int* np) {
     const int n = parts_for((long long)L.nx * L.ny * L.nz);
     if (np) *np = n;
-    KS_LAUNCH(c, k_nd_resid, n, BS, L, sigma, parts);
+    KS_LAUNCH(c, k_nd_resid, n, BS, B8 * 3.0 * nnd(L), L, sigma, parts);
 }
 void launch_nd_restrict(Ctx& c, const NDLevelDev& F, const NDLevelDev& C) {
-    KS_LAUNCH(c, k_nd_restrict, nblocks((long long)C.nx * C.ny * C.nz, BS), BS, F, C);
+    KS_LAUNCH(c, k_nd_restrict, nblocks((long long)C.nx * C.ny * C.nz, BS), BS, B8 * (nnd(F) + 2.0 * nnd(C)), F, C);
 }
 void launch_nd_prolong(Ctx& c, const NDLevelDev& F, const NDLevelDev& C) {
-    KS_LAUNCH(c, k_nd_prolong, nblocks((long long)F.nx * F.ny * F.nz, BS), BS, F, C);
+    KS_LAUNCH(c, k_nd_prolong, nblocks((long long)F.nx * F.ny * F.nz, BS), BS, B8 * (2.0 * nnd(F) + nnd(C)), F, C);
 }
 void launch_nd_bottom(Ctx& c, const NDLevelDev& L, double sigma, double omega, int sweeps) {
-    KS_LAUNCH(c, k_nd_bottom, 1, 256, L, sigma, omega, sweeps);
+    KS_LAUNCH(c, k_nd_bottom, 1, 256, B8 * 4.0 * nnd(L), L, sigma, omega, sweeps);
 }
 
 }  // namespace ks

@@ -29,7 +29,8 @@ FIELDS = ["velocity", "velocity_old", "gp", "p", "src_term", "forces", "diff_ter
 SYMBOLS = ["ks_create", "ks_destroy", "ks_last_error", "ks_init_data", "ks_compute_dt", "ks_pre_advance",
            "ks_prepare_time_step", "ks_advance", "ks_apply_predictor", "ks_apply_corrector", "ks_apply_projection",
            "ks_evolve", "ks_step", "ks_field_layout", "ks_get_field", "ks_set_field", "ks_get_scalar",
-           "ks_last_solver_stats", "ks_set_precision", "ks_synchronize", "ks_kernel_launches"]
+           "ks_last_solver_stats", "ks_set_precision", "ks_synchronize", "ks_kernel_launches", "ks_get_stream",
+           "ks_profile_kernels", "ks_profile_report"]
 
 
 class KsError(RuntimeError):
@@ -86,6 +87,10 @@ def load_library(path=None):
     lib.ks_last_solver_stats.argtypes = [vp, ctypes.POINTER(_Stats)]
     lib.ks_set_precision.argtypes = [vp, ip]
     lib.ks_kernel_launches.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+    lib.ks_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
+    lib.ks_profile_kernels.argtypes = [vp, ctypes.c_char_p]
+    lib.ks_profile_report.argtypes = [vp, ctypes.c_char_p, ctypes.c_longlong]
+    lib.ks_profile_report.restype = ctypes.c_longlong
     if path is None:
         _LIB = lib
     return lib
@@ -165,8 +170,9 @@ class Incflo:
         torch CUDA tensor of that size when ``out`` is one."""
         shape = self.layout(name)
         if out is not None and hasattr(out, "data_ptr"):
-            assert out.is_cuda and out.numel() == int(np.prod(shape)) and out.is_contiguous()
-            self._check(self._lib.ks_get_field(self._h, name.encode(), ctypes.c_void_p(out.data_ptr()), KS_DEVICE))
+            assert out.numel() == int(np.prod(shape)) and out.is_contiguous() and out.element_size() == 8
+            where = KS_DEVICE if out.is_cuda else KS_HOST
+            self._check(self._lib.ks_get_field(self._h, name.encode(), ctypes.c_void_p(out.data_ptr()), where))
             return out
         a = np.empty(shape, dtype=np.float64) if out is None else out
         self._check(self._lib.ks_get_field(self._h, name.encode(), a.ctypes.data_as(ctypes.c_void_p), KS_HOST))
@@ -174,9 +180,10 @@ class Incflo:
 
     def set_field(self, name, value):
         shape = self.layout(name)
-        if hasattr(value, "data_ptr") and getattr(value, "is_cuda", False):
-            assert value.numel() == int(np.prod(shape)) and value.is_contiguous()
-            self._check(self._lib.ks_set_field(self._h, name.encode(), ctypes.c_void_p(value.data_ptr()), KS_DEVICE))
+        if hasattr(value, "data_ptr"):
+            assert value.numel() == int(np.prod(shape)) and value.is_contiguous() and value.element_size() == 8
+            where = KS_DEVICE if value.is_cuda else KS_HOST
+            self._check(self._lib.ks_set_field(self._h, name.encode(), ctypes.c_void_p(value.data_ptr()), where))
             return
         a = np.ascontiguousarray(value, dtype=np.float64).reshape(shape)
         self._check(self._lib.ks_set_field(self._h, name.encode(), a.ctypes.data_as(ctypes.c_void_p), KS_HOST))
@@ -196,6 +203,28 @@ class Incflo:
 
     def synchronize(self):
         self._check(self._lib.ks_synchronize(self._h))
+
+    def stream(self):
+        """The cudaStream_t (as an int) all kernels of this handle run on."""
+        p = ctypes.c_void_p()
+        self._check(self._lib.ks_get_stream(self._h, ctypes.byref(p)))
+        return p.value or 0
+
+    def profile_kernels(self, kernel="*"):
+        self._check(self._lib.ks_profile_kernels(self._h, kernel.encode() if kernel else None))
+
+    def profile_report(self):
+        """{kernel name: (launches, total ms, algorithmic bytes)} since the last report; clears it."""
+        need = self._lib.ks_profile_report(self._h, None, 0)
+        if need < 0:
+            raise KsError(-need, self._lib.ks_last_error(self._h).decode())
+        buf = ctypes.create_string_buffer(int(need))
+        self._lib.ks_profile_report(self._h, buf, need)
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, n, ms, nbytes = line.split()
+            out[name] = (int(n), float(ms), float(nbytes))
+        return out
 
     def kernel_launches(self):
         c = ctypes.c_longlong()
