@@ -461,16 +461,20 @@ void Sim::alloc() {
     umac_[0].alloc(N);
     umac_[1].alloc(N);
     umac_[2].alloc(NF);
-    // Godunov scratch: ad[3], edge[3][3], tr[6 pairs][3], flux[3][3]
+    // Godunov scratch: per face direction ad, edge[3], lo[3], hi[3], tedge[3],
+    // flux[3]; tr[a][b][3] for the six (a, b) pairs
     const size_t fsz[3] = {N, N, NF};
     size_t total = 0;
-    for (int d = 0; d < 3; ++d) total += fsz[d] * (1 + 3 + 3);  // ad, edge, flux
-    for (int a = 0; a < 3; ++a) total += 2 * 3 * fsz[a];        // tr[a][b][n], b != a
+    for (int d = 0; d < 3; ++d) total += fsz[d] * 16;
+    for (int a = 0; a < 3; ++a) total += 2 * 3 * fsz[a];
     gbuf_.alloc(total);
     double* q = gbuf_.p;
     for (int d = 0; d < 3; ++d) {
         gb_.ad[d] = q; q += fsz[d];
         for (int n = 0; n < 3; ++n) { gb_.edge[d][n] = q; q += fsz[d]; }
+        for (int n = 0; n < 3; ++n) { gb_.lo[d][n] = q; q += fsz[d]; }
+        for (int n = 0; n < 3; ++n) { gb_.hi[d][n] = q; q += fsz[d]; }
+        for (int n = 0; n < 3; ++n) { gb_.tedge[d][n] = q; q += fsz[d]; }
         for (int n = 0; n < 3; ++n) { gb_.flux[d][n] = q; q += fsz[d]; }
     }
     for (int a = 0; a < 3; ++a)
@@ -713,6 +717,12 @@ void Sim::cc_vcycle(size_t l) {
 
 void Sim::mac_project() {
     const double beta = 1.0 / rho_;
+    for (auto& L : cc_) {
+        const double d0 = 2.0 * L.ix2 + 2.0 * L.iy2;
+        L.inv_diag[0] = 1.0 / (-beta * (d0 + 2.0 * L.iz2));
+        L.inv_diag[1] = 1.0 / (-beta * (d0 + L.iz2));
+        L.inv_diag[2] = 1.0 / (-beta * d0);
+    }
     CCLevelDev& L = cc_[0];
     int np = 0;
     launch_mac_rhs(ctx_, g_, umac_[0].p, umac_[1].p, umac_[2].p, L.rhs, parts_.p, &np);
@@ -770,6 +780,7 @@ void Sim::apply_projection(double time, double scaling, bool incremental) {
     launch_sub_ratio(ctx_, L.rhs, M, red_.p, 0.0);
     launch_fill(ctx_, L.phi, 0.0, M);
     const double sigma = scaling / rho_;
+    for (auto& Lv : nd_) Lv.inv_diag = 1.0 / (sigma * Lv.W[13]);
     launch_nd_resid(ctx_, L, sigma, parts_.p, &np);
     const double r0 = reduce(np, 1, 1, nullptr);
     nod_r0_ = r0;
@@ -794,7 +805,9 @@ void Sim::apply_predictor(bool incremental) {
     launch_smagorinsky(ctx_, g_, vel_old_.p, mueff_.p, S_);
     launch_sources(ctx_, g_, vel_old_.p, gp_.p, act_.p, src_.p, S_);
     if (wallmodel_) launch_wall_grad(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, shear_, utau_ * utau_, um_[0], um_[1], vmag_, rho_);
-    launch_divtau(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, divtau_.p, 1, src_.p, forces_.p, nullptr, nullptr, dt, rho_);
+    double* fl[9] = {gb_.flux[0][0], gb_.flux[0][1], gb_.flux[0][2], gb_.flux[1][0], gb_.flux[1][1],
+                     gb_.flux[1][2], gb_.flux[2][0], gb_.flux[2][1], gb_.flux[2][2]};
+    launch_divtau(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, divtau_.p, 1, src_.p, forces_.p, nullptr, nullptr, dt, rho_, fl);
     double* mac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
     launch_premac(ctx_, g_, vel_old_.p, forces_.p, dt, gb_, mac);
     mac_project();
@@ -803,7 +816,7 @@ void Sim::apply_predictor(bool incremental) {
     // compute_source_term(NPH) and compute_diffusion_term(Old) reproduce src
     // and divtau on this path (Coriolis reads the Old velocity, gp unchanged).
     launch_predictor_rhs(ctx_, g_, vel_old_.p, conv_.p, src_.p, divtau_.p, vel_.p, dt, rho_);
-    launch_divtau(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, 2, nullptr, nullptr, vel_.p, divtau_.p, dt, rho_);
+    launch_divtau(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, 2, nullptr, nullptr, vel_.p, divtau_.p, dt, rho_, fl);
     std::swap(vel_.p, vel_tmp_.p);
     apply_projection(t_.next, dt, incremental);
 }

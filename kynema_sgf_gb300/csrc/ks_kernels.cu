@@ -241,19 +241,19 @@ __device__ inline void tensor_flux(const Grid& g, const VelDiff& V, const double
         const long long cm = cidx(g, wrapn(im, g.nx), wrapn(jm, g.ny), g.zper ? wrapn(km, g.nz) : km);
         mf = 0.5 * (mu[cm] + mu[cc]);
     }
-    const double h[3] = {g.dx, g.dy, g.dz};
+    const double ih[3] = {1.0 / g.dx, 1.0 / g.dy, 1.0 / g.dz};
     double gr[3][3];  // gr[m][n] = d u_n / d x_m on the face
     for (int n = 0; n < 3; ++n) {
         for (int m = 0; m < 3; ++m) {
             if (m == d) {
-                gr[m][n] = (V(n, i, j, k) - V(n, im, jm, km)) / h[m];
+                gr[m][n] = (V(n, i, j, k) - V(n, im, jm, km)) * ih[m];
             } else {
                 int f[3] = {0, 0, 0};
                 f[m] = 1;
                 gr[m][n] = 0.25 *
                            (V(n, i + f[0], j + f[1], k + f[2]) + V(n, im + f[0], jm + f[1], km + f[2]) - V(n, i - f[0], j - f[1], k - f[2]) -
-                            V(n, im - f[0], jm - f[1], km - f[2])) /
-                           h[m];
+                            V(n, im - f[0], jm - f[1], km - f[2])) *
+                           ih[m];
             }
         }
     }
@@ -264,19 +264,41 @@ __device__ inline void tensor_flux(const Grid& g, const VelDiff& V, const double
     }
 }
 
-__global__ void k_divtau(Grid g, const double* vel, const double* mueff, const double* wg, double* out, int mode, const double* src,
-                         double* forces, const double* base, const double* dold, double dt, double rho) {
+// Tensor fluxes on the d-faces, all three components, computed once per face.
+__global__ void k_tau_flux(Grid g, int d, const double* vel, const double* mueff, const double* wg, double* F0, double* F1, double* F2) {
+    const int nzl = (d == 2) ? nzfaces(g) : g.nz;
+    const long long M = (long long)g.nx * g.ny * nzl;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= M) return;
+    int i, j, k;
+    cell_of(g, t, i, j, k);
+    VelDiff V{vel, wg, g};
+    double F[3];
+    tensor_flux(g, V, mueff, d, i, j, k, F);
+    const long long f = fidx(g, d, i, j, k);
+    F0[f] = F[0];
+    F1[f] = F[1];
+    F2[f] = F[2];
+}
+
+struct Flux9 {
+    const double* p[9];
+};
+
+// divtau = sum_d (F_d(c + e_d) - F_d(c)) / h_d ; mode 0: store; mode 1: also
+// forces = (src + divtau)/rho; mode 2: out = base + 0.5 dt (divtau - dold)/rho
+__global__ void k_tau_div(Grid g, Flux9 F, double* out, int mode, const double* src, double* forces, const double* base,
+                          const double* dold, double dt, double rho) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= g.N) return;
     int i, j, k;
     cell_of(g, t, i, j, k);
-    VelDiff V{vel, wg, g};
-    double Fl[3], Fh[3], acc[3] = {0, 0, 0};
-    const double h[3] = {g.dx, g.dy, g.dz};
+    const double ih[3] = {1.0 / g.dx, 1.0 / g.dy, 1.0 / g.dz};
+    const double irho = 1.0 / rho;
+    double acc[3] = {0, 0, 0};
     for (int d = 0; d < 3; ++d) {
-        tensor_flux(g, V, mueff, d, i, j, k, Fl);
-        tensor_flux(g, V, mueff, d, i + (d == 0), j + (d == 1), k + (d == 2), Fh);
-        for (int n = 0; n < 3; ++n) acc[n] += (Fh[n] - Fl[n]) / h[d];
+        const long long lo = fidx(g, d, i, j, k), hi = fidx(g, d, i + (d == 0), j + (d == 1), k + (d == 2));
+        for (int n = 0; n < 3; ++n) acc[n] += (F.p[3 * d + n][hi] - F.p[3 * d + n][lo]) * ih[d];
     }
     const long long N = g.N;
     if (mode == 0) {
@@ -284,10 +306,10 @@ __global__ void k_divtau(Grid g, const double* vel, const double* mueff, const d
     } else if (mode == 1) {
         for (int n = 0; n < 3; ++n) {
             out[n * N + t] = acc[n];
-            forces[n * N + t] = (src[n * N + t] + acc[n]) / rho;
+            forces[n * N + t] = (src[n * N + t] + acc[n]) * irho;
         }
     } else {
-        for (int n = 0; n < 3; ++n) out[n * N + t] = base[n * N + t] + 0.5 * dt * (acc[n] - dold[n * N + t]) / rho;
+        for (int n = 0; n < 3; ++n) out[n * N + t] = base[n * N + t] + 0.5 * dt * (acc[n] - dold[n * N + t]) * irho;
     }
 }
 
@@ -296,7 +318,7 @@ __global__ void k_pred_rhs(long long N3, const double* vo, const double* conv, c
                            double rho) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= N3) return;
-    vel[t] = (rho * vo[t] + dt * (conv[t] + src[t] + dt_[t])) / rho;
+    vel[t] = (rho * vo[t] + dt * (conv[t] + src[t] + dt_[t])) * (1.0 / rho);
 }
 
 // ---------------------------------------------------------------- projection
@@ -305,7 +327,7 @@ __global__ void k_proj_pre(long long N3, double* vel, const double* vo, const do
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= N3) return;
     double v = vel[t];
-    if (add_gp) v += gp[t] * scaling / rho;
+    if (add_gp) v += gp[t] * (scaling / rho);
     if (sub_old) v -= vo[t];
     vel[t] = v;
 }
@@ -546,9 +568,16 @@ void launch_wall_grad(Ctx& c, const Grid& g, const double* vel_old, const double
               um1, vm, rho);
 }
 void launch_divtau(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, int mode,
-                   const double* src, double* forces, const double* base, const double* dold, double dt, double rho) {
-    const double per_cell = 3 + 1 + 3 + (mode == 1 ? 6 : 0) + (mode == 2 ? 6 : 0);
-    KS_LAUNCH(c, k_divtau, nblocks(g.N, BS), BS, B8 * per_cell * g.N, g, vel, mueff, wg, out, mode, src, forces, base, dold, dt, rho);
+                   const double* src, double* forces, const double* base, const double* dold, double dt, double rho, double* const fl[9]) {
+    for (int d = 0; d < 3; ++d) {
+        const long long M = (long long)g.nx * g.ny * (d == 2 ? nzfaces(g) : g.nz);
+        KS_LAUNCH(c, k_tau_flux, nblocks(M, BS), BS, B8 * (4.0 * g.N + 3.0 * M), g, d, vel, mueff, wg, fl[3 * d], fl[3 * d + 1],
+                  fl[3 * d + 2]);
+    }
+    Flux9 F;
+    for (int m = 0; m < 9; ++m) F.p[m] = fl[m];
+    const double per_cell = 9 + 3 + (mode == 1 ? 6 : 0) + (mode == 2 ? 6 : 0);
+    KS_LAUNCH(c, k_tau_div, nblocks(g.N, BS), BS, B8 * per_cell * g.N, g, F, out, mode, src, forces, base, dold, dt, rho);
 }
 void launch_predictor_rhs(Ctx& c, const Grid& g, const double* vo, const double* conv, const double* src, const double* dtau, double* vel,
                           double dt, double rho) {

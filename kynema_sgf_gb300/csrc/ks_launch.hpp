@@ -108,7 +108,8 @@ void launch_wall_grad(Ctx& c, const Grid& g, const double* vel_old, const double
 // out = divtau(vel) ; mode 0: plain, mode 1: forces = (src + divtau)/rho also written,
 // mode 2: out = base + 0.5*dt*(divtau(vel) - dold)/rho (RK2 correction into out)
 void launch_divtau(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, int mode,
-                   const double* src, double* forces, const double* base, const double* dold, double dt, double rho);
+                   const double* src, double* forces, const double* base, const double* dold, double dt, double rho,
+                   double* const face_scratch[9]);
 void launch_predictor_rhs(Ctx& c, const Grid& g, const double* vel_old, const double* conv, const double* src, const double* divtau,
                           double* vel, double dt, double rho);
 void launch_proj_pre(Ctx& c, const Grid& g, double* vel, const double* vel_old, const double* gp, double scaling, double rho,
@@ -130,10 +131,13 @@ void launch_act_spread(Ctx& c, const Grid& g, double* act, const double* pts, in
 
 // ---- Godunov (ks_godunov.cu)
 struct GodunovBufs {
-    double* ad[3];
-    double* edge[3][3];   // premac: edge[d][n], n != d ; postmac: all n
-    double* tr[3][3][3];  // tr[a][b][n]
-    double* flux[3][3];   // flux[d][n]
+    double* ad[3];        // pre-MAC advective velocities on d-faces
+    double* edge[3][3];   // unlimited PPM edge values edge[d][n] on d-faces
+    double* lo[3][3];     // left states lo[d][n]
+    double* hi[3][3];     // right states hi[d][n]
+    double* tedge[3][3];  // upwinded states tedge[d][n]
+    double* tr[3][3][3];  // transverse-corrected states tr[a][b][n]
+    double* flux[3][3];   // fluxes flux[d][n]
 };
 void launch_premac(Ctx& c, const Grid& g, const double* vel_old, const double* forces, double dt, GodunovBufs& B, double* mac[3]);
 void launch_advection(Ctx& c, const Grid& g, const double* vel_old, const double* forces, const double* mac[3], double dt, double rho,
@@ -143,12 +147,14 @@ void launch_advection(Ctx& c, const Grid& g, const double* vel_old, const double
 struct CCLevelDev {
     int nx, ny, nz, zper;
     double ix2, iy2, iz2;
+    double inv_diag[3];  // 1/(-beta d): interior, wall-adjacent, single layer
     double *phi, *rhs, *res;
 };
 struct NDLevelDev {
     int nx, ny, nz;  // nodes
     int zper;
     double W[27];
+    double inv_diag;  // 1/(sigma W_centre)
     double *phi, *rhs, *res, *tmp;
 };
 void launch_cc_gsrb(Ctx& c, const CCLevelDev& L, double beta, int color);

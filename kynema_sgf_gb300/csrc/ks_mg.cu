@@ -69,6 +69,13 @@ __device__ inline void cc_ax(const CCLevelDev& L, const double* p, double beta, 
     dg = -beta * d;
 }
 
+// inverse of the diagonal -beta*d for the cell at z index k (the wall-adjacent
+// layers drop one z neighbour)
+__device__ inline double cc_inv_diag(const CCLevelDev& L, int k) {
+    if (L.zper || (k > 0 && k < L.nz - 1)) return L.inv_diag[0];
+    return (L.nz == 1) ? L.inv_diag[2] : L.inv_diag[1];
+}
+
 __global__ void k_cc_gsrb(CCLevelDev L, double beta, int color) {
     const long long half = (long long)L.nx * L.ny * L.nz / 2;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -81,7 +88,7 @@ __global__ void k_cc_gsrb(CCLevelDev L, double beta, int color) {
     double Ax, dg;
     cc_ax(L, L.phi, beta, i, j, k, Ax, dg);
     const long long c = ci3(L, i, j, k);
-    L.phi[c] += (L.rhs[c] - Ax) / dg;
+    L.phi[c] += (L.rhs[c] - Ax) * cc_inv_diag(L, k);
 }
 
 __global__ void k_cc_resid(CCLevelDev L, double beta, double* parts) {
@@ -137,7 +144,7 @@ __global__ void k_cc_bottom(CCLevelDev L, double beta, int sweeps) {
                 if (((i + j + k) & 1) != color) continue;
                 double Ax, dg;
                 cc_ax(L, L.phi, beta, i, j, k, Ax, dg);
-                L.phi[t] += (L.rhs[t] - Ax) / dg;
+                L.phi[t] += (L.rhs[t] - Ax) * cc_inv_diag(L, k);
             }
             __syncthreads();
         }
@@ -152,11 +159,35 @@ __device__ inline double nd_at(const NDLevelDev& L, const double* p, int i, int 
     return p[((long long)k * L.ny + j) * L.nx + i];
 }
 
+// sigma * (27-point Q1 stencil) at node (i,j,k); the weights are symmetric in
+// each direction, so neighbours are summed by weight class first.
 __device__ inline double nd_ax(const NDLevelDev& L, const double* p, double sigma, int i, int j, int k) {
-    double s = 0.0;
-    for (int c = -1; c <= 1; ++c)
-        for (int b = -1; b <= 1; ++b)
-            for (int a = -1; a <= 1; ++a) s += L.W[((c + 1) * 3 + b + 1) * 3 + a + 1] * nd_at(L, p, i + a, j + b, k + c);
+    const int im = i == 0 ? L.nx - 1 : i - 1, ip = i + 1 == L.nx ? 0 : i + 1;
+    const int jm = j == 0 ? L.ny - 1 : j - 1, jp = j + 1 == L.ny ? 0 : j + 1;
+    int km, kp;
+    if (L.zper) {
+        km = k == 0 ? L.nz - 1 : k - 1;
+        kp = k + 1 == L.nz ? 0 : k + 1;
+    } else {
+        km = k == 0 ? 1 : k - 1;
+        kp = k + 1 == L.nz ? L.nz - 2 : k + 1;
+    }
+    const long long sx = 1, sy = L.nx, sz = (long long)L.nx * L.ny;
+    (void)sx;
+    const long long rm = km * sz, r0 = k * sz, rp = kp * sz;
+    const long long cm = jm * sy, c0 = j * sy, cp = jp * sy;
+    auto at = [&](long long r, long long c, int x) { return p[r + c + x]; };
+    const double ctr = at(r0, c0, i);
+    const double fx = at(r0, c0, im) + at(r0, c0, ip);
+    const double fy = at(r0, cm, i) + at(r0, cp, i);
+    const double fz = at(rm, c0, i) + at(rp, c0, i);
+    const double exy = at(r0, cm, im) + at(r0, cm, ip) + at(r0, cp, im) + at(r0, cp, ip);
+    const double exz = at(rm, c0, im) + at(rm, c0, ip) + at(rp, c0, im) + at(rp, c0, ip);
+    const double eyz = at(rm, cm, i) + at(rm, cp, i) + at(rp, cm, i) + at(rp, cp, i);
+    const double cr = at(rm, cm, im) + at(rm, cm, ip) + at(rm, cp, im) + at(rm, cp, ip) + at(rp, cm, im) + at(rp, cm, ip) +
+                      at(rp, cp, im) + at(rp, cp, ip);
+    const double s = L.W[13] * ctr + L.W[12] * fx + L.W[10] * fy + L.W[4] * fz + L.W[9] * exy + L.W[3] * exz + L.W[1] * eyz +
+                     L.W[0] * cr;
     return sigma * s;
 }
 
@@ -167,8 +198,7 @@ __global__ void k_nd_jacobi(NDLevelDev L, double sigma, double omega, const doub
     const int i = (int)(t % L.nx);
     const long long r = t / L.nx;
     const int j = (int)(r % L.ny), k = (int)(r / L.ny);
-    const double diag = sigma * L.W[13];
-    out[t] = in[t] + omega * (L.rhs[t] - nd_ax(L, in, sigma, i, j, k)) / diag;
+    out[t] = in[t] + omega * (L.rhs[t] - nd_ax(L, in, sigma, i, j, k)) * L.inv_diag;
 }
 
 __global__ void k_nd_resid(NDLevelDev L, double sigma, double* parts) {
@@ -219,13 +249,12 @@ __global__ void k_nd_prolong(NDLevelDev F, NDLevelDev C) {
 
 __global__ void k_nd_bottom(NDLevelDev L, double sigma, double omega, int sweeps) {
     const long long N = (long long)L.nx * L.ny * L.nz;
-    const double diag = sigma * L.W[13];
     for (int s = 0; s < sweeps; ++s) {
         for (long long t = threadIdx.x; t < N; t += blockDim.x) {
             const int i = (int)(t % L.nx);
             const long long r = t / L.nx;
             const int j = (int)(r % L.ny), k = (int)(r / L.ny);
-            L.tmp[t] = L.phi[t] + omega * (L.rhs[t] - nd_ax(L, L.phi, sigma, i, j, k)) / diag;
+            L.tmp[t] = L.phi[t] + omega * (L.rhs[t] - nd_ax(L, L.phi, sigma, i, j, k)) * L.inv_diag;
         }
         __syncthreads();
         for (long long t = threadIdx.x; t < N; t += blockDim.x) L.phi[t] = L.tmp[t];
