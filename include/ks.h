@@ -103,6 +103,28 @@ int ks_get_stream(ks_handle* h, void** stream);
 int ks_profile_kernels(ks_handle* h, const char* kernel);
 long long ks_profile_report(ks_handle* h, char* buf, long long len);
 
+/* Allocation-free tensor diffusion term (no counterpart in the reference).
+ *
+ * For callers that cannot call cudaMalloc where they need the viscous term:
+ * code running inside a CUDA stream capture in global or thread-local mode
+ * (where cudaMalloc is illegal), hosts whose device memory is reserved up
+ * front by another allocator, latency-critical loops that must not trigger an
+ * allocation.  Computes divtau = div(mu (grad u + grad u^T) - 2/3 mu div(u) I)
+ * for a caller-owned device velocity (3 components, SoA, x fastest), cell
+ * viscosity mueff and output divtau (3 components), on stream `stream` (NULL =
+ * legacy default stream), with the boundary treatment of the advance: x and y
+ * periodic; z periodic or slip walls, or a wall-model bottom whose wall-normal
+ * tangential-velocity gradient is given in wall_grad (2 x nx*ny, device).
+ * Its face-flux scratch lives in a static device array sized for at most
+ * KS_NOALLOC_MAX_CELLS cells (about 24 MB, held by every GPU that loads the
+ * library until exit); larger grids are rejected with KS_ERR_ARG.  The first
+ * call on a device looks up that array's address with that device current;
+ * make that first call before any stream capture.  All calls share the
+ * array: calls whose kernels overlap on the GPU race, order them. */
+#define KS_NOALLOC_MAX_CELLS 262144
+int ks_divtau_noalloc(const double* vel, const double* mueff, const double* wall_grad, double* divtau, int nx, int ny, int nz,
+                      double dx, double dy, double dz, int z_periodic, int zlo_wall_model, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

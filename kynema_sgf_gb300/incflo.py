@@ -30,7 +30,7 @@ SYMBOLS = ["ks_create", "ks_destroy", "ks_last_error", "ks_init_data", "ks_compu
            "ks_prepare_time_step", "ks_advance", "ks_apply_predictor", "ks_apply_corrector", "ks_apply_projection",
            "ks_evolve", "ks_step", "ks_field_layout", "ks_get_field", "ks_set_field", "ks_get_scalar",
            "ks_last_solver_stats", "ks_set_precision", "ks_synchronize", "ks_kernel_launches", "ks_get_stream",
-           "ks_profile_kernels", "ks_profile_report"]
+           "ks_profile_kernels", "ks_profile_report", "ks_divtau_noalloc"]
 
 
 class KsError(RuntimeError):
@@ -91,6 +91,7 @@ def load_library(path=None):
     lib.ks_profile_kernels.argtypes = [vp, ctypes.c_char_p]
     lib.ks_profile_report.argtypes = [vp, ctypes.c_char_p, ctypes.c_longlong]
     lib.ks_profile_report.restype = ctypes.c_longlong
+    lib.ks_divtau_noalloc.argtypes = [vp, vp, vp, vp, ip, ip, ip, dp, dp, dp, ip, ip, vp]
     if path is None:
         _LIB = lib
     return lib
