@@ -44,6 +44,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision form of the same workload")
     p.add_argument("--profile-all", action="store_true", help="print the per-kernel breakdown to stderr")
     p.add_argument("--size", default="256,256,128")
     p.add_argument("--cpu-worker", default="", help=argparse.SUPPRESS)
@@ -203,6 +204,7 @@ def our_arm(args, rank, world, local_rank):
     dom = sim.profile_report().get(dominant, (0, 0.0, 0.0))
     sim.profile_kernels("")
     value = cells * args.steps * world / (ms_max * 1e-3) / 1e6
+    ref_state = {f: sim.get_field(f) for f in ("velocity", "gp")} if not args.no_mixed else None
 
     # end to end through the public API: host inputs in, host result out
     e2e = None
@@ -229,8 +231,42 @@ def our_arm(args, rank, world, local_rank):
         hin = sum(host[f].numel() * 8 for f in host)
         e2e = {"value": cells * args.steps * world / el / 1e6, "unit": UNIT, "h2d_bytes_per_step": hin,
                "d2h_bytes_per_step": host["velocity"].numel() * 8}
+    mixed = None
+    if not args.no_mixed:
+        del sim
+        mx = ks.Incflo(decks.abl(nx, ny, nz, steps=10 ** 9) + "\nks.precision = mixed\n")
+        mx.InitData()
+        for _ in range(args.warmup):
+            mx.step()
+        stream = torch.cuda.ExternalStream(mx.stream())
+        if dist:
+            tdist.barrier()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        mres, nres = [], []
+        for _ in range(args.steps):
+            mx.step()
+            mres.append(mx.scalar("mac_res") / max(mx.scalar("mac_res0"), 1e-300))
+            nres.append(mx.scalar("nodal_res") / max(mx.scalar("nodal_res0"), 1e-300))
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        mms = ev0.elapsed_time(ev1)
+        t = torch.tensor([mms], dtype=torch.float64, device="cuda")
+        if dist:
+            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        mms = float(t.item())
+        v = mx.get_field("velocity")
+        gpm = mx.get_field("gp")
+        rv, rg = ref_state["velocity"], ref_state["gp"]
+        mixed = {"value": cells * args.steps * world / (mms * 1e-3) / 1e6, "ms_per_step": mms / args.steps,
+                 "speedup_vs_fp64": ms_max / mms, "steps_compared": args.warmup + args.steps,
+                 "velocity_rel_err_linf": float(abs(v - rv).max() / abs(rv).max()),
+                 "velocity_rel_err_l2": float(((v - rv) ** 2).sum() ** 0.5 / (rv ** 2).sum() ** 0.5),
+                 "gp_rel_err_linf": float(abs(gpm - rg).max() / abs(rg).max()),
+                 "mac_residual_rel_max": max(mres), "nodal_residual_rel_max": max(nres),
+                 "note": "FP32 advection and multigrid cycles, FP64 residuals / defect correction / RHS / velocity update"}
     return dict(value=value, ms=ms_max, cells=cells, launches=launches, dominant=dominant, dom=dom, clocks=clk, e2e=e2e,
-                mac=statistics.mean(mac_it), nodal=statistics.mean(nod_it), size=(nx, ny, nz))
+                mac=statistics.mean(mac_it), nodal=statistics.mean(nod_it), size=(nx, ny, nz), mixed=mixed)
 
 
 def main():
@@ -282,7 +318,7 @@ def main():
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic, "peak_kind": peak_kind,
                          "launches": n_l, "avg_launch_us": 1e3 * ms_l / n_l if n_l else None,
                          "algorithmic_bytes_per_launch": by_l / n_l if n_l else None},
-            "gpu_launches": r["launches"], "clocks": r["clocks"], "e2e": r["e2e"]}
+            "gpu_launches": r["launches"], "clocks": r["clocks"], "e2e": r["e2e"], "mixed_precision": r["mixed"]}
     # whole-step algorithmic traffic: 8 * (125 + 20.86 * V-cycles) bytes per cell
     bstep = 8.0 * (125.0 + 20.86 * (r["mac"] + r["nodal"])) * r["cells"]
     line["step_roofline"] = {"algorithmic_bytes_per_step": bstep, "achieved_GBs": bstep / (r["ms"] / args.steps * 1e-3) / 1e9,

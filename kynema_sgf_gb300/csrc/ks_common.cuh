@@ -45,42 +45,49 @@ __host__ __device__ inline long long fidx(const Grid& g, int d, int i, int j, in
 // Cell-centred velocity (or rho*velocity) with fill-patch ghost values:
 // periodic wrap in x, y (and z); at walls the tangential components take the
 // high-order extrapolation to the face, (15 q0 - 10 q1 + 3 q2)/8, in every
-// ghost layer and the normal component is 0.
-struct VelFP {
+// ghost layer and the normal component is 0.  The stored field is FP64; the
+// value is returned in the arithmetic type T of the caller.
+template <typename T = double>
+struct VelFPT {
     const double* v;
     Grid g;
-    double scale;
-    __device__ inline double operator()(int n, int i, int j, int k) const {
+    T scale;
+    __device__ inline T operator()(int n, int i, int j, int k) const {
         i = wrapn(i, g.nx);
         j = wrapn(j, g.ny);
         const long long N = g.N;
         const double* c = v + n * N;
-        if (g.zper) return scale * c[cidx(g, i, j, wrapn(k, g.nz))];
+        if (g.zper) return scale * (T)c[cidx(g, i, j, wrapn(k, g.nz))];
         if (k < 0) {
-            if (n == 2) return 0.0;
-            return scale * 0.125 * (15.0 * c[cidx(g, i, j, 0)] - 10.0 * c[cidx(g, i, j, 1)] + 3.0 * c[cidx(g, i, j, 2)]);
+            if (n == 2) return T(0);
+            const T q0 = (T)c[cidx(g, i, j, 0)], q1 = (T)c[cidx(g, i, j, 1)], q2 = (T)c[cidx(g, i, j, 2)];
+            return scale * (T(0.125) * (T(15) * q0 - T(10) * q1 + T(3) * q2));
         }
         if (k >= g.nz) {
-            if (n == 2) return 0.0;
+            if (n == 2) return T(0);
             const int t = g.nz - 1;
-            return scale * 0.125 * (15.0 * c[cidx(g, i, j, t)] - 10.0 * c[cidx(g, i, j, t - 1)] + 3.0 * c[cidx(g, i, j, t - 2)]);
+            const T q0 = (T)c[cidx(g, i, j, t)], q1 = (T)c[cidx(g, i, j, t - 1)], q2 = (T)c[cidx(g, i, j, t - 2)];
+            return scale * (T(0.125) * (T(15) * q0 - T(10) * q1 + T(3) * q2));
         }
-        return scale * c[cidx(g, i, j, k)];
+        return scale * (T)c[cidx(g, i, j, k)];
     }
 };
+using VelFP = VelFPT<double>;
 
 // Cell field with first-order extrapolation ghosts in z (forces, viscosity).
-struct CellFO {
+template <typename T = double>
+struct CellFOT {
     const double* v;
     Grid g;
-    __device__ inline double operator()(int n, int i, int j, int k) const {
+    __device__ inline T operator()(int n, int i, int j, int k) const {
         i = wrapn(i, g.nx);
         j = wrapn(j, g.ny);
         if (g.zper) k = wrapn(k, g.nz);
         else k = k < 0 ? 0 : (k >= g.nz ? g.nz - 1 : k);
-        return v[n * g.N + cidx(g, i, j, k)];
+        return (T)v[n * g.N + cidx(g, i, j, k)];
     }
 };
+using CellFO = CellFOT<double>;
 
 inline unsigned nblocks(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 

@@ -23,14 +23,17 @@ namespace {
 
 constexpr int BS = 256;
 
-__device__ inline double vls(double a, double b, double c) {
-    const double dsc = 0.5 * (c - a), dsl = 2.0 * (b - a), dsr = 2.0 * (c - b);
-    return (dsl * dsr > 0.0) ? copysign(fmin(fabs(dsc), fmin(fabs(dsl), fabs(dsr))), dsc) : 0.0;
+template <typename T>
+__device__ inline T vls(T a, T b, T c) {
+    const T dsc = T(0.5) * (c - a), dsl = T(2) * (b - a), dsr = T(2) * (c - b);
+    return (dsl * dsr > T(0)) ? copysign(fmin(fabs(dsc), fmin(fabs(dsl), fabs(dsr))), dsc) : T(0);
 }
-__device__ inline double clipe(double e, double a, double b) { return fmin(fmax(e, fmin(a, b)), fmax(a, b)); }
+template <typename T>
+__device__ inline T clipe(T e, T a, T b) { return fmin(fmax(e, fmin(a, b)), fmax(a, b)); }
 
+template <typename T>
 struct Dt {  // dt / h along x, y, z
-    double v[3];
+    T v[3];
 };
 
 __device__ inline bool face_of(const Grid& g, int d, long long t, int& i, int& j, int& k) {
@@ -50,87 +53,96 @@ inline long long nfaces(const Grid& g, int d) { return (long long)g.nx * g.ny * 
 // cell of the same index), 3 components.  Wall-bounded z: the wall faces take
 // the boundary (ghost) value, the faces one cell inside the one-sided
 // fourth-order formula, clipped to the two adjacent cells.
-__global__ void k_edges(Grid g, int d, const double* vel, double* e0, double* e1, double* e2) {
+template <typename T>
+__global__ void k_edges(Grid g, int d, const double* vel, T* e0, T* e1, T* e2) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_of(g, d, t, i, j, k)) return;
-    VelFP q{vel, g, 1.0};
+    VelFPT<T> q{vel, g, T(1)};
     const int di = (d == 0), dj = (d == 1), dk = (d == 2);
     const bool wall = (d == 2 && !g.zper);
-    double* e[3] = {e0, e1, e2};
+    T* e[3] = {e0, e1, e2};
     const long long f = fidx(g, d, i, j, k);
     for (int n = 0; n < 3; ++n) {
-        double v;
+        T v;
         if (wall && k == 0) {
             v = q(n, i, j, -1);
         } else if (wall && k == g.nz) {
             v = q(n, i, j, g.nz);
         } else if (wall && k == 1) {
-            const double b = q(n, i, j, -1), q0 = q(n, i, j, 0), q1 = q(n, i, j, 1), q2 = q(n, i, j, 2);
-            v = clipe(-0.2 * b + 0.75 * q0 + 0.5 * q1 - 0.05 * q2, q0, q1);
+            const T b = q(n, i, j, -1), q0 = q(n, i, j, 0), q1 = q(n, i, j, 1), q2 = q(n, i, j, 2);
+            v = clipe(T(-0.2) * b + T(0.75) * q0 + T(0.5) * q1 - T(0.05) * q2, q0, q1);
         } else if (wall && k == g.nz - 1) {
             const int t0 = g.nz - 1;
-            const double b = q(n, i, j, g.nz), q0 = q(n, i, j, t0), q1 = q(n, i, j, t0 - 1), q2 = q(n, i, j, t0 - 2);
-            v = clipe(-0.2 * b + 0.75 * q0 + 0.5 * q1 - 0.05 * q2, q0, q1);
+            const T b = q(n, i, j, g.nz), q0 = q(n, i, j, t0), q1 = q(n, i, j, t0 - 1), q2 = q(n, i, j, t0 - 2);
+            v = clipe(T(-0.2) * b + T(0.75) * q0 + T(0.5) * q1 - T(0.05) * q2, q0, q1);
         } else {
-            const double am = q(n, i - 2 * di, j - 2 * dj, k - 2 * dk), a0 = q(n, i - di, j - dj, k - dk);
-            const double a1 = q(n, i, j, k), a2 = q(n, i + di, j + dj, k + dk);
-            v = clipe(0.5 * (a0 + a1) - (1.0 / 6.0) * (vls(a0, a1, a2) - vls(am, a0, a1)), a0, a1);
+            const T am = q(n, i - 2 * di, j - 2 * dj, k - 2 * dk), a0 = q(n, i - di, j - dj, k - dk);
+            const T a1 = q(n, i, j, k), a2 = q(n, i + di, j + dj, k + dk);
+            v = clipe(T(0.5) * (a0 + a1) - T(1.0 / 6.0) * (vls(a0, a1, a2) - vls(am, a0, a1)), a0, a1);
         }
         e[n][f] = v;
     }
 }
 
 // limited parabola of a cell: (sm, sp) from its two stored edges and s0
-__device__ inline void cw84(double s0, double& sm, double& sp) {
-    if ((sp - s0) * (s0 - sm) <= 0.0) {
+template <typename T>
+__device__ inline void cw84(T s0, T& sm, T& sp) {
+    if ((sp - s0) * (s0 - sm) <= T(0)) {
         sp = s0;
         sm = s0;
-    } else if (fabs(sp - s0) >= 2.0 * fabs(sm - s0)) {
-        sp = 3.0 * s0 - 2.0 * sm;
-    } else if (fabs(sm - s0) >= 2.0 * fabs(sp - s0)) {
-        sm = 3.0 * s0 - 2.0 * sp;
+    } else if (fabs(sp - s0) >= T(2) * fabs(sm - s0)) {
+        sp = T(3) * s0 - T(2) * sm;
+    } else if (fabs(sm - s0) >= T(2) * fabs(sp - s0)) {
+        sm = T(3) * s0 - T(2) * sp;
     }
 }
 
 // average of the limited parabola over the part of the cell that crosses its
 // high (trace_hi) or low (trace_lo) face in dt, sig = |u| dt / h
-__device__ inline double trace_hi(double sm, double s0, double sp, double sig) {
-    const double s6 = 6.0 * s0 - 3.0 * (sm + sp);
-    return sp - 0.5 * sig * ((sp - sm) - (1.0 - 2.0 / 3.0 * sig) * s6);
+template <typename T>
+__device__ inline T trace_hi(T sm, T s0, T sp, T sig) {
+    const T s6 = T(6) * s0 - T(3) * (sm + sp);
+    return sp - T(0.5) * sig * ((sp - sm) - (T(1) - T(2.0 / 3.0) * sig) * s6);
 }
-__device__ inline double trace_lo(double sm, double s0, double sp, double sig) {
-    const double s6 = 6.0 * s0 - 3.0 * (sm + sp);
-    return sm + 0.5 * sig * ((sp - sm) + (1.0 - 2.0 / 3.0 * sig) * s6);
+template <typename T>
+__device__ inline T trace_lo(T sm, T s0, T sp, T sig) {
+    const T s6 = T(6) * s0 - T(3) * (sm + sp);
+    return sm + T(0.5) * sig * ((sp - sm) + (T(1) - T(2.0 / 3.0) * sig) * s6);
 }
 
 // Wall face treatment (SetZEdgeBCs): tangential components take the interior
 // state, the normal component is zero on both sides.
-__device__ inline void zbc(const Grid& g, int k, int n, double& lo, double& hi) {
+template <typename T>
+__device__ inline void zbc(const Grid& g, int k, int n, T& lo, T& hi) {
     if (g.zper) return;
     if (k == 0) {
-        if (n == 2) { lo = 0.0; hi = 0.0; } else lo = hi;
+        if (n == 2) { lo = T(0); hi = T(0); } else lo = hi;
     } else if (k == g.nz) {
-        if (n == 2) { lo = 0.0; hi = 0.0; } else hi = lo;
+        if (n == 2) { lo = T(0); hi = T(0); } else hi = lo;
     }
 }
 
-__device__ inline double upwind(double vel, double lo, double hi) {
-    const double st = (vel >= 0.0) ? lo : hi;
-    const double fu = (fabs(vel) < kSmallVel) ? 0.0 : 1.0;
-    return fu * st + (1.0 - fu) * 0.5 * (lo + hi);
+template <typename T>
+__device__ inline T upwind(T vel, T lo, T hi) {
+    const T st = (vel >= T(0)) ? lo : hi;
+    const T fu = (fabs(vel) < T(kSmallVel)) ? T(0) : T(1);
+    return fu * st + (T(1) - fu) * T(0.5) * (lo + hi);
 }
-__device__ inline double riemann(double lo, double hi) {
-    const double st = (lo + hi >= 0.0) ? lo : hi;
-    const bool ltm = (lo <= 0.0 && hi >= 0.0) || (fabs(lo + hi) < kSmallVel);
-    return ltm ? 0.0 : st;
+template <typename T>
+__device__ inline T riemann(T lo, T hi) {
+    const T st = (lo + hi >= T(0)) ? lo : hi;
+    const bool ltm = (lo <= T(0) && hi >= T(0)) || (fabs(lo + hi) < T(kSmallVel));
+    return ltm ? T(0) : st;
 }
 
+template <typename T>
 struct P3 {
-    double* p[3];
+    T* p[3];
 };
+template <typename T>
 struct C3 {
-    const double* p[3];
+    const T* p[3];
 };
 
 // ---- stage 1 of both passes: left/right states of all components on d-faces.
@@ -139,43 +151,43 @@ struct C3 {
 // Pre-MAC also writes the Riemann-solved advective velocity and the states of
 // the two transverse components upwinded with it; post-MAC writes the states of
 // all three components upwinded with the MAC velocity.
-template <int MODE>
-__global__ void k_faces(Grid g, int d, const double* vel, C3 E, Dt dtdx, double rho, const double* umac_d, P3 LO, P3 HI, double* ad,
-                        P3 edge) {
+template <int MODE, typename T>
+__global__ void k_faces(Grid g, int d, const double* vel, C3<T> E, Dt<T> dtdx, T rho, const double* umac_d, P3<T> LO, P3<T> HI, T* ad,
+                        P3<T> edge) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_of(g, d, t, i, j, k)) return;
-    VelFP q{vel, g, 1.0};
+    VelFPT<T> q{vel, g, T(1)};
     const int di = (d == 0), dj = (d == 1), dk = (d == 2);
     const bool wl = (d == 2 && !g.zper && k == 0), wh = (d == 2 && !g.zper && k == g.nz);
     const long long f = fidx(g, d, i, j, k);
     const long long fm = fidx(g, d, i - di, j - dj, k - dk), fp = fidx(g, d, i + di, j + dj, k + dk);
-    const double s = dtdx.v[d];
+    const T s = dtdx.v[d];
     // characteristic speeds: cell velocities (pre-MAC) or the face velocities
     // of the low / high face of each cell (post-MAC)
-    double ul = 0.0, uh = 0.0, umf = 0.0;
+    T ul = T(0), uh = T(0), umf = T(0);
     if (MODE == 0) {
         if (!wl) ul = q(d, i - di, j - dj, k - dk);
         if (!wh) uh = q(d, i, j, k);
     } else {
-        umf = umac_d[f];
+        umf = (T)umac_d[f];
         ul = umf;  // high face of cell c - e_d
         uh = umf;  // low face of cell c
     }
-    double lo[3], hi[3];
+    T lo[3], hi[3];
     for (int n = 0; n < 3; ++n) {
-        double l = 0.0, h = 0.0;
+        T l = T(0), h = T(0);
         if (!wl) {  // high-side trace of cell c - e_d
-            const double s0 = q(n, i - di, j - dj, k - dk);
-            double sm = E.p[n][fm], sp = E.p[n][f];
+            const T s0 = q(n, i - di, j - dj, k - dk);
+            T sm = E.p[n][fm], sp = E.p[n][f];
             cw84(s0, sm, sp);
-            l = (ul > kSmallVel) ? trace_hi(sm, s0, sp, fabs(ul) * s) : s0;
+            l = (ul > T(kSmallVel)) ? trace_hi(sm, s0, sp, fabs(ul) * s) : s0;
         }
         if (!wh) {  // low-side trace of cell c
-            const double s0 = q(n, i, j, k);
-            double sm = E.p[n][f], sp = E.p[n][fp];
+            const T s0 = q(n, i, j, k);
+            T sm = E.p[n][f], sp = E.p[n][fp];
             cw84(s0, sm, sp);
-            h = (uh < -kSmallVel) ? trace_lo(sm, s0, sp, fabs(uh) * s) : s0;
+            h = (uh < -T(kSmallVel)) ? trace_lo(sm, s0, sp, fabs(uh) * s) : s0;
         }
         if (MODE == 1) {
             l *= rho;
@@ -188,7 +200,7 @@ __global__ void k_faces(Grid g, int d, const double* vel, C3 E, Dt dtdx, double 
         HI.p[n][f] = h;
     }
     if (MODE == 0) {
-        const double a = riemann(lo[d], hi[d]);
+        const T a = riemann(lo[d], hi[d]);
         ad[f] = a;
         for (int n = 0; n < 3; ++n)
             if (n != d) edge.p[n][f] = upwind(a, lo[n], hi[n]);
@@ -198,13 +210,14 @@ __global__ void k_faces(Grid g, int d, const double* vel, C3 E, Dt dtdx, double 
 }
 
 // ---- pre-MAC stage 2: a-face states of component n corrected along b
-__global__ void k_pm_trans(Grid g, int a, int b, int n, double cb, const double* lo_an, const double* hi_an, const double* ad_a,
-                           const double* ad_b, const double* edge_b, double* out) {
+template <typename T>
+__global__ void k_pm_trans(Grid g, int a, int b, int n, T cb, const T* lo_an, const T* hi_an, const T* ad_a, const T* ad_b, const T* edge_b,
+                           T* out) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_of(g, a, t, i, j, k)) return;
     const long long f = fidx(g, a, i, j, k);
-    double l = lo_an[f], h = hi_an[f];
+    T l = lo_an[f], h = hi_an[f];
     const bool wl = (a == 2 && !g.zper && k == 0), wh = (a == 2 && !g.zper && k == g.nz);
     const int eb0 = (b == 0), eb1 = (b == 1), eb2 = (b == 2);
     if (!wh) {
@@ -221,49 +234,51 @@ __global__ void k_pm_trans(Grid g, int a, int b, int n, double cb, const double*
 }
 
 // ---- pre-MAC stage 3: final normal velocity on d-faces
-__global__ void k_pm_final(Grid g, int d, const double* lo_dd, const double* hi_dd, const double* forces, double dt, double c1, double c2,
-                           C3 AD, const double* T1, const double* T2, double* mac) {
+template <typename T>
+__global__ void k_pm_final(Grid g, int d, const T* lo_dd, const T* hi_dd, const double* forces, T dt, T c1, T c2, C3<T> AD, const T* T1,
+                           const T* T2, double* mac) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_of(g, d, t, i, j, k)) return;
-    CellFO F{forces, g};
+    CellFOT<T> F{forces, g};
     const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
     const long long f = fidx(g, d, i, j, k);
     const bool wl = (d == 2 && !g.zper && k == 0), wh = (d == 2 && !g.zper && k == g.nz);
-    auto side = [&](int ci, int cj, int ck, double base) {
+    auto side = [&](int ci, int cj, int ck, T base) {
         const long long p1 = fidx(g, b1, ci + (b1 == 0), cj + (b1 == 1), ck + (b1 == 2)), m1 = fidx(g, b1, ci, cj, ck);
         const long long p2 = fidx(g, b2, ci + (b2 == 0), cj + (b2 == 1), ck + (b2 == 2)), m2 = fidx(g, b2, ci, cj, ck);
-        double s = base;
+        T s = base;
         s -= c1 * (AD.p[b1][p1] + AD.p[b1][m1]) * (T1[p1] - T1[m1]);
         s -= c2 * (AD.p[b2][p2] + AD.p[b2][m2]) * (T2[p2] - T2[m2]);
-        s += 0.5 * dt * F(d, ci, cj, ck);
+        s += T(0.5) * dt * F(d, ci, cj, ck);
         return s;
     };
-    double stl = 0.0, sth = 0.0;
+    T stl = T(0), sth = T(0);
     if (!wl) stl = side(i - (d == 0), j - (d == 1), k - (d == 2), lo_dd[f]);
     if (!wh) sth = side(i, j, k, hi_dd[f]);
     if (d == 2) zbc(g, k, d, stl, sth);
-    mac[f] = riemann(stl, sth);
+    mac[f] = (double)riemann(stl, sth);
 }
 
 // ---- post-MAC stage 2: a-face states corrected along b (conservative form)
-__global__ void k_adv_trans(Grid g, int a, int b, const double* vel, double rho, double cb, const double* ua, const double* vb, C3 LO,
-                            C3 HI, C3 E, P3 out) {
+template <typename T>
+__global__ void k_adv_trans(Grid g, int a, int b, const double* vel, T rho, T cb, const double* ua, const double* vb, C3<T> LO, C3<T> HI,
+                            C3<T> E, P3<T> out) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_of(g, a, t, i, j, k)) return;
-    VelFP q{vel, g, rho};
+    VelFPT<T> q{vel, g, rho};
     const bool wl = (a == 2 && !g.zper && k == 0), wh = (a == 2 && !g.zper && k == g.nz);
     const long long f = fidx(g, a, i, j, k);
-    const double u = ua[f];
+    const T u = (T)ua[f];
     const int ci = i - (a == 0), cj = j - (a == 1), ck = k - (a == 2);
     const long long h0 = fidx(g, b, i, j, k), h1 = fidx(g, b, i + (b == 0), j + (b == 1), k + (b == 2));
     const long long l0 = fidx(g, b, ci, cj, ck), l1 = fidx(g, b, ci + (b == 0), cj + (b == 1), ck + (b == 2));
-    double vhp = 0.0, vhm = 0.0, vlp = 0.0, vlm = 0.0;
-    if (!wh) { vhp = vb[h1]; vhm = vb[h0]; }
-    if (!wl) { vlp = vb[l1]; vlm = vb[l0]; }
+    T vhp = T(0), vhm = T(0), vlp = T(0), vlm = T(0);
+    if (!wh) { vhp = (T)vb[h1]; vhm = (T)vb[h0]; }
+    if (!wl) { vlp = (T)vb[l1]; vlm = (T)vb[l0]; }
     for (int n = 0; n < 3; ++n) {
-        double l = LO.p[n][f], h = HI.p[n][f];
+        T l = LO.p[n][f], h = HI.p[n][f];
         if (!wh) h += -cb * (vhp * E.p[n][h1] - vhm * E.p[n][h0]) + cb * q(n, i, j, k) * (vhp - vhm);
         if (!wl) l += -cb * (vlp * E.p[n][l1] - vlm * E.p[n][l0]) + cb * q(n, ci, cj, ck) * (vlp - vlm);
         if (a == 2) zbc(g, k, n, l, h);
@@ -272,140 +287,164 @@ __global__ void k_adv_trans(Grid g, int a, int b, const double* vel, double rho,
 }
 
 // ---- post-MAC stage 3: final states and fluxes on d-faces
-__global__ void k_adv_flux(Grid g, int d, const double* vel, const double* forces, double rho, double dt, double c1, double c2, C3 U,
-                           C3 LO, C3 HI, C3 T1, C3 T2, P3 Fl) {
+template <typename T>
+__global__ void k_adv_flux(Grid g, int d, const double* vel, const double* forces, T rho, T dt, T c1, T c2, C3<double> U, C3<T> LO, C3<T> HI,
+                           C3<T> T1, C3<T> T2, P3<T> Fl) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_of(g, d, t, i, j, k)) return;
-    VelFP q{vel, g, rho};
-    CellFO Fo{forces, g};
+    VelFPT<T> q{vel, g, rho};
+    CellFOT<T> Fo{forces, g};
     const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
     const bool wl = (d == 2 && !g.zper && k == 0), wh = (d == 2 && !g.zper && k == g.nz);
     const long long f = fidx(g, d, i, j, k);
-    const double um = U.p[d][f];
+    const T um = (T)U.p[d][f];
     const int li = i - (d == 0), lj = j - (d == 1), lk = k - (d == 2);
     const long long lp1 = fidx(g, b1, li + (b1 == 0), lj + (b1 == 1), lk + (b1 == 2)), lm1 = fidx(g, b1, li, lj, lk);
     const long long lp2 = fidx(g, b2, li + (b2 == 0), lj + (b2 == 1), lk + (b2 == 2)), lm2 = fidx(g, b2, li, lj, lk);
     const long long hp1 = fidx(g, b1, i + (b1 == 0), j + (b1 == 1), k + (b1 == 2)), hm1 = fidx(g, b1, i, j, k);
     const long long hp2 = fidx(g, b2, i + (b2 == 0), j + (b2 == 1), k + (b2 == 2)), hm2 = fidx(g, b2, i, j, k);
-    double l1p = 0, l1m = 0, l2p = 0, l2m = 0, h1p = 0, h1m = 0, h2p = 0, h2m = 0;
-    if (!wl) { l1p = U.p[b1][lp1]; l1m = U.p[b1][lm1]; l2p = U.p[b2][lp2]; l2m = U.p[b2][lm2]; }
-    if (!wh) { h1p = U.p[b1][hp1]; h1m = U.p[b1][hm1]; h2p = U.p[b2][hp2]; h2m = U.p[b2][hm2]; }
+    T l1p = 0, l1m = 0, l2p = 0, l2m = 0, h1p = 0, h1m = 0, h2p = 0, h2m = 0;
+    if (!wl) { l1p = (T)U.p[b1][lp1]; l1m = (T)U.p[b1][lm1]; l2p = (T)U.p[b2][lp2]; l2m = (T)U.p[b2][lm2]; }
+    if (!wh) { h1p = (T)U.p[b1][hp1]; h1m = (T)U.p[b1][hm1]; h2p = (T)U.p[b2][hp2]; h2m = (T)U.p[b2][hm2]; }
     for (int n = 0; n < 3; ++n) {
-        double stl = 0.0, sth = 0.0;
+        T stl = T(0), sth = T(0);
         if (!wl) {
-            const double qc = q(n, li, lj, lk);
-            double s = LO.p[n][f];
+            const T qc = q(n, li, lj, lk);
+            T s = LO.p[n][f];
             s -= c1 * (T1.p[n][lp1] * l1p - T1.p[n][lm1] * l1m);
             s -= c2 * (T2.p[n][lp2] * l2p - T2.p[n][lm2] * l2m);
             s += c1 * qc * (l1p - l1m);
             s += c2 * qc * (l2p - l2m);
-            s += 0.5 * dt * (rho * Fo(n, li, lj, lk));
+            s += T(0.5) * dt * (rho * Fo(n, li, lj, lk));
             stl = s;
         }
         if (!wh) {
-            const double qc = q(n, i, j, k);
-            double s = HI.p[n][f];
+            const T qc = q(n, i, j, k);
+            T s = HI.p[n][f];
             s -= c1 * (T1.p[n][hp1] * h1p - T1.p[n][hm1] * h1m);
             s -= c2 * (T2.p[n][hp2] * h2p - T2.p[n][hm2] * h2m);
             s += c1 * qc * (h1p - h1m);
             s += c2 * qc * (h2p - h2m);
-            s += 0.5 * dt * (rho * Fo(n, i, j, k));
+            s += T(0.5) * dt * (rho * Fo(n, i, j, k));
             sth = s;
         }
         if (d == 2) zbc(g, k, n, stl, sth);
-        double st = (um >= 0.0) ? stl : sth;
-        if (fabs(um) < kSmallVel) st = 0.5 * (stl + sth);
+        T st = (um >= T(0)) ? stl : sth;
+        if (fabs(um) < T(kSmallVel)) st = T(0.5) * (stl + sth);
         Fl.p[n][f] = um * st;
     }
 }
 
+template <typename T>
 struct FluxPtrs {
-    const double* p[9];
+    const T* p[9];
 };
-__global__ void k_adv_div(Grid g, FluxPtrs F, double* conv) {
+template <typename T>
+__global__ void k_adv_div(Grid g, FluxPtrs<T> F, double* conv) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= g.N) return;
     const int i = (int)(t % g.nx);
     const long long r = t / g.nx;
     const int j = (int)(r % g.ny), k = (int)(r / g.ny);
     const long long xp = fidx(g, 0, i + 1, j, k), yp = fidx(g, 1, i, j + 1, k), zp = fidx(g, 2, i, j, k + 1), zm = fidx(g, 2, i, j, k);
-    const double ix = 1.0 / g.dx, iy = 1.0 / g.dy, iz = 1.0 / g.dz;
+    const T ix = T(1.0 / g.dx), iy = T(1.0 / g.dy), iz = T(1.0 / g.dz);
     for (int n = 0; n < 3; ++n)
-        conv[n * g.N + t] = -((F.p[n][xp] - F.p[n][t]) * ix + (F.p[3 + n][yp] - F.p[3 + n][t]) * iy + (F.p[6 + n][zp] - F.p[6 + n][zm]) * iz);
+        conv[n * g.N + t] =
+            (double)(-((F.p[n][xp] - F.p[n][t]) * ix + (F.p[3 + n][yp] - F.p[3 + n][t]) * iy + (F.p[6 + n][zp] - F.p[6 + n][zm]) * iz));
 }
 
 }  // namespace
 
-void launch_premac(Ctx& c, const Grid& g, const double* vel, const double* forces, double dt, GodunovBufs& B, double* mac[3]) {
-    const double B8 = 8.0;
-    const Dt dtdx{{dt / g.dx, dt / g.dy, dt / g.dz}};
+template <typename T>
+static T* tp(void* p) {
+    return static_cast<T*>(p);
+}
+
+template <typename T>
+static void premac_t(Ctx& c, const Grid& g, const double* vel, const double* forces, double dt, GodunovBufs& B, double* mac[3]) {
+    const double BT = (double)sizeof(T), B8 = 8.0;
+    const Dt<T> dtdx{{T(dt / g.dx), T(dt / g.dy), T(dt / g.dz)}};
     for (int d = 0; d < 3; ++d)
-        KS_LAUNCH(c, k_edges, nblocks(nfaces(g, d), BS), BS, B8 * (3.0 * g.N + 3.0 * nfaces(g, d)), g, d, vel, B.edge[d][0], B.edge[d][1],
-                  B.edge[d][2]);
+        KS_LAUNCH(c, k_edges<T>, nblocks(nfaces(g, d), BS), BS, B8 * 3.0 * g.N + BT * 3.0 * nfaces(g, d), g, d, vel, tp<T>(B.edge[d][0]),
+                  tp<T>(B.edge[d][1]), tp<T>(B.edge[d][2]));
     for (int d = 0; d < 3; ++d) {
-        C3 E{{B.edge[d][0], B.edge[d][1], B.edge[d][2]}};
-        P3 LO{{B.lo[d][0], B.lo[d][1], B.lo[d][2]}}, HI{{B.hi[d][0], B.hi[d][1], B.hi[d][2]}};
-        P3 ED{{B.tedge[d][0], B.tedge[d][1], B.tedge[d][2]}};
+        C3<T> E{{tp<T>(B.edge[d][0]), tp<T>(B.edge[d][1]), tp<T>(B.edge[d][2])}};
+        P3<T> LO{{tp<T>(B.lo[d][0]), tp<T>(B.lo[d][1]), tp<T>(B.lo[d][2])}}, HI{{tp<T>(B.hi[d][0]), tp<T>(B.hi[d][1]), tp<T>(B.hi[d][2])}};
+        P3<T> ED{{tp<T>(B.tedge[d][0]), tp<T>(B.tedge[d][1]), tp<T>(B.tedge[d][2])}};
         const double nf = (double)nfaces(g, d);
-        KS_LAUNCH(c, k_faces<0>, nblocks(nfaces(g, d), BS), BS, B8 * (3.0 * g.N + 12.0 * nf), g, d, vel, E, dtdx, 1.0, nullptr, LO, HI,
-                  B.ad[d], ED);
+        KS_LAUNCH(c, (k_faces<0, T>), nblocks(nfaces(g, d), BS), BS, B8 * 3.0 * g.N + BT * 12.0 * nf, g, d, vel, E, dtdx, T(1), nullptr,
+                  LO, HI, tp<T>(B.ad[d]), ED);
     }
     // (a, b, n): states on a-faces of component n corrected along b
-    const int tp[6][3] = {{1, 2, 0}, {2, 1, 0}, {0, 2, 1}, {2, 0, 1}, {0, 1, 2}, {1, 0, 2}};
-    for (auto& p : tp) {
+    const int tpl[6][3] = {{1, 2, 0}, {2, 1, 0}, {0, 2, 1}, {2, 0, 1}, {0, 1, 2}, {1, 0, 2}};
+    for (auto& p : tpl) {
         const int a = p[0], b = p[1], n = p[2];
-        const double bytes = B8 * (4.0 * nfaces(g, a) + 2.0 * nfaces(g, b));
-        const double cb = dt / (6.0 * hd(g, b));
-        KS_LAUNCH(c, k_pm_trans, nblocks(nfaces(g, a), BS), BS, bytes, g, a, b, n, cb, B.lo[a][n], B.hi[a][n], B.ad[a], B.ad[b],
-                  B.tedge[b][n], B.tr[a][b][0]);
+        const double bytes = BT * (4.0 * nfaces(g, a) + 2.0 * nfaces(g, b));
+        const T cb = T(dt / (6.0 * hd(g, b)));
+        KS_LAUNCH(c, k_pm_trans<T>, nblocks(nfaces(g, a), BS), BS, bytes, g, a, b, n, cb, tp<T>(B.lo[a][n]), tp<T>(B.hi[a][n]),
+                  tp<T>(B.ad[a]), tp<T>(B.ad[b]), tp<T>(B.tedge[b][n]), tp<T>(B.tr[a][b][0]));
     }
-    C3 AD{{B.ad[0], B.ad[1], B.ad[2]}};
+    C3<T> AD{{tp<T>(B.ad[0]), tp<T>(B.ad[1]), tp<T>(B.ad[2])}};
     for (int d = 0; d < 3; ++d) {
         const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
-        const double bytes = B8 * (1.0 * g.N + 4.0 * nfaces(g, d) + 2.0 * nfaces(g, b1) + 2.0 * nfaces(g, b2));
-        const double c1 = dt / (4.0 * hd(g, b1)), c2 = dt / (4.0 * hd(g, b2));
-        KS_LAUNCH(c, k_pm_final, nblocks(nfaces(g, d), BS), BS, bytes, g, d, B.lo[d][d], B.hi[d][d], forces, dt, c1, c2, AD,
-                  B.tr[b1][b2][0], B.tr[b2][b1][0], mac[d]);
+        const double bytes = B8 * (1.0 * g.N + nfaces(g, d)) + BT * (3.0 * nfaces(g, d) + 2.0 * nfaces(g, b1) + 2.0 * nfaces(g, b2));
+        const T c1 = T(dt / (4.0 * hd(g, b1))), c2 = T(dt / (4.0 * hd(g, b2)));
+        KS_LAUNCH(c, k_pm_final<T>, nblocks(nfaces(g, d), BS), BS, bytes, g, d, tp<T>(B.lo[d][d]), tp<T>(B.hi[d][d]), forces, T(dt), c1, c2,
+                  AD, tp<T>(B.tr[b1][b2][0]), tp<T>(B.tr[b2][b1][0]), mac[d]);
     }
 }
 
-void launch_advection(Ctx& c, const Grid& g, const double* vel, const double* forces, const double* mac[3], double dt, double rho,
-                      GodunovBufs& B, double* conv) {
-    const double B8 = 8.0;
-    const Dt dtdx{{dt / g.dx, dt / g.dy, dt / g.dz}};
+template <typename T>
+static void advection_t(Ctx& c, const Grid& g, const double* vel, const double* forces, const double* mac[3], double dt, double rho,
+                        GodunovBufs& B, double* conv) {
+    const double BT = (double)sizeof(T), B8 = 8.0;
+    const Dt<T> dtdx{{T(dt / g.dx), T(dt / g.dy), T(dt / g.dz)}};
     // the unlimited edge values of the pre-MAC pass are reused (same field)
     for (int a = 0; a < 3; ++a) {
-        C3 E{{B.edge[a][0], B.edge[a][1], B.edge[a][2]}};
-        P3 LO{{B.lo[a][0], B.lo[a][1], B.lo[a][2]}}, HI{{B.hi[a][0], B.hi[a][1], B.hi[a][2]}};
-        P3 ED{{B.tedge[a][0], B.tedge[a][1], B.tedge[a][2]}};
-        KS_LAUNCH(c, k_faces<1>, nblocks(nfaces(g, a), BS), BS, B8 * (3.0 * g.N + 13.0 * nfaces(g, a)), g, a, vel, E, dtdx, rho, mac[a],
-                  LO, HI, nullptr, ED);
+        C3<T> E{{tp<T>(B.edge[a][0]), tp<T>(B.edge[a][1]), tp<T>(B.edge[a][2])}};
+        P3<T> LO{{tp<T>(B.lo[a][0]), tp<T>(B.lo[a][1]), tp<T>(B.lo[a][2])}}, HI{{tp<T>(B.hi[a][0]), tp<T>(B.hi[a][1]), tp<T>(B.hi[a][2])}};
+        P3<T> ED{{tp<T>(B.tedge[a][0]), tp<T>(B.tedge[a][1]), tp<T>(B.tedge[a][2])}};
+        KS_LAUNCH(c, (k_faces<1, T>), nblocks(nfaces(g, a), BS), BS, B8 * (3.0 * g.N + nfaces(g, a)) + BT * 12.0 * nfaces(g, a), g, a, vel,
+                  E, dtdx, T(rho), mac[a], LO, HI, (T*)nullptr, ED);
     }
     for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 3; ++b) {
             if (a == b) continue;
-            const double bytes = B8 * (3.0 * g.N + 10.0 * nfaces(g, a) + 4.0 * nfaces(g, b));
-            C3 LO{{B.lo[a][0], B.lo[a][1], B.lo[a][2]}}, HI{{B.hi[a][0], B.hi[a][1], B.hi[a][2]}};
-            C3 E{{B.tedge[b][0], B.tedge[b][1], B.tedge[b][2]}};
-            P3 O{{B.tr[a][b][0], B.tr[a][b][1], B.tr[a][b][2]}};
-            KS_LAUNCH(c, k_adv_trans, nblocks(nfaces(g, a), BS), BS, bytes, g, a, b, vel, rho, dt / (3.0 * hd(g, b)), mac[a], mac[b], LO,
-                      HI, E, O);
+            const double bytes = B8 * (3.0 * g.N + nfaces(g, a) + nfaces(g, b)) + BT * (9.0 * nfaces(g, a) + 3.0 * nfaces(g, b));
+            C3<T> LO{{tp<T>(B.lo[a][0]), tp<T>(B.lo[a][1]), tp<T>(B.lo[a][2])}}, HI{{tp<T>(B.hi[a][0]), tp<T>(B.hi[a][1]), tp<T>(B.hi[a][2])}};
+            C3<T> E{{tp<T>(B.tedge[b][0]), tp<T>(B.tedge[b][1]), tp<T>(B.tedge[b][2])}};
+            P3<T> O{{tp<T>(B.tr[a][b][0]), tp<T>(B.tr[a][b][1]), tp<T>(B.tr[a][b][2])}};
+            KS_LAUNCH(c, k_adv_trans<T>, nblocks(nfaces(g, a), BS), BS, bytes, g, a, b, vel, T(rho), T(dt / (3.0 * hd(g, b))), mac[a],
+                      mac[b], LO, HI, E, O);
         }
-    C3 U{{mac[0], mac[1], mac[2]}};
+    C3<double> U{{mac[0], mac[1], mac[2]}};
     for (int d = 0; d < 3; ++d) {
         const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
-        const double bytes = B8 * (6.0 * g.N + 10.0 * nfaces(g, d) + 4.0 * nfaces(g, b1) + 4.0 * nfaces(g, b2));
-        C3 LO{{B.lo[d][0], B.lo[d][1], B.lo[d][2]}}, HI{{B.hi[d][0], B.hi[d][1], B.hi[d][2]}};
-        C3 T1{{B.tr[b1][b2][0], B.tr[b1][b2][1], B.tr[b1][b2][2]}}, T2{{B.tr[b2][b1][0], B.tr[b2][b1][1], B.tr[b2][b1][2]}};
-        P3 F{{B.flux[d][0], B.flux[d][1], B.flux[d][2]}};
-        KS_LAUNCH(c, k_adv_flux, nblocks(nfaces(g, d), BS), BS, bytes, g, d, vel, forces, rho, dt, dt / (2.0 * hd(g, b1)),
-                  dt / (2.0 * hd(g, b2)), U, LO, HI, T1, T2, F);
+        const double bytes = B8 * (6.0 * g.N + nfaces(g, d) + nfaces(g, b1) + nfaces(g, b2)) +
+                             BT * (9.0 * nfaces(g, d) + 3.0 * nfaces(g, b1) + 3.0 * nfaces(g, b2));
+        C3<T> LO{{tp<T>(B.lo[d][0]), tp<T>(B.lo[d][1]), tp<T>(B.lo[d][2])}}, HI{{tp<T>(B.hi[d][0]), tp<T>(B.hi[d][1]), tp<T>(B.hi[d][2])}};
+        C3<T> T1{{tp<T>(B.tr[b1][b2][0]), tp<T>(B.tr[b1][b2][1]), tp<T>(B.tr[b1][b2][2])}};
+        C3<T> T2{{tp<T>(B.tr[b2][b1][0]), tp<T>(B.tr[b2][b1][1]), tp<T>(B.tr[b2][b1][2])}};
+        P3<T> F{{tp<T>(B.flux[d][0]), tp<T>(B.flux[d][1]), tp<T>(B.flux[d][2])}};
+        KS_LAUNCH(c, k_adv_flux<T>, nblocks(nfaces(g, d), BS), BS, bytes, g, d, vel, forces, T(rho), T(dt), T(dt / (2.0 * hd(g, b1))),
+                  T(dt / (2.0 * hd(g, b2))), U, LO, HI, T1, T2, F);
     }
-    FluxPtrs F;
+    FluxPtrs<T> F;
     for (int d = 0; d < 3; ++d)
-        for (int n = 0; n < 3; ++n) F.p[d * 3 + n] = B.flux[d][n];
-    KS_LAUNCH(c, k_adv_div, nblocks(g.N, BS), BS, B8 * (9.0 * g.N + 3.0 * g.N), g, F, conv);
+        for (int n = 0; n < 3; ++n) F.p[d * 3 + n] = tp<T>(B.flux[d][n]);
+    KS_LAUNCH(c, k_adv_div<T>, nblocks(g.N, BS), BS, BT * 9.0 * g.N + B8 * 3.0 * g.N, g, F, conv);
+}
+
+void launch_premac(Ctx& c, const Grid& g, const double* vel, const double* forces, double dt, GodunovBufs& B, double* mac[3], int fp32) {
+    if (fp32) premac_t<float>(c, g, vel, forces, dt, B, mac);
+    else premac_t<double>(c, g, vel, forces, dt, B, mac);
+}
+
+void launch_advection(Ctx& c, const Grid& g, const double* vel, const double* forces, const double* mac[3], double dt, double rho,
+                      GodunovBufs& B, double* conv, int fp32) {
+    if (fp32) advection_t<float>(c, g, vel, forces, mac, dt, rho, B, conv);
+    else advection_t<double>(c, g, vel, forces, mac, dt, rho, B, conv);
 }
 
 }  // namespace ks

@@ -208,6 +208,7 @@ class Sim {
     Grid g_{};
     Clock t_;
     int mac_it_ = 0, nod_it_ = 0;
+    int mixed_ = 0;  // 1: FP32 advection and multigrid cycles with FP64 defect correction
     double mac_r0_ = 0, mac_r_ = 0, nod_r0_ = 0, nod_r_ = 0;
     std::string err_;
 
@@ -219,8 +220,14 @@ class Sim {
     void actuator_update();
     void mac_project();
     double reduce(int np, int ncomp, int op_max, double* host);
-    void cc_vcycle(size_t l);
-    void nd_vcycle(size_t l, double sigma);
+    template <typename T>
+    void cc_vcycle(std::vector<CCLevelT<T>>& Ls, size_t l, double beta);
+    template <typename T>
+    void nd_vcycle(std::vector<NDLevelT<T>>& Ls, size_t l, double sigma);
+   public:
+    void set_mixed(int on);
+
+   private:
     double* field(const std::string& name, int& ncomp, int& kind);
 
     double plo_[3], phi_[3];
@@ -239,7 +246,10 @@ class Sim {
     GodunovBufs gb_{};
     std::vector<CCLevelDev> cc_;
     std::vector<NDLevelDev> nd_;
+    std::vector<CCLevelT<float>> cc32_;  // mixed precision: FP32 cycle levels
+    std::vector<NDLevelT<float>> nd32_;
     DevBuf<double> mgbuf_;
+    DevBuf<float> mgbuf32_;
     DevBuf<double> parts_, red_;
     DevBuf<double> pts_, samp_;
     double* hred_ = nullptr;  // pinned
@@ -252,6 +262,9 @@ Sim::Sim(const std::string& text) {
     ck(cudaMallocHost(&hred_, 64 * sizeof(double)), "pinned alloc");
     alloc();
     init_fields(D);
+    const std::string prec = lc(D.str("ks.precision", "fp64"));
+    if (prec == "mixed") set_mixed(1);
+    else if (prec != "fp64") throw KsError(KS_ERR_DECK, "ks.precision must be fp64 or mixed");
     sync();
 }
 
@@ -694,10 +707,10 @@ void Sim::actuator_update() {
 }
 
 // ---------------------------------------------------------------- MAC projection
-void Sim::cc_vcycle(size_t l) {
-    const double beta = 1.0 / rho_;
-    CCLevelDev& L = cc_[l];
-    if (l + 1 == cc_.size()) {
+template <typename T>
+void Sim::cc_vcycle(std::vector<CCLevelT<T>>& Ls, size_t l, double beta) {
+    CCLevelT<T>& L = Ls[l];
+    if (l + 1 == Ls.size()) {
         launch_cc_bottom(ctx_, L, beta, mac_.bottom);
         return;
     }
@@ -706,12 +719,42 @@ void Sim::cc_vcycle(size_t l) {
         launch_cc_gsrb(ctx_, L, beta, 1);
     }
     launch_cc_resid(ctx_, L, beta, nullptr, nullptr);
-    launch_cc_restrict(ctx_, L, cc_[l + 1]);
-    cc_vcycle(l + 1);
-    launch_cc_prolong(ctx_, L, cc_[l + 1]);
+    launch_cc_restrict(ctx_, L, Ls[l + 1]);
+    cc_vcycle(Ls, l + 1, beta);
+    launch_cc_prolong(ctx_, L, Ls[l + 1]);
     for (int s = 0; s < mac_.nu2; ++s) {
         launch_cc_gsrb(ctx_, L, beta, 0);
         launch_cc_gsrb(ctx_, L, beta, 1);
+    }
+}
+
+// Mixed precision: FP32 copies of the multigrid hierarchies.  The FP64
+// residual, right-hand side and solution of the finest level stay in the
+// FP64 levels; each outer (defect-correction) iteration solves the FP64
+// residual equation with one FP32 V-cycle and adds the correction in FP64.
+void Sim::set_mixed(int on) {
+    mixed_ = on ? 1 : 0;
+    if (!mixed_ || !cc32_.empty()) return;
+    size_t tot = 0;
+    for (size_t l = 0; l < cc_.size(); ++l) {
+        tot += 3 * (size_t)cc_[l].nx * cc_[l].ny * cc_[l].nz;
+        tot += 4 * (size_t)nd_[l].nx * nd_[l].ny * nd_[l].nz;
+    }
+    mgbuf32_.alloc(tot);
+    float* q = mgbuf32_.p;
+    for (size_t l = 0; l < cc_.size(); ++l) {
+        CCLevelT<float> C{};
+        C.nx = cc_[l].nx; C.ny = cc_[l].ny; C.nz = cc_[l].nz; C.zper = cc_[l].zper;
+        C.ix2 = (float)cc_[l].ix2; C.iy2 = (float)cc_[l].iy2; C.iz2 = (float)cc_[l].iz2;
+        const size_t nc = (size_t)C.nx * C.ny * C.nz;
+        C.phi = q; q += nc; C.rhs = q; q += nc; C.res = q; q += nc;
+        cc32_.push_back(C);
+        NDLevelT<float> Nd{};
+        Nd.nx = nd_[l].nx; Nd.ny = nd_[l].ny; Nd.nz = nd_[l].nz; Nd.zper = nd_[l].zper;
+        for (int m = 0; m < 27; ++m) Nd.W[m] = (float)nd_[l].W[m];
+        const size_t nn = (size_t)Nd.nx * Nd.ny * Nd.nz;
+        Nd.phi = q; q += nn; Nd.rhs = q; q += nn; Nd.res = q; q += nn; Nd.tmp = q; q += nn;
+        nd32_.push_back(Nd);
     }
 }
 
@@ -723,6 +766,8 @@ void Sim::mac_project() {
         L.inv_diag[1] = 1.0 / (-beta * (d0 + L.iz2));
         L.inv_diag[2] = 1.0 / (-beta * d0);
     }
+    for (size_t l = 0; l < cc32_.size(); ++l)
+        for (int m = 0; m < 3; ++m) cc32_[l].inv_diag[m] = (float)cc_[l].inv_diag[m];
     CCLevelDev& L = cc_[0];
     int np = 0;
     launch_mac_rhs(ctx_, g_, umac_[0].p, umac_[1].p, umac_[2].p, L.rhs, parts_.p, &np);
@@ -736,7 +781,13 @@ void Sim::mac_project() {
     int it = 0;
     double rn = r0;
     while (rn > target && it < mac_.maxiter) {
-        cc_vcycle(0);
+        if (mixed_) {
+            launch_to_f32(ctx_, L.res, cc32_[0].rhs, cc32_[0].phi, g_.N);
+            cc_vcycle(cc32_, 0, beta);
+            launch_add_f32(ctx_, L.phi, cc32_[0].phi, g_.N);
+        } else {
+            cc_vcycle(cc_, 0, beta);
+        }
         launch_cc_resid(ctx_, L, beta, parts_.p, &np);
         rn = reduce(np, 1, 1, nullptr);
         ++it;
@@ -748,9 +799,10 @@ void Sim::mac_project() {
 }
 
 // ---------------------------------------------------------------- nodal projection
-void Sim::nd_vcycle(size_t l, double sigma) {
-    NDLevelDev& L = nd_[l];
-    if (l + 1 == nd_.size()) {
+template <typename T>
+void Sim::nd_vcycle(std::vector<NDLevelT<T>>& Ls, size_t l, double sigma) {
+    NDLevelT<T>& L = Ls[l];
+    if (l + 1 == Ls.size()) {
         launch_nd_bottom(ctx_, L, sigma, nod_.omega, nod_.bottom);
         return;
     }
@@ -759,9 +811,9 @@ void Sim::nd_vcycle(size_t l, double sigma) {
         std::swap(L.phi, L.tmp);
     }
     launch_nd_resid(ctx_, L, sigma, nullptr, nullptr);
-    launch_nd_restrict(ctx_, L, nd_[l + 1]);
-    nd_vcycle(l + 1, sigma);
-    launch_nd_prolong(ctx_, L, nd_[l + 1]);
+    launch_nd_restrict(ctx_, L, Ls[l + 1]);
+    nd_vcycle(Ls, l + 1, sigma);
+    launch_nd_prolong(ctx_, L, Ls[l + 1]);
     for (int s = 0; s < nod_.nu2; ++s) {
         launch_nd_jacobi(ctx_, L, sigma, nod_.omega, L.phi, L.tmp);
         std::swap(L.phi, L.tmp);
@@ -781,6 +833,7 @@ void Sim::apply_projection(double time, double scaling, bool incremental) {
     launch_fill(ctx_, L.phi, 0.0, M);
     const double sigma = scaling / rho_;
     for (auto& Lv : nd_) Lv.inv_diag = 1.0 / (sigma * Lv.W[13]);
+    for (size_t l = 0; l < nd32_.size(); ++l) nd32_[l].inv_diag = (float)nd_[l].inv_diag;
     launch_nd_resid(ctx_, L, sigma, parts_.p, &np);
     const double r0 = reduce(np, 1, 1, nullptr);
     nod_r0_ = r0;
@@ -788,7 +841,13 @@ void Sim::apply_projection(double time, double scaling, bool incremental) {
     int it = 0;
     double rn = r0;
     while (rn > target && it < nod_.maxiter) {
-        nd_vcycle(0, sigma);
+        if (mixed_) {
+            launch_to_f32(ctx_, L.res, nd32_[0].rhs, nd32_[0].phi, M);
+            nd_vcycle(nd32_, 0, sigma);
+            launch_add_f32(ctx_, L.phi, nd32_[0].phi, M);
+        } else {
+            nd_vcycle(nd_, 0, sigma);
+        }
         launch_nd_resid(ctx_, L, sigma, parts_.p, &np);
         rn = reduce(np, 1, 1, nullptr);
         ++it;
@@ -805,14 +864,14 @@ void Sim::apply_predictor(bool incremental) {
     launch_smagorinsky(ctx_, g_, vel_old_.p, mueff_.p, S_);
     launch_sources(ctx_, g_, vel_old_.p, gp_.p, act_.p, src_.p, S_);
     if (wallmodel_) launch_wall_grad(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, shear_, utau_ * utau_, um_[0], um_[1], vmag_, rho_);
-    double* fl[9] = {gb_.flux[0][0], gb_.flux[0][1], gb_.flux[0][2], gb_.flux[1][0], gb_.flux[1][1],
-                     gb_.flux[1][2], gb_.flux[2][0], gb_.flux[2][1], gb_.flux[2][2]};
+    double* fl[9];
+    for (int m = 0; m < 9; ++m) fl[m] = static_cast<double*>(gb_.flux[m / 3][m % 3]);
     launch_divtau(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, divtau_.p, 1, src_.p, forces_.p, nullptr, nullptr, dt, rho_, fl);
     double* mac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
-    launch_premac(ctx_, g_, vel_old_.p, forces_.p, dt, gb_, mac);
+    launch_premac(ctx_, g_, vel_old_.p, forces_.p, dt, gb_, mac, mixed_);
     mac_project();
     const double* cmac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
-    launch_advection(ctx_, g_, vel_old_.p, forces_.p, cmac, dt, rho_, gb_, conv_.p);
+    launch_advection(ctx_, g_, vel_old_.p, forces_.p, cmac, dt, rho_, gb_, conv_.p, mixed_);
     // compute_source_term(NPH) and compute_diffusion_term(Old) reproduce src
     // and divtau on this path (Coriolis reads the Old velocity, gp unchanged).
     launch_predictor_rhs(ctx_, g_, vel_old_.p, conv_.p, src_.p, divtau_.p, vel_.p, dt, rho_);
@@ -951,6 +1010,7 @@ double Sim::scalar(const std::string& n) {
     if (n == "src_cfl") return t_.src_cfl;
     if (n == "density") return rho_;
     if (n == "ncells") return (double)g_.N;
+    if (n == "precision") return (double)mixed_;
     if (n == "ke") {
         int np = 0;
         launch_ke(ctx_, g_, vel_.p, rho_, parts_.p, &np);
@@ -1109,10 +1169,11 @@ int ks_last_solver_stats(const ks_handle* h, ks_mg_stats* st) {
 }
 
 int ks_set_precision(ks_handle* h, int precision) {
-    if (!h || !h->sim) return KS_ERR_ARG;
-    if (precision == KS_FP64) return KS_OK;
-    h->err = "mixed precision is not built yet";
-    return KS_ERR_UNSUPPORTED;
+    if (precision != KS_FP64 && precision != KS_MIXED) return KS_ERR_ARG;
+    return guarded(h, [&](ks::Sim& s) {
+        s.set_mixed(precision == KS_MIXED);
+        return 0;
+    });
 }
 
 int ks_synchronize(ks_handle* h) { return guarded(h, [](ks::Sim& s) { s.sync(); return 0; }); }
@@ -1146,7 +1207,10 @@ long long ks_profile_report(ks_handle* h, char* buf, long long len) {
     std::string out;
     char line[256];
     for (auto& kv : s.ctx_.acc) {
-        std::snprintf(line, sizeof(line), "%s %lld %.6f %.0f\n", kv.first.c_str(), kv.second.launches, kv.second.ms, kv.second.bytes);
+        std::string name;
+        for (char ch : kv.first)
+            if (ch != ' ') name += ch;
+        std::snprintf(line, sizeof(line), "%s %lld %.6f %.0f\n", name.c_str(), kv.second.launches, kv.second.ms, kv.second.bytes);
         out += line;
     }
     const long long need = (long long)out.size() + 1;

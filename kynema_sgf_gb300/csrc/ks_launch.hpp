@@ -130,42 +130,62 @@ void launch_act_spread(Ctx& c, const Grid& g, double* act, const double* pts, in
                        const double plo[3], const int lo[3], const int hi[3]);
 
 // ---- Godunov (ks_godunov.cu)
+// Godunov face scratch; each array holds FP64 or FP32 values (fp32 flag of
+// the launchers), sized for FP64.
 struct GodunovBufs {
-    double* ad[3];        // pre-MAC advective velocities on d-faces
-    double* edge[3][3];   // unlimited PPM edge values edge[d][n] on d-faces
-    double* lo[3][3];     // left states lo[d][n]
-    double* hi[3][3];     // right states hi[d][n]
-    double* tedge[3][3];  // upwinded states tedge[d][n]
-    double* tr[3][3][3];  // transverse-corrected states tr[a][b][n]
-    double* flux[3][3];   // fluxes flux[d][n]
+    void* ad[3];        // pre-MAC advective velocities on d-faces
+    void* edge[3][3];   // unlimited PPM edge values edge[d][n] on d-faces
+    void* lo[3][3];     // left states lo[d][n]
+    void* hi[3][3];     // right states hi[d][n]
+    void* tedge[3][3];  // upwinded states tedge[d][n]
+    void* tr[3][3][3];  // transverse-corrected states tr[a][b][n]
+    void* flux[3][3];   // fluxes flux[d][n]
 };
-void launch_premac(Ctx& c, const Grid& g, const double* vel_old, const double* forces, double dt, GodunovBufs& B, double* mac[3]);
+void launch_premac(Ctx& c, const Grid& g, const double* vel_old, const double* forces, double dt, GodunovBufs& B, double* mac[3],
+                   int fp32);
 void launch_advection(Ctx& c, const Grid& g, const double* vel_old, const double* forces, const double* mac[3], double dt, double rho,
-                      GodunovBufs& B, double* conv);
+                      GodunovBufs& B, double* conv, int fp32);
 
-// ---- multigrid (ks_mg.cu)
-struct CCLevelDev {
+// ---- multigrid (ks_mg.cu); T = double (FP64 path) or float (cycles of the
+// mixed-precision defect correction)
+template <typename T>
+struct CCLevelT {
     int nx, ny, nz, zper;
-    double ix2, iy2, iz2;
-    double inv_diag[3];  // 1/(-beta d): interior, wall-adjacent, single layer
-    double *phi, *rhs, *res;
+    T ix2, iy2, iz2;
+    T inv_diag[3];  // 1/(-beta d): interior, wall-adjacent, single layer
+    T *phi, *rhs, *res;
 };
-struct NDLevelDev {
+template <typename T>
+struct NDLevelT {
     int nx, ny, nz;  // nodes
     int zper;
-    double W[27];
-    double inv_diag;  // 1/(sigma W_centre)
-    double *phi, *rhs, *res, *tmp;
+    T W[27];
+    T inv_diag;  // 1/(sigma W_centre)
+    T *phi, *rhs, *res, *tmp;
 };
-void launch_cc_gsrb(Ctx& c, const CCLevelDev& L, double beta, int color);
-void launch_cc_resid(Ctx& c, const CCLevelDev& L, double beta, double* partials, int* nparts);
-void launch_cc_restrict(Ctx& c, const CCLevelDev& F, const CCLevelDev& C);
-void launch_cc_prolong(Ctx& c, const CCLevelDev& F, const CCLevelDev& C);
-void launch_cc_bottom(Ctx& c, const CCLevelDev& L, double beta, int sweeps);
-void launch_nd_jacobi(Ctx& c, const NDLevelDev& L, double sigma, double omega, const double* in, double* out);
-void launch_nd_resid(Ctx& c, const NDLevelDev& L, double sigma, double* partials, int* nparts);
-void launch_nd_restrict(Ctx& c, const NDLevelDev& F, const NDLevelDev& C);
-void launch_nd_prolong(Ctx& c, const NDLevelDev& F, const NDLevelDev& C);
-void launch_nd_bottom(Ctx& c, const NDLevelDev& L, double sigma, double omega, int sweeps);
+using CCLevelDev = CCLevelT<double>;
+using NDLevelDev = NDLevelT<double>;
+template <typename T>
+void launch_cc_gsrb(Ctx& c, const CCLevelT<T>& L, double beta, int color);
+template <typename T>
+void launch_cc_resid(Ctx& c, const CCLevelT<T>& L, double beta, double* partials, int* nparts);
+template <typename T>
+void launch_cc_restrict(Ctx& c, const CCLevelT<T>& F, const CCLevelT<T>& C);
+template <typename T>
+void launch_cc_prolong(Ctx& c, const CCLevelT<T>& F, const CCLevelT<T>& C);
+template <typename T>
+void launch_cc_bottom(Ctx& c, const CCLevelT<T>& L, double beta, int sweeps);
+template <typename T>
+void launch_nd_jacobi(Ctx& c, const NDLevelT<T>& L, double sigma, double omega, const T* in, T* out);
+template <typename T>
+void launch_nd_resid(Ctx& c, const NDLevelT<T>& L, double sigma, double* partials, int* nparts);
+template <typename T>
+void launch_nd_restrict(Ctx& c, const NDLevelT<T>& F, const NDLevelT<T>& C);
+template <typename T>
+void launch_nd_prolong(Ctx& c, const NDLevelT<T>& F, const NDLevelT<T>& C);
+template <typename T>
+void launch_nd_bottom(Ctx& c, const NDLevelT<T>& L, double sigma, double omega, int sweeps);
+void launch_to_f32(Ctx& c, const double* r, float* rhs, float* phi, long long n);
+void launch_add_f32(Ctx& c, double* phi, const float* e, long long n);
 
 }  // namespace ks

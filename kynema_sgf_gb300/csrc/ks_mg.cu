@@ -46,14 +46,16 @@ inline int parts_for(long long n) {
 }
 
 // ---------------------------------------------------------------- cell-centred
-__device__ inline long long ci3(const CCLevelDev& L, int i, int j, int k) { return ((long long)k * L.ny + j) * L.nx + i; }
+template <typename T>
+__device__ inline long long ci3(const CCLevelT<T>& L, int i, int j, int k) { return ((long long)k * L.ny + j) * L.nx + i; }
 
 // beta * laplacian at (i,j,k) and its diagonal
-__device__ inline void cc_ax(const CCLevelDev& L, const double* p, double beta, int i, int j, int k, double& Ax, double& dg) {
+template <typename T>
+__device__ inline void cc_ax(const CCLevelT<T>& L, const T* p, T beta, int i, int j, int k, T& Ax, T& dg) {
     const int ip = i + 1 == L.nx ? 0 : i + 1, im = i == 0 ? L.nx - 1 : i - 1;
     const int jp = j + 1 == L.ny ? 0 : j + 1, jm = j == 0 ? L.ny - 1 : j - 1;
-    double s = L.ix2 * (p[ci3(L, ip, j, k)] + p[ci3(L, im, j, k)]) + L.iy2 * (p[ci3(L, i, jp, k)] + p[ci3(L, i, jm, k)]);
-    double d = 2.0 * L.ix2 + 2.0 * L.iy2;
+    T s = L.ix2 * (p[ci3(L, ip, j, k)] + p[ci3(L, im, j, k)]) + L.iy2 * (p[ci3(L, i, jp, k)] + p[ci3(L, i, jm, k)]);
+    T d = T(2) * L.ix2 + T(2) * L.iy2;
     if (L.zper) {
         const int km = k == 0 ? L.nz - 1 : k - 1;
         s += L.iz2 * p[ci3(L, i, j, km)];
@@ -71,12 +73,14 @@ __device__ inline void cc_ax(const CCLevelDev& L, const double* p, double beta, 
 
 // inverse of the diagonal -beta*d for the cell at z index k (the wall-adjacent
 // layers drop one z neighbour)
-__device__ inline double cc_inv_diag(const CCLevelDev& L, int k) {
+template <typename T>
+__device__ inline T cc_inv_diag(const CCLevelT<T>& L, int k) {
     if (L.zper || (k > 0 && k < L.nz - 1)) return L.inv_diag[0];
     return (L.nz == 1) ? L.inv_diag[2] : L.inv_diag[1];
 }
 
-__global__ void k_cc_gsrb(CCLevelDev L, double beta, int color) {
+template <typename T>
+__global__ void k_cc_gsrb(CCLevelT<T> L, T beta, int color) {
     const long long half = (long long)L.nx * L.ny * L.nz / 2;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= half) return;
@@ -85,45 +89,48 @@ __global__ void k_cc_gsrb(CCLevelDev L, double beta, int color) {
     const long long r = t / hx;
     const int j = (int)(r % L.ny), k = (int)(r / L.ny);
     const int i = 2 * i2 + ((j + k + color) & 1);
-    double Ax, dg;
+    T Ax, dg;
     cc_ax(L, L.phi, beta, i, j, k, Ax, dg);
     const long long c = ci3(L, i, j, k);
     L.phi[c] += (L.rhs[c] - Ax) * cc_inv_diag(L, k);
 }
 
-__global__ void k_cc_resid(CCLevelDev L, double beta, double* parts) {
+template <typename T>
+__global__ void k_cc_resid(CCLevelT<T> L, T beta, double* parts) {
     const long long N = (long long)L.nx * L.ny * L.nz;
     double mx = 0.0;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N; t += (long long)gridDim.x * blockDim.x) {
         const int i = (int)(t % L.nx);
         const long long r = t / L.nx;
         const int j = (int)(r % L.ny), k = (int)(r / L.ny);
-        double Ax, dg;
+        T Ax, dg;
         cc_ax(L, L.phi, beta, i, j, k, Ax, dg);
-        const double v = L.rhs[t] - Ax;
+        const T v = L.rhs[t] - Ax;
         L.res[t] = v;
-        mx = fmax(mx, fabs(v));
+        mx = fmax(mx, fabs((double)v));
     }
     mx = bred<1>(mx);
     if (threadIdx.x == 0 && parts) parts[blockIdx.x] = mx;
 }
 
-__global__ void k_cc_restrict(CCLevelDev F, CCLevelDev C) {
+template <typename T>
+__global__ void k_cc_restrict(CCLevelT<T> F, CCLevelT<T> C) {
     const long long N = (long long)C.nx * C.ny * C.nz;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= N) return;
     const int i = (int)(t % C.nx);
     const long long r = t / C.nx;
     const int j = (int)(r % C.ny), k = (int)(r / C.ny);
-    double s = 0.0;
+    T s = T(0);
     for (int c = 0; c < 2; ++c)
         for (int b = 0; b < 2; ++b)
             for (int a = 0; a < 2; ++a) s += F.res[ci3(F, 2 * i + a, 2 * j + b, 2 * k + c)];
-    C.rhs[t] = 0.125 * s;
-    C.phi[t] = 0.0;
+    C.rhs[t] = T(0.125) * s;
+    C.phi[t] = T(0);
 }
 
-__global__ void k_cc_prolong(CCLevelDev F, CCLevelDev C) {
+template <typename T>
+__global__ void k_cc_prolong(CCLevelT<T> F, CCLevelT<T> C) {
     const long long N = (long long)F.nx * F.ny * F.nz;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= N) return;
@@ -133,7 +140,8 @@ __global__ void k_cc_prolong(CCLevelDev F, CCLevelDev C) {
     F.phi[t] += C.phi[ci3(C, i / 2, j / 2, k / 2)];
 }
 
-__global__ void k_cc_bottom(CCLevelDev L, double beta, int sweeps) {
+template <typename T>
+__global__ void k_cc_bottom(CCLevelT<T> L, T beta, int sweeps) {
     const long long N = (long long)L.nx * L.ny * L.nz;
     for (int s = 0; s < sweeps; ++s)
         for (int color = 0; color < 2; ++color) {
@@ -142,7 +150,7 @@ __global__ void k_cc_bottom(CCLevelDev L, double beta, int sweeps) {
                 const long long r = t / L.nx;
                 const int j = (int)(r % L.ny), k = (int)(r / L.ny);
                 if (((i + j + k) & 1) != color) continue;
-                double Ax, dg;
+                T Ax, dg;
                 cc_ax(L, L.phi, beta, i, j, k, Ax, dg);
                 L.phi[t] += (L.rhs[t] - Ax) * cc_inv_diag(L, k);
             }
@@ -151,7 +159,8 @@ __global__ void k_cc_bottom(CCLevelDev L, double beta, int sweeps) {
 }
 
 // ---------------------------------------------------------------- nodal
-__device__ inline double nd_at(const NDLevelDev& L, const double* p, int i, int j, int k) {
+template <typename T>
+__device__ inline T nd_at(const NDLevelT<T>& L, const T* p, int i, int j, int k) {
     i = i < 0 ? i + L.nx : (i >= L.nx ? i - L.nx : i);
     j = j < 0 ? j + L.ny : (j >= L.ny ? j - L.ny : j);
     if (L.zper) k = k < 0 ? k + L.nz : (k >= L.nz ? k - L.nz : k);
@@ -161,7 +170,8 @@ __device__ inline double nd_at(const NDLevelDev& L, const double* p, int i, int 
 
 // sigma * (27-point Q1 stencil) at node (i,j,k); the weights are symmetric in
 // each direction, so neighbours are summed by weight class first.
-__device__ inline double nd_ax(const NDLevelDev& L, const double* p, double sigma, int i, int j, int k) {
+template <typename T>
+__device__ inline T nd_ax(const NDLevelT<T>& L, const T* p, T sigma, int i, int j, int k) {
     const int im = i == 0 ? L.nx - 1 : i - 1, ip = i + 1 == L.nx ? 0 : i + 1;
     const int jm = j == 0 ? L.ny - 1 : j - 1, jp = j + 1 == L.ny ? 0 : j + 1;
     int km, kp;
@@ -177,21 +187,22 @@ __device__ inline double nd_ax(const NDLevelDev& L, const double* p, double sigm
     const long long rm = km * sz, r0 = k * sz, rp = kp * sz;
     const long long cm = jm * sy, c0 = j * sy, cp = jp * sy;
     auto at = [&](long long r, long long c, int x) { return p[r + c + x]; };
-    const double ctr = at(r0, c0, i);
-    const double fx = at(r0, c0, im) + at(r0, c0, ip);
-    const double fy = at(r0, cm, i) + at(r0, cp, i);
-    const double fz = at(rm, c0, i) + at(rp, c0, i);
-    const double exy = at(r0, cm, im) + at(r0, cm, ip) + at(r0, cp, im) + at(r0, cp, ip);
-    const double exz = at(rm, c0, im) + at(rm, c0, ip) + at(rp, c0, im) + at(rp, c0, ip);
-    const double eyz = at(rm, cm, i) + at(rm, cp, i) + at(rp, cm, i) + at(rp, cp, i);
-    const double cr = at(rm, cm, im) + at(rm, cm, ip) + at(rm, cp, im) + at(rm, cp, ip) + at(rp, cm, im) + at(rp, cm, ip) +
-                      at(rp, cp, im) + at(rp, cp, ip);
-    const double s = L.W[13] * ctr + L.W[12] * fx + L.W[10] * fy + L.W[4] * fz + L.W[9] * exy + L.W[3] * exz + L.W[1] * eyz +
+    const T ctr = at(r0, c0, i);
+    const T fx = at(r0, c0, im) + at(r0, c0, ip);
+    const T fy = at(r0, cm, i) + at(r0, cp, i);
+    const T fz = at(rm, c0, i) + at(rp, c0, i);
+    const T exy = at(r0, cm, im) + at(r0, cm, ip) + at(r0, cp, im) + at(r0, cp, ip);
+    const T exz = at(rm, c0, im) + at(rm, c0, ip) + at(rp, c0, im) + at(rp, c0, ip);
+    const T eyz = at(rm, cm, i) + at(rm, cp, i) + at(rp, cm, i) + at(rp, cp, i);
+    const T cr = at(rm, cm, im) + at(rm, cm, ip) + at(rm, cp, im) + at(rm, cp, ip) + at(rp, cm, im) + at(rp, cm, ip) + at(rp, cp, im) +
+                 at(rp, cp, ip);
+    const T s = L.W[13] * ctr + L.W[12] * fx + L.W[10] * fy + L.W[4] * fz + L.W[9] * exy + L.W[3] * exz + L.W[1] * eyz +
                      L.W[0] * cr;
     return sigma * s;
 }
 
-__global__ void k_nd_jacobi(NDLevelDev L, double sigma, double omega, const double* in, double* out) {
+template <typename T>
+__global__ void k_nd_jacobi(NDLevelT<T> L, T sigma, T omega, const T* in, T* out) {
     const long long N = (long long)L.nx * L.ny * L.nz;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= N) return;
@@ -201,38 +212,41 @@ __global__ void k_nd_jacobi(NDLevelDev L, double sigma, double omega, const doub
     out[t] = in[t] + omega * (L.rhs[t] - nd_ax(L, in, sigma, i, j, k)) * L.inv_diag;
 }
 
-__global__ void k_nd_resid(NDLevelDev L, double sigma, double* parts) {
+template <typename T>
+__global__ void k_nd_resid(NDLevelT<T> L, T sigma, double* parts) {
     const long long N = (long long)L.nx * L.ny * L.nz;
     double mx = 0.0;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N; t += (long long)gridDim.x * blockDim.x) {
         const int i = (int)(t % L.nx);
         const long long r = t / L.nx;
         const int j = (int)(r % L.ny), k = (int)(r / L.ny);
-        const double v = L.rhs[t] - nd_ax(L, L.phi, sigma, i, j, k);
+        const T v = L.rhs[t] - nd_ax(L, L.phi, sigma, i, j, k);
         L.res[t] = v;
-        mx = fmax(mx, fabs(v));
+        mx = fmax(mx, fabs((double)v));
     }
     mx = bred<1>(mx);
     if (threadIdx.x == 0 && parts) parts[blockIdx.x] = mx;
 }
 
-__global__ void k_nd_restrict(NDLevelDev F, NDLevelDev C) {
+template <typename T>
+__global__ void k_nd_restrict(NDLevelT<T> F, NDLevelT<T> C) {
     const long long N = (long long)C.nx * C.ny * C.nz;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= N) return;
     const int i = (int)(t % C.nx);
     const long long r = t / C.nx;
     const int j = (int)(r % C.ny), k = (int)(r / C.ny);
-    const double w1[3] = {0.25, 0.5, 0.25};
-    double s = 0.0;
+    const T w1[3] = {T(0.25), T(0.5), T(0.25)};
+    T s = T(0);
     for (int c = -1; c <= 1; ++c)
         for (int b = -1; b <= 1; ++b)
             for (int a = -1; a <= 1; ++a) s += w1[a + 1] * w1[b + 1] * w1[c + 1] * nd_at(F, F.res, 2 * i + a, 2 * j + b, 2 * k + c);
     C.rhs[t] = s;
-    C.phi[t] = 0.0;
+    C.phi[t] = T(0);
 }
 
-__global__ void k_nd_prolong(NDLevelDev F, NDLevelDev C) {
+template <typename T>
+__global__ void k_nd_prolong(NDLevelT<T> F, NDLevelT<T> C) {
     const long long N = (long long)F.nx * F.ny * F.nz;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= N) return;
@@ -240,14 +254,16 @@ __global__ void k_nd_prolong(NDLevelDev F, NDLevelDev C) {
     const long long r = t / F.nx;
     const int j = (int)(r % F.ny), k = (int)(r / F.ny);
     const int ci = i >> 1, cj = j >> 1, ck = k >> 1, oi = i & 1, oj = j & 1, ok = k & 1;
-    double s = 0.0;
+    T s = T(0);
     for (int c = 0; c <= ok; ++c)
         for (int b = 0; b <= oj; ++b)
             for (int a = 0; a <= oi; ++a) s += nd_at(C, C.phi, ci + a, cj + b, ck + c);
-    F.phi[t] += s / (double)((1 + oi) * (1 + oj) * (1 + ok));
+    const int cnt = (1 + oi) * (1 + oj) * (1 + ok);
+    F.phi[t] += (cnt == 1) ? s : (cnt == 2 ? T(0.5) * s : (cnt == 4 ? T(0.25) * s : T(0.125) * s));
 }
 
-__global__ void k_nd_bottom(NDLevelDev L, double sigma, double omega, int sweeps) {
+template <typename T>
+__global__ void k_nd_bottom(NDLevelT<T> L, T sigma, T omega, int sweeps) {
     const long long N = (long long)L.nx * L.ny * L.nz;
     for (int s = 0; s < sweeps; ++s) {
         for (long long t = threadIdx.x; t < N; t += blockDim.x) {
@@ -262,46 +278,95 @@ __global__ void k_nd_bottom(NDLevelDev L, double sigma, double omega, int sweeps
     }
 }
 
+// defect correction helpers: rhs32 = (float) r64, phi32 = 0 ; phi64 += phi32
+__global__ void k_to_f32(const double* r, float* rhs, float* phi, long long n) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    rhs[t] = (float)r[t];
+    phi[t] = 0.0f;
+}
+__global__ void k_add_f32(double* phi, const float* e, long long n) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    phi[t] += (double)e[t];
+}
+
 }  // namespace
 
 
-inline double ncc(const CCLevelDev& L) { return (double)L.nx * L.ny * L.nz; }
-inline double nnd(const NDLevelDev& L) { return (double)L.nx * L.ny * L.nz; }
-constexpr double B8 = 8.0;
+template <typename T>
+inline double ncc(const CCLevelT<T>& L) {
+    return (double)L.nx * L.ny * L.nz;
+}
+template <typename T>
+inline double nnd(const NDLevelT<T>& L) {
+    return (double)L.nx * L.ny * L.nz;
+}
 
-void launch_cc_gsrb(Ctx& c, const CCLevelDev& L, double beta, int color) {
-    KS_LAUNCH(c, k_cc_gsrb, nblocks((long long)L.nx * L.ny * L.nz / 2, BS), BS, B8 * 2.0 * ncc(L), L, beta, color);
+template <typename T>
+void launch_cc_gsrb(Ctx& c, const CCLevelT<T>& L, double beta, int color) {
+    KS_LAUNCH(c, k_cc_gsrb<T>, nblocks((long long)L.nx * L.ny * L.nz / 2, BS), BS, sizeof(T) * 2.0 * ncc(L), L, T(beta), color);
 }
-void launch_cc_resid(Ctx& c, const CCLevelDev& L, double beta, double* parts, int* np) {
+template <typename T>
+void launch_cc_resid(Ctx& c, const CCLevelT<T>& L, double beta, double* parts, int* np) {
     const int n = parts_for((long long)L.nx * L.ny * L.nz);
     if (np) *np = n;
-    KS_LAUNCH(c, k_cc_resid, n, BS, B8 * 3.0 * ncc(L), L, beta, parts);
+    KS_LAUNCH(c, k_cc_resid<T>, n, BS, sizeof(T) * 3.0 * ncc(L), L, T(beta), parts);
 }
-void launch_cc_restrict(Ctx& c, const CCLevelDev& F, const CCLevelDev& C) {
-    KS_LAUNCH(c, k_cc_restrict, nblocks((long long)C.nx * C.ny * C.nz, BS), BS, B8 * (ncc(F) + 2.0 * ncc(C)), F, C);
+template <typename T>
+void launch_cc_restrict(Ctx& c, const CCLevelT<T>& F, const CCLevelT<T>& C) {
+    KS_LAUNCH(c, k_cc_restrict<T>, nblocks((long long)C.nx * C.ny * C.nz, BS), BS, sizeof(T) * (ncc(F) + 2.0 * ncc(C)), F, C);
 }
-void launch_cc_prolong(Ctx& c, const CCLevelDev& F, const CCLevelDev& C) {
-    KS_LAUNCH(c, k_cc_prolong, nblocks((long long)F.nx * F.ny * F.nz, BS), BS, B8 * (2.0 * ncc(F) + ncc(C)), F, C);
+template <typename T>
+void launch_cc_prolong(Ctx& c, const CCLevelT<T>& F, const CCLevelT<T>& C) {
+    KS_LAUNCH(c, k_cc_prolong<T>, nblocks((long long)F.nx * F.ny * F.nz, BS), BS, sizeof(T) * (2.0 * ncc(F) + ncc(C)), F, C);
 }
-void launch_cc_bottom(Ctx& c, const CCLevelDev& L, double beta, int sweeps) {
-    KS_LAUNCH(c, k_cc_bottom, 1, 256, B8 * 3.0 * ncc(L), L, beta, sweeps);
+template <typename T>
+void launch_cc_bottom(Ctx& c, const CCLevelT<T>& L, double beta, int sweeps) {
+    KS_LAUNCH(c, k_cc_bottom<T>, 1, 256, sizeof(T) * 3.0 * ncc(L), L, T(beta), sweeps);
 }
-void launch_nd_jacobi(Ctx& c, const NDLevelDev& L, double sigma, double omega, const double* in, double* out) {
-    KS_LAUNCH(c, k_nd_jacobi, nblocks((long long)L.nx * L.ny * L.nz, BS), BS, B8 * 3.0 * nnd(L), L, sigma, omega, in, out);
+template <typename T>
+void launch_nd_jacobi(Ctx& c, const NDLevelT<T>& L, double sigma, double omega, const T* in, T* out) {
+    KS_LAUNCH(c, k_nd_jacobi<T>, nblocks((long long)L.nx * L.ny * L.nz, BS), BS, sizeof(T) * 3.0 * nnd(L), L, T(sigma), T(omega), in, out);
 }
-void launch_nd_resid(Ctx& c, const NDLevelDev& L, double sigma, double* parts, int* np) {
+template <typename T>
+void launch_nd_resid(Ctx& c, const NDLevelT<T>& L, double sigma, double* parts, int* np) {
     const int n = parts_for((long long)L.nx * L.ny * L.nz);
     if (np) *np = n;
-    KS_LAUNCH(c, k_nd_resid, n, BS, B8 * 3.0 * nnd(L), L, sigma, parts);
+    KS_LAUNCH(c, k_nd_resid<T>, n, BS, sizeof(T) * 3.0 * nnd(L), L, T(sigma), parts);
 }
-void launch_nd_restrict(Ctx& c, const NDLevelDev& F, const NDLevelDev& C) {
-    KS_LAUNCH(c, k_nd_restrict, nblocks((long long)C.nx * C.ny * C.nz, BS), BS, B8 * (nnd(F) + 2.0 * nnd(C)), F, C);
+template <typename T>
+void launch_nd_restrict(Ctx& c, const NDLevelT<T>& F, const NDLevelT<T>& C) {
+    KS_LAUNCH(c, k_nd_restrict<T>, nblocks((long long)C.nx * C.ny * C.nz, BS), BS, sizeof(T) * (nnd(F) + 2.0 * nnd(C)), F, C);
 }
-void launch_nd_prolong(Ctx& c, const NDLevelDev& F, const NDLevelDev& C) {
-    KS_LAUNCH(c, k_nd_prolong, nblocks((long long)F.nx * F.ny * F.nz, BS), BS, B8 * (2.0 * nnd(F) + nnd(C)), F, C);
+template <typename T>
+void launch_nd_prolong(Ctx& c, const NDLevelT<T>& F, const NDLevelT<T>& C) {
+    KS_LAUNCH(c, k_nd_prolong<T>, nblocks((long long)F.nx * F.ny * F.nz, BS), BS, sizeof(T) * (2.0 * nnd(F) + nnd(C)), F, C);
 }
-void launch_nd_bottom(Ctx& c, const NDLevelDev& L, double sigma, double omega, int sweeps) {
-    KS_LAUNCH(c, k_nd_bottom, 1, 256, B8 * 4.0 * nnd(L), L, sigma, omega, sweeps);
+template <typename T>
+void launch_nd_bottom(Ctx& c, const NDLevelT<T>& L, double sigma, double omega, int sweeps) {
+    KS_LAUNCH(c, k_nd_bottom<T>, 1, 256, sizeof(T) * 4.0 * nnd(L), L, T(sigma), T(omega), sweeps);
 }
+void launch_to_f32(Ctx& c, const double* r, float* rhs, float* phi, long long n) {
+    KS_LAUNCH(c, k_to_f32, nblocks(n, BS), BS, 16.0 * n, r, rhs, phi, n);
+}
+void launch_add_f32(Ctx& c, double* phi, const float* e, long long n) {
+    KS_LAUNCH(c, k_add_f32, nblocks(n, BS), BS, 20.0 * n, phi, e, n);
+}
+
+#define KS_INST(T)                                                                                           \
+    template void launch_cc_gsrb<T>(Ctx&, const CCLevelT<T>&, double, int);                                  \
+    template void launch_cc_resid<T>(Ctx&, const CCLevelT<T>&, double, double*, int*);                       \
+    template void launch_cc_restrict<T>(Ctx&, const CCLevelT<T>&, const CCLevelT<T>&);                       \
+    template void launch_cc_prolong<T>(Ctx&, const CCLevelT<T>&, const CCLevelT<T>&);                        \
+    template void launch_cc_bottom<T>(Ctx&, const CCLevelT<T>&, double, int);                                \
+    template void launch_nd_jacobi<T>(Ctx&, const NDLevelT<T>&, double, double, const T*, T*);               \
+    template void launch_nd_resid<T>(Ctx&, const NDLevelT<T>&, double, double*, int*);                       \
+    template void launch_nd_restrict<T>(Ctx&, const NDLevelT<T>&, const NDLevelT<T>&);                       \
+    template void launch_nd_prolong<T>(Ctx&, const NDLevelT<T>&, const NDLevelT<T>&);                        \
+    template void launch_nd_bottom<T>(Ctx&, const NDLevelT<T>&, double, double, int);
+KS_INST(double)
+KS_INST(float)
+#undef KS_INST
 
 }  // namespace ks
