@@ -20,6 +20,7 @@ struct Grid {
     int zper;
     int zlo, zhi;
     double dx, dy, dz;
+    double idx, idy, idz;  // 1/dx, 1/dy, 1/dz (FP64 division is expensive on this GPU)
     long long N;    // cells
     long long NFz;  // z faces stored: nx*ny*(nz+1)
 };
@@ -29,6 +30,7 @@ __host__ __device__ inline long long cidx(const Grid& g, int i, int j, int k) {
 }
 __host__ __device__ inline int wrapn(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 __host__ __device__ inline double hd(const Grid& g, int d) { return d == 0 ? g.dx : (d == 1 ? g.dy : g.dz); }
+__host__ __device__ inline double ihd(const Grid& g, int d) { return d == 0 ? g.idx : (d == 1 ? g.idy : g.idz); }
 __host__ __device__ inline int nd(const Grid& g, int d) { return d == 0 ? g.nx : (d == 1 ? g.ny : g.nz); }
 __host__ __device__ inline int nzfaces(const Grid& g) { return g.zper ? g.nz : g.nz + 1; }
 

@@ -348,7 +348,7 @@ __global__ void k_adv_div(Grid g, FluxPtrs<T> F, double* conv) {
     const long long r = t / g.nx;
     const int j = (int)(r % g.ny), k = (int)(r / g.ny);
     const long long xp = fidx(g, 0, i + 1, j, k), yp = fidx(g, 1, i, j + 1, k), zp = fidx(g, 2, i, j, k + 1), zm = fidx(g, 2, i, j, k);
-    const T ix = T(1.0 / g.dx), iy = T(1.0 / g.dy), iz = T(1.0 / g.dz);
+    const T ix = T(g.idx), iy = T(g.idy), iz = T(g.idz);
     for (int n = 0; n < 3; ++n)
         conv[n * g.N + t] =
             (double)(-((F.p[n][xp] - F.p[n][t]) * ix + (F.p[3 + n][yp] - F.p[3 + n][t]) * iy + (F.p[6 + n][zp] - F.p[6 + n][zm]) * iz));

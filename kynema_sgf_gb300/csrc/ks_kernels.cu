@@ -117,9 +117,9 @@ __global__ void k_smag(Grid g, const double* vel, double* mueff, double mu, doub
     if (!g.zper && k == g.nz - 1) { a = 4.0 / 3.0; b = -1.0; c = -1.0 / 3.0; }
     double gx[3], gy[3], gz[3];
     for (int n = 0; n < 3; ++n) {
-        gx[n] = 0.5 * (V(n, i + 1, j, k) - V(n, i - 1, j, k)) / g.dx;
-        gy[n] = 0.5 * (V(n, i, j + 1, k) - V(n, i, j - 1, k)) / g.dy;
-        gz[n] = (a * V(n, i, j, k + 1) + b * V(n, i, j, k) + c * V(n, i, j, k - 1)) / g.dz;
+        gx[n] = 0.5 * (V(n, i + 1, j, k) - V(n, i - 1, j, k)) * g.idx;
+        gy[n] = 0.5 * (V(n, i, j + 1, k) - V(n, i, j - 1, k)) * g.idy;
+        gz[n] = (a * V(n, i, j, k + 1) + b * V(n, i, j, k) + c * V(n, i, j, k - 1)) * g.idz;
     }
     const double s = sqrt(2.0 * gx[0] * gx[0] + 2.0 * gy[1] * gy[1] + 2.0 * gz[2] * gz[2] + (gy[0] + gx[1]) * (gy[0] + gx[1]) +
                           (gz[1] + gy[2]) * (gz[1] + gy[2]) + (gx[2] + gz[0]) * (gx[2] + gz[0]));
@@ -135,7 +135,7 @@ __global__ void k_sources(Grid g, const double* vel, const double* gp, const dou
     if (t >= g.N) return;
     const long long N = g.N;
     double f[3];
-    for (int n = 0; n < 3; ++n) f[n] = -gp[n * N + t] / s.rho;
+    for (int n = 0; n < 3; ++n) f[n] = -gp[n * N + t] * s.irho;
     if (s.geo)
         for (int n = 0; n < 3; ++n) f[n] += (n == 2 ? s.hfac : 1.0) * s.gf[n];
     if (s.cor) {
@@ -241,7 +241,7 @@ __device__ inline void tensor_flux(const Grid& g, const VelDiff& V, const double
         const long long cm = cidx(g, wrapn(im, g.nx), wrapn(jm, g.ny), g.zper ? wrapn(km, g.nz) : km);
         mf = 0.5 * (mu[cm] + mu[cc]);
     }
-    const double ih[3] = {1.0 / g.dx, 1.0 / g.dy, 1.0 / g.dz};
+    const double ih[3] = {g.idx, g.idy, g.idz};
     double gr[3][3];  // gr[m][n] = d u_n / d x_m on the face
     for (int n = 0; n < 3; ++n) {
         for (int m = 0; m < 3; ++m) {
@@ -293,8 +293,8 @@ __global__ void k_tau_div(Grid g, Flux9 F, double* out, int mode, const double* 
     if (t >= g.N) return;
     int i, j, k;
     cell_of(g, t, i, j, k);
-    const double ih[3] = {1.0 / g.dx, 1.0 / g.dy, 1.0 / g.dz};
-    const double irho = 1.0 / rho;
+    const double ih[3] = {g.idx, g.idy, g.idz};
+    const double irho = 1.0 / rho;  // once per thread
     double acc[3] = {0, 0, 0};
     for (int d = 0; d < 3; ++d) {
         const long long lo = fidx(g, d, i, j, k), hi = fidx(g, d, i + (d == 0), j + (d == 1), k + (d == 2));
@@ -357,9 +357,9 @@ __global__ void k_nodal_rhs(Grid g, const double* vel, double* rhs, double* part
         double dv = 0;
         for (int c = 0; c < 2; ++c)
             for (int b = 0; b < 2; ++b) {
-                dv += 0.25 / g.dx * (vel_mirror(g, vel, 0, i, j - b, k - c) - vel_mirror(g, vel, 0, i - 1, j - b, k - c));
-                dv += 0.25 / g.dy * (vel_mirror(g, vel, 1, i - b, j, k - c) - vel_mirror(g, vel, 1, i - b, j - 1, k - c));
-                dv += 0.25 / g.dz * (vel_mirror(g, vel, 2, i - b, j - c, k) - vel_mirror(g, vel, 2, i - b, j - c, k - 1));
+                dv += 0.25 * g.idx * (vel_mirror(g, vel, 0, i, j - b, k - c) - vel_mirror(g, vel, 0, i - 1, j - b, k - c));
+                dv += 0.25 * g.idy * (vel_mirror(g, vel, 1, i - b, j, k - c) - vel_mirror(g, vel, 1, i - b, j - 1, k - c));
+                dv += 0.25 * g.idz * (vel_mirror(g, vel, 2, i - b, j - c, k) - vel_mirror(g, vel, 2, i - b, j - c, k - 1));
             }
         rhs[t] = dv;
         const double w = (!g.zper && (k == 0 || k == nzn - 1)) ? 0.5 : 1.0;
@@ -394,7 +394,7 @@ __global__ void k_nodal_post_cells(Grid g, const double* phi, double* vel, const
             gy += node_at(g, phi, i + b, j + 1, k + c) - node_at(g, phi, i + b, j, k + c);
             gz += node_at(g, phi, i + b, j + c, k + 1) - node_at(g, phi, i + b, j + c, k);
         }
-    const double G[3] = {0.25 * gx / g.dx, 0.25 * gy / g.dy, 0.25 * gz / g.dz};
+    const double G[3] = {0.25 * gx * g.idx, 0.25 * gy * g.idy, 0.25 * gz * g.idz};
     const long long N = g.N;
     for (int n = 0; n < 3; ++n) {
         double v = vel[n * N + t] - sigma * G[n];
@@ -418,8 +418,8 @@ __global__ void k_mac_rhs(Grid g, const double* um, const double* vm, const doub
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < g.N; t += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         cell_of(g, t, i, j, k);
-        const double r = (um[fidx(g, 0, i + 1, j, k)] - um[t]) / g.dx + (vm[fidx(g, 1, i, j + 1, k)] - vm[t]) / g.dy +
-                         (wm[fidx(g, 2, i, j, k + 1)] - wm[fidx(g, 2, i, j, k)]) / g.dz;
+        const double r = (um[fidx(g, 0, i + 1, j, k)] - um[t]) * g.idx + (vm[fidx(g, 1, i, j + 1, k)] - vm[t]) * g.idy +
+                         (wm[fidx(g, 2, i, j, k + 1)] - wm[fidx(g, 2, i, j, k)]) * g.idz;
         rhs[t] = r;
         s += r;
     }
@@ -433,23 +433,24 @@ __global__ void k_mac_correct(Grid g, const double* phi, double* um, double* vm,
     int i, j, k;
     cell_of(g, t, i, j, k);
     const double p0 = phi[t];
-    um[t] -= beta * (p0 - phi[cidx(g, wrapn(i - 1, g.nx), j, k)]) / g.dx;
-    vm[t] -= beta * (p0 - phi[cidx(g, i, wrapn(j - 1, g.ny), k)]) / g.dy;
-    if (g.zper) wm[t] -= beta * (p0 - phi[cidx(g, i, j, wrapn(k - 1, g.nz))]) / g.dz;
-    else if (k > 0) wm[t] -= beta * (p0 - phi[cidx(g, i, j, k - 1)]) / g.dz;
+    um[t] -= beta * (p0 - phi[cidx(g, wrapn(i - 1, g.nx), j, k)]) * g.idx;
+    vm[t] -= beta * (p0 - phi[cidx(g, i, wrapn(j - 1, g.ny), k)]) * g.idy;
+    if (g.zper) wm[t] -= beta * (p0 - phi[cidx(g, i, j, wrapn(k - 1, g.nz))]) * g.idz;
+    else if (k > 0) wm[t] -= beta * (p0 - phi[cidx(g, i, j, k - 1)]) * g.idz;
 }
 
 // ---------------------------------------------------------------- reductions
 __global__ void k_cfl(Grid g, const double* vel, const double* src, const double* mu, double rho, double* parts, int np) {
     double c = 0, d = 0, f = 0;
-    const double dxi[3] = {1.0 / g.dx, 1.0 / g.dy, 1.0 / g.dz};
+    const double dxi[3] = {g.idx, g.idy, g.idz};
+    const double irho = 1.0 / rho;
     const double dxinv2 = 2.0 * (dxi[0] * dxi[0] + dxi[1] * dxi[1] + dxi[2] * dxi[2]);
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < g.N; t += (long long)gridDim.x * blockDim.x) {
         for (int n = 0; n < 3; ++n) {
             c = fmax(c, fabs(vel[n * g.N + t]) * dxi[n]);
-            f = fmax(f, fabs(src[n * g.N + t]) * dxi[n] / rho);
+            f = fmax(f, fabs(src[n * g.N + t]) * dxi[n] * irho);
         }
-        d = fmax(d, mu[t] * dxinv2 / rho);
+        d = fmax(d, mu[t] * dxinv2 * irho);
     }
     c = block_reduce<1>(c);
     d = block_reduce<1>(d);

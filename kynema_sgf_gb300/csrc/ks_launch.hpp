@@ -85,7 +85,7 @@ struct Ctx {
     } while (0)
 
 struct Scalars {  // values fed to the pointwise kernels
-    double rho, mu, smag_fac;
+    double rho, irho, mu, smag_fac;
     int smag;
     int geo, cor, body, act;
     double gf[3];
@@ -160,7 +160,8 @@ struct NDLevelT {
     int nx, ny, nz;  // nodes
     int zper;
     T W[27];
-    T inv_diag;  // 1/(sigma W_centre)
+    T inv_diag;      // 1/(sigma W_centre)
+    int faces_zero;  // face-neighbour weights vanish (equal spacings): skipped
     T *phi, *rhs, *res, *tmp;
 };
 using CCLevelDev = CCLevelT<double>;
@@ -179,6 +180,10 @@ template <typename T>
 void launch_nd_jacobi(Ctx& c, const NDLevelT<T>& L, double sigma, double omega, const T* in, T* out);
 template <typename T>
 void launch_nd_resid(Ctx& c, const NDLevelT<T>& L, double sigma, double* partials, int* nparts);
+// Jacobi sweep that also writes block maxima of |rhs - A in| (the residual of
+// the input iterate) for the convergence test
+void launch_nd_jacobi_norm(Ctx& c, const NDLevelT<double>& L, double sigma, double omega, const double* in, double* out,
+                           double* partials, int* nparts);
 template <typename T>
 void launch_nd_restrict(Ctx& c, const NDLevelT<T>& F, const NDLevelT<T>& C);
 template <typename T>

@@ -188,16 +188,19 @@ __device__ inline T nd_ax(const NDLevelT<T>& L, const T* p, T sigma, int i, int 
     const long long cm = jm * sy, c0 = j * sy, cp = jp * sy;
     auto at = [&](long long r, long long c, int x) { return p[r + c + x]; };
     const T ctr = at(r0, c0, i);
-    const T fx = at(r0, c0, im) + at(r0, c0, ip);
-    const T fy = at(r0, cm, i) + at(r0, cp, i);
-    const T fz = at(rm, c0, i) + at(rp, c0, i);
+    T fx = T(0), fy = T(0), fz = T(0);
+    if (!L.faces_zero) {
+        fx = at(r0, c0, im) + at(r0, c0, ip);
+        fy = at(r0, cm, i) + at(r0, cp, i);
+        fz = at(rm, c0, i) + at(rp, c0, i);
+    }
     const T exy = at(r0, cm, im) + at(r0, cm, ip) + at(r0, cp, im) + at(r0, cp, ip);
     const T exz = at(rm, c0, im) + at(rm, c0, ip) + at(rp, c0, im) + at(rp, c0, ip);
     const T eyz = at(rm, cm, i) + at(rm, cp, i) + at(rp, cm, i) + at(rp, cp, i);
     const T cr = at(rm, cm, im) + at(rm, cm, ip) + at(rm, cp, im) + at(rm, cp, ip) + at(rp, cm, im) + at(rp, cm, ip) + at(rp, cp, im) +
                  at(rp, cp, ip);
-    const T s = L.W[13] * ctr + L.W[12] * fx + L.W[10] * fy + L.W[4] * fz + L.W[9] * exy + L.W[3] * exz + L.W[1] * eyz +
-                     L.W[0] * cr;
+    T s = L.W[13] * ctr + L.W[9] * exy + L.W[3] * exz + L.W[1] * eyz + L.W[0] * cr;
+    if (!L.faces_zero) s += L.W[12] * fx + L.W[10] * fy + L.W[4] * fz;
     return sigma * s;
 }
 
@@ -210,6 +213,21 @@ __global__ void k_nd_jacobi(NDLevelT<T> L, T sigma, T omega, const T* in, T* out
     const long long r = t / L.nx;
     const int j = (int)(r % L.ny), k = (int)(r / L.ny);
     out[t] = in[t] + omega * (L.rhs[t] - nd_ax(L, in, sigma, i, j, k)) * L.inv_diag;
+}
+
+__global__ void k_nd_jacobi_norm(NDLevelT<double> L, double sigma, double omega, const double* in, double* out, double* parts) {
+    const long long N = (long long)L.nx * L.ny * L.nz;
+    double mx = 0.0;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N; t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % L.nx);
+        const long long r = t / L.nx;
+        const int j = (int)(r % L.ny), k = (int)(r / L.ny);
+        const double res = L.rhs[t] - nd_ax(L, in, sigma, i, j, k);
+        out[t] = in[t] + omega * res * L.inv_diag;
+        mx = fmax(mx, fabs(res));
+    }
+    mx = bred<1>(mx);
+    if (threadIdx.x == 0) parts[blockIdx.x] = mx;
 }
 
 template <typename T>
@@ -346,6 +364,12 @@ void launch_nd_prolong(Ctx& c, const NDLevelT<T>& F, const NDLevelT<T>& C) {
 template <typename T>
 void launch_nd_bottom(Ctx& c, const NDLevelT<T>& L, double sigma, double omega, int sweeps) {
     KS_LAUNCH(c, k_nd_bottom<T>, 1, 256, sizeof(T) * 4.0 * nnd(L), L, T(sigma), T(omega), sweeps);
+}
+void launch_nd_jacobi_norm(Ctx& c, const NDLevelT<double>& L, double sigma, double omega, const double* in, double* out, double* parts,
+                           int* np) {
+    const int n = parts_for((long long)L.nx * L.ny * L.nz);
+    *np = n;
+    KS_LAUNCH(c, k_nd_jacobi_norm, n, BS, 8.0 * 3.0 * nnd(L), L, sigma, omega, in, out, parts);
 }
 void launch_to_f32(Ctx& c, const double* r, float* rhs, float* phi, long long n) {
     KS_LAUNCH(c, k_to_f32, nblocks(n, BS), BS, 16.0 * n, r, rhs, phi, n);

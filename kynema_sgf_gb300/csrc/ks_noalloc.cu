@@ -76,6 +76,9 @@ extern "C" int ks_divtau_noalloc(const double* vel, const double* mueff, const d
     g.dx = dx;
     g.dy = dy;
     g.dz = dz;
+    g.idx = 1.0 / dx;
+    g.idy = 1.0 / dy;
+    g.idz = 1.0 / dz;
     g.N = cells;
     g.NFz = (long long)nx * ny * (nz + 1);
 
