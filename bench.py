@@ -34,6 +34,8 @@ METRIC = "Mcell-steps/s at 256^3 (FP64 vs mixed-precision at stated error) + adj
 UNIT = "Mcell-steps/s"
 WORKLOAD = "ABL LES 256x256x128 FP64 (5120x5120x1280 m, Smagorinsky, geostrophic+Coriolis, wall model, CFL 0.9)"
 CPU_SAMPLE = (128, 128, 64)  # same dx, physics and deck as the workload, 1/8 of the cells
+# FP64 flops per algorithmic byte of the kernels that can dominate the FP64 step
+FP64_FLOPS_PER_BYTE = {"k_nd_jacobi<T>": 40.0 / 24.0, "k_nd_resid<T>": 39.0 / 24.0, "k_cc_gsrb<T>": 14.0 / 16.0}
 
 
 def parse():
@@ -143,10 +145,13 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel):
+def ncu_traffic(kernel, algorithmic_bytes_per_launch):
+    """DRAM bytes per launch of `kernel`, from the committed ncu summary: the
+    captured launch's DRAM/algorithmic ratio scaled to this run's launches."""
     try:
         t = json.load(open(os.path.join(ROOT, "profiles", "ncu_traffic.json")))
-        return t.get(kernel, {}).get("dram_bytes_per_launch")
+        ratio = t.get(kernel, {}).get("dram_to_algorithmic_ratio")
+        return ratio * algorithmic_bytes_per_launch if (ratio and algorithmic_bytes_per_launch) else None
     except Exception:
         return None
 
@@ -202,6 +207,7 @@ def our_arm(args, rank, world, local_rank):
         tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
     ms_max = float(t.item())
     dom = sim.profile_report().get(dominant, (0, 0.0, 0.0))
+    fp64_peak = ks.fma_peak(True)
     sim.profile_kernels("")
     value = cells * args.steps * world / (ms_max * 1e-3) / 1e6
     ref_state = {f: sim.get_field(f) for f in ("velocity", "gp")} if not args.no_mixed else None
@@ -265,7 +271,7 @@ def our_arm(args, rank, world, local_rank):
                  "gp_rel_err_linf": float(abs(gpm - rg).max() / abs(rg).max()),
                  "mac_residual_rel_max": max(mres), "nodal_residual_rel_max": max(nres),
                  "note": "FP32 advection and multigrid cycles, FP64 residuals / defect correction / RHS / velocity update"}
-    return dict(value=value, ms=ms_max, cells=cells, launches=launches, dominant=dominant, dom=dom, clocks=clk, e2e=e2e,
+    return dict(value=value, ms=ms_max, cells=cells, launches=launches, dominant=dominant, dom=dom, clocks=clk, e2e=e2e, fp64_peak=fp64_peak,
                 mac=statistics.mean(mac_it), nodal=statistics.mean(nod_it), size=(nx, ny, nz), mixed=mixed)
 
 
@@ -306,7 +312,7 @@ def main():
     peak, peak_kind = peaks()
     n_l, ms_l, by_l = r["dom"]
     achieved = (by_l / n_l) / ((ms_l / n_l) * 1e-3) / 1e9 if n_l else None
-    traffic = ncu_traffic(r["dominant"])
+    traffic = ncu_traffic(r["dominant"], by_l / n_l if n_l else None)
     nx, ny, nz = r["size"]
     line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -319,6 +325,13 @@ def main():
                          "launches": n_l, "avg_launch_us": 1e3 * ms_l / n_l if n_l else None,
                          "algorithmic_bytes_per_launch": by_l / n_l if n_l else None},
             "gpu_launches": r["launches"], "clocks": r["clocks"], "e2e": r["e2e"], "mixed_precision": r["mixed"]}
+    # The FP64 path is bound by FP64 issue on this GPU (profiles/k_nd_jacobi_abl192_fp64.md): report the
+    # dominant kernel against the FMA peak measured live by ks_fma_peak as well.
+    fl = FP64_FLOPS_PER_BYTE.get(r["dominant"])
+    if fl and achieved:
+        line["fp64_roofline"] = {"kernel": r["dominant"], "achieved_gflops": achieved * fl, "peak_gflops": r["fp64_peak"],
+                                 "frac": achieved * fl / r["fp64_peak"], "peak_kind": "measured live (ks_fma_peak, FP64 FMA chains)",
+                                 "flops_per_unit": "about 40 FP64 flops per node per Jacobi sweep (24 B algorithmic)"}
     # whole-step algorithmic traffic: 8 * (125 + 20.86 * V-cycles) bytes per cell
     bstep = 8.0 * (125.0 + 20.86 * (r["mac"] + r["nodal"])) * r["cells"]
     line["step_roofline"] = {"algorithmic_bytes_per_step": bstep, "achieved_GBs": bstep / (r["ms"] / args.steps * 1e-3) / 1e9,

@@ -103,6 +103,11 @@ int ks_get_stream(ks_handle* h, void** stream);
 int ks_profile_kernels(ks_handle* h, const char* kernel);
 long long ks_profile_report(ks_handle* h, char* buf, long long len);
 
+/* Compute-roofline probe (no counterpart in the reference): FMA throughput
+ * in GFLOP/s of the current device for FP64 (fp64 = 1) or FP32 (fp64 = 0),
+ * measured with independent in-register FMA chains. */
+int ks_fma_peak(int fp64, double* gflops);
+
 /* Allocation-free tensor diffusion term (no counterpart in the reference).
  *
  * For callers that cannot call cudaMalloc where they need the viscous term:

@@ -30,7 +30,7 @@ SYMBOLS = ["ks_create", "ks_destroy", "ks_last_error", "ks_init_data", "ks_compu
            "ks_prepare_time_step", "ks_advance", "ks_apply_predictor", "ks_apply_corrector", "ks_apply_projection",
            "ks_evolve", "ks_step", "ks_field_layout", "ks_get_field", "ks_set_field", "ks_get_scalar",
            "ks_last_solver_stats", "ks_set_precision", "ks_synchronize", "ks_kernel_launches", "ks_get_stream",
-           "ks_profile_kernels", "ks_profile_report", "ks_divtau_noalloc"]
+           "ks_profile_kernels", "ks_profile_report", "ks_divtau_noalloc", "ks_fma_peak"]
 
 
 class KsError(RuntimeError):
@@ -92,9 +92,20 @@ def load_library(path=None):
     lib.ks_profile_report.argtypes = [vp, ctypes.c_char_p, ctypes.c_longlong]
     lib.ks_profile_report.restype = ctypes.c_longlong
     lib.ks_divtau_noalloc.argtypes = [vp, vp, vp, vp, ip, ip, ip, dp, dp, dp, ip, ip, vp]
+    lib.ks_fma_peak.argtypes = [ip, ctypes.POINTER(dp)]
     if path is None:
         _LIB = lib
     return lib
+
+
+def fma_peak(fp64=True):
+    """Measured FMA throughput of the current device, GFLOP/s."""
+    lib = load_library()
+    v = ctypes.c_double()
+    rc = lib.ks_fma_peak(int(bool(fp64)), ctypes.byref(v))
+    if rc != 0:
+        raise KsError(rc, "ks_fma_peak failed")
+    return v.value
 
 
 class Incflo:
