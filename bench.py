@@ -47,6 +47,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision form of the same workload")
+    p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost / gradient check (128x128x64, 3 disks)")
     p.add_argument("--profile-all", action="store_true", help="print the per-kernel breakdown to stderr")
     p.add_argument("--size", default="256,256,128")
     p.add_argument("--cpu-worker", default="", help=argparse.SUPPRESS)
@@ -271,8 +272,100 @@ def our_arm(args, rank, world, local_rank):
                  "gp_rel_err_linf": float(abs(gpm - rg).max() / abs(rg).max()),
                  "mac_residual_rel_max": max(mres), "nodal_residual_rel_max": max(nres),
                  "note": "FP32 advection and multigrid cycles, FP64 residuals / defect correction / RHS / velocity update"}
+    adj = None if args.no_adjoint else adjoint_bench(args, torch, ks, decks)
     return dict(value=value, ms=ms_max, cells=cells, launches=launches, dominant=dominant, dom=dom, clocks=clk, e2e=e2e, fp64_peak=fp64_peak,
-                mac=statistics.mean(mac_it), nodal=statistics.mean(nod_it), size=(nx, ny, nz), mixed=mixed)
+                mac=statistics.mean(mac_it), nodal=statistics.mean(nod_it), size=(nx, ny, nz), mixed=mixed, adjoint=adj)
+
+
+def adjoint_bench(args, torch, ks, decks):
+    """Reverse mode on the adjoint-check workload: 128 x 128 x 64 periodic box,
+    3 uniform-Ct disks, J = wake-box kinetic energy after 40 steps.  Device
+    time (CUDA events on the handle's stream) of forward steps, of reverse
+    steps (each recomputes its forward step in FP64) and of a whole
+    checkpointed run; dJ/dCt against central finite differences."""
+    nsteps, slots = 40, 6  # binomial schedule; the store-every-state run uses nsteps slots
+    deck, lo, hi, cts = decks.adjoint_c3()
+    sim = ks.Incflo(deck)
+    sim.InitData()
+    sim.set_objective_box(lo, hi)
+    x0 = {f: sim.get_field(f) for f in ("velocity", "gp", "p")}
+    ct = [float(c) for c in cts]
+    stream = torch.cuda.ExternalStream(sim.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def restore():
+        for f, v in x0.items():
+            sim.set_field(f, v)
+        sim.set_disk_ct(ct)
+
+    def timed(fn, k):
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(k):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    for _ in range(args.warmup):
+        sim.step()
+    fwd = timed(sim.step, args.steps) / args.steps
+    sim.adjoint_reset()
+    sim.objective(seed=True)
+    for _ in range(args.warmup):
+        sim.adjoint_step()
+    rev = timed(sim.adjoint_step, args.steps) / args.steps
+    restore()
+    J = [None]
+
+    def run():
+        J[0] = sim.adjoint_run(nsteps, slots)
+
+    run_ms = timed(run, 1)
+    g = sim.ct_gradient()
+    added = sim.scalar("adj_forward_steps")
+    restore()
+    J_all = [None]
+
+    def run_all():
+        J_all[0] = sim.adjoint_run(nsteps, nsteps)
+
+    all_ms = timed(run_all, 1)
+    g_all = sim.ct_gradient()
+    added_all = sim.scalar("adj_forward_steps")
+    free, total = torch.cuda.mem_get_info()
+
+    def fJ(c):
+        for f, v in x0.items():
+            sim.set_field(f, v)
+        sim.set_disk_ct(c)
+        for _ in range(nsteps):
+            sim.step()
+        return sim.objective()
+
+    fd = {}
+    for h in (1e-8, 1e-6):
+        est = []
+        for k in range(len(ct)):
+            cp = list(ct)
+            cm = list(ct)
+            cp[k] += h
+            cm[k] -= h
+            est.append((fJ(cp) - fJ(cm)) / (2 * h))
+        fd["%g" % h] = max(abs(a - b) for a, b in zip(est, g)) / max(abs(x) for x in g)
+    return {"workload": "128x128x64 periodic, 8 m/s + 0.2 m/s noise, 3 UniformCt disks (D = 16 cells), laminar, dt = 1 s, "
+                        "J = mean 0.5|u|^2 in the wake box after %d steps" % nsteps,
+            "forward_ms_per_step": fwd, "adjoint_ms_per_step": rev, "adjoint_over_forward_step": rev / fwd,
+            "checkpointed_run": {"steps": nsteps, "snapshots": slots, "forward_steps_added": added, "ms": run_ms,
+                                 "over_forward_run": run_ms / (nsteps * fwd)},
+            "store_all_run": {"steps": nsteps, "snapshots": nsteps, "forward_steps_added": added_all, "ms": all_ms,
+                              "over_forward_run": all_ms / (nsteps * fwd),
+                              "grad_rel_diff_vs_checkpointed": max(abs(a - b) for a, b in zip(g, g_all)) / max(abs(x) for x in g)},
+            "J": J[0], "dJ_dCt": list(g), "Ct": ct,
+            "fd_rel_err": {"h=1e-8": fd["1e-08"], "h=1e-6": fd["1e-06"],
+                           "note": "jumps of the PPM small_vel trace switch / Riemann selection lie within 1e-7 of this "
+                                   "point; h = 1e-8 resolves the smooth piece"},
+            "device_mem_in_use_GB": (total - free) / 1e9}
 
 
 def main():
@@ -324,7 +417,8 @@ def main():
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic, "peak_kind": peak_kind,
                          "launches": n_l, "avg_launch_us": 1e3 * ms_l / n_l if n_l else None,
                          "algorithmic_bytes_per_launch": by_l / n_l if n_l else None},
-            "gpu_launches": r["launches"], "clocks": r["clocks"], "e2e": r["e2e"], "mixed_precision": r["mixed"]}
+            "gpu_launches": r["launches"], "clocks": r["clocks"], "e2e": r["e2e"], "mixed_precision": r["mixed"],
+            "adjoint": r["adjoint"]}
     # The FP64 path is bound by FP64 issue on this GPU (profiles/k_nd_jacobi_abl192_fp64.md): report the
     # dominant kernel against the FMA peak measured live by ks_fma_peak as well.
     fl = FP64_FLOPS_PER_BYTE.get(r["dominant"])

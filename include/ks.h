@@ -93,6 +93,46 @@ int ks_set_precision(ks_handle* h, int precision);
 int ks_synchronize(ks_handle* h);
 int ks_kernel_launches(const ks_handle* h, long long* count);
 
+/* Reverse mode of the advance (no counterpart in the reference: the adjoint
+ * entry points ks_adjoint_step / ks_set_objective_box / ks_get_ct_gradient
+ * extend the operator surface of src/incflo.H:51-233).
+ *
+ * Differentiable configuration: triply periodic, turbulence.model = laminar,
+ * time.fixed_dt > 0, momentum sources among ActuatorForcing, BodyForce and
+ * GeostrophicForcing, UniformCtDisk actuators with one thrust_coeff value
+ * each.  Other decks return KS_ERR_UNSUPPORTED from every call below.
+ * The objective J is the mean of 0.5 |u|^2 over the cells whose centres lie in
+ * the box [lo, hi] (physical units).  The adjoint state is held in the fields
+ * "velocity_adjoint" and "gp_adjoint" (layouts of "velocity" and "gp"; get and
+ * set them with ks_get_field / ks_set_field).  Limiter, Riemann and upwind
+ * branches are frozen at the forward state; projections are reversed with
+ * solves of the same self-adjoint operators at the forward tolerances. */
+int ks_set_objective_box(ks_handle* h, const double lo[3], const double hi[3]);
+/* J at the current state; seed != 0 also sets the adjoint fields to dJ/du
+ * and 0 (the terminal condition of a reverse sweep). */
+int ks_objective(ks_handle* h, int seed, double* J);
+/* One reverse step at the current state x^n = (velocity, gp): the adjoint
+ * fields go from the adjoint of x^{n+1} to that of x^n (the step is
+ * recomputed from x^n in FP64) and dJ/dct accumulates; the forward state and
+ * the clock are left at x^n. */
+int ks_adjoint_step(ks_handle* h);
+/* nsteps forward steps from the current state with binomial checkpointing in
+ * device memory (`snapshots` slots of (velocity, gp), the first holding the
+ * initial state; snapshots >= nsteps stores every state), J at the final
+ * state, and the reverse sweep.  On return: *J set, the forward state and the
+ * clock are those after nsteps steps, the adjoint fields hold dJ/d(velocity,
+ * gp) of the initial state, and ks_get_ct_gradient returns dJ/dct. */
+int ks_adjoint_run(ks_handle* h, int nsteps, int snapshots, double* J);
+/* Accumulated dJ/dct per disk (deck order, n = number of disks). */
+int ks_get_ct_gradient(ks_handle* h, double* grad, int n);
+/* Zero the adjoint fields and the accumulated dJ/dct. */
+int ks_adjoint_reset(ks_handle* h);
+/* Thrust coefficient of every disk (deck order, n = number of disks). */
+int ks_set_disk_ct(ks_handle* h, const double* ct, int n);
+/* Forward steps beyond the reverse steps' own that a binomial schedule needs
+ * to reverse nsteps steps with `snapshots` slots (host only, no device). */
+int ks_checkpoint_cost(int nsteps, int snapshots, long long* forward_steps);
+
 /* Instrumentation (no counterpart in the reference): the CUDA stream all
  * kernels of the handle run on, and CUDA-event timing of kernels whose name
  * matches `kernel` ("*" = every kernel, NULL or "" = off).  The report is

@@ -7,253 +7,9 @@
 // pass is a hand-written kernel in ks_kernels.cu, ks_godunov.cu or ks_mg.cu;
 // the host only computes scalars (dt, u_tau, disk forces) and launches.
 #include <cuda_runtime.h>
-
-#include <algorithm>
-#include <array>
-#include <cmath>
-#include <cstdio>
-#include <cstring>
-#include <map>
-#include <memory>
-#include <sstream>
-#include <stdexcept>
-#include <string>
-#include <vector>
-
-#include "../../include/ks.h"
-#include "ks_launch.hpp"
+#include "ks_sim.hpp"
 
 namespace ks {
-
-struct KsError : std::runtime_error {
-    int code;
-    KsError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
-};
-
-static void ck(cudaError_t e, const char* what) {
-    if (e != cudaSuccess) {
-        const int code = (e == cudaErrorMemoryAllocation) ? KS_ERR_OOM : KS_ERR_CUDA;
-        throw KsError(code, std::string(what) + ": " + cudaGetErrorString(e));
-    }
-}
-
-static std::string lc(std::string s) {
-    for (auto& c : s) c = (char)std::tolower((unsigned char)c);
-    return s;
-}
-
-// ---------------------------------------------------------------- deck
-// ParmParse-style input: "prefix.key = v1 v2 ...", '#' starts a comment.
-class Deck {
-   public:
-    explicit Deck(const std::string& text) {
-        std::istringstream in(text);
-        std::string ln;
-        while (std::getline(in, ln)) {
-            const auto hash = ln.find('#');
-            if (hash != std::string::npos) ln.resize(hash);
-            const auto eq = ln.find('=');
-            if (eq == std::string::npos) continue;
-            std::string k = trim(ln.substr(0, eq));
-            std::istringstream vs(ln.substr(eq + 1));
-            std::vector<std::string> v;
-            for (std::string w; vs >> w;) {
-                if (w.size() >= 2 && (w[0] == '"' || w[0] == '\'')) w = w.substr(1, w.size() - 2);
-                v.push_back(w);
-            }
-            if (!k.empty()) kv_[k] = v;
-        }
-    }
-    bool has(const std::string& k) const { return kv_.count(k) > 0; }
-    std::vector<std::string> strs(const std::string& k) const {
-        auto it = kv_.find(k);
-        return it == kv_.end() ? std::vector<std::string>{} : it->second;
-    }
-    std::string str(const std::string& k, const std::string& def) const {
-        auto v = strs(k);
-        return v.empty() ? def : v[0];
-    }
-    double num(const std::string& k, double def) const {
-        auto v = strs(k);
-        return v.empty() ? def : std::stod(v[0]);
-    }
-    int flag(const std::string& k, int def) const {
-        auto v = strs(k);
-        if (v.empty()) return def;
-        if (v[0] == "true") return 1;
-        if (v[0] == "false") return 0;
-        return std::stoi(v[0]);
-    }
-    std::vector<double> nums(const std::string& k) const {
-        auto it = kv_.find(k);
-        if (it == kv_.end()) throw KsError(KS_ERR_DECK, "missing deck key " + k);
-        std::vector<double> r;
-        for (auto& s : it->second) r.push_back(std::stod(s));
-        return r;
-    }
-
-   private:
-    static std::string trim(std::string s) {
-        const auto a = s.find_first_not_of(" \t\r");
-        if (a == std::string::npos) return "";
-        const auto b = s.find_last_not_of(" \t\r");
-        return s.substr(a, b - a + 1);
-    }
-    std::map<std::string, std::vector<std::string>> kv_;
-};
-
-// ---------------------------------------------------------------- SimTime
-// src/core/SimTime.cpp:11-324 semantics for the keys on this path.
-struct Clock {
-    double cur = 0, next = 0, dt[3] = {-1, -1, -1};
-    double cfl = 1, fixed_dt = -1, init_dt = -1, max_dt = -1, min_dt = -1, shrink = 0.1, growth = 0.1, stop = -1;
-    int max_step = -1, step = 0;
-    bool adaptive = false, init = true, force_cfl = true;
-    double cur_cfl = 0, conv_cfl = 0, diff_cfl = 0, src_cfl = 0;
-
-    void set_cfl(double conv, double diff, double src) {
-        const double eps = 2.220446049250313e-16;
-        const double cd = conv + diff;
-        const double unit = cd + std::sqrt(cd * cd + 4.0 * src);
-        bool use_init = false;
-        if (adaptive && !init && unit < eps) {
-            if (cur < eps && init_dt > 0) use_init = true;
-            else throw KsError(KS_ERR_NONFINITE, "CFL is below machine epsilon and the time step is adaptive");
-        }
-        double d = use_init ? init_dt : 2.0 * cfl / std::max(unit, eps);
-        if (init) d *= shrink;
-        if (dt[0] > 0 && adaptive) d = std::min(d, (1.0 + growth) * dt[0]);
-        if (adaptive) {
-            if (max_dt > 0) d = std::min(d, max_dt);
-            if (min_dt > 0 && d < min_dt) throw KsError(KS_ERR_NONFINITE, "adaptive dt fell below time.min_dt");
-            if (stop > 0 && cur + d > stop) d = stop - cur;
-            if (init && init_dt > 0) d = std::min(d, init_dt);
-            dt[0] = d;
-        } else {
-            dt[0] = fixed_dt;
-        }
-        cur_cfl = 0.5 * unit * dt[0];
-        conv_cfl = conv * dt[0];
-        diff_cfl = diff * dt[0];
-        src_cfl = std::sqrt(src) * dt[0];
-    }
-    bool keep_going() const {
-        if (max_step >= 0 && step >= max_step) return false;
-        if (stop > 0 && next >= stop - 2.220446049250313e-12) return false;
-        return true;
-    }
-    bool new_step() {
-        const bool go = keep_going();
-        init = false;
-        if (go) {
-            dt[2] = dt[1];
-            dt[1] = dt[0];
-            ++step;
-            cur = next;
-        }
-        return go;
-    }
-};
-
-struct Disk {
-    double center[3], normal[3], cvec[3];
-    double D, eps, to_sample, dr;
-    std::vector<double> ct, ws;
-    int nr, nt;
-    bool about_center;
-    double ct_now = 0, uinf2 = 0, ref[3] = {0, 0, 0};
-};
-
-struct MGParams {
-    double rtol = 1.0e5 * 2.220446049250313e-16, atol = 1.0e2 * 2.220446049250313e-16;
-    int maxiter = 200, nu1 = 2, nu2 = 2, bottom = 100;
-    double omega = 0.9;
-};
-
-template <typename T>
-struct DevBuf {
-    T* p = nullptr;
-    size_t n = 0;
-    void alloc(size_t count) {
-        n = count;
-        ck(cudaMalloc(&p, std::max<size_t>(1, count) * sizeof(T)), "cudaMalloc");
-        ck(cudaMemset(p, 0, std::max<size_t>(1, count) * sizeof(T)), "cudaMemset");
-    }
-    ~DevBuf() {
-        if (p) cudaFree(p);
-    }
-};
-
-// ---------------------------------------------------------------- simulation
-class Sim {
-   public:
-    explicit Sim(const std::string& text);
-    ~Sim();
-
-    void init_data();
-    void compute_dt();
-    void pre_advance();
-    void prepare_time_step();
-    void apply_predictor(bool incremental);
-    void apply_projection(double time, double scaling, bool incremental);
-    int step();
-
-    double scalar(const std::string& name);
-    void layout(const std::string& name, ks_layout& L);
-    void get(const std::string& name, void* dst, int where);
-    void set(const std::string& name, const void* src, int where);
-    void sync() { ck(cudaStreamSynchronize(ctx_.stream), "stream synchronize"); }
-
-    Ctx ctx_;
-    Grid g_{};
-    Clock t_;
-    int mac_it_ = 0, nod_it_ = 0;
-    int mixed_ = 0;  // 1: FP32 advection and multigrid cycles with FP64 defect correction
-    double mac_r0_ = 0, mac_r_ = 0, nod_r0_ = 0, nod_r_ = 0;
-    std::string err_;
-
-   private:
-    void setup(const Deck& D);
-    void alloc();
-    void init_fields(const Deck& D);
-    void abl_update();
-    void actuator_update();
-    void mac_project();
-    double reduce(int np, int ncomp, int op_max, double* host);
-    template <typename T>
-    void cc_vcycle(std::vector<CCLevelT<T>>& Ls, size_t l, double beta);
-    template <typename T>
-    void nd_vcycle(std::vector<NDLevelT<T>>& Ls, size_t l, double sigma, int skip_sweeps = 0);
-   public:
-    void set_mixed(int on);
-
-   private:
-    double* field(const std::string& name, int& ncomp, int& kind);
-
-    double plo_[3], phi_[3];
-    double rho_ = 1, mu_ = 0;
-    Scalars S_{};
-    bool wallmodel_ = false;
-    int shear_ = 0;
-    double kappa_ = 0.41, z0_ = 0.1, zref_ = 0, utau_ = 0, um_[2] = {0, 0}, vmag_ = 0;
-    std::vector<Disk> disks_;
-    MGParams mac_, nod_;
-    int initial_proj_ = 1, initial_iters_ = 3;
-
-    DevBuf<double> vel_, vel_old_, vel_tmp_, gp_, p_, src_, forces_, mueff_, divtau_, conv_, act_, wg_;
-    DevBuf<double> umac_[3];
-    DevBuf<double> gbuf_;
-    GodunovBufs gb_{};
-    std::vector<CCLevelDev> cc_;
-    std::vector<NDLevelDev> nd_;
-    std::vector<CCLevelT<float>> cc32_;  // mixed precision: FP32 cycle levels
-    std::vector<NDLevelT<float>> nd32_;
-    DevBuf<double> mgbuf_;
-    DevBuf<float> mgbuf32_;
-    DevBuf<double> parts_, red_;
-    DevBuf<double> pts_, samp_;
-    double* hred_ = nullptr;  // pinned
-};
 
 Sim::Sim(const std::string& text) {
     Deck D(text);
@@ -619,6 +375,43 @@ static void rot(const double* a, double ang, const double* v, double* o) {
     for (int m = 0; m < 3; ++m) o[m] = v[m] * c + x[m] * s + a[m] * dd * (1 - c);
 }
 
+// Sampling points (disk_ops.cpp:378-412) and force ring points
+// (disk_spreading.H:45-105) of one disk, x/y/z per point, ordered radius-major.
+void Sim::disk_points(const Disk& d, std::vector<double>& sample, std::vector<double>& ring) const {
+    const double pi = 3.14159265358979323846;
+    const double* ax = d.normal;
+    double rv[3] = {-ax[1], ax[0], 0.0};
+    const double rm = std::sqrt(rv[0] * rv[0] + rv[1] * rv[1]);
+    rv[0] /= rm;
+    rv[1] /= rm;
+    const double drs = 0.5 * d.D / d.nr;
+    const double shift = d.nr == 1 ? 0.0 : 0.5;
+    const int np = d.nr * d.nt;
+    sample.assign(3 * (size_t)np, 0.0);
+    for (int ir = 0; ir < d.nr; ++ir)
+        for (int it = 0; it < d.nt; ++it) {
+            double r[3];
+            rot(ax, 2 * pi / d.nt * it, rv, r);
+            for (int m = 0; m < 3; ++m) sample[3 * (ir * d.nt + it) + m] = d.center[m] + d.to_sample * d.D * ax[m] + drs * (ir + shift) * r[m];
+        }
+    ring.assign(3 * (size_t)np, 0.0);
+    for (int ip = 0; ip < d.nr; ++ip) {
+        double pos[3];
+        for (int m = 0; m < 3; ++m) pos[m] = d.center[m] + (ip + 0.5) * d.dr * d.cvec[m];
+        for (int it = 0; it < d.nt; ++it) {
+            const double ang = 2 * pi / d.nt * it;
+            double* o = &ring[3 * (ip * d.nt + it)];
+            if (d.about_center) {
+                const double rel[3] = {pos[0] - d.center[0], pos[1] - d.center[1], pos[2] - d.center[2]};
+                rot(ax, ang, rel, o);
+                for (int m = 0; m < 3; ++m) o[m] += d.center[m];
+            } else {
+                rot(ax, ang, pos, o);  // the reference rotates the absolute position (disk_spreading.H:85-86)
+            }
+        }
+    }
+}
+
 void Sim::actuator_update() {
     if (!S_.act) return;
     const double pi = 3.14159265358979323846;
@@ -626,21 +419,9 @@ void Sim::actuator_update() {
     for (auto& d : disks_) {
         // sample points on the sampling disk (disk_ops.cpp:378-412)
         const double* ax = d.normal;
-        double rv[3] = {-ax[1], ax[0], 0.0};
-        const double rm = std::sqrt(rv[0] * rv[0] + rv[1] * rv[1]);
-        rv[0] /= rm;
-        rv[1] /= rm;
-        const double drs = 0.5 * d.D / d.nr;
-        const double shift = d.nr == 1 ? 0.0 : 0.5;
         const int np = d.nr * d.nt;
-        std::vector<double> hp(3 * (size_t)np);
-        for (int ir = 0; ir < d.nr; ++ir)
-            for (int it = 0; it < d.nt; ++it) {
-                double r[3];
-                rot(ax, 2 * pi / d.nt * it, rv, r);
-                for (int m = 0; m < 3; ++m)
-                    hp[3 * (ir * d.nt + it) + m] = d.center[m] + d.to_sample * d.D * ax[m] + drs * (ir + shift) * r[m];
-            }
+        std::vector<double> hp, rpos;
+        disk_points(d, hp, rpos);
         for (int p = 0; p < np; ++p) {
             const double hh[3] = {g_.dx, g_.dy, g_.dz};
             const int nn[3] = {g_.nx, g_.ny, g_.nz};
@@ -678,18 +459,8 @@ void Sim::actuator_update() {
         for (int ip = 0; ip < d.nr; ++ip) {
             const double r = (ip + 0.5) * d.dr, rp = r + 0.5 * d.dr, rmn = r - 0.5 * d.dr;
             const double f = aero * pi * (rp * rp - rmn * rmn);
-            double pos[3];
-            for (int m = 0; m < 3; ++m) pos[m] = d.center[m] + (ip + 0.5) * d.dr * d.cvec[m];
             for (int it = 0; it < d.nt; ++it) {
-                const double ang = 2 * pi / d.nt * it;
-                double o[3];
-                if (d.about_center) {
-                    const double rel[3] = {pos[0] - d.center[0], pos[1] - d.center[1], pos[2] - d.center[2]};
-                    rot(ax, ang, rel, o);
-                    for (int m = 0; m < 3; ++m) o[m] += d.center[m];
-                } else {
-                    rot(ax, ang, pos, o);  // the reference rotates the absolute position (disk_spreading.H:85-86)
-                }
+                const double* o = &rpos[3 * (ip * d.nt + it)];
                 for (int m = 0; m < 3; ++m) {
                     ring.push_back(o[m]);
                     bmin[m] = std::min(bmin[m], o[m]);
@@ -828,18 +599,24 @@ void Sim::nd_vcycle(std::vector<NDLevelT<T>>& Ls, size_t l, double sigma, int sk
     }
 }
 
-void Sim::apply_projection(double time, double scaling, bool incremental) {
-    const bool small_dt = (time > 0.0 && t_.dt[0] < 0.1 * t_.dt[1]);
-    const bool sub_old = small_dt || incremental;
-    launch_proj_pre(ctx_, g_, vel_.p, vel_old_.p, gp_.p, scaling, rho_, incremental ? 0 : 1, sub_old ? 1 : 0);
+// Nodal divergence of a cell field into the finest level's right-hand side,
+// made solvable (weighted mean removed); the initial guess is zero.
+void Sim::nd_rhs(const double* cell_field) {
     NDLevelDev& L = nd_[0];
     const long long M = (long long)L.nx * L.ny * L.nz;
     int np = 0;
-    launch_nodal_rhs(ctx_, g_, vel_.p, L.rhs, parts_.p, &np);
+    launch_nodal_rhs(ctx_, g_, cell_field, L.rhs, parts_.p, &np);
     launch_reduce(ctx_, parts_.p, np, 2, 0, red_.p);
     launch_sub_ratio(ctx_, L.rhs, M, red_.p, 0.0);
     launch_fill(ctx_, L.phi, 0.0, M);
-    const double sigma = scaling / rho_;
+}
+
+// Solve sigma A phi = rhs on the finest nodal level to the relative /
+// absolute tolerance of nodal_proj (solution in nd_[0].phi).
+void Sim::nd_solve(double sigma) {
+    NDLevelDev& L = nd_[0];
+    const long long M = (long long)L.nx * L.ny * L.nz;
+    int np = 0;
     for (auto& Lv : nd_) Lv.inv_diag = 1.0 / (sigma * Lv.W[13]);
     for (size_t l = 0; l < nd32_.size(); ++l) nd32_[l].inv_diag = (float)nd_[l].inv_diag;
     int it = 0;
@@ -880,7 +657,16 @@ void Sim::apply_projection(double time, double scaling, bool incremental) {
     }
     nod_it_ = it;
     nod_r_ = rn;
-    launch_nodal_post(ctx_, g_, L.phi, vel_.p, vel_old_.p, gp_.p, p_.p, sigma, sub_old ? 1 : 0, incremental ? 1 : 0);
+}
+
+void Sim::apply_projection(double time, double scaling, bool incremental) {
+    const bool small_dt = (time > 0.0 && t_.dt[0] < 0.1 * t_.dt[1]);
+    const bool sub_old = small_dt || incremental;
+    launch_proj_pre(ctx_, g_, vel_.p, vel_old_.p, gp_.p, scaling, rho_, incremental ? 0 : 1, sub_old ? 1 : 0);
+    nd_rhs(vel_.p);
+    const double sigma = scaling / rho_;
+    nd_solve(sigma);
+    launch_nodal_post(ctx_, g_, nd_[0].phi, vel_.p, vel_old_.p, gp_.p, p_.p, sigma, sub_old ? 1 : 0, incremental ? 1 : 0);
 }
 
 // ---------------------------------------------------------------- ApplyPredictor
@@ -952,6 +738,10 @@ double* Sim::field(const std::string& name, int& nc, int& kind) {
     if (name == "forces") return forces_.p;
     if (name == "diff_term") return divtau_.p;
     if (name == "conv_term") return conv_.p;
+    if (name == "velocity_adjoint" || name == "gp_adjoint") {
+        adj_alloc();
+        return name == "velocity_adjoint" ? adj_->ub.p : adj_->gpb.p;
+    }
     if (name == "actuator_src_term") { if (!S_.act) throw KsError(KS_ERR_ARG, "no actuator source"); return act_.p; }
     nc = 1;
     if (name == "velocity_mueff") return mueff_.p;
@@ -1041,6 +831,8 @@ double Sim::scalar(const std::string& n) {
         launch_ke(ctx_, g_, vel_.p, rho_, parts_.p, &np);
         return reduce(np, 1, 0, nullptr) / (double)g_.N;
     }
+    if (n == "ndisks") return (double)disks_.size();
+    if (n.rfind("adj_", 0) == 0 || n == "objective") return adjoint_stat(n);
     if (n.rfind("disk_ct:", 0) == 0) return disks_.at(std::stoul(n.substr(8))).ct_now;
     if (n.rfind("disk_uinf2:", 0) == 0) return disks_.at(std::stoul(n.substr(11))).uinf2;
     throw KsError(KS_ERR_ARG, "unknown scalar " + n);
@@ -1244,6 +1036,56 @@ long long ks_profile_report(ks_handle* h, char* buf, long long len) {
         s.ctx_.acc.clear();
     }
     return need;
+}
+
+int ks_set_objective_box(ks_handle* h, const double lo[3], const double hi[3]) {
+    if (!lo || !hi) return KS_ERR_ARG;
+    return guarded(h, [&](ks::Sim& s) { s.set_objective_box(lo, hi); return 0; });
+}
+
+int ks_objective(ks_handle* h, int seed, double* J) {
+    return guarded(h, [&](ks::Sim& s) {
+        const double v = s.objective(seed != 0);
+        if (J) *J = v;
+        return 0;
+    });
+}
+
+int ks_adjoint_step(ks_handle* h) { return guarded(h, [](ks::Sim& s) { s.adjoint_step(); return 0; }); }
+
+int ks_adjoint_run(ks_handle* h, int nsteps, int snapshots, double* J) {
+    return guarded(h, [&](ks::Sim& s) {
+        const double v = s.adjoint_run(nsteps, snapshots);
+        if (J) *J = v;
+        return 0;
+    });
+}
+
+int ks_get_ct_gradient(ks_handle* h, double* grad, int n) {
+    if (!grad) return KS_ERR_ARG;
+    return guarded(h, [&](ks::Sim& s) {
+        if (n != s.ndisks()) throw ks::KsError(KS_ERR_ARG, "ks_get_ct_gradient: n differs from the number of disks");
+        const auto& g = s.ct_gradient();
+        for (int m = 0; m < n; ++m) grad[m] = m < (int)g.size() ? g[m] : 0.0;
+        return 0;
+    });
+}
+
+int ks_adjoint_reset(ks_handle* h) { return guarded(h, [](ks::Sim& s) { s.adjoint_reset(); return 0; }); }
+
+int ks_set_disk_ct(ks_handle* h, const double* ct, int n) {
+    if (!ct) return KS_ERR_ARG;
+    return guarded(h, [&](ks::Sim& s) { s.set_disk_ct(ct, n); return 0; });
+}
+
+int ks_checkpoint_cost(int nsteps, int snapshots, long long* forward_steps) {
+    if (!forward_steps || nsteps < 1 || snapshots < 1 || nsteps > 100000) return KS_ERR_ARG;
+    try {
+        *forward_steps = ks::checkpoint_cost(nsteps, snapshots);
+    } catch (const std::exception&) {
+        return KS_ERR_OOM;
+    }
+    return KS_OK;
 }
 
 int ks_kernel_launches(const ks_handle* h, long long* count) {

@@ -146,6 +146,39 @@ void launch_premac(Ctx& c, const Grid& g, const double* vel_old, const double* f
 void launch_advection(Ctx& c, const Grid& g, const double* vel_old, const double* forces, const double* mac[3], double dt, double rho,
                       GodunovBufs& B, double* conv, int fp32);
 
+// ---- reverse mode of the Godunov passes (ks_adjoint.cu), FP64, periodic.
+// Adjoints of the GodunovBufs arrays (same shapes) plus those of the MAC
+// velocities, of the cell velocity (u: the input of both passes, 3N) and of
+// the forces (3N).  Kernels accumulate into these arrays.
+struct AdjBufs {
+    double* ad[3];
+    double* edge[3][3];
+    double* lo[3][3];
+    double* hi[3][3];
+    double* tedge[3][3];
+    double* tr[3][3][3];
+    double* flux[3][3];
+    double* umac[3];
+    double* u;
+    double* forces;
+};
+void launch_adj_edges(Ctx& c, const Grid& g, int d, const double* u, double* const Eb[3], double* ub);
+void launch_adj_faces(Ctx& c, const Grid& g, int d, int mode, const double* u, const GodunovBufs& B, const AdjBufs& A, double dt, double rho,
+                      const double* umac_d);
+void launch_adj_pm_trans(Ctx& c, const Grid& g, int a, int b, int n, double dt, const GodunovBufs& B, const AdjBufs& A);
+void launch_adj_pm_final(Ctx& c, const Grid& g, int d, double dt, const GodunovBufs& B, const double* forces, const AdjBufs& A);
+void launch_adj_adv_trans(Ctx& c, const Grid& g, int a, int b, const double* u, double rho, double dt, const double* const mac[3],
+                          const GodunovBufs& B, const AdjBufs& A);
+void launch_adj_adv_flux(Ctx& c, const Grid& g, int d, const double* u, const double* forces, double rho, double dt, const double* const mac[3],
+                         const GodunovBufs& B, const AdjBufs& A);
+void launch_adj_div(Ctx& c, const Grid& g, const double* convb, const AdjBufs& A);
+void launch_adj_nodal_post(Ctx& c, const Grid& g, const double* psi, const double* ub, double* out);
+void launch_axpby(Ctx& c, long long n, double a, const double* x, double b, const double* y, double* out);
+void launch_objective(Ctx& c, const Grid& g, const double* u, const int lo[3], const int hi[3], double invM, double* ub, double* parts, int* np);
+void launch_act_adj_dot(Ctx& c, const Grid& g, const double* actb, const double* pts, int npts, const double ax[3], double eps, const double plo[3],
+                        const int lo[3], const int hi[3], double* parts, int* np);
+void launch_act_sample_adj(Ctx& c, const Grid& g, const double* pts, const double* wb, int npts, const double plo[3], double* ub);
+
 // ---- multigrid (ks_mg.cu); T = double (FP64 path) or float (cycles of the
 // mixed-precision defect correction)
 template <typename T>

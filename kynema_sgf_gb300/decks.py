@@ -96,7 +96,7 @@ Actuator.UniformCtDisk.epsilon = {eps_cells * dx}
 Actuator.UniformCtDisk.num_points_r = {nr}
 Actuator.UniformCtDisk.num_points_t = {nt}
 Actuator.UniformCtDisk.spreading_type = UniformGaussian
-Actuator.UniformCtDisk.disk_normal = 1.0 0.0 0.0
+Actuator.UniformCtDisk.disk_normal = -1.0 0.0 0.0
 Actuator.UniformCtDisk.ks_spread_about_center = {about_center}
 {body}
 incflo.use_godunov = 1
@@ -107,3 +107,65 @@ time.max_step = {steps}
 ks_init.noise_amplitude = 0.2
 ks_init.noise_seed = {seed}
 """
+
+
+def adjoint_c3(nx=128, ny=128, nz=64, dcells=16, seed=7, ct_seed=11, n_disks=3, nr=5, nt=20, eps_cells=2.0,
+               dt=1.0, viscosity=1.0, about_center=1, cts=None, crossflow=(0.0, 0.0), noise=0.2):
+    """Differentiable configuration (adjoint check): triply periodic box of
+    8 x 8 x 4 rotor diameters at 10 m cells, uniform 8 m/s inflow plus
+    uniform +-0.2 m/s noise, laminar viscosity, fixed dt (CFL about 0.82) and
+    ``n_disks`` uniform-Ct disks of ``dcells`` cells in a row along x at
+    1, 2, 3 ... diameters facing the flow (normal -x, the force opposes the
+    flow), sampling 0.5 D upstream; Ct drawn from U(0.6, 0.9) with numpy's
+    default_rng(ct_seed) unless ``cts`` is given.  ``crossflow`` adds a
+    uniform (v, w) to the inflow.  Returns
+    (deck, box_lo, box_hi, cts), the box being the wake region from the last
+    disk to 5 D downstream, one diameter either side of the axis."""
+    import numpy as np
+
+    dx = 10.0
+    D = dcells * dx
+    if cts is None:
+        cts = np.random.default_rng(ct_seed).uniform(0.6, 0.9, n_disks)
+    cts = [float(c) for c in cts]
+    yc, zc = 0.5 * ny * dx, 0.5 * nz * dx
+    labels = " ".join("T%d" % i for i in range(len(cts)))
+    lines = []
+    for i, ct in enumerate(cts):
+        lines.append(f"Actuator.T{i}.disk_center = {(1 + i) * D} {yc} {zc}")
+        lines.append(f"Actuator.T{i}.thrust_coeff = {ct!r}")
+    body = "\n".join(lines)
+    deck = f"""
+geometry.prob_lo = 0 0 0
+geometry.prob_hi = {nx * dx} {ny * dx} {nz * dx}
+geometry.is_periodic = 1 1 1
+amr.n_cell = {nx} {ny} {nz}
+incflo.physics = FreeStream
+incflo.velocity = 8.0 {crossflow[0]} {crossflow[1]}
+incflo.density = 1.0
+transport.viscosity = {viscosity}
+turbulence.model = Laminar
+ICNS.source_terms = ActuatorForcing
+Actuator.labels = {labels}
+Actuator.type = UniformCtDisk
+Actuator.UniformCtDisk.rotor_diameter = {D}
+Actuator.UniformCtDisk.epsilon = {eps_cells * dx}
+Actuator.UniformCtDisk.num_points_r = {nr}
+Actuator.UniformCtDisk.num_points_t = {nt}
+Actuator.UniformCtDisk.spreading_type = UniformGaussian
+Actuator.UniformCtDisk.disk_normal = -1.0 0.0 0.0
+Actuator.UniformCtDisk.diameters_to_sample = 0.5
+Actuator.UniformCtDisk.ks_spread_about_center = {about_center}
+{body}
+incflo.use_godunov = 1
+incflo.godunov_type = ppm
+incflo.diffusion_type = 0
+time.fixed_dt = {dt}
+time.max_step = 1000000
+ks_init.noise_amplitude = {noise}
+ks_init.noise_seed = {seed}
+"""
+    xl = len(cts) * D
+    lo = (xl, yc - D, zc - D)
+    hi = (min(xl + 5 * D, nx * dx), yc + D, zc + D)
+    return deck, lo, hi, cts

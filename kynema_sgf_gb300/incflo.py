@@ -23,14 +23,16 @@ KS_DONE = 7
 KS_HOST, KS_DEVICE = 0, 1
 
 FIELDS = ["velocity", "velocity_old", "gp", "p", "src_term", "forces", "diff_term", "conv_term", "velocity_mueff",
-          "u_mac", "v_mac", "w_mac", "actuator_src_term"]
+          "u_mac", "v_mac", "w_mac", "actuator_src_term", "velocity_adjoint", "gp_adjoint"]
 
 # every symbol declared in include/ks.h
 SYMBOLS = ["ks_create", "ks_destroy", "ks_last_error", "ks_init_data", "ks_compute_dt", "ks_pre_advance",
            "ks_prepare_time_step", "ks_advance", "ks_apply_predictor", "ks_apply_corrector", "ks_apply_projection",
            "ks_evolve", "ks_step", "ks_field_layout", "ks_get_field", "ks_set_field", "ks_get_scalar",
            "ks_last_solver_stats", "ks_set_precision", "ks_synchronize", "ks_kernel_launches", "ks_get_stream",
-           "ks_profile_kernels", "ks_profile_report", "ks_divtau_noalloc", "ks_fma_peak"]
+           "ks_profile_kernels", "ks_profile_report", "ks_divtau_noalloc", "ks_fma_peak", "ks_set_objective_box",
+           "ks_objective", "ks_adjoint_step", "ks_adjoint_run", "ks_get_ct_gradient", "ks_adjoint_reset",
+           "ks_set_disk_ct", "ks_checkpoint_cost"]
 
 
 class KsError(RuntimeError):
@@ -93,6 +95,15 @@ def load_library(path=None):
     lib.ks_profile_report.restype = ctypes.c_longlong
     lib.ks_divtau_noalloc.argtypes = [vp, vp, vp, vp, ip, ip, ip, dp, dp, dp, ip, ip, vp]
     lib.ks_fma_peak.argtypes = [ip, ctypes.POINTER(dp)]
+    d3 = ctypes.POINTER(dp)
+    lib.ks_set_objective_box.argtypes = [vp, d3, d3]
+    lib.ks_objective.argtypes = [vp, ip, d3]
+    lib.ks_adjoint_step.argtypes = [vp]
+    lib.ks_adjoint_run.argtypes = [vp, ip, ip, d3]
+    lib.ks_get_ct_gradient.argtypes = [vp, d3, ip]
+    lib.ks_adjoint_reset.argtypes = [vp]
+    lib.ks_set_disk_ct.argtypes = [vp, d3, ip]
+    lib.ks_checkpoint_cost.argtypes = [ip, ip, ctypes.POINTER(ctypes.c_longlong)]
     if path is None:
         _LIB = lib
     return lib
@@ -105,6 +116,17 @@ def fma_peak(fp64=True):
     rc = lib.ks_fma_peak(int(bool(fp64)), ctypes.byref(v))
     if rc != 0:
         raise KsError(rc, "ks_fma_peak failed")
+    return v.value
+
+
+def checkpoint_cost(nsteps, snapshots):
+    """Forward steps a binomial schedule adds to reverse ``nsteps`` steps with
+    ``snapshots`` checkpoint slots (host-only computation)."""
+    lib = load_library()
+    v = ctypes.c_longlong()
+    rc = lib.ks_checkpoint_cost(int(nsteps), int(snapshots), ctypes.byref(v))
+    if rc != 0:
+        raise KsError(rc, "ks_checkpoint_cost failed")
     return v.value
 
 
@@ -242,3 +264,42 @@ class Incflo:
         c = ctypes.c_longlong()
         self._check(self._lib.ks_kernel_launches(self._h, ctypes.byref(c)))
         return c.value
+
+    # --- reverse mode
+    def set_objective_box(self, lo, hi):
+        """J = mean of 0.5 |u|^2 over the cells whose centres lie in [lo, hi]."""
+        a = (ctypes.c_double * 3)(*[float(x) for x in lo])
+        b = (ctypes.c_double * 3)(*[float(x) for x in hi])
+        self._check(self._lib.ks_set_objective_box(self._h, a, b))
+
+    def objective(self, seed=False):
+        J = ctypes.c_double()
+        self._check(self._lib.ks_objective(self._h, int(bool(seed)), ctypes.byref(J)))
+        return J.value
+
+    def adjoint_step(self):
+        self._check(self._lib.ks_adjoint_step(self._h))
+
+    def adjoint_run(self, nsteps, snapshots):
+        """Forward ``nsteps`` steps, J at the end, reverse sweep with binomial
+        checkpointing in ``snapshots`` device slots; returns J."""
+        J = ctypes.c_double()
+        self._check(self._lib.ks_adjoint_run(self._h, int(nsteps), int(snapshots), ctypes.byref(J)))
+        return J.value
+
+    def ndisks(self):
+        return int(self.scalar("ndisks"))
+
+    def ct_gradient(self):
+        n = self.ndisks()
+        g = (ctypes.c_double * max(n, 1))()
+        self._check(self._lib.ks_get_ct_gradient(self._h, g, n))
+        return np.array(g[:n])
+
+    def adjoint_reset(self):
+        self._check(self._lib.ks_adjoint_reset(self._h))
+
+    def set_disk_ct(self, ct):
+        ct = [float(x) for x in ct]
+        a = (ctypes.c_double * max(len(ct), 1))(*ct)
+        self._check(self._lib.ks_set_disk_ct(self._h, a, len(ct)))

@@ -187,7 +187,7 @@ def test_disk_total_thrust(oracle_mod):
     o.InitData()
     o.step()
     act = o.get_field("actuator_src_term")
-    total = act[0].sum() * 10.0 ** 3
+    total = -act[0].sum() * 10.0 ** 3  # component along the disk normal (-1, 0, 0)
     R = 40.0
     expect = 0.5 * o.scalar("disk_uinf2:0") * 0.75 * math.pi * R * R
     assert abs(total - expect) / expect < 1e-6
