@@ -48,6 +48,11 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision form of the same workload")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost / gradient check (128x128x64, 3 disks)")
+    p.add_argument("--c4", action="store_true",
+                   help="only the production forward + adjoint run: 512x512x256 ABL, 16 disks, mixed forward, FP64 adjoint")
+    p.add_argument("--c4-steps", type=int, default=200)
+    p.add_argument("--c4-slots", type=int, default=12)
+    p.add_argument("--c4-fd-h", default="1e-6,1e-8", help="finite-difference steps for the 2-disk gradient check")
     p.add_argument("--profile-all", action="store_true", help="print the per-kernel breakdown to stderr")
     p.add_argument("--size", default="256,256,128")
     p.add_argument("--cpu-worker", default="", help=argparse.SUPPRESS)
@@ -368,8 +373,106 @@ def adjoint_bench(args, torch, ks, decks):
             "device_mem_in_use_GB": (total - free) / 1e9}
 
 
+def c4_bench(args):
+    """Production forward + adjoint run: 512x512x256 ABL (C1 physics at 10 m
+    cells, 5120x5120x2560 m) with a 4x4 farm of uniform-Ct
+    disks (D = 20 cells, spacing 7 D), fixed dt 0.5 s, mixed-precision forward
+    with binomial checkpoints in HBM and the FP64 reverse sweep; dJ/dCt of two
+    disks against central finite differences of the FP64 forward."""
+    import torch
+    import kynema_sgf_gb300 as ks
+    from kynema_sgf_gb300 import decks
+    nsteps, slots = args.c4_steps, args.c4_slots
+    deck, lo, hi, cts = decks.abl_disks()
+    sim = ks.Incflo(deck)
+    sim.InitData()
+    sim.set_objective_box(lo, hi)
+    dev = torch.device("cuda:0")
+    x0 = {f: torch.empty(sim.layout(f), dtype=torch.float64, device=dev) for f in ("velocity", "gp", "p")}
+    for f, t in x0.items():
+        sim.get_field(f, out=t)
+    stream = torch.cuda.ExternalStream(sim.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def restore(c=cts):
+        for f, t in x0.items():
+            sim.set_field(f, t)
+        sim.set_disk_ct(c)
+
+    def timed(fn, k):
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(k):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    restore()
+    sim.step()
+    fwd_mixed = timed(sim.step, 3) / 3
+    restore()
+    sim.set_precision(0)
+    fwd64 = timed(sim.step, 3) / 3
+    sim.set_precision(1)
+    restore()
+    sim.adjoint_reset()
+    sim.objective(seed=True)
+    sim.adjoint_step()
+    rev = timed(sim.adjoint_step, 2) / 2
+    sim.profile_kernels("*")
+    sim.adjoint_step()
+    rep = sim.profile_report()
+    sim.profile_kernels("")
+    tot = sum(v[1] for v in rep.values())
+    top = [[k, v[0], round(v[1], 2), round(v[1] / tot, 3)] for k, v in sorted(rep.items(), key=lambda kv: -kv[1][1])[:16]]
+    restore()
+    out = {}
+
+    def run():
+        out["J"] = sim.adjoint_run(nsteps, slots)
+
+    run_ms = timed(run, 1)
+    g = [float(x) for x in sim.ct_gradient()]
+    added = sim.scalar("adj_forward_steps")
+    free, total = torch.cuda.mem_get_info()
+    lib_mem = (total - free) - torch.cuda.memory_reserved()
+    sim.set_precision(0)
+
+    def fJ(c):
+        restore(c)
+        for _ in range(nsteps):
+            sim.step()
+        return sim.objective()
+
+    J64 = fJ(cts)
+    fd = {}
+    for h in (float(x) for x in args.c4_fd_h.split(",") if x):
+        est = []
+        for k in (0, 1):
+            cp, cm = list(cts), list(cts)
+            cp[k] += h
+            cm[k] -= h
+            est.append((fJ(cp) - fJ(cm)) / (2 * h))
+        fd["h=%g" % h] = {"fd": est, "rel_err": [abs(a - b) / max(abs(x) for x in g[:2]) for a, b in zip(est, g[:2])]}
+    line = {"c4": {
+        "workload": "512x512x256 ABL (C1 physics, 10 m cells), 4x4 UniformCt disks D = 20 cells spaced 7 D, fixed dt 0.5 s, "
+                    "J = mean 0.5|u|^2 in the rotor layer 0..5 D behind the first column, %d steps" % nsteps,
+        "forward_mixed_ms_per_step": fwd_mixed, "forward_fp64_ms_per_step": fwd64,
+        "reverse_step_ms": rev, "reverse_step_over_mixed_forward": rev / fwd_mixed,
+        "reverse_step_kernels": {"note": "one reverse step (with its recompute), kernel, launches, ms, share", "top": top},
+        "run": {"steps": nsteps, "snapshots": slots, "forward_steps_added": added, "ms": run_ms,
+                "over_mixed_forward_run": run_ms / (nsteps * fwd_mixed)},
+        "device_mem_library_GB": lib_mem / 1e9, "device_mem_in_use_GB": (total - free) / 1e9,
+        "J_mixed_forward": out["J"], "J_fp64_forward": J64, "dJ_dCt": g, "fd_fp64_disks_0_1": fd}}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
+    if args.c4:
+        c4_bench(args)
+        return
     if args.cpu_worker:
         cpu_worker(args.cpu_worker)
         return

@@ -112,9 +112,11 @@ int ks_set_objective_box(ks_handle* h, const double lo[3], const double hi[3]);
  * and 0 (the terminal condition of a reverse sweep). */
 int ks_objective(ks_handle* h, int seed, double* J);
 /* One reverse step at the current state x^n = (velocity, gp): the adjoint
- * fields go from the adjoint of x^{n+1} to that of x^n (the step is
- * recomputed from x^n in FP64) and dJ/dct accumulates; the forward state and
- * the clock are left at x^n. */
+ * fields go from the adjoint of x^{n+1} to that of x^n and dJ/dct
+ * accumulates; the forward state and the clock are left at x^n.  The step is
+ * recomputed from x^n with FP64 Godunov passes; its projections (and the two
+ * reverse solves) run at the handle's precision, which reaches the FP64
+ * multigrid tolerance either way. */
 int ks_adjoint_step(ks_handle* h);
 /* nsteps forward steps from the current state with binomial checkpointing in
  * device memory (`snapshots` slots of (velocity, gp), the first holding the

@@ -1,14 +1,16 @@
-// Reverse (adjoint) kernels of the advance, FP64, triply periodic grids.
+// Reverse (adjoint) kernels of the advance, FP64.
 //
 // Every forward pass y = K(x) gets a kernel that accumulates x_bar += (dK/dx)^T
 // y_bar at the forward linearisation point.  The PPM limiter, clipping,
 // Riemann and upwind selections are re-evaluated from the stored forward
 // values and frozen (their derivatives are the derivatives of the selected
 // branch).  Inputs that several outputs read are accumulated with atomicAdd.
-// Passes that are linear and self-adjoint on periodic grids reuse the forward
-// kernels (tensor diffusion with constant viscosity, MAC projection); the
-// nodal projection uses D^T = -G and G^T = -D of its divergence / gradient
-// pair (ks_host.cpp).
+// Boundary handling mirrors the forward kernels: x/y periodic; z periodic or
+// walls, where the forward reads fill-patch ghosts (high-order extrapolation
+// of the tangential components, zero normal component) for Godunov, odd/even
+// reflections or the wall-model shift for diffusion, and replaces wall-face
+// states (zbc); the reverse scatters every ghost read back onto the interior
+// cells it was built from.
 #include "ks_launch.hpp"
 
 namespace ks {
@@ -22,21 +24,70 @@ __device__ inline void aadd(double* p, double v) {
     if (v != 0.0) atomicAdd(p, v);
 }
 
-__device__ inline bool face3(const Grid& g, long long t, int& i, int& j, int& k) {
-    if (t >= g.N) return false;
+// faces of direction d, the same index domain as the forward kernels
+__device__ inline bool face_at(const Grid& g, int d, long long t, int& i, int& j, int& k) {
+    const int nzl = (d == 2) ? nzfaces(g) : g.nz;
+    const long long M = (long long)g.nx * g.ny * nzl;
+    if (t >= M) return false;
     i = (int)(t % g.nx);
     const long long r = t / g.nx;
     j = (int)(r % g.ny);
     k = (int)(r / g.ny);
     return true;
 }
+inline long long nfaces(const Grid& g, int d) { return (long long)g.nx * g.ny * (d == 2 ? nzfaces(g) : g.nz); }
 
-// cell value of velocity component n (periodic)
-__device__ inline double U(const Grid& g, const double* u, int n, int i, int j, int k) {
-    return u[n * g.N + cidx(g, wrapn(i, g.nx), wrapn(j, g.ny), wrapn(k, g.nz))];
+// velocity read with the Godunov fill-patch ghosts (VelFPT, scale 1) and its adjoint
+__device__ inline double Q(const Grid& g, const double* u, int n, int i, int j, int k) {
+    const VelFPT<double> q{u, g, 1.0};
+    return q(n, i, j, k);
 }
-__device__ inline double* Ub(const Grid& g, double* u, int n, int i, int j, int k) {
-    return u + n * g.N + cidx(g, wrapn(i, g.nx), wrapn(j, g.ny), wrapn(k, g.nz));
+__device__ inline void Qb(const Grid& g, double* ub, int n, int i, int j, int k, double v) {
+    if (v == 0.0) return;
+    i = wrapn(i, g.nx);
+    j = wrapn(j, g.ny);
+    double* c = ub + (long long)n * g.N;
+    if (g.zper) {
+        atomicAdd(c + cidx(g, i, j, wrapn(k, g.nz)), v);
+        return;
+    }
+    if (k < 0 || k >= g.nz) {  // ghost = (15 q0 - 10 q1 + 3 q2) / 8 of the nearest cells; normal component 0
+        if (n == 2) return;
+        const int k0 = k < 0 ? 0 : g.nz - 1, s = k < 0 ? 1 : -1;
+        atomicAdd(c + cidx(g, i, j, k0), 1.875 * v);
+        atomicAdd(c + cidx(g, i, j, k0 + s), -1.25 * v);
+        atomicAdd(c + cidx(g, i, j, k0 + 2 * s), 0.375 * v);
+        return;
+    }
+    atomicAdd(c + cidx(g, i, j, k), v);
+}
+
+// wall-face state replacement of the forward (zbc) and its adjoint
+__device__ inline void zbc_fwd(const Grid& g, int k, int n, double& lo, double& hi) {
+    if (g.zper) return;
+    if (k == 0) {
+        if (n == 2) lo = hi = 0.0; else lo = hi;
+    } else if (k == g.nz) {
+        if (n == 2) lo = hi = 0.0; else hi = lo;
+    }
+}
+__device__ inline void zbc_rev(const Grid& g, int k, int n, double& lb, double& hb) {
+    if (g.zper) return;
+    if (k == 0) {
+        if (n == 2) {
+            lb = hb = 0.0;
+        } else {
+            hb += lb;
+            lb = 0.0;
+        }
+    } else if (k == g.nz) {
+        if (n == 2) {
+            lb = hb = 0.0;
+        } else {
+            lb += hb;
+            hb = 0.0;
+        }
+    }
 }
 
 // ---- van Leer slope: value and the coefficients of (a, b, c)
@@ -60,34 +111,60 @@ __device__ inline double vls_d(double a, double b, double c, double& ca, double&
     return dsr;
 }
 
-// ---- reverse of the unlimited PPM edge on d-faces (k_edges):
-// E = clip(0.5(a0+a1) - (vl(a0,a1,a2) - vl(am,a0,a1))/6, a0, a1)
+// adjoint of clip(e, a, b) = min(max(e, min(a, b)), max(a, b)) given the
+// adjoint of the result: returns the adjoint of e; adds to those of a, b
+__device__ inline double clip_rev(double e, double a, double b, double rb, double& ga, double& gb) {
+    const double lo = fmin(a, b), hi = fmax(a, b);
+    if (fmax(e, lo) > hi) {
+        if (a >= b) ga += rb; else gb += rb;
+        return 0.0;
+    }
+    if (e < lo) {
+        if (a <= b) ga += rb; else gb += rb;
+        return 0.0;
+    }
+    return rb;
+}
+
+// ---- reverse of the unlimited PPM edges on d-faces (k_edges)
 __global__ void k_adj_edges(Grid g, int d, const double* u, const double* Eb0, const double* Eb1, const double* Eb2, double* ub) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (!face3(g, t, i, j, k)) return;
+    if (!face_at(g, d, t, i, j, k)) return;
     const int di = (d == 0), dj = (d == 1), dk = (d == 2);
+    const bool wall = (d == 2 && !g.zper);
     const double* Eb[3] = {Eb0, Eb1, Eb2};
     for (int n = 0; n < 3; ++n) {
         const double eb = Eb[n][t];
         if (eb == 0.0) continue;
-        const double am = U(g, u, n, i - 2 * di, j - 2 * dj, k - 2 * dk), a0 = U(g, u, n, i - di, j - dj, k - dk);
-        const double a1 = U(g, u, n, i, j, k), a2 = U(g, u, n, i + di, j + dj, k + dk);
+        if (wall && (k == 0 || k == g.nz)) {  // the wall face takes the ghost value
+            Qb(g, ub, n, i, j, k == 0 ? -1 : g.nz, eb);
+            continue;
+        }
+        if (wall && (k == 1 || k == g.nz - 1)) {  // one-sided fourth order, clipped to the adjacent cells
+            const int kb = (k == 1) ? -1 : g.nz, k0 = (k == 1) ? 0 : g.nz - 1, s = (k == 1) ? 1 : -1;
+            const double b = Q(g, u, n, i, j, kb), q0 = Q(g, u, n, i, j, k0), q1 = Q(g, u, n, i, j, k0 + s), q2 = Q(g, u, n, i, j, k0 + 2 * s);
+            const double e = -0.2 * b + 0.75 * q0 + 0.5 * q1 - 0.05 * q2;
+            double g0 = 0.0, g1 = 0.0;
+            const double ebar = clip_rev(e, q0, q1, eb, g0, g1);
+            Qb(g, ub, n, i, j, kb, -0.2 * ebar);
+            Qb(g, ub, n, i, j, k0, 0.75 * ebar + g0);
+            Qb(g, ub, n, i, j, k0 + s, 0.5 * ebar + g1);
+            Qb(g, ub, n, i, j, k0 + 2 * s, -0.05 * ebar);
+            continue;
+        }
+        const double am = Q(g, u, n, i - 2 * di, j - 2 * dj, k - 2 * dk), a0 = Q(g, u, n, i - di, j - dj, k - dk);
+        const double a1 = Q(g, u, n, i, j, k), a2 = Q(g, u, n, i + di, j + dj, k + dk);
         double c1a, c1b, c1c, c0a, c0b, c0c;
         const double s1 = vls_d(a0, a1, a2, c1a, c1b, c1c);
         const double s0 = vls_d(am, a0, a1, c0a, c0b, c0c);
         const double e = 0.5 * (a0 + a1) - (1.0 / 6.0) * (s1 - s0);
-        const double lo = fmin(a0, a1), hi = fmax(a0, a1);
-        double gm = 0, g0 = 0, g1 = 0, g2 = 0;
-        const double r = fmax(e, lo);
-        if (r > hi) {  // clipped to the larger neighbour
-            if (a0 >= a1) g0 += eb; else g1 += eb;
-        } else if (e < lo) {  // clipped to the smaller neighbour
-            if (a0 <= a1) g0 += eb; else g1 += eb;
-        } else {
-            g0 += 0.5 * eb;
-            g1 += 0.5 * eb;
-            const double ds1 = -eb / 6.0, ds0 = eb / 6.0;
+        double gm = 0.0, g0 = 0.0, g1 = 0.0, g2 = 0.0;
+        const double ebar = clip_rev(e, a0, a1, eb, g0, g1);
+        if (ebar != 0.0) {
+            g0 += 0.5 * ebar;
+            g1 += 0.5 * ebar;
+            const double ds1 = -ebar / 6.0, ds0 = ebar / 6.0;
             g0 += ds1 * c1a;
             g1 += ds1 * c1b;
             g2 += ds1 * c1c;
@@ -95,19 +172,18 @@ __global__ void k_adj_edges(Grid g, int d, const double* u, const double* Eb0, c
             g0 += ds0 * c0b;
             g1 += ds0 * c0c;
         }
-        aadd(Ub(g, ub, n, i - 2 * di, j - 2 * dj, k - 2 * dk), gm);
-        aadd(Ub(g, ub, n, i - di, j - dj, k - dk), g0);
-        aadd(Ub(g, ub, n, i, j, k), g1);
-        aadd(Ub(g, ub, n, i + di, j + dj, k + dk), g2);
+        Qb(g, ub, n, i - 2 * di, j - 2 * dj, k - 2 * dk, gm);
+        Qb(g, ub, n, i - di, j - dj, k - dk, g0);
+        Qb(g, ub, n, i, j, k, g1);
+        Qb(g, ub, n, i + di, j + dj, k + dk, g2);
     }
 }
 
 // ---- reverse of the CW84 limiter + trace.  Given the adjoint tb of the trace
-// value (after any rho scaling), accumulate into sm_in, s0, sp_in adjoints and
-// return the adjoint of sig.
+// value, accumulate into the adjoints of sm_in, s0, sp_in and return the
+// adjoint of sig.
 __device__ inline double rev_trace(bool hi_side, double smi, double s0, double spi, double sig, double tb, double& gsm, double& gs0,
                                    double& gsp) {
-    // forward limiter with case record
     double sm = smi, sp = spi;
     int cs = 0;
     if ((sp - s0) * (s0 - sm) <= 0.0) {
@@ -136,7 +212,6 @@ __device__ inline double rev_trace(bool hi_side, double smi, double s0, double s
         dsig = 0.5 * ((sp - sm) + Bf * s6) - (1.0 / 3.0) * sig * s6;
     }
     double bsm = dsm * tb, bsp = dsp * tb, bs0 = ds0 * tb;
-    // reverse the limiter
     if (cs == 1) {
         bs0 += bsm + bsp;
         bsm = 0.0;
@@ -157,8 +232,7 @@ __device__ inline double rev_trace(bool hi_side, double smi, double s0, double s
 }
 
 __device__ inline void rev_upwind(double vel, double ob, double& lb, double& hb) {
-    const bool fu = !(fabs(vel) < kSV);
-    if (fu) {
+    if (!(fabs(vel) < kSV)) {
         if (vel >= 0.0) lb += ob; else hb += ob;
     } else {
         lb += 0.5 * ob;
@@ -186,8 +260,9 @@ __global__ void k_adj_faces(Grid g, int d, const double* u, K3 E, double s, doub
                             K3 LOb, K3 HIb, const double* adb, K3 TEb, A3 Eb, double* ub, double* umacb_d) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (!face3(g, t, i, j, k)) return;
+    if (!face_at(g, d, t, i, j, k)) return;
     const int di = (d == 0), dj = (d == 1), dk = (d == 2);
+    const bool wl = (d == 2 && !g.zper && k == 0), wh = (d == 2 && !g.zper && k == g.nz);
     const long long f = t;
     const long long fm = fidx(g, d, i - di, j - dj, k - dk), fp = fidx(g, d, i + di, j + dj, k + dk);
     double lb[3], hb[3];
@@ -195,76 +270,77 @@ __global__ void k_adj_faces(Grid g, int d, const double* u, K3 E, double s, doub
         lb[n] = LOb.p[n][f];
         hb[n] = HIb.p[n][f];
     }
-    double ul, uh, umf = 0.0;
+    double ul = 0.0, uh = 0.0;
     if (MODE == 0) {
-        ul = U(g, u, d, i - di, j - dj, k - dk);
-        uh = U(g, u, d, i, j, k);
-        const double a = ad[f];
+        if (!wl) ul = Q(g, u, d, i - di, j - dj, k - dk);
+        if (!wh) uh = Q(g, u, d, i, j, k);
         rev_riemann(LO.p[d][f], HI.p[d][f], adb[f], lb[d], hb[d]);
+        const double a = ad[f];
         for (int n = 0; n < 3; ++n)
             if (n != d) rev_upwind(a, TEb.p[n][f], lb[n], hb[n]);
     } else {
-        umf = umac_d[f];
+        const double umf = umac_d[f];
         ul = uh = umf;
         for (int n = 0; n < 3; ++n) rev_upwind(umf, TEb.p[n][f], lb[n], hb[n]);
     }
+    if (d == 2)
+        for (int n = 0; n < 3; ++n) zbc_rev(g, k, n, lb[n], hb[n]);
     const double scale = (MODE == 1) ? rho : 1.0;
     double gul = 0.0, guh = 0.0;
     for (int n = 0; n < 3; ++n) {
-        // low side: high-face trace of cell c - e_d
         const double tl = lb[n] * scale, th = hb[n] * scale;
-        double gsm = 0, gs0 = 0, gsp = 0;
-        if (tl != 0.0) {
-            const double s0 = U(g, u, n, i - di, j - dj, k - dk);
+        if (!wl && tl != 0.0) {  // high-side trace of cell c - e_d
+            double gsm = 0.0, gs0 = 0.0, gsp = 0.0;
+            const double s0 = Q(g, u, n, i - di, j - dj, k - dk);
             if (ul > kSV) {
-                const double sig = fabs(ul) * s;
-                const double bsig = rev_trace(true, E.p[n][fm], s0, E.p[n][f], sig, tl, gsm, gs0, gsp);
+                const double bsig = rev_trace(true, E.p[n][fm], s0, E.p[n][f], fabs(ul) * s, tl, gsm, gs0, gsp);
                 gul += bsig * s * (ul >= 0.0 ? 1.0 : -1.0);
             } else {
                 gs0 += tl;
             }
             aadd(&Eb.p[n][fm], gsm);
             aadd(&Eb.p[n][f], gsp);
-            aadd(Ub(g, ub, n, i - di, j - dj, k - dk), gs0);
+            Qb(g, ub, n, i - di, j - dj, k - dk, gs0);
         }
-        gsm = gs0 = gsp = 0;
-        if (th != 0.0) {
-            const double s0 = U(g, u, n, i, j, k);
+        if (!wh && th != 0.0) {  // low-side trace of cell c
+            double gsm = 0.0, gs0 = 0.0, gsp = 0.0;
+            const double s0 = Q(g, u, n, i, j, k);
             if (uh < -kSV) {
-                const double sig = fabs(uh) * s;
-                const double bsig = rev_trace(false, E.p[n][f], s0, E.p[n][fp], sig, th, gsm, gs0, gsp);
+                const double bsig = rev_trace(false, E.p[n][f], s0, E.p[n][fp], fabs(uh) * s, th, gsm, gs0, gsp);
                 guh += bsig * s * (uh >= 0.0 ? 1.0 : -1.0);
             } else {
                 gs0 += th;
             }
             aadd(&Eb.p[n][f], gsm);
             aadd(&Eb.p[n][fp], gsp);
-            aadd(Ub(g, ub, n, i, j, k), gs0);
+            Qb(g, ub, n, i, j, k, gs0);
         }
     }
     if (MODE == 0) {
-        aadd(Ub(g, ub, d, i - di, j - dj, k - dk), gul);
-        aadd(Ub(g, ub, d, i, j, k), guh);
+        if (!wl) Qb(g, ub, d, i - di, j - dj, k - dk, gul);
+        if (!wh) Qb(g, ub, d, i, j, k, guh);
     } else {
         aadd(&umacb_d[f], gul + guh);
     }
 }
 
 // ---- reverse of k_pm_trans (a, b, n)
-__global__ void k_adj_pm_trans(Grid g, int a, int b, double cb, const double* ad_a, const double* ad_b, const double* edge_b, const double* lo_an,
-                               const double* hi_an, const double* outb, double* lo_anb, double* hi_anb, double* ad_bb, double* edge_bb) {
+__global__ void k_adj_pm_trans(Grid g, int a, int b, int n, double cb, const double* ad_a, const double* ad_b, const double* edge_b,
+                               const double* outb, double* lo_anb, double* hi_anb, double* ad_bb, double* edge_bb) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (!face3(g, t, i, j, k)) return;
+    if (!face_at(g, a, t, i, j, k)) return;
     const long long f = t;
     const double ob = outb[f];
     if (ob == 0.0) return;
-    double lb = 0, hb = 0;
+    const bool wl = (a == 2 && !g.zper && k == 0), wh = (a == 2 && !g.zper && k == g.nz);
+    double lb = 0.0, hb = 0.0;
     rev_upwind(ad_a[f], ob, lb, hb);
+    if (a == 2) zbc_rev(g, k, n, lb, hb);
     lo_anb[f] += lb;
     hi_anb[f] += hb;
     const int e0 = (b == 0), e1 = (b == 1), e2 = (b == 2);
-    {
+    if (!wh && hb != 0.0) {
         const long long f0 = fidx(g, b, i, j, k), f1 = fidx(g, b, i + e0, j + e1, k + e2);
         const double S = ad_b[f1] + ad_b[f0], Dd = edge_b[f1] - edge_b[f0];
         aadd(&ad_bb[f1], -cb * Dd * hb);
@@ -272,7 +348,7 @@ __global__ void k_adj_pm_trans(Grid g, int a, int b, double cb, const double* ad
         aadd(&edge_bb[f1], -cb * S * hb);
         aadd(&edge_bb[f0], cb * S * hb);
     }
-    {
+    if (!wl && lb != 0.0) {
         const int ci = i - (a == 0), cj = j - (a == 1), ck = k - (a == 2);
         const long long f0 = fidx(g, b, ci, cj, ck), f1 = fidx(g, b, ci + e0, cj + e1, ck + e2);
         const double S = ad_b[f1] + ad_b[f0], Dd = edge_b[f1] - edge_b[f0];
@@ -283,13 +359,23 @@ __global__ void k_adj_pm_trans(Grid g, int a, int b, double cb, const double* ad
     }
 }
 
+// forces with the first-order extrapolated ghosts of CellFOT and the adjoint
+__device__ inline long long cell_fo(const Grid& g, int i, int j, int k) {
+    i = wrapn(i, g.nx);
+    j = wrapn(j, g.ny);
+    if (g.zper) k = wrapn(k, g.nz);
+    else k = k < 0 ? 0 : (k >= g.nz ? g.nz - 1 : k);
+    return cidx(g, i, j, k);
+}
+
 // ---- reverse of k_pm_final (d)
 __global__ void k_adj_pm_final(Grid g, int d, double dt, double c1, double c2, const double* lo_dd, const double* hi_dd, K3 AD, const double* T1,
                                const double* T2, const double* forces, const double* macb, double* lo_ddb, double* hi_ddb, A3 ADb,
                                double* T1b, double* T2b, double* forcesb) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (!face3(g, t, i, j, k)) return;
+    if (!face_at(g, d, t, i, j, k)) return;
+    if (d == 2 && !g.zper && (k == 0 || k == g.nz)) return;  // wall faces: the normal velocity is 0 whatever the input
     const long long f = t;
     const double mb = macb[f];
     if (mb == 0.0) return;
@@ -300,7 +386,7 @@ __global__ void k_adj_pm_final(Grid g, int d, double dt, double c1, double c2, c
         double s = base;
         s -= c1 * (AD.p[b1][p1] + AD.p[b1][m1]) * (T1[p1] - T1[m1]);
         s -= c2 * (AD.p[b2][p2] + AD.p[b2][m2]) * (T2[p2] - T2[m2]);
-        s += 0.5 * dt * forces[d * g.N + cidx(g, wrapn(ci, g.nx), wrapn(cj, g.ny), wrapn(ck, g.nz))];
+        s += 0.5 * dt * forces[d * g.N + cell_fo(g, ci, cj, ck)];
         return s;
     };
     auto side_rev = [&](int ci, int cj, int ck, double sb) {
@@ -316,11 +402,11 @@ __global__ void k_adj_pm_final(Grid g, int d, double dt, double c1, double c2, c
         aadd(&ADb.p[b2][m2], -c2 * D2 * sb);
         aadd(&T2b[p2], -c2 * S2 * sb);
         aadd(&T2b[m2], c2 * S2 * sb);
-        aadd(&forcesb[d * g.N + cidx(g, wrapn(ci, g.nx), wrapn(cj, g.ny), wrapn(ck, g.nz))], 0.5 * dt * sb);
+        aadd(&forcesb[d * g.N + cell_fo(g, ci, cj, ck)], 0.5 * dt * sb);
     };
     const int li = i - (d == 0), lj = j - (d == 1), lk = k - (d == 2);
     const double stl = side_val(li, lj, lk, lo_dd[f]), sth = side_val(i, j, k, hi_dd[f]);
-    double bl = 0, bh = 0;
+    double bl = 0.0, bh = 0.0;
     rev_riemann(stl, sth, mb, bl, bh);
     if (bl != 0.0) {
         lo_ddb[f] += bl;
@@ -338,36 +424,46 @@ __global__ void k_adj_adv_trans(Grid g, int a, int b, const double* u, double rh
                                 A3 LOb, A3 HIb, A3 Ebb, double* vbb, double* ub) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (!face3(g, t, i, j, k)) return;
+    if (!face_at(g, a, t, i, j, k)) return;
+    const bool wl = (a == 2 && !g.zper && k == 0), wh = (a == 2 && !g.zper && k == g.nz);
     const long long f = t;
     const double uaf = ua[f];
     const int ci = i - (a == 0), cj = j - (a == 1), ck = k - (a == 2);
     const long long h0 = fidx(g, b, i, j, k), h1 = fidx(g, b, i + (b == 0), j + (b == 1), k + (b == 2));
     const long long l0 = fidx(g, b, ci, cj, ck), l1 = fidx(g, b, ci + (b == 0), cj + (b == 1), ck + (b == 2));
-    const double vhp = vb[h1], vhm = vb[h0], vlp = vb[l1], vlm = vb[l0];
-    double gvhp = 0, gvhm = 0, gvlp = 0, gvlm = 0;
+    double vhp = 0.0, vhm = 0.0, vlp = 0.0, vlm = 0.0;
+    if (!wh) {
+        vhp = vb[h1];
+        vhm = vb[h0];
+    }
+    if (!wl) {
+        vlp = vb[l1];
+        vlm = vb[l0];
+    }
+    double gvhp = 0.0, gvhm = 0.0, gvlp = 0.0, gvlm = 0.0;
     for (int n = 0; n < 3; ++n) {
         const double ob = Ob.p[n][f];
         if (ob == 0.0) continue;
-        double lb = 0, hb = 0;
+        double lb = 0.0, hb = 0.0;
         rev_upwind(uaf, ob, lb, hb);
+        if (a == 2) zbc_rev(g, k, n, lb, hb);
         LOb.p[n][f] += lb;
         HIb.p[n][f] += hb;
-        if (hb != 0.0) {
-            const double qc = rho * U(g, u, n, i, j, k);
+        if (!wh && hb != 0.0) {
+            const double qc = rho * Q(g, u, n, i, j, k);
             aadd(&Ebb.p[n][h1], -cb * vhp * hb);
             aadd(&Ebb.p[n][h0], cb * vhm * hb);
             gvhp += (-cb * E.p[n][h1] + cb * qc) * hb;
             gvhm += (cb * E.p[n][h0] - cb * qc) * hb;
-            aadd(Ub(g, ub, n, i, j, k), rho * cb * (vhp - vhm) * hb);
+            Qb(g, ub, n, i, j, k, rho * cb * (vhp - vhm) * hb);
         }
-        if (lb != 0.0) {
-            const double qc = rho * U(g, u, n, ci, cj, ck);
+        if (!wl && lb != 0.0) {
+            const double qc = rho * Q(g, u, n, ci, cj, ck);
             aadd(&Ebb.p[n][l1], -cb * vlp * lb);
             aadd(&Ebb.p[n][l0], cb * vlm * lb);
             gvlp += (-cb * E.p[n][l1] + cb * qc) * lb;
             gvlm += (cb * E.p[n][l0] - cb * qc) * lb;
-            aadd(Ub(g, ub, n, ci, cj, ck), rho * cb * (vlp - vlm) * lb);
+            Qb(g, ub, n, ci, cj, ck, rho * cb * (vlp - vlm) * lb);
         }
     }
     aadd(&vbb[h1], gvhp);
@@ -381,7 +477,8 @@ __global__ void k_adj_adv_flux(Grid g, int d, const double* u, const double* for
                                K3 HI, K3 T1, K3 T2, K3 Fb, A3 Ufb, A3 LOb, A3 HIb, A3 T1b, A3 T2b, double* ub, double* forcesb) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (!face3(g, t, i, j, k)) return;
+    if (!face_at(g, d, t, i, j, k)) return;
+    const bool wl = (d == 2 && !g.zper && k == 0), wh = (d == 2 && !g.zper && k == g.nz);
     const long long f = t;
     const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
     const double um = Uf.p[d][f];
@@ -390,40 +487,60 @@ __global__ void k_adj_adv_flux(Grid g, int d, const double* u, const double* for
     const long long lp2 = fidx(g, b2, li + (b2 == 0), lj + (b2 == 1), lk + (b2 == 2)), lm2 = fidx(g, b2, li, lj, lk);
     const long long hp1 = fidx(g, b1, i + (b1 == 0), j + (b1 == 1), k + (b1 == 2)), hm1 = fidx(g, b1, i, j, k);
     const long long hp2 = fidx(g, b2, i + (b2 == 0), j + (b2 == 1), k + (b2 == 2)), hm2 = fidx(g, b2, i, j, k);
-    const double l1p = Uf.p[b1][lp1], l1m = Uf.p[b1][lm1], l2p = Uf.p[b2][lp2], l2m = Uf.p[b2][lm2];
-    const double h1p = Uf.p[b1][hp1], h1m = Uf.p[b1][hm1], h2p = Uf.p[b2][hp2], h2m = Uf.p[b2][hm2];
+    double l1p = 0, l1m = 0, l2p = 0, l2m = 0, h1p = 0, h1m = 0, h2p = 0, h2m = 0;
+    if (!wl) {
+        l1p = Uf.p[b1][lp1];
+        l1m = Uf.p[b1][lm1];
+        l2p = Uf.p[b2][lp2];
+        l2m = Uf.p[b2][lm2];
+    }
+    if (!wh) {
+        h1p = Uf.p[b1][hp1];
+        h1m = Uf.p[b1][hm1];
+        h2p = Uf.p[b2][hp2];
+        h2m = Uf.p[b2][hm2];
+    }
     double gum = 0, gl1p = 0, gl1m = 0, gl2p = 0, gl2m = 0, gh1p = 0, gh1m = 0, gh2p = 0, gh2m = 0;
-    const long long cl = cidx(g, wrapn(li, g.nx), wrapn(lj, g.ny), wrapn(lk, g.nz));
-    const long long ch = cidx(g, i, j, k);
+    const long long cl = wl ? 0 : cell_fo(g, li, lj, lk);
+    const long long ch = wh ? 0 : cell_fo(g, i, j, k);
     for (int n = 0; n < 3; ++n) {
         const double fb = Fb.p[n][f];
         if (fb == 0.0) continue;
-        const double ql = rho * u[n * g.N + cl], qh = rho * u[n * g.N + ch];
-        double stl = LO.p[n][f];
-        stl -= c1 * (T1.p[n][lp1] * l1p - T1.p[n][lm1] * l1m);
-        stl -= c2 * (T2.p[n][lp2] * l2p - T2.p[n][lm2] * l2m);
-        stl += c1 * ql * (l1p - l1m);
-        stl += c2 * ql * (l2p - l2m);
-        stl += 0.5 * dt * (rho * forces[n * g.N + cl]);
-        double sth = HI.p[n][f];
-        sth -= c1 * (T1.p[n][hp1] * h1p - T1.p[n][hm1] * h1m);
-        sth -= c2 * (T2.p[n][hp2] * h2p - T2.p[n][hm2] * h2m);
-        sth += c1 * qh * (h1p - h1m);
-        sth += c2 * qh * (h2p - h2m);
-        sth += 0.5 * dt * (rho * forces[n * g.N + ch]);
-        double st, bl = 0, bh = 0;
+        double ql = 0.0, qh = 0.0, stl = 0.0, sth = 0.0;
+        if (!wl) {
+            ql = rho * u[n * g.N + cl];
+            stl = LO.p[n][f];
+            stl -= c1 * (T1.p[n][lp1] * l1p - T1.p[n][lm1] * l1m);
+            stl -= c2 * (T2.p[n][lp2] * l2p - T2.p[n][lm2] * l2m);
+            stl += c1 * ql * (l1p - l1m);
+            stl += c2 * ql * (l2p - l2m);
+            stl += 0.5 * dt * (rho * forces[n * g.N + cl]);
+        }
+        if (!wh) {
+            qh = rho * u[n * g.N + ch];
+            sth = HI.p[n][f];
+            sth -= c1 * (T1.p[n][hp1] * h1p - T1.p[n][hm1] * h1m);
+            sth -= c2 * (T2.p[n][hp2] * h2p - T2.p[n][hm2] * h2m);
+            sth += c1 * qh * (h1p - h1m);
+            sth += c2 * qh * (h2p - h2m);
+            sth += 0.5 * dt * (rho * forces[n * g.N + ch]);
+        }
+        double zl = stl, zh = sth;
+        if (d == 2) zbc_fwd(g, k, n, zl, zh);
+        double st, bl = 0.0, bh = 0.0;
         if (fabs(um) < kSV) {
-            st = 0.5 * (stl + sth);
+            st = 0.5 * (zl + zh);
             bl = bh = 0.5 * um * fb;
         } else if (um >= 0.0) {
-            st = stl;
+            st = zl;
             bl = um * fb;
         } else {
-            st = sth;
+            st = zh;
             bh = um * fb;
         }
         gum += st * fb;
-        if (bl != 0.0) {
+        if (d == 2) zbc_rev(g, k, n, bl, bh);
+        if (!wl && bl != 0.0) {
             LOb.p[n][f] += bl;
             aadd(&T1b.p[n][lp1], -c1 * l1p * bl);
             aadd(&T1b.p[n][lm1], c1 * l1m * bl);
@@ -436,7 +553,7 @@ __global__ void k_adj_adv_flux(Grid g, int d, const double* u, const double* for
             aadd(&ub[n * g.N + cl], rho * (c1 * (l1p - l1m) + c2 * (l2p - l2m)) * bl);
             aadd(&forcesb[n * g.N + cl], 0.5 * dt * rho * bl);
         }
-        if (bh != 0.0) {
+        if (!wh && bh != 0.0) {
             HIb.p[n][f] += bh;
             aadd(&T1b.p[n][hp1], -c1 * h1p * bh);
             aadd(&T1b.p[n][hm1], c1 * h1m * bh);
@@ -461,26 +578,293 @@ __global__ void k_adj_adv_flux(Grid g, int d, const double* u, const double* for
     aadd(&Ufb.p[b2][hm2], gh2m);
 }
 
-// ---- reverse of conv = -div F: Fb_d,n(f) = (convb(c_f) - convb(c_f - e_d)) / h_d
-__global__ void k_adj_div(Grid g, const double* convb, A3 F0, A3 F1, A3 F2) {
+// ---- reverse of conv = -div F on d-faces: Fb(f) = (convb(cell above f) - convb(cell below f)) / h_d
+__global__ void k_adj_div(Grid g, int d, const double* convb, double* F0, double* F1, double* F2) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (!face3(g, t, i, j, k)) return;
-    A3* F[3] = {&F0, &F1, &F2};
+    if (!face_at(g, d, t, i, j, k)) return;
+    const bool has_hi = !(d == 2 && !g.zper && k == g.nz), has_lo = !(d == 2 && !g.zper && k == 0);
+    const long long ch = has_hi ? cidx(g, i, j, k) : 0;
+    const long long cl = has_lo ? cidx(g, wrapn(i - (d == 0), g.nx), wrapn(j - (d == 1), g.ny), g.zper ? wrapn(k - (d == 2), g.nz) : k - (d == 2)) : 0;
+    const double ih = ihd(g, d);
+    double* F[3] = {F0, F1, F2};
+    for (int n = 0; n < 3; ++n)
+        F[n][t] = ((has_hi ? convb[n * g.N + ch] : 0.0) - (has_lo ? convb[n * g.N + cl] : 0.0)) * ih;
+}
+
+// ---- tensor diffusion: the velocity seen by the flux stencil (VelDiff of the
+// forward) and its adjoint
+__device__ inline double Vd(const Grid& g, const double* v, const double* wg, int n, int i, int j, int k) {
+    i = wrapn(i, g.nx);
+    j = wrapn(j, g.ny);
+    const double* c = v + (long long)n * g.N;
+    if (g.zper) return c[cidx(g, i, j, wrapn(k, g.nz))];
+    if (k < 0) {
+        const double q0 = c[cidx(g, i, j, 0)];
+        if (n == 2) return -q0;
+        if (g.zlo == ZWALLMODEL) return q0 - wg[(long long)n * g.nx * g.ny + (long long)j * g.nx + i] * g.dz;
+        return q0;
+    }
+    if (k >= g.nz) {
+        const double q0 = c[cidx(g, i, j, g.nz - 1)];
+        return n == 2 ? -q0 : q0;
+    }
+    return c[cidx(g, i, j, k)];
+}
+__device__ inline void Vdb(const Grid& g, double* ub, double* wgb, int n, int i, int j, int k, double v) {
+    if (v == 0.0) return;
+    i = wrapn(i, g.nx);
+    j = wrapn(j, g.ny);
+    double* c = ub + (long long)n * g.N;
+    if (g.zper) {
+        atomicAdd(c + cidx(g, i, j, wrapn(k, g.nz)), v);
+        return;
+    }
+    if (k < 0) {
+        if (n == 2) {
+            atomicAdd(c + cidx(g, i, j, 0), -v);
+            return;
+        }
+        if (g.zlo == ZWALLMODEL && wgb) atomicAdd(wgb + (long long)n * g.nx * g.ny + (long long)j * g.nx + i, -v * g.dz);
+        atomicAdd(c + cidx(g, i, j, 0), v);
+        return;
+    }
+    if (k >= g.nz) {
+        atomicAdd(c + cidx(g, i, j, g.nz - 1), n == 2 ? -v : v);
+        return;
+    }
+    atomicAdd(c + cidx(g, i, j, k), v);
+}
+
+// ---- reverse of the tensor flux on d-faces and of its divergence
+// divtau(c) = sum_d (F_d(c + e_d) - F_d(c)) / h_d,  F_d = mu_f S_d(V):
+// given s * db (adjoint of divtau), accumulate into ub (velocity), mub (cell
+// viscosity; may be null) and wgb (wall-model gradient; may be null).
+__global__ void k_adj_tau(Grid g, int d, const double* vel, const double* mu, const double* wg, const double* db, double s, double* ub,
+                          double* mub, double* wgb) {
+    int i, j, k;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (!face_at(g, d, t, i, j, k)) return;
+    const int e[3] = {d == 0, d == 1, d == 2};
+    const int im = i - e[0], jm = j - e[1], km = k - e[2];
+    const bool has_hi = !(d == 2 && !g.zper && k == g.nz), has_lo = !(d == 2 && !g.zper && k == 0);
     const double ih[3] = {g.idx, g.idy, g.idz};
-    for (int d = 0; d < 3; ++d) {
-        const long long cm = cidx(g, wrapn(i - (d == 0), g.nx), wrapn(j - (d == 1), g.ny), wrapn(k - (d == 2), g.nz));
-        for (int n = 0; n < 3; ++n) F[d]->p[n][t] = (convb[n * g.N + t] - convb[n * g.N + cm]) * ih[d];
+    const long long ch = has_hi ? cidx(g, i, j, k) : 0;
+    const long long cl = has_lo ? cidx(g, wrapn(im, g.nx), wrapn(jm, g.ny), g.zper ? wrapn(km, g.nz) : km) : 0;
+    double Fb[3];
+    bool any = false;
+    for (int n = 0; n < 3; ++n) {
+        Fb[n] = s * ((has_lo ? db[n * g.N + cl] : 0.0) - (has_hi ? db[n * g.N + ch] : 0.0)) * ih[d];
+        any = any || Fb[n] != 0.0;
+    }
+    if (!any) return;
+    // face viscosity (wall faces take the adjacent cell's value)
+    double mf;
+    long long mc0 = -1, mc1 = -1;
+    if (!has_lo) {
+        mc0 = cidx(g, i, j, 0);
+        mf = mu[mc0];
+    } else if (!has_hi) {
+        mc0 = cidx(g, i, j, g.nz - 1);
+        mf = mu[mc0];
+    } else {
+        mc0 = cl;
+        mc1 = ch;
+        mf = 0.5 * (mu[cl] + mu[ch]);
+    }
+    double gr[3][3];
+    for (int n = 0; n < 3; ++n)
+        for (int m = 0; m < 3; ++m) {
+            if (m == d) {
+                gr[m][n] = (Vd(g, vel, wg, n, i, j, k) - Vd(g, vel, wg, n, im, jm, km)) * ih[m];
+            } else {
+                const int f0 = (m == 0), f1 = (m == 1), f2 = (m == 2);
+                gr[m][n] = 0.25 *
+                           (Vd(g, vel, wg, n, i + f0, j + f1, k + f2) + Vd(g, vel, wg, n, im + f0, jm + f1, km + f2) -
+                            Vd(g, vel, wg, n, i - f0, j - f1, k - f2) - Vd(g, vel, wg, n, im - f0, jm - f1, km - f2)) *
+                           ih[m];
+            }
+        }
+    const double dv = gr[0][0] + gr[1][1] + gr[2][2];
+    double mfb = 0.0;
+    double grb[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    double dvb = 0.0;
+    for (int n = 0; n < 3; ++n) {
+        const double Sn = (n == d) ? (2.0 * gr[d][d] - (2.0 / 3.0) * dv) : (gr[d][n] + gr[n][d]);
+        mfb += Fb[n] * Sn;
+        const double sb = mf * Fb[n];
+        if (n == d) {
+            grb[d][d] += 2.0 * sb;
+            dvb += -(2.0 / 3.0) * sb;
+        } else {
+            grb[d][n] += sb;
+            grb[n][d] += sb;
+        }
+    }
+    for (int m = 0; m < 3; ++m) grb[m][m] += dvb;
+    if (mub) {
+        if (mc1 < 0) aadd(&mub[mc0], mfb);
+        else {
+            aadd(&mub[mc0], 0.5 * mfb);
+            aadd(&mub[mc1], 0.5 * mfb);
+        }
+    }
+    for (int n = 0; n < 3; ++n)
+        for (int m = 0; m < 3; ++m) {
+            const double b = grb[m][n];
+            if (b == 0.0) continue;
+            if (m == d) {
+                Vdb(g, ub, wgb, n, i, j, k, b * ih[m]);
+                Vdb(g, ub, wgb, n, im, jm, km, -b * ih[m]);
+            } else {
+                const int f0 = (m == 0), f1 = (m == 1), f2 = (m == 2);
+                const double w = 0.25 * b * ih[m];
+                Vdb(g, ub, wgb, n, i + f0, j + f1, k + f2, w);
+                Vdb(g, ub, wgb, n, im + f0, jm + f1, km + f2, w);
+                Vdb(g, ub, wgb, n, i - f0, j - f1, k - f2, -w);
+                Vdb(g, ub, wgb, n, im - f0, jm - f1, km - f2, -w);
+            }
+        }
+}
+
+// ---- reverse of the Smagorinsky viscosity mu_eff = mu + rho fac |S|(u)
+__global__ void k_adj_smag(Grid g, const double* vel, const double* mub, double rho, double fac, double* ub) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= g.N) return;
+    const double mb = mub[t];
+    if (mb == 0.0) return;
+    const int i = (int)(t % g.nx);
+    const long long r = t / g.nx;
+    const int j = (int)(r % g.ny), k = (int)(r / g.ny);
+    double a = 0.5, b = 0.0, c = -0.5;
+    if (!g.zper && k == 0) {
+        a = 1.0 / 3.0;
+        b = 1.0;
+        c = -4.0 / 3.0;
+    }
+    if (!g.zper && k == g.nz - 1) {
+        a = 4.0 / 3.0;
+        b = -1.0;
+        c = -1.0 / 3.0;
+    }
+    double gx[3], gy[3], gz[3];
+    for (int n = 0; n < 3; ++n) {
+        gx[n] = 0.5 * (Q(g, vel, n, i + 1, j, k) - Q(g, vel, n, i - 1, j, k)) * g.idx;
+        gy[n] = 0.5 * (Q(g, vel, n, i, j + 1, k) - Q(g, vel, n, i, j - 1, k)) * g.idy;
+        gz[n] = (a * Q(g, vel, n, i, j, k + 1) + b * Q(g, vel, n, i, j, k) + c * Q(g, vel, n, i, j, k - 1)) * g.idz;
+    }
+    const double S = sqrt(2.0 * gx[0] * gx[0] + 2.0 * gy[1] * gy[1] + 2.0 * gz[2] * gz[2] + (gy[0] + gx[1]) * (gy[0] + gx[1]) +
+                          (gz[1] + gy[2]) * (gz[1] + gy[2]) + (gx[2] + gz[0]) * (gx[2] + gz[0]));
+    if (!(S > 0.0)) return;
+    const double q = rho * fac * mb / S;
+    double gxb[3] = {2.0 * q * gx[0], 0.0, 0.0}, gyb[3] = {0.0, 2.0 * q * gy[1], 0.0}, gzb[3] = {0.0, 0.0, 2.0 * q * gz[2]};
+    const double t1 = q * (gy[0] + gx[1]), t2 = q * (gz[1] + gy[2]), t3 = q * (gx[2] + gz[0]);
+    gyb[0] += t1;
+    gxb[1] += t1;
+    gzb[1] += t2;
+    gyb[2] += t2;
+    gxb[2] += t3;
+    gzb[0] += t3;
+    for (int n = 0; n < 3; ++n) {
+        Qb(g, ub, n, i + 1, j, k, 0.5 * g.idx * gxb[n]);
+        Qb(g, ub, n, i - 1, j, k, -0.5 * g.idx * gxb[n]);
+        Qb(g, ub, n, i, j + 1, k, 0.5 * g.idy * gyb[n]);
+        Qb(g, ub, n, i, j - 1, k, -0.5 * g.idy * gyb[n]);
+        Qb(g, ub, n, i, j, k + 1, a * g.idz * gzb[n]);
+        Qb(g, ub, n, i, j, k, b * g.idz * gzb[n]);
+        Qb(g, ub, n, i, j, k - 1, c * g.idz * gzb[n]);
     }
 }
 
-// ---- nodal projection adjoint: out = ub + G psi
+__device__ inline double block_sum(double v, double* sh) {
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    const double r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+// ---- reverse of the Moeng wall stress (k_wall_grad), local part.  wg =
+// tau rho / mu_eff of the first cell layer, tau_x = ut2 ((u - um0) vm +
+// |u_h| um0) / vm^2 (tau_y likewise with v, um1).  Accumulates the first-layer
+// velocity and viscosity adjoints and block sums of the adjoints of the plane
+// means um0, um1, vm and of ut2 = u_tau^2.
+__global__ void k_adj_wall_local(Grid g, const double* vel, const double* mueff, const double* wgb, double ut2, double um0, double um1,
+                                 double vm, double rho, double* ub, double* mub, double* parts, int np) {
+    __shared__ double sh[256];
+    const long long M = (long long)g.nx * g.ny;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < M; t += (long long)gridDim.x * blockDim.x) {
+        const double u = vel[t], v = vel[g.N + t];
+        const double ws = sqrt(u * u + v * v), iws = ws > 0.0 ? 1.0 / ws : 0.0;
+        const double m = mueff[t];
+        const double c = ut2 / (vm * vm);
+        const double tx = ((u - um0) * vm + ws * um0) * c, ty = ((v - um1) * vm + ws * um1) * c;
+        const double bx = wgb[t] * rho / m, by = wgb[M + t] * rho / m;
+        if (bx == 0.0 && by == 0.0) continue;
+        mub[t] += -(bx * tx + by * ty) / m;
+        ub[t] += bx * c * (vm + um0 * u * iws) + by * c * um1 * u * iws;
+        ub[g.N + t] += by * c * (vm + um1 * v * iws) + bx * c * um0 * v * iws;
+        s0 += bx * c * (ws - vm);
+        s1 += by * c * (ws - vm);
+        s2 += ut2 * (bx * (-(u - um0) / (vm * vm) - 2.0 * ws * um0 / (vm * vm * vm)) +
+                     by * (-(v - um1) / (vm * vm) - 2.0 * ws * um1 / (vm * vm * vm)));
+        s3 += (bx * tx + by * ty) / ut2;
+    }
+    s0 = block_sum(s0, sh);
+    s1 = block_sum(s1, sh);
+    s2 = block_sum(s2, sh);
+    s3 = block_sum(s3, sh);
+    if (threadIdx.x == 0) {
+        parts[blockIdx.x] = s0;
+        parts[np + blockIdx.x] = s1;
+        parts[2 * np + blockIdx.x] = s2;
+        parts[3 * np + blockIdx.x] = s3;
+    }
+}
+
+// plane means um0 = <u>, um1 = <v>, vm = <|u_h|> of the first layer: spread
+// their adjoints (already divided by nx ny) back to the cells
+__global__ void k_adj_wall_global(Grid g, const double* vel, double bu, double bv, double bm, double* ub) {
+    const long long M = (long long)g.nx * g.ny;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= M) return;
+    const double u = vel[t], v = vel[g.N + t];
+    const double ws = sqrt(u * u + v * v), iws = ws > 0.0 ? 1.0 / ws : 0.0;
+    ub[t] += bu + bm * u * iws;
+    ub[g.N + t] += bv + bm * v * iws;
+}
+
+// ---- reverse of the Coriolis source src = rho (C u): u_bar += rho C^T src_bar
+__global__ void k_adj_coriolis(Grid g, const double* srcb, Scalars s, double* ub) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= g.N) return;
+    const long long N = g.N;
+    double fb[3];
+    for (int n = 0; n < 3; ++n) fb[n] = s.rho * srcb[n * N + t];
+    const double aeb = fb[0] * s.east[0] + fb[1] * s.east[1] + fb[2] * s.east[2];
+    const double anb = fb[0] * s.north[0] + fb[1] * s.north[1] + fb[2] * s.north[2];
+    const double aub = fb[0] * s.up[0] + fb[1] * s.up[1] + fb[2] * s.up[2];
+    const double unb = s.corfac * s.sinphi * aeb;
+    const double uub = -s.hfac * s.corfac * s.cosphi * aeb;
+    const double ueb = -s.corfac * s.sinphi * anb + s.hfac * s.corfac * s.cosphi * aub;
+    for (int n = 0; n < 3; ++n) ub[n * N + t] += ueb * s.east[n] + unb * s.north[n] + uub * s.up[n];
+}
+
+// ---- nodal projection adjoint: out = ub + Gn psi
 __global__ void k_adj_nodal_post(Grid g, const double* psi, const double* ub, double* out) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= g.N) return;
-    int i, j, k;
-    face3(g, t, i, j, k);
-    auto P = [&](int a, int b, int c) { return psi[cidx(g, wrapn(a, g.nx), wrapn(b, g.ny), wrapn(c, g.nz))]; };
+    const int i = (int)(t % g.nx);
+    const long long r = t / g.nx;
+    const int j = (int)(r % g.ny), k = (int)(r / g.ny);
+    auto P = [&](int a, int b, int c) {
+        return psi[((long long)(g.zper ? wrapn(c, g.nz) : c) * g.ny + wrapn(b, g.ny)) * g.nx + wrapn(a, g.nx)];
+    };
     double gx = 0, gy = 0, gz = 0;
     for (int c = 0; c < 2; ++c)
         for (int b = 0; b < 2; ++b) {
@@ -502,10 +886,12 @@ __global__ void k_axpby(long long n, double a, const double* x, double b, const 
 // objective: J = (1/M) sum_box 0.5 |u|^2 ; its gradient u/M in the box
 __global__ void k_objective(Grid g, const double* u, int lo0, int lo1, int lo2, int hi0, int hi1, int hi2, double invM, double* ub,
                             double* parts) {
+    __shared__ double sh[256];
     double s = 0.0;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < g.N; t += (long long)gridDim.x * blockDim.x) {
-        int i, j, k;
-        face3(g, t, i, j, k);
+        const int i = (int)(t % g.nx);
+        const long long r = t / g.nx;
+        const int j = (int)(r % g.ny), k = (int)(r / g.ny);
         const bool in = i >= lo0 && i <= hi0 && j >= lo1 && j <= hi1 && k >= lo2 && k <= hi2;
         for (int n = 0; n < 3; ++n) {
             const double v = u[n * g.N + t];
@@ -513,24 +899,18 @@ __global__ void k_objective(Grid g, const double* u, int lo0, int lo1, int lo2, 
             if (ub) ub[n * g.N + t] = in ? v * invM : 0.0;
         }
     }
-    __shared__ double sh[256];
-    sh[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) parts[blockIdx.x] = sh[0] * invM;
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) parts[blockIdx.x] = s * invM;
 }
 
 // disk adjoint: partial sums over the cut-off box of  sum_x (actb(x) . n) B(x),
 // B(x) = sum_points w_p g3(x - p) with the per-point weights w_p in pts[4p+3]
 __global__ void k_act_adj_dot(Grid g, const double* actb, const double* pts, int npts, double ax0, double ax1, double ax2, double eps, double x0,
                               double y0, double z0, int lo0, int lo1, int lo2, int n0, int n1, int n2, double* parts) {
+    __shared__ double sh[256];
     double acc = 0.0;
     const long long M = (long long)n0 * n1 * n2;
     const double gfac = 0.17958712212516656 / (eps * eps * eps);
-    const double ie = 1.0 / eps;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < M; t += (long long)gridDim.x * blockDim.x) {
         const int a = (int)(t % n0);
         const long long r = t / n0;
@@ -539,45 +919,42 @@ __global__ void k_act_adj_dot(Grid g, const double* actb, const double* pts, int
         const double x = x0 + (i + 0.5) * g.dx, y = y0 + (j + 0.5) * g.dy, z = z0 + (k + 0.5) * g.dz;
         double s = 0;
         for (int m = 0; m < npts; ++m) {
-            const double rx = (pts[4 * m] - x) * ie, ry = (pts[4 * m + 1] - y) * ie, rz = (pts[4 * m + 2] - z) * ie;
+            const double rx = (pts[4 * m] - x) / eps, ry = (pts[4 * m + 1] - y) / eps, rz = (pts[4 * m + 2] - z) / eps;
             const double r2 = rx * rx + ry * ry + rz * rz;
-            if (r2 < 16.0) s += gfac * exp(-r2) * pts[4 * m + 3];
+            if (r2 < 16.0) s += gfac * exp(-rx * rx - ry * ry - rz * rz) * pts[4 * m + 3];
         }
         const long long cc = cidx(g, i, j, k);
         acc += s * (actb[cc] * ax0 + actb[g.N + cc] * ax1 + actb[2 * g.N + cc] * ax2);
     }
-    __shared__ double sh[256];
-    sh[threadIdx.x] = acc;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) parts[blockIdx.x] = sh[0];
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) parts[blockIdx.x] = acc;
 }
 
 // scatter of the sampled-velocity adjoint to the trilinear corners
 __global__ void k_act_sample_adj(Grid g, const double* pts, const double* wb, int npts, double x0, double y0, double z0, double* ub) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npts) return;
-    const double fx = (pts[3 * p] - x0 - 0.5 * g.dx) * g.idx;
-    const double fy = (pts[3 * p + 1] - y0 - 0.5 * g.dy) * g.idy;
-    const double fz = (pts[3 * p + 2] - z0 - 0.5 * g.dz) * g.idz;
+    const double fx = (pts[3 * p] - x0 - 0.5 * g.dx) / g.dx;
+    const double fy = (pts[3 * p + 1] - y0 - 0.5 * g.dy) / g.dy;
+    const double fz = (pts[3 * p + 2] - z0 - 0.5 * g.dz) / g.dz;
     const int i = (int)floor(fx), j = (int)floor(fy), k = (int)floor(fz);
     const double wx = fx - i, wy = fy - j, wz = fz - k;
     for (int c = 0; c < 2; ++c)
         for (int b = 0; b < 2; ++b)
             for (int a = 0; a < 2; ++a) {
                 const double w = (a ? wx : 1 - wx) * (b ? wy : 1 - wy) * (c ? wz : 1 - wz);
-                for (int n = 0; n < 3; ++n) aadd(Ub(g, ub, n, i + a, j + b, k + c), w * wb[3 * p + n]);
+                for (int n = 0; n < 3; ++n) Qb(g, ub, n, i + a, j + b, k + c, w * wb[3 * p + n]);
             }
 }
 
 }  // namespace
 
 // ---------------------------------------------------------------- launchers
+constexpr double B8 = 8.0;
+
 void launch_adj_edges(Ctx& c, const Grid& g, int d, const double* u, double* const Eb[3], double* ub) {
-    KS_LAUNCH(c, k_adj_edges, nblocks(g.N, BS), BS, 8.0 * 7 * g.N, g, d, u, Eb[0], Eb[1], Eb[2], ub);
+    const long long nf = nfaces(g, d);
+    KS_LAUNCH(c, k_adj_edges, nblocks(nf, BS), BS, B8 * (3.0 * nf + 6.0 * g.N), g, d, u, Eb[0], Eb[1], Eb[2], ub);
 }
 void launch_adj_faces(Ctx& c, const Grid& g, int d, int mode, const double* u, const GodunovBufs& B, const AdjBufs& A, double dt, double rho,
                       const double* umac_d) {
@@ -587,26 +964,29 @@ void launch_adj_faces(Ctx& c, const Grid& g, int d, int mode, const double* u, c
     K3 TEb{{A.tedge[d][0], A.tedge[d][1], A.tedge[d][2]}};
     A3 Eb{{A.edge[d][0], A.edge[d][1], A.edge[d][2]}};
     const double s = dt * ihd(g, d);
+    const long long nf = nfaces(g, d);
     if (mode == 0)
-        KS_LAUNCH(c, k_adj_faces<0>, nblocks(g.N, BS), BS, 8.0 * 30 * g.N, g, d, u, E, s, rho, nullptr, LO, HI, (const double*)B.ad[d], LOb,
-                  HIb, A.ad[d], TEb, Eb, A.u, nullptr);
+        KS_LAUNCH(c, k_adj_faces<0>, nblocks(nf, BS), BS, B8 * (6.0 * g.N + 17.0 * nf), g, d, u, E, s, rho, nullptr, LO, HI,
+                  (const double*)B.ad[d], LOb, HIb, A.ad[d], TEb, Eb, A.u, nullptr);
     else
-        KS_LAUNCH(c, k_adj_faces<1>, nblocks(g.N, BS), BS, 8.0 * 30 * g.N, g, d, u, E, s, rho, umac_d, LO, HI, nullptr, LOb, HIb, nullptr, TEb,
-                  Eb, A.u, A.umac[d]);
+        KS_LAUNCH(c, k_adj_faces<1>, nblocks(nf, BS), BS, B8 * (6.0 * g.N + 18.0 * nf), g, d, u, E, s, rho, umac_d, LO, HI, nullptr, LOb, HIb,
+                  nullptr, TEb, Eb, A.u, A.umac[d]);
 }
 void launch_adj_pm_trans(Ctx& c, const Grid& g, int a, int b, int n, double dt, const GodunovBufs& B, const AdjBufs& A) {
     const double cb = dt / (6.0 * hd(g, b));
-    KS_LAUNCH(c, k_adj_pm_trans, nblocks(g.N, BS), BS, 8.0 * 10 * g.N, g, a, b, cb, (const double*)B.ad[a], (const double*)B.ad[b],
-              (const double*)B.tedge[b][n], (const double*)B.lo[a][n], (const double*)B.hi[a][n], A.tr[a][b][0], A.lo[a][n], A.hi[a][n], A.ad[b],
-              A.tedge[b][n]);
+    const long long na = nfaces(g, a), nb = nfaces(g, b);
+    KS_LAUNCH(c, k_adj_pm_trans, nblocks(na, BS), BS, B8 * (4.0 * na + 4.0 * nb), g, a, b, n, cb, (const double*)B.ad[a],
+              (const double*)B.ad[b], (const double*)B.tedge[b][n], A.tr[a][b][0], A.lo[a][n], A.hi[a][n], A.ad[b], A.tedge[b][n]);
 }
 void launch_adj_pm_final(Ctx& c, const Grid& g, int d, double dt, const GodunovBufs& B, const double* forces, const AdjBufs& A) {
     const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
     K3 AD{{(double*)B.ad[0], (double*)B.ad[1], (double*)B.ad[2]}};
     A3 ADb{{A.ad[0], A.ad[1], A.ad[2]}};
-    KS_LAUNCH(c, k_adj_pm_final, nblocks(g.N, BS), BS, 8.0 * 14 * g.N, g, d, dt, dt / (4.0 * hd(g, b1)), dt / (4.0 * hd(g, b2)),
-              (const double*)B.lo[d][d], (const double*)B.hi[d][d], AD, (const double*)B.tr[b1][b2][0], (const double*)B.tr[b2][b1][0], forces,
-              A.umac[d], A.lo[d][d], A.hi[d][d], ADb, A.tr[b1][b2][0], A.tr[b2][b1][0], A.forces);
+    const long long nf = nfaces(g, d);
+    KS_LAUNCH(c, k_adj_pm_final, nblocks(nf, BS), BS, B8 * (2.0 * g.N + 5.0 * nf + 8.0 * (nfaces(g, b1) + nfaces(g, b2)) / 2.0), g, d, dt,
+              dt / (4.0 * hd(g, b1)), dt / (4.0 * hd(g, b2)), (const double*)B.lo[d][d], (const double*)B.hi[d][d], AD,
+              (const double*)B.tr[b1][b2][0], (const double*)B.tr[b2][b1][0], forces, A.umac[d], A.lo[d][d], A.hi[d][d], ADb, A.tr[b1][b2][0],
+              A.tr[b2][b1][0], A.forces);
 }
 void launch_adj_adv_trans(Ctx& c, const Grid& g, int a, int b, const double* u, double rho, double dt, const double* const mac[3],
                           const GodunovBufs& B, const AdjBufs& A) {
@@ -614,8 +994,9 @@ void launch_adj_adv_trans(Ctx& c, const Grid& g, int a, int b, const double* u, 
     K3 Ob{{A.tr[a][b][0], A.tr[a][b][1], A.tr[a][b][2]}};
     A3 LOb{{A.lo[a][0], A.lo[a][1], A.lo[a][2]}}, HIb{{A.hi[a][0], A.hi[a][1], A.hi[a][2]}};
     A3 Ebb{{A.tedge[b][0], A.tedge[b][1], A.tedge[b][2]}};
-    KS_LAUNCH(c, k_adj_adv_trans, nblocks(g.N, BS), BS, 8.0 * 24 * g.N, g, a, b, u, rho, dt / (3.0 * hd(g, b)), mac[a], mac[b], E, Ob, LOb, HIb,
-              Ebb, A.umac[b], A.u);
+    const long long na = nfaces(g, a), nb = nfaces(g, b);
+    KS_LAUNCH(c, k_adj_adv_trans, nblocks(na, BS), BS, B8 * (6.0 * g.N + 10.0 * na + 8.0 * nb), g, a, b, u, rho, dt / (3.0 * hd(g, b)), mac[a],
+              mac[b], E, Ob, LOb, HIb, Ebb, A.umac[b], A.u);
 }
 void launch_adj_adv_flux(Ctx& c, const Grid& g, int d, const double* u, const double* forces, double rho, double dt, const double* const mac[3],
                          const GodunovBufs& B, const AdjBufs& A) {
@@ -628,33 +1009,58 @@ void launch_adj_adv_flux(Ctx& c, const Grid& g, int d, const double* u, const do
     A3 Ufb{{A.umac[0], A.umac[1], A.umac[2]}};
     A3 LOb{{A.lo[d][0], A.lo[d][1], A.lo[d][2]}}, HIb{{A.hi[d][0], A.hi[d][1], A.hi[d][2]}};
     A3 T1b{{A.tr[b1][b2][0], A.tr[b1][b2][1], A.tr[b1][b2][2]}}, T2b{{A.tr[b2][b1][0], A.tr[b2][b1][1], A.tr[b2][b1][2]}};
-    KS_LAUNCH(c, k_adj_adv_flux, nblocks(g.N, BS), BS, 8.0 * 40 * g.N, g, d, u, forces, rho, dt, dt / (2.0 * hd(g, b1)), dt / (2.0 * hd(g, b2)),
-              Uf, LO, HI, T1, T2, Fb, Ufb, LOb, HIb, T1b, T2b, A.u, A.forces);
+    const long long nf = nfaces(g, d);
+    KS_LAUNCH(c, k_adj_adv_flux, nblocks(nf, BS), BS, B8 * (12.0 * g.N + 14.0 * nf + 14.0 * (nfaces(g, b1) + nfaces(g, b2))), g, d, u, forces,
+              rho, dt, dt / (2.0 * hd(g, b1)), dt / (2.0 * hd(g, b2)), Uf, LO, HI, T1, T2, Fb, Ufb, LOb, HIb, T1b, T2b, A.u, A.forces);
 }
 void launch_adj_div(Ctx& c, const Grid& g, const double* convb, const AdjBufs& A) {
-    A3 F0{{A.flux[0][0], A.flux[0][1], A.flux[0][2]}}, F1{{A.flux[1][0], A.flux[1][1], A.flux[1][2]}},
-        F2{{A.flux[2][0], A.flux[2][1], A.flux[2][2]}};
-    KS_LAUNCH(c, k_adj_div, nblocks(g.N, BS), BS, 8.0 * 15 * g.N, g, convb, F0, F1, F2);
+    for (int d = 0; d < 3; ++d) {
+        const long long nf = nfaces(g, d);
+        KS_LAUNCH(c, k_adj_div, nblocks(nf, BS), BS, B8 * (3.0 * g.N + 3.0 * nf), g, d, convb, A.flux[d][0], A.flux[d][1], A.flux[d][2]);
+    }
+}
+void launch_adj_tau(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, const double* divtau_b, double s, double* ub,
+                    double* mub, double* wgb) {
+    for (int d = 0; d < 3; ++d) {
+        const long long nf = nfaces(g, d);
+        KS_LAUNCH(c, k_adj_tau, nblocks(nf, BS), BS, B8 * 10.0 * g.N, g, d, vel, mueff, wg, divtau_b, s, ub, mub, wgb);
+    }
+}
+void launch_adj_smag(Ctx& c, const Grid& g, const double* vel, const double* mub, const Scalars& s, double* ub) {
+    KS_LAUNCH(c, k_adj_smag, nblocks(g.N, BS), BS, B8 * 7.0 * g.N, g, vel, mub, s.rho, s.smag_fac, ub);
+}
+void launch_adj_wall_local(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wgb, double ut2, double um0, double um1,
+                           double vm, double rho, double* ub, double* mub, double* parts, int* np) {
+    const long long M = (long long)g.nx * g.ny;
+    *np = (int)std::min<long long>(1216, (M + 255) / 256);
+    KS_LAUNCH(c, k_adj_wall_local, *np, 256, B8 * 9.0 * M, g, vel, mueff, wgb, ut2, um0, um1, vm, rho, ub, mub, parts, *np);
+}
+void launch_adj_wall_global(Ctx& c, const Grid& g, const double* vel, double bu, double bv, double bm, double* ub) {
+    const long long M = (long long)g.nx * g.ny;
+    KS_LAUNCH(c, k_adj_wall_global, nblocks(M, BS), BS, B8 * 6.0 * M, g, vel, bu, bv, bm, ub);
+}
+void launch_adj_coriolis(Ctx& c, const Grid& g, const double* srcb, const Scalars& s, double* ub) {
+    KS_LAUNCH(c, k_adj_coriolis, nblocks(g.N, BS), BS, B8 * 9.0 * g.N, g, srcb, s, ub);
 }
 void launch_adj_nodal_post(Ctx& c, const Grid& g, const double* psi, const double* ub, double* out) {
-    KS_LAUNCH(c, k_adj_nodal_post, nblocks(g.N, BS), BS, 8.0 * 7 * g.N, g, psi, ub, out);
+    KS_LAUNCH(c, k_adj_nodal_post, nblocks(g.N, BS), BS, B8 * 7.0 * g.N, g, psi, ub, out);
 }
 void launch_axpby(Ctx& c, long long n, double a, const double* x, double b, const double* y, double* out) {
-    KS_LAUNCH(c, k_axpby, nblocks(n, BS), BS, 24.0 * n, n, a, x, b, y, out);
+    KS_LAUNCH(c, k_axpby, nblocks(n, BS), BS, B8 * 3.0 * n, n, a, x, b, y, out);
 }
 void launch_objective(Ctx& c, const Grid& g, const double* u, const int lo[3], const int hi[3], double invM, double* ub, double* parts, int* np) {
     *np = 1216;
-    KS_LAUNCH(c, k_objective, *np, 256, 8.0 * 6 * g.N, g, u, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], invM, ub, parts);
+    KS_LAUNCH(c, k_objective, *np, 256, B8 * 6.0 * g.N, g, u, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], invM, ub, parts);
 }
 void launch_act_adj_dot(Ctx& c, const Grid& g, const double* actb, const double* pts, int npts, const double ax[3], double eps, const double plo[3],
                         const int lo[3], const int hi[3], double* parts, int* np) {
     const int n0 = hi[0] - lo[0] + 1, n1 = hi[1] - lo[1] + 1, n2 = hi[2] - lo[2] + 1;
     *np = 1216;
-    KS_LAUNCH(c, k_act_adj_dot, *np, 256, 8.0 * 3 * n0 * n1 * n2, g, actb, pts, npts, ax[0], ax[1], ax[2], eps, plo[0], plo[1], plo[2], lo[0], lo[1],
-              lo[2], n0, n1, n2, parts);
+    KS_LAUNCH(c, k_act_adj_dot, *np, 256, B8 * 3.0 * n0 * n1 * n2, g, actb, pts, npts, ax[0], ax[1], ax[2], eps, plo[0], plo[1], plo[2], lo[0],
+              lo[1], lo[2], n0, n1, n2, parts);
 }
 void launch_act_sample_adj(Ctx& c, const Grid& g, const double* pts, const double* wb, int npts, const double plo[3], double* ub) {
-    KS_LAUNCH(c, k_act_sample_adj, nblocks(npts, 64), 64, 8.0 * 30 * npts, g, pts, wb, npts, plo[0], plo[1], plo[2], ub);
+    KS_LAUNCH(c, k_act_sample_adj, nblocks(npts, 64), 64, B8 * 30.0 * npts, g, pts, wb, npts, plo[0], plo[1], plo[2], ub);
 }
 
 }  // namespace ks

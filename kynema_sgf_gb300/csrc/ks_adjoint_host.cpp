@@ -2,23 +2,25 @@
 // binomial (revolve-type) checkpointed reverse sweep over many steps.
 //
 // The reference has no adjoint; this is the differentiated form of the same
-// single-level step (incflo::advance, src/incflo_advance.cpp:63-438) for the
-// configuration in which every pass is differentiable: triply periodic,
-// laminar (constant viscosity), fixed dt, UniformCtDisk actuators with a
-// single thrust coefficient, and constant or actuator momentum sources.
+// single-level step (incflo::advance, src/incflo_advance.cpp:63-438) for a
+// fixed dt: every pass of the path (periodic or wall-bounded z, laminar or
+// Smagorinsky viscosity, Moeng wall model, geostrophic / Coriolis / body /
+// actuator sources, UniformCtDisk actuators with a single thrust coefficient).
 //
 // Step n maps (u, gp) -> (u', gp'):
+//   mu    = mu0 + rho Cs^2 D^2 |S(u)|;  wg = W(u_1, <u_1>, u_tau(<|u_1|>), mu)
 //   act   = sum_d 0.5 ct_d (s_d . a_d)^2 B_d a_d,  s_d = sum_p w_p u(x_p)
-//   src   = -gp + rho (act + const);  dold = L u;  forces = (src + dold)/rho
+//   src   = -gp + rho (C u + act + const);  dold = L(u; mu, wg)
+//   forces = (src + dold)/rho
 //   mac   = P_mac PREMAC(u, forces);  conv = ADV(u, mac, forces)
 //   v*    = u + dt/rho (conv + src + dold)
-//   v**   = v* + dt/(2 rho) (L v* - dold)
+//   v**   = v* + dt/(2 rho) (L(v*; mu, wg) - dold)
 //   v     = v** + sigma gp,  sigma = dt/rho
 //   phi   = (sigma A)^-1 Dn v;  u' = v - sigma Gn phi;  gp' = Gn phi
-// L (constant-viscosity tensor diffusion) and P_mac are symmetric on
-// periodic grids; Gn^T = -Dn for the nodal pair, so the nodal adjoint is one
-// more solve with A: sigma A psi = Dn(gp_bar - sigma u_bar),
-// v_bar = u_bar + Gn psi.  PREMAC and ADV are reversed by the kernels of
+// P_mac is symmetric on the faces it changes; Gn^T = -Dn for the nodal pair
+// (the wall rows of both carry the same half weight), so the nodal adjoint is
+// one more solve with A: sigma A psi = Dn(gp_bar - sigma u_bar),
+// v_bar = u_bar + Gn psi.  The other passes are reversed by the kernels of
 // ks_adjoint.cu at the forward linearisation point, recomputed from the
 // checkpointed (u, gp) in FP64.
 #include "ks_sim.hpp"
@@ -26,10 +28,8 @@
 namespace ks {
 
 void Sim::adj_check() const {
-    if (!g_.zper) throw KsError(KS_ERR_UNSUPPORTED, "the adjoint needs a triply periodic domain");
-    if (S_.smag) throw KsError(KS_ERR_UNSUPPORTED, "the adjoint needs turbulence.model = laminar");
-    if (S_.cor) throw KsError(KS_ERR_UNSUPPORTED, "the adjoint does not include CoriolisForcing");
     if (t_.adaptive) throw KsError(KS_ERR_UNSUPPORTED, "the adjoint needs a fixed time step (time.fixed_dt > 0)");
+    if (wallmodel_ && shear_ != 0) throw KsError(KS_ERR_UNSUPPORTED, "the adjoint's wall model is ABL.wall_shear_stress_type = moeng");
     for (auto& d : disks_)
         if (d.ct.size() != 1) throw KsError(KS_ERR_UNSUPPORTED, "the adjoint needs a single thrust_coeff value per disk");
 }
@@ -71,6 +71,8 @@ void Sim::adj_alloc() {
     A.u = S->ub.p;
     for (auto* b : {&S->w, &S->t1, &S->t2, &S->srcb, &S->doldb, &S->su, &S->sgp}) b->alloc(N3);
     S->sp.alloc(p_.n);
+    S->mub.alloc(N);
+    S->wgb.alloc(2 * (size_t)g_.nx * g_.ny);
     S->macs.alloc(2 * N + NF);
     size_t maxpts = 1;
     for (auto& d : disks_) maxpts = std::max(maxpts, (size_t)d.nr * d.nt);
@@ -130,8 +132,7 @@ double Sim::objective(bool seed) {
 // One forward step from the current state with the step's dt, without the
 // clock (dt is fixed in the differentiable configuration).
 void Sim::forward_core() {
-    t_.next = t_.cur + t_.dt[0];
-    actuator_update();
+    pre_advance();
     prepare_time_step();
     apply_predictor(false);
 }
@@ -205,16 +206,20 @@ void Sim::adjoint_step_impl(bool seed) {
     AdjBufs& A = S.A;
     const long long N3 = 3 * g_.N;
     const double dt = t_.dt[0], sigma = dt / rho_, dr = dt / rho_;
-    struct Restore {  // precision and clock, also when a solve throws
+    struct Restore {  // Godunov precision and clock, also when a solve throws
         Sim& s;
-        int mixed;
         Clock clock;
         ~Restore() {
-            s.mixed_ = mixed;
+            s.godunov64_ = 0;
             s.t_ = clock;
         }
-    } restore{*this, mixed_, t_};
-    mixed_ = 0;  // the linearisation point is recomputed in FP64
+    } restore{*this, t_};
+    // The linearisation point is recomputed with FP64 Godunov passes (the
+    // reverse kernels read their FP64 intermediates).  A mixed-precision
+    // handle keeps its FP32 multigrid cycles: the FP64 defect correction
+    // brings both projections to the FP64 tolerance, here and in the two
+    // reverse solves.
+    godunov64_ = 1;
     launch_copy(ctx_, S.su.p, vel_.p, N3);
     launch_copy(ctx_, S.sgp.p, gp_.p, N3);
     launch_copy(ctx_, S.sp.p, p_.p, (long long)p_.n);
@@ -232,17 +237,19 @@ void Sim::adjoint_step_impl(bool seed) {
     }
     double* ub = S.ub.p;
     double* gpb = S.gpb.p;
-    double* fl[9];
-    for (int m = 0; m < 9; ++m) fl[m] = static_cast<double*>(gb_.flux[m / 3][m % 3]);  // forward fluxes are not read again
 
+    double* mub = S_.smag ? S.mub.p : nullptr;
+    double* wgb = wallmodel_ ? S.wgb.p : nullptr;
+    launch_fill(ctx_, S.mub.p, 0.0, g_.N);
+    launch_fill(ctx_, S.wgb.p, 0.0, 2LL * g_.nx * g_.ny);
     // ---- nodal projection: sigma A psi = Dn(gp_bar - sigma u_bar); v_bar = u_bar + Gn psi
     launch_axpby(ctx_, N3, 1.0, gpb, -sigma, ub, S.w.p);
     nd_rhs(S.w.p);
     nd_solve(sigma);
     launch_adj_nodal_post(ctx_, g_, nd_[0].phi, ub, S.t1.p);  // t1 = v_bar = adjoint of v**
-    // ---- v** = v* + dt/(2 rho) (L v* - dold)
-    launch_divtau(ctx_, g_, S.t1.p, mueff_.p, wg_.p, S.t2.p, 0, nullptr, nullptr, nullptr, nullptr, dt, rho_, fl);
-    launch_axpby(ctx_, N3, 1.0, S.t1.p, 0.5 * dr, S.t2.p, ub);            // ub = v*_bar (u_bar accumulates from here)
+    // ---- v** = v* + dt/(2 rho) (L(v*) - dold); vel_tmp_ still holds v*
+    launch_copy(ctx_, ub, S.t1.p, N3);
+    launch_adj_tau(ctx_, g_, vel_tmp_.p, mueff_.p, wg_.p, S.t1.p, 0.5 * dr, ub, mub, wgb);  // ub = v*_bar
     launch_axpby(ctx_, N3, -0.5 * dr, S.t1.p, dr, ub, S.doldb.p);         // dold_bar
     launch_axpby(ctx_, N3, sigma, S.t1.p, 0.0, S.t1.p, gpb);              // gp_bar = sigma v_bar (v = v** + sigma gp)
     launch_axpby(ctx_, N3, dr, ub, 0.0, ub, S.srcb.p);                    // src_bar = conv_bar = dt/rho v*_bar
@@ -257,7 +264,13 @@ void Sim::adjoint_step_impl(bool seed) {
         for (int b = 0; b < 3; ++b)
             if (a != b) launch_adj_adv_trans(ctx_, g_, a, b, vel_old_.p, rho_, dt, mac, gb_, A);
     for (int a = 0; a < 3; ++a) launch_adj_faces(ctx_, g_, a, 1, vel_old_.p, gb_, A, dt, rho_, umac_[a].p);
-    // ---- MAC projection (symmetric): umac_bar <- P umac_bar
+    // ---- MAC projection (symmetric on the faces it changes): the pre-MAC
+    // output on wall faces is 0 whatever the input, so their adjoint is dropped
+    if (!g_.zper) {
+        const size_t layer = (size_t)g_.nx * g_.ny;
+        ck(cudaMemsetAsync(A.umac[2], 0, layer * sizeof(double), ctx_.stream), "memset");
+        ck(cudaMemsetAsync(A.umac[2] + (size_t)g_.nz * layer, 0, layer * sizeof(double), ctx_.stream), "memset");
+    }
     {
         struct Swap {  // the MAC solver works on umac_; swap back even if it throws
             DevBuf<double>* f;
@@ -294,12 +307,24 @@ void Sim::adjoint_step_impl(bool seed) {
     // ---- forces = (src + dold)/rho
     launch_axpby(ctx_, N3, 1.0, S.srcb.p, 1.0 / rho_, A.forces, S.srcb.p);
     launch_axpby(ctx_, N3, 1.0, S.doldb.p, 1.0 / rho_, A.forces, S.doldb.p);
-    // ---- dold = L u
-    launch_divtau(ctx_, g_, S.doldb.p, mueff_.p, wg_.p, S.t2.p, 0, nullptr, nullptr, nullptr, nullptr, dt, rho_, fl);
-    launch_axpby(ctx_, N3, 1.0, ub, 1.0, S.t2.p, ub);
-    // ---- src = -gp + rho (act + const)
+    // ---- dold = L(u; mu_eff, wg)
+    launch_adj_tau(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, S.doldb.p, 1.0, ub, mub, wgb);
+    // ---- src = -gp + rho (Coriolis(u) + act + const)
     launch_axpby(ctx_, N3, 1.0, gpb, -1.0, S.srcb.p, gpb);
+    if (S_.cor) launch_adj_coriolis(ctx_, g_, S.srcb.p, S_, ub);
     adjoint_disks(S.srcb.p);
+    // ---- wall model: wg(u first layer, plane means, u_tau, mu_eff)
+    if (wallmodel_) {
+        int np = 0;
+        launch_adj_wall_local(ctx_, g_, vel_old_.p, mueff_.p, S.wgb.p, utau_ * utau_, um_[0], um_[1], vmag_, rho_, ub, S.mub.p, parts_.p, &np);
+        double b[4];
+        reduce(np, 4, 0, b);
+        const double M = (double)g_.nx * g_.ny;
+        const double vmb = b[2] + b[3] * 2.0 * utau_ * utau_ / vmag_;  // u_tau^2 = (kappa vm / ln(zref/z0))^2
+        launch_adj_wall_global(ctx_, g_, vel_old_.p, b[0] / M, b[1] / M, vmb / M, ub);
+    }
+    // ---- Smagorinsky: mu_eff(u)
+    if (S_.smag) launch_adj_smag(ctx_, g_, vel_old_.p, S.mub.p, S_, ub);
     // ---- back to x^n
     launch_copy(ctx_, vel_.p, S.su.p, N3);
     launch_copy(ctx_, gp_.p, S.sgp.p, N3);

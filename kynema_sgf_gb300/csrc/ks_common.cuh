@@ -93,4 +93,8 @@ using CellFO = CellFOT<double>;
 
 inline unsigned nblocks(long long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
+// max that keeps a NaN operand (fmax drops it): a non-finite residual or CFL
+// maximum must reach the host's finiteness checks
+__host__ __device__ inline double nmax(double a, double b) { return (a != a || b != b) ? a + b : (a > b ? a : b); }
+
 }  // namespace ks

@@ -216,6 +216,31 @@ void Sim::setup(const Deck& D) {
     }
 }
 
+// Weighted-Jacobi weight of the nodal smoother.  The largest eigenvalue of
+// D^-1 A for the Q1 stencil lies at a corner of the frequency cube; it is 1.5
+// on isotropic cells (omega 0.9 gives omega * lambda_max = 1.35) and grows with
+// the cell aspect ratio (3.0 at dz = dx / 2, where omega = 0.9 diverges).  The
+// weight is reduced so that omega * lambda_max stays at 1.35.  All levels have
+// the same aspect ratio, so the finest level's stencil decides.
+static double nodal_jacobi_weight(const double* W, double omega) {
+    double lmax = 0.0;
+    for (int m = 1; m < 8; ++m) {
+        double A = 0.0;
+        for (int c = 0; c < 3; ++c)
+            for (int b = 0; b < 3; ++b)
+                for (int a = 0; a < 3; ++a) {
+                    double f = 1.0;
+                    if ((m & 1) && a != 1) f = -f;
+                    if ((m & 2) && b != 1) f = -f;
+                    if ((m & 4) && c != 1) f = -f;
+                    A += W[(c * 3 + b) * 3 + a] * f;
+                }
+        lmax = std::max(lmax, A / W[13]);
+    }
+    if (omega * lmax > 1.35 * (1.0 + 1e-9)) omega = 1.35 / lmax;
+    return omega;
+}
+
 // ---------------------------------------------------------------- allocation
 void Sim::alloc() {
     const size_t N = (size_t)g_.N, NF = (size_t)g_.NFz;
@@ -300,6 +325,7 @@ void Sim::alloc() {
         nd_.push_back(Nd);
         for (int d = 0; d < 3; ++d) h[d] *= 2;
     }
+    nod_.omega = nodal_jacobi_weight(nd_[0].W, nod_.omega);
     parts_.alloc(4 * 1216);
     red_.alloc(8);
     size_t maxpts = 1;
@@ -572,6 +598,8 @@ void Sim::mac_project() {
         ++it;
         if (!std::isfinite(rn)) throw KsError(KS_ERR_NONFINITE, "MAC projection diverged");
     }
+    // MLMG aborts when maxiter is reached above the tolerance (MLMG::solve)
+    if (rn > target) throw KsError(KS_ERR_NOT_CONVERGED, "MAC projection did not converge in mac_proj.maxiter V-cycles");
     mac_it_ = it;
     mac_r_ = rn;
     launch_mac_correct(ctx_, g_, L.phi, umac_[0].p, umac_[1].p, umac_[2].p, beta);
@@ -655,6 +683,7 @@ void Sim::nd_solve(double sigma) {
             ++it;
         }
     }
+    if (rn > target) throw KsError(KS_ERR_NOT_CONVERGED, "nodal projection did not converge in nodal_proj.maxiter V-cycles");
     nod_it_ = it;
     nod_r_ = rn;
 }
@@ -679,10 +708,11 @@ void Sim::apply_predictor(bool incremental) {
     for (int m = 0; m < 9; ++m) fl[m] = static_cast<double*>(gb_.flux[m / 3][m % 3]);
     launch_divtau(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, divtau_.p, 1, src_.p, forces_.p, nullptr, nullptr, dt, rho_, fl);
     double* mac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
-    launch_premac(ctx_, g_, vel_old_.p, forces_.p, dt, gb_, mac, mixed_);
+    const int g32 = mixed_ && !godunov64_;
+    launch_premac(ctx_, g_, vel_old_.p, forces_.p, dt, gb_, mac, g32);
     mac_project();
     const double* cmac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
-    launch_advection(ctx_, g_, vel_old_.p, forces_.p, cmac, dt, rho_, gb_, conv_.p, mixed_);
+    launch_advection(ctx_, g_, vel_old_.p, forces_.p, cmac, dt, rho_, gb_, conv_.p, g32);
     // compute_source_term(NPH) and compute_diffusion_term(Old) reproduce src
     // and divtau on this path (Coriolis reads the Old velocity, gp unchanged).
     launch_predictor_rhs(ctx_, g_, vel_old_.p, conv_.p, src_.p, divtau_.p, vel_.p, dt, rho_);
@@ -832,6 +862,7 @@ double Sim::scalar(const std::string& n) {
         return reduce(np, 1, 0, nullptr) / (double)g_.N;
     }
     if (n == "ndisks") return (double)disks_.size();
+    if (n == "nodal_omega") return nod_.omega;
     if (n.rfind("adj_", 0) == 0 || n == "objective") return adjoint_stat(n);
     if (n.rfind("disk_ct:", 0) == 0) return disks_.at(std::stoul(n.substr(8))).ct_now;
     if (n.rfind("disk_uinf2:", 0) == 0) return disks_.at(std::stoul(n.substr(11))).uinf2;

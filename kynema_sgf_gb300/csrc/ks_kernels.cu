@@ -28,7 +28,7 @@ __device__ inline double block_reduce(double v) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int o = 16; o > 0; o >>= 1) {
         const double x = __shfl_down_sync(0xffffffffu, v, o);
-        v = OPMAX ? fmax(v, x) : v + x;
+        v = OPMAX ? nmax(v, x) : v + x;
     }
     __syncthreads();
     if (lane == 0) sh[w] = v;
@@ -38,7 +38,7 @@ __device__ inline double block_reduce(double v) {
     if (w == 0)
         for (int o = 16; o > 0; o >>= 1) {
             const double x = __shfl_down_sync(0xffffffffu, v, o);
-            v = OPMAX ? fmax(v, x) : v + x;
+            v = OPMAX ? nmax(v, x) : v + x;
         }
     return v;
 }
@@ -447,10 +447,10 @@ __global__ void k_cfl(Grid g, const double* vel, const double* src, const double
     const double dxinv2 = 2.0 * (dxi[0] * dxi[0] + dxi[1] * dxi[1] + dxi[2] * dxi[2]);
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < g.N; t += (long long)gridDim.x * blockDim.x) {
         for (int n = 0; n < 3; ++n) {
-            c = fmax(c, fabs(vel[n * g.N + t]) * dxi[n]);
-            f = fmax(f, fabs(src[n * g.N + t]) * dxi[n] * irho);
+            c = nmax(c, fabs(vel[n * g.N + t]) * dxi[n]);
+            f = nmax(f, fabs(src[n * g.N + t]) * dxi[n] * irho);
         }
-        d = fmax(d, mu[t] * dxinv2 * irho);
+        d = nmax(d, mu[t] * dxinv2 * irho);
     }
     c = block_reduce<1>(c);
     d = block_reduce<1>(d);
@@ -474,7 +474,7 @@ __global__ void k_reduce(const double* parts, int np, int op_max, double* out) {
     double v = op_max ? -1.0e300 : 0.0;
     for (int m = threadIdx.x; m < np; m += blockDim.x) {
         const double x = parts[comp * np + m];
-        v = op_max ? fmax(v, x) : v + x;
+        v = op_max ? nmax(v, x) : v + x;
     }
     v = op_max ? block_reduce<1>(v) : block_reduce<0>(v);
     if (threadIdx.x == 0) out[comp] = v;

@@ -172,6 +172,15 @@ void launch_adj_adv_trans(Ctx& c, const Grid& g, int a, int b, const double* u, 
 void launch_adj_adv_flux(Ctx& c, const Grid& g, int d, const double* u, const double* forces, double rho, double dt, const double* const mac[3],
                          const GodunovBufs& B, const AdjBufs& A);
 void launch_adj_div(Ctx& c, const Grid& g, const double* convb, const AdjBufs& A);
+// reverse of divtau(vel; mueff, wg) for the adjoint s * divtau_b: accumulates the
+// velocity (ub), cell viscosity (mub, may be null) and wall-gradient (wgb, may be null) adjoints
+void launch_adj_tau(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, const double* divtau_b, double s, double* ub,
+                    double* mub, double* wgb);
+void launch_adj_smag(Ctx& c, const Grid& g, const double* vel, const double* mub, const Scalars& s, double* ub);
+void launch_adj_wall_local(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wgb, double ut2, double um0, double um1,
+                           double vm, double rho, double* ub, double* mub, double* parts, int* np);
+void launch_adj_wall_global(Ctx& c, const Grid& g, const double* vel, double bu, double bv, double bm, double* ub);
+void launch_adj_coriolis(Ctx& c, const Grid& g, const double* srcb, const Scalars& s, double* ub);
 void launch_adj_nodal_post(Ctx& c, const Grid& g, const double* psi, const double* ub, double* out);
 void launch_axpby(Ctx& c, long long n, double a, const double* x, double b, const double* y, double* out);
 void launch_objective(Ctx& c, const Grid& g, const double* u, const int lo[3], const int hi[3], double invM, double* ub, double* parts, int* np);

@@ -25,7 +25,7 @@ __device__ inline double bred(double v) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int o = 16; o > 0; o >>= 1) {
         const double x = __shfl_down_sync(0xffffffffu, v, o);
-        v = OPMAX ? fmax(v, x) : v + x;
+        v = OPMAX ? nmax(v, x) : v + x;
     }
     __syncthreads();
     if (lane == 0) sh[w] = v;
@@ -35,7 +35,7 @@ __device__ inline double bred(double v) {
     if (w == 0)
         for (int o = 16; o > 0; o >>= 1) {
             const double x = __shfl_down_sync(0xffffffffu, v, o);
-            v = OPMAX ? fmax(v, x) : v + x;
+            v = OPMAX ? nmax(v, x) : v + x;
         }
     return v;
 }
@@ -107,7 +107,7 @@ __global__ void k_cc_resid(CCLevelT<T> L, T beta, double* parts) {
         cc_ax(L, L.phi, beta, i, j, k, Ax, dg);
         const T v = L.rhs[t] - Ax;
         L.res[t] = v;
-        mx = fmax(mx, fabs((double)v));
+        mx = nmax(mx, fabs((double)v));
     }
     mx = bred<1>(mx);
     if (threadIdx.x == 0 && parts) parts[blockIdx.x] = mx;
@@ -224,7 +224,7 @@ __global__ void k_nd_jacobi_norm(NDLevelT<double> L, double sigma, double omega,
         const int j = (int)(r % L.ny), k = (int)(r / L.ny);
         const double res = L.rhs[t] - nd_ax(L, in, sigma, i, j, k);
         out[t] = in[t] + omega * res * L.inv_diag;
-        mx = fmax(mx, fabs(res));
+        mx = nmax(mx, fabs(res));
     }
     mx = bred<1>(mx);
     if (threadIdx.x == 0) parts[blockIdx.x] = mx;
@@ -240,7 +240,7 @@ __global__ void k_nd_resid(NDLevelT<T> L, T sigma, double* parts) {
         const int j = (int)(r % L.ny), k = (int)(r / L.ny);
         const T v = L.rhs[t] - nd_ax(L, L.phi, sigma, i, j, k);
         L.res[t] = v;
-        mx = fmax(mx, fabs((double)v));
+        mx = nmax(mx, fabs((double)v));
     }
     mx = bred<1>(mx);
     if (threadIdx.x == 0 && parts) parts[blockIdx.x] = mx;

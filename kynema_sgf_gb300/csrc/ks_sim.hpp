@@ -197,6 +197,7 @@ struct AdjState {
     AdjBufs A{};
     DevBuf<double> ub, gpb;         // adjoints of (velocity, gp) at the current time level
     DevBuf<double> w, t1, t2, srcb, doldb, forcesb;  // 3N scratch
+    DevBuf<double> mub, wgb;        // adjoints of mu_eff (N) and of the wall-model gradient (2 nx ny)
     DevBuf<double> umacb[3];        // adjoint of the MAC velocities
     DevBuf<double> macs;            // pre-MAC recompute output (discarded)
     DevBuf<double> su, sgp, sp;     // forward state saved across a reverse step
@@ -252,6 +253,7 @@ class Sim {
     Clock t_;
     int mac_it_ = 0, nod_it_ = 0;
     int mixed_ = 0;  // 1: FP32 advection and multigrid cycles with FP64 defect correction
+    int godunov64_ = 0;  // 1: FP64 Godunov passes even when mixed_ (reverse-step recompute)
     double mac_r0_ = 0, mac_r_ = 0, nod_r0_ = 0, nod_r_ = 0;
     std::string err_;
 

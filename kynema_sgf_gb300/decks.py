@@ -169,3 +169,78 @@ ks_init.noise_seed = {seed}
     lo = (xl, yc - D, zc - D)
     hi = (min(xl + 5 * D, nx * dx), yc + D, zc + D)
     return deck, lo, hi, cts
+
+
+def abl_disks(nx=512, ny=512, nz=256, dx=10.0, dz=10.0, dcells=20, ngrid=4, spacing=7.0, dt=0.5, seed=42, ct_seed=11, nr=5, nt=20,
+              eps_cells=2.0, precision="mixed", cts=None):
+    """ABL with a wind farm (production forward + adjoint run): the physics of
+    ``abl`` (wall model, slip top, Smagorinsky, geostrophic + Coriolis forcing
+    for 8 m/s, log-law + noise initial field) on nx x ny x nz cells of
+    dx x dx x dz (default 10 m cubes: 5120 x 5120 x 2560 m), with
+    ngrid x ngrid uniform-Ct disks of ``dcells`` cells
+    (D = dcells dx) on a square grid spaced ``spacing`` D, hub height D,
+    facing -x, Ct drawn from U(0.6, 0.9) with numpy's default_rng(ct_seed)
+    unless ``cts`` is given; fixed dt.  Disk k sits in column k // ngrid
+    (x) and row k % ngrid (y).  Returns (deck, box_lo, box_hi, cts), the box
+    being the rotor-height layer from the first disk column to 5 D
+    downstream over the whole width."""
+    import numpy as np
+
+    D = dcells * dx
+    n = ngrid * ngrid
+    if cts is None:
+        cts = np.random.default_rng(ct_seed).uniform(0.6, 0.9, n)
+    cts = [float(c) for c in cts]
+    labels = " ".join("T%d" % i for i in range(n))
+    lines = []
+    for k, ct in enumerate(cts):
+        x = (0.5 + k // ngrid) * spacing * D
+        y = (0.5 + k % ngrid) * spacing * D
+        lines.append(f"Actuator.T{k}.disk_center = {x} {y} {D}")
+        lines.append(f"Actuator.T{k}.thrust_coeff = {ct!r}")
+    body = "\n".join(lines)
+    deck = f"""
+geometry.prob_lo = 0 0 0
+geometry.prob_hi = {nx * dx} {ny * dx} {nz * dz}
+geometry.is_periodic = 1 1 0
+amr.n_cell = {nx} {ny} {nz}
+amr.max_level = 0
+zlo.type = wall_model
+zhi.type = slip_wall
+incflo.physics = ABL
+incflo.density = 1.225
+transport.viscosity = 1.8e-5
+turbulence.model = Smagorinsky
+Smagorinsky_coeffs.Cs = 0.135
+ICNS.source_terms = GeostrophicForcing CoriolisForcing ActuatorForcing
+CoriolisForcing.latitude = 45.0
+GeostrophicForcing.geostrophic_wind = 8 0 0
+ABL.kappa = 0.41
+ABL.surface_roughness_z0 = 0.1
+ABL.wall_shear_stress_type = moeng
+Actuator.labels = {labels}
+Actuator.type = UniformCtDisk
+Actuator.UniformCtDisk.rotor_diameter = {D}
+Actuator.UniformCtDisk.epsilon = {eps_cells * dx}
+Actuator.UniformCtDisk.num_points_r = {nr}
+Actuator.UniformCtDisk.num_points_t = {nt}
+Actuator.UniformCtDisk.spreading_type = UniformGaussian
+Actuator.UniformCtDisk.disk_normal = -1.0 0.0 0.0
+Actuator.UniformCtDisk.diameters_to_sample = 1.0
+Actuator.UniformCtDisk.ks_spread_about_center = 1
+{body}
+incflo.use_godunov = 1
+incflo.godunov_type = ppm
+incflo.diffusion_type = 0
+time.fixed_dt = {dt}
+time.max_step = 1000000
+ks_init.loglaw_utop = 8.0
+ks_init.noise_amplitude = 0.5
+ks_init.noise_zmax = 300
+ks_init.noise_seed = {seed}
+ks.precision = {precision}
+"""
+    x0 = 0.5 * spacing * D
+    lo = (x0, 0.0, 0.5 * D)
+    hi = (min(x0 + 5 * D, nx * dx), ny * dx, 1.5 * D)
+    return deck, lo, hi, cts

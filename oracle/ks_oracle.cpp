@@ -1187,6 +1187,8 @@ void Sim::mac_project() {
         ++it;
         if (!std::isfinite(rn)) throw Error(ERR_NONFINITE, "MAC projection diverged");
     }
+    // MLMG aborts when maxiter is reached above the tolerance (MLMG::solve)
+    if (rn > target) throw Error(ERR_NOT_CONVERGED, "MAC projection did not converge in mac_proj.maxiter V-cycles");
     mac_iters = it;
     mac_res = rn;
     cc_fill(L.phi, L.n, zper);
@@ -1450,6 +1452,30 @@ static void nd_vcycle(std::vector<NDLevel>& Ls, size_t l, double sigma, bool zpe
     nd_smooth(L, sigma, zper, o.nu2, o.omega);
 }
 
+// Weighted-Jacobi weight of the nodal smoother.  The largest eigenvalue of
+// D^-1 A for the Q1 stencil lies at a corner of the frequency cube; it is 1.5
+// on isotropic cells (omega 0.9 gives omega * lambda_max = 1.35) and grows with
+// the cell aspect ratio (3.0 at dz = dx / 2, where omega = 0.9 diverges).  The
+// weight is reduced so that omega * lambda_max stays at 1.35.
+static double nodal_jacobi_weight(const double* W, double omega) {
+    double lmax = 0.0;
+    for (int m = 1; m < 8; ++m) {
+        double A = 0.0;
+        for (int c = 0; c < 3; ++c)
+            for (int b = 0; b < 3; ++b)
+                for (int a = 0; a < 3; ++a) {
+                    double f = 1.0;
+                    if ((m & 1) && a != 1) f = -f;
+                    if ((m & 2) && b != 1) f = -f;
+                    if ((m & 4) && c != 1) f = -f;
+                    A += W[(c * 3 + b) * 3 + a] * f;
+                }
+        lmax = std::max(lmax, A / W[13]);
+    }
+    if (omega * lmax > 1.35 * (1.0 + 1e-9)) omega = 1.35 / lmax;
+    return omega;
+}
+
 static std::vector<NDLevel> nd_levels(const Geo& g) {
     std::vector<NDLevel> Ls;
     int n[3] = {g.n[0], g.n[1], g.n[2]};
@@ -1529,12 +1555,15 @@ void Sim::nodal_project(double time, double scaling, bool incremental) {
     const double target = std::max(nod.atol, nod.rtol * r0);
     int it = 0;
     double rn = r0;
+    MGOpts o = nod;
+    o.omega = nodal_jacobi_weight(L.W, nod.omega);
     while (rn > target && it < nod.maxiter) {
-        nd_vcycle(Ls, 0, sigma, zper, nod);
+        nd_vcycle(Ls, 0, sigma, zper, o);
         rn = nd_residual(L, sigma, zper);
         ++it;
         if (!std::isfinite(rn)) throw Error(ERR_NONFINITE, "nodal projection diverged");
     }
+    if (rn > target) throw Error(ERR_NOT_CONVERGED, "nodal projection did not converge in nodal_proj.maxiter V-cycles");
     nodal_iters = it;
     nodal_res = rn;
     nd_fill(L.phi, L, zper);

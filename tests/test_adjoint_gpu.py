@@ -200,3 +200,67 @@ def test_adjoint_unsupported_decks(cuda_dev):
     assert e.value.code == 6
     with pytest.raises(cuda_dev.KsError):
         sim.set_disk_ct([0.7])
+
+
+FARM = dict(nx=48, ny=48, nz=24, dx=20.0, dz=20.0, dcells=6, ngrid=2, spacing=3.0, dt=1.0, nr=3, nt=8)
+
+
+def test_abl_farm_ct_gradient(cuda_dev):
+    """Wall model, slip top, Smagorinsky, geostrophic + Coriolis, 2 x 2 disks."""
+    deck, lo, hi, cts = decks.abl_disks(precision="fp64", **FARM)
+    sim = cuda_dev.Incflo(deck)
+    sim.InitData()
+    sim.set_objective_box(lo, hi)
+    x0 = {f: sim.get_field(f) for f in ("velocity", "gp", "p")}
+    ct = np.array(cts)
+    J, g = adjoint(sim, x0, ct, 10, 4)
+    assert J == forward_J(sim, x0, ct, 10)
+    assert np.all(g < 0)
+    assert fd_rel(sim, x0, ct, 10, g, 1e-6) < TOL
+
+
+@pytest.mark.parametrize("extra", ["", "\nks.precision = mixed\n"])
+def test_abl_farm_one_step_vjp(cuda_dev, extra):
+    """Every reverse pass of the ABL step (walls, wall model, Smagorinsky,
+    Coriolis, disks) at once; the mixed-precision handle re-linearises in FP64."""
+    deck, lo, hi, cts = decks.abl_disks(precision="fp64", **FARM)
+    sim = cuda_dev.Incflo(deck + extra)
+    sim.InitData()
+    for _ in range(3):
+        sim.step()
+    sim.set_precision(0)
+    xs = {f: sim.get_field(f) for f in ("velocity", "gp", "p")}
+    rng = np.random.default_rng(5)
+    sh = xs["velocity"].shape
+    w, w2, du, dg = rng.standard_normal(sh), rng.standard_normal(sh), rng.uniform(-1, 1, sh), rng.uniform(-1, 1, sh)
+
+    def F(h):
+        restore(sim, xs)
+        sim.set_field("velocity", xs["velocity"] + h * du)
+        sim.set_field("gp", xs["gp"] + h * dg)
+        sim.step()
+        return float((w * sim.get_field("velocity")).sum() + (w2 * sim.get_field("gp")).sum())
+
+    restore(sim, xs)
+    sim.adjoint_reset()
+    sim.set_field("velocity_adjoint", w)
+    sim.set_field("gp_adjoint", w2)
+    sim.adjoint_step()
+    adj = float((sim.get_field("velocity_adjoint") * du).sum() + (sim.get_field("gp_adjoint") * dg).sum())
+    h = 1e-9  # random directions cross the scheme's jumps at larger h
+    assert abs((F(h) - F(-h)) / (2 * h) - adj) <= 1e-5 * abs(adj)
+
+
+def test_mixed_forward_fp64_adjoint(cuda_dev):
+    """Mixed-precision forward with the FP64 reverse sweep against FP64 finite differences."""
+    deck, lo, hi, cts = decks.abl_disks(precision="mixed", **FARM)
+    sim = cuda_dev.Incflo(deck)
+    sim.InitData()
+    sim.set_objective_box(lo, hi)
+    x0 = {f: sim.get_field(f) for f in ("velocity", "gp", "p")}
+    ct = np.array(cts)
+    J_mixed, g = adjoint(sim, x0, ct, 10, 3)
+    sim.set_precision(0)
+    J64 = forward_J(sim, x0, ct, 10)
+    assert abs(J_mixed - J64) <= 1e-6 * J64
+    assert fd_rel(sim, x0, ct, 10, g, 1e-6) < 1e-3

@@ -216,3 +216,29 @@ def test_noise_initial_field(oracle_mod):
     assert np.abs(w).max() <= 0.5
     assert np.all(w[z > 300] == 0.0)
     assert abs(w[z < 300].mean()) < 0.05
+
+
+def _aspect2_abl():
+    # dz = dx / 2: the 27-point nodal stencil's D^-1 A reaches 3.0, beyond 2 / 0.9
+    return decks.abl(32, 32, 16, steps=3).replace("geometry.prob_hi = 640.0 640.0 320.0", "geometry.prob_hi = 640.0 640.0 160.0")
+
+
+def test_projections_converge_on_anisotropic_cells(oracle_mod):
+    """The nodal Jacobi weight drops to 1.35 / lambda_max (0.45 at dz = dx / 2,
+    where 0.9 diverges); both projections reach the MLMG target."""
+    o = oracle_mod.Oracle(_aspect2_abl())
+    o.InitData()
+    for _ in range(2):
+        o.step()
+        assert o.scalar("nodal_res") <= max(1e2 * EPS, 1e5 * EPS * o.scalar("nodal_res0"))
+        assert o.scalar("mac_res") <= max(1e2 * EPS, 1e5 * EPS * o.scalar("mac_res0"))
+        assert o.scalar("nodal_iters") < 60
+
+
+def test_maxiter_reports_not_converged(oracle_mod):
+    """MLMG aborts when maxiter is reached above the tolerance; the status is
+    KS_ERR_NOT_CONVERGED (3)."""
+    o = oracle_mod.Oracle(decks.tgv(16, steps=2) + "\nnodal_proj.maxiter = 1\n")
+    with pytest.raises(oracle_mod.OracleError) as e:
+        o.InitData()
+    assert e.value.code == 3

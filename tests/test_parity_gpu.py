@@ -127,3 +127,22 @@ def test_invalid_decks_fail_loudly(cuda_dev):
         cuda_dev.Incflo(bad)
     with pytest.raises(cuda_dev.KsError):
         cuda_dev.Incflo(decks.tgv(16).replace("time.cfl = 0.5", "time.cfl = 1.5"))
+
+
+def test_anisotropic_cells(cuda_dev, oracle_mod):
+    """dz = dx / 2: both sides reduce the nodal Jacobi weight to 1.35 / 3.0."""
+    d = decks.abl(32, 32, 16, steps=3).replace("geometry.prob_hi = 640.0 640.0 320.0", "geometry.prob_hi = 640.0 640.0 160.0")
+    g, o = pair(cuda_dev, oracle_mod, d)
+    assert abs(g.scalar("nodal_omega") - 0.45) < 1e-12
+    g.InitData()
+    o.InitData()
+    for _ in range(2):
+        assert g.step() and o.step()
+        check_fields(g, o, ["velocity", "p", "gp"])
+
+
+def test_maxiter_reports_not_converged(cuda_dev):
+    g = cuda_dev.Incflo(decks.tgv(16, steps=2) + "\nnodal_proj.maxiter = 1\n")
+    with pytest.raises(cuda_dev.KsError) as e:
+        g.InitData()
+    assert e.value.code == 3
