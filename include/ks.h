@@ -114,9 +114,8 @@ int ks_objective(ks_handle* h, int seed, double* J);
 /* One reverse step at the current state x^n = (velocity, gp): the adjoint
  * fields go from the adjoint of x^{n+1} to that of x^n and dJ/dct
  * accumulates; the forward state and the clock are left at x^n.  The step is
- * recomputed from x^n with FP64 Godunov passes; its projections (and the two
- * reverse solves) run at the handle's precision, which reaches the FP64
- * multigrid tolerance either way. */
+ * recomputed from x^n at the handle's precision (ks_set_precision) and
+ * linearised there; the reverse arithmetic is FP64. */
 int ks_adjoint_step(ks_handle* h);
 /* nsteps forward steps from the current state with binomial checkpointing in
  * device memory (`snapshots` slots of (velocity, gp), the first holding the

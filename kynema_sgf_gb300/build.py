@@ -39,7 +39,9 @@ def build(verbose=False, extra=()):
     os.makedirs(OUT, exist_ok=True)
     lib = os.path.join(OUT, "libks.so")
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(HERE, "..", "include", "ks.h")]
-    if os.path.exists(lib) and all(os.path.getmtime(lib) >= os.path.getmtime(d) for d in deps) and not extra:
+    exe = driver_path()
+    if (os.path.exists(lib) and os.path.exists(exe) and not extra
+            and all(min(os.path.getmtime(lib), os.path.getmtime(exe)) >= os.path.getmtime(d) for d in deps)):
         return lib
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         results = list(ex.map(lambda s: _compile(s, list(extra)), SOURCES))
@@ -54,7 +56,19 @@ def build(verbose=False, extra=()):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s" % r.stderr)
     os.replace(tmp, lib)
+    # deck-compatible driver executable over the C ABI (reference: src/main.cpp)
+    cmd = [nvcc(), "-O2", "-std=c++17", os.path.join(CSRC, "ks_main.cpp"), "-L" + OUT, "-lks", "-Xlinker", "-rpath",
+           "-Xlinker", "$ORIGIN", "-o", exe + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("driver build failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    os.replace(exe + ".tmp", exe)
     return lib
+
+
+def driver_path():
+    """The ks_run executable: `ks_run <input_file> [param=value ...]`."""
+    return os.path.join(OUT, "ks_run")
 
 
 if __name__ == "__main__":

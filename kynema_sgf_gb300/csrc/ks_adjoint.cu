@@ -127,6 +127,7 @@ __device__ inline double clip_rev(double e, double a, double b, double rb, doubl
 }
 
 // ---- reverse of the unlimited PPM edges on d-faces (k_edges)
+template <typename TI>
 __global__ void k_adj_edges(Grid g, int d, const double* u, const double* Eb0, const double* Eb1, const double* Eb2, double* ub) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -143,7 +144,8 @@ __global__ void k_adj_edges(Grid g, int d, const double* u, const double* Eb0, c
         }
         if (wall && (k == 1 || k == g.nz - 1)) {  // one-sided fourth order, clipped to the adjacent cells
             const int kb = (k == 1) ? -1 : g.nz, k0 = (k == 1) ? 0 : g.nz - 1, s = (k == 1) ? 1 : -1;
-            const double b = Q(g, u, n, i, j, kb), q0 = Q(g, u, n, i, j, k0), q1 = Q(g, u, n, i, j, k0 + s), q2 = Q(g, u, n, i, j, k0 + 2 * s);
+            const double b = (TI)Q(g, u, n, i, j, kb), q0 = (TI)Q(g, u, n, i, j, k0), q1 = (TI)Q(g, u, n, i, j, k0 + s),
+                         q2 = (TI)Q(g, u, n, i, j, k0 + 2 * s);
             const double e = -0.2 * b + 0.75 * q0 + 0.5 * q1 - 0.05 * q2;
             double g0 = 0.0, g1 = 0.0;
             const double ebar = clip_rev(e, q0, q1, eb, g0, g1);
@@ -153,8 +155,8 @@ __global__ void k_adj_edges(Grid g, int d, const double* u, const double* Eb0, c
             Qb(g, ub, n, i, j, k0 + 2 * s, -0.05 * ebar);
             continue;
         }
-        const double am = Q(g, u, n, i - 2 * di, j - 2 * dj, k - 2 * dk), a0 = Q(g, u, n, i - di, j - dj, k - dk);
-        const double a1 = Q(g, u, n, i, j, k), a2 = Q(g, u, n, i + di, j + dj, k + dk);
+        const double am = (TI)Q(g, u, n, i - 2 * di, j - 2 * dj, k - 2 * dk), a0 = (TI)Q(g, u, n, i - di, j - dj, k - dk);
+        const double a1 = (TI)Q(g, u, n, i, j, k), a2 = (TI)Q(g, u, n, i + di, j + dj, k + dk);
         double c1a, c1b, c1c, c0a, c0b, c0c;
         const double s1 = vls_d(a0, a1, a2, c1a, c1b, c1c);
         const double s0 = vls_d(am, a0, a1, c0a, c0b, c0c);
@@ -251,13 +253,18 @@ struct A3 {
 struct K3 {
     const double* p[3];
 };
+// forward intermediates, stored in FP64 or FP32 (TI)
+template <typename TI>
+struct KI {
+    const TI* p[3];
+};
 
 // ---- reverse of k_faces (both passes).  MODE 0: pre-MAC (cell speed), the
 // adjoints of ad and of the upwinded transverse states are folded in here;
 // MODE 1: post-MAC (face speed, rho scaling), upwinded states folded in.
-template <int MODE>
-__global__ void k_adj_faces(Grid g, int d, const double* u, K3 E, double s, double rho, const double* umac_d, K3 LO, K3 HI, const double* ad,
-                            K3 LOb, K3 HIb, const double* adb, K3 TEb, A3 Eb, double* ub, double* umacb_d) {
+template <int MODE, typename TI>
+__global__ void k_adj_faces(Grid g, int d, const double* u, KI<TI> E, double s, double rho, const double* umac_d, KI<TI> LO, KI<TI> HI,
+                            const TI* ad, K3 LOb, K3 HIb, const double* adb, K3 TEb, A3 Eb, double* ub, double* umacb_d) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_at(g, d, t, i, j, k)) return;
@@ -272,28 +279,29 @@ __global__ void k_adj_faces(Grid g, int d, const double* u, K3 E, double s, doub
     }
     double ul = 0.0, uh = 0.0;
     if (MODE == 0) {
-        if (!wl) ul = Q(g, u, d, i - di, j - dj, k - dk);
-        if (!wh) uh = Q(g, u, d, i, j, k);
+        if (!wl) ul = (TI)Q(g, u, d, i - di, j - dj, k - dk);
+        if (!wh) uh = (TI)Q(g, u, d, i, j, k);
         rev_riemann(LO.p[d][f], HI.p[d][f], adb[f], lb[d], hb[d]);
         const double a = ad[f];
         for (int n = 0; n < 3; ++n)
             if (n != d) rev_upwind(a, TEb.p[n][f], lb[n], hb[n]);
     } else {
-        const double umf = umac_d[f];
+        const double umf = (TI)umac_d[f];
         ul = uh = umf;
         for (int n = 0; n < 3; ++n) rev_upwind(umf, TEb.p[n][f], lb[n], hb[n]);
     }
     if (d == 2)
         for (int n = 0; n < 3; ++n) zbc_rev(g, k, n, lb[n], hb[n]);
-    const double scale = (MODE == 1) ? rho : 1.0;
+    const double scale = (MODE == 1) ? (double)(TI)rho : 1.0;
+    const double sT = (TI)s;
     double gul = 0.0, guh = 0.0;
     for (int n = 0; n < 3; ++n) {
         const double tl = lb[n] * scale, th = hb[n] * scale;
         if (!wl && tl != 0.0) {  // high-side trace of cell c - e_d
             double gsm = 0.0, gs0 = 0.0, gsp = 0.0;
-            const double s0 = Q(g, u, n, i - di, j - dj, k - dk);
+            const double s0 = (TI)Q(g, u, n, i - di, j - dj, k - dk);
             if (ul > kSV) {
-                const double bsig = rev_trace(true, E.p[n][fm], s0, E.p[n][f], fabs(ul) * s, tl, gsm, gs0, gsp);
+                const double bsig = rev_trace(true, E.p[n][fm], s0, E.p[n][f], (TI)(fabs(ul) * sT), tl, gsm, gs0, gsp);
                 gul += bsig * s * (ul >= 0.0 ? 1.0 : -1.0);
             } else {
                 gs0 += tl;
@@ -304,9 +312,9 @@ __global__ void k_adj_faces(Grid g, int d, const double* u, K3 E, double s, doub
         }
         if (!wh && th != 0.0) {  // low-side trace of cell c
             double gsm = 0.0, gs0 = 0.0, gsp = 0.0;
-            const double s0 = Q(g, u, n, i, j, k);
+            const double s0 = (TI)Q(g, u, n, i, j, k);
             if (uh < -kSV) {
-                const double bsig = rev_trace(false, E.p[n][f], s0, E.p[n][fp], fabs(uh) * s, th, gsm, gs0, gsp);
+                const double bsig = rev_trace(false, E.p[n][f], s0, E.p[n][fp], (TI)(fabs(uh) * sT), th, gsm, gs0, gsp);
                 guh += bsig * s * (uh >= 0.0 ? 1.0 : -1.0);
             } else {
                 gs0 += th;
@@ -325,8 +333,9 @@ __global__ void k_adj_faces(Grid g, int d, const double* u, K3 E, double s, doub
 }
 
 // ---- reverse of k_pm_trans (a, b, n)
-__global__ void k_adj_pm_trans(Grid g, int a, int b, int n, double cb, const double* ad_a, const double* ad_b, const double* edge_b,
-                               const double* outb, double* lo_anb, double* hi_anb, double* ad_bb, double* edge_bb) {
+template <typename TI>
+__global__ void k_adj_pm_trans(Grid g, int a, int b, int n, double cb, const TI* ad_a, const TI* ad_b, const TI* edge_b, const double* outb,
+                               double* lo_anb, double* hi_anb, double* ad_bb, double* edge_bb) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_at(g, a, t, i, j, k)) return;
@@ -342,7 +351,7 @@ __global__ void k_adj_pm_trans(Grid g, int a, int b, int n, double cb, const dou
     const int e0 = (b == 0), e1 = (b == 1), e2 = (b == 2);
     if (!wh && hb != 0.0) {
         const long long f0 = fidx(g, b, i, j, k), f1 = fidx(g, b, i + e0, j + e1, k + e2);
-        const double S = ad_b[f1] + ad_b[f0], Dd = edge_b[f1] - edge_b[f0];
+        const double S = (double)ad_b[f1] + ad_b[f0], Dd = (double)edge_b[f1] - edge_b[f0];
         aadd(&ad_bb[f1], -cb * Dd * hb);
         aadd(&ad_bb[f0], -cb * Dd * hb);
         aadd(&edge_bb[f1], -cb * S * hb);
@@ -351,7 +360,7 @@ __global__ void k_adj_pm_trans(Grid g, int a, int b, int n, double cb, const dou
     if (!wl && lb != 0.0) {
         const int ci = i - (a == 0), cj = j - (a == 1), ck = k - (a == 2);
         const long long f0 = fidx(g, b, ci, cj, ck), f1 = fidx(g, b, ci + e0, cj + e1, ck + e2);
-        const double S = ad_b[f1] + ad_b[f0], Dd = edge_b[f1] - edge_b[f0];
+        const double S = (double)ad_b[f1] + ad_b[f0], Dd = (double)edge_b[f1] - edge_b[f0];
         aadd(&ad_bb[f1], -cb * Dd * lb);
         aadd(&ad_bb[f0], -cb * Dd * lb);
         aadd(&edge_bb[f1], -cb * S * lb);
@@ -369,9 +378,10 @@ __device__ inline long long cell_fo(const Grid& g, int i, int j, int k) {
 }
 
 // ---- reverse of k_pm_final (d)
-__global__ void k_adj_pm_final(Grid g, int d, double dt, double c1, double c2, const double* lo_dd, const double* hi_dd, K3 AD, const double* T1,
-                               const double* T2, const double* forces, const double* macb, double* lo_ddb, double* hi_ddb, A3 ADb,
-                               double* T1b, double* T2b, double* forcesb) {
+template <typename TI>
+__global__ void k_adj_pm_final(Grid g, int d, double dt, double c1, double c2, const TI* lo_dd, const TI* hi_dd, KI<TI> AD, const TI* T1,
+                               const TI* T2, const double* forces, const double* macb, double* lo_ddb, double* hi_ddb, A3 ADb, double* T1b,
+                               double* T2b, double* forcesb) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_at(g, d, t, i, j, k)) return;
@@ -383,17 +393,19 @@ __global__ void k_adj_pm_final(Grid g, int d, double dt, double c1, double c2, c
     auto side_val = [&](int ci, int cj, int ck, double base) {
         const long long p1 = fidx(g, b1, ci + (b1 == 0), cj + (b1 == 1), ck + (b1 == 2)), m1 = fidx(g, b1, ci, cj, ck);
         const long long p2 = fidx(g, b2, ci + (b2 == 0), cj + (b2 == 1), ck + (b2 == 2)), m2 = fidx(g, b2, ci, cj, ck);
-        double s = base;
-        s -= c1 * (AD.p[b1][p1] + AD.p[b1][m1]) * (T1[p1] - T1[m1]);
-        s -= c2 * (AD.p[b2][p2] + AD.p[b2][m2]) * (T2[p2] - T2[m2]);
-        s += 0.5 * dt * forces[d * g.N + cell_fo(g, ci, cj, ck)];
-        return s;
+        // the forward's sum in its own precision (decides the Riemann branch)
+        const TI tc1 = (TI)c1, tc2 = (TI)c2;
+        TI s = (TI)base;
+        s -= tc1 * (AD.p[b1][p1] + AD.p[b1][m1]) * (T1[p1] - T1[m1]);
+        s -= tc2 * (AD.p[b2][p2] + AD.p[b2][m2]) * (T2[p2] - T2[m2]);
+        s += TI(0.5) * (TI)dt * (TI)forces[d * g.N + cell_fo(g, ci, cj, ck)];
+        return (double)s;
     };
     auto side_rev = [&](int ci, int cj, int ck, double sb) {
         const long long p1 = fidx(g, b1, ci + (b1 == 0), cj + (b1 == 1), ck + (b1 == 2)), m1 = fidx(g, b1, ci, cj, ck);
         const long long p2 = fidx(g, b2, ci + (b2 == 0), cj + (b2 == 1), ck + (b2 == 2)), m2 = fidx(g, b2, ci, cj, ck);
-        const double S1 = AD.p[b1][p1] + AD.p[b1][m1], D1 = T1[p1] - T1[m1];
-        const double S2 = AD.p[b2][p2] + AD.p[b2][m2], D2 = T2[p2] - T2[m2];
+        const double S1 = (double)AD.p[b1][p1] + AD.p[b1][m1], D1 = (double)T1[p1] - T1[m1];
+        const double S2 = (double)AD.p[b2][p2] + AD.p[b2][m2], D2 = (double)T2[p2] - T2[m2];
         aadd(&ADb.p[b1][p1], -c1 * D1 * sb);
         aadd(&ADb.p[b1][m1], -c1 * D1 * sb);
         aadd(&T1b[p1], -c1 * S1 * sb);
@@ -420,25 +432,26 @@ __global__ void k_adj_pm_final(Grid g, int d, double dt, double c1, double c2, c
 
 // ---- reverse of k_adv_trans (a, b): out_n = upwind(u_a; l, h),
 // h = HI + (-cb (vp E(h1) - vm E(h0)) + cb q(c) (vp - vm)), l likewise at c - e_a
-__global__ void k_adj_adv_trans(Grid g, int a, int b, const double* u, double rho, double cb, const double* ua, const double* vb, K3 E, K3 Ob,
-                                A3 LOb, A3 HIb, A3 Ebb, double* vbb, double* ub) {
+template <typename TI>
+__global__ void k_adj_adv_trans(Grid g, int a, int b, const double* u, double rho, double cb, const double* ua, const double* vb, KI<TI> E,
+                                K3 Ob, A3 LOb, A3 HIb, A3 Ebb, double* vbb, double* ub) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_at(g, a, t, i, j, k)) return;
     const bool wl = (a == 2 && !g.zper && k == 0), wh = (a == 2 && !g.zper && k == g.nz);
     const long long f = t;
-    const double uaf = ua[f];
+    const double uaf = (TI)ua[f];
     const int ci = i - (a == 0), cj = j - (a == 1), ck = k - (a == 2);
     const long long h0 = fidx(g, b, i, j, k), h1 = fidx(g, b, i + (b == 0), j + (b == 1), k + (b == 2));
     const long long l0 = fidx(g, b, ci, cj, ck), l1 = fidx(g, b, ci + (b == 0), cj + (b == 1), ck + (b == 2));
     double vhp = 0.0, vhm = 0.0, vlp = 0.0, vlm = 0.0;
     if (!wh) {
-        vhp = vb[h1];
-        vhm = vb[h0];
+        vhp = (TI)vb[h1];
+        vhm = (TI)vb[h0];
     }
     if (!wl) {
-        vlp = vb[l1];
-        vlm = vb[l0];
+        vlp = (TI)vb[l1];
+        vlm = (TI)vb[l0];
     }
     double gvhp = 0.0, gvhm = 0.0, gvlp = 0.0, gvlm = 0.0;
     for (int n = 0; n < 3; ++n) {
@@ -450,7 +463,7 @@ __global__ void k_adj_adv_trans(Grid g, int a, int b, const double* u, double rh
         LOb.p[n][f] += lb;
         HIb.p[n][f] += hb;
         if (!wh && hb != 0.0) {
-            const double qc = rho * Q(g, u, n, i, j, k);
+            const double qc = (TI)rho * (TI)Q(g, u, n, i, j, k);
             aadd(&Ebb.p[n][h1], -cb * vhp * hb);
             aadd(&Ebb.p[n][h0], cb * vhm * hb);
             gvhp += (-cb * E.p[n][h1] + cb * qc) * hb;
@@ -458,7 +471,7 @@ __global__ void k_adj_adv_trans(Grid g, int a, int b, const double* u, double rh
             Qb(g, ub, n, i, j, k, rho * cb * (vhp - vhm) * hb);
         }
         if (!wl && lb != 0.0) {
-            const double qc = rho * Q(g, u, n, ci, cj, ck);
+            const double qc = (TI)rho * (TI)Q(g, u, n, ci, cj, ck);
             aadd(&Ebb.p[n][l1], -cb * vlp * lb);
             aadd(&Ebb.p[n][l0], cb * vlm * lb);
             gvlp += (-cb * E.p[n][l1] + cb * qc) * lb;
@@ -473,15 +486,17 @@ __global__ void k_adj_adv_trans(Grid g, int a, int b, const double* u, double rh
 }
 
 // ---- reverse of k_adv_flux (d) with the flux adjoint Fb given
-__global__ void k_adj_adv_flux(Grid g, int d, const double* u, const double* forces, double rho, double dt, double c1, double c2, K3 Uf, K3 LO,
-                               K3 HI, K3 T1, K3 T2, K3 Fb, A3 Ufb, A3 LOb, A3 HIb, A3 T1b, A3 T2b, double* ub, double* forcesb) {
+template <typename TI>
+__global__ void k_adj_adv_flux(Grid g, int d, const double* u, const double* forces, double rho, double dt, double c1, double c2, K3 Uf,
+                               KI<TI> LO, KI<TI> HI, KI<TI> T1, KI<TI> T2, K3 Fb, A3 Ufb, A3 LOb, A3 HIb, A3 T1b, A3 T2b, double* ub,
+                               double* forcesb) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_at(g, d, t, i, j, k)) return;
     const bool wl = (d == 2 && !g.zper && k == 0), wh = (d == 2 && !g.zper && k == g.nz);
     const long long f = t;
     const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
-    const double um = Uf.p[d][f];
+    const double um = (TI)Uf.p[d][f];
     const int li = i - (d == 0), lj = j - (d == 1), lk = k - (d == 2);
     const long long lp1 = fidx(g, b1, li + (b1 == 0), lj + (b1 == 1), lk + (b1 == 2)), lm1 = fidx(g, b1, li, lj, lk);
     const long long lp2 = fidx(g, b2, li + (b2 == 0), lj + (b2 == 1), lk + (b2 == 2)), lm2 = fidx(g, b2, li, lj, lk);
@@ -489,16 +504,16 @@ __global__ void k_adj_adv_flux(Grid g, int d, const double* u, const double* for
     const long long hp2 = fidx(g, b2, i + (b2 == 0), j + (b2 == 1), k + (b2 == 2)), hm2 = fidx(g, b2, i, j, k);
     double l1p = 0, l1m = 0, l2p = 0, l2m = 0, h1p = 0, h1m = 0, h2p = 0, h2m = 0;
     if (!wl) {
-        l1p = Uf.p[b1][lp1];
-        l1m = Uf.p[b1][lm1];
-        l2p = Uf.p[b2][lp2];
-        l2m = Uf.p[b2][lm2];
+        l1p = (TI)Uf.p[b1][lp1];
+        l1m = (TI)Uf.p[b1][lm1];
+        l2p = (TI)Uf.p[b2][lp2];
+        l2m = (TI)Uf.p[b2][lm2];
     }
     if (!wh) {
-        h1p = Uf.p[b1][hp1];
-        h1m = Uf.p[b1][hm1];
-        h2p = Uf.p[b2][hp2];
-        h2m = Uf.p[b2][hm2];
+        h1p = (TI)Uf.p[b1][hp1];
+        h1m = (TI)Uf.p[b1][hm1];
+        h2p = (TI)Uf.p[b2][hp2];
+        h2m = (TI)Uf.p[b2][hm2];
     }
     double gum = 0, gl1p = 0, gl1m = 0, gl2p = 0, gl2m = 0, gh1p = 0, gh1m = 0, gh2p = 0, gh2m = 0;
     const long long cl = wl ? 0 : cell_fo(g, li, lj, lk);
@@ -506,24 +521,30 @@ __global__ void k_adj_adv_flux(Grid g, int d, const double* u, const double* for
     for (int n = 0; n < 3; ++n) {
         const double fb = Fb.p[n][f];
         if (fb == 0.0) continue;
+        // the forward's face states in its own precision (decide the upwind branch)
+        const TI tr = (TI)rho, tc1 = (TI)c1, tc2 = (TI)c2, thd = TI(0.5) * (TI)dt;
         double ql = 0.0, qh = 0.0, stl = 0.0, sth = 0.0;
         if (!wl) {
-            ql = rho * u[n * g.N + cl];
-            stl = LO.p[n][f];
-            stl -= c1 * (T1.p[n][lp1] * l1p - T1.p[n][lm1] * l1m);
-            stl -= c2 * (T2.p[n][lp2] * l2p - T2.p[n][lm2] * l2m);
-            stl += c1 * ql * (l1p - l1m);
-            stl += c2 * ql * (l2p - l2m);
-            stl += 0.5 * dt * (rho * forces[n * g.N + cl]);
+            const TI q = tr * (TI)u[n * g.N + cl];
+            ql = q;
+            TI s_ = LO.p[n][f];
+            s_ -= tc1 * (T1.p[n][lp1] * (TI)l1p - T1.p[n][lm1] * (TI)l1m);
+            s_ -= tc2 * (T2.p[n][lp2] * (TI)l2p - T2.p[n][lm2] * (TI)l2m);
+            s_ += tc1 * q * (TI)(l1p - l1m);
+            s_ += tc2 * q * (TI)(l2p - l2m);
+            s_ += thd * (tr * (TI)forces[n * g.N + cl]);
+            stl = s_;
         }
         if (!wh) {
-            qh = rho * u[n * g.N + ch];
-            sth = HI.p[n][f];
-            sth -= c1 * (T1.p[n][hp1] * h1p - T1.p[n][hm1] * h1m);
-            sth -= c2 * (T2.p[n][hp2] * h2p - T2.p[n][hm2] * h2m);
-            sth += c1 * qh * (h1p - h1m);
-            sth += c2 * qh * (h2p - h2m);
-            sth += 0.5 * dt * (rho * forces[n * g.N + ch]);
+            const TI q = tr * (TI)u[n * g.N + ch];
+            qh = q;
+            TI s_ = HI.p[n][f];
+            s_ -= tc1 * (T1.p[n][hp1] * (TI)h1p - T1.p[n][hm1] * (TI)h1m);
+            s_ -= tc2 * (T2.p[n][hp2] * (TI)h2p - T2.p[n][hm2] * (TI)h2m);
+            s_ += tc1 * q * (TI)(h1p - h1m);
+            s_ += tc2 * q * (TI)(h2p - h2m);
+            s_ += thd * (tr * (TI)forces[n * g.N + ch]);
+            sth = s_;
         }
         double zl = stl, zh = sth;
         if (d == 2) zbc_fwd(g, k, n, zl, zh);
@@ -952,66 +973,108 @@ __global__ void k_act_sample_adj(Grid g, const double* pts, const double* wb, in
 // ---------------------------------------------------------------- launchers
 constexpr double B8 = 8.0;
 
-void launch_adj_edges(Ctx& c, const Grid& g, int d, const double* u, double* const Eb[3], double* ub) {
-    const long long nf = nfaces(g, d);
-    KS_LAUNCH(c, k_adj_edges, nblocks(nf, BS), BS, B8 * (3.0 * nf + 6.0 * g.N), g, d, u, Eb[0], Eb[1], Eb[2], ub);
+template <typename TI>
+static const TI* ti(void* p) {
+    return static_cast<const TI*>(p);
 }
-void launch_adj_faces(Ctx& c, const Grid& g, int d, int mode, const double* u, const GodunovBufs& B, const AdjBufs& A, double dt, double rho,
-                      const double* umac_d) {
-    K3 E{{(double*)B.edge[d][0], (double*)B.edge[d][1], (double*)B.edge[d][2]}};
-    K3 LO{{(double*)B.lo[d][0], (double*)B.lo[d][1], (double*)B.lo[d][2]}}, HI{{(double*)B.hi[d][0], (double*)B.hi[d][1], (double*)B.hi[d][2]}};
+
+void launch_adj_edges(Ctx& c, const Grid& g, int d, const double* u, double* const Eb[3], double* ub, int fp32) {
+    const long long nf = nfaces(g, d);
+    if (fp32)
+        KS_LAUNCH(c, k_adj_edges<float>, nblocks(nf, BS), BS, B8 * (3.0 * nf + 6.0 * g.N), g, d, u, Eb[0], Eb[1], Eb[2], ub);
+    else
+        KS_LAUNCH(c, k_adj_edges<double>, nblocks(nf, BS), BS, B8 * (3.0 * nf + 6.0 * g.N), g, d, u, Eb[0], Eb[1], Eb[2], ub);
+}
+
+template <typename TI>
+static void adj_faces_t(Ctx& c, const Grid& g, int d, int mode, const double* u, const GodunovBufs& B, const AdjBufs& A, double dt, double rho,
+                        const double* umac_d) {
+    KI<TI> E{{ti<TI>(B.edge[d][0]), ti<TI>(B.edge[d][1]), ti<TI>(B.edge[d][2])}};
+    KI<TI> LO{{ti<TI>(B.lo[d][0]), ti<TI>(B.lo[d][1]), ti<TI>(B.lo[d][2])}}, HI{{ti<TI>(B.hi[d][0]), ti<TI>(B.hi[d][1]), ti<TI>(B.hi[d][2])}};
     K3 LOb{{A.lo[d][0], A.lo[d][1], A.lo[d][2]}}, HIb{{A.hi[d][0], A.hi[d][1], A.hi[d][2]}};
     K3 TEb{{A.tedge[d][0], A.tedge[d][1], A.tedge[d][2]}};
     A3 Eb{{A.edge[d][0], A.edge[d][1], A.edge[d][2]}};
     const double s = dt * ihd(g, d);
     const long long nf = nfaces(g, d);
+    const double bytes = B8 * (6.0 * g.N + 13.0 * nf) + sizeof(TI) * 9.0 * nf;
     if (mode == 0)
-        KS_LAUNCH(c, k_adj_faces<0>, nblocks(nf, BS), BS, B8 * (6.0 * g.N + 17.0 * nf), g, d, u, E, s, rho, nullptr, LO, HI,
-                  (const double*)B.ad[d], LOb, HIb, A.ad[d], TEb, Eb, A.u, nullptr);
+        KS_LAUNCH(c, (k_adj_faces<0, TI>), nblocks(nf, BS), BS, bytes, g, d, u, E, s, rho, nullptr, LO, HI, ti<TI>(B.ad[d]), LOb, HIb, A.ad[d], TEb,
+                  Eb, A.u, nullptr);
     else
-        KS_LAUNCH(c, k_adj_faces<1>, nblocks(nf, BS), BS, B8 * (6.0 * g.N + 18.0 * nf), g, d, u, E, s, rho, umac_d, LO, HI, nullptr, LOb, HIb,
-                  nullptr, TEb, Eb, A.u, A.umac[d]);
+        KS_LAUNCH(c, (k_adj_faces<1, TI>), nblocks(nf, BS), BS, bytes, g, d, u, E, s, rho, umac_d, LO, HI, (const TI*)nullptr, LOb, HIb, nullptr,
+                  TEb, Eb, A.u, A.umac[d]);
 }
-void launch_adj_pm_trans(Ctx& c, const Grid& g, int a, int b, int n, double dt, const GodunovBufs& B, const AdjBufs& A) {
+void launch_adj_faces(Ctx& c, const Grid& g, int d, int mode, const double* u, const GodunovBufs& B, const AdjBufs& A, double dt, double rho,
+                      const double* umac_d, int fp32) {
+    if (fp32) adj_faces_t<float>(c, g, d, mode, u, B, A, dt, rho, umac_d);
+    else adj_faces_t<double>(c, g, d, mode, u, B, A, dt, rho, umac_d);
+}
+
+template <typename TI>
+static void adj_pm_trans_t(Ctx& c, const Grid& g, int a, int b, int n, double dt, const GodunovBufs& B, const AdjBufs& A) {
     const double cb = dt / (6.0 * hd(g, b));
     const long long na = nfaces(g, a), nb = nfaces(g, b);
-    KS_LAUNCH(c, k_adj_pm_trans, nblocks(na, BS), BS, B8 * (4.0 * na + 4.0 * nb), g, a, b, n, cb, (const double*)B.ad[a],
-              (const double*)B.ad[b], (const double*)B.tedge[b][n], A.tr[a][b][0], A.lo[a][n], A.hi[a][n], A.ad[b], A.tedge[b][n]);
+    KS_LAUNCH(c, k_adj_pm_trans<TI>, nblocks(na, BS), BS, B8 * (3.0 * na + 2.0 * nb) + sizeof(TI) * (na + 2.0 * nb), g, a, b, n, cb,
+              ti<TI>(B.ad[a]), ti<TI>(B.ad[b]), ti<TI>(B.tedge[b][n]), A.tr[a][b][0], A.lo[a][n], A.hi[a][n], A.ad[b], A.tedge[b][n]);
 }
-void launch_adj_pm_final(Ctx& c, const Grid& g, int d, double dt, const GodunovBufs& B, const double* forces, const AdjBufs& A) {
+void launch_adj_pm_trans(Ctx& c, const Grid& g, int a, int b, int n, double dt, const GodunovBufs& B, const AdjBufs& A, int fp32) {
+    if (fp32) adj_pm_trans_t<float>(c, g, a, b, n, dt, B, A);
+    else adj_pm_trans_t<double>(c, g, a, b, n, dt, B, A);
+}
+
+template <typename TI>
+static void adj_pm_final_t(Ctx& c, const Grid& g, int d, double dt, const GodunovBufs& B, const double* forces, const AdjBufs& A) {
     const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
-    K3 AD{{(double*)B.ad[0], (double*)B.ad[1], (double*)B.ad[2]}};
+    KI<TI> AD{{ti<TI>(B.ad[0]), ti<TI>(B.ad[1]), ti<TI>(B.ad[2])}};
     A3 ADb{{A.ad[0], A.ad[1], A.ad[2]}};
     const long long nf = nfaces(g, d);
-    KS_LAUNCH(c, k_adj_pm_final, nblocks(nf, BS), BS, B8 * (2.0 * g.N + 5.0 * nf + 8.0 * (nfaces(g, b1) + nfaces(g, b2)) / 2.0), g, d, dt,
-              dt / (4.0 * hd(g, b1)), dt / (4.0 * hd(g, b2)), (const double*)B.lo[d][d], (const double*)B.hi[d][d], AD,
-              (const double*)B.tr[b1][b2][0], (const double*)B.tr[b2][b1][0], forces, A.umac[d], A.lo[d][d], A.hi[d][d], ADb, A.tr[b1][b2][0],
-              A.tr[b2][b1][0], A.forces);
+    KS_LAUNCH(c, k_adj_pm_final<TI>, nblocks(nf, BS), BS, B8 * (2.0 * g.N + 3.0 * nf + 3.0 * (nfaces(g, b1) + nfaces(g, b2))) +
+              sizeof(TI) * (2.0 * nf + 2.0 * (nfaces(g, b1) + nfaces(g, b2))), g, d, dt, dt / (4.0 * hd(g, b1)), dt / (4.0 * hd(g, b2)),
+              ti<TI>(B.lo[d][d]), ti<TI>(B.hi[d][d]), AD, ti<TI>(B.tr[b1][b2][0]), ti<TI>(B.tr[b2][b1][0]), forces, A.umac[d], A.lo[d][d],
+              A.hi[d][d], ADb, A.tr[b1][b2][0], A.tr[b2][b1][0], A.forces);
 }
-void launch_adj_adv_trans(Ctx& c, const Grid& g, int a, int b, const double* u, double rho, double dt, const double* const mac[3],
-                          const GodunovBufs& B, const AdjBufs& A) {
-    K3 E{{(double*)B.tedge[b][0], (double*)B.tedge[b][1], (double*)B.tedge[b][2]}};
+void launch_adj_pm_final(Ctx& c, const Grid& g, int d, double dt, const GodunovBufs& B, const double* forces, const AdjBufs& A, int fp32) {
+    if (fp32) adj_pm_final_t<float>(c, g, d, dt, B, forces, A);
+    else adj_pm_final_t<double>(c, g, d, dt, B, forces, A);
+}
+
+template <typename TI>
+static void adj_adv_trans_t(Ctx& c, const Grid& g, int a, int b, const double* u, double rho, double dt, const double* const mac[3],
+                            const GodunovBufs& B, const AdjBufs& A) {
+    KI<TI> E{{ti<TI>(B.tedge[b][0]), ti<TI>(B.tedge[b][1]), ti<TI>(B.tedge[b][2])}};
     K3 Ob{{A.tr[a][b][0], A.tr[a][b][1], A.tr[a][b][2]}};
     A3 LOb{{A.lo[a][0], A.lo[a][1], A.lo[a][2]}}, HIb{{A.hi[a][0], A.hi[a][1], A.hi[a][2]}};
     A3 Ebb{{A.tedge[b][0], A.tedge[b][1], A.tedge[b][2]}};
     const long long na = nfaces(g, a), nb = nfaces(g, b);
-    KS_LAUNCH(c, k_adj_adv_trans, nblocks(na, BS), BS, B8 * (6.0 * g.N + 10.0 * na + 8.0 * nb), g, a, b, u, rho, dt / (3.0 * hd(g, b)), mac[a],
-              mac[b], E, Ob, LOb, HIb, Ebb, A.umac[b], A.u);
+    KS_LAUNCH(c, k_adj_adv_trans<TI>, nblocks(na, BS), BS, B8 * (6.0 * g.N + 10.0 * na + 5.0 * nb) + sizeof(TI) * 3.0 * nb, g, a, b, u, rho,
+              dt / (3.0 * hd(g, b)), mac[a], mac[b], E, Ob, LOb, HIb, Ebb, A.umac[b], A.u);
 }
-void launch_adj_adv_flux(Ctx& c, const Grid& g, int d, const double* u, const double* forces, double rho, double dt, const double* const mac[3],
-                         const GodunovBufs& B, const AdjBufs& A) {
+void launch_adj_adv_trans(Ctx& c, const Grid& g, int a, int b, const double* u, double rho, double dt, const double* const mac[3],
+                          const GodunovBufs& B, const AdjBufs& A, int fp32) {
+    if (fp32) adj_adv_trans_t<float>(c, g, a, b, u, rho, dt, mac, B, A);
+    else adj_adv_trans_t<double>(c, g, a, b, u, rho, dt, mac, B, A);
+}
+
+template <typename TI>
+static void adj_adv_flux_t(Ctx& c, const Grid& g, int d, const double* u, const double* forces, double rho, double dt, const double* const mac[3],
+                           const GodunovBufs& B, const AdjBufs& A) {
     const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
     K3 Uf{{mac[0], mac[1], mac[2]}};
-    K3 LO{{(double*)B.lo[d][0], (double*)B.lo[d][1], (double*)B.lo[d][2]}}, HI{{(double*)B.hi[d][0], (double*)B.hi[d][1], (double*)B.hi[d][2]}};
-    K3 T1{{(double*)B.tr[b1][b2][0], (double*)B.tr[b1][b2][1], (double*)B.tr[b1][b2][2]}};
-    K3 T2{{(double*)B.tr[b2][b1][0], (double*)B.tr[b2][b1][1], (double*)B.tr[b2][b1][2]}};
+    KI<TI> LO{{ti<TI>(B.lo[d][0]), ti<TI>(B.lo[d][1]), ti<TI>(B.lo[d][2])}}, HI{{ti<TI>(B.hi[d][0]), ti<TI>(B.hi[d][1]), ti<TI>(B.hi[d][2])}};
+    KI<TI> T1{{ti<TI>(B.tr[b1][b2][0]), ti<TI>(B.tr[b1][b2][1]), ti<TI>(B.tr[b1][b2][2])}};
+    KI<TI> T2{{ti<TI>(B.tr[b2][b1][0]), ti<TI>(B.tr[b2][b1][1]), ti<TI>(B.tr[b2][b1][2])}};
     K3 Fb{{A.flux[d][0], A.flux[d][1], A.flux[d][2]}};
     A3 Ufb{{A.umac[0], A.umac[1], A.umac[2]}};
     A3 LOb{{A.lo[d][0], A.lo[d][1], A.lo[d][2]}}, HIb{{A.hi[d][0], A.hi[d][1], A.hi[d][2]}};
     A3 T1b{{A.tr[b1][b2][0], A.tr[b1][b2][1], A.tr[b1][b2][2]}}, T2b{{A.tr[b2][b1][0], A.tr[b2][b1][1], A.tr[b2][b1][2]}};
-    const long long nf = nfaces(g, d);
-    KS_LAUNCH(c, k_adj_adv_flux, nblocks(nf, BS), BS, B8 * (12.0 * g.N + 14.0 * nf + 14.0 * (nfaces(g, b1) + nfaces(g, b2))), g, d, u, forces,
-              rho, dt, dt / (2.0 * hd(g, b1)), dt / (2.0 * hd(g, b2)), Uf, LO, HI, T1, T2, Fb, Ufb, LOb, HIb, T1b, T2b, A.u, A.forces);
+    const long long nf = nfaces(g, d), nt = nfaces(g, b1) + nfaces(g, b2);
+    KS_LAUNCH(c, k_adj_adv_flux<TI>, nblocks(nf, BS), BS, B8 * (12.0 * g.N + 10.0 * nf + 8.0 * nt) + sizeof(TI) * (6.0 * nf + 6.0 * nt), g, d, u,
+              forces, rho, dt, dt / (2.0 * hd(g, b1)), dt / (2.0 * hd(g, b2)), Uf, LO, HI, T1, T2, Fb, Ufb, LOb, HIb, T1b, T2b, A.u, A.forces);
+}
+void launch_adj_adv_flux(Ctx& c, const Grid& g, int d, const double* u, const double* forces, double rho, double dt, const double* const mac[3],
+                         const GodunovBufs& B, const AdjBufs& A, int fp32) {
+    if (fp32) adj_adv_flux_t<float>(c, g, d, u, forces, rho, dt, mac, B, A);
+    else adj_adv_flux_t<double>(c, g, d, u, forces, rho, dt, mac, B, A);
 }
 void launch_adj_div(Ctx& c, const Grid& g, const double* convb, const AdjBufs& A) {
     for (int d = 0; d < 3; ++d) {

@@ -73,7 +73,28 @@ void Sim::adj_alloc() {
     S->sp.alloc(p_.n);
     S->mub.alloc(N);
     S->wgb.alloc(2 * (size_t)g_.nx * g_.ny);
-    S->macs.alloc(2 * N + NF);
+    // post-MAC intermediates of the recompute: lo, hi, tedge, flux per direction and tr
+    size_t total2 = 0;
+    for (int d = 0; d < 3; ++d) total2 += fsz[d] * 12 + 2 * 3 * fsz[d];
+    S->gbuf2.alloc(total2);
+    GodunovBufs& G2 = S->gb2;
+    q = S->gbuf2.p;
+    for (int d = 0; d < 3; ++d) {
+        G2.ad[d] = gb_.ad[d];
+        for (int n = 0; n < 3; ++n) {
+            G2.edge[d][n] = gb_.edge[d][n];  // the unlimited edges are shared by both passes
+            G2.lo[d][n] = q; q += fsz[d];
+            G2.hi[d][n] = q; q += fsz[d];
+            G2.tedge[d][n] = q; q += fsz[d];
+            G2.flux[d][n] = q; q += fsz[d];
+        }
+    }
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+            for (int n = 0; n < 3; ++n) {
+                G2.tr[a][b][n] = nullptr;
+                if (a != b) { G2.tr[a][b][n] = q; q += fsz[a]; }
+            }
     size_t maxpts = 1;
     for (auto& d : disks_) maxpts = std::max(maxpts, (size_t)d.nr * d.nt);
     S->pts.alloc(4 * maxpts);
@@ -206,20 +227,22 @@ void Sim::adjoint_step_impl(bool seed) {
     AdjBufs& A = S.A;
     const long long N3 = 3 * g_.N;
     const double dt = t_.dt[0], sigma = dt / rho_, dr = dt / rho_;
-    struct Restore {  // Godunov precision and clock, also when a solve throws
+    struct Restore {  // post-MAC buffers and clock, also when a solve throws
         Sim& s;
         Clock clock;
         ~Restore() {
-            s.godunov64_ = 0;
+            s.adv_bufs_ = nullptr;
             s.t_ = clock;
         }
     } restore{*this, t_};
-    // The linearisation point is recomputed with FP64 Godunov passes (the
-    // reverse kernels read their FP64 intermediates).  A mixed-precision
-    // handle keeps its FP32 multigrid cycles: the FP64 defect correction
-    // brings both projections to the FP64 tolerance, here and in the two
-    // reverse solves.
-    godunov64_ = 1;
+    // The linearisation point is the handle's own forward step, recomputed
+    // at its precision: a mixed-precision handle's reverse kernels read the
+    // FP32 Godunov intermediates its forward used (and accumulate in FP64);
+    // its multigrid keeps FP32 cycles under the FP64 defect correction, here
+    // and in the two reverse solves.  The post-MAC pass writes its own
+    // buffers so that the pre-MAC intermediates survive for the reverse.
+    adv_bufs_ = &S.gb2;
+    const int fp32 = mixed_;
     launch_copy(ctx_, S.su.p, vel_.p, N3);
     launch_copy(ctx_, S.sgp.p, gp_.p, N3);
     launch_copy(ctx_, S.sp.p, p_.p, (long long)p_.n);
@@ -259,11 +282,11 @@ void Sim::adjoint_step_impl(bool seed) {
     launch_fill(ctx_, A.forces, 0.0, N3);
     const double* mac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
     launch_adj_div(ctx_, g_, S.srcb.p, A);
-    for (int d = 0; d < 3; ++d) launch_adj_adv_flux(ctx_, g_, d, vel_old_.p, forces_.p, rho_, dt, mac, gb_, A);
+    for (int d = 0; d < 3; ++d) launch_adj_adv_flux(ctx_, g_, d, vel_old_.p, forces_.p, rho_, dt, mac, S.gb2, A, fp32);
     for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 3; ++b)
-            if (a != b) launch_adj_adv_trans(ctx_, g_, a, b, vel_old_.p, rho_, dt, mac, gb_, A);
-    for (int a = 0; a < 3; ++a) launch_adj_faces(ctx_, g_, a, 1, vel_old_.p, gb_, A, dt, rho_, umac_[a].p);
+            if (a != b) launch_adj_adv_trans(ctx_, g_, a, b, vel_old_.p, rho_, dt, mac, S.gb2, A, fp32);
+    for (int a = 0; a < 3; ++a) launch_adj_faces(ctx_, g_, a, 1, vel_old_.p, S.gb2, A, dt, rho_, umac_[a].p, fp32);
     // ---- MAC projection (symmetric on the faces it changes): the pre-MAC
     // output on wall faces is 0 whatever the input, so their adjoint is dropped
     if (!g_.zper) {
@@ -284,9 +307,7 @@ void Sim::adjoint_step_impl(bool seed) {
         } swap(umac_, A.umac);
         mac_project();
     }
-    // ---- pre-MAC pass: its intermediates were overwritten by the post-MAC pass
-    double* macs[3] = {S.macs.p, S.macs.p + g_.N, S.macs.p + 2 * g_.N};
-    launch_premac(ctx_, g_, vel_old_.p, forces_.p, dt, gb_, macs, 0);
+    // ---- pre-MAC pass (its intermediates are in gb_)
     const size_t fsz[3] = {(size_t)g_.N, (size_t)g_.N, (size_t)g_.NFz};
     for (int d = 0; d < 3; ++d) {
         ck(cudaMemsetAsync(A.ad[d], 0, fsz[d] * sizeof(double), ctx_.stream), "memset");
@@ -298,12 +319,12 @@ void Sim::adjoint_step_impl(bool seed) {
         for (int b = 0; b < 3; ++b)
             if (b != d) ck(cudaMemsetAsync(A.tr[d][b][0], 0, fsz[d] * sizeof(double), ctx_.stream), "memset");
     }
-    for (int d = 0; d < 3; ++d) launch_adj_pm_final(ctx_, g_, d, dt, gb_, forces_.p, A);
+    for (int d = 0; d < 3; ++d) launch_adj_pm_final(ctx_, g_, d, dt, gb_, forces_.p, A, fp32);
     const int tpl[6][3] = {{1, 2, 0}, {2, 1, 0}, {0, 2, 1}, {2, 0, 1}, {0, 1, 2}, {1, 0, 2}};
-    for (auto& t : tpl) launch_adj_pm_trans(ctx_, g_, t[0], t[1], t[2], dt, gb_, A);
-    for (int d = 0; d < 3; ++d) launch_adj_faces(ctx_, g_, d, 0, vel_old_.p, gb_, A, dt, 1.0, nullptr);
+    for (auto& t : tpl) launch_adj_pm_trans(ctx_, g_, t[0], t[1], t[2], dt, gb_, A, fp32);
+    for (int d = 0; d < 3; ++d) launch_adj_faces(ctx_, g_, d, 0, vel_old_.p, gb_, A, dt, 1.0, nullptr, fp32);
     // ---- unlimited edges (shared by both passes)
-    for (int d = 0; d < 3; ++d) launch_adj_edges(ctx_, g_, d, vel_old_.p, A.edge[d], ub);
+    for (int d = 0; d < 3; ++d) launch_adj_edges(ctx_, g_, d, vel_old_.p, A.edge[d], ub, fp32);
     // ---- forces = (src + dold)/rho
     launch_axpby(ctx_, N3, 1.0, S.srcb.p, 1.0 / rho_, A.forces, S.srcb.p);
     launch_axpby(ctx_, N3, 1.0, S.doldb.p, 1.0 / rho_, A.forces, S.doldb.p);

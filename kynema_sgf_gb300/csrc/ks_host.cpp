@@ -146,6 +146,7 @@ void Sim::setup(const Deck& D) {
         m.maxiter = D.flag(p + ".maxiter", m.maxiter);
         m.nu1 = D.flag(p + ".num_pre_smooth", m.nu1);
         m.nu2 = D.flag(p + ".num_post_smooth", m.nu2);
+        m.fixed_iters = D.flag(p + ".do_fixed_iters", m.fixed_iters);
     };
     mg(mac_, "mac_proj");
     mg(nod_, "nodal_proj");
@@ -597,9 +598,12 @@ void Sim::mac_project() {
         rn = reduce(np, 1, 1, nullptr);
         ++it;
         if (!std::isfinite(rn)) throw KsError(KS_ERR_NONFINITE, "MAC projection diverged");
+        if (rn > 1e20 * r0) throw KsError(KS_ERR_NOT_CONVERGED, "MAC projection diverged (residual above 1e20 times the initial one)");
     }
-    // MLMG aborts when maxiter is reached above the tolerance (MLMG::solve)
-    if (rn > target) throw KsError(KS_ERR_NOT_CONVERGED, "MAC projection did not converge in mac_proj.maxiter V-cycles");
+    // MLMGOptions sets fixed-iteration mode by default (src/core/MLMGOptions.H:126-128,
+    // MLMGOptions.cpp:65-66): MLMG then stops at maxiter without aborting;
+    // with do_fixed_iters = 0 it aborts
+    if (rn > target && !mac_.fixed_iters) throw KsError(KS_ERR_NOT_CONVERGED, "MAC projection did not converge in mac_proj.maxiter V-cycles");
     mac_it_ = it;
     mac_r_ = rn;
     launch_mac_correct(ctx_, g_, L.phi, umac_[0].p, umac_[1].p, umac_[2].p, beta);
@@ -663,6 +667,7 @@ void Sim::nd_solve(double sigma) {
             rn = reduce(np, 1, 1, nullptr);
             ++it;
             if (!std::isfinite(rn)) throw KsError(KS_ERR_NONFINITE, "nodal projection diverged");
+            if (rn > 1e20 * r0) throw KsError(KS_ERR_NOT_CONVERGED, "nodal projection diverged (residual above 1e20 times the initial one)");
         }
     } else {
         // The first pre-smoothing sweep of each V-cycle evaluates the residual
@@ -677,13 +682,14 @@ void Sim::nd_solve(double sigma) {
                 nod_r0_ = rn;
                 target = std::max(nod_.atol, nod_.rtol * rn);
             }
+            if (rn > 1e20 * nod_r0_) throw KsError(KS_ERR_NOT_CONVERGED, "nodal projection diverged (residual above 1e20 times the initial one)");
             if (rn <= target || it >= nod_.maxiter) break;
             if (nod_.nu1 > 0) std::swap(L.phi, L.tmp);
             nd_vcycle(nd_, 0, sigma, nod_.nu1 > 0 ? 1 : 0);
             ++it;
         }
     }
-    if (rn > target) throw KsError(KS_ERR_NOT_CONVERGED, "nodal projection did not converge in nodal_proj.maxiter V-cycles");
+    if (rn > target && !nod_.fixed_iters) throw KsError(KS_ERR_NOT_CONVERGED, "nodal projection did not converge in nodal_proj.maxiter V-cycles");
     nod_it_ = it;
     nod_r_ = rn;
 }
@@ -708,11 +714,10 @@ void Sim::apply_predictor(bool incremental) {
     for (int m = 0; m < 9; ++m) fl[m] = static_cast<double*>(gb_.flux[m / 3][m % 3]);
     launch_divtau(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, divtau_.p, 1, src_.p, forces_.p, nullptr, nullptr, dt, rho_, fl);
     double* mac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
-    const int g32 = mixed_ && !godunov64_;
-    launch_premac(ctx_, g_, vel_old_.p, forces_.p, dt, gb_, mac, g32);
+    launch_premac(ctx_, g_, vel_old_.p, forces_.p, dt, gb_, mac, mixed_);
     mac_project();
     const double* cmac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
-    launch_advection(ctx_, g_, vel_old_.p, forces_.p, cmac, dt, rho_, gb_, conv_.p, g32);
+    launch_advection(ctx_, g_, vel_old_.p, forces_.p, cmac, dt, rho_, adv_bufs_ ? *adv_bufs_ : gb_, conv_.p, mixed_);
     // compute_source_term(NPH) and compute_diffusion_term(Old) reproduce src
     // and divtau on this path (Coriolis reads the Old velocity, gp unchanged).
     launch_predictor_rhs(ctx_, g_, vel_old_.p, conv_.p, src_.p, divtau_.p, vel_.p, dt, rho_);

@@ -162,15 +162,17 @@ struct AdjBufs {
     double* u;
     double* forces;
 };
-void launch_adj_edges(Ctx& c, const Grid& g, int d, const double* u, double* const Eb[3], double* ub);
+// fp32: the forward intermediates in B are FP32 (mixed-precision Godunov passes);
+// the reverse arithmetic is FP64 either way
+void launch_adj_edges(Ctx& c, const Grid& g, int d, const double* u, double* const Eb[3], double* ub, int fp32);
 void launch_adj_faces(Ctx& c, const Grid& g, int d, int mode, const double* u, const GodunovBufs& B, const AdjBufs& A, double dt, double rho,
-                      const double* umac_d);
-void launch_adj_pm_trans(Ctx& c, const Grid& g, int a, int b, int n, double dt, const GodunovBufs& B, const AdjBufs& A);
-void launch_adj_pm_final(Ctx& c, const Grid& g, int d, double dt, const GodunovBufs& B, const double* forces, const AdjBufs& A);
+                      const double* umac_d, int fp32);
+void launch_adj_pm_trans(Ctx& c, const Grid& g, int a, int b, int n, double dt, const GodunovBufs& B, const AdjBufs& A, int fp32);
+void launch_adj_pm_final(Ctx& c, const Grid& g, int d, double dt, const GodunovBufs& B, const double* forces, const AdjBufs& A, int fp32);
 void launch_adj_adv_trans(Ctx& c, const Grid& g, int a, int b, const double* u, double rho, double dt, const double* const mac[3],
-                          const GodunovBufs& B, const AdjBufs& A);
+                          const GodunovBufs& B, const AdjBufs& A, int fp32);
 void launch_adj_adv_flux(Ctx& c, const Grid& g, int d, const double* u, const double* forces, double rho, double dt, const double* const mac[3],
-                         const GodunovBufs& B, const AdjBufs& A);
+                         const GodunovBufs& B, const AdjBufs& A, int fp32);
 void launch_adj_div(Ctx& c, const Grid& g, const double* convb, const AdjBufs& A);
 // reverse of divtau(vel; mueff, wg) for the adjoint s * divtau_b: accumulates the
 // velocity (ub), cell viscosity (mub, may be null) and wall-gradient (wgb, may be null) adjoints

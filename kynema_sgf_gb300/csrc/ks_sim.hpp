@@ -164,6 +164,7 @@ struct Disk {
 struct MGParams {
     double rtol = 1.0e5 * 2.220446049250313e-16, atol = 1.0e2 * 2.220446049250313e-16;
     int maxiter = 200, nu1 = 2, nu2 = 2, bottom = 100;
+    int fixed_iters = 1;  // MLMGOptions do_fixed_iters: stop at maxiter without an error
     double omega = 0.9;
 };
 
@@ -199,7 +200,8 @@ struct AdjState {
     DevBuf<double> w, t1, t2, srcb, doldb, forcesb;  // 3N scratch
     DevBuf<double> mub, wgb;        // adjoints of mu_eff (N) and of the wall-model gradient (2 nx ny)
     DevBuf<double> umacb[3];        // adjoint of the MAC velocities
-    DevBuf<double> macs;            // pre-MAC recompute output (discarded)
+    DevBuf<double> gbuf2;           // post-MAC intermediates of the recompute (the pre-MAC ones stay in gb_)
+    GodunovBufs gb2{};
     DevBuf<double> su, sgp, sp;     // forward state saved across a reverse step
     DevBuf<double> fu, fgp, fp;     // forward state at the end of an adjoint run
     DevBuf<double> snaps;           // binomial checkpoints, 6N values per slot
@@ -253,7 +255,7 @@ class Sim {
     Clock t_;
     int mac_it_ = 0, nod_it_ = 0;
     int mixed_ = 0;  // 1: FP32 advection and multigrid cycles with FP64 defect correction
-    int godunov64_ = 0;  // 1: FP64 Godunov passes even when mixed_ (reverse-step recompute)
+    GodunovBufs* adv_bufs_ = nullptr;  // post-MAC pass scratch when not gb_ (reverse-step recompute keeps both passes)
     double mac_r0_ = 0, mac_r_ = 0, nod_r0_ = 0, nod_r_ = 0;
     std::string err_;
 

@@ -190,6 +190,7 @@ struct MGOpts {
     double rtol = 1.0e5 * kEps, atol = 1.0e2 * kEps;
     int maxiter = 200, nu1 = 2, nu2 = 2, bottom = 100;
     double omega = 0.9;  // nodal Jacobi weight
+    int fixed_iters = 1;  // MLMGOptions do_fixed_iters: stop at maxiter without an error
 };
 
 struct SimTime {
@@ -381,6 +382,7 @@ void Sim::setup(const std::string& text) {
         o.maxiter = D.i(pfx + ".maxiter", o.maxiter);
         o.nu1 = D.i(pfx + ".num_pre_smooth", o.nu1);
         o.nu2 = D.i(pfx + ".num_post_smooth", o.nu2);
+        o.fixed_iters = D.i(pfx + ".do_fixed_iters", o.fixed_iters);
     };
     rd(mac, "mac_proj");
     rd(nod, "nodal_proj");
@@ -1186,9 +1188,10 @@ void Sim::mac_project() {
         rn = cc_residual(L, beta, zper);
         ++it;
         if (!std::isfinite(rn)) throw Error(ERR_NONFINITE, "MAC projection diverged");
+        if (rn > 1e20 * r0) throw Error(ERR_NOT_CONVERGED, "MAC projection diverged (residual above 1e20 times the initial one)");
     }
-    // MLMG aborts when maxiter is reached above the tolerance (MLMG::solve)
-    if (rn > target) throw Error(ERR_NOT_CONVERGED, "MAC projection did not converge in mac_proj.maxiter V-cycles");
+    // fixed-iteration mode is the MLMGOptions default (MLMGOptions.H:126-128): no abort at maxiter
+    if (rn > target && !mac.fixed_iters) throw Error(ERR_NOT_CONVERGED, "MAC projection did not converge in mac_proj.maxiter V-cycles");
     mac_iters = it;
     mac_res = rn;
     cc_fill(L.phi, L.n, zper);
@@ -1562,8 +1565,9 @@ void Sim::nodal_project(double time, double scaling, bool incremental) {
         rn = nd_residual(L, sigma, zper);
         ++it;
         if (!std::isfinite(rn)) throw Error(ERR_NONFINITE, "nodal projection diverged");
+        if (rn > 1e20 * r0) throw Error(ERR_NOT_CONVERGED, "nodal projection diverged (residual above 1e20 times the initial one)");
     }
-    if (rn > target) throw Error(ERR_NOT_CONVERGED, "nodal projection did not converge in nodal_proj.maxiter V-cycles");
+    if (rn > target && !nod.fixed_iters) throw Error(ERR_NOT_CONVERGED, "nodal projection did not converge in nodal_proj.maxiter V-cycles");
     nodal_iters = it;
     nodal_res = rn;
     nd_fill(L.phi, L, zper);

@@ -39,3 +39,16 @@ def test_null_handle_is_rejected(ks_lib):
     lib = ks_lib.load_library()
     assert lib.ks_init_data(None) == 6
     assert lib.ks_apply_corrector(None) == 6
+
+
+def test_driver_executable_usage(ks_lib):
+    """ks_run mirrors the reference executable's argument handling (no device needed)."""
+    import subprocess
+    from kynema_sgf_gb300 import build
+    exe = build.driver_path()
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 1 and "Usage:" in r.stdout and "No input file" in r.stderr
+    r = subprocess.run([exe, "--help"], capture_output=True, text=True)
+    assert r.returncode == 0 and "param=value" in r.stdout
+    r = subprocess.run([exe, "/nonexistent/deck.inp"], capture_output=True, text=True)
+    assert r.returncode == 1 and "does not exist" in r.stderr

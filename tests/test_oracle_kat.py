@@ -236,9 +236,13 @@ def test_projections_converge_on_anisotropic_cells(oracle_mod):
 
 
 def test_maxiter_reports_not_converged(oracle_mod):
-    """MLMG aborts when maxiter is reached above the tolerance; the status is
-    KS_ERR_NOT_CONVERGED (3)."""
+    """MLMGOptions runs MLMG in fixed-iteration mode by default (no abort at
+    maxiter, MLMGOptions.H:126-128); with do_fixed_iters = 0 a solve that ends
+    above the tolerance is KS_ERR_NOT_CONVERGED (3)."""
     o = oracle_mod.Oracle(decks.tgv(16, steps=2) + "\nnodal_proj.maxiter = 1\n")
+    o.InitData()
+    assert o.scalar("nodal_iters") == 1
+    o = oracle_mod.Oracle(decks.tgv(16, steps=2) + "\nnodal_proj.maxiter = 1\nnodal_proj.do_fixed_iters = 0\n")
     with pytest.raises(oracle_mod.OracleError) as e:
         o.InitData()
     assert e.value.code == 3

@@ -142,7 +142,7 @@ def test_anisotropic_cells(cuda_dev, oracle_mod):
 
 
 def test_maxiter_reports_not_converged(cuda_dev):
-    g = cuda_dev.Incflo(decks.tgv(16, steps=2) + "\nnodal_proj.maxiter = 1\n")
+    g = cuda_dev.Incflo(decks.tgv(16, steps=2) + "\nnodal_proj.maxiter = 1\nnodal_proj.do_fixed_iters = 0\n")
     with pytest.raises(cuda_dev.KsError) as e:
         g.InitData()
     assert e.value.code == 3
