@@ -252,8 +252,18 @@ def our_arm(args, rank, world, local_rank):
         del sim
         mx = ks.Incflo(decks.abl(nx, ny, nz, steps=10 ** 9) + "\nks.precision = mixed\n")
         mx.InitData()
-        for _ in range(args.warmup):
+        for w in range(args.warmup):
+            if args.profile_all and w == args.warmup - 1:
+                mx.profile_kernels("*")
             mx.step()
+        if args.profile_all and rank == 0:
+            rep = mx.profile_report()
+            mx.profile_kernels("")
+            tot = sum(v[1] for v in rep.values())
+            sys.stderr.write("-- mixed precision step --\n")
+            for k, v in sorted(rep.items(), key=lambda kv: -kv[1][1]):
+                sys.stderr.write("%-22s %6d launches %9.3f ms %5.1f%% %8.1f GB/s\n" % (k, v[0], v[1], 100 * v[1] / tot,
+                                                                                      v[2] / (v[1] * 1e-3) / 1e9 if v[1] else 0))
         stream = torch.cuda.ExternalStream(mx.stream())
         if dist:
             tdist.barrier()

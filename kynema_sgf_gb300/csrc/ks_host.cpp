@@ -571,9 +571,20 @@ void Sim::mac_project() {
         L.inv_diag[0] = 1.0 / (-beta * (d0 + 2.0 * L.iz2));
         L.inv_diag[1] = 1.0 / (-beta * (d0 + L.iz2));
         L.inv_diag[2] = 1.0 / (-beta * d0);
+        const double dc[3] = {d0 + 2.0 * L.iz2, d0 + L.iz2, d0};
+        for (int m = 0; m < 3; ++m) {
+            L.dg[m] = -beta * dc[m];
+            L.gs[m][0] = L.ix2 / dc[m];
+            L.gs[m][1] = L.iy2 / dc[m];
+            L.gs[m][2] = L.iz2 / dc[m];
+        }
     }
     for (size_t l = 0; l < cc32_.size(); ++l)
-        for (int m = 0; m < 3; ++m) cc32_[l].inv_diag[m] = (float)cc_[l].inv_diag[m];
+        for (int m = 0; m < 3; ++m) {
+            cc32_[l].inv_diag[m] = (float)cc_[l].inv_diag[m];
+            cc32_[l].dg[m] = (float)cc_[l].dg[m];
+            for (int q = 0; q < 3; ++q) cc32_[l].gs[m][q] = (float)cc_[l].gs[m][q];
+        }
     CCLevelDev& L = cc_[0];
     int np = 0;
     launch_mac_rhs(ctx_, g_, umac_[0].p, umac_[1].p, umac_[2].p, L.rhs, parts_.p, &np);

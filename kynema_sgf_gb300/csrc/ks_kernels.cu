@@ -313,6 +313,115 @@ __global__ void k_tau_div(Grid g, Flux9 F, double* out, int mode, const double* 
     }
 }
 
+// ---- fused tiled form of k_tau_flux + k_tau_div.  A block owns a
+// TX x TY x TZ tile of cells; it stages the velocity seen by the flux stencil
+// (VelDiff, ghosts included) and mu_eff for the tile plus a one-cell halo in
+// shared memory, computes every face flux the tile needs once (the same
+// arithmetic as tensor_flux) into shared memory, then forms the divergence
+// and the mode epilogue of k_tau_div for its cells.  No face arrays touch HBM.
+constexpr int TTX = 32, TTY = 4, TTZ = 4;
+constexpr int THX = TTX + 2, THY = TTY + 2, THZ = TTZ + 2;
+constexpr int TNH = THX * THY * THZ;
+constexpr int TNFX = (TTX + 1) * TTY * TTZ, TNFY = TTX * (TTY + 1) * TTZ, TNFZ = TTX * TTY * (TTZ + 1);
+constexpr size_t TAU_SMEM = sizeof(double) * (4 * (size_t)TNH + 3 * ((size_t)TNFX + TNFY + TNFZ));
+
+__global__ void __launch_bounds__(TTX* TTY* TTZ) k_divtau_tile(Grid g, const double* vel, const double* mueff, const double* wg, double* out,
+                                                               int mode, const double* src, double* forces, const double* base,
+                                                               const double* dold, double dt, double rho) {
+    extern __shared__ double sm[];
+    double* sV = sm;                // [3][THZ][THY][THX]
+    double* sM = sm + 3 * TNH;      // [THZ][THY][THX]
+    double* sFx = sm + 4 * TNH;     // [3][TTZ][TTY][TTX + 1]
+    double* sFy = sFx + 3 * TNFX;   // [3][TTZ][TTY + 1][TTX]
+    double* sFz = sFy + 3 * TNFY;   // [3][TTZ + 1][TTY][TTX]
+    const int i0 = blockIdx.x * TTX, j0 = blockIdx.y * TTY, k0 = blockIdx.z * TTZ;
+    const int tid = threadIdx.x;
+    const int nthr = TTX * TTY * TTZ;
+    const VelDiff V{vel, wg, g};
+    auto hidx = [](int hx, int hy, int hz) { return (hz * THY + hy) * THX + hx; };
+    for (int h = tid; h < TNH; h += nthr) {
+        const int hx = h % THX, hy = (h / THX) % THY, hz = h / (THX * THY);
+        // a tile may be wider than the grid (nx < TTX): wrap x, y (and periodic z) fully
+        const int gi = ((i0 + hx - 1) % g.nx + g.nx) % g.nx, gj = ((j0 + hy - 1) % g.ny + g.ny) % g.ny;
+        int gk = k0 + hz - 1;
+        if (g.zper) gk = (gk % g.nz + g.nz) % g.nz;
+        for (int n = 0; n < 3; ++n) sV[n * TNH + h] = V(n, gi, gj, gk);
+        const int kk = g.zper ? gk : (gk < 0 ? 0 : (gk >= g.nz ? g.nz - 1 : gk));
+        sM[h] = mueff[cidx(g, gi, gj, kk)];
+    }
+    __syncthreads();
+    const double ih[3] = {g.idx, g.idy, g.idz};
+    // flux through the d-face at the low side of halo cell (hx, hy, hz)
+    auto flux = [&](int d, int hx, int hy, int hz, int gk, double F[3]) {
+        const int e0 = (d == 0), e1 = (d == 1), e2 = (d == 2);
+        const int mx = hx - e0, my = hy - e1, mz = hz - e2;
+        double mf;
+        if (d == 2 && !g.zper && gk == 0) mf = sM[hidx(hx, hy, hz)];
+        else if (d == 2 && !g.zper && gk == g.nz) mf = sM[hidx(mx, my, mz)];
+        else mf = 0.5 * (sM[hidx(mx, my, mz)] + sM[hidx(hx, hy, hz)]);
+        double gr[3][3];
+        for (int n = 0; n < 3; ++n) {
+            const double* v = sV + n * TNH;
+            for (int m = 0; m < 3; ++m) {
+                if (m == d) {
+                    gr[m][n] = (v[hidx(hx, hy, hz)] - v[hidx(mx, my, mz)]) * ih[m];
+                } else {
+                    const int f0 = (m == 0), f1 = (m == 1), f2 = (m == 2);
+                    gr[m][n] = 0.25 *
+                               (v[hidx(hx + f0, hy + f1, hz + f2)] + v[hidx(mx + f0, my + f1, mz + f2)] - v[hidx(hx - f0, hy - f1, hz - f2)] -
+                                v[hidx(mx - f0, my - f1, mz - f2)]) *
+                               ih[m];
+                }
+            }
+        }
+        const double dv = gr[0][0] + gr[1][1] + gr[2][2];
+        for (int n = 0; n < 3; ++n) {
+            if (n == d) F[n] = mf * (2.0 * gr[d][d] - (2.0 / 3.0) * dv);
+            else F[n] = mf * (gr[d][n] + gr[n][d]);
+        }
+    };
+    for (int f = tid; f < TNFX + TNFY + TNFZ; f += nthr) {
+        double F[3];
+        if (f < TNFX) {
+            const int fx = f % (TTX + 1), fy = (f / (TTX + 1)) % TTY, fz = f / ((TTX + 1) * TTY);
+            flux(0, fx + 1, fy + 1, fz + 1, k0 + fz, F);
+            for (int n = 0; n < 3; ++n) sFx[n * TNFX + f] = F[n];
+        } else if (f < TNFX + TNFY) {
+            const int q = f - TNFX;
+            const int fx = q % TTX, fy = (q / TTX) % (TTY + 1), fz = q / (TTX * (TTY + 1));
+            flux(1, fx + 1, fy + 1, fz + 1, k0 + fz, F);
+            for (int n = 0; n < 3; ++n) sFy[n * TNFY + q] = F[n];
+        } else {
+            const int q = f - TNFX - TNFY;
+            const int fx = q % TTX, fy = (q / TTX) % TTY, fz = q / (TTX * TTY);
+            flux(2, fx + 1, fy + 1, fz + 1, k0 + fz, F);
+            for (int n = 0; n < 3; ++n) sFz[n * TNFZ + q] = F[n];
+        }
+    }
+    __syncthreads();
+    const int tx = tid % TTX, ty = (tid / TTX) % TTY, tz = tid / (TTX * TTY);
+    const int i = i0 + tx, j = j0 + ty, k = k0 + tz;
+    if (i >= g.nx || j >= g.ny || k >= g.nz) return;
+    const double irho = 1.0 / rho;
+    const long long N = g.N, t = cidx(g, i, j, k);
+    for (int n = 0; n < 3; ++n) {
+        const int ax = (tz * TTY + ty) * (TTX + 1) + tx;
+        const int ay = (tz * (TTY + 1) + ty) * TTX + tx;
+        const int az = (tz * TTY + ty) * TTX + tx;
+        double acc = (sFx[n * TNFX + ax + 1] - sFx[n * TNFX + ax]) * ih[0];
+        acc += (sFy[n * TNFY + ay + TTX] - sFy[n * TNFY + ay]) * ih[1];
+        acc += (sFz[n * TNFZ + az + TTX * TTY] - sFz[n * TNFZ + az]) * ih[2];
+        if (mode == 0) {
+            out[n * N + t] = acc;
+        } else if (mode == 1) {
+            out[n * N + t] = acc;
+            forces[n * N + t] = (src[n * N + t] + acc) * irho;
+        } else {
+            out[n * N + t] = base[n * N + t] + 0.5 * dt * (acc - dold[n * N + t]) * irho;
+        }
+    }
+}
+
 // predictor_rhs, Explicit (src/equation_systems/CompRHSOps.H:32-141)
 __global__ void k_pred_rhs(long long N3, const double* vo, const double* conv, const double* src, const double* dt_, double* vel, double dt,
                            double rho) {
@@ -568,8 +677,9 @@ void launch_wall_grad(Ctx& c, const Grid& g, const double* vel_old, const double
     KS_LAUNCH(c, k_wall_grad, nblocks((long long)g.nx * g.ny, BS), BS, B8 * 5 * g.nx * g.ny, g, vel_old, mueff, wg, type, ut2, um0,
               um1, vm, rho);
 }
-void launch_divtau(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, int mode,
-                   const double* src, double* forces, const double* base, const double* dold, double dt, double rho, double* const fl[9]) {
+void launch_divtau_faces(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, int mode,
+                         const double* src, double* forces, const double* base, const double* dold, double dt, double rho,
+                         double* const fl[9]) {
     for (int d = 0; d < 3; ++d) {
         const long long M = (long long)g.nx * g.ny * (d == 2 ? nzfaces(g) : g.nz);
         KS_LAUNCH(c, k_tau_flux, nblocks(M, BS), BS, B8 * (4.0 * g.N + 3.0 * M), g, d, vel, mueff, wg, fl[3 * d], fl[3 * d + 1],
@@ -579,6 +689,16 @@ void launch_divtau(Ctx& c, const Grid& g, const double* vel, const double* mueff
     for (int m = 0; m < 9; ++m) F.p[m] = fl[m];
     const double per_cell = 9 + 3 + (mode == 1 ? 6 : 0) + (mode == 2 ? 6 : 0);
     KS_LAUNCH(c, k_tau_div, nblocks(g.N, BS), BS, B8 * per_cell * g.N, g, F, out, mode, src, forces, base, dold, dt, rho);
+}
+
+void launch_divtau(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, int mode,
+                   const double* src, double* forces, const double* base, const double* dold, double dt, double rho, double* const fl[9]) {
+    (void)fl;  // the tiled kernel keeps its face fluxes in shared memory
+    cudaFuncSetAttribute(k_divtau_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAU_SMEM);
+    const dim3 grid((g.nx + TTX - 1) / TTX, (g.ny + TTY - 1) / TTY, (g.nz + TTZ - 1) / TTZ);
+    const double per_cell = 4 + 3 + (mode == 1 ? 6 : 0) + (mode == 2 ? 6 : 0);
+    KS_LAUNCH_SMEM(c, k_divtau_tile, grid, TTX * TTY * TTZ, TAU_SMEM, B8 * per_cell * g.N, g, vel, mueff, wg, out, mode, src, forces, base, dold,
+                   dt, rho);
 }
 void launch_predictor_rhs(Ctx& c, const Grid& g, const double* vo, const double* conv, const double* src, const double* dtau, double* vel,
                           double dt, double rho) {

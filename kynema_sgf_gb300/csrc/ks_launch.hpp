@@ -33,7 +33,18 @@ struct Ctx {
     std::vector<cudaEvent_t> pool;
     std::map<std::string, Acc> acc;  // kernel name -> totals
 
-    bool prof_match(const char* name) const { return !prof.empty() && (prof == "*" || prof == name); }
+    // names compare without spaces (the report prints them without, e.g. "(k_nd_col<T,0>)")
+    bool prof_match(const char* name) const {
+        if (prof.empty()) return false;
+        if (prof == "*") return true;
+        size_t q = 0;
+        for (const char* c = name; *c; ++c) {
+            if (*c == ' ') continue;
+            if (q >= prof.size() || prof[q] != *c) return false;
+            ++q;
+        }
+        return q == prof.size();
+    }
     cudaEvent_t ev() {
         cudaEvent_t e;
         if (!pool.empty()) {
@@ -84,6 +95,16 @@ struct Ctx {
         ++(c).launches;                                        \
     } while (0)
 
+// the same with dynamic shared memory
+#define KS_LAUNCH_SMEM(c, kern, grid, block, smem, bytes, ...)        \
+    do {                                                               \
+        const bool ks_p_ = (c).prof_match(#kern);                      \
+        if (ks_p_) (c).prof_begin(#kern, (double)(bytes));             \
+        kern<<<(grid), (block), (smem), (c).stream>>>(__VA_ARGS__);    \
+        if (ks_p_) (c).prof_end();                                     \
+        ++(c).launches;                                                \
+    } while (0)
+
 struct Scalars {  // values fed to the pointwise kernels
     double rho, irho, mu, smag_fac;
     int smag;
@@ -106,10 +127,16 @@ void launch_plane_sums(Ctx& c, const Grid& g, const double* vel, double* partial
 void launch_wall_grad(Ctx& c, const Grid& g, const double* vel_old, const double* mueff, double* wg, int shear_type, double ut2,
                       double um0, double um1, double vmag, double rho);
 // out = divtau(vel) ; mode 0: plain, mode 1: forces = (src + divtau)/rho also written,
-// mode 2: out = base + 0.5*dt*(divtau(vel) - dold)/rho (RK2 correction into out)
+// mode 2: out = base + 0.5*dt*(divtau(vel) - dold)/rho (RK2 correction into out).
+// Fused shared-memory tiles; face_scratch is not used.
 void launch_divtau(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, int mode,
                    const double* src, double* forces, const double* base, const double* dold, double dt, double rho,
                    double* const face_scratch[9]);
+// the same result through face-flux arrays in caller-provided scratch (9 arrays:
+// N cells for x and y faces, nx*ny*(nz+1) for z faces) and a divergence pass
+void launch_divtau_faces(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, int mode,
+                         const double* src, double* forces, const double* base, const double* dold, double dt, double rho,
+                         double* const face_scratch[9]);
 void launch_predictor_rhs(Ctx& c, const Grid& g, const double* vel_old, const double* conv, const double* src, const double* divtau,
                           double* vel, double dt, double rho);
 void launch_proj_pre(Ctx& c, const Grid& g, double* vel, const double* vel_old, const double* gp, double scaling, double rho,
@@ -197,6 +224,8 @@ struct CCLevelT {
     int nx, ny, nz, zper;
     T ix2, iy2, iz2;
     T inv_diag[3];  // 1/(-beta d): interior, wall-adjacent, single layer
+    T gs[3][3];     // Gauss-Seidel neighbour weights w_m / d per class (x, y, z)
+    T dg[3];        // diagonal -beta d per class
     T *phi, *rhs, *res;
 };
 template <typename T>

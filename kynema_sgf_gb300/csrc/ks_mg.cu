@@ -49,34 +49,28 @@ inline int parts_for(long long n) {
 template <typename T>
 __device__ inline long long ci3(const CCLevelT<T>& L, int i, int j, int k) { return ((long long)k * L.ny + j) * L.nx + i; }
 
-// beta * laplacian at (i,j,k) and its diagonal
+// Weighted neighbour sum S = sum_m (w_m / d) p_m of the cell's class
+// (interior, wall-adjacent, single layer; Neumann walls drop a z neighbour).
+// The operator is beta * laplacian = dg * (p - S), dg = -beta d.
 template <typename T>
-__device__ inline void cc_ax(const CCLevelT<T>& L, const T* p, T beta, int i, int j, int k, T& Ax, T& dg) {
+__device__ inline T cc_nsum(const CCLevelT<T>& L, const T* p, int i, int j, int k, int& cls) {
     const int ip = i + 1 == L.nx ? 0 : i + 1, im = i == 0 ? L.nx - 1 : i - 1;
     const int jp = j + 1 == L.ny ? 0 : j + 1, jm = j == 0 ? L.ny - 1 : j - 1;
-    T s = L.ix2 * (p[ci3(L, ip, j, k)] + p[ci3(L, im, j, k)]) + L.iy2 * (p[ci3(L, i, jp, k)] + p[ci3(L, i, jm, k)]);
-    T d = T(2) * L.ix2 + T(2) * L.iy2;
-    if (L.zper) {
-        const int km = k == 0 ? L.nz - 1 : k - 1;
-        s += L.iz2 * p[ci3(L, i, j, km)];
-        d += L.iz2;
-        const int kp = k + 1 == L.nz ? 0 : k + 1;
-        s += L.iz2 * p[ci3(L, i, j, kp)];
-        d += L.iz2;
-    } else {
-        if (k > 0) { s += L.iz2 * p[ci3(L, i, j, k - 1)]; d += L.iz2; }
-        if (k < L.nz - 1) { s += L.iz2 * p[ci3(L, i, j, k + 1)]; d += L.iz2; }
-    }
-    Ax = beta * (s - d * p[ci3(L, i, j, k)]);
-    dg = -beta * d;
+    cls = (L.zper || (k > 0 && k < L.nz - 1)) ? 0 : (L.nz == 1 ? 2 : 1);
+    T zs;
+    if (L.zper) zs = p[ci3(L, i, j, k == 0 ? L.nz - 1 : k - 1)] + p[ci3(L, i, j, k + 1 == L.nz ? 0 : k + 1)];
+    else zs = (k > 0 ? p[ci3(L, i, j, k - 1)] : T(0)) + (k < L.nz - 1 ? p[ci3(L, i, j, k + 1)] : T(0));
+    return L.gs[cls][0] * (p[ci3(L, ip, j, k)] + p[ci3(L, im, j, k)]) + L.gs[cls][1] * (p[ci3(L, i, jp, k)] + p[ci3(L, i, jm, k)]) +
+           L.gs[cls][2] * zs;
 }
 
-// inverse of the diagonal -beta*d for the cell at z index k (the wall-adjacent
-// layers drop one z neighbour)
+// Gauss-Seidel point update solved for the new value:
+// dg (p - S) = rhs  =>  p = rhs / dg + S
 template <typename T>
-__device__ inline T cc_inv_diag(const CCLevelT<T>& L, int k) {
-    if (L.zper || (k > 0 && k < L.nz - 1)) return L.inv_diag[0];
-    return (L.nz == 1) ? L.inv_diag[2] : L.inv_diag[1];
+__device__ inline T cc_gs_point(const CCLevelT<T>& L, const T* p, int i, int j, int k, T rhs) {
+    int cls;
+    const T S = cc_nsum(L, p, i, j, k, cls);
+    return L.inv_diag[cls] * rhs + S;
 }
 
 template <typename T>
@@ -89,10 +83,9 @@ __global__ void k_cc_gsrb(CCLevelT<T> L, T beta, int color) {
     const long long r = t / hx;
     const int j = (int)(r % L.ny), k = (int)(r / L.ny);
     const int i = 2 * i2 + ((j + k + color) & 1);
-    T Ax, dg;
-    cc_ax(L, L.phi, beta, i, j, k, Ax, dg);
     const long long c = ci3(L, i, j, k);
-    L.phi[c] += (L.rhs[c] - Ax) * cc_inv_diag(L, k);
+    L.phi[c] = cc_gs_point(L, L.phi, i, j, k, L.rhs[c]);
+    (void)beta;
 }
 
 template <typename T>
@@ -103,9 +96,9 @@ __global__ void k_cc_resid(CCLevelT<T> L, T beta, double* parts) {
         const int i = (int)(t % L.nx);
         const long long r = t / L.nx;
         const int j = (int)(r % L.ny), k = (int)(r / L.ny);
-        T Ax, dg;
-        cc_ax(L, L.phi, beta, i, j, k, Ax, dg);
-        const T v = L.rhs[t] - Ax;
+        int cls;
+        const T S = cc_nsum(L, L.phi, i, j, k, cls);
+        const T v = L.rhs[t] - L.dg[cls] * (L.phi[t] - S);
         L.res[t] = v;
         mx = nmax(mx, fabs((double)v));
     }
@@ -150,9 +143,7 @@ __global__ void k_cc_bottom(CCLevelT<T> L, T beta, int sweeps) {
                 const long long r = t / L.nx;
                 const int j = (int)(r % L.ny), k = (int)(r / L.ny);
                 if (((i + j + k) & 1) != color) continue;
-                T Ax, dg;
-                cc_ax(L, L.phi, beta, i, j, k, Ax, dg);
-                L.phi[t] += (L.rhs[t] - Ax) * cc_inv_diag(L, k);
+                L.phi[t] = cc_gs_point(L, L.phi, i, j, k, L.rhs[t]);
             }
             __syncthreads();
         }

@@ -91,6 +91,6 @@ extern "C" int ks_divtau_noalloc(const double* vel, const double* mueff, const d
         }
     ks::Ctx ctx;
     ctx.stream = static_cast<cudaStream_t>(stream);
-    ks::launch_divtau(ctx, g, vel, mueff, wall_grad, divtau, 0, nullptr, nullptr, nullptr, nullptr, 0.0, 1.0, fl);
+    ks::launch_divtau_faces(ctx, g, vel, mueff, wall_grad, divtau, 0, nullptr, nullptr, nullptr, nullptr, 0.0, 1.0, fl);
     return cudaGetLastError() == cudaSuccess ? KS_OK : KS_ERR_CUDA;
 }
