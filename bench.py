@@ -536,7 +536,7 @@ def main():
                          "algorithmic_bytes_per_launch": by_l / n_l if n_l else None},
             "gpu_launches": r["launches"], "clocks": r["clocks"], "e2e": r["e2e"], "mixed_precision": r["mixed"],
             "adjoint": r["adjoint"]}
-    # The FP64 path is bound by FP64 issue on this GPU (profiles/k_nd_jacobi_abl192_fp64.md): report the
+    # The FP64 path is bound by FP64 issue on this GPU (profiles/k_nd_col_abl256_fp64.md): report the
     # dominant kernel against the FMA peak measured live by ks_fma_peak as well.
     fl = FP64_FLOPS_PER_BYTE.get(r["dominant"])
     if fl and achieved:
