@@ -65,12 +65,17 @@ def parse():
 
 # ---------------------------------------------------------------- CPU side
 def cpu_worker(spec):
-    """Runs in a child process: times the oracle on the bounded CPU sample."""
-    warm, steps = (int(x) for x in spec.split(","))
+    """Runs in a child process: times the oracle on the bounded CPU sample
+    (the ABL sample, or the whole 64^3 Taylor-Green case when spec ends in ',tgv')."""
+    parts = spec.split(",")
+    warm, steps = int(parts[0]), int(parts[1])
     from kynema_sgf_gb300 import decks
     from oracle.oracle import Oracle
     nx, ny, nz = CPU_SAMPLE
     deck = decks.abl(nx, ny, nz, steps=10 ** 6) + "\nincflo.do_initial_proj = 0\nincflo.initial_iterations = 0\n"
+    if len(parts) > 2 and parts[2] == "tgv":
+        nx = ny = nz = 64
+        deck = decks.tgv(64, steps=10 ** 6)
     o = Oracle(deck)
     for _ in range(warm):
         o.step()
@@ -82,12 +87,13 @@ def cpu_worker(spec):
     print(json.dumps({"per_step_s": per, "cells": nx * ny * nz}))
 
 
-def run_cpu(warm, steps):
+def run_cpu(warm, steps, case=""):
     from oracle import oracle as orc
     orc.build()
     cores = os.cpu_count() or 1
     env = dict(os.environ, OMP_NUM_THREADS=str(cores), OMP_PROC_BIND="spread", OMP_PLACES="cores")
-    r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-worker", "%d,%d" % (warm, steps)],
+    spec = "%d,%d" % (warm, steps) + ("," + case if case else "")
+    r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-worker", spec],
                        capture_output=True, text=True, env=env, cwd=ROOT)
     if r.returncode != 0:
         raise RuntimeError("CPU baseline failed: " + r.stderr[-2000:])
@@ -292,8 +298,24 @@ def our_arm(args, rank, world, local_rank):
                  "mac_residual_rel_max": max(mres), "nodal_residual_rel_max": max(nres),
                  "note": "FP32 advection and multigrid cycles, FP64 residuals / defect correction / RHS / velocity update"}
     adj = None if args.no_adjoint else adjoint_bench(args, torch, ks, decks)
+    # the reference's own CPU-runnable case: Taylor-Green vortex 64^3, Re 1600, CFL 0.5, 20 steps
+    tg = ks.Incflo(decks.tgv(64, steps=10 ** 6))
+    tg.InitData()
+    for _ in range(args.warmup):
+        tg.step()
+    tstream = torch.cuda.ExternalStream(tg.stream())
+    torch.cuda.synchronize()
+    ev0.record(tstream)
+    for _ in range(20):
+        tg.step()
+    ev1.record(tstream)
+    torch.cuda.synchronize()
+    tms = ev0.elapsed_time(ev1) / 20
+    tgv = {"workload": "Taylor-Green vortex 64^3, Re 1600, CFL 0.5, FP64, 20 timed steps", "value": 64 ** 3 / (tms * 1e-3) / 1e6,
+           "unit": UNIT, "ms_per_step": tms}
+    del tg
     return dict(value=value, ms=ms_max, cells=cells, launches=launches, dominant=dominant, dom=dom, clocks=clk, e2e=e2e, fp64_peak=fp64_peak,
-                mac=statistics.mean(mac_it), nodal=statistics.mean(nod_it), size=(nx, ny, nz), mixed=mixed, adjoint=adj)
+                mac=statistics.mean(mac_it), nodal=statistics.mean(nod_it), size=(nx, ny, nz), mixed=mixed, adjoint=adj, tgv=tgv)
 
 
 def adjoint_bench(args, torch, ks, decks):
@@ -452,6 +474,16 @@ def c4_bench(args):
     free, total = torch.cuda.mem_get_info()
     lib_mem = (total - free) - torch.cuda.memory_reserved()
     sim.set_precision(0)
+    # the same checkpointed run on the FP64 forward: separates the effect of
+    # the mixed-precision trajectory from finite-difference error
+    restore()
+    out64 = {}
+
+    def run64():
+        out64["J"] = sim.adjoint_run(nsteps, slots)
+
+    run64_ms = timed(run64, 1)
+    g64 = [float(x) for x in sim.ct_gradient()]
 
     def fJ(c):
         restore(c)
@@ -468,7 +500,9 @@ def c4_bench(args):
             cp[k] += h
             cm[k] -= h
             est.append((fJ(cp) - fJ(cm)) / (2 * h))
-        fd["h=%g" % h] = {"fd": est, "rel_err": [abs(a - b) / max(abs(x) for x in g[:2]) for a, b in zip(est, g[:2])]}
+        gm = max(abs(x) for x in g[:2])
+        fd["h=%g" % h] = {"fd": est, "rel_err_mixed_adjoint": [abs(a - b) / gm for a, b in zip(est, g[:2])],
+                          "rel_err_fp64_adjoint": [abs(a - b) / gm for a, b in zip(est, g64[:2])]}
     line = {"c4": {
         "workload": "512x512x256 ABL (C1 physics, 10 m cells), 4x4 UniformCt disks D = 20 cells spaced 7 D, fixed dt 0.5 s, "
                     "J = mean 0.5|u|^2 in the rotor layer 0..5 D behind the first column, %d steps" % nsteps,
@@ -478,7 +512,10 @@ def c4_bench(args):
         "run": {"steps": nsteps, "snapshots": slots, "forward_steps_added": added, "ms": run_ms,
                 "over_mixed_forward_run": run_ms / (nsteps * fwd_mixed)},
         "device_mem_library_GB": lib_mem / 1e9, "device_mem_in_use_GB": (total - free) / 1e9,
-        "J_mixed_forward": out["J"], "J_fp64_forward": J64, "dJ_dCt": g, "fd_fp64_disks_0_1": fd}}
+        "J_mixed_forward": out["J"], "J_fp64_forward": J64, "dJ_dCt": g,
+        "fp64_run": {"ms": run64_ms, "J": out64["J"], "dJ_dCt": g64,
+                     "rel_diff_mixed_vs_fp64_adjoint": max(abs(a - b) for a, b in zip(g, g64)) / max(abs(x) for x in g64)},
+        "fd_fp64_disks_0_1": fd}}
     print(json.dumps(line))
 
 
@@ -535,7 +572,7 @@ def main():
                          "launches": n_l, "avg_launch_us": 1e3 * ms_l / n_l if n_l else None,
                          "algorithmic_bytes_per_launch": by_l / n_l if n_l else None},
             "gpu_launches": r["launches"], "clocks": r["clocks"], "e2e": r["e2e"], "mixed_precision": r["mixed"],
-            "adjoint": r["adjoint"]}
+            "adjoint": r["adjoint"], "tgv64": r["tgv"]}
     # The FP64 path is bound by FP64 issue on this GPU (profiles/k_nd_col_abl256_fp64.md): report the
     # dominant kernel against the FMA peak measured live by ks_fma_peak as well.
     fl = FP64_FLOPS_PER_BYTE.get(r["dominant"])
@@ -554,6 +591,12 @@ def main():
                                     "sample": cpu_sample_text(len(per))}
         except Exception as e:  # reported, never silently replaced
             line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": "failed: %s" % e}
+        try:
+            cells, per, cores = run_cpu(1, 3, "tgv")
+            r["tgv"]["cpu"] = {"value": cells * len(per) / sum(per) / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": "CPU restatement, the same 64^3 deck, %d timed steps after 1" % len(per)}
+        except Exception as e:
+            r["tgv"]["cpu"] = {"value": None, "sample": "failed: %s" % e}
     print(json.dumps(line))
     if world > 1:
         import torch.distributed as tdist

@@ -657,95 +657,149 @@ __device__ inline void Vdb(const Grid& g, double* ub, double* wgb, int n, int i,
     atomicAdd(c + cidx(g, i, j, k), v);
 }
 
-// ---- reverse of the tensor flux on d-faces and of its divergence
-// divtau(c) = sum_d (F_d(c + e_d) - F_d(c)) / h_d,  F_d = mu_f S_d(V):
-// given s * db (adjoint of divtau), accumulate into ub (velocity), mub (cell
-// viscosity; may be null) and wgb (wall-model gradient; may be null).
-__global__ void k_adj_tau(Grid g, int d, const double* vel, const double* mu, const double* wg, const double* db, double s, double* ub,
-                          double* mub, double* wgb) {
-    int i, j, k;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (!face_at(g, d, t, i, j, k)) return;
-    const int e[3] = {d == 0, d == 1, d == 2};
-    const int im = i - e[0], jm = j - e[1], km = k - e[2];
-    const bool has_hi = !(d == 2 && !g.zper && k == g.nz), has_lo = !(d == 2 && !g.zper && k == 0);
+// ---- tiled form of k_adj_tau.  A block owns the faces at the low side of a
+// TX x TY x TZ tile of cells (plus the top wall faces when the tile holds the
+// last cell layer), stages the diffusion velocity (VelDiff ghosts included),
+// mu_eff and the divergence adjoint of the tile and a one-cell halo in shared
+// memory, scatters the face contributions into shared accumulators over the
+// same box, and flushes them with one global atomic per box cell, mapping
+// ghost positions back to the cells (and wall-model gradients) they come from.
+constexpr int ATX = 32, ATY = 4, ATZ = 4;
+constexpr int AHX = ATX + 2, AHY = ATY + 2, AHZ = ATZ + 2;
+constexpr int ANH = AHX * AHY * AHZ;
+constexpr size_t ADJ_TAU_SMEM = sizeof(double) * 11 * (size_t)ANH;
+
+__global__ void __launch_bounds__(ATX* ATY* ATZ) k_adj_tau_tile(Grid g, const double* vel, const double* mu, const double* wg,
+                                                                const double* db, double s, double* ub, double* mub, double* wgb) {
+    extern __shared__ double sm[];
+    double* sV = sm;              // [3][box]
+    double* sD = sm + 3 * ANH;    // [3][box] divergence adjoint (cells in the domain, else 0)
+    double* sM = sm + 6 * ANH;    // [box]
+    double* aU = sm + 7 * ANH;    // [3][box] accumulated velocity adjoint
+    double* aM = sm + 10 * ANH;   // [box] accumulated viscosity adjoint
+    const int i0 = blockIdx.x * ATX, j0 = blockIdx.y * ATY, k0 = blockIdx.z * ATZ;
+    const int tid = threadIdx.x, nthr = ATX * ATY * ATZ;
+    auto hb = [](int hx, int hy, int hz) { return (hz * AHY + hy) * AHX + hx; };
+    for (int h = tid; h < ANH; h += nthr) {
+        const int hx = h % AHX, hy = (h / AHX) % AHY, hz = h / (AHX * AHY);
+        const int gi = ((i0 + hx - 1) % g.nx + g.nx) % g.nx, gj = ((j0 + hy - 1) % g.ny + g.ny) % g.ny;
+        int gk = k0 + hz - 1;
+        const bool inz = g.zper || (gk >= 0 && gk < g.nz);
+        if (g.zper) gk = (gk % g.nz + g.nz) % g.nz;
+        for (int n = 0; n < 3; ++n) sV[n * ANH + h] = Vd(g, vel, wg, n, gi, gj, gk);
+        const int kk = g.zper ? gk : (gk < 0 ? 0 : (gk >= g.nz ? g.nz - 1 : gk));
+        const long long c = cidx(g, gi, gj, kk);
+        sM[h] = mu[c];
+        for (int n = 0; n < 3; ++n) {
+            sD[n * ANH + h] = inz ? s * db[n * g.N + c] : 0.0;
+            aU[n * ANH + h] = 0.0;
+        }
+        aM[h] = 0.0;
+    }
+    __syncthreads();
     const double ih[3] = {g.idx, g.idy, g.idz};
-    const long long ch = has_hi ? cidx(g, i, j, k) : 0;
-    const long long cl = has_lo ? cidx(g, wrapn(im, g.nx), wrapn(jm, g.ny), g.zper ? wrapn(km, g.nz) : km) : 0;
-    double Fb[3];
-    bool any = false;
-    for (int n = 0; n < 3; ++n) {
-        Fb[n] = s * ((has_lo ? db[n * g.N + cl] : 0.0) - (has_hi ? db[n * g.N + ch] : 0.0)) * ih[d];
-        any = any || Fb[n] != 0.0;
-    }
-    if (!any) return;
-    // face viscosity (wall faces take the adjacent cell's value)
-    double mf;
-    long long mc0 = -1, mc1 = -1;
-    if (!has_lo) {
-        mc0 = cidx(g, i, j, 0);
-        mf = mu[mc0];
-    } else if (!has_hi) {
-        mc0 = cidx(g, i, j, g.nz - 1);
-        mf = mu[mc0];
-    } else {
-        mc0 = cl;
-        mc1 = ch;
-        mf = 0.5 * (mu[cl] + mu[ch]);
-    }
-    double gr[3][3];
-    for (int n = 0; n < 3; ++n)
-        for (int m = 0; m < 3; ++m) {
-            if (m == d) {
-                gr[m][n] = (Vd(g, vel, wg, n, i, j, k) - Vd(g, vel, wg, n, im, jm, km)) * ih[m];
-            } else {
-                const int f0 = (m == 0), f1 = (m == 1), f2 = (m == 2);
-                gr[m][n] = 0.25 *
-                           (Vd(g, vel, wg, n, i + f0, j + f1, k + f2) + Vd(g, vel, wg, n, im + f0, jm + f1, km + f2) -
-                            Vd(g, vel, wg, n, i - f0, j - f1, k - f2) - Vd(g, vel, wg, n, im - f0, jm - f1, km - f2)) *
-                           ih[m];
-            }
-        }
-    const double dv = gr[0][0] + gr[1][1] + gr[2][2];
-    double mfb = 0.0;
-    double grb[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
-    double dvb = 0.0;
-    for (int n = 0; n < 3; ++n) {
-        const double Sn = (n == d) ? (2.0 * gr[d][d] - (2.0 / 3.0) * dv) : (gr[d][n] + gr[n][d]);
-        mfb += Fb[n] * Sn;
-        const double sb = mf * Fb[n];
-        if (n == d) {
-            grb[d][d] += 2.0 * sb;
-            dvb += -(2.0 / 3.0) * sb;
+    const bool top = !g.zper && k0 + ATZ >= g.nz;  // this tile also owns the top wall faces
+    const int nface = 3 * nthr + (top ? ATX * ATY : 0);
+    for (int q = tid; q < nface; q += nthr) {
+        int d, tx, ty, tz;
+        if (q < 3 * nthr) {
+            d = q / nthr;
+            const int r = q % nthr;
+            tx = r % ATX;
+            ty = (r / ATX) % ATY;
+            tz = r / (ATX * ATY);
         } else {
-            grb[d][n] += sb;
-            grb[n][d] += sb;
+            d = 2;
+            const int r = q - 3 * nthr;
+            tx = r % ATX;
+            ty = r / ATX;
+            tz = g.nz - k0;  // face k = nz
         }
-    }
-    for (int m = 0; m < 3; ++m) grb[m][m] += dvb;
-    if (mub) {
-        if (mc1 < 0) aadd(&mub[mc0], mfb);
-        else {
-            aadd(&mub[mc0], 0.5 * mfb);
-            aadd(&mub[mc1], 0.5 * mfb);
+        const int gi = i0 + tx, gj = j0 + ty, gk = k0 + tz;
+        if (gi >= g.nx || gj >= g.ny) continue;
+        if (q < 3 * nthr && gk >= g.nz) continue;
+        const int e0 = (d == 0), e1 = (d == 1), e2 = (d == 2);
+        const int hx = tx + 1, hy = ty + 1, hz = tz + 1;     // cell above the face
+        const int mx = hx - e0, my = hy - e1, mz = hz - e2;  // cell below
+        const bool has_hi = !(d == 2 && !g.zper && gk == g.nz), has_lo = !(d == 2 && !g.zper && gk == 0);
+        double Fb[3];
+        bool any = false;
+        for (int n = 0; n < 3; ++n) {
+            Fb[n] = ((has_lo ? sD[n * ANH + hb(mx, my, mz)] : 0.0) - (has_hi ? sD[n * ANH + hb(hx, hy, hz)] : 0.0)) * ih[d];
+            any = any || Fb[n] != 0.0;
         }
-    }
-    for (int n = 0; n < 3; ++n)
-        for (int m = 0; m < 3; ++m) {
-            const double b = grb[m][n];
-            if (b == 0.0) continue;
-            if (m == d) {
-                Vdb(g, ub, wgb, n, i, j, k, b * ih[m]);
-                Vdb(g, ub, wgb, n, im, jm, km, -b * ih[m]);
-            } else {
-                const int f0 = (m == 0), f1 = (m == 1), f2 = (m == 2);
-                const double w = 0.25 * b * ih[m];
-                Vdb(g, ub, wgb, n, i + f0, j + f1, k + f2, w);
-                Vdb(g, ub, wgb, n, im + f0, jm + f1, km + f2, w);
-                Vdb(g, ub, wgb, n, i - f0, j - f1, k - f2, -w);
-                Vdb(g, ub, wgb, n, im - f0, jm - f1, km - f2, -w);
+        if (!any) continue;
+        double mf;
+        if (!has_lo) mf = sM[hb(hx, hy, hz)];
+        else if (!has_hi) mf = sM[hb(mx, my, mz)];
+        else mf = 0.5 * (sM[hb(mx, my, mz)] + sM[hb(hx, hy, hz)]);
+        double gr[3][3];
+        for (int n = 0; n < 3; ++n) {
+            const double* v = sV + n * ANH;
+            for (int m = 0; m < 3; ++m) {
+                if (m == d) {
+                    gr[m][n] = (v[hb(hx, hy, hz)] - v[hb(mx, my, mz)]) * ih[m];
+                } else {
+                    const int f0 = (m == 0), f1 = (m == 1), f2 = (m == 2);
+                    gr[m][n] = 0.25 *
+                               (v[hb(hx + f0, hy + f1, hz + f2)] + v[hb(mx + f0, my + f1, mz + f2)] - v[hb(hx - f0, hy - f1, hz - f2)] -
+                                v[hb(mx - f0, my - f1, mz - f2)]) *
+                               ih[m];
+                }
             }
         }
+        const double dv = gr[0][0] + gr[1][1] + gr[2][2];
+        double mfb = 0.0, dvb = 0.0;
+        double grb[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        for (int n = 0; n < 3; ++n) {
+            const double Sn = (n == d) ? (2.0 * gr[d][d] - (2.0 / 3.0) * dv) : (gr[d][n] + gr[n][d]);
+            mfb += Fb[n] * Sn;
+            const double sb = mf * Fb[n];
+            if (n == d) {
+                grb[d][d] += 2.0 * sb;
+                dvb += -(2.0 / 3.0) * sb;
+            } else {
+                grb[d][n] += sb;
+                grb[n][d] += sb;
+            }
+        }
+        for (int m = 0; m < 3; ++m) grb[m][m] += dvb;
+        if (!has_lo) atomicAdd(&aM[hb(hx, hy, hz)], mfb);
+        else if (!has_hi) atomicAdd(&aM[hb(mx, my, mz)], mfb);
+        else {
+            atomicAdd(&aM[hb(mx, my, mz)], 0.5 * mfb);
+            atomicAdd(&aM[hb(hx, hy, hz)], 0.5 * mfb);
+        }
+        for (int n = 0; n < 3; ++n) {
+            double* a = aU + n * ANH;
+            for (int m = 0; m < 3; ++m) {
+                const double b = grb[m][n];
+                if (b == 0.0) continue;
+                if (m == d) {
+                    atomicAdd(&a[hb(hx, hy, hz)], b * ih[m]);
+                    atomicAdd(&a[hb(mx, my, mz)], -b * ih[m]);
+                } else {
+                    const int f0 = (m == 0), f1 = (m == 1), f2 = (m == 2);
+                    const double w = 0.25 * b * ih[m];
+                    atomicAdd(&a[hb(hx + f0, hy + f1, hz + f2)], w);
+                    atomicAdd(&a[hb(mx + f0, my + f1, mz + f2)], w);
+                    atomicAdd(&a[hb(hx - f0, hy - f1, hz - f2)], -w);
+                    atomicAdd(&a[hb(mx - f0, my - f1, mz - f2)], -w);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    // flush: box positions to cells (ghost positions through the diffusion ghost rules)
+    for (int h = tid; h < ANH; h += nthr) {
+        const int hx = h % AHX, hy = (h / AHX) % AHY, hz = h / (AHX * AHY);
+        const int gi = ((i0 + hx - 1) % g.nx + g.nx) % g.nx, gj = ((j0 + hy - 1) % g.ny + g.ny) % g.ny;
+        const int gk = k0 + hz - 1;
+        for (int n = 0; n < 3; ++n) Vdb(g, ub, wgb, n, gi, gj, gk, aU[n * ANH + h]);
+        if (mub && aM[h] != 0.0) {
+            if (g.zper || (gk >= 0 && gk < g.nz)) atomicAdd(&mub[cidx(g, gi, gj, g.zper ? (gk % g.nz + g.nz) % g.nz : gk)], aM[h]);
+        }
+    }
 }
 
 // ---- reverse of the Smagorinsky viscosity mu_eff = mu + rho fac |S|(u)
@@ -1084,10 +1138,9 @@ void launch_adj_div(Ctx& c, const Grid& g, const double* convb, const AdjBufs& A
 }
 void launch_adj_tau(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, const double* divtau_b, double s, double* ub,
                     double* mub, double* wgb) {
-    for (int d = 0; d < 3; ++d) {
-        const long long nf = nfaces(g, d);
-        KS_LAUNCH(c, k_adj_tau, nblocks(nf, BS), BS, B8 * 10.0 * g.N, g, d, vel, mueff, wg, divtau_b, s, ub, mub, wgb);
-    }
+    cudaFuncSetAttribute(k_adj_tau_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ADJ_TAU_SMEM);
+    const dim3 grid((g.nx + ATX - 1) / ATX, (g.ny + ATY - 1) / ATY, (g.nz + ATZ - 1) / ATZ);
+    KS_LAUNCH_SMEM(c, k_adj_tau_tile, grid, ATX * ATY * ATZ, ADJ_TAU_SMEM, B8 * 14.0 * g.N, g, vel, mueff, wg, divtau_b, s, ub, mub, wgb);
 }
 void launch_adj_smag(Ctx& c, const Grid& g, const double* vel, const double* mub, const Scalars& s, double* ub) {
     KS_LAUNCH(c, k_adj_smag, nblocks(g.N, BS), BS, B8 * 7.0 * g.N, g, vel, mub, s.rho, s.smag_fac, ub);

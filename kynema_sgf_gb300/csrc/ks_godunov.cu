@@ -260,10 +260,14 @@ __global__ void k_pm_final(Grid g, int d, const T* lo_dd, const T* hi_dd, const 
     mac[f] = (double)riemann(stl, sth);
 }
 
-// ---- post-MAC stage 2: a-face states corrected along b (conservative form)
+// ---- post-MAC stage 2 for both transverse directions of the a-faces in one
+// pass: the face states, the two adjacent cell values and the MAC velocity are
+// loaded once for the corrections along b1 = a+1 and b2 = a+2 (each is the
+// k_adv_trans arithmetic).
 template <typename T>
-__global__ void k_adv_trans(Grid g, int a, int b, const double* vel, T rho, T cb, const double* ua, const double* vb, C3<T> LO, C3<T> HI,
-                            C3<T> E, P3<T> out) {
+__global__ void __launch_bounds__(256, 2) k_adv_trans2(Grid g, int a, const double* vel, T rho, T cb1, T cb2, const double* ua,
+                                                       const double* vb1, const double* vb2, C3<T> LO, C3<T> HI, C3<T> E1, C3<T> E2,
+                                                       P3<T> out1, P3<T> out2) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_of(g, a, t, i, j, k)) return;
@@ -272,23 +276,49 @@ __global__ void k_adv_trans(Grid g, int a, int b, const double* vel, T rho, T cb
     const long long f = fidx(g, a, i, j, k);
     const T u = (T)ua[f];
     const int ci = i - (a == 0), cj = j - (a == 1), ck = k - (a == 2);
-    const long long h0 = fidx(g, b, i, j, k), h1 = fidx(g, b, i + (b == 0), j + (b == 1), k + (b == 2));
-    const long long l0 = fidx(g, b, ci, cj, ck), l1 = fidx(g, b, ci + (b == 0), cj + (b == 1), ck + (b == 2));
-    T vhp = T(0), vhm = T(0), vlp = T(0), vlm = T(0);
-    if (!wh) { vhp = (T)vb[h1]; vhm = (T)vb[h0]; }
-    if (!wl) { vlp = (T)vb[l1]; vlm = (T)vb[l0]; }
+    const int b1 = (a + 1) % 3, b2 = (a + 2) % 3;
+    auto fc = [&](int b, int ii, int jj, int kk, long long& m, long long& p) {
+        m = fidx(g, b, ii, jj, kk);
+        p = fidx(g, b, ii + (b == 0), jj + (b == 1), kk + (b == 2));
+    };
+    long long h0a, h1a, l0a, l1a, h0b, h1b, l0b, l1b;
+    fc(b1, i, j, k, h0a, h1a);
+    fc(b1, ci, cj, ck, l0a, l1a);
+    fc(b2, i, j, k, h0b, h1b);
+    fc(b2, ci, cj, ck, l0b, l1b);
+    T vhp1 = T(0), vhm1 = T(0), vlp1 = T(0), vlm1 = T(0), vhp2 = T(0), vhm2 = T(0), vlp2 = T(0), vlm2 = T(0);
+    if (!wh) {
+        vhp1 = (T)vb1[h1a];
+        vhm1 = (T)vb1[h0a];
+        vhp2 = (T)vb2[h1b];
+        vhm2 = (T)vb2[h0b];
+    }
+    if (!wl) {
+        vlp1 = (T)vb1[l1a];
+        vlm1 = (T)vb1[l0a];
+        vlp2 = (T)vb2[l1b];
+        vlm2 = (T)vb2[l0b];
+    }
     for (int n = 0; n < 3; ++n) {
-        T l = LO.p[n][f], h = HI.p[n][f];
-        if (!wh) h += -cb * (vhp * E.p[n][h1] - vhm * E.p[n][h0]) + cb * q(n, i, j, k) * (vhp - vhm);
-        if (!wl) l += -cb * (vlp * E.p[n][l1] - vlm * E.p[n][l0]) + cb * q(n, ci, cj, ck) * (vlp - vlm);
+        const T l0 = LO.p[n][f], h0 = HI.p[n][f];
+        const T qh = wh ? T(0) : q(n, i, j, k), ql = wl ? T(0) : q(n, ci, cj, ck);
+        T l = l0, h = h0;
+        if (!wh) h += -cb1 * (vhp1 * E1.p[n][h1a] - vhm1 * E1.p[n][h0a]) + cb1 * qh * (vhp1 - vhm1);
+        if (!wl) l += -cb1 * (vlp1 * E1.p[n][l1a] - vlm1 * E1.p[n][l0a]) + cb1 * ql * (vlp1 - vlm1);
         if (a == 2) zbc(g, k, n, l, h);
-        out.p[n][f] = upwind(u, l, h);
+        out1.p[n][f] = upwind(u, l, h);
+        l = l0;
+        h = h0;
+        if (!wh) h += -cb2 * (vhp2 * E2.p[n][h1b] - vhm2 * E2.p[n][h0b]) + cb2 * qh * (vhp2 - vhm2);
+        if (!wl) l += -cb2 * (vlp2 * E2.p[n][l1b] - vlm2 * E2.p[n][l0b]) + cb2 * ql * (vlp2 - vlm2);
+        if (a == 2) zbc(g, k, n, l, h);
+        out2.p[n][f] = upwind(u, l, h);
     }
 }
 
 // ---- post-MAC stage 3: final states and fluxes on d-faces
 template <typename T>
-__global__ void k_adv_flux(Grid g, int d, const double* vel, const double* forces, T rho, T dt, T c1, T c2, C3<double> U, C3<T> LO, C3<T> HI,
+__global__ void __launch_bounds__(256, 3) k_adv_flux(Grid g, int d, const double* vel, const double* forces, T rho, T dt, T c1, T c2, C3<double> U, C3<T> LO, C3<T> HI,
                            C3<T> T1, C3<T> T2, P3<T> Fl) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -408,16 +438,18 @@ static void advection_t(Ctx& c, const Grid& g, const double* vel, const double* 
         KS_LAUNCH(c, (k_faces<1, T>), nblocks(nfaces(g, a), BS), BS, B8 * (3.0 * g.N + nfaces(g, a)) + BT * 12.0 * nfaces(g, a), g, a, vel,
                   E, dtdx, T(rho), mac[a], LO, HI, (T*)nullptr, ED);
     }
-    for (int a = 0; a < 3; ++a)
-        for (int b = 0; b < 3; ++b) {
-            if (a == b) continue;
-            const double bytes = B8 * (3.0 * g.N + nfaces(g, a) + nfaces(g, b)) + BT * (9.0 * nfaces(g, a) + 3.0 * nfaces(g, b));
-            C3<T> LO{{tp<T>(B.lo[a][0]), tp<T>(B.lo[a][1]), tp<T>(B.lo[a][2])}}, HI{{tp<T>(B.hi[a][0]), tp<T>(B.hi[a][1]), tp<T>(B.hi[a][2])}};
-            C3<T> E{{tp<T>(B.tedge[b][0]), tp<T>(B.tedge[b][1]), tp<T>(B.tedge[b][2])}};
-            P3<T> O{{tp<T>(B.tr[a][b][0]), tp<T>(B.tr[a][b][1]), tp<T>(B.tr[a][b][2])}};
-            KS_LAUNCH(c, k_adv_trans<T>, nblocks(nfaces(g, a), BS), BS, bytes, g, a, b, vel, T(rho), T(dt / (3.0 * hd(g, b))), mac[a],
-                      mac[b], LO, HI, E, O);
-        }
+    for (int a = 0; a < 3; ++a) {
+        const int b1 = (a + 1) % 3, b2 = (a + 2) % 3;
+        const double na = (double)nfaces(g, a), nt = (double)(nfaces(g, b1) + nfaces(g, b2));
+        const double bytes = B8 * (3.0 * g.N + na + nt) + BT * (12.0 * na + 3.0 * nt);
+        C3<T> LO{{tp<T>(B.lo[a][0]), tp<T>(B.lo[a][1]), tp<T>(B.lo[a][2])}}, HI{{tp<T>(B.hi[a][0]), tp<T>(B.hi[a][1]), tp<T>(B.hi[a][2])}};
+        C3<T> E1{{tp<T>(B.tedge[b1][0]), tp<T>(B.tedge[b1][1]), tp<T>(B.tedge[b1][2])}};
+        C3<T> E2{{tp<T>(B.tedge[b2][0]), tp<T>(B.tedge[b2][1]), tp<T>(B.tedge[b2][2])}};
+        P3<T> O1{{tp<T>(B.tr[a][b1][0]), tp<T>(B.tr[a][b1][1]), tp<T>(B.tr[a][b1][2])}};
+        P3<T> O2{{tp<T>(B.tr[a][b2][0]), tp<T>(B.tr[a][b2][1]), tp<T>(B.tr[a][b2][2])}};
+        KS_LAUNCH(c, k_adv_trans2<T>, nblocks(nfaces(g, a), BS), BS, bytes, g, a, vel, T(rho), T(dt / (3.0 * hd(g, b1))),
+                  T(dt / (3.0 * hd(g, b2))), mac[a], mac[b1], mac[b2], LO, HI, E1, E2, O1, O2);
+    }
     C3<double> U{{mac[0], mac[1], mac[2]}};
     for (int d = 0; d < 3; ++d) {
         const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
