@@ -63,6 +63,23 @@ def parse():
     return p.parse_args()
 
 
+# ---------------------------------------------------------------- replicas
+def max_over_ranks(value, world, device="cuda"):
+    """The slowest rank's time: every rank advances its own replica (the path
+    does not shard), so the job ends when the last replica does."""
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(cells, steps, world, seconds):
+    """Whole-job Mcell-steps/s: all replicas' cell-steps over the slowest rank's time."""
+    return cells * steps * world / seconds / 1e6
+
+
 # ---------------------------------------------------------------- CPU side
 def cpu_worker(spec):
     """Runs in a child process: times the oracle on the bounded CPU sample
@@ -217,15 +234,11 @@ def our_arm(args, rank, world, local_rank):
     if dist:
         tdist.barrier()
     launches = sim.kernel_launches() - l0
-    ms = ev0.elapsed_time(ev1)
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if dist:
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-    ms_max = float(t.item())
+    ms_max = max_over_ranks(ev0.elapsed_time(ev1), world)
     dom = sim.profile_report().get(dominant, (0, 0.0, 0.0))
     fp64_peak = ks.fma_peak(True)
     sim.profile_kernels("")
-    value = cells * args.steps * world / (ms_max * 1e-3) / 1e6
+    value = replica_throughput(cells, args.steps, world, ms_max * 1e-3)
     ref_state = {f: sim.get_field(f) for f in ("velocity", "gp")} if not args.no_mixed else None
 
     # end to end through the public API: host inputs in, host result out
@@ -245,13 +258,9 @@ def our_arm(args, rank, world, local_rank):
             sim.step()
             sim.get_field("velocity", out=host["velocity"])
         torch.cuda.synchronize()
-        el = time.perf_counter() - t0
-        te = torch.tensor([el], dtype=torch.float64, device="cuda")
-        if dist:
-            tdist.all_reduce(te, op=tdist.ReduceOp.MAX)
-        el = float(te.item())
+        el = max_over_ranks(time.perf_counter() - t0, world)
         hin = sum(host[f].numel() * 8 for f in host)
-        e2e = {"value": cells * args.steps * world / el / 1e6, "unit": UNIT, "h2d_bytes_per_step": hin,
+        e2e = {"value": replica_throughput(cells, args.steps, world, el), "unit": UNIT, "h2d_bytes_per_step": hin,
                "d2h_bytes_per_step": host["velocity"].numel() * 8}
     mixed = None
     if not args.no_mixed:
@@ -282,15 +291,11 @@ def our_arm(args, rank, world, local_rank):
             nres.append(mx.scalar("nodal_res") / max(mx.scalar("nodal_res0"), 1e-300))
         ev1.record(stream)
         torch.cuda.synchronize()
-        mms = ev0.elapsed_time(ev1)
-        t = torch.tensor([mms], dtype=torch.float64, device="cuda")
-        if dist:
-            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        mms = float(t.item())
+        mms = max_over_ranks(ev0.elapsed_time(ev1), world)
         v = mx.get_field("velocity")
         gpm = mx.get_field("gp")
         rv, rg = ref_state["velocity"], ref_state["gp"]
-        mixed = {"value": cells * args.steps * world / (mms * 1e-3) / 1e6, "ms_per_step": mms / args.steps,
+        mixed = {"value": replica_throughput(cells, args.steps, world, mms * 1e-3), "ms_per_step": mms / args.steps,
                  "speedup_vs_fp64": ms_max / mms, "steps_compared": args.warmup + args.steps,
                  "velocity_rel_err_linf": float(abs(v - rv).max() / abs(rv).max()),
                  "velocity_rel_err_l2": float(((v - rv) ** 2).sum() ** 0.5 / (rv ** 2).sum() ** 0.5),

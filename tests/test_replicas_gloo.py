@@ -1,0 +1,54 @@
+"""The multi-rank path of bench.py on CPU ranks (gloo, world size 2): the path
+runs one independent replica per rank, so the only cross-rank steps are the
+barrier and the max-over-ranks time; rank 0 reports the whole-job rate.  The
+reference arm runs on rank 0 alone and the other ranks exit without output."""
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, world, port, local_times, out):
+    import torch.distributed as tdist
+    sys.path.insert(0, ROOT)
+    import bench
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    tdist.init_process_group("gloo", rank=rank, world_size=world)
+    tdist.barrier()
+    t = bench.max_over_ranks(local_times[rank], world, device="cpu")
+    out.put((rank, t, bench.replica_throughput(1000, 10, world, t)))
+    tdist.destroy_process_group()
+
+
+def test_max_over_ranks_gloo():
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    times = [0.75, 1.25]
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, times, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert [r[1] for r in res] == [1.25, 1.25]          # both ranks see the slowest replica
+    assert res[0][2] == pytest.approx(1000 * 10 * 2 / 1.25 / 1e6)
+
+
+def test_reference_arm_other_ranks_exit_quietly():
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2"],
+                       capture_output=True, text=True, env=env, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == ""
