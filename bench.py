@@ -52,6 +52,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision form of the same workload")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost / gradient check (128x128x64, 3 disks)")
+    p.add_argument("--no-mol", action="store_true", help="skip the MOL predictor-corrector form of the ABL workload")
     p.add_argument("--c4", action="store_true",
                    help="only the production forward + adjoint run: 512x512x256 ABL, 16 disks, mixed forward, FP64 adjoint")
     p.add_argument("--c4-steps", type=int, default=200)
@@ -93,6 +94,8 @@ def cpu_worker(spec):
     if len(parts) > 2 and parts[2] == "tgv":
         nx = ny = nz = 64
         deck = decks.tgv(64, steps=10 ** 6)
+    if len(parts) > 2 and parts[2] == "mol":
+        deck = decks.mol(decks.abl(nx, ny, nz, steps=10 ** 6, cfl=0.45)) + "\nincflo.do_initial_proj = 0\nincflo.initial_iterations = 0\n"
     o = Oracle(deck)
     for _ in range(warm):
         o.step()
@@ -302,6 +305,7 @@ def our_arm(args, rank, world, local_rank):
                  "gp_rel_err_linf": float(abs(gpm - rg).max() / abs(rg).max()),
                  "mac_residual_rel_max": max(mres), "nodal_residual_rel_max": max(nres),
                  "note": "FP32 advection and multigrid cycles, FP64 residuals / defect correction / RHS / velocity update"}
+    mol = None if args.no_mol else mol_bench(args, torch, ks, decks, nx, ny, nz, world, rank)
     adj = None if args.no_adjoint else adjoint_bench(args, torch, ks, decks)
     # the reference's own CPU-runnable case: Taylor-Green vortex 64^3, Re 1600, CFL 0.5, 20 steps
     tg = ks.Incflo(decks.tgv(64, steps=10 ** 6))
@@ -320,7 +324,47 @@ def our_arm(args, rank, world, local_rank):
            "unit": UNIT, "ms_per_step": tms}
     del tg
     return dict(value=value, ms=ms_max, cells=cells, launches=launches, dominant=dominant, dom=dom, clocks=clk, e2e=e2e, fp64_peak=fp64_peak,
-                mac=statistics.mean(mac_it), nodal=statistics.mean(nod_it), size=(nx, ny, nz), mixed=mixed, adjoint=adj, tgv=tgv)
+                mac=statistics.mean(mac_it), nodal=statistics.mean(nod_it), size=(nx, ny, nz), mixed=mixed, adjoint=adj, tgv=tgv, mol=mol)
+
+
+def mol_bench(args, torch, ks, decks, nx, ny, nz, world, rank):
+    """The same ABL workload advanced with the MOL predictor-corrector
+    (incflo.use_godunov = false, explicit diffusion) at CFL 0.45 (MOL requires
+    <= 0.5): two MAC and two nodal projections per step.  Device time of
+    --steps steps after --warmup, FP64."""
+    sim = ks.Incflo(decks.mol(decks.abl(nx, ny, nz, steps=10 ** 9, cfl=0.45)))
+    sim.InitData()
+    cells = sim.scalar("ncells")
+    for w in range(args.warmup):
+        if args.profile_all and w == args.warmup - 1:
+            sim.profile_kernels("*")
+        sim.step()
+    if args.profile_all and rank == 0:
+        rep = sim.profile_report()
+        tot = sum(v[1] for v in rep.values())
+        sys.stderr.write("-- MOL step --\n")
+        for k, v in sorted(rep.items(), key=lambda kv: -kv[1][1]):
+            sys.stderr.write("%-22s %6d launches %9.3f ms %5.1f%% %8.1f GB/s\n" % (k, v[0], v[1], 100 * v[1] / tot,
+                                                                                  v[2] / (v[1] * 1e-3) / 1e9 if v[1] else 0))
+    sim.profile_kernels("")
+    stream = torch.cuda.ExternalStream(sim.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    mac_it, nod_it = [], []
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        sim.step()
+        mac_it.append(sim.scalar("mac_iters"))
+        nod_it.append(sim.scalar("nodal_iters"))
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = max_over_ranks(ev0.elapsed_time(ev1), world)
+    out = {"workload": "ABL %dx%dx%d, MOL predictor-corrector, explicit diffusion, CFL 0.45, FP64" % (nx, ny, nz),
+           "value": replica_throughput(cells, args.steps, world, ms * 1e-3), "unit": UNIT, "ms_per_step": ms / args.steps,
+           "dt": sim.scalar("dt"), "mac_vcycles_per_step": statistics.mean(mac_it), "nodal_vcycles_per_step": statistics.mean(nod_it),
+           "projections_per_step": {"mac": 2, "nodal": 2}}
+    del sim
+    return out
 
 
 def adjoint_bench(args, torch, ks, decks):
@@ -577,7 +621,7 @@ def main():
                          "launches": n_l, "avg_launch_us": 1e3 * ms_l / n_l if n_l else None,
                          "algorithmic_bytes_per_launch": by_l / n_l if n_l else None},
             "gpu_launches": r["launches"], "clocks": r["clocks"], "e2e": r["e2e"], "mixed_precision": r["mixed"],
-            "adjoint": r["adjoint"], "tgv64": r["tgv"]}
+            "adjoint": r["adjoint"], "tgv64": r["tgv"], "mol": r["mol"]}
     # The FP64 path is bound by FP64 issue on this GPU (profiles/k_nd_col_abl256_fp64.md): report the
     # dominant kernel against the FMA peak measured live by ks_fma_peak as well.
     fl = FP64_FLOPS_PER_BYTE.get(r["dominant"])
@@ -602,6 +646,13 @@ def main():
                                "sample": "CPU restatement, the same 64^3 deck, %d timed steps after 1" % len(per)}
         except Exception as e:
             r["tgv"]["cpu"] = {"value": None, "sample": "failed: %s" % e}
+        if r["mol"]:
+            try:
+                cells, per, cores = run_cpu(1, 2, "mol")
+                r["mol"]["cpu"] = {"value": cells * len(per) / sum(per) / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
+                                   "sample": "CPU restatement, MOL form of the %dx%dx%d ABL sample, %d timed steps after 1" % (CPU_SAMPLE + (len(per),))}
+            except Exception as e:
+                r["mol"]["cpu"] = {"value": None, "sample": "failed: %s" % e}
     print(json.dumps(line))
     if world > 1:
         import torch.distributed as tdist

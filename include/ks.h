@@ -15,7 +15,7 @@
  *   ks_prepare_time_step       incflo::prepare_time_step (New -> Old)          src/incflo_advance.cpp:34-44
  *   ks_advance                 incflo::advance(fixed_point_iteration)          src/incflo_advance.cpp:63-79
  *   ks_apply_predictor         incflo::ApplyPredictor                          src/incflo_advance.cpp:186-438
- *   ks_apply_corrector         incflo::ApplyCorrector (MOL only)               src/incflo_advance.cpp:528-652
+ *   ks_apply_corrector         incflo::ApplyCorrector (MOL: incflo.use_godunov = false)  src/incflo_advance.cpp:528-652
  *   ks_apply_projection        incflo::ApplyProjection                         src/projection/incflo_apply_nodal_projection.cpp:149-465
  *   ks_evolve                  incflo::Evolve time loop                        src/incflo.cpp:338-411
  *   ks_set_field / ks_get_field  FieldRepo field access by name              src/core/FieldRepo.H:139-173
@@ -97,8 +97,10 @@ int ks_kernel_launches(const ks_handle* h, long long* count);
  * entry points ks_adjoint_step / ks_set_objective_box / ks_get_ct_gradient
  * extend the operator surface of src/incflo.H:51-233).
  *
- * Differentiable configuration: triply periodic, turbulence.model = laminar,
- * time.fixed_dt > 0, momentum sources among ActuatorForcing, BodyForce and
+ * Differentiable configuration: the Godunov scheme (incflo.use_godunov = 1),
+ * time.fixed_dt > 0, periodic z or slip / wall-model walls (wall model with
+ * ABL.wall_shear_stress_type = moeng), laminar or Smagorinsky viscosity,
+ * momentum sources among ActuatorForcing, BodyForce, CoriolisForcing and
  * GeostrophicForcing, UniformCtDisk actuators with one thrust_coeff value
  * each.  Other decks return KS_ERR_UNSUPPORTED from every call below.
  * The objective J is the mean of 0.5 |u|^2 over the cells whose centres lie in

@@ -74,10 +74,12 @@ void Sim::setup(const Deck& D) {
 
     rho_ = D.num("incflo.density", 1.0);
     mu_ = D.num("transport.viscosity", 0.0);
-    if (D.flag("incflo.use_godunov", 1) != 1) throw KsError(KS_ERR_UNSUPPORTED, "the MOL scheme is outside this path");
-    if (lc(D.str("incflo.godunov_type", "weno_z")) != "ppm") throw KsError(KS_ERR_UNSUPPORTED, "incflo.godunov_type must be ppm");
+    godunov_ = D.flag("incflo.use_godunov", 1) != 0;
+    if (godunov_) {
+        if (lc(D.str("incflo.godunov_type", "weno_z")) != "ppm") throw KsError(KS_ERR_UNSUPPORTED, "incflo.godunov_type must be ppm");
+        if (D.flag("incflo.godunov_use_forces_in_trans", 0) != 0) throw KsError(KS_ERR_UNSUPPORTED, "godunov_use_forces_in_trans");
+    }
     if (D.flag("incflo.diffusion_type", 1) != 0) throw KsError(KS_ERR_UNSUPPORTED, "only explicit diffusion (incflo.diffusion_type = 0)");
-    if (D.flag("incflo.godunov_use_forces_in_trans", 0) != 0) throw KsError(KS_ERR_UNSUPPORTED, "godunov_use_forces_in_trans");
     if (D.flag("incflo.icns_conserv", 1) != 1) throw KsError(KS_ERR_UNSUPPORTED, "non-conservative momentum form");
     initial_proj_ = D.flag("incflo.do_initial_proj", 1);
     initial_iters_ = D.flag("incflo.initial_iterations", 3);
@@ -163,7 +165,9 @@ void Sim::setup(const Deck& D) {
     t_.force_cfl = D.flag("time.use_force_cfl", 1) != 0;
     if (t_.fixed_dt > 0) t_.dt[0] = t_.fixed_dt;
     else t_.adaptive = true;
-    if (t_.cfl > 1.0) throw KsError(KS_ERR_DECK, "We currently require cfl <= 1.0 when using the Godunov advection scheme");
+    // src/setup/init.cpp:78-88
+    if (!godunov_ && t_.cfl > 0.5) throw KsError(KS_ERR_DECK, "We currently require cfl <= 0.5 when using the MOL advection scheme");
+    if (godunov_ && t_.cfl > 1.0) throw KsError(KS_ERR_DECK, "We currently require cfl <= 1.0 when using the Godunov advection scheme");
 
     // Actuator disks (src/wind_energy/actuator/disk/disk_ops.cpp:182-276,
     // uniform_ct_ops.cpp:53-88)
@@ -261,14 +265,20 @@ void Sim::alloc() {
     umac_[1].alloc(N);
     umac_[2].alloc(NF);
     // Godunov scratch: per face direction ad, edge[3], lo[3], hi[3], tedge[3],
-    // flux[3]; tr[a][b][3] for the six (a, b) pairs
+    // flux[3]; tr[a][b][3] for the six (a, b) pairs.  MOL needs the fluxes only.
     const size_t fsz[3] = {N, N, NF};
     size_t total = 0;
-    for (int d = 0; d < 3; ++d) total += fsz[d] * 16;
-    for (int a = 0; a < 3; ++a) total += 2 * 3 * fsz[a];
+    for (int d = 0; d < 3; ++d) total += fsz[d] * (godunov_ ? 16 : 3);
+    if (godunov_)
+        for (int a = 0; a < 3; ++a) total += 2 * 3 * fsz[a];
     gbuf_.alloc(total);
     double* q = gbuf_.p;
-    for (int d = 0; d < 3; ++d) {
+    if (!godunov_) {
+        conv_old_.alloc(3 * N);
+        for (int d = 0; d < 3; ++d)
+            for (int n = 0; n < 3; ++n) { gb_.flux[d][n] = q; q += fsz[d]; }
+    }
+    for (int d = 0; d < 3 && godunov_; ++d) {
         gb_.ad[d] = q; q += fsz[d];
         for (int n = 0; n < 3; ++n) { gb_.edge[d][n] = q; q += fsz[d]; }
         for (int n = 0; n < 3; ++n) { gb_.lo[d][n] = q; q += fsz[d]; }
@@ -276,7 +286,7 @@ void Sim::alloc() {
         for (int n = 0; n < 3; ++n) { gb_.tedge[d][n] = q; q += fsz[d]; }
         for (int n = 0; n < 3; ++n) { gb_.flux[d][n] = q; q += fsz[d]; }
     }
-    for (int a = 0; a < 3; ++a)
+    for (int a = 0; a < 3 && godunov_; ++a)
         for (int b = 0; b < 3; ++b) {
             if (a == b) continue;
             for (int n = 0; n < 3; ++n) { gb_.tr[a][b][n] = q; q += fsz[a]; }
@@ -717,6 +727,10 @@ void Sim::apply_projection(double time, double scaling, bool incremental) {
 
 // ---------------------------------------------------------------- ApplyPredictor
 void Sim::apply_predictor(bool incremental) {
+    if (!godunov_) {
+        mol_predictor(incremental);
+        return;
+    }
     const double dt = t_.dt[0];
     launch_smagorinsky(ctx_, g_, vel_old_.p, mueff_.p, S_);
     launch_sources(ctx_, g_, vel_old_.p, gp_.p, act_.p, src_.p, S_);
@@ -735,6 +749,51 @@ void Sim::apply_predictor(bool incremental) {
     launch_divtau(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, 2, nullptr, nullptr, vel_.p, divtau_.p, dt, rho_, fl);
     std::swap(vel_.p, vel_tmp_.p);
     apply_projection(t_.next, dt, incremental);
+}
+
+// ---------------------------------------------------------------- MOL
+// ApplyPredictor for MOL with explicit diffusion (src/incflo_advance.cpp:186-438):
+// mu_eff, wall gradient and diff_term(Old) from the Old velocity, sources at
+// NPH (the Coriolis term reads Old), face velocities extrapolated from Old and
+// MAC-projected, conv_term(Old) with predictor_rhs (fstate Old,
+// CompRHSOps.H:32-141) fused into its divergence pass, nodal projection.
+void Sim::mol_predictor(bool incremental) {
+    const double dt = t_.dt[0];
+    launch_smagorinsky(ctx_, g_, vel_old_.p, mueff_.p, S_);
+    if (wallmodel_) launch_wall_grad(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, shear_, utau_ * utau_, um_[0], um_[1], vmag_, rho_);
+    double* fl[9];
+    for (int m = 0; m < 9; ++m) fl[m] = static_cast<double*>(gb_.flux[m / 3][m % 3]);
+    launch_divtau(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, divtau_.p, 0, nullptr, nullptr, nullptr, nullptr, dt, rho_, fl);
+    launch_sources(ctx_, g_, vel_old_.p, gp_.p, act_.p, src_.p, S_);
+    double* mac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
+    launch_mol_extrap(ctx_, g_, vel_old_.p, mac);
+    mac_project();
+    const double* cmac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
+    launch_mol_advection(ctx_, g_, vel_old_.p, cmac, rho_, fl, conv_old_.p, 1, vel_old_.p, src_.p, divtau_.p, vel_.p, dt);
+    apply_projection(t_.next, dt, incremental);
+}
+
+// ApplyCorrector (src/incflo_advance.cpp:528-652): face velocities from the
+// predicted velocity and MAC projection, conv_term(New), mu_eff(New), the
+// wall-model gradient (Old velocity, new mu_eff: ABLWallFunction.cpp:236-300),
+// sources at New, diff_term(New) fused with corrector_rhs (explicit factors
+// 1/2, 1/2: CompRHSOps.H:160-250), non-incremental nodal projection.
+void Sim::apply_corrector() {
+    if (godunov_) throw KsError(KS_ERR_UNSUPPORTED, "ApplyCorrector is the MOL corrector; the Godunov path completes in ApplyPredictor");
+    const double dt = t_.dt[0];
+    double* fl[9];
+    for (int m = 0; m < 9; ++m) fl[m] = static_cast<double*>(gb_.flux[m / 3][m % 3]);
+    double* mac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
+    launch_mol_extrap(ctx_, g_, vel_.p, mac);
+    mac_project();
+    const double* cmac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
+    launch_mol_advection(ctx_, g_, vel_.p, cmac, rho_, fl, conv_.p, 0, nullptr, nullptr, nullptr, nullptr, dt);
+    launch_smagorinsky(ctx_, g_, vel_.p, mueff_.p, S_);
+    if (wallmodel_) launch_wall_grad(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, shear_, utau_ * utau_, um_[0], um_[1], vmag_, rho_);
+    launch_sources(ctx_, g_, vel_.p, gp_.p, act_.p, src_.p, S_);
+    launch_divtau_corrector(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, vel_old_.p, conv_old_.p, conv_.p, divtau_.p, src_.p, dt, rho_);
+    std::swap(vel_.p, vel_tmp_.p);
+    apply_projection(t_.next, dt, false);
 }
 
 void Sim::prepare_time_step() { launch_copy(ctx_, vel_old_.p, vel_.p, 3 * g_.N); }
@@ -769,6 +828,7 @@ int Sim::step() {
     pre_advance();
     prepare_time_step();
     apply_predictor(false);
+    if (!godunov_) apply_corrector();  // incflo::advance (src/incflo_advance.cpp:63-79)
     return KS_OK;
 }
 
@@ -784,6 +844,7 @@ double* Sim::field(const std::string& name, int& nc, int& kind) {
     if (name == "forces") return forces_.p;
     if (name == "diff_term") return divtau_.p;
     if (name == "conv_term") return conv_.p;
+    if (name == "conv_term_old" && !godunov_) return conv_old_.p;
     if (name == "velocity_adjoint" || name == "gp_adjoint") {
         adj_alloc();
         return name == "velocity_adjoint" ? adj_->ub.p : adj_->gpb.p;
@@ -955,6 +1016,7 @@ int ks_advance(ks_handle* h, int fpi) {
         if (fpi != 0) throw ks::KsError(KS_ERR_UNSUPPORTED, "fixed-point iterations > 0");
         s.prepare_time_step();
         s.apply_predictor(false);
+        if (!s.godunov()) s.apply_corrector();
         s.sync();
         return 0;
     });
@@ -970,9 +1032,11 @@ int ks_apply_predictor(ks_handle* h, int incremental, int fpi) {
 }
 
 int ks_apply_corrector(ks_handle* h) {
-    if (!h || !h->sim) return KS_ERR_ARG;
-    h->err = "ApplyCorrector is the MOL corrector; the Godunov path completes in ApplyPredictor";
-    return KS_ERR_UNSUPPORTED;
+    return guarded(h, [](ks::Sim& s) {
+        s.apply_corrector();
+        s.sync();
+        return 0;
+    });
 }
 
 int ks_apply_projection(ks_handle* h, double time, double scaling, int incremental) {

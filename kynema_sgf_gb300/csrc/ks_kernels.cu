@@ -325,9 +325,12 @@ constexpr int TNH = THX * THY * THZ;
 constexpr int TNFX = (TTX + 1) * TTY * TTZ, TNFY = TTX * (TTY + 1) * TTZ, TNFZ = TTX * TTY * (TTZ + 1);
 constexpr size_t TAU_SMEM = sizeof(double) * (4 * (size_t)TNH + 3 * ((size_t)TNFX + TNFY + TNFZ));
 
+// mode 3 (MOL corrector_rhs, explicit): out = (rho base + dt (0.5 (conv_o + conv_n)
+// + 0.5 (dold + divtau(vel)) + src)) / rho, base = u_old
 __global__ void __launch_bounds__(TTX* TTY* TTZ) k_divtau_tile(Grid g, const double* vel, const double* mueff, const double* wg, double* out,
                                                                int mode, const double* src, double* forces, const double* base,
-                                                               const double* dold, double dt, double rho) {
+                                                               const double* dold, double dt, double rho, const double* conv_o,
+                                                               const double* conv_n) {
     extern __shared__ double sm[];
     double* sV = sm;                // [3][THZ][THY][THX]
     double* sM = sm + 3 * TNH;      // [THZ][THY][THX]
@@ -416,8 +419,11 @@ __global__ void __launch_bounds__(TTX* TTY* TTZ) k_divtau_tile(Grid g, const dou
         } else if (mode == 1) {
             out[n * N + t] = acc;
             forces[n * N + t] = (src[n * N + t] + acc) * irho;
-        } else {
+        } else if (mode == 2) {
             out[n * N + t] = base[n * N + t] + 0.5 * dt * (acc - dold[n * N + t]) * irho;
+        } else {
+            const long long m = n * N + t;
+            out[m] = (rho * base[m] + dt * (0.5 * (conv_o[m] + conv_n[m]) + 0.5 * dold[m] + 0.5 * acc + src[m])) * irho;
         }
     }
 }
@@ -698,7 +704,14 @@ void launch_divtau(Ctx& c, const Grid& g, const double* vel, const double* mueff
     const dim3 grid((g.nx + TTX - 1) / TTX, (g.ny + TTY - 1) / TTY, (g.nz + TTZ - 1) / TTZ);
     const double per_cell = 4 + 3 + (mode == 1 ? 6 : 0) + (mode == 2 ? 6 : 0);
     KS_LAUNCH_SMEM(c, k_divtau_tile, grid, TTX * TTY * TTZ, TAU_SMEM, B8 * per_cell * g.N, g, vel, mueff, wg, out, mode, src, forces, base, dold,
-                   dt, rho);
+                   dt, rho, nullptr, nullptr);
+}
+void launch_divtau_corrector(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, const double* vel_old,
+                             const double* conv_old, const double* conv_new, const double* dold, const double* src, double dt, double rho) {
+    cudaFuncSetAttribute(k_divtau_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAU_SMEM);
+    const dim3 grid((g.nx + TTX - 1) / TTX, (g.ny + TTY - 1) / TTY, (g.nz + TTZ - 1) / TTZ);
+    KS_LAUNCH_SMEM(c, k_divtau_tile, grid, TTX * TTY * TTZ, TAU_SMEM, B8 * 22.0 * g.N, g, vel, mueff, wg, out, 3, src, nullptr, vel_old, dold, dt,
+                   rho, conv_old, conv_new);
 }
 void launch_predictor_rhs(Ctx& c, const Grid& g, const double* vo, const double* conv, const double* src, const double* dtau, double* vel,
                           double dt, double rho) {

@@ -137,6 +137,10 @@ void launch_divtau(Ctx& c, const Grid& g, const double* vel, const double* mueff
 void launch_divtau_faces(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, int mode,
                          const double* src, double* forces, const double* base, const double* dold, double dt, double rho,
                          double* const face_scratch[9]);
+// MOL corrector_rhs (explicit) fused into the tiled divtau of vel:
+// out = (rho u_old + dt (0.5 (conv_old + conv_new) + 0.5 (dold + divtau(vel)) + src)) / rho
+void launch_divtau_corrector(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, const double* vel_old,
+                             const double* conv_old, const double* conv_new, const double* dold, const double* src, double dt, double rho);
 void launch_predictor_rhs(Ctx& c, const Grid& g, const double* vel_old, const double* conv, const double* src, const double* divtau,
                           double* vel, double dt, double rho);
 void launch_proj_pre(Ctx& c, const Grid& g, double* vel, const double* vel_old, const double* gp, double scaling, double rho,
@@ -172,6 +176,15 @@ void launch_premac(Ctx& c, const Grid& g, const double* vel_old, const double* f
                    int fp32);
 void launch_advection(Ctx& c, const Grid& g, const double* vel_old, const double* forces, const double* mac[3], double dt, double rho,
                       GodunovBufs& B, double* conv, int fp32);
+
+// ---- MOL advection (ks_mol.cu), FP64
+// face-normal velocities extrapolated from vel (before the MAC projection)
+void launch_mol_extrap(Ctx& c, const Grid& g, const double* vel, double* const mac[3]);
+// conv = -div(u_mac (rho u)_face) through the nine face-flux arrays fl; mode 1
+// also writes vel_out = (rho vel_old + dt (conv + src + dold)) / rho
+void launch_mol_advection(Ctx& c, const Grid& g, const double* vel, const double* const mac[3], double rho, double* const fl[9],
+                          double* conv, int mode, const double* vel_old, const double* src, const double* dold, double* vel_out,
+                          double dt);
 
 // ---- reverse mode of the Godunov passes (ks_adjoint.cu), FP64, periodic.
 // Adjoints of the GodunovBufs arrays (same shapes) plus those of the MAC

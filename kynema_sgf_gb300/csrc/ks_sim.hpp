@@ -229,9 +229,13 @@ class Sim {
     void compute_dt();
     void pre_advance();
     void prepare_time_step();
+    // ApplyPredictor of the deck's scheme (Godunov: the whole advance; MOL: its
+    // predictor), ApplyCorrector (MOL only)
     void apply_predictor(bool incremental);
+    void apply_corrector();
     void apply_projection(double time, double scaling, bool incremental);
     int step();
+    bool godunov() const { return godunov_; }
 
     double scalar(const std::string& name);
     void layout(const std::string& name, ks_layout& L);
@@ -278,6 +282,7 @@ class Sim {
     double* field(const std::string& name, int& ncomp, int& kind);
     void nd_rhs(const double* cell_field);
     void nd_solve(double sigma);
+    void mol_predictor(bool incremental);
     void disk_points(const Disk& d, std::vector<double>& sample, std::vector<double>& ring) const;
     // reverse mode
     void adj_check() const;
@@ -298,8 +303,10 @@ class Sim {
     std::vector<Disk> disks_;
     MGParams mac_, nod_;
     int initial_proj_ = 1, initial_iters_ = 3;
+    bool godunov_ = true;  // incflo.use_godunov; false: MOL predictor-corrector
 
     DevBuf<double> vel_, vel_old_, vel_tmp_, gp_, p_, src_, forces_, mueff_, divtau_, conv_, act_, wg_;
+    DevBuf<double> conv_old_;  // MOL: conv_term(Old) of the predictor
     DevBuf<double> umac_[3];
     DevBuf<double> gbuf_;
     GodunovBufs gb_{};

@@ -30,6 +30,15 @@ time.max_step = {steps}
 """
 
 
+def mol(deck):
+    """The same deck advanced with the MOL predictor-corrector
+    (``incflo.use_godunov = false``); the deck's ``time.cfl`` must be <= 0.5."""
+    out = deck.replace("incflo.use_godunov = 1\nincflo.godunov_type = ppm\n", "incflo.use_godunov = false\n")
+    if out == deck:
+        raise ValueError("deck does not select the Godunov scheme")
+    return out
+
+
 def abl(nx=256, ny=256, nz=128, steps=100, dx=20.0, cfl=0.9, seed=42):
     """Neutral ABL LES: periodic x/y, wall-model bottom, slip top,
     Smagorinsky Cs = 0.135, geostrophic forcing for 8 m/s with Coriolis."""

@@ -22,7 +22,7 @@ STATUS = {
 KS_DONE = 7
 KS_HOST, KS_DEVICE = 0, 1
 
-FIELDS = ["velocity", "velocity_old", "gp", "p", "src_term", "forces", "diff_term", "conv_term", "velocity_mueff",
+FIELDS = ["velocity", "velocity_old", "gp", "p", "src_term", "forces", "diff_term", "conv_term", "conv_term_old", "velocity_mueff",
           "u_mac", "v_mac", "w_mac", "actuator_src_term", "velocity_adjoint", "gp_adjoint"]
 
 # every symbol declared in include/ks.h

@@ -33,6 +33,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <memory>
 #include <sstream>
@@ -267,11 +268,12 @@ struct Sim {
     std::vector<DiskParams> disks;
     MGOpts mac, nod;
     int do_initial_proj = 1, initial_iterations = 3;
+    bool godunov = true;  // incflo.use_godunov; false selects the MOL predictor-corrector
     SimTime t;
     std::string err;
 
     // fields
-    Arr vel, vel_old, gp, p, src, forces, mueff, divtau, divtau_new, conv, act_src;
+    Arr vel, vel_old, gp, p, src, forces, mueff, divtau, divtau_new, conv, conv_old, act_src;
     Arr umac, vmac, wmac;
     int mac_iters = 0, nodal_iters = 0;
     double mac_res0 = 0, mac_res = 0, nodal_res0 = 0, nodal_res = 0;
@@ -281,8 +283,8 @@ struct Sim {
     // passes
     void fill_vel(Arr& v) const;
     void fill_cc_foextrap(Arr& a) const;
-    void update_mueff();
-    void compute_sources();
+    void update_mueff(Arr& v);
+    void compute_sources(const Arr& v);
     void wall_gradient(std::vector<double>& gx, std::vector<double>& gy) const;
     void divtau_op(const Arr& v_in, Arr& out);
     void premac(double dt);
@@ -293,6 +295,10 @@ struct Sim {
     void abl_update_umean();
     void actuator_update();
     void apply_predictor(bool incremental);
+    void mol_extrap(Arr& v);
+    void mol_conv(Arr& v, Arr& out);
+    void mol_predictor(bool incremental);
+    void mol_corrector();
     void init_data();
     int step_once();
     double ke() const;
@@ -333,11 +339,13 @@ void Sim::setup(const std::string& text) {
 
     rho = D.d("incflo.density", 1.0);
     mu = D.d("transport.viscosity", 0.0);
-    if (D.i("incflo.use_godunov", 1) != 1) throw Error(ERR_UNSUPPORTED, "only incflo.use_godunov = 1");
-    std::string gt = lower(D.s("incflo.godunov_type", "weno_z"));
-    if (gt != "ppm") throw Error(ERR_UNSUPPORTED, "only incflo.godunov_type = ppm");
+    godunov = D.i("incflo.use_godunov", 1) != 0;
+    if (godunov) {
+        std::string gt = lower(D.s("incflo.godunov_type", "weno_z"));
+        if (gt != "ppm") throw Error(ERR_UNSUPPORTED, "only incflo.godunov_type = ppm");
+        if (D.i("incflo.godunov_use_forces_in_trans", 0) != 0) throw Error(ERR_UNSUPPORTED, "forces_in_trans");
+    }
     if (D.i("incflo.diffusion_type", 1) != 0) throw Error(ERR_UNSUPPORTED, "only incflo.diffusion_type = 0");
-    if (D.i("incflo.godunov_use_forces_in_trans", 0) != 0) throw Error(ERR_UNSUPPORTED, "forces_in_trans");
     if (D.i("incflo.icns_conserv", 1) != 1) throw Error(ERR_UNSUPPORTED, "icns_conserv = 0");
     do_initial_proj = D.i("incflo.do_initial_proj", 1);
     initial_iterations = D.i("incflo.initial_iterations", 3);
@@ -398,7 +406,9 @@ void Sim::setup(const std::string& text) {
     t.max_cfl = D.d("time.cfl", 1.0);
     t.use_force_cfl = D.i("time.use_force_cfl", 1) != 0;
     if (t.fixed_dt > 0) t.dt[0] = t.fixed_dt; else t.adaptive = true;
-    if (t.max_cfl > 1.0) throw Error(ERR_DECK, "We currently require cfl <= 1.0 when using the Godunov advection scheme");
+    // src/setup/init.cpp:78-88
+    if (!godunov && t.max_cfl > 0.5) throw Error(ERR_DECK, "We currently require cfl <= 0.5 when using the MOL advection scheme");
+    if (godunov && t.max_cfl > 1.0) throw Error(ERR_DECK, "We currently require cfl <= 1.0 when using the Godunov advection scheme");
 
     // actuators: src/wind_energy/actuator/disk/disk_ops.cpp:182-276
     if (src_act) {
@@ -446,6 +456,7 @@ void Sim::setup(const std::string& text) {
     def_cc(gp, g, 1, 3); def_cc(src, g, 1, 3); def_cc(forces, g, 1, 3);
     def_cc(mueff, g, 1, 1); def_cc(divtau, g, 0, 3); def_cc(divtau_new, g, 0, 3);
     def_cc(conv, g, 0, 3); def_cc(act_src, g, 0, 3);
+    if (!godunov) def_cc(conv_old, g, 0, 3);
     const int nzn = g.n[2] + (g.per[2] ? 0 : 1);
     p.define(-1, -1, -1, g.n[0], g.n[1], nzn, 1);
     umac.define(-1, -1, -1, g.n[0] + 1, g.n[1], g.n[2], 1);
@@ -554,10 +565,9 @@ void Sim::fill_cc_foextrap(Arr& a) const {
 // ---- Smagorinsky ---------------------------------------------------------------
 // src/turbulence/LES/Smagorinsky.cpp:22-62, src/fvm/strainrate.H:24-86,
 // one-sided stencils src/fvm/stencils.H:166-330 at non-periodic z faces.
-void Sim::update_mueff() {
+void Sim::update_mueff(Arr& v) {
     const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
     if (!smag) { mueff.setval(mu); return; }
-    Arr& v = vel_old;
     fill_vel(v);
     const double idx = 1.0 / g.dx[0], idy = 1.0 / g.dx[1], idz = 1.0 / g.dx[2];
     const double ds = std::cbrt(g.dx[0] * g.dx[1] * g.dx[2]);
@@ -584,8 +594,10 @@ void Sim::update_mueff() {
 
 // ---- momentum sources ------------------------------------------------------------
 // src/equation_systems/icns/icns_ops.H:78-124 and PDEOps.H:94-145:
-// src = rho * (-gp/rho + sum of sources); sources at state Old.
-void Sim::compute_sources() {
+// src = rho * (-gp/rho + sum of sources); the Coriolis term reads the velocity
+// state v (Old for the predictor's Old and NPH states, New for the corrector:
+// field_impl::dof_state, src/core/FieldUtils.H:110-113).
+void Sim::compute_sources(const Arr& v) {
     const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
     const double omega = 2 * kPi / rot_period;
     const double latr = lat * kPi / 180.0;
@@ -603,7 +615,7 @@ void Sim::compute_sources() {
                 if (src_geo)
                     for (int n = 0; n < 3; ++n) s[n] += (n == 2 ? hfac : 1.0) * gf[n];
                 if (src_cor) {  // CoriolisForcing.cpp:60-108
-                    const double u0 = vel_old(i, j, k, 0), u1 = vel_old(i, j, k, 1), u2 = vel_old(i, j, k, 2);
+                    const double u0 = v(i, j, k, 0), u1 = v(i, j, k, 1), u2 = v(i, j, k, 2);
                     const double ue = east[0] * u0 + east[1] * u1 + east[2] * u2;
                     const double un = north[0] * u0 + north[1] * u1 + north[2] * u2;
                     const double uu = up[0] * u0 + up[1] * u1 + up[2] * u2;
@@ -1739,8 +1751,8 @@ void Sim::actuator_update() {
 void Sim::apply_predictor(bool incremental) {
     const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
     const double dt = t.dt[0];
-    update_mueff();
-    compute_sources();
+    update_mueff(vel_old);
+    compute_sources(vel_old);
     divtau_op(vel_old, divtau);  // divtau with u = Old (copied into New)
     for (int n = 0; n < 3; ++n)
 #pragma omp parallel for collapse(2)
@@ -1752,7 +1764,7 @@ void Sim::apply_predictor(bool incremental) {
     advection(dt);
     // compute_source_term(NPH) reproduces src (Old velocity, same gp);
     // compute_diffusion_term(Old) reproduces divtau.
-    compute_sources();
+    compute_sources(vel_old);
     // predictor_rhs (CompRHSOps.H:32-141), Explicit factor 1
     for (int n = 0; n < 3; ++n)
 #pragma omp parallel for collapse(2)
@@ -1770,6 +1782,174 @@ void Sim::apply_predictor(bool incremental) {
     nodal_project(incremental ? t.newt : t.newt, dt, incremental);
 }
 
+// ---- MOL scheme -------------------------------------------------------------------------------
+// Monotonized-central slope of order 2 (AMReX's amrex_calc_{x,y,z}slope and
+// their _extdir forms, AMReX_Slopes_K.H in the AMReX submodule): the minmod of
+// the doubled one-sided differences and the central difference.  In the cell
+// next to an ext_dir / hoextrap domain face (edge -1 low side, +1 high side)
+// the central difference becomes the one-sided quadratic through the face value
+// held in the ghost cell: (q+ + 3 q0 - 4 qb)/3 and (4 qb - 3 q0 - q-)/3.
+static double mc_slope(double qm, double q0, double qp, int edge) {
+    const double dl = 2.0 * (q0 - qm), dr = 2.0 * (qp - q0);
+    double dc = 0.5 * (qp - qm);
+    if (edge < 0) dc = (qp + 3.0 * q0 - 4.0 * qm) / 3.0;
+    else if (edge > 0) dc = (4.0 * qp - 3.0 * q0 - qm) / 3.0;
+    double s = std::min(std::fabs(dl), std::min(std::fabs(dc), std::fabs(dr)));
+    if (!(dr * dl > 0.0)) s = 0.0;
+    return dc > 0.0 ? s : -s;
+}
+
+// Slope along d of component n at cell (i, j, k) of a ghost-filled array.  Every
+// velocity component is ext_dir (normal) or hoextrap (tangential) at a z wall,
+// so the one-sided form applies at k = 0 and k = nz - 1 when z is bounded.
+static double mol_slope(const Arr& a, const Geo& g, int d, int i, int j, int k, int n) {
+    int c[3] = {i, j, k};
+    c[d] -= 1;
+    const double qm = a(c[0], c[1], c[2], n);
+    c[d] += 2;
+    const double qp = a(c[0], c[1], c[2], n);
+    int edge = 0;
+    if (d == 2 && !g.per[2]) edge = (k == 0) ? -1 : (k == g.n[2] - 1 ? 1 : 0);
+    return mc_slope(qm, a(i, j, k, n), qp, edge);
+}
+
+// MOL::ExtrapVelToFaces (AMReX-Hydro's MOL velocity extrapolation, called from
+// icns_advection.H:501-527 before the MAC projection): the normal velocity on
+// each face from the MC-limited states of its two cells, zero where they
+// diverge (umns < 0 < upls) or where their mean is below small_vel = 1e-10,
+// else the upwind state.  A face on an ext_dir boundary (the normal component
+// at a z wall) takes the ghost value, which is the wall velocity 0.
+void Sim::mol_extrap(Arr& v) {
+    fill_vel(v);
+    const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+    const double small_vel = 1.0e-10;
+    auto pick = [&](double umns, double upls) {
+        if (umns < 0.0 && upls > 0.0) return 0.0;
+        const double avg = 0.5 * (upls + umns);
+        if (std::fabs(avg) < small_vel) return 0.0;
+        return avg >= 0.0 ? umns : upls;
+    };
+    Arr* mac[3] = {&umac, &vmac, &wmac};
+    for (int d = 0; d < 3; ++d) {
+        const int hi[3] = {nx - 1 + (d == 0), ny - 1 + (d == 1), nz - 1 + (d == 2)};
+        Arr& M = *mac[d];
+#pragma omp parallel for collapse(2)
+        for (int k = 0; k <= hi[2]; ++k)
+            for (int j = 0; j <= hi[1]; ++j)
+                for (int i = 0; i <= hi[0]; ++i) {
+                    if (d == 2 && !g.per[2] && (k == 0 || k == nz)) { M(i, j, k) = 0.0; continue; }
+                    int c[3] = {i, j, k};
+                    c[d] -= 1;
+                    const double umns = v(c[0], c[1], c[2], d) + 0.5 * mol_slope(v, g, d, c[0], c[1], c[2], d);
+                    const double upls = v(i, j, k, d) - 0.5 * mol_slope(v, g, d, i, j, k, d);
+                    M(i, j, k) = pick(umns, upls);
+                }
+    }
+    const int fx[3] = {1, 0, 0}, fy[3] = {0, 1, 0}, fz[3] = {0, 0, 1};
+    fill_periodic(umac, g, fx);
+    fill_periodic(vmac, g, fy);
+    fill_periodic(wmac, g, fz);
+}
+
+// MOL convective term (icns_advection.H:531-594: q = rho u,
+// mol::compute_convective_fluxes and mol::compute_convective_rate,
+// src/convection/incflo_mol_fluxes.cpp:9-268): the face state is the
+// MC-limited extrapolation upwinded with the MAC velocity, the mean of both
+// states where |u_mac| <= small_vel = FLT_EPSILON, and the ghost value on an
+// ext_dir face; flux = q_face u_mac; conv = sum_d dxinv_d (F_lo - F_hi).
+void Sim::mol_conv(Arr& v, Arr& out) {
+    const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+    fill_vel(v);
+    Arr q;
+    def_cc(q, g, 3, 3);
+    for (size_t m = 0; m < q.d.size(); ++m) q.d[m] = rho * v.d[m];
+    const double small_vel = (double)std::numeric_limits<float>::epsilon();
+    const Arr* mac[3] = {&umac, &vmac, &wmac};
+    Arr F[3];
+    F[0].define(0, 0, 0, nx, ny - 1, nz - 1, 3);
+    F[1].define(0, 0, 0, nx - 1, ny, nz - 1, 3);
+    F[2].define(0, 0, 0, nx - 1, ny - 1, nz, 3);
+    for (int d = 0; d < 3; ++d)
+        for (int n = 0; n < 3; ++n)
+#pragma omp parallel for collapse(2)
+            for (int k = 0; k <= F[d].hi[2]; ++k)
+                for (int j = 0; j <= F[d].hi[1]; ++j)
+                    for (int i = 0; i <= F[d].hi[0]; ++i) {
+                        const double um = (*mac[d])(i, j, k);
+                        double qs;
+                        if (d == 2 && !g.per[2] && n == 2 && (k == 0 || k == nz)) {
+                            qs = q(i, j, k == 0 ? -1 : nz, n);  // ext_dir: the boundary value in the ghost cell
+                        } else {
+                            int c[3] = {i, j, k};
+                            c[d] -= 1;
+                            const double qmns = q(c[0], c[1], c[2], n) + 0.5 * mol_slope(q, g, d, c[0], c[1], c[2], n);
+                            const double qpls = q(i, j, k, n) - 0.5 * mol_slope(q, g, d, i, j, k, n);
+                            if (um > small_vel) qs = qmns;
+                            else if (um < -small_vel) qs = qpls;
+                            else qs = 0.5 * (qmns + qpls);
+                        }
+                        F[d](i, j, k, n) = qs * um;
+                    }
+    const double dxi[3] = {1.0 / g.dx[0], 1.0 / g.dx[1], 1.0 / g.dx[2]};
+    for (int n = 0; n < 3; ++n)
+#pragma omp parallel for collapse(2)
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i)
+                    out(i, j, k, n) = (dxi[0] * (F[0](i, j, k, n) - F[0](i + 1, j, k, n))) +
+                                      (dxi[1] * (F[1](i, j, k, n) - F[1](i, j + 1, k, n))) +
+                                      (dxi[2] * (F[2](i, j, k, n) - F[2](i, j, k + 1, n)));
+}
+
+// ApplyPredictor for MOL with explicit diffusion (src/incflo_advance.cpp:186-438):
+// mu_eff and diff_term(Old) from the Old velocity, face velocities extrapolated
+// from Old and MAC-projected, conv_term(Old), sources at NPH (Old velocity),
+// predictor_rhs with fstate Old (CompRHSOps.H:32-141), nodal projection.
+void Sim::mol_predictor(bool incremental) {
+    const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+    const double dt = t.dt[0];
+    update_mueff(vel_old);
+    divtau_op(vel_old, divtau);
+    mol_extrap(vel_old);
+    mac_project();
+    mol_conv(vel_old, conv_old);
+    compute_sources(vel_old);
+    for (int n = 0; n < 3; ++n)
+#pragma omp parallel for collapse(2)
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i)
+                    vel(i, j, k, n) = (rho * vel_old(i, j, k, n) + dt * (conv_old(i, j, k, n) + src(i, j, k, n) + divtau(i, j, k, n))) / rho;
+    nodal_project(t.newt, dt, incremental);
+}
+
+// ApplyCorrector (src/incflo_advance.cpp:528-652): face velocities from the
+// predicted velocity and MAC projection, conv_term(New), mu_eff(New),
+// diff_term(New) (the wall-model gradient keeps the Old velocity and takes the
+// new mu_eff, ABLWallFunction.cpp:236-300), sources at New, corrector_rhs
+// with the explicit factors 1/2, 1/2 (CompRHSOps.H:160-250) and a
+// non-incremental nodal projection.
+void Sim::mol_corrector() {
+    const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+    const double dt = t.dt[0];
+    mol_extrap(vel);
+    mac_project();
+    mol_conv(vel, conv);
+    update_mueff(vel);
+    divtau_op(vel, divtau_new);
+    compute_sources(vel);
+    for (int n = 0; n < 3; ++n)
+#pragma omp parallel for collapse(2)
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i)
+                    vel(i, j, k, n) = (rho * vel_old(i, j, k, n) +
+                                       dt * (0.5 * (conv_old(i, j, k, n) + conv(i, j, k, n)) + 0.5 * divtau(i, j, k, n) +
+                                             0.5 * divtau_new(i, j, k, n) + src(i, j, k, n))) /
+                                      rho;
+    nodal_project(t.newt, dt, false);
+}
+
 // ---- InitData (src/setup/init.cpp:104-225) -------------------------------------------------------
 void Sim::init_data() {
     abl_update_umean();  // ABL::post_init_actions
@@ -1782,7 +1962,8 @@ void Sim::init_data() {
         compute_dt();
         vel_old = vel;
         for (int it = 0; it < initial_iterations; ++it) {
-            apply_predictor(true);
+            if (godunov) apply_predictor(true);
+            else mol_predictor(true);  // init.cpp:153-159: ApplyPredictor only, for both schemes
             vel = vel_old;
         }
     }
@@ -1795,7 +1976,12 @@ int Sim::step_once() {
     abl_update_umean();  // ABL::pre_advance_work
     actuator_update();   // Actuator::pre_advance_work
     vel_old = vel;       // prepare_time_step / advance_states
-    apply_predictor(false);
+    if (godunov) {
+        apply_predictor(false);
+    } else {  // incflo::advance (src/incflo_advance.cpp:63-79)
+        mol_predictor(false);
+        mol_corrector();
+    }
     return OK;
 }
 
@@ -1846,6 +2032,7 @@ static kso::Arr* field_ptr(Sim& s, const std::string& name, int& nodal_z, int& f
     if (name == "diff_term") return &s.divtau;
     if (name == "diff_term_new") return &s.divtau_new;
     if (name == "conv_term") return &s.conv;
+    if (name == "conv_term_old") return s.godunov ? nullptr : &s.conv_old;
     if (name == "actuator_src_term") return &s.act_src;
     if (name == "u_mac") { fdir = 0; return &s.umac; }
     if (name == "v_mac") { fdir = 1; return &s.vmac; }
@@ -1891,7 +2078,16 @@ int kso_prepare_time_step(void* h) { return guard(h, [](Sim& s) { s.vel_old = s.
 int kso_apply_predictor(void* h, int incremental, int fpi) {
     return guard(h, [&](Sim& s) {
         if (fpi != 0) throw kso::Error(kso::ERR_UNSUPPORTED, "fixed-point iterations");
-        s.apply_predictor(incremental != 0);
+        if (s.godunov) s.apply_predictor(incremental != 0);
+        else s.mol_predictor(incremental != 0);
+        return 0;
+    });
+}
+
+int kso_apply_corrector(void* h) {
+    return guard(h, [](Sim& s) {
+        if (s.godunov) throw kso::Error(kso::ERR_UNSUPPORTED, "ApplyCorrector belongs to the MOL scheme");
+        s.mol_corrector();
         return 0;
     });
 }
@@ -1900,7 +2096,7 @@ int kso_apply_projection(void* h, double time, double scaling, int incremental) 
     return guard(h, [&](Sim& s) { s.nodal_project(time, scaling, incremental != 0); return 0; });
 }
 
-int kso_update_mueff(void* h) { return guard(h, [](Sim& s) { s.update_mueff(); return 0; }); }
+int kso_update_mueff(void* h) { return guard(h, [](Sim& s) { s.update_mueff(s.vel_old); return 0; }); }
 
 int kso_compute_divtau(void* h, int use_new) {
     return guard(h, [&](Sim& s) {
@@ -1910,7 +2106,7 @@ int kso_compute_divtau(void* h, int use_new) {
     });
 }
 
-int kso_compute_sources(void* h) { return guard(h, [](Sim& s) { s.compute_sources(); return 0; }); }
+int kso_compute_sources(void* h) { return guard(h, [](Sim& s) { s.compute_sources(s.vel_old); return 0; }); }
 
 int kso_field_shape(void* h, const char* name, int* nc, int* nx, int* ny, int* nz) {
     return guard(h, [&](Sim& s) {

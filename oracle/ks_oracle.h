@@ -2,7 +2,7 @@
  * CPU oracle for the single-level incompressible advance (test infrastructure).
  *
  * This header declares the C entry points of the FP64 CPU restatement of
- * Kynema-SGF's Godunov / explicit-diffusion step (oracle/ks_oracle.cpp).  It is
+ * Kynema-SGF's Godunov and MOL explicit-diffusion steps (oracle/ks_oracle.cpp).  It is
  * used ONLY by tests/, the package smoke check and the CPU-baseline leg of
  * bench.py, as the checker and as the timed CPU baseline.  The product library
  * (include/ks.h) never links, loads or calls it.
@@ -31,6 +31,7 @@ int kso_compute_dt(void* h, double* dt);
 int kso_pre_advance(void* h);
 int kso_prepare_time_step(void* h);
 int kso_apply_predictor(void* h, int incremental, int fixed_point_iteration);
+int kso_apply_corrector(void* h);
 int kso_apply_projection(void* h, double time, double scaling, int incremental);
 
 int kso_field_shape(void* h, const char* name, int* ncomp, int* nx, int* ny, int* nz);

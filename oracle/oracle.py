@@ -40,7 +40,8 @@ def load():
         lib.kso_destroy.restype = None
         lib.kso_last_error.argtypes = [vp]
         lib.kso_last_error.restype = ctypes.c_char_p
-        for n in ["kso_init_data", "kso_step", "kso_pre_advance", "kso_prepare_time_step", "kso_update_mueff", "kso_compute_sources"]:
+        for n in ["kso_init_data", "kso_step", "kso_pre_advance", "kso_prepare_time_step", "kso_update_mueff", "kso_compute_sources",
+                  "kso_apply_corrector"]:
             getattr(lib, n).argtypes = [vp]
         lib.kso_evolve.argtypes = [vp, ip]
         lib.kso_compute_dt.argtypes = [vp, ctypes.POINTER(dp)]
@@ -102,6 +103,9 @@ class Oracle:
 
     def ApplyPredictor(self, incremental_projection=False, fixed_point_iteration=0):
         self._check(self._lib.kso_apply_predictor(self._h, int(bool(incremental_projection)), int(fixed_point_iteration)))
+
+    def ApplyCorrector(self):
+        self._check(self._lib.kso_apply_corrector(self._h))
 
     def ApplyProjection(self, time, scaling_factor, incremental=False):
         self._check(self._lib.kso_apply_projection(self._h, float(time), float(scaling_factor), int(bool(incremental))))
