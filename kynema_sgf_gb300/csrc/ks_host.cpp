@@ -79,7 +79,10 @@ void Sim::setup(const Deck& D) {
         if (lc(D.str("incflo.godunov_type", "weno_z")) != "ppm") throw KsError(KS_ERR_UNSUPPORTED, "incflo.godunov_type must be ppm");
         if (D.flag("incflo.godunov_use_forces_in_trans", 0) != 0) throw KsError(KS_ERR_UNSUPPORTED, "godunov_use_forces_in_trans");
     }
-    if (D.flag("incflo.diffusion_type", 1) != 0) throw KsError(KS_ERR_UNSUPPORTED, "only explicit diffusion (incflo.diffusion_type = 0)");
+    // src/setup/init.cpp:60-76 (the default is Crank-Nicolson)
+    diff_type_ = D.flag("incflo.diffusion_type", 1);
+    if (diff_type_ < 0 || diff_type_ > 2)
+        throw KsError(KS_ERR_DECK, "We currently require diffusion_type = 0 for explicit, 1 for Crank-Nicolson or 2 for implicit");
     if (D.flag("incflo.icns_conserv", 1) != 1) throw KsError(KS_ERR_UNSUPPORTED, "non-conservative momentum form");
     initial_proj_ = D.flag("incflo.do_initial_proj", 1);
     initial_iters_ = D.flag("incflo.initial_iterations", 3);
@@ -152,6 +155,8 @@ void Sim::setup(const Deck& D) {
     };
     mg(mac_, "mac_proj");
     mg(nod_, "nodal_proj");
+    mg(dif_, "diffusion");  // MLMGOptions(default prefix, custom prefix), src/core/MLMGOptions.cpp:8-13
+    mg(dif_, "velocity_diffusion");
 
     t_.stop = D.num("time.stop_time", -1);
     t_.max_step = D.flag("time.max_step", -1);
@@ -387,7 +392,8 @@ void Sim::compute_dt() {
     double m[3];
     reduce(np, 3, 1, m);
     if (!std::isfinite(m[0]) || !std::isfinite(m[1]) || !std::isfinite(m[2])) throw KsError(KS_ERR_NONFINITE, "non-finite CFL");
-    t_.set_cfl(m[0], m[1], t_.force_cfl ? m[2] : 0.0);
+    // the diffusion CFL counts for explicit diffusion only (incflo_compute_dt.cpp:37,140-145,211-214)
+    t_.set_cfl(m[0], diff_type_ == 0 ? m[1] : 0.0, t_.force_cfl ? m[2] : 0.0);
 }
 
 // ---------------------------------------------------------------- ABL
@@ -715,6 +721,138 @@ void Sim::nd_solve(double sigma) {
     nod_r_ = rn;
 }
 
+// ---------------------------------------------------------------- diffusion solve
+// rho u - dtd divtau(u) = rho u_rhs (DiffSolverIface::linsys_solve,
+// src/equation_systems/DiffusionOps.cpp:114-159: MLTensorOp, alpha 1, a = rho,
+// beta = dtd, face viscosity of the current mu_eff, wall-model data from the Old
+// velocity), u_rhs the current velocity and initial guess.  Geometric
+// multigrid on the MAC hierarchy's levels: V-cycles of weighted-Jacobi sweeps
+// of the full tensor operator (each sweep one tiled divtau pass with the
+// update fused), 8-cell averaging restriction, piecewise-constant
+// prolongation, viscosity averaged to the coarse cells, homogeneous boundary
+// data below the finest level.  The first sweep of every cycle also returns
+// the max-norm residual of the incoming iterate; the solve stops as MLMG does,
+// at max(atol, rtol * initial residual) or maxiter cycles.
+constexpr double kDiffOmega = 0.8;  // Jacobi weight: D^-1 A has its spectrum in (0, 2)
+constexpr int kDiffBottom = 24;     // sweeps on the coarsest level
+
+void Sim::diff_alloc() {
+    if (!dl_.empty()) return;
+    size_t tot = 0;
+    for (size_t l = 0; l < cc_.size(); ++l) {
+        const size_t n = (size_t)cc_[l].nx * cc_[l].ny * cc_[l].nz;
+        tot += l == 0 ? 6 * n : 16 * n;  // level 0: r, dinv; coarser: x, b, r, t, dinv (3 each) + mu
+    }
+    dbuf_.alloc(tot);
+    dtmp_.alloc(3 * (size_t)g_.N);
+    dparts_.alloc((size_t)divtau_tile_blocks(g_));
+    double* q = dbuf_.p;
+    for (size_t l = 0; l < cc_.size(); ++l) {
+        DiffLevel L{};
+        L.g = g_;
+        L.g.nx = cc_[l].nx;
+        L.g.ny = cc_[l].ny;
+        L.g.nz = cc_[l].nz;
+        const double f = (double)(1 << l);
+        L.g.dx = g_.dx * f;
+        L.g.dy = g_.dy * f;
+        L.g.dz = g_.dz * f;
+        L.g.idx = 1.0 / L.g.dx;
+        L.g.idy = 1.0 / L.g.dy;
+        L.g.idz = 1.0 / L.g.dz;
+        L.g.N = (long long)L.g.nx * L.g.ny * L.g.nz;
+        L.g.NFz = (long long)L.g.nx * L.g.ny * (L.g.nz + 1);
+        if (l > 0 && L.g.zlo == ZWALLMODEL) L.g.zlo = ZSLIP;  // the correction equation has zero Neumann data
+        const size_t n = (size_t)L.g.N;
+        if (l == 0) {
+            L.r = q; q += 3 * n;
+            L.dinv = q; q += 3 * n;
+            L.mu = mueff_.p;
+        } else {
+            L.x = q; q += 3 * n;
+            L.b = q; q += 3 * n;
+            L.r = q; q += 3 * n;
+            L.t = q; q += 3 * n;
+            L.dinv = q; q += 3 * n;
+            L.mu = q; q += n;
+        }
+        dl_.push_back(L);
+    }
+}
+
+void Sim::diff_vcycle(size_t l, double dtd) {
+    DiffLevel& L = dl_[l];
+    auto sweep = [&]() {
+        launch_divtau_jacobi(ctx_, L.g, L.x, L.mu, nullptr, L.b, L.dinv, L.t, rho_, dtd, kDiffOmega, nullptr);
+        std::swap(L.x, L.t);
+    };
+    if (l + 1 == dl_.size()) {
+        for (int s = 0; s < kDiffBottom; ++s) sweep();
+        return;
+    }
+    for (int s = 0; s < dif_.nu1; ++s) sweep();
+    launch_divtau_jacobi(ctx_, L.g, L.x, L.mu, nullptr, L.b, nullptr, L.r, rho_, dtd, 0.0, nullptr);
+    DiffLevel& C = dl_[l + 1];
+    launch_avg8(ctx_, L.g, C.g, L.r, C.b, 3);
+    launch_fill(ctx_, C.x, 0.0, 3 * C.g.N);
+    diff_vcycle(l + 1, dtd);
+    launch_prolong_add(ctx_, L.g, C.g, C.x, L.x);
+    for (int s = 0; s < dif_.nu2; ++s) sweep();
+}
+
+void Sim::diffuse_solve(double dtd) {
+    diff_alloc();
+    const long long N3 = 3 * g_.N;
+    DiffLevel& L0 = dl_[0];
+    L0.mu = mueff_.p;
+    launch_scale(ctx_, vel_tmp_.p, vel_.p, rho_, N3);  // b = rho u_rhs
+    launch_diff_dinv(ctx_, g_, mueff_.p, rho_, dtd, L0.dinv);
+    for (size_t l = 1; l < dl_.size(); ++l) {
+        launch_avg8(ctx_, dl_[l - 1].g, dl_[l].g, dl_[l - 1].mu, dl_[l].mu, 1);
+        launch_diff_dinv(ctx_, dl_[l].g, dl_[l].mu, rho_, dtd, dl_[l].dinv);
+    }
+    const int np = divtau_tile_blocks(g_);
+    int it = 0;
+    double r0 = 0.0, rn = 0.0, target = 0.0;
+    while (true) {
+        launch_divtau_jacobi(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, L0.dinv, dtmp_.p, rho_, dtd, kDiffOmega, dparts_.p);
+        std::swap(vel_.p, dtmp_.p);
+        launch_reduce(ctx_, dparts_.p, np, 1, 1, red_.p);
+        ck(cudaMemcpyAsync(hred_, red_.p, sizeof(double), cudaMemcpyDeviceToHost, ctx_.stream), "D2H");
+        sync();
+        rn = hred_[0];
+        if (it == 0) {
+            r0 = rn;
+            target = std::max(dif_.atol, dif_.rtol * r0);
+        }
+        if (!std::isfinite(rn)) throw KsError(KS_ERR_NONFINITE, "diffusion solve diverged");
+        if (rn > 1e20 * r0) throw KsError(KS_ERR_NOT_CONVERGED, "diffusion solve diverged (residual above 1e20 times the initial one)");
+        if (rn <= target || it >= dif_.maxiter) break;
+        ++it;
+        // the rest of a V-cycle on the finest level (its first sweep is the one above)
+        for (int s = 1; s < dif_.nu1; ++s) {
+            launch_divtau_jacobi(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, L0.dinv, dtmp_.p, rho_, dtd, kDiffOmega, nullptr);
+            std::swap(vel_.p, dtmp_.p);
+        }
+        if (dl_.size() > 1) {
+            launch_divtau_jacobi(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, nullptr, L0.r, rho_, dtd, 0.0, nullptr);
+            DiffLevel& C = dl_[1];
+            launch_avg8(ctx_, g_, C.g, L0.r, C.b, 3);
+            launch_fill(ctx_, C.x, 0.0, 3 * C.g.N);
+            diff_vcycle(1, dtd);
+            launch_prolong_add(ctx_, g_, C.g, C.x, vel_.p);
+        }
+        for (int s = 0; s < dif_.nu2; ++s) {
+            launch_divtau_jacobi(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, L0.dinv, dtmp_.p, rho_, dtd, kDiffOmega, nullptr);
+            std::swap(vel_.p, dtmp_.p);
+        }
+    }
+    if (rn > target && !dif_.fixed_iters) throw KsError(KS_ERR_NOT_CONVERGED, "diffusion solve did not converge in diffusion.maxiter V-cycles");
+    dif_it_ = it;
+    dif_r0_ = r0;
+    dif_r_ = rn;
+}
+
 void Sim::apply_projection(double time, double scaling, bool incremental) {
     const bool small_dt = (time > 0.0 && t_.dt[0] < 0.1 * t_.dt[1]);
     const bool sub_old = small_dt || incremental;
@@ -745,9 +883,13 @@ void Sim::apply_predictor(bool incremental) {
     launch_advection(ctx_, g_, vel_old_.p, forces_.p, cmac, dt, rho_, adv_bufs_ ? *adv_bufs_ : gb_, conv_.p, mixed_);
     // compute_source_term(NPH) and compute_diffusion_term(Old) reproduce src
     // and divtau on this path (Coriolis reads the Old velocity, gp unchanged).
-    launch_predictor_rhs(ctx_, g_, vel_old_.p, conv_.p, src_.p, divtau_.p, vel_.p, dt, rho_);
-    launch_divtau(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, 2, nullptr, nullptr, vel_.p, divtau_.p, dt, rho_, fl);
-    std::swap(vel_.p, vel_tmp_.p);
+    launch_predictor_rhs(ctx_, g_, vel_old_.p, conv_.p, src_.p, divtau_.p, vel_.p, dt, rho_, diff_fac());
+    if (diff_type_ == 0) {  // explicit RK2 correction (incflo_advance.cpp:388-400)
+        launch_divtau(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, 2, nullptr, nullptr, vel_.p, divtau_.p, dt, rho_, fl);
+        std::swap(vel_.p, vel_tmp_.p);
+    } else {  // icns().solve(dt_diff) (incflo_advance.cpp:376-386)
+        diffuse_solve(diff_type_ == 2 ? dt : 0.5 * dt);
+    }
     apply_projection(t_.next, dt, incremental);
 }
 
@@ -763,13 +905,16 @@ void Sim::mol_predictor(bool incremental) {
     if (wallmodel_) launch_wall_grad(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, shear_, utau_ * utau_, um_[0], um_[1], vmag_, rho_);
     double* fl[9];
     for (int m = 0; m < 9; ++m) fl[m] = static_cast<double*>(gb_.flux[m / 3][m % 3]);
-    launch_divtau(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, divtau_.p, 0, nullptr, nullptr, nullptr, nullptr, dt, rho_, fl);
+    // diff_term(Old) enters predictor_rhs with factor 1 / 0.5 / 0 (implicit: not formed)
+    const double fac = diff_fac();
+    if (fac != 0.0) launch_divtau(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, divtau_.p, 0, nullptr, nullptr, nullptr, nullptr, dt, rho_, fl);
     launch_sources(ctx_, g_, vel_old_.p, gp_.p, act_.p, src_.p, S_);
     double* mac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
     launch_mol_extrap(ctx_, g_, vel_old_.p, mac);
     mac_project();
     const double* cmac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
-    launch_mol_advection(ctx_, g_, vel_old_.p, cmac, rho_, fl, conv_old_.p, 1, vel_old_.p, src_.p, divtau_.p, vel_.p, dt);
+    launch_mol_advection(ctx_, g_, vel_old_.p, cmac, rho_, fl, conv_old_.p, 1, vel_old_.p, src_.p, divtau_.p, nullptr, vel_.p, dt, fac);
+    if (diff_type_ != 0) diffuse_solve(diff_type_ == 2 ? dt : 0.5 * dt);
     apply_projection(t_.next, dt, incremental);
 }
 
@@ -787,7 +932,20 @@ void Sim::apply_corrector() {
     launch_mol_extrap(ctx_, g_, vel_.p, mac);
     mac_project();
     const double* cmac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
-    launch_mol_advection(ctx_, g_, vel_.p, cmac, rho_, fl, conv_.p, 0, nullptr, nullptr, nullptr, nullptr, dt);
+    if (diff_type_ != 0) {
+        // corrector_rhs with ofac 1/2 (Crank-Nicolson) or 0 (implicit) and nfac 0, fused into the
+        // divergence of the fluxes, then the solve with mu_eff(New) (incflo_advance.cpp:620-640)
+        launch_sources(ctx_, g_, vel_.p, gp_.p, act_.p, src_.p, S_);
+        launch_mol_advection(ctx_, g_, vel_.p, cmac, rho_, fl, conv_.p, 2, vel_old_.p, src_.p, divtau_.p, conv_old_.p, vel_tmp_.p, dt,
+                             diff_type_ == 1 ? 0.5 : 0.0);
+        std::swap(vel_.p, vel_tmp_.p);
+        launch_smagorinsky(ctx_, g_, vel_tmp_.p, mueff_.p, S_);
+        if (wallmodel_) launch_wall_grad(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, shear_, utau_ * utau_, um_[0], um_[1], vmag_, rho_);
+        diffuse_solve(diff_type_ == 2 ? dt : 0.5 * dt);
+        apply_projection(t_.next, dt, false);
+        return;
+    }
+    launch_mol_advection(ctx_, g_, vel_.p, cmac, rho_, fl, conv_.p, 0, nullptr, nullptr, nullptr, nullptr, nullptr, dt, 0.0);
     launch_smagorinsky(ctx_, g_, vel_.p, mueff_.p, S_);
     if (wallmodel_) launch_wall_grad(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, shear_, utau_ * utau_, um_[0], um_[1], vmag_, rho_);
     launch_sources(ctx_, g_, vel_.p, gp_.p, act_.p, src_.p, S_);
@@ -921,6 +1079,9 @@ double Sim::scalar(const std::string& n) {
     if (n == "step") return t_.step;
     if (n == "mac_iters") return mac_it_;
     if (n == "nodal_iters") return nod_it_;
+    if (n == "diff_iters") return dif_it_;
+    if (n == "diff_res0") return dif_r0_;
+    if (n == "diff_res") return dif_r_;
     if (n == "mac_res0") return mac_r0_;
     if (n == "mac_res") return mac_r_;
     if (n == "nodal_res0") return nod_r0_;

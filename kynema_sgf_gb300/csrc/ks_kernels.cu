@@ -325,12 +325,24 @@ constexpr int TNH = THX * THY * THZ;
 constexpr int TNFX = (TTX + 1) * TTY * TTZ, TNFY = TTX * (TTY + 1) * TTZ, TNFZ = TTX * TTY * (TTZ + 1);
 constexpr size_t TAU_SMEM = sizeof(double) * (4 * (size_t)TNH + 3 * ((size_t)TNFX + TNFY + TNFZ));
 
-// mode 3 (MOL corrector_rhs, explicit): out = (rho base + dt (0.5 (conv_o + conv_n)
-// + 0.5 (dold + divtau(vel)) + src)) / rho, base = u_old
+// Epilogue of the tiled tensor-diffusion kernel (acc = divtau(vel) of a cell):
+//   0: out = acc
+//   1: out = acc, forces = (src + acc) / rho
+//   2: out = base + 0.5 dt (acc - dold) / rho                        (explicit RK2 correction)
+//   3: out = (rho base + dt (0.5 (conv_o + conv_n) + 0.5 (dold + acc) + src)) / rho  (MOL corrector_rhs)
+//   7: out = x + omega dinv (base - rho x + dt acc), x = vel           (Jacobi sweep of rho x - dt divtau x = base)
+//   8: out = base - rho x + dt acc                                    (its residual)
+// Modes 7 and 8 write block maxima of the residual's magnitude to parts when it is set.
+struct TauEpi {
+    int mode;
+    const double *src, *base, *dold, *conv_o, *conv_n, *dinv;
+    double* forces;
+    double* parts;
+    double dt, rho, omega;
+};
+
 __global__ void __launch_bounds__(TTX* TTY* TTZ) k_divtau_tile(Grid g, const double* vel, const double* mueff, const double* wg, double* out,
-                                                               int mode, const double* src, double* forces, const double* base,
-                                                               const double* dold, double dt, double rho, const double* conv_o,
-                                                               const double* conv_n) {
+                                                               TauEpi E) {
     extern __shared__ double sm[];
     double* sV = sm;                // [3][THZ][THY][THX]
     double* sM = sm + 3 * TNH;      // [THZ][THY][THX]
@@ -404,36 +416,53 @@ __global__ void __launch_bounds__(TTX* TTY* TTZ) k_divtau_tile(Grid g, const dou
     __syncthreads();
     const int tx = tid % TTX, ty = (tid / TTX) % TTY, tz = tid / (TTX * TTY);
     const int i = i0 + tx, j = j0 + ty, k = k0 + tz;
-    if (i >= g.nx || j >= g.ny || k >= g.nz) return;
-    const double irho = 1.0 / rho;
-    const long long N = g.N, t = cidx(g, i, j, k);
-    for (int n = 0; n < 3; ++n) {
+    const bool live = i < g.nx && j < g.ny && k < g.nz;
+    const double rho = E.rho, dt = E.dt, irho = 1.0 / rho;
+    const long long N = g.N, t = live ? cidx(g, i, j, k) : 0;
+    double rmax = 0.0;
+    for (int n = 0; n < 3 && live; ++n) {
         const int ax = (tz * TTY + ty) * (TTX + 1) + tx;
         const int ay = (tz * (TTY + 1) + ty) * TTX + tx;
         const int az = (tz * TTY + ty) * TTX + tx;
         double acc = (sFx[n * TNFX + ax + 1] - sFx[n * TNFX + ax]) * ih[0];
         acc += (sFy[n * TNFY + ay + TTX] - sFy[n * TNFY + ay]) * ih[1];
         acc += (sFz[n * TNFZ + az + TTX * TTY] - sFz[n * TNFZ + az]) * ih[2];
-        if (mode == 0) {
-            out[n * N + t] = acc;
-        } else if (mode == 1) {
-            out[n * N + t] = acc;
-            forces[n * N + t] = (src[n * N + t] + acc) * irho;
-        } else if (mode == 2) {
-            out[n * N + t] = base[n * N + t] + 0.5 * dt * (acc - dold[n * N + t]) * irho;
+        const long long m = n * N + t;
+        if (E.mode == 0) {
+            out[m] = acc;
+        } else if (E.mode == 1) {
+            out[m] = acc;
+            E.forces[m] = (E.src[m] + acc) * irho;
+        } else if (E.mode == 2) {
+            out[m] = E.base[m] + 0.5 * dt * (acc - E.dold[m]) * irho;
+        } else if (E.mode == 3) {
+            out[m] = (rho * E.base[m] + dt * (0.5 * (E.conv_o[m] + E.conv_n[m]) + 0.5 * E.dold[m] + 0.5 * acc + E.src[m])) * irho;
         } else {
-            const long long m = n * N + t;
-            out[m] = (rho * base[m] + dt * (0.5 * (conv_o[m] + conv_n[m]) + 0.5 * dold[m] + 0.5 * acc + src[m])) * irho;
+            const double x = sV[n * TNH + hidx(tx + 1, ty + 1, tz + 1)];
+            const double r = E.base[m] - rho * x + dt * acc;
+            rmax = nmax(rmax, fabs(r));
+            out[m] = E.mode == 7 ? x + E.omega * E.dinv[m] * r : r;
         }
+    }
+    if (!E.parts) return;  // uniform over the block
+    for (int o = 16; o > 0; o >>= 1) rmax = nmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+    __shared__ double wmax[TTX * TTY * TTZ / 32];
+    if ((tid & 31) == 0) wmax[tid >> 5] = rmax;
+    __syncthreads();
+    if (tid == 0) {
+        double b = 0.0;
+        for (int w = 0; w < TTX * TTY * TTZ / 32; ++w) b = nmax(b, wmax[w]);
+        E.parts[(blockIdx.z * (long long)gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = b;
     }
 }
 
-// predictor_rhs, Explicit (src/equation_systems/CompRHSOps.H:32-141)
+// predictor_rhs (src/equation_systems/CompRHSOps.H:32-141); fac = 1 explicit,
+// 1/2 Crank-Nicolson, 0 implicit
 __global__ void k_pred_rhs(long long N3, const double* vo, const double* conv, const double* src, const double* dt_, double* vel, double dt,
-                           double rho) {
+                           double rho, double fac) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= N3) return;
-    vel[t] = (rho * vo[t] + dt * (conv[t] + src[t] + dt_[t])) * (1.0 / rho);
+    vel[t] = (rho * vo[t] + dt * (conv[t] + src[t] + fac * dt_[t])) * (1.0 / rho);
 }
 
 // ---------------------------------------------------------------- projection
@@ -703,19 +732,27 @@ void launch_divtau(Ctx& c, const Grid& g, const double* vel, const double* mueff
     cudaFuncSetAttribute(k_divtau_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAU_SMEM);
     const dim3 grid((g.nx + TTX - 1) / TTX, (g.ny + TTY - 1) / TTY, (g.nz + TTZ - 1) / TTZ);
     const double per_cell = 4 + 3 + (mode == 1 ? 6 : 0) + (mode == 2 ? 6 : 0);
-    KS_LAUNCH_SMEM(c, k_divtau_tile, grid, TTX * TTY * TTZ, TAU_SMEM, B8 * per_cell * g.N, g, vel, mueff, wg, out, mode, src, forces, base, dold,
-                   dt, rho, nullptr, nullptr);
+    TauEpi E{mode, src, base, dold, nullptr, nullptr, nullptr, forces, nullptr, dt, rho, 0.0};
+    KS_LAUNCH_SMEM(c, k_divtau_tile, grid, TTX * TTY * TTZ, TAU_SMEM, B8 * per_cell * g.N, g, vel, mueff, wg, out, E);
 }
 void launch_divtau_corrector(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, const double* vel_old,
                              const double* conv_old, const double* conv_new, const double* dold, const double* src, double dt, double rho) {
     cudaFuncSetAttribute(k_divtau_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAU_SMEM);
     const dim3 grid((g.nx + TTX - 1) / TTX, (g.ny + TTY - 1) / TTY, (g.nz + TTZ - 1) / TTZ);
-    KS_LAUNCH_SMEM(c, k_divtau_tile, grid, TTX * TTY * TTZ, TAU_SMEM, B8 * 22.0 * g.N, g, vel, mueff, wg, out, 3, src, nullptr, vel_old, dold, dt,
-                   rho, conv_old, conv_new);
+    TauEpi E{3, src, vel_old, dold, conv_old, conv_new, nullptr, nullptr, nullptr, dt, rho, 0.0};
+    KS_LAUNCH_SMEM(c, k_divtau_tile, grid, TTX * TTY * TTZ, TAU_SMEM, B8 * 22.0 * g.N, g, vel, mueff, wg, out, E);
+}
+int divtau_tile_blocks(const Grid& g) { return ((g.nx + TTX - 1) / TTX) * ((g.ny + TTY - 1) / TTY) * ((g.nz + TTZ - 1) / TTZ); }
+void launch_divtau_jacobi(Ctx& c, const Grid& g, const double* x, const double* mueff, const double* wg, const double* b, const double* dinv,
+                          double* out, double rho, double dtd, double omega, double* parts) {
+    cudaFuncSetAttribute(k_divtau_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAU_SMEM);
+    const dim3 grid((g.nx + TTX - 1) / TTX, (g.ny + TTY - 1) / TTY, (g.nz + TTZ - 1) / TTZ);
+    TauEpi E{omega > 0.0 ? 7 : 8, nullptr, b, nullptr, nullptr, nullptr, dinv, nullptr, parts, dtd, rho, omega};
+    KS_LAUNCH_SMEM(c, k_divtau_tile, grid, TTX * TTY * TTZ, TAU_SMEM, B8 * ((omega > 0.0 ? 13.0 : 10.0) * g.N), g, x, mueff, wg, out, E);
 }
 void launch_predictor_rhs(Ctx& c, const Grid& g, const double* vo, const double* conv, const double* src, const double* dtau, double* vel,
-                          double dt, double rho) {
-    KS_LAUNCH(c, k_pred_rhs, nblocks(3 * g.N, BS), BS, B8 * 15 * g.N, 3 * g.N, vo, conv, src, dtau, vel, dt, rho);
+                          double dt, double rho, double fac) {
+    KS_LAUNCH(c, k_pred_rhs, nblocks(3 * g.N, BS), BS, B8 * 15 * g.N, 3 * g.N, vo, conv, src, dtau, vel, dt, rho, fac);
 }
 void launch_proj_pre(Ctx& c, const Grid& g, double* vel, const double* vo, const double* gp, double scaling, double rho, int add_gp,
                      int sub_old) {

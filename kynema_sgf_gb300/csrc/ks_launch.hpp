@@ -141,8 +141,15 @@ void launch_divtau_faces(Ctx& c, const Grid& g, const double* vel, const double*
 // out = (rho u_old + dt (0.5 (conv_old + conv_new) + 0.5 (dold + divtau(vel)) + src)) / rho
 void launch_divtau_corrector(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, const double* vel_old,
                              const double* conv_old, const double* conv_new, const double* dold, const double* src, double dt, double rho);
+// Tensor-diffusion solve passes on any level grid g: out = x + omega dinv (b - rho x + dtd divtau(x))
+// (omega > 0, a Jacobi sweep) or out = b - rho x + dtd divtau(x) (omega = 0, the residual), with
+// block maxima of the residual's magnitude in parts (divtau_tile_blocks(g) entries) when parts is set.
+int divtau_tile_blocks(const Grid& g);
+void launch_divtau_jacobi(Ctx& c, const Grid& g, const double* x, const double* mueff, const double* wg, const double* b, const double* dinv,
+                          double* out, double rho, double dtd, double omega, double* parts);
+// predictor_rhs: vel = (rho vel_old + dt (conv + src + fac divtau)) / rho
 void launch_predictor_rhs(Ctx& c, const Grid& g, const double* vel_old, const double* conv, const double* src, const double* divtau,
-                          double* vel, double dt, double rho);
+                          double* vel, double dt, double rho, double fac);
 void launch_proj_pre(Ctx& c, const Grid& g, double* vel, const double* vel_old, const double* gp, double scaling, double rho,
                      int add_gp, int sub_old);
 void launch_nodal_rhs(Ctx& c, const Grid& g, const double* vel, double* rhs, double* partials, int* nparts);
@@ -181,10 +188,21 @@ void launch_advection(Ctx& c, const Grid& g, const double* vel_old, const double
 // face-normal velocities extrapolated from vel (before the MAC projection)
 void launch_mol_extrap(Ctx& c, const Grid& g, const double* vel, double* const mac[3]);
 // conv = -div(u_mac (rho u)_face) through the nine face-flux arrays fl; mode 1
-// also writes vel_out = (rho vel_old + dt (conv + src + dold)) / rho
+// also writes vel_out = (rho vel_old + dt (conv + src + fac dold)) / rho (predictor_rhs),
+// mode 2 vel_out = (rho vel_old + dt (0.5 (conv_old + conv) + fac dold + src)) / rho
+// (corrector_rhs of Crank-Nicolson / implicit diffusion)
 void launch_mol_advection(Ctx& c, const Grid& g, const double* vel, const double* const mac[3], double rho, double* const fl[9],
-                          double* conv, int mode, const double* vel_old, const double* src, const double* dold, double* vel_out,
-                          double dt);
+                          double* conv, int mode, const double* vel_old, const double* src, const double* dold, const double* conv_old,
+                          double* vel_out, double dt, double fac);
+
+// ---- implicit / Crank-Nicolson tensor diffusion solve (ks_implicit.cu)
+// 1 / diagonal of rho - dtd divtau per cell and component (3 N_g values)
+void launch_diff_dinv(Ctx& c, const Grid& g, const double* mueff, double rho, double dtd, double* dinv);
+// coarse = mean of the 8 fine cells below each coarse cell, ncomp components
+void launch_avg8(Ctx& c, const Grid& fine, const Grid& coarse, const double* f, double* cr, int ncomp);
+// fine += coarse value of the parent cell (piecewise-constant prolongation), 3 components
+void launch_prolong_add(Ctx& c, const Grid& fine, const Grid& coarse, const double* cr, double* f);
+void launch_scale(Ctx& c, double* out, const double* in, double a, long long n);
 
 // ---- reverse mode of the Godunov passes (ks_adjoint.cu), FP64, periodic.
 // Adjoints of the GodunovBufs arrays (same shapes) plus those of the MAC

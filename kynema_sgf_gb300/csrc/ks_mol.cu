@@ -9,9 +9,12 @@
 // icns_advection.H:531-594 with q = rho u), with AMReX's order-2
 // monotonized-central slopes (amrex_calc_{x,y,z}slope and their _extdir forms).
 //
-// Every face state is computed once: one thread per face forms the two
-// one-sided states of all three components, the divergence pass reads the
-// nine face-flux arrays and, in the predictor, also forms predictor_rhs.
+// FP64 issue is the bound, so every cell's slope is computed once per
+// component (a few more at segment ends) and every face state once: the x-face
+// kernel passes slopes between neighbouring lanes of a warp, the y- and z-face
+// kernels march along columns.
+// The divergence pass reads the nine face-flux arrays and, in the predictor,
+// also forms predictor_rhs.
 #include <cfloat>
 
 #include "ks_launch.hpp"
@@ -43,19 +46,6 @@ __device__ inline int z_edge(const Grid& g, int d, int k) {
     return k == 0 ? -1 : (k == g.nz - 1 ? 1 : 0);
 }
 
-// States of component n on the d-face at the low side of cell (i, j, k):
-// qmns extrapolated from the cell below, qpls from the cell above.
-__device__ inline void mol_states(const VelFP& q, const Grid& g, int d, int n, int i, int j, int k, double& qmns, double& qpls) {
-    const int e0 = d == 0, e1 = d == 1, e2 = d == 2;
-    const double a = q(n, i - 2 * e0, j - 2 * e1, k - 2 * e2);
-    const double b = q(n, i - e0, j - e1, k - e2);
-    const double c = q(n, i, j, k);
-    const double e = q(n, i + e0, j + e1, k + e2);
-    const int kd = d == 0 ? i : (d == 1 ? j : k);
-    qmns = b + 0.5 * mc_slope(a, b, c, z_edge(g, d, kd - 1));
-    qpls = c - 0.5 * mc_slope(b, c, e, z_edge(g, d, kd));
-}
-
 // ExtrapVelToFaces choice: zero where the states diverge or their mean is
 // below small_vel = 1e-10, else the upwind state
 __device__ inline double mol_pick(double umns, double upls) {
@@ -65,61 +55,118 @@ __device__ inline double mol_pick(double umns, double upls) {
     return avg >= 0.0 ? umns : upls;
 }
 
-// One thread per (i, j, k) of the z-face layers: the x, y and z faces at the
-// low side of the cell (z walls: the face takes the ghost value 0).
-__global__ void k_mol_extrap(Grid g, const double* vel, double* um, double* vm, double* wm) {
+// compute_convective_fluxes choice: the upwind state, the mean of both where
+// |u_mac| <= small_vel = FLT_EPSILON
+__device__ inline double mol_upwind(double u, double qmns, double qpls) {
+    const double small_vel = (double)FLT_EPSILON;
+    return u > small_vel ? qmns : (u < -small_vel ? qpls : 0.5 * (qmns + qpls));
+}
+
+__device__ inline double* pick3(int n, double* a, double* b, double* c) { return n == 0 ? a : (n == 1 ? b : c); }
+
+// The face kernels come in two kinds: KIND 0 extrapolates the normal velocity
+// component d of u to the d-faces (ExtrapVelToFaces, written to mac); KIND 1
+// forms the fluxes of rho u (three components, upwinded with mac) through
+// them.  Each computes the MC slope of every cell once per component: the
+// x kernel takes the slope of cell i - 1 from the neighbouring lane of its warp,
+// the y and z kernels march along a column of MOL_CHUNK faces and carry it.
+
+// x faces: each warp covers 31 consecutive faces of one x row.  Lane l forms
+// the slope of cell i = 31 s + l - 1 (s: the warp's segment of the row);
+// lanes 1..31 take the slope of cell i - 1 from the lane below and form face i.
+// Every lane does the same work, so no lane's extra slope stalls the others.
+constexpr int XSEG = 31;
+template <int KIND>
+__global__ void k_mol_x(Grid g, const double* vel, double rho, const double* mac, double* o0, double* o1, double* o2) {
+    const int nseg = (g.nx + XSEG - 1) / XSEG;
+    const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const long long rows = (long long)g.ny * g.nz;
+    if (w >= rows * nseg) return;  // whole warps leave together
+    const long long row = w / nseg;
+    const int i = (int)(w % nseg) * XSEG + lane - 1;
+    const int j = (int)(row % g.ny), k = (int)(row / g.ny);
+    const bool face = lane > 0 && i < g.nx;
+    const int ic = min(i, g.nx - 1);  // lanes past the row end read in range and write nothing
+    const long long t = ((long long)k * g.ny + j) * g.nx + (face ? i : 0);
+    const VelFP Q{vel, g, KIND ? rho : 1.0};
+    const double u = (KIND && face) ? mac[t] : 0.0;
+    constexpr int nend = KIND ? 3 : 1;
+    for (int n = 0; n < nend; ++n) {
+        const double b = Q(n, ic - 1, j, k), c = Q(n, ic, j, k), e = Q(n, ic + 1, j, k);
+        const double s0 = mc_slope(b, c, e, 0);
+        const double sm = __shfl_up_sync(0xffffffffu, s0, 1);
+        if (!face) continue;
+        const double qmns = b + 0.5 * sm, qpls = c - 0.5 * s0;
+        if (KIND == 0) o0[t] = mol_pick(qmns, qpls);
+        else pick3(n, o0, o1, o2)[t] = mol_upwind(u, qmns, qpls) * u;
+    }
+}
+
+constexpr int MOL_CHUNK = 16;
+
+// y faces: one thread per (i, k, chunk of MOL_CHUNK faces along y)
+template <int KIND>
+__global__ void k_mol_y(Grid g, const double* vel, double rho, const double* mac, double* o0, double* o1, double* o2) {
+    const int nch = (g.ny + MOL_CHUNK - 1) / MOL_CHUNK;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const long long M = (long long)g.nx * g.ny * nzfaces(g);
-    if (t >= M) return;
+    if (t >= (long long)g.nx * g.nz * nch) return;
     const int i = (int)(t % g.nx);
     const long long r = t / g.nx;
-    const int j = (int)(r % g.ny), k = (int)(r / g.ny);
-    const VelFP V{vel, g, 1.0};
-    double mn, pl;
-    if (k < g.nz) {
-        mol_states(V, g, 0, 0, i, j, k, mn, pl);
-        um[t] = mol_pick(mn, pl);
-        mol_states(V, g, 1, 1, i, j, k, mn, pl);
-        vm[t] = mol_pick(mn, pl);
-    }
-    if (!g.zper && (k == 0 || k == g.nz)) {
-        wm[t] = 0.0;
-    } else {
-        mol_states(V, g, 2, 2, i, j, k, mn, pl);
-        wm[t] = mol_pick(mn, pl);
-    }
-}
-
-__device__ inline bool face_cell(const Grid& g, int d, long long t, int& i, int& j, int& k) {
-    const long long M = (long long)g.nx * g.ny * (d == 2 ? nzfaces(g) : g.nz);
-    if (t >= M) return false;
-    i = (int)(t % g.nx);
-    const long long r = t / g.nx;
-    j = (int)(r % g.ny);
-    k = (int)(r / g.ny);
-    return true;
-}
-
-// Fluxes of rho u through the d-faces: the MC-limited states upwinded with
-// the MAC velocity (their mean where |u_mac| <= FLT_EPSILON); on a z wall the
-// normal component takes the ghost (boundary) value 0.
-__global__ void k_mol_flux(Grid g, int d, const double* vel, const double* mac, double rho, double* F0, double* F1, double* F2) {
-    int i, j, k;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (!face_cell(g, d, t, i, j, k)) return;
-    const VelFP Q{vel, g, rho};
-    const double u = mac[t];
-    const double small_vel = (double)FLT_EPSILON;
-    const bool wall = d == 2 && !g.zper && (k == 0 || k == g.nz);
-    double* F[3] = {F0, F1, F2};
-    for (int n = 0; n < 3; ++n) {
-        double qs = 0.0;
-        if (!(wall && n == 2)) {
-            double mn, pl;
-            mol_states(Q, g, d, n, i, j, k, mn, pl);
-            qs = u > small_vel ? mn : (u < -small_vel ? pl : 0.5 * (mn + pl));
+    const int k = (int)(r % g.nz), ch = (int)(r / g.nz);
+    const int j0 = ch * MOL_CHUNK, j1 = min(j0 + MOL_CHUNK, g.ny);
+    const VelFP Q{vel, g, KIND ? rho : 1.0};
+    const int nbeg = KIND ? 0 : 1, nend = KIND ? 3 : 2;
+    for (int n = nbeg; n < nend; ++n) {
+        double qb = Q(n, i, j0 - 1, k), qc = Q(n, i, j0, k);
+        double sb = mc_slope(Q(n, i, j0 - 2, k), qb, qc, 0);
+        for (int j = j0; j < j1; ++j) {
+            const double qe = Q(n, i, j + 1, k);
+            const double sc = mc_slope(qb, qc, qe, 0);
+            const double qmns = qb + 0.5 * sb, qpls = qc - 0.5 * sc;
+            const long long f = cidx(g, i, j, k);
+            if (KIND == 0) o0[f] = mol_pick(qmns, qpls);
+            else pick3(n, o0, o1, o2)[f] = mol_upwind(mac[f], qmns, qpls) * mac[f];
+            qb = qc;
+            qc = qe;
+            sb = sc;
         }
-        F[n][t] = qs * u;
+    }
+}
+
+// z faces: one thread per (i, j, chunk of MOL_CHUNK face layers); on a wall
+// face the normal component takes the ghost (boundary) value 0
+template <int KIND>
+__global__ void k_mol_z(Grid g, const double* vel, double rho, const double* mac, double* o0, double* o1, double* o2) {
+    const int nzf = nzfaces(g);
+    const int nch = (nzf + MOL_CHUNK - 1) / MOL_CHUNK;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)g.nx * g.ny * nch) return;
+    const int i = (int)(t % g.nx);
+    const long long r = t / g.nx;
+    const int j = (int)(r % g.ny), ch = (int)(r / g.ny);
+    const int k0 = ch * MOL_CHUNK, k1 = min(k0 + MOL_CHUNK, nzf);
+    const VelFP Q{vel, g, KIND ? rho : 1.0};
+    const int nbeg = KIND ? 0 : 2;
+    for (int n = nbeg; n < 3; ++n) {
+        double qb = Q(n, i, j, k0 - 1), qc = Q(n, i, j, k0);
+        double sb = mc_slope(Q(n, i, j, k0 - 2), qb, qc, z_edge(g, 2, k0 - 1));
+        for (int k = k0; k < k1; ++k) {
+            const double qe = Q(n, i, j, k + 1);
+            const double sc = mc_slope(qb, qc, qe, z_edge(g, 2, k));
+            const double qmns = qb + 0.5 * sb, qpls = qc - 0.5 * sc;
+            const long long f = fidx(g, 2, i, j, k);
+            const bool wall = !g.zper && (k == 0 || k == g.nz);
+            if (KIND == 0) {
+                o0[f] = wall ? 0.0 : mol_pick(qmns, qpls);
+            } else {
+                const double u = mac[f];
+                pick3(n, o0, o1, o2)[f] = ((wall && n == 2) ? 0.0 : mol_upwind(u, qmns, qpls)) * u;
+            }
+            qb = qc;
+            qc = qe;
+            sb = sc;
+        }
     }
 }
 
@@ -128,9 +175,11 @@ struct MolFlux {
 };
 
 // conv = sum_d dxinv_d (F_lo - F_hi); mode 1 also forms predictor_rhs with
-// fstate Old: vel = (rho u_old + dt (conv + src + divtau_old)) / rho
+// fstate Old, vel = (rho u_old + dt (conv + src + fac divtau_old)) / rho; mode 2
+// corrector_rhs without the new diffusion term (Crank-Nicolson / implicit),
+// vel = (rho u_old + dt (0.5 (conv_old + conv) + fac divtau_old + src)) / rho
 __global__ void k_mol_div(Grid g, MolFlux F, double* conv, int mode, const double* vo, const double* src, const double* dold,
-                          double* vel, double dt, double rho) {
+                          const double* conv_o, double* vel, double dt, double rho, double fac) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= g.N) return;
     const int i = (int)(t % g.nx);
@@ -143,7 +192,9 @@ __global__ void k_mol_div(Grid g, MolFlux F, double* conv, int mode, const doubl
         const double c = (g.idx * (F.p[n][t] - F.p[n][xp])) + (g.idy * (F.p[3 + n][t] - F.p[3 + n][yp])) +
                          (g.idz * (F.p[6 + n][zm] - F.p[6 + n][zp]));
         conv[n * N + t] = c;
-        if (mode == 1) vel[n * N + t] = (rho * vo[n * N + t] + dt * (c + src[n * N + t] + dold[n * N + t])) * (1.0 / rho);
+        const long long m = n * N + t;
+        if (mode == 1) vel[m] = (rho * vo[m] + dt * (c + src[m] + fac * dold[m])) * (1.0 / rho);
+        else if (mode == 2) vel[m] = (rho * vo[m] + dt * (0.5 * (conv_o[m] + c) + fac * dold[m] + src[m])) * (1.0 / rho);
     }
 }
 
@@ -151,24 +202,37 @@ inline long long nfaces_d(const Grid& g, int d) { return (long long)g.nx * g.ny 
 
 }  // namespace
 
+template <int KIND>
+static void mol_faces(Ctx& c, const Grid& g, const double* vel, double rho, const double* const mac[3], double* const out[9]) {
+    const double nc = KIND ? 3.0 : 1.0;  // components read and written per face
+    const long long ty = (long long)g.nx * g.nz * ((g.ny + MOL_CHUNK - 1) / MOL_CHUNK);
+    const long long tz = (long long)g.nx * g.ny * ((nzfaces(g) + MOL_CHUNK - 1) / MOL_CHUNK);
+    const double nfz = (double)nfaces_d(g, 2);
+    auto o = [&](int d, int n) { return out[KIND ? 3 * d + n : d]; };
+    const double* m0 = KIND ? mac[0] : nullptr;
+    const double* m1 = KIND ? mac[1] : nullptr;
+    const double* m2 = KIND ? mac[2] : nullptr;
+    const long long tx = 32LL * g.ny * g.nz * ((g.nx + XSEG - 1) / XSEG);
+    KS_LAUNCH(c, k_mol_x<KIND>, nblocks(tx, BS), BS, 8.0 * (2.0 * nc + KIND) * g.N, g, vel, rho, m0, o(0, 0), o(0, 1), o(0, 2));
+    KS_LAUNCH(c, k_mol_y<KIND>, nblocks(ty, BS), BS, 8.0 * (2.0 * nc + KIND) * g.N, g, vel, rho, m1, o(1, 0), o(1, 1), o(1, 2));
+    KS_LAUNCH(c, k_mol_z<KIND>, nblocks(tz, BS), BS, 8.0 * (nc * g.N + (nc + KIND) * nfz), g, vel, rho, m2, o(2, 0), o(2, 1),
+              o(2, 2));
+}
+
 void launch_mol_extrap(Ctx& c, const Grid& g, const double* vel, double* const mac[3]) {
-    const long long M = (long long)g.nx * g.ny * nzfaces(g);
-    KS_LAUNCH(c, k_mol_extrap, nblocks(M, BS), BS, 8.0 * (3.0 * g.N + 2.0 * g.N + M), g, vel, mac[0], mac[1], mac[2]);
+    double* out[9] = {mac[0], mac[1], mac[2], nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    mol_faces<0>(c, g, vel, 1.0, nullptr, out);
 }
 
 void launch_mol_advection(Ctx& c, const Grid& g, const double* vel, const double* const mac[3], double rho, double* const fl[9],
-                          double* conv, int mode, const double* vel_old, const double* src, const double* dold, double* vel_out,
-                          double dt) {
-    for (int d = 0; d < 3; ++d) {
-        const double nf = (double)nfaces_d(g, d);
-        KS_LAUNCH(c, k_mol_flux, nblocks(nfaces_d(g, d), BS), BS, 8.0 * (3.0 * g.N + 4.0 * nf), g, d, vel, mac[d], rho, fl[3 * d],
-                  fl[3 * d + 1], fl[3 * d + 2]);
-    }
+                          double* conv, int mode, const double* vel_old, const double* src, const double* dold, const double* conv_old,
+                          double* vel_out, double dt, double fac) {
+    mol_faces<1>(c, g, vel, rho, mac, fl);
     MolFlux F;
     for (int m = 0; m < 9; ++m) F.p[m] = fl[m];
     const double nfz = (double)nfaces_d(g, 2);
-    const double bytes = 8.0 * (6.0 * g.N + 3.0 * nfz + 3.0 * g.N + (mode == 1 ? 12.0 * g.N : 0.0));
-    KS_LAUNCH(c, k_mol_div, nblocks(g.N, BS), BS, bytes, g, F, conv, mode, vel_old, src, dold, vel_out, dt, rho);
+    const double bytes = 8.0 * (6.0 * g.N + 3.0 * nfz + 3.0 * g.N + (mode == 1 ? 12.0 * g.N : (mode == 2 ? 15.0 * g.N : 0.0)));
+    KS_LAUNCH(c, k_mol_div, nblocks(g.N, BS), BS, bytes, g, F, conv, mode, vel_old, src, dold, conv_old, vel_out, dt, rho, fac);
 }
 
 }  // namespace ks

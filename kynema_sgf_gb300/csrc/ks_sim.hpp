@@ -257,7 +257,8 @@ class Sim {
     Ctx ctx_;
     Grid g_{};
     Clock t_;
-    int mac_it_ = 0, nod_it_ = 0;
+    int mac_it_ = 0, nod_it_ = 0, dif_it_ = 0;
+    double dif_r0_ = 0, dif_r_ = 0;
     int mixed_ = 0;  // 1: FP32 advection and multigrid cycles with FP64 defect correction
     GodunovBufs* adv_bufs_ = nullptr;  // post-MAC pass scratch when not gb_ (reverse-step recompute keeps both passes)
     double mac_r0_ = 0, mac_r_ = 0, nod_r0_ = 0, nod_r_ = 0;
@@ -283,6 +284,10 @@ class Sim {
     void nd_rhs(const double* cell_field);
     void nd_solve(double sigma);
     void mol_predictor(bool incremental);
+    void diff_alloc();
+    void diffuse_solve(double dtd);
+    void diff_vcycle(size_t l, double dtd);
+    double diff_fac() const { return diff_type_ == 0 ? 1.0 : (diff_type_ == 1 ? 0.5 : 0.0); }
     void disk_points(const Disk& d, std::vector<double>& sample, std::vector<double>& ring) const;
     // reverse mode
     void adj_check() const;
@@ -304,6 +309,16 @@ class Sim {
     MGParams mac_, nod_;
     int initial_proj_ = 1, initial_iters_ = 3;
     bool godunov_ = true;  // incflo.use_godunov; false: MOL predictor-corrector
+    int diff_type_ = 1;    // incflo.diffusion_type: 0 explicit, 1 Crank-Nicolson, 2 implicit
+    MGParams dif_;         // tensor diffusion solve (prefixes diffusion, velocity_diffusion)
+    // one level of the diffusion solve's multigrid: grid, iterate, right-hand
+    // side, residual, sweep target, cell viscosity, inverse diagonal
+    struct DiffLevel {
+        Grid g;
+        double *x, *b, *r, *t, *mu, *dinv;
+    };
+    std::vector<DiffLevel> dl_;
+    DevBuf<double> dbuf_, dtmp_, dparts_;
 
     DevBuf<double> vel_, vel_old_, vel_tmp_, gp_, p_, src_, forces_, mueff_, divtau_, conv_, act_, wg_;
     DevBuf<double> conv_old_;  // MOL: conv_term(Old) of the predictor

@@ -266,9 +266,10 @@ struct Sim {
     std::string shear_type = "moeng";
     double utau = 0, umean[2] = {0, 0}, vmag_mean = 0, zref = 0;
     std::vector<DiskParams> disks;
-    MGOpts mac, nod;
+    MGOpts mac, nod, dif;  // dif: the tensor diffusion solve (prefixes diffusion, velocity_diffusion)
     int do_initial_proj = 1, initial_iterations = 3;
     bool godunov = true;  // incflo.use_godunov; false selects the MOL predictor-corrector
+    int diff_type = 1;    // incflo.diffusion_type: 0 explicit, 1 Crank-Nicolson, 2 implicit
     SimTime t;
     std::string err;
 
@@ -277,6 +278,8 @@ struct Sim {
     Arr umac, vmac, wmac;
     int mac_iters = 0, nodal_iters = 0;
     double mac_res0 = 0, mac_res = 0, nodal_res0 = 0, nodal_res = 0;
+    int diff_iters = 0;
+    double diff_res0 = 0, diff_res = 0;
 
     void setup(const std::string& text);
     void init_fields();
@@ -299,6 +302,7 @@ struct Sim {
     void mol_conv(Arr& v, Arr& out);
     void mol_predictor(bool incremental);
     void mol_corrector();
+    void diffuse_solve(double dtd);
     void init_data();
     int step_once();
     double ke() const;
@@ -345,7 +349,10 @@ void Sim::setup(const std::string& text) {
         if (gt != "ppm") throw Error(ERR_UNSUPPORTED, "only incflo.godunov_type = ppm");
         if (D.i("incflo.godunov_use_forces_in_trans", 0) != 0) throw Error(ERR_UNSUPPORTED, "forces_in_trans");
     }
-    if (D.i("incflo.diffusion_type", 1) != 0) throw Error(ERR_UNSUPPORTED, "only incflo.diffusion_type = 0");
+    // src/setup/init.cpp:60-76 (the default is Crank-Nicolson)
+    diff_type = D.i("incflo.diffusion_type", 1);
+    if (diff_type < 0 || diff_type > 2)
+        throw Error(ERR_DECK, "We currently require diffusion_type = 0 for explicit, 1 for Crank-Nicolson or 2 for implicit");
     if (D.i("incflo.icns_conserv", 1) != 1) throw Error(ERR_UNSUPPORTED, "icns_conserv = 0");
     do_initial_proj = D.i("incflo.do_initial_proj", 1);
     initial_iterations = D.i("incflo.initial_iterations", 3);
@@ -394,6 +401,8 @@ void Sim::setup(const std::string& text) {
     };
     rd(mac, "mac_proj");
     rd(nod, "nodal_proj");
+    rd(dif, "diffusion");  // MLMGOptions(default prefix, custom prefix), MLMGOptions.cpp:8-13
+    rd(dif, "velocity_diffusion");
 
     t.stop_time = D.d("time.stop_time", -1);
     t.max_step = D.i("time.max_step", -1);
@@ -1628,6 +1637,7 @@ void Sim::compute_dt() {
                 diff = std::max(diff, mueff(i, j, k) * dxinv2 / rho);
             }
     if (!t.use_force_cfl) frc = 0;
+    if (diff_type != 0) diff = 0;  // incflo_compute_dt.cpp:37,140-145,211-214: explicit diffusion only
     t.set_current_cfl(conv, diff, frc);
 }
 
@@ -1765,13 +1775,19 @@ void Sim::apply_predictor(bool incremental) {
     // compute_source_term(NPH) reproduces src (Old velocity, same gp);
     // compute_diffusion_term(Old) reproduces divtau.
     compute_sources(vel_old);
-    // predictor_rhs (CompRHSOps.H:32-141), Explicit factor 1
+    // predictor_rhs (CompRHSOps.H:32-141): diffusion factor 1 explicit, 1/2 Crank-Nicolson, 0 implicit
+    const double fac = diff_type == 0 ? 1.0 : (diff_type == 1 ? 0.5 : 0.0);
     for (int n = 0; n < 3; ++n)
 #pragma omp parallel for collapse(2)
         for (int k = 0; k < nz; ++k)
             for (int j = 0; j < ny; ++j)
                 for (int i = 0; i < nx; ++i)
-                    vel(i, j, k, n) = (rho * vel_old(i, j, k, n) + dt * (conv(i, j, k, n) + src(i, j, k, n) + divtau(i, j, k, n))) / rho;
+                    vel(i, j, k, n) = (rho * vel_old(i, j, k, n) + dt * (conv(i, j, k, n) + src(i, j, k, n) + fac * divtau(i, j, k, n))) / rho;
+    if (diff_type != 0) {  // icns().solve(dt_diff), incflo_advance.cpp:376-386
+        diffuse_solve(diff_type == 2 ? dt : 0.5 * dt);
+        nodal_project(t.newt, dt, incremental);
+        return;
+    }
     // explicit RK2 correction (incflo_advance.cpp:388-400, CompRHSOps.H:267-300)
     divtau_op(vel, divtau_new);
     for (int n = 0; n < 3; ++n)
@@ -1914,12 +1930,15 @@ void Sim::mol_predictor(bool incremental) {
     mac_project();
     mol_conv(vel_old, conv_old);
     compute_sources(vel_old);
+    const double fac = diff_type == 0 ? 1.0 : (diff_type == 1 ? 0.5 : 0.0);
     for (int n = 0; n < 3; ++n)
 #pragma omp parallel for collapse(2)
         for (int k = 0; k < nz; ++k)
             for (int j = 0; j < ny; ++j)
                 for (int i = 0; i < nx; ++i)
-                    vel(i, j, k, n) = (rho * vel_old(i, j, k, n) + dt * (conv_old(i, j, k, n) + src(i, j, k, n) + divtau(i, j, k, n))) / rho;
+                    vel(i, j, k, n) =
+                        (rho * vel_old(i, j, k, n) + dt * (conv_old(i, j, k, n) + src(i, j, k, n) + fac * divtau(i, j, k, n))) / rho;
+    if (diff_type != 0) diffuse_solve(diff_type == 2 ? dt : 0.5 * dt);
     nodal_project(t.newt, dt, incremental);
 }
 
@@ -1936,6 +1955,21 @@ void Sim::mol_corrector() {
     mac_project();
     mol_conv(vel, conv);
     update_mueff(vel);
+    if (diff_type != 0) {  // corrector_rhs with ofac 1/2 (Crank-Nicolson) or 0 (implicit), nfac 0, then the solve
+        compute_sources(vel);
+        const double ofac = diff_type == 1 ? 0.5 : 0.0;
+        for (int n = 0; n < 3; ++n)
+#pragma omp parallel for collapse(2)
+            for (int k = 0; k < nz; ++k)
+                for (int j = 0; j < ny; ++j)
+                    for (int i = 0; i < nx; ++i)
+                        vel(i, j, k, n) = (rho * vel_old(i, j, k, n) +
+                                           dt * (0.5 * (conv_old(i, j, k, n) + conv(i, j, k, n)) + ofac * divtau(i, j, k, n) + src(i, j, k, n))) /
+                                          rho;
+        diffuse_solve(diff_type == 2 ? dt : 0.5 * dt);
+        nodal_project(t.newt, dt, false);
+        return;
+    }
     divtau_op(vel, divtau_new);
     compute_sources(vel);
     for (int n = 0; n < 3; ++n)
@@ -1948,6 +1982,79 @@ void Sim::mol_corrector() {
                                              0.5 * divtau_new(i, j, k, n) + src(i, j, k, n))) /
                                       rho;
     nodal_project(t.newt, dt, false);
+}
+
+// ---- implicit / Crank-Nicolson tensor diffusion solve -------------------------------------
+// DiffSolverIface::linsys_solve (src/equation_systems/DiffusionOps.cpp:114-159):
+// MLTensorOp with alpha 1, a = rho, beta = dtd and the face viscosity of the
+// current mu_eff: rho u - dtd divtau(u) = rho u_rhs, u_rhs the current velocity
+// (also the initial guess), divtau the operator of divtau_op with its wall-model
+// data (Old velocity, current mu_eff).  MLMG stops when the max-norm residual
+// is below max(atol, rtol * initial residual) (MLMGOptions defaults, prefixes
+// diffusion and velocity_diffusion).  The oracle reaches that point by Jacobi
+// iterations, a different solver from the CUDA path's, so that parity
+// checks the discrete solution rather than a shared iteration.
+void Sim::diffuse_solve(double dtd) {
+    const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+    Arr b, L, R, Dg;
+    def_cc(b, g, 0, 3);
+    def_cc(L, g, 0, 3);
+    def_cc(R, g, 0, 3);
+    def_cc(Dg, g, 0, 3);
+    Arr m;
+    def_cc(m, g, 1, 1);
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) m(i, j, k) = mueff(i, j, k);
+    fill_cc_foextrap(m);
+    const double ih2[3] = {1.0 / (g.dx[0] * g.dx[0]), 1.0 / (g.dx[1] * g.dx[1]), 1.0 / (g.dx[2] * g.dx[2])};
+    // diagonal of rho - dtd divtau: the normal-derivative coefficient of the
+    // own component is 4/3 along its own direction and 1 across; at a z wall the
+    // normal component's face gradient is 2 q0 / dz and the tangential ones' is fixed
+    for (int n = 0; n < 3; ++n)
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) {
+                    const double c0 = m(i, j, k);
+                    double s = 0;
+                    const double cx = n == 0 ? 4.0 / 3.0 : 1.0, cy = n == 1 ? 4.0 / 3.0 : 1.0, cz = n == 2 ? 4.0 / 3.0 : 1.0;
+                    s += cx * (0.5 * (m(i - 1, j, k) + c0) + 0.5 * (m(i + 1, j, k) + c0)) * ih2[0];
+                    s += cy * (0.5 * (m(i, j - 1, k) + c0) + 0.5 * (m(i, j + 1, k) + c0)) * ih2[1];
+                    const double wall_w = n == 2 ? 2.0 : 0.0;
+                    const double zlo = (!g.per[2] && k == 0) ? wall_w * c0 : 0.5 * (m(i, j, k - 1) + c0);
+                    const double zhi = (!g.per[2] && k == nz - 1) ? wall_w * c0 : 0.5 * (m(i, j, k + 1) + c0);
+                    s += cz * (zlo + zhi) * ih2[2];
+                    Dg(i, j, k, n) = rho + dtd * s;
+                    b(i, j, k, n) = rho * vel(i, j, k, n);
+                }
+    auto residual = [&]() {
+        divtau_op(vel, L);
+        double rn = 0;
+        for (int n = 0; n < 3; ++n)
+            for (int k = 0; k < nz; ++k)
+                for (int j = 0; j < ny; ++j)
+                    for (int i = 0; i < nx; ++i) {
+                        const double r = b(i, j, k, n) - rho * vel(i, j, k, n) + dtd * L(i, j, k, n);
+                        R(i, j, k, n) = r;
+                        rn = std::max(rn, std::fabs(r));
+                    }
+        if (!std::isfinite(rn)) throw Error(ERR_NONFINITE, "diffusion solve diverged");
+        return rn;
+    };
+    double rn = residual();
+    diff_res0 = rn;
+    const double target = std::max(dif.atol, dif.rtol * rn);
+    int it = 0;
+    while (rn > target) {
+        if (++it > 200000) throw Error(ERR_NOT_CONVERGED, "oracle Jacobi iterations of the diffusion solve did not converge");
+        for (int n = 0; n < 3; ++n)
+            for (int k = 0; k < nz; ++k)
+                for (int j = 0; j < ny; ++j)
+                    for (int i = 0; i < nx; ++i) vel(i, j, k, n) += R(i, j, k, n) / Dg(i, j, k, n);
+        rn = residual();
+    }
+    diff_iters = it;
+    diff_res = rn;
 }
 
 // ---- InitData (src/setup/init.cpp:104-225) -------------------------------------------------------
@@ -2159,6 +2266,9 @@ double kso_get_scalar(void* h, const char* name) {
     if (n == "mac_res") return s.mac_res;
     if (n == "nodal_res0") return s.nodal_res0;
     if (n == "nodal_res") return s.nodal_res;
+    if (n == "diff_iters") return s.diff_iters;
+    if (n == "diff_res0") return s.diff_res0;
+    if (n == "diff_res") return s.diff_res;
     if (n == "utau") return s.utau;
     if (n == "ke") return s.ke();
     if (n == "cfl") return s.t.cur_cfl;

@@ -72,7 +72,7 @@ def test_deck_checks(oracle_mod):
         oracle_mod.Oracle(decks.mol(decks.tgv(16, cfl=0.5)).replace("time.cfl = 0.5", "time.cfl = 0.6"))
     assert e.value.code == 1 and "0.5" in str(e.value)
     with pytest.raises(oracle_mod.OracleError):
-        oracle_mod.Oracle(decks.mol(decks.tgv(16, cfl=0.45)).replace("incflo.diffusion_type = 0", "incflo.diffusion_type = 1"))
+        oracle_mod.Oracle(decks.mol(decks.tgv(16, cfl=0.45)).replace("incflo.diffusion_type = 0", "incflo.diffusion_type = 3"))
     o = oracle_mod.Oracle(decks.tgv(16, cfl=0.45))
     with pytest.raises(oracle_mod.OracleError):
         o.ApplyCorrector()
