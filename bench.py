@@ -52,7 +52,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision form of the same workload")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost / gradient check (128x128x64, 3 disks)")
-    p.add_argument("--no-mol", action="store_true", help="skip the MOL predictor-corrector form of the ABL workload")
+    p.add_argument("--no-mol", action="store_true", help="skip the MOL and Crank-Nicolson forms of the ABL workload")
     p.add_argument("--c4", action="store_true",
                    help="only the production forward + adjoint run: 512x512x256 ABL, 16 disks, mixed forward, FP64 adjoint")
     p.add_argument("--c4-steps", type=int, default=200)
@@ -306,6 +306,7 @@ def our_arm(args, rank, world, local_rank):
                  "mac_residual_rel_max": max(mres), "nodal_residual_rel_max": max(nres),
                  "note": "FP32 advection and multigrid cycles, FP64 residuals / defect correction / RHS / velocity update"}
     mol = None if args.no_mol else mol_bench(args, torch, ks, decks, nx, ny, nz, world, rank)
+    cn = None if args.no_mol else cn_bench(args, torch, ks, decks, nx, ny, nz, world, rank)
     adj = None if args.no_adjoint else adjoint_bench(args, torch, ks, decks)
     # the reference's own CPU-runnable case: Taylor-Green vortex 64^3, Re 1600, CFL 0.5, 20 steps
     tg = ks.Incflo(decks.tgv(64, steps=10 ** 6))
@@ -324,15 +325,13 @@ def our_arm(args, rank, world, local_rank):
            "unit": UNIT, "ms_per_step": tms}
     del tg
     return dict(value=value, ms=ms_max, cells=cells, launches=launches, dominant=dominant, dom=dom, clocks=clk, e2e=e2e, fp64_peak=fp64_peak,
-                mac=statistics.mean(mac_it), nodal=statistics.mean(nod_it), size=(nx, ny, nz), mixed=mixed, adjoint=adj, tgv=tgv, mol=mol)
+                mac=statistics.mean(mac_it), nodal=statistics.mean(nod_it), size=(nx, ny, nz), mixed=mixed, adjoint=adj, tgv=tgv, mol=mol, cn=cn)
 
 
-def mol_bench(args, torch, ks, decks, nx, ny, nz, world, rank):
-    """The same ABL workload advanced with the MOL predictor-corrector
-    (incflo.use_godunov = false, explicit diffusion) at CFL 0.45 (MOL requires
-    <= 0.5): two MAC and two nodal projections per step.  Device time of
-    --steps steps after --warmup, FP64."""
-    sim = ks.Incflo(decks.mol(decks.abl(nx, ny, nz, steps=10 ** 9, cfl=0.45)))
+def variant_bench(args, torch, ks, deck, workload, world, rank, label):
+    """Another form of the ABL workload (scheme or diffusion treatment): device
+    time of --steps steps after --warmup, FP64, with the per-step V-cycle counts."""
+    sim = ks.Incflo(deck)
     sim.InitData()
     cells = sim.scalar("ncells")
     for w in range(args.warmup):
@@ -342,29 +341,49 @@ def mol_bench(args, torch, ks, decks, nx, ny, nz, world, rank):
     if args.profile_all and rank == 0:
         rep = sim.profile_report()
         tot = sum(v[1] for v in rep.values())
-        sys.stderr.write("-- MOL step --\n")
+        sys.stderr.write("-- %s step --\n" % label)
         for k, v in sorted(rep.items(), key=lambda kv: -kv[1][1]):
             sys.stderr.write("%-22s %6d launches %9.3f ms %5.1f%% %8.1f GB/s\n" % (k, v[0], v[1], 100 * v[1] / tot,
                                                                                   v[2] / (v[1] * 1e-3) / 1e9 if v[1] else 0))
     sim.profile_kernels("")
     stream = torch.cuda.ExternalStream(sim.stream())
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    mac_it, nod_it = [], []
+    mac_it, nod_it, dif_it = [], [], []
     torch.cuda.synchronize()
     ev0.record(stream)
     for _ in range(args.steps):
         sim.step()
         mac_it.append(sim.scalar("mac_iters"))
         nod_it.append(sim.scalar("nodal_iters"))
+        dif_it.append(sim.scalar("diff_iters"))
     ev1.record(stream)
     torch.cuda.synchronize()
     ms = max_over_ranks(ev0.elapsed_time(ev1), world)
-    out = {"workload": "ABL %dx%dx%d, MOL predictor-corrector, explicit diffusion, CFL 0.45, FP64" % (nx, ny, nz),
-           "value": replica_throughput(cells, args.steps, world, ms * 1e-3), "unit": UNIT, "ms_per_step": ms / args.steps,
-           "dt": sim.scalar("dt"), "mac_vcycles_per_step": statistics.mean(mac_it), "nodal_vcycles_per_step": statistics.mean(nod_it),
-           "projections_per_step": {"mac": 2, "nodal": 2}}
+    out = {"workload": workload, "value": replica_throughput(cells, args.steps, world, ms * 1e-3), "unit": UNIT,
+           "ms_per_step": ms / args.steps, "dt": sim.scalar("dt"), "mac_vcycles_per_step": statistics.mean(mac_it),
+           "nodal_vcycles_per_step": statistics.mean(nod_it), "diffusion_vcycles_per_solve": statistics.mean(dif_it)}
     del sim
     return out
+
+
+def mol_bench(args, torch, ks, decks, nx, ny, nz, world, rank):
+    """The ABL workload advanced with the MOL predictor-corrector
+    (incflo.use_godunov = false, explicit diffusion) at CFL 0.45 (MOL requires
+    <= 0.5): two MAC and two nodal projections per step."""
+    out = variant_bench(args, torch, ks, decks.mol(decks.abl(nx, ny, nz, steps=10 ** 9, cfl=0.45)),
+                        "ABL %dx%dx%d, MOL predictor-corrector, explicit diffusion, CFL 0.45, FP64" % (nx, ny, nz), world, rank, "MOL")
+    out["projections_per_step"] = {"mac": 2, "nodal": 2}
+    return out
+
+
+def cn_bench(args, torch, ks, decks, nx, ny, nz, world, rank):
+    """The ABL workload with the reference's default diffusion treatment,
+    Crank-Nicolson (incflo.diffusion_type = 1): predictor_rhs with half the old
+    diffusion term and a multigrid solve of rho u - dt/2 divtau(u) per step; no
+    diffusion CFL."""
+    d = decks.abl(nx, ny, nz, steps=10 ** 9).replace("incflo.diffusion_type = 0", "incflo.diffusion_type = 1")
+    return variant_bench(args, torch, ks, d, "ABL %dx%dx%d, Godunov, Crank-Nicolson diffusion, CFL 0.9, FP64" % (nx, ny, nz), world, rank,
+                         "Crank-Nicolson")
 
 
 def adjoint_bench(args, torch, ks, decks):
@@ -621,7 +640,7 @@ def main():
                          "launches": n_l, "avg_launch_us": 1e3 * ms_l / n_l if n_l else None,
                          "algorithmic_bytes_per_launch": by_l / n_l if n_l else None},
             "gpu_launches": r["launches"], "clocks": r["clocks"], "e2e": r["e2e"], "mixed_precision": r["mixed"],
-            "adjoint": r["adjoint"], "tgv64": r["tgv"], "mol": r["mol"]}
+            "adjoint": r["adjoint"], "tgv64": r["tgv"], "mol": r["mol"], "crank_nicolson": r["cn"]}
     # The FP64 path is bound by FP64 issue on this GPU (profiles/k_nd_col_abl256_fp64.md): report the
     # dominant kernel against the FMA peak measured live by ks_fma_peak as well.
     fl = FP64_FLOPS_PER_BYTE.get(r["dominant"])

@@ -725,16 +725,22 @@ void Sim::nd_solve(double sigma) {
 // rho u - dtd divtau(u) = rho u_rhs (DiffSolverIface::linsys_solve,
 // src/equation_systems/DiffusionOps.cpp:114-159: MLTensorOp, alpha 1, a = rho,
 // beta = dtd, face viscosity of the current mu_eff, wall-model data from the Old
-// velocity), u_rhs the current velocity and initial guess.  Geometric
-// multigrid on the MAC hierarchy's levels: V-cycles of weighted-Jacobi sweeps
-// of the full tensor operator (each sweep one tiled divtau pass with the
-// update fused), 8-cell averaging restriction, piecewise-constant
-// prolongation, viscosity averaged to the coarse cells, homogeneous boundary
-// data below the finest level.  The first sweep of every cycle also returns
-// the max-norm residual of the incoming iterate; the solve stops as MLMG does,
-// at max(atol, rtol * initial residual) or maxiter cycles.
-constexpr double kDiffOmega = 0.8;  // Jacobi weight: D^-1 A has its spectrum in (0, 2)
-constexpr int kDiffBottom = 24;     // sweeps on the coarsest level
+// velocity), u_rhs the current velocity and initial guess.  The stopping test
+// is MLMG's: max-norm residual <= max(atol, rtol * max(|rhs|, initial
+// residual)), or maxiter iterations.
+//
+// Every iteration is built from weighted-Jacobi sweeps of the full tensor
+// operator, each one tiled divtau pass with the update fused in; the first
+// sweep of an iteration also returns the max-norm residual of the incoming
+// iterate.  With s = max(1 - rho / D) over the rows (D the diagonal), the
+// eigenvalues of D^-1 A lie in [1 - s, 1 + s], so an unweighted sweep
+// contracts the error by s.  When s < 0.1 (every LES and laminar case whose
+// diffusion number dt nu / h^2 is small) an iteration is that one sweep.
+// Otherwise it is a V-cycle on the MAC hierarchy's levels: weight 0.8 where
+// s_l >= 0.5 (smoothing of the 1 + s end), 1 below, 8-cell averaging
+// restriction, piecewise-constant prolongation, viscosity averaged to the
+// coarse cells and homogeneous boundary data below the finest level.
+constexpr int kDiffBottom = 24;  // sweeps on the coarsest level
 
 void Sim::diff_alloc() {
     if (!dl_.empty()) return;
@@ -745,7 +751,7 @@ void Sim::diff_alloc() {
     }
     dbuf_.alloc(tot);
     dtmp_.alloc(3 * (size_t)g_.N);
-    dparts_.alloc((size_t)divtau_tile_blocks(g_));
+    dparts_.alloc((size_t)std::max(divtau_tile_blocks(g_), 2 * diff_cell_blocks(g_)));
     double* q = dbuf_.p;
     for (size_t l = 0; l < cc_.size(); ++l) {
         DiffLevel L{};
@@ -783,7 +789,7 @@ void Sim::diff_alloc() {
 void Sim::diff_vcycle(size_t l, double dtd) {
     DiffLevel& L = dl_[l];
     auto sweep = [&]() {
-        launch_divtau_jacobi(ctx_, L.g, L.x, L.mu, nullptr, L.b, L.dinv, L.t, rho_, dtd, kDiffOmega, nullptr);
+        launch_divtau_jacobi(ctx_, L.g, L.x, L.mu, nullptr, L.b, L.dinv, L.t, rho_, dtd, L.omega, nullptr);
         std::swap(L.x, L.t);
     };
     if (l + 1 == dl_.size()) {
@@ -802,55 +808,60 @@ void Sim::diff_vcycle(size_t l, double dtd) {
 
 void Sim::diffuse_solve(double dtd) {
     diff_alloc();
-    const long long N3 = 3 * g_.N;
     DiffLevel& L0 = dl_[0];
     L0.mu = mueff_.p;
-    launch_scale(ctx_, vel_tmp_.p, vel_.p, rho_, N3);  // b = rho u_rhs
-    launch_diff_dinv(ctx_, g_, mueff_.p, rho_, dtd, L0.dinv);
-    for (size_t l = 1; l < dl_.size(); ++l) {
-        launch_avg8(ctx_, dl_[l - 1].g, dl_[l].g, dl_[l - 1].mu, dl_[l].mu, 1);
-        launch_diff_dinv(ctx_, dl_[l].g, dl_[l].mu, rho_, dtd, dl_[l].dinv);
-    }
+    const int nc = diff_cell_blocks(g_);
+    launch_rhs_b(ctx_, g_, vel_.p, rho_, vel_tmp_.p, dparts_.p);  // b = rho u_rhs, |b| maxima
+    launch_diff_dinv(ctx_, g_, mueff_.p, rho_, dtd, L0.dinv, dparts_.p + nc);
+    launch_reduce(ctx_, dparts_.p, nc, 2, 1, red_.p);
+    ck(cudaMemcpyAsync(hred_, red_.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx_.stream), "D2H");
+    sync();
+    const double bnorm = hred_[0], s0 = hred_[1];
+    if (!std::isfinite(bnorm) || !std::isfinite(s0)) throw KsError(KS_ERR_NONFINITE, "non-finite diffusion right-hand side or coefficients");
+    const bool cycles = s0 >= 0.1 && dl_.size() > 1;
+    for (size_t l = 0; l < dl_.size(); ++l) dl_[l].omega = s0 / (double)(1u << (2 * l)) < 0.5 ? 1.0 : 0.8;
+    if (cycles)
+        for (size_t l = 1; l < dl_.size(); ++l) {
+            launch_avg8(ctx_, dl_[l - 1].g, dl_[l].g, dl_[l - 1].mu, dl_[l].mu, 1);
+            launch_diff_dinv(ctx_, dl_[l].g, dl_[l].mu, rho_, dtd, dl_[l].dinv, nullptr);
+        }
+    auto sweep0 = [&](double* parts) {
+        launch_divtau_jacobi(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, L0.dinv, dtmp_.p, rho_, dtd, L0.omega, parts);
+        std::swap(vel_.p, dtmp_.p);
+    };
     const int np = divtau_tile_blocks(g_);
     int it = 0;
     double r0 = 0.0, rn = 0.0, target = 0.0;
     while (true) {
-        launch_divtau_jacobi(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, L0.dinv, dtmp_.p, rho_, dtd, kDiffOmega, dparts_.p);
-        std::swap(vel_.p, dtmp_.p);
+        sweep0(dparts_.p);
         launch_reduce(ctx_, dparts_.p, np, 1, 1, red_.p);
         ck(cudaMemcpyAsync(hred_, red_.p, sizeof(double), cudaMemcpyDeviceToHost, ctx_.stream), "D2H");
         sync();
         rn = hred_[0];
         if (it == 0) {
             r0 = rn;
-            target = std::max(dif_.atol, dif_.rtol * r0);
+            target = std::max(dif_.atol, dif_.rtol * std::max(bnorm, r0));
         }
         if (!std::isfinite(rn)) throw KsError(KS_ERR_NONFINITE, "diffusion solve diverged");
-        if (rn > 1e20 * r0) throw KsError(KS_ERR_NOT_CONVERGED, "diffusion solve diverged (residual above 1e20 times the initial one)");
+        if (rn > 1e20 * std::max(r0, 1e-300)) throw KsError(KS_ERR_NOT_CONVERGED, "diffusion solve diverged (residual above 1e20 times the initial one)");
         if (rn <= target || it >= dif_.maxiter) break;
         ++it;
+        if (!cycles) continue;
         // the rest of a V-cycle on the finest level (its first sweep is the one above)
-        for (int s = 1; s < dif_.nu1; ++s) {
-            launch_divtau_jacobi(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, L0.dinv, dtmp_.p, rho_, dtd, kDiffOmega, nullptr);
-            std::swap(vel_.p, dtmp_.p);
-        }
-        if (dl_.size() > 1) {
-            launch_divtau_jacobi(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, nullptr, L0.r, rho_, dtd, 0.0, nullptr);
-            DiffLevel& C = dl_[1];
-            launch_avg8(ctx_, g_, C.g, L0.r, C.b, 3);
-            launch_fill(ctx_, C.x, 0.0, 3 * C.g.N);
-            diff_vcycle(1, dtd);
-            launch_prolong_add(ctx_, g_, C.g, C.x, vel_.p);
-        }
-        for (int s = 0; s < dif_.nu2; ++s) {
-            launch_divtau_jacobi(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, L0.dinv, dtmp_.p, rho_, dtd, kDiffOmega, nullptr);
-            std::swap(vel_.p, dtmp_.p);
-        }
+        for (int s = 1; s < dif_.nu1; ++s) sweep0(nullptr);
+        launch_divtau_jacobi(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, nullptr, L0.r, rho_, dtd, 0.0, nullptr);
+        DiffLevel& C = dl_[1];
+        launch_avg8(ctx_, g_, C.g, L0.r, C.b, 3);
+        launch_fill(ctx_, C.x, 0.0, 3 * C.g.N);
+        diff_vcycle(1, dtd);
+        launch_prolong_add(ctx_, g_, C.g, C.x, vel_.p);
+        for (int s = 0; s < dif_.nu2; ++s) sweep0(nullptr);
     }
-    if (rn > target && !dif_.fixed_iters) throw KsError(KS_ERR_NOT_CONVERGED, "diffusion solve did not converge in diffusion.maxiter V-cycles");
+    if (rn > target && !dif_.fixed_iters) throw KsError(KS_ERR_NOT_CONVERGED, "diffusion solve did not converge in diffusion.maxiter iterations");
     dif_it_ = it;
     dif_r0_ = r0;
     dif_r_ = rn;
+    dif_b_ = bnorm;
 }
 
 void Sim::apply_projection(double time, double scaling, bool incremental) {
@@ -1082,6 +1093,7 @@ double Sim::scalar(const std::string& n) {
     if (n == "diff_iters") return dif_it_;
     if (n == "diff_res0") return dif_r0_;
     if (n == "diff_res") return dif_r_;
+    if (n == "diff_rhs_norm") return dif_b_;
     if (n == "mac_res0") return mac_r0_;
     if (n == "mac_res") return mac_r_;
     if (n == "nodal_res0") return nod_r0_;

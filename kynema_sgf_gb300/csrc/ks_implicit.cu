@@ -13,14 +13,30 @@ namespace {
 
 constexpr int BS = 256;
 
+// block maximum (NaN-propagating) written by thread 0 to out
+__device__ inline void block_max_to(double v, double* out) {
+    __shared__ double w[BS / 32];
+    for (int o = 16; o > 0; o >>= 1) v = nmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) w[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = w[0];
+        for (int k = 1; k < BS / 32; ++k) m = nmax(m, w[k]);
+        *out = m;
+    }
+}
+
 // Diagonal of rho - dtd divtau: the own component's normal-derivative
 // coefficient is 4/3 along its own direction and 1 across, times the face
 // viscosity (mean of the two cells, the cell value on a z wall).  On a z wall
 // the normal component's face gradient is 2 q0 / dz (odd reflection) and the
 // tangential components' is fixed (Neumann data), so they carry weight 2 and 0.
-__global__ void k_diff_dinv(Grid g, const double* mu, double rho, double dtd, double* dinv) {
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (t >= g.N) return;
+// Also the block maxima of s = 1 - rho / D (off-diagonal weight of a row: the
+// Jacobi iteration contracts by about s per sweep).
+__global__ void k_diff_dinv(Grid g, const double* mu, double rho, double dtd, double* dinv, double* parts) {
+    const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const bool live = t0 < g.N;
+    const long long t = live ? t0 : 0;
     const int i = (int)(t % g.nx);
     const long long r = t / g.nx;
     const int j = (int)(r % g.ny), k = (int)(r / g.ny);
@@ -31,12 +47,16 @@ __global__ void k_diff_dinv(Grid g, const double* mu, double rho, double dtd, do
     const double zlo = wlo ? c0 : 0.5 * (mu[cidx(g, i, j, g.zper ? wrapn(k - 1, g.nz) : k - 1)] + c0);
     const double zhi = whi ? c0 : 0.5 * (mu[cidx(g, i, j, g.zper ? wrapn(k + 1, g.nz) : k + 1)] + c0);
     const double ix2 = g.idx * g.idx, iy2 = g.idy * g.idy, iz2 = g.idz * g.idz;
-    for (int n = 0; n < 3; ++n) {
+    double smax = 0.0;
+    for (int n = 0; n < 3 && live; ++n) {
         const double w = n == 2 ? 2.0 : 0.0;
         const double sz = (wlo ? w * zlo : zlo) + (whi ? w * zhi : zhi);
         const double s = (n == 0 ? 4.0 / 3.0 : 1.0) * mx * ix2 + (n == 1 ? 4.0 / 3.0 : 1.0) * my * iy2 + (n == 2 ? 4.0 / 3.0 : 1.0) * sz * iz2;
-        dinv[n * g.N + t] = 1.0 / (rho + dtd * s);
+        const double d = 1.0 / (rho + dtd * s);
+        dinv[n * g.N + t] = d;
+        smax = nmax(smax, 1.0 - rho * d);
     }
+    if (parts) block_max_to(smax, parts + blockIdx.x);
 }
 
 __global__ void k_avg8(Grid f, Grid c, const double* fv, double* cv, int ncomp) {
@@ -65,15 +85,24 @@ __global__ void k_prolong_add(Grid f, Grid c, const double* cv, double* fv) {
     for (int n = 0; n < 3; ++n) fv[n * f.N + t] += cv[n * c.N + p];
 }
 
-__global__ void k_scale(double* out, const double* in, double a, long long n) {
+// b = rho u (3 components) with the block maxima of |b|
+__global__ void k_rhs_b(Grid g, const double* u, double rho, double* b, double* parts) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (t < n) out[t] = a * in[t];
+    double m = 0.0;
+    if (t < g.N)
+        for (int n = 0; n < 3; ++n) {
+            const double v = rho * u[n * g.N + t];
+            b[n * g.N + t] = v;
+            m = nmax(m, fabs(v));
+        }
+    block_max_to(m, parts + blockIdx.x);
 }
 
 }  // namespace
 
-void launch_diff_dinv(Ctx& c, const Grid& g, const double* mueff, double rho, double dtd, double* dinv) {
-    KS_LAUNCH(c, k_diff_dinv, nblocks(g.N, BS), BS, 8.0 * 4.0 * g.N, g, mueff, rho, dtd, dinv);
+int diff_cell_blocks(const Grid& g) { return (int)nblocks(g.N, BS); }
+void launch_diff_dinv(Ctx& c, const Grid& g, const double* mueff, double rho, double dtd, double* dinv, double* parts) {
+    KS_LAUNCH(c, k_diff_dinv, nblocks(g.N, BS), BS, 8.0 * 4.0 * g.N, g, mueff, rho, dtd, dinv, parts);
 }
 void launch_avg8(Ctx& c, const Grid& fine, const Grid& coarse, const double* f, double* cr, int ncomp) {
     KS_LAUNCH(c, k_avg8, nblocks(coarse.N, BS), BS, 8.0 * ncomp * (fine.N + coarse.N), fine, coarse, f, cr, ncomp);
@@ -81,8 +110,8 @@ void launch_avg8(Ctx& c, const Grid& fine, const Grid& coarse, const double* f, 
 void launch_prolong_add(Ctx& c, const Grid& fine, const Grid& coarse, const double* cr, double* f) {
     KS_LAUNCH(c, k_prolong_add, nblocks(fine.N, BS), BS, 8.0 * 3.0 * (2.0 * fine.N + coarse.N), fine, coarse, cr, f);
 }
-void launch_scale(Ctx& c, double* out, const double* in, double a, long long n) {
-    KS_LAUNCH(c, k_scale, nblocks(n, BS), BS, 16.0 * n, out, in, a, n);
+void launch_rhs_b(Ctx& c, const Grid& g, const double* u, double rho, double* b, double* parts) {
+    KS_LAUNCH(c, k_rhs_b, nblocks(g.N, BS), BS, 8.0 * 6.0 * g.N, g, u, rho, b, parts);
 }
 
 }  // namespace ks

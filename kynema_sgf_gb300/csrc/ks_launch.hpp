@@ -196,13 +196,16 @@ void launch_mol_advection(Ctx& c, const Grid& g, const double* vel, const double
                           double* vel_out, double dt, double fac);
 
 // ---- implicit / Crank-Nicolson tensor diffusion solve (ks_implicit.cu)
-// 1 / diagonal of rho - dtd divtau per cell and component (3 N_g values)
-void launch_diff_dinv(Ctx& c, const Grid& g, const double* mueff, double rho, double dtd, double* dinv);
+// 1 / diagonal of rho - dtd divtau per cell and component (3 N_g values); parts, when
+// set, receives diff_cell_blocks(g) block maxima of 1 - rho / diagonal
+int diff_cell_blocks(const Grid& g);
+void launch_diff_dinv(Ctx& c, const Grid& g, const double* mueff, double rho, double dtd, double* dinv, double* parts);
 // coarse = mean of the 8 fine cells below each coarse cell, ncomp components
 void launch_avg8(Ctx& c, const Grid& fine, const Grid& coarse, const double* f, double* cr, int ncomp);
 // fine += coarse value of the parent cell (piecewise-constant prolongation), 3 components
 void launch_prolong_add(Ctx& c, const Grid& fine, const Grid& coarse, const double* cr, double* f);
-void launch_scale(Ctx& c, double* out, const double* in, double a, long long n);
+// b = rho u with diff_cell_blocks(g) block maxima of |b| in parts
+void launch_rhs_b(Ctx& c, const Grid& g, const double* u, double rho, double* b, double* parts);
 
 // ---- reverse mode of the Godunov passes (ks_adjoint.cu), FP64, periodic.
 // Adjoints of the GodunovBufs arrays (same shapes) plus those of the MAC

@@ -258,7 +258,7 @@ class Sim {
     Grid g_{};
     Clock t_;
     int mac_it_ = 0, nod_it_ = 0, dif_it_ = 0;
-    double dif_r0_ = 0, dif_r_ = 0;
+    double dif_r0_ = 0, dif_r_ = 0, dif_b_ = 0;
     int mixed_ = 0;  // 1: FP32 advection and multigrid cycles with FP64 defect correction
     GodunovBufs* adv_bufs_ = nullptr;  // post-MAC pass scratch when not gb_ (reverse-step recompute keeps both passes)
     double mac_r0_ = 0, mac_r_ = 0, nod_r0_ = 0, nod_r_ = 0;
@@ -316,6 +316,7 @@ class Sim {
     struct DiffLevel {
         Grid g;
         double *x, *b, *r, *t, *mu, *dinv;
+        double omega;  // Jacobi weight of the level's sweeps
     };
     std::vector<DiffLevel> dl_;
     DevBuf<double> dbuf_, dtmp_, dparts_;

@@ -279,7 +279,7 @@ struct Sim {
     int mac_iters = 0, nodal_iters = 0;
     double mac_res0 = 0, mac_res = 0, nodal_res0 = 0, nodal_res = 0;
     int diff_iters = 0;
-    double diff_res0 = 0, diff_res = 0;
+    double diff_res0 = 0, diff_res = 0, diff_bnorm = 0;
 
     void setup(const std::string& text);
     void init_fields();
@@ -1990,8 +1990,8 @@ void Sim::mol_corrector() {
 // current mu_eff: rho u - dtd divtau(u) = rho u_rhs, u_rhs the current velocity
 // (also the initial guess), divtau the operator of divtau_op with its wall-model
 // data (Old velocity, current mu_eff).  MLMG stops when the max-norm residual
-// is below max(atol, rtol * initial residual) (MLMGOptions defaults, prefixes
-// diffusion and velocity_diffusion).  The oracle reaches that point by Jacobi
+// is below max(atol, rtol * max(|rhs|, initial residual)) (MLMGOptions
+// defaults, prefixes diffusion and velocity_diffusion).  The oracle reaches that point by Jacobi
 // iterations, a different solver from the CUDA path's, so that parity
 // checks the discrete solution rather than a shared iteration.
 void Sim::diffuse_solve(double dtd) {
@@ -2043,7 +2043,10 @@ void Sim::diffuse_solve(double dtd) {
     };
     double rn = residual();
     diff_res0 = rn;
-    const double target = std::max(dif.atol, dif.rtol * rn);
+    double bnorm = 0;
+    for (double v : b.d) bnorm = std::max(bnorm, std::fabs(v));
+    // MLMG measures against the larger of |rhs| and the initial residual ("bnorm" / "resid0")
+    const double target = std::max(dif.atol, dif.rtol * std::max(bnorm, rn));
     int it = 0;
     while (rn > target) {
         if (++it > 200000) throw Error(ERR_NOT_CONVERGED, "oracle Jacobi iterations of the diffusion solve did not converge");
@@ -2055,6 +2058,7 @@ void Sim::diffuse_solve(double dtd) {
     }
     diff_iters = it;
     diff_res = rn;
+    diff_bnorm = bnorm;
 }
 
 // ---- InitData (src/setup/init.cpp:104-225) -------------------------------------------------------
@@ -2269,6 +2273,7 @@ double kso_get_scalar(void* h, const char* name) {
     if (n == "diff_iters") return s.diff_iters;
     if (n == "diff_res0") return s.diff_res0;
     if (n == "diff_res") return s.diff_res;
+    if (n == "diff_rhs_norm") return s.diff_bnorm;
     if (n == "utau") return s.utau;
     if (n == "ke") return s.ke();
     if (n == "cfl") return s.t.cur_cfl;

@@ -54,6 +54,8 @@ def test_implicit_parity(cuda_dev, oracle_mod, case):
         d = d.replace("transport.viscosity = 0.000625", "transport.viscosity = 0.3")
     if case.endswith("mol"):
         d = decks.mol(d)
+    # the two sides solve with different iterations; compare them well below the default tolerance
+    d += "diffusion.mg_rtol = 1e-13\n"
     g, o = cuda_dev.Incflo(d), oracle_mod.Oracle(d)
     g.InitData()
     o.InitData()
@@ -62,5 +64,5 @@ def test_implicit_parity(cuda_dev, oracle_mod, case):
         assert g.step() and o.step()
         assert abs(g.scalar("dt") - o.scalar("dt")) <= 1e-12 * o.scalar("dt")
         check(g, o, ["velocity", "p", "gp", "velocity_mueff"])
-        assert g.scalar("diff_res") <= max(2.2e-14, 2.2e-11 * g.scalar("diff_res0"))
+        assert g.scalar("diff_res") <= max(2.2e-14, 1e-13 * max(g.scalar("diff_res0"), g.scalar("diff_rhs_norm")))
         assert 1 <= g.scalar("diff_iters") <= 30
