@@ -29,6 +29,8 @@ namespace ks {
 
 void Sim::adj_check() const {
     if (!godunov_) throw KsError(KS_ERR_UNSUPPORTED, "the reverse mode differentiates the Godunov scheme (incflo.use_godunov = 1)");
+    if (diff_type_ != 0) throw KsError(KS_ERR_UNSUPPORTED, "the reverse mode differentiates explicit diffusion (incflo.diffusion_type = 0)");
+    if (temp_ || S_.bous || S_.ablf) throw KsError(KS_ERR_UNSUPPORTED, "the reverse mode has no temperature, BoussinesqBuoyancy or ABLForcing");
     if (t_.adaptive) throw KsError(KS_ERR_UNSUPPORTED, "the adjoint needs a fixed time step (time.fixed_dt > 0)");
     if (wallmodel_ && shear_ != 0) throw KsError(KS_ERR_UNSUPPORTED, "the adjoint's wall model is ABL.wall_shear_stress_type = moeng");
     for (auto& d : disks_)

@@ -53,7 +53,7 @@ inline long long nfaces(const Grid& g, int d) { return (long long)g.nx * g.ny * 
 // cell of the same index), 3 components.  Wall-bounded z: the wall faces take
 // the boundary (ghost) value, the faces one cell inside the one-sided
 // fourth-order formula, clipped to the two adjacent cells.
-template <typename T>
+template <typename T, int NC = 3>
 __global__ void k_edges(Grid g, int d, const double* vel, T* e0, T* e1, T* e2) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -63,7 +63,7 @@ __global__ void k_edges(Grid g, int d, const double* vel, T* e0, T* e1, T* e2) {
     const bool wall = (d == 2 && !g.zper);
     T* e[3] = {e0, e1, e2};
     const long long f = fidx(g, d, i, j, k);
-    for (int n = 0; n < 3; ++n) {
+    for (int n = 0; n < NC; ++n) {
         T v;
         if (wall && k == 0) {
             v = q(n, i, j, -1);
@@ -151,7 +151,7 @@ struct C3 {
 // Pre-MAC also writes the Riemann-solved advective velocity and the states of
 // the two transverse components upwinded with it; post-MAC writes the states of
 // all three components upwinded with the MAC velocity.
-template <int MODE, typename T>
+template <int MODE, typename T, int NC = 3>
 __global__ void k_faces(Grid g, int d, const double* vel, C3<T> E, Dt<T> dtdx, T rho, const double* umac_d, P3<T> LO, P3<T> HI, T* ad,
                         P3<T> edge) {
     int i, j, k;
@@ -175,7 +175,7 @@ __global__ void k_faces(Grid g, int d, const double* vel, C3<T> E, Dt<T> dtdx, T
         uh = umf;  // low face of cell c
     }
     T lo[3], hi[3];
-    for (int n = 0; n < 3; ++n) {
+    for (int n = 0; n < NC; ++n) {
         T l = T(0), h = T(0);
         if (!wl) {  // high-side trace of cell c - e_d
             const T s0 = q(n, i - di, j - dj, k - dk);
@@ -205,7 +205,7 @@ __global__ void k_faces(Grid g, int d, const double* vel, C3<T> E, Dt<T> dtdx, T
         for (int n = 0; n < 3; ++n)
             if (n != d) edge.p[n][f] = upwind(a, lo[n], hi[n]);
     } else {
-        for (int n = 0; n < 3; ++n) edge.p[n][f] = upwind(umf, lo[n], hi[n]);
+        for (int n = 0; n < NC; ++n) edge.p[n][f] = upwind(umf, lo[n], hi[n]);
     }
 }
 
@@ -264,7 +264,7 @@ __global__ void k_pm_final(Grid g, int d, const T* lo_dd, const T* hi_dd, const 
 // pass: the face states, the two adjacent cell values and the MAC velocity are
 // loaded once for the corrections along b1 = a+1 and b2 = a+2 (each is the
 // k_adv_trans arithmetic).
-template <typename T>
+template <typename T, int NC = 3>
 __global__ void __launch_bounds__(256, 2) k_adv_trans2(Grid g, int a, const double* vel, T rho, T cb1, T cb2, const double* ua,
                                                        const double* vb1, const double* vb2, C3<T> LO, C3<T> HI, C3<T> E1, C3<T> E2,
                                                        P3<T> out1, P3<T> out2) {
@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(256, 2) k_adv_trans2(Grid g, int a, const doub
         vlp2 = (T)vb2[l1b];
         vlm2 = (T)vb2[l0b];
     }
-    for (int n = 0; n < 3; ++n) {
+    for (int n = 0; n < NC; ++n) {
         const T l0 = LO.p[n][f], h0 = HI.p[n][f];
         const T qh = wh ? T(0) : q(n, i, j, k), ql = wl ? T(0) : q(n, ci, cj, ck);
         T l = l0, h = h0;
@@ -317,9 +317,11 @@ __global__ void __launch_bounds__(256, 2) k_adv_trans2(Grid g, int a, const doub
 }
 
 // ---- post-MAC stage 3: final states and fluxes on d-faces
-template <typename T>
-__global__ void __launch_bounds__(256, 3) k_adv_flux(Grid g, int d, const double* vel, const double* forces, T rho, T dt, T c1, T c2, C3<double> U, C3<T> LO, C3<T> HI,
-                           C3<T> T1, C3<T> T2, P3<T> Fl) {
+// The forces enter scaled by rho for the velocity (forces = (src + divtau) / rho)
+// and as they are for a scalar (NC = 1: forces = src + diff, AdvOp_Godunov.H:114-329).
+template <typename T, int NC = 3>
+__global__ void __launch_bounds__(256, 3) k_adv_flux(Grid g, int d, const double* vel, const double* forces, T rho, T dt, T c1, T c2,
+                                                     C3<double> U, C3<T> LO, C3<T> HI, C3<T> T1, C3<T> T2, P3<T> Fl) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_of(g, d, t, i, j, k)) return;
@@ -337,7 +339,7 @@ __global__ void __launch_bounds__(256, 3) k_adv_flux(Grid g, int d, const double
     T l1p = 0, l1m = 0, l2p = 0, l2m = 0, h1p = 0, h1m = 0, h2p = 0, h2m = 0;
     if (!wl) { l1p = (T)U.p[b1][lp1]; l1m = (T)U.p[b1][lm1]; l2p = (T)U.p[b2][lp2]; l2m = (T)U.p[b2][lm2]; }
     if (!wh) { h1p = (T)U.p[b1][hp1]; h1m = (T)U.p[b1][hm1]; h2p = (T)U.p[b2][hp2]; h2m = (T)U.p[b2][hm2]; }
-    for (int n = 0; n < 3; ++n) {
+    for (int n = 0; n < NC; ++n) {
         T stl = T(0), sth = T(0);
         if (!wl) {
             const T qc = q(n, li, lj, lk);
@@ -346,7 +348,7 @@ __global__ void __launch_bounds__(256, 3) k_adv_flux(Grid g, int d, const double
             s -= c2 * (T2.p[n][lp2] * l2p - T2.p[n][lm2] * l2m);
             s += c1 * qc * (l1p - l1m);
             s += c2 * qc * (l2p - l2m);
-            s += T(0.5) * dt * (rho * Fo(n, li, lj, lk));
+            s += T(0.5) * dt * ((NC == 3 ? rho : T(1)) * Fo(n, li, lj, lk));
             stl = s;
         }
         if (!wh) {
@@ -356,7 +358,7 @@ __global__ void __launch_bounds__(256, 3) k_adv_flux(Grid g, int d, const double
             s -= c2 * (T2.p[n][hp2] * h2p - T2.p[n][hm2] * h2m);
             s += c1 * qc * (h1p - h1m);
             s += c2 * qc * (h2p - h2m);
-            s += T(0.5) * dt * (rho * Fo(n, i, j, k));
+            s += T(0.5) * dt * ((NC == 3 ? rho : T(1)) * Fo(n, i, j, k));
             sth = s;
         }
         if (d == 2) zbc(g, k, n, stl, sth);
@@ -370,7 +372,7 @@ template <typename T>
 struct FluxPtrs {
     const T* p[9];
 };
-template <typename T>
+template <typename T, int NC = 3>
 __global__ void k_adv_div(Grid g, FluxPtrs<T> F, double* conv) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= g.N) return;
@@ -379,7 +381,7 @@ __global__ void k_adv_div(Grid g, FluxPtrs<T> F, double* conv) {
     const int j = (int)(r % g.ny), k = (int)(r / g.ny);
     const long long xp = fidx(g, 0, i + 1, j, k), yp = fidx(g, 1, i, j + 1, k), zp = fidx(g, 2, i, j, k + 1), zm = fidx(g, 2, i, j, k);
     const T ix = T(g.idx), iy = T(g.idy), iz = T(g.idz);
-    for (int n = 0; n < 3; ++n)
+    for (int n = 0; n < NC; ++n)
         conv[n * g.N + t] =
             (double)(-((F.p[n][xp] - F.p[n][t]) * ix + (F.p[3 + n][yp] - F.p[3 + n][t]) * iy + (F.p[6 + n][zp] - F.p[6 + n][zm]) * iz));
 }
@@ -466,6 +468,49 @@ static void advection_t(Ctx& c, const Grid& g, const double* vel, const double* 
     for (int d = 0; d < 3; ++d)
         for (int n = 0; n < 3; ++n) F.p[d * 3 + n] = tp<T>(B.flux[d][n]);
     KS_LAUNCH(c, k_adv_div<T>, nblocks(g.N, BS), BS, BT * 9.0 * g.N + B8 * 3.0 * g.N, g, F, conv);
+}
+
+// Godunov fluxes of rho s for a cell scalar s (hoextrap at z walls, like a
+// tangential velocity component) with the forces fs = src + diff, and conv =
+// -div(flux) (AdvOp_Godunov.H:114-329).  FP64; edges[3] holds the scalar's
+// unlimited edge values; the other face arrays are the component-0 slots of B.
+void launch_scalar_advection(Ctx& c, const Grid& g, const double* s, const double* fs, const double* mac[3], double dt, double rho,
+                             double* const edges[3], GodunovBufs& B, double* conv) {
+    using T = double;
+    const double B8 = 8.0;
+    const Dt<T> dtdx{{dt / g.dx, dt / g.dy, dt / g.dz}};
+    for (int d = 0; d < 3; ++d)
+        KS_LAUNCH(c, (k_edges<T, 1>), nblocks(nfaces(g, d), BS), BS, B8 * (g.N + nfaces(g, d)), g, d, s, edges[d], nullptr, nullptr);
+    for (int a = 0; a < 3; ++a) {
+        C3<T> E{{edges[a], nullptr, nullptr}};
+        P3<T> LO{{tp<T>(B.lo[a][0]), nullptr, nullptr}}, HI{{tp<T>(B.hi[a][0]), nullptr, nullptr}};
+        P3<T> ED{{tp<T>(B.tedge[a][0]), nullptr, nullptr}};
+        KS_LAUNCH(c, (k_faces<1, T, 1>), nblocks(nfaces(g, a), BS), BS, B8 * (g.N + 5.0 * nfaces(g, a)), g, a, s, E, dtdx, T(rho), mac[a], LO,
+                  HI, (T*)nullptr, ED);
+    }
+    for (int a = 0; a < 3; ++a) {
+        const int b1 = (a + 1) % 3, b2 = (a + 2) % 3;
+        const double na = (double)nfaces(g, a), nt = (double)(nfaces(g, b1) + nfaces(g, b2));
+        C3<T> LO{{tp<T>(B.lo[a][0]), nullptr, nullptr}}, HI{{tp<T>(B.hi[a][0]), nullptr, nullptr}};
+        C3<T> E1{{tp<T>(B.tedge[b1][0]), nullptr, nullptr}}, E2{{tp<T>(B.tedge[b2][0]), nullptr, nullptr}};
+        P3<T> O1{{tp<T>(B.tr[a][b1][0]), nullptr, nullptr}}, O2{{tp<T>(B.tr[a][b2][0]), nullptr, nullptr}};
+        KS_LAUNCH(c, (k_adv_trans2<T, 1>), nblocks(nfaces(g, a), BS), BS, B8 * (g.N + 5.0 * na + 2.0 * nt), g, a, s, T(rho),
+                  T(dt / (3.0 * hd(g, b1))), T(dt / (3.0 * hd(g, b2))), mac[a], mac[b1], mac[b2], LO, HI, E1, E2, O1, O2);
+    }
+    C3<double> U{{mac[0], mac[1], mac[2]}};
+    for (int d = 0; d < 3; ++d) {
+        const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
+        C3<T> LO{{tp<T>(B.lo[d][0]), nullptr, nullptr}}, HI{{tp<T>(B.hi[d][0]), nullptr, nullptr}};
+        C3<T> T1{{tp<T>(B.tr[b1][b2][0]), nullptr, nullptr}}, T2{{tp<T>(B.tr[b2][b1][0]), nullptr, nullptr}};
+        P3<T> F{{tp<T>(B.flux[d][0]), nullptr, nullptr}};
+        const double bytes = B8 * (2.0 * g.N + 4.0 * nfaces(g, d) + 2.0 * (nfaces(g, b1) + nfaces(g, b2)));
+        KS_LAUNCH(c, (k_adv_flux<T, 1>), nblocks(nfaces(g, d), BS), BS, bytes, g, d, s, fs, T(rho), T(dt), T(dt / (2.0 * hd(g, b1))),
+                  T(dt / (2.0 * hd(g, b2))), U, LO, HI, T1, T2, F);
+    }
+    FluxPtrs<T> F;
+    for (int m = 0; m < 9; ++m) F.p[m] = nullptr;
+    for (int d = 0; d < 3; ++d) F.p[3 * d] = tp<T>(B.flux[d][0]);
+    KS_LAUNCH(c, (k_adv_div<T, 1>), nblocks(g.N, BS), BS, B8 * (3.0 * g.N + g.N), g, F, conv);
 }
 
 void launch_premac(Ctx& c, const Grid& g, const double* vel, const double* forces, double dt, GodunovBufs& B, double* mac[3], int fp32) {

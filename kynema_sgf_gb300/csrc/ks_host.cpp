@@ -101,6 +101,8 @@ void Sim::setup(const Deck& D) {
         else if (s == "CoriolisForcing") S_.cor = 1;
         else if (s == "BodyForce") S_.body = 1;
         else if (s == "ActuatorForcing") S_.act = 1;
+        else if (s == "BoussinesqBuoyancy") S_.bous = 1;
+        else if (s == "ABLForcing") S_.ablf = 1;
         else throw KsError(KS_ERR_UNSUPPORTED, "momentum source " + s);
     }
     const double pi = 3.14159265358979323846;
@@ -145,6 +147,57 @@ void Sim::setup(const Deck& D) {
     if (wallmodel_ && std::fabs(zref_ - 0.5 * g_.dz) > 1e-12 * g_.dz)
         throw KsError(KS_ERR_UNSUPPORTED, "ABL.log_law_height other than the first cell centre");
 
+    // Temperature transport: the ABL physics registers the Temperature PDE
+    // (src/wind_energy/ABL.cpp:27-28); it is advanced when the deck gives the
+    // initial profile (ABL.temperature_heights, required by ABLFieldInit.cpp:96-99).
+    const std::string phys = D.str("incflo.physics", "");
+    temp_ = phys == "ABL" && D.has("ABL.temperature_heights");
+    S_.temp = temp_ ? 1 : 0;
+    S_.grav[0] = 0.0; S_.grav[1] = 0.0; S_.grav[2] = -9.81;
+    if (D.has("incflo.gravity")) { auto gv = D.nums("incflo.gravity"); for (int d = 0; d < 3; ++d) S_.grav[d] = gv.at(d); }
+    const double Pr = D.num("transport.laminar_prandtl", 1.0), Prt = D.num("transport.turbulent_prandtl", 1.0);  // ConstTransport.H:20-95
+    S_.mu_pr = mu_ / Pr;
+    S_.iprt = 1.0 / Prt;
+    S_.T_ref = D.num("transport.reference_temperature", -1.0);
+    if (S_.bous) {  // BoussinesqBuoyancy.cpp:10-17, ConstTransport.H:32-95,184-200
+        if (!temp_) throw KsError(KS_ERR_DECK, "BoussinesqBuoyancy needs the temperature field (ABL.temperature_heights)");
+        if (S_.T_ref < 0.0) throw KsError(KS_ERR_DECK, "Reference temperature was not set");
+        S_.beta_T = D.has("transport.thermal_expansion_coefficient") ? D.num("transport.thermal_expansion_coefficient", 0.0) : 1.0 / S_.T_ref;
+    }
+    if (S_.ablf) {  // ABLForcing.cpp:13-60
+        if (phys != "ABL") throw KsError(KS_ERR_DECK, "ABLForcing needs the ABL physics");
+        if (D.has("ABLForcing.velocity_timetable")) throw KsError(KS_ERR_UNSUPPORTED, "ABLForcing.velocity_timetable");
+        ablf_h_ = D.nums("ABLForcing.abl_forcing_height").at(0);
+        auto tv = D.nums("incflo.velocity");
+        ablf_target_[0] = tv.at(0);
+        ablf_target_[1] = tv.at(1);
+    }
+    if (temp_) {
+        if (!godunov_) throw KsError(KS_ERR_UNSUPPORTED, "temperature transport with the MOL scheme");
+        if (D.has("ABL.surface_temp_rate") || D.has("ABL.surface_temp_timetable") || std::fabs(D.num("ABL.surface_temp_flux", 0.0)) > 0.0)
+            throw KsError(KS_ERR_UNSUPPORTED, "non-neutral surface temperature forcing (only ABL.surface_temp_flux = 0)");
+        if (D.flag("ABL.perturb_temperature", 0)) throw KsError(KS_ERR_UNSUPPORTED, "ABL.perturb_temperature (random perturbations)");
+        z0t_ = D.num("ABL.surface_roughness_z0t", z0_);
+        // temperature BCs (BCInterface.cpp:289-350, incflo_diffusion.cpp:71-104);
+        // <face>.temperature_type overrides the face's velocity BC type
+        auto tbc = [&](const char* face, int zbc) {
+            const std::string key = std::string(face) + ".temperature_type";
+            const std::string t = lc(D.str(key, zbc == ZWALLMODEL ? "wall_model" : "slip_wall"));
+            if (t == "wall_model") return 1;
+            if (t == "fixed_gradient") return 2;
+            if (t == "slip_wall" || t == "zero_gradient" || t == "symmetric_wall") return 0;
+            throw KsError(KS_ERR_UNSUPPORTED, key + " = " + t);
+        };
+        if (!g_.zper) {
+            tzlo_ = tbc("zlo", g_.zlo);
+            tzhi_ = tbc("zhi", g_.zhi);
+            if (tzhi_ == 1) throw KsError(KS_ERR_DECK, "ABL wall models are not applicable to a zhi BC");
+            if (tzlo_ == 1 && g_.zlo != ZWALLMODEL) throw KsError(KS_ERR_UNSUPPORTED, "temperature wall model without the velocity wall model");
+            if (tzlo_ == 2) throw KsError(KS_ERR_UNSUPPORTED, "zlo fixed_gradient temperature");
+            if (tzhi_ == 2) tgtop_ = D.nums("zhi.temperature").at(0);
+        }
+    }
+
     auto mg = [&](MGParams& m, const std::string& p) {
         m.rtol = D.num(p + ".mg_rtol", m.rtol);
         m.atol = D.num(p + ".mg_atol", m.atol);
@@ -157,6 +210,8 @@ void Sim::setup(const Deck& D) {
     mg(nod_, "nodal_proj");
     mg(dif_, "diffusion");  // MLMGOptions(default prefix, custom prefix), src/core/MLMGOptions.cpp:8-13
     mg(dif_, "velocity_diffusion");
+    mg(tdif_, "diffusion");
+    mg(tdif_, "temperature_diffusion");
 
     t_.stop = D.num("time.stop_time", -1);
     t_.max_step = D.flag("time.max_step", -1);
@@ -344,6 +399,14 @@ void Sim::alloc() {
     nod_.omega = nodal_jacobi_weight(nd_[0].W, nod_.omega);
     parts_.alloc(4 * 1216);
     red_.alloc(8);
+    if (temp_ || S_.ablf) layer_.alloc(3 * (size_t)g_.nz);
+    if (temp_) {
+        for (DevBuf<double>* b : {&theta_, &theta_old_, &theta_nph_, &alpha_, &tdiff_, &tconv_, &ttmp_, &tb_, &tdinv_}) b->alloc(N);
+        tgz_.alloc((size_t)g_.nx * g_.ny);
+        tedge_.alloc(2 * N + NF);
+        tparts_.alloc((size_t)tdiff_blocks(g_));
+        if (gb_.lo[0][0] == nullptr) throw KsError(KS_ERR_UNSUPPORTED, "temperature transport needs the Godunov face scratch");
+    }
     size_t maxpts = 1;
     for (auto& d : disks_) maxpts = std::max(maxpts, (size_t)d.nr * d.nt);
     pts_.alloc(4 * maxpts);
@@ -359,6 +422,18 @@ void Sim::init_fields(const Deck& D) {
         S_.irho = 1.0 / rho_;
         const double L[3] = {phi_[0] - plo_[0], phi_[1] - plo_[1], phi_[2] - plo_[2]};
         launch_init_tgv(ctx_, g_, vel_.p, plo_, L);
+    } else if (phys == "ABL" && !D.has_prefix("ks_init.")) {
+        // ABLFieldInit (src/wind_energy/ABLFieldInit.cpp:215-372), uniform-wind branch:
+        // incflo.velocity plus the sinusoidal perturbation (perturb_velocity, default on)
+        auto u = D.nums("incflo.velocity");
+        const double U[3] = {u.at(0), u.at(1), u.at(2)};
+        if (D.flag("ABL.linear_profile", 0)) throw KsError(KS_ERR_UNSUPPORTED, "ABL.linear_profile");
+        const double pi = 3.14159265358979323846;
+        const double refh = D.num("ABL.perturb_ref_height", 50.0), ibh = D.num("ABL.ib_height", 0.0);
+        const double aval = D.num("ABL.Uperiods", 4.0) * 2.0 * pi / (phi_[1] - plo_[1]);
+        const double bval = D.num("ABL.Vperiods", 4.0) * 2.0 * pi / (phi_[0] - plo_[0]);
+        const double ufac = D.num("ABL.deltaU", 1.0) * std::exp(0.5) / refh, vfac = D.num("ABL.deltaV", 1.0) * std::exp(0.5) / refh;
+        launch_init_abl_ref(ctx_, g_, vel_.p, plo_, U, D.flag("ABL.perturb_velocity", 1), aval, bval, ufac, vfac, refh, ibh);
     } else if (phys == "ABL" || phys == "FreeStream") {
         const std::string prof = lc(D.str("ks_init.profile", phys == "ABL" ? "loglaw" : "uniform"));
         double U[3] = {0, 0, 0};
@@ -372,6 +447,15 @@ void Sim::init_fields(const Deck& D) {
         launch_init_abl(ctx_, g_, vel_.p, prof == "loglaw", U, ut / kappa_, z0_, amp, zmax - plo_[2], seed);
     } else if (!phys.empty()) {
         throw KsError(KS_ERR_UNSUPPORTED, "incflo.physics = " + phys);
+    }
+    if (temp_) {  // piecewise-linear temperature profile (ABLFieldInit.cpp:318-327)
+        auto th = D.nums("ABL.temperature_heights"), tv = D.nums("ABL.temperature_values");
+        if (th.size() != tv.size() || th.empty()) throw KsError(KS_ERR_DECK, "ABL.temperature_heights and temperature_values differ in length");
+        std::vector<double> hv(th);
+        hv.insert(hv.end(), tv.begin(), tv.end());
+        tprof_.alloc(hv.size());
+        ck(cudaMemcpy(tprof_.p, hv.data(), hv.size() * sizeof(double), cudaMemcpyHostToDevice), "H2D");
+        launch_theta_profile(ctx_, g_, theta_.p, plo_[2], tprof_.p, tprof_.p + th.size(), (int)th.size());
     }
 }
 
@@ -408,6 +492,42 @@ void Sim::abl_update() {
     um_[1] = s[1] / M;
     vmag_ = s[2] / M;
     utau_ = kappa_ * vmag_ / std::log(zref_ / z0_);
+    if (temp_) {  // theta_mean at z_ref for the heat flux (ABLWallFunction.cpp:206-207)
+        launch_layer_sums(ctx_, g_, theta_.p, layer_.p);
+        ck(cudaMemcpyAsync(hred_, layer_.p, sizeof(double), cudaMemcpyDeviceToHost, ctx_.stream), "D2H");
+        sync();
+        theta_mean_ = hred_[0] / M;
+    }
+}
+
+// ABL::pre_advance_work -> ABLForcing::set_mean_velocities (ABL.cpp:176-205,
+// ABLForcing.H:37-64): layer averages of u and v interpolated to the forcing
+// height as FieldPlaneAveraging does (FieldPlaneAveraging.cpp:78-96,151-164),
+// force = (target - mean) / dt.
+void Sim::abl_forcing_update() {
+    if (!S_.ablf) return;
+    const int nz = g_.nz;
+    launch_layer_sums(ctx_, g_, vel_.p, layer_.p);
+    launch_layer_sums(ctx_, g_, vel_.p + g_.N, layer_.p + nz);
+    std::vector<double> h(2 * (size_t)nz);
+    ck(cudaMemcpyAsync(h.data(), layer_.p, 2 * nz * sizeof(double), cudaMemcpyDeviceToHost, ctx_.stream), "D2H");
+    sync();
+    const double M = (double)g_.nx * g_.ny;
+    int ind = 0;
+    double c = 0.0;
+    const double x = ablf_h_, xlo = plo_[2], dz = g_.dz;
+    if (x > xlo + 0.5 * dz) {
+        ind = (int)std::floor((x - xlo) / dz - 0.5);
+        c = (x - (xlo + (ind + 0.5) * dz)) / dz;
+    }
+    if (ind + 1 >= nz) {
+        ind = nz - 2;
+        c = 1.0;
+    }
+    const double mu0 = (h[ind] / M) * (1.0 - c) + (h[ind + 1] / M) * c;
+    const double mv0 = (h[nz + ind] / M) * (1.0 - c) + (h[nz + ind + 1] / M) * c;
+    S_.ablf_force[0] = (ablf_target_[0] - mu0) / t_.dt[0];
+    S_.ablf_force[1] = (ablf_target_[1] - mv0) / t_.dt[0];
 }
 
 // ---------------------------------------------------------------- actuators
@@ -881,19 +1001,28 @@ void Sim::apply_predictor(bool incremental) {
         return;
     }
     const double dt = t_.dt[0];
-    launch_smagorinsky(ctx_, g_, vel_old_.p, mueff_.p, S_);
-    launch_sources(ctx_, g_, vel_old_.p, gp_.p, act_.p, src_.p, S_);
+    launch_smagorinsky(ctx_, g_, vel_old_.p, mueff_.p, S_, alpha_.p);
+    launch_sources(ctx_, g_, vel_old_.p, gp_.p, act_.p, src_.p, S_, theta_old_.p);  // BoussinesqBuoyancy: theta at Old
     if (wallmodel_) launch_wall_grad(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, shear_, utau_ * utau_, um_[0], um_[1], vmag_, rho_);
     double* fl[9];
     for (int m = 0; m < 9; ++m) fl[m] = static_cast<double*>(gb_.flux[m / 3][m % 3]);
     launch_divtau(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, divtau_.p, 1, src_.p, forces_.p, nullptr, nullptr, dt, rho_, fl);
+    if (temp_) {  // the temperature's diff_term(Old) (no temperature sources)
+        if (tzlo_ == 1)
+            launch_theta_wall_grad(ctx_, g_, vel_old_.p, theta_old_.p, alpha_.p, tgz_.p, shear_, utau_, kappa_, std::log(zref_ / z0t_), vmag_,
+                                   theta_mean_, rho_);
+        launch_tdiff(ctx_, g_, theta_old_.p, alpha_.p, tbc(), tdiff_.p, 0, nullptr, nullptr, nullptr, nullptr, nullptr, dt, rho_, 0.0);
+    }
     double* mac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
     launch_premac(ctx_, g_, vel_old_.p, forces_.p, dt, gb_, mac, mixed_);
     mac_project();
+    if (temp_) temperature_predictor(dt);
     const double* cmac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
     launch_advection(ctx_, g_, vel_old_.p, forces_.p, cmac, dt, rho_, adv_bufs_ ? *adv_bufs_ : gb_, conv_.p, mixed_);
-    // compute_source_term(NPH) and compute_diffusion_term(Old) reproduce src
-    // and divtau on this path (Coriolis reads the Old velocity, gp unchanged).
+    // compute_source_term(NPH): Coriolis reads the Old velocity and gp is
+    // unchanged, so only BoussinesqBuoyancy (theta at n+1/2) changes src;
+    // compute_diffusion_term(Old) reproduces divtau.
+    if (S_.bous) launch_sources(ctx_, g_, vel_old_.p, gp_.p, act_.p, src_.p, S_, theta_nph_.p);
     launch_predictor_rhs(ctx_, g_, vel_old_.p, conv_.p, src_.p, divtau_.p, vel_.p, dt, rho_, diff_fac());
     if (diff_type_ == 0) {  // explicit RK2 correction (incflo_advance.cpp:388-400)
         launch_divtau(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, 2, nullptr, nullptr, vel_.p, divtau_.p, dt, rho_, fl);
@@ -965,12 +1094,70 @@ void Sim::apply_corrector() {
     apply_projection(t_.next, dt, false);
 }
 
-void Sim::prepare_time_step() { launch_copy(ctx_, vel_old_.p, vel_.p, 3 * g_.N); }
+void Sim::prepare_time_step() {
+    launch_copy(ctx_, vel_old_.p, vel_.p, 3 * g_.N);
+    if (temp_) launch_copy(ctx_, theta_old_.p, theta_.p, g_.N);
+}
 
 void Sim::pre_advance() {
     t_.next = t_.cur + t_.dt[0];
     abl_update();
+    abl_forcing_update();
     actuator_update();
+}
+
+// ---------------------------------------------------------------- temperature
+// The scalar part of ApplyPredictor (incflo_advance.cpp:296-341) after the MAC
+// projection: Godunov fluxes of rho theta with the forces src + diff (no
+// temperature sources), predictor_rhs, the explicit RK2 correction or the
+// diffusion solve, theta_nph = (theta_old + theta) / 2 for the buoyancy.
+void Sim::temperature_predictor(double dt) {
+    const long long N = g_.N;
+    const double* cmac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
+    double* edges[3] = {tedge_.p, tedge_.p + N, tedge_.p + 2 * N};
+    launch_scalar_advection(ctx_, g_, theta_old_.p, tdiff_.p, cmac, dt, rho_, edges, gb_, tconv_.p);
+    launch_scalar_pred(ctx_, N, theta_old_.p, tconv_.p, tdiff_.p, theta_.p, dt, rho_, diff_fac());
+    if (diff_type_ == 0) {  // explicit RK2 correction with the same wall data
+        launch_tdiff(ctx_, g_, theta_.p, alpha_.p, tbc(), ttmp_.p, 2, theta_.p, tdiff_.p, nullptr, nullptr, nullptr, dt, rho_, 0.0);
+        std::swap(theta_.p, ttmp_.p);
+    } else {
+        tdiffuse_solve(diff_type_ == 2 ? dt : 0.5 * dt);
+    }
+    launch_lincomb(ctx_, N, 0.5, theta_old_.p, 0.5, theta_.p, theta_nph_.p);
+}
+
+// rho theta - dtd div(alpha grad theta) = rho theta_rhs (MLABecLaplacian solve,
+// DiffusionOps.cpp:114-159) by unweighted Jacobi sweeps, one scalar stencil pass
+// each with the residual of the incoming iterate; D^-1 A has its spectrum in
+// [1 - s, 1 + s], s = max(1 - rho / D) < 1, so every sweep contracts the error
+// by s.  MLMG's stopping target on max(|rhs|, initial residual).
+void Sim::tdiffuse_solve(double dtd) {
+    const int np = tdiff_blocks(g_);
+    launch_scalar_rhs(ctx_, g_, theta_.p, rho_, tb_.p, tparts_.p);
+    launch_reduce(ctx_, tparts_.p, np, 1, 1, red_.p);
+    launch_tdiff_dinv(ctx_, g_, alpha_.p, tbc(), rho_, dtd, tdinv_.p, nullptr);
+    ck(cudaMemcpyAsync(hred_, red_.p, sizeof(double), cudaMemcpyDeviceToHost, ctx_.stream), "D2H");
+    sync();
+    const double bnorm = hred_[0];
+    int it = 0;
+    double r0 = 0.0, rn = 0.0, target = 0.0;
+    while (true) {
+        launch_tdiff(ctx_, g_, theta_.p, alpha_.p, tbc(), ttmp_.p, 7, nullptr, nullptr, tb_.p, tdinv_.p, tparts_.p, dtd, rho_, 1.0);
+        std::swap(theta_.p, ttmp_.p);
+        launch_reduce(ctx_, tparts_.p, np, 1, 1, red_.p);
+        ck(cudaMemcpyAsync(hred_, red_.p, sizeof(double), cudaMemcpyDeviceToHost, ctx_.stream), "D2H");
+        sync();
+        rn = hred_[0];
+        if (it == 0) {
+            r0 = rn;
+            target = std::max(tdif_.atol, tdif_.rtol * std::max(bnorm, r0));
+        }
+        if (!std::isfinite(rn)) throw KsError(KS_ERR_NONFINITE, "temperature diffusion solve diverged");
+        if (rn <= target || it >= tdif_.maxiter) break;
+        ++it;
+    }
+    if (rn > target && !tdif_.fixed_iters) throw KsError(KS_ERR_NOT_CONVERGED, "temperature diffusion solve did not converge");
+    tdif_it_ = it;
 }
 
 void Sim::init_data() {
@@ -982,10 +1169,11 @@ void Sim::init_data() {
     }
     if (initial_iters_ > 0) {
         compute_dt();
-        launch_copy(ctx_, vel_old_.p, vel_.p, 3 * g_.N);
+        prepare_time_step();
         for (int it = 0; it < initial_iters_; ++it) {
             apply_predictor(true);
             launch_copy(ctx_, vel_.p, vel_old_.p, 3 * g_.N);
+            if (temp_) launch_copy(ctx_, theta_.p, theta_old_.p, g_.N);
         }
     }
     sync();
@@ -1014,6 +1202,14 @@ double* Sim::field(const std::string& name, int& nc, int& kind) {
     if (name == "diff_term") return divtau_.p;
     if (name == "conv_term") return conv_.p;
     if (name == "conv_term_old" && !godunov_) return conv_old_.p;
+    if (temp_ && name.rfind("temperature", 0) == 0) {
+        nc = 1;
+        if (name == "temperature") return theta_.p;
+        if (name == "temperature_old") return theta_old_.p;
+        if (name == "temperature_mueff") return alpha_.p;
+        if (name == "temperature_conv_term") return tconv_.p;
+        if (name == "temperature_diff_term") return tdiff_.p;
+    }
     if (name == "velocity_adjoint" || name == "gp_adjoint") {
         adj_alloc();
         return name == "velocity_adjoint" ? adj_->ub.p : adj_->gpb.p;
@@ -1094,6 +1290,10 @@ double Sim::scalar(const std::string& n) {
     if (n == "diff_res0") return dif_r0_;
     if (n == "diff_res") return dif_r_;
     if (n == "diff_rhs_norm") return dif_b_;
+    if (n == "temperature_diff_iters") return tdif_it_;
+    if (n == "theta_mean") return theta_mean_;
+    if (n == "abl_forcing_x") return S_.ablf_force[0];
+    if (n == "abl_forcing_y") return S_.ablf_force[1];
     if (n == "mac_res0") return mac_r0_;
     if (n == "mac_res") return mac_r_;
     if (n == "nodal_res0") return nod_r0_;

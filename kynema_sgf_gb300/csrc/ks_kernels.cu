@@ -105,10 +105,16 @@ __global__ void k_copy(double* d, const double* s, long long n) {
 // mu_eff = mu + rho Cs^2 Delta^2 |S| (src/turbulence/LES/Smagorinsky.cpp:22-62,
 // strain rate src/fvm/strainrate.H:24-86, one-sided z stencils at walls
 // src/fvm/stencils.H:166-330).
-__global__ void k_smag(Grid g, const double* vel, double* mueff, double mu, double rho, double fac, int smag) {
+// alpha_eff = mu / Pr + mu_t / Pr_t (TurbModelBase.H:28-35) when alpha is set
+__global__ void k_smag(Grid g, const double* vel, double* mueff, double mu, double rho, double fac, int smag, double* alpha, double mu_pr,
+                       double iprt) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= g.N) return;
-    if (!smag) { mueff[t] = mu; return; }
+    if (!smag) {
+        mueff[t] = mu;
+        if (alpha) alpha[t] = mu_pr;
+        return;
+    }
     int i, j, k;
     cell_of(g, t, i, j, k);
     VelFP V{vel, g, 1.0};
@@ -123,14 +129,16 @@ __global__ void k_smag(Grid g, const double* vel, double* mueff, double mu, doub
     }
     const double s = sqrt(2.0 * gx[0] * gx[0] + 2.0 * gy[1] * gy[1] + 2.0 * gz[2] * gz[2] + (gy[0] + gx[1]) * (gy[0] + gx[1]) +
                           (gz[1] + gy[2]) * (gz[1] + gy[2]) + (gx[2] + gz[0]) * (gx[2] + gz[0]));
-    mueff[t] = mu + rho * fac * s;
+    const double mut = rho * fac * s;
+    mueff[t] = mu + mut;
+    if (alpha) alpha[t] = mu_pr + iprt * mut;
 }
 
 // ---------------------------------------------------------------- sources
 // src = rho (-gp/rho + geostrophic + Coriolis(u_old) + body + actuator)
 // (icns_ops.H:78-124, PDEOps.H:94-145, GeostrophicForcing.cpp:103-,
 // CoriolisForcing.cpp:60-108, BodyForce.cpp:117-169, ActuatorForcing.cpp:19-29)
-__global__ void k_sources(Grid g, const double* vel, const double* gp, const double* act, double* src, Scalars s) {
+__global__ void k_sources(Grid g, const double* vel, const double* gp, const double* act, double* src, Scalars s, const double* theta) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= g.N) return;
     const long long N = g.N;
@@ -152,6 +160,14 @@ __global__ void k_sources(Grid g, const double* vel, const double* gp, const dou
         for (int n = 0; n < 3; ++n) f[n] += s.body_force[n];
     if (s.act)
         for (int n = 0; n < 3; ++n) f[n] += act[n * N + t];
+    if (s.bous) {  // BoussinesqBuoyancy.cpp:22-50
+        const double fac = s.beta_T * (s.T_ref - theta[t]);
+        for (int n = 0; n < 3; ++n) f[n] += s.grav[n] * fac;
+    }
+    if (s.ablf) {  // ABLForcing.cpp:97-139
+        f[0] += s.ablf_force[0];
+        f[1] += s.ablf_force[1];
+    }
     for (int n = 0; n < 3; ++n) src[n * N + t] = s.rho * f[n];
 }
 
@@ -697,11 +713,14 @@ void launch_init_abl(Ctx& c, const Grid& g, double* vel, int loglaw, const doubl
 }
 void launch_fill(Ctx& c, double* p, double v, long long n) { KS_LAUNCH(c, k_fill, nblocks(n, BS), BS, B8 * n, p, v, n); }
 void launch_copy(Ctx& c, double* d, const double* s, long long n) { KS_LAUNCH(c, k_copy, nblocks(n, BS), BS, B8 * 2 * n, d, s, n); }
-void launch_smagorinsky(Ctx& c, const Grid& g, const double* vel, double* mueff, const Scalars& s) {
-    KS_LAUNCH(c, k_smag, nblocks(g.N, BS), BS, B8 * (s.smag ? 4 : 1) * g.N, g, vel, mueff, s.mu, s.rho, s.smag_fac, s.smag);
+void launch_smagorinsky(Ctx& c, const Grid& g, const double* vel, double* mueff, const Scalars& s, double* alpha) {
+    if (!s.temp) alpha = nullptr;
+    KS_LAUNCH(c, k_smag, nblocks(g.N, BS), BS, B8 * ((s.smag ? 4 : 1) + (alpha ? 1 : 0)) * g.N, g, vel, mueff, s.mu, s.rho, s.smag_fac, s.smag,
+              alpha, s.mu_pr, s.iprt);
 }
-void launch_sources(Ctx& c, const Grid& g, const double* vel_old, const double* gp, const double* act, double* src, const Scalars& s) {
-    KS_LAUNCH(c, k_sources, nblocks(g.N, BS), BS, B8 * (6 + 3 * s.cor + 3 * s.act) * g.N, g, vel_old, gp, act, src, s);
+void launch_sources(Ctx& c, const Grid& g, const double* vel_old, const double* gp, const double* act, double* src, const Scalars& s,
+                    const double* theta) {
+    KS_LAUNCH(c, k_sources, nblocks(g.N, BS), BS, B8 * (6 + 3 * s.cor + 3 * s.act + s.bous) * g.N, g, vel_old, gp, act, src, s, theta);
 }
 void launch_plane_sums(Ctx& c, const Grid& g, const double* vel, double* parts, int* np) {
     *np = parts_for((long long)g.nx * g.ny);

@@ -113,16 +113,24 @@ struct Scalars {  // values fed to the pointwise kernels
     double east[3], north[3], up[3];
     double corfac, sinphi, cosphi, hfac;
     double body_force[3];
+    // temperature: alpha_eff = mu / Pr + mu_t / Pr_t; BoussinesqBuoyancy g beta (T0 - T); ABLForcing
+    int temp, bous, ablf;
+    double mu_pr, iprt;
+    double grav[3], beta_T, T_ref;
+    double ablf_force[2];
 };
 
 // ---- pointwise / stencil passes (ks_kernels.cu)
 void launch_init_tgv(Ctx& c, const Grid& g, double* vel, const double plo[3], const double L[3]);
 void launch_init_abl(Ctx& c, const Grid& g, double* vel, int loglaw, const double U[3], double ut_over_kappa, double z0,
                      double amp, double zmax_rel, unsigned long long seed);
-void launch_smagorinsky(Ctx& c, const Grid& g, const double* vel, double* mueff, const Scalars& s);
+// mu_eff (and alpha_eff when s.temp is set and alpha is not null)
+void launch_smagorinsky(Ctx& c, const Grid& g, const double* vel, double* mueff, const Scalars& s, double* alpha = nullptr);
 void launch_fill(Ctx& c, double* p, double v, long long n);
 void launch_copy(Ctx& c, double* dst, const double* src, long long n);
-void launch_sources(Ctx& c, const Grid& g, const double* vel_old, const double* gp, const double* act, double* src, const Scalars& s);
+// src = rho (-gp / rho + sources); theta: the temperature state BoussinesqBuoyancy reads
+void launch_sources(Ctx& c, const Grid& g, const double* vel_old, const double* gp, const double* act, double* src, const Scalars& s,
+                    const double* theta = nullptr);
 void launch_plane_sums(Ctx& c, const Grid& g, const double* vel, double* partials, int* nparts);
 void launch_wall_grad(Ctx& c, const Grid& g, const double* vel_old, const double* mueff, double* wg, int shear_type, double ut2,
                       double um0, double um1, double vmag, double rho);
@@ -183,6 +191,43 @@ void launch_premac(Ctx& c, const Grid& g, const double* vel_old, const double* f
                    int fp32);
 void launch_advection(Ctx& c, const Grid& g, const double* vel_old, const double* forces, const double* mac[3], double dt, double rho,
                       GodunovBufs& B, double* conv, int fp32);
+// Godunov fluxes and conv = -div(flux) of rho s for a cell scalar s with forces fs = src + diff (FP64);
+// edges: three face arrays for the scalar's edge values; B: component-0 face slots reused as scratch
+void launch_scalar_advection(Ctx& c, const Grid& g, const double* s, const double* fs, const double* mac[3], double dt, double rho,
+                             double* const edges[3], GodunovBufs& B, double* conv);
+
+// ---- temperature transport (ks_temperature.cu), FP64
+// ABLFieldInit uniform-wind branch: velocity = U + sinusoidal perturbation (pert != 0)
+void launch_init_abl_ref(Ctx& c, const Grid& g, double* vel, const double plo[3], const double U[3], int pert, double aval, double bval,
+                         double ufac, double vfac, double ref_height, double ib_height);
+// piecewise-linear temperature profile from (heights, values) in device memory (n points)
+void launch_theta_profile(Ctx& c, const Grid& g, double* theta, double zlo, const double* heights, const double* values, int n);
+// per-layer sums of f over x and y: out[k], k < nz (one block per layer)
+void launch_layer_sums(Ctx& c, const Grid& g, const double* f, double* out);
+// wall-normal temperature gradient at z-lo, rho q / alpha (nx ny values): type as the shear stress type,
+// phi_h = ln(z_ref / z0t), neutral surface (surface temperature = theta_mean)
+void launch_theta_wall_grad(Ctx& c, const Grid& g, const double* vel_old, const double* theta_old, const double* alpha, double* gz, int type,
+                            double utau, double kappa, double phi_h, double vmag_mean, double theta_mean, double rho);
+// scalar diffusion div(alpha grad theta) with z data: tzlo/tzhi 0 Neumann 0, 1 wall-model gradient gz, 2 fixed gradient gtop.
+// mode 0: out = acc; 2: out = base + 0.5 dt (acc - dold) / rho; 7: Jacobi sweep out = th + omega dinv (b - rho th + dt acc);
+// 8: residual out = b - rho th + dt acc.  Modes 7 / 8 write block maxima of the residual to parts when set.
+struct ScalarBC {
+    int zlo, zhi;
+    const double* gz;
+    double gtop;
+};
+int tdiff_blocks(const Grid& g);
+void launch_tdiff(Ctx& c, const Grid& g, const double* th, const double* alpha, const ScalarBC& bc, double* out, int mode, const double* base,
+                  const double* dold, const double* b, const double* dinv, double* parts, double dt, double rho, double omega);
+// 1 / diagonal of rho - dtd div(alpha grad), with block maxima of 1 - rho / D in parts
+void launch_tdiff_dinv(Ctx& c, const Grid& g, const double* alpha, const ScalarBC& bc, double rho, double dtd, double* dinv, double* parts);
+// b = rho theta with block maxima of |b| in parts (tdiff_blocks(g) entries)
+void launch_scalar_rhs(Ctx& c, const Grid& g, const double* th, double rho, double* b, double* parts);
+// predictor_rhs of a scalar without sources: out = (rho s_old + dt (conv + fac dold)) / rho
+void launch_scalar_pred(Ctx& c, long long n, const double* s_old, const double* conv, const double* dold, double* out, double dt, double rho,
+                        double fac);
+// out = a x + b y (n values)
+void launch_lincomb(Ctx& c, long long n, double a, const double* x, double b, const double* y, double* out);
 
 // ---- MOL advection (ks_mol.cu), FP64
 // face-normal velocities extrapolated from vel (before the MAC projection)

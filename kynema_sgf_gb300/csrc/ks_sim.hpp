@@ -62,6 +62,10 @@ class Deck {
         }
     }
     bool has(const std::string& k) const { return kv_.count(k) > 0; }
+    bool has_prefix(const std::string& p) const {
+        auto it = kv_.lower_bound(p);
+        return it != kv_.end() && it->first.compare(0, p.size(), p) == 0;
+    }
     std::vector<std::string> strs(const std::string& k) const {
         auto it = kv_.find(k);
         return it == kv_.end() ? std::vector<std::string>{} : it->second;
@@ -287,6 +291,10 @@ class Sim {
     void diff_alloc();
     void diffuse_solve(double dtd);
     void diff_vcycle(size_t l, double dtd);
+    void temperature_predictor(double dt);
+    void tdiffuse_solve(double dtd);
+    void abl_forcing_update();
+    ScalarBC tbc() const { return ScalarBC{tzlo_, tzhi_, tgz_.p, tgtop_}; }
     double diff_fac() const { return diff_type_ == 0 ? 1.0 : (diff_type_ == 1 ? 0.5 : 0.0); }
     void disk_points(const Disk& d, std::vector<double>& sample, std::vector<double>& ring) const;
     // reverse mode
@@ -323,6 +331,14 @@ class Sim {
 
     DevBuf<double> vel_, vel_old_, vel_tmp_, gp_, p_, src_, forces_, mueff_, divtau_, conv_, act_, wg_;
     DevBuf<double> conv_old_;  // MOL: conv_term(Old) of the predictor
+    // temperature transport (ABL physics with a temperature profile)
+    bool temp_ = false;
+    int tzlo_ = 0, tzhi_ = 0;  // 0 Neumann 0, 1 wall-model heat flux, 2 fixed gradient
+    double tgtop_ = 0.0, z0t_ = 0.1, theta_mean_ = 0.0;
+    double ablf_h_ = 0.0, ablf_target_[2] = {0.0, 0.0};
+    int tdif_it_ = 0;
+    MGParams tdif_;
+    DevBuf<double> theta_, theta_old_, theta_nph_, alpha_, tdiff_, tconv_, ttmp_, tb_, tdinv_, tgz_, tedge_, tprof_, layer_, tparts_;
     DevBuf<double> umac_[3];
     DevBuf<double> gbuf_;
     GodunovBufs gb_{};

@@ -253,3 +253,47 @@ ks.precision = {precision}
     lo = (x0, 0.0, 0.5 * D)
     hi = (min(x0 + 5 * D, nx * dx), ny * dx, 1.5 * D)
     return deck, lo, hi, cts
+
+
+def abl_temperature(n=(48, 48, 48), steps=10, diffusion_type=0, fixed_dt=-0.5, cfl=0.95, use_force_cfl=0):
+    """Stably stratified ABL with temperature transport, the configuration of
+    the reference's abl_godunov regression decks (1000 m cube, Boussinesq
+    buoyancy about 300 K, Coriolis at 41.3 deg, ABLForcing at 90 m toward
+    (6.128, 5.142) m/s, Moeng wall model, capping inversion 650-750 m with a
+    3 K/km gradient imposed at the top), PPM Godunov."""
+    nx, ny, nz = n
+    return f"""
+time.max_step = {steps}
+time.fixed_dt = {fixed_dt}
+time.cfl = {cfl}
+time.use_force_cfl = {use_force_cfl}
+incflo.gravity = 0. 0. -9.81
+incflo.density = 1.0
+incflo.use_godunov = 1
+incflo.godunov_type = ppm
+incflo.diffusion_type = {diffusion_type}
+transport.viscosity = 1.0e-5
+transport.laminar_prandtl = 0.7
+transport.turbulent_prandtl = 0.3333
+transport.reference_temperature = 300.0
+turbulence.model = Smagorinsky
+Smagorinsky_coeffs.Cs = 0.135
+incflo.physics = ABL
+ICNS.source_terms = BoussinesqBuoyancy CoriolisForcing ABLForcing
+CoriolisForcing.latitude = 41.3
+ABLForcing.abl_forcing_height = 90
+incflo.velocity = 6.128355544951824 5.142300877492314 0.0
+ABL.temperature_heights = 650.0 750.0 1000.0
+ABL.temperature_values = 300.0 308.0 308.75
+ABL.kappa = .41
+ABL.surface_roughness_z0 = 0.15
+amr.n_cell = {nx} {ny} {nz}
+amr.max_level = 0
+geometry.prob_lo = 0. 0. 0.
+geometry.prob_hi = 1000. 1000. 1000.
+geometry.is_periodic = 1 1 0
+zlo.type = "wall_model"
+zhi.type = "slip_wall"
+zhi.temperature_type = "fixed_gradient"
+zhi.temperature = 0.003
+"""

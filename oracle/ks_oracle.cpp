@@ -80,6 +80,10 @@ struct Deck {
         }
     }
     bool has(const std::string& k) const { return kv.count(k) != 0; }
+    bool has_prefix(const std::string& p) const {
+        auto it = kv.lower_bound(p);
+        return it != kv.end() && it->first.compare(0, p.size(), p) == 0;
+    }
     const std::vector<std::string>& raw(const std::string& k) const {
         auto it = kv.find(k);
         if (it == kv.end()) throw Error(ERR_DECK, "missing deck key " + k);
@@ -258,6 +262,14 @@ struct Sim {
     double Cs = 0.135;
     std::string physics;
     bool src_geo = false, src_cor = false, src_body = false, src_act = false;
+    // temperature transport (ABL physics with a temperature profile)
+    bool has_temp = false, src_bous = false, src_ablf = false;
+    double gravity[3] = {0.0, 0.0, -9.81};
+    double Pr = 1.0, Prt = 1.0, T_ref = -1.0, beta_T = 0.0;
+    double z0t = 0.1, theta_mean = 0.0;
+    int tzlo = 0, tzhi = 0;     // temperature z BCs: 0 Neumann 0, 1 wall model heat flux, 2 fixed gradient
+    double tgrad_hi = 0.0;      // fixed gradient at zhi
+    double ablf_height = 0.0, ablf_target[2] = {0.0, 0.0}, ablf_force[2] = {0.0, 0.0};
     double lat = 90.0, rot_period = 86164.091;
     double east[3] = {1, 0, 0}, north[3] = {0, 1, 0}, up[3] = {0, 0, 1};
     bool cor_horizontal = false;
@@ -267,6 +279,8 @@ struct Sim {
     double utau = 0, umean[2] = {0, 0}, vmag_mean = 0, zref = 0;
     std::vector<DiskParams> disks;
     MGOpts mac, nod, dif;  // dif: the tensor diffusion solve (prefixes diffusion, velocity_diffusion)
+    MGOpts tdif;           // the temperature diffusion solve (prefixes diffusion, temperature_diffusion)
+    int tdiff_iters = 0;
     int do_initial_proj = 1, initial_iterations = 3;
     bool godunov = true;  // incflo.use_godunov; false selects the MOL predictor-corrector
     int diff_type = 1;    // incflo.diffusion_type: 0 explicit, 1 Crank-Nicolson, 2 implicit
@@ -275,6 +289,7 @@ struct Sim {
 
     // fields
     Arr vel, vel_old, gp, p, src, forces, mueff, divtau, divtau_new, conv, conv_old, act_src;
+    Arr theta, theta_old, theta_nph, alpha, tsrc, tdiff, tdiff_new, tconv;
     Arr umac, vmac, wmac;
     int mac_iters = 0, nodal_iters = 0;
     double mac_res0 = 0, mac_res = 0, nodal_res0 = 0, nodal_res = 0;
@@ -287,12 +302,19 @@ struct Sim {
     void fill_vel(Arr& v) const;
     void fill_cc_foextrap(Arr& a) const;
     void update_mueff(Arr& v);
-    void compute_sources(const Arr& v);
+    void compute_sources(const Arr& v, const Arr* th = nullptr);
+    void fill_scalar(Arr& a) const;
+    void theta_wall_gradient(std::vector<double>& gz) const;
+    void tdiff_op(const Arr& th_in, Arr& out);
+    void temperature_predictor(double dt);
+    void tdiffuse_solve(double dtd);
+    void abl_forcing_update();
     void wall_gradient(std::vector<double>& gx, std::vector<double>& gy) const;
     void divtau_op(const Arr& v_in, Arr& out);
     void premac(double dt);
     void mac_project();
     void advection(double dt);
+    void advect_field(const Arr& q, const Arr& fq, int normal, double dt, Arr& out);
     void nodal_project(double time, double scaling, bool incremental);
     void compute_dt();
     void abl_update_umean();
@@ -367,6 +389,8 @@ void Sim::setup(const std::string& text) {
         else if (s == "CoriolisForcing") src_cor = true;
         else if (s == "BodyForce") src_body = true;
         else if (s == "ActuatorForcing") src_act = true;
+        else if (s == "BoussinesqBuoyancy") src_bous = true;
+        else if (s == "ABLForcing") src_ablf = true;
         else throw Error(ERR_UNSUPPORTED, "source term " + s);
     }
     rot_period = D.d("CoriolisForcing.rotational_time_period", 86164.091);
@@ -391,6 +415,54 @@ void Sim::setup(const std::string& text) {
     if (std::fabs(zref - 0.5 * g.dx[2]) > 1e-12 * g.dx[2] && g.zlo == WALLMODEL)
         throw Error(ERR_UNSUPPORTED, "ABL.log_law_height other than the first cell centre");
 
+    // Temperature transport: the ABL physics registers the Temperature PDE
+    // (src/wind_energy/ABL.cpp:27-28); here it is advanced when the deck gives the
+    // initial profile (ABL.temperature_heights, required by ABLFieldInit.cpp:96-99).
+    has_temp = physics == "ABL" && D.has("ABL.temperature_heights");
+    if (D.has("incflo.gravity")) { auto gv = D.v("incflo.gravity"); for (int d = 0; d < 3; ++d) gravity[d] = gv.at(d); }
+    Pr = D.d("transport.laminar_prandtl", 1.0);   // ConstTransport.H:20-95
+    Prt = D.d("transport.turbulent_prandtl", 1.0);
+    T_ref = D.d("transport.reference_temperature", -1.0);
+    if (src_bous) {
+        if (!has_temp) throw Error(ERR_DECK, "BoussinesqBuoyancy needs the temperature field (ABL.temperature_heights)");
+        beta_T = D.has("transport.thermal_expansion_coefficient") ? D.d("transport.thermal_expansion_coefficient", 0.0) : 1.0 / T_ref;
+        if (T_ref < 0.0) throw Error(ERR_DECK, "Reference temperature was not set");
+    }
+    if (src_ablf) {  // ABLForcing.cpp:13-60
+        if (physics != "ABL") throw Error(ERR_DECK, "ABLForcing needs the ABL physics");
+        ablf_height = D.v("ABLForcing.abl_forcing_height").at(0);
+        if (D.has("ABLForcing.velocity_timetable")) throw Error(ERR_UNSUPPORTED, "ABLForcing.velocity_timetable");
+        auto tv = D.v("incflo.velocity");
+        ablf_target[0] = tv.at(0);
+        ablf_target[1] = tv.at(1);
+    }
+    if (has_temp) {
+        if (!godunov) throw Error(ERR_UNSUPPORTED, "temperature transport with the MOL scheme");
+        if (D.has("ABL.surface_temp_rate") || D.has("ABL.surface_temp_timetable") ||
+            std::fabs(D.d("ABL.surface_temp_flux", 0.0)) > 0.0)
+            throw Error(ERR_UNSUPPORTED, "non-neutral surface temperature forcing (only ABL.surface_temp_flux = 0)");
+        if (D.i("ABL.perturb_temperature", 0)) throw Error(ERR_UNSUPPORTED, "ABL.perturb_temperature (random perturbations)");
+        z0t = D.d("ABL.surface_roughness_z0t", z0);
+        // temperature BCs (BCInterface.cpp:289-350, incflo_diffusion.cpp:71-104): a face's
+        // <face>.temperature_type overrides its velocity BC type
+        auto tbc = [&](const char* face, int zbc) {
+            const std::string key = std::string(face) + ".temperature_type";
+            std::string t = lower(D.s(key, zbc == WALLMODEL ? "wall_model" : "slip_wall"));
+            if (t == "wall_model") return 1;
+            if (t == "fixed_gradient") return 2;
+            if (t == "slip_wall" || t == "zero_gradient" || t == "symmetric_wall") return 0;
+            throw Error(ERR_UNSUPPORTED, key + " = " + t);
+        };
+        if (!g.per[2]) {
+            tzlo = tbc("zlo", g.zlo);
+            tzhi = tbc("zhi", g.zhi);
+            if (tzhi == 1) throw Error(ERR_DECK, "ABL wall models are not applicable to a zhi BC");
+            if (tzlo == 1 && g.zlo != WALLMODEL) throw Error(ERR_UNSUPPORTED, "temperature wall model without the velocity wall model");
+            if (tzlo == 2) throw Error(ERR_UNSUPPORTED, "zlo fixed_gradient temperature");
+            if (tzhi == 2) tgrad_hi = D.v("zhi.temperature").at(0);
+        }
+    }
+
     auto rd = [&](MGOpts& o, const std::string& pfx) {
         o.rtol = D.d(pfx + ".mg_rtol", o.rtol);
         o.atol = D.d(pfx + ".mg_atol", o.atol);
@@ -403,6 +475,8 @@ void Sim::setup(const std::string& text) {
     rd(nod, "nodal_proj");
     rd(dif, "diffusion");  // MLMGOptions(default prefix, custom prefix), MLMGOptions.cpp:8-13
     rd(dif, "velocity_diffusion");
+    rd(tdif, "diffusion");
+    rd(tdif, "temperature_diffusion");
 
     t.stop_time = D.d("time.stop_time", -1);
     t.max_step = D.i("time.max_step", -1);
@@ -466,6 +540,11 @@ void Sim::setup(const std::string& text) {
     def_cc(mueff, g, 1, 1); def_cc(divtau, g, 0, 3); def_cc(divtau_new, g, 0, 3);
     def_cc(conv, g, 0, 3); def_cc(act_src, g, 0, 3);
     if (!godunov) def_cc(conv_old, g, 0, 3);
+    if (has_temp) {
+        def_cc(theta, g, 3, 1); def_cc(theta_old, g, 3, 1); def_cc(theta_nph, g, 0, 1);
+        def_cc(alpha, g, 1, 1); def_cc(tsrc, g, 1, 1); def_cc(tdiff, g, 0, 1);
+        def_cc(tdiff_new, g, 0, 1); def_cc(tconv, g, 0, 1);
+    }
     const int nzn = g.n[2] + (g.per[2] ? 0 : 1);
     p.define(-1, -1, -1, g.n[0], g.n[1], nzn, 1);
     umac.define(-1, -1, -1, g.n[0] + 1, g.n[1], g.n[2], 1);
@@ -498,6 +577,32 @@ void Sim::init_fields() {
                     vel(i, j, k, 1) = -std::cos(2 * kPi * x / Lx) * std::sin(2 * kPi * y / Ly) * std::cos(2 * kPi * z / Lz);
                     vel(i, j, k, 2) = 0.0;
                 }
+    } else if (physics == "ABL" && !D.has_prefix("ks_init.")) {
+        // ABLFieldInit (src/wind_energy/ABLFieldInit.cpp:215-372), uniform-wind
+        // branch: incflo.velocity plus the sinusoidal perturbation (perturb_velocity,
+        // default on) damped by exp(-z^2 / (2 ref_height^2))
+        auto u = D.v("incflo.velocity");
+        const bool pert = D.i("ABL.perturb_velocity", 1) != 0;
+        const double refh = D.d("ABL.perturb_ref_height", 50.0), ibh = D.d("ABL.ib_height", 0.0);
+        const double Up = D.d("ABL.Uperiods", 4.0), Vp = D.d("ABL.Vperiods", 4.0);
+        const double dU = D.d("ABL.deltaU", 1.0), dV = D.d("ABL.deltaV", 1.0);
+        if (D.i("ABL.linear_profile", 0)) throw Error(ERR_UNSUPPORTED, "ABL.linear_profile");
+        const double aval = Up * 2.0 * kPi / (g.phi[1] - g.plo[1]);
+        const double bval = Vp * 2.0 * kPi / (g.phi[0] - g.plo[0]);
+        const double ufac = dU * std::exp(0.5) / refh, vfac = dV * std::exp(0.5) / refh;
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) {
+                    vel(i, j, k, 0) = u.at(0);
+                    vel(i, j, k, 1) = u.at(1);
+                    vel(i, j, k, 2) = u.at(2);
+                    if (!pert) continue;
+                    const double x = g.plo[0] + (i + 0.5) * g.dx[0], y = g.plo[1] + (j + 0.5) * g.dx[1];
+                    const double z = std::max(g.plo[2] + (k + 0.5) * g.dx[2] - ibh, 0.0);
+                    const double zl = z / refh, damp = std::exp(-0.5 * zl * zl);
+                    vel(i, j, k, 0) += ufac * damp * z * std::cos(aval * (y - g.plo[1]));
+                    vel(i, j, k, 1) += vfac * damp * z * std::cos(bval * (x - g.plo[0]));
+                }
     } else if (physics == "ABL" || physics == "FreeStream") {
         // Synthetic initial fields (not a reference feature): log-law or
         // uniform mean plus seeded uniform noise from SplitMix64 keyed on
@@ -528,6 +633,18 @@ void Sim::init_fields() {
                     }
     } else if (!physics.empty()) {
         throw Error(ERR_UNSUPPORTED, "incflo.physics " + physics);
+    }
+    if (has_temp) {  // piecewise-linear profile, tv[0] outside the segments (ABLFieldInit.cpp:318-327)
+        auto th = D.v("ABL.temperature_heights"), tv = D.v("ABL.temperature_values");
+        if (th.size() != tv.size() || th.empty()) throw Error(ERR_DECK, "ABL.temperature_heights and temperature_values differ in length");
+        for (int k = 0; k < nz; ++k) {
+            const double z = g.plo[2] + (k + 0.5) * g.dx[2];
+            double t = tv[0];
+            for (size_t m = 0; m + 1 < th.size(); ++m)
+                if (z > th[m] && z <= th[m + 1]) t = tv[m] + (z - th[m]) * ((tv[m + 1] - tv[m]) / (th[m + 1] - th[m]));
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) theta(i, j, k) = 0.0 + t;
+        }
     }
 }
 
@@ -576,7 +693,12 @@ void Sim::fill_cc_foextrap(Arr& a) const {
 // one-sided stencils src/fvm/stencils.H:166-330 at non-periodic z faces.
 void Sim::update_mueff(Arr& v) {
     const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
-    if (!smag) { mueff.setval(mu); return; }
+    // alpha_eff = mu / Pr + mu_t / Pr_t (TurbModelBase.H:28-35, LaminarModel.cpp:90-94)
+    if (!smag) {
+        mueff.setval(mu);
+        if (has_temp) alpha.setval(mu / Pr);
+        return;
+    }
     fill_vel(v);
     const double idx = 1.0 / g.dx[0], idy = 1.0 / g.dx[1], idz = 1.0 / g.dx[2];
     const double ds = std::cbrt(g.dx[0] * g.dx[1] * g.dx[2]);
@@ -597,7 +719,9 @@ void Sim::update_mueff(Arr& v) {
                 const double sr = std::sqrt(2 * gx[0] * gx[0] + 2 * gy[1] * gy[1] + 2 * gz[2] * gz[2] +
                                             (gy[0] + gx[1]) * (gy[0] + gx[1]) + (gz[1] + gy[2]) * (gz[1] + gy[2]) +
                                             (gx[2] + gz[0]) * (gx[2] + gz[0]));
-                mueff(i, j, k) = mu + rho * fac * sr;
+                const double mut = rho * fac * sr;
+                mueff(i, j, k) = mu + mut;
+                if (has_temp) alpha(i, j, k) = mu / Pr + (1.0 / Prt) * mut;
             }
 }
 
@@ -606,7 +730,7 @@ void Sim::update_mueff(Arr& v) {
 // src = rho * (-gp/rho + sum of sources); the Coriolis term reads the velocity
 // state v (Old for the predictor's Old and NPH states, New for the corrector:
 // field_impl::dof_state, src/core/FieldUtils.H:110-113).
-void Sim::compute_sources(const Arr& v) {
+void Sim::compute_sources(const Arr& v, const Arr* th) {
     const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
     const double omega = 2 * kPi / rot_period;
     const double latr = lat * kPi / 180.0;
@@ -637,6 +761,14 @@ void Sim::compute_sources(const Arr& v) {
                     for (int n = 0; n < 3; ++n) s[n] += body_force[n];
                 if (src_act)
                     for (int n = 0; n < 3; ++n) s[n] += act_src(i, j, k, n);
+                if (src_bous) {  // BoussinesqBuoyancy.cpp:22-50: g beta (T0 - T)
+                    const double fac = beta_T * (T_ref - (*th)(i, j, k));
+                    for (int n = 0; n < 3; ++n) s[n] += gravity[n] * fac;
+                }
+                if (src_ablf) {  // ABLForcing.cpp:97-139: horizontal components
+                    s[0] += ablf_force[0];
+                    s[1] += ablf_force[1];
+                }
                 for (int n = 0; n < 3; ++n) src(i, j, k, n) = rho * s[n];
             }
 }
@@ -657,6 +789,39 @@ void Sim::abl_update_umean() {
     umean[1] = sv / (nx * ny);
     vmag_mean = sm / (nx * ny);
     utau = kappa * vmag_mean / std::log(zref / z0);
+    if (has_temp) {  // theta_mean at z_ref for the heat flux (ABLWallFunction.cpp:206-207)
+        double st = 0;
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) st += theta(i, j, 0);
+        theta_mean = st / (nx * ny);
+    }
+}
+
+// ABL::pre_advance_work -> ABLForcing::set_mean_velocities (ABL.cpp:176-205,
+// ABLForcing.H:37-64): plane averages of u and v interpolated to the forcing
+// height (FieldPlaneAveraging.cpp:78-96,151-164), force = (target - mean) / dt.
+void Sim::abl_forcing_update() {
+    if (!src_ablf) return;
+    const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+    std::vector<double> ua(nz), va(nz);
+    for (int k = 0; k < nz; ++k) {
+        double su = 0, sv = 0;
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) { su += vel(i, j, k, 0); sv += vel(i, j, k, 1); }
+        ua[k] = su / (nx * ny);
+        va[k] = sv / (nx * ny);
+    }
+    int ind = 0;
+    double c = 0.0;
+    const double x = ablf_height, xlo = g.plo[2], dz = g.dx[2];
+    if (x > xlo + 0.5 * dz) {
+        ind = (int)std::floor((x - xlo) / dz - 0.5);
+        c = (x - (xlo + (ind + 0.5) * dz)) / dz;
+    }
+    if (ind + 1 >= nz) { ind = nz - 2; c = 1.0; }
+    const double mu0 = ua[ind] * (1.0 - c) + ua[ind + 1] * c, mv0 = va[ind] * (1.0 - c) + va[ind + 1] * c;
+    ablf_force[0] = (ablf_target[0] - mu0) / t.dt[0];
+    ablf_force[1] = (ablf_target[1] - mv0) / t.dt[0];
 }
 
 // Wall-normal velocity gradient imposed at z-lo for the tangential components:
@@ -844,14 +1009,15 @@ static int line(const Arr& a, const Geo& g, int d, int i, int j, int k, int n, d
     return (d == 2 && !g.per[2]) ? g.n[2] : -1;
 }
 
-// SetXEdgeBCs restricted to z walls: tangential components take the interior
-// state, the normal component is Dirichlet 0 on both sides.
-static void zedge_bc(const Geo& g, int k, int n, double& lo, double& hi) {
+// SetXEdgeBCs restricted to z walls: tangential components (and hoextrap
+// scalars) take the interior state, the normal component is Dirichlet 0 on
+// both sides.
+static void zedge_bc(const Geo& g, int k, bool normal, double& lo, double& hi) {
     if (g.per[2]) return;
     if (k == 0) {
-        if (n == 2) { lo = 0.0; hi = 0.0; } else lo = hi;
+        if (normal) { lo = 0.0; hi = 0.0; } else lo = hi;
     } else if (k == g.n[2]) {
-        if (n == 2) { lo = 0.0; hi = 0.0; } else hi = lo;
+        if (normal) { lo = 0.0; hi = 0.0; } else hi = lo;
     }
 }
 
@@ -879,10 +1045,10 @@ static void compute_traces(const Arr& q, const Geo& g, double dt, int mode, cons
     const int nz = g.n[2];
     const int klo = g.per[2] ? -1 : 0, khi = g.per[2] ? nz : nz - 1;
     for (int d = 0; d < 3; ++d) {
-        T.Im[d].define(-1, -1, klo, g.n[0], g.n[1], khi, 3);
-        T.Ip[d].define(-1, -1, klo, g.n[0], g.n[1], khi, 3);
+        T.Im[d].define(-1, -1, klo, g.n[0], g.n[1], khi, q.nc);
+        T.Ip[d].define(-1, -1, klo, g.n[0], g.n[1], khi, q.nc);
         const double dtdx = dt / g.dx[d];
-        for (int n = 0; n < 3; ++n)
+        for (int n = 0; n < q.nc; ++n)
 #pragma omp parallel for collapse(2)
             for (int k = klo; k <= khi; ++k)
                 for (int j = -1; j <= g.n[1]; ++j)
@@ -970,7 +1136,7 @@ void Sim::premac(double dt) {
                         if (!(wall && k == 0)) l = T.Ip[d](c[0], c[1], c[2], n);
                         c[d] += 1;
                         if (!(wall && k == nz)) h = T.Im[d](c[0], c[1], c[2], n);
-                        if (d == 2) zedge_bc(G, k, n, l, h);
+                        if (d == 2) zedge_bc(G, k, n == 2, l, h);
                         lo[d](i, j, k, n) = l;
                         hi[d](i, j, k, n) = h;
                         if (n == d) A(i, j, k) = riemann(l, h);
@@ -1017,7 +1183,7 @@ void Sim::premac(double dt) {
                         l -= cb * (ad[b](cq[0], cq[1], cq[2]) + ad[b](cl[0], cl[1], cl[2])) *
                              (edge[b](cq[0], cq[1], cq[2], n) - edge[b](cl[0], cl[1], cl[2], n));
                     }
-                    if (a == 2) zedge_bc(G, k, n, l, h);
+                    if (a == 2) zedge_bc(G, k, n == 2, l, h);
                     R(i, j, k) = upwind(ad[a](i, j, k), l, h);
                 }
     }
@@ -1060,7 +1226,7 @@ void Sim::premac(double dt) {
                     cl[d] -= 1;
                     if (!(wall && k == 0)) stl = side(cl, lo[d](i, j, k, d));
                     if (!(wall && k == nz)) sth = side(c, hi[d](i, j, k, d));
-                    if (d == 2) zedge_bc(G, k, d, stl, sth);
+                    if (d == 2) zedge_bc(G, k, d == 2, stl, sth);
                     (*mac[d])(i, j, k) = riemann(stl, sth);
                     (void)nd;
                 }
@@ -1237,31 +1403,216 @@ void Sim::mac_project() {
     fill_periodic(wmac, g, fz);
 }
 
+// ---- temperature transport (Godunov; src/incflo_advance.cpp:296-341) -----------------------------
+// hoextrap ghosts at z walls (BCScalar::set_bcrec, BCInterface.cpp:289-350), periodic wrap
+void Sim::fill_scalar(Arr& a) const {
+    const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+    const int ng = -a.lo[2];
+    if (!g.per[2])
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const double lo = 0.125 * (15 * a(i, j, 0) - 10 * a(i, j, 1) + 3 * a(i, j, 2));
+                const double hi = 0.125 * (15 * a(i, j, nz - 1) - 10 * a(i, j, nz - 2) + 3 * a(i, j, nz - 3));
+                for (int m = 1; m <= ng; ++m) { a(i, j, -m) = lo; a(i, j, nz - 1 + m) = hi; }
+            }
+    const int cc[3] = {0, 0, 0};
+    fill_periodic(a, g, cc);
+}
+
+// Wall-normal temperature gradient at z-lo, rho q / alpha_eff (ABLTempWallFunc,
+// ABLWallFunction.cpp:392-480) with the heat flux q of the shear-stress model
+// (ShearStress.H:22-167); neutral surface (surface_temp_flux = 0): the surface
+// temperature equals theta_mean (MOData.cpp:66-71) and phi_h = ln(z_ref / z0t).
+void Sim::theta_wall_gradient(std::vector<double>& gz) const {
+    const int nx = g.n[0], ny = g.n[1];
+    gz.assign((size_t)nx * ny, 0.0);
+    if (tzlo != 1) return;
+    const double phi_h = std::log(zref / z0t);
+    const double ts = theta_mean;
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            const double u = vel_old(i, j, 0, 0), v = vel_old(i, j, 0, 1);
+            const double wspd = std::sqrt(u * u + v * v);
+            const double th = theta_old(i, j, 0);
+            double q;
+            if (shear_type == "moeng") {
+                const double term1 = utau * kappa / (vmag_mean * phi_h);
+                q = term1 * ((th - theta_mean) * vmag_mean + (theta_mean - ts) * wspd);
+            } else if (shear_type == "constant") {
+                q = utau * kappa / phi_h * (theta_mean - ts);
+            } else {  // local, schumann
+                q = utau * kappa / phi_h * (th - ts);
+            }
+            gz[(size_t)j * nx + i] = rho * q / alpha(i, j, 0);
+        }
+}
+
+// div(alpha grad theta): MLABecLaplacian apply with alpha 0, beta -1, face
+// diffusivity the mean of the two cells (the cell value on domain faces), z
+// boundaries through one ghost layer: Neumann 0 (slip wall), the wall-model
+// gradient at z-lo, the fixed gradient at z-hi (incflo_diffusion.cpp:71-104).
+void Sim::tdiff_op(const Arr& th_in, Arr& out) {
+    const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+    Arr q;
+    def_cc(q, g, 1, 1);
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) q(i, j, k) = th_in(i, j, k);
+    std::vector<double> gz;
+    theta_wall_gradient(gz);
+    if (!g.per[2])
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                q(i, j, -1) = q(i, j, 0) - (tzlo == 1 ? gz[(size_t)j * nx + i] : 0.0) * g.dx[2];
+                q(i, j, nz) = q(i, j, nz - 1) + (tzhi == 2 ? tgrad_hi : 0.0) * g.dx[2];
+            }
+    const int cc[3] = {0, 0, 0};
+    fill_periodic(q, g, cc);
+    Arr a;
+    def_cc(a, g, 1, 1);
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) a(i, j, k) = alpha(i, j, k);
+    fill_cc_foextrap(a);
+    const double dx = g.dx[0], dy = g.dx[1], dz = g.dx[2];
+#pragma omp parallel for collapse(2)
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                auto fx = [&](int ii) { return 0.5 * (a(ii - 1, j, k) + a(ii, j, k)) * (q(ii, j, k) - q(ii - 1, j, k)) / dx; };
+                auto fy = [&](int jj) { return 0.5 * (a(i, jj - 1, k) + a(i, jj, k)) * (q(i, jj, k) - q(i, jj - 1, k)) / dy; };
+                auto fz = [&](int kk) {
+                    double af;
+                    if (!g.per[2] && kk == 0) af = a(i, j, 0);
+                    else if (!g.per[2] && kk == nz) af = a(i, j, nz - 1);
+                    else af = 0.5 * (a(i, j, kk - 1) + a(i, j, kk));
+                    return af * (q(i, j, kk) - q(i, j, kk - 1)) / dz;
+                };
+                out(i, j, k) = (fx(i + 1) - fx(i)) / dx + (fy(j + 1) - fy(j)) / dy + (fz(k + 1) - fz(k)) / dz;
+            }
+}
+
+// rho theta - dtd div(alpha grad theta) = rho theta_rhs (DiffSolverIface::linsys_solve
+// with MLABecLaplacian), solved by Jacobi iterations to MLMG's target
+void Sim::tdiffuse_solve(double dtd) {
+    const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+    Arr b, L, R, Dg;
+    def_cc(b, g, 0, 1); def_cc(L, g, 0, 1); def_cc(R, g, 0, 1); def_cc(Dg, g, 0, 1);
+    Arr a;
+    def_cc(a, g, 1, 1);
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) a(i, j, k) = alpha(i, j, k);
+    fill_cc_foextrap(a);
+    const double ih2[3] = {1.0 / (g.dx[0] * g.dx[0]), 1.0 / (g.dx[1] * g.dx[1]), 1.0 / (g.dx[2] * g.dx[2])};
+    double bnorm = 0;
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const double c0 = a(i, j, k);
+                double s = (0.5 * (a(i - 1, j, k) + c0) + 0.5 * (a(i + 1, j, k) + c0)) * ih2[0] +
+                           (0.5 * (a(i, j - 1, k) + c0) + 0.5 * (a(i, j + 1, k) + c0)) * ih2[1];
+                const double zlo = (!g.per[2] && k == 0) ? 0.0 : 0.5 * (a(i, j, k - 1) + c0);
+                const double zhi = (!g.per[2] && k == nz - 1) ? 0.0 : 0.5 * (a(i, j, k + 1) + c0);
+                s += (zlo + zhi) * ih2[2];
+                Dg(i, j, k) = rho + dtd * s;
+                b(i, j, k) = rho * theta(i, j, k);
+                bnorm = std::max(bnorm, std::fabs(b(i, j, k)));
+            }
+    auto residual = [&]() {
+        tdiff_op(theta, L);
+        double rn = 0;
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) {
+                    const double r = b(i, j, k) - rho * theta(i, j, k) + dtd * L(i, j, k);
+                    R(i, j, k) = r;
+                    rn = std::max(rn, std::fabs(r));
+                }
+        if (!std::isfinite(rn)) throw Error(ERR_NONFINITE, "temperature diffusion solve diverged");
+        return rn;
+    };
+    double rn = residual();
+    const double target = std::max(tdif.atol, tdif.rtol * std::max(bnorm, rn));
+    int it = 0;
+    while (rn > target) {
+        if (++it > 200000) throw Error(ERR_NOT_CONVERGED, "oracle Jacobi iterations of the temperature solve did not converge");
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) theta(i, j, k) += R(i, j, k) / Dg(i, j, k);
+        rn = residual();
+    }
+    tdiff_iters = it;
+}
+
+// The scalar part of ApplyPredictor (incflo_advance.cpp:296-341) after the MAC
+// projection: Godunov fluxes of rho theta with the forces src + diff
+// (AdvOp_Godunov.H:114-329), sources at NPH (none), predictor_rhs, explicit RK2
+// correction or the diffusion solve, theta_nph = (theta_old + theta) / 2.
+// diff_term(Old) (tdiff) and alpha_eff are formed before the MAC projection.
+void Sim::temperature_predictor(double dt) {
+    const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+    Arr q, fq;
+    def_cc(q, g, 3, 1);
+    def_cc(fq, g, 1, 1);
+    fill_scalar(theta_old);
+    for (size_t m = 0; m < q.d.size(); ++m) q.d[m] = rho * theta_old.d[m];
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) fq(i, j, k) = tsrc(i, j, k) + tdiff(i, j, k);
+    fill_cc_foextrap(fq);
+    advect_field(q, fq, -1, dt, tconv);
+    tsrc.setval(0.0);  // compute_source_term(NPH): the deck has no temperature sources
+    const double fac = diff_type == 0 ? 1.0 : (diff_type == 1 ? 0.5 : 0.0);
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i)
+                theta(i, j, k) = (rho * theta_old(i, j, k) + dt * (tconv(i, j, k) + tsrc(i, j, k) + fac * tdiff(i, j, k))) / rho;
+    if (diff_type == 0) {
+        tdiff_op(theta, tdiff_new);
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) theta(i, j, k) += 0.5 * dt * (tdiff_new(i, j, k) - tdiff(i, j, k)) / rho;
+    } else {
+        tdiffuse_solve(diff_type == 2 ? dt : 0.5 * dt);
+    }
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) theta_nph(i, j, k) = 0.5 * theta_old(i, j, k) + 0.5 * theta(i, j, k);
+}
+
 // ---- post-MAC advective fluxes ----------------------------------------------------------------------
 // HydroUtils::ComputeFluxesOnBoxFromState + ComputeDivergence
-// (icns_advection.H:250-442) with q = rho u, conservative transverse terms
-// (dt/3 corner corrections), forces added at the end, flux = u_mac * q_edge,
-// conv = -div(flux).
+// (icns_advection.H:250-442 for q = rho u; AdvOp_Godunov.H:114-329 for
+// q = rho theta of a scalar) with conservative transverse terms (dt/3 corner
+// corrections), forces added at the end, flux = u_mac * q_edge, conv =
+// -div(flux).  q and fq carry three ghost layers and one; component `normal`
+// (2 for the velocity, -1 for a scalar) is the Dirichlet-0 one at z walls.
 void Sim::advection(double dt) {
-    const Geo& G = g;
-    const int nx = G.n[0], ny = G.n[1], nz = G.n[2];
     Arr q, fq;
-    def_cc(q, G, 3, 3);
-    def_cc(fq, G, 1, 3);
+    def_cc(q, g, 3, 3);
+    def_cc(fq, g, 1, 3);
     fill_vel(vel_old);
     for (size_t m = 0; m < q.d.size(); ++m) q.d[m] = rho * vel_old.d[m];
     fill_cc_foextrap(forces);
     for (size_t m = 0; m < fq.d.size(); ++m) fq.d[m] = rho * forces.d[m];
+    advect_field(q, fq, 2, dt, conv);
+}
+
+void Sim::advect_field(const Arr& q, const Arr& fq, int normal, double dt, Arr& out) {
+    const Geo& G = g;
+    const int nx = G.n[0], ny = G.n[1], nz = G.n[2];
+    const int nc = q.nc;
     const Arr* fv[3] = {&umac, &vmac, &wmac};
     Traces T;
     compute_traces(q, G, dt, 1, nullptr, fv, T);
     Arr lo[3], hi[3], edge[3];
     for (int d = 0; d < 3; ++d) {
-        def_face(lo[d], G, d, 3);
-        def_face(hi[d], G, d, 3);
-        def_face(edge[d], G, d, 3);
+        def_face(lo[d], G, d, nc);
+        def_face(hi[d], G, d, nc);
+        def_face(edge[d], G, d, nc);
         Arr& A = lo[d];
-        for (int n = 0; n < 3; ++n)
+        for (int n = 0; n < nc; ++n)
 #pragma omp parallel for collapse(2)
             for (int k = A.lo[2]; k <= A.hi[2]; ++k)
                 for (int j = A.lo[1]; j <= A.hi[1]; ++j)
@@ -1273,7 +1624,7 @@ void Sim::advection(double dt) {
                         if (!(wall && k == 0)) l = T.Ip[d](c[0], c[1], c[2], n);
                         c[d] += 1;
                         if (!(wall && k == nz)) h = T.Im[d](c[0], c[1], c[2], n);
-                        if (d == 2) zedge_bc(G, k, n, l, h);
+                        if (d == 2) zedge_bc(G, k, n == normal, l, h);
                         lo[d](i, j, k, n) = l;
                         hi[d](i, j, k, n) = h;
                         edge[d](i, j, k, n) = upwind((*fv[d])(i, j, k), l, h);
@@ -1284,10 +1635,10 @@ void Sim::advection(double dt) {
     for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 3; ++b) {
             if (a == b) continue;
-            def_trans(tr[a][b], G, a, b, 3);
+            def_trans(tr[a][b], G, a, b, nc);
             Arr& R = tr[a][b];
             const double cb = dt / (3.0 * G.dx[b]);
-            for (int n = 0; n < 3; ++n)
+            for (int n = 0; n < nc; ++n)
 #pragma omp parallel for collapse(2)
                 for (int k = R.lo[2]; k <= R.hi[2]; ++k)
                     for (int j = R.lo[1]; j <= R.hi[1]; ++j)
@@ -1306,20 +1657,20 @@ void Sim::advection(double dt) {
                             int cl[3] = {i, j, k};
                             cl[a] -= 1;
                             if (!(wall && k == 0)) l += corr(cl);
-                            if (a == 2) zedge_bc(G, k, n, l, h);
+                            if (a == 2) zedge_bc(G, k, n == normal, l, h);
                             R(i, j, k, n) = upwind((*fv[a])(i, j, k), l, h);
                         }
         }
     // final states and fluxes
     Arr F[3];
-    F[0].define(0, 0, 0, nx, ny - 1, nz - 1, 3);
-    F[1].define(0, 0, 0, nx - 1, ny, nz - 1, 3);
-    F[2].define(0, 0, 0, nx - 1, ny - 1, nz, 3);
+    F[0].define(0, 0, 0, nx, ny - 1, nz - 1, nc);
+    F[1].define(0, 0, 0, nx - 1, ny, nz - 1, nc);
+    F[2].define(0, 0, 0, nx - 1, ny - 1, nz, nc);
     for (int d = 0; d < 3; ++d) {
         const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
         const double c1 = dt / (2.0 * G.dx[b1]), c2 = dt / (2.0 * G.dx[b2]);
         Arr& R = F[d];
-        for (int n = 0; n < 3; ++n)
+        for (int n = 0; n < nc; ++n)
 #pragma omp parallel for collapse(2)
             for (int k = 0; k <= R.hi[2]; ++k)
                 for (int j = 0; j <= R.hi[1]; ++j)
@@ -1346,7 +1697,7 @@ void Sim::advection(double dt) {
                         double stl = 0, sth = 0;
                         if (!(wall && k == 0)) stl = side(cl, lo[d](i, j, k, n));
                         if (!(wall && k == nz)) sth = side(c, hi[d](i, j, k, n));
-                        if (d == 2) zedge_bc(G, k, n, stl, sth);
+                        if (d == 2) zedge_bc(G, k, n == normal, stl, sth);
                         const double um = (*fv[d])(i, j, k);
                         double st = (um >= 0.0) ? stl : sth;
                         if (std::fabs(um) < kSmallVel) st = 0.5 * (stl + sth);
@@ -1357,8 +1708,8 @@ void Sim::advection(double dt) {
     for (int k = 0; k < nz; ++k)
         for (int j = 0; j < ny; ++j)
             for (int i = 0; i < nx; ++i)
-                for (int n = 0; n < 3; ++n)
-                    conv(i, j, k, n) = -((F[0](i + 1, j, k, n) - F[0](i, j, k, n)) / G.dx[0] +
+                for (int n = 0; n < nc; ++n)
+                    out(i, j, k, n) = -((F[0](i + 1, j, k, n) - F[0](i, j, k, n)) / G.dx[0] +
                                          (F[1](i, j + 1, k, n) - F[1](i, j, k, n)) / G.dx[1] +
                                          (F[2](i, j, k + 1, n) - F[2](i, j, k, n)) / G.dx[2]);
 }
@@ -1762,19 +2113,25 @@ void Sim::apply_predictor(bool incremental) {
     const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
     const double dt = t.dt[0];
     update_mueff(vel_old);
-    compute_sources(vel_old);
+    const Arr* th_old = has_temp ? &theta_old : nullptr;
+    compute_sources(vel_old, th_old);  // BoussinesqBuoyancy reads theta at Old (phi_state)
     divtau_op(vel_old, divtau);  // divtau with u = Old (copied into New)
     for (int n = 0; n < 3; ++n)
 #pragma omp parallel for collapse(2)
         for (int k = 0; k < nz; ++k)
             for (int j = 0; j < ny; ++j)
                 for (int i = 0; i < nx; ++i) forces(i, j, k, n) = (src(i, j, k, n) + divtau(i, j, k, n)) / rho;
+    if (has_temp) {  // temperature sources at Old (none) and diff_term(Old)
+        tsrc.setval(0.0);
+        tdiff_op(theta_old, tdiff);
+    }
     premac(dt);
     mac_project();
+    if (has_temp) temperature_predictor(dt);
     advection(dt);
-    // compute_source_term(NPH) reproduces src (Old velocity, same gp);
-    // compute_diffusion_term(Old) reproduces divtau.
-    compute_sources(vel_old);
+    // compute_source_term(NPH): Coriolis reads the Old velocity, BoussinesqBuoyancy
+    // theta at n+1/2; compute_diffusion_term(Old) reproduces divtau.
+    compute_sources(vel_old, has_temp ? &theta_nph : nullptr);
     // predictor_rhs (CompRHSOps.H:32-141): diffusion factor 1 explicit, 1/2 Crank-Nicolson, 0 implicit
     const double fac = diff_type == 0 ? 1.0 : (diff_type == 1 ? 0.5 : 0.0);
     for (int n = 0; n < 3; ++n)
@@ -2072,10 +2429,12 @@ void Sim::init_data() {
     if (initial_iterations > 0) {
         compute_dt();
         vel_old = vel;
+        if (has_temp) theta_old = theta;
         for (int it = 0; it < initial_iterations; ++it) {
             if (godunov) apply_predictor(true);
             else mol_predictor(true);  // init.cpp:153-159: ApplyPredictor only, for both schemes
             vel = vel_old;
+            if (has_temp) theta = theta_old;
         }
     }
 }
@@ -2084,9 +2443,11 @@ int Sim::step_once() {
     if (!t.new_timestep()) return DONE;
     compute_dt();
     t.advance_time();
-    abl_update_umean();  // ABL::pre_advance_work
-    actuator_update();   // Actuator::pre_advance_work
-    vel_old = vel;       // prepare_time_step / advance_states
+    abl_update_umean();    // ABL::pre_advance_work
+    abl_forcing_update();
+    actuator_update();     // Actuator::pre_advance_work
+    vel_old = vel;         // prepare_time_step / advance_states
+    if (has_temp) theta_old = theta;
     if (godunov) {
         apply_predictor(false);
     } else {  // incflo::advance (src/incflo_advance.cpp:63-79)
@@ -2144,6 +2505,13 @@ static kso::Arr* field_ptr(Sim& s, const std::string& name, int& nodal_z, int& f
     if (name == "diff_term_new") return &s.divtau_new;
     if (name == "conv_term") return &s.conv;
     if (name == "conv_term_old") return s.godunov ? nullptr : &s.conv_old;
+    if (s.has_temp) {
+        if (name == "temperature") return &s.theta;
+        if (name == "temperature_old") return &s.theta_old;
+        if (name == "temperature_mueff") return &s.alpha;
+        if (name == "temperature_conv_term") return &s.tconv;
+        if (name == "temperature_diff_term") return &s.tdiff;
+    }
     if (name == "actuator_src_term") return &s.act_src;
     if (name == "u_mac") { fdir = 0; return &s.umac; }
     if (name == "v_mac") { fdir = 1; return &s.vmac; }
@@ -2181,10 +2549,22 @@ int kso_compute_dt(void* h, double* dt) {
 }
 
 int kso_pre_advance(void* h) {
-    return guard(h, [](Sim& s) { s.t.advance_time(); s.abl_update_umean(); s.actuator_update(); return 0; });
+    return guard(h, [](Sim& s) {
+        s.t.advance_time();
+        s.abl_update_umean();
+        s.abl_forcing_update();
+        s.actuator_update();
+        return 0;
+    });
 }
 
-int kso_prepare_time_step(void* h) { return guard(h, [](Sim& s) { s.vel_old = s.vel; return 0; }); }
+int kso_prepare_time_step(void* h) {
+    return guard(h, [](Sim& s) {
+        s.vel_old = s.vel;
+        if (s.has_temp) s.theta_old = s.theta;
+        return 0;
+    });
+}
 
 int kso_apply_predictor(void* h, int incremental, int fpi) {
     return guard(h, [&](Sim& s) {
@@ -2274,6 +2654,10 @@ double kso_get_scalar(void* h, const char* name) {
     if (n == "diff_res0") return s.diff_res0;
     if (n == "diff_res") return s.diff_res;
     if (n == "diff_rhs_norm") return s.diff_bnorm;
+    if (n == "temperature_diff_iters") return s.tdiff_iters;
+    if (n == "theta_mean") return s.theta_mean;
+    if (n == "abl_forcing_x") return s.ablf_force[0];
+    if (n == "abl_forcing_y") return s.ablf_force[1];
     if (n == "utau") return s.utau;
     if (n == "ke") return s.ke();
     if (n == "cfl") return s.t.cur_cfl;
