@@ -307,6 +307,7 @@ def our_arm(args, rank, world, local_rank):
                  "note": "FP32 advection and multigrid cycles, FP64 residuals / defect correction / RHS / velocity update"}
     mol = None if args.no_mol else mol_bench(args, torch, ks, decks, nx, ny, nz, world, rank)
     cn = None if args.no_mol else cn_bench(args, torch, ks, decks, nx, ny, nz, world, rank)
+    strat = None if args.no_mol else stratified_bench(args, torch, ks, decks, nx, ny, nz, world, rank)
     adj = None if args.no_adjoint else adjoint_bench(args, torch, ks, decks)
     # the reference's own CPU-runnable case: Taylor-Green vortex 64^3, Re 1600, CFL 0.5, 20 steps
     tg = ks.Incflo(decks.tgv(64, steps=10 ** 6))
@@ -325,7 +326,7 @@ def our_arm(args, rank, world, local_rank):
            "unit": UNIT, "ms_per_step": tms}
     del tg
     return dict(value=value, ms=ms_max, cells=cells, launches=launches, dominant=dominant, dom=dom, clocks=clk, e2e=e2e, fp64_peak=fp64_peak,
-                mac=statistics.mean(mac_it), nodal=statistics.mean(nod_it), size=(nx, ny, nz), mixed=mixed, adjoint=adj, tgv=tgv, mol=mol, cn=cn)
+                mac=statistics.mean(mac_it), nodal=statistics.mean(nod_it), size=(nx, ny, nz), mixed=mixed, adjoint=adj, tgv=tgv, mol=mol, cn=cn, strat=strat)
 
 
 def variant_bench(args, torch, ks, deck, workload, world, rank, label):
@@ -384,6 +385,18 @@ def cn_bench(args, torch, ks, decks, nx, ny, nz, world, rank):
     d = decks.abl(nx, ny, nz, steps=10 ** 9).replace("incflo.diffusion_type = 0", "incflo.diffusion_type = 1")
     return variant_bench(args, torch, ks, d, "ABL %dx%dx%d, Godunov, Crank-Nicolson diffusion, CFL 0.9, FP64" % (nx, ny, nz), world, rank,
                          "Crank-Nicolson")
+
+
+def stratified_bench(args, torch, ks, decks, nx, ny, nz, world, rank):
+    """The reference's stratified ABL configuration (abl_godunov: temperature
+    transport, Boussinesq buoyancy, Coriolis, ABLForcing, heat-flux wall model,
+    Crank-Nicolson diffusion of velocity and temperature) on the ABL grid:
+    20 m cells, the 3 K/km gradient continued to the top."""
+    d = decks.abl_temperature((nx, ny, nz), steps=10 ** 9, diffusion_type=1, fixed_dt=-0.5, size=(20.0 * nx, 20.0 * ny, 20.0 * nz),
+                              heights=(650.0, 750.0, 20.0 * nz), values=(300.0, 308.0, 308.0 + 0.003 * (20.0 * nz - 750.0)))
+    out = variant_bench(args, torch, ks, d, "stratified ABL %dx%dx%d (20 m cells), temperature + Boussinesq + ABLForcing, Crank-Nicolson, CFL 0.95, "
+                        "FP64" % (nx, ny, nz), world, rank, "stratified ABL")
+    return out
 
 
 def adjoint_bench(args, torch, ks, decks):
@@ -640,7 +653,8 @@ def main():
                          "launches": n_l, "avg_launch_us": 1e3 * ms_l / n_l if n_l else None,
                          "algorithmic_bytes_per_launch": by_l / n_l if n_l else None},
             "gpu_launches": r["launches"], "clocks": r["clocks"], "e2e": r["e2e"], "mixed_precision": r["mixed"],
-            "adjoint": r["adjoint"], "tgv64": r["tgv"], "mol": r["mol"], "crank_nicolson": r["cn"]}
+            "adjoint": r["adjoint"], "tgv64": r["tgv"], "mol": r["mol"], "crank_nicolson": r["cn"],
+            "stratified_abl": r["strat"]}
     # The FP64 path is bound by FP64 issue on this GPU (profiles/k_nd_col_abl256_fp64.md): report the
     # dominant kernel against the FMA peak measured live by ks_fma_peak as well.
     fl = FP64_FLOPS_PER_BYTE.get(r["dominant"])

@@ -255,13 +255,17 @@ ks.precision = {precision}
     return deck, lo, hi, cts
 
 
-def abl_temperature(n=(48, 48, 48), steps=10, diffusion_type=0, fixed_dt=-0.5, cfl=0.95, use_force_cfl=0):
+def abl_temperature(n=(48, 48, 48), steps=10, diffusion_type=0, fixed_dt=-0.5, cfl=0.95, use_force_cfl=0, size=(1000.0, 1000.0, 1000.0),
+                    heights=(650.0, 750.0, 1000.0), values=(300.0, 308.0, 308.75)):
     """Stably stratified ABL with temperature transport, the configuration of
-    the reference's abl_godunov regression decks (1000 m cube, Boussinesq
-    buoyancy about 300 K, Coriolis at 41.3 deg, ABLForcing at 90 m toward
-    (6.128, 5.142) m/s, Moeng wall model, capping inversion 650-750 m with a
-    3 K/km gradient imposed at the top), PPM Godunov."""
+    the reference's abl_godunov regression decks (by default the 1000 m cube,
+    Boussinesq buoyancy about 300 K, Coriolis at 41.3 deg, ABLForcing at 90 m
+    toward (6.128, 5.142) m/s, Moeng wall model, capping inversion 650-750 m
+    with a 3 K/km gradient imposed at the top), PPM Godunov."""
     nx, ny, nz = n
+    lx, ly, lz = size
+    hs = " ".join(repr(float(h)) for h in heights)
+    vs = " ".join(repr(float(v)) for v in values)
     return f"""
 time.max_step = {steps}
 time.fixed_dt = {fixed_dt}
@@ -283,14 +287,14 @@ ICNS.source_terms = BoussinesqBuoyancy CoriolisForcing ABLForcing
 CoriolisForcing.latitude = 41.3
 ABLForcing.abl_forcing_height = 90
 incflo.velocity = 6.128355544951824 5.142300877492314 0.0
-ABL.temperature_heights = 650.0 750.0 1000.0
-ABL.temperature_values = 300.0 308.0 308.75
+ABL.temperature_heights = {hs}
+ABL.temperature_values = {vs}
 ABL.kappa = .41
 ABL.surface_roughness_z0 = 0.15
 amr.n_cell = {nx} {ny} {nz}
 amr.max_level = 0
 geometry.prob_lo = 0. 0. 0.
-geometry.prob_hi = 1000. 1000. 1000.
+geometry.prob_hi = {lx} {ly} {lz}
 geometry.is_periodic = 1 1 0
 zlo.type = "wall_model"
 zhi.type = "slip_wall"

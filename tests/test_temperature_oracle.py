@@ -124,4 +124,4 @@ def test_deck_checks(oracle_mod):
     with pytest.raises(oracle_mod.OracleError):
         oracle_mod.Oracle(base + "ABL.surface_temp_flux = 0.05\n")
     with pytest.raises(oracle_mod.OracleError):
-        oracle_mod.Oracle(base.replace("ABL.temperature_heights = 650.0 750.0 1000.0\n", ""))
+        oracle_mod.Oracle(base.replace("ABL.temperature_heights = 650.0 750.0 1000.0\n", ""))  # buoyancy without temperature
