@@ -20,6 +20,8 @@
  *   ks_evolve                  incflo::Evolve time loop                        src/incflo.cpp:338-411
  *   ks_set_field / ks_get_field  FieldRepo field access by name              src/core/FieldRepo.H:139-173
  *   ks_last_solver_stats       io::print_mlmg_info                            src/utilities/console_io.cpp:178-186
+ *   ks_write_plotfile / ks_write_checkpoint / ks_write_outputs  IOManager      src/utilities/IOManager.cpp:135-330
+ *   ks_read_checkpoint         incflo::ReadCheckpointFile                      src/utilities/io.cpp:11-220
  *
  * Deck: ParmParse text ("prefix.key = values" lines), the reference's keys.
  * Field exchange: valid region only, structure of arrays, x fastest, then y,
@@ -92,6 +94,29 @@ int ks_last_solver_stats(const ks_handle* h, ks_mg_stats* stats);
 int ks_set_precision(ks_handle* h, int precision);
 int ks_synchronize(ks_handle* h);
 int ks_kernel_launches(const ks_handle* h, long long* count);
+
+/* Plot files, checkpoints and restart (IOManager, src/utilities/IOManager.cpp:34-330;
+ * incflo::ReadCheckpointFile, src/utilities/io.cpp:11-220).
+ * ks_write_plotfile: an AMReX plot file directory (HyperCLaw-V1.1 Header,
+ * Level_0/Cell_H + Cell_D_00000) with the reference's default variables
+ * (density, gp, p, velocity; mu_turb, velocity_mueff with Smagorinsky;
+ * temperature [+ temperature_mueff]) at the current step and time.
+ * ks_write_checkpoint / ks_read_checkpoint: the reference's checkpoint layout
+ * (Header + one VisMF MultiFab per restart field); reading restores the step,
+ * the time, dt_nm1 / dt_nm2 and the fields; a domain that is an integer
+ * multiple of the checkpoint's replicates it.  The deck key io.restart_file
+ * makes ks_init_data restart instead of initialising.
+ * ks_write_outputs: the files due at the current step under time.plot_interval
+ * and time.checkpoint_interval (prefixes io.plot_file, io.check_file; last != 0:
+ * the end-of-run rules), as incflo::Evolve writes them.
+ * ks_plotfile_write_host: the plot file writer on host data only (no device):
+ * nvars cell fields of n[0]*n[1]*n[2] values each, component-major, x fastest. */
+int ks_write_plotfile(ks_handle* h, const char* path);
+int ks_write_checkpoint(ks_handle* h, const char* path);
+int ks_read_checkpoint(ks_handle* h, const char* path);
+int ks_write_outputs(ks_handle* h, int last);
+int ks_plotfile_write_host(const char* path, int nvars, const char* const* names, const int n[3], const double prob_lo[3],
+                           const double prob_hi[3], double time, int step, const double* data);
 
 /* Reverse mode of the advance (no counterpart in the reference: the adjoint
  * entry points ks_adjoint_step / ks_set_objective_box / ks_get_ct_gradient

@@ -6,6 +6,7 @@ reference's ``incflo`` operator surface as :class:`Incflo`.  There is no CPU
 fallback: if the library is missing or no CUDA device is visible, the calls
 raise.
 """
-from .incflo import Incflo, KsError, library_path, load_library, build_library, fma_peak, checkpoint_cost, FIELDS
+from .incflo import Incflo, KsError, library_path, load_library, build_library, fma_peak, checkpoint_cost, FIELDS, write_plotfile_host
 
-__all__ = ["Incflo", "KsError", "library_path", "load_library", "build_library", "fma_peak", "checkpoint_cost", "FIELDS"]
+__all__ = ["Incflo", "KsError", "library_path", "load_library", "build_library", "fma_peak", "checkpoint_cost", "FIELDS",
+           "write_plotfile_host"]

@@ -13,7 +13,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
-SOURCES = ["ks_host.cpp", "ks_adjoint_host.cpp", "ks_kernels.cu", "ks_godunov.cu", "ks_mol.cu", "ks_implicit.cu", "ks_temperature.cu", "ks_mg.cu", "ks_adjoint.cu", "ks_noalloc.cu", "ks_probe.cu"]
+SOURCES = ["ks_host.cpp", "ks_adjoint_host.cpp", "ks_io.cpp", "ks_kernels.cu", "ks_godunov.cu", "ks_mol.cu", "ks_implicit.cu", "ks_temperature.cu", "ks_mg.cu", "ks_adjoint.cu", "ks_noalloc.cu", "ks_probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3"]
 

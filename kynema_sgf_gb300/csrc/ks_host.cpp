@@ -13,6 +13,7 @@ namespace ks {
 
 Sim::Sim(const std::string& text) {
     Deck D(text);
+    deck_text_ = text;
     setup(D);
     ck(cudaStreamCreateWithFlags(&ctx_.stream, cudaStreamNonBlocking), "stream create");
     ck(cudaMallocHost(&hred_, 64 * sizeof(double)), "pinned alloc");
@@ -212,6 +213,12 @@ void Sim::setup(const Deck& D) {
     mg(dif_, "velocity_diffusion");
     mg(tdif_, "diffusion");
     mg(tdif_, "temperature_diffusion");
+    // I/O (IOManager::initialize_io, SimTime::parse_parameters)
+    restart_file_ = D.str("io.restart_file", "");
+    plt_prefix_ = D.str("io.plot_file", "plt");
+    chk_prefix_ = D.str("io.check_file", "chk");
+    plot_interval_ = D.flag("time.plot_interval", -1);
+    chk_interval_ = D.flag("time.checkpoint_interval", -1);
 
     t_.stop = D.num("time.stop_time", -1);
     t_.max_step = D.flag("time.max_step", -1);
@@ -1161,6 +1168,13 @@ void Sim::tdiffuse_solve(double dtd) {
 }
 
 void Sim::init_data() {
+    if (!restart_file_.empty()) {  // restart: fields from the checkpoint, no initial projection or iterations
+        read_checkpoint(restart_file_);
+        plot_start_ = chk_start_ = t_.step;  // SimTime::set_restart_time
+        abl_update();
+        sync();
+        return;
+    }
     abl_update();
     if (initial_proj_) {
         apply_projection(t_.cur, 1.0, false);
@@ -1570,6 +1584,39 @@ int ks_checkpoint_cost(int nsteps, int snapshots, long long* forward_steps) {
         return KS_ERR_OOM;
     }
     return KS_OK;
+}
+
+int ks_write_plotfile(ks_handle* h, const char* path) {
+    if (!path) return KS_ERR_ARG;
+    return guarded(h, [&](ks::Sim& s) { s.write_plotfile(path); return 0; });
+}
+
+int ks_write_checkpoint(ks_handle* h, const char* path) {
+    if (!path) return KS_ERR_ARG;
+    return guarded(h, [&](ks::Sim& s) { s.write_checkpoint(path); return 0; });
+}
+
+int ks_read_checkpoint(ks_handle* h, const char* path) {
+    if (!path) return KS_ERR_ARG;
+    return guarded(h, [&](ks::Sim& s) { s.read_checkpoint(path); return 0; });
+}
+
+int ks_write_outputs(ks_handle* h, int last) {
+    return guarded(h, [&](ks::Sim& s) { s.write_outputs(last != 0); return 0; });
+}
+
+int ks_plotfile_write_host(const char* path, int nvars, const char* const* names, const int n[3], const double prob_lo[3],
+                           const double prob_hi[3], double time, int step, const double* data) {
+    if (!path || nvars < 1 || !names || !n || !prob_lo || !prob_hi || !data) return KS_ERR_ARG;
+    try {
+        std::vector<std::string> nm(names, names + nvars);
+        ks::write_plotfile_host(path, nm, n, prob_lo, prob_hi, time, step, data, "");
+        return KS_OK;
+    } catch (const ks::KsError& e) {
+        return e.code;
+    } catch (const std::exception&) {
+        return KS_ERR_ARG;
+    }
 }
 
 int ks_kernel_launches(const ks_handle* h, long long* count) {

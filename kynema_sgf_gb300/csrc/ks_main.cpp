@@ -1,6 +1,8 @@
 // Deck-compatible driver executable over the C ABI (the counterpart of the
 // reference's src/main.cpp: `exe <input_file> [key=value ...]`, InitData, then
-// the Evolve loop with its per-step console lines).  Command-line key=value
+// the Evolve loop with its per-step console lines and the plot / checkpoint
+// files of time.plot_interval / time.checkpoint_interval; io.restart_file
+// restarts from a checkpoint).  Command-line key=value
 // pairs override the input file, as ParmParse does.
 #include <cstdio>
 #include <cstring>
@@ -71,6 +73,8 @@ int main(int argc, char** argv) {
     if (rc != KS_OK) return fail(h, rc);
     rc = ks_init_data(h);
     if (rc != KS_OK) return fail(h, rc);
+    rc = ks_write_outputs(h, 0);  // plot / checkpoint files of step 0 (incflo.cpp:203-208)
+    if (rc != KS_OK) return fail(h, rc);
     double ncells = 0.0;
     ks_get_scalar(h, "ncells", &ncells);
     std::printf("\nBegin simulation: %.0f cells\n", ncells);
@@ -93,7 +97,11 @@ int main(int argc, char** argv) {
         ks_mg_stats st{};
         ks_last_solver_stats(h, &st);
         solver_table(st);
+        rc = ks_write_outputs(h, 0);  // post_advance_work (incflo.cpp:321-327)
+        if (rc != KS_OK) return fail(h, rc);
     }
+    rc = ks_write_outputs(h, 1);  // write_last_plot_file / write_last_checkpoint (incflo.cpp:404-409)
+    if (rc != KS_OK) return fail(h, rc);
     std::printf("\n==============================================================================\n");
     std::printf("Time stepping finished.\n");
     ks_destroy(h);

@@ -219,6 +219,11 @@ struct AdjState {
     std::vector<std::vector<int>> split;  // optimal first split per (steps, free slots)
 };
 
+// An AMReX plot file (single level, one box) from host data: nvars = names.size()
+// cell fields of n[0] n[1] n[2] values each, component-major, x fastest.
+void write_plotfile_host(const std::string& dir, const std::vector<std::string>& names, const int n[3], const double plo[3], const double phi[3],
+                         double time, int step, const double* data, const std::string& info);
+
 // Fewest forward steps (beyond the one inside each reverse step) that reverse
 // n steps with `snapshots` checkpoint slots, the first holding the initial state.
 long long checkpoint_cost(int n, int snapshots);
@@ -258,6 +263,14 @@ class Sim {
     int ndisks() const { return (int)disks_.size(); }
     double adjoint_stat(const std::string& name) const;
 
+    // ---- plot files, checkpoints and restart (ks_io.cpp)
+    void write_plotfile(const std::string& dir);
+    void write_checkpoint(const std::string& dir);
+    void read_checkpoint(const std::string& dir);
+    // the plot / checkpoint files due at the current step (SimTime::write_plot_file,
+    // write_checkpoint; last = the end-of-run rules write_last_plot_file / _checkpoint)
+    void write_outputs(bool last);
+
     Ctx ctx_;
     Grid g_{};
     Clock t_;
@@ -295,6 +308,11 @@ class Sim {
     void tdiffuse_solve(double dtd);
     void abl_forcing_update();
     ScalarBC tbc() const { return ScalarBC{tzlo_, tzhi_, tgz_.p, tgtop_}; }
+    std::vector<std::pair<std::string, int>> plot_fields() const;
+    std::vector<double> host_field(const std::string& name, int nc);
+    std::string info_text() const;
+    std::string deck_text_, restart_file_, plt_prefix_ = "plt", chk_prefix_ = "chk";
+    int plot_interval_ = -1, chk_interval_ = -1, plot_start_ = 0, chk_start_ = 0;
     double diff_fac() const { return diff_type_ == 0 ? 1.0 : (diff_type_ == 1 ? 0.5 : 0.0); }
     void disk_points(const Disk& d, std::vector<double>& sample, std::vector<double>& ring) const;
     // reverse mode

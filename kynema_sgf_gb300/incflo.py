@@ -33,7 +33,8 @@ SYMBOLS = ["ks_create", "ks_destroy", "ks_last_error", "ks_init_data", "ks_compu
            "ks_last_solver_stats", "ks_set_precision", "ks_synchronize", "ks_kernel_launches", "ks_get_stream",
            "ks_profile_kernels", "ks_profile_report", "ks_divtau_noalloc", "ks_fma_peak", "ks_set_objective_box",
            "ks_objective", "ks_adjoint_step", "ks_adjoint_run", "ks_get_ct_gradient", "ks_adjoint_reset",
-           "ks_set_disk_ct", "ks_checkpoint_cost"]
+           "ks_set_disk_ct", "ks_checkpoint_cost", "ks_write_plotfile", "ks_write_checkpoint", "ks_read_checkpoint",
+           "ks_write_outputs", "ks_plotfile_write_host"]
 
 
 class KsError(RuntimeError):
@@ -105,6 +106,11 @@ def load_library(path=None):
     lib.ks_adjoint_reset.argtypes = [vp]
     lib.ks_set_disk_ct.argtypes = [vp, d3, ip]
     lib.ks_checkpoint_cost.argtypes = [ip, ip, ctypes.POINTER(ctypes.c_longlong)]
+    for name in ("ks_write_plotfile", "ks_write_checkpoint", "ks_read_checkpoint"):
+        getattr(lib, name).argtypes = [vp, ctypes.c_char_p]
+    lib.ks_write_outputs.argtypes = [vp, ip]
+    i3 = ctypes.POINTER(ctypes.c_int)
+    lib.ks_plotfile_write_host.argtypes = [ctypes.c_char_p, ip, ctypes.POINTER(ctypes.c_char_p), i3, d3, d3, dp, ip, vp]
     if path is None:
         _LIB = lib
     return lib
@@ -129,6 +135,22 @@ def checkpoint_cost(nsteps, snapshots):
     if rc != 0:
         raise KsError(rc, "ks_checkpoint_cost failed")
     return v.value
+
+
+def write_plotfile_host(path, names, data, prob_lo, prob_hi, time=0.0, step=0):
+    """AMReX plot file from host data (no device): ``data`` is (nvars, nz, ny, nx)."""
+    lib = load_library()
+    a = np.ascontiguousarray(data, dtype=np.float64)
+    nv, nz, ny, nx = a.shape
+    if nv != len(names):
+        raise ValueError("one name per variable")
+    nm = (ctypes.c_char_p * nv)(*[n.encode() for n in names])
+    n3 = (ctypes.c_int * 3)(nx, ny, nz)
+    lo = (ctypes.c_double * 3)(*[float(x) for x in prob_lo])
+    hi = (ctypes.c_double * 3)(*[float(x) for x in prob_hi])
+    rc = lib.ks_plotfile_write_host(str(path).encode(), nv, nm, n3, lo, hi, float(time), int(step), a.ctypes.data)
+    if rc != 0:
+        raise KsError(rc, "ks_plotfile_write_host failed")
 
 
 class Incflo:
@@ -299,6 +321,19 @@ class Incflo:
 
     def adjoint_reset(self):
         self._check(self._lib.ks_adjoint_reset(self._h))
+
+    # ---- IOManager counterparts
+    def write_plot_file(self, path):
+        self._check(self._lib.ks_write_plotfile(self._h, str(path).encode()))
+
+    def write_checkpoint_file(self, path):
+        self._check(self._lib.ks_write_checkpoint(self._h, str(path).encode()))
+
+    def read_checkpoint_file(self, path):
+        self._check(self._lib.ks_read_checkpoint(self._h, str(path).encode()))
+
+    def write_outputs(self, last=False):
+        self._check(self._lib.ks_write_outputs(self._h, int(bool(last))))
 
     def set_disk_ct(self, ct):
         ct = [float(x) for x in ct]
