@@ -174,7 +174,6 @@ void Sim::setup(const Deck& D) {
         ablf_target_[1] = tv.at(1);
     }
     if (temp_) {
-        if (!godunov_) throw KsError(KS_ERR_UNSUPPORTED, "temperature transport with the MOL scheme");
         if (D.has("ABL.surface_temp_rate") || D.has("ABL.surface_temp_timetable") || std::fabs(D.num("ABL.surface_temp_flux", 0.0)) > 0.0)
             throw KsError(KS_ERR_UNSUPPORTED, "non-neutral surface temperature forcing (only ABL.surface_temp_flux = 0)");
         if (D.flag("ABL.perturb_temperature", 0)) throw KsError(KS_ERR_UNSUPPORTED, "ABL.perturb_temperature (random perturbations)");
@@ -412,7 +411,8 @@ void Sim::alloc() {
         tgz_.alloc((size_t)g_.nx * g_.ny);
         tedge_.alloc(2 * N + NF);
         tparts_.alloc((size_t)tdiff_blocks(g_));
-        if (gb_.lo[0][0] == nullptr) throw KsError(KS_ERR_UNSUPPORTED, "temperature transport needs the Godunov face scratch");
+        if (!godunov_) tconv_old_.alloc(N);
+        if (gb_.flux[0][0] == nullptr) throw KsError(KS_ERR_UNSUPPORTED, "temperature transport needs the face scratch");
     }
     size_t maxpts = 1;
     for (auto& d : disks_) maxpts = std::max(maxpts, (size_t)d.nr * d.nt);
@@ -1048,18 +1048,27 @@ void Sim::apply_predictor(bool incremental) {
 // CompRHSOps.H:32-141) fused into its divergence pass, nodal projection.
 void Sim::mol_predictor(bool incremental) {
     const double dt = t_.dt[0];
-    launch_smagorinsky(ctx_, g_, vel_old_.p, mueff_.p, S_);
+    launch_smagorinsky(ctx_, g_, vel_old_.p, mueff_.p, S_, alpha_.p);
     if (wallmodel_) launch_wall_grad(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, shear_, utau_ * utau_, um_[0], um_[1], vmag_, rho_);
     double* fl[9];
     for (int m = 0; m < 9; ++m) fl[m] = static_cast<double*>(gb_.flux[m / 3][m % 3]);
     // diff_term(Old) enters predictor_rhs with factor 1 / 0.5 / 0 (implicit: not formed)
     const double fac = diff_fac();
     if (fac != 0.0) launch_divtau(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, divtau_.p, 0, nullptr, nullptr, nullptr, nullptr, dt, rho_, fl);
-    launch_sources(ctx_, g_, vel_old_.p, gp_.p, act_.p, src_.p, S_);
+    if (temp_) {
+        if (tzlo_ == 1)
+            launch_theta_wall_grad(ctx_, g_, vel_old_.p, theta_old_.p, alpha_.p, tgz_.p, shear_, utau_, kappa_, std::log(zref_ / z0t_), vmag_,
+                                   theta_mean_, rho_);
+        if (fac != 0.0)
+            launch_tdiff(ctx_, g_, theta_old_.p, alpha_.p, tbc(), tdiff_.p, 0, nullptr, nullptr, nullptr, nullptr, nullptr, dt, rho_, 0.0);
+    }
     double* mac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
     launch_mol_extrap(ctx_, g_, vel_old_.p, mac);
     mac_project();
     const double* cmac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
+    if (temp_) temperature_mol(false, dt);
+    // sources at NPH: the Coriolis term reads Old, BoussinesqBuoyancy theta at n+1/2
+    launch_sources(ctx_, g_, vel_old_.p, gp_.p, act_.p, src_.p, S_, temp_ ? theta_nph_.p : nullptr);
     launch_mol_advection(ctx_, g_, vel_old_.p, cmac, rho_, fl, conv_old_.p, 1, vel_old_.p, src_.p, divtau_.p, nullptr, vel_.p, dt, fac);
     if (diff_type_ != 0) diffuse_solve(diff_type_ == 2 ? dt : 0.5 * dt);
     apply_projection(t_.next, dt, incremental);
@@ -1079,23 +1088,27 @@ void Sim::apply_corrector() {
     launch_mol_extrap(ctx_, g_, vel_.p, mac);
     mac_project();
     const double* cmac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
+    if (temp_) {  // conv_term(New) of the scalar from the predicted temperature
+        double* tfl[3] = {fl[0], fl[3], fl[6]};
+        launch_mol_scalar_advection(ctx_, g_, theta_.p, cmac, rho_, tfl, tconv_.p);
+    }
+    // mu_eff(New) and the wall data from the predicted velocity (it is read before the corrector overwrites it)
+    launch_smagorinsky(ctx_, g_, vel_.p, mueff_.p, S_, alpha_.p);
+    if (wallmodel_) launch_wall_grad(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, shear_, utau_ * utau_, um_[0], um_[1], vmag_, rho_);
+    if (temp_) temperature_mol(true, dt);
+    // sources at New: the Coriolis term reads the predicted velocity, BoussinesqBuoyancy theta at n+1/2
+    launch_sources(ctx_, g_, vel_.p, gp_.p, act_.p, src_.p, S_, temp_ ? theta_nph_.p : nullptr);
     if (diff_type_ != 0) {
         // corrector_rhs with ofac 1/2 (Crank-Nicolson) or 0 (implicit) and nfac 0, fused into the
         // divergence of the fluxes, then the solve with mu_eff(New) (incflo_advance.cpp:620-640)
-        launch_sources(ctx_, g_, vel_.p, gp_.p, act_.p, src_.p, S_);
         launch_mol_advection(ctx_, g_, vel_.p, cmac, rho_, fl, conv_.p, 2, vel_old_.p, src_.p, divtau_.p, conv_old_.p, vel_tmp_.p, dt,
                              diff_type_ == 1 ? 0.5 : 0.0);
         std::swap(vel_.p, vel_tmp_.p);
-        launch_smagorinsky(ctx_, g_, vel_tmp_.p, mueff_.p, S_);
-        if (wallmodel_) launch_wall_grad(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, shear_, utau_ * utau_, um_[0], um_[1], vmag_, rho_);
         diffuse_solve(diff_type_ == 2 ? dt : 0.5 * dt);
         apply_projection(t_.next, dt, false);
         return;
     }
     launch_mol_advection(ctx_, g_, vel_.p, cmac, rho_, fl, conv_.p, 0, nullptr, nullptr, nullptr, nullptr, nullptr, dt, 0.0);
-    launch_smagorinsky(ctx_, g_, vel_.p, mueff_.p, S_);
-    if (wallmodel_) launch_wall_grad(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, shear_, utau_ * utau_, um_[0], um_[1], vmag_, rho_);
-    launch_sources(ctx_, g_, vel_.p, gp_.p, act_.p, src_.p, S_);
     launch_divtau_corrector(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, vel_old_.p, conv_old_.p, conv_.p, divtau_.p, src_.p, dt, rho_);
     std::swap(vel_.p, vel_tmp_.p);
     apply_projection(t_.next, dt, false);
@@ -1130,6 +1143,36 @@ void Sim::temperature_predictor(double dt) {
     } else {
         tdiffuse_solve(diff_type_ == 2 ? dt : 0.5 * dt);
     }
+    launch_lincomb(ctx_, N, 0.5, theta_old_.p, 0.5, theta_.p, theta_nph_.p);
+}
+
+// The scalar parts of the MOL ApplyPredictor / ApplyCorrector
+// (incflo_advance.cpp:296-341, 555-600): predictor — conv_term(Old) of rho theta
+// and predictor_rhs with the diffusion factor; corrector — conv_term(New)
+// (formed by the caller), diff_term(New) for explicit diffusion (wall data from
+// the Old state and the new alpha_eff), corrector_rhs (1/2, 1/2 explicit; 1/2, 0
+// Crank-Nicolson; 0, 0 implicit); then the solve and theta_nph.
+void Sim::temperature_mol(bool corrector, double dt) {
+    const long long N = g_.N;
+    double* fl[3] = {static_cast<double*>(gb_.flux[0][0]), static_cast<double*>(gb_.flux[1][0]), static_cast<double*>(gb_.flux[2][0])};
+    const double* cmac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
+    if (!corrector) {
+        launch_mol_scalar_advection(ctx_, g_, theta_old_.p, cmac, rho_, fl, tconv_old_.p);
+        launch_scalar_pred(ctx_, N, theta_old_.p, tconv_old_.p, tdiff_.p, theta_.p, dt, rho_, diff_fac());
+    } else {
+        const double ofac = diff_type_ == 2 ? 0.0 : 0.5;
+        const double* dnew = nullptr;
+        if (tzlo_ == 1)  // the new alpha_eff enters the wall gradient
+            launch_theta_wall_grad(ctx_, g_, vel_old_.p, theta_old_.p, alpha_.p, tgz_.p, shear_, utau_, kappa_, std::log(zref_ / z0t_), vmag_,
+                                   theta_mean_, rho_);
+        if (diff_type_ == 0) {
+            launch_tdiff(ctx_, g_, theta_.p, alpha_.p, tbc(), ttmp_.p, 0, nullptr, nullptr, nullptr, nullptr, nullptr, dt, rho_, 0.0);
+            dnew = ttmp_.p;
+        }
+        launch_scalar_corr(ctx_, N, theta_old_.p, tconv_old_.p, tconv_.p, tdiff_.p, dnew, tb_.p, dt, rho_, ofac, diff_type_ == 0 ? 0.5 : 0.0);
+        std::swap(theta_.p, tb_.p);
+    }
+    if (diff_type_ != 0) tdiffuse_solve(diff_type_ == 2 ? dt : 0.5 * dt);
     launch_lincomb(ctx_, N, 0.5, theta_old_.p, 0.5, theta_.p, theta_nph_.p);
 }
 

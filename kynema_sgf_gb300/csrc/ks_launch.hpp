@@ -226,6 +226,10 @@ void launch_scalar_rhs(Ctx& c, const Grid& g, const double* th, double rho, doub
 // predictor_rhs of a scalar without sources: out = (rho s_old + dt (conv + fac dold)) / rho
 void launch_scalar_pred(Ctx& c, long long n, const double* s_old, const double* conv, const double* dold, double* out, double dt, double rho,
                         double fac);
+// corrector_rhs of a scalar without sources:
+// out = (rho s_old + dt (0.5 (conv_old + conv) + ofac dold + nfac dnew)) / rho (dnew may be null when nfac = 0)
+void launch_scalar_corr(Ctx& c, long long n, const double* s_old, const double* conv_old, const double* conv, const double* dold,
+                        const double* dnew, double* out, double dt, double rho, double ofac, double nfac);
 // out = a x + b y (n values)
 void launch_lincomb(Ctx& c, long long n, double a, const double* x, double b, const double* y, double* out);
 
@@ -239,6 +243,10 @@ void launch_mol_extrap(Ctx& c, const Grid& g, const double* vel, double* const m
 void launch_mol_advection(Ctx& c, const Grid& g, const double* vel, const double* const mac[3], double rho, double* const fl[9],
                           double* conv, int mode, const double* vel_old, const double* src, const double* dold, const double* conv_old,
                           double* vel_out, double dt, double fac);
+
+// conv = -div(u_mac (rho s)_face) of a cell scalar s (hoextrap at z walls) through three face arrays
+void launch_mol_scalar_advection(Ctx& c, const Grid& g, const double* s, const double* const mac[3], double rho, double* const fl[3],
+                                 double* conv);
 
 // ---- implicit / Crank-Nicolson tensor diffusion solve (ks_implicit.cu)
 // 1 / diagonal of rho - dtd divtau per cell and component (3 N_g values); parts, when

@@ -64,10 +64,11 @@ __device__ inline double mol_upwind(double u, double qmns, double qpls) {
 
 __device__ inline double* pick3(int n, double* a, double* b, double* c) { return n == 0 ? a : (n == 1 ? b : c); }
 
-// The face kernels come in two kinds: KIND 0 extrapolates the normal velocity
+// The face kernels come in three kinds: KIND 0 extrapolates the normal velocity
 // component d of u to the d-faces (ExtrapVelToFaces, written to mac); KIND 1
 // forms the fluxes of rho u (three components, upwinded with mac) through
-// them.  Each computes the MC slope of every cell once per component: the
+// them; KIND 2 the fluxes of rho s for a cell scalar s (AdvOp_MOL.H:38-118),
+// hoextrap at z walls like a tangential component.  Each computes the MC slope of every cell once per component: the
 // x kernel takes the slope of cell i - 1 from the neighbouring lane of its warp,
 // the y and z kernels march along a column of MOL_CHUNK faces and carry it.
 
@@ -91,7 +92,7 @@ __global__ void k_mol_x(Grid g, const double* vel, double rho, const double* mac
     const long long t = ((long long)k * g.ny + j) * g.nx + (face ? i : 0);
     const VelFP Q{vel, g, KIND ? rho : 1.0};
     const double u = (KIND && face) ? mac[t] : 0.0;
-    constexpr int nend = KIND ? 3 : 1;
+    constexpr int nend = KIND == 1 ? 3 : 1;
     for (int n = 0; n < nend; ++n) {
         const double b = Q(n, ic - 1, j, k), c = Q(n, ic, j, k), e = Q(n, ic + 1, j, k);
         const double s0 = mc_slope(b, c, e, 0);
@@ -116,7 +117,7 @@ __global__ void k_mol_y(Grid g, const double* vel, double rho, const double* mac
     const int k = (int)(r % g.nz), ch = (int)(r / g.nz);
     const int j0 = ch * MOL_CHUNK, j1 = min(j0 + MOL_CHUNK, g.ny);
     const VelFP Q{vel, g, KIND ? rho : 1.0};
-    const int nbeg = KIND ? 0 : 1, nend = KIND ? 3 : 2;
+    const int nbeg = KIND == 0 ? 1 : 0, nend = KIND == 0 ? 2 : (KIND == 1 ? 3 : 1);
     for (int n = nbeg; n < nend; ++n) {
         double qb = Q(n, i, j0 - 1, k), qc = Q(n, i, j0, k);
         double sb = mc_slope(Q(n, i, j0 - 2, k), qb, qc, 0);
@@ -147,8 +148,8 @@ __global__ void k_mol_z(Grid g, const double* vel, double rho, const double* mac
     const int j = (int)(r % g.ny), ch = (int)(r / g.ny);
     const int k0 = ch * MOL_CHUNK, k1 = min(k0 + MOL_CHUNK, nzf);
     const VelFP Q{vel, g, KIND ? rho : 1.0};
-    const int nbeg = KIND ? 0 : 2;
-    for (int n = nbeg; n < 3; ++n) {
+    const int nbeg = KIND == 0 ? 2 : 0, nend = KIND == 2 ? 1 : 3;
+    for (int n = nbeg; n < nend; ++n) {
         double qb = Q(n, i, j, k0 - 1), qc = Q(n, i, j, k0);
         double sb = mc_slope(Q(n, i, j, k0 - 2), qb, qc, z_edge(g, 2, k0 - 1));
         for (int k = k0; k < k1; ++k) {
@@ -178,7 +179,7 @@ struct MolFlux {
 // fstate Old, vel = (rho u_old + dt (conv + src + fac divtau_old)) / rho; mode 2
 // corrector_rhs without the new diffusion term (Crank-Nicolson / implicit),
 // vel = (rho u_old + dt (0.5 (conv_old + conv) + fac divtau_old + src)) / rho
-__global__ void k_mol_div(Grid g, MolFlux F, double* conv, int mode, const double* vo, const double* src, const double* dold,
+__global__ void k_mol_div(Grid g, MolFlux F, int nc, double* conv, int mode, const double* vo, const double* src, const double* dold,
                           const double* conv_o, double* vel, double dt, double rho, double fac) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= g.N) return;
@@ -188,7 +189,7 @@ __global__ void k_mol_div(Grid g, MolFlux F, double* conv, int mode, const doubl
     const long long xp = fidx(g, 0, i + 1, j, k), yp = fidx(g, 1, i, j + 1, k);
     const long long zm = fidx(g, 2, i, j, k), zp = fidx(g, 2, i, j, k + 1);
     const long long N = g.N;
-    for (int n = 0; n < 3; ++n) {
+    for (int n = 0; n < nc; ++n) {
         const double c = (g.idx * (F.p[n][t] - F.p[n][xp])) + (g.idy * (F.p[3 + n][t] - F.p[3 + n][yp])) +
                          (g.idz * (F.p[6 + n][zm] - F.p[6 + n][zp]));
         conv[n * N + t] = c;
@@ -204,11 +205,11 @@ inline long long nfaces_d(const Grid& g, int d) { return (long long)g.nx * g.ny 
 
 template <int KIND>
 static void mol_faces(Ctx& c, const Grid& g, const double* vel, double rho, const double* const mac[3], double* const out[9]) {
-    const double nc = KIND ? 3.0 : 1.0;  // components read and written per face
+    const double nc = KIND == 1 ? 3.0 : 1.0;  // components read and written per face
     const long long ty = (long long)g.nx * g.nz * ((g.ny + MOL_CHUNK - 1) / MOL_CHUNK);
     const long long tz = (long long)g.nx * g.ny * ((nzfaces(g) + MOL_CHUNK - 1) / MOL_CHUNK);
     const double nfz = (double)nfaces_d(g, 2);
-    auto o = [&](int d, int n) { return out[KIND ? 3 * d + n : d]; };
+    auto o = [&](int d, int n) { return out[KIND == 1 ? 3 * d + n : d]; };
     const double* m0 = KIND ? mac[0] : nullptr;
     const double* m1 = KIND ? mac[1] : nullptr;
     const double* m2 = KIND ? mac[2] : nullptr;
@@ -232,7 +233,21 @@ void launch_mol_advection(Ctx& c, const Grid& g, const double* vel, const double
     for (int m = 0; m < 9; ++m) F.p[m] = fl[m];
     const double nfz = (double)nfaces_d(g, 2);
     const double bytes = 8.0 * (6.0 * g.N + 3.0 * nfz + 3.0 * g.N + (mode == 1 ? 12.0 * g.N : (mode == 2 ? 15.0 * g.N : 0.0)));
-    KS_LAUNCH(c, k_mol_div, nblocks(g.N, BS), BS, bytes, g, F, conv, mode, vel_old, src, dold, conv_old, vel_out, dt, rho, fac);
+    KS_LAUNCH(c, k_mol_div, nblocks(g.N, BS), BS, bytes, g, F, 3, conv, mode, vel_old, src, dold, conv_old, vel_out, dt, rho, fac);
+}
+
+void launch_mol_scalar_advection(Ctx& c, const Grid& g, const double* s, const double* const mac[3], double rho, double* const fl[3],
+                                 double* conv) {
+    double* out[9] = {fl[0], fl[1], fl[2], nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    mol_faces<2>(c, g, s, rho, mac, out);
+    MolFlux F;
+    for (int m = 0; m < 9; ++m) F.p[m] = nullptr;
+    F.p[0] = fl[0];
+    F.p[3] = fl[1];
+    F.p[6] = fl[2];
+    const double nfz = (double)nfaces_d(g, 2);
+    KS_LAUNCH(c, k_mol_div, nblocks(g.N, BS), BS, 8.0 * (3.0 * g.N + nfz), g, F, 1, conv, 0, nullptr, nullptr, nullptr, nullptr, nullptr, 0.0,
+              rho, 0.0);
 }
 
 }  // namespace ks

@@ -305,6 +305,7 @@ class Sim {
     void diffuse_solve(double dtd);
     void diff_vcycle(size_t l, double dtd);
     void temperature_predictor(double dt);
+    void temperature_mol(bool corrector, double dt);
     void tdiffuse_solve(double dtd);
     void abl_forcing_update();
     ScalarBC tbc() const { return ScalarBC{tzlo_, tzhi_, tgz_.p, tgtop_}; }
@@ -357,6 +358,7 @@ class Sim {
     int tdif_it_ = 0;
     MGParams tdif_;
     DevBuf<double> theta_, theta_old_, theta_nph_, alpha_, tdiff_, tconv_, ttmp_, tb_, tdinv_, tgz_, tedge_, tprof_, layer_, tparts_;
+    DevBuf<double> tconv_old_;  // MOL: the scalar's conv_term(Old)
     DevBuf<double> umac_[3];
     DevBuf<double> gbuf_;
     GodunovBufs gb_{};

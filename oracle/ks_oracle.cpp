@@ -289,7 +289,7 @@ struct Sim {
 
     // fields
     Arr vel, vel_old, gp, p, src, forces, mueff, divtau, divtau_new, conv, conv_old, act_src;
-    Arr theta, theta_old, theta_nph, alpha, tsrc, tdiff, tdiff_new, tconv;
+    Arr theta, theta_old, theta_nph, alpha, tsrc, tdiff, tdiff_new, tconv, tconv_old;
     Arr umac, vmac, wmac;
     int mac_iters = 0, nodal_iters = 0;
     double mac_res0 = 0, mac_res = 0, nodal_res0 = 0, nodal_res = 0;
@@ -322,6 +322,8 @@ struct Sim {
     void apply_predictor(bool incremental);
     void mol_extrap(Arr& v);
     void mol_conv(Arr& v, Arr& out);
+    void mol_conv_field(const Arr& q, int normal, Arr& out);
+    void temperature_mol(bool corrector, double dt);
     void mol_predictor(bool incremental);
     void mol_corrector();
     void diffuse_solve(double dtd);
@@ -437,7 +439,6 @@ void Sim::setup(const std::string& text) {
         ablf_target[1] = tv.at(1);
     }
     if (has_temp) {
-        if (!godunov) throw Error(ERR_UNSUPPORTED, "temperature transport with the MOL scheme");
         if (D.has("ABL.surface_temp_rate") || D.has("ABL.surface_temp_timetable") ||
             std::fabs(D.d("ABL.surface_temp_flux", 0.0)) > 0.0)
             throw Error(ERR_UNSUPPORTED, "non-neutral surface temperature forcing (only ABL.surface_temp_flux = 0)");
@@ -543,7 +544,7 @@ void Sim::setup(const std::string& text) {
     if (has_temp) {
         def_cc(theta, g, 3, 1); def_cc(theta_old, g, 3, 1); def_cc(theta_nph, g, 0, 1);
         def_cc(alpha, g, 1, 1); def_cc(tsrc, g, 1, 1); def_cc(tdiff, g, 0, 1);
-        def_cc(tdiff_new, g, 0, 1); def_cc(tconv, g, 0, 1);
+        def_cc(tdiff_new, g, 0, 1); def_cc(tconv, g, 0, 1); def_cc(tconv_old, g, 0, 1);
     }
     const int nzn = g.n[2] + (g.per[2] ? 0 : 1);
     p.define(-1, -1, -1, g.n[0], g.n[1], nzn, 1);
@@ -2231,26 +2232,35 @@ void Sim::mol_extrap(Arr& v) {
 // states where |u_mac| <= small_vel = FLT_EPSILON, and the ghost value on an
 // ext_dir face; flux = q_face u_mac; conv = sum_d dxinv_d (F_lo - F_hi).
 void Sim::mol_conv(Arr& v, Arr& out) {
-    const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
     fill_vel(v);
     Arr q;
     def_cc(q, g, 3, 3);
     for (size_t m = 0; m < q.d.size(); ++m) q.d[m] = rho * v.d[m];
+    mol_conv_field(q, 2, out);
+}
+
+// The same for a ghost-filled field q of any component count; component
+// `normal` (2 for the velocity, -1 for a scalar) is ext_dir at z walls.
+// Scalars are hoextrap there, so their wall faces take the slope branch
+// (AdvOp_MOL.H:38-118 with the scalar's BCRec).
+void Sim::mol_conv_field(const Arr& q, int normal, Arr& out) {
+    const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+    const int nc = q.nc;
     const double small_vel = (double)std::numeric_limits<float>::epsilon();
     const Arr* mac[3] = {&umac, &vmac, &wmac};
     Arr F[3];
-    F[0].define(0, 0, 0, nx, ny - 1, nz - 1, 3);
-    F[1].define(0, 0, 0, nx - 1, ny, nz - 1, 3);
-    F[2].define(0, 0, 0, nx - 1, ny - 1, nz, 3);
+    F[0].define(0, 0, 0, nx, ny - 1, nz - 1, nc);
+    F[1].define(0, 0, 0, nx - 1, ny, nz - 1, nc);
+    F[2].define(0, 0, 0, nx - 1, ny - 1, nz, nc);
     for (int d = 0; d < 3; ++d)
-        for (int n = 0; n < 3; ++n)
+        for (int n = 0; n < nc; ++n)
 #pragma omp parallel for collapse(2)
             for (int k = 0; k <= F[d].hi[2]; ++k)
                 for (int j = 0; j <= F[d].hi[1]; ++j)
                     for (int i = 0; i <= F[d].hi[0]; ++i) {
                         const double um = (*mac[d])(i, j, k);
                         double qs;
-                        if (d == 2 && !g.per[2] && n == 2 && (k == 0 || k == nz)) {
+                        if (d == 2 && !g.per[2] && n == normal && (k == 0 || k == nz)) {
                             qs = q(i, j, k == 0 ? -1 : nz, n);  // ext_dir: the boundary value in the ghost cell
                         } else {
                             int c[3] = {i, j, k};
@@ -2264,7 +2274,7 @@ void Sim::mol_conv(Arr& v, Arr& out) {
                         F[d](i, j, k, n) = qs * um;
                     }
     const double dxi[3] = {1.0 / g.dx[0], 1.0 / g.dx[1], 1.0 / g.dx[2]};
-    for (int n = 0; n < 3; ++n)
+    for (int n = 0; n < nc; ++n)
 #pragma omp parallel for collapse(2)
         for (int k = 0; k < nz; ++k)
             for (int j = 0; j < ny; ++j)
@@ -2272,6 +2282,45 @@ void Sim::mol_conv(Arr& v, Arr& out) {
                     out(i, j, k, n) = (dxi[0] * (F[0](i, j, k, n) - F[0](i + 1, j, k, n))) +
                                       (dxi[1] * (F[1](i, j, k, n) - F[1](i, j + 1, k, n))) +
                                       (dxi[2] * (F[2](i, j, k, n) - F[2](i, j, k + 1, n)));
+}
+
+// The scalar parts of the MOL ApplyPredictor / ApplyCorrector
+// (incflo_advance.cpp:296-341, 555-600): predictor — conv_term(Old) of rho
+// theta from the MAC velocities of the Old state, predictor_rhs with the
+// factor of the diffusion type, the solve (Crank-Nicolson / implicit);
+// corrector — conv_term(New) (formed by the caller before mu_eff is updated),
+// diff_term(New) for explicit diffusion, corrector_rhs (1/2, 1/2 explicit; 1/2,
+// 0 Crank-Nicolson; 0, 0 implicit), the solve.  Both end with theta_nph =
+// (theta_old + theta) / 2 for the buoyancy; no temperature sources.
+void Sim::temperature_mol(bool corrector, double dt) {
+    const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+    if (!corrector) {
+        Arr q;
+        def_cc(q, g, 3, 1);
+        fill_scalar(theta_old);
+        for (size_t m = 0; m < q.d.size(); ++m) q.d[m] = rho * theta_old.d[m];
+        mol_conv_field(q, -1, tconv_old);
+        const double fac = diff_type == 0 ? 1.0 : (diff_type == 1 ? 0.5 : 0.0);
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i)
+                    theta(i, j, k) = (rho * theta_old(i, j, k) + dt * (tconv_old(i, j, k) + 0.0 + fac * tdiff(i, j, k))) / rho;
+    } else {
+        const double ofac = diff_type == 2 ? 0.0 : 0.5, nfac = diff_type == 0 ? 0.5 : 0.0;
+        if (diff_type == 0) tdiff_op(theta, tdiff_new);  // wall data: Old theta and velocity, the new alpha_eff
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) {
+                    const double dn = diff_type == 0 ? nfac * tdiff_new(i, j, k) : 0.0;
+                    theta(i, j, k) = (rho * theta_old(i, j, k) +
+                                      dt * (0.5 * (tconv_old(i, j, k) + tconv(i, j, k)) + ofac * tdiff(i, j, k) + dn + 0.0)) /
+                                     rho;
+                }
+    }
+    if (diff_type != 0) tdiffuse_solve(diff_type == 2 ? dt : 0.5 * dt);
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) theta_nph(i, j, k) = 0.5 * theta_old(i, j, k) + 0.5 * theta(i, j, k);
 }
 
 // ApplyPredictor for MOL with explicit diffusion (src/incflo_advance.cpp:186-438):
@@ -2283,10 +2332,12 @@ void Sim::mol_predictor(bool incremental) {
     const double dt = t.dt[0];
     update_mueff(vel_old);
     divtau_op(vel_old, divtau);
+    if (has_temp && diff_type != 2) tdiff_op(theta_old, tdiff);  // need_divtau(): not for implicit MOL
     mol_extrap(vel_old);
     mac_project();
+    if (has_temp) temperature_mol(false, dt);
     mol_conv(vel_old, conv_old);
-    compute_sources(vel_old);
+    compute_sources(vel_old, has_temp ? &theta_nph : nullptr);
     const double fac = diff_type == 0 ? 1.0 : (diff_type == 1 ? 0.5 : 0.0);
     for (int n = 0; n < 3; ++n)
 #pragma omp parallel for collapse(2)
@@ -2310,10 +2361,20 @@ void Sim::mol_corrector() {
     const double dt = t.dt[0];
     mol_extrap(vel);
     mac_project();
+    Arr th_star;
+    if (has_temp) {  // conv_term(New) of the scalar, from the predicted temperature
+        th_star = theta;
+        Arr q;
+        def_cc(q, g, 3, 1);
+        fill_scalar(th_star);
+        for (size_t m = 0; m < q.d.size(); ++m) q.d[m] = rho * th_star.d[m];
+        mol_conv_field(q, -1, tconv);
+    }
     mol_conv(vel, conv);
     update_mueff(vel);
+    if (has_temp) temperature_mol(true, dt);
     if (diff_type != 0) {  // corrector_rhs with ofac 1/2 (Crank-Nicolson) or 0 (implicit), nfac 0, then the solve
-        compute_sources(vel);
+        compute_sources(vel, has_temp ? &theta_nph : nullptr);
         const double ofac = diff_type == 1 ? 0.5 : 0.0;
         for (int n = 0; n < 3; ++n)
 #pragma omp parallel for collapse(2)
@@ -2328,7 +2389,7 @@ void Sim::mol_corrector() {
         return;
     }
     divtau_op(vel, divtau_new);
-    compute_sources(vel);
+    compute_sources(vel, has_temp ? &theta_nph : nullptr);
     for (int n = 0; n < 3; ++n)
 #pragma omp parallel for collapse(2)
         for (int k = 0; k < nz; ++k)

@@ -27,11 +27,15 @@ def check(g, o, names, tol=TOL):
         assert e < tol, "%s rel err %.3e" % (f, e)
 
 
-@pytest.mark.parametrize("dtype", [0, 1])
-def test_stratified_abl_parity(cuda_dev, oracle_mod, dtype):
+@pytest.mark.parametrize("case", ["godunov0", "godunov1", "mol0", "mol2"])
+def test_stratified_abl_parity(cuda_dev, oracle_mod, case):
     """The reference's abl_godunov configuration (explicit, and Crank-Nicolson
-    as in its default deck) at 32^3 for three steps."""
+    as in its default deck) and its MOL form (explicit; implicit as in the
+    reference's abl_mol deck) at 32^3 for three steps."""
+    dtype = int(case[-1])
     d = decks.abl_temperature((32, 32, 32), diffusion_type=dtype, fixed_dt=0.5 if dtype else -0.5)
+    if case.startswith("mol"):
+        d = decks.mol(d.replace("time.cfl = 0.95", "time.cfl = 0.45"))
     d += "diffusion.mg_rtol = 1e-13\n"
     g, o = cuda_dev.Incflo(d), oracle_mod.Oracle(d)
     check(g, o, ["velocity", "temperature"], tol=1e-14)
@@ -47,11 +51,15 @@ def test_stratified_abl_parity(cuda_dev, oracle_mod, dtype):
         check(g, o, ["velocity", "p", "gp", "temperature", "temperature_mueff", "src_term", "velocity_mueff"])
 
 
+@pytest.mark.parametrize("scheme", ["godunov", "mol"])
 @pytest.mark.parametrize("dtype", [0, 1, 2])
-def test_scalar_diffusion_amplification(cuda_dev, dtype):
+def test_scalar_diffusion_amplification(cuda_dev, dtype, scheme):
     n, nu, pr, dt = 16, 400.0, 0.7, 0.5
-    g = cuda_dev.Incflo(box_deck(n=n, dtype=dtype, sources="", periodic_z=True, nu=nu, pr=pr, dt=dt,
-                                 extra="diffusion.mg_rtol = 1e-14\ntemperature_diffusion.mg_rtol = 1e-14\n"))
+    d = box_deck(n=n, dtype=dtype, sources="", periodic_z=True, nu=nu, pr=pr, dt=dt,
+                 extra="diffusion.mg_rtol = 1e-14\ntemperature_diffusion.mg_rtol = 1e-14\n")
+    if scheme == "mol":
+        d = decks.mol(d.replace("time.cfl = 0.9", "time.cfl = 0.45"))
+    g = cuda_dev.Incflo(d)
     h = 1000.0 / n
     z = (np.arange(n) + 0.5) * h
     th0 = np.broadcast_to((300.0 + 2.0 * np.cos(2 * math.pi * z / 1000.0))[None, :, None, None], (1, n, n, n)).copy()
@@ -75,7 +83,5 @@ def test_hydrostatic_balance(cuda_dev):
 
 def test_temperature_rejections(cuda_dev):
     base = decks.abl_temperature((16, 16, 16))
-    with pytest.raises(cuda_dev.KsError):
-        cuda_dev.Incflo(decks.mol(base.replace("time.cfl = 0.95", "time.cfl = 0.45")))
     with pytest.raises(cuda_dev.KsError):
         cuda_dev.Incflo(base + "ABL.surface_temp_flux = 0.05\n")
