@@ -97,4 +97,49 @@ inline unsigned nblocks(long long n, int bs) { return (unsigned)((n + bs - 1) / 
 // maximum must reach the host's finiteness checks
 __host__ __device__ inline double nmax(double a, double b) { return (a != a || b != b) ? a + b : (a > b ? a : b); }
 
+// ---- FP64 decisions on the integer pipe.
+// On this GPU every FP64 instruction -- DFMA, DADD, DMUL, and also the
+// compares (DSETP) and min/max (DMNMX) -- issues at one sixty-fourth of the
+// FP32 rate, while 64-bit integer compares and selects cost no FP64 issue
+// slot.  Doubles that are not NaN order like their bit patterns read as
+// sign-magnitude integers, so signs, comparisons, minima and maxima are taken
+// on the bits.  Results equal the FP64 forms for every non-NaN operand, except
+// that -0 orders below +0 (min/max may return the other zero).  NaN operands
+// are not ordered like IEEE does; a NaN field still reaches the host through
+// the arithmetic it enters and the residual / CFL maxima (imax_abs keeps it).
+#ifdef __CUDACC__
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ double bitsd(long long b) { return __longlong_as_double(b); }
+constexpr long long kMag = 0x7fffffffffffffffLL;
+// signed integer with the order of the doubles
+__device__ __forceinline__ long long okey(double x) {
+    const long long b = dbits(x);
+    return b ^ ((b >> 63) & kMag);
+}
+__device__ __forceinline__ bool igt0(double x) { return dbits(x) > 0; }   // x > 0
+__device__ __forceinline__ bool ile0(double x) { return dbits(x) <= 0; }  // x <= 0
+__device__ __forceinline__ bool ilt0(double x) { return okey(x) < -1; }   // x < 0 (-0 is not)
+__device__ __forceinline__ bool ige0(double x) { return okey(x) >= -1; }  // x >= 0 (-0 is)
+__device__ __forceinline__ bool ilt(double a, double b) { return okey(a) < okey(b); }
+__device__ __forceinline__ double imin(double a, double b) { return okey(a) < okey(b) ? a : b; }
+__device__ __forceinline__ double imax(double a, double b) { return okey(a) > okey(b) ? a : b; }
+__device__ __forceinline__ double iabs(double x) { return bitsd(dbits(x) & kMag); }
+// |x| < c for c > 0
+__device__ __forceinline__ bool iabs_lt(double x, double c) { return (dbits(x) & kMag) < dbits(c); }
+// |a| < |b|
+__device__ __forceinline__ bool iabs_lt2(double a, double b) { return (dbits(a) & kMag) < (dbits(b) & kMag); }
+// a and b non-zero with the same sign (a * b > 0 unless the product underflows)
+__device__ __forceinline__ bool isame_sign(double a, double b) {
+    return (dbits(a) ^ dbits(b)) >= 0 && (dbits(a) & kMag) != 0 && (dbits(b) & kMag) != 0;
+}
+// copysign(m, s) for m >= 0
+__device__ __forceinline__ double isign(double m, double s) { return bitsd(dbits(m) | (dbits(s) & ~kMag)); }
+// running max of |x| kept as bits: NaN patterns order above infinity, so a
+// NaN operand survives to the host
+__device__ __forceinline__ long long imax_abs(long long m, double x) {
+    const long long b = dbits(x) & kMag;
+    return b > m ? b : m;
+}
+#endif
+
 }  // namespace ks

@@ -9,12 +9,15 @@
 // dt/6 (velocity form) or dt/3 (conservative form) corner factors, forces
 // added after the transverse step, upwinding with AMReX-Hydro's small_vel.
 //
-// FP64 arithmetic is the scarce resource on GB300, so nothing is computed
-// twice: the unlimited PPM edge value of every face is computed once
-// (k_edges), the left/right traces of every face once per stage (k_faces) and
-// stored; the transverse and final stages only read them.  Post-MAC states of
-// rho*u are rho times the traces of u (the PPM limiter and the traces are
-// homogeneous of degree one in the advected field).
+// FP64 issue is the scarce resource on GB300 (every FP64 instruction,
+// compares and min/max included, issues at 1/64 of the FP32 rate), so nothing
+// is computed twice and no FP64 instruction makes a decision: every cell's
+// slope, unlimited edge and limited parabola is formed once per component and
+// pass (k_ppm_x / k_ppm_col), the face states are stored, and the transverse
+// and final stages only read them; signs, comparisons, minima and maxima are
+// taken on the integer pipe (ks_common.cuh).  Post-MAC states of rho*u are rho
+// times the traces of u (the PPM limiter and the traces are homogeneous of
+// degree one in the advected field).
 #include "ks_launch.hpp"
 
 namespace ks {
@@ -22,19 +25,6 @@ namespace ks {
 namespace {
 
 constexpr int BS = 256;
-
-template <typename T>
-__device__ inline T vls(T a, T b, T c) {
-    const T dsc = T(0.5) * (c - a), dsl = T(2) * (b - a), dsr = T(2) * (c - b);
-    return (dsl * dsr > T(0)) ? copysign(fmin(fabs(dsc), fmin(fabs(dsl), fabs(dsr))), dsc) : T(0);
-}
-template <typename T>
-__device__ inline T clipe(T e, T a, T b) { return fmin(fmax(e, fmin(a, b)), fmax(a, b)); }
-
-template <typename T>
-struct Dt {  // dt / h along x, y, z
-    T v[3];
-};
 
 __device__ inline bool face_of(const Grid& g, int d, long long t, int& i, int& j, int& k) {
     const int nzl = (d == 2) ? nzfaces(g) : g.nz;
@@ -49,66 +39,98 @@ __device__ inline bool face_of(const Grid& g, int d, long long t, int& i, int& j
 
 inline long long nfaces(const Grid& g, int d) { return (long long)g.nx * g.ny * (d == 2 ? nzfaces(g) : g.nz); }
 
-// ---- unlimited PPM edge values on the d-faces (face at the low side of the
-// cell of the same index), 3 components.  Wall-bounded z: the wall faces take
-// the boundary (ghost) value, the faces one cell inside the one-sided
-// fourth-order formula, clipped to the two adjacent cells.
-template <typename T, int NC = 3>
-__global__ void k_edges(Grid g, int d, const double* vel, T* e0, T* e1, T* e2) {
-    int i, j, k;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (!face_of(g, d, t, i, j, k)) return;
-    VelFPT<T> q{vel, g, T(1)};
-    const int di = (d == 0), dj = (d == 1), dk = (d == 2);
-    const bool wall = (d == 2 && !g.zper);
-    T* e[3] = {e0, e1, e2};
-    const long long f = fidx(g, d, i, j, k);
-    for (int n = 0; n < NC; ++n) {
-        T v;
-        if (wall && k == 0) {
-            v = q(n, i, j, -1);
-        } else if (wall && k == g.nz) {
-            v = q(n, i, j, g.nz);
-        } else if (wall && k == 1) {
-            const T b = q(n, i, j, -1), q0 = q(n, i, j, 0), q1 = q(n, i, j, 1), q2 = q(n, i, j, 2);
-            v = clipe(T(-0.2) * b + T(0.75) * q0 + T(0.5) * q1 - T(0.05) * q2, q0, q1);
-        } else if (wall && k == g.nz - 1) {
-            const int t0 = g.nz - 1;
-            const T b = q(n, i, j, g.nz), q0 = q(n, i, j, t0), q1 = q(n, i, j, t0 - 1), q2 = q(n, i, j, t0 - 2);
-            v = clipe(T(-0.2) * b + T(0.75) * q0 + T(0.5) * q1 - T(0.05) * q2, q0, q1);
-        } else {
-            const T am = q(n, i - 2 * di, j - 2 * dj, k - 2 * dk), a0 = q(n, i - di, j - dj, k - dk);
-            const T a1 = q(n, i, j, k), a2 = q(n, i + di, j + dj, k + dk);
-            v = clipe(T(0.5) * (a0 + a1) - T(1.0 / 6.0) * (vls(a0, a1, a2) - vls(am, a0, a1)), a0, a1);
-        }
-        e[n][f] = v;
-    }
+// ---- FP64 decisions of the limiters on the integer pipe (double), plain
+// compares for the FP32 arithmetic of the mixed-precision form
+__device__ inline bool same_sign(double a, double b) { return isame_sign(a, b); }
+__device__ inline bool same_sign(float a, float b) { return a * b > 0.0f; }
+__device__ inline bool abs_lt(double a, double b) { return iabs_lt2(a, b); }  // |a| < |b|
+__device__ inline bool abs_lt(float a, float b) { return fabsf(a) < fabsf(b); }
+__device__ inline double mag_sign(double m, double s) { return isign(iabs(m), s); }  // |m| with the sign of s
+__device__ inline float mag_sign(float m, float s) { return copysignf(fabsf(m), s); }
+__device__ inline double clip2(double e, double a, double b) { return imin(imax(e, imin(a, b)), imax(a, b)); }
+__device__ inline float clip2(float e, float a, float b) { return fminf(fmaxf(e, fminf(a, b)), fmaxf(a, b)); }
+__device__ inline bool gt0(double x) { return igt0(x); }
+__device__ inline bool gt0(float x) { return x > 0.0f; }
+__device__ inline bool le0(double x) { return ile0(x); }
+__device__ inline bool le0(float x) { return x <= 0.0f; }
+__device__ inline bool ge0(double x) { return ige0(x); }
+__device__ inline bool ge0(float x) { return x >= 0.0f; }
+__device__ inline bool above_small(double u) { return dbits(u) > dbits(kSmallVel); }          // u > small_vel
+__device__ inline bool above_small(float u) { return u > (float)kSmallVel; }
+__device__ inline bool below_msmall(double u) { return okey(u) < okey(-kSmallVel); }      // u < -small_vel
+__device__ inline bool below_msmall(float u) { return u < -(float)kSmallVel; }
+__device__ inline bool below_small_abs(double u) { return iabs_lt(u, kSmallVel); }        // |u| < small_vel
+__device__ inline bool below_small_abs(float u) { return fabsf(u) < (float)kSmallVel; }
+__device__ inline double absv(double x) { return iabs(x); }
+__device__ inline float absv(float x) { return fabsf(x); }
+__device__ inline double neg_if(bool c, double x) { return c ? bitsd(dbits(x) ^ ~kMag) : x; }
+__device__ inline float neg_if(bool c, float x) { return c ? -x : x; }
+
+// van Leer limited slope of the middle cell of (a, b, c):
+// copysign(min(|dsc|, |dsl|, |dsr|), dsc) where dsl dsr > 0, else 0
+template <typename T>
+__device__ inline T vls(T a, T b, T c) {
+    const T dsc = T(0.5) * (c - a), dsl = T(2) * (b - a), dsr = T(2) * (c - b);
+    if (!same_sign(dsl, dsr)) return T(0);
+    T m = abs_lt(dsl, dsr) ? dsl : dsr;
+    m = abs_lt(dsc, m) ? dsc : m;
+    return mag_sign(m, dsc);
 }
 
-// limited parabola of a cell: (sm, sp) from its two stored edges and s0
+// unlimited PPM edge value between cells with values a0, a1 and slopes s0, s1,
+// clipped to the two cells
+template <typename T>
+__device__ inline T ppm_edge(T a0, T a1, T s0, T s1) {
+    return clip2(T(0.5) * (a0 + a1) - T(1.0 / 6.0) * (s1 - s0), a0, a1);
+}
+
+// Edge value on the face with index k along d from the cell values
+// a(k-2), a(k-1), a(k), a(k+1) and the slopes s(k-1), s(k).  Wall-bounded z:
+// the wall faces take the boundary (ghost) value, the faces one cell inside
+// the one-sided fourth-order formula clipped to the two adjacent cells.
+template <typename T>
+__device__ inline T edge_at(bool walls, int k, int nz, T am2, T am1, T a0, T ap1, T sm1, T s0) {
+    if (walls) {
+        if (k == 0) return am1;
+        if (k == nz) return a0;
+        if (k == 1) return clip2(T(-0.2) * am2 + T(0.75) * am1 + T(0.5) * a0 - T(0.05) * ap1, am1, a0);
+        if (k == nz - 1) return clip2(T(-0.2) * ap1 + T(0.75) * a0 + T(0.5) * am1 - T(0.05) * am2, a0, am1);
+    }
+    return ppm_edge(am1, a0, sm1, s0);
+}
+
+// limited parabola of a cell (Colella-Woodward 1984): (sm, sp) from its two
+// edges and the cell value s0.  3 s0 - 2 sm = s0 + 2 (s0 - sm), and
+// 3 s0 - 2 sp = s0 - 2 (sp - s0).
 template <typename T>
 __device__ inline void cw84(T s0, T& sm, T& sp) {
-    if ((sp - s0) * (s0 - sm) <= T(0)) {
+    const T dp = sp - s0, dm = s0 - sm;
+    if (!same_sign(dp, dm)) {
         sp = s0;
         sm = s0;
-    } else if (fabs(sp - s0) >= T(2) * fabs(sm - s0)) {
-        sp = T(3) * s0 - T(2) * sm;
-    } else if (fabs(sm - s0) >= T(2) * fabs(sp - s0)) {
-        sm = T(3) * s0 - T(2) * sp;
+        return;
     }
+    const T dp2 = T(2) * dp, dm2 = T(2) * dm;
+    if (!abs_lt(dp, dm2)) sp = s0 + dm2;
+    else if (!abs_lt(dm, dp2)) sm = s0 - dp2;
 }
 
-// average of the limited parabola over the part of the cell that crosses its
-// high (trace_hi) or low (trace_lo) face in dt, sig = |u| dt / h
+// Average of the limited parabola (sm, s0, sp) over the part of the cell that
+// crosses its high face (hi = true) or low face in dt, sig = |u| dt / h:
+//   high: sp - h D + h g s6,   low: sm + h D + h g s6,
+// h = sig / 2, g = 1 - 2 sig / 3, D = sp - sm, s6 = 6 s0 - 3 (sm + sp).
 template <typename T>
-__device__ inline T trace_hi(T sm, T s0, T sp, T sig) {
-    const T s6 = T(6) * s0 - T(3) * (sm + sp);
-    return sp - T(0.5) * sig * ((sp - sm) - (T(1) - T(2.0 / 3.0) * sig) * s6);
-}
+struct TraceCoef {
+    T h, hg;
+    __device__ inline TraceCoef(T sig) {
+        h = T(0.5) * sig;
+        hg = h * (T(1) - T(2.0 / 3.0) * sig);
+    }
+};
 template <typename T>
-__device__ inline T trace_lo(T sm, T s0, T sp, T sig) {
-    const T s6 = T(6) * s0 - T(3) * (sm + sp);
-    return sm + T(0.5) * sig * ((sp - sm) + (T(1) - T(2.0 / 3.0) * sig) * s6);
+__device__ inline T ppm_trace(bool hi, T sm, T s0, T sp, const TraceCoef<T>& c) {
+    const T D = sp - sm, s6 = T(6) * s0 - T(3) * (sm + sp);
+    return c.hg * s6 + (neg_if(hi, c.h) * D + (hi ? sp : sm));
 }
 
 // Wall face treatment (SetZEdgeBCs): tangential components take the interior
@@ -123,17 +145,18 @@ __device__ inline void zbc(const Grid& g, int k, int n, T& lo, T& hi) {
     }
 }
 
+// upwind state with AMReX-Hydro's small_vel: the mean of both states where
+// |vel| < small_vel
 template <typename T>
 __device__ inline T upwind(T vel, T lo, T hi) {
-    const T st = (vel >= T(0)) ? lo : hi;
-    const T fu = (fabs(vel) < T(kSmallVel)) ? T(0) : T(1);
-    return fu * st + (T(1) - fu) * T(0.5) * (lo + hi);
+    if (below_small_abs(vel)) return T(0.5) * (lo + hi);
+    return ge0(vel) ? lo : hi;
 }
 template <typename T>
 __device__ inline T riemann(T lo, T hi) {
-    const T st = (lo + hi >= T(0)) ? lo : hi;
-    const bool ltm = (lo <= T(0) && hi >= T(0)) || (fabs(lo + hi) < T(kSmallVel));
-    return ltm ? T(0) : st;
+    const T sum = lo + hi;
+    const bool ltm = (le0(lo) && ge0(hi)) || below_small_abs(sum);
+    return ltm ? T(0) : (ge0(sum) ? lo : hi);
 }
 
 template <typename T>
@@ -146,66 +169,280 @@ struct C3 {
 };
 
 // ---- stage 1 of both passes: left/right states of all components on d-faces.
-// MODE 0 (pre-MAC): the characteristic speed is the cell velocity component d;
-// MODE 1 (post-MAC): the face velocities; states are scaled by rho.
-// Pre-MAC also writes the Riemann-solved advective velocity and the states of
-// the two transverse components upwinded with it; post-MAC writes the states of
-// all three components upwinded with the MAC velocity.
-template <int MODE, typename T, int NC = 3>
-__global__ void k_faces(Grid g, int d, const double* vel, C3<T> E, Dt<T> dtdx, T rho, const double* umac_d, P3<T> LO, P3<T> HI, T* ad,
-                        P3<T> edge) {
-    int i, j, k;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (!face_of(g, d, t, i, j, k)) return;
-    VelFPT<T> q{vel, g, T(1)};
-    const int di = (d == 0), dj = (d == 1), dk = (d == 2);
-    const bool wl = (d == 2 && !g.zper && k == 0), wh = (d == 2 && !g.zper && k == g.nz);
-    const long long f = fidx(g, d, i, j, k);
-    const long long fm = fidx(g, d, i - di, j - dj, k - dk), fp = fidx(g, d, i + di, j + dj, k + dk);
-    const T s = dtdx.v[d];
-    // characteristic speeds: cell velocities (pre-MAC) or the face velocities
-    // of the low / high face of each cell (post-MAC)
-    T ul = T(0), uh = T(0), umf = T(0);
-    if (MODE == 0) {
-        if (!wl) ul = q(d, i - di, j - dj, k - dk);
-        if (!wh) uh = q(d, i, j, k);
-    } else {
-        umf = (T)umac_d[f];
-        ul = umf;  // high face of cell c - e_d
-        uh = umf;  // low face of cell c
+// MODE 0 (pre-MAC): the characteristic speed of a cell is its velocity
+// component d, so one trace per cell (its downwind face; the other face
+// takes the cell value).  Computes the unlimited edges from the slopes and
+// stores them (reused by the post-MAC pass), writes the left/right states, the
+// Riemann-solved advective velocity and the two transverse components
+// upwinded with it.
+// MODE 1 (post-MAC): the speed is the MAC velocity of the face, so one trace
+// per face (from its upwind cell); states are scaled by rho and all NC
+// components are upwinded with the MAC velocity.  EDGES = 0 reads the stored
+// unlimited edges, EDGES = 1 computes them (a scalar's only pass).
+//
+// Every cell's slope, edge and limited parabola is computed once per
+// component: the y and z kernels march along a column of faces and carry
+// them, the x kernel passes them between neighbouring lanes of a warp.
+struct PpmArgs {
+    Grid g;
+    int d;
+    const double* vel;   // advected field(s), NC components of N
+    const double* umac;  // MAC velocity on d-faces (MODE 1)
+};
+
+template <typename T, int NC>
+struct PpmOut {
+    T* E[3];   // unlimited edges (MODE 0 writes, MODE 1 EDGES = 0 reads)
+    T* LO[3];  // left / right states
+    T* HI[3];
+    T* TE[3];  // upwinded states
+    T* ad;     // advective velocity (MODE 0)
+};
+
+// the face states of one component on the face between cells with the
+// limited parabolas (pm, p0, pp) (low cell) and (qm, q0, qp) (high cell)
+// for the MAC velocity u (MODE 1)
+template <typename T>
+__device__ inline void face_states_mac(T u, T s, T pm, T p0, T pp, T qm, T q0, T qp, T& l, T& h) {
+    l = p0;
+    h = q0;
+    const bool up = above_small(u), dn = below_msmall(u);
+    if (up || dn) {
+        const TraceCoef<T> c(absv(u) * s);
+        const T t = ppm_trace(up, up ? pm : qm, up ? p0 : q0, up ? pp : qp, c);
+        if (up) l = t;
+        else h = t;
     }
-    T lo[3], hi[3];
+}
+
+// a[n] for a run-time n without addressing the register array
+template <typename T, int NC>
+__device__ inline T sel(const T (&a)[NC], int n) {
+    T r = a[0];
+#pragma unroll
+    for (int m = 1; m < NC; ++m)
+        if (n == m) r = a[m];
+    return r;
+}
+
+// y (d = 1) and z (d = 2) faces: one thread per (i, transverse index, chunk of
+// faces along d).  Face m lies between cells m-1 and m.
+template <typename T, int NC, int MODE, int EDGES>
+__global__ void __launch_bounds__(256) k_ppm_col(PpmArgs A, T s, T rho, PpmOut<T, NC> O, int chunk) {
+    const Grid& g = A.g;
+    const int d = A.d;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.nx) return;
+    const bool walls = (d == 2 && !g.zper);
+    const int nl = d == 1 ? g.ny : g.nz;  // cells along d
+    const int nf = walls ? g.nz + 1 : nl;  // faces along d
+    const int no = d == 1 ? g.nz : g.ny;
+    const int o = blockIdx.y % no, ch = blockIdx.y / no;
+    const int m0 = ch * chunk, m1 = min(m0 + chunk, nf);
+    if (m0 >= m1) return;
+    VelFPT<T> q{A.vel, g, T(1)};
+    auto val = [&](int n, int m) -> T {
+        if (!walls) m = ((m % nl) + nl) % nl;
+        return d == 1 ? q(n, i, m, o) : q(n, i, o, m);
+    };
+    auto fid = [&](int m) -> long long { return d == 1 ? fidx(g, 1, i, m, o) : fidx(g, 2, i, o, m); };
+    // per component at face m: a(m-1), a(m), a(m+1), the slope s(m), the edge
+    // e(m), and cell m-1's high-face trace (MODE 0) or limited parabola (MODE 1)
+    T am1[NC], a0[NC], ap1[NC], sl0[NC], e0[NC], lo0[NC], pm[NC], pp[NC];
+    {
+        T u = T(0);
+        if (MODE == 0) u = val(d, m0 - 1);
+#pragma unroll
+        for (int n = 0; n < NC; ++n) {
+            T em1;
+            am1[n] = val(n, m0 - 1);
+            a0[n] = val(n, m0);
+            if (MODE == 1 && !EDGES) {
+                em1 = (walls && m0 == 0) ? am1[n] : O.E[n][fid(m0 - 1)];  // no face below a wall
+                e0[n] = O.E[n][fid(m0)];
+            } else {
+                const T x3 = val(n, m0 - 3), x2 = val(n, m0 - 2);
+                ap1[n] = val(n, m0 + 1);
+                const T s2 = vls(x3, x2, am1[n]), s1 = vls(x2, am1[n], a0[n]);
+                sl0[n] = vls(am1[n], a0[n], ap1[n]);
+                em1 = edge_at(walls, m0 - 1, g.nz, x3, x2, am1[n], a0[n], s2, s1);
+                e0[n] = edge_at(walls, m0, g.nz, x2, am1[n], a0[n], ap1[n], s1, sl0[n]);
+            }
+            T sm = em1, sp = e0[n];
+            cw84(am1[n], sm, sp);
+            pm[n] = sm;
+            pp[n] = sp;
+            lo0[n] = am1[n];
+            if (MODE == 0 && above_small(u)) lo0[n] = ppm_trace(true, sm, am1[n], sp, TraceCoef<T>(absv(u) * s));
+        }
+    }
+    for (int m = m0; m < m1; ++m) {
+        const long long f = fid(m);
+        T e1[NC], ap2[NC], s1[NC];
+#pragma unroll
+        for (int n = 0; n < NC; ++n) {
+            if (MODE == 1 && !EDGES) {
+                e1[n] = O.E[n][fid(m + 1)];
+                ap1[n] = val(n, m + 1);
+            } else {
+                ap2[n] = val(n, m + 2);
+                s1[n] = vls(a0[n], ap1[n], ap2[n]);
+                e1[n] = edge_at(walls, m + 1, g.nz, am1[n], a0[n], ap1[n], ap2[n], sl0[n], s1[n]);
+            }
+        }
+        T lo[NC], hi[NC];
+        if (MODE == 0) {
+            const T u = sel(a0, d);  // cell m's velocity component d
+            const bool up = above_small(u), dn = below_msmall(u);
+            const TraceCoef<T> c(absv(u) * s);
+#pragma unroll
+            for (int n = 0; n < NC; ++n) {
+                T sm = e0[n], sp = e1[n];
+                cw84(a0[n], sm, sp);
+                T h = a0[n], lnext = a0[n];
+                if (up || dn) {
+                    const T t = ppm_trace(up, sm, a0[n], sp, c);
+                    if (up) lnext = t;
+                    else h = t;
+                }
+                lo[n] = lo0[n];
+                hi[n] = h;
+                lo0[n] = lnext;
+            }
+        } else {
+            const T u = (T)A.umac[f];
+#pragma unroll
+            for (int n = 0; n < NC; ++n) {
+                T sm = e0[n], sp = e1[n];
+                cw84(a0[n], sm, sp);
+                T l, h;
+                face_states_mac(u, s, pm[n], am1[n], pp[n], sm, a0[n], sp, l, h);
+                lo[n] = rho * l;
+                hi[n] = rho * h;
+                pm[n] = sm;
+                pp[n] = sp;
+            }
+        }
+        if (walls) {
+#pragma unroll
+            for (int n = 0; n < NC; ++n) {
+                if (m == 0) lo[n] = T(0);
+                if (m == g.nz) hi[n] = T(0);
+                zbc(g, m, n, lo[n], hi[n]);
+            }
+        }
+#pragma unroll
+        for (int n = 0; n < NC; ++n) {
+            O.LO[n][f] = lo[n];
+            O.HI[n][f] = hi[n];
+            if (MODE == 0) O.E[n][f] = e0[n];
+        }
+        if (MODE == 0) {
+            const T a = riemann(sel(lo, d), sel(hi, d));
+            O.ad[f] = a;
+#pragma unroll
+            for (int n = 0; n < NC; ++n)
+                if (n != d) O.TE[n][f] = upwind(a, lo[n], hi[n]);
+        } else {
+            const T u = (T)A.umac[f];
+#pragma unroll
+            for (int n = 0; n < NC; ++n) O.TE[n][f] = upwind(u, lo[n], hi[n]);
+        }
+#pragma unroll
+        for (int n = 0; n < NC; ++n) {
+            e0[n] = e1[n];
+            am1[n] = a0[n];
+            a0[n] = ap1[n];
+            if (!(MODE == 1 && !EDGES)) {
+                ap1[n] = ap2[n];
+                sl0[n] = s1[n];
+            }
+        }
+    }
+}
+
+// x faces: each warp covers XF consecutive faces of one x row; lane l holds
+// cell c = XF seg + l - H.  Computed edges (H = 2, XF = 29): every lane forms
+// its cell's slope, lanes >= 1 the edge of face c with the slope of lane l-1,
+// lanes 1..30 their cell's parabola with the edge of lane l+1, lanes 2..30 the
+// states of face c.  Stored edges (H = 1, XF = 31): every lane reads both
+// edges of its cell and forms its parabola; lanes 1..31 form face c.  Every
+// lane does the same work, so no lane's extra cell stalls the others.
+template <typename T, int NC, int MODE, int EDGES>
+__global__ void __launch_bounds__(256) k_ppm_x(PpmArgs A, T s, T rho, PpmOut<T, NC> O) {
+    constexpr bool LOADE = (MODE == 1 && !EDGES);
+    constexpr int H = LOADE ? 1 : 2, XF = LOADE ? 31 : 29;
+    const Grid& g = A.g;
+    const int nseg = (g.nx + XF - 1) / XF;
+    const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const long long rows = (long long)g.ny * g.nz;
+    if (w >= rows * nseg) return;  // whole warps leave together
+    const int row = (int)(w / nseg), seg = (int)(w % nseg);
+    const int c = seg * XF + lane - H;
+    const bool own = lane >= H && lane <= (LOADE ? 31 : 30) && c < g.nx;
+    auto wx = [&](int x) { return ((x % g.nx) + g.nx) % g.nx; };
+    const long long rb = (long long)row * g.nx;  // row base: cells and x faces share the index
+    const long long fc = rb + wx(c);
+    auto ld = [&](int n, int x) -> T { return (T)A.vel[n * g.N + rb + wx(x)]; };
+    const unsigned FULL = 0xffffffffu;
+    T lo[NC], hi[NC], ev[NC];
+    T u = T(0);
+    if (MODE == 0) u = ld(0, c);
+    else u = (T)A.umac[fc];
+    const bool up = above_small(u), dn = below_msmall(u);
+    const TraceCoef<T> tc(absv(u) * s);
+#pragma unroll
     for (int n = 0; n < NC; ++n) {
-        T l = T(0), h = T(0);
-        if (!wl) {  // high-side trace of cell c - e_d
-            const T s0 = q(n, i - di, j - dj, k - dk);
-            T sm = E.p[n][fm], sp = E.p[n][f];
-            cw84(s0, sm, sp);
-            l = (ul > T(kSmallVel)) ? trace_hi(sm, s0, sp, fabs(ul) * s) : s0;
+        const T a0 = ld(n, c);
+        T e0, e1, am1;
+        if (LOADE) {
+            e0 = O.E[n][fc];
+            e1 = O.E[n][rb + wx(c + 1)];
+            am1 = __shfl_up_sync(FULL, a0, 1);
+        } else {
+            am1 = ld(n, c - 1);
+            const T ap1 = ld(n, c + 1);
+            const T sl = vls(am1, a0, ap1);
+            const T slm = __shfl_up_sync(FULL, sl, 1);
+            e0 = ppm_edge(am1, a0, slm, sl);
+            e1 = __shfl_down_sync(FULL, e0, 1);
         }
-        if (!wh) {  // low-side trace of cell c
-            const T s0 = q(n, i, j, k);
-            T sm = E.p[n][f], sp = E.p[n][fp];
-            cw84(s0, sm, sp);
-            h = (uh < -T(kSmallVel)) ? trace_lo(sm, s0, sp, fabs(uh) * s) : s0;
+        ev[n] = e0;
+        T sm = e0, sp = e1;
+        cw84(a0, sm, sp);
+        if (MODE == 0) {
+            T h = a0, lnext = a0;
+            if (up || dn) {
+                const T t = ppm_trace(up, sm, a0, sp, tc);
+                if (up) lnext = t;
+                else h = t;
+            }
+            lo[n] = __shfl_up_sync(FULL, lnext, 1);
+            hi[n] = h;
+        } else {
+            const T pm = __shfl_up_sync(FULL, sm, 1), pp = __shfl_up_sync(FULL, sp, 1);
+            T l, h;
+            face_states_mac(u, s, pm, am1, pp, sm, a0, sp, l, h);
+            lo[n] = rho * l;
+            hi[n] = rho * h;
         }
-        if (MODE == 1) {
-            l *= rho;
-            h *= rho;
-        }
-        if (d == 2) zbc(g, k, n, l, h);
-        lo[n] = l;
-        hi[n] = h;
-        LO.p[n][f] = l;
-        HI.p[n][f] = h;
+    }
+    if (!own) return;
+#pragma unroll
+    for (int n = 0; n < NC; ++n) {
+        O.LO[n][fc] = lo[n];
+        O.HI[n][fc] = hi[n];
+        if (MODE == 0) O.E[n][fc] = ev[n];
     }
     if (MODE == 0) {
-        const T a = riemann(lo[d], hi[d]);
-        ad[f] = a;
-        for (int n = 0; n < 3; ++n)
-            if (n != d) edge.p[n][f] = upwind(a, lo[n], hi[n]);
+        const T a = riemann(lo[0], hi[0]);
+        O.ad[fc] = a;
+#pragma unroll
+        for (int n = 1; n < NC; ++n) O.TE[n][fc] = upwind(a, lo[n], hi[n]);
     } else {
-        for (int n = 0; n < NC; ++n) edge.p[n][f] = upwind(umf, lo[n], hi[n]);
+#pragma unroll
+        for (int n = 0; n < NC; ++n) O.TE[n][fc] = upwind(u, lo[n], hi[n]);
     }
 }
 
@@ -271,7 +508,7 @@ __global__ void __launch_bounds__(256, 2) k_adv_trans2(Grid g, int a, const doub
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_of(g, a, t, i, j, k)) return;
-    VelFPT<T> q{vel, g, rho};
+    VelFPT<T> q{vel, g, T(1)};
     const bool wl = (a == 2 && !g.zper && k == 0), wh = (a == 2 && !g.zper && k == g.nz);
     const long long f = fidx(g, a, i, j, k);
     const T u = (T)ua[f];
@@ -299,20 +536,26 @@ __global__ void __launch_bounds__(256, 2) k_adv_trans2(Grid g, int a, const doub
         vlp2 = (T)vb2[l1b];
         vlm2 = (T)vb2[l0b];
     }
+    // rho cb (v+ - v-) of each correction, shared by the components: the cell
+    // values enter unscaled
+    const T rh1 = rho * cb1 * (vhp1 - vhm1), rl1 = rho * cb1 * (vlp1 - vlm1);
+    const T rh2 = rho * cb2 * (vhp2 - vhm2), rl2 = rho * cb2 * (vlp2 - vlm2);
+    const bool usmall = below_small_abs(u), upos = ge0(u);
+    auto pick = [&](T l, T h) { return usmall ? T(0.5) * (l + h) : (upos ? l : h); };
     for (int n = 0; n < NC; ++n) {
         const T l0 = LO.p[n][f], h0 = HI.p[n][f];
         const T qh = wh ? T(0) : q(n, i, j, k), ql = wl ? T(0) : q(n, ci, cj, ck);
         T l = l0, h = h0;
-        if (!wh) h += -cb1 * (vhp1 * E1.p[n][h1a] - vhm1 * E1.p[n][h0a]) + cb1 * qh * (vhp1 - vhm1);
-        if (!wl) l += -cb1 * (vlp1 * E1.p[n][l1a] - vlm1 * E1.p[n][l0a]) + cb1 * ql * (vlp1 - vlm1);
+        if (!wh) h = qh * rh1 + (h0 - cb1 * (vhp1 * E1.p[n][h1a] - vhm1 * E1.p[n][h0a]));
+        if (!wl) l = ql * rl1 + (l0 - cb1 * (vlp1 * E1.p[n][l1a] - vlm1 * E1.p[n][l0a]));
         if (a == 2) zbc(g, k, n, l, h);
-        out1.p[n][f] = upwind(u, l, h);
+        out1.p[n][f] = pick(l, h);
         l = l0;
         h = h0;
-        if (!wh) h += -cb2 * (vhp2 * E2.p[n][h1b] - vhm2 * E2.p[n][h0b]) + cb2 * qh * (vhp2 - vhm2);
-        if (!wl) l += -cb2 * (vlp2 * E2.p[n][l1b] - vlm2 * E2.p[n][l0b]) + cb2 * ql * (vlp2 - vlm2);
+        if (!wh) h = qh * rh2 + (h0 - cb2 * (vhp2 * E2.p[n][h1b] - vhm2 * E2.p[n][h0b]));
+        if (!wl) l = ql * rl2 + (l0 - cb2 * (vlp2 * E2.p[n][l1b] - vlm2 * E2.p[n][l0b]));
         if (a == 2) zbc(g, k, n, l, h);
-        out2.p[n][f] = upwind(u, l, h);
+        out2.p[n][f] = pick(l, h);
     }
 }
 
@@ -320,12 +563,12 @@ __global__ void __launch_bounds__(256, 2) k_adv_trans2(Grid g, int a, const doub
 // The forces enter scaled by rho for the velocity (forces = (src + divtau) / rho)
 // and as they are for a scalar (NC = 1: forces = src + diff, AdvOp_Godunov.H:114-329).
 template <typename T, int NC = 3>
-__global__ void __launch_bounds__(256, 3) k_adv_flux(Grid g, int d, const double* vel, const double* forces, T rho, T dt, T c1, T c2,
+__global__ void __launch_bounds__(256, 2) k_adv_flux(Grid g, int d, const double* vel, const double* forces, T rho, T dt, T c1, T c2,
                                                      C3<double> U, C3<T> LO, C3<T> HI, C3<T> T1, C3<T> T2, P3<T> Fl) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_of(g, d, t, i, j, k)) return;
-    VelFPT<T> q{vel, g, rho};
+    VelFPT<T> q{vel, g, T(1)};
     CellFOT<T> Fo{forces, g};
     const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
     const bool wl = (d == 2 && !g.zper && k == 0), wh = (d == 2 && !g.zper && k == g.nz);
@@ -339,31 +582,23 @@ __global__ void __launch_bounds__(256, 3) k_adv_flux(Grid g, int d, const double
     T l1p = 0, l1m = 0, l2p = 0, l2m = 0, h1p = 0, h1m = 0, h2p = 0, h2m = 0;
     if (!wl) { l1p = (T)U.p[b1][lp1]; l1m = (T)U.p[b1][lm1]; l2p = (T)U.p[b2][lp2]; l2m = (T)U.p[b2][lm2]; }
     if (!wh) { h1p = (T)U.p[b1][hp1]; h1m = (T)U.p[b1][hm1]; h2p = (T)U.p[b2][hp2]; h2m = (T)U.p[b2][hm2]; }
+    // rho (c1 (v1+ - v1-) + c2 (v2+ - v2-)) of each side and dt/2 times the
+    // force scale, shared by the components: the cell values enter unscaled
+    const T rl = rho * (c1 * (l1p - l1m) + c2 * (l2p - l2m)), rh = rho * (c1 * (h1p - h1m) + c2 * (h2p - h2m));
+    const T hdt = T(0.5) * dt * (NC == 3 ? rho : T(1));
+    const bool usmall = below_small_abs(um), upos = ge0(um);
     for (int n = 0; n < NC; ++n) {
         T stl = T(0), sth = T(0);
         if (!wl) {
-            const T qc = q(n, li, lj, lk);
-            T s = LO.p[n][f];
-            s -= c1 * (T1.p[n][lp1] * l1p - T1.p[n][lm1] * l1m);
-            s -= c2 * (T2.p[n][lp2] * l2p - T2.p[n][lm2] * l2m);
-            s += c1 * qc * (l1p - l1m);
-            s += c2 * qc * (l2p - l2m);
-            s += T(0.5) * dt * ((NC == 3 ? rho : T(1)) * Fo(n, li, lj, lk));
-            stl = s;
+            const T x1 = T1.p[n][lp1] * l1p - T1.p[n][lm1] * l1m, x2 = T2.p[n][lp2] * l2p - T2.p[n][lm2] * l2m;
+            stl = hdt * Fo(n, li, lj, lk) + (q(n, li, lj, lk) * rl + ((LO.p[n][f] - c1 * x1) - c2 * x2));
         }
         if (!wh) {
-            const T qc = q(n, i, j, k);
-            T s = HI.p[n][f];
-            s -= c1 * (T1.p[n][hp1] * h1p - T1.p[n][hm1] * h1m);
-            s -= c2 * (T2.p[n][hp2] * h2p - T2.p[n][hm2] * h2m);
-            s += c1 * qc * (h1p - h1m);
-            s += c2 * qc * (h2p - h2m);
-            s += T(0.5) * dt * ((NC == 3 ? rho : T(1)) * Fo(n, i, j, k));
-            sth = s;
+            const T x1 = T1.p[n][hp1] * h1p - T1.p[n][hm1] * h1m, x2 = T2.p[n][hp2] * h2p - T2.p[n][hm2] * h2m;
+            sth = hdt * Fo(n, i, j, k) + (q(n, i, j, k) * rh + ((HI.p[n][f] - c1 * x1) - c2 * x2));
         }
         if (d == 2) zbc(g, k, n, stl, sth);
-        T st = (um >= T(0)) ? stl : sth;
-        if (fabs(um) < T(kSmallVel)) st = T(0.5) * (stl + sth);
+        const T st = usmall ? T(0.5) * (stl + sth) : (upos ? stl : sth);
         Fl.p[n][f] = um * st;
     }
 }
@@ -393,20 +628,39 @@ static T* tp(void* p) {
     return static_cast<T*>(p);
 }
 
+// stage 1 on the d-faces: the x kernel for d = 0, the column march otherwise
+constexpr int PPM_CHUNK = 32;
+template <typename T, int NC, int MODE, int EDGES>
+static void launch_ppm(Ctx& c, const Grid& g, int d, const double* vel, const double* umac, double dt, double rho, const PpmOut<T, NC>& O,
+                       double bytes) {
+    const PpmArgs A{g, d, vel, umac};
+    const T s = T(dt / hd(g, d));
+    if (d == 0) {
+        constexpr int XF = (MODE == 1 && !EDGES) ? 31 : 29;
+        const long long warps = (long long)g.ny * g.nz * ((g.nx + XF - 1) / XF);
+        KS_LAUNCH(c, (k_ppm_x<T, NC, MODE, EDGES>), nblocks(warps * 32, BS), BS, bytes, A, s, T(rho), O);
+    } else {
+        const int nf = (d == 2) ? nzfaces(g) : g.ny;
+        const int nch = (nf + PPM_CHUNK - 1) / PPM_CHUNK, chunk = (nf + nch - 1) / nch;
+        const int bx = g.nx >= BS ? BS : 32 * ((g.nx + 31) / 32);
+        const dim3 grid((unsigned)((g.nx + bx - 1) / bx), (unsigned)((d == 1 ? g.nz : g.ny) * nch));
+        KS_LAUNCH(c, (k_ppm_col<T, NC, MODE, EDGES>), grid, bx, bytes, A, s, T(rho), O, chunk);
+    }
+}
+
 template <typename T>
 static void premac_t(Ctx& c, const Grid& g, const double* vel, const double* forces, double dt, GodunovBufs& B, double* mac[3]) {
     const double BT = (double)sizeof(T), B8 = 8.0;
-    const Dt<T> dtdx{{T(dt / g.dx), T(dt / g.dy), T(dt / g.dz)}};
-    for (int d = 0; d < 3; ++d)
-        KS_LAUNCH(c, k_edges<T>, nblocks(nfaces(g, d), BS), BS, B8 * 3.0 * g.N + BT * 3.0 * nfaces(g, d), g, d, vel, tp<T>(B.edge[d][0]),
-                  tp<T>(B.edge[d][1]), tp<T>(B.edge[d][2]));
     for (int d = 0; d < 3; ++d) {
-        C3<T> E{{tp<T>(B.edge[d][0]), tp<T>(B.edge[d][1]), tp<T>(B.edge[d][2])}};
-        P3<T> LO{{tp<T>(B.lo[d][0]), tp<T>(B.lo[d][1]), tp<T>(B.lo[d][2])}}, HI{{tp<T>(B.hi[d][0]), tp<T>(B.hi[d][1]), tp<T>(B.hi[d][2])}};
-        P3<T> ED{{tp<T>(B.tedge[d][0]), tp<T>(B.tedge[d][1]), tp<T>(B.tedge[d][2])}};
-        const double nf = (double)nfaces(g, d);
-        KS_LAUNCH(c, (k_faces<0, T>), nblocks(nfaces(g, d), BS), BS, B8 * 3.0 * g.N + BT * 12.0 * nf, g, d, vel, E, dtdx, T(1), nullptr,
-                  LO, HI, tp<T>(B.ad[d]), ED);
+        PpmOut<T, 3> O{};
+        for (int n = 0; n < 3; ++n) {
+            O.E[n] = tp<T>(B.edge[d][n]);
+            O.LO[n] = tp<T>(B.lo[d][n]);
+            O.HI[n] = tp<T>(B.hi[d][n]);
+            O.TE[n] = tp<T>(B.tedge[d][n]);
+        }
+        O.ad = tp<T>(B.ad[d]);
+        launch_ppm<T, 3, 0, 1>(c, g, d, vel, nullptr, dt, 1.0, O, B8 * 3.0 * g.N + BT * 12.0 * nfaces(g, d));
     }
     // (a, b, n): states on a-faces of component n corrected along b
     const int tpl[6][3] = {{1, 2, 0}, {2, 1, 0}, {0, 2, 1}, {2, 0, 1}, {0, 1, 2}, {1, 0, 2}};
@@ -431,14 +685,16 @@ template <typename T>
 static void advection_t(Ctx& c, const Grid& g, const double* vel, const double* forces, const double* mac[3], double dt, double rho,
                         GodunovBufs& B, double* conv) {
     const double BT = (double)sizeof(T), B8 = 8.0;
-    const Dt<T> dtdx{{T(dt / g.dx), T(dt / g.dy), T(dt / g.dz)}};
     // the unlimited edge values of the pre-MAC pass are reused (same field)
     for (int a = 0; a < 3; ++a) {
-        C3<T> E{{tp<T>(B.edge[a][0]), tp<T>(B.edge[a][1]), tp<T>(B.edge[a][2])}};
-        P3<T> LO{{tp<T>(B.lo[a][0]), tp<T>(B.lo[a][1]), tp<T>(B.lo[a][2])}}, HI{{tp<T>(B.hi[a][0]), tp<T>(B.hi[a][1]), tp<T>(B.hi[a][2])}};
-        P3<T> ED{{tp<T>(B.tedge[a][0]), tp<T>(B.tedge[a][1]), tp<T>(B.tedge[a][2])}};
-        KS_LAUNCH(c, (k_faces<1, T>), nblocks(nfaces(g, a), BS), BS, B8 * (3.0 * g.N + nfaces(g, a)) + BT * 12.0 * nfaces(g, a), g, a, vel,
-                  E, dtdx, T(rho), mac[a], LO, HI, (T*)nullptr, ED);
+        PpmOut<T, 3> O{};
+        for (int n = 0; n < 3; ++n) {
+            O.E[n] = tp<T>(B.edge[a][n]);
+            O.LO[n] = tp<T>(B.lo[a][n]);
+            O.HI[n] = tp<T>(B.hi[a][n]);
+            O.TE[n] = tp<T>(B.tedge[a][n]);
+        }
+        launch_ppm<T, 3, 1, 0>(c, g, a, vel, mac[a], dt, rho, O, B8 * (3.0 * g.N + nfaces(g, a)) + BT * 12.0 * nfaces(g, a));
     }
     for (int a = 0; a < 3; ++a) {
         const int b1 = (a + 1) % 3, b2 = (a + 2) % 3;
@@ -472,21 +728,18 @@ static void advection_t(Ctx& c, const Grid& g, const double* vel, const double* 
 
 // Godunov fluxes of rho s for a cell scalar s (hoextrap at z walls, like a
 // tangential velocity component) with the forces fs = src + diff, and conv =
-// -div(flux) (AdvOp_Godunov.H:114-329).  FP64; edges[3] holds the scalar's
-// unlimited edge values; the other face arrays are the component-0 slots of B.
+// -div(flux) (AdvOp_Godunov.H:114-329).  FP64; the face arrays are the
+// component-0 slots of B.
 void launch_scalar_advection(Ctx& c, const Grid& g, const double* s, const double* fs, const double* mac[3], double dt, double rho,
-                             double* const edges[3], GodunovBufs& B, double* conv) {
+                             GodunovBufs& B, double* conv) {
     using T = double;
     const double B8 = 8.0;
-    const Dt<T> dtdx{{dt / g.dx, dt / g.dy, dt / g.dz}};
-    for (int d = 0; d < 3; ++d)
-        KS_LAUNCH(c, (k_edges<T, 1>), nblocks(nfaces(g, d), BS), BS, B8 * (g.N + nfaces(g, d)), g, d, s, edges[d], nullptr, nullptr);
     for (int a = 0; a < 3; ++a) {
-        C3<T> E{{edges[a], nullptr, nullptr}};
-        P3<T> LO{{tp<T>(B.lo[a][0]), nullptr, nullptr}}, HI{{tp<T>(B.hi[a][0]), nullptr, nullptr}};
-        P3<T> ED{{tp<T>(B.tedge[a][0]), nullptr, nullptr}};
-        KS_LAUNCH(c, (k_faces<1, T, 1>), nblocks(nfaces(g, a), BS), BS, B8 * (g.N + 5.0 * nfaces(g, a)), g, a, s, E, dtdx, T(rho), mac[a], LO,
-                  HI, (T*)nullptr, ED);
+        PpmOut<T, 1> O{};
+        O.LO[0] = tp<T>(B.lo[a][0]);
+        O.HI[0] = tp<T>(B.hi[a][0]);
+        O.TE[0] = tp<T>(B.tedge[a][0]);
+        launch_ppm<T, 1, 1, 1>(c, g, a, s, mac[a], dt, rho, O, B8 * (g.N + 4.0 * nfaces(g, a)));
     }
     for (int a = 0; a < 3; ++a) {
         const int b1 = (a + 1) % 3, b2 = (a + 2) % 3;

@@ -373,6 +373,8 @@ void Sim::alloc() {
         const size_t nn = (size_t)dm[0] * dm[1] * (dm[2] + (g_.zper ? 0 : 1));
         mgtot += 3 * nc + 4 * nn;
     }
+    // the multigrid and face kernels index a level with 32-bit integers
+    if ((long long)g_.nx * g_.ny * (g_.nz + 1) >= (1LL << 31)) throw KsError(KS_ERR_UNSUPPORTED, "grid of 2^31 or more nodes");
     mgbuf_.alloc(mgtot);
     q = mgbuf_.p;
     double h[3] = {g_.dx, g_.dy, g_.dz};
@@ -409,7 +411,6 @@ void Sim::alloc() {
     if (temp_) {
         for (DevBuf<double>* b : {&theta_, &theta_old_, &theta_nph_, &alpha_, &tdiff_, &tconv_, &ttmp_, &tb_, &tdinv_}) b->alloc(N);
         tgz_.alloc((size_t)g_.nx * g_.ny);
-        tedge_.alloc(2 * N + NF);
         tparts_.alloc((size_t)tdiff_blocks(g_));
         if (!godunov_) tconv_old_.alloc(N);
         if (gb_.flux[0][0] == nullptr) throw KsError(KS_ERR_UNSUPPORTED, "temperature transport needs the face scratch");
@@ -1134,8 +1135,7 @@ void Sim::pre_advance() {
 void Sim::temperature_predictor(double dt) {
     const long long N = g_.N;
     const double* cmac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
-    double* edges[3] = {tedge_.p, tedge_.p + N, tedge_.p + 2 * N};
-    launch_scalar_advection(ctx_, g_, theta_old_.p, tdiff_.p, cmac, dt, rho_, edges, gb_, tconv_.p);
+    launch_scalar_advection(ctx_, g_, theta_old_.p, tdiff_.p, cmac, dt, rho_, gb_, tconv_.p);
     launch_scalar_pred(ctx_, N, theta_old_.p, tconv_.p, tdiff_.p, theta_.p, dt, rho_, diff_fac());
     if (diff_type_ == 0) {  // explicit RK2 correction with the same wall data
         launch_tdiff(ctx_, g_, theta_.p, alpha_.p, tbc(), ttmp_.p, 2, theta_.p, tdiff_.p, nullptr, nullptr, nullptr, dt, rho_, 0.0);

@@ -192,9 +192,9 @@ void launch_premac(Ctx& c, const Grid& g, const double* vel_old, const double* f
 void launch_advection(Ctx& c, const Grid& g, const double* vel_old, const double* forces, const double* mac[3], double dt, double rho,
                       GodunovBufs& B, double* conv, int fp32);
 // Godunov fluxes and conv = -div(flux) of rho s for a cell scalar s with forces fs = src + diff (FP64);
-// edges: three face arrays for the scalar's edge values; B: component-0 face slots reused as scratch
+// B: component-0 face slots reused as scratch
 void launch_scalar_advection(Ctx& c, const Grid& g, const double* s, const double* fs, const double* mac[3], double dt, double rho,
-                             double* const edges[3], GodunovBufs& B, double* conv);
+                             GodunovBufs& B, double* conv);
 
 // ---- temperature transport (ks_temperature.cu), FP64
 // ABLFieldInit uniform-wind branch: velocity = U + sinusoidal perturbation (pert != 0)

@@ -45,9 +45,35 @@ inline int parts_for(long long n) {
     return (int)(b < MAXPARTS ? (b < 1 ? 1 : b) : MAXPARTS);
 }
 
+// Index maps use 32-bit arithmetic (every level holds fewer than 2^31
+// points): a 64-bit division costs as much issue as the FP64 work of these
+// light kernels.
+__device__ inline void split3(unsigned t, unsigned nx, unsigned ny, int& i, int& j, int& k) {
+    const unsigned r = t / nx;
+    i = (int)(t - r * nx);
+    k = (int)(r / ny);
+    j = (int)(r - (unsigned)k * ny);
+}
+
+// running maximum of |x|: FP64 on the integer pipe (NaN kept), FP32 compares
+template <typename T>
+struct MaxAbs;
+template <>
+struct MaxAbs<double> {
+    long long b = 0;
+    __device__ inline void add(double x) { b = imax_abs(b, x); }
+    __device__ inline double get() const { return bitsd(b); }
+};
+template <>
+struct MaxAbs<float> {
+    float m = 0.0f;
+    __device__ inline void add(float x) { m = (x != x) ? x : fmaxf(m, fabsf(x)); }
+    __device__ inline double get() const { return (double)m; }
+};
+
 // ---------------------------------------------------------------- cell-centred
 template <typename T>
-__device__ inline long long ci3(const CCLevelT<T>& L, int i, int j, int k) { return ((long long)k * L.ny + j) * L.nx + i; }
+__device__ inline int ci3(const CCLevelT<T>& L, int i, int j, int k) { return (k * L.ny + j) * L.nx + i; }
 
 // Weighted neighbour sum S = sum_m (w_m / d) p_m of the cell's class
 // (interior, wall-adjacent, single layer; Neumann walls drop a z neighbour).
@@ -75,78 +101,89 @@ __device__ inline T cc_gs_point(const CCLevelT<T>& L, const T* p, int i, int j, 
 
 template <typename T>
 __global__ void k_cc_gsrb(CCLevelT<T> L, T beta, int color) {
-    const long long half = (long long)L.nx * L.ny * L.nz / 2;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const unsigned half = (unsigned)(L.nx * L.ny * L.nz / 2);
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= half) return;
-    const int hx = L.nx / 2;
-    const int i2 = (int)(t % hx);
-    const long long r = t / hx;
-    const int j = (int)(r % L.ny), k = (int)(r / L.ny);
+    int i2, j, k;
+    split3(t, (unsigned)(L.nx / 2), (unsigned)L.ny, i2, j, k);
     const int i = 2 * i2 + ((j + k + color) & 1);
-    const long long c = ci3(L, i, j, k);
+    const int c = ci3(L, i, j, k);
     L.phi[c] = cc_gs_point(L, L.phi, i, j, k, L.rhs[c]);
     (void)beta;
 }
 
 template <typename T>
 __global__ void k_cc_resid(CCLevelT<T> L, T beta, double* parts) {
-    const long long N = (long long)L.nx * L.ny * L.nz;
-    double mx = 0.0;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N; t += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(t % L.nx);
-        const long long r = t / L.nx;
-        const int j = (int)(r % L.ny), k = (int)(r / L.ny);
+    const unsigned N = (unsigned)(L.nx * L.ny * L.nz);
+    MaxAbs<T> mx;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x) {
+        int i, j, k;
+        split3(t, (unsigned)L.nx, (unsigned)L.ny, i, j, k);
         int cls;
         const T S = cc_nsum(L, L.phi, i, j, k, cls);
         const T v = L.rhs[t] - L.dg[cls] * (L.phi[t] - S);
         L.res[t] = v;
-        mx = nmax(mx, fabs((double)v));
+        mx.add(v);
     }
-    mx = bred<1>(mx);
-    if (threadIdx.x == 0 && parts) parts[blockIdx.x] = mx;
+    const double m = bred<1>(mx.get());
+    if (threadIdx.x == 0 && parts) parts[blockIdx.x] = m;
 }
 
 template <typename T>
 __global__ void k_cc_restrict(CCLevelT<T> F, CCLevelT<T> C) {
-    const long long N = (long long)C.nx * C.ny * C.nz;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const unsigned N = (unsigned)(C.nx * C.ny * C.nz);
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= N) return;
-    const int i = (int)(t % C.nx);
-    const long long r = t / C.nx;
-    const int j = (int)(r % C.ny), k = (int)(r / C.ny);
-    T s = T(0);
-    for (int c = 0; c < 2; ++c)
-        for (int b = 0; b < 2; ++b)
-            for (int a = 0; a < 2; ++a) s += F.res[ci3(F, 2 * i + a, 2 * j + b, 2 * k + c)];
+    int i, j, k;
+    split3(t, (unsigned)C.nx, (unsigned)C.ny, i, j, k);
+    const T* r = F.res + ci3(F, 2 * i, 2 * j, 2 * k);
+    const int sy = F.nx, sz = F.nx * F.ny;
+    const T s = ((r[0] + r[1]) + (r[sy] + r[sy + 1])) + ((r[sz] + r[sz + 1]) + (r[sz + sy] + r[sz + sy + 1]));
     C.rhs[t] = T(0.125) * s;
     C.phi[t] = T(0);
 }
 
 template <typename T>
 __global__ void k_cc_prolong(CCLevelT<T> F, CCLevelT<T> C) {
-    const long long N = (long long)F.nx * F.ny * F.nz;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const unsigned N = (unsigned)(F.nx * F.ny * F.nz);
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= N) return;
-    const int i = (int)(t % F.nx);
-    const long long r = t / F.nx;
-    const int j = (int)(r % F.ny), k = (int)(r / F.ny);
+    int i, j, k;
+    split3(t, (unsigned)F.nx, (unsigned)F.ny, i, j, k);
     F.phi[t] += C.phi[ci3(C, i / 2, j / 2, k / 2)];
 }
 
-template <typename T>
+// Bottom solve: red-black sweeps by one CTA.  Levels of up to BOTTOM_SMEM
+// points are staged in shared memory (phi and rhs), larger ones sweep in
+// global memory.
+constexpr int BOTTOM_SMEM = 2048;
+template <typename T, bool SMEM>
 __global__ void k_cc_bottom(CCLevelT<T> L, T beta, int sweeps) {
-    const long long N = (long long)L.nx * L.ny * L.nz;
+    const int N = L.nx * L.ny * L.nz;
+    __shared__ T sp[SMEM ? BOTTOM_SMEM : 1], sr[SMEM ? BOTTOM_SMEM : 1];
+    T* p = L.phi;
+    const T* r = L.rhs;
+    if (SMEM) {
+        for (int t = threadIdx.x; t < N; t += blockDim.x) {
+            sp[t] = L.phi[t];
+            sr[t] = L.rhs[t];
+        }
+        __syncthreads();
+        p = sp;
+        r = sr;
+    }
     for (int s = 0; s < sweeps; ++s)
         for (int color = 0; color < 2; ++color) {
-            for (long long t = threadIdx.x; t < N; t += blockDim.x) {
-                const int i = (int)(t % L.nx);
-                const long long r = t / L.nx;
-                const int j = (int)(r % L.ny), k = (int)(r / L.ny);
+            for (int t = threadIdx.x; t < N; t += blockDim.x) {
+                int i, j, k;
+                split3((unsigned)t, (unsigned)L.nx, (unsigned)L.ny, i, j, k);
                 if (((i + j + k) & 1) != color) continue;
-                L.phi[t] = cc_gs_point(L, L.phi, i, j, k, L.rhs[t]);
+                p[t] = cc_gs_point(L, p, i, j, k, r[t]);
             }
             __syncthreads();
         }
+    if (SMEM)
+        for (int t = threadIdx.x; t < N; t += blockDim.x) L.phi[t] = sp[t];
 }
 
 // ---------------------------------------------------------------- nodal
@@ -156,7 +193,7 @@ __device__ inline T nd_at(const NDLevelT<T>& L, const T* p, int i, int j, int k)
     j = j < 0 ? j + L.ny : (j >= L.ny ? j - L.ny : j);
     if (L.zper) k = k < 0 ? k + L.nz : (k >= L.nz ? k - L.nz : k);
     else k = k < 0 ? -k : (k >= L.nz ? 2 * (L.nz - 1) - k : k);
-    return p[((long long)k * L.ny + j) * L.nx + i];
+    return p[(k * L.ny + j) * L.nx + i];
 }
 
 // sigma * (27-point Q1 stencil) at node (i,j,k); the weights are symmetric in
@@ -173,11 +210,10 @@ __device__ inline T nd_ax(const NDLevelT<T>& L, const T* p, T sigma, int i, int 
         km = k == 0 ? 1 : k - 1;
         kp = k + 1 == L.nz ? L.nz - 2 : k + 1;
     }
-    const long long sx = 1, sy = L.nx, sz = (long long)L.nx * L.ny;
-    (void)sx;
-    const long long rm = km * sz, r0 = k * sz, rp = kp * sz;
-    const long long cm = jm * sy, c0 = j * sy, cp = jp * sy;
-    auto at = [&](long long r, long long c, int x) { return p[r + c + x]; };
+    const int sy = L.nx, sz = L.nx * L.ny;
+    const int rm = km * sz, r0 = k * sz, rp = kp * sz;
+    const int cm = jm * sy, c0 = j * sy, cp = jp * sy;
+    auto at = [&](int r, int c, int x) { return p[r + c + x]; };
     const T ctr = at(r0, c0, i);
     T fx = T(0), fy = T(0), fz = T(0);
     if (!L.faces_zero) {
@@ -195,32 +231,53 @@ __device__ inline T nd_ax(const NDLevelT<T>& L, const T* p, T sigma, int i, int 
     return sigma * s;
 }
 
+// sigma-scaled weight classes of the stencil (negated) and the Jacobi factor
+// omega / (sigma W_centre), formed on the host once per launch
+template <typename T>
+struct NdCoef {
+    T c13, c9, c3, c1, c0, c12, c10, c4, oinv;
+};
+template <typename T>
+inline NdCoef<T> nd_coef(const NDLevelT<T>& L, double sigma, double omega) {
+    NdCoef<T> c;
+    c.c13 = T(-sigma * (double)L.W[13]);
+    c.c9 = T(-sigma * (double)L.W[9]);
+    c.c3 = T(-sigma * (double)L.W[3]);
+    c.c1 = T(-sigma * (double)L.W[1]);
+    c.c0 = T(-sigma * (double)L.W[0]);
+    c.c12 = T(-sigma * (double)L.W[12]);
+    c.c10 = T(-sigma * (double)L.W[10]);
+    c.c4 = T(-sigma * (double)L.W[4]);
+    c.oinv = T(omega * (double)L.inv_diag);
+    return c;
+}
+
 // Column (z-marching) form of the same stencil for the sweeps over a whole
 // level: each thread walks k through a chunk of one (i, j) column.  Per node
 // plane it forms the in-plane corner sum P, the x- and y-neighbour sums Ex, Ey
 // and the centre value C once; node k combines planes k-1, k, k+1:
 //   A phi = W13 C0 + W9 P0 + W3 (Ex- + Ex+) + W1 (Ey- + Ey+) + W0 (P- + P+)
 //           [+ W12 Ex0 + W10 Ey0 + W4 (C- + C+) when face weights are non-zero],
-// about half the FP64 operations of the node-by-node sums.
+// about half the FP64 operations of the node-by-node sums; the residual is
+// one FMA chain from rhs with the sigma-scaled weights.
 // MODE 0: out = in + omega (rhs - A in) / diag.  MODE 1: the same plus block
 // maxima of |rhs - A in|.  MODE 2: res = rhs - A phi plus block maxima.
 template <typename T, int MODE>
-__global__ void k_nd_col(NDLevelT<T> L, T sigma, T omega, const T* in, T* out, int kc, double* parts) {
-    const long long sz = (long long)L.nx * L.ny;
+__global__ void k_nd_col(NDLevelT<T> L, NdCoef<T> w, const T* in, T* out, int kc, double* parts) {
+    const int sz = L.nx * L.ny;
     const int nch = (L.nz + kc - 1) / kc;
-    const long long M = sz * nch;
-    double mx = 0.0;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < M; t += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(t % L.nx);
-        const long long r = t / L.nx;
-        const int j = (int)(r % L.ny), ch = (int)(r / L.ny);
+    const unsigned M = (unsigned)(sz * nch);
+    MaxAbs<T> mx;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < M; t += gridDim.x * blockDim.x) {
+        int i, j, ch;
+        split3(t, (unsigned)L.nx, (unsigned)L.ny, i, j, ch);
         const int im = i == 0 ? L.nx - 1 : i - 1, ip = i + 1 == L.nx ? 0 : i + 1;
-        const long long cm = (long long)(j == 0 ? L.ny - 1 : j - 1) * L.nx, c0 = (long long)j * L.nx;
-        const long long cp = (long long)(j + 1 == L.ny ? 0 : j + 1) * L.nx;
+        const int cm = (j == 0 ? L.ny - 1 : j - 1) * L.nx, c0 = j * L.nx;
+        const int cp = (j + 1 == L.ny ? 0 : j + 1) * L.nx;
         auto plane = [&](int k, T& P, T& Ex, T& Ey, T& C) {
             if (L.zper) k = k < 0 ? k + L.nz : (k >= L.nz ? k - L.nz : k);
             else k = k < 0 ? -k : (k >= L.nz ? 2 * (L.nz - 1) - k : k);
-            const T* q = in + (long long)k * sz;
+            const T* q = in + k * sz;
             P = (q[cm + im] + q[cm + ip]) + (q[cp + im] + q[cp + ip]);
             Ex = q[c0 + im] + q[c0 + ip];
             Ey = q[cm + i] + q[cp + i];
@@ -233,13 +290,21 @@ __global__ void k_nd_col(NDLevelT<T> L, T sigma, T omega, const T* in, T* out, i
         for (int k = k0; k < k1; ++k) {
             T Pp, Exp, Eyp, Cp;
             plane(k + 1, Pp, Exp, Eyp, Cp);
-            T s = L.W[13] * C0 + L.W[9] * P0 + L.W[3] * (Exm + Exp) + L.W[1] * (Eym + Eyp) + L.W[0] * (Pm + Pp);
-            if (!L.faces_zero) s += L.W[12] * Ex0 + L.W[10] * Ey0 + L.W[4] * (Cm + Cp);
-            const long long idx = (long long)k * sz + c0 + i;
-            const T res = L.rhs[idx] - sigma * s;
+            const int idx = k * sz + c0 + i;
+            T res = L.rhs[idx];
+            res = w.c13 * C0 + res;
+            res = w.c9 * P0 + res;
+            res = w.c3 * (Exm + Exp) + res;
+            res = w.c1 * (Eym + Eyp) + res;
+            res = w.c0 * (Pm + Pp) + res;
+            if (!L.faces_zero) {
+                res = w.c12 * Ex0 + res;
+                res = w.c10 * Ey0 + res;
+                res = w.c4 * (Cm + Cp) + res;
+            }
             if (MODE == 2) L.res[idx] = res;
-            else out[idx] = C0 + omega * res * L.inv_diag;
-            if (MODE >= 1) mx = nmax(mx, fabs((double)res));
+            else out[idx] = w.oinv * res + C0;
+            if (MODE >= 1) mx.add(res);
             Pm = P0;
             Exm = Ex0;
             Eym = Ey0;
@@ -251,8 +316,8 @@ __global__ void k_nd_col(NDLevelT<T> L, T sigma, T omega, const T* in, T* out, i
         }
     }
     if (MODE >= 1) {
-        mx = bred<1>(mx);
-        if (threadIdx.x == 0 && parts) parts[blockIdx.x] = mx;
+        const double m = bred<1>(mx.get());
+        if (threadIdx.x == 0 && parts) parts[blockIdx.x] = m;
     }
 }
 
@@ -270,29 +335,33 @@ inline long long nd_cols(const NDLevelT<T>& L, int kc) {
 
 template <typename T>
 __global__ void k_nd_restrict(NDLevelT<T> F, NDLevelT<T> C) {
-    const long long N = (long long)C.nx * C.ny * C.nz;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const unsigned N = (unsigned)(C.nx * C.ny * C.nz);
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= N) return;
-    const int i = (int)(t % C.nx);
-    const long long r = t / C.nx;
-    const int j = (int)(r % C.ny), k = (int)(r / C.ny);
-    const T w1[3] = {T(0.25), T(0.5), T(0.25)};
-    T s = T(0);
-    for (int c = -1; c <= 1; ++c)
-        for (int b = -1; b <= 1; ++b)
-            for (int a = -1; a <= 1; ++a) s += w1[a + 1] * w1[b + 1] * w1[c + 1] * nd_at(F, F.res, 2 * i + a, 2 * j + b, 2 * k + c);
-    C.rhs[t] = s;
+    int i, j, k;
+    split3(t, (unsigned)C.nx, (unsigned)C.ny, i, j, k);
+    // full weighting: (1/4, 1/2, 1/4) in each direction, summed by weight class
+    T lay[3];
+    for (int c = -1; c <= 1; ++c) {
+        const T e = nd_at(F, F.res, 2 * i, 2 * j, 2 * k + c);
+        const T ex = nd_at(F, F.res, 2 * i - 1, 2 * j, 2 * k + c) + nd_at(F, F.res, 2 * i + 1, 2 * j, 2 * k + c);
+        const T ey = nd_at(F, F.res, 2 * i, 2 * j - 1, 2 * k + c) + nd_at(F, F.res, 2 * i, 2 * j + 1, 2 * k + c);
+        const T cr = (nd_at(F, F.res, 2 * i - 1, 2 * j - 1, 2 * k + c) + nd_at(F, F.res, 2 * i + 1, 2 * j - 1, 2 * k + c)) +
+                     (nd_at(F, F.res, 2 * i - 1, 2 * j + 1, 2 * k + c) + nd_at(F, F.res, 2 * i + 1, 2 * j + 1, 2 * k + c));
+        // in-plane weights 1/4 e + 1/8 (ex + ey) + 1/16 cr
+        lay[c + 1] = T(0.25) * e + (T(0.125) * (ex + ey) + T(0.0625) * cr);
+    }
+    C.rhs[t] = T(0.5) * lay[1] + T(0.25) * (lay[0] + lay[2]);
     C.phi[t] = T(0);
 }
 
 template <typename T>
 __global__ void k_nd_prolong(NDLevelT<T> F, NDLevelT<T> C) {
-    const long long N = (long long)F.nx * F.ny * F.nz;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const unsigned N = (unsigned)(F.nx * F.ny * F.nz);
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= N) return;
-    const int i = (int)(t % F.nx);
-    const long long r = t / F.nx;
-    const int j = (int)(r % F.ny), k = (int)(r / F.ny);
+    int i, j, k;
+    split3(t, (unsigned)F.nx, (unsigned)F.ny, i, j, k);
     const int ci = i >> 1, cj = j >> 1, ck = k >> 1, oi = i & 1, oj = j & 1, ok = k & 1;
     T s = T(0);
     for (int c = 0; c <= ok; ++c)
@@ -302,20 +371,38 @@ __global__ void k_nd_prolong(NDLevelT<T> F, NDLevelT<T> C) {
     F.phi[t] += (cnt == 1) ? s : (cnt == 2 ? T(0.5) * s : (cnt == 4 ? T(0.25) * s : T(0.125) * s));
 }
 
-template <typename T>
+// Bottom solve: weighted-Jacobi sweeps by one CTA, staged in shared memory
+// (phi, rhs and the sweep's output) for levels of up to BOTTOM_SMEM nodes
+template <typename T, bool SMEM>
 __global__ void k_nd_bottom(NDLevelT<T> L, T sigma, T omega, int sweeps) {
-    const long long N = (long long)L.nx * L.ny * L.nz;
-    for (int s = 0; s < sweeps; ++s) {
-        for (long long t = threadIdx.x; t < N; t += blockDim.x) {
-            const int i = (int)(t % L.nx);
-            const long long r = t / L.nx;
-            const int j = (int)(r % L.ny), k = (int)(r / L.ny);
-            L.tmp[t] = L.phi[t] + omega * (L.rhs[t] - nd_ax(L, L.phi, sigma, i, j, k)) * L.inv_diag;
+    const int N = L.nx * L.ny * L.nz;
+    __shared__ T sp[SMEM ? BOTTOM_SMEM : 1], sr[SMEM ? BOTTOM_SMEM : 1], st[SMEM ? BOTTOM_SMEM : 1];
+    T* p = L.phi;
+    const T* r = L.rhs;
+    T* q = L.tmp;
+    if (SMEM) {
+        for (int t = threadIdx.x; t < N; t += blockDim.x) {
+            sp[t] = L.phi[t];
+            sr[t] = L.rhs[t];
         }
         __syncthreads();
-        for (long long t = threadIdx.x; t < N; t += blockDim.x) L.phi[t] = L.tmp[t];
-        __syncthreads();
+        p = sp;
+        r = sr;
+        q = st;
     }
+    for (int s = 0; s < sweeps; ++s) {
+        for (int t = threadIdx.x; t < N; t += blockDim.x) {
+            int i, j, k;
+            split3((unsigned)t, (unsigned)L.nx, (unsigned)L.ny, i, j, k);
+            q[t] = p[t] + omega * (r[t] - nd_ax(L, p, sigma, i, j, k)) * L.inv_diag;
+        }
+        __syncthreads();
+        T* x = p;
+        p = q;
+        q = x;
+    }
+    // p holds the last sweep's output
+    for (int t = threadIdx.x; t < N; t += blockDim.x) L.phi[t] = p[t];
 }
 
 // defect correction helpers: rhs32 = (float) r64, phi32 = 0 ; phi64 += phi32
@@ -363,19 +450,21 @@ void launch_cc_prolong(Ctx& c, const CCLevelT<T>& F, const CCLevelT<T>& C) {
 }
 template <typename T>
 void launch_cc_bottom(Ctx& c, const CCLevelT<T>& L, double beta, int sweeps) {
-    KS_LAUNCH(c, k_cc_bottom<T>, 1, 256, sizeof(T) * 3.0 * ncc(L), L, T(beta), sweeps);
+    if (ncc(L) <= BOTTOM_SMEM) KS_LAUNCH(c, (k_cc_bottom<T, true>), 1, 256, sizeof(T) * 3.0 * ncc(L), L, T(beta), sweeps);
+    else KS_LAUNCH(c, (k_cc_bottom<T, false>), 1, 256, sizeof(T) * 3.0 * ncc(L), L, T(beta), sweeps);
 }
 template <typename T>
 void launch_nd_jacobi(Ctx& c, const NDLevelT<T>& L, double sigma, double omega, const T* in, T* out) {
     const int kc = nd_chunk(L);
-    KS_LAUNCH(c, (k_nd_col<T, 0>), nblocks(nd_cols(L, kc), BS), BS, sizeof(T) * 3.0 * nnd(L), L, T(sigma), T(omega), in, out, kc, nullptr);
+    KS_LAUNCH(c, (k_nd_col<T, 0>), nblocks(nd_cols(L, kc), BS), BS, sizeof(T) * 3.0 * nnd(L), L, nd_coef(L, sigma, omega), in, out, kc,
+              nullptr);
 }
 template <typename T>
 void launch_nd_resid(Ctx& c, const NDLevelT<T>& L, double sigma, double* parts, int* np) {
     const int kc = nd_chunk(L);
     const int n = parts_for(nd_cols(L, kc));
     if (np) *np = n;
-    KS_LAUNCH(c, (k_nd_col<T, 2>), n, BS, sizeof(T) * 3.0 * nnd(L), L, T(sigma), T(0), (const T*)L.phi, (T*)nullptr, kc, parts);
+    KS_LAUNCH(c, (k_nd_col<T, 2>), n, BS, sizeof(T) * 3.0 * nnd(L), L, nd_coef(L, sigma, 0.0), (const T*)L.phi, (T*)nullptr, kc, parts);
 }
 template <typename T>
 void launch_nd_restrict(Ctx& c, const NDLevelT<T>& F, const NDLevelT<T>& C) {
@@ -387,14 +476,15 @@ void launch_nd_prolong(Ctx& c, const NDLevelT<T>& F, const NDLevelT<T>& C) {
 }
 template <typename T>
 void launch_nd_bottom(Ctx& c, const NDLevelT<T>& L, double sigma, double omega, int sweeps) {
-    KS_LAUNCH(c, k_nd_bottom<T>, 1, 256, sizeof(T) * 4.0 * nnd(L), L, T(sigma), T(omega), sweeps);
+    if (nnd(L) <= BOTTOM_SMEM) KS_LAUNCH(c, (k_nd_bottom<T, true>), 1, 256, sizeof(T) * 4.0 * nnd(L), L, T(sigma), T(omega), sweeps);
+    else KS_LAUNCH(c, (k_nd_bottom<T, false>), 1, 256, sizeof(T) * 4.0 * nnd(L), L, T(sigma), T(omega), sweeps);
 }
 void launch_nd_jacobi_norm(Ctx& c, const NDLevelT<double>& L, double sigma, double omega, const double* in, double* out, double* parts,
                            int* np) {
     const int kc = nd_chunk(L);
     const int n = parts_for(nd_cols(L, kc));
     *np = n;
-    KS_LAUNCH(c, (k_nd_col<double, 1>), n, BS, 8.0 * 3.0 * nnd(L), L, sigma, omega, in, out, kc, parts);
+    KS_LAUNCH(c, (k_nd_col<double, 1>), n, BS, 8.0 * 3.0 * nnd(L), L, nd_coef(L, sigma, omega), in, out, kc, parts);
 }
 void launch_to_f32(Ctx& c, const double* r, float* rhs, float* phi, long long n) {
     KS_LAUNCH(c, k_to_f32, nblocks(n, BS), BS, 16.0 * n, r, rhs, phi, n);

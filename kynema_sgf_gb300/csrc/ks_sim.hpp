@@ -357,7 +357,7 @@ class Sim {
     double ablf_h_ = 0.0, ablf_target_[2] = {0.0, 0.0};
     int tdif_it_ = 0;
     MGParams tdif_;
-    DevBuf<double> theta_, theta_old_, theta_nph_, alpha_, tdiff_, tconv_, ttmp_, tb_, tdinv_, tgz_, tedge_, tprof_, layer_, tparts_;
+    DevBuf<double> theta_, theta_old_, theta_nph_, alpha_, tdiff_, tconv_, ttmp_, tb_, tdinv_, tgz_, tprof_, layer_, tparts_;
     DevBuf<double> tconv_old_;  // MOL: the scalar's conv_term(Old)
     DevBuf<double> umac_[3];
     DevBuf<double> gbuf_;
