@@ -312,6 +312,113 @@ static double nodal_jacobi_weight(const double* W, double omega) {
     return omega;
 }
 
+// Inverse of the singular operator A (n x n, row-major, null space the
+// constants) restricted to the unknowns 1..n-1: the returned n x n matrix maps
+// a compatible right-hand side to the solution with x[0] = 0 (row and column 0
+// are zero).  Gauss-Jordan with partial pivoting; false when a pivot is below
+// 1e-12 of the largest entry (no direct bottom solve).
+static bool pinned_inverse(const std::vector<double>& A, int n, std::vector<double>& inv) {
+    const int m = n - 1;
+    if (m < 1) return false;
+    std::vector<double> a((size_t)m * 2 * m, 0.0);
+    double amax = 0.0;
+    for (int r = 0; r < m; ++r)
+        for (int c = 0; c < m; ++c) {
+            a[(size_t)r * 2 * m + c] = A[(size_t)(r + 1) * n + (c + 1)];
+            amax = std::max(amax, std::fabs(A[(size_t)(r + 1) * n + (c + 1)]));
+        }
+    for (int r = 0; r < m; ++r) a[(size_t)r * 2 * m + m + r] = 1.0;
+    for (int c = 0; c < m; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < m; ++r)
+            if (std::fabs(a[(size_t)r * 2 * m + c]) > std::fabs(a[(size_t)piv * 2 * m + c])) piv = r;
+        if (!(std::fabs(a[(size_t)piv * 2 * m + c]) > 1e-12 * amax)) return false;
+        if (piv != c)
+            for (int q = 0; q < 2 * m; ++q) std::swap(a[(size_t)c * 2 * m + q], a[(size_t)piv * 2 * m + q]);
+        const double d = 1.0 / a[(size_t)c * 2 * m + c];
+        for (int q = 0; q < 2 * m; ++q) a[(size_t)c * 2 * m + q] *= d;
+        for (int r = 0; r < m; ++r) {
+            if (r == c) continue;
+            const double f = a[(size_t)r * 2 * m + c];
+            if (f == 0.0) continue;
+            for (int q = 0; q < 2 * m; ++q) a[(size_t)r * 2 * m + q] -= f * a[(size_t)c * 2 * m + q];
+        }
+    }
+    inv.assign((size_t)n * n, 0.0);
+    for (int r = 0; r < m; ++r)
+        for (int c = 0; c < m; ++c) inv[(size_t)(r + 1) * n + (c + 1)] = a[(size_t)r * 2 * m + m + c];
+    return true;
+}
+
+// Bottom levels of up to 256 points are solved exactly: the coarsest MAC
+// operator d p - sum w p (scaled by -beta in the solve) and the coarsest nodal
+// stencil (scaled by sigma) are assembled on the host, their pinned inverses
+// uploaded once.  A bottom solve is then one small matrix-vector product in
+// place of relaxation sweeps, whose FP64 dependency chains on one SM cost
+// about 0.1 ms per solve on this GPU.
+void Sim::bottom_setup() {
+    constexpr int kMaxDirect = 256;
+    binv_cc_h_.clear();
+    binv_nd_h_.clear();
+    CCLevelDev& C = cc_.back();
+    NDLevelDev& D = nd_.back();
+    const int nc = C.nx * C.ny * C.nz, nn = D.nx * D.ny * D.nz;
+    if (nc <= kMaxDirect && cc_.size() > 1) {
+        std::vector<double> A((size_t)nc * nc, 0.0);
+        const double d0 = 2.0 * C.ix2 + 2.0 * C.iy2;
+        for (int k = 0; k < C.nz; ++k)
+            for (int j = 0; j < C.ny; ++j)
+                for (int i = 0; i < C.nx; ++i) {
+                    const int r = (k * C.ny + j) * C.nx + i;
+                    auto at = [&](int ii, int jj, int kk) { return (kk * C.ny + jj) * C.nx + ii; };
+                    const int ip = (i + 1) % C.nx, im = (i + C.nx - 1) % C.nx, jp = (j + 1) % C.ny, jm = (j + C.ny - 1) % C.ny;
+                    double d = d0;
+                    A[(size_t)r * nc + at(ip, j, k)] -= C.ix2;
+                    A[(size_t)r * nc + at(im, j, k)] -= C.ix2;
+                    A[(size_t)r * nc + at(i, jp, k)] -= C.iy2;
+                    A[(size_t)r * nc + at(i, jm, k)] -= C.iy2;
+                    if (C.zper) {
+                        d += 2.0 * C.iz2;
+                        A[(size_t)r * nc + at(i, j, (k + 1) % C.nz)] -= C.iz2;
+                        A[(size_t)r * nc + at(i, j, (k + C.nz - 1) % C.nz)] -= C.iz2;
+                    } else {
+                        if (k > 0) { d += C.iz2; A[(size_t)r * nc + at(i, j, k - 1)] -= C.iz2; }
+                        if (k < C.nz - 1) { d += C.iz2; A[(size_t)r * nc + at(i, j, k + 1)] -= C.iz2; }
+                    }
+                    A[(size_t)r * nc + r] += d;
+                }
+        if (!pinned_inverse(A, nc, binv_cc_h_)) binv_cc_h_.clear();
+    }
+    if (nn <= kMaxDirect && nd_.size() > 1) {
+        std::vector<double> A((size_t)nn * nn, 0.0);
+        for (int k = 0; k < D.nz; ++k)
+            for (int j = 0; j < D.ny; ++j)
+                for (int i = 0; i < D.nx; ++i) {
+                    const int r = (k * D.ny + j) * D.nx + i;
+                    for (int c = 0; c < 3; ++c)
+                        for (int b = 0; b < 3; ++b)
+                            for (int a = 0; a < 3; ++a) {
+                                const int w = (c * 3 + b) * 3 + a;
+                                if (D.faces_zero && (w == 4 || w == 10 || w == 12 || w == 14 || w == 16 || w == 22)) continue;
+                                const int ii = (i + a - 1 + D.nx) % D.nx, jj = (j + b - 1 + D.ny) % D.ny;
+                                int kk = k + c - 1;
+                                if (D.zper) kk = (kk + D.nz) % D.nz;
+                                else kk = kk < 0 ? -kk : (kk >= D.nz ? 2 * (D.nz - 1) - kk : kk);
+                                A[(size_t)r * nn + (kk * D.ny + jj) * D.nx + ii] += D.W[w];
+                            }
+                }
+        if (!pinned_inverse(A, nn, binv_nd_h_)) binv_nd_h_.clear();
+    }
+    binv_.alloc(std::max<size_t>(1, binv_cc_h_.size() + binv_nd_h_.size()));
+    if (!binv_cc_h_.empty())
+        ck(cudaMemcpy(binv_.p, binv_cc_h_.data(), binv_cc_h_.size() * sizeof(double), cudaMemcpyHostToDevice), "H2D bottom inverse");
+    if (!binv_nd_h_.empty())
+        ck(cudaMemcpy(binv_.p + binv_cc_h_.size(), binv_nd_h_.data(), binv_nd_h_.size() * sizeof(double), cudaMemcpyHostToDevice),
+           "H2D bottom inverse");
+    C.binv = binv_cc_h_.empty() ? nullptr : binv_.p;
+    D.binv = binv_nd_h_.empty() ? nullptr : binv_.p + binv_cc_h_.size();
+}
+
 // ---------------------------------------------------------------- allocation
 void Sim::alloc() {
     const size_t N = (size_t)g_.N, NF = (size_t)g_.NFz;
@@ -405,6 +512,7 @@ void Sim::alloc() {
         for (int d = 0; d < 3; ++d) h[d] *= 2;
     }
     nod_.omega = nodal_jacobi_weight(nd_[0].W, nod_.omega);
+    bottom_setup();
     parts_.alloc(4 * 1216);
     red_.alloc(8);
     if (temp_ || S_.ablf) layer_.alloc(3 * (size_t)g_.nz);
@@ -706,6 +814,14 @@ void Sim::set_mixed(int on) {
         Nd.phi = q; q += nn; Nd.rhs = q; q += nn; Nd.res = q; q += nn; Nd.tmp = q; q += nn;
         nd32_.push_back(Nd);
     }
+    // FP32 copies of the bottom inverses
+    std::vector<float> b32(binv_cc_h_.size() + binv_nd_h_.size());
+    for (size_t m = 0; m < binv_cc_h_.size(); ++m) b32[m] = (float)binv_cc_h_[m];
+    for (size_t m = 0; m < binv_nd_h_.size(); ++m) b32[binv_cc_h_.size() + m] = (float)binv_nd_h_[m];
+    binv32_.alloc(std::max<size_t>(1, b32.size()));
+    if (!b32.empty()) ck(cudaMemcpy(binv32_.p, b32.data(), b32.size() * sizeof(float), cudaMemcpyHostToDevice), "H2D bottom inverse");
+    cc32_.back().binv = binv_cc_h_.empty() ? nullptr : binv32_.p;
+    nd32_.back().binv = binv_nd_h_.empty() ? nullptr : binv32_.p + binv_cc_h_.size();
 }
 
 void Sim::mac_project() {

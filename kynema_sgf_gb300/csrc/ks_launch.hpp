@@ -314,6 +314,7 @@ struct CCLevelT {
     T gs[3][3];     // Gauss-Seidel neighbour weights w_m / d per class (x, y, z)
     T dg[3];        // diagonal -beta d per class
     T *phi, *rhs, *res;
+    const T* binv;  // bottom level: pinned inverse of d p - sum w p (row-major), or null
 };
 template <typename T>
 struct NDLevelT {
@@ -323,6 +324,7 @@ struct NDLevelT {
     T inv_diag;      // 1/(sigma W_centre)
     int faces_zero;  // face-neighbour weights vanish (equal spacings): skipped
     T *phi, *rhs, *res, *tmp;
+    const T* binv;  // bottom level: pinned inverse of the unscaled stencil (row-major), or null
 };
 using CCLevelDev = CCLevelT<double>;
 using NDLevelDev = NDLevelT<double>;

@@ -186,6 +186,20 @@ __global__ void k_cc_bottom(CCLevelT<T> L, T beta, int sweeps) {
         for (int t = threadIdx.x; t < N; t += blockDim.x) L.phi[t] = sp[t];
 }
 
+// Direct bottom solve: phi = scale * Binv rhs, Binv the pinned inverse of the
+// bottom level's operator (the solution with phi[0] = 0 of the singular
+// system), one warp per row with the lanes over the columns.
+template <typename T>
+__global__ void k_bottom_direct(const T* __restrict__ binv, int n, const T* rhs, T* phi, T scale) {
+    const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (r >= n) return;  // whole warps
+    const T* row = binv + (long long)r * n;
+    T acc = T(0);
+    for (int c = lane; c < n; c += 32) acc += row[c] * rhs[c];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) phi[r] = scale * acc;
+}
+
 // ---------------------------------------------------------------- nodal
 template <typename T>
 __device__ inline T nd_at(const NDLevelT<T>& L, const T* p, int i, int j, int k) {
@@ -450,6 +464,12 @@ void launch_cc_prolong(Ctx& c, const CCLevelT<T>& F, const CCLevelT<T>& C) {
 }
 template <typename T>
 void launch_cc_bottom(Ctx& c, const CCLevelT<T>& L, double beta, int sweeps) {
+    const int n = L.nx * L.ny * L.nz;
+    if (L.binv) {
+        KS_LAUNCH(c, k_bottom_direct<T>, (unsigned)((n + 7) / 8), 256, sizeof(T) * ((double)n * n + 2.0 * n), L.binv, n, (const T*)L.rhs,
+                  L.phi, T(-1.0 / beta));
+        return;
+    }
     if (ncc(L) <= BOTTOM_SMEM) KS_LAUNCH(c, (k_cc_bottom<T, true>), 1, 256, sizeof(T) * 3.0 * ncc(L), L, T(beta), sweeps);
     else KS_LAUNCH(c, (k_cc_bottom<T, false>), 1, 256, sizeof(T) * 3.0 * ncc(L), L, T(beta), sweeps);
 }
@@ -476,6 +496,12 @@ void launch_nd_prolong(Ctx& c, const NDLevelT<T>& F, const NDLevelT<T>& C) {
 }
 template <typename T>
 void launch_nd_bottom(Ctx& c, const NDLevelT<T>& L, double sigma, double omega, int sweeps) {
+    const int n = L.nx * L.ny * L.nz;
+    if (L.binv) {
+        KS_LAUNCH(c, k_bottom_direct<T>, (unsigned)((n + 7) / 8), 256, sizeof(T) * ((double)n * n + 2.0 * n), L.binv, n, (const T*)L.rhs,
+                  L.phi, T(1.0 / sigma));
+        return;
+    }
     if (nnd(L) <= BOTTOM_SMEM) KS_LAUNCH(c, (k_nd_bottom<T, true>), 1, 256, sizeof(T) * 4.0 * nnd(L), L, T(sigma), T(omega), sweeps);
     else KS_LAUNCH(c, (k_nd_bottom<T, false>), 1, 256, sizeof(T) * 4.0 * nnd(L), L, T(sigma), T(omega), sweeps);
 }

@@ -368,6 +368,11 @@ class Sim {
     std::vector<NDLevelT<float>> nd32_;
     DevBuf<double> mgbuf_;
     DevBuf<float> mgbuf32_;
+    // direct bottom solves: pinned inverses of the coarsest MAC and nodal operators
+    std::vector<double> binv_cc_h_, binv_nd_h_;
+    DevBuf<double> binv_;
+    DevBuf<float> binv32_;
+    void bottom_setup();
     DevBuf<double> parts_, red_;
     DevBuf<double> pts_, samp_;
     double* hred_ = nullptr;  // pinned
