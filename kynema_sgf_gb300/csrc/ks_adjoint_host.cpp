@@ -39,6 +39,11 @@ void Sim::adj_check() const {
 
 void Sim::adj_alloc() {
     adj_check();
+    // The recomputation from checkpoints must repeat each forward step bit for
+    // bit, so the Poisson solves start from zero (a warm start would carry
+    // state the checkpoints do not hold).
+    mg_warm_ = 0;
+    mac_prev_ok_ = false;
     if (adj_) return;
     auto S = std::make_unique<AdjState>();
     const size_t N = (size_t)g_.N, NF = (size_t)g_.NFz, N3 = 3 * N;

@@ -47,18 +47,19 @@ __host__ __device__ inline long long fidx(const Grid& g, int d, int i, int j, in
 // Cell-centred velocity (or rho*velocity) with fill-patch ghost values:
 // periodic wrap in x, y (and z); at walls the tangential components take the
 // high-order extrapolation to the face, (15 q0 - 10 q1 + 3 q2)/8, in every
-// ghost layer and the normal component is 0.  The stored field is FP64; the
-// value is returned in the arithmetic type T of the caller.
-template <typename T = double>
+// ghost layer and the normal component is 0.  The field is stored as S
+// (FP64, or its FP32 copy in the mixed-precision advection); the value is
+// returned in the arithmetic type T of the caller.
+template <typename T = double, typename S = double>
 struct VelFPT {
-    const double* v;
+    const S* v;
     Grid g;
     T scale;
     __device__ inline T operator()(int n, int i, int j, int k) const {
         i = wrapn(i, g.nx);
         j = wrapn(j, g.ny);
         const long long N = g.N;
-        const double* c = v + n * N;
+        const S* c = v + n * N;
         if (g.zper) return scale * (T)c[cidx(g, i, j, wrapn(k, g.nz))];
         if (k < 0) {
             if (n == 2) return T(0);
@@ -77,9 +78,9 @@ struct VelFPT {
 using VelFP = VelFPT<double>;
 
 // Cell field with first-order extrapolation ghosts in z (forces, viscosity).
-template <typename T = double>
+template <typename T = double, typename S = double>
 struct CellFOT {
-    const double* v;
+    const S* v;
     Grid g;
     __device__ inline T operator()(int n, int i, int j, int k) const {
         i = wrapn(i, g.nx);

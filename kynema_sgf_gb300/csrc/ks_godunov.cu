@@ -26,14 +26,16 @@ namespace {
 
 constexpr int BS = 256;
 
+// face index -> (i, j, k) in 32-bit arithmetic (a 64-bit division costs as
+// much issue as tens of FP64 operations)
 __device__ inline bool face_of(const Grid& g, int d, long long t, int& i, int& j, int& k) {
     const int nzl = (d == 2) ? nzfaces(g) : g.nz;
     const long long M = (long long)g.nx * g.ny * nzl;
     if (t >= M) return false;
-    i = (int)(t % g.nx);
-    const long long r = t / g.nx;
-    j = (int)(r % g.ny);
-    k = (int)(r / g.ny);
+    const unsigned u = (unsigned)t, r = u / (unsigned)g.nx;
+    i = (int)(u - r * (unsigned)g.nx);
+    k = (int)(r / (unsigned)g.ny);
+    j = (int)(r - (unsigned)k * (unsigned)g.ny);
     return true;
 }
 
@@ -183,11 +185,12 @@ struct C3 {
 // Every cell's slope, edge and limited parabola is computed once per
 // component: the y and z kernels march along a column of faces and carry
 // them, the x kernel passes them between neighbouring lanes of a warp.
+template <typename T>
 struct PpmArgs {
     Grid g;
     int d;
-    const double* vel;   // advected field(s), NC components of N
-    const double* umac;  // MAC velocity on d-faces (MODE 1)
+    const T* vel;   // advected field(s), NC components of N
+    const T* umac;  // MAC velocity on d-faces (MODE 1)
 };
 
 template <typename T, int NC>
@@ -228,7 +231,7 @@ __device__ inline T sel(const T (&a)[NC], int n) {
 // y (d = 1) and z (d = 2) faces: one thread per (i, transverse index, chunk of
 // faces along d).  Face m lies between cells m-1 and m.
 template <typename T, int NC, int MODE, int EDGES>
-__global__ void __launch_bounds__(256) k_ppm_col(PpmArgs A, T s, T rho, PpmOut<T, NC> O, int chunk) {
+__global__ void __launch_bounds__(256) k_ppm_col(PpmArgs<T> A, T s, T rho, PpmOut<T, NC> O, int chunk) {
     const Grid& g = A.g;
     const int d = A.d;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -240,7 +243,7 @@ __global__ void __launch_bounds__(256) k_ppm_col(PpmArgs A, T s, T rho, PpmOut<T
     const int o = blockIdx.y % no, ch = blockIdx.y / no;
     const int m0 = ch * chunk, m1 = min(m0 + chunk, nf);
     if (m0 >= m1) return;
-    VelFPT<T> q{A.vel, g, T(1)};
+    VelFPT<T, T> q{A.vel, g, T(1)};
     auto val = [&](int n, int m) -> T {
         if (!walls) m = ((m % nl) + nl) % nl;
         return d == 1 ? q(n, i, m, o) : q(n, i, o, m);
@@ -369,7 +372,7 @@ __global__ void __launch_bounds__(256) k_ppm_col(PpmArgs A, T s, T rho, PpmOut<T
 // edges of its cell and forms its parabola; lanes 1..31 form face c.  Every
 // lane does the same work, so no lane's extra cell stalls the others.
 template <typename T, int NC, int MODE, int EDGES>
-__global__ void __launch_bounds__(256) k_ppm_x(PpmArgs A, T s, T rho, PpmOut<T, NC> O) {
+__global__ void __launch_bounds__(256) k_ppm_x(PpmArgs<T> A, T s, T rho, PpmOut<T, NC> O) {
     constexpr bool LOADE = (MODE == 1 && !EDGES);
     constexpr int H = LOADE ? 1 : 2, XF = LOADE ? 31 : 29;
     const Grid& g = A.g;
@@ -472,12 +475,12 @@ __global__ void k_pm_trans(Grid g, int a, int b, int n, T cb, const T* lo_an, co
 
 // ---- pre-MAC stage 3: final normal velocity on d-faces
 template <typename T>
-__global__ void k_pm_final(Grid g, int d, const T* lo_dd, const T* hi_dd, const double* forces, T dt, T c1, T c2, C3<T> AD, const T* T1,
+__global__ void k_pm_final(Grid g, int d, const T* lo_dd, const T* hi_dd, const T* forces, T dt, T c1, T c2, C3<T> AD, const T* T1,
                            const T* T2, double* mac) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_of(g, d, t, i, j, k)) return;
-    CellFOT<T> F{forces, g};
+    CellFOT<T, T> F{forces, g};
     const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
     const long long f = fidx(g, d, i, j, k);
     const bool wl = (d == 2 && !g.zper && k == 0), wh = (d == 2 && !g.zper && k == g.nz);
@@ -502,13 +505,12 @@ __global__ void k_pm_final(Grid g, int d, const T* lo_dd, const T* hi_dd, const 
 // loaded once for the corrections along b1 = a+1 and b2 = a+2 (each is the
 // k_adv_trans arithmetic).
 template <typename T, int NC = 3>
-__global__ void __launch_bounds__(256, 2) k_adv_trans2(Grid g, int a, const double* vel, T rho, T cb1, T cb2, const double* ua,
-                                                       const double* vb1, const double* vb2, C3<T> LO, C3<T> HI, C3<T> E1, C3<T> E2,
-                                                       P3<T> out1, P3<T> out2) {
+__global__ void __launch_bounds__(256, 2) k_adv_trans2(Grid g, int a, const T* vel, T rho, T cb1, T cb2, const T* ua, const T* vb1,
+                                                       const T* vb2, C3<T> LO, C3<T> HI, C3<T> E1, C3<T> E2, P3<T> out1, P3<T> out2) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_of(g, a, t, i, j, k)) return;
-    VelFPT<T> q{vel, g, T(1)};
+    VelFPT<T, T> q{vel, g, T(1)};
     const bool wl = (a == 2 && !g.zper && k == 0), wh = (a == 2 && !g.zper && k == g.nz);
     const long long f = fidx(g, a, i, j, k);
     const T u = (T)ua[f];
@@ -563,13 +565,13 @@ __global__ void __launch_bounds__(256, 2) k_adv_trans2(Grid g, int a, const doub
 // The forces enter scaled by rho for the velocity (forces = (src + divtau) / rho)
 // and as they are for a scalar (NC = 1: forces = src + diff, AdvOp_Godunov.H:114-329).
 template <typename T, int NC = 3>
-__global__ void __launch_bounds__(256, 2) k_adv_flux(Grid g, int d, const double* vel, const double* forces, T rho, T dt, T c1, T c2,
-                                                     C3<double> U, C3<T> LO, C3<T> HI, C3<T> T1, C3<T> T2, P3<T> Fl) {
+__global__ void __launch_bounds__(256, 2) k_adv_flux(Grid g, int d, const T* vel, const T* forces, T rho, T dt, T c1, T c2, C3<T> U,
+                                                     C3<T> LO, C3<T> HI, C3<T> T1, C3<T> T2, P3<T> Fl) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_of(g, d, t, i, j, k)) return;
-    VelFPT<T> q{vel, g, T(1)};
-    CellFOT<T> Fo{forces, g};
+    VelFPT<T, T> q{vel, g, T(1)};
+    CellFOT<T, T> Fo{forces, g};
     const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
     const bool wl = (d == 2 && !g.zper && k == 0), wh = (d == 2 && !g.zper && k == g.nz);
     const long long f = fidx(g, d, i, j, k);
@@ -631,9 +633,9 @@ static T* tp(void* p) {
 // stage 1 on the d-faces: the x kernel for d = 0, the column march otherwise
 constexpr int PPM_CHUNK = 32;
 template <typename T, int NC, int MODE, int EDGES>
-static void launch_ppm(Ctx& c, const Grid& g, int d, const double* vel, const double* umac, double dt, double rho, const PpmOut<T, NC>& O,
+static void launch_ppm(Ctx& c, const Grid& g, int d, const T* vel, const T* umac, double dt, double rho, const PpmOut<T, NC>& O,
                        double bytes) {
-    const PpmArgs A{g, d, vel, umac};
+    const PpmArgs<T> A{g, d, vel, umac};
     const T s = T(dt / hd(g, d));
     if (d == 0) {
         constexpr int XF = (MODE == 1 && !EDGES) ? 31 : 29;
@@ -649,7 +651,7 @@ static void launch_ppm(Ctx& c, const Grid& g, int d, const double* vel, const do
 }
 
 template <typename T>
-static void premac_t(Ctx& c, const Grid& g, const double* vel, const double* forces, double dt, GodunovBufs& B, double* mac[3]) {
+static void premac_t(Ctx& c, const Grid& g, const T* vel, const T* forces, double dt, GodunovBufs& B, double* mac[3]) {
     const double BT = (double)sizeof(T), B8 = 8.0;
     for (int d = 0; d < 3; ++d) {
         PpmOut<T, 3> O{};
@@ -660,7 +662,7 @@ static void premac_t(Ctx& c, const Grid& g, const double* vel, const double* for
             O.TE[n] = tp<T>(B.tedge[d][n]);
         }
         O.ad = tp<T>(B.ad[d]);
-        launch_ppm<T, 3, 0, 1>(c, g, d, vel, nullptr, dt, 1.0, O, B8 * 3.0 * g.N + BT * 12.0 * nfaces(g, d));
+        launch_ppm<T, 3, 0, 1>(c, g, d, vel, (const T*)nullptr, dt, 1.0, O, BT * 3.0 * g.N + BT * 12.0 * nfaces(g, d));
     }
     // (a, b, n): states on a-faces of component n corrected along b
     const int tpl[6][3] = {{1, 2, 0}, {2, 1, 0}, {0, 2, 1}, {2, 0, 1}, {0, 1, 2}, {1, 0, 2}};
@@ -674,7 +676,7 @@ static void premac_t(Ctx& c, const Grid& g, const double* vel, const double* for
     C3<T> AD{{tp<T>(B.ad[0]), tp<T>(B.ad[1]), tp<T>(B.ad[2])}};
     for (int d = 0; d < 3; ++d) {
         const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
-        const double bytes = B8 * (1.0 * g.N + nfaces(g, d)) + BT * (3.0 * nfaces(g, d) + 2.0 * nfaces(g, b1) + 2.0 * nfaces(g, b2));
+        const double bytes = BT * (1.0 * g.N + 3.0 * nfaces(g, d) + 2.0 * nfaces(g, b1) + 2.0 * nfaces(g, b2)) + B8 * nfaces(g, d);
         const T c1 = T(dt / (4.0 * hd(g, b1))), c2 = T(dt / (4.0 * hd(g, b2)));
         KS_LAUNCH(c, k_pm_final<T>, nblocks(nfaces(g, d), BS), BS, bytes, g, d, tp<T>(B.lo[d][d]), tp<T>(B.hi[d][d]), forces, T(dt), c1, c2,
                   AD, tp<T>(B.tr[b1][b2][0]), tp<T>(B.tr[b2][b1][0]), mac[d]);
@@ -682,7 +684,7 @@ static void premac_t(Ctx& c, const Grid& g, const double* vel, const double* for
 }
 
 template <typename T>
-static void advection_t(Ctx& c, const Grid& g, const double* vel, const double* forces, const double* mac[3], double dt, double rho,
+static void advection_t(Ctx& c, const Grid& g, const T* vel, const T* forces, const T* const mac[3], double dt, double rho,
                         GodunovBufs& B, double* conv) {
     const double BT = (double)sizeof(T), B8 = 8.0;
     // the unlimited edge values of the pre-MAC pass are reused (same field)
@@ -694,12 +696,12 @@ static void advection_t(Ctx& c, const Grid& g, const double* vel, const double* 
             O.HI[n] = tp<T>(B.hi[a][n]);
             O.TE[n] = tp<T>(B.tedge[a][n]);
         }
-        launch_ppm<T, 3, 1, 0>(c, g, a, vel, mac[a], dt, rho, O, B8 * (3.0 * g.N + nfaces(g, a)) + BT * 12.0 * nfaces(g, a));
+        launch_ppm<T, 3, 1, 0>(c, g, a, vel, mac[a], dt, rho, O, BT * (3.0 * g.N + nfaces(g, a)) + BT * 12.0 * nfaces(g, a));
     }
     for (int a = 0; a < 3; ++a) {
         const int b1 = (a + 1) % 3, b2 = (a + 2) % 3;
         const double na = (double)nfaces(g, a), nt = (double)(nfaces(g, b1) + nfaces(g, b2));
-        const double bytes = B8 * (3.0 * g.N + na + nt) + BT * (12.0 * na + 3.0 * nt);
+        const double bytes = BT * (3.0 * g.N + na + nt) + BT * (12.0 * na + 3.0 * nt);
         C3<T> LO{{tp<T>(B.lo[a][0]), tp<T>(B.lo[a][1]), tp<T>(B.lo[a][2])}}, HI{{tp<T>(B.hi[a][0]), tp<T>(B.hi[a][1]), tp<T>(B.hi[a][2])}};
         C3<T> E1{{tp<T>(B.tedge[b1][0]), tp<T>(B.tedge[b1][1]), tp<T>(B.tedge[b1][2])}};
         C3<T> E2{{tp<T>(B.tedge[b2][0]), tp<T>(B.tedge[b2][1]), tp<T>(B.tedge[b2][2])}};
@@ -708,10 +710,10 @@ static void advection_t(Ctx& c, const Grid& g, const double* vel, const double* 
         KS_LAUNCH(c, k_adv_trans2<T>, nblocks(nfaces(g, a), BS), BS, bytes, g, a, vel, T(rho), T(dt / (3.0 * hd(g, b1))),
                   T(dt / (3.0 * hd(g, b2))), mac[a], mac[b1], mac[b2], LO, HI, E1, E2, O1, O2);
     }
-    C3<double> U{{mac[0], mac[1], mac[2]}};
+    C3<T> U{{mac[0], mac[1], mac[2]}};
     for (int d = 0; d < 3; ++d) {
         const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
-        const double bytes = B8 * (6.0 * g.N + nfaces(g, d) + nfaces(g, b1) + nfaces(g, b2)) +
+        const double bytes = BT * (6.0 * g.N + nfaces(g, d) + nfaces(g, b1) + nfaces(g, b2)) +
                              BT * (9.0 * nfaces(g, d) + 3.0 * nfaces(g, b1) + 3.0 * nfaces(g, b2));
         C3<T> LO{{tp<T>(B.lo[d][0]), tp<T>(B.lo[d][1]), tp<T>(B.lo[d][2])}}, HI{{tp<T>(B.hi[d][0]), tp<T>(B.hi[d][1]), tp<T>(B.hi[d][2])}};
         C3<T> T1{{tp<T>(B.tr[b1][b2][0]), tp<T>(B.tr[b1][b2][1]), tp<T>(B.tr[b1][b2][2])}};
@@ -730,7 +732,7 @@ static void advection_t(Ctx& c, const Grid& g, const double* vel, const double* 
 // tangential velocity component) with the forces fs = src + diff, and conv =
 // -div(flux) (AdvOp_Godunov.H:114-329).  FP64; the face arrays are the
 // component-0 slots of B.
-void launch_scalar_advection(Ctx& c, const Grid& g, const double* s, const double* fs, const double* mac[3], double dt, double rho,
+void launch_scalar_advection(Ctx& c, const Grid& g, const double* s, const double* fs, const double* const mac[3], double dt, double rho,
                              GodunovBufs& B, double* conv) {
     using T = double;
     const double B8 = 8.0;
@@ -766,15 +768,37 @@ void launch_scalar_advection(Ctx& c, const Grid& g, const double* s, const doubl
     KS_LAUNCH(c, (k_adv_div<T, 1>), nblocks(g.N, BS), BS, B8 * (3.0 * g.N + g.N), g, F, conv);
 }
 
-void launch_premac(Ctx& c, const Grid& g, const double* vel, const double* forces, double dt, GodunovBufs& B, double* mac[3], int fp32) {
-    if (fp32) premac_t<float>(c, g, vel, forces, dt, B, mac);
-    else premac_t<double>(c, g, vel, forces, dt, B, mac);
+// FP64 -> FP32 copy of an array (the mixed-precision advection reads FP32
+// copies of its inputs: a conversion per load would cost an FP64 issue slot)
+__global__ void k_to_single(const double* __restrict__ a, float* __restrict__ b, long long n) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) b[t] = (float)a[t];
+}
+static void to_single(Ctx& c, const double* a, float* b, long long n) {
+    const long long nb = (n + BS - 1) / BS;
+    KS_LAUNCH(c, k_to_single, (unsigned)(nb < 152 * 16 ? nb : 152 * 16), BS, 12.0 * n, a, b, n);
+}
+
+void launch_premac(Ctx& c, const Grid& g, const double* vel, const double* forces, double dt, GodunovBufs& B, double* mac[3], int fp32,
+                   GodunovIn32* in32) {
+    if (fp32) {
+        to_single(c, vel, in32->vel, 3 * g.N);
+        to_single(c, forces, in32->forces, 3 * g.N);
+        premac_t<float>(c, g, in32->vel, in32->forces, dt, B, mac);
+    } else {
+        premac_t<double>(c, g, vel, forces, dt, B, mac);
+    }
 }
 
 void launch_advection(Ctx& c, const Grid& g, const double* vel, const double* forces, const double* mac[3], double dt, double rho,
-                      GodunovBufs& B, double* conv, int fp32) {
-    if (fp32) advection_t<float>(c, g, vel, forces, mac, dt, rho, B, conv);
-    else advection_t<double>(c, g, vel, forces, mac, dt, rho, B, conv);
+                      GodunovBufs& B, double* conv, int fp32, GodunovIn32* in32) {
+    if (fp32) {
+        // vel and forces: the FP32 copies made by launch_premac of the same step
+        for (int d = 0; d < 3; ++d) to_single(c, mac[d], in32->mac[d], nfaces(g, d));
+        const float* m32[3] = {in32->mac[0], in32->mac[1], in32->mac[2]};
+        advection_t<float>(c, g, in32->vel, in32->forces, m32, dt, rho, B, conv);
+    } else {
+        advection_t<double>(c, g, vel, forces, mac, dt, rho, B, conv);
+    }
 }
 
 }  // namespace ks

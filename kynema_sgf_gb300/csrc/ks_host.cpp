@@ -27,6 +27,8 @@ Sim::Sim(const std::string& text) {
 
 Sim::~Sim() {
     if (ctx_.stream) cudaStreamSynchronize(ctx_.stream);
+    for (MGGraph* G : {&gcc_[0], &gcc_[1], &gnd_[0], &gnd_[1]})
+        if (G->exec) cudaGraphExecDestroy(G->exec);
     if (hred_) cudaFreeHost(hred_);
     if (ctx_.stream) cudaStreamDestroy(ctx_.stream);
 }
@@ -213,6 +215,12 @@ void Sim::setup(const Deck& D) {
     mg(tdif_, "diffusion");
     mg(tdif_, "temperature_diffusion");
     // I/O (IOManager::initialize_io, SimTime::parse_parameters)
+    // Warm start of the Poisson solves (not a reference key): the nodal projection starts
+    // from the current pressure, the MAC projection from the previous MAC potential.  The
+    // stopping test stays MLMG's: max-norm residual <= max(atol, rtol * max(|rhs|, initial
+    // residual)), so a solve ends at the same tolerance as one from zero, in fewer V-cycles.
+    mg_warm_ = D.flag("ks.mg_warm_start", 1);
+    mg_graphs_ = D.flag("ks.mg_graphs", 1);  // coarse V-cycle levels as CUDA graphs (not a reference key)
     restart_file_ = D.str("io.restart_file", "");
     plt_prefix_ = D.str("io.plot_file", "plt");
     chk_prefix_ = D.str("io.check_file", "chk");
@@ -317,6 +325,8 @@ static double nodal_jacobi_weight(const double* W, double omega) {
 // a compatible right-hand side to the solution with x[0] = 0 (row and column 0
 // are zero).  Gauss-Jordan with partial pivoting; false when a pivot is below
 // 1e-12 of the largest entry (no direct bottom solve).
+constexpr int kDirectBottom = 512;
+
 static bool pinned_inverse(const std::vector<double>& A, int n, std::vector<double>& inv) {
     const int m = n - 1;
     if (m < 1) return false;
@@ -350,14 +360,14 @@ static bool pinned_inverse(const std::vector<double>& A, int n, std::vector<doub
     return true;
 }
 
-// Bottom levels of up to 256 points are solved exactly: the coarsest MAC
+// Bottom levels of up to kDirectBottom points are solved exactly: the coarsest MAC
 // operator d p - sum w p (scaled by -beta in the solve) and the coarsest nodal
 // stencil (scaled by sigma) are assembled on the host, their pinned inverses
 // uploaded once.  A bottom solve is then one small matrix-vector product in
 // place of relaxation sweeps, whose FP64 dependency chains on one SM cost
 // about 0.1 ms per solve on this GPU.
 void Sim::bottom_setup() {
-    constexpr int kMaxDirect = 256;
+    constexpr int kMaxDirect = kDirectBottom;
     binv_cc_h_.clear();
     binv_nd_h_.clear();
     CCLevelDev& C = cc_.back();
@@ -472,6 +482,10 @@ void Sim::alloc() {
         bool can = true;
         for (int d = 0; d < 3; ++d) can = can && (n3[d] % 4 == 0);
         if (!can) break;
+        // a level of at most kDirectBottom cells and nodes is solved exactly
+        // (bottom_setup), cheaper than the launch-bound levels below it
+        const long long ncl = (long long)n3[0] * n3[1] * n3[2], nnl = (long long)n3[0] * n3[1] * (n3[2] + (g_.zper ? 0 : 1));
+        if (dims.size() > 1 && ncl <= kDirectBottom && nnl <= kDirectBottom) break;
         for (int d = 0; d < 3; ++d) n3[d] /= 2;
     }
     size_t mgtot = 0;
@@ -513,6 +527,14 @@ void Sim::alloc() {
     }
     nod_.omega = nodal_jacobi_weight(nd_[0].W, nod_.omega);
     bottom_setup();
+    // graphed tail: from the first level below level 0 of at most 2^18 cells
+    // (its kernels fill a fraction of the GPU and are bound by launch latency)
+    glev_ = 0;
+    for (size_t l = 1; l + 1 < cc_.size(); ++l)
+        if ((long long)cc_[l].nx * cc_[l].ny * cc_[l].nz <= (1LL << 18)) {
+            glev_ = l;
+            break;
+        }
     parts_.alloc(4 * 1216);
     red_.alloc(8);
     if (temp_ || S_.ablf) layer_.alloc(3 * (size_t)g_.nz);
@@ -764,9 +786,44 @@ void Sim::actuator_update() {
 }
 
 // ---------------------------------------------------------------- MAC projection
+template <typename F>
+void Sim::mg_graph_run(MGGraph& G, double key, F&& body) {
+    if (!G.exec || G.key != key) {
+        cudaGraph_t graph = nullptr;
+        const long long l0 = ctx_.launches;
+        ck(cudaStreamBeginCapture(ctx_.stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+        ctx_.capturing = true;
+        body();
+        ctx_.capturing = false;
+        ck(cudaStreamEndCapture(ctx_.stream, &graph), "graph capture");
+        G.nodes = ctx_.launches - l0;
+        ctx_.launches = l0;
+        if (G.exec) {
+            cudaGraphExecUpdateResultInfo info;
+            if (cudaGraphExecUpdate(G.exec, graph, &info) != cudaSuccess) {
+                (void)cudaGetLastError();
+                cudaGraphExecDestroy(G.exec);
+                G.exec = nullptr;
+            }
+        }
+        if (!G.exec) ck(cudaGraphInstantiate(&G.exec, graph, 0), "graph instantiate");
+        cudaGraphDestroy(graph);
+        G.key = key;
+    }
+    const bool p = ctx_.prof_match("(mg_coarse_graph)");
+    if (p) ctx_.prof_begin("(mg_coarse_graph)", 0.0);
+    ck(cudaGraphLaunch(G.exec, ctx_.stream), "graph launch");
+    if (p) ctx_.prof_end();
+    ctx_.launches += G.nodes;
+}
+
 template <typename T>
-void Sim::cc_vcycle(std::vector<CCLevelT<T>>& Ls, size_t l, double beta) {
+void Sim::cc_vcycle(std::vector<CCLevelT<T>>& Ls, size_t l, double beta, bool in_graph) {
     CCLevelT<T>& L = Ls[l];
+    if (!in_graph && mg_graphs_ && glev_ > 0 && l == glev_) {
+        mg_graph_run(gcc_[sizeof(T) == 4 ? 1 : 0], beta, [&]() { cc_vcycle(Ls, l, beta, true); });
+        return;
+    }
     if (l + 1 == Ls.size()) {
         launch_cc_bottom(ctx_, L, beta, mac_.bottom);
         return;
@@ -777,7 +834,7 @@ void Sim::cc_vcycle(std::vector<CCLevelT<T>>& Ls, size_t l, double beta) {
     }
     launch_cc_resid(ctx_, L, beta, nullptr, nullptr);
     launch_cc_restrict(ctx_, L, Ls[l + 1]);
-    cc_vcycle(Ls, l + 1, beta);
+    cc_vcycle(Ls, l + 1, beta, in_graph);
     launch_cc_prolong(ctx_, L, Ls[l + 1]);
     for (int s = 0; s < mac_.nu2; ++s) {
         launch_cc_gsrb(ctx_, L, beta, 0);
@@ -814,6 +871,17 @@ void Sim::set_mixed(int on) {
         Nd.phi = q; q += nn; Nd.rhs = q; q += nn; Nd.res = q; q += nn; Nd.tmp = q; q += nn;
         nd32_.push_back(Nd);
     }
+    // FP32 copies of the advection inputs
+    {
+        const size_t N = (size_t)g_.N;
+        g32_.alloc(6 * N + 2 * N + (size_t)g_.NFz);
+        float* f = g32_.p;
+        in32_.vel = f; f += 3 * N;
+        in32_.forces = f; f += 3 * N;
+        in32_.mac[0] = f; f += N;
+        in32_.mac[1] = f; f += N;
+        in32_.mac[2] = f;
+    }
     // FP32 copies of the bottom inverses
     std::vector<float> b32(binv_cc_h_.size() + binv_nd_h_.size());
     for (size_t m = 0; m < binv_cc_h_.size(); ++m) b32[m] = (float)binv_cc_h_[m];
@@ -849,23 +917,34 @@ void Sim::mac_project() {
     int np = 0;
     launch_mac_rhs(ctx_, g_, umac_[0].p, umac_[1].p, umac_[2].p, L.rhs, parts_.p, &np);
     launch_reduce(ctx_, parts_.p, np, 1, 0, red_.p);
-    launch_sub_ratio(ctx_, L.rhs, g_.N, red_.p, (double)g_.N);
-    launch_fill(ctx_, L.phi, 0.0, g_.N);
-    launch_cc_resid(ctx_, L, beta, parts_.p, &np);
+    const bool warm = mg_warm_ && mac_prev_ok_;
+    launch_sub_ratio(ctx_, L.rhs, g_.N, red_.p, (double)g_.N, warm ? parts_.p : nullptr, &np);
+    double bnorm = 0.0;  // |rhs|, the initial residual of a zero start
+    if (warm) {
+        bnorm = reduce(np, 1, 1, nullptr);
+        ck(cudaMemcpyAsync(L.phi, mac_phi_prev_.p, sizeof(double) * g_.N, cudaMemcpyDeviceToDevice, ctx_.stream), "D2D");
+    } else {
+        launch_fill(ctx_, L.phi, 0.0, g_.N);
+    }
+    // mixed precision: each FP64 residual is the next FP32 cycle's right-hand side
+    auto resid = [&]() {
+        if (mixed_) launch_cc_resid32(ctx_, L, beta, cc32_[0].rhs, cc32_[0].phi, parts_.p, &np);
+        else launch_cc_resid(ctx_, L, beta, parts_.p, &np);
+    };
+    resid();
     const double r0 = reduce(np, 1, 1, nullptr);
     mac_r0_ = r0;
-    const double target = std::max(mac_.atol, mac_.rtol * r0);
+    const double target = std::max(mac_.atol, mac_.rtol * std::max(bnorm, r0));
     int it = 0;
     double rn = r0;
     while (rn > target && it < mac_.maxiter) {
         if (mixed_) {
-            launch_to_f32(ctx_, L.res, cc32_[0].rhs, cc32_[0].phi, g_.N);
             cc_vcycle(cc32_, 0, beta);
             launch_add_f32(ctx_, L.phi, cc32_[0].phi, g_.N);
         } else {
             cc_vcycle(cc_, 0, beta);
         }
-        launch_cc_resid(ctx_, L, beta, parts_.p, &np);
+        resid();
         rn = reduce(np, 1, 1, nullptr);
         ++it;
         if (!std::isfinite(rn)) throw KsError(KS_ERR_NONFINITE, "MAC projection diverged");
@@ -878,12 +957,23 @@ void Sim::mac_project() {
     mac_it_ = it;
     mac_r_ = rn;
     launch_mac_correct(ctx_, g_, L.phi, umac_[0].p, umac_[1].p, umac_[2].p, beta);
+    if (mg_warm_) {
+        if (mac_phi_prev_.n != (size_t)g_.N) mac_phi_prev_.alloc(g_.N);
+        ck(cudaMemcpyAsync(mac_phi_prev_.p, L.phi, sizeof(double) * g_.N, cudaMemcpyDeviceToDevice, ctx_.stream), "D2D");
+        mac_prev_ok_ = true;
+    }
 }
 
 // ---------------------------------------------------------------- nodal projection
 template <typename T>
-void Sim::nd_vcycle(std::vector<NDLevelT<T>>& Ls, size_t l, double sigma, int skip_sweeps) {
+void Sim::nd_vcycle(std::vector<NDLevelT<T>>& Ls, size_t l, double sigma, int skip_sweeps, bool in_graph) {
     NDLevelT<T>& L = Ls[l];
+    // a replay must leave the host's phi / tmp pointers as the recording did:
+    // an even number of Jacobi swaps per level returns them to their start
+    if (!in_graph && mg_graphs_ && glev_ > 0 && l == glev_ && (nod_.nu1 + nod_.nu2) % 2 == 0) {
+        mg_graph_run(gnd_[sizeof(T) == 4 ? 1 : 0], sigma, [&]() { nd_vcycle(Ls, l, sigma, 0, true); });
+        return;
+    }
     if (l + 1 == Ls.size()) {
         launch_nd_bottom(ctx_, L, sigma, nod_.omega, nod_.bottom);
         return;
@@ -894,7 +984,7 @@ void Sim::nd_vcycle(std::vector<NDLevelT<T>>& Ls, size_t l, double sigma, int sk
     }
     launch_nd_resid(ctx_, L, sigma, nullptr, nullptr);
     launch_nd_restrict(ctx_, L, Ls[l + 1]);
-    nd_vcycle(Ls, l + 1, sigma);
+    nd_vcycle(Ls, l + 1, sigma, 0, in_graph);
     launch_nd_prolong(ctx_, L, Ls[l + 1]);
     for (int s = 0; s < nod_.nu2; ++s) {
         launch_nd_jacobi(ctx_, L, sigma, nod_.omega, L.phi, L.tmp);
@@ -904,14 +994,20 @@ void Sim::nd_vcycle(std::vector<NDLevelT<T>>& Ls, size_t l, double sigma, int sk
 
 // Nodal divergence of a cell field into the finest level's right-hand side,
 // made solvable (weighted mean removed); the initial guess is zero.
-void Sim::nd_rhs(const double* cell_field) {
+void Sim::nd_rhs(const double* cell_field, bool from_pressure) {
     NDLevelDev& L = nd_[0];
     const long long M = (long long)L.nx * L.ny * L.nz;
     int np = 0;
     launch_nodal_rhs(ctx_, g_, cell_field, L.rhs, parts_.p, &np);
     launch_reduce(ctx_, parts_.p, np, 2, 0, red_.p);
-    launch_sub_ratio(ctx_, L.rhs, M, red_.p, 0.0);
-    launch_fill(ctx_, L.phi, 0.0, M);
+    launch_sub_ratio(ctx_, L.rhs, M, red_.p, 0.0, from_pressure ? parts_.p : nullptr, &np);
+    nod_bnorm_ = 0.0;
+    if (from_pressure) {  // the pressure is the unknown of a non-incremental projection
+        nod_bnorm_ = reduce(np, 1, 1, nullptr);
+        ck(cudaMemcpyAsync(L.phi, p_.p, sizeof(double) * M, cudaMemcpyDeviceToDevice, ctx_.stream), "D2D");
+    } else {
+        launch_fill(ctx_, L.phi, 0.0, M);
+    }
 }
 
 // Solve sigma A phi = rhs on the finest nodal level to the relative /
@@ -924,17 +1020,16 @@ void Sim::nd_solve(double sigma) {
     for (size_t l = 0; l < nd32_.size(); ++l) nd32_[l].inv_diag = (float)nd_[l].inv_diag;
     int it = 0;
     double rn = 0.0, target = 0.0;
-    if (mixed_) {
-        launch_nd_resid(ctx_, L, sigma, parts_.p, &np);
+    if (mixed_) {  // each FP64 residual is the next FP32 cycle's right-hand side
+        launch_nd_resid32(ctx_, L, sigma, nd32_[0].rhs, nd32_[0].phi, parts_.p, &np);
         const double r0 = reduce(np, 1, 1, nullptr);
         nod_r0_ = r0;
-        target = std::max(nod_.atol, nod_.rtol * r0);
+        target = std::max(nod_.atol, nod_.rtol * std::max(nod_bnorm_, r0));
         rn = r0;
         while (rn > target && it < nod_.maxiter) {
-            launch_to_f32(ctx_, L.res, nd32_[0].rhs, nd32_[0].phi, M);
             nd_vcycle(nd32_, 0, sigma);
             launch_add_f32(ctx_, L.phi, nd32_[0].phi, M);
-            launch_nd_resid(ctx_, L, sigma, parts_.p, &np);
+            launch_nd_resid32(ctx_, L, sigma, nd32_[0].rhs, nd32_[0].phi, parts_.p, &np);
             rn = reduce(np, 1, 1, nullptr);
             ++it;
             if (!std::isfinite(rn)) throw KsError(KS_ERR_NONFINITE, "nodal projection diverged");
@@ -951,7 +1046,7 @@ void Sim::nd_solve(double sigma) {
             if (!std::isfinite(rn)) throw KsError(KS_ERR_NONFINITE, "nodal projection diverged");
             if (it == 0) {
                 nod_r0_ = rn;
-                target = std::max(nod_.atol, nod_.rtol * rn);
+                target = std::max(nod_.atol, nod_.rtol * std::max(nod_bnorm_, rn));
             }
             if (rn > 1e20 * nod_r0_) throw KsError(KS_ERR_NOT_CONVERGED, "nodal projection diverged (residual above 1e20 times the initial one)");
             if (rn <= target || it >= nod_.maxiter) break;
@@ -1112,7 +1207,7 @@ void Sim::apply_projection(double time, double scaling, bool incremental) {
     const bool small_dt = (time > 0.0 && t_.dt[0] < 0.1 * t_.dt[1]);
     const bool sub_old = small_dt || incremental;
     launch_proj_pre(ctx_, g_, vel_.p, vel_old_.p, gp_.p, scaling, rho_, incremental ? 0 : 1, sub_old ? 1 : 0);
-    nd_rhs(vel_.p);
+    nd_rhs(vel_.p, mg_warm_ && !incremental);
     const double sigma = scaling / rho_;
     nd_solve(sigma);
     launch_nodal_post(ctx_, g_, nd_[0].phi, vel_.p, vel_old_.p, gp_.p, p_.p, sigma, sub_old ? 1 : 0, incremental ? 1 : 0);
@@ -1138,11 +1233,11 @@ void Sim::apply_predictor(bool incremental) {
         launch_tdiff(ctx_, g_, theta_old_.p, alpha_.p, tbc(), tdiff_.p, 0, nullptr, nullptr, nullptr, nullptr, nullptr, dt, rho_, 0.0);
     }
     double* mac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
-    launch_premac(ctx_, g_, vel_old_.p, forces_.p, dt, gb_, mac, mixed_);
+    launch_premac(ctx_, g_, vel_old_.p, forces_.p, dt, gb_, mac, mixed_, mixed_ ? &in32_ : nullptr);
     mac_project();
     if (temp_) temperature_predictor(dt);
     const double* cmac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
-    launch_advection(ctx_, g_, vel_old_.p, forces_.p, cmac, dt, rho_, adv_bufs_ ? *adv_bufs_ : gb_, conv_.p, mixed_);
+    launch_advection(ctx_, g_, vel_old_.p, forces_.p, cmac, dt, rho_, adv_bufs_ ? *adv_bufs_ : gb_, conv_.p, mixed_, mixed_ ? &in32_ : nullptr);
     // compute_source_term(NPH): Coriolis reads the Old velocity and gp is
     // unchanged, so only BoussinesqBuoyancy (theta at n+1/2) changes src;
     // compute_diffusion_term(Old) reproduces divtau.
@@ -1327,6 +1422,7 @@ void Sim::tdiffuse_solve(double dtd) {
 }
 
 void Sim::init_data() {
+    mac_prev_ok_ = false;
     if (!restart_file_.empty()) {  // restart: fields from the checkpoint, no initial projection or iterations
         read_checkpoint(restart_file_);
         plot_start_ = chk_start_ = t_.step;  // SimTime::set_restart_time

@@ -259,6 +259,12 @@ void Sim::write_checkpoint(const std::string& dir) {
         cell("velocity_mueff", 1, 1);
     }
     if (temp_) cell("temperature", 1, 3);
+    if (mg_warm_ && mac_prev_ok_) {  // the MAC projection's warm start: a restart continues bit for bit
+        std::vector<double> h((size_t)g_.N);
+        sync();
+        ck(cudaMemcpy(h.data(), mac_phi_prev_.p, sizeof(double) * g_.N, cudaMemcpyDeviceToHost), "D2H");
+        write_vismf(dir + "/Level_0/mac_phi", 1, 0, 0, hi, grown(h, 1, n, 0, g_.zper));
+    }
     {  // nodal p on the nodes 0..n in every direction (periodic duplicates wrapped)
         ks_layout L;
         layout("p", L);
@@ -313,25 +319,38 @@ void Sim::read_checkpoint(const std::string& dir) {
             throw KsError(KS_ERR_DECK, "checkpoint domain does not tile the deck's domain (amr.n_cell, geometry.prob_lo/hi)");
     }
     if (rep[2] != 1 && !g_.zper) throw KsError(KS_ERR_DECK, "replication along a bounded z");
-    auto load = [&](const std::string& name, int nc, bool required) {
+    // a cell field of the checkpoint tiled over the deck's domain (empty: absent)
+    auto tiled = [&](const std::string& name, int nc, bool required) {
+        std::vector<double> full;
         std::ifstream probe(dir + "/Level_0/" + name + "_H");
         if (!probe) {
             if (required) throw KsError(KS_ERR_ARG, "checkpoint lacks " + name);
-            return;
+            return full;
         }
         auto v = read_vismf(dir + "/Level_0/" + name, nc, cn);
-        std::vector<double> full((size_t)g_.N * nc);
+        full.resize((size_t)g_.N * nc);
         for (int c = 0; c < nc; ++c)
             for (int k = 0; k < n[2]; ++k)
                 for (int j = 0; j < n[1]; ++j)
                     for (int i = 0; i < n[0]; ++i)
                         full[(((size_t)c * n[2] + k) * n[1] + j) * n[0] + i] =
                             v[(((size_t)c * cn[2] + k % cn[2]) * cn[1] + j % cn[1]) * cn[0] + i % cn[0]];
-        set(name, full.data(), 0);
+        return full;
     };
-    load("velocity", 3, true);
-    load("gp", 3, true);
-    if (temp_) load("temperature", 1, true);
+    auto load = [&](const std::string& name, int nc) { set(name, tiled(name, nc, true).data(), 0); };
+    load("velocity", 3);
+    load("gp", 3);
+    if (temp_) load("temperature", 1);
+    // the MAC projection's warm start (written by this implementation only)
+    mac_prev_ok_ = false;
+    if (mg_warm_) {
+        auto m = tiled("mac_phi", 1, false);
+        if (!m.empty()) {
+            if (mac_phi_prev_.n != (size_t)g_.N) mac_phi_prev_.alloc(g_.N);
+            ck(cudaMemcpy(mac_phi_prev_.p, m.data(), sizeof(double) * g_.N, cudaMemcpyHostToDevice), "H2D");
+            mac_prev_ok_ = true;
+        }
+    }
     {  // nodal p: nodes 0..n of the checkpoint, stored without periodic duplicates
         const int nn[3] = {cn[0] + 1, cn[1] + 1, cn[2] + 1};
         auto pv = read_vismf(dir + "/Level_0/p", 1, nn);

@@ -640,10 +640,20 @@ __global__ void k_reduce(const double* parts, int np, int op_max, double* out) {
     if (threadIdx.x == 0) out[comp] = v;
 }
 
-// a -= s[0] / den (den > 0) or a -= s[0] / s[1]
-__global__ void k_sub_ratio(double* a, long long n, const double* s, double den) {
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (t < n) a[t] -= s[0] / (den > 0.0 ? den : s[1]);
+// a -= s[0] / den (den > 0) or a -= s[0] / s[1]; with parts, block maxima of
+// |a| after the shift.  Grid-stride, so the FP64 division is formed once per
+// thread rather than once per element.
+__global__ void k_sub_ratio(double* a, long long n, const double* s, double den, double* parts) {
+    const double r = s[0] / (den > 0.0 ? den : s[1]);
+    long long mb = 0;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const double v = a[t] - r;
+        a[t] = v;
+        mb = imax_abs(mb, v);
+    }
+    if (!parts) return;
+    const double m = block_reduce<1>(bitsd(mb));
+    if (threadIdx.x == 0) parts[blockIdx.x] = m;
 }
 
 // ---------------------------------------------------------------- actuator
@@ -808,8 +818,10 @@ void launch_ke(Ctx& c, const Grid& g, const double* vel, double rho, double* par
 void launch_reduce(Ctx& c, const double* parts, int np, int ncomp, int op_max, double* out) {
     KS_LAUNCH(c, k_reduce, ncomp, 256, B8 * (np + 1) * ncomp, parts, np, op_max, out);
 }
-void launch_sub_ratio(Ctx& c, double* a, long long n, const double* s, double den) {
-    KS_LAUNCH(c, k_sub_ratio, nblocks(n, BS), BS, B8 * 2 * n, a, n, s, den);
+void launch_sub_ratio(Ctx& c, double* a, long long n, const double* s, double den, double* parts, int* np) {
+    const int nb = parts_for(n);
+    if (np) *np = nb;
+    KS_LAUNCH(c, k_sub_ratio, nb, BS, B8 * 2 * n, a, n, s, den, parts);
 }
 void launch_act_sample(Ctx& c, const Grid& g, const double* vel, const double* pts, int npts, const double plo[3], double* out) {
     KS_LAUNCH(c, k_act_sample, nblocks(npts, 64), 64, B8 * 6 * npts, g, vel, pts, npts, plo[0], plo[1], plo[2], out);

@@ -19,6 +19,7 @@ namespace ks {
 struct Ctx {
     cudaStream_t stream = nullptr;
     long long launches = 0;
+    bool capturing = false;  // recording a CUDA graph: no per-launch profiling events
     std::string prof;
     struct Open {
         std::string name;
@@ -35,7 +36,7 @@ struct Ctx {
 
     // names compare without spaces (the report prints them without, e.g. "(k_nd_col<T,0>)")
     bool prof_match(const char* name) const {
-        if (prof.empty()) return false;
+        if (prof.empty() || capturing) return false;
         if (prof == "*") return true;
         size_t q = 0;
         for (const char* c = name; *c; ++c) {
@@ -169,7 +170,8 @@ void launch_mac_correct(Ctx& c, const Grid& g, const double* phi, double* um, do
 void launch_cfl(Ctx& c, const Grid& g, const double* vel, const double* src, const double* mueff, double rho, double* partials,
                 int* nparts);
 void launch_ke(Ctx& c, const Grid& g, const double* vel, double rho, double* partials, int* nparts);
-void launch_sub_ratio(Ctx& c, double* a, long long n, const double* s, double den);
+// a -= s[0] / den (or s[0] / s[1] when den <= 0); with parts, block maxima of the shifted |a| (count in *np)
+void launch_sub_ratio(Ctx& c, double* a, long long n, const double* s, double den, double* parts = nullptr, int* np = nullptr);
 void launch_reduce(Ctx& c, const double* partials, int nparts, int ncomp, int op_max, double* out);
 void launch_act_sample(Ctx& c, const Grid& g, const double* vel, const double* pts, int npts, const double plo[3], double* out);
 void launch_act_spread(Ctx& c, const Grid& g, double* act, const double* pts, int npts, const double ax[3], double eps,
@@ -187,13 +189,20 @@ struct GodunovBufs {
     void* tr[3][3][3];  // transverse-corrected states tr[a][b][n]
     void* flux[3][3];   // fluxes flux[d][n]
 };
+// FP32 copies of the advection inputs for the mixed-precision form: launch_premac fills vel and
+// forces, launch_advection (same step) the MAC velocities
+struct GodunovIn32 {
+    float* vel;     // 3 N
+    float* forces;  // 3 N
+    float* mac[3];  // face arrays
+};
 void launch_premac(Ctx& c, const Grid& g, const double* vel_old, const double* forces, double dt, GodunovBufs& B, double* mac[3],
-                   int fp32);
+                   int fp32, GodunovIn32* in32);
 void launch_advection(Ctx& c, const Grid& g, const double* vel_old, const double* forces, const double* mac[3], double dt, double rho,
-                      GodunovBufs& B, double* conv, int fp32);
+                      GodunovBufs& B, double* conv, int fp32, GodunovIn32* in32);
 // Godunov fluxes and conv = -div(flux) of rho s for a cell scalar s with forces fs = src + diff (FP64);
 // B: component-0 face slots reused as scratch
-void launch_scalar_advection(Ctx& c, const Grid& g, const double* s, const double* fs, const double* mac[3], double dt, double rho,
+void launch_scalar_advection(Ctx& c, const Grid& g, const double* s, const double* fs, const double* const mac[3], double dt, double rho,
                              GodunovBufs& B, double* conv);
 
 // ---- temperature transport (ks_temperature.cu), FP64
@@ -332,6 +341,10 @@ template <typename T>
 void launch_cc_gsrb(Ctx& c, const CCLevelT<T>& L, double beta, int color);
 template <typename T>
 void launch_cc_resid(Ctx& c, const CCLevelT<T>& L, double beta, double* partials, int* nparts);
+// FP64 residuals of the mixed-precision defect correction, written as the FP32 cycle's
+// right-hand side r32 with its solution z32 zeroed (L.res untouched)
+void launch_cc_resid32(Ctx& c, const CCLevelT<double>& L, double beta, float* r32, float* z32, double* partials, int* nparts);
+void launch_nd_resid32(Ctx& c, const NDLevelT<double>& L, double sigma, float* r32, float* z32, double* partials, int* nparts);
 template <typename T>
 void launch_cc_restrict(Ctx& c, const CCLevelT<T>& F, const CCLevelT<T>& C);
 template <typename T>
@@ -352,7 +365,6 @@ template <typename T>
 void launch_nd_prolong(Ctx& c, const NDLevelT<T>& F, const NDLevelT<T>& C);
 template <typename T>
 void launch_nd_bottom(Ctx& c, const NDLevelT<T>& L, double sigma, double omega, int sweeps);
-void launch_to_f32(Ctx& c, const double* r, float* rhs, float* phi, long long n);
 void launch_add_f32(Ctx& c, double* phi, const float* e, long long n);
 
 }  // namespace ks

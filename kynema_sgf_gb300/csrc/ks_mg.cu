@@ -112,8 +112,11 @@ __global__ void k_cc_gsrb(CCLevelT<T> L, T beta, int color) {
     (void)beta;
 }
 
+// residual with block maxima of its magnitude; with r32 (defect correction of
+// the mixed-precision form) it goes to the FP32 cycle's right-hand side r32,
+// whose solution z32 starts at zero, instead of L.res
 template <typename T>
-__global__ void k_cc_resid(CCLevelT<T> L, T beta, double* parts) {
+__global__ void k_cc_resid(CCLevelT<T> L, T beta, double* parts, float* r32, float* z32) {
     const unsigned N = (unsigned)(L.nx * L.ny * L.nz);
     MaxAbs<T> mx;
     for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x) {
@@ -122,7 +125,12 @@ __global__ void k_cc_resid(CCLevelT<T> L, T beta, double* parts) {
         int cls;
         const T S = cc_nsum(L, L.phi, i, j, k, cls);
         const T v = L.rhs[t] - L.dg[cls] * (L.phi[t] - S);
-        L.res[t] = v;
+        if (r32) {
+            r32[t] = (float)v;
+            z32[t] = 0.0f;
+        } else {
+            L.res[t] = v;
+        }
         mx.add(v);
     }
     const double m = bred<1>(mx.get());
@@ -277,7 +285,8 @@ inline NdCoef<T> nd_coef(const NDLevelT<T>& L, double sigma, double omega) {
 // MODE 0: out = in + omega (rhs - A in) / diag.  MODE 1: the same plus block
 // maxima of |rhs - A in|.  MODE 2: res = rhs - A phi plus block maxima.
 template <typename T, int MODE>
-__global__ void k_nd_col(NDLevelT<T> L, NdCoef<T> w, const T* in, T* out, int kc, double* parts) {
+__global__ void k_nd_col(NDLevelT<T> L, NdCoef<T> w, const T* in, T* out, int kc, double* parts, float* r32 = nullptr,
+                         float* z32 = nullptr) {
     const int sz = L.nx * L.ny;
     const int nch = (L.nz + kc - 1) / kc;
     const unsigned M = (unsigned)(sz * nch);
@@ -316,8 +325,16 @@ __global__ void k_nd_col(NDLevelT<T> L, NdCoef<T> w, const T* in, T* out, int kc
                 res = w.c10 * Ey0 + res;
                 res = w.c4 * (Cm + Cp) + res;
             }
-            if (MODE == 2) L.res[idx] = res;
-            else out[idx] = w.oinv * res + C0;
+            if (MODE == 2) {
+                if (r32) {  // residual to the FP32 cycle's right-hand side (as in k_cc_resid)
+                    r32[idx] = (float)res;
+                    z32[idx] = 0.0f;
+                } else {
+                    L.res[idx] = res;
+                }
+            } else {
+                out[idx] = w.oinv * res + C0;
+            }
             if (MODE >= 1) mx.add(res);
             Pm = P0;
             Exm = Ex0;
@@ -419,13 +436,7 @@ __global__ void k_nd_bottom(NDLevelT<T> L, T sigma, T omega, int sweeps) {
     for (int t = threadIdx.x; t < N; t += blockDim.x) L.phi[t] = p[t];
 }
 
-// defect correction helpers: rhs32 = (float) r64, phi32 = 0 ; phi64 += phi32
-__global__ void k_to_f32(const double* r, float* rhs, float* phi, long long n) {
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    rhs[t] = (float)r[t];
-    phi[t] = 0.0f;
-}
+// defect correction: phi64 += phi32
 __global__ void k_add_f32(double* phi, const float* e, long long n) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= n) return;
@@ -452,7 +463,19 @@ template <typename T>
 void launch_cc_resid(Ctx& c, const CCLevelT<T>& L, double beta, double* parts, int* np) {
     const int n = parts_for((long long)L.nx * L.ny * L.nz);
     if (np) *np = n;
-    KS_LAUNCH(c, k_cc_resid<T>, n, BS, sizeof(T) * 3.0 * ncc(L), L, T(beta), parts);
+    KS_LAUNCH(c, k_cc_resid<T>, n, BS, sizeof(T) * 3.0 * ncc(L), L, T(beta), parts, (float*)nullptr, (float*)nullptr);
+}
+void launch_cc_resid32(Ctx& c, const CCLevelT<double>& L, double beta, float* r32, float* z32, double* parts, int* np) {
+    const int n = parts_for((long long)L.nx * L.ny * L.nz);
+    *np = n;
+    KS_LAUNCH(c, k_cc_resid<double>, n, BS, 8.0 * 2.0 * ncc(L) + 8.0 * ncc(L), L, beta, parts, r32, z32);
+}
+void launch_nd_resid32(Ctx& c, const NDLevelT<double>& L, double sigma, float* r32, float* z32, double* parts, int* np) {
+    const int kc = nd_chunk(L);
+    const int n = parts_for(nd_cols(L, kc));
+    *np = n;
+    KS_LAUNCH(c, (k_nd_col<double, 2>), n, BS, 8.0 * 2.0 * nnd(L) + 8.0 * nnd(L), L, nd_coef(L, sigma, 0.0), (const double*)L.phi,
+              (double*)nullptr, kc, parts, r32, z32);
 }
 template <typename T>
 void launch_cc_restrict(Ctx& c, const CCLevelT<T>& F, const CCLevelT<T>& C) {
@@ -511,9 +534,6 @@ void launch_nd_jacobi_norm(Ctx& c, const NDLevelT<double>& L, double sigma, doub
     const int n = parts_for(nd_cols(L, kc));
     *np = n;
     KS_LAUNCH(c, (k_nd_col<double, 1>), n, BS, 8.0 * 3.0 * nnd(L), L, nd_coef(L, sigma, omega), in, out, kc, parts);
-}
-void launch_to_f32(Ctx& c, const double* r, float* rhs, float* phi, long long n) {
-    KS_LAUNCH(c, k_to_f32, nblocks(n, BS), BS, 16.0 * n, r, rhs, phi, n);
 }
 void launch_add_f32(Ctx& c, double* phi, const float* e, long long n) {
     KS_LAUNCH(c, k_add_f32, nblocks(n, BS), BS, 20.0 * n, phi, e, n);

@@ -290,15 +290,27 @@ class Sim {
     void mac_project();
     double reduce(int np, int ncomp, int op_max, double* host);
     template <typename T>
-    void cc_vcycle(std::vector<CCLevelT<T>>& Ls, size_t l, double beta);
+    void cc_vcycle(std::vector<CCLevelT<T>>& Ls, size_t l, double beta, bool in_graph = false);
     template <typename T>
-    void nd_vcycle(std::vector<NDLevelT<T>>& Ls, size_t l, double sigma, int skip_sweeps = 0);
+    void nd_vcycle(std::vector<NDLevelT<T>>& Ls, size_t l, double sigma, int skip_sweeps = 0, bool in_graph = false);
+    // The launch-bound coarse tail of a V-cycle (levels >= glev_) recorded once
+    // as a CUDA graph and replayed; re-recorded when its scalar key changes.
+    struct MGGraph {
+        cudaGraphExec_t exec = nullptr;
+        long long nodes = 0;
+        double key = 0.0;
+    };
+    MGGraph gcc_[2], gnd_[2];  // [FP64, FP32] MAC and nodal tails
+    size_t glev_ = 0;          // first graphed level (0: none)
+    int mg_graphs_ = 1;        // ks.mg_graphs
+    template <typename F>
+    void mg_graph_run(MGGraph& G, double key, F&& body);
    public:
     void set_mixed(int on);
 
    private:
     double* field(const std::string& name, int& ncomp, int& kind);
-    void nd_rhs(const double* cell_field);
+    void nd_rhs(const double* cell_field, bool from_pressure = false);
     void nd_solve(double sigma);
     void mol_predictor(bool incremental);
     void diff_alloc();
@@ -372,7 +384,13 @@ class Sim {
     std::vector<double> binv_cc_h_, binv_nd_h_;
     DevBuf<double> binv_;
     DevBuf<float> binv32_;
+    DevBuf<float> g32_;  // mixed precision: FP32 copies of the advection inputs
+    GodunovIn32 in32_{};
     void bottom_setup();
+    int mg_warm_ = 1;          // ks.mg_warm_start
+    bool mac_prev_ok_ = false; // mac_phi_prev_ holds the last MAC potential
+    DevBuf<double> mac_phi_prev_;
+    double nod_bnorm_ = 0.0;   // |rhs| of a warm-started nodal solve (0: zero start)
     DevBuf<double> parts_, red_;
     DevBuf<double> pts_, samp_;
     double* hred_ = nullptr;  // pinned

@@ -30,7 +30,7 @@ def pair(cuda_dev, oracle_mod, deck):
 
 @pytest.mark.parametrize("n", [16, 32])
 def test_tgv_mol_steps(cuda_dev, oracle_mod, n):
-    g, o = pair(cuda_dev, oracle_mod, decks.mol(decks.tgv(n, steps=4, cfl=0.45)))
+    g, o = pair(cuda_dev, oracle_mod, decks.mol(decks.tgv(n, steps=4, cfl=0.45)) + "ks.mg_warm_start = 0\n")
     g.InitData()
     o.InitData()
     check(g, o, ["velocity", "p", "gp"])
