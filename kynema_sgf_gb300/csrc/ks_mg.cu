@@ -99,42 +99,114 @@ __device__ inline T cc_gs_point(const CCLevelT<T>& L, const T* p, int i, int j, 
     return L.inv_diag[cls] * rhs + S;
 }
 
+// Red-black Gauss-Seidel half-sweep (cells with (i + j + k) % 2 == color),
+// z-marching: thread (i2, j) owns the cell pair (2 i2, 2 i2 + 1) of row j and
+// walks k through a chunk of the column, updating the pair member of the
+// sweep's colour at each k.  The per-class weights are scalars selected by the
+// layer's class, the neighbour offsets are formed once per thread: about 30
+// instructions per update where a thread-per-cell launch spends ~300 on index
+// maps and indexed parameter loads (it is instruction-bound, in FP32 as in
+// FP64).  The level's x extent is even (coarsening keeps it a multiple of 4).
 template <typename T>
-__global__ void k_cc_gsrb(CCLevelT<T> L, T beta, int color) {
-    const unsigned half = (unsigned)(L.nx * L.ny * L.nz / 2);
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= half) return;
-    int i2, j, k;
-    split3(t, (unsigned)(L.nx / 2), (unsigned)L.ny, i2, j, k);
-    const int i = 2 * i2 + ((j + k + color) & 1);
-    const int c = ci3(L, i, j, k);
-    L.phi[c] = cc_gs_point(L, L.phi, i, j, k, L.rhs[c]);
-    (void)beta;
+struct CCCoef {  // per class (interior, wall-adjacent, single layer): w_x / d, w_y / d, w_z / d, 1 / dg, dg
+    T gx0, gx1, gx2, gy0, gy1, gy2, gz0, gz1, gz2, iv0, iv1, iv2, dg0, dg1, dg2;
+};
+template <typename T>
+inline CCCoef<T> cc_coef(const CCLevelT<T>& L) {
+    return CCCoef<T>{L.gs[0][0], L.gs[1][0], L.gs[2][0], L.gs[0][1], L.gs[1][1], L.gs[2][1], L.gs[0][2], L.gs[1][2],
+                     L.gs[2][2], L.inv_diag[0], L.inv_diag[1], L.inv_diag[2], L.dg[0], L.dg[1], L.dg[2]};
+}
+template <typename T>
+__global__ void k_cc_gsrb(CCLevelT<T> L, CCCoef<T> w, int color, int kc) {
+    const int i2 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i2 >= (L.nx >> 1)) return;
+    const int j = blockIdx.y;
+    const int k0 = blockIdx.z * kc, k1 = min(k0 + kc, L.nz);
+    const int sy = L.nx, sz = L.nx * L.ny;
+    const int dyp = (j + 1 == L.ny ? -j : 1) * sy, dym = (j == 0 ? L.ny - 1 : -1) * sy;
+    T* p = L.phi;
+    const T* rhs = L.rhs;
+    for (int k = k0; k < k1; ++k) {
+        const int s = (j + k + color) & 1;
+        const int i = 2 * i2 + s;
+        const int c = k * sz + j * sy + i;
+        const int dxp = i + 1 == L.nx ? 1 - L.nx : 1, dxm = i == 0 ? L.nx - 1 : -1;
+        T zs;
+        T gx = w.gx0, gy = w.gy0, gz = w.gz0, iv = w.iv0;
+        if (L.zper) {
+            const int kp = k + 1 == L.nz ? 0 : k + 1, km = k == 0 ? L.nz - 1 : k - 1;
+            zs = p[c + (kp - k) * sz] + p[c + (km - k) * sz];
+        } else {
+            const bool lo = k == 0, hi = k + 1 == L.nz;
+            zs = (lo ? T(0) : p[c - sz]) + (hi ? T(0) : p[c + sz]);
+            if (lo || hi) {
+                const bool one = lo && hi;
+                gx = one ? w.gx2 : w.gx1;
+                gy = one ? w.gy2 : w.gy1;
+                gz = one ? w.gz2 : w.gz1;
+                iv = one ? w.iv2 : w.iv1;
+            }
+        }
+        p[c] = iv * rhs[c] + (gx * (p[c + dxp] + p[c + dxm]) + gy * (p[c + dyp] + p[c + dym]) + gz * zs);
+    }
 }
 
 // residual with block maxima of its magnitude; with r32 (defect correction of
 // the mixed-precision form) it goes to the FP32 cycle's right-hand side r32,
-// whose solution z32 starts at zero, instead of L.res
+// whose solution z32 starts at zero, instead of L.res.  Grid-stride over
+// (i, j, chunk of kc layers) columns marching in k, with the class weights
+// selected from scalars (as in k_cc_gsrb).
 template <typename T>
-__global__ void k_cc_resid(CCLevelT<T> L, T beta, double* parts, float* r32, float* z32) {
-    const unsigned N = (unsigned)(L.nx * L.ny * L.nz);
+__global__ void k_cc_resid(CCLevelT<T> L, CCCoef<T> w, int kc, double* parts, float* r32, float* z32) {
+    const int sy = L.nx, sz = L.nx * L.ny;
+    const int nch = (L.nz + kc - 1) / kc;
+    const unsigned M = (unsigned)(sz * nch);
     MaxAbs<T> mx;
-    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x) {
-        int i, j, k;
-        split3(t, (unsigned)L.nx, (unsigned)L.ny, i, j, k);
-        int cls;
-        const T S = cc_nsum(L, L.phi, i, j, k, cls);
-        const T v = L.rhs[t] - L.dg[cls] * (L.phi[t] - S);
-        if (r32) {
-            r32[t] = (float)v;
-            z32[t] = 0.0f;
-        } else {
-            L.res[t] = v;
+    const T* p = L.phi;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < M; t += gridDim.x * blockDim.x) {
+        int i, j, ch;
+        split3(t, (unsigned)L.nx, (unsigned)L.ny, i, j, ch);
+        const int dxp = i + 1 == L.nx ? 1 - L.nx : 1, dxm = i == 0 ? L.nx - 1 : -1;
+        const int dyp = (j + 1 == L.ny ? -j : 1) * sy, dym = (j == 0 ? L.ny - 1 : -1) * sy;
+        const int k0 = ch * kc, k1 = min(k0 + kc, L.nz);
+        for (int k = k0; k < k1; ++k) {
+            const int c = k * sz + j * sy + i;
+            T zs;
+            T gx = w.gx0, gy = w.gy0, gz = w.gz0, dg = w.dg0;
+            if (L.zper) {
+                const int kp = k + 1 == L.nz ? 0 : k + 1, km = k == 0 ? L.nz - 1 : k - 1;
+                zs = p[c + (kp - k) * sz] + p[c + (km - k) * sz];
+            } else {
+                const bool lo = k == 0, hi = k + 1 == L.nz;
+                zs = (lo ? T(0) : p[c - sz]) + (hi ? T(0) : p[c + sz]);
+                if (lo || hi) {
+                    const bool one = lo && hi;
+                    gx = one ? w.gx2 : w.gx1;
+                    gy = one ? w.gy2 : w.gy1;
+                    gz = one ? w.gz2 : w.gz1;
+                    dg = one ? w.dg2 : w.dg1;
+                }
+            }
+            const T S = gx * (p[c + dxp] + p[c + dxm]) + gy * (p[c + dyp] + p[c + dym]) + gz * zs;
+            const T v = L.rhs[c] - dg * (p[c] - S);
+            if (r32) {
+                r32[c] = (float)v;
+                z32[c] = 0.0f;
+            } else {
+                L.res[c] = v;
+            }
+            mx.add(v);
         }
-        mx.add(v);
     }
     const double m = bred<1>(mx.get());
     if (threadIdx.x == 0 && parts) parts[blockIdx.x] = m;
+}
+
+// layers per thread of the column kernels: long columns on the large levels
+template <typename T>
+inline int cc_chunk(const CCLevelT<T>& L) {
+    const long long work = (long long)L.nx * L.ny * L.nz / 300000;
+    return (int)(work < 1 ? 1 : (work > 16 ? 16 : work));
 }
 
 template <typename T>
@@ -457,18 +529,28 @@ inline double nnd(const NDLevelT<T>& L) {
 
 template <typename T>
 void launch_cc_gsrb(Ctx& c, const CCLevelT<T>& L, double beta, int color) {
-    KS_LAUNCH(c, k_cc_gsrb<T>, nblocks((long long)L.nx * L.ny * L.nz / 2, BS), BS, sizeof(T) * 2.0 * ncc(L), L, T(beta), color);
+    (void)beta;
+    // z chunk: long columns on the large levels, one layer on the small ones
+    const long long work = (long long)(L.nx / 2) * L.ny * L.nz / 150000;
+    const int kc = (int)(work < 1 ? 1 : (work > 16 ? 16 : work));
+    const int hx = L.nx / 2, bx = hx >= 128 ? 128 : 32 * ((hx + 31) / 32);
+    const dim3 grid((unsigned)((hx + bx - 1) / bx), (unsigned)L.ny, (unsigned)((L.nz + kc - 1) / kc));
+    KS_LAUNCH(c, k_cc_gsrb<T>, grid, bx, sizeof(T) * 2.0 * ncc(L), L, cc_coef(L), color, kc);
 }
 template <typename T>
 void launch_cc_resid(Ctx& c, const CCLevelT<T>& L, double beta, double* parts, int* np) {
-    const int n = parts_for((long long)L.nx * L.ny * L.nz);
+    (void)beta;
+    const int kc = cc_chunk(L);
+    const int n = parts_for((long long)L.nx * L.ny * ((L.nz + kc - 1) / kc));
     if (np) *np = n;
-    KS_LAUNCH(c, k_cc_resid<T>, n, BS, sizeof(T) * 3.0 * ncc(L), L, T(beta), parts, (float*)nullptr, (float*)nullptr);
+    KS_LAUNCH(c, k_cc_resid<T>, n, BS, sizeof(T) * 3.0 * ncc(L), L, cc_coef(L), kc, parts, (float*)nullptr, (float*)nullptr);
 }
 void launch_cc_resid32(Ctx& c, const CCLevelT<double>& L, double beta, float* r32, float* z32, double* parts, int* np) {
-    const int n = parts_for((long long)L.nx * L.ny * L.nz);
+    (void)beta;
+    const int kc = cc_chunk(L);
+    const int n = parts_for((long long)L.nx * L.ny * ((L.nz + kc - 1) / kc));
     *np = n;
-    KS_LAUNCH(c, k_cc_resid<double>, n, BS, 8.0 * 2.0 * ncc(L) + 8.0 * ncc(L), L, beta, parts, r32, z32);
+    KS_LAUNCH(c, k_cc_resid<double>, n, BS, 8.0 * 2.0 * ncc(L) + 8.0 * ncc(L), L, cc_coef(L), kc, parts, r32, z32);
 }
 void launch_nd_resid32(Ctx& c, const NDLevelT<double>& L, double sigma, float* r32, float* z32, double* parts, int* np) {
     const int kc = nd_chunk(L);
