@@ -15,11 +15,13 @@ namespace {
 constexpr int BS = 256;
 constexpr int MAXPARTS = 1216;  // 152 SMs x 8
 
+// cell index -> (i, j, k) in 32-bit arithmetic (grids hold fewer than 2^31
+// cells; a 64-bit division costs as much issue as tens of FP64 operations)
 __device__ inline void cell_of(const Grid& g, long long t, int& i, int& j, int& k) {
-    i = (int)(t % g.nx);
-    long long r = t / g.nx;
-    j = (int)(r % g.ny);
-    k = (int)(r / g.ny);
+    const unsigned u = (unsigned)t, r = u / (unsigned)g.nx;
+    i = (int)(u - r * (unsigned)g.nx);
+    k = (int)(r / (unsigned)g.ny);
+    j = (int)(r - (unsigned)k * (unsigned)g.ny);
 }
 
 template <int OPMAX>
@@ -118,18 +120,23 @@ __global__ void k_smag(Grid g, const double* vel, double* mueff, double mu, doub
     int i, j, k;
     cell_of(g, t, i, j, k);
     VelFP V{vel, g, 1.0};
-    double a = 0.5, b = 0.0, c = -0.5;
-    if (!g.zper && k == 0) { a = 1.0 / 3.0; b = 1.0; c = -4.0 / 3.0; }
-    if (!g.zper && k == g.nz - 1) { a = 4.0 / 3.0; b = -1.0; c = -1.0 / 3.0; }
+    const double hx = 0.5 * g.idx, hy = 0.5 * g.idy;
     double gx[3], gy[3], gz[3];
     for (int n = 0; n < 3; ++n) {
-        gx[n] = 0.5 * (V(n, i + 1, j, k) - V(n, i - 1, j, k)) * g.idx;
-        gy[n] = 0.5 * (V(n, i, j + 1, k) - V(n, i, j - 1, k)) * g.idy;
-        gz[n] = (a * V(n, i, j, k + 1) + b * V(n, i, j, k) + c * V(n, i, j, k - 1)) * g.idz;
+        gx[n] = hx * (V(n, i + 1, j, k) - V(n, i - 1, j, k));
+        gy[n] = hy * (V(n, i, j + 1, k) - V(n, i, j - 1, k));
     }
-    const double s = sqrt(2.0 * gx[0] * gx[0] + 2.0 * gy[1] * gy[1] + 2.0 * gz[2] * gz[2] + (gy[0] + gx[1]) * (gy[0] + gx[1]) +
-                          (gz[1] + gy[2]) * (gz[1] + gy[2]) + (gx[2] + gz[0]) * (gx[2] + gz[0]));
-    const double mut = rho * fac * s;
+    if (!g.zper && (k == 0 || k == g.nz - 1)) {  // one-sided through the wall (ghost) value
+        double a = 1.0 / 3.0, b = 1.0, c = -4.0 / 3.0;
+        if (k == g.nz - 1) { a = 4.0 / 3.0; b = -1.0; c = -1.0 / 3.0; }
+        for (int n = 0; n < 3; ++n) gz[n] = (a * V(n, i, j, k + 1) + b * V(n, i, j, k) + c * V(n, i, j, k - 1)) * g.idz;
+    } else {
+        const double hz = 0.5 * g.idz;
+        for (int n = 0; n < 3; ++n) gz[n] = hz * (V(n, i, j, k + 1) - V(n, i, j, k - 1));
+    }
+    const double sxy = gy[0] + gx[1], syz = gz[1] + gy[2], szx = gx[2] + gz[0];
+    const double s = sqrt(2.0 * (gx[0] * gx[0] + gy[1] * gy[1] + gz[2] * gz[2]) + (sxy * sxy + syz * syz + szx * szx));
+    const double mut = (rho * fac) * s;
     mueff[t] = mu + mut;
     if (alpha) alpha[t] = mu_pr + iprt * mut;
 }
@@ -382,6 +389,7 @@ __global__ void __launch_bounds__(TTX* TTY* TTZ) k_divtau_tile(Grid g, const dou
     }
     __syncthreads();
     const double ih[3] = {g.idx, g.idy, g.idz};
+    const double qh[3] = {0.25 * g.idx, 0.25 * g.idy, 0.25 * g.idz};
     // flux through the d-face at the low side of halo cell (hx, hy, hz)
     auto flux = [&](int d, int hx, int hy, int hz, int gk, double F[3]) {
         const int e0 = (d == 0), e1 = (d == 1), e2 = (d == 2);
@@ -391,17 +399,15 @@ __global__ void __launch_bounds__(TTX* TTY* TTZ) k_divtau_tile(Grid g, const dou
         else if (d == 2 && !g.zper && gk == g.nz) mf = sM[hidx(mx, my, mz)];
         else mf = 0.5 * (sM[hidx(mx, my, mz)] + sM[hidx(hx, hy, hz)]);
         double gr[3][3];
+        const int hc = hidx(hx, hy, hz), hm = hidx(mx, my, mz);
         for (int n = 0; n < 3; ++n) {
             const double* v = sV + n * TNH;
             for (int m = 0; m < 3; ++m) {
                 if (m == d) {
-                    gr[m][n] = (v[hidx(hx, hy, hz)] - v[hidx(mx, my, mz)]) * ih[m];
-                } else {
-                    const int f0 = (m == 0), f1 = (m == 1), f2 = (m == 2);
-                    gr[m][n] = 0.25 *
-                               (v[hidx(hx + f0, hy + f1, hz + f2)] + v[hidx(mx + f0, my + f1, mz + f2)] - v[hidx(hx - f0, hy - f1, hz - f2)] -
-                                v[hidx(mx - f0, my - f1, mz - f2)]) *
-                               ih[m];
+                    gr[m][n] = (v[hc] - v[hm]) * ih[m];
+                } else {  // mean of the two cells' central differences along m
+                    const int f = m == 0 ? 1 : (m == 1 ? THX : THX * THY);
+                    gr[m][n] = qh[m] * ((v[hc + f] + v[hm + f]) - (v[hc - f] + v[hm - f]));
                 }
             }
         }
@@ -601,17 +607,26 @@ __global__ void k_mac_correct(Grid g, const double* phi, double* um, double* vm,
 
 // ---------------------------------------------------------------- reductions
 __global__ void k_cfl(Grid g, const double* vel, const double* src, const double* mu, double rho, double* parts, int np) {
-    double c = 0, d = 0, f = 0;
+    // The maxima of |u_n|, |src_n| and mu are taken on the integer pipe and
+    // scaled once per thread: rounding is monotone, so max(|u|) / dx equals
+    // max(|u| / dx) exactly, and no FP64 instruction runs per cell.
     const double dxi[3] = {g.idx, g.idy, g.idz};
     const double irho = 1.0 / rho;
     const double dxinv2 = 2.0 * (dxi[0] * dxi[0] + dxi[1] * dxi[1] + dxi[2] * dxi[2]);
+    long long um[3] = {0, 0, 0}, sm[3] = {0, 0, 0}, mm = 0;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < g.N; t += (long long)gridDim.x * blockDim.x) {
         for (int n = 0; n < 3; ++n) {
-            c = nmax(c, fabs(vel[n * g.N + t]) * dxi[n]);
-            f = nmax(f, fabs(src[n * g.N + t]) * dxi[n] * irho);
+            um[n] = imax_abs(um[n], vel[n * g.N + t]);
+            sm[n] = imax_abs(sm[n], src[n * g.N + t]);
         }
-        d = nmax(d, mu[t] * dxinv2 * irho);
+        mm = imax_abs(mm, mu[t]);  // mu_eff >= 0
     }
+    double c = 0, d = 0, f = 0;
+    for (int n = 0; n < 3; ++n) {
+        c = nmax(c, bitsd(um[n]) * dxi[n]);
+        f = nmax(f, bitsd(sm[n]) * dxi[n] * irho);
+    }
+    d = bitsd(mm) * dxinv2 * irho;
     c = block_reduce<1>(c);
     d = block_reduce<1>(d);
     f = block_reduce<1>(f);
