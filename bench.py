@@ -38,8 +38,11 @@ CPU_SAMPLE = (128, 128, 64)  # same dx, physics and deck as the workload, 1/8 of
 # FP64 flops (an FMA counts 2) per algorithmic byte of the kernels that can
 # dominate the step: the column nodal sweeps (22 flops per node, 3 FP64 arrays),
 # the red-black Gauss-Seidel half-sweep (14 flops per updated cell, 2 arrays)
-FP64_FLOPS_PER_BYTE = {"(k_nd_col<T,0>)": 22.0 / 24.0, "(k_nd_col<double,1>)": 22.0 / 24.0, "(k_nd_col<T,2>)": 19.0 / 24.0,
-                       "k_cc_gsrb<T>": 14.0 / 16.0}
+# FP64 flops per algorithmic byte (an FMA counts 2): nodal column sweep 20 flops per node (5 plane
+# sums, 3 pair sums, 5 FMAs from the right-hand side, 1 FMA update) over 24 bytes; residual form 18;
+# red-black update 10 flops over 16 bytes
+FP64_FLOPS_PER_BYTE = {"(k_nd_col<T,0>)": 20.0 / 24.0, "(k_nd_col<double,1>)": 20.0 / 24.0, "(k_nd_col<T,2>)": 18.0 / 24.0,
+                       "k_cc_gsrb<T>": 10.0 / 16.0}
 
 
 def parse():
@@ -210,7 +213,8 @@ def our_arm(args, rank, world, local_rank):
             sim.profile_kernels("*")
         sim.step()
     breakdown = sim.profile_report()
-    dominant = max(breakdown, key=lambda k: breakdown[k][1])
+    # "(mg_coarse_graph)" times whole graph replays (many kernels), not one kernel
+    dominant = max((k for k in breakdown if not k.startswith("(mg_")), key=lambda k: breakdown[k][1])
     if args.profile_all and rank == 0:
         tot = sum(v[1] for v in breakdown.values())
         for k, v in sorted(breakdown.items(), key=lambda kv: -kv[1][1]):
@@ -655,7 +659,7 @@ def main():
             "gpu_launches": r["launches"], "clocks": r["clocks"], "e2e": r["e2e"], "mixed_precision": r["mixed"],
             "adjoint": r["adjoint"], "tgv64": r["tgv"], "mol": r["mol"], "crank_nicolson": r["cn"],
             "stratified_abl": r["strat"]}
-    # The FP64 path is bound by FP64 issue on this GPU (profiles/k_nd_col_abl256_fp64.md): report the
+    # The FP64 path is bound by FP64 issue on this GPU (profiles/k_nd_col_abl128_fp64.md): report the
     # dominant kernel against the FMA peak measured live by ks_fma_peak as well.
     fl = FP64_FLOPS_PER_BYTE.get(r["dominant"])
     if fl and achieved:

@@ -436,6 +436,9 @@ inline long long nd_cols(const NDLevelT<T>& L, int kc) {
     return (long long)L.nx * L.ny * ((L.nz + kc - 1) / kc);
 }
 
+// Full weighting (1/4, 1/2, 1/4 in each direction) of the fine residual at a
+// coarse node, summed by weight class per fine layer; the wrapped / mirrored
+// fine indices are formed once (3 per direction) rather than per load.
 template <typename T>
 __global__ void k_nd_restrict(NDLevelT<T> F, NDLevelT<T> C) {
     const unsigned N = (unsigned)(C.nx * C.ny * C.nz);
@@ -443,35 +446,66 @@ __global__ void k_nd_restrict(NDLevelT<T> F, NDLevelT<T> C) {
     if (t >= N) return;
     int i, j, k;
     split3(t, (unsigned)C.nx, (unsigned)C.ny, i, j, k);
-    // full weighting: (1/4, 1/2, 1/4) in each direction, summed by weight class
-    T lay[3];
+    const int fi = 2 * i, fj = 2 * j, fk = 2 * k;
+    const int xm = fi == 0 ? F.nx - 1 : fi - 1, xp = fi + 1 == F.nx ? 0 : fi + 1;
+    const int sy = F.nx, sz = F.nx * F.ny;
+    const int ym = (fj == 0 ? F.ny - 1 : fj - 1) * sy, y0 = fj * sy, yp = (fj + 1 == F.ny ? 0 : fj + 1) * sy;
+    int zl[3];
     for (int c = -1; c <= 1; ++c) {
-        const T e = nd_at(F, F.res, 2 * i, 2 * j, 2 * k + c);
-        const T ex = nd_at(F, F.res, 2 * i - 1, 2 * j, 2 * k + c) + nd_at(F, F.res, 2 * i + 1, 2 * j, 2 * k + c);
-        const T ey = nd_at(F, F.res, 2 * i, 2 * j - 1, 2 * k + c) + nd_at(F, F.res, 2 * i, 2 * j + 1, 2 * k + c);
-        const T cr = (nd_at(F, F.res, 2 * i - 1, 2 * j - 1, 2 * k + c) + nd_at(F, F.res, 2 * i + 1, 2 * j - 1, 2 * k + c)) +
-                     (nd_at(F, F.res, 2 * i - 1, 2 * j + 1, 2 * k + c) + nd_at(F, F.res, 2 * i + 1, 2 * j + 1, 2 * k + c));
+        int kk = fk + c;
+        if (F.zper) kk = kk < 0 ? kk + F.nz : (kk >= F.nz ? kk - F.nz : kk);
+        else kk = kk < 0 ? -kk : (kk >= F.nz ? 2 * (F.nz - 1) - kk : kk);
+        zl[c + 1] = kk * sz;
+    }
+    const T* r = F.res;
+    T lay[3];
+    for (int c = 0; c < 3; ++c) {
+        const T* q = r + zl[c];
+        const T e = q[y0 + fi];
+        const T ex = q[y0 + xm] + q[y0 + xp];
+        const T ey = q[ym + fi] + q[yp + fi];
+        const T cr = (q[ym + xm] + q[ym + xp]) + (q[yp + xm] + q[yp + xp]);
         // in-plane weights 1/4 e + 1/8 (ex + ey) + 1/16 cr
-        lay[c + 1] = T(0.25) * e + (T(0.125) * (ex + ey) + T(0.0625) * cr);
+        lay[c] = T(0.25) * e + (T(0.125) * (ex + ey) + T(0.0625) * cr);
     }
     C.rhs[t] = T(0.5) * lay[1] + T(0.25) * (lay[0] + lay[2]);
     C.phi[t] = T(0);
 }
 
+// Trilinear prolongation added to the fine level, one thread per coarse node:
+// it reads the 8 coarse nodes of the cube above it once and writes the up to 8
+// fine nodes it spans (the midpoints take the mean of 2, 4 or 8 coarse
+// values), with the pair sums shared.  A fine node of a wall-bounded z level
+// above the last coarse layer does not exist.
 template <typename T>
 __global__ void k_nd_prolong(NDLevelT<T> F, NDLevelT<T> C) {
-    const unsigned N = (unsigned)(F.nx * F.ny * F.nz);
+    const unsigned N = (unsigned)(C.nx * C.ny * C.nz);
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= N) return;
-    int i, j, k;
-    split3(t, (unsigned)F.nx, (unsigned)F.ny, i, j, k);
-    const int ci = i >> 1, cj = j >> 1, ck = k >> 1, oi = i & 1, oj = j & 1, ok = k & 1;
-    T s = T(0);
-    for (int c = 0; c <= ok; ++c)
-        for (int b = 0; b <= oj; ++b)
-            for (int a = 0; a <= oi; ++a) s += nd_at(C, C.phi, ci + a, cj + b, ck + c);
-    const int cnt = (1 + oi) * (1 + oj) * (1 + ok);
-    F.phi[t] += (cnt == 1) ? s : (cnt == 2 ? T(0.5) * s : (cnt == 4 ? T(0.25) * s : T(0.125) * s));
+    int ci, cj, ck;
+    split3(t, (unsigned)C.nx, (unsigned)C.ny, ci, cj, ck);
+    const int cip = ci + 1 == C.nx ? 0 : ci + 1, cjp = cj + 1 == C.ny ? 0 : cj + 1;
+    const bool up = C.zper || ck + 1 < C.nz;  // the fine layer 2 ck + 1 exists
+    const int ckp = ck + 1 == C.nz ? 0 : ck + 1;
+    const int csy = C.nx, csz = C.nx * C.ny;
+    const T* c = C.phi;
+    const T c000 = c[ck * csz + cj * csy + ci], c100 = c[ck * csz + cj * csy + cip];
+    const T c010 = c[ck * csz + cjp * csy + ci], c110 = c[ck * csz + cjp * csy + cip];
+    const T x00 = c000 + c100, x10 = c010 + c110, y00 = c000 + c010;
+    const int fsy = F.nx, fsz = F.nx * F.ny;
+    T* f = F.phi + (2 * ck) * fsz + (2 * cj) * fsy + 2 * ci;
+    f[0] += c000;
+    f[1] += T(0.5) * x00;
+    f[fsy] += T(0.5) * y00;
+    f[fsy + 1] += T(0.25) * (x00 + x10);
+    if (!up) return;
+    const T c001 = c[ckp * csz + cj * csy + ci], c101 = c[ckp * csz + cj * csy + cip];
+    const T c011 = c[ckp * csz + cjp * csy + ci], c111 = c[ckp * csz + cjp * csy + cip];
+    const T x01 = c001 + c101, x11 = c011 + c111;
+    f[fsz] += T(0.5) * (c000 + c001);
+    f[fsz + 1] += T(0.25) * (x00 + x01);
+    f[fsz + fsy] += T(0.25) * (y00 + (c001 + c011));
+    f[fsz + fsy + 1] += T(0.125) * ((x00 + x10) + (x01 + x11));
 }
 
 // Bottom solve: weighted-Jacobi sweeps by one CTA, staged in shared memory
@@ -597,7 +631,7 @@ void launch_nd_restrict(Ctx& c, const NDLevelT<T>& F, const NDLevelT<T>& C) {
 }
 template <typename T>
 void launch_nd_prolong(Ctx& c, const NDLevelT<T>& F, const NDLevelT<T>& C) {
-    KS_LAUNCH(c, k_nd_prolong<T>, nblocks((long long)F.nx * F.ny * F.nz, BS), BS, sizeof(T) * (2.0 * nnd(F) + nnd(C)), F, C);
+    KS_LAUNCH(c, k_nd_prolong<T>, nblocks((long long)C.nx * C.ny * C.nz, BS), BS, sizeof(T) * (2.0 * nnd(F) + nnd(C)), F, C);
 }
 template <typename T>
 void launch_nd_bottom(Ctx& c, const NDLevelT<T>& L, double sigma, double omega, int sweeps) {

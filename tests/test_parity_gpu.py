@@ -155,3 +155,18 @@ def test_maxiter_reports_not_converged(cuda_dev):
     with pytest.raises(cuda_dev.KsError) as e:
         g.InitData()
     assert e.value.code == 3
+
+
+def test_graph_replay_matches_launches(cuda_dev):
+    """The coarse V-cycle tails replayed as CUDA graphs run the same kernels
+    with the same arguments as launching them one by one: bitwise equal."""
+    base = decks.abl(64, 64, 32, steps=4)
+    out = {}
+    for graphs in (0, 1):
+        g = cuda_dev.Incflo(base + "ks.mg_graphs = %d\n" % graphs)
+        g.InitData()
+        for _ in range(2):
+            assert g.step()
+        out[graphs] = (g.get_field("velocity"), g.get_field("p"), g.scalar("mac_iters"), g.scalar("nodal_iters"))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert out[0][2:] == out[1][2:]
