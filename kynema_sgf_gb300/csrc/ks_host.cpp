@@ -494,8 +494,12 @@ void Sim::alloc() {
         const size_t nn = (size_t)dm[0] * dm[1] * (dm[2] + (g_.zper ? 0 : 1));
         mgtot += 3 * nc + 4 * nn;
     }
-    // the multigrid and face kernels index a level with 32-bit integers
+    // the multigrid and face kernels index a level with 32-bit integers and put
+    // y (and z chunks) on the second grid dimension of their launches
     if ((long long)g_.nx * g_.ny * (g_.nz + 1) >= (1LL << 31)) throw KsError(KS_ERR_UNSUPPORTED, "grid of 2^31 or more nodes");
+    auto chunks = [](long long n) { return (n + 31) / 32; };
+    if (g_.ny > 65535 || g_.nz > 65535 || g_.ny * chunks(g_.nz + 1) > 65535 || g_.nz * chunks(g_.ny) > 65535)
+        throw KsError(KS_ERR_UNSUPPORTED, "amr.n_cell too large in y or z for the column launches");
     mgbuf_.alloc(mgtot);
     q = mgbuf_.p;
     double h[3] = {g_.dx, g_.dy, g_.dz};

@@ -145,37 +145,33 @@ __global__ void k_smag(Grid g, const double* vel, double* mueff, double mu, doub
 // src = rho (-gp/rho + geostrophic + Coriolis(u_old) + body + actuator)
 // (icns_ops.H:78-124, PDEOps.H:94-145, GeostrophicForcing.cpp:103-,
 // CoriolisForcing.cpp:60-108, BodyForce.cpp:117-169, ActuatorForcing.cpp:19-29)
-__global__ void k_sources(Grid g, const double* vel, const double* gp, const double* act, double* src, Scalars s, const double* theta) {
+// The sources are affine in the Old velocity, so the launcher folds them on
+// the host: src_n = (c_n - gp_n) + sum_m M_nm u_m + rho act_n + rho g_n beta (T0 - theta),
+// with c = rho (geostrophic + body + ABLForcing) and M = rho x the Coriolis
+// map.  About 12 FP64 instructions per cell where the term-by-term form took 45.
+struct SrcCoef {
+    double c[3];
+    double M[3][3];
+    double rho, bous_g[3], T_ref;
+    int cor, act, bous;
+};
+__global__ void k_sources(Grid g, const double* vel, const double* gp, const double* act, double* src, SrcCoef s, const double* theta) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= g.N) return;
     const long long N = g.N;
     double f[3];
-    for (int n = 0; n < 3; ++n) f[n] = -gp[n * N + t] * s.irho;
-    if (s.geo)
-        for (int n = 0; n < 3; ++n) f[n] += (n == 2 ? s.hfac : 1.0) * s.gf[n];
+    for (int n = 0; n < 3; ++n) f[n] = s.c[n] - gp[n * N + t];
     if (s.cor) {
         const double u0 = vel[t], u1 = vel[N + t], u2 = vel[2 * N + t];
-        const double ue = s.east[0] * u0 + s.east[1] * u1 + s.east[2] * u2;
-        const double un = s.north[0] * u0 + s.north[1] * u1 + s.north[2] * u2;
-        const double uu = s.up[0] * u0 + s.up[1] * u1 + s.up[2] * u2;
-        const double ae = s.corfac * (un * s.sinphi - s.hfac * uu * s.cosphi);
-        const double an = -s.corfac * ue * s.sinphi;
-        const double au = s.hfac * s.corfac * ue * s.cosphi;
-        for (int n = 0; n < 3; ++n) f[n] += ae * s.east[n] + an * s.north[n] + au * s.up[n];
+        for (int n = 0; n < 3; ++n) f[n] += s.M[n][0] * u0 + s.M[n][1] * u1 + s.M[n][2] * u2;
     }
-    if (s.body)
-        for (int n = 0; n < 3; ++n) f[n] += s.body_force[n];
     if (s.act)
-        for (int n = 0; n < 3; ++n) f[n] += act[n * N + t];
-    if (s.bous) {  // BoussinesqBuoyancy.cpp:22-50
-        const double fac = s.beta_T * (s.T_ref - theta[t]);
-        for (int n = 0; n < 3; ++n) f[n] += s.grav[n] * fac;
+        for (int n = 0; n < 3; ++n) f[n] += s.rho * act[n * N + t];
+    if (s.bous) {  // BoussinesqBuoyancy.cpp:22-50: rho g beta (T0 - theta)
+        const double dT = s.T_ref - theta[t];
+        for (int n = 0; n < 3; ++n) f[n] += s.bous_g[n] * dT;
     }
-    if (s.ablf) {  // ABLForcing.cpp:97-139
-        f[0] += s.ablf_force[0];
-        f[1] += s.ablf_force[1];
-    }
-    for (int n = 0; n < 3; ++n) src[n * N + t] = s.rho * f[n];
+    for (int n = 0; n < 3; ++n) src[n * N + t] = f[n];
 }
 
 // ---------------------------------------------------------------- ABL wall
@@ -743,9 +739,32 @@ void launch_smagorinsky(Ctx& c, const Grid& g, const double* vel, double* mueff,
     KS_LAUNCH(c, k_smag, nblocks(g.N, BS), BS, B8 * ((s.smag ? 4 : 1) + (alpha ? 1 : 0)) * g.N, g, vel, mueff, s.mu, s.rho, s.smag_fac, s.smag,
               alpha, s.mu_pr, s.iprt);
 }
+// src = rho (-gp/rho + geostrophic + Coriolis(u_old) + body + actuator + Boussinesq + ABLForcing)
+// (icns_ops.H:78-124, PDEOps.H:94-145, GeostrophicForcing.cpp:103-, CoriolisForcing.cpp:60-108,
+// BodyForce.cpp:117-169, ActuatorForcing.cpp:19-29): the Coriolis acceleration
+//   ae e + an n + au u,  ae = f (un sin - h uu cos), an = -f ue sin, au = h f ue cos
+// (e, n, u the east / north / up unit vectors, ue = e.u etc., f = corfac, h = hfac) is the linear map
+//   M = f sin (e n^T - n e^T) + f h cos (u e^T - e u^T).
 void launch_sources(Ctx& c, const Grid& g, const double* vel_old, const double* gp, const double* act, double* src, const Scalars& s,
                     const double* theta) {
-    KS_LAUNCH(c, k_sources, nblocks(g.N, BS), BS, B8 * (6 + 3 * s.cor + 3 * s.act + s.bous) * g.N, g, vel_old, gp, act, src, s, theta);
+    SrcCoef k{};
+    k.rho = s.rho;
+    k.cor = s.cor;
+    k.act = s.act;
+    k.bous = s.bous;
+    k.T_ref = s.T_ref;
+    for (int n = 0; n < 3; ++n) {
+        double a = 0.0;
+        if (s.geo) a += (n == 2 ? s.hfac : 1.0) * s.gf[n];
+        if (s.body) a += s.body_force[n];
+        if (s.ablf && n < 2) a += s.ablf_force[n];
+        k.c[n] = s.rho * a;
+        k.bous_g[n] = s.rho * s.grav[n] * s.beta_T;
+        for (int m = 0; m < 3; ++m)
+            k.M[n][m] = s.rho * s.corfac *
+                        (s.sinphi * (s.east[n] * s.north[m] - s.north[n] * s.east[m]) + s.hfac * s.cosphi * (s.up[n] * s.east[m] - s.east[n] * s.up[m]));
+    }
+    KS_LAUNCH(c, k_sources, nblocks(g.N, BS), BS, B8 * (6 + 3 * s.cor + 3 * s.act + s.bous) * g.N, g, vel_old, gp, act, src, k, theta);
 }
 void launch_plane_sums(Ctx& c, const Grid& g, const double* vel, double* parts, int* np) {
     *np = parts_for((long long)g.nx * g.ny);

@@ -126,28 +126,45 @@ __global__ void k_cc_gsrb(CCLevelT<T> L, CCCoef<T> w, int color, int kc) {
     const int dyp = (j + 1 == L.ny ? -j : 1) * sy, dym = (j == 0 ? L.ny - 1 : -1) * sy;
     T* p = L.phi;
     const T* rhs = L.rhs;
-    for (int k = k0; k < k1; ++k) {
-        const int s = (j + k + color) & 1;
-        const int i = 2 * i2 + s;
-        const int c = k * sz + j * sy + i;
+    // The values one update needs: its right-hand side, the x and y neighbour
+    // pair sums and the z neighbour sum (all of the other colour, which this
+    // half-sweep does not write).  They are loaded one layer ahead, before the
+    // store of the current layer, so the loads of layer k + 1 overlap the
+    // FP64 work of layer k.
+    struct Upd {
+        int c;
+        T r, sx, sy, sz;
+    };
+    auto fetch = [&](int k) {
+        Upd u;
+        const int i = 2 * i2 + ((j + k + color) & 1);
+        u.c = k * sz + j * sy + i;
         const int dxp = i + 1 == L.nx ? 1 - L.nx : 1, dxm = i == 0 ? L.nx - 1 : -1;
-        T zs;
-        T gx = w.gx0, gy = w.gy0, gz = w.gz0, iv = w.iv0;
+        u.r = rhs[u.c];
+        u.sx = p[u.c + dxp] + p[u.c + dxm];
+        u.sy = p[u.c + dyp] + p[u.c + dym];
         if (L.zper) {
             const int kp = k + 1 == L.nz ? 0 : k + 1, km = k == 0 ? L.nz - 1 : k - 1;
-            zs = p[c + (kp - k) * sz] + p[c + (km - k) * sz];
+            u.sz = p[u.c + (kp - k) * sz] + p[u.c + (km - k) * sz];
         } else {
-            const bool lo = k == 0, hi = k + 1 == L.nz;
-            zs = (lo ? T(0) : p[c - sz]) + (hi ? T(0) : p[c + sz]);
-            if (lo || hi) {
-                const bool one = lo && hi;
-                gx = one ? w.gx2 : w.gx1;
-                gy = one ? w.gy2 : w.gy1;
-                gz = one ? w.gz2 : w.gz1;
-                iv = one ? w.iv2 : w.iv1;
-            }
+            u.sz = (k == 0 ? T(0) : p[u.c - sz]) + (k + 1 == L.nz ? T(0) : p[u.c + sz]);
         }
-        p[c] = iv * rhs[c] + (gx * (p[c + dxp] + p[c + dxm]) + gy * (p[c + dyp] + p[c + dym]) + gz * zs);
+        return u;
+    };
+    Upd cur = fetch(k0);
+    for (int k = k0; k < k1; ++k) {
+        Upd nxt = cur;
+        if (k + 1 < k1) nxt = fetch(k + 1);
+        T gx = w.gx0, gy = w.gy0, gz = w.gz0, iv = w.iv0;
+        if (!L.zper && (k == 0 || k + 1 == L.nz)) {
+            const bool one = L.nz == 1;
+            gx = one ? w.gx2 : w.gx1;
+            gy = one ? w.gy2 : w.gy1;
+            gz = one ? w.gz2 : w.gz1;
+            iv = one ? w.iv2 : w.iv1;
+        }
+        p[cur.c] = iv * cur.r + (gx * cur.sx + gy * cur.sy + gz * cur.sz);
+        cur = nxt;
     }
 }
 
@@ -169,26 +186,41 @@ __global__ void k_cc_resid(CCLevelT<T> L, CCCoef<T> w, int kc, double* parts, fl
         const int dxp = i + 1 == L.nx ? 1 - L.nx : 1, dxm = i == 0 ? L.nx - 1 : -1;
         const int dyp = (j + 1 == L.ny ? -j : 1) * sy, dym = (j == 0 ? L.ny - 1 : -1) * sy;
         const int k0 = ch * kc, k1 = min(k0 + kc, L.nz);
-        for (int k = k0; k < k1; ++k) {
+        // the loads of layer k + 1 are issued before the stores of layer k
+        struct Ld {
+            T r, pc, sx, sy, sz;
+        };
+        auto fetch = [&](int k) {
+            Ld u;
             const int c = k * sz + j * sy + i;
-            T zs;
-            T gx = w.gx0, gy = w.gy0, gz = w.gz0, dg = w.dg0;
+            u.r = L.rhs[c];
+            u.pc = p[c];
+            u.sx = p[c + dxp] + p[c + dxm];
+            u.sy = p[c + dyp] + p[c + dym];
             if (L.zper) {
                 const int kp = k + 1 == L.nz ? 0 : k + 1, km = k == 0 ? L.nz - 1 : k - 1;
-                zs = p[c + (kp - k) * sz] + p[c + (km - k) * sz];
+                u.sz = p[c + (kp - k) * sz] + p[c + (km - k) * sz];
             } else {
-                const bool lo = k == 0, hi = k + 1 == L.nz;
-                zs = (lo ? T(0) : p[c - sz]) + (hi ? T(0) : p[c + sz]);
-                if (lo || hi) {
-                    const bool one = lo && hi;
-                    gx = one ? w.gx2 : w.gx1;
-                    gy = one ? w.gy2 : w.gy1;
-                    gz = one ? w.gz2 : w.gz1;
-                    dg = one ? w.dg2 : w.dg1;
-                }
+                u.sz = (k == 0 ? T(0) : p[c - sz]) + (k + 1 == L.nz ? T(0) : p[c + sz]);
             }
-            const T S = gx * (p[c + dxp] + p[c + dxm]) + gy * (p[c + dyp] + p[c + dym]) + gz * zs;
-            const T v = L.rhs[c] - dg * (p[c] - S);
+            return u;
+        };
+        Ld cur = fetch(k0);
+        for (int k = k0; k < k1; ++k) {
+            Ld nxt = cur;
+            if (k + 1 < k1) nxt = fetch(k + 1);
+            const int c = k * sz + j * sy + i;
+            T gx = w.gx0, gy = w.gy0, gz = w.gz0, dg = w.dg0;
+            if (!L.zper && (k == 0 || k + 1 == L.nz)) {
+                const bool one = L.nz == 1;
+                gx = one ? w.gx2 : w.gx1;
+                gy = one ? w.gy2 : w.gy1;
+                gz = one ? w.gz2 : w.gz1;
+                dg = one ? w.dg2 : w.dg1;
+            }
+            const T S = gx * cur.sx + gy * cur.sy + gz * cur.sz;
+            const T v = cur.r - dg * (cur.pc - S);
+            cur = nxt;
             if (r32) {
                 r32[c] = (float)v;
                 z32[c] = 0.0f;
