@@ -29,10 +29,10 @@ __device__ inline bool face_at(const Grid& g, int d, long long t, int& i, int& j
     const int nzl = (d == 2) ? nzfaces(g) : g.nz;
     const long long M = (long long)g.nx * g.ny * nzl;
     if (t >= M) return false;
-    i = (int)(t % g.nx);
-    const long long r = t / g.nx;
-    j = (int)(r % g.ny);
-    k = (int)(r / g.ny);
+    const unsigned u = (unsigned)t, r = u / (unsigned)g.nx;
+    i = (int)(u - r * (unsigned)g.nx);
+    k = (int)(r / (unsigned)g.ny);
+    j = (int)(r - (unsigned)k * (unsigned)g.ny);
     return true;
 }
 inline long long nfaces(const Grid& g, int d) { return (long long)g.nx * g.ny * (d == 2 ? nzfaces(g) : g.nz); }

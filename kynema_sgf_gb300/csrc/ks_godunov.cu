@@ -613,9 +613,9 @@ template <typename T, int NC = 3>
 __global__ void k_adv_div(Grid g, FluxPtrs<T> F, double* conv) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= g.N) return;
-    const int i = (int)(t % g.nx);
-    const long long r = t / g.nx;
-    const int j = (int)(r % g.ny), k = (int)(r / g.ny);
+    const unsigned u = (unsigned)t, r = u / (unsigned)g.nx;
+    const int i = (int)(u - r * (unsigned)g.nx);
+    const int k = (int)(r / (unsigned)g.ny), j = (int)(r - (unsigned)k * (unsigned)g.ny);
     const long long xp = fidx(g, 0, i + 1, j, k), yp = fidx(g, 1, i, j + 1, k), zp = fidx(g, 2, i, j, k + 1), zm = fidx(g, 2, i, j, k);
     const T ix = T(g.idx), iy = T(g.idy), iz = T(g.idz);
     for (int n = 0; n < NC; ++n)

@@ -37,9 +37,9 @@ __global__ void k_diff_dinv(Grid g, const double* mu, double rho, double dtd, do
     const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const bool live = t0 < g.N;
     const long long t = live ? t0 : 0;
-    const int i = (int)(t % g.nx);
-    const long long r = t / g.nx;
-    const int j = (int)(r % g.ny), k = (int)(r / g.ny);
+    const unsigned u = (unsigned)t, r = u / (unsigned)g.nx;
+    const int i = (int)(u - r * (unsigned)g.nx);
+    const int k = (int)(r / (unsigned)g.ny), j = (int)(r - (unsigned)k * (unsigned)g.ny);
     const double c0 = mu[t];
     const double mx = 0.5 * (mu[cidx(g, wrapn(i - 1, g.nx), j, k)] + c0) + 0.5 * (mu[cidx(g, wrapn(i + 1, g.nx), j, k)] + c0);
     const double my = 0.5 * (mu[cidx(g, i, wrapn(j - 1, g.ny), k)] + c0) + 0.5 * (mu[cidx(g, i, wrapn(j + 1, g.ny), k)] + c0);

@@ -358,6 +358,7 @@ struct TauEpi {
     double* forces;
     double* parts;
     double dt, rho, omega;
+    double irho;  // 1 / rho, formed on the host
 };
 
 __global__ void __launch_bounds__(TTX* TTY* TTZ) k_divtau_tile(Grid g, const double* vel, const double* mueff, const double* wg, double* out,
@@ -435,7 +436,7 @@ __global__ void __launch_bounds__(TTX* TTY* TTZ) k_divtau_tile(Grid g, const dou
     const int tx = tid % TTX, ty = (tid / TTX) % TTY, tz = tid / (TTX * TTY);
     const int i = i0 + tx, j = j0 + ty, k = k0 + tz;
     const bool live = i < g.nx && j < g.ny && k < g.nz;
-    const double rho = E.rho, dt = E.dt, irho = 1.0 / rho;
+    const double rho = E.rho, dt = E.dt, irho = E.irho;
     const long long N = g.N, t = live ? cidx(g, i, j, k) : 0;
     double rmax = 0.0;
     for (int n = 0; n < 3 && live; ++n) {
@@ -477,93 +478,107 @@ __global__ void __launch_bounds__(TTX* TTY* TTZ) k_divtau_tile(Grid g, const dou
 // predictor_rhs (src/equation_systems/CompRHSOps.H:32-141); fac = 1 explicit,
 // 1/2 Crank-Nicolson, 0 implicit
 __global__ void k_pred_rhs(long long N3, const double* vo, const double* conv, const double* src, const double* dt_, double* vel, double dt,
-                           double rho, double fac) {
+                           double rho, double irho, double fac) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= N3) return;
-    vel[t] = (rho * vo[t] + dt * (conv[t] + src[t] + fac * dt_[t])) * (1.0 / rho);
+    vel[t] = (rho * vo[t] + dt * (conv[t] + src[t] + fac * dt_[t])) * irho;
 }
 
 // ---------------------------------------------------------------- projection
-__global__ void k_proj_pre(long long N3, double* vel, const double* vo, const double* gp, double scaling, double rho, int add_gp,
-                           int sub_old) {
+__global__ void k_proj_pre(long long N3, double* vel, const double* vo, const double* gp, double sr, int add_gp, int sub_old) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= N3) return;
     double v = vel[t];
-    if (add_gp) v += gp[t] * (scaling / rho);
+    if (add_gp) v += gp[t] * sr;  // sr = scaling / rho, formed on the host
     if (sub_old) v -= vo[t];
     vel[t] = v;
 }
 
-// Cell velocity as seen by the nodal divergence: periodic wrap, mirror images
-// across z walls (normal component odd, tangential even).
-__device__ inline double vel_mirror(const Grid& g, const double* v, int n, int i, int j, int k) {
-    i = wrapn(i, g.nx);
-    j = wrapn(j, g.ny);
-    double s = 1.0;
-    if (g.zper) k = wrapn(k, g.nz);
-    else if (k < 0) { k = -1 - k; s = (n == 2) ? -1.0 : 1.0; }
-    else if (k >= g.nz) { k = 2 * g.nz - 1 - k; s = (n == 2) ? -1.0 : 1.0; }
-    return s * v[n * g.N + cidx(g, i, j, k)];
-}
-
 // Nodal divergence (the MLNodeLaplacian right-hand side) with weighted partial
-// sums (boundary nodes carry half weight) for the solvability shift.
-__global__ void k_nodal_rhs(Grid g, const double* vel, double* rhs, double* parts, int np) {
+// sums (boundary nodes carry half weight) for the solvability shift.  The cell
+// velocity is seen with periodic wrap and mirror images across z walls (normal
+// component odd, tangential even; the sign flip is taken on the bits).  Each
+// direction's four edge differences are summed before its one scale
+// q = dx^-1 / 4.
+__global__ void k_nodal_rhs(Grid g, const double* vel, double* rhs, double* parts, int np, double qx, double qy, double qz) {
     const int nzn = g.zper ? g.nz : g.nz + 1;
-    const long long M = (long long)g.nx * g.ny * nzn;
+    const unsigned M = (unsigned)(g.nx * g.ny * nzn);
     double ws = 0, wt = 0;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < M; t += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(t % g.nx);
-        const long long r = t / g.nx;
-        const int j = (int)(r % g.ny), k = (int)(r / g.ny);
-        double dv = 0;
-        for (int c = 0; c < 2; ++c)
-            for (int b = 0; b < 2; ++b) {
-                dv += 0.25 * g.idx * (vel_mirror(g, vel, 0, i, j - b, k - c) - vel_mirror(g, vel, 0, i - 1, j - b, k - c));
-                dv += 0.25 * g.idy * (vel_mirror(g, vel, 1, i - b, j, k - c) - vel_mirror(g, vel, 1, i - b, j - 1, k - c));
-                dv += 0.25 * g.idz * (vel_mirror(g, vel, 2, i - b, j - c, k) - vel_mirror(g, vel, 2, i - b, j - c, k - 1));
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < M; t += gridDim.x * blockDim.x) {
+        const unsigned r = t / (unsigned)g.nx;
+        const int i = (int)(t - r * (unsigned)g.nx);
+        const int k = (int)(r / (unsigned)g.ny), j = (int)(r - (unsigned)k * (unsigned)g.ny);
+        const int im = i == 0 ? g.nx - 1 : i - 1, jm = j == 0 ? g.ny - 1 : j - 1;
+        // cell layers k - 1 and k as seen from the node (mirrored at walls)
+        int kk[2];
+        bool flip[2];
+        for (int c = 0; c < 2; ++c) {
+            int q = k - c;
+            flip[c] = false;
+            if (g.zper) q = q < 0 ? q + g.nz : (q >= g.nz ? q - g.nz : q);
+            else if (q < 0) { q = -1 - q; flip[c] = true; }
+            else if (q >= g.nz) { q = 2 * g.nz - 1 - q; flip[c] = true; }
+            kk[c] = q;
+        }
+        const long long N = g.N;
+        // the 8 cells around the node: layers k-1 (c = 1) and k (c = 0), columns (i, j), (i-1, j), (i, j-1), (i-1, j-1)
+        double u[2][4], v[2][4], w[2][4];
+        for (int c = 0; c < 2; ++c) {
+            const long long r0 = (long long)kk[c] * g.ny;
+            const long long o[4] = {(r0 + j) * g.nx + i, (r0 + j) * g.nx + im, (r0 + jm) * g.nx + i, (r0 + jm) * g.nx + im};
+            for (int q = 0; q < 4; ++q) {
+                u[c][q] = vel[o[q]];
+                v[c][q] = vel[N + o[q]];
+                const double z = vel[2 * N + o[q]];
+                w[c][q] = flip[c] ? bitsd(dbits(z) ^ ~kMag) : z;
             }
+        }
+        double dx = 0, dy = 0, dz = 0;
+        for (int c = 0; c < 2; ++c) {
+            dx += (u[c][0] - u[c][1]) + (u[c][2] - u[c][3]);
+            dy += (v[c][0] - v[c][2]) + (v[c][1] - v[c][3]);
+        }
+        // z: differences of w between the layers k and k - 1 over the four cells
+        dz = ((w[0][0] - w[1][0]) + (w[0][1] - w[1][1])) + ((w[0][2] - w[1][2]) + (w[0][3] - w[1][3]));
+        const double dv = qx * dx + (qy * dy + qz * dz);
         rhs[t] = dv;
-        const double w = (!g.zper && (k == 0 || k == nzn - 1)) ? 0.5 : 1.0;
-        ws += w * dv;
-        wt += w;
+        const double wgt = (!g.zper && (k == 0 || k == nzn - 1)) ? 0.5 : 1.0;
+        ws += wgt * dv;
+        wt += wgt;
     }
     ws = block_reduce<0>(ws);
     wt = block_reduce<0>(wt);
     if (threadIdx.x == 0) { parts[blockIdx.x] = ws; parts[np + blockIdx.x] = wt; }
 }
 
-__device__ inline double node_at(const Grid& g, const double* phi, int i, int j, int k) {
-    const int nzn = g.zper ? g.nz : g.nz + 1;
-    i = wrapn(i, g.nx);
-    j = wrapn(j, g.ny);
-    if (g.zper) k = wrapn(k, g.nz);
-    return phi[((long long)k * g.ny + j) * g.nx + i];
-    (void)nzn;
-}
-
-// u -= sigma G phi ; gp = (or +=) G phi ; optional add-back of u_old.
-__global__ void k_nodal_post_cells(Grid g, const double* phi, double* vel, const double* vo, double* gp, double sigma, int add_old,
-                                   int incr) {
+// u -= sigma G phi ; gp = (or +=) G phi ; optional add-back of u_old.  G is the
+// cell gradient of the nodal phi (the mean of the four edge differences in
+// each direction), formed from the cell's 8 corner nodes with shared pair sums;
+// q = dx^-1 / 4 and sigma q are folded on the host.
+__global__ void k_nodal_post_cells(Grid g, const double* phi, double* vel, const double* vo, double* gp, double qx, double qy, double qz,
+                                   double sqx, double sqy, double sqz, int add_old, int incr) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= g.N) return;
     int i, j, k;
     cell_of(g, t, i, j, k);
-    double gx = 0, gy = 0, gz = 0;
-    for (int c = 0; c < 2; ++c)
-        for (int b = 0; b < 2; ++b) {
-            gx += node_at(g, phi, i + 1, j + b, k + c) - node_at(g, phi, i, j + b, k + c);
-            gy += node_at(g, phi, i + b, j + 1, k + c) - node_at(g, phi, i + b, j, k + c);
-            gz += node_at(g, phi, i + b, j + c, k + 1) - node_at(g, phi, i + b, j + c, k);
-        }
-    const double G[3] = {0.25 * gx * g.idx, 0.25 * gy * g.idy, 0.25 * gz * g.idz};
+    const int ip = i + 1 == g.nx ? 0 : i + 1, jp = j + 1 == g.ny ? 0 : j + 1;
+    const int kp = (g.zper && k + 1 == g.nz) ? 0 : k + 1;  // nodes 0..nz at walls
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    const long long r0 = k * sz, r1 = kp * sz, c0 = j * sy, c1 = jp * sy;
+    const double n000 = phi[r0 + c0 + i], n100 = phi[r0 + c0 + ip], n010 = phi[r0 + c1 + i], n110 = phi[r0 + c1 + ip];
+    const double n001 = phi[r1 + c0 + i], n101 = phi[r1 + c0 + ip], n011 = phi[r1 + c1 + i], n111 = phi[r1 + c1 + ip];
+    const double za = n000 + n001, zb = n100 + n101, zc = n010 + n011, zd = n110 + n111;
+    const double gx = (zb + zd) - (za + zc), gy = (zc + zd) - (za + zb);
+    const double gz = ((n001 + n101) + (n011 + n111)) - ((n000 + n100) + (n010 + n110));
+    const double Gv[3] = {gx, gy, gz}, q[3] = {qx, qy, qz}, sq[3] = {sqx, sqy, sqz};
     const long long N = g.N;
     for (int n = 0; n < 3; ++n) {
-        double v = vel[n * N + t] - sigma * G[n];
+        double v = vel[n * N + t] - sq[n] * Gv[n];
         if (add_old) v += vo[n * N + t];
         vel[n * N + t] = v;
-        if (incr) gp[n * N + t] += G[n];
-        else gp[n * N + t] = G[n];
+        const double G = q[n] * Gv[n];
+        if (incr) gp[n * N + t] += G;
+        else gp[n * N + t] = G;
     }
 }
 
@@ -795,14 +810,14 @@ void launch_divtau(Ctx& c, const Grid& g, const double* vel, const double* mueff
     cudaFuncSetAttribute(k_divtau_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAU_SMEM);
     const dim3 grid((g.nx + TTX - 1) / TTX, (g.ny + TTY - 1) / TTY, (g.nz + TTZ - 1) / TTZ);
     const double per_cell = 4 + 3 + (mode == 1 ? 6 : 0) + (mode == 2 ? 6 : 0);
-    TauEpi E{mode, src, base, dold, nullptr, nullptr, nullptr, forces, nullptr, dt, rho, 0.0};
+    TauEpi E{mode, src, base, dold, nullptr, nullptr, nullptr, forces, nullptr, dt, rho, 0.0, 1.0 / rho};
     KS_LAUNCH_SMEM(c, k_divtau_tile, grid, TTX * TTY * TTZ, TAU_SMEM, B8 * per_cell * g.N, g, vel, mueff, wg, out, E);
 }
 void launch_divtau_corrector(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, const double* vel_old,
                              const double* conv_old, const double* conv_new, const double* dold, const double* src, double dt, double rho) {
     cudaFuncSetAttribute(k_divtau_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAU_SMEM);
     const dim3 grid((g.nx + TTX - 1) / TTX, (g.ny + TTY - 1) / TTY, (g.nz + TTZ - 1) / TTZ);
-    TauEpi E{3, src, vel_old, dold, conv_old, conv_new, nullptr, nullptr, nullptr, dt, rho, 0.0};
+    TauEpi E{3, src, vel_old, dold, conv_old, conv_new, nullptr, nullptr, nullptr, dt, rho, 0.0, 1.0 / rho};
     KS_LAUNCH_SMEM(c, k_divtau_tile, grid, TTX * TTY * TTZ, TAU_SMEM, B8 * 22.0 * g.N, g, vel, mueff, wg, out, E);
 }
 int divtau_tile_blocks(const Grid& g) { return ((g.nx + TTX - 1) / TTX) * ((g.ny + TTY - 1) / TTY) * ((g.nz + TTZ - 1) / TTZ); }
@@ -810,28 +825,28 @@ void launch_divtau_jacobi(Ctx& c, const Grid& g, const double* x, const double* 
                           double* out, double rho, double dtd, double omega, double* parts) {
     cudaFuncSetAttribute(k_divtau_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAU_SMEM);
     const dim3 grid((g.nx + TTX - 1) / TTX, (g.ny + TTY - 1) / TTY, (g.nz + TTZ - 1) / TTZ);
-    TauEpi E{omega > 0.0 ? 7 : 8, nullptr, b, nullptr, nullptr, nullptr, dinv, nullptr, parts, dtd, rho, omega};
+    TauEpi E{omega > 0.0 ? 7 : 8, nullptr, b, nullptr, nullptr, nullptr, dinv, nullptr, parts, dtd, rho, omega, 1.0 / rho};
     KS_LAUNCH_SMEM(c, k_divtau_tile, grid, TTX * TTY * TTZ, TAU_SMEM, B8 * ((omega > 0.0 ? 13.0 : 10.0) * g.N), g, x, mueff, wg, out, E);
 }
 void launch_predictor_rhs(Ctx& c, const Grid& g, const double* vo, const double* conv, const double* src, const double* dtau, double* vel,
                           double dt, double rho, double fac) {
-    KS_LAUNCH(c, k_pred_rhs, nblocks(3 * g.N, BS), BS, B8 * 15 * g.N, 3 * g.N, vo, conv, src, dtau, vel, dt, rho, fac);
+    KS_LAUNCH(c, k_pred_rhs, nblocks(3 * g.N, BS), BS, B8 * 15 * g.N, 3 * g.N, vo, conv, src, dtau, vel, dt, rho, 1.0 / rho, fac);
 }
 void launch_proj_pre(Ctx& c, const Grid& g, double* vel, const double* vo, const double* gp, double scaling, double rho, int add_gp,
                      int sub_old) {
-    KS_LAUNCH(c, k_proj_pre, nblocks(3 * g.N, BS), BS, B8 * 3 * (2 + add_gp + sub_old) * g.N, 3 * g.N, vel, vo, gp, scaling, rho, add_gp,
-              sub_old);
+    KS_LAUNCH(c, k_proj_pre, nblocks(3 * g.N, BS), BS, B8 * 3 * (2 + add_gp + sub_old) * g.N, 3 * g.N, vel, vo, gp, scaling / rho, add_gp, sub_old);
 }
 void launch_nodal_rhs(Ctx& c, const Grid& g, const double* vel, double* rhs, double* parts, int* np) {
     const long long M = (long long)g.nx * g.ny * (g.zper ? g.nz : g.nz + 1);
     *np = parts_for(M);
-    KS_LAUNCH(c, k_nodal_rhs, *np, BS, B8 * (3 * g.N + M), g, vel, rhs, parts, *np);
+    KS_LAUNCH(c, k_nodal_rhs, *np, BS, B8 * (3 * g.N + M), g, vel, rhs, parts, *np, 0.25 * g.idx, 0.25 * g.idy, 0.25 * g.idz);
 }
 void launch_nodal_post(Ctx& c, const Grid& g, const double* phi, double* vel, const double* vo, double* gp, double* p, double sigma,
                        int add_old, int incr) {
     const long long M = (long long)g.nx * g.ny * (g.zper ? g.nz : g.nz + 1);
-    KS_LAUNCH(c, k_nodal_post_cells, nblocks(g.N, BS), BS, B8 * (M + (9 + 3 * add_old + 3 * incr) * g.N), g, phi, vel, vo, gp, sigma,
-              add_old, incr);
+    const double qx = 0.25 * g.idx, qy = 0.25 * g.idy, qz = 0.25 * g.idz;
+    KS_LAUNCH(c, k_nodal_post_cells, nblocks(g.N, BS), BS, B8 * (M + (9 + 3 * add_old + 3 * incr) * g.N), g, phi, vel, vo, gp, qx, qy, qz,
+              sigma * qx, sigma * qy, sigma * qz, add_old, incr);
     KS_LAUNCH(c, k_nodal_post_nodes, nblocks(M, BS), BS, B8 * (2 + incr) * M, M, phi, p, incr);
 }
 void launch_mac_rhs(Ctx& c, const Grid& g, const double* um, const double* vm, const double* wm, double* rhs, double* parts, int* np) {

@@ -180,12 +180,12 @@ struct MolFlux {
 // corrector_rhs without the new diffusion term (Crank-Nicolson / implicit),
 // vel = (rho u_old + dt (0.5 (conv_old + conv) + fac divtau_old + src)) / rho
 __global__ void k_mol_div(Grid g, MolFlux F, int nc, double* conv, int mode, const double* vo, const double* src, const double* dold,
-                          const double* conv_o, double* vel, double dt, double rho, double fac) {
+                          const double* conv_o, double* vel, double dt, double rho, double fac, double irho) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= g.N) return;
-    const int i = (int)(t % g.nx);
-    const long long r = t / g.nx;
-    const int j = (int)(r % g.ny), k = (int)(r / g.ny);
+    const unsigned ut = (unsigned)t, r = ut / (unsigned)g.nx;
+    const int i = (int)(ut - r * (unsigned)g.nx);
+    const int k = (int)(r / (unsigned)g.ny), j = (int)(r - (unsigned)k * (unsigned)g.ny);
     const long long xp = fidx(g, 0, i + 1, j, k), yp = fidx(g, 1, i, j + 1, k);
     const long long zm = fidx(g, 2, i, j, k), zp = fidx(g, 2, i, j, k + 1);
     const long long N = g.N;
@@ -194,8 +194,8 @@ __global__ void k_mol_div(Grid g, MolFlux F, int nc, double* conv, int mode, con
                          (g.idz * (F.p[6 + n][zm] - F.p[6 + n][zp]));
         conv[n * N + t] = c;
         const long long m = n * N + t;
-        if (mode == 1) vel[m] = (rho * vo[m] + dt * (c + src[m] + fac * dold[m])) * (1.0 / rho);
-        else if (mode == 2) vel[m] = (rho * vo[m] + dt * (0.5 * (conv_o[m] + c) + fac * dold[m] + src[m])) * (1.0 / rho);
+        if (mode == 1) vel[m] = (rho * vo[m] + dt * (c + src[m] + fac * dold[m])) * irho;
+        else if (mode == 2) vel[m] = (rho * vo[m] + dt * (0.5 * (conv_o[m] + c) + fac * dold[m] + src[m])) * irho;
     }
 }
 
@@ -233,7 +233,7 @@ void launch_mol_advection(Ctx& c, const Grid& g, const double* vel, const double
     for (int m = 0; m < 9; ++m) F.p[m] = fl[m];
     const double nfz = (double)nfaces_d(g, 2);
     const double bytes = 8.0 * (6.0 * g.N + 3.0 * nfz + 3.0 * g.N + (mode == 1 ? 12.0 * g.N : (mode == 2 ? 15.0 * g.N : 0.0)));
-    KS_LAUNCH(c, k_mol_div, nblocks(g.N, BS), BS, bytes, g, F, 3, conv, mode, vel_old, src, dold, conv_old, vel_out, dt, rho, fac);
+    KS_LAUNCH(c, k_mol_div, nblocks(g.N, BS), BS, bytes, g, F, 3, conv, mode, vel_old, src, dold, conv_old, vel_out, dt, rho, fac, 1.0 / rho);
 }
 
 void launch_mol_scalar_advection(Ctx& c, const Grid& g, const double* s, const double* const mac[3], double rho, double* const fl[3],
@@ -247,7 +247,7 @@ void launch_mol_scalar_advection(Ctx& c, const Grid& g, const double* s, const d
     F.p[6] = fl[2];
     const double nfz = (double)nfaces_d(g, 2);
     KS_LAUNCH(c, k_mol_div, nblocks(g.N, BS), BS, 8.0 * (3.0 * g.N + nfz), g, F, 1, conv, 0, nullptr, nullptr, nullptr, nullptr, nullptr, 0.0,
-              rho, 0.0);
+              rho, 0.0, 1.0 / rho);
 }
 
 }  // namespace ks

@@ -193,17 +193,17 @@ __global__ void k_scalar_rhs(Grid g, const double* th, double rho, double* b, do
 
 // predictor_rhs of a scalar without sources: (rho s_old + dt (conv + 0 + fac dold)) / rho
 __global__ void k_scalar_pred(long long n, const double* so, const double* conv, const double* dold, double* out, double dt, double rho,
-                              double fac) {
+                              double fac, double irho) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (t < n) out[t] = (rho * so[t] + dt * (conv[t] + 0.0 + fac * dold[t])) * (1.0 / rho);
+    if (t < n) out[t] = (rho * so[t] + dt * (conv[t] + 0.0 + fac * dold[t])) * irho;
 }
 
 __global__ void k_scalar_corr(long long n, const double* so, const double* co, const double* cn, const double* dold, const double* dnew,
-                              double* out, double dt, double rho, double ofac, double nfac) {
+                              double* out, double dt, double rho, double ofac, double nfac, double irho) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= n) return;
     const double dn = dnew ? nfac * dnew[t] : 0.0;
-    out[t] = (rho * so[t] + dt * (0.5 * (co[t] + cn[t]) + ofac * dold[t] + dn + 0.0)) * (1.0 / rho);
+    out[t] = (rho * so[t] + dt * (0.5 * (co[t] + cn[t]) + ofac * dold[t] + dn + 0.0)) * irho;
 }
 
 __global__ void k_lincomb(long long n, double a, const double* x, double b, const double* y, double* out) {
@@ -246,12 +246,12 @@ void launch_scalar_rhs(Ctx& c, const Grid& g, const double* th, double rho, doub
 }
 void launch_scalar_pred(Ctx& c, long long n, const double* so, const double* conv, const double* dold, double* out, double dt, double rho,
                         double fac) {
-    KS_LAUNCH(c, k_scalar_pred, nblocks(n, BS), BS, 8.0 * 4.0 * n, n, so, conv, dold, out, dt, rho, fac);
+    KS_LAUNCH(c, k_scalar_pred, nblocks(n, BS), BS, 8.0 * 4.0 * n, n, so, conv, dold, out, dt, rho, fac, 1.0 / rho);
 }
 void launch_scalar_corr(Ctx& c, long long n, const double* s_old, const double* conv_old, const double* conv, const double* dold,
                         const double* dnew, double* out, double dt, double rho, double ofac, double nfac) {
     KS_LAUNCH(c, k_scalar_corr, nblocks(n, BS), BS, 8.0 * (6.0 + (dnew ? 1.0 : 0.0)) * n, n, s_old, conv_old, conv, dold, dnew, out, dt, rho,
-              ofac, nfac);
+              ofac, nfac, 1.0 / rho);
 }
 void launch_lincomb(Ctx& c, long long n, double a, const double* x, double b, const double* y, double* out) {
     KS_LAUNCH(c, k_lincomb, nblocks(n, BS), BS, 8.0 * 3.0 * n, n, a, x, b, y, out);
