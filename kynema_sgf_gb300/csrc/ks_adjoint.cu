@@ -21,7 +21,7 @@ constexpr int BS = 256;
 constexpr double kSV = kSmallVel;
 
 __device__ inline void aadd(double* p, double v) {
-    if (v != 0.0) atomicAdd(p, v);
+    if ((dbits(v) & kMag)) atomicAdd(p, v);
 }
 
 // faces of direction d, the same index domain as the forward kernels
@@ -43,7 +43,7 @@ __device__ inline double Q(const Grid& g, const double* u, int n, int i, int j, 
     return q(n, i, j, k);
 }
 __device__ inline void Qb(const Grid& g, double* ub, int n, int i, int j, int k, double v) {
-    if (v == 0.0) return;
+    if (!(dbits(v) & kMag)) return;
     i = wrapn(i, g.nx);
     j = wrapn(j, g.ny);
     double* c = ub + (long long)n * g.N;
@@ -94,9 +94,10 @@ __device__ inline void zbc_rev(const Grid& g, int k, int n, double& lb, double& 
 __device__ inline double vls_d(double a, double b, double c, double& ca, double& cb, double& cc) {
     const double dsc = 0.5 * (c - a), dsl = 2.0 * (b - a), dsr = 2.0 * (c - b);
     ca = cb = cc = 0.0;
-    if (!(dsl * dsr > 0.0)) return 0.0;
-    const double ac = fabs(dsc), al = fabs(dsl), ar = fabs(dsr);
-    if (ac <= fmin(al, ar)) {
+    if (!isame_sign(dsl, dsr)) return 0.0;
+    // magnitudes compared on the integer pipe (non-negative doubles order like their bits)
+    const long long ac = dbits(dsc) & kMag, al = dbits(dsl) & kMag, ar = dbits(dsr) & kMag;
+    if (ac <= (al < ar ? al : ar)) {
         ca = -0.5;
         cc = 0.5;
         return dsc;
@@ -114,13 +115,13 @@ __device__ inline double vls_d(double a, double b, double c, double& ca, double&
 // adjoint of clip(e, a, b) = min(max(e, min(a, b)), max(a, b)) given the
 // adjoint of the result: returns the adjoint of e; adds to those of a, b
 __device__ inline double clip_rev(double e, double a, double b, double rb, double& ga, double& gb) {
-    const double lo = fmin(a, b), hi = fmax(a, b);
-    if (fmax(e, lo) > hi) {
-        if (a >= b) ga += rb; else gb += rb;
+    const double lo = imin(a, b), hi = imax(a, b);
+    if (ilt(hi, imax(e, lo))) {
+        if (!ilt(a, b)) ga += rb; else gb += rb;
         return 0.0;
     }
-    if (e < lo) {
-        if (a <= b) ga += rb; else gb += rb;
+    if (ilt(e, lo)) {
+        if (!ilt(b, a)) ga += rb; else gb += rb;
         return 0.0;
     }
     return rb;
@@ -137,7 +138,7 @@ __global__ void k_adj_edges(Grid g, int d, const double* u, const double* Eb0, c
     const double* Eb[3] = {Eb0, Eb1, Eb2};
     for (int n = 0; n < 3; ++n) {
         const double eb = Eb[n][t];
-        if (eb == 0.0) continue;
+        if (!(dbits(eb) & kMag)) continue;
         if (wall && (k == 0 || k == g.nz)) {  // the wall face takes the ghost value
             Qb(g, ub, n, i, j, k == 0 ? -1 : g.nz, eb);
             continue;
@@ -163,7 +164,7 @@ __global__ void k_adj_edges(Grid g, int d, const double* u, const double* Eb0, c
         const double e = 0.5 * (a0 + a1) - (1.0 / 6.0) * (s1 - s0);
         double gm = 0.0, g0 = 0.0, g1 = 0.0, g2 = 0.0;
         const double ebar = clip_rev(e, a0, a1, eb, g0, g1);
-        if (ebar != 0.0) {
+        if ((dbits(ebar) & kMag)) {
             g0 += 0.5 * ebar;
             g1 += 0.5 * ebar;
             const double ds1 = -ebar / 6.0, ds0 = ebar / 6.0;
@@ -188,16 +189,18 @@ __device__ inline double rev_trace(bool hi_side, double smi, double s0, double s
                                    double& gsp) {
     double sm = smi, sp = spi;
     int cs = 0;
-    if ((sp - s0) * (s0 - sm) <= 0.0) {
+    // the forward's CW84 decisions (k_ppm_*: cw84), on the integer pipe
+    const double dp = sp - s0, dm = s0 - sm;
+    if (!isame_sign(dp, dm)) {
         cs = 1;
         sp = s0;
         sm = s0;
-    } else if (fabs(sp - s0) >= 2.0 * fabs(sm - s0)) {
+    } else if (!iabs_lt2(dp, 2.0 * dm)) {
         cs = 2;
-        sp = 3.0 * s0 - 2.0 * sm;
-    } else if (fabs(sm - s0) >= 2.0 * fabs(sp - s0)) {
+        sp = s0 + 2.0 * dm;
+    } else if (!iabs_lt2(dm, 2.0 * dp)) {
         cs = 3;
-        sm = 3.0 * s0 - 2.0 * sp;
+        sm = s0 - 2.0 * dp;
     }
     const double Bf = 1.0 - 2.0 / 3.0 * sig;
     const double s6 = 6.0 * s0 - 3.0 * (sm + sp);
@@ -234,17 +237,18 @@ __device__ inline double rev_trace(bool hi_side, double smi, double s0, double s
 }
 
 __device__ inline void rev_upwind(double vel, double ob, double& lb, double& hb) {
-    if (!(fabs(vel) < kSV)) {
-        if (vel >= 0.0) lb += ob; else hb += ob;
+    if (!iabs_lt(vel, kSV)) {
+        if (ige0(vel)) lb += ob; else hb += ob;
     } else {
         lb += 0.5 * ob;
         hb += 0.5 * ob;
     }
 }
 __device__ inline void rev_riemann(double lo, double hi, double ob, double& lb, double& hb) {
-    const bool ltm = (lo <= 0.0 && hi >= 0.0) || (fabs(lo + hi) < kSV);
+    const double sum = lo + hi;
+    const bool ltm = (ile0(lo) && ige0(hi)) || iabs_lt(sum, kSV);
     if (ltm) return;
-    if (lo + hi >= 0.0) lb += ob; else hb += ob;
+    if (ige0(sum)) lb += ob; else hb += ob;
 }
 
 struct A3 {
@@ -297,12 +301,12 @@ __global__ void k_adj_faces(Grid g, int d, const double* u, KI<TI> E, double s, 
     double gul = 0.0, guh = 0.0;
     for (int n = 0; n < 3; ++n) {
         const double tl = lb[n] * scale, th = hb[n] * scale;
-        if (!wl && tl != 0.0) {  // high-side trace of cell c - e_d
+        if (!wl && (dbits(tl) & kMag)) {  // high-side trace of cell c - e_d
             double gsm = 0.0, gs0 = 0.0, gsp = 0.0;
             const double s0 = (TI)Q(g, u, n, i - di, j - dj, k - dk);
-            if (ul > kSV) {
-                const double bsig = rev_trace(true, E.p[n][fm], s0, E.p[n][f], (TI)(fabs(ul) * sT), tl, gsm, gs0, gsp);
-                gul += bsig * s * (ul >= 0.0 ? 1.0 : -1.0);
+            if (dbits(ul) > dbits(kSV)) {
+                const double bsig = rev_trace(true, E.p[n][fm], s0, E.p[n][f], (TI)(iabs(ul) * sT), tl, gsm, gs0, gsp);
+                gul += bsig * s * (ige0(ul) ? 1.0 : -1.0);
             } else {
                 gs0 += tl;
             }
@@ -310,12 +314,12 @@ __global__ void k_adj_faces(Grid g, int d, const double* u, KI<TI> E, double s, 
             aadd(&Eb.p[n][f], gsp);
             Qb(g, ub, n, i - di, j - dj, k - dk, gs0);
         }
-        if (!wh && th != 0.0) {  // low-side trace of cell c
+        if (!wh && (dbits(th) & kMag)) {  // low-side trace of cell c
             double gsm = 0.0, gs0 = 0.0, gsp = 0.0;
             const double s0 = (TI)Q(g, u, n, i, j, k);
-            if (uh < -kSV) {
-                const double bsig = rev_trace(false, E.p[n][f], s0, E.p[n][fp], (TI)(fabs(uh) * sT), th, gsm, gs0, gsp);
-                guh += bsig * s * (uh >= 0.0 ? 1.0 : -1.0);
+            if (okey(uh) < okey(-kSV)) {
+                const double bsig = rev_trace(false, E.p[n][f], s0, E.p[n][fp], (TI)(iabs(uh) * sT), th, gsm, gs0, gsp);
+                guh += bsig * s * (ige0(uh) ? 1.0 : -1.0);
             } else {
                 gs0 += th;
             }
@@ -341,7 +345,7 @@ __global__ void k_adj_pm_trans(Grid g, int a, int b, int n, double cb, const TI*
     if (!face_at(g, a, t, i, j, k)) return;
     const long long f = t;
     const double ob = outb[f];
-    if (ob == 0.0) return;
+    if (!(dbits(ob) & kMag)) return;
     const bool wl = (a == 2 && !g.zper && k == 0), wh = (a == 2 && !g.zper && k == g.nz);
     double lb = 0.0, hb = 0.0;
     rev_upwind(ad_a[f], ob, lb, hb);
@@ -349,7 +353,7 @@ __global__ void k_adj_pm_trans(Grid g, int a, int b, int n, double cb, const TI*
     lo_anb[f] += lb;
     hi_anb[f] += hb;
     const int e0 = (b == 0), e1 = (b == 1), e2 = (b == 2);
-    if (!wh && hb != 0.0) {
+    if (!wh && (dbits(hb) & kMag)) {
         const long long f0 = fidx(g, b, i, j, k), f1 = fidx(g, b, i + e0, j + e1, k + e2);
         const double S = (double)ad_b[f1] + ad_b[f0], Dd = (double)edge_b[f1] - edge_b[f0];
         aadd(&ad_bb[f1], -cb * Dd * hb);
@@ -357,7 +361,7 @@ __global__ void k_adj_pm_trans(Grid g, int a, int b, int n, double cb, const TI*
         aadd(&edge_bb[f1], -cb * S * hb);
         aadd(&edge_bb[f0], cb * S * hb);
     }
-    if (!wl && lb != 0.0) {
+    if (!wl && (dbits(lb) & kMag)) {
         const int ci = i - (a == 0), cj = j - (a == 1), ck = k - (a == 2);
         const long long f0 = fidx(g, b, ci, cj, ck), f1 = fidx(g, b, ci + e0, cj + e1, ck + e2);
         const double S = (double)ad_b[f1] + ad_b[f0], Dd = (double)edge_b[f1] - edge_b[f0];
@@ -388,7 +392,7 @@ __global__ void k_adj_pm_final(Grid g, int d, double dt, double c1, double c2, c
     if (d == 2 && !g.zper && (k == 0 || k == g.nz)) return;  // wall faces: the normal velocity is 0 whatever the input
     const long long f = t;
     const double mb = macb[f];
-    if (mb == 0.0) return;
+    if (!(dbits(mb) & kMag)) return;
     const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
     auto side_val = [&](int ci, int cj, int ck, double base) {
         const long long p1 = fidx(g, b1, ci + (b1 == 0), cj + (b1 == 1), ck + (b1 == 2)), m1 = fidx(g, b1, ci, cj, ck);
@@ -420,11 +424,11 @@ __global__ void k_adj_pm_final(Grid g, int d, double dt, double c1, double c2, c
     const double stl = side_val(li, lj, lk, lo_dd[f]), sth = side_val(i, j, k, hi_dd[f]);
     double bl = 0.0, bh = 0.0;
     rev_riemann(stl, sth, mb, bl, bh);
-    if (bl != 0.0) {
+    if ((dbits(bl) & kMag)) {
         lo_ddb[f] += bl;
         side_rev(li, lj, lk, bl);
     }
-    if (bh != 0.0) {
+    if ((dbits(bh) & kMag)) {
         hi_ddb[f] += bh;
         side_rev(i, j, k, bh);
     }
@@ -456,13 +460,13 @@ __global__ void k_adj_adv_trans(Grid g, int a, int b, const double* u, double rh
     double gvhp = 0.0, gvhm = 0.0, gvlp = 0.0, gvlm = 0.0;
     for (int n = 0; n < 3; ++n) {
         const double ob = Ob.p[n][f];
-        if (ob == 0.0) continue;
+        if (!(dbits(ob) & kMag)) continue;
         double lb = 0.0, hb = 0.0;
         rev_upwind(uaf, ob, lb, hb);
         if (a == 2) zbc_rev(g, k, n, lb, hb);
         LOb.p[n][f] += lb;
         HIb.p[n][f] += hb;
-        if (!wh && hb != 0.0) {
+        if (!wh && (dbits(hb) & kMag)) {
             const double qc = (TI)rho * (TI)Q(g, u, n, i, j, k);
             aadd(&Ebb.p[n][h1], -cb * vhp * hb);
             aadd(&Ebb.p[n][h0], cb * vhm * hb);
@@ -470,7 +474,7 @@ __global__ void k_adj_adv_trans(Grid g, int a, int b, const double* u, double rh
             gvhm += (cb * E.p[n][h0] - cb * qc) * hb;
             Qb(g, ub, n, i, j, k, rho * cb * (vhp - vhm) * hb);
         }
-        if (!wl && lb != 0.0) {
+        if (!wl && (dbits(lb) & kMag)) {
             const double qc = (TI)rho * (TI)Q(g, u, n, ci, cj, ck);
             aadd(&Ebb.p[n][l1], -cb * vlp * lb);
             aadd(&Ebb.p[n][l0], cb * vlm * lb);
@@ -520,7 +524,7 @@ __global__ void k_adj_adv_flux(Grid g, int d, const double* u, const double* for
     const long long ch = wh ? 0 : cell_fo(g, i, j, k);
     for (int n = 0; n < 3; ++n) {
         const double fb = Fb.p[n][f];
-        if (fb == 0.0) continue;
+        if (!(dbits(fb) & kMag)) continue;
         // the forward's face states in its own precision (decide the upwind branch)
         const TI tr = (TI)rho, tc1 = (TI)c1, tc2 = (TI)c2, thd = TI(0.5) * (TI)dt;
         double ql = 0.0, qh = 0.0, stl = 0.0, sth = 0.0;
@@ -549,10 +553,10 @@ __global__ void k_adj_adv_flux(Grid g, int d, const double* u, const double* for
         double zl = stl, zh = sth;
         if (d == 2) zbc_fwd(g, k, n, zl, zh);
         double st, bl = 0.0, bh = 0.0;
-        if (fabs(um) < kSV) {
+        if (iabs_lt(um, kSV)) {
             st = 0.5 * (zl + zh);
             bl = bh = 0.5 * um * fb;
-        } else if (um >= 0.0) {
+        } else if (ige0(um)) {
             st = zl;
             bl = um * fb;
         } else {
@@ -561,7 +565,7 @@ __global__ void k_adj_adv_flux(Grid g, int d, const double* u, const double* for
         }
         gum += st * fb;
         if (d == 2) zbc_rev(g, k, n, bl, bh);
-        if (!wl && bl != 0.0) {
+        if (!wl && (dbits(bl) & kMag)) {
             LOb.p[n][f] += bl;
             aadd(&T1b.p[n][lp1], -c1 * l1p * bl);
             aadd(&T1b.p[n][lm1], c1 * l1m * bl);
@@ -574,7 +578,7 @@ __global__ void k_adj_adv_flux(Grid g, int d, const double* u, const double* for
             aadd(&ub[n * g.N + cl], rho * (c1 * (l1p - l1m) + c2 * (l2p - l2m)) * bl);
             aadd(&forcesb[n * g.N + cl], 0.5 * dt * rho * bl);
         }
-        if (!wh && bh != 0.0) {
+        if (!wh && (dbits(bh) & kMag)) {
             HIb.p[n][f] += bh;
             aadd(&T1b.p[n][hp1], -c1 * h1p * bh);
             aadd(&T1b.p[n][hm1], c1 * h1m * bh);
@@ -633,7 +637,7 @@ __device__ inline double Vd(const Grid& g, const double* v, const double* wg, in
     return c[cidx(g, i, j, k)];
 }
 __device__ inline void Vdb(const Grid& g, double* ub, double* wgb, int n, int i, int j, int k, double v) {
-    if (v == 0.0) return;
+    if (!(dbits(v) & kMag)) return;
     i = wrapn(i, g.nx);
     j = wrapn(j, g.ny);
     double* c = ub + (long long)n * g.N;
@@ -726,7 +730,7 @@ __global__ void __launch_bounds__(ATX* ATY* ATZ) k_adj_tau_tile(Grid g, const do
         bool any = false;
         for (int n = 0; n < 3; ++n) {
             Fb[n] = ((has_lo ? sD[n * ANH + hb(mx, my, mz)] : 0.0) - (has_hi ? sD[n * ANH + hb(hx, hy, hz)] : 0.0)) * ih[d];
-            any = any || Fb[n] != 0.0;
+            any = any || (dbits(Fb[n]) & kMag);
         }
         if (!any) continue;
         double mf;
@@ -774,7 +778,7 @@ __global__ void __launch_bounds__(ATX* ATY* ATZ) k_adj_tau_tile(Grid g, const do
             double* a = aU + n * ANH;
             for (int m = 0; m < 3; ++m) {
                 const double b = grb[m][n];
-                if (b == 0.0) continue;
+                if (!(dbits(b) & kMag)) continue;
                 if (m == d) {
                     atomicAdd(&a[hb(hx, hy, hz)], b * ih[m]);
                     atomicAdd(&a[hb(mx, my, mz)], -b * ih[m]);
@@ -796,7 +800,7 @@ __global__ void __launch_bounds__(ATX* ATY* ATZ) k_adj_tau_tile(Grid g, const do
         const int gi = ((i0 + hx - 1) % g.nx + g.nx) % g.nx, gj = ((j0 + hy - 1) % g.ny + g.ny) % g.ny;
         const int gk = k0 + hz - 1;
         for (int n = 0; n < 3; ++n) Vdb(g, ub, wgb, n, gi, gj, gk, aU[n * ANH + h]);
-        if (mub && aM[h] != 0.0) {
+        if (mub && (dbits(aM[h]) & kMag)) {
             if (g.zper || (gk >= 0 && gk < g.nz)) atomicAdd(&mub[cidx(g, gi, gj, g.zper ? (gk % g.nz + g.nz) % g.nz : gk)], aM[h]);
         }
     }
@@ -807,7 +811,7 @@ __global__ void k_adj_smag(Grid g, const double* vel, const double* mub, double 
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= g.N) return;
     const double mb = mub[t];
-    if (mb == 0.0) return;
+    if (!(dbits(mb) & kMag)) return;
     const int i = (int)(t % g.nx);
     const long long r = t / g.nx;
     const int j = (int)(r % g.ny), k = (int)(r / g.ny);
@@ -880,7 +884,7 @@ __global__ void k_adj_wall_local(Grid g, const double* vel, const double* mueff,
         const double c = ut2 / (vm * vm);
         const double tx = ((u - um0) * vm + ws * um0) * c, ty = ((v - um1) * vm + ws * um1) * c;
         const double bx = wgb[t] * rho / m, by = wgb[M + t] * rho / m;
-        if (bx == 0.0 && by == 0.0) continue;
+        if (!(dbits(bx) & kMag) && !(dbits(by) & kMag)) continue;
         mub[t] += -(bx * tx + by * ty) / m;
         ub[t] += bx * c * (vm + um0 * u * iws) + by * c * um1 * u * iws;
         ub[g.N + t] += by * c * (vm + um1 * v * iws) + bx * c * um0 * v * iws;

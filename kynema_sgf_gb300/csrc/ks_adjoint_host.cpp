@@ -90,7 +90,9 @@ void Sim::adj_alloc() {
     for (int d = 0; d < 3; ++d) {
         G2.ad[d] = gb_.ad[d];
         for (int n = 0; n < 3; ++n) {
-            G2.edge[d][n] = gb_.edge[d][n];  // the unlimited edges are shared by both passes
+            G2.edge[d][n] = gb_.edge[d][n];  // the unlimited edges and limited parabolas are shared by both passes
+            G2.pm[d][n] = gb_.pm[d][n];
+            G2.pp[d][n] = gb_.pp[d][n];
             G2.lo[d][n] = q; q += fsz[d];
             G2.hi[d][n] = q; q += fsz[d];
             G2.tedge[d][n] = q; q += fsz[d];

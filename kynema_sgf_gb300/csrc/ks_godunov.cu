@@ -195,7 +195,9 @@ struct PpmArgs {
 
 template <typename T, int NC>
 struct PpmOut {
-    T* E[3];   // unlimited edges (MODE 0 writes, MODE 1 EDGES = 0 reads)
+    T* E[3];   // unlimited edges (MODE 0 writes them for the adjoint)
+    T* PM[3];  // limited parabola (sm, sp) of every cell (MODE 0 writes, MODE 1 EDGES = 0 reads)
+    T* PP[3];
     T* LO[3];  // left / right states
     T* HI[3];
     T* TE[3];  // upwinded states
@@ -249,6 +251,7 @@ __global__ void __launch_bounds__(256) k_ppm_col(PpmArgs<T> A, T s, T rho, PpmOu
         return d == 1 ? q(n, i, m, o) : q(n, i, o, m);
     };
     auto fid = [&](int m) -> long long { return d == 1 ? fidx(g, 1, i, m, o) : fidx(g, 2, i, o, m); };
+    auto cellid = [&](int m) -> long long { return d == 1 ? cidx(g, i, m, o) : cidx(g, i, o, m); };  // 0 <= m < nl
     // per component at face m: a(m-1), a(m), a(m+1), the slope s(m), the edge
     // e(m), and cell m-1's high-face trace (MODE 0) or limited parabola (MODE 1)
     T am1[NC], a0[NC], ap1[NC], sl0[NC], e0[NC], lo0[NC], pm[NC], pp[NC];
@@ -261,8 +264,16 @@ __global__ void __launch_bounds__(256) k_ppm_col(PpmArgs<T> A, T s, T rho, PpmOu
             am1[n] = val(n, m0 - 1);
             a0[n] = val(n, m0);
             if (MODE == 1 && !EDGES) {
-                em1 = (walls && m0 == 0) ? am1[n] : O.E[n][fid(m0 - 1)];  // no face below a wall
-                e0[n] = O.E[n][fid(m0)];
+                // the stored limited parabola of cell m0 - 1 (none below a wall)
+                if (walls && m0 == 0) {
+                    pm[n] = am1[n];
+                    pp[n] = am1[n];
+                } else {
+                    const long long cm = cellid(((m0 - 1) % nl + nl) % nl);
+                    pm[n] = O.PM[n][cm];
+                    pp[n] = O.PP[n][cm];
+                }
+                continue;
             } else {
                 const T x3 = val(n, m0 - 3), x2 = val(n, m0 - 2);
                 ap1[n] = val(n, m0 + 1);
@@ -285,7 +296,6 @@ __global__ void __launch_bounds__(256) k_ppm_col(PpmArgs<T> A, T s, T rho, PpmOu
 #pragma unroll
         for (int n = 0; n < NC; ++n) {
             if (MODE == 1 && !EDGES) {
-                e1[n] = O.E[n][fid(m + 1)];
                 ap1[n] = val(n, m + 1);
             } else {
                 ap2[n] = val(n, m + 2);
@@ -302,6 +312,10 @@ __global__ void __launch_bounds__(256) k_ppm_col(PpmArgs<T> A, T s, T rho, PpmOu
             for (int n = 0; n < NC; ++n) {
                 T sm = e0[n], sp = e1[n];
                 cw84(a0[n], sm, sp);
+                if (m < nl) {  // the post-MAC pass reads the limited parabola of every cell
+                    O.PM[n][cellid(m)] = sm;
+                    O.PP[n][cellid(m)] = sp;
+                }
                 T h = a0[n], lnext = a0[n];
                 if (up || dn) {
                     const T t = ppm_trace(up, sm, a0[n], sp, c);
@@ -316,8 +330,20 @@ __global__ void __launch_bounds__(256) k_ppm_col(PpmArgs<T> A, T s, T rho, PpmOu
             const T u = (T)A.umac[f];
 #pragma unroll
             for (int n = 0; n < NC; ++n) {
-                T sm = e0[n], sp = e1[n];
-                cw84(a0[n], sm, sp);
+                T sm, sp;
+                if (MODE == 1 && !EDGES) {
+                    if (m < nl) {
+                        sm = O.PM[n][cellid(m)];
+                        sp = O.PP[n][cellid(m)];
+                    } else {  // the ghost cell above a wall: its state is replaced below
+                        sm = a0[n];
+                        sp = a0[n];
+                    }
+                } else {
+                    sm = e0[n];
+                    sp = e1[n];
+                    cw84(a0[n], sm, sp);
+                }
                 T l, h;
                 face_states_mac(u, s, pm[n], am1[n], pp[n], sm, a0[n], sp, l, h);
                 lo[n] = rho * l;
@@ -353,10 +379,10 @@ __global__ void __launch_bounds__(256) k_ppm_col(PpmArgs<T> A, T s, T rho, PpmOu
         }
 #pragma unroll
         for (int n = 0; n < NC; ++n) {
-            e0[n] = e1[n];
             am1[n] = a0[n];
             a0[n] = ap1[n];
             if (!(MODE == 1 && !EDGES)) {
+                e0[n] = e1[n];
                 ap1[n] = ap2[n];
                 sl0[n] = s1[n];
             }
@@ -396,24 +422,29 @@ __global__ void __launch_bounds__(256) k_ppm_x(PpmArgs<T> A, T s, T rho, PpmOut<
     const bool up = above_small(u), dn = below_msmall(u);
     const TraceCoef<T> tc(absv(u) * s);
 #pragma unroll
+    T pmv[NC], ppv[NC];
     for (int n = 0; n < NC; ++n) {
         const T a0 = ld(n, c);
-        T e0, e1, am1;
-        if (LOADE) {
-            e0 = O.E[n][fc];
-            e1 = O.E[n][rb + wx(c + 1)];
+        T am1, sm, sp;
+        if (LOADE) {  // the limited parabola of the lane's cell, stored by the pre-MAC pass
+            sm = O.PM[n][fc];
+            sp = O.PP[n][fc];
             am1 = __shfl_up_sync(FULL, a0, 1);
+            ev[n] = T(0);
         } else {
             am1 = ld(n, c - 1);
             const T ap1 = ld(n, c + 1);
             const T sl = vls(am1, a0, ap1);
             const T slm = __shfl_up_sync(FULL, sl, 1);
-            e0 = ppm_edge(am1, a0, slm, sl);
-            e1 = __shfl_down_sync(FULL, e0, 1);
+            const T e0 = ppm_edge(am1, a0, slm, sl);
+            const T e1 = __shfl_down_sync(FULL, e0, 1);
+            ev[n] = e0;
+            sm = e0;
+            sp = e1;
+            cw84(a0, sm, sp);
         }
-        ev[n] = e0;
-        T sm = e0, sp = e1;
-        cw84(a0, sm, sp);
+        pmv[n] = sm;
+        ppv[n] = sp;
         if (MODE == 0) {
             T h = a0, lnext = a0;
             if (up || dn) {
@@ -436,7 +467,11 @@ __global__ void __launch_bounds__(256) k_ppm_x(PpmArgs<T> A, T s, T rho, PpmOut<
     for (int n = 0; n < NC; ++n) {
         O.LO[n][fc] = lo[n];
         O.HI[n][fc] = hi[n];
-        if (MODE == 0) O.E[n][fc] = ev[n];
+        if (MODE == 0) {  // x faces and cells share the index: face c is owned with cell c
+            O.E[n][fc] = ev[n];
+            O.PM[n][fc] = pmv[n];
+            O.PP[n][fc] = ppv[n];
+        }
     }
     if (MODE == 0) {
         const T a = riemann(lo[0], hi[0]);
@@ -657,6 +692,8 @@ static void premac_t(Ctx& c, const Grid& g, const T* vel, const T* forces, doubl
         PpmOut<T, 3> O{};
         for (int n = 0; n < 3; ++n) {
             O.E[n] = tp<T>(B.edge[d][n]);
+            O.PM[n] = tp<T>(B.pm[d][n]);
+            O.PP[n] = tp<T>(B.pp[d][n]);
             O.LO[n] = tp<T>(B.lo[d][n]);
             O.HI[n] = tp<T>(B.hi[d][n]);
             O.TE[n] = tp<T>(B.tedge[d][n]);
@@ -687,11 +724,13 @@ template <typename T>
 static void advection_t(Ctx& c, const Grid& g, const T* vel, const T* forces, const T* const mac[3], double dt, double rho,
                         GodunovBufs& B, double* conv) {
     const double BT = (double)sizeof(T), B8 = 8.0;
-    // the unlimited edge values of the pre-MAC pass are reused (same field)
+    // the limited parabolas of the pre-MAC pass are reused (same field)
     for (int a = 0; a < 3; ++a) {
         PpmOut<T, 3> O{};
         for (int n = 0; n < 3; ++n) {
             O.E[n] = tp<T>(B.edge[a][n]);
+            O.PM[n] = tp<T>(B.pm[a][n]);
+            O.PP[n] = tp<T>(B.pp[a][n]);
             O.LO[n] = tp<T>(B.lo[a][n]);
             O.HI[n] = tp<T>(B.hi[a][n]);
             O.TE[n] = tp<T>(B.tedge[a][n]);

@@ -453,7 +453,7 @@ void Sim::alloc() {
     size_t total = 0;
     for (int d = 0; d < 3; ++d) total += fsz[d] * (godunov_ ? 16 : 3);
     if (godunov_)
-        for (int a = 0; a < 3; ++a) total += 2 * 3 * fsz[a];
+        for (int a = 0; a < 3; ++a) total += 2 * 3 * fsz[a] + 2 * 3 * N;
     gbuf_.alloc(total);
     double* q = gbuf_.p;
     if (!godunov_) {
@@ -473,6 +473,11 @@ void Sim::alloc() {
         for (int b = 0; b < 3; ++b) {
             if (a == b) continue;
             for (int n = 0; n < 3; ++n) { gb_.tr[a][b][n] = q; q += fsz[a]; }
+        }
+    for (int d = 0; d < 3 && godunov_; ++d)
+        for (int n = 0; n < 3; ++n) {
+            gb_.pm[d][n] = q; q += N;
+            gb_.pp[d][n] = q; q += N;
         }
     // multigrid hierarchies
     std::vector<std::array<int, 3>> dims;

@@ -183,6 +183,8 @@ void launch_act_spread(Ctx& c, const Grid& g, double* act, const double* pts, in
 struct GodunovBufs {
     void* ad[3];        // pre-MAC advective velocities on d-faces
     void* edge[3][3];   // unlimited PPM edge values edge[d][n] on d-faces
+    void* pm[3][3];     // limited PPM parabola (sm, sp) of every cell along d, component n (pre-MAC pass)
+    void* pp[3][3];
     void* lo[3][3];     // left states lo[d][n]
     void* hi[3][3];     // right states hi[d][n]
     void* tedge[3][3];  // upwinded states tedge[d][n]
