@@ -27,6 +27,8 @@ import sys
 import tempfile
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -34,13 +36,16 @@ METRIC = "Mcell-steps/s at 256^3 (FP64 vs mixed-precision at stated error) + adj
 UNIT = "Mcell-steps/s"
 WORKLOAD = "ABL LES 256x256x128 FP64 (5120x5120x1280 m, Smagorinsky, geostrophic+Coriolis, wall model, CFL 0.9)"
 CPU_SAMPLE = (128, 128, 64)  # same dx, physics and deck as the workload, 1/8 of the cells
-# FP64 flops per algorithmic byte of the kernels that can dominate the FP64 step
-# FP64 flops (an FMA counts 2) per algorithmic byte of the kernels that can
-# dominate the step: the column nodal sweeps (22 flops per node, 3 FP64 arrays),
-# the red-black Gauss-Seidel half-sweep (14 flops per updated cell, 2 arrays)
-# FP64 flops per algorithmic byte (an FMA counts 2): nodal column sweep 20 flops per node (5 plane
-# sums, 3 pair sums, 5 FMAs from the right-hand side, 1 FMA update) over 24 bytes; residual form 18;
-# red-black update 10 flops over 16 bytes
+DATA = "synthetic (log-law + seeded uniform noise, SplitMix64 seed 42)"
+
+
+def workload_config(size, world=1):
+    """The `config` object both arms print (the workload, not a measurement)."""
+    return {"workload": WORKLOAD, "cells": list(size), "parallelism": "replicas" if world > 1 else "single GPU",
+            "l2": "state larger than L2 (no flush)"}
+# FP64 flops per algorithmic byte (an FMA counts 2) of the kernels that can dominate the FP64 step:
+# nodal column sweep 20 flops per node (5 plane sums, 3 pair sums, 5 FMAs from the right-hand side,
+# 1 FMA update) over 24 bytes; residual form 18; red-black update 10 flops over 16 bytes
 FP64_FLOPS_PER_BYTE = {"(k_nd_col<T,0>)": 20.0 / 24.0, "(k_nd_col<double,1>)": 20.0 / 24.0, "(k_nd_col<T,2>)": 18.0 / 24.0,
                        "k_cc_gsrb<T>": 10.0 / 16.0}
 
@@ -54,6 +59,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision form of the same workload")
+    p.add_argument("--c2-steps", type=int, default=100, help="steps of the FP64 / mixed-precision comparison")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost / gradient check (128x128x64, 3 disks)")
     p.add_argument("--no-mol", action="store_true", help="skip the MOL and Crank-Nicolson forms of the ABL workload")
     p.add_argument("--c4", action="store_true",
@@ -86,49 +92,89 @@ def replica_throughput(cells, steps, world, seconds):
 
 # ---------------------------------------------------------------- CPU side
 def cpu_worker(spec):
-    """Runs in a child process: times the oracle on the bounded CPU sample
-    (the ABL sample, or the whole 64^3 Taylor-Green case when spec ends in ',tgv')."""
+    """Runs in a child process: times the oracle.  spec = "warm,steps,repeats,nx,ny,nz[,case]":
+    `repeats` fresh runs of the ABL deck on nx x ny x nz cells (or the 64^3
+    Taylor-Green case, or the MOL form of the ABL deck), each timing `steps`
+    Evolve steps after `warm` untimed ones, initialisation skipped."""
     parts = spec.split(",")
-    warm, steps = int(parts[0]), int(parts[1])
+    warm, steps, repeats = int(parts[0]), int(parts[1]), int(parts[2])
+    nx, ny, nz = int(parts[3]), int(parts[4]), int(parts[5])
+    case = parts[6] if len(parts) > 6 else ""
     from kynema_sgf_gb300 import decks
     from oracle.oracle import Oracle
-    nx, ny, nz = CPU_SAMPLE
-    deck = decks.abl(nx, ny, nz, steps=10 ** 6) + "\nincflo.do_initial_proj = 0\nincflo.initial_iterations = 0\n"
-    if len(parts) > 2 and parts[2] == "tgv":
+    skip_init = "\nincflo.do_initial_proj = 0\nincflo.initial_iterations = 0\n"
+    deck = decks.abl(nx, ny, nz, steps=10 ** 6) + skip_init
+    if case == "tgv":
         nx = ny = nz = 64
         deck = decks.tgv(64, steps=10 ** 6)
-    if len(parts) > 2 and parts[2] == "mol":
-        deck = decks.mol(decks.abl(nx, ny, nz, steps=10 ** 6, cfl=0.45)) + "\nincflo.do_initial_proj = 0\nincflo.initial_iterations = 0\n"
-    o = Oracle(deck)
-    for _ in range(warm):
-        o.step()
-    per = []
-    for _ in range(steps):
-        t0 = time.perf_counter()
-        o.step()
-        per.append(time.perf_counter() - t0)
-    print(json.dumps({"per_step_s": per, "cells": nx * ny * nz}))
+    if case == "mol":
+        deck = decks.mol(decks.abl(nx, ny, nz, steps=10 ** 6, cfl=0.45)) + skip_init
+    runs = []
+    for _ in range(repeats):
+        o = Oracle(deck)
+        for _ in range(warm):
+            o.step()
+        per = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            o.step()
+            per.append(time.perf_counter() - t0)
+        runs.append(per)
+        del o
+    print(json.dumps({"runs": runs, "cells": nx * ny * nz}))
 
 
-def run_cpu(warm, steps, case=""):
+def cpu_model():
+    """Host CPU model name and logical core count (lscpu, else /proc/cpuinfo)."""
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                name = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if not name:
+        try:
+            for line in open("/proc/cpuinfo"):
+                if line.lower().startswith(("model name", "cpu part")):
+                    name = line.split(":", 1)[1].strip()
+                    break
+        except Exception:
+            pass
+    import platform
+    return {"model": name, "logical_cores": os.cpu_count(), "machine": platform.machine()}
+
+
+def run_cpu(warm, steps, repeats=1, size=CPU_SAMPLE, case=""):
+    """Time the oracle on all host cores in a child process; returns (cells,
+    per-run Mcell-steps/s list, per-run step times, cores)."""
     from oracle import oracle as orc
     orc.build()
     cores = os.cpu_count() or 1
     env = dict(os.environ, OMP_NUM_THREADS=str(cores), OMP_PROC_BIND="spread", OMP_PLACES="cores")
-    spec = "%d,%d" % (warm, steps) + ("," + case if case else "")
+    spec = "%d,%d,%d,%d,%d,%d" % ((warm, steps, repeats) + tuple(size)) + ("," + case if case else "")
     r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-worker", spec],
                        capture_output=True, text=True, env=env, cwd=ROOT)
     if r.returncode != 0:
         raise RuntimeError("CPU baseline failed: " + r.stderr[-2000:])
     out = json.loads(r.stdout.strip().splitlines()[-1])
-    per = out["per_step_s"]
-    return out["cells"], per, cores
+    cells = out["cells"]
+    rates = [cells * len(per) / sum(per) / 1e6 for per in out["runs"]]
+    return cells, rates, out["runs"], cores
 
 
-def cpu_sample_text(steps):
-    nx, ny, nz = CPU_SAMPLE
-    return ("CPU restatement (oracle/ks_oracle.cpp, g++ -O3 -fopenmp) on %dx%dx%d cells of the same ABL deck "
-            "(same dx and physics, 1/8 of the cells), %d timed Evolve step(s) after 1 warm-up, init skipped" % (nx, ny, nz, steps))
+def cpu_baseline_entry(warm, steps, repeats, size=CPU_SAMPLE, case="", what=None):
+    """The median over `repeats` fresh runs of the oracle's rate."""
+    cells, rates, runs, cores = run_cpu(warm, steps, repeats, size, case)
+    nx, ny, nz = size if case != "tgv" else (64, 64, 64)
+    what = what or ("CPU restatement (oracle/ks_oracle.cpp, g++ -O3 -fopenmp) on %dx%dx%d cells of the same ABL deck (same dx and "
+                    "physics%s)" % (nx, ny, nz, ", 1/8 of the cells" if (nx, ny, nz) == CPU_SAMPLE else ""))
+    return {"value": statistics.median(rates), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%s; median of %d fresh runs, each %d timed Evolve steps after %d untimed, initialisation skipped"
+                      % (what, repeats, steps, warm),
+            "runs": [round(x, 4) for x in rates], "cpu": cpu_model()}
 
 
 # ---------------------------------------------------------------- clocks
@@ -241,12 +287,12 @@ def our_arm(args, rank, world, local_rank):
     if dist:
         tdist.barrier()
     launches = sim.kernel_launches() - l0
+    div = divergence(sim)
     ms_max = max_over_ranks(ev0.elapsed_time(ev1), world)
     dom = sim.profile_report().get(dominant, (0, 0.0, 0.0))
     fp64_peak = ks.fma_peak(True)
     sim.profile_kernels("")
     value = replica_throughput(cells, args.steps, world, ms_max * 1e-3)
-    ref_state = {f: sim.get_field(f) for f in ("velocity", "gp")} if not args.no_mixed else None
 
     # end to end through the public API: host inputs in, host result out
     e2e = None
@@ -272,43 +318,7 @@ def our_arm(args, rank, world, local_rank):
     mixed = None
     if not args.no_mixed:
         del sim
-        mx = ks.Incflo(decks.abl(nx, ny, nz, steps=10 ** 9) + "\nks.precision = mixed\n")
-        mx.InitData()
-        for w in range(args.warmup):
-            if args.profile_all and w == args.warmup - 1:
-                mx.profile_kernels("*")
-            mx.step()
-        if args.profile_all and rank == 0:
-            rep = mx.profile_report()
-            mx.profile_kernels("")
-            tot = sum(v[1] for v in rep.values())
-            sys.stderr.write("-- mixed precision step --\n")
-            for k, v in sorted(rep.items(), key=lambda kv: -kv[1][1]):
-                sys.stderr.write("%-22s %6d launches %9.3f ms %5.1f%% %8.1f GB/s\n" % (k, v[0], v[1], 100 * v[1] / tot,
-                                                                                      v[2] / (v[1] * 1e-3) / 1e9 if v[1] else 0))
-        stream = torch.cuda.ExternalStream(mx.stream())
-        if dist:
-            tdist.barrier()
-        torch.cuda.synchronize()
-        ev0.record(stream)
-        mres, nres = [], []
-        for _ in range(args.steps):
-            mx.step()
-            mres.append(mx.scalar("mac_res") / max(mx.scalar("mac_res0"), 1e-300))
-            nres.append(mx.scalar("nodal_res") / max(mx.scalar("nodal_res0"), 1e-300))
-        ev1.record(stream)
-        torch.cuda.synchronize()
-        mms = max_over_ranks(ev0.elapsed_time(ev1), world)
-        v = mx.get_field("velocity")
-        gpm = mx.get_field("gp")
-        rv, rg = ref_state["velocity"], ref_state["gp"]
-        mixed = {"value": replica_throughput(cells, args.steps, world, mms * 1e-3), "ms_per_step": mms / args.steps,
-                 "speedup_vs_fp64": ms_max / mms, "steps_compared": args.warmup + args.steps,
-                 "velocity_rel_err_linf": float(abs(v - rv).max() / abs(rv).max()),
-                 "velocity_rel_err_l2": float(((v - rv) ** 2).sum() ** 0.5 / (rv ** 2).sum() ** 0.5),
-                 "gp_rel_err_linf": float(abs(gpm - rg).max() / abs(rg).max()),
-                 "mac_residual_rel_max": max(mres), "nodal_residual_rel_max": max(nres),
-                 "note": "FP32 advection and multigrid cycles, FP64 residuals / defect correction / RHS / velocity update"}
+        mixed = c2_bench(args, torch, ks, decks, nx, ny, nz, world, rank, ms_max / args.steps)
     mol = None if args.no_mol else mol_bench(args, torch, ks, decks, nx, ny, nz, world, rank)
     cn = None if args.no_mol else cn_bench(args, torch, ks, decks, nx, ny, nz, world, rank)
     strat = None if args.no_mol else stratified_bench(args, torch, ks, decks, nx, ny, nz, world, rank)
@@ -329,8 +339,123 @@ def our_arm(args, rank, world, local_rank):
     tgv = {"workload": "Taylor-Green vortex 64^3, Re 1600, CFL 0.5, FP64, 20 timed steps", "value": 64 ** 3 / (tms * 1e-3) / 1e6,
            "unit": UNIT, "ms_per_step": tms}
     del tg
-    return dict(value=value, ms=ms_max, cells=cells, launches=launches, dominant=dominant, dom=dom, clocks=clk, e2e=e2e, fp64_peak=fp64_peak,
+    return dict(value=value, ms=ms_max, cells=cells, launches=launches, dominant=dominant, dom=dom, clocks=clk, e2e=e2e, fp64_peak=fp64_peak, div=div,
                 mac=statistics.mean(mac_it), nodal=statistics.mean(nod_it), size=(nx, ny, nz), mixed=mixed, adjoint=adj, tgv=tgv, mol=mol, cn=cn, strat=strat)
+
+
+def divergence(sim):
+    """Post-projection divergence of the current state.  The MAC projection is
+    exact: max|div u_mac| is its FP64 residual.  The nodal projection is an
+    approximate projection: the nodal divergence of the cell velocity is
+    truncation-sized, and the solve's own divergence is its final residual.
+    Relative forms scale by max|u| / min(dx, dy, dz)."""
+    return {"mac_divu_rel": sim.scalar("mac_divu_rel"), "mac_divu": sim.scalar("mac_divu"),
+            "nodal_residual_rel": sim.scalar("nodal_res") / max(sim.scalar("nodal_res0"), 1e-300),
+            "mac_residual_rel": sim.scalar("mac_res") / max(sim.scalar("mac_res0"), 1e-300),
+            "cell_nodal_divu_rel": sim.scalar("divu_rel"), "cell_nodal_divu": sim.scalar("divu")}
+
+
+def kernel_table(rep, top=12):
+    tot = sum(v[1] for v in rep.values())
+    rows = sorted(rep.items(), key=lambda kv: -kv[1][1])[:top]
+    return [[k, v[0], round(v[1], 3), round(v[1] / tot, 4), round(v[2] / (v[1] * 1e-3) / 1e9, 1) if v[1] else None] for k, v in rows]
+
+
+def c2_bench(args, torch, ks, decks, nx, ny, nz, world, rank, fp64_ms_main):
+    """The mixed-precision form of the ABL workload against its FP64 form: both
+    advance the same deck from the same initial state for --c2-steps steps.
+    The FP64 fields after those steps are the reference for the mixed form's
+    errors (velocity, pressure, pressure gradient; relative L2 and max-norm);
+    both forms' post-projection divergence is taken after every step.  Time:
+    CUDA events around each step (the divergence reads between steps are not
+    timed); throughput over the last --steps steps (dt at the CFL limit) and
+    over all steps.  The mixed form's dominant kernel is timed over the last
+    --steps steps for its roofline."""
+    nsteps = max(args.c2_steps, args.steps + 1)
+    peak, peak_kind = peaks()
+    res = {}
+    for form in ("fp64", "mixed"):
+        deck = decks.abl(nx, ny, nz, steps=10 ** 9) + ("\nks.precision = mixed\n" if form == "mixed" else "")
+        sim = ks.Incflo(deck)
+        sim.InitData()
+        cells = sim.scalar("ncells")
+        stream = torch.cuda.ExternalStream(sim.stream())
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nsteps)]
+        worst = {"mac_divu_rel": 0.0, "nodal_residual_rel": 0.0, "cell_nodal_divu_rel": 0.0}
+        dominant, rep = None, None
+        torch.cuda.synchronize()
+        for m in range(nsteps):
+            # the mixed form's step before the timed window times every kernel (the divergence
+            # reads after it are not part of the step); the window times the dominant one
+            profiled = form == "mixed" and m == nsteps - args.steps - 1
+            if profiled:
+                sim.profile_kernels("*")
+            ev[m][0].record(stream)
+            sim.step()
+            ev[m][1].record(stream)
+            if profiled:
+                rep = sim.profile_report()
+                dominant = max((k for k in rep if not k.startswith("(mg_")), key=lambda k: rep[k][1])
+                sim.profile_kernels("")
+            d = divergence(sim)
+            if profiled:
+                sim.profile_kernels(dominant)
+            for k in worst:
+                worst[k] = max(worst[k], d[k])
+        torch.cuda.synchronize()
+        ms = [a.elapsed_time(b) for a, b in ev]
+        out = {"ms_all": sum(ms), "ms_last": sum(ms[-args.steps:]), "divergence_max_over_steps": worst, "divergence_final": divergence(sim),
+               "fields": {f: sim.get_field(f) for f in ("velocity", "p", "gp")}, "cells": cells}
+        if form == "mixed":
+            dom = sim.profile_report().get(dominant, (0, 0.0, 0.0))
+            sim.profile_kernels("")
+            n_l, ms_l, by_l = dom
+            achieved = (by_l / n_l) / ((ms_l / n_l) * 1e-3) / 1e9 if n_l else None
+            step_bytes = sum(v[2] for v in rep.values())
+            step_ms = sum(v[1] for v in rep.values())
+            out["roofline"] = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                               "frac": achieved / peak if achieved else None, "peak_kind": peak_kind, "launches": n_l,
+                               "avg_launch_us": 1e3 * ms_l / n_l if n_l else None,
+                               "algorithmic_bytes_per_launch": by_l / n_l if n_l else None,
+                               "traffic": ncu_traffic("mixed:" + dominant, by_l / n_l if n_l else None)}
+            out["step_roofline"] = {"algorithmic_bytes_per_step": step_bytes,
+                                    "achieved_GBs": step_bytes / (out["ms_last"] / args.steps * 1e-3) / 1e9,
+                                    "frac": step_bytes / (out["ms_last"] / args.steps * 1e-3) / 1e9 / peak,
+                                    "note": "bytes: every kernel launcher's algorithmic bytes over one profiled step, at the "
+                                            "precision each pass runs in; time: the timed steps' average"}
+            out["kernels"] = {"note": "one profiled step: kernel, launches, ms, share, algorithmic GB/s", "top": kernel_table(rep)}
+        res[form] = out
+        del sim
+    r64, rmx = res["fp64"]["fields"], res["mixed"]["fields"]
+
+    def errs(name):
+        a, b = rmx[name], r64[name]
+        if name == "p":
+            a, b = a - a.mean(), b - b.mean()
+        d = np.abs(a - b)
+        return {"rel_l2": float(np.sqrt((d ** 2).sum() / (b ** 2).sum())), "rel_linf": float(d.max() / np.abs(b).max())}
+
+    dv = np.abs(rmx["velocity"] - r64["velocity"]).ravel() / np.abs(r64["velocity"]).max()
+    q = np.quantile(dv, [0.5, 0.99, 0.999, 0.9999])
+    cells = res["fp64"]["cells"]
+    mx = res["mixed"]
+    return {"value": replica_throughput(cells, args.steps, world, mx["ms_last"] * 1e-3), "unit": UNIT,
+            "ms_per_step": mx["ms_last"] / args.steps,
+            "speedup_vs_fp64": res["fp64"]["ms_last"] / mx["ms_last"],
+            "speedup_vs_fp64_all_steps": res["fp64"]["ms_all"] / mx["ms_all"],
+            "speedup_vs_fp64_main_run": fp64_ms_main / (mx["ms_last"] / args.steps),
+            "steps_compared": nsteps, "timed_window": "last %d of %d steps" % (args.steps, nsteps),
+            "errors_vs_fp64": {"velocity": errs("velocity"), "p": errs("p"), "gp": errs("gp"),
+                               "velocity_pointwise_rel_quantiles": {"p50": float(q[0]), "p99": float(q[1]), "p99.9": float(q[2]),
+                                                                    "p99.99": float(q[3]), "max": float(dv.max())},
+                               "velocity_points_above_1e-6": int((dv > 1e-6).sum()), "velocity_points": int(dv.size)},
+            "divergence": {"fp64": res["fp64"]["divergence_max_over_steps"], "mixed": mx["divergence_max_over_steps"],
+                           "note": "largest value over all steps; mac_divu_rel = max|div u_mac| min(dx) / max|u_mac| after the "
+                                   "(exact) MAC projection; nodal_residual_rel = the nodal solve's final / initial residual; "
+                                   "cell_nodal_divu_rel = the nodal divergence of the cell velocity after the (approximate) "
+                                   "nodal projection, truncation-sized in both forms"},
+            "roofline": mx["roofline"], "step_roofline": mx["step_roofline"], "kernels": mx["kernels"],
+            "note": "FP32 advection and multigrid cycles, FP64 residuals / defect correction / RHS / velocity update"}
 
 
 def variant_bench(args, torch, ks, deck, workload, world, rank, label):
@@ -366,7 +491,8 @@ def variant_bench(args, torch, ks, deck, workload, world, rank, label):
     ms = max_over_ranks(ev0.elapsed_time(ev1), world)
     out = {"workload": workload, "value": replica_throughput(cells, args.steps, world, ms * 1e-3), "unit": UNIT,
            "ms_per_step": ms / args.steps, "dt": sim.scalar("dt"), "mac_vcycles_per_step": statistics.mean(mac_it),
-           "nodal_vcycles_per_step": statistics.mean(nod_it), "diffusion_vcycles_per_solve": statistics.mean(dif_it)}
+           "nodal_vcycles_per_step": statistics.mean(nod_it), "diffusion_vcycles_per_solve": statistics.mean(dif_it),
+           "divergence": divergence(sim)}
     del sim
     return out
 
@@ -619,13 +745,18 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        cells, per, cores = run_cpu(args.warmup, args.steps)
-        v = cells * len(per) / sum(per) / 1e6
+        # the full workload (not a sample): every Evolve step of the 256x256x128 deck on all host cores
+        size = tuple(int(x) for x in args.size.split(","))
+        cells, rates, runs, cores = run_cpu(args.warmup, args.steps, 1, size)
+        per = runs[0]
+        v = rates[0]
+        what = ("CPU restatement (oracle/ks_oracle.cpp, g++ -O3 -fopenmp; the reference's own build cannot be compiled: its "
+                "AMReX / AMReX-Hydro submodules are absent) on the full %dx%dx%d workload, %d timed Evolve steps after %d untimed, "
+                "initialisation skipped" % (size + (len(per), args.warmup)))
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * sum(per) / len(per), "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": WORKLOAD, "sample": "%dx%dx%d" % CPU_SAMPLE},
-                "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": cpu_sample_text(len(per))},
+                "vs_baseline": None, "dtype": "f64", "data": DATA, "config": workload_config(size, world),
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": what, "cpu": cpu_model()},
                 "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -648,10 +779,9 @@ def main():
     nx, ny, nz = r["size"]
     line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (log-law + seeded uniform noise, SplitMix64 seed 42)",
-            "config": {"workload": WORKLOAD, "cells": [nx, ny, nz], "parallelism": "replicas" if world > 1 else "single GPU",
-                       "l2": "state larger than L2 (no flush)", "mac_vcycles_per_step": r["mac"],
-                       "nodal_vcycles_per_step": r["nodal"]},
+            "data": DATA, "config": workload_config((nx, ny, nz), world),
+            "solver": {"mac_vcycles_per_step": r["mac"], "nodal_vcycles_per_step": r["nodal"]},
+            "divergence": r["div"],
             "roofline": {"bound": "hbm", "kernel": r["dominant"], "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic, "peak_kind": peak_kind,
                          "launches": n_l, "avg_launch_us": 1e3 * ms_l / n_l if n_l else None,
@@ -659,8 +789,8 @@ def main():
             "gpu_launches": r["launches"], "clocks": r["clocks"], "e2e": r["e2e"], "mixed_precision": r["mixed"],
             "adjoint": r["adjoint"], "tgv64": r["tgv"], "mol": r["mol"], "crank_nicolson": r["cn"],
             "stratified_abl": r["strat"]}
-    # The FP64 path is bound by FP64 issue on this GPU (profiles/k_nd_col_abl128_fp64.md): report the
-    # dominant kernel against the FMA peak measured live by ks_fma_peak as well.
+    # The FP64 path is bound by FP64 issue on this GPU (the nodal sweep's FP64 pipe is 81-83 % busy
+    # under ncu): report the dominant kernel against the FMA peak measured live by ks_fma_peak as well.
     fl = FP64_FLOPS_PER_BYTE.get(r["dominant"])
     if fl and achieved:
         line["fp64_roofline"] = {"kernel": r["dominant"], "achieved_gflops": achieved * fl, "peak_gflops": r["fp64_peak"],
@@ -672,22 +802,17 @@ def main():
                              "frac": bstep / (r["ms"] / args.steps * 1e-3) / 1e9 / peak}
     if world == 1 and not args.no_cpu_baseline:
         try:
-            cells, per, cores = run_cpu(1, 2)
-            line["cpu_baseline"] = {"value": cells * len(per) / sum(per) / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
-                                    "sample": cpu_sample_text(len(per))}
+            line["cpu_baseline"] = cpu_baseline_entry(1, 5, 5)
         except Exception as e:  # reported, never silently replaced
             line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": "failed: %s" % e}
         try:
-            cells, per, cores = run_cpu(1, 3, "tgv")
-            r["tgv"]["cpu"] = {"value": cells * len(per) / sum(per) / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
-                               "sample": "CPU restatement, the same 64^3 deck, %d timed steps after 1" % len(per)}
+            r["tgv"]["cpu"] = cpu_baseline_entry(1, 5, 3, case="tgv", what="CPU restatement, the same 64^3 Taylor-Green deck")
         except Exception as e:
             r["tgv"]["cpu"] = {"value": None, "sample": "failed: %s" % e}
         if r["mol"]:
             try:
-                cells, per, cores = run_cpu(1, 2, "mol")
-                r["mol"]["cpu"] = {"value": cells * len(per) / sum(per) / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
-                                   "sample": "CPU restatement, MOL form of the %dx%dx%d ABL sample, %d timed steps after 1" % (CPU_SAMPLE + (len(per),))}
+                r["mol"]["cpu"] = cpu_baseline_entry(1, 3, 3, case="mol", what="CPU restatement, MOL form of the %dx%dx%d ABL sample"
+                                                     % CPU_SAMPLE)
             except Exception as e:
                 r["mol"]["cpu"] = {"value": None, "sample": "failed: %s" % e}
     print(json.dumps(line))

@@ -179,10 +179,9 @@ int ks_fma_peak(int fp64, double* gflops);
 /* Allocation-free tensor diffusion term (no counterpart in the reference).
  *
  * For callers that cannot call cudaMalloc where they need the viscous term:
- * code running inside a CUDA stream capture in global or thread-local mode
- * (where cudaMalloc is illegal), hosts whose device memory is reserved up
- * front by another allocator, latency-critical loops that must not trigger an
- * allocation.  Computes divtau = div(mu (grad u + grad u^T) - 2/3 mu div(u) I)
+ * hosts whose device memory is reserved up front by another allocator,
+ * plug-in code inside an application that owns every device allocation,
+ * latency-critical loops that must not trigger an allocation.  Computes divtau = div(mu (grad u + grad u^T) - 2/3 mu div(u) I)
  * for a caller-owned device velocity (3 components, SoA, x fastest), cell
  * viscosity mueff and output divtau (3 components), on stream `stream` (NULL =
  * legacy default stream), with the boundary treatment of the advance: x and y
@@ -193,7 +192,10 @@ int ks_fma_peak(int fp64, double* gflops);
  * library until exit); larger grids are rejected with KS_ERR_ARG.  The first
  * call on a device looks up that array's address with that device current;
  * make that first call before any stream capture.  All calls share the
- * array: calls whose kernels overlap on the GPU race, order them. */
+ * array: calls whose kernels overlap on the GPU race, order them.  A CUDA
+ * error already pending on the calling thread is left in place and the call
+ * returns KS_ERR_CUDA without launching; calls after cudaDeviceReset are not
+ * supported. */
 #define KS_NOALLOC_MAX_CELLS 262144
 int ks_divtau_noalloc(const double* vel, const double* mueff, const double* wall_grad, double* divtau, int nx, int ny, int nz,
                       double dx, double dy, double dz, int z_periodic, int zlo_wall_model, void* stream);

@@ -113,7 +113,10 @@ __device__ inline double vls_d(double a, double b, double c, double& ca, double&
 }
 
 // adjoint of clip(e, a, b) = min(max(e, min(a, b)), max(a, b)) given the
-// adjoint of the result: returns the adjoint of e; adds to those of a, b
+// adjoint of the result: returns the adjoint of e; adds to those of a, b.
+// The selections order -0 below +0 (the integer-pipe comparisons of
+// ks_common.cuh), as the forward clip does, so a signed-zero tie routes the
+// adjoint to the operand the forward selected.
 __device__ inline double clip_rev(double e, double a, double b, double rb, double& ga, double& gb) {
     const double lo = imin(a, b), hi = imax(a, b);
     if (ilt(hi, imax(e, lo))) {

@@ -1468,10 +1468,16 @@ int Sim::step() {
 }
 
 // ---------------------------------------------------------------- field access
-// kind: 0 cell, 1 node, 2/3/4 x/y/z face
+// kind: 0 cell, 1 node, 2/3/4 x/y/z face, 5 bottom-wall plane (nx x ny)
 double* Sim::field(const std::string& name, int& nc, int& kind) {
     kind = 0;
     nc = 3;
+    if (name == "wall_grad") {  // wall-model gradient of u, v at z-lo (read-only)
+        if (!wallmodel_) throw KsError(KS_ERR_ARG, "wall_grad needs zlo.type = wall_model");
+        nc = 2;
+        kind = 5;
+        return wg_.p;
+    }
     if (name == "velocity") return vel_.p;
     if (name == "velocity_old") return vel_old_.p;
     if (name == "gp") return gp_.p;
@@ -1508,7 +1514,7 @@ void Sim::layout(const std::string& name, ks_layout& L) {
     L.ncomp = nc;
     L.nx = g_.nx + (kind == 2);
     L.ny = g_.ny + (kind == 3);
-    L.nz = g_.nz + (kind == 4) + ((kind == 1 && !g_.zper) ? 1 : 0);
+    L.nz = kind == 5 ? 1 : g_.nz + (kind == 4) + ((kind == 1 && !g_.zper) ? 1 : 0);
 }
 
 void Sim::get(const std::string& name, void* dst, int where) {
@@ -1517,7 +1523,7 @@ void Sim::get(const std::string& name, void* dst, int where) {
     ks_layout L;
     layout(name, L);
     const size_t out = (size_t)L.ncomp * L.nx * L.ny * L.nz;
-    if (kind < 2) {
+    if (kind < 2 || kind == 5) {
         ck(cudaMemcpyAsync(dst, f, out * sizeof(double), where == KS_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, ctx_.stream),
            "get_field");
         sync();
@@ -1547,7 +1553,7 @@ void Sim::get(const std::string& name, void* dst, int where) {
 void Sim::set(const std::string& name, const void* src, int where) {
     int nc, kind;
     double* f = field(name, nc, kind);
-    if (kind >= 2) throw KsError(KS_ERR_ARG, "face fields are derived and cannot be set");
+    if (kind >= 2) throw KsError(KS_ERR_ARG, "face fields and the wall gradient are derived and cannot be set");
     ks_layout L;
     layout(name, L);
     const size_t n = (size_t)L.ncomp * L.nx * L.ny * L.nz;
@@ -1588,6 +1594,22 @@ double Sim::scalar(const std::string& n) {
         int np = 0;
         launch_ke(ctx_, g_, vel_.p, rho_, parts_.p, &np);
         return reduce(np, 1, 0, nullptr) / (double)g_.N;
+    }
+    if (n == "divu" || n == "divu_rel" || n == "mac_divu" || n == "mac_divu_rel") {
+        // Post-projection divergence, max-norm (1/s): "divu" is the nodal
+        // divergence of the cell velocity (the right-hand side operator of the
+        // nodal projection, which is an approximate projection: this is
+        // truncation-sized, not zero); "mac_divu" is the divergence of the MAC
+        // face velocities (an exact projection: it is the MAC solve's residual).
+        // The _rel forms scale by max|u| / min(dx, dy, dz).
+        int np = 0;
+        if (n[0] == 'm') launch_mac_divmax(ctx_, g_, umac_[0].p, umac_[1].p, umac_[2].p, parts_.p, &np);
+        else launch_nodal_divmax(ctx_, g_, vel_.p, parts_.p, &np);
+        double m[2];
+        reduce(np, 2, 1, m);
+        if (n.back() != 'l') return m[0];
+        const double hmin = std::min(g_.dx, std::min(g_.dy, g_.dz));
+        return m[1] > 0.0 ? m[0] * hmin / m[1] : m[0];
     }
     if (n == "ndisks") return (double)disks_.size();
     if (n == "nodal_omega") return nod_.omega;

@@ -494,53 +494,60 @@ __global__ void k_proj_pre(long long N3, double* vel, const double* vo, const do
     vel[t] = v;
 }
 
-// Nodal divergence (the MLNodeLaplacian right-hand side) with weighted partial
-// sums (boundary nodes carry half weight) for the solvability shift.  The cell
-// velocity is seen with periodic wrap and mirror images across z walls (normal
-// component odd, tangential even; the sign flip is taken on the bits).  Each
-// direction's four edge differences are summed before its one scale
-// q = dx^-1 / 4.
+// Nodal divergence of the cell velocity at node t (the MLNodeLaplacian
+// right-hand side).  The cell velocity is seen with periodic wrap and mirror
+// images across z walls (normal component odd, tangential even; the sign flip
+// is taken on the bits).  Each direction's four edge differences are summed
+// before its one scale q = dx^-1 / 4.
+__device__ inline double nodal_div_at(const Grid& g, const double* vel, unsigned t, int& k, double qx, double qy, double qz) {
+    const unsigned r = t / (unsigned)g.nx;
+    const int i = (int)(t - r * (unsigned)g.nx);
+    k = (int)(r / (unsigned)g.ny);
+    const int j = (int)(r - (unsigned)k * (unsigned)g.ny);
+    const int im = i == 0 ? g.nx - 1 : i - 1, jm = j == 0 ? g.ny - 1 : j - 1;
+    // cell layers k - 1 and k as seen from the node (mirrored at walls)
+    int kk[2];
+    bool flip[2];
+    for (int c = 0; c < 2; ++c) {
+        int q = k - c;
+        flip[c] = false;
+        if (g.zper) q = q < 0 ? q + g.nz : (q >= g.nz ? q - g.nz : q);
+        else if (q < 0) { q = -1 - q; flip[c] = true; }
+        else if (q >= g.nz) { q = 2 * g.nz - 1 - q; flip[c] = true; }
+        kk[c] = q;
+    }
+    const long long N = g.N;
+    // the 8 cells around the node: layers k-1 (c = 1) and k (c = 0), columns (i, j), (i-1, j), (i, j-1), (i-1, j-1)
+    double u[2][4], v[2][4], w[2][4];
+    for (int c = 0; c < 2; ++c) {
+        const long long r0 = (long long)kk[c] * g.ny;
+        const long long o[4] = {(r0 + j) * g.nx + i, (r0 + j) * g.nx + im, (r0 + jm) * g.nx + i, (r0 + jm) * g.nx + im};
+        for (int q = 0; q < 4; ++q) {
+            u[c][q] = vel[o[q]];
+            v[c][q] = vel[N + o[q]];
+            const double z = vel[2 * N + o[q]];
+            w[c][q] = flip[c] ? bitsd(dbits(z) ^ ~kMag) : z;
+        }
+    }
+    double dx = 0, dy = 0, dz = 0;
+    for (int c = 0; c < 2; ++c) {
+        dx += (u[c][0] - u[c][1]) + (u[c][2] - u[c][3]);
+        dy += (v[c][0] - v[c][2]) + (v[c][1] - v[c][3]);
+    }
+    // z: differences of w between the layers k and k - 1 over the four cells
+    dz = ((w[0][0] - w[1][0]) + (w[0][1] - w[1][1])) + ((w[0][2] - w[1][2]) + (w[0][3] - w[1][3]));
+    return qx * dx + (qy * dy + qz * dz);
+}
+
+// Nodal divergence into the right-hand side, with weighted partial sums
+// (boundary nodes carry half weight) for the solvability shift.
 __global__ void k_nodal_rhs(Grid g, const double* vel, double* rhs, double* parts, int np, double qx, double qy, double qz) {
     const int nzn = g.zper ? g.nz : g.nz + 1;
     const unsigned M = (unsigned)(g.nx * g.ny * nzn);
     double ws = 0, wt = 0;
     for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < M; t += gridDim.x * blockDim.x) {
-        const unsigned r = t / (unsigned)g.nx;
-        const int i = (int)(t - r * (unsigned)g.nx);
-        const int k = (int)(r / (unsigned)g.ny), j = (int)(r - (unsigned)k * (unsigned)g.ny);
-        const int im = i == 0 ? g.nx - 1 : i - 1, jm = j == 0 ? g.ny - 1 : j - 1;
-        // cell layers k - 1 and k as seen from the node (mirrored at walls)
-        int kk[2];
-        bool flip[2];
-        for (int c = 0; c < 2; ++c) {
-            int q = k - c;
-            flip[c] = false;
-            if (g.zper) q = q < 0 ? q + g.nz : (q >= g.nz ? q - g.nz : q);
-            else if (q < 0) { q = -1 - q; flip[c] = true; }
-            else if (q >= g.nz) { q = 2 * g.nz - 1 - q; flip[c] = true; }
-            kk[c] = q;
-        }
-        const long long N = g.N;
-        // the 8 cells around the node: layers k-1 (c = 1) and k (c = 0), columns (i, j), (i-1, j), (i, j-1), (i-1, j-1)
-        double u[2][4], v[2][4], w[2][4];
-        for (int c = 0; c < 2; ++c) {
-            const long long r0 = (long long)kk[c] * g.ny;
-            const long long o[4] = {(r0 + j) * g.nx + i, (r0 + j) * g.nx + im, (r0 + jm) * g.nx + i, (r0 + jm) * g.nx + im};
-            for (int q = 0; q < 4; ++q) {
-                u[c][q] = vel[o[q]];
-                v[c][q] = vel[N + o[q]];
-                const double z = vel[2 * N + o[q]];
-                w[c][q] = flip[c] ? bitsd(dbits(z) ^ ~kMag) : z;
-            }
-        }
-        double dx = 0, dy = 0, dz = 0;
-        for (int c = 0; c < 2; ++c) {
-            dx += (u[c][0] - u[c][1]) + (u[c][2] - u[c][3]);
-            dy += (v[c][0] - v[c][2]) + (v[c][1] - v[c][3]);
-        }
-        // z: differences of w between the layers k and k - 1 over the four cells
-        dz = ((w[0][0] - w[1][0]) + (w[0][1] - w[1][1])) + ((w[0][2] - w[1][2]) + (w[0][3] - w[1][3]));
-        const double dv = qx * dx + (qy * dy + qz * dz);
+        int k;
+        const double dv = nodal_div_at(g, vel, t, k, qx, qy, qz);
         rhs[t] = dv;
         const double wgt = (!g.zper && (k == 0 || k == nzn - 1)) ? 0.5 : 1.0;
         ws += wgt * dv;
@@ -549,6 +556,23 @@ __global__ void k_nodal_rhs(Grid g, const double* vel, double* rhs, double* part
     ws = block_reduce<0>(ws);
     wt = block_reduce<0>(wt);
     if (threadIdx.x == 0) { parts[blockIdx.x] = ws; parts[np + blockIdx.x] = wt; }
+}
+
+// Post-projection diagnostic: per-block max-norm of the nodal divergence of
+// the velocity (the operator the projection drives to zero) and of |u|.
+// Both maxima are kept as bits, so a NaN survives to the host.
+__global__ void k_nodal_divmax(Grid g, const double* vel, double* parts, int np, double qx, double qy, double qz) {
+    const int nzn = g.zper ? g.nz : g.nz + 1;
+    const unsigned M = (unsigned)(g.nx * g.ny * nzn);
+    const unsigned stride = gridDim.x * blockDim.x;
+    long long md = 0, mu = 0;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < M; t += stride) {
+        int k;
+        md = imax_abs(md, nodal_div_at(g, vel, t, k, qx, qy, qz));
+    }
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < (unsigned)(3 * g.N); t += stride) mu = imax_abs(mu, vel[t]);
+    const double a = block_reduce<1>(bitsd(md)), b = block_reduce<1>(bitsd(mu));
+    if (threadIdx.x == 0) { parts[blockIdx.x] = a; parts[np + blockIdx.x] = b; }
 }
 
 // u -= sigma G phi ; gp = (or +=) G phi ; optional add-back of u_old.  G is the
@@ -602,6 +626,22 @@ __global__ void k_mac_rhs(Grid g, const double* um, const double* vm, const doub
     }
     s = block_reduce<0>(s);
     if (threadIdx.x == 0) parts[blockIdx.x] = s;
+}
+
+// Post-projection diagnostic: per-block maxima of |div u_mac| (the MAC
+// projection's exact discrete divergence) and of the face speeds, as bits.
+__global__ void k_mac_divmax(Grid g, const double* um, const double* vm, const double* wm, double* parts, int np) {
+    long long md = 0, mu = 0;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < g.N; t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        cell_of(g, t, i, j, k);
+        const double r = (um[fidx(g, 0, i + 1, j, k)] - um[t]) * g.idx + (vm[fidx(g, 1, i, j + 1, k)] - vm[t]) * g.idy +
+                         (wm[fidx(g, 2, i, j, k + 1)] - wm[fidx(g, 2, i, j, k)]) * g.idz;
+        md = imax_abs(md, r);
+        mu = imax_abs(imax_abs(imax_abs(mu, um[t]), vm[t]), wm[fidx(g, 2, i, j, k)]);
+    }
+    const double a = block_reduce<1>(bitsd(md)), b = block_reduce<1>(bitsd(mu));
+    if (threadIdx.x == 0) { parts[blockIdx.x] = a; parts[np + blockIdx.x] = b; }
 }
 
 __global__ void k_mac_correct(Grid g, const double* phi, double* um, double* vm, double* wm, double beta) {
@@ -841,6 +881,11 @@ void launch_nodal_rhs(Ctx& c, const Grid& g, const double* vel, double* rhs, dou
     *np = parts_for(M);
     KS_LAUNCH(c, k_nodal_rhs, *np, BS, B8 * (3 * g.N + M), g, vel, rhs, parts, *np, 0.25 * g.idx, 0.25 * g.idy, 0.25 * g.idz);
 }
+void launch_nodal_divmax(Ctx& c, const Grid& g, const double* vel, double* parts, int* np) {
+    const long long M = (long long)g.nx * g.ny * (g.zper ? g.nz : g.nz + 1);
+    *np = parts_for(M);
+    KS_LAUNCH(c, k_nodal_divmax, *np, BS, B8 * 3 * g.N, g, vel, parts, *np, 0.25 * g.idx, 0.25 * g.idy, 0.25 * g.idz);
+}
 void launch_nodal_post(Ctx& c, const Grid& g, const double* phi, double* vel, const double* vo, double* gp, double* p, double sigma,
                        int add_old, int incr) {
     const long long M = (long long)g.nx * g.ny * (g.zper ? g.nz : g.nz + 1);
@@ -852,6 +897,10 @@ void launch_nodal_post(Ctx& c, const Grid& g, const double* phi, double* vel, co
 void launch_mac_rhs(Ctx& c, const Grid& g, const double* um, const double* vm, const double* wm, double* rhs, double* parts, int* np) {
     *np = parts_for(g.N);
     KS_LAUNCH(c, k_mac_rhs, *np, BS, B8 * (3 * g.N + g.NFz), g, um, vm, wm, rhs, parts, *np);
+}
+void launch_mac_divmax(Ctx& c, const Grid& g, const double* um, const double* vm, const double* wm, double* parts, int* np) {
+    *np = parts_for(g.N);
+    KS_LAUNCH(c, k_mac_divmax, *np, BS, B8 * (2 * g.N + g.NFz), g, um, vm, wm, parts, *np);
 }
 void launch_mac_correct(Ctx& c, const Grid& g, const double* phi, double* um, double* vm, double* wm, double beta) {
     KS_LAUNCH(c, k_mac_correct, nblocks(g.N, BS), BS, B8 * 7 * g.N, g, phi, um, vm, wm, beta);

@@ -162,10 +162,14 @@ void launch_predictor_rhs(Ctx& c, const Grid& g, const double* vel_old, const do
 void launch_proj_pre(Ctx& c, const Grid& g, double* vel, const double* vel_old, const double* gp, double scaling, double rho,
                      int add_gp, int sub_old);
 void launch_nodal_rhs(Ctx& c, const Grid& g, const double* vel, double* rhs, double* partials, int* nparts);
+// per-block maxima of |nodal divergence of vel| (parts[0..np)) and |vel| (parts[np..2np))
+void launch_nodal_divmax(Ctx& c, const Grid& g, const double* vel, double* partials, int* nparts);
 void launch_nodal_post(Ctx& c, const Grid& g, const double* phi, double* vel, const double* vel_old, double* gp, double* p,
                        double sigma, int add_old, int incremental);
 void launch_mac_rhs(Ctx& c, const Grid& g, const double* um, const double* vm, const double* wm, double* rhs, double* partials,
                     int* nparts);
+// per-block maxima of |div u_mac| (parts[0..np)) and of the face speeds (parts[np..2np))
+void launch_mac_divmax(Ctx& c, const Grid& g, const double* um, const double* vm, const double* wm, double* partials, int* nparts);
 void launch_mac_correct(Ctx& c, const Grid& g, const double* phi, double* um, double* vm, double* wm, double beta);
 void launch_cfl(Ctx& c, const Grid& g, const double* vel, const double* src, const double* mueff, double rho, double* partials,
                 int* nparts);

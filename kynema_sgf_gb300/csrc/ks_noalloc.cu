@@ -1,14 +1,14 @@
 // Allocation-free entry point for the tensor diffusion term.
 //
 // Some callers of this library cannot call cudaMalloc at the point where they
-// need the viscous term: code that runs inside a CUDA stream capture in the
-// global or thread-local capture mode (cudaMalloc is an illegal call there),
-// hosts whose device memory is reserved up front by another allocator or
-// framework and must not grow, and latency-critical loops that cannot afford
-// the device-wide synchronisation an allocation may cause.  For them,
-// ks_divtau_noalloc evaluates div(mu (grad u + grad u^T) - 2/3 mu div(u) I) on
-// caller-owned device buffers, and keeps the nine face-flux scratch arrays it
-// needs in the file-scope device array below instead of allocating them.
+// need the viscous term: hosts whose device memory is reserved up front by
+// another allocator or framework and must not grow, plug-in code that runs
+// inside an application that owns every device allocation, and
+// latency-critical loops that cannot afford the device-wide synchronisation
+// an allocation may cause.  For them, ks_divtau_noalloc evaluates
+// div(mu (grad u + grad u^T) - 2/3 mu div(u) I) on caller-owned device
+// buffers, and keeps the nine face-flux scratch arrays it needs in the
+// file-scope device array below instead of allocating them.
 //
 // The scratch array holds KS_NOALLOC_MAX_CELLS cells' worth of face fluxes
 // (about 24 MB of FP64).  Every GPU that loads the library holds it until the
@@ -16,6 +16,11 @@
 // (different streams, or different host threads on one device) race on it, so
 // callers must order them.  Each call writes every scratch value it reads
 // before reading it, so nothing carries over from the previous call.
+//
+// The first call on a device looks up the array's device address with that
+// device current (cudaGetSymbolAddress) and caches it; make that first call
+// before any stream capture.  A device reset (cudaDeviceReset) unloads the
+// module that holds the array, so calls after a reset are not supported.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -89,8 +94,12 @@ extern "C" int ks_divtau_noalloc(const double* vel, const double* mueff, const d
             fl[3 * d + n] = q;
             q += (d == 2) ? g.NFz : g.N;
         }
+    // A CUDA error already pending on this thread belongs to the caller: it is
+    // left in place for the caller's own check, and nothing is launched.
+    if (cudaPeekAtLastError() != cudaSuccess) return KS_ERR_CUDA;
     ks::Ctx ctx;
     ctx.stream = static_cast<cudaStream_t>(stream);
     ks::launch_divtau_faces(ctx, g, vel, mueff, wall_grad, divtau, 0, nullptr, nullptr, nullptr, nullptr, 0.0, 1.0, fl);
-    return cudaGetLastError() == cudaSuccess ? KS_OK : KS_ERR_CUDA;
+    // a launch failure stays pending (as the runtime leaves it) for the caller to read
+    return cudaPeekAtLastError() == cudaSuccess ? KS_OK : KS_ERR_CUDA;
 }

@@ -24,7 +24,7 @@ KS_HOST, KS_DEVICE = 0, 1
 
 FIELDS = ["velocity", "velocity_old", "gp", "p", "src_term", "forces", "diff_term", "conv_term", "conv_term_old", "velocity_mueff",
           "u_mac", "v_mac", "w_mac", "actuator_src_term", "velocity_adjoint", "gp_adjoint", "temperature", "temperature_old",
-          "temperature_mueff", "temperature_conv_term", "temperature_diff_term"]
+          "temperature_mueff", "temperature_conv_term", "temperature_diff_term", "wall_grad"]
 
 # every symbol declared in include/ks.h
 SYMBOLS = ["ks_create", "ks_destroy", "ks_last_error", "ks_init_data", "ks_compute_dt", "ks_pre_advance",

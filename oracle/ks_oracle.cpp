@@ -330,6 +330,8 @@ struct Sim {
     void init_data();
     int step_once();
     double ke() const;
+    double divu(double* umax) const;
+    double mac_divu(double* umax) const;
 };
 
 // ---- setup -----------------------------------------------------------------
@@ -1877,6 +1879,76 @@ static std::vector<NDLevel> nd_levels(const Geo& g) {
     return Ls;
 }
 
+// Nodal divergence of a cell velocity (NodalProjector::computeRHS, the
+// MLNodeLaplacian right-hand side, absent AMReX submodule; call site
+// src/projection/incflo_apply_nodal_projection.cpp:344-355): at each node the
+// mean over the four surrounding cell edges of each direction's difference,
+// with the velocity zero outside a wall (setBndry(0)) and periodic wrap; wall
+// nodes see half the support and are scaled by 2.  out: nodes (nx, ny, nzn).
+static void nodal_divergence(const Geo& g, const Arr& vel, Arr& out) {
+    const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+    const bool zper = g.per[2];
+    Arr v;
+    def_cc(v, g, 1, 3);
+    for (int n = 0; n < 3; ++n)
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) v(i, j, k, n) = vel(i, j, k, n);
+    const int cc[3] = {0, 0, 0};
+    fill_periodic(v, g, cc);
+    const int nzn = nz + (zper ? 0 : 1);
+#pragma omp parallel for collapse(2)
+    for (int k = 0; k < nzn; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                double dv = 0;
+                for (int c = 0; c < 2; ++c)
+                    for (int b = 0; b < 2; ++b) {
+                        dv += 0.25 / g.dx[0] * (v(i, j - b, k - c, 0) - v(i - 1, j - b, k - c, 0));
+                        dv += 0.25 / g.dx[1] * (v(i - b, j, k - c, 1) - v(i - b, j - 1, k - c, 1));
+                        dv += 0.25 / g.dx[2] * (v(i - b, j - c, k, 2) - v(i - b, j - c, k - 1, 2));
+                    }
+                if (!zper && (k == 0 || k == nzn - 1)) dv *= 2.0;
+                out(i, j, k) = dv;
+            }
+}
+
+// Post-projection diagnostic: max-norm of the divergence of the MAC face
+// velocities (1/s; the MAC projection is exact, so this is its residual);
+// umax receives the largest face speed.
+double Sim::mac_divu(double* umax) const {
+    const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
+    double m = 0, mu = 0;
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const double r = (umac(i + 1, j, k) - umac(i, j, k)) / g.dx[0] + (vmac(i, j + 1, k) - vmac(i, j, k)) / g.dx[1] +
+                                 (wmac(i, j, k + 1) - wmac(i, j, k)) / g.dx[2];
+                m = std::max(m, std::fabs(r));
+                mu = std::max(mu, std::max(std::fabs(umac(i, j, k)), std::max(std::fabs(vmac(i, j, k)), std::fabs(wmac(i, j, k)))));
+            }
+    if (umax) *umax = mu;
+    return m;
+}
+
+// Post-projection diagnostic: max-norm of the nodal divergence of the current
+// velocity (1/s; the nodal projection is approximate, so this is
+// truncation-sized); umax receives max |u| over all components.
+double Sim::divu(double* umax) const {
+    const int nzn = g.n[2] + (g.per[2] ? 0 : 1);
+    Arr d;
+    d.define(0, 0, 0, g.n[0] - 1, g.n[1] - 1, nzn - 1, 1);
+    nodal_divergence(g, vel, d);
+    double m = 0, mu = 0;
+    for (double x : d.d) m = std::max(m, std::fabs(x));
+    for (int n = 0; n < 3; ++n)
+        for (int k = 0; k < g.n[2]; ++k)
+            for (int j = 0; j < g.n[1]; ++j)
+                for (int i = 0; i < g.n[0]; ++i) mu = std::max(mu, std::fabs(vel(i, j, k, n)));
+    if (umax) *umax = mu;
+    return m;
+}
+
 // incflo::ApplyProjection (src/projection/incflo_apply_nodal_projection.cpp:149-465)
 void Sim::nodal_project(double time, double scaling, bool incremental) {
     const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
@@ -1896,32 +1968,15 @@ void Sim::nodal_project(double time, double scaling, bool incremental) {
     const double sigma = scaling / rho;
     std::vector<NDLevel> Ls = nd_levels(g);
     NDLevel& L = Ls[0];
-    // velocity with zero ghosts at walls (setBndry(0)), periodic wrap
-    Arr v;
-    def_cc(v, g, 1, 3);
-    for (int n = 0; n < 3; ++n)
-        for (int k = 0; k < nz; ++k)
-            for (int j = 0; j < ny; ++j)
-                for (int i = 0; i < nx; ++i) v(i, j, k, n) = vel(i, j, k, n);
-    const int cc[3] = {0, 0, 0};
-    fill_periodic(v, g, cc);
+    nodal_divergence(g, vel, L.rhs);
     const int nzn = L.nn[2];
     double wsum = 0, wtot = 0;
 #pragma omp parallel for collapse(2) reduction(+ : wsum, wtot)
     for (int k = 0; k < nzn; ++k)
         for (int j = 0; j < ny; ++j)
             for (int i = 0; i < nx; ++i) {
-                double dv = 0;
-                for (int c = 0; c < 2; ++c)
-                    for (int b = 0; b < 2; ++b) {
-                        dv += 0.25 / g.dx[0] * (v(i, j - b, k - c, 0) - v(i - 1, j - b, k - c, 0));
-                        dv += 0.25 / g.dx[1] * (v(i - b, j, k - c, 1) - v(i - b, j - 1, k - c, 1));
-                        dv += 0.25 / g.dx[2] * (v(i - b, j - c, k, 2) - v(i - b, j - c, k - 1, 2));
-                    }
-                double w = 1.0;
-                if (!zper && (k == 0 || k == nzn - 1)) { dv *= 2.0; w = 0.5; }
-                L.rhs(i, j, k) = dv;
-                wsum += w * dv;
+                const double w = (!zper && (k == 0 || k == nzn - 1)) ? 0.5 : 1.0;
+                wsum += w * L.rhs(i, j, k);
                 wtot += w;
             }
     const double mean = wsum / wtot;
@@ -2721,6 +2776,14 @@ double kso_get_scalar(void* h, const char* name) {
     if (n == "abl_forcing_y") return s.ablf_force[1];
     if (n == "utau") return s.utau;
     if (n == "ke") return s.ke();
+    if (n == "divu") return s.divu(nullptr);
+    if (n == "mac_divu") return s.mac_divu(nullptr);
+    if (n == "divu_rel" || n == "mac_divu_rel") {
+        double um = 0;
+        const double d = n[0] == 'm' ? s.mac_divu(&um) : s.divu(&um);
+        const double hmin = std::min(s.g.dx[0], std::min(s.g.dx[1], s.g.dx[2]));
+        return um > 0.0 ? d * hmin / um : d;
+    }
     if (n == "cfl") return s.t.cur_cfl;
     if (n == "conv_cfl") return s.t.conv_cfl;
     if (n == "diff_cfl") return s.t.diff_cfl;

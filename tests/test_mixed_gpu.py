@@ -35,6 +35,9 @@ def test_mixed_matches_fp64(cuda_dev):
         assert mix.scalar("nodal_res") <= max(1e2 * EPS, 1e5 * EPS * mix.scalar("nodal_res0"))
         assert mix.scalar("mac_iters") <= ref.scalar("mac_iters") + 2
         assert mix.scalar("nodal_iters") <= ref.scalar("nodal_iters") + 2
+        # post-projection divergence: the MAC projection is exact (its
+        # divergence is the FP64 residual) in both forms
+        assert mix.scalar("mac_divu_rel") <= 1e-10 and ref.scalar("mac_divu_rel") <= 1e-10
     v, r = mix.get_field("velocity"), ref.get_field("velocity")
     ev = rel(v, r)
     e2 = np.sqrt(((v - r) ** 2).sum() / (r ** 2).sum())
