@@ -134,9 +134,16 @@ void Sim::setup(const Deck& D) {
         S_.gf[2] = 0.0;
     }
     if (S_.body) {
-        if (lc(D.str("BodyForce.type", "constant")) != "constant") throw KsError(KS_ERR_UNSUPPORTED, "BodyForce.type");
+        // BodyForce::BodyForce (BodyForce.cpp:20-58): uniform_constant (default) or
+        // oscillatory with angular_frequency; the file-driven types are not built
+        const std::string bt = lc(D.str("BodyForce.type", "uniform_constant"));
+        if (bt == "height_varying" || bt == "height-varying" || bt == "uniform_timetable" || D.has("BodyForce.uniform_timetable_file"))
+            throw KsError(KS_ERR_UNSUPPORTED, "BodyForce.type " + bt + " (file-driven forcing)");
+        if (bt != "uniform_constant" && bt != "oscillatory") throw KsError(KS_ERR_DECK, "BodyForce.type " + bt);
         auto m = D.nums("BodyForce.magnitude");
         for (int d = 0; d < 3; ++d) S_.body_force[d] = m.at(d);
+        S_.body_osc = bt == "oscillatory";
+        if (S_.body_osc) S_.body_omega = D.nums("BodyForce.angular_frequency").at(0);
     }
     kappa_ = D.num("ABL.kappa", 0.41);
     z0_ = D.num("ABL.surface_roughness_z0", 0.1);
@@ -625,6 +632,13 @@ void Sim::compute_dt() {
     if (!std::isfinite(m[0]) || !std::isfinite(m[1]) || !std::isfinite(m[2])) throw KsError(KS_ERR_NONFINITE, "non-finite CFL");
     // the diffusion CFL counts for explicit diffusion only (incflo_compute_dt.cpp:37,140-145,211-214)
     t_.set_cfl(m[0], diff_type_ == 0 ? m[1] : 0.0, t_.force_cfl ? m[2] : 0.0);
+}
+
+// SrcTermOp<ICNS> (icns_ops.H:78-124) at the clock's current step: the
+// oscillatory BodyForce takes its factor at the mid-step time (BodyForce.cpp:145-160)
+void Sim::sources(const double* vel, const double* theta) {
+    S_.t_nph = 0.5 * (t_.cur + t_.next);
+    launch_sources(ctx_, g_, vel, gp_.p, act_.p, src_.p, S_, theta);
 }
 
 // ---------------------------------------------------------------- ABL
@@ -1229,12 +1243,12 @@ void Sim::apply_predictor(bool incremental) {
         return;
     }
     const double dt = t_.dt[0];
-    launch_smagorinsky(ctx_, g_, vel_old_.p, mueff_.p, S_, alpha_.p);
-    launch_sources(ctx_, g_, vel_old_.p, gp_.p, act_.p, src_.p, S_, theta_old_.p);  // BoussinesqBuoyancy: theta at Old
+    launch_smagorinsky(ctx_, g_, vel_old_.p, mueff_.p, S_, alpha_.p, mixed_);
+    sources(vel_old_.p, theta_old_.p);  // BoussinesqBuoyancy: theta at Old
     if (wallmodel_) launch_wall_grad(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, shear_, utau_ * utau_, um_[0], um_[1], vmag_, rho_);
     double* fl[9];
     for (int m = 0; m < 9; ++m) fl[m] = static_cast<double*>(gb_.flux[m / 3][m % 3]);
-    launch_divtau(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, divtau_.p, 1, src_.p, forces_.p, nullptr, nullptr, dt, rho_, fl);
+    launch_divtau(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, divtau_.p, 1, src_.p, forces_.p, nullptr, nullptr, dt, rho_, fl, mixed_);
     if (temp_) {  // the temperature's diff_term(Old) (no temperature sources)
         if (tzlo_ == 1)
             launch_theta_wall_grad(ctx_, g_, vel_old_.p, theta_old_.p, alpha_.p, tgz_.p, shear_, utau_, kappa_, std::log(zref_ / z0t_), vmag_,
@@ -1250,10 +1264,10 @@ void Sim::apply_predictor(bool incremental) {
     // compute_source_term(NPH): Coriolis reads the Old velocity and gp is
     // unchanged, so only BoussinesqBuoyancy (theta at n+1/2) changes src;
     // compute_diffusion_term(Old) reproduces divtau.
-    if (S_.bous) launch_sources(ctx_, g_, vel_old_.p, gp_.p, act_.p, src_.p, S_, theta_nph_.p);
+    if (S_.bous) sources(vel_old_.p, theta_nph_.p);
     launch_predictor_rhs(ctx_, g_, vel_old_.p, conv_.p, src_.p, divtau_.p, vel_.p, dt, rho_, diff_fac());
     if (diff_type_ == 0) {  // explicit RK2 correction (incflo_advance.cpp:388-400)
-        launch_divtau(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, 2, nullptr, nullptr, vel_.p, divtau_.p, dt, rho_, fl);
+        launch_divtau(ctx_, g_, vel_.p, mueff_.p, wg_.p, vel_tmp_.p, 2, nullptr, nullptr, vel_.p, divtau_.p, dt, rho_, fl, mixed_);
         std::swap(vel_.p, vel_tmp_.p);
     } else {  // icns().solve(dt_diff) (incflo_advance.cpp:376-386)
         diffuse_solve(diff_type_ == 2 ? dt : 0.5 * dt);
@@ -1289,7 +1303,7 @@ void Sim::mol_predictor(bool incremental) {
     const double* cmac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
     if (temp_) temperature_mol(false, dt);
     // sources at NPH: the Coriolis term reads Old, BoussinesqBuoyancy theta at n+1/2
-    launch_sources(ctx_, g_, vel_old_.p, gp_.p, act_.p, src_.p, S_, temp_ ? theta_nph_.p : nullptr);
+    sources(vel_old_.p, temp_ ? theta_nph_.p : nullptr);
     launch_mol_advection(ctx_, g_, vel_old_.p, cmac, rho_, fl, conv_old_.p, 1, vel_old_.p, src_.p, divtau_.p, nullptr, vel_.p, dt, fac);
     if (diff_type_ != 0) diffuse_solve(diff_type_ == 2 ? dt : 0.5 * dt);
     apply_projection(t_.next, dt, incremental);
@@ -1318,7 +1332,7 @@ void Sim::apply_corrector() {
     if (wallmodel_) launch_wall_grad(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, shear_, utau_ * utau_, um_[0], um_[1], vmag_, rho_);
     if (temp_) temperature_mol(true, dt);
     // sources at New: the Coriolis term reads the predicted velocity, BoussinesqBuoyancy theta at n+1/2
-    launch_sources(ctx_, g_, vel_.p, gp_.p, act_.p, src_.p, S_, temp_ ? theta_nph_.p : nullptr);
+    sources(vel_.p, temp_ ? theta_nph_.p : nullptr);
     if (diff_type_ != 0) {
         // corrector_rhs with ofac 1/2 (Crank-Nicolson) or 0 (implicit) and nfac 0, fused into the
         // divergence of the fluxes, then the solve with mu_eff(New) (incflo_advance.cpp:620-640)

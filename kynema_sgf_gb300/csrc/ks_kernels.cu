@@ -108,6 +108,10 @@ __global__ void k_copy(double* d, const double* s, long long n) {
 // strain rate src/fvm/strainrate.H:24-86, one-sided z stencils at walls
 // src/fvm/stencils.H:166-330).
 // alpha_eff = mu / Pr + mu_t / Pr_t (TurbModelBase.H:28-35) when alpha is set
+// T is the arithmetic type: double, or float in the mixed-precision form (the
+// strain rate of the FP64 velocity read once per cell and rounded; mu_eff is
+// stored in FP64).
+template <typename T>
 __global__ void k_smag(Grid g, const double* vel, double* mueff, double mu, double rho, double fac, int smag, double* alpha, double mu_pr,
                        double iprt) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -119,24 +123,25 @@ __global__ void k_smag(Grid g, const double* vel, double* mueff, double mu, doub
     }
     int i, j, k;
     cell_of(g, t, i, j, k);
-    VelFP V{vel, g, 1.0};
-    const double hx = 0.5 * g.idx, hy = 0.5 * g.idy;
-    double gx[3], gy[3], gz[3];
+    VelFPT<T, double> V{vel, g, T(1)};
+    const T hx = T(0.5 * g.idx), hy = T(0.5 * g.idy);
+    T gx[3], gy[3], gz[3];
     for (int n = 0; n < 3; ++n) {
         gx[n] = hx * (V(n, i + 1, j, k) - V(n, i - 1, j, k));
         gy[n] = hy * (V(n, i, j + 1, k) - V(n, i, j - 1, k));
     }
     if (!g.zper && (k == 0 || k == g.nz - 1)) {  // one-sided through the wall (ghost) value
-        double a = 1.0 / 3.0, b = 1.0, c = -4.0 / 3.0;
-        if (k == g.nz - 1) { a = 4.0 / 3.0; b = -1.0; c = -1.0 / 3.0; }
-        for (int n = 0; n < 3; ++n) gz[n] = (a * V(n, i, j, k + 1) + b * V(n, i, j, k) + c * V(n, i, j, k - 1)) * g.idz;
+        T a = T(1.0 / 3.0), b = T(1), c = T(-4.0 / 3.0);
+        if (k == g.nz - 1) { a = T(4.0 / 3.0); b = T(-1); c = T(-1.0 / 3.0); }
+        const T iz = T(g.idz);
+        for (int n = 0; n < 3; ++n) gz[n] = (a * V(n, i, j, k + 1) + b * V(n, i, j, k) + c * V(n, i, j, k - 1)) * iz;
     } else {
-        const double hz = 0.5 * g.idz;
+        const T hz = T(0.5 * g.idz);
         for (int n = 0; n < 3; ++n) gz[n] = hz * (V(n, i, j, k + 1) - V(n, i, j, k - 1));
     }
-    const double sxy = gy[0] + gx[1], syz = gz[1] + gy[2], szx = gx[2] + gz[0];
-    const double s = sqrt(2.0 * (gx[0] * gx[0] + gy[1] * gy[1] + gz[2] * gz[2]) + (sxy * sxy + syz * syz + szx * szx));
-    const double mut = (rho * fac) * s;
+    const T sxy = gy[0] + gx[1], syz = gz[1] + gy[2], szx = gx[2] + gz[0];
+    const T s = sqrt(T(2) * (gx[0] * gx[0] + gy[1] * gy[1] + gz[2] * gz[2]) + (sxy * sxy + syz * syz + szx * szx));
+    const double mut = (rho * fac) * (double)s;
     mueff[t] = mu + mut;
     if (alpha) alpha[t] = mu_pr + iprt * mut;
 }
@@ -342,7 +347,9 @@ constexpr int TTX = 32, TTY = 4, TTZ = 4;
 constexpr int THX = TTX + 2, THY = TTY + 2, THZ = TTZ + 2;
 constexpr int TNH = THX * THY * THZ;
 constexpr int TNFX = (TTX + 1) * TTY * TTZ, TNFY = TTX * (TTY + 1) * TTZ, TNFZ = TTX * TTY * (TTZ + 1);
-constexpr size_t TAU_SMEM = sizeof(double) * (4 * (size_t)TNH + 3 * ((size_t)TNFX + TNFY + TNFZ));
+// dynamic shared memory of the tile kernel staging and computing in type T
+template <typename T>
+constexpr size_t tau_smem() { return sizeof(T) * (4 * (size_t)TNH + 3 * ((size_t)TNFX + TNFY + TNFZ)); }
 
 // Epilogue of the tiled tensor-diffusion kernel (acc = divtau(vel) of a cell):
 //   0: out = acc
@@ -361,14 +368,19 @@ struct TauEpi {
     double irho;  // 1 / rho, formed on the host
 };
 
+// T: type of the staged values, the face fluxes and their arithmetic (double;
+// float for the mixed-precision form, modes 0-2 only).  The inputs are FP64
+// and rounded once when staged; the epilogue runs in FP64.
+template <typename T>
 __global__ void __launch_bounds__(TTX* TTY* TTZ) k_divtau_tile(Grid g, const double* vel, const double* mueff, const double* wg, double* out,
                                                                TauEpi E) {
-    extern __shared__ double sm[];
-    double* sV = sm;                // [3][THZ][THY][THX]
-    double* sM = sm + 3 * TNH;      // [THZ][THY][THX]
-    double* sFx = sm + 4 * TNH;     // [3][TTZ][TTY][TTX + 1]
-    double* sFy = sFx + 3 * TNFX;   // [3][TTZ][TTY + 1][TTX]
-    double* sFz = sFy + 3 * TNFY;   // [3][TTZ + 1][TTY][TTX]
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    T* sm = reinterpret_cast<T*>(sm_raw);
+    T* sV = sm;                // [3][THZ][THY][THX]
+    T* sM = sm + 3 * TNH;      // [THZ][THY][THX]
+    T* sFx = sm + 4 * TNH;     // [3][TTZ][TTY][TTX + 1]
+    T* sFy = sFx + 3 * TNFX;   // [3][TTZ][TTY + 1][TTX]
+    T* sFz = sFy + 3 * TNFY;   // [3][TTZ + 1][TTY][TTX]
     const int i0 = blockIdx.x * TTX, j0 = blockIdx.y * TTY, k0 = blockIdx.z * TTZ;
     const int tid = threadIdx.x;
     const int nthr = TTX * TTY * TTZ;
@@ -380,25 +392,25 @@ __global__ void __launch_bounds__(TTX* TTY* TTZ) k_divtau_tile(Grid g, const dou
         const int gi = ((i0 + hx - 1) % g.nx + g.nx) % g.nx, gj = ((j0 + hy - 1) % g.ny + g.ny) % g.ny;
         int gk = k0 + hz - 1;
         if (g.zper) gk = (gk % g.nz + g.nz) % g.nz;
-        for (int n = 0; n < 3; ++n) sV[n * TNH + h] = V(n, gi, gj, gk);
+        for (int n = 0; n < 3; ++n) sV[n * TNH + h] = (T)V(n, gi, gj, gk);
         const int kk = g.zper ? gk : (gk < 0 ? 0 : (gk >= g.nz ? g.nz - 1 : gk));
-        sM[h] = mueff[cidx(g, gi, gj, kk)];
+        sM[h] = (T)mueff[cidx(g, gi, gj, kk)];
     }
     __syncthreads();
-    const double ih[3] = {g.idx, g.idy, g.idz};
-    const double qh[3] = {0.25 * g.idx, 0.25 * g.idy, 0.25 * g.idz};
+    const T ih[3] = {(T)g.idx, (T)g.idy, (T)g.idz};
+    const T qh[3] = {T(0.25 * g.idx), T(0.25 * g.idy), T(0.25 * g.idz)};
     // flux through the d-face at the low side of halo cell (hx, hy, hz)
-    auto flux = [&](int d, int hx, int hy, int hz, int gk, double F[3]) {
+    auto flux = [&](int d, int hx, int hy, int hz, int gk, T F[3]) {
         const int e0 = (d == 0), e1 = (d == 1), e2 = (d == 2);
         const int mx = hx - e0, my = hy - e1, mz = hz - e2;
-        double mf;
+        T mf;
         if (d == 2 && !g.zper && gk == 0) mf = sM[hidx(hx, hy, hz)];
         else if (d == 2 && !g.zper && gk == g.nz) mf = sM[hidx(mx, my, mz)];
-        else mf = 0.5 * (sM[hidx(mx, my, mz)] + sM[hidx(hx, hy, hz)]);
-        double gr[3][3];
+        else mf = T(0.5) * (sM[hidx(mx, my, mz)] + sM[hidx(hx, hy, hz)]);
+        T gr[3][3];
         const int hc = hidx(hx, hy, hz), hm = hidx(mx, my, mz);
         for (int n = 0; n < 3; ++n) {
-            const double* v = sV + n * TNH;
+            const T* v = sV + n * TNH;
             for (int m = 0; m < 3; ++m) {
                 if (m == d) {
                     gr[m][n] = (v[hc] - v[hm]) * ih[m];
@@ -408,14 +420,14 @@ __global__ void __launch_bounds__(TTX* TTY* TTZ) k_divtau_tile(Grid g, const dou
                 }
             }
         }
-        const double dv = gr[0][0] + gr[1][1] + gr[2][2];
+        const T dv = gr[0][0] + gr[1][1] + gr[2][2];
         for (int n = 0; n < 3; ++n) {
-            if (n == d) F[n] = mf * (2.0 * gr[d][d] - (2.0 / 3.0) * dv);
+            if (n == d) F[n] = mf * (T(2) * gr[d][d] - T(2.0 / 3.0) * dv);
             else F[n] = mf * (gr[d][n] + gr[n][d]);
         }
     };
     for (int f = tid; f < TNFX + TNFY + TNFZ; f += nthr) {
-        double F[3];
+        T F[3];
         if (f < TNFX) {
             const int fx = f % (TTX + 1), fy = (f / (TTX + 1)) % TTY, fz = f / ((TTX + 1) * TTY);
             flux(0, fx + 1, fy + 1, fz + 1, k0 + fz, F);
@@ -443,9 +455,10 @@ __global__ void __launch_bounds__(TTX* TTY* TTZ) k_divtau_tile(Grid g, const dou
         const int ax = (tz * TTY + ty) * (TTX + 1) + tx;
         const int ay = (tz * (TTY + 1) + ty) * TTX + tx;
         const int az = (tz * TTY + ty) * TTX + tx;
-        double acc = (sFx[n * TNFX + ax + 1] - sFx[n * TNFX + ax]) * ih[0];
-        acc += (sFy[n * TNFY + ay + TTX] - sFy[n * TNFY + ay]) * ih[1];
-        acc += (sFz[n * TNFZ + az + TTX * TTY] - sFz[n * TNFZ + az]) * ih[2];
+        T acc_t = (sFx[n * TNFX + ax + 1] - sFx[n * TNFX + ax]) * ih[0];
+        acc_t += (sFy[n * TNFY + ay + TTX] - sFy[n * TNFY + ay]) * ih[1];
+        acc_t += (sFz[n * TNFZ + az + TTX * TTY] - sFz[n * TNFZ + az]) * ih[2];
+        const double acc = (double)acc_t;
         const long long m = n * N + t;
         if (E.mode == 0) {
             out[m] = acc;
@@ -457,7 +470,7 @@ __global__ void __launch_bounds__(TTX* TTY* TTZ) k_divtau_tile(Grid g, const dou
         } else if (E.mode == 3) {
             out[m] = (rho * E.base[m] + dt * (0.5 * (E.conv_o[m] + E.conv_n[m]) + 0.5 * E.dold[m] + 0.5 * acc + E.src[m])) * irho;
         } else {
-            const double x = sV[n * TNH + hidx(tx + 1, ty + 1, tz + 1)];
+            const double x = (double)sV[n * TNH + hidx(tx + 1, ty + 1, tz + 1)];
             const double r = E.base[m] - rho * x + dt * acc;
             rmax = nmax(rmax, fabs(r));
             out[m] = E.mode == 7 ? x + E.omega * E.dinv[m] * r : r;
@@ -789,10 +802,13 @@ void launch_init_abl(Ctx& c, const Grid& g, double* vel, int loglaw, const doubl
 }
 void launch_fill(Ctx& c, double* p, double v, long long n) { KS_LAUNCH(c, k_fill, nblocks(n, BS), BS, B8 * n, p, v, n); }
 void launch_copy(Ctx& c, double* d, const double* s, long long n) { KS_LAUNCH(c, k_copy, nblocks(n, BS), BS, B8 * 2 * n, d, s, n); }
-void launch_smagorinsky(Ctx& c, const Grid& g, const double* vel, double* mueff, const Scalars& s, double* alpha) {
+void launch_smagorinsky(Ctx& c, const Grid& g, const double* vel, double* mueff, const Scalars& s, double* alpha, int fp32) {
     if (!s.temp) alpha = nullptr;
-    KS_LAUNCH(c, k_smag, nblocks(g.N, BS), BS, B8 * ((s.smag ? 4 : 1) + (alpha ? 1 : 0)) * g.N, g, vel, mueff, s.mu, s.rho, s.smag_fac, s.smag,
-              alpha, s.mu_pr, s.iprt);
+    const double bytes = B8 * ((s.smag ? 4 : 1) + (alpha ? 1 : 0)) * g.N;
+    if (fp32)
+        KS_LAUNCH(c, k_smag<float>, nblocks(g.N, BS), BS, bytes, g, vel, mueff, s.mu, s.rho, s.smag_fac, s.smag, alpha, s.mu_pr, s.iprt);
+    else
+        KS_LAUNCH(c, k_smag<double>, nblocks(g.N, BS), BS, bytes, g, vel, mueff, s.mu, s.rho, s.smag_fac, s.smag, alpha, s.mu_pr, s.iprt);
 }
 // src = rho (-gp/rho + geostrophic + Coriolis(u_old) + body + actuator + Boussinesq + ABLForcing)
 // (icns_ops.H:78-124, PDEOps.H:94-145, GeostrophicForcing.cpp:103-, CoriolisForcing.cpp:60-108,
@@ -811,7 +827,7 @@ void launch_sources(Ctx& c, const Grid& g, const double* vel_old, const double* 
     for (int n = 0; n < 3; ++n) {
         double a = 0.0;
         if (s.geo) a += (n == 2 ? s.hfac : 1.0) * s.gf[n];
-        if (s.body) a += s.body_force[n];
+        if (s.body) a += (s.body_osc ? std::cos(s.body_omega * s.t_nph) : 1.0) * s.body_force[n];
         if (s.ablf && n < 2) a += s.ablf_force[n];
         k.c[n] = s.rho * a;
         k.bous_g[n] = s.rho * s.grav[n] * s.beta_T;
@@ -845,28 +861,34 @@ void launch_divtau_faces(Ctx& c, const Grid& g, const double* vel, const double*
 }
 
 void launch_divtau(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, int mode,
-                   const double* src, double* forces, const double* base, const double* dold, double dt, double rho, double* const fl[9]) {
+                   const double* src, double* forces, const double* base, const double* dold, double dt, double rho, double* const fl[9],
+                   int fp32) {
     (void)fl;  // the tiled kernel keeps its face fluxes in shared memory
-    cudaFuncSetAttribute(k_divtau_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAU_SMEM);
     const dim3 grid((g.nx + TTX - 1) / TTX, (g.ny + TTY - 1) / TTY, (g.nz + TTZ - 1) / TTZ);
     const double per_cell = 4 + 3 + (mode == 1 ? 6 : 0) + (mode == 2 ? 6 : 0);
     TauEpi E{mode, src, base, dold, nullptr, nullptr, nullptr, forces, nullptr, dt, rho, 0.0, 1.0 / rho};
-    KS_LAUNCH_SMEM(c, k_divtau_tile, grid, TTX * TTY * TTZ, TAU_SMEM, B8 * per_cell * g.N, g, vel, mueff, wg, out, E);
+    if (fp32) {
+        cudaFuncSetAttribute(k_divtau_tile<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tau_smem<float>());
+        KS_LAUNCH_SMEM(c, k_divtau_tile<float>, grid, TTX * TTY * TTZ, tau_smem<float>(), B8 * per_cell * g.N, g, vel, mueff, wg, out, E);
+    } else {
+        cudaFuncSetAttribute(k_divtau_tile<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tau_smem<double>());
+        KS_LAUNCH_SMEM(c, k_divtau_tile<double>, grid, TTX * TTY * TTZ, tau_smem<double>(), B8 * per_cell * g.N, g, vel, mueff, wg, out, E);
+    }
 }
 void launch_divtau_corrector(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, const double* vel_old,
                              const double* conv_old, const double* conv_new, const double* dold, const double* src, double dt, double rho) {
-    cudaFuncSetAttribute(k_divtau_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAU_SMEM);
+    cudaFuncSetAttribute(k_divtau_tile<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tau_smem<double>());
     const dim3 grid((g.nx + TTX - 1) / TTX, (g.ny + TTY - 1) / TTY, (g.nz + TTZ - 1) / TTZ);
     TauEpi E{3, src, vel_old, dold, conv_old, conv_new, nullptr, nullptr, nullptr, dt, rho, 0.0, 1.0 / rho};
-    KS_LAUNCH_SMEM(c, k_divtau_tile, grid, TTX * TTY * TTZ, TAU_SMEM, B8 * 22.0 * g.N, g, vel, mueff, wg, out, E);
+    KS_LAUNCH_SMEM(c, k_divtau_tile<double>, grid, TTX * TTY * TTZ, tau_smem<double>(), B8 * 22.0 * g.N, g, vel, mueff, wg, out, E);
 }
 int divtau_tile_blocks(const Grid& g) { return ((g.nx + TTX - 1) / TTX) * ((g.ny + TTY - 1) / TTY) * ((g.nz + TTZ - 1) / TTZ); }
 void launch_divtau_jacobi(Ctx& c, const Grid& g, const double* x, const double* mueff, const double* wg, const double* b, const double* dinv,
                           double* out, double rho, double dtd, double omega, double* parts) {
-    cudaFuncSetAttribute(k_divtau_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAU_SMEM);
+    cudaFuncSetAttribute(k_divtau_tile<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tau_smem<double>());
     const dim3 grid((g.nx + TTX - 1) / TTX, (g.ny + TTY - 1) / TTY, (g.nz + TTZ - 1) / TTZ);
     TauEpi E{omega > 0.0 ? 7 : 8, nullptr, b, nullptr, nullptr, nullptr, dinv, nullptr, parts, dtd, rho, omega, 1.0 / rho};
-    KS_LAUNCH_SMEM(c, k_divtau_tile, grid, TTX * TTY * TTZ, TAU_SMEM, B8 * ((omega > 0.0 ? 13.0 : 10.0) * g.N), g, x, mueff, wg, out, E);
+    KS_LAUNCH_SMEM(c, k_divtau_tile<double>, grid, TTX * TTY * TTZ, tau_smem<double>(), B8 * ((omega > 0.0 ? 13.0 : 10.0) * g.N), g, x, mueff, wg, out, E);
 }
 void launch_predictor_rhs(Ctx& c, const Grid& g, const double* vo, const double* conv, const double* src, const double* dtau, double* vel,
                           double dt, double rho, double fac) {

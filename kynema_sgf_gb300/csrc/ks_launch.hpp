@@ -114,6 +114,10 @@ struct Scalars {  // values fed to the pointwise kernels
     double east[3], north[3], up[3];
     double corfac, sinphi, cosphi, hfac;
     double body_force[3];
+    // BodyForce type oscillatory: body_force * cos(body_omega t_nph), t_nph the
+    // mid-step time (BodyForce.cpp:145-160); body_osc = 0: uniform_constant
+    int body_osc;
+    double body_omega, t_nph;
     // temperature: alpha_eff = mu / Pr + mu_t / Pr_t; BoussinesqBuoyancy g beta (T0 - T); ABLForcing
     int temp, bous, ablf;
     double mu_pr, iprt;
@@ -126,7 +130,8 @@ void launch_init_tgv(Ctx& c, const Grid& g, double* vel, const double plo[3], co
 void launch_init_abl(Ctx& c, const Grid& g, double* vel, int loglaw, const double U[3], double ut_over_kappa, double z0,
                      double amp, double zmax_rel, unsigned long long seed);
 // mu_eff (and alpha_eff when s.temp is set and alpha is not null)
-void launch_smagorinsky(Ctx& c, const Grid& g, const double* vel, double* mueff, const Scalars& s, double* alpha = nullptr);
+// fp32 = 1: strain rate in FP32 arithmetic (mixed-precision form), mu_eff stored in FP64
+void launch_smagorinsky(Ctx& c, const Grid& g, const double* vel, double* mueff, const Scalars& s, double* alpha = nullptr, int fp32 = 0);
 void launch_fill(Ctx& c, double* p, double v, long long n);
 void launch_copy(Ctx& c, double* dst, const double* src, long long n);
 // src = rho (-gp / rho + sources); theta: the temperature state BoussinesqBuoyancy reads
@@ -138,9 +143,10 @@ void launch_wall_grad(Ctx& c, const Grid& g, const double* vel_old, const double
 // out = divtau(vel) ; mode 0: plain, mode 1: forces = (src + divtau)/rho also written,
 // mode 2: out = base + 0.5*dt*(divtau(vel) - dold)/rho (RK2 correction into out).
 // Fused shared-memory tiles; face_scratch is not used.
+// fp32 = 1 (modes 0-2): staging, face fluxes and divergence in FP32 (mixed-precision form), epilogue in FP64
 void launch_divtau(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, int mode,
                    const double* src, double* forces, const double* base, const double* dold, double dt, double rho,
-                   double* const face_scratch[9]);
+                   double* const face_scratch[9], int fp32 = 0);
 // the same result through face-flux arrays in caller-provided scratch (9 arrays:
 // N cells for x and y faces, nx*ny*(nz+1) for z faces) and a divergence pass
 void launch_divtau_faces(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, double* out, int mode,

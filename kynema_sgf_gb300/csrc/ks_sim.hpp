@@ -106,7 +106,7 @@ class Deck {
 // ---------------------------------------------------------------- SimTime
 // src/core/SimTime.cpp:11-324 semantics for the keys on this path.
 struct Clock {
-    double cur = 0, next = 0, dt[3] = {-1, -1, -1};
+    double cur = 0, next = 0, dt[3] = {0, 0, 0};  // SimTime::m_dt starts at 0 (SimTime.H:194-195)
     double cfl = 1, fixed_dt = -1, init_dt = -1, max_dt = -1, min_dt = -1, shrink = 0.1, growth = 0.1, stop = -1;
     int max_step = -1, step = 0;
     bool adaptive = false, init = true, force_cfl = true;
@@ -235,6 +235,7 @@ class Sim {
     ~Sim();
 
     void init_data();
+    void sources(const double* vel, const double* theta);
     void compute_dt();
     void pre_advance();
     void prepare_time_step();

@@ -199,7 +199,7 @@ struct MGOpts {
 };
 
 struct SimTime {
-    double cur = 0, newt = 0, dt[3] = {-1, -1, -1};
+    double cur = 0, newt = 0, dt[3] = {0, 0, 0};  // SimTime::m_dt starts at 0 (SimTime.H:194-195)
     double max_cfl = 1, fixed_dt = -1, init_dt = -1, max_dt = -1, min_dt = -1;
     double init_shrink = 0.1, growth = 0.1, stop_time = -1, dt_calc = 0;
     int max_step = -1, step = 0;
@@ -274,6 +274,8 @@ struct Sim {
     double east[3] = {1, 0, 0}, north[3] = {0, 1, 0}, up[3] = {0, 0, 1};
     bool cor_horizontal = false;
     double geo_wind[3] = {0, 0, 0}, body_force[3] = {0, 0, 0};
+    bool body_osc = false;
+    double body_omega = 0;
     double kappa = 0.41, z0 = 0.1;
     std::string shear_type = "moeng";
     double utau = 0, umean[2] = {0, 0}, vmag_mean = 0, zref = 0;
@@ -331,6 +333,8 @@ struct Sim {
     int step_once();
     double ke() const;
     double divu(double* umax) const;
+    void predictor_rhs(double dt, double fac);
+    void explicit_rk2_post_hoc(double dt, const Arr& d);
     double mac_divu(double* umax) const;
 };
 
@@ -407,8 +411,15 @@ void Sim::setup(const std::string& text) {
     cor_horizontal = D.i("CoriolisForcing.is_horizontal", 0) != 0;
     if (src_geo) { auto w = D.v("GeostrophicForcing.geostrophic_wind"); for (int d = 0; d < 3; ++d) geo_wind[d] = w.at(d); }
     if (src_body) {
-        if (lower(D.s("BodyForce.type", "constant")) != "constant") throw Error(ERR_UNSUPPORTED, "BodyForce.type");
+        // BodyForce::BodyForce (src/equation_systems/icns/source_terms/BodyForce.cpp:20-58):
+        // uniform_constant (default) or oscillatory with angular_frequency
+        const std::string bt = lower(D.s("BodyForce.type", "uniform_constant"));
+        if (bt == "height_varying" || bt == "height-varying" || bt == "uniform_timetable" || D.has("BodyForce.uniform_timetable_file"))
+            throw Error(ERR_UNSUPPORTED, "BodyForce.type " + bt);
+        if (bt != "uniform_constant" && bt != "oscillatory") throw Error(ERR_DECK, "BodyForce.type " + bt);
         auto m = D.v("BodyForce.magnitude"); for (int d = 0; d < 3; ++d) body_force[d] = m.at(d);
+        body_osc = bt == "oscillatory";
+        if (body_osc) body_omega = D.v("BodyForce.angular_frequency").at(0);
     }
     kappa = D.d("ABL.kappa", 0.41);
     z0 = D.d("ABL.surface_roughness_z0", 0.1);
@@ -742,6 +753,9 @@ void Sim::compute_sources(const Arr& v, const Arr* th) {
     const double gf[3] = {-geo_cf * geo_wind[1], geo_cf * geo_wind[0], 0.0};
     const double hfac = cor_horizontal ? 0.0 : 1.0;
     const double corfac = 2 * omega;
+    // BodyForce::operator() (BodyForce.cpp:117-169): the oscillatory type scales
+    // the magnitude by cos(omega t) at t = (current + new time) / 2
+    const double bcoef = body_osc ? std::cos(body_omega * 0.5 * (t.cur + t.newt)) : 1.0;
 #pragma omp parallel for collapse(2)
     for (int k = 0; k < nz; ++k)
         for (int j = 0; j < ny; ++j)
@@ -761,7 +775,7 @@ void Sim::compute_sources(const Arr& v, const Arr* th) {
                     for (int n = 0; n < 3; ++n) s[n] += ae * east[n] + an * north[n] + au * up[n];
                 }
                 if (src_body)
-                    for (int n = 0; n < 3; ++n) s[n] += body_force[n];
+                    for (int n = 0; n < 3; ++n) s[n] += bcoef * body_force[n];
                 if (src_act)
                     for (int n = 0; n < 3; ++n) s[n] += act_src(i, j, k, n);
                 if (src_bous) {  // BoussinesqBuoyancy.cpp:22-50: g beta (T0 - T)
@@ -2189,26 +2203,46 @@ void Sim::apply_predictor(bool incremental) {
     // theta at n+1/2; compute_diffusion_term(Old) reproduces divtau.
     compute_sources(vel_old, has_temp ? &theta_nph : nullptr);
     // predictor_rhs (CompRHSOps.H:32-141): diffusion factor 1 explicit, 1/2 Crank-Nicolson, 0 implicit
-    const double fac = diff_type == 0 ? 1.0 : (diff_type == 1 ? 0.5 : 0.0);
+    predictor_rhs(dt, diff_type == 0 ? 1.0 : (diff_type == 1 ? 0.5 : 0.0));
+    if (diff_type != 0) {  // icns().solve(dt_diff), incflo_advance.cpp:376-386
+        diffuse_solve(diff_type == 2 ? dt : 0.5 * dt);
+        nodal_project(t.newt, dt, incremental);
+        return;
+    }
+    // explicit RK2 correction (incflo_advance.cpp:388-400): divtau(New) - divtau(Old), then
+    // improve_explicit_diffusion
+    divtau_op(vel, divtau_new);
+    for (int n = 0; n < 3; ++n)
+#pragma omp parallel for collapse(2)
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) divtau_new(i, j, k, n) = divtau_new(i, j, k, n) - divtau(i, j, k, n);
+    explicit_rk2_post_hoc(dt, divtau_new);
+    nodal_project(incremental ? t.newt : t.newt, dt, incremental);
+}
+
+// ComputeRHSOp::predictor_rhs (src/equation_systems/CompRHSOps.H:32-141) for
+// the explicit / Crank-Nicolson / implicit diffusion factor fac (1, 1/2, 0),
+// constant density: u = (rho u_old + dt (conv + src + fac divtau)) / rho.
+void Sim::predictor_rhs(double dt, double fac) {
+    const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
     for (int n = 0; n < 3; ++n)
 #pragma omp parallel for collapse(2)
         for (int k = 0; k < nz; ++k)
             for (int j = 0; j < ny; ++j)
                 for (int i = 0; i < nx; ++i)
                     vel(i, j, k, n) = (rho * vel_old(i, j, k, n) + dt * (conv(i, j, k, n) + src(i, j, k, n) + fac * divtau(i, j, k, n))) / rho;
-    if (diff_type != 0) {  // icns().solve(dt_diff), incflo_advance.cpp:376-386
-        diffuse_solve(diff_type == 2 ? dt : 0.5 * dt);
-        nodal_project(t.newt, dt, incremental);
-        return;
-    }
-    // explicit RK2 correction (incflo_advance.cpp:388-400, CompRHSOps.H:267-300)
-    divtau_op(vel, divtau_new);
+}
+
+// ComputeRHSOp::explicit_rk2_post_hoc (src/equation_systems/CompRHSOps.H:267-300):
+// d holds divtau(New) - divtau(Old); u += 1/2 dt d / rho.
+void Sim::explicit_rk2_post_hoc(double dt, const Arr& d) {
+    const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
     for (int n = 0; n < 3; ++n)
 #pragma omp parallel for collapse(2)
         for (int k = 0; k < nz; ++k)
             for (int j = 0; j < ny; ++j)
-                for (int i = 0; i < nx; ++i) vel(i, j, k, n) += 0.5 * dt * (divtau_new(i, j, k, n) - divtau(i, j, k, n)) / rho;
-    nodal_project(incremental ? t.newt : t.newt, dt, incremental);
+                for (int i = 0; i < nx; ++i) vel(i, j, k, n) += 0.5 * dt * d(i, j, k, n) / rho;
 }
 
 // ---- MOL scheme -------------------------------------------------------------------------------
@@ -2714,6 +2748,12 @@ int kso_compute_divtau(void* h, int use_new) {
 }
 
 int kso_compute_sources(void* h) { return guard(h, [](Sim& s) { s.compute_sources(s.vel_old); return 0; }); }
+
+int kso_predictor_rhs(void* h, double fac) { return guard(h, [&](Sim& s) { s.predictor_rhs(s.t.dt[0], fac); return 0; }); }
+
+int kso_improve_explicit_diffusion(void* h) {
+    return guard(h, [](Sim& s) { s.explicit_rk2_post_hoc(s.t.dt[0], s.divtau); return 0; });
+}
 
 int kso_field_shape(void* h, const char* name, int* nc, int* nx, int* ny, int* nz) {
     return guard(h, [&](Sim& s) {

@@ -44,6 +44,12 @@ int kso_set_scalar(void* h, const char* name, double value);
 int kso_update_mueff(void* h);
 int kso_compute_divtau(void* h, int use_new_state);
 int kso_compute_sources(void* h);
+/* predictor_rhs with diffusion factor fac and dt = the clock's dt (velocity
+ * from velocity_old, conv_term, src_term, diff_term). */
+int kso_predictor_rhs(void* h, double fac);
+/* explicit_rk2_post_hoc: velocity += dt/2 diff_term / rho, diff_term holding
+ * divtau(New) - divtau(Old) (the caller sets it). */
+int kso_improve_explicit_diffusion(void* h);
 
 #ifdef __cplusplus
 }

@@ -48,6 +48,8 @@ def load():
         lib.kso_apply_predictor.argtypes = [vp, ip, ip]
         lib.kso_apply_projection.argtypes = [vp, dp, dp, ip]
         lib.kso_compute_divtau.argtypes = [vp, ip]
+        lib.kso_predictor_rhs.argtypes = [vp, dp]
+        lib.kso_improve_explicit_diffusion.argtypes = [vp]
         lib.kso_field_shape.argtypes = [vp, ctypes.c_char_p] + [ctypes.POINTER(ip)] * 4
         lib.kso_get_field.argtypes = [vp, ctypes.c_char_p, vp]
         lib.kso_set_field.argtypes = [vp, ctypes.c_char_p, vp]
@@ -124,6 +126,12 @@ class Oracle:
 
     def compute_divtau(self, use_new_state=False):
         self._check(self._lib.kso_compute_divtau(self._h, int(bool(use_new_state))))
+
+    def predictor_rhs(self, fac=1.0):
+        self._check(self._lib.kso_predictor_rhs(self._h, float(fac)))
+
+    def improve_explicit_diffusion(self):
+        self._check(self._lib.kso_improve_explicit_diffusion(self._h))
 
     def layout(self, name):
         v = [ctypes.c_int() for _ in range(4)]

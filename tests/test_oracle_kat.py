@@ -246,3 +246,205 @@ def test_maxiter_reports_not_converged(oracle_mod):
     with pytest.raises(oracle_mod.OracleError) as e:
         o.InitData()
     assert e.value.code == 3
+
+
+def body_force_deck(btype="oscillatory", extra=""):
+    return box_deck(n=(8, 8, 8), extra="ICNS.source_terms = BodyForce\nincflo.density = 1.0\nBodyForce.type = %s\n"
+                                        "BodyForce.magnitude = 1.0 2.0 3.0\nBodyForce.angular_frequency = 1.0\n%s" % (btype, extra))
+
+
+def test_body_force_gold(oracle_mod):
+    """unit_tests/wind_energy/test_abl_src.cpp:115-160 (parameters of
+    abl_test_utils.cpp:40-47): oscillatory BodyForce, magnitude (1, 2, 3),
+    angular frequency 1: (1, 2, 3) at t = 0, then (1, 2, 3) cos(0.5 (0.05 +
+    t_new)) with the current time 0.05 (BodyForce.cpp:117-169 evaluates at
+    the mid-step time)."""
+    tol = 1.0e4 * EPS
+    o = oracle_mod.Oracle(body_force_deck())
+    o.compute_sources()
+    src = o.get_field("src_term")
+    for n, gold in enumerate((1.0, 2.0, 3.0)):
+        assert np.allclose(src[n], gold, rtol=0, atol=tol)
+    o.set_scalar("time", 0.05)
+    o.set_scalar("new_time", 0.15)
+    o.compute_sources()
+    src = o.get_field("src_term")
+    for n, mag in enumerate((1.0, 2.0, 3.0)):
+        assert np.allclose(src[n], mag * math.cos(0.5 * (0.05 + 0.15)), rtol=0, atol=tol)
+
+
+def test_body_force_types(oracle_mod):
+    """uniform_constant (the default) ignores the time; the reference aborts
+    on any other name (BodyForce.cpp:47-56) and the file-driven types are
+    outside this path."""
+    o = oracle_mod.Oracle(body_force_deck("uniform_constant"))
+    o.set_scalar("time", 3.0)
+    o.set_scalar("new_time", 4.0)
+    o.compute_sources()
+    src = o.get_field("src_term")
+    for n, gold in enumerate((1.0, 2.0, 3.0)):
+        assert np.allclose(src[n], gold, rtol=0, atol=1.0e4 * EPS)
+    with pytest.raises(oracle_mod.OracleError) as e:
+        oracle_mod.Oracle(body_force_deck("constant"))
+    assert e.value.code == 1
+    with pytest.raises(oracle_mod.OracleError) as e:
+        oracle_mod.Oracle(body_force_deck("height_varying"))
+    assert e.value.code == 2
+
+
+def hydrostatic_deck(n=(4, 4, 16)):
+    return box_deck(n=n, hi=(1.0, 1.0, 1.0), periodic=(1, 1, 0),
+                    extra="zlo.type = slip_wall\nzhi.type = slip_wall\nincflo.density = 1.0\ntransport.viscosity = 0.0\n"
+                          "nodal_proj.mg_rtol = 1e-13\nnodal_proj.mg_atol = 1e-14")
+
+
+def hydrostatic_column(sim, w0=-9.81):
+    """unit_tests/projection/test_pressure_offset.cpp:173-203 restated for a
+    column closed at both ends: a uniform vertical velocity w0 (the velocity
+    gravity F_g = w0 would produce in one unit step) projected with dt = 1 at
+    time 1.  The projected velocity vanishes and the pressure carries the
+    hydrostatic difference p(bottom) - p(top) = -F_g over the unit column (the
+    reference's pressure_outflow top pins p(top) = 0 and checks p(bottom) =
+    -F_g to 1e8 eps); gp_z = F_g."""
+    v = np.zeros(sim.layout("velocity"))
+    v[2] = w0
+    for f in ("velocity", "velocity_old"):
+        sim.set_field(f, v if f == "velocity" else np.zeros_like(v))
+    sim.set_field("gp", np.zeros(sim.layout("gp")))
+    sim.ApplyProjection(1.0, 1.0, False)
+    p = sim.get_field("p")[0]
+    tol = 1.0e8 * EPS
+    assert np.abs(sim.get_field("velocity")).max() < tol
+    assert abs((p[0].mean() - p[-1].mean()) - (-w0)) < tol
+    assert np.abs(p[0] - p[0].mean()).max() < tol  # every bottom node alike
+    gp = sim.get_field("gp")
+    assert np.allclose(gp[2], w0, rtol=0, atol=tol) and np.abs(gp[:2]).max() < tol
+
+
+def test_pressure_offset_hydrostatic_column(oracle_mod):
+    hydrostatic_column(oracle_mod.Oracle(hydrostatic_deck()))
+
+
+def rk2_deck():
+    return box_deck(n=(8, 8, 16), hi=(1.0, 1.0, 1.0), extra="incflo.density = 2.0\ntransport.viscosity = 0.1\ntime.fixed_dt = 0.5")
+
+
+def rk2_scalar(shape):
+    # init_scalar of unit_tests/equation_systems/test_explicit_diffusion_rk2.cpp:15-31
+    nc, nz, ny, nx = shape
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    f = 1.0 + i * i + 0.2 * (j - 1) * (j - 1) + 0.01 * (k + 1) ** 3
+    return np.broadcast_to(f, shape).copy()
+
+
+@pytest.mark.parametrize("approach", ["old", "correct"])
+def test_explicit_diffusion_rk2(oracle_mod, approach):
+    """unit_tests/equation_systems/test_explicit_diffusion_rk2.cpp:116-184
+    (rho 2, mu 0.1, dt 0.5, 8 x 8 x 16): predictor_rhs with only the explicit
+    diffusion term gives u_old + dt D / rho.  old: subtracting dt D does not
+    return u_old (error above 10 FP32 eps).  correct: with the diffusion term
+    replaced by -2 D, improve_explicit_diffusion (explicit_rk2_post_hoc,
+    u += dt/2 diff / rho) returns u_old to 1e4 eps."""
+    o = oracle_mod.Oracle(rk2_deck())
+    o.set_scalar("dt", 0.5)
+    f = rk2_scalar(o.layout("velocity_old"))
+    o.set_field("velocity_old", f)
+    o.compute_divtau()
+    D = o.get_field("diff_term")
+    assert np.abs(D).max() > 1.0e4 * EPS
+    o.set_field("conv_term", np.zeros_like(D))
+    o.set_field("src_term", np.zeros_like(D))
+    o.predictor_rhs(1.0)
+    u = o.get_field("velocity")
+    assert np.allclose(u, f + 0.5 * D / 2.0, rtol=0, atol=1.0e4 * EPS * np.abs(f).max())
+    if approach == "old":
+        assert np.abs(u - 0.5 * D - f).max() > 10 * np.finfo(np.float32).eps
+    else:
+        o.set_field("diff_term", -2.0 * D)
+        o.improve_explicit_diffusion()
+        assert np.abs(o.get_field("velocity") - f).max() < 1.0e4 * EPS
+
+
+def wall_model_deck(stress="local", fixed_dt=0.1, extra=""):
+    # unit_tests/wind_energy/test_abl_bc.cpp:69-170 on the default test mesh (8^3 cells on [0, 8]^3)
+    return box_deck(n=(8, 8, 8), hi=(8.0, 8.0, 8.0), periodic=(1, 1, 0),
+                    extra=f"zlo.type = wall_model\nzhi.type = slip_wall\nincflo.physics = FreeStream\nincflo.velocity = 5.0 0.0 0.0\n"
+                          f"incflo.density = 1.0\ntransport.viscosity = 0.01\nturbulence.model = Laminar\ntime.fixed_dt = {fixed_dt}\n"
+                          f"ABL.wall_shear_stress_type = {stress}\nABL.kappa = 0.4\nABL.surface_roughness_z0 = 0.11\n"
+                          f"incflo.do_initial_proj = 0\nincflo.initial_iterations = 0\n{extra}")
+
+
+def wall_model_gold(vval=5.0, dz=1.0, kappa=0.4, z0=0.11):
+    utau = kappa * vval / math.log(0.5 * dz / z0)
+    return utau, utau ** 2
+
+
+@pytest.mark.parametrize("stress", ["local", "moeng"])
+def test_abl_wall_model_gold(oracle_mod, stress):
+    """unit_tests/wind_energy/test_abl_bc.cpp:69-170: uniform u = 5 over a
+    wall-model bottom (kappa 0.4, z0 0.11, mu 0.01, dt 0.1): the explicit
+    diffusion term of the first layer is -tau_wall / dz with tau_wall =
+    u_tau^2, u_tau = kappa U / ln(z_ref / z0), so predictor_rhs with only
+    diffusion gives u = 5 - dt tau_wall / dz there (and leaves every other
+    cell at 5).  For a uniform field the Moeng stress equals the local one."""
+    o = oracle_mod.Oracle(wall_model_deck(stress))
+    o.InitData()
+    o.set_scalar("dt", 0.1)
+    o.pre_advance()
+    utau, tau = wall_model_gold()
+    assert abs(o.scalar("utau") - utau) < 1.0e4 * EPS
+    o.prepare_time_step()
+    o.update_mueff()
+    o.compute_divtau()
+    D = o.get_field("diff_term")
+    assert np.allclose(D[0, 0], -tau, rtol=0, atol=1.0e4 * EPS)
+    assert np.abs(D[0, 1:]).max() < 1.0e4 * EPS and np.abs(D[1:]).max() < 1.0e4 * EPS
+    o.set_field("conv_term", np.zeros_like(D))
+    o.set_field("src_term", np.zeros_like(D))
+    o.predictor_rhs(1.0)
+    u = o.get_field("velocity")
+    assert np.allclose(u[0, 0], 5.0 - 0.1 * tau, rtol=0, atol=1.0e4 * EPS)
+    assert np.allclose(u[0, 1:], 5.0, rtol=0, atol=1.0e4 * EPS)
+
+
+def quadratic_velocity(shape, L):
+    """Velocity quadratic in z with w = 0 on both walls (z = 0, L)."""
+    nc, nz, ny, nx = shape
+    z = (np.arange(nz) + 0.5) * (L / nz)
+    v = np.zeros(shape)
+    v[0] = (0.3 * z * z + 0.7 * z + 1.0)[:, None, None]
+    v[1] = (-0.2 * z * z + 0.1 * z)[:, None, None]
+    v[2] = (0.05 * z * (L - z))[:, None, None]
+    return v
+
+
+def quadratic_strain_mueff(shape, L, Cs, dx):
+    nc, nz, ny, nx = shape
+    z = (np.arange(nz) + 0.5) * (L / nz)
+    dudz, dvdz, dwdz = 0.6 * z + 0.7, -0.4 * z + 0.1, 0.05 * (L - 2 * z)
+    s = np.sqrt(2.0 * dwdz ** 2 + dudz ** 2 + dvdz ** 2)
+    return (Cs ** 2 * np.cbrt(dx[0] * dx[1] * dx[2]) ** 2 * s)[:, None, None] * np.ones((nz, ny, nx))
+
+
+def quadratic_deck(n=(4, 4, 16), L=4.0):
+    return box_deck(n=n, hi=(1.0, 1.0, L), periodic=(1, 1, 0),
+                    extra="zlo.type = slip_wall\nzhi.type = slip_wall\nturbulence.model = Smagorinsky\nSmagorinsky_coeffs.Cs = 0.16\n"
+                          "transport.viscosity = 0.0\nincflo.density = 1.0")
+
+
+def test_strain_rate_exact_for_quadratics(oracle_mod):
+    """unit_tests/fvm/test_fvm_operators.cpp:258-341 checks the FVM gradient
+    on degree-2 polynomials with wall ghosts holding the wall values; on this
+    path the strain rate (fvm::StrainRate, central interior stencils and the
+    one-sided wall stencils of stencils.H:166-330) sees the fill-patch ghosts
+    (hoextrap (15 q0 - 10 q1 + 3 q2) / 8, which is the wall value of a
+    quadratic, and w = 0), so |S| of a quadratic profile is exact in every
+    cell, wall cells included."""
+    n, L = (4, 4, 16), 4.0
+    o = oracle_mod.Oracle(quadratic_deck(n, L))
+    shape = o.layout("velocity_old")
+    o.set_field("velocity_old", quadratic_velocity(shape, L))
+    o.update_mueff()
+    dx = (1.0 / n[0], 1.0 / n[1], L / n[2])
+    mu = o.get_field("velocity_mueff")[0]
+    assert np.allclose(mu, quadratic_strain_mueff(shape, L, 0.16, dx), rtol=1.0e6 * EPS, atol=0)
