@@ -11,6 +11,7 @@
 // reflections or the wall-model shift for diffusion, and replaces wall-face
 // states (zbc); the reverse scatters every ghost read back onto the interior
 // cells it was built from.
+#include "ks_decide.cuh"
 #include "ks_launch.hpp"
 
 namespace ks {
@@ -37,9 +38,11 @@ __device__ inline bool face_at(const Grid& g, int d, long long t, int& i, int& j
 }
 inline long long nfaces(const Grid& g, int d) { return (long long)g.nx * g.ny * (d == 2 ? nzfaces(g) : g.nz); }
 
-// velocity read with the Godunov fill-patch ghosts (VelFPT, scale 1) and its adjoint
-__device__ inline double Q(const Grid& g, const double* u, int n, int i, int j, int k) {
-    const VelFPT<double> q{u, g, 1.0};
+// velocity read with the Godunov fill-patch ghosts (VelFPT, scale 1) in the
+// arithmetic type A of the pass, and its adjoint (FP64 accumulation)
+template <typename A = double>
+__device__ inline A Q(const Grid& g, const double* u, int n, int i, int j, int k) {
+    const VelFPT<A, double> q{u, g, A(1)};
     return q(n, i, j, k);
 }
 __device__ inline void Qb(const Grid& g, double* ub, int n, int i, int j, int k, double v) {
@@ -63,76 +66,82 @@ __device__ inline void Qb(const Grid& g, double* ub, int n, int i, int j, int k,
 }
 
 // wall-face state replacement of the forward (zbc) and its adjoint
-__device__ inline void zbc_fwd(const Grid& g, int k, int n, double& lo, double& hi) {
+template <typename A>
+__device__ inline void zbc_fwd(const Grid& g, int k, int n, A& lo, A& hi) {
     if (g.zper) return;
     if (k == 0) {
-        if (n == 2) lo = hi = 0.0; else lo = hi;
+        if (n == 2) lo = hi = A(0); else lo = hi;
     } else if (k == g.nz) {
-        if (n == 2) lo = hi = 0.0; else hi = lo;
+        if (n == 2) lo = hi = A(0); else hi = lo;
     }
 }
-__device__ inline void zbc_rev(const Grid& g, int k, int n, double& lb, double& hb) {
+template <typename A>
+__device__ inline void zbc_rev(const Grid& g, int k, int n, A& lb, A& hb) {
     if (g.zper) return;
     if (k == 0) {
         if (n == 2) {
-            lb = hb = 0.0;
+            lb = hb = A(0);
         } else {
             hb += lb;
-            lb = 0.0;
+            lb = A(0);
         }
     } else if (k == g.nz) {
         if (n == 2) {
-            lb = hb = 0.0;
+            lb = hb = A(0);
         } else {
             lb += hb;
-            hb = 0.0;
+            hb = A(0);
         }
     }
 }
 
-// ---- van Leer slope: value and the coefficients of (a, b, c)
-__device__ inline double vls_d(double a, double b, double c, double& ca, double& cb, double& cc) {
-    const double dsc = 0.5 * (c - a), dsl = 2.0 * (b - a), dsr = 2.0 * (c - b);
-    ca = cb = cc = 0.0;
-    if (!isame_sign(dsl, dsr)) return 0.0;
-    // magnitudes compared on the integer pipe (non-negative doubles order like their bits)
-    const long long ac = dbits(dsc) & kMag, al = dbits(dsl) & kMag, ar = dbits(dsr) & kMag;
-    if (ac <= (al < ar ? al : ar)) {
-        ca = -0.5;
-        cc = 0.5;
+// ---- van Leer slope (the forward's vls, ks_godunov.cu): value and the
+// coefficients of (a, b, c), with the forward's branch order
+template <typename A>
+__device__ inline A vls_d(A a, A b, A c, A& ca, A& cb, A& cc) {
+    const A dsc = A(0.5) * (c - a), dsl = A(2) * (b - a), dsr = A(2) * (c - b);
+    ca = cb = cc = A(0);
+    if (!same_sign(dsl, dsr)) return A(0);
+    const bool left = abs_lt(dsl, dsr);  // forward: m = |dsl| < |dsr| ? dsl : dsr
+    if (abs_lt(dsc, left ? dsl : dsr)) {
+        ca = A(-0.5);
+        cc = A(0.5);
         return dsc;
     }
-    if (al <= ar) {
-        ca = -2.0;
-        cb = 2.0;
+    if (left) {
+        ca = A(-2);
+        cb = A(2);
         return dsl;
     }
-    cb = -2.0;
-    cc = 2.0;
+    cb = A(-2);
+    cc = A(2);
     return dsr;
 }
 
 // adjoint of clip(e, a, b) = min(max(e, min(a, b)), max(a, b)) given the
 // adjoint of the result: returns the adjoint of e; adds to those of a, b.
-// The selections order -0 below +0 (the integer-pipe comparisons of
-// ks_common.cuh), as the forward clip does, so a signed-zero tie routes the
-// adjoint to the operand the forward selected.
-__device__ inline double clip_rev(double e, double a, double b, double rb, double& ga, double& gb) {
-    const double lo = imin(a, b), hi = imax(a, b);
-    if (ilt(hi, imax(e, lo))) {
-        if (!ilt(a, b)) ga += rb; else gb += rb;
-        return 0.0;
+// The selections are the forward's (ks_decide.cuh): for FP64 they order -0
+// below +0, so a signed-zero tie routes the adjoint to the operand the
+// forward selected.
+template <typename A>
+__device__ inline A clip_rev(A e, A a, A b, A rb, A& ga, A& gb) {
+    const A lo = min2(a, b), hi = max2(a, b);
+    if (lt(hi, max2(e, lo))) {
+        if (!lt(a, b)) ga += rb; else gb += rb;
+        return A(0);
     }
-    if (ilt(e, lo)) {
-        if (!ilt(b, a)) ga += rb; else gb += rb;
-        return 0.0;
+    if (lt(e, lo)) {
+        if (!lt(b, a)) ga += rb; else gb += rb;
+        return A(0);
     }
     return rb;
 }
 
-// ---- reverse of the unlimited PPM edges on d-faces (k_edges)
+// ---- reverse of the unlimited PPM edges on d-faces (k_edges).  TI is the
+// forward's precision and the arithmetic type of the reverse pass.
 template <typename TI>
 __global__ void k_adj_edges(Grid g, int d, const double* u, const double* Eb0, const double* Eb1, const double* Eb2, double* ub) {
+    using A = TI;
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_at(g, d, t, i, j, k)) return;
@@ -140,37 +149,38 @@ __global__ void k_adj_edges(Grid g, int d, const double* u, const double* Eb0, c
     const bool wall = (d == 2 && !g.zper);
     const double* Eb[3] = {Eb0, Eb1, Eb2};
     for (int n = 0; n < 3; ++n) {
-        const double eb = Eb[n][t];
-        if (!(dbits(eb) & kMag)) continue;
+        const double eb64 = Eb[n][t];
+        if (!(dbits(eb64) & kMag)) continue;
         if (wall && (k == 0 || k == g.nz)) {  // the wall face takes the ghost value
-            Qb(g, ub, n, i, j, k == 0 ? -1 : g.nz, eb);
+            Qb(g, ub, n, i, j, k == 0 ? -1 : g.nz, eb64);
             continue;
         }
+        const A eb = (A)eb64;
         if (wall && (k == 1 || k == g.nz - 1)) {  // one-sided fourth order, clipped to the adjacent cells
             const int kb = (k == 1) ? -1 : g.nz, k0 = (k == 1) ? 0 : g.nz - 1, s = (k == 1) ? 1 : -1;
-            const double b = (TI)Q(g, u, n, i, j, kb), q0 = (TI)Q(g, u, n, i, j, k0), q1 = (TI)Q(g, u, n, i, j, k0 + s),
-                         q2 = (TI)Q(g, u, n, i, j, k0 + 2 * s);
-            const double e = -0.2 * b + 0.75 * q0 + 0.5 * q1 - 0.05 * q2;
-            double g0 = 0.0, g1 = 0.0;
-            const double ebar = clip_rev(e, q0, q1, eb, g0, g1);
-            Qb(g, ub, n, i, j, kb, -0.2 * ebar);
-            Qb(g, ub, n, i, j, k0, 0.75 * ebar + g0);
-            Qb(g, ub, n, i, j, k0 + s, 0.5 * ebar + g1);
-            Qb(g, ub, n, i, j, k0 + 2 * s, -0.05 * ebar);
+            const A b = Q<A>(g, u, n, i, j, kb), q0 = Q<A>(g, u, n, i, j, k0), q1 = Q<A>(g, u, n, i, j, k0 + s),
+                    q2 = Q<A>(g, u, n, i, j, k0 + 2 * s);
+            const A e = A(-0.2) * b + A(0.75) * q0 + A(0.5) * q1 - A(0.05) * q2;
+            A g0 = A(0), g1 = A(0);
+            const A ebar = clip_rev(e, q0, q1, eb, g0, g1);
+            Qb(g, ub, n, i, j, kb, (double)(A(-0.2) * ebar));
+            Qb(g, ub, n, i, j, k0, (double)(A(0.75) * ebar + g0));
+            Qb(g, ub, n, i, j, k0 + s, (double)(A(0.5) * ebar + g1));
+            Qb(g, ub, n, i, j, k0 + 2 * s, (double)(A(-0.05) * ebar));
             continue;
         }
-        const double am = (TI)Q(g, u, n, i - 2 * di, j - 2 * dj, k - 2 * dk), a0 = (TI)Q(g, u, n, i - di, j - dj, k - dk);
-        const double a1 = (TI)Q(g, u, n, i, j, k), a2 = (TI)Q(g, u, n, i + di, j + dj, k + dk);
-        double c1a, c1b, c1c, c0a, c0b, c0c;
-        const double s1 = vls_d(a0, a1, a2, c1a, c1b, c1c);
-        const double s0 = vls_d(am, a0, a1, c0a, c0b, c0c);
-        const double e = 0.5 * (a0 + a1) - (1.0 / 6.0) * (s1 - s0);
-        double gm = 0.0, g0 = 0.0, g1 = 0.0, g2 = 0.0;
-        const double ebar = clip_rev(e, a0, a1, eb, g0, g1);
-        if ((dbits(ebar) & kMag)) {
-            g0 += 0.5 * ebar;
-            g1 += 0.5 * ebar;
-            const double ds1 = -ebar / 6.0, ds0 = ebar / 6.0;
+        const A am = Q<A>(g, u, n, i - 2 * di, j - 2 * dj, k - 2 * dk), a0 = Q<A>(g, u, n, i - di, j - dj, k - dk);
+        const A a1 = Q<A>(g, u, n, i, j, k), a2 = Q<A>(g, u, n, i + di, j + dj, k + dk);
+        A c1a, c1b, c1c, c0a, c0b, c0c;
+        const A s1 = vls_d(a0, a1, a2, c1a, c1b, c1c);
+        const A s0 = vls_d(am, a0, a1, c0a, c0b, c0c);
+        const A e = A(0.5) * (a0 + a1) - A(1.0 / 6.0) * (s1 - s0);
+        A gm = A(0), g0 = A(0), g1 = A(0), g2 = A(0);
+        const A ebar = clip_rev(e, a0, a1, eb, g0, g1);
+        if (nonzero(ebar)) {
+            g0 += A(0.5) * ebar;
+            g1 += A(0.5) * ebar;
+            const A ds1 = -ebar * A(1.0 / 6.0), ds0 = ebar * A(1.0 / 6.0);
             g0 += ds1 * c1a;
             g1 += ds1 * c1b;
             g2 += ds1 * c1c;
@@ -178,60 +188,60 @@ __global__ void k_adj_edges(Grid g, int d, const double* u, const double* Eb0, c
             g0 += ds0 * c0b;
             g1 += ds0 * c0c;
         }
-        Qb(g, ub, n, i - 2 * di, j - 2 * dj, k - 2 * dk, gm);
-        Qb(g, ub, n, i - di, j - dj, k - dk, g0);
-        Qb(g, ub, n, i, j, k, g1);
-        Qb(g, ub, n, i + di, j + dj, k + dk, g2);
+        Qb(g, ub, n, i - 2 * di, j - 2 * dj, k - 2 * dk, (double)gm);
+        Qb(g, ub, n, i - di, j - dj, k - dk, (double)g0);
+        Qb(g, ub, n, i, j, k, (double)g1);
+        Qb(g, ub, n, i + di, j + dj, k + dk, (double)g2);
     }
 }
 
 // ---- reverse of the CW84 limiter + trace.  Given the adjoint tb of the trace
 // value, accumulate into the adjoints of sm_in, s0, sp_in and return the
 // adjoint of sig.
-__device__ inline double rev_trace(bool hi_side, double smi, double s0, double spi, double sig, double tb, double& gsm, double& gs0,
-                                   double& gsp) {
-    double sm = smi, sp = spi;
+template <typename A>
+__device__ inline A rev_trace(bool hi_side, A smi, A s0, A spi, A sig, A tb, A& gsm, A& gs0, A& gsp) {
+    A sm = smi, sp = spi;
     int cs = 0;
-    // the forward's CW84 decisions (k_ppm_*: cw84), on the integer pipe
-    const double dp = sp - s0, dm = s0 - sm;
-    if (!isame_sign(dp, dm)) {
+    // the forward's CW84 decisions (k_ppm_*: cw84)
+    const A dp = sp - s0, dm = s0 - sm;
+    if (!same_sign(dp, dm)) {
         cs = 1;
         sp = s0;
         sm = s0;
-    } else if (!iabs_lt2(dp, 2.0 * dm)) {
+    } else if (!abs_lt(dp, A(2) * dm)) {
         cs = 2;
-        sp = s0 + 2.0 * dm;
-    } else if (!iabs_lt2(dm, 2.0 * dp)) {
+        sp = s0 + A(2) * dm;
+    } else if (!abs_lt(dm, A(2) * dp)) {
         cs = 3;
-        sm = s0 - 2.0 * dp;
+        sm = s0 - A(2) * dp;
     }
-    const double Bf = 1.0 - 2.0 / 3.0 * sig;
-    const double s6 = 6.0 * s0 - 3.0 * (sm + sp);
-    double dsm, dsp, ds0, dsig;
+    const A Bf = A(1) - A(2.0 / 3.0) * sig;
+    const A s6 = A(6) * s0 - A(3) * (sm + sp);
+    A dsm, dsp, ds0, dsig;
     if (hi_side) {
-        dsp = 1.0 - 0.5 * sig * (1.0 + 3.0 * Bf);
-        dsm = 0.5 * sig * (1.0 - 3.0 * Bf);
-        ds0 = 3.0 * sig * Bf;
-        dsig = -0.5 * ((sp - sm) - Bf * s6) - (1.0 / 3.0) * sig * s6;
+        dsp = A(1) - A(0.5) * sig * (A(1) + A(3) * Bf);
+        dsm = A(0.5) * sig * (A(1) - A(3) * Bf);
+        ds0 = A(3) * sig * Bf;
+        dsig = A(-0.5) * ((sp - sm) - Bf * s6) - A(1.0 / 3.0) * sig * s6;
     } else {
-        dsm = 1.0 - 0.5 * sig * (1.0 + 3.0 * Bf);
-        dsp = 0.5 * sig * (1.0 - 3.0 * Bf);
-        ds0 = 3.0 * sig * Bf;
-        dsig = 0.5 * ((sp - sm) + Bf * s6) - (1.0 / 3.0) * sig * s6;
+        dsm = A(1) - A(0.5) * sig * (A(1) + A(3) * Bf);
+        dsp = A(0.5) * sig * (A(1) - A(3) * Bf);
+        ds0 = A(3) * sig * Bf;
+        dsig = A(0.5) * ((sp - sm) + Bf * s6) - A(1.0 / 3.0) * sig * s6;
     }
-    double bsm = dsm * tb, bsp = dsp * tb, bs0 = ds0 * tb;
+    A bsm = dsm * tb, bsp = dsp * tb, bs0 = ds0 * tb;
     if (cs == 1) {
         bs0 += bsm + bsp;
-        bsm = 0.0;
-        bsp = 0.0;
+        bsm = A(0);
+        bsp = A(0);
     } else if (cs == 2) {
-        bs0 += 3.0 * bsp;
-        bsm += -2.0 * bsp;
-        bsp = 0.0;
+        bs0 += A(3) * bsp;
+        bsm += A(-2) * bsp;
+        bsp = A(0);
     } else if (cs == 3) {
-        bs0 += 3.0 * bsm;
-        bsp += -2.0 * bsm;
-        bsm = 0.0;
+        bs0 += A(3) * bsm;
+        bsp += A(-2) * bsm;
+        bsm = A(0);
     }
     gsm += bsm;
     gsp += bsp;
@@ -239,19 +249,21 @@ __device__ inline double rev_trace(bool hi_side, double smi, double s0, double s
     return dsig * tb;
 }
 
-__device__ inline void rev_upwind(double vel, double ob, double& lb, double& hb) {
-    if (!iabs_lt(vel, kSV)) {
-        if (ige0(vel)) lb += ob; else hb += ob;
+template <typename A>
+__device__ inline void rev_upwind(A vel, A ob, A& lb, A& hb) {
+    if (!below_small_abs(vel)) {
+        if (ge0(vel)) lb += ob; else hb += ob;
     } else {
-        lb += 0.5 * ob;
-        hb += 0.5 * ob;
+        lb += A(0.5) * ob;
+        hb += A(0.5) * ob;
     }
 }
-__device__ inline void rev_riemann(double lo, double hi, double ob, double& lb, double& hb) {
-    const double sum = lo + hi;
-    const bool ltm = (ile0(lo) && ige0(hi)) || iabs_lt(sum, kSV);
+template <typename A>
+__device__ inline void rev_riemann(A lo, A hi, A ob, A& lb, A& hb) {
+    const A sum = lo + hi;
+    const bool ltm = (le0(lo) && ge0(hi)) || below_small_abs(sum);
     if (ltm) return;
-    if (ige0(sum)) lb += ob; else hb += ob;
+    if (ge0(sum)) lb += ob; else hb += ob;
 }
 
 struct A3 {
@@ -269,9 +281,11 @@ struct KI {
 // ---- reverse of k_faces (both passes).  MODE 0: pre-MAC (cell speed), the
 // adjoints of ad and of the upwinded transverse states are folded in here;
 // MODE 1: post-MAC (face speed, rho scaling), upwinded states folded in.
+// Arithmetic in the forward's precision TI; adjoint arrays FP64.
 template <int MODE, typename TI>
 __global__ void k_adj_faces(Grid g, int d, const double* u, KI<TI> E, double s, double rho, const double* umac_d, KI<TI> LO, KI<TI> HI,
                             const TI* ad, K3 LOb, K3 HIb, const double* adb, K3 TEb, A3 Eb, double* ub, double* umacb_d) {
+    using A = TI;
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_at(g, d, t, i, j, k)) return;
@@ -279,99 +293,101 @@ __global__ void k_adj_faces(Grid g, int d, const double* u, KI<TI> E, double s, 
     const bool wl = (d == 2 && !g.zper && k == 0), wh = (d == 2 && !g.zper && k == g.nz);
     const long long f = t;
     const long long fm = fidx(g, d, i - di, j - dj, k - dk), fp = fidx(g, d, i + di, j + dj, k + dk);
-    double lb[3], hb[3];
+    A lb[3], hb[3];
     for (int n = 0; n < 3; ++n) {
-        lb[n] = LOb.p[n][f];
-        hb[n] = HIb.p[n][f];
+        lb[n] = (A)LOb.p[n][f];
+        hb[n] = (A)HIb.p[n][f];
     }
-    double ul = 0.0, uh = 0.0;
+    A ul = A(0), uh = A(0);
     if (MODE == 0) {
-        if (!wl) ul = (TI)Q(g, u, d, i - di, j - dj, k - dk);
-        if (!wh) uh = (TI)Q(g, u, d, i, j, k);
-        rev_riemann(LO.p[d][f], HI.p[d][f], adb[f], lb[d], hb[d]);
-        const double a = ad[f];
+        if (!wl) ul = Q<A>(g, u, d, i - di, j - dj, k - dk);
+        if (!wh) uh = Q<A>(g, u, d, i, j, k);
+        rev_riemann(LO.p[d][f], HI.p[d][f], (A)adb[f], lb[d], hb[d]);
+        const A a = ad[f];
         for (int n = 0; n < 3; ++n)
-            if (n != d) rev_upwind(a, TEb.p[n][f], lb[n], hb[n]);
+            if (n != d) rev_upwind(a, (A)TEb.p[n][f], lb[n], hb[n]);
     } else {
-        const double umf = (TI)umac_d[f];
+        const A umf = (A)umac_d[f];
         ul = uh = umf;
-        for (int n = 0; n < 3; ++n) rev_upwind(umf, TEb.p[n][f], lb[n], hb[n]);
+        for (int n = 0; n < 3; ++n) rev_upwind(umf, (A)TEb.p[n][f], lb[n], hb[n]);
     }
     if (d == 2)
         for (int n = 0; n < 3; ++n) zbc_rev(g, k, n, lb[n], hb[n]);
-    const double scale = (MODE == 1) ? (double)(TI)rho : 1.0;
-    const double sT = (TI)s;
-    double gul = 0.0, guh = 0.0;
+    const A scale = (MODE == 1) ? (A)rho : A(1);
+    const A sT = (A)s;
+    A gul = A(0), guh = A(0);
     for (int n = 0; n < 3; ++n) {
-        const double tl = lb[n] * scale, th = hb[n] * scale;
-        if (!wl && (dbits(tl) & kMag)) {  // high-side trace of cell c - e_d
-            double gsm = 0.0, gs0 = 0.0, gsp = 0.0;
-            const double s0 = (TI)Q(g, u, n, i - di, j - dj, k - dk);
-            if (dbits(ul) > dbits(kSV)) {
-                const double bsig = rev_trace(true, E.p[n][fm], s0, E.p[n][f], (TI)(iabs(ul) * sT), tl, gsm, gs0, gsp);
-                gul += bsig * s * (ige0(ul) ? 1.0 : -1.0);
+        const A tl = lb[n] * scale, th = hb[n] * scale;
+        if (!wl && nonzero(tl)) {  // high-side trace of cell c - e_d
+            A gsm = A(0), gs0 = A(0), gsp = A(0);
+            const A s0 = Q<A>(g, u, n, i - di, j - dj, k - dk);
+            if (above_small(ul)) {
+                const A bsig = rev_trace(true, E.p[n][fm], s0, E.p[n][f], absv(ul) * sT, tl, gsm, gs0, gsp);
+                gul += bsig * sT * (ge0(ul) ? A(1) : A(-1));
             } else {
                 gs0 += tl;
             }
-            aadd(&Eb.p[n][fm], gsm);
-            aadd(&Eb.p[n][f], gsp);
-            Qb(g, ub, n, i - di, j - dj, k - dk, gs0);
+            aadd(&Eb.p[n][fm], (double)gsm);
+            aadd(&Eb.p[n][f], (double)gsp);
+            Qb(g, ub, n, i - di, j - dj, k - dk, (double)gs0);
         }
-        if (!wh && (dbits(th) & kMag)) {  // low-side trace of cell c
-            double gsm = 0.0, gs0 = 0.0, gsp = 0.0;
-            const double s0 = (TI)Q(g, u, n, i, j, k);
-            if (okey(uh) < okey(-kSV)) {
-                const double bsig = rev_trace(false, E.p[n][f], s0, E.p[n][fp], (TI)(iabs(uh) * sT), th, gsm, gs0, gsp);
-                guh += bsig * s * (ige0(uh) ? 1.0 : -1.0);
+        if (!wh && nonzero(th)) {  // low-side trace of cell c
+            A gsm = A(0), gs0 = A(0), gsp = A(0);
+            const A s0 = Q<A>(g, u, n, i, j, k);
+            if (below_msmall(uh)) {
+                const A bsig = rev_trace(false, E.p[n][f], s0, E.p[n][fp], absv(uh) * sT, th, gsm, gs0, gsp);
+                guh += bsig * sT * (ge0(uh) ? A(1) : A(-1));
             } else {
                 gs0 += th;
             }
-            aadd(&Eb.p[n][f], gsm);
-            aadd(&Eb.p[n][fp], gsp);
-            Qb(g, ub, n, i, j, k, gs0);
+            aadd(&Eb.p[n][f], (double)gsm);
+            aadd(&Eb.p[n][fp], (double)gsp);
+            Qb(g, ub, n, i, j, k, (double)gs0);
         }
     }
     if (MODE == 0) {
-        if (!wl) Qb(g, ub, d, i - di, j - dj, k - dk, gul);
-        if (!wh) Qb(g, ub, d, i, j, k, guh);
+        if (!wl) Qb(g, ub, d, i - di, j - dj, k - dk, (double)gul);
+        if (!wh) Qb(g, ub, d, i, j, k, (double)guh);
     } else {
-        aadd(&umacb_d[f], gul + guh);
+        aadd(&umacb_d[f], (double)(gul + guh));
     }
 }
 
 // ---- reverse of k_pm_trans (a, b, n)
 template <typename TI>
-__global__ void k_adj_pm_trans(Grid g, int a, int b, int n, double cb, const TI* ad_a, const TI* ad_b, const TI* edge_b, const double* outb,
+__global__ void k_adj_pm_trans(Grid g, int a, int b, int n, double cb64, const TI* ad_a, const TI* ad_b, const TI* edge_b, const double* outb,
                                double* lo_anb, double* hi_anb, double* ad_bb, double* edge_bb) {
+    using A = TI;
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_at(g, a, t, i, j, k)) return;
     const long long f = t;
-    const double ob = outb[f];
-    if (!(dbits(ob) & kMag)) return;
+    const double ob64 = outb[f];
+    if (!(dbits(ob64) & kMag)) return;
+    const A ob = (A)ob64, cb = (A)cb64;
     const bool wl = (a == 2 && !g.zper && k == 0), wh = (a == 2 && !g.zper && k == g.nz);
-    double lb = 0.0, hb = 0.0;
+    A lb = A(0), hb = A(0);
     rev_upwind(ad_a[f], ob, lb, hb);
     if (a == 2) zbc_rev(g, k, n, lb, hb);
-    lo_anb[f] += lb;
-    hi_anb[f] += hb;
+    lo_anb[f] += (double)lb;
+    hi_anb[f] += (double)hb;
     const int e0 = (b == 0), e1 = (b == 1), e2 = (b == 2);
-    if (!wh && (dbits(hb) & kMag)) {
+    if (!wh && nonzero(hb)) {
         const long long f0 = fidx(g, b, i, j, k), f1 = fidx(g, b, i + e0, j + e1, k + e2);
-        const double S = (double)ad_b[f1] + ad_b[f0], Dd = (double)edge_b[f1] - edge_b[f0];
-        aadd(&ad_bb[f1], -cb * Dd * hb);
-        aadd(&ad_bb[f0], -cb * Dd * hb);
-        aadd(&edge_bb[f1], -cb * S * hb);
-        aadd(&edge_bb[f0], cb * S * hb);
+        const A S = ad_b[f1] + ad_b[f0], Dd = edge_b[f1] - edge_b[f0];
+        aadd(&ad_bb[f1], (double)(-cb * Dd * hb));
+        aadd(&ad_bb[f0], (double)(-cb * Dd * hb));
+        aadd(&edge_bb[f1], (double)(-cb * S * hb));
+        aadd(&edge_bb[f0], (double)(cb * S * hb));
     }
-    if (!wl && (dbits(lb) & kMag)) {
+    if (!wl && nonzero(lb)) {
         const int ci = i - (a == 0), cj = j - (a == 1), ck = k - (a == 2);
         const long long f0 = fidx(g, b, ci, cj, ck), f1 = fidx(g, b, ci + e0, cj + e1, ck + e2);
-        const double S = (double)ad_b[f1] + ad_b[f0], Dd = (double)edge_b[f1] - edge_b[f0];
-        aadd(&ad_bb[f1], -cb * Dd * lb);
-        aadd(&ad_bb[f0], -cb * Dd * lb);
-        aadd(&edge_bb[f1], -cb * S * lb);
-        aadd(&edge_bb[f0], cb * S * lb);
+        const A S = ad_b[f1] + ad_b[f0], Dd = edge_b[f1] - edge_b[f0];
+        aadd(&ad_bb[f1], (double)(-cb * Dd * lb));
+        aadd(&ad_bb[f0], (double)(-cb * Dd * lb));
+        aadd(&edge_bb[f1], (double)(-cb * S * lb));
+        aadd(&edge_bb[f0], (double)(cb * S * lb));
     }
 }
 
@@ -386,53 +402,54 @@ __device__ inline long long cell_fo(const Grid& g, int i, int j, int k) {
 
 // ---- reverse of k_pm_final (d)
 template <typename TI>
-__global__ void k_adj_pm_final(Grid g, int d, double dt, double c1, double c2, const TI* lo_dd, const TI* hi_dd, KI<TI> AD, const TI* T1,
+__global__ void k_adj_pm_final(Grid g, int d, double dt, double c1_64, double c2_64, const TI* lo_dd, const TI* hi_dd, KI<TI> AD, const TI* T1,
                                const TI* T2, const double* forces, const double* macb, double* lo_ddb, double* hi_ddb, A3 ADb, double* T1b,
                                double* T2b, double* forcesb) {
+    using A = TI;
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_at(g, d, t, i, j, k)) return;
     if (d == 2 && !g.zper && (k == 0 || k == g.nz)) return;  // wall faces: the normal velocity is 0 whatever the input
     const long long f = t;
-    const double mb = macb[f];
-    if (!(dbits(mb) & kMag)) return;
+    const double mb64 = macb[f];
+    if (!(dbits(mb64) & kMag)) return;
+    const A mb = (A)mb64, c1 = (A)c1_64, c2 = (A)c2_64, hdt = A(0.5) * (A)dt;
     const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
-    auto side_val = [&](int ci, int cj, int ck, double base) {
+    auto side_val = [&](int ci, int cj, int ck, A base) {
         const long long p1 = fidx(g, b1, ci + (b1 == 0), cj + (b1 == 1), ck + (b1 == 2)), m1 = fidx(g, b1, ci, cj, ck);
         const long long p2 = fidx(g, b2, ci + (b2 == 0), cj + (b2 == 1), ck + (b2 == 2)), m2 = fidx(g, b2, ci, cj, ck);
         // the forward's sum in its own precision (decides the Riemann branch)
-        const TI tc1 = (TI)c1, tc2 = (TI)c2;
-        TI s = (TI)base;
-        s -= tc1 * (AD.p[b1][p1] + AD.p[b1][m1]) * (T1[p1] - T1[m1]);
-        s -= tc2 * (AD.p[b2][p2] + AD.p[b2][m2]) * (T2[p2] - T2[m2]);
-        s += TI(0.5) * (TI)dt * (TI)forces[d * g.N + cell_fo(g, ci, cj, ck)];
-        return (double)s;
+        A s = base;
+        s -= c1 * (AD.p[b1][p1] + AD.p[b1][m1]) * (T1[p1] - T1[m1]);
+        s -= c2 * (AD.p[b2][p2] + AD.p[b2][m2]) * (T2[p2] - T2[m2]);
+        s += hdt * (A)forces[d * g.N + cell_fo(g, ci, cj, ck)];
+        return s;
     };
-    auto side_rev = [&](int ci, int cj, int ck, double sb) {
+    auto side_rev = [&](int ci, int cj, int ck, A sb) {
         const long long p1 = fidx(g, b1, ci + (b1 == 0), cj + (b1 == 1), ck + (b1 == 2)), m1 = fidx(g, b1, ci, cj, ck);
         const long long p2 = fidx(g, b2, ci + (b2 == 0), cj + (b2 == 1), ck + (b2 == 2)), m2 = fidx(g, b2, ci, cj, ck);
-        const double S1 = (double)AD.p[b1][p1] + AD.p[b1][m1], D1 = (double)T1[p1] - T1[m1];
-        const double S2 = (double)AD.p[b2][p2] + AD.p[b2][m2], D2 = (double)T2[p2] - T2[m2];
-        aadd(&ADb.p[b1][p1], -c1 * D1 * sb);
-        aadd(&ADb.p[b1][m1], -c1 * D1 * sb);
-        aadd(&T1b[p1], -c1 * S1 * sb);
-        aadd(&T1b[m1], c1 * S1 * sb);
-        aadd(&ADb.p[b2][p2], -c2 * D2 * sb);
-        aadd(&ADb.p[b2][m2], -c2 * D2 * sb);
-        aadd(&T2b[p2], -c2 * S2 * sb);
-        aadd(&T2b[m2], c2 * S2 * sb);
-        aadd(&forcesb[d * g.N + cell_fo(g, ci, cj, ck)], 0.5 * dt * sb);
+        const A S1 = AD.p[b1][p1] + AD.p[b1][m1], D1 = T1[p1] - T1[m1];
+        const A S2 = AD.p[b2][p2] + AD.p[b2][m2], D2 = T2[p2] - T2[m2];
+        aadd(&ADb.p[b1][p1], (double)(-c1 * D1 * sb));
+        aadd(&ADb.p[b1][m1], (double)(-c1 * D1 * sb));
+        aadd(&T1b[p1], (double)(-c1 * S1 * sb));
+        aadd(&T1b[m1], (double)(c1 * S1 * sb));
+        aadd(&ADb.p[b2][p2], (double)(-c2 * D2 * sb));
+        aadd(&ADb.p[b2][m2], (double)(-c2 * D2 * sb));
+        aadd(&T2b[p2], (double)(-c2 * S2 * sb));
+        aadd(&T2b[m2], (double)(c2 * S2 * sb));
+        aadd(&forcesb[d * g.N + cell_fo(g, ci, cj, ck)], (double)(hdt * sb));
     };
     const int li = i - (d == 0), lj = j - (d == 1), lk = k - (d == 2);
-    const double stl = side_val(li, lj, lk, lo_dd[f]), sth = side_val(i, j, k, hi_dd[f]);
-    double bl = 0.0, bh = 0.0;
+    const A stl = side_val(li, lj, lk, lo_dd[f]), sth = side_val(i, j, k, hi_dd[f]);
+    A bl = A(0), bh = A(0);
     rev_riemann(stl, sth, mb, bl, bh);
-    if ((dbits(bl) & kMag)) {
-        lo_ddb[f] += bl;
+    if (nonzero(bl)) {
+        lo_ddb[f] += (double)bl;
         side_rev(li, lj, lk, bl);
     }
-    if ((dbits(bh) & kMag)) {
-        hi_ddb[f] += bh;
+    if (nonzero(bh)) {
+        hi_ddb[f] += (double)bh;
         side_rev(i, j, k, bh);
     }
 }
@@ -440,126 +457,130 @@ __global__ void k_adj_pm_final(Grid g, int d, double dt, double c1, double c2, c
 // ---- reverse of k_adv_trans (a, b): out_n = upwind(u_a; l, h),
 // h = HI + (-cb (vp E(h1) - vm E(h0)) + cb q(c) (vp - vm)), l likewise at c - e_a
 template <typename TI>
-__global__ void k_adj_adv_trans(Grid g, int a, int b, const double* u, double rho, double cb, const double* ua, const double* vb, KI<TI> E,
+__global__ void k_adj_adv_trans(Grid g, int a, int b, const double* u, double rho64, double cb64, const double* ua, const double* vb, KI<TI> E,
                                 K3 Ob, A3 LOb, A3 HIb, A3 Ebb, double* vbb, double* ub) {
+    using A = TI;
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_at(g, a, t, i, j, k)) return;
     const bool wl = (a == 2 && !g.zper && k == 0), wh = (a == 2 && !g.zper && k == g.nz);
     const long long f = t;
-    const double uaf = (TI)ua[f];
+    const A uaf = (A)ua[f], rho = (A)rho64, cb = (A)cb64;
     const int ci = i - (a == 0), cj = j - (a == 1), ck = k - (a == 2);
     const long long h0 = fidx(g, b, i, j, k), h1 = fidx(g, b, i + (b == 0), j + (b == 1), k + (b == 2));
     const long long l0 = fidx(g, b, ci, cj, ck), l1 = fidx(g, b, ci + (b == 0), cj + (b == 1), ck + (b == 2));
-    double vhp = 0.0, vhm = 0.0, vlp = 0.0, vlm = 0.0;
+    A vhp = A(0), vhm = A(0), vlp = A(0), vlm = A(0);
     if (!wh) {
-        vhp = (TI)vb[h1];
-        vhm = (TI)vb[h0];
+        vhp = (A)vb[h1];
+        vhm = (A)vb[h0];
     }
     if (!wl) {
-        vlp = (TI)vb[l1];
-        vlm = (TI)vb[l0];
+        vlp = (A)vb[l1];
+        vlm = (A)vb[l0];
     }
-    double gvhp = 0.0, gvhm = 0.0, gvlp = 0.0, gvlm = 0.0;
+    A gvhp = A(0), gvhm = A(0), gvlp = A(0), gvlm = A(0);
     for (int n = 0; n < 3; ++n) {
-        const double ob = Ob.p[n][f];
-        if (!(dbits(ob) & kMag)) continue;
-        double lb = 0.0, hb = 0.0;
+        const double ob64 = Ob.p[n][f];
+        if (!(dbits(ob64) & kMag)) continue;
+        const A ob = (A)ob64;
+        A lb = A(0), hb = A(0);
         rev_upwind(uaf, ob, lb, hb);
         if (a == 2) zbc_rev(g, k, n, lb, hb);
-        LOb.p[n][f] += lb;
-        HIb.p[n][f] += hb;
-        if (!wh && (dbits(hb) & kMag)) {
-            const double qc = (TI)rho * (TI)Q(g, u, n, i, j, k);
-            aadd(&Ebb.p[n][h1], -cb * vhp * hb);
-            aadd(&Ebb.p[n][h0], cb * vhm * hb);
+        LOb.p[n][f] += (double)lb;
+        HIb.p[n][f] += (double)hb;
+        if (!wh && nonzero(hb)) {
+            const A qc = rho * Q<A>(g, u, n, i, j, k);
+            aadd(&Ebb.p[n][h1], (double)(-cb * vhp * hb));
+            aadd(&Ebb.p[n][h0], (double)(cb * vhm * hb));
             gvhp += (-cb * E.p[n][h1] + cb * qc) * hb;
             gvhm += (cb * E.p[n][h0] - cb * qc) * hb;
-            Qb(g, ub, n, i, j, k, rho * cb * (vhp - vhm) * hb);
+            Qb(g, ub, n, i, j, k, (double)(rho * cb * (vhp - vhm) * hb));
         }
-        if (!wl && (dbits(lb) & kMag)) {
-            const double qc = (TI)rho * (TI)Q(g, u, n, ci, cj, ck);
-            aadd(&Ebb.p[n][l1], -cb * vlp * lb);
-            aadd(&Ebb.p[n][l0], cb * vlm * lb);
+        if (!wl && nonzero(lb)) {
+            const A qc = rho * Q<A>(g, u, n, ci, cj, ck);
+            aadd(&Ebb.p[n][l1], (double)(-cb * vlp * lb));
+            aadd(&Ebb.p[n][l0], (double)(cb * vlm * lb));
             gvlp += (-cb * E.p[n][l1] + cb * qc) * lb;
             gvlm += (cb * E.p[n][l0] - cb * qc) * lb;
-            Qb(g, ub, n, ci, cj, ck, rho * cb * (vlp - vlm) * lb);
+            Qb(g, ub, n, ci, cj, ck, (double)(rho * cb * (vlp - vlm) * lb));
         }
     }
-    aadd(&vbb[h1], gvhp);
-    aadd(&vbb[h0], gvhm);
-    aadd(&vbb[l1], gvlp);
-    aadd(&vbb[l0], gvlm);
+    aadd(&vbb[h1], (double)gvhp);
+    aadd(&vbb[h0], (double)gvhm);
+    aadd(&vbb[l1], (double)gvlp);
+    aadd(&vbb[l0], (double)gvlm);
 }
 
 // ---- reverse of k_adv_flux (d) with the flux adjoint Fb given
 template <typename TI>
-__global__ void k_adj_adv_flux(Grid g, int d, const double* u, const double* forces, double rho, double dt, double c1, double c2, K3 Uf,
-                               KI<TI> LO, KI<TI> HI, KI<TI> T1, KI<TI> T2, K3 Fb, A3 Ufb, A3 LOb, A3 HIb, A3 T1b, A3 T2b, double* ub,
+__global__ void k_adj_adv_flux(Grid g, int d, const double* u, const double* forces, double rho64, double dt64, double c1_64, double c2_64,
+                               K3 Uf, KI<TI> LO, KI<TI> HI, KI<TI> T1, KI<TI> T2, K3 Fb, A3 Ufb, A3 LOb, A3 HIb, A3 T1b, A3 T2b, double* ub,
                                double* forcesb) {
+    using A = TI;
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (!face_at(g, d, t, i, j, k)) return;
     const bool wl = (d == 2 && !g.zper && k == 0), wh = (d == 2 && !g.zper && k == g.nz);
     const long long f = t;
     const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
-    const double um = (TI)Uf.p[d][f];
+    const A um = (A)Uf.p[d][f];
+    const A rho = (A)rho64, c1 = (A)c1_64, c2 = (A)c2_64, hdt = A(0.5) * (A)dt64;
     const int li = i - (d == 0), lj = j - (d == 1), lk = k - (d == 2);
     const long long lp1 = fidx(g, b1, li + (b1 == 0), lj + (b1 == 1), lk + (b1 == 2)), lm1 = fidx(g, b1, li, lj, lk);
     const long long lp2 = fidx(g, b2, li + (b2 == 0), lj + (b2 == 1), lk + (b2 == 2)), lm2 = fidx(g, b2, li, lj, lk);
     const long long hp1 = fidx(g, b1, i + (b1 == 0), j + (b1 == 1), k + (b1 == 2)), hm1 = fidx(g, b1, i, j, k);
     const long long hp2 = fidx(g, b2, i + (b2 == 0), j + (b2 == 1), k + (b2 == 2)), hm2 = fidx(g, b2, i, j, k);
-    double l1p = 0, l1m = 0, l2p = 0, l2m = 0, h1p = 0, h1m = 0, h2p = 0, h2m = 0;
+    A l1p = A(0), l1m = A(0), l2p = A(0), l2m = A(0), h1p = A(0), h1m = A(0), h2p = A(0), h2m = A(0);
     if (!wl) {
-        l1p = (TI)Uf.p[b1][lp1];
-        l1m = (TI)Uf.p[b1][lm1];
-        l2p = (TI)Uf.p[b2][lp2];
-        l2m = (TI)Uf.p[b2][lm2];
+        l1p = (A)Uf.p[b1][lp1];
+        l1m = (A)Uf.p[b1][lm1];
+        l2p = (A)Uf.p[b2][lp2];
+        l2m = (A)Uf.p[b2][lm2];
     }
     if (!wh) {
-        h1p = (TI)Uf.p[b1][hp1];
-        h1m = (TI)Uf.p[b1][hm1];
-        h2p = (TI)Uf.p[b2][hp2];
-        h2m = (TI)Uf.p[b2][hm2];
+        h1p = (A)Uf.p[b1][hp1];
+        h1m = (A)Uf.p[b1][hm1];
+        h2p = (A)Uf.p[b2][hp2];
+        h2m = (A)Uf.p[b2][hm2];
     }
-    double gum = 0, gl1p = 0, gl1m = 0, gl2p = 0, gl2m = 0, gh1p = 0, gh1m = 0, gh2p = 0, gh2m = 0;
+    A gum = A(0), gl1p = A(0), gl1m = A(0), gl2p = A(0), gl2m = A(0), gh1p = A(0), gh1m = A(0), gh2p = A(0), gh2m = A(0);
     const long long cl = wl ? 0 : cell_fo(g, li, lj, lk);
     const long long ch = wh ? 0 : cell_fo(g, i, j, k);
     for (int n = 0; n < 3; ++n) {
-        const double fb = Fb.p[n][f];
-        if (!(dbits(fb) & kMag)) continue;
+        const double fb64 = Fb.p[n][f];
+        if (!(dbits(fb64) & kMag)) continue;
+        const A fb = (A)fb64;
         // the forward's face states in its own precision (decide the upwind branch)
-        const TI tr = (TI)rho, tc1 = (TI)c1, tc2 = (TI)c2, thd = TI(0.5) * (TI)dt;
-        double ql = 0.0, qh = 0.0, stl = 0.0, sth = 0.0;
+        A ql = A(0), qh = A(0), stl = A(0), sth = A(0);
         if (!wl) {
-            const TI q = tr * (TI)u[n * g.N + cl];
+            const A q = rho * (A)u[n * g.N + cl];
             ql = q;
-            TI s_ = LO.p[n][f];
-            s_ -= tc1 * (T1.p[n][lp1] * (TI)l1p - T1.p[n][lm1] * (TI)l1m);
-            s_ -= tc2 * (T2.p[n][lp2] * (TI)l2p - T2.p[n][lm2] * (TI)l2m);
-            s_ += tc1 * q * (TI)(l1p - l1m);
-            s_ += tc2 * q * (TI)(l2p - l2m);
-            s_ += thd * (tr * (TI)forces[n * g.N + cl]);
+            A s_ = LO.p[n][f];
+            s_ -= c1 * (T1.p[n][lp1] * l1p - T1.p[n][lm1] * l1m);
+            s_ -= c2 * (T2.p[n][lp2] * l2p - T2.p[n][lm2] * l2m);
+            s_ += c1 * q * (l1p - l1m);
+            s_ += c2 * q * (l2p - l2m);
+            s_ += hdt * (rho * (A)forces[n * g.N + cl]);
             stl = s_;
         }
         if (!wh) {
-            const TI q = tr * (TI)u[n * g.N + ch];
+            const A q = rho * (A)u[n * g.N + ch];
             qh = q;
-            TI s_ = HI.p[n][f];
-            s_ -= tc1 * (T1.p[n][hp1] * (TI)h1p - T1.p[n][hm1] * (TI)h1m);
-            s_ -= tc2 * (T2.p[n][hp2] * (TI)h2p - T2.p[n][hm2] * (TI)h2m);
-            s_ += tc1 * q * (TI)(h1p - h1m);
-            s_ += tc2 * q * (TI)(h2p - h2m);
-            s_ += thd * (tr * (TI)forces[n * g.N + ch]);
+            A s_ = HI.p[n][f];
+            s_ -= c1 * (T1.p[n][hp1] * h1p - T1.p[n][hm1] * h1m);
+            s_ -= c2 * (T2.p[n][hp2] * h2p - T2.p[n][hm2] * h2m);
+            s_ += c1 * q * (h1p - h1m);
+            s_ += c2 * q * (h2p - h2m);
+            s_ += hdt * (rho * (A)forces[n * g.N + ch]);
             sth = s_;
         }
-        double zl = stl, zh = sth;
+        A zl = stl, zh = sth;
         if (d == 2) zbc_fwd(g, k, n, zl, zh);
-        double st, bl = 0.0, bh = 0.0;
-        if (iabs_lt(um, kSV)) {
-            st = 0.5 * (zl + zh);
-            bl = bh = 0.5 * um * fb;
-        } else if (ige0(um)) {
+        A st, bl = A(0), bh = A(0);
+        if (below_small_abs(um)) {
+            st = A(0.5) * (zl + zh);
+            bl = bh = A(0.5) * um * fb;
+        } else if (ge0(um)) {
             st = zl;
             bl = um * fb;
         } else {
@@ -568,42 +589,42 @@ __global__ void k_adj_adv_flux(Grid g, int d, const double* u, const double* for
         }
         gum += st * fb;
         if (d == 2) zbc_rev(g, k, n, bl, bh);
-        if (!wl && (dbits(bl) & kMag)) {
-            LOb.p[n][f] += bl;
-            aadd(&T1b.p[n][lp1], -c1 * l1p * bl);
-            aadd(&T1b.p[n][lm1], c1 * l1m * bl);
-            aadd(&T2b.p[n][lp2], -c2 * l2p * bl);
-            aadd(&T2b.p[n][lm2], c2 * l2m * bl);
+        if (!wl && nonzero(bl)) {
+            LOb.p[n][f] += (double)bl;
+            aadd(&T1b.p[n][lp1], (double)(-c1 * l1p * bl));
+            aadd(&T1b.p[n][lm1], (double)(c1 * l1m * bl));
+            aadd(&T2b.p[n][lp2], (double)(-c2 * l2p * bl));
+            aadd(&T2b.p[n][lm2], (double)(c2 * l2m * bl));
             gl1p += (-c1 * T1.p[n][lp1] + c1 * ql) * bl;
             gl1m += (c1 * T1.p[n][lm1] - c1 * ql) * bl;
             gl2p += (-c2 * T2.p[n][lp2] + c2 * ql) * bl;
             gl2m += (c2 * T2.p[n][lm2] - c2 * ql) * bl;
-            aadd(&ub[n * g.N + cl], rho * (c1 * (l1p - l1m) + c2 * (l2p - l2m)) * bl);
-            aadd(&forcesb[n * g.N + cl], 0.5 * dt * rho * bl);
+            aadd(&ub[n * g.N + cl], (double)(rho * (c1 * (l1p - l1m) + c2 * (l2p - l2m)) * bl));
+            aadd(&forcesb[n * g.N + cl], (double)(hdt * rho * bl));
         }
-        if (!wh && (dbits(bh) & kMag)) {
-            HIb.p[n][f] += bh;
-            aadd(&T1b.p[n][hp1], -c1 * h1p * bh);
-            aadd(&T1b.p[n][hm1], c1 * h1m * bh);
-            aadd(&T2b.p[n][hp2], -c2 * h2p * bh);
-            aadd(&T2b.p[n][hm2], c2 * h2m * bh);
+        if (!wh && nonzero(bh)) {
+            HIb.p[n][f] += (double)bh;
+            aadd(&T1b.p[n][hp1], (double)(-c1 * h1p * bh));
+            aadd(&T1b.p[n][hm1], (double)(c1 * h1m * bh));
+            aadd(&T2b.p[n][hp2], (double)(-c2 * h2p * bh));
+            aadd(&T2b.p[n][hm2], (double)(c2 * h2m * bh));
             gh1p += (-c1 * T1.p[n][hp1] + c1 * qh) * bh;
             gh1m += (c1 * T1.p[n][hm1] - c1 * qh) * bh;
             gh2p += (-c2 * T2.p[n][hp2] + c2 * qh) * bh;
             gh2m += (c2 * T2.p[n][hm2] - c2 * qh) * bh;
-            aadd(&ub[n * g.N + ch], rho * (c1 * (h1p - h1m) + c2 * (h2p - h2m)) * bh);
-            aadd(&forcesb[n * g.N + ch], 0.5 * dt * rho * bh);
+            aadd(&ub[n * g.N + ch], (double)(rho * (c1 * (h1p - h1m) + c2 * (h2p - h2m)) * bh));
+            aadd(&forcesb[n * g.N + ch], (double)(hdt * rho * bh));
         }
     }
-    aadd(&Ufb.p[d][f], gum);
-    aadd(&Ufb.p[b1][lp1], gl1p);
-    aadd(&Ufb.p[b1][lm1], gl1m);
-    aadd(&Ufb.p[b2][lp2], gl2p);
-    aadd(&Ufb.p[b2][lm2], gl2m);
-    aadd(&Ufb.p[b1][hp1], gh1p);
-    aadd(&Ufb.p[b1][hm1], gh1m);
-    aadd(&Ufb.p[b2][hp2], gh2p);
-    aadd(&Ufb.p[b2][hm2], gh2m);
+    aadd(&Ufb.p[d][f], (double)gum);
+    aadd(&Ufb.p[b1][lp1], (double)gl1p);
+    aadd(&Ufb.p[b1][lm1], (double)gl1m);
+    aadd(&Ufb.p[b2][lp2], (double)gl2p);
+    aadd(&Ufb.p[b2][lm2], (double)gl2m);
+    aadd(&Ufb.p[b1][hp1], (double)gh1p);
+    aadd(&Ufb.p[b1][hm1], (double)gh1m);
+    aadd(&Ufb.p[b2][hp2], (double)gh2p);
+    aadd(&Ufb.p[b2][hm2], (double)gh2m);
 }
 
 // ---- reverse of conv = -div F on d-faces: Fb(f) = (convb(cell above f) - convb(cell below f)) / h_d
@@ -674,37 +695,44 @@ __device__ inline void Vdb(const Grid& g, double* ub, double* wgb, int n, int i,
 constexpr int ATX = 32, ATY = 4, ATZ = 4;
 constexpr int AHX = ATX + 2, AHY = ATY + 2, AHZ = ATZ + 2;
 constexpr int ANH = AHX * AHY * AHZ;
-constexpr size_t ADJ_TAU_SMEM = sizeof(double) * 11 * (size_t)ANH;
+// shared memory of the reverse diffusion tile: FP64 accumulators (4 per box
+// cell) and the staged values in the arithmetic type A (7 per box cell)
+template <typename A>
+constexpr size_t adj_tau_smem() { return sizeof(double) * 4 * (size_t)ANH + sizeof(A) * 7 * (size_t)ANH; }
 
+// A: arithmetic of the face terms, double, or float for the reverse of the
+// mixed-precision form's FP32 diffusion; the accumulators are FP64.
+template <typename A>
 __global__ void __launch_bounds__(ATX* ATY* ATZ) k_adj_tau_tile(Grid g, const double* vel, const double* mu, const double* wg,
                                                                 const double* db, double s, double* ub, double* mub, double* wgb) {
-    extern __shared__ double sm[];
-    double* sV = sm;              // [3][box]
-    double* sD = sm + 3 * ANH;    // [3][box] divergence adjoint (cells in the domain, else 0)
-    double* sM = sm + 6 * ANH;    // [box]
-    double* aU = sm + 7 * ANH;    // [3][box] accumulated velocity adjoint
-    double* aM = sm + 10 * ANH;   // [box] accumulated viscosity adjoint
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    double* aU = reinterpret_cast<double*>(sm_raw);  // [3][box] accumulated velocity adjoint
+    double* aM = aU + 3 * ANH;                       // [box] accumulated viscosity adjoint
+    A* sV = reinterpret_cast<A*>(aM + ANH);          // [3][box]
+    A* sD = sV + 3 * ANH;                            // [3][box] divergence adjoint (cells in the domain, else 0)
+    A* sM = sV + 6 * ANH;                            // [box]
     const int i0 = blockIdx.x * ATX, j0 = blockIdx.y * ATY, k0 = blockIdx.z * ATZ;
     const int tid = threadIdx.x, nthr = ATX * ATY * ATZ;
     auto hb = [](int hx, int hy, int hz) { return (hz * AHY + hy) * AHX + hx; };
+    const A sA = (A)s;
     for (int h = tid; h < ANH; h += nthr) {
         const int hx = h % AHX, hy = (h / AHX) % AHY, hz = h / (AHX * AHY);
         const int gi = ((i0 + hx - 1) % g.nx + g.nx) % g.nx, gj = ((j0 + hy - 1) % g.ny + g.ny) % g.ny;
         int gk = k0 + hz - 1;
         const bool inz = g.zper || (gk >= 0 && gk < g.nz);
         if (g.zper) gk = (gk % g.nz + g.nz) % g.nz;
-        for (int n = 0; n < 3; ++n) sV[n * ANH + h] = Vd(g, vel, wg, n, gi, gj, gk);
+        for (int n = 0; n < 3; ++n) sV[n * ANH + h] = (A)Vd(g, vel, wg, n, gi, gj, gk);
         const int kk = g.zper ? gk : (gk < 0 ? 0 : (gk >= g.nz ? g.nz - 1 : gk));
         const long long c = cidx(g, gi, gj, kk);
-        sM[h] = mu[c];
+        sM[h] = (A)mu[c];
         for (int n = 0; n < 3; ++n) {
-            sD[n * ANH + h] = inz ? s * db[n * g.N + c] : 0.0;
+            sD[n * ANH + h] = inz ? sA * (A)db[n * g.N + c] : A(0);
             aU[n * ANH + h] = 0.0;
         }
         aM[h] = 0.0;
     }
     __syncthreads();
-    const double ih[3] = {g.idx, g.idy, g.idz};
+    const A ih[3] = {(A)g.idx, (A)g.idy, (A)g.idz};
     const bool top = !g.zper && k0 + ATZ >= g.nz;  // this tile also owns the top wall faces
     const int nface = 3 * nthr + (top ? ATX * ATY : 0);
     for (int q = tid; q < nface; q += nthr) {
@@ -729,65 +757,67 @@ __global__ void __launch_bounds__(ATX* ATY* ATZ) k_adj_tau_tile(Grid g, const do
         const int hx = tx + 1, hy = ty + 1, hz = tz + 1;     // cell above the face
         const int mx = hx - e0, my = hy - e1, mz = hz - e2;  // cell below
         const bool has_hi = !(d == 2 && !g.zper && gk == g.nz), has_lo = !(d == 2 && !g.zper && gk == 0);
-        double Fb[3];
+        A Fb[3];
         bool any = false;
         for (int n = 0; n < 3; ++n) {
-            Fb[n] = ((has_lo ? sD[n * ANH + hb(mx, my, mz)] : 0.0) - (has_hi ? sD[n * ANH + hb(hx, hy, hz)] : 0.0)) * ih[d];
-            any = any || (dbits(Fb[n]) & kMag);
+            Fb[n] = ((has_lo ? sD[n * ANH + hb(mx, my, mz)] : A(0)) - (has_hi ? sD[n * ANH + hb(hx, hy, hz)] : A(0))) * ih[d];
+            any = any || nonzero(Fb[n]);
         }
         if (!any) continue;
-        double mf;
+        A mf;
         if (!has_lo) mf = sM[hb(hx, hy, hz)];
         else if (!has_hi) mf = sM[hb(mx, my, mz)];
-        else mf = 0.5 * (sM[hb(mx, my, mz)] + sM[hb(hx, hy, hz)]);
-        double gr[3][3];
+        else mf = A(0.5) * (sM[hb(mx, my, mz)] + sM[hb(hx, hy, hz)]);
+        A gr[3][3];
         for (int n = 0; n < 3; ++n) {
-            const double* v = sV + n * ANH;
+            const A* v = sV + n * ANH;
             for (int m = 0; m < 3; ++m) {
                 if (m == d) {
                     gr[m][n] = (v[hb(hx, hy, hz)] - v[hb(mx, my, mz)]) * ih[m];
                 } else {
                     const int f0 = (m == 0), f1 = (m == 1), f2 = (m == 2);
-                    gr[m][n] = 0.25 *
+                    gr[m][n] = A(0.25) *
                                (v[hb(hx + f0, hy + f1, hz + f2)] + v[hb(mx + f0, my + f1, mz + f2)] - v[hb(hx - f0, hy - f1, hz - f2)] -
                                 v[hb(mx - f0, my - f1, mz - f2)]) *
                                ih[m];
                 }
             }
         }
-        const double dv = gr[0][0] + gr[1][1] + gr[2][2];
-        double mfb = 0.0, dvb = 0.0;
-        double grb[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        const A dv = gr[0][0] + gr[1][1] + gr[2][2];
+        A mfb = A(0), dvb = A(0);
+        A grb[3][3] = {{A(0), A(0), A(0)}, {A(0), A(0), A(0)}, {A(0), A(0), A(0)}};
         for (int n = 0; n < 3; ++n) {
-            const double Sn = (n == d) ? (2.0 * gr[d][d] - (2.0 / 3.0) * dv) : (gr[d][n] + gr[n][d]);
+            const A Sn = (n == d) ? (A(2) * gr[d][d] - A(2.0 / 3.0) * dv) : (gr[d][n] + gr[n][d]);
             mfb += Fb[n] * Sn;
-            const double sb = mf * Fb[n];
+            const A sb = mf * Fb[n];
             if (n == d) {
-                grb[d][d] += 2.0 * sb;
-                dvb += -(2.0 / 3.0) * sb;
+                grb[d][d] += A(2) * sb;
+                dvb += A(-2.0 / 3.0) * sb;
             } else {
                 grb[d][n] += sb;
                 grb[n][d] += sb;
             }
         }
         for (int m = 0; m < 3; ++m) grb[m][m] += dvb;
-        if (!has_lo) atomicAdd(&aM[hb(hx, hy, hz)], mfb);
-        else if (!has_hi) atomicAdd(&aM[hb(mx, my, mz)], mfb);
+        if (!has_lo) atomicAdd(&aM[hb(hx, hy, hz)], (double)mfb);
+        else if (!has_hi) atomicAdd(&aM[hb(mx, my, mz)], (double)mfb);
         else {
-            atomicAdd(&aM[hb(mx, my, mz)], 0.5 * mfb);
-            atomicAdd(&aM[hb(hx, hy, hz)], 0.5 * mfb);
+            const double hm = (double)(A(0.5) * mfb);
+            atomicAdd(&aM[hb(mx, my, mz)], hm);
+            atomicAdd(&aM[hb(hx, hy, hz)], hm);
         }
         for (int n = 0; n < 3; ++n) {
             double* a = aU + n * ANH;
             for (int m = 0; m < 3; ++m) {
-                const double b = grb[m][n];
-                if (!(dbits(b) & kMag)) continue;
+                const A b = grb[m][n];
+                if (!nonzero(b)) continue;
                 if (m == d) {
-                    atomicAdd(&a[hb(hx, hy, hz)], b * ih[m]);
-                    atomicAdd(&a[hb(mx, my, mz)], -b * ih[m]);
+                    const double w = (double)(b * ih[m]);
+                    atomicAdd(&a[hb(hx, hy, hz)], w);
+                    atomicAdd(&a[hb(mx, my, mz)], -w);
                 } else {
                     const int f0 = (m == 0), f1 = (m == 1), f2 = (m == 2);
-                    const double w = 0.25 * b * ih[m];
+                    const double w = (double)(A(0.25) * b * ih[m]);
                     atomicAdd(&a[hb(hx + f0, hy + f1, hz + f2)], w);
                     atomicAdd(&a[hb(mx + f0, my + f1, mz + f2)], w);
                     atomicAdd(&a[hb(hx - f0, hy - f1, hz - f2)], -w);
@@ -809,7 +839,9 @@ __global__ void __launch_bounds__(ATX* ATY* ATZ) k_adj_tau_tile(Grid g, const do
     }
 }
 
-// ---- reverse of the Smagorinsky viscosity mu_eff = mu + rho fac |S|(u)
+// ---- reverse of the Smagorinsky viscosity mu_eff = mu + rho fac |S|(u), in
+// the arithmetic type of the forward's strain rate (A)
+template <typename A>
 __global__ void k_adj_smag(Grid g, const double* vel, const double* mub, double rho, double fac, double* ub) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= g.N) return;
@@ -818,29 +850,30 @@ __global__ void k_adj_smag(Grid g, const double* vel, const double* mub, double 
     const int i = (int)(t % g.nx);
     const long long r = t / g.nx;
     const int j = (int)(r % g.ny), k = (int)(r / g.ny);
-    double a = 0.5, b = 0.0, c = -0.5;
+    A a = A(0.5), b = A(0), c = A(-0.5);
     if (!g.zper && k == 0) {
-        a = 1.0 / 3.0;
-        b = 1.0;
-        c = -4.0 / 3.0;
+        a = A(1.0 / 3.0);
+        b = A(1);
+        c = A(-4.0 / 3.0);
     }
     if (!g.zper && k == g.nz - 1) {
-        a = 4.0 / 3.0;
-        b = -1.0;
-        c = -1.0 / 3.0;
+        a = A(4.0 / 3.0);
+        b = A(-1);
+        c = A(-1.0 / 3.0);
     }
-    double gx[3], gy[3], gz[3];
+    const A hx = A(0.5 * g.idx), hy = A(0.5 * g.idy), iz = (A)g.idz;
+    A gx[3], gy[3], gz[3];
     for (int n = 0; n < 3; ++n) {
-        gx[n] = 0.5 * (Q(g, vel, n, i + 1, j, k) - Q(g, vel, n, i - 1, j, k)) * g.idx;
-        gy[n] = 0.5 * (Q(g, vel, n, i, j + 1, k) - Q(g, vel, n, i, j - 1, k)) * g.idy;
-        gz[n] = (a * Q(g, vel, n, i, j, k + 1) + b * Q(g, vel, n, i, j, k) + c * Q(g, vel, n, i, j, k - 1)) * g.idz;
+        gx[n] = hx * (Q<A>(g, vel, n, i + 1, j, k) - Q<A>(g, vel, n, i - 1, j, k));
+        gy[n] = hy * (Q<A>(g, vel, n, i, j + 1, k) - Q<A>(g, vel, n, i, j - 1, k));
+        gz[n] = (a * Q<A>(g, vel, n, i, j, k + 1) + b * Q<A>(g, vel, n, i, j, k) + c * Q<A>(g, vel, n, i, j, k - 1)) * iz;
     }
-    const double S = sqrt(2.0 * gx[0] * gx[0] + 2.0 * gy[1] * gy[1] + 2.0 * gz[2] * gz[2] + (gy[0] + gx[1]) * (gy[0] + gx[1]) +
-                          (gz[1] + gy[2]) * (gz[1] + gy[2]) + (gx[2] + gz[0]) * (gx[2] + gz[0]));
-    if (!(S > 0.0)) return;
-    const double q = rho * fac * mb / S;
-    double gxb[3] = {2.0 * q * gx[0], 0.0, 0.0}, gyb[3] = {0.0, 2.0 * q * gy[1], 0.0}, gzb[3] = {0.0, 0.0, 2.0 * q * gz[2]};
-    const double t1 = q * (gy[0] + gx[1]), t2 = q * (gz[1] + gy[2]), t3 = q * (gx[2] + gz[0]);
+    const A S = sqrt(A(2) * gx[0] * gx[0] + A(2) * gy[1] * gy[1] + A(2) * gz[2] * gz[2] + (gy[0] + gx[1]) * (gy[0] + gx[1]) +
+                     (gz[1] + gy[2]) * (gz[1] + gy[2]) + (gx[2] + gz[0]) * (gx[2] + gz[0]));
+    if (!(S > A(0))) return;
+    const A q = (A)(rho * fac * mb) / S;
+    A gxb[3] = {A(2) * q * gx[0], A(0), A(0)}, gyb[3] = {A(0), A(2) * q * gy[1], A(0)}, gzb[3] = {A(0), A(0), A(2) * q * gz[2]};
+    const A t1 = q * (gy[0] + gx[1]), t2 = q * (gz[1] + gy[2]), t3 = q * (gx[2] + gz[0]);
     gyb[0] += t1;
     gxb[1] += t1;
     gzb[1] += t2;
@@ -848,13 +881,14 @@ __global__ void k_adj_smag(Grid g, const double* vel, const double* mub, double 
     gxb[2] += t3;
     gzb[0] += t3;
     for (int n = 0; n < 3; ++n) {
-        Qb(g, ub, n, i + 1, j, k, 0.5 * g.idx * gxb[n]);
-        Qb(g, ub, n, i - 1, j, k, -0.5 * g.idx * gxb[n]);
-        Qb(g, ub, n, i, j + 1, k, 0.5 * g.idy * gyb[n]);
-        Qb(g, ub, n, i, j - 1, k, -0.5 * g.idy * gyb[n]);
-        Qb(g, ub, n, i, j, k + 1, a * g.idz * gzb[n]);
-        Qb(g, ub, n, i, j, k, b * g.idz * gzb[n]);
-        Qb(g, ub, n, i, j, k - 1, c * g.idz * gzb[n]);
+        const double wx = (double)(hx * gxb[n]), wy = (double)(hy * gyb[n]);
+        Qb(g, ub, n, i + 1, j, k, wx);
+        Qb(g, ub, n, i - 1, j, k, -wx);
+        Qb(g, ub, n, i, j + 1, k, wy);
+        Qb(g, ub, n, i, j - 1, k, -wy);
+        Qb(g, ub, n, i, j, k + 1, (double)(a * iz * gzb[n]));
+        Qb(g, ub, n, i, j, k, (double)(b * iz * gzb[n]));
+        Qb(g, ub, n, i, j, k - 1, (double)(c * iz * gzb[n]));
     }
 }
 
@@ -1144,13 +1178,21 @@ void launch_adj_div(Ctx& c, const Grid& g, const double* convb, const AdjBufs& A
     }
 }
 void launch_adj_tau(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, const double* divtau_b, double s, double* ub,
-                    double* mub, double* wgb) {
-    cudaFuncSetAttribute(k_adj_tau_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ADJ_TAU_SMEM);
+                    double* mub, double* wgb, int fp32) {
     const dim3 grid((g.nx + ATX - 1) / ATX, (g.ny + ATY - 1) / ATY, (g.nz + ATZ - 1) / ATZ);
-    KS_LAUNCH_SMEM(c, k_adj_tau_tile, grid, ATX * ATY * ATZ, ADJ_TAU_SMEM, B8 * 14.0 * g.N, g, vel, mueff, wg, divtau_b, s, ub, mub, wgb);
+    if (fp32) {
+        cudaFuncSetAttribute(k_adj_tau_tile<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)adj_tau_smem<float>());
+        KS_LAUNCH_SMEM(c, k_adj_tau_tile<float>, grid, ATX * ATY * ATZ, adj_tau_smem<float>(), B8 * 14.0 * g.N, g, vel, mueff, wg, divtau_b, s,
+                       ub, mub, wgb);
+    } else {
+        cudaFuncSetAttribute(k_adj_tau_tile<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)adj_tau_smem<double>());
+        KS_LAUNCH_SMEM(c, k_adj_tau_tile<double>, grid, ATX * ATY * ATZ, adj_tau_smem<double>(), B8 * 14.0 * g.N, g, vel, mueff, wg, divtau_b, s,
+                       ub, mub, wgb);
+    }
 }
-void launch_adj_smag(Ctx& c, const Grid& g, const double* vel, const double* mub, const Scalars& s, double* ub) {
-    KS_LAUNCH(c, k_adj_smag, nblocks(g.N, BS), BS, B8 * 7.0 * g.N, g, vel, mub, s.rho, s.smag_fac, ub);
+void launch_adj_smag(Ctx& c, const Grid& g, const double* vel, const double* mub, const Scalars& s, double* ub, int fp32) {
+    if (fp32) KS_LAUNCH(c, k_adj_smag<float>, nblocks(g.N, BS), BS, B8 * 7.0 * g.N, g, vel, mub, s.rho, s.smag_fac, ub);
+    else KS_LAUNCH(c, k_adj_smag<double>, nblocks(g.N, BS), BS, B8 * 7.0 * g.N, g, vel, mub, s.rho, s.smag_fac, ub);
 }
 void launch_adj_wall_local(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wgb, double ut2, double um0, double um1,
                            double vm, double rho, double* ub, double* mub, double* parts, int* np) {

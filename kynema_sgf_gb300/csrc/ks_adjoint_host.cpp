@@ -282,7 +282,7 @@ void Sim::adjoint_step_impl(bool seed) {
     launch_adj_nodal_post(ctx_, g_, nd_[0].phi, ub, S.t1.p);  // t1 = v_bar = adjoint of v**
     // ---- v** = v* + dt/(2 rho) (L(v*) - dold); vel_tmp_ still holds v*
     launch_copy(ctx_, ub, S.t1.p, N3);
-    launch_adj_tau(ctx_, g_, vel_tmp_.p, mueff_.p, wg_.p, S.t1.p, 0.5 * dr, ub, mub, wgb);  // ub = v*_bar
+    launch_adj_tau(ctx_, g_, vel_tmp_.p, mueff_.p, wg_.p, S.t1.p, 0.5 * dr, ub, mub, wgb, fp32);  // ub = v*_bar
     launch_axpby(ctx_, N3, -0.5 * dr, S.t1.p, dr, ub, S.doldb.p);         // dold_bar
     launch_axpby(ctx_, N3, sigma, S.t1.p, 0.0, S.t1.p, gpb);              // gp_bar = sigma v_bar (v = v** + sigma gp)
     launch_axpby(ctx_, N3, dr, ub, 0.0, ub, S.srcb.p);                    // src_bar = conv_bar = dt/rho v*_bar
@@ -339,7 +339,7 @@ void Sim::adjoint_step_impl(bool seed) {
     launch_axpby(ctx_, N3, 1.0, S.srcb.p, 1.0 / rho_, A.forces, S.srcb.p);
     launch_axpby(ctx_, N3, 1.0, S.doldb.p, 1.0 / rho_, A.forces, S.doldb.p);
     // ---- dold = L(u; mu_eff, wg)
-    launch_adj_tau(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, S.doldb.p, 1.0, ub, mub, wgb);
+    launch_adj_tau(ctx_, g_, vel_old_.p, mueff_.p, wg_.p, S.doldb.p, 1.0, ub, mub, wgb, fp32);
     // ---- src = -gp + rho (Coriolis(u) + act + const)
     launch_axpby(ctx_, N3, 1.0, gpb, -1.0, S.srcb.p, gpb);
     if (S_.cor) launch_adj_coriolis(ctx_, g_, S.srcb.p, S_, ub);
@@ -355,7 +355,7 @@ void Sim::adjoint_step_impl(bool seed) {
         launch_adj_wall_global(ctx_, g_, vel_old_.p, b[0] / M, b[1] / M, vmb / M, ub);
     }
     // ---- Smagorinsky: mu_eff(u)
-    if (S_.smag) launch_adj_smag(ctx_, g_, vel_old_.p, S.mub.p, S_, ub);
+    if (S_.smag) launch_adj_smag(ctx_, g_, vel_old_.p, S.mub.p, S_, ub, fp32);
     // ---- back to x^n
     launch_copy(ctx_, vel_.p, S.su.p, N3);
     launch_copy(ctx_, gp_.p, S.sgp.p, N3);

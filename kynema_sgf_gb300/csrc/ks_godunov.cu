@@ -18,6 +18,7 @@
 // taken on the integer pipe (ks_common.cuh).  Post-MAC states of rho*u are rho
 // times the traces of u (the PPM limiter and the traces are homogeneous of
 // degree one in the advected field).
+#include "ks_decide.cuh"
 #include "ks_launch.hpp"
 
 namespace ks {
@@ -40,33 +41,6 @@ __device__ inline bool face_of(const Grid& g, int d, long long t, int& i, int& j
 }
 
 inline long long nfaces(const Grid& g, int d) { return (long long)g.nx * g.ny * (d == 2 ? nzfaces(g) : g.nz); }
-
-// ---- FP64 decisions of the limiters on the integer pipe (double), plain
-// compares for the FP32 arithmetic of the mixed-precision form
-__device__ inline bool same_sign(double a, double b) { return isame_sign(a, b); }
-__device__ inline bool same_sign(float a, float b) { return a * b > 0.0f; }
-__device__ inline bool abs_lt(double a, double b) { return iabs_lt2(a, b); }  // |a| < |b|
-__device__ inline bool abs_lt(float a, float b) { return fabsf(a) < fabsf(b); }
-__device__ inline double mag_sign(double m, double s) { return isign(iabs(m), s); }  // |m| with the sign of s
-__device__ inline float mag_sign(float m, float s) { return copysignf(fabsf(m), s); }
-__device__ inline double clip2(double e, double a, double b) { return imin(imax(e, imin(a, b)), imax(a, b)); }
-__device__ inline float clip2(float e, float a, float b) { return fminf(fmaxf(e, fminf(a, b)), fmaxf(a, b)); }
-__device__ inline bool gt0(double x) { return igt0(x); }
-__device__ inline bool gt0(float x) { return x > 0.0f; }
-__device__ inline bool le0(double x) { return ile0(x); }
-__device__ inline bool le0(float x) { return x <= 0.0f; }
-__device__ inline bool ge0(double x) { return ige0(x); }
-__device__ inline bool ge0(float x) { return x >= 0.0f; }
-__device__ inline bool above_small(double u) { return dbits(u) > dbits(kSmallVel); }          // u > small_vel
-__device__ inline bool above_small(float u) { return u > (float)kSmallVel; }
-__device__ inline bool below_msmall(double u) { return okey(u) < okey(-kSmallVel); }      // u < -small_vel
-__device__ inline bool below_msmall(float u) { return u < -(float)kSmallVel; }
-__device__ inline bool below_small_abs(double u) { return iabs_lt(u, kSmallVel); }        // |u| < small_vel
-__device__ inline bool below_small_abs(float u) { return fabsf(u) < (float)kSmallVel; }
-__device__ inline double absv(double x) { return iabs(x); }
-__device__ inline float absv(float x) { return fabsf(x); }
-__device__ inline double neg_if(bool c, double x) { return c ? bitsd(dbits(x) ^ ~kMag) : x; }
-__device__ inline float neg_if(bool c, float x) { return c ? -x : x; }
 
 // van Leer limited slope of the middle cell of (a, b, c):
 // copysign(min(|dsc|, |dsl|, |dsr|), dsc) where dsl dsr > 0, else 0

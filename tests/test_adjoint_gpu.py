@@ -326,7 +326,10 @@ def test_abl_farm_one_step_vjp(cuda_dev, extra):
 
 
 def test_mixed_forward_fp64_adjoint(cuda_dev):
-    """Mixed-precision forward with the FP64 reverse sweep against FP64 finite differences."""
+    """Mixed-precision forward and its reverse sweep (the reverse of each FP32
+    Godunov / diffusion pass evaluated in FP32, every adjoint array and every
+    accumulation FP64) against the FP64 handle's adjoint of the FP64 forward
+    (1e-4 of the gradient) and against FP64 finite differences."""
     deck, lo, hi, cts = decks.abl_disks(precision="mixed", **FARM)
     sim = cuda_dev.Incflo(deck)
     sim.InitData()
@@ -335,6 +338,7 @@ def test_mixed_forward_fp64_adjoint(cuda_dev):
     ct = np.array(cts)
     J_mixed, g = adjoint(sim, x0, ct, 10, 3)
     sim.set_precision(0)
-    J64 = forward_J(sim, x0, ct, 10)
+    J64, g64 = adjoint(sim, x0, ct, 10, 3)
     assert abs(J_mixed - J64) <= 1e-6 * J64
+    assert np.abs(g - g64).max() <= 1e-4 * np.abs(g64).max(), (g, g64)
     assert fd_rel(sim, x0, ct, 10, g, 1e-6) < 1e-3
