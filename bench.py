@@ -705,15 +705,20 @@ def c4_bench(args):
     J64 = fJ(cts)
     fd = {}
     for h in (float(x) for x in args.c4_fd_h.split(",") if x):
-        est = []
+        est, fwd, bwd = [], [], []
         for k in (0, 1):
             cp, cm = list(cts), list(cts)
             cp[k] += h
             cm[k] -= h
-            est.append((fJ(cp) - fJ(cm)) / (2 * h))
+            Jp, Jm = fJ(cp), fJ(cm)
+            est.append((Jp - Jm) / (2 * h))
+            fwd.append((Jp - J64) / h)  # one-sided slopes: they differ where a jump of the discrete map lies within h
+            bwd.append((J64 - Jm) / h)
         gm = max(abs(x) for x in g[:2])
         fd["h=%g" % h] = {"fd": est, "rel_err_mixed_adjoint": [abs(a - b) / gm for a, b in zip(est, g[:2])],
-                          "rel_err_fp64_adjoint": [abs(a - b) / gm for a, b in zip(est, g64[:2])]}
+                          "rel_err_fp64_adjoint": [abs(a - b) / gm for a, b in zip(est, g64[:2])],
+                          "one_sided_fp64_adjoint_rel_err": [[abs(a - c) / gm, abs(b - c) / gm] for a, b, c in zip(fwd, bwd, g64[:2])],
+                          "J_rounding_as_slope_rel": float(np.spacing(J64)) / h / gm}
     line = {"c4": {
         "workload": "512x512x256 ABL (C1 physics, 10 m cells), 4x4 UniformCt disks D = 20 cells spaced 7 D, fixed dt 0.5 s, "
                     "J = mean 0.5|u|^2 in the rotor layer 0..5 D behind the first column, %d steps" % nsteps,

@@ -513,8 +513,10 @@ __global__ void k_pm_final(Grid g, int d, const T* lo_dd, const T* hi_dd, const 
 // pass: the face states, the two adjacent cell values and the MAC velocity are
 // loaded once for the corrections along b1 = a+1 and b2 = a+2 (each is the
 // k_adv_trans arithmetic).
+// FP64 (issue bound): 2 blocks of 256 threads per SM, 128 registers; FP32
+// (latency bound): 3 blocks, 80 registers, for half again the warps in flight
 template <typename T, int NC = 3>
-__global__ void __launch_bounds__(256, 2) k_adv_trans2(Grid g, int a, const T* vel, T rho, T cb1, T cb2, const T* ua, const T* vb1,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_adv_trans2(Grid g, int a, const T* vel, T rho, T cb1, T cb2, const T* ua, const T* vb1,
                                                        const T* vb2, C3<T> LO, C3<T> HI, C3<T> E1, C3<T> E2, P3<T> out1, P3<T> out2) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -574,7 +576,7 @@ __global__ void __launch_bounds__(256, 2) k_adv_trans2(Grid g, int a, const T* v
 // The forces enter scaled by rho for the velocity (forces = (src + divtau) / rho)
 // and as they are for a scalar (NC = 1: forces = src + diff, AdvOp_Godunov.H:114-329).
 template <typename T, int NC = 3>
-__global__ void __launch_bounds__(256, 2) k_adv_flux(Grid g, int d, const T* vel, const T* forces, T rho, T dt, T c1, T c2, C3<T> U,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_adv_flux(Grid g, int d, const T* vel, const T* forces, T rho, T dt, T c1, T c2, C3<T> U,
                                                      C3<T> LO, C3<T> HI, C3<T> T1, C3<T> T2, P3<T> Fl) {
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;

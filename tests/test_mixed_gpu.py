@@ -1,12 +1,16 @@
-"""Mixed-precision form (FP32 advection and multigrid cycles, FP64 residuals,
-defect correction, right-hand sides and velocity update) against the FP64
-form on the same deck.
+"""Mixed-precision form (FP32 advection, diffusion operator and multigrid
+cycles; FP64 residuals, defect correction, right-hand sides and velocity
+update) against the FP64 form on the same deck.
 
 Stated error (ABL deck, 64 x 64 x 32, 40 steps, against the FP64 run):
-velocity relative L2 error <= 1e-6, velocity max-norm relative error <=
-2e-4 (FP32 rounding flips PPM limiter branches at isolated cells),
-pressure-gradient max-norm error <= 5e-3; both projections still reach the
-FP64 multigrid tolerance on every step (defect correction in FP64).
+- velocity relative L2 error <= 1e-6 (the target of the stated error);
+- 99.9 % of the velocity values within 1e-6 of max|u|;
+- velocity max-norm relative error <= 2e-4: the PPM limiter, trace switch
+  and Riemann selections are discontinuous, and FP32 rounding flips them at
+  isolated cells;
+- pressure-gradient max-norm error <= 5e-3;
+- both projections reach the FP64 multigrid tolerance on every step (defect
+  correction in FP64) and the MAC divergence stays below 1e-10 relative.
 """
 import numpy as np
 import pytest
@@ -41,9 +45,11 @@ def test_mixed_matches_fp64(cuda_dev):
     v, r = mix.get_field("velocity"), ref.get_field("velocity")
     ev = rel(v, r)
     e2 = np.sqrt(((v - r) ** 2).sum() / (r ** 2).sum())
+    p999 = np.quantile(np.abs(v - r) / np.abs(r).max(), 0.999)
     eg = rel(mix.get_field("gp"), ref.get_field("gp"))
-    print("mixed vs fp64 after 40 steps: vel linf %.3e l2 %.3e gp linf %.3e" % (ev, e2, eg))
-    assert e2 < 1e-6, e2
+    print("mixed vs fp64 after 40 steps: vel l2 %.3e p99.9 %.3e linf %.3e gp linf %.3e" % (e2, p999, ev, eg))
+    assert e2 <= 1e-6, e2
+    assert p999 <= 1e-6, p999
     assert ev < 2e-4, ev
     assert eg < 5e-3, eg
 

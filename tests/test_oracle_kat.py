@@ -433,8 +433,9 @@ def quadratic_deck(n=(4, 4, 16), L=4.0):
 
 
 def test_strain_rate_exact_for_quadratics(oracle_mod):
-    """unit_tests/fvm/test_fvm_operators.cpp:258-341 checks the FVM gradient
-    on degree-2 polynomials with wall ghosts holding the wall values; on this
+    """unit_tests/fvm/test_fvm_ops.cpp:427-454 (strain rate) and
+    test_fvm_operators.cpp:258-341 (gradient) check the FVM operators on
+    degree-2 polynomials with wall ghosts holding the wall values; on this
     path the strain rate (fvm::StrainRate, central interior stencils and the
     one-sided wall stencils of stencils.H:166-330) sees the fill-patch ghosts
     (hoextrap (15 q0 - 10 q1 + 3 q2) / 8, which is the wall value of a
