@@ -388,13 +388,8 @@ inline NdCoef<T> nd_coef(const NDLevelT<T>& L, double sigma, double omega) {
 // one FMA chain from rhs with the sigma-scaled weights.
 // MODE 0: out = in + omega (rhs - A in) / diag.  MODE 1: the same plus block
 // maxima of |rhs - A in|.  MODE 2: res = rhs - A phi plus block maxima.
-template <typename T>
-__device__ inline T rhs_ld(const NDLevelT<T>& L, int idx) {
-    return __ldg(L.rhs + idx);
-}
-
 template <typename T, int MODE>
-__global__ void k_nd_col(NDLevelT<T> L, NdCoef<T> w, const T* __restrict__ in, T* __restrict__ out, int kc, double* parts, float* r32 = nullptr,
+__global__ void k_nd_col(NDLevelT<T> L, NdCoef<T> w, const T* in, T* out, int kc, double* parts, float* r32 = nullptr,
                          float* z32 = nullptr) {
     const int sz = L.nx * L.ny;
     const int nch = (L.nz + kc - 1) / kc;
@@ -406,51 +401,24 @@ __global__ void k_nd_col(NDLevelT<T> L, NdCoef<T> w, const T* __restrict__ in, T
         const int im = i == 0 ? L.nx - 1 : i - 1, ip = i + 1 == L.nx ? 0 : i + 1;
         const int cm = (j == 0 ? L.ny - 1 : j - 1) * L.nx, c0 = j * L.nx;
         const int cp = (j + 1 == L.ny ? 0 : j + 1) * L.nx;
-        // the 3 x 3 node values of plane k (wrapped / mirrored) and their sums
-        struct Raw {
-            T v[9];
-        };
-        auto load = [&](int k) {
+        auto plane = [&](int k, T& P, T& Ex, T& Ey, T& C) {
             if (L.zper) k = k < 0 ? k + L.nz : (k >= L.nz ? k - L.nz : k);
             else k = k < 0 ? -k : (k >= L.nz ? 2 * (L.nz - 1) - k : k);
             const T* q = in + k * sz;
-            return Raw{{q[cm + im], q[cm + ip], q[cp + im], q[cp + ip], q[c0 + im], q[c0 + ip], q[cm + i], q[cp + i], q[c0 + i]}};
-        };
-        auto sums = [](const Raw& r, T& P, T& Ex, T& Ey, T& C) {
-            P = (r.v[0] + r.v[1]) + (r.v[2] + r.v[3]);
-            Ex = r.v[4] + r.v[5];
-            Ey = r.v[6] + r.v[7];
-            C = r.v[8];
+            P = (q[cm + im] + q[cm + ip]) + (q[cp + im] + q[cp + ip]);
+            Ex = q[c0 + im] + q[c0 + ip];
+            Ey = q[cm + i] + q[cp + i];
+            C = q[c0 + i];
         };
         const int k0 = ch * kc, k1 = min(k0 + kc, L.nz);
         T Pm, Exm, Eym, Cm, P0, Ex0, Ey0, C0;
-        sums(load(k0 - 1), Pm, Exm, Eym, Cm);
-        sums(load(k0), P0, Ex0, Ey0, C0);
-        // FP32 (memory-latency bound): the loads of plane k + 2 and the
-        // right-hand side of node k + 1 are issued a step ahead, so they are
-        // in flight while node k is formed and stored.  FP64 (issue bound)
-        // keeps one plane in registers.
-        constexpr bool ahead = sizeof(T) == 4;
-        Raw nxt = load(k0 + 1);
-        T rnext = rhs_ld(L, k0 * sz + c0 + i);
+        plane(k0 - 1, Pm, Exm, Eym, Cm);
+        plane(k0, P0, Ex0, Ey0, C0);
         for (int k = k0; k < k1; ++k) {
             T Pp, Exp, Eyp, Cp;
+            plane(k + 1, Pp, Exp, Eyp, Cp);
             const int idx = k * sz + c0 + i;
-            T res;
-            if (ahead) {
-                const Raw cur = nxt;
-                if (k + 1 < k1) {
-                    nxt = load(k + 2);
-                    res = rnext;
-                    rnext = rhs_ld(L, idx + sz);
-                } else {
-                    res = rnext;
-                }
-                sums(cur, Pp, Exp, Eyp, Cp);
-            } else {
-                sums(load(k + 1), Pp, Exp, Eyp, Cp);
-                res = L.rhs[idx];
-            }
+            T res = L.rhs[idx];
             res = w.c13 * C0 + res;
             res = w.c9 * P0 + res;
             res = w.c3 * (Exm + Exp) + res;
