@@ -253,6 +253,29 @@ void Sim::setup(const Deck& D) {
     // Actuator disks (src/wind_energy/actuator/disk/disk_ops.cpp:182-276,
     // uniform_ct_ops.cpp:53-88)
     if (S_.act) {
+        // Disk orientation (disk_ops.cpp:125-147, 182-264): the reference vectors
+        // come from the "Coriolis" / "Coriolis.Forcing" parameters (defaults
+        // north = y, east = x); tilt turns the normal by -tilt degrees about east,
+        // then yaw by -yaw degrees about z (clockwise seen from above).
+        auto orient = [&](const std::string& k, const double* def, double* out) {
+            const std::string a = "Coriolis." + k, b = "Coriolis.Forcing." + k;
+            const std::string key = D.has(a) ? a : (D.has(b) ? b : std::string());
+            for (int m = 0; m < 3; ++m) out[m] = key.empty() ? def[m] : D.nums(key).at(m);
+        };
+        const double jhat[3] = {0.0, 1.0, 0.0}, ihat[3] = {1.0, 0.0, 0.0}, khat[3] = {0.0, 0.0, 1.0};
+        double dnorth[3], deast[3];
+        orient("north_vector", jhat, dnorth);
+        orient("east_vector", ihat, deast);
+        auto turn = [](const double* axis, double deg, double* v) {  // v rotated by deg about axis (right-handed)
+            const double am = std::sqrt(axis[0] * axis[0] + axis[1] * axis[1] + axis[2] * axis[2]);
+            const double a[3] = {axis[0] / am, axis[1] / am, axis[2] / am};
+            const double th = deg * 3.14159265358979323846 / 180.0, c = std::cos(th), sn = std::sin(th);
+            const double dd = a[0] * v[0] + a[1] * v[1] + a[2] * v[2];
+            const double x[3] = {a[1] * v[2] - a[2] * v[1], a[2] * v[0] - a[0] * v[2], a[0] * v[1] - a[1] * v[0]};
+            double o[3];
+            for (int m = 0; m < 3; ++m) o[m] = v[m] * c + x[m] * sn + a[m] * dd * (1.0 - c);
+            for (int m = 0; m < 3; ++m) v[m] = o[m];
+        };
         for (auto& lab : D.strs("Actuator.labels")) {
             const std::string type = D.str("Actuator." + lab + ".type", D.str("Actuator.type", ""));
             if (type != "UniformCtDisk") throw KsError(KS_ERR_UNSUPPORTED, "actuator type " + type);
@@ -273,21 +296,46 @@ void Sim::setup(const Deck& D) {
             if (d.nr < 1 || d.nt < 1) throw KsError(KS_ERR_DECK, "num_points_r and num_points_t must both be >=1");
             if (lc(D.str(key("spreading_type"), "LinearBasis")) != "uniformgaussian")
                 throw KsError(KS_ERR_UNSUPPORTED, "only spreading_type = UniformGaussian");
-            for (int m = 0; m < 3; ++m) { d.center[m] = 0; d.normal[m] = S_.north[m]; }
+            // check_for_parse_conflicts (disk_ops.cpp:278-300)
+            auto conflict = [&](const char* a, const char* b) {
+                if (D.has(key(a)) && D.has(key(b)))
+                    throw KsError(KS_ERR_DECK, std::string("ActuatorDisk Conflict: ") + a + " and " + b);
+            };
+            conflict("disk_normal", "yaw");
+            conflict("disk_normal", "tilt");
+            conflict("sample_normal", "sample_yaw");
+            conflict("sample_normal", "sample_tilt");
+            conflict("disk_center", "base_position");
+            conflict("disk_center", "hub_height");
+            if (D.has(key("base_position")) != D.has(key("hub_height")))
+                throw KsError(KS_ERR_DECK, "ActuatorDisk Dependency Missing: base_position and hub_height go together");
+            for (int m = 0; m < 3; ++m) { d.center[m] = 0; d.normal[m] = dnorth[m]; d.sample[m] = dnorth[m]; }
             if (D.has(key("disk_center"))) {
                 auto c = D.nums(key("disk_center"));
                 for (int m = 0; m < 3; ++m) d.center[m] = c.at(m);
             } else if (D.has(key("base_position"))) {
                 auto b = D.nums(key("base_position"));
                 for (int m = 0; m < 3; ++m) d.center[m] = b.at(m);
-                d.center[2] += D.num(key("hub_height"), 0);
+                d.center[2] += D.nums(key("hub_height")).at(0);
             }
             if (D.has(key("disk_normal"))) {
                 auto v = D.nums(key("disk_normal"));
                 for (int m = 0; m < 3; ++m) d.normal[m] = v.at(m);
             }
+            if (D.has(key("tilt"))) turn(deast, -D.nums(key("tilt")).at(0), d.normal);
+            if (D.has(key("yaw"))) turn(khat, -D.nums(key("yaw")).at(0), d.normal);
+            const bool own_sample = D.has(key("sample_normal")) || D.has(key("sample_yaw")) || D.has(key("sample_tilt"));
+            if (D.has(key("sample_normal"))) {
+                auto v = D.nums(key("sample_normal"));
+                for (int m = 0; m < 3; ++m) d.sample[m] = v.at(m);
+            }
+            if (D.has(key("sample_tilt"))) turn(deast, -D.nums(key("sample_tilt")).at(0), d.sample);
+            if (D.has(key("sample_yaw"))) turn(khat, -D.nums(key("sample_yaw")).at(0), d.sample);
+            if (!own_sample)
+                for (int m = 0; m < 3; ++m) d.sample[m] = d.normal[m];
             unit(d.normal);
-            if (d.normal[0] * d.normal[0] + d.normal[1] * d.normal[1] < 1e-28)
+            unit(d.sample);
+            if (d.normal[0] * d.normal[0] + d.normal[1] * d.normal[1] <= 2.220446049250313e-16)  // |k x n|^2 <= eps (disk_ops.cpp:335-337)
                 throw KsError(KS_ERR_DECK, "A constant Ct disk normal is too close to vertical.");
             d.cvec[0] = -d.normal[1];
             d.cvec[1] = d.normal[0];
@@ -703,7 +751,7 @@ static void rot(const double* a, double ang, const double* v, double* o) {
 // (disk_spreading.H:45-105) of one disk, x/y/z per point, ordered radius-major.
 void Sim::disk_points(const Disk& d, std::vector<double>& sample, std::vector<double>& ring) const {
     const double pi = 3.14159265358979323846;
-    const double* ax = d.normal;
+    const double* ax = d.sample;  // the sampling disk's axis (compute_disk_points with sample_vec)
     double rv[3] = {-ax[1], ax[0], 0.0};
     const double rm = std::sqrt(rv[0] * rv[0] + rv[1] * rv[1]);
     rv[0] /= rm;
@@ -719,6 +767,7 @@ void Sim::disk_points(const Disk& d, std::vector<double>& sample, std::vector<do
             for (int m = 0; m < 3; ++m) sample[3 * (ir * d.nt + it) + m] = d.center[m] + d.to_sample * d.D * ax[m] + drs * (ir + shift) * r[m];
         }
     ring.assign(3 * (size_t)np, 0.0);
+    ax = d.normal;  // the force ring lies in the disk plane
     for (int ip = 0; ip < d.nr; ++ip) {
         double pos[3];
         for (int m = 0; m < 3; ++m) pos[m] = d.center[m] + (ip + 0.5) * d.dr * d.cvec[m];
@@ -1630,6 +1679,14 @@ double Sim::scalar(const std::string& n) {
     if (n.rfind("adj_", 0) == 0 || n == "objective") return adjoint_stat(n);
     if (n.rfind("disk_ct:", 0) == 0) return disks_.at(std::stoul(n.substr(8))).ct_now;
     if (n.rfind("disk_uinf2:", 0) == 0) return disks_.at(std::stoul(n.substr(11))).uinf2;
+    if (n.rfind("disk_normal:", 0) == 0 || n.rfind("disk_sample:", 0) == 0) {  // disk_normal:<disk>:<component>
+        const size_t c = n.find(':', 12);
+        if (c == std::string::npos) throw KsError(KS_ERR_ARG, "unknown scalar " + n);
+        const Disk& d = disks_.at(std::stoul(n.substr(12, c - 12)));
+        const int m = std::stoi(n.substr(c + 1));
+        if (m < 0 || m > 2) throw KsError(KS_ERR_ARG, "unknown scalar " + n);
+        return n[5] == 'n' ? d.normal[m] : d.sample[m];
+    }
     throw KsError(KS_ERR_ARG, "unknown scalar " + n);
 }
 

@@ -158,6 +158,7 @@ struct Clock {
 
 struct Disk {
     double center[3], normal[3], cvec[3];
+    double sample[3];  // axis of the upstream sampling disk (sample_vec)
     double D, eps, to_sample, dr;
     std::vector<double> ct, ws;
     int nr, nt;

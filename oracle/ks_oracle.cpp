@@ -181,7 +181,7 @@ static void fill_periodic(Arr& a, const Geo& g, const int nodal[3]) {
 // ---------------------------------------------------------------- params
 struct DiskParams {
     std::string label;
-    double center[3] = {0, 0, 0}, normal[3] = {0, 1, 0};
+    double center[3] = {0, 0, 0}, normal[3] = {0, 1, 0}, sample[3] = {0, 1, 0};
     double diameter = 0, epsilon = 0, diameters_to_sample = 0;
     std::vector<double> ct, wind_speed;
     int nr = 1, nt = 1;
@@ -528,15 +528,65 @@ void Sim::setup(const std::string& text) {
             dp.nt = D.i(key("num_points_t"), 1);
             if (lower(D.s(key("spreading_type"), "LinearBasis")) != "uniformgaussian")
                 throw Error(ERR_UNSUPPORTED, "only spreading_type = UniformGaussian");
+            // ops::base::check_for_parse_conflicts (disk_ops.cpp:278-300)
+            const char* pairs[6][2] = {{"disk_normal", "yaw"}, {"disk_normal", "tilt"}, {"sample_normal", "sample_yaw"},
+                                       {"sample_normal", "sample_tilt"}, {"disk_center", "base_position"}, {"disk_center", "hub_height"}};
+            for (auto& pr : pairs)
+                if (D.has(key(pr[0])) && D.has(key(pr[1]))) throw Error(ERR_DECK, std::string("ActuatorDisk Conflict: ") + pr[0] + " and " + pr[1]);
+            if (D.has(key("base_position")) != D.has(key("hub_height"))) throw Error(ERR_DECK, "base_position requires hub_height");
             if (D.has(key("disk_center"))) { auto c = D.v(key("disk_center")); for (int d = 0; d < 3; ++d) dp.center[d] = c.at(d); }
             else if (D.has(key("base_position"))) {
-                auto b = D.v(key("base_position")); double hh = D.d(key("hub_height"), 0);
+                auto b = D.v(key("base_position")); double hh = D.v(key("hub_height")).at(0);
                 for (int d = 0; d < 3; ++d) dp.center[d] = b.at(d);
                 dp.center[2] += hh;
             }
-            for (int d = 0; d < 3; ++d) dp.normal[d] = north[d];
+            // ops::base::optional_parameters (disk_ops.cpp:182-264): reference
+            // vectors from the "Coriolis" (then "Coriolis.Forcing") parameters;
+            // normal = R_z(-yaw) R_east(-tilt) normal0, with the rotation tensors
+            // (vs::zrot, vs::quaternion) applied as v & T = T^T v
+            double dn[3] = {0, 1, 0}, de[3] = {1, 0, 0};
+            for (const char* pre : {"Coriolis.Forcing.", "Coriolis."}) {
+                if (D.has(std::string(pre) + "north_vector")) { auto v = D.v(std::string(pre) + "north_vector"); for (int d = 0; d < 3; ++d) dn[d] = v.at(d); }
+                if (D.has(std::string(pre) + "east_vector")) { auto v = D.v(std::string(pre) + "east_vector"); for (int d = 0; d < 3; ++d) de[d] = v.at(d); }
+            }
+            for (int d = 0; d < 3; ++d) { dp.normal[d] = dn[d]; dp.sample[d] = dn[d]; }
             if (D.has(key("disk_normal"))) { auto nn = D.v(key("disk_normal")); for (int d = 0; d < 3; ++d) dp.normal[d] = nn.at(d); }
+            if (D.has(key("sample_normal"))) { auto nn = D.v(key("sample_normal")); for (int d = 0; d < 3; ++d) dp.sample[d] = nn.at(d); }
+            auto apply = [&](double* v, const char* tilt_key, const char* yaw_key) {
+                double T[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+                auto mul = [&](const double* B) {  // T = T B
+                    double R[9];
+                    for (int a = 0; a < 3; ++a)
+                        for (int b = 0; b < 3; ++b) R[3 * a + b] = T[3 * a] * B[b] + T[3 * a + 1] * B[3 + b] + T[3 * a + 2] * B[6 + b];
+                    for (int q = 0; q < 9; ++q) T[q] = R[q];
+                };
+                if (D.has(key(tilt_key))) {  // vs::quaternion(east, -tilt)
+                    const double ang = -(-D.v(key(tilt_key)).at(0)) * kPi / 180.0;
+                    const double am = std::sqrt(de[0] * de[0] + de[1] * de[1] + de[2] * de[2]);
+                    const double q0 = std::cos(0.5 * ang), sv = std::sin(0.5 * ang);
+                    const double q1 = sv * de[0] / am, q2 = sv * de[1] / am, q3 = sv * de[2] / am;
+                    const double Q[9] = {q0 * q0 + q1 * q1 - q2 * q2 - q3 * q3, 2 * (q1 * q2 - q0 * q3), 2 * (q0 * q2 + q1 * q3),
+                                         2 * (q1 * q2 + q0 * q3), q0 * q0 - q1 * q1 + q2 * q2 - q3 * q3, 2 * (q2 * q3 - q0 * q1),
+                                         2 * (q1 * q3 - q0 * q2), 2 * (q0 * q1 + q2 * q3), q0 * q0 - q1 * q1 - q2 * q2 + q3 * q3};
+                    mul(Q);
+                }
+                if (D.has(key(yaw_key))) {  // vs::zrot(-yaw)
+                    const double ang = -D.v(key(yaw_key)).at(0) * kPi / 180.0, c = std::cos(ang), sn = std::sin(ang);
+                    const double Z[9] = {c, sn, 0, -sn, c, 0, 0, 0, 1};
+                    mul(Z);
+                }
+                const double o[3] = {T[0] * v[0] + T[3] * v[1] + T[6] * v[2], T[1] * v[0] + T[4] * v[1] + T[7] * v[2],
+                                     T[2] * v[0] + T[5] * v[1] + T[8] * v[2]};
+                for (int d = 0; d < 3; ++d) v[d] = o[d];
+            };
+            apply(dp.normal, "tilt", "yaw");
+            apply(dp.sample, "sample_tilt", "sample_yaw");
+            if (!D.has(key("sample_normal")) && !D.has(key("sample_tilt")) && !D.has(key("sample_yaw")))
+                for (int d = 0; d < 3; ++d) dp.sample[d] = dp.normal[d];
             nrm(dp.normal);
+            nrm(dp.sample);
+            if (dp.normal[0] * dp.normal[0] + dp.normal[1] * dp.normal[1] <= 2.220446049250313e-16)
+                throw Error(ERR_DECK, "A constant Ct disk normal is too close to vertical.");
             dp.diameters_to_sample = D.d(key("diameters_to_sample"), 0.0);
             dp.about_center = D.i(key("ks_spread_about_center"), 0) != 0;
             // coplanar vector k x n (disk_ops.cpp:278-282)
@@ -2084,7 +2134,7 @@ void Sim::actuator_update() {
         const double R = 0.5 * dp.diameter;
         // sampling points on the upstream (sample) disk
         double ref[3] = {0, 0, 0};
-        const double* ax = dp.normal;
+        const double* ax = dp.sample;  // the sampling disk is normal to sample_vec (compute_disk_points)
         double refv[3] = {-ax[1], ax[0], 0.0};
         {
             double m = std::sqrt(refv[0] * refv[0] + refv[1] * refv[1]);
@@ -2121,6 +2171,7 @@ void Sim::actuator_update() {
             }
         }
         for (int n = 0; n < 3; ++n) dp.ref_vel[n] = ref[n];
+        ax = dp.normal;  // U_inf is the sampled velocity along the disk normal; the force ring lies in the disk plane
         const double un = ref[0] * ax[0] + ref[1] * ax[1] + ref[2] * ax[2];
         dp.uinf_sqr = un * un;
         // linear table with end clamping
@@ -2831,6 +2882,12 @@ double kso_get_scalar(void* h, const char* name) {
     if (n == "density") return s.rho;
     if (n.rfind("disk_ct:", 0) == 0) return s.disks.at(std::stoi(n.substr(8))).current_ct;
     if (n.rfind("disk_uinf2:", 0) == 0) return s.disks.at(std::stoi(n.substr(11))).uinf_sqr;
+    if (n.rfind("disk_normal:", 0) == 0 || n.rfind("disk_sample:", 0) == 0) {
+        const size_t c = n.find(':', 12);
+        const auto& dp = s.disks.at(std::stoi(n.substr(12, c - 12)));
+        const int m = std::stoi(n.substr(c + 1));
+        return n[5] == 'n' ? dp.normal[m] : dp.sample[m];
+    }
     return NAN;
 }
 

@@ -3,15 +3,17 @@ cuda:0) as the oracle's copies in test_oracle_kat.py check the restatement:
 BodyForce (unit_tests/wind_energy/test_abl_src.cpp:115-160), the hydrostatic
 pressure of a projected column (unit_tests/projection/test_pressure_offset.cpp:
 173-203), the wall-model stress in the first layer's diffusion term
-(unit_tests/wind_energy/test_abl_bc.cpp:69-170) and the strain rate of
-quadratic profiles at wall cells (unit_tests/fvm/test_fvm_operators.cpp:258-341).
+(unit_tests/wind_energy/test_abl_bc.cpp:69-170), the strain rate of
+quadratic profiles at wall cells (unit_tests/fvm/test_fvm_operators.cpp:258-341)
+and the disk orientation from yaw / tilt
+(unit_tests/wind_energy/actuator/test_disk_uniform_ct.cpp:35-294).
 """
 import numpy as np
 import pytest
 
 from kynema_sgf_gb300 import decks
-from test_oracle_kat import (EPS, hydrostatic_column, hydrostatic_deck, quadratic_deck, quadratic_strain_mueff, quadratic_velocity,
-                             wall_model_deck, wall_model_gold)
+from test_oracle_kat import (DISK_ORIENT_GOLDS, EPS, check_disk_orientation, disk_orient_deck, hydrostatic_column, hydrostatic_deck,
+                             quadratic_deck, quadratic_strain_mueff, quadratic_velocity, wall_model_deck, wall_model_gold)
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-9
@@ -90,3 +92,36 @@ def test_strain_rate_exact_for_quadratics(cuda_dev):
     dx = (1.0 / n[0], 1.0 / n[1], L / n[2])
     mu = g.get_field("velocity_mueff")[0]
     assert np.allclose(mu, quadratic_strain_mueff(shape, L, 0.16, dx), rtol=1.0e6 * EPS, atol=0)
+
+
+@pytest.mark.parametrize("case", range(len(DISK_ORIENT_GOLDS)))
+def test_disk_orientation_golds(cuda_dev, case):
+    keys, cor, normal, sample = DISK_ORIENT_GOLDS[case]
+    check_disk_orientation(cuda_dev.Incflo(disk_orient_deck(keys, cor)), normal, sample)
+
+
+def test_disk_orientation_errors(cuda_dev):
+    for keys in ("yaw = 270;tilt = -90", "disk_normal = 1 0 0;yaw = 10", "sample_normal = 1 0 0;sample_tilt = 10"):
+        with pytest.raises(cuda_dev.KsError) as e:
+            cuda_dev.Incflo(disk_orient_deck(keys))
+        assert e.value.code == 1, keys
+
+
+def test_yawed_disk_steps(cuda_dev, oracle_mod):
+    """A disk yawed 80 degrees and tilted 5, sampling upstream along its own
+    vector (sample_yaw 60, sample_tilt -10, 1.5 diameters): the sampled U_inf,
+    Ct, actuator source and state agree with the oracle after every step."""
+    d = disk_orient_deck("yaw = 80;tilt = 5;sample_yaw = 60;sample_tilt = -10;diameters_to_sample = 1.5;ks_spread_about_center = 1",
+                         "ks_init.noise_amplitude = 0.2\nks_init.noise_seed = 3")
+    g, o = cuda_dev.Incflo(d), oracle_mod.Oracle(d)
+    g.InitData()
+    o.InitData()
+    for _ in range(2):
+        assert g.step() and o.step()
+        ug, uo = g.scalar("disk_uinf2:0"), o.scalar("disk_uinf2:0")
+        assert abs(ug - uo) < 1e-9 * uo
+        for f in ("actuator_src_term", "velocity", "p"):
+            a, b = g.get_field(f), o.get_field(f)
+            if f == "p":
+                a, b = a - a.mean(), b - b.mean()
+            assert rel(a, b) < TOL, f

@@ -449,3 +449,87 @@ def test_strain_rate_exact_for_quadratics(oracle_mod):
     dx = (1.0 / n[0], 1.0 / n[1], L / n[2])
     mu = o.get_field("velocity_mueff")[0]
     assert np.allclose(mu, quadratic_strain_mueff(shape, L, 0.16, dx), rtol=1.0e6 * EPS, atol=0)
+
+
+def disk_orient_deck(extra="", coriolis=""):
+    """One uniform-Ct disk in a 16^3 box; `extra` adds keys of the disk."""
+    lines = "\n".join("Actuator.T0.%s" % e for e in extra.split(";") if e.strip())
+    return f"""
+geometry.prob_lo = 0 0 0
+geometry.prob_hi = 160 160 160
+geometry.is_periodic = 1 1 1
+amr.n_cell = 16 16 16
+incflo.physics = FreeStream
+incflo.velocity = 8.0 0.0 0.0
+transport.viscosity = 1e-5
+turbulence.model = Laminar
+ICNS.source_terms = ActuatorForcing
+Actuator.labels = T0
+Actuator.type = UniformCtDisk
+Actuator.UniformCtDisk.rotor_diameter = 40
+Actuator.UniformCtDisk.epsilon = 10
+Actuator.UniformCtDisk.thrust_coeff = 0.75
+Actuator.UniformCtDisk.num_points_r = 3
+Actuator.UniformCtDisk.num_points_t = 4
+Actuator.UniformCtDisk.spreading_type = UniformGaussian
+Actuator.T0.disk_center = 80 80 80
+{lines}
+{coriolis}
+incflo.use_godunov = 1
+incflo.godunov_type = ppm
+incflo.diffusion_type = 0
+time.cfl = 0.5
+time.max_step = 2
+"""
+
+
+DIFFERENT_NORTH = "Coriolis.Forcing.north_vector = 1 0 0\nCoriolis.Forcing.east_vector = 0 -1 0"
+_R2 = math.sqrt(0.5)
+# (disk keys, Coriolis keys, gold normal, gold sample vector): the cases of
+# unit_tests/wind_energy/actuator/test_disk_uniform_ct.cpp:35-166, 218-294
+DISK_ORIENT_GOLDS = [
+    ("yaw = 90;sample_yaw = 45", "", (1, 0, 0), (_R2, _R2, 0)),
+    ("yaw = 270;sample_yaw = -315;sample_tilt = -45", "", (-1, 0, 0), (0.5, 0.5, _R2)),
+    ("", DIFFERENT_NORTH, (1, 0, 0), (1, 0, 0)),
+    ("yaw = 90;sample_yaw = 45;sample_tilt = -45", DIFFERENT_NORTH, (0, -1, 0), (0.5, -0.5, _R2)),
+    ("yaw = 0", "", (0, 1, 0), (0, 1, 0)),
+    ("yaw = 180", "", (0, -1, 0), (0, -1, 0)),
+    ("yaw = 270", "", (-1, 0, 0), (-1, 0, 0)),
+    ("yaw = 90", "", (1, 0, 0), (1, 0, 0)),
+    ("sample_yaw = 0", "", (0, 1, 0), (0, 1, 0)),
+    ("sample_yaw = 180", "", (0, 1, 0), (0, -1, 0)),
+    ("sample_yaw = 270", "", (0, 1, 0), (-1, 0, 0)),
+    ("sample_yaw = 90", "", (0, 1, 0), (1, 0, 0)),
+]
+
+
+def check_disk_orientation(sim, normal, sample):
+    for m in range(3):
+        assert abs(sim.scalar("disk_normal:0:%d" % m) - normal[m]) < 1e4 * EPS
+        assert abs(sim.scalar("disk_sample:0:%d" % m) - sample[m]) < 1e4 * EPS
+
+
+@pytest.mark.parametrize("case", range(len(DISK_ORIENT_GOLDS)))
+def test_disk_orientation_golds(oracle_mod, case):
+    """Disk normal and sampling vector from yaw / tilt / sample_yaw /
+    sample_tilt and the Coriolis north / east vectors
+    (ops::base::optional_parameters, disk_ops.cpp:182-264): the reference's
+    golds, including a yaw of 0 / 180 / 270 / 90 degrees pointing the normal
+    against a wind from north / south / west / east."""
+    keys, cor, normal, sample = DISK_ORIENT_GOLDS[case]
+    check_disk_orientation(oracle_mod.Oracle(disk_orient_deck(keys, cor)), normal, sample)
+
+
+@pytest.mark.parametrize("keys", ["yaw = 270;tilt = -90", "disk_normal = 1 0 0;yaw = 10", "sample_normal = 1 0 0;sample_tilt = 10",
+                                  "base_position = 80 80 0"])
+def test_disk_orientation_errors(oracle_mod, keys):
+    """A tilt of -90 degrees points the normal up, which the coplanar vector
+    rejects (test_disk_uniform_ct.cpp:93-97); disk_normal with yaw / tilt,
+    sample_normal with sample_yaw / sample_tilt and base_position without
+    hub_height are parse conflicts (disk_ops.cpp:278-300)."""
+    d = disk_orient_deck(keys)
+    if "base_position" in keys:
+        d = d.replace("Actuator.T0.disk_center = 80 80 80\n", "")
+    with pytest.raises(oracle_mod.OracleError) as e:
+        oracle_mod.Oracle(d)
+    assert e.value.code == 1
