@@ -228,6 +228,9 @@ void Sim::setup(const Deck& D) {
     // residual)), so a solve ends at the same tolerance as one from zero, in fewer V-cycles.
     mg_warm_ = D.flag("ks.mg_warm_start", 1);
     mg_graphs_ = D.flag("ks.mg_graphs", 1);  // coarse V-cycle levels as CUDA graphs (not a reference key)
+    // mixed precision: FP32 V-cycles per FP64 defect-correction residual (not a reference key)
+    mg_inner_ = D.flag("ks.mixed_inner_cycles", 2);
+    if (mg_inner_ < 1) throw KsError(KS_ERR_DECK, "ks.mixed_inner_cycles must be >= 1");
     restart_file_ = D.str("io.restart_file", "");
     plt_prefix_ = D.str("io.plot_file", "plt");
     chk_prefix_ = D.str("io.check_file", "chk");
@@ -1010,15 +1013,17 @@ void Sim::mac_project() {
     int it = 0;
     double rn = r0;
     while (rn > target && it < mac_.maxiter) {
-        if (mixed_) {
-            cc_vcycle(cc32_, 0, beta);
+        int inner = 1;
+        if (mixed_) {  // up to mg_inner_ FP32 V-cycles on the correction equation (as the nodal solve)
+            inner = std::min(mg_inner_, mac_.maxiter - it);
+            for (int c = 0; c < inner; ++c) cc_vcycle(cc32_, 0, beta);
             launch_add_f32(ctx_, L.phi, cc32_[0].phi, g_.N);
         } else {
             cc_vcycle(cc_, 0, beta);
         }
         resid();
         rn = reduce(np, 1, 1, nullptr);
-        ++it;
+        it += inner;
         if (!std::isfinite(rn)) throw KsError(KS_ERR_NONFINITE, "MAC projection diverged");
         if (rn > 1e20 * r0) throw KsError(KS_ERR_NOT_CONVERGED, "MAC projection diverged (residual above 1e20 times the initial one)");
     }
@@ -1099,11 +1104,15 @@ void Sim::nd_solve(double sigma) {
         target = std::max(nod_.atol, nod_.rtol * std::max(nod_bnorm_, r0));
         rn = r0;
         while (rn > target && it < nod_.maxiter) {
-            nd_vcycle(nd32_, 0, sigma);
+            // the correction equation gets up to mg_inner_ FP32 V-cycles (each
+            // continues from the last; FP32 holds the correction to ~1e-7 of
+            // the FP64 residual, far below one cycle's 0.1 contraction)
+            const int inner = std::min(mg_inner_, nod_.maxiter - it);
+            for (int c = 0; c < inner; ++c) nd_vcycle(nd32_, 0, sigma);
             launch_add_f32(ctx_, L.phi, nd32_[0].phi, M);
             launch_nd_resid32(ctx_, L, sigma, nd32_[0].rhs, nd32_[0].phi, parts_.p, &np);
             rn = reduce(np, 1, 1, nullptr);
-            ++it;
+            it += inner;
             if (!std::isfinite(rn)) throw KsError(KS_ERR_NONFINITE, "nodal projection diverged");
             if (rn > 1e20 * r0) throw KsError(KS_ERR_NOT_CONVERGED, "nodal projection diverged (residual above 1e20 times the initial one)");
         }

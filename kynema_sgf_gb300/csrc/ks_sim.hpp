@@ -305,6 +305,7 @@ class Sim {
     MGGraph gcc_[2], gnd_[2];  // [FP64, FP32] MAC and nodal tails
     size_t glev_ = 0;          // first graphed level (0: none)
     int mg_graphs_ = 1;        // ks.mg_graphs
+    int mg_inner_ = 2;         // ks.mixed_inner_cycles
     template <typename F>
     void mg_graph_run(MGGraph& G, double key, F&& body);
    public:
