@@ -456,6 +456,80 @@ __global__ void k_nd_col(NDLevelT<T> L, NdCoef<T> w, const T* in, T* out, int kc
     }
 }
 
+// FP32 form of k_nd_col for the sweeps (MODE 0) and residuals (MODE 2) of the
+// mixed-precision cycles: two nodes per step of the column, so the loads of
+// planes k + 1 and k + 2 are in flight together.  The FP32 sweep waits on
+// memory latency rather than on issue (one plane of loads per step kept each
+// warp idle for most of a DRAM round trip).
+template <int MODE>
+__global__ void __launch_bounds__(256, 4) k_nd_col2(NDLevelT<float> L, NdCoef<float> w, const float* in, float* out, int kc,
+                                                    double* parts) {
+    const int sz = L.nx * L.ny;
+    const int nch = (L.nz + kc - 1) / kc;
+    const unsigned M = (unsigned)(sz * nch);
+    MaxAbs<float> mx;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < M; t += gridDim.x * blockDim.x) {
+        int i, j, ch;
+        split3(t, (unsigned)L.nx, (unsigned)L.ny, i, j, ch);
+        const int im = i == 0 ? L.nx - 1 : i - 1, ip = i + 1 == L.nx ? 0 : i + 1;
+        const int cm = (j == 0 ? L.ny - 1 : j - 1) * L.nx, c0 = j * L.nx;
+        const int cp = (j + 1 == L.ny ? 0 : j + 1) * L.nx;
+        auto plane = [&](int k, float& P, float& Ex, float& Ey, float& C) {
+            if (L.zper) k = k < 0 ? k + L.nz : (k >= L.nz ? k - L.nz : k);
+            else k = k < 0 ? -k : (k >= L.nz ? 2 * (L.nz - 1) - k : k);
+            const float* q = in + k * sz;
+            P = (q[cm + im] + q[cm + ip]) + (q[cp + im] + q[cp + ip]);
+            Ex = q[c0 + im] + q[c0 + ip];
+            Ey = q[cm + i] + q[cp + i];
+            C = q[c0 + i];
+        };
+        auto node = [&](float res, float Pm, float Exm, float Eym, float Cm, float P0, float Ex0, float Ey0, float C0, float Pp, float Exp,
+                        float Eyp, float Cp, int idx) {
+            res = w.c13 * C0 + res;
+            res = w.c9 * P0 + res;
+            res = w.c3 * (Exm + Exp) + res;
+            res = w.c1 * (Eym + Eyp) + res;
+            res = w.c0 * (Pm + Pp) + res;
+            if (!L.faces_zero) {
+                res = w.c12 * Ex0 + res;
+                res = w.c10 * Ey0 + res;
+                res = w.c4 * (Cm + Cp) + res;
+            }
+            if (MODE == 2) L.res[idx] = res;
+            else out[idx] = w.oinv * res + C0;
+            if (MODE == 2) mx.add(res);
+        };
+        const int k0 = ch * kc, k1 = min(k0 + kc, L.nz);
+        float Pm, Exm, Eym, Cm, P0, Ex0, Ey0, C0;
+        plane(k0 - 1, Pm, Exm, Eym, Cm);
+        plane(k0, P0, Ex0, Ey0, C0);
+        for (int k = k0; k < k1; k += 2) {
+            const bool two = k + 1 < k1;
+            const int idx = k * sz + c0 + i;
+            float Pp, Exp, Eyp, Cp, Pq = 0.0f, Exq = 0.0f, Eyq = 0.0f, Cq = 0.0f, r1 = 0.0f;
+            plane(k + 1, Pp, Exp, Eyp, Cp);
+            const float r0 = L.rhs[idx];
+            if (two) {
+                plane(k + 2, Pq, Exq, Eyq, Cq);
+                r1 = L.rhs[idx + sz];
+            }
+            node(r0, Pm, Exm, Eym, Cm, P0, Ex0, Ey0, C0, Pp, Exp, Eyp, Cp, idx);
+            if (two) {
+                node(r1, P0, Ex0, Ey0, C0, Pp, Exp, Eyp, Cp, Pq, Exq, Eyq, Cq, idx + sz);
+                Pm = Pp; Exm = Exp; Eym = Eyp; Cm = Cp;
+                P0 = Pq; Ex0 = Exq; Ey0 = Eyq; C0 = Cq;
+            } else {
+                Pm = P0; Exm = Ex0; Eym = Ey0; Cm = C0;
+                P0 = Pp; Ex0 = Exp; Ey0 = Eyp; C0 = Cp;
+            }
+        }
+    }
+    if (MODE == 2) {
+        const double m = bred<1>(mx.get());
+        if (threadIdx.x == 0 && parts) parts[blockIdx.x] = m;
+    }
+}
+
 // planes per thread: long columns on the large levels, short ones on the
 // coarse levels so that they still fill the GPU
 template <typename T>
@@ -647,15 +721,22 @@ void launch_cc_bottom(Ctx& c, const CCLevelT<T>& L, double beta, int sweeps) {
 template <typename T>
 void launch_nd_jacobi(Ctx& c, const NDLevelT<T>& L, double sigma, double omega, const T* in, T* out) {
     const int kc = nd_chunk(L);
-    KS_LAUNCH(c, (k_nd_col<T, 0>), nblocks(nd_cols(L, kc), BS), BS, sizeof(T) * 3.0 * nnd(L), L, nd_coef(L, sigma, omega), in, out, kc,
-              nullptr);
+    if constexpr (sizeof(T) == 4)
+        KS_LAUNCH(c, k_nd_col2<0>, nblocks(nd_cols(L, kc), BS), BS, sizeof(T) * 3.0 * nnd(L), L, nd_coef(L, sigma, omega), in, out, kc,
+                  nullptr);
+    else
+        KS_LAUNCH(c, (k_nd_col<T, 0>), nblocks(nd_cols(L, kc), BS), BS, sizeof(T) * 3.0 * nnd(L), L, nd_coef(L, sigma, omega), in, out, kc,
+                  nullptr);
 }
 template <typename T>
 void launch_nd_resid(Ctx& c, const NDLevelT<T>& L, double sigma, double* parts, int* np) {
     const int kc = nd_chunk(L);
     const int n = parts_for(nd_cols(L, kc));
     if (np) *np = n;
-    KS_LAUNCH(c, (k_nd_col<T, 2>), n, BS, sizeof(T) * 3.0 * nnd(L), L, nd_coef(L, sigma, 0.0), (const T*)L.phi, (T*)nullptr, kc, parts);
+    if constexpr (sizeof(T) == 4)
+        KS_LAUNCH(c, k_nd_col2<2>, n, BS, sizeof(T) * 3.0 * nnd(L), L, nd_coef(L, sigma, 0.0), (const T*)L.phi, (T*)nullptr, kc, parts);
+    else
+        KS_LAUNCH(c, (k_nd_col<T, 2>), n, BS, sizeof(T) * 3.0 * nnd(L), L, nd_coef(L, sigma, 0.0), (const T*)L.phi, (T*)nullptr, kc, parts);
 }
 template <typename T>
 void launch_nd_restrict(Ctx& c, const NDLevelT<T>& F, const NDLevelT<T>& C) {
