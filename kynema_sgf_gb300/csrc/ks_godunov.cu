@@ -509,110 +509,245 @@ __global__ void k_pm_final(Grid g, int d, const T* lo_dd, const T* hi_dd, const 
     mac[f] = (double)riemann(stl, sth);
 }
 
-// ---- post-MAC stage 2 for both transverse directions of the a-faces in one
-// pass: the face states, the two adjacent cell values and the MAC velocity are
-// loaded once for the corrections along b1 = a+1 and b2 = a+2 (each is the
-// k_adv_trans arithmetic).
-// FP64 (issue bound): 2 blocks of 256 threads per SM, 128 registers; FP32
-// (latency bound): 3 blocks, 80 registers, for half again the warps in flight
-template <typename T, int NC = 3>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_adv_trans2(Grid g, int a, const T* vel, T rho, T cb1, T cb2, const T* ua, const T* vb1,
-                                                       const T* vb2, C3<T> LO, C3<T> HI, C3<T> E1, C3<T> E2, P3<T> out1, P3<T> out2) {
-    int i, j, k;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (!face_of(g, a, t, i, j, k)) return;
-    VelFPT<T, T> q{vel, g, T(1)};
-    const bool wl = (a == 2 && !g.zper && k == 0), wh = (a == 2 && !g.zper && k == g.nz);
-    const long long f = fidx(g, a, i, j, k);
-    const T u = (T)ua[f];
-    const int ci = i - (a == 0), cj = j - (a == 1), ck = k - (a == 2);
-    const int b1 = (a + 1) % 3, b2 = (a + 2) % 3;
-    auto fc = [&](int b, int ii, int jj, int kk, long long& m, long long& p) {
-        m = fidx(g, b, ii, jj, kk);
-        p = fidx(g, b, ii + (b == 0), jj + (b == 1), kk + (b == 2));
-    };
-    long long h0a, h1a, l0a, l1a, h0b, h1b, l0b, l1b;
-    fc(b1, i, j, k, h0a, h1a);
-    fc(b1, ci, cj, ck, l0a, l1a);
-    fc(b2, i, j, k, h0b, h1b);
-    fc(b2, ci, cj, ck, l0b, l1b);
-    T vhp1 = T(0), vhm1 = T(0), vlp1 = T(0), vlm1 = T(0), vhp2 = T(0), vhm2 = T(0), vlp2 = T(0), vlm2 = T(0);
-    if (!wh) {
-        vhp1 = (T)vb1[h1a];
-        vhm1 = (T)vb1[h0a];
-        vhp2 = (T)vb2[h1b];
-        vhm2 = (T)vb2[h0b];
+// ---- post-MAC stage 2: the a-face states corrected along both transverse
+// directions b1 = a+1 and b2 = a+2 (conservative form, dt/3 corner factors).
+// Stage 2 by cells: the corrections of a face state along b1 and b2 depend only
+// on the cell the state is traced from,
+//   corr_b(c) = q(c) rho cb (v_b+ - v_b-) - cb (v_b+ E_b(+) - v_b- E_b(-))
+// over the b faces of c, so that each state is its stage-1 value plus the
+// corr of its cell; the kernels below form each cell's pair once.
+template <typename T, int NC>
+struct TransCell {
+    Grid g;
+    int a, b1, b2;
+    const T* vel;
+    T rho, cb1, cb2;
+    const T *vb1, *vb2;
+    C3<T> E1, E2;
+    __device__ inline void operator()(int i, int j, int k, T c1[NC], T c2[NC]) const {
+        const long long p1 = fidx(g, b1, i + (b1 == 0), j + (b1 == 1), k + (b1 == 2)), m1 = fidx(g, b1, i, j, k);
+        const long long p2 = fidx(g, b2, i + (b2 == 0), j + (b2 == 1), k + (b2 == 2)), m2 = fidx(g, b2, i, j, k);
+        const T v1p = (T)vb1[p1], v1m = (T)vb1[m1], v2p = (T)vb2[p2], v2m = (T)vb2[m2];
+        const T r1 = rho * cb1 * (v1p - v1m), r2 = rho * cb2 * (v2p - v2m);
+        const VelFPT<T, T> q{vel, g, T(1)};
+        for (int n = 0; n < NC; ++n) {
+            const T qc = q(n, i, j, k);
+            c1[n] = qc * r1 - cb1 * (v1p * E1.p[n][p1] - v1m * E1.p[n][m1]);
+            c2[n] = qc * r2 - cb2 * (v2p * E2.p[n][p2] - v2m * E2.p[n][m2]);
+        }
     }
-    if (!wl) {
-        vlp1 = (T)vb1[l1a];
-        vlm1 = (T)vb1[l0a];
-        vlp2 = (T)vb2[l1b];
-        vlm2 = (T)vb2[l0b];
-    }
-    // rho cb (v+ - v-) of each correction, shared by the components: the cell
-    // values enter unscaled
-    const T rh1 = rho * cb1 * (vhp1 - vhm1), rl1 = rho * cb1 * (vlp1 - vlm1);
-    const T rh2 = rho * cb2 * (vhp2 - vhm2), rl2 = rho * cb2 * (vlp2 - vlm2);
+};
+
+template <typename T, int NC>
+__device__ inline void trans_out(const Grid& g, int a, int k, long long f, T u, const C3<T>& LO, const C3<T>& HI, bool wl, bool wh,
+                                 const T* l1, const T* l2, const T* h1, const T* h2, P3<T>& out1, P3<T>& out2) {
     const bool usmall = below_small_abs(u), upos = ge0(u);
     auto pick = [&](T l, T h) { return usmall ? T(0.5) * (l + h) : (upos ? l : h); };
     for (int n = 0; n < NC; ++n) {
         const T l0 = LO.p[n][f], h0 = HI.p[n][f];
-        const T qh = wh ? T(0) : q(n, i, j, k), ql = wl ? T(0) : q(n, ci, cj, ck);
-        T l = l0, h = h0;
-        if (!wh) h = qh * rh1 + (h0 - cb1 * (vhp1 * E1.p[n][h1a] - vhm1 * E1.p[n][h0a]));
-        if (!wl) l = ql * rl1 + (l0 - cb1 * (vlp1 * E1.p[n][l1a] - vlm1 * E1.p[n][l0a]));
+        T l = wl ? l0 : l0 + l1[n], h = wh ? h0 : h0 + h1[n];
         if (a == 2) zbc(g, k, n, l, h);
         out1.p[n][f] = pick(l, h);
-        l = l0;
-        h = h0;
-        if (!wh) h = qh * rh2 + (h0 - cb2 * (vhp2 * E2.p[n][h1b] - vhm2 * E2.p[n][h0b]));
-        if (!wl) l = ql * rl2 + (l0 - cb2 * (vlp2 * E2.p[n][l1b] - vlm2 * E2.p[n][l0b]));
+        l = wl ? l0 : l0 + l2[n];
+        h = wh ? h0 : h0 + h2[n];
         if (a == 2) zbc(g, k, n, l, h);
         out2.p[n][f] = pick(l, h);
+    }
+}
+
+// x faces: lanes along a row, the low cell's corrections from the previous lane
+template <typename T, int NC = 3>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_adv_trans_x(TransCell<T, NC> C, const T* ua, C3<T> LO, C3<T> HI, P3<T> out1,
+                                                                             P3<T> out2) {
+    const Grid& g = C.g;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const bool live = t < g.N;
+    int i = 0, j = 0, k = 0;
+    T h1[NC], h2[NC], l1[NC], l2[NC];
+    for (int n = 0; n < NC; ++n) h1[n] = h2[n] = T(0);
+    if (live) {
+        const unsigned u = (unsigned)t, r = u / (unsigned)g.nx;
+        i = (int)(u - r * (unsigned)g.nx);
+        k = (int)(r / (unsigned)g.ny);
+        j = (int)(r - (unsigned)k * (unsigned)g.ny);
+        C(i, j, k, h1, h2);
+    }
+    for (int n = 0; n < NC; ++n) {
+        l1[n] = __shfl_up_sync(0xffffffffu, h1[n], 1);
+        l2[n] = __shfl_up_sync(0xffffffffu, h2[n], 1);
+    }
+    if (!live) return;
+    if ((threadIdx.x & 31) == 0 || i == 0) C(i == 0 ? g.nx - 1 : i - 1, j, k, l1, l2);
+    trans_out<T, NC>(g, 0, k, t, (T)ua[t], LO, HI, false, false, l1, l2, h1, h2, out1, out2);
+}
+
+// y and z faces: a thread per (i, other index) marches a chunk of faces along a
+template <typename T, int NC = 3>
+__global__ void __launch_bounds__(128) k_adv_trans_col(TransCell<T, NC> C, const T* ua, C3<T> LO, C3<T> HI, P3<T> out1, P3<T> out2, int chunk) {
+    const Grid& g = C.g;
+    const int a = C.a;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.nx) return;
+    const int nf = a == 1 ? g.ny : nzfaces(g);
+    const int no = a == 1 ? g.nz : g.ny;
+    const int o = (int)(blockIdx.y % (unsigned)no), chn = (int)(blockIdx.y / (unsigned)no);
+    const int m0 = chn * chunk, m1 = min(m0 + chunk, nf);
+    if (m0 >= m1) return;
+    const bool walls = a == 2 && !g.zper;
+    const int ncell = a == 1 ? g.ny : g.nz;
+    auto cellc = [&](int m, T c1[NC], T c2[NC]) {
+        m = m < 0 ? m + ncell : (m >= ncell ? m - ncell : m);
+        if (a == 1) C(i, m, o, c1, c2);
+        else C(i, o, m, c1, c2);
+    };
+    T l1[NC], l2[NC], h1[NC], h2[NC];
+    for (int n = 0; n < NC; ++n) l1[n] = l2[n] = h1[n] = h2[n] = T(0);
+    if (!(walls && m0 == 0)) cellc(m0 - 1, l1, l2);
+    for (int m = m0; m < m1; ++m) {
+        const bool wl = walls && m == 0, wh = walls && m == g.nz;
+        if (!wh) cellc(m, h1, h2);
+        const long long f = a == 1 ? fidx(g, 1, i, m, o) : fidx(g, 2, i, o, m);
+        trans_out<T, NC>(g, a, m, f, (T)ua[f], LO, HI, wl, wh, l1, l2, h1, h2, out1, out2);
+        for (int n = 0; n < NC; ++n) {
+            l1[n] = h1[n];
+            l2[n] = h2[n];
+        }
+    }
+}
+
+template <typename T, int NC>
+static void launch_adv_trans(Ctx& c, const Grid& g, int a, const T* vel, double rho, double dt, const T* ua, const T* vb1, const T* vb2,
+                             C3<T> LO, C3<T> HI, C3<T> E1, C3<T> E2, P3<T> O1, P3<T> O2, double bytes) {
+    const int b1 = (a + 1) % 3, b2 = (a + 2) % 3;
+    const TransCell<T, NC> C{g, a, b1, b2, vel, T(rho), T(dt / (3.0 * hd(g, b1))), T(dt / (3.0 * hd(g, b2))), vb1, vb2, E1, E2};
+    if (a == 0) {
+        KS_LAUNCH(c, (k_adv_trans_x<T, NC>), nblocks(g.N, 256), 256, bytes, C, ua, LO, HI, O1, O2);
+    } else {
+        constexpr int chunk = 16;
+        const int nf = a == 1 ? g.ny : nzfaces(g), no = a == 1 ? g.nz : g.ny;
+        const int bx = g.nx >= 128 ? 128 : 32 * ((g.nx + 31) / 32);
+        const dim3 grid((unsigned)((g.nx + bx - 1) / bx), (unsigned)(no * ((nf + chunk - 1) / chunk)));
+        KS_LAUNCH(c, (k_adv_trans_col<T, NC>), grid, bx, bytes, C, ua, LO, HI, O1, O2, chunk);
     }
 }
 
 // ---- post-MAC stage 3: final states and fluxes on d-faces
 // The forces enter scaled by rho for the velocity (forces = (src + divtau) / rho)
 // and as they are for a scalar (NC = 1: forces = src + diff, AdvOp_Godunov.H:114-329).
+// Stage 3 by cells: the part of a face state that depends only on the cell
+// it is traced from,
+//   corr(c) = hdt forces(c) + (q(c) r(c) - c1 x1(c) - c2 x2(c)),
+//   r = rho (c1 (v1+ - v1-) + c2 (v2+ - v2-)),  x_b = T_b(+) v_b+ - T_b(-) v_b-
+// over the b1 / b2 faces of c, so that a face state is its stage-1 state plus
+// corr of its cell.  The low-side state of face c + e_d and the high-side state
+// of face c share it: the kernels below form each cell's corr once (half the
+// FP64 work of forming it per face side).
+template <typename T, int NC>
+struct FluxCell {
+    Grid g;
+    int d, b1, b2;
+    const T *vel, *forces;
+    T rho, hdt, c1, c2;
+    C3<T> U, T1, T2;
+    __device__ inline void operator()(int i, int j, int k, T corr[NC]) const {
+        const long long p1 = fidx(g, b1, i + (b1 == 0), j + (b1 == 1), k + (b1 == 2)), m1 = fidx(g, b1, i, j, k);
+        const long long p2 = fidx(g, b2, i + (b2 == 0), j + (b2 == 1), k + (b2 == 2)), m2 = fidx(g, b2, i, j, k);
+        const T v1p = (T)U.p[b1][p1], v1m = (T)U.p[b1][m1], v2p = (T)U.p[b2][p2], v2m = (T)U.p[b2][m2];
+        const T r = rho * (c1 * (v1p - v1m) + c2 * (v2p - v2m));
+        const VelFPT<T, T> q{vel, g, T(1)};
+        const CellFOT<T, T> Fo{forces, g};
+        for (int n = 0; n < NC; ++n) {
+            const T x1 = T1.p[n][p1] * v1p - T1.p[n][m1] * v1m, x2 = T2.p[n][p2] * v2p - T2.p[n][m2] * v2m;
+            corr[n] = hdt * Fo(n, i, j, k) + ((q(n, i, j, k) * r - c1 * x1) - c2 * x2);
+        }
+    }
+};
+
+// x faces: a thread per face, lanes of a warp along a row of faces; the
+// low-side cell correction of face i is the high-side one of face i - 1, taken
+// from the previous lane (lane 0 and the periodic wrap form their own).
 template <typename T, int NC = 3>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_adv_flux(Grid g, int d, const T* vel, const T* forces, T rho, T dt, T c1, T c2, C3<T> U,
-                                                     C3<T> LO, C3<T> HI, C3<T> T1, C3<T> T2, P3<T> Fl) {
-    int i, j, k;
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_adv_flux_x(FluxCell<T, NC> C, C3<T> LO, C3<T> HI, P3<T> Fl) {
+    const Grid& g = C.g;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (!face_of(g, d, t, i, j, k)) return;
-    VelFPT<T, T> q{vel, g, T(1)};
-    CellFOT<T, T> Fo{forces, g};
-    const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
-    const bool wl = (d == 2 && !g.zper && k == 0), wh = (d == 2 && !g.zper && k == g.nz);
-    const long long f = fidx(g, d, i, j, k);
-    const T um = (T)U.p[d][f];
-    const int li = i - (d == 0), lj = j - (d == 1), lk = k - (d == 2);
-    const long long lp1 = fidx(g, b1, li + (b1 == 0), lj + (b1 == 1), lk + (b1 == 2)), lm1 = fidx(g, b1, li, lj, lk);
-    const long long lp2 = fidx(g, b2, li + (b2 == 0), lj + (b2 == 1), lk + (b2 == 2)), lm2 = fidx(g, b2, li, lj, lk);
-    const long long hp1 = fidx(g, b1, i + (b1 == 0), j + (b1 == 1), k + (b1 == 2)), hm1 = fidx(g, b1, i, j, k);
-    const long long hp2 = fidx(g, b2, i + (b2 == 0), j + (b2 == 1), k + (b2 == 2)), hm2 = fidx(g, b2, i, j, k);
-    T l1p = 0, l1m = 0, l2p = 0, l2m = 0, h1p = 0, h1m = 0, h2p = 0, h2m = 0;
-    if (!wl) { l1p = (T)U.p[b1][lp1]; l1m = (T)U.p[b1][lm1]; l2p = (T)U.p[b2][lp2]; l2m = (T)U.p[b2][lm2]; }
-    if (!wh) { h1p = (T)U.p[b1][hp1]; h1m = (T)U.p[b1][hm1]; h2p = (T)U.p[b2][hp2]; h2m = (T)U.p[b2][hm2]; }
-    // rho (c1 (v1+ - v1-) + c2 (v2+ - v2-)) of each side and dt/2 times the
-    // force scale, shared by the components: the cell values enter unscaled
-    const T rl = rho * (c1 * (l1p - l1m) + c2 * (l2p - l2m)), rh = rho * (c1 * (h1p - h1m) + c2 * (h2p - h2m));
-    const T hdt = T(0.5) * dt * (NC == 3 ? rho : T(1));
+    const bool live = t < g.N;
+    int i = 0, j = 0, k = 0;
+    T ch[NC], cl[NC];
+    for (int n = 0; n < NC; ++n) ch[n] = T(0);
+    if (live) {
+        const unsigned u = (unsigned)t, r = u / (unsigned)g.nx;
+        i = (int)(u - r * (unsigned)g.nx);
+        k = (int)(r / (unsigned)g.ny);
+        j = (int)(r - (unsigned)k * (unsigned)g.ny);
+        C(i, j, k, ch);
+    }
+    for (int n = 0; n < NC; ++n) cl[n] = __shfl_up_sync(0xffffffffu, ch[n], 1);
+    if (!live) return;
+    if ((threadIdx.x & 31) == 0 || i == 0) C(i == 0 ? g.nx - 1 : i - 1, j, k, cl);
+    const T um = (T)C.U.p[0][t];
     const bool usmall = below_small_abs(um), upos = ge0(um);
     for (int n = 0; n < NC; ++n) {
-        T stl = T(0), sth = T(0);
-        if (!wl) {
-            const T x1 = T1.p[n][lp1] * l1p - T1.p[n][lm1] * l1m, x2 = T2.p[n][lp2] * l2p - T2.p[n][lm2] * l2m;
-            stl = hdt * Fo(n, li, lj, lk) + (q(n, li, lj, lk) * rl + ((LO.p[n][f] - c1 * x1) - c2 * x2));
-        }
-        if (!wh) {
-            const T x1 = T1.p[n][hp1] * h1p - T1.p[n][hm1] * h1m, x2 = T2.p[n][hp2] * h2p - T2.p[n][hm2] * h2m;
-            sth = hdt * Fo(n, i, j, k) + (q(n, i, j, k) * rh + ((HI.p[n][f] - c1 * x1) - c2 * x2));
-        }
-        if (d == 2) zbc(g, k, n, stl, sth);
+        const T stl = LO.p[n][t] + cl[n], sth = HI.p[n][t] + ch[n];
         const T st = usmall ? T(0.5) * (stl + sth) : (upos ? stl : sth);
-        Fl.p[n][f] = um * st;
+        Fl.p[n][t] = um * st;
+    }
+}
+
+// y and z faces: a thread per (i, other index) marches a chunk of faces along d
+// and carries the cell correction from one face to the next.
+template <typename T, int NC = 3>
+__global__ void __launch_bounds__(128) k_adv_flux_col(FluxCell<T, NC> C, C3<T> LO, C3<T> HI, P3<T> Fl, int chunk) {
+    const Grid& g = C.g;
+    const int d = C.d;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.nx) return;
+    const int nf = d == 1 ? g.ny : nzfaces(g);
+    const int no = d == 1 ? g.nz : g.ny;
+    const int o = (int)(blockIdx.y % (unsigned)no), chn = (int)(blockIdx.y / (unsigned)no);
+    const int m0 = chn * chunk, m1 = min(m0 + chunk, nf);
+    if (m0 >= m1) return;
+    const bool walls = d == 2 && !g.zper;
+    const int ncell = d == 1 ? g.ny : g.nz;
+    // cell m along d (periodic wrap), as (j, k)
+    auto cellc = [&](int m, T corr[NC]) {
+        m = m < 0 ? m + ncell : (m >= ncell ? m - ncell : m);
+        if (d == 1) C(i, m, o, corr);
+        else C(i, o, m, corr);
+    };
+    T cl[NC], ch[NC];
+    for (int n = 0; n < NC; ++n) cl[n] = ch[n] = T(0);
+    if (!(walls && m0 == 0)) cellc(m0 - 1, cl);
+    for (int m = m0; m < m1; ++m) {
+        const bool wl = walls && m == 0, wh = walls && m == g.nz;
+        if (!wh) cellc(m, ch);
+        const long long f = d == 1 ? fidx(g, 1, i, m, o) : fidx(g, 2, i, o, m);
+        const T um = (T)C.U.p[d][f];
+        const bool usmall = below_small_abs(um), upos = ge0(um);
+        for (int n = 0; n < NC; ++n) {
+            T stl = wl ? T(0) : LO.p[n][f] + cl[n];
+            T sth = wh ? T(0) : HI.p[n][f] + ch[n];
+            if (d == 2) zbc(g, m, n, stl, sth);
+            const T st = usmall ? T(0.5) * (stl + sth) : (upos ? stl : sth);
+            Fl.p[n][f] = um * st;
+            cl[n] = ch[n];
+        }
+    }
+}
+
+template <typename T, int NC>
+static void launch_adv_flux(Ctx& c, const Grid& g, int d, const T* vel, const T* forces, double rho, double dt, C3<T> U, C3<T> LO, C3<T> HI,
+                            C3<T> T1, C3<T> T2, P3<T> F, double bytes) {
+    const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
+    const FluxCell<T, NC> C{g, d, b1, b2, vel, forces, T(rho), T(0.5) * T(dt) * (NC == 3 ? T(rho) : T(1)), T(dt / (2.0 * hd(g, b1))),
+                            T(dt / (2.0 * hd(g, b2))), U, T1, T2};
+    if (d == 0) {
+        KS_LAUNCH(c, (k_adv_flux_x<T, NC>), nblocks(g.N, 256), 256, bytes, C, LO, HI, F);
+    } else {
+        constexpr int chunk = 16;
+        const int nf = d == 1 ? g.ny : nzfaces(g), no = d == 1 ? g.nz : g.ny;
+        const int bx = g.nx >= 128 ? 128 : 32 * ((g.nx + 31) / 32);
+        const dim3 grid((unsigned)((g.nx + bx - 1) / bx), (unsigned)(no * ((nf + chunk - 1) / chunk)));
+        KS_LAUNCH(c, (k_adv_flux_col<T, NC>), grid, bx, bytes, C, LO, HI, F, chunk);
     }
 }
 
@@ -722,8 +857,7 @@ static void advection_t(Ctx& c, const Grid& g, const T* vel, const T* forces, co
         C3<T> E2{{tp<T>(B.tedge[b2][0]), tp<T>(B.tedge[b2][1]), tp<T>(B.tedge[b2][2])}};
         P3<T> O1{{tp<T>(B.tr[a][b1][0]), tp<T>(B.tr[a][b1][1]), tp<T>(B.tr[a][b1][2])}};
         P3<T> O2{{tp<T>(B.tr[a][b2][0]), tp<T>(B.tr[a][b2][1]), tp<T>(B.tr[a][b2][2])}};
-        KS_LAUNCH(c, k_adv_trans2<T>, nblocks(nfaces(g, a), BS), BS, bytes, g, a, vel, T(rho), T(dt / (3.0 * hd(g, b1))),
-                  T(dt / (3.0 * hd(g, b2))), mac[a], mac[b1], mac[b2], LO, HI, E1, E2, O1, O2);
+        launch_adv_trans<T, 3>(c, g, a, vel, rho, dt, mac[a], mac[b1], mac[b2], LO, HI, E1, E2, O1, O2, bytes);
     }
     C3<T> U{{mac[0], mac[1], mac[2]}};
     for (int d = 0; d < 3; ++d) {
@@ -734,8 +868,7 @@ static void advection_t(Ctx& c, const Grid& g, const T* vel, const T* forces, co
         C3<T> T1{{tp<T>(B.tr[b1][b2][0]), tp<T>(B.tr[b1][b2][1]), tp<T>(B.tr[b1][b2][2])}};
         C3<T> T2{{tp<T>(B.tr[b2][b1][0]), tp<T>(B.tr[b2][b1][1]), tp<T>(B.tr[b2][b1][2])}};
         P3<T> F{{tp<T>(B.flux[d][0]), tp<T>(B.flux[d][1]), tp<T>(B.flux[d][2])}};
-        KS_LAUNCH(c, k_adv_flux<T>, nblocks(nfaces(g, d), BS), BS, bytes, g, d, vel, forces, T(rho), T(dt), T(dt / (2.0 * hd(g, b1))),
-                  T(dt / (2.0 * hd(g, b2))), U, LO, HI, T1, T2, F);
+        launch_adv_flux<T, 3>(c, g, d, vel, forces, rho, dt, U, LO, HI, T1, T2, F, bytes);
     }
     FluxPtrs<T> F;
     for (int d = 0; d < 3; ++d)
@@ -764,8 +897,7 @@ void launch_scalar_advection(Ctx& c, const Grid& g, const double* s, const doubl
         C3<T> LO{{tp<T>(B.lo[a][0]), nullptr, nullptr}}, HI{{tp<T>(B.hi[a][0]), nullptr, nullptr}};
         C3<T> E1{{tp<T>(B.tedge[b1][0]), nullptr, nullptr}}, E2{{tp<T>(B.tedge[b2][0]), nullptr, nullptr}};
         P3<T> O1{{tp<T>(B.tr[a][b1][0]), nullptr, nullptr}}, O2{{tp<T>(B.tr[a][b2][0]), nullptr, nullptr}};
-        KS_LAUNCH(c, (k_adv_trans2<T, 1>), nblocks(nfaces(g, a), BS), BS, B8 * (g.N + 5.0 * na + 2.0 * nt), g, a, s, T(rho),
-                  T(dt / (3.0 * hd(g, b1))), T(dt / (3.0 * hd(g, b2))), mac[a], mac[b1], mac[b2], LO, HI, E1, E2, O1, O2);
+        launch_adv_trans<T, 1>(c, g, a, s, rho, dt, mac[a], mac[b1], mac[b2], LO, HI, E1, E2, O1, O2, B8 * (g.N + 5.0 * na + 2.0 * nt));
     }
     C3<double> U{{mac[0], mac[1], mac[2]}};
     for (int d = 0; d < 3; ++d) {
@@ -774,8 +906,7 @@ void launch_scalar_advection(Ctx& c, const Grid& g, const double* s, const doubl
         C3<T> T1{{tp<T>(B.tr[b1][b2][0]), nullptr, nullptr}}, T2{{tp<T>(B.tr[b2][b1][0]), nullptr, nullptr}};
         P3<T> F{{tp<T>(B.flux[d][0]), nullptr, nullptr}};
         const double bytes = B8 * (2.0 * g.N + 4.0 * nfaces(g, d) + 2.0 * (nfaces(g, b1) + nfaces(g, b2)));
-        KS_LAUNCH(c, (k_adv_flux<T, 1>), nblocks(nfaces(g, d), BS), BS, bytes, g, d, s, fs, T(rho), T(dt), T(dt / (2.0 * hd(g, b1))),
-                  T(dt / (2.0 * hd(g, b2))), U, LO, HI, T1, T2, F);
+        launch_adv_flux<T, 1>(c, g, d, s, fs, rho, dt, U, LO, HI, T1, T2, F, bytes);
     }
     FluxPtrs<T> F;
     for (int m = 0; m < 9; ++m) F.p[m] = nullptr;
