@@ -10,6 +10,8 @@
 // (the transpose of trilinear prolongation over 8), trilinear prolongation,
 // single-CTA bottom sweeps.  Wall-bounded z uses mirror images of the
 // node values about the boundary node plane.
+#include <cstdint>
+
 #include "ks_launch.hpp"
 
 namespace ks {
@@ -530,12 +532,137 @@ __global__ void __launch_bounds__(256, 4) k_nd_col2(NDLevelT<float> L, NdCoef<fl
     }
 }
 
+// V consecutive nodes of a row as one vector access (the row offset is a
+// multiple of V, the level's arrays V-element aligned: checked by the launchers)
+template <int V, typename T>
+__device__ inline void ldv(const T* p, T* v) {
+    if constexpr (V == 4 && sizeof(T) == 4) {
+        const float4 x = *reinterpret_cast<const float4*>(p);
+        v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+    } else if constexpr (V == 2 && sizeof(T) == 8) {
+        const double2 x = *reinterpret_cast<const double2*>(p);
+        v[0] = x.x; v[1] = x.y;
+    } else if constexpr (V == 2 && sizeof(T) == 4) {
+        const float2 x = *reinterpret_cast<const float2*>(p);
+        v[0] = x.x; v[1] = x.y;
+    } else {
+        for (int m = 0; m < V; ++m) v[m] = p[m];
+    }
+}
+template <int V, typename T>
+__device__ inline void stv(T* p, const T* v) {
+    if constexpr (V == 4 && sizeof(T) == 4) {
+        *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    } else if constexpr (V == 2 && sizeof(T) == 8) {
+        *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+    } else if constexpr (V == 2 && sizeof(T) == 4) {
+        *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+    } else {
+        for (int m = 0; m < V; ++m) p[m] = v[m];
+    }
+}
+
+// FP32 column kernel over V = 4 nodes of a row per thread, for the sweeps
+// (MODE 0) and residuals (MODE 2) of the mixed-precision cycles, which wait on
+// load latency rather than on arithmetic.  A node plane's row j and its
+// neighbour rows j -+ 1 are read as one vector each plus the two x-edge
+// values (3 vector + 6 scalar loads per 4 nodes, where k_nd_col2 issues 9
+// scalar loads per node), and adjacent nodes share their x sums:
+//   Ey_m = a_m + c_m (rows j - 1, j + 1),  P_m = Ey_{m-1} + Ey_{m+1},
+//   Ex_m = b_{m-1} + b_{m+1} (row j),      C_m = b_m.
+// Each plane is reduced once to the terms a node takes from it as a z
+// neighbour, Q = c3 Ex + c1 Ey + c0 P [+ c4 C], and as the centre plane,
+// R = c13 C + c9 P [+ c12 Ex + c10 Ey], so that node k's residual is
+//   rhs + R_k + (Q_{k-1} + Q_{k+1})
+// (the sigma-scaled weights negated; the brackets when the face weights are
+// non-zero).  FP64 keeps k_nd_col: it is bound by the FP64 pipe, and with
+// equal spacings (face weights zero) the plane terms save no FP64 operation
+// over its per-node chain once the planes above and below a column chunk
+// are counted.  The template stays general in T and V (ldv / stv).
+template <typename T, int V, int MODE>
+__global__ void __launch_bounds__(256) k_nd_xv(NDLevelT<T> L, NdCoef<T> w, const T* in, T* out, int kc, double* parts) {
+    const int nq = L.nx / V, sz = L.nx * L.ny;
+    const int nch = (L.nz + kc - 1) / kc;
+    const unsigned M = (unsigned)(nq * L.ny * nch);
+    MaxAbs<T> mx;
+    struct Pl {
+        T Q[V], R[V], C[V];
+    };
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < M; t += gridDim.x * blockDim.x) {
+        int q, j, ch;
+        split3(t, (unsigned)nq, (unsigned)L.ny, q, j, ch);
+        const int i0 = V * q;
+        const int im = i0 == 0 ? L.nx - 1 : i0 - 1, ip = i0 + V == L.nx ? 0 : i0 + V;
+        const int cm = (j == 0 ? L.ny - 1 : j - 1) * L.nx, c0 = j * L.nx;
+        const int cp = (j + 1 == L.ny ? 0 : j + 1) * L.nx;
+        auto plane = [&](int k, Pl& o) {
+            if (L.zper) k = k < 0 ? k + L.nz : (k >= L.nz ? k - L.nz : k);
+            else k = k < 0 ? -k : (k >= L.nz ? 2 * (L.nz - 1) - k : k);
+            const T* p = in + k * sz;
+            T a[V + 2], b[V + 2], c[V + 2];
+            ldv<V>(p + cm + i0, a + 1);
+            ldv<V>(p + c0 + i0, b + 1);
+            ldv<V>(p + cp + i0, c + 1);
+            a[0] = p[cm + im]; a[V + 1] = p[cm + ip];
+            b[0] = p[c0 + im]; b[V + 1] = p[c0 + ip];
+            c[0] = p[cp + im]; c[V + 1] = p[cp + ip];
+            T ey[V + 2];
+            for (int m = 0; m < V + 2; ++m) ey[m] = a[m] + c[m];
+            for (int m = 0; m < V; ++m) {
+                const T P = ey[m] + ey[m + 2], Ex = b[m] + b[m + 2], Ey = ey[m + 1], C = b[m + 1];
+                T Qv = w.c0 * P;
+                Qv = w.c1 * Ey + Qv;
+                Qv = w.c3 * Ex + Qv;
+                T Rv = w.c13 * C;
+                Rv = w.c9 * P + Rv;
+                if (!L.faces_zero) {
+                    Qv = w.c4 * C + Qv;
+                    Rv = w.c12 * Ex + Rv;
+                    Rv = w.c10 * Ey + Rv;
+                }
+                o.Q[m] = Qv;
+                o.R[m] = Rv;
+                o.C[m] = C;
+            }
+        };
+        const int k0 = ch * kc, k1 = min(k0 + kc, L.nz);
+        Pl pm, p0, pp;
+        plane(k0 - 1, pm);
+        plane(k0, p0);
+        for (int k = k0; k < k1; ++k) {
+            plane(k + 1, pp);
+            const int idx = k * sz + c0 + i0;
+            T r[V];
+            ldv<V>(L.rhs + idx, r);
+            for (int m = 0; m < V; ++m) {
+                const T res = (r[m] + p0.R[m]) + (pm.Q[m] + pp.Q[m]);
+                if (MODE >= 1) mx.add(res);
+                r[m] = MODE == 2 ? res : w.oinv * res + p0.C[m];
+            }
+            stv<V>((MODE == 2 ? L.res : out) + idx, r);
+            pm = p0;
+            p0 = pp;
+        }
+    }
+    if (MODE >= 1) {
+        const double m = bred<1>(mx.get());
+        if (threadIdx.x == 0 && parts) parts[blockIdx.x] = m;
+    }
+}
+
 // planes per thread: long columns on the large levels, short ones on the
 // coarse levels so that they still fill the GPU
 template <typename T>
 inline int nd_chunk(const NDLevelT<T>& L) {
     const long long work = (long long)L.nx * L.ny * L.nz / 300000;
     return (int)(work < 2 ? 2 : (work > 16 ? 16 : work));
+}
+// whether a launch uses k_nd_xv<float, 4>: levels of more than 2^18 nodes
+// (on smaller ones a quarter of the threads leaves the GPU short of warps),
+// the row length a multiple of 4 and every array it touches 16-byte aligned
+inline bool nd_vec_ok(const NDLevelT<float>& L, const void* a, const void* b) {
+    auto al = [](const void* p) { return ((uintptr_t)p & 15) == 0; };
+    return (long long)L.nx * L.ny * L.nz > (1LL << 18) && L.nx % 4 == 0 && al(L.rhs) && al(a) && al(b);
 }
 template <typename T>
 inline long long nd_cols(const NDLevelT<T>& L, int kc) {
@@ -721,22 +848,35 @@ void launch_cc_bottom(Ctx& c, const CCLevelT<T>& L, double beta, int sweeps) {
 template <typename T>
 void launch_nd_jacobi(Ctx& c, const NDLevelT<T>& L, double sigma, double omega, const T* in, T* out) {
     const int kc = nd_chunk(L);
-    if constexpr (sizeof(T) == 4)
-        KS_LAUNCH(c, k_nd_col2<0>, nblocks(nd_cols(L, kc), BS), BS, sizeof(T) * 3.0 * nnd(L), L, nd_coef(L, sigma, omega), in, out, kc,
-                  nullptr);
-    else
-        KS_LAUNCH(c, (k_nd_col<T, 0>), nblocks(nd_cols(L, kc), BS), BS, sizeof(T) * 3.0 * nnd(L), L, nd_coef(L, sigma, omega), in, out, kc,
-                  nullptr);
+    const double bytes = sizeof(T) * 3.0 * nnd(L);
+    if constexpr (sizeof(T) == 4) {
+        if (nd_vec_ok(L, in, out))
+            KS_LAUNCH(c, (k_nd_xv<float, 4, 0>), nblocks(nd_cols(L, kc) / 4, BS), BS, bytes, L, nd_coef(L, sigma, omega), in, out, kc,
+                      nullptr);
+        else
+            KS_LAUNCH(c, k_nd_col2<0>, nblocks(nd_cols(L, kc), BS), BS, bytes, L, nd_coef(L, sigma, omega), in, out, kc, nullptr);
+    } else {
+        KS_LAUNCH(c, (k_nd_col<T, 0>), nblocks(nd_cols(L, kc), BS), BS, bytes, L, nd_coef(L, sigma, omega), in, out, kc, nullptr);
+    }
 }
 template <typename T>
 void launch_nd_resid(Ctx& c, const NDLevelT<T>& L, double sigma, double* parts, int* np) {
     const int kc = nd_chunk(L);
+    const double bytes = sizeof(T) * 3.0 * nnd(L);
+    if constexpr (sizeof(T) == 4) {
+        if (nd_vec_ok(L, L.phi, L.res)) {
+            const int n = parts_for(nd_cols(L, kc) / 4);
+            if (np) *np = n;
+            KS_LAUNCH(c, (k_nd_xv<float, 4, 2>), n, BS, bytes, L, nd_coef(L, sigma, 0.0), (const float*)L.phi, (float*)nullptr, kc, parts);
+            return;
+        }
+    }
     const int n = parts_for(nd_cols(L, kc));
     if (np) *np = n;
     if constexpr (sizeof(T) == 4)
-        KS_LAUNCH(c, k_nd_col2<2>, n, BS, sizeof(T) * 3.0 * nnd(L), L, nd_coef(L, sigma, 0.0), (const T*)L.phi, (T*)nullptr, kc, parts);
+        KS_LAUNCH(c, k_nd_col2<2>, n, BS, bytes, L, nd_coef(L, sigma, 0.0), (const T*)L.phi, (T*)nullptr, kc, parts);
     else
-        KS_LAUNCH(c, (k_nd_col<T, 2>), n, BS, sizeof(T) * 3.0 * nnd(L), L, nd_coef(L, sigma, 0.0), (const T*)L.phi, (T*)nullptr, kc, parts);
+        KS_LAUNCH(c, (k_nd_col<T, 2>), n, BS, bytes, L, nd_coef(L, sigma, 0.0), (const T*)L.phi, (T*)nullptr, kc, parts);
 }
 template <typename T>
 void launch_nd_restrict(Ctx& c, const NDLevelT<T>& F, const NDLevelT<T>& C) {
