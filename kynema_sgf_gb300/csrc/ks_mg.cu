@@ -650,6 +650,138 @@ __global__ void __launch_bounds__(256) k_nd_xv(NDLevelT<T> L, NdCoef<T> w, const
     }
 }
 
+// FP32 forms of k_cc_gsrb and k_cc_resid over 4 cells of a row per thread
+// (the mixed-precision cycles on the large levels).  A layer's row j and its
+// neighbour rows j -+ 1 and the right-hand side are read as one vector each,
+// and the row j vectors of layers k -+ 1 are the ones the column step before
+// and after reads as its centre, so that a layer costs 4 vector loads and one
+// or two edge values where the scalar kernels issue 7 loads per cell.  Every
+// cell is evaluated with the scalar kernels' expression (bitwise the same
+// result).  In the half-sweep the thread updates the 2 cells of the colour,
+// at offsets o and o + 2 (o = (j + k + colour) & 1); the values it keeps from
+// one layer to the next are read only where they are of the other colour,
+// which the half-sweep does not write.
+__device__ inline float sel2(const float v[4], int o, int m) { return o ? v[m + 1] : v[m]; }
+
+__global__ void __launch_bounds__(128) k_cc_gsrb4(CCLevelT<float> L, CCCoef<float> w, int color, int kc) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (L.nx >> 2)) return;
+    const int j = blockIdx.y;
+    const int k0 = blockIdx.z * kc, k1 = min(k0 + kc, L.nz);
+    const int sy = L.nx, sz = L.nx * L.ny, i0 = 4 * q;
+    const int dyp = (j + 1 == L.ny ? -j : 1) * sy, dym = (j == 0 ? L.ny - 1 : -1) * sy;
+    const int el = i0 == 0 ? L.nx - 1 : -1, er = i0 + 4 == L.nx ? -i0 : 4;  // edge cells, from the quad's first
+    float* p = L.phi;
+    auto row = [&](int k, float v[4]) {
+        if (L.zper) k = k < 0 ? k + L.nz : (k >= L.nz ? k - L.nz : k);
+        if (k < 0 || k >= L.nz) {
+            v[0] = v[1] = v[2] = v[3] = 0.0f;
+            return;
+        }
+        ldv<4>(p + k * sz + j * sy + i0, v);
+    };
+    struct Ld {
+        float ym[4], yp[4], r[4], up[4], e;
+    };
+    auto fetch = [&](int k, Ld& u) {
+        const int b = k * sz + j * sy + i0;
+        ldv<4>(p + b + dym, u.ym);
+        ldv<4>(p + b + dyp, u.yp);
+        ldv<4>(L.rhs + b, u.r);
+        row(k + 1, u.up);
+        u.e = p[b + (((j + k + color) & 1) ? er : el)];
+    };
+    float dn[4], cur[4];
+    row(k0 - 1, dn);
+    row(k0, cur);
+    Ld a, nx;
+    fetch(k0, a);
+    for (int k = k0; k < k1; ++k) {
+        if (k + 1 < k1) fetch(k + 1, nx);
+        const int o = (j + k + color) & 1;
+        float gx = w.gx0, gy = w.gy0, gz = w.gz0, iv = w.iv0;
+        if (!L.zper && (k == 0 || k + 1 == L.nz)) {
+            const bool one = L.nz == 1;
+            gx = one ? w.gx2 : w.gx1;
+            gy = one ? w.gy2 : w.gy1;
+            gz = one ? w.gz2 : w.gz1;
+            iv = one ? w.iv2 : w.iv1;
+        }
+        // x neighbours of the cells at o and o + 2: (edge, 1), (1, 3) or (0, 2), (2, edge)
+        const float sx0 = o ? cur[0] + cur[2] : cur[1] + a.e, sx1 = o ? a.e + cur[2] : cur[3] + cur[1];
+        const float sy0 = sel2(a.yp, o, 0) + sel2(a.ym, o, 0), sy1 = sel2(a.yp, o, 2) + sel2(a.ym, o, 2);
+        const float sz0 = sel2(dn, o, 0) + sel2(a.up, o, 0), sz1 = sel2(dn, o, 2) + sel2(a.up, o, 2);
+        const int b = k * sz + j * sy + i0 + o;
+        p[b] = iv * sel2(a.r, o, 0) + (gx * sx0 + gy * sy0 + gz * sz0);
+        p[b + 2] = iv * sel2(a.r, o, 2) + (gx * sx1 + gy * sy1 + gz * sz1);
+        for (int m = 0; m < 4; ++m) {
+            dn[m] = cur[m];
+            cur[m] = a.up[m];
+        }
+        a = nx;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_cc_resid4(CCLevelT<float> L, CCCoef<float> w, int kc, double* parts) {
+    const int nq = L.nx >> 2, sy = L.nx, sz = L.nx * L.ny;
+    const int nch = (L.nz + kc - 1) / kc;
+    const unsigned M = (unsigned)(nq * L.ny * nch);
+    MaxAbs<float> mx;
+    const float* p = L.phi;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < M; t += gridDim.x * blockDim.x) {
+        int q, j, ch;
+        split3(t, (unsigned)nq, (unsigned)L.ny, q, j, ch);
+        const int i0 = 4 * q;
+        const int dyp = (j + 1 == L.ny ? -j : 1) * sy, dym = (j == 0 ? L.ny - 1 : -1) * sy;
+        const int el = i0 == 0 ? L.nx - 1 : -1, er = i0 + 4 == L.nx ? -i0 : 4;
+        const int k0 = ch * kc, k1 = min(k0 + kc, L.nz);
+        auto row = [&](int k, float v[4]) {
+            if (L.zper) k = k < 0 ? k + L.nz : (k >= L.nz ? k - L.nz : k);
+            if (k < 0 || k >= L.nz) {
+                v[0] = v[1] = v[2] = v[3] = 0.0f;
+                return;
+            }
+            ldv<4>(p + k * sz + j * sy + i0, v);
+        };
+        float dn[4], cur[4];
+        row(k0 - 1, dn);
+        row(k0, cur);
+        for (int k = k0; k < k1; ++k) {
+            const int b = k * sz + j * sy + i0;
+            float ym[4], yp[4], r[4], up[4];
+            ldv<4>(p + b + dym, ym);
+            ldv<4>(p + b + dyp, yp);
+            ldv<4>(L.rhs + b, r);
+            row(k + 1, up);
+            float x[6];  // row j with its two edge cells
+            x[0] = p[b + el];
+            x[5] = p[b + er];
+            for (int m = 0; m < 4; ++m) x[m + 1] = cur[m];
+            float gx = w.gx0, gy = w.gy0, gz = w.gz0, dg = w.dg0;
+            if (!L.zper && (k == 0 || k + 1 == L.nz)) {
+                const bool one = L.nz == 1;
+                gx = one ? w.gx2 : w.gx1;
+                gy = one ? w.gy2 : w.gy1;
+                gz = one ? w.gz2 : w.gz1;
+                dg = one ? w.dg2 : w.dg1;
+            }
+            float v[4];
+            for (int m = 0; m < 4; ++m) {
+                const float S = gx * (x[m + 2] + x[m]) + gy * (yp[m] + ym[m]) + gz * (up[m] + dn[m]);
+                v[m] = r[m] - dg * (cur[m] - S);
+                mx.add(v[m]);
+            }
+            stv<4>(L.res + b, v);
+            for (int m = 0; m < 4; ++m) {
+                dn[m] = cur[m];
+                cur[m] = up[m];
+            }
+        }
+    }
+    const double m = bred<1>(mx.get());
+    if (threadIdx.x == 0 && parts) parts[blockIdx.x] = m;
+}
+
 // planes per thread: long columns on the large levels, short ones on the
 // coarse levels so that they still fill the GPU
 template <typename T>
@@ -794,9 +926,26 @@ inline double nnd(const NDLevelT<T>& L) {
     return (double)L.nx * L.ny * L.nz;
 }
 
+// whether a launch uses the 4-cell FP32 kernels: as nd_vec_ok
+inline bool cc_vec_ok(const CCLevelT<float>& L) {
+    auto al = [](const void* p) { return ((uintptr_t)p & 15) == 0; };
+    return (long long)L.nx * L.ny * L.nz > (1LL << 18) && L.nx % 4 == 0 && al(L.phi) && al(L.rhs) && al(L.res);
+}
+
 template <typename T>
 void launch_cc_gsrb(Ctx& c, const CCLevelT<T>& L, double beta, int color) {
     (void)beta;
+    if constexpr (sizeof(T) == 4) {
+        if (cc_vec_ok(L)) {
+            const int nq = L.nx / 4;
+            const long long work = (long long)nq * L.ny * L.nz / 150000;
+            const int kc = (int)(work < 1 ? 1 : (work > 8 ? 8 : work));
+            const int bx = nq >= 128 ? 128 : 32 * ((nq + 31) / 32);
+            const dim3 grid((unsigned)((nq + bx - 1) / bx), (unsigned)L.ny, (unsigned)((L.nz + kc - 1) / kc));
+            KS_LAUNCH(c, k_cc_gsrb4, grid, bx, 4.0 * 2.0 * ncc(L), L, cc_coef(L), color, kc);
+            return;
+        }
+    }
     // z chunk: long columns on the large levels, one layer on the small ones
     const long long work = (long long)(L.nx / 2) * L.ny * L.nz / 150000;
     const int kc = (int)(work < 1 ? 1 : (work > 16 ? 16 : work));
@@ -808,6 +957,14 @@ template <typename T>
 void launch_cc_resid(Ctx& c, const CCLevelT<T>& L, double beta, double* parts, int* np) {
     (void)beta;
     const int kc = cc_chunk(L);
+    if constexpr (sizeof(T) == 4) {
+        if (cc_vec_ok(L)) {
+            const int n = parts_for((long long)(L.nx / 4) * L.ny * ((L.nz + kc - 1) / kc));
+            if (np) *np = n;
+            KS_LAUNCH(c, k_cc_resid4, n, BS, 4.0 * 3.0 * ncc(L), L, cc_coef(L), kc, parts);
+            return;
+        }
+    }
     const int n = parts_for((long long)L.nx * L.ny * ((L.nz + kc - 1) / kc));
     if (np) *np = n;
     KS_LAUNCH(c, k_cc_resid<T>, n, BS, sizeof(T) * 3.0 * ncc(L), L, cc_coef(L), kc, parts, (float*)nullptr, (float*)nullptr);

@@ -58,6 +58,29 @@ def test_mixed_matches_fp64(cuda_dev):
     assert eg < 5e-3, eg
 
 
+def test_mixed_large_levels(cuda_dev):
+    """128 x 128 x 32 cells: the levels above 2^18 points run the FP32
+    vector-load sweeps (k_nd_xv, k_cc_gsrb4, k_cc_resid4); both solves reach
+    the FP64 tolerance within the FP64 form's V-cycle counts + 2 and the
+    velocity stays within the stated error after 6 steps."""
+    deck = decks.abl(128, 128, 32, steps=6)
+    ref = cuda_dev.Incflo(deck)
+    mix = cuda_dev.Incflo(deck + "\nks.precision = mixed\n")
+    ref.InitData()
+    mix.InitData()
+    for _ in range(6):
+        ref.step()
+        mix.step()
+        assert mix.scalar("mac_res") <= max(1e2 * EPS, 1e5 * EPS * mix.scalar("mac_res0"))
+        assert mix.scalar("nodal_res") <= max(1e2 * EPS, 1e5 * EPS * mix.scalar("nodal_res0"))
+        assert mix.scalar("mac_iters") <= ref.scalar("mac_iters") + 2
+        assert mix.scalar("nodal_iters") <= ref.scalar("nodal_iters") + 2
+        assert mix.scalar("mac_divu_rel") <= 1e-10
+    v, r = mix.get_field("velocity"), ref.get_field("velocity")
+    e2 = np.sqrt(((v - r) ** 2).sum() / (r ** 2).sum())
+    assert e2 <= 1e-6, e2
+
+
 def test_precision_switch_through_abi(cuda_dev):
     sim = cuda_dev.Incflo(decks.tgv(16, steps=2))
     sim.set_precision(1)
