@@ -1082,8 +1082,10 @@ void Sim::nd_rhs(const double* cell_field, bool from_pressure) {
     if (from_pressure) {  // the pressure is the unknown of a non-incremental projection
         nod_bnorm_ = reduce(np, 1, 1, nullptr);
         ck(cudaMemcpyAsync(L.phi, p_.p, sizeof(double) * M, cudaMemcpyDeviceToDevice, ctx_.stream), "D2D");
+        nod_zero_ = false;
     } else {
         launch_fill(ctx_, L.phi, 0.0, M);
+        nod_zero_ = true;
     }
 }
 
@@ -1097,8 +1099,13 @@ void Sim::nd_solve(double sigma) {
     for (size_t l = 0; l < nd32_.size(); ++l) nd32_[l].inv_diag = (float)nd_[l].inv_diag;
     int it = 0;
     double rn = 0.0, target = 0.0;
+    // a solve from zero (set up by nd_rhs) takes its first residual from the
+    // right-hand side without a stencil pass
+    const bool zero = nod_zero_;
+    nod_zero_ = false;
     if (mixed_) {  // each FP64 residual is the next FP32 cycle's right-hand side
-        launch_nd_resid32(ctx_, L, sigma, nd32_[0].rhs, nd32_[0].phi, parts_.p, &np);
+        if (zero) launch_nd_zero_start(ctx_, L, sigma, nod_.omega, nullptr, nd32_[0].rhs, nd32_[0].phi, parts_.p, &np);
+        else launch_nd_resid32(ctx_, L, sigma, nd32_[0].rhs, nd32_[0].phi, parts_.p, &np);
         const double r0 = reduce(np, 1, 1, nullptr);
         nod_r0_ = r0;
         target = std::max(nod_.atol, nod_.rtol * std::max(nod_bnorm_, r0));
@@ -1121,7 +1128,8 @@ void Sim::nd_solve(double sigma) {
         // of the current iterate; its max-norm is the convergence test.  When
         // the test passes, that sweep's output is discarded.
         while (true) {
-            if (nod_.nu1 > 0) launch_nd_jacobi_norm(ctx_, L, sigma, nod_.omega, L.phi, L.tmp, parts_.p, &np);
+            if (it == 0 && zero) launch_nd_zero_start(ctx_, L, sigma, nod_.omega, nod_.nu1 > 0 ? L.tmp : nullptr, nullptr, nullptr, parts_.p, &np);
+            else if (nod_.nu1 > 0) launch_nd_jacobi_norm(ctx_, L, sigma, nod_.omega, L.phi, L.tmp, parts_.p, &np);
             else launch_nd_resid(ctx_, L, sigma, parts_.p, &np);
             rn = reduce(np, 1, 1, nullptr);
             if (!std::isfinite(rn)) throw KsError(KS_ERR_NONFINITE, "nodal projection diverged");

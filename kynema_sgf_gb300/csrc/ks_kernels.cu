@@ -608,18 +608,61 @@ __device__ inline double nodal_div_at(const Grid& g, const double* vel, unsigned
 }
 
 // Nodal divergence into the right-hand side, with weighted partial sums
-// (boundary nodes carry half weight) for the solvability shift.
-__global__ void k_nodal_rhs(Grid g, const double* vel, double* rhs, double* parts, int np, double qx, double qy, double qz) {
+// (boundary nodes carry half weight) for the solvability shift.  A thread
+// walks a chunk of the node column (i, j); the four cells around the column
+// in cell layer c (mirrored at walls as in nodal_div_at) give
+//   X(c) = (u(i,j) - u(i-1,j)) + (u(i,j-1) - u(i-1,j-1)),
+//   Y(c) = (v(i,j) - v(i,j-1)) + (v(i-1,j) - v(i-1,j-1))
+// and their four w values, and node k combines layers k and k - 1 in
+// nodal_div_at's order (the same result): each cell layer is loaded and
+// differenced once for the two nodes it borders, 20 FP64 operations per node
+// where nodal_div_at spends 28.
+__global__ void k_nodal_rhs(Grid g, const double* vel, double* rhs, double* parts, int np, double qx, double qy, double qz, int kc) {
     const int nzn = g.zper ? g.nz : g.nz + 1;
-    const unsigned M = (unsigned)(g.nx * g.ny * nzn);
+    const int nch = (nzn + kc - 1) / kc;
+    const unsigned M = (unsigned)(g.nx * g.ny * nch);
+    const long long N = g.N;
     double ws = 0, wt = 0;
+    struct Lay {
+        double X, Y, w[4];
+    };
     for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < M; t += gridDim.x * blockDim.x) {
-        int k;
-        const double dv = nodal_div_at(g, vel, t, k, qx, qy, qz);
-        rhs[t] = dv;
-        const double wgt = (!g.zper && (k == 0 || k == nzn - 1)) ? 0.5 : 1.0;
-        ws += wgt * dv;
-        wt += wgt;
+        const unsigned r = t / (unsigned)g.nx;
+        const int i = (int)(t - r * (unsigned)g.nx);
+        const int ch = (int)(r / (unsigned)g.ny);
+        const int j = (int)(r - (unsigned)ch * (unsigned)g.ny);
+        const int im = i == 0 ? g.nx - 1 : i - 1, jm = j == 0 ? g.ny - 1 : j - 1;
+        auto layer = [&](int q, Lay& L) {
+            bool flip = false;
+            if (g.zper) q = q < 0 ? q + g.nz : (q >= g.nz ? q - g.nz : q);
+            else if (q < 0) { q = -1 - q; flip = true; }
+            else if (q >= g.nz) { q = 2 * g.nz - 1 - q; flip = true; }
+            const long long r0 = (long long)q * g.ny;
+            const long long o[4] = {(r0 + j) * g.nx + i, (r0 + j) * g.nx + im, (r0 + jm) * g.nx + i, (r0 + jm) * g.nx + im};
+            double u[4], v[4];
+            for (int m = 0; m < 4; ++m) {
+                u[m] = vel[o[m]];
+                v[m] = vel[N + o[m]];
+                const double z = vel[2 * N + o[m]];
+                L.w[m] = flip ? bitsd(dbits(z) ^ ~kMag) : z;
+            }
+            L.X = (u[0] - u[1]) + (u[2] - u[3]);
+            L.Y = (v[0] - v[2]) + (v[1] - v[3]);
+        };
+        const int k0 = ch * kc, k1 = min(k0 + kc, nzn);
+        Lay lo, hi;  // cell layers k - 1 and k
+        layer(k0 - 1, lo);
+        for (int k = k0; k < k1; ++k) {
+            layer(k, hi);
+            const double dx = hi.X + lo.X, dy = hi.Y + lo.Y;
+            const double dz = ((hi.w[0] - lo.w[0]) + (hi.w[1] - lo.w[1])) + ((hi.w[2] - lo.w[2]) + (hi.w[3] - lo.w[3]));
+            const double dv = qx * dx + (qy * dy + qz * dz);
+            rhs[((long long)k * g.ny + j) * g.nx + i] = dv;
+            const double wgt = (!g.zper && (k == 0 || k == nzn - 1)) ? 0.5 : 1.0;
+            ws += wgt * dv;
+            wt += wgt;
+            lo = hi;
+        }
     }
     ws = block_reduce<0>(ws);
     wt = block_reduce<0>(wt);
@@ -957,9 +1000,12 @@ void launch_proj_pre(Ctx& c, const Grid& g, double* vel, const double* vo, const
     KS_LAUNCH(c, k_proj_pre, nblocks(3 * g.N, BS), BS, B8 * 3 * (2 + add_gp + sub_old) * g.N, 3 * g.N, vel, vo, gp, scaling / rho, add_gp, sub_old);
 }
 void launch_nodal_rhs(Ctx& c, const Grid& g, const double* vel, double* rhs, double* parts, int* np) {
-    const long long M = (long long)g.nx * g.ny * (g.zper ? g.nz : g.nz + 1);
-    *np = parts_for(M);
-    KS_LAUNCH(c, k_nodal_rhs, *np, BS, B8 * (3 * g.N + M), g, vel, rhs, parts, *np, 0.25 * g.idx, 0.25 * g.idy, 0.25 * g.idz);
+    const int nzn = g.zper ? g.nz : g.nz + 1;
+    const long long M = (long long)g.nx * g.ny * nzn;
+    const long long work = M / 300000;  // node layers per thread: long columns on large grids
+    const int kc = (int)(work < 2 ? 2 : (work > 16 ? 16 : work));
+    *np = parts_for((long long)g.nx * g.ny * ((nzn + kc - 1) / kc));
+    KS_LAUNCH(c, k_nodal_rhs, *np, BS, B8 * (3 * g.N + M), g, vel, rhs, parts, *np, 0.25 * g.idx, 0.25 * g.idy, 0.25 * g.idz, kc);
 }
 void launch_nodal_divmax(Ctx& c, const Grid& g, const double* vel, double* parts, int* np) {
     const long long M = (long long)g.nx * g.ny * (g.zper ? g.nz : g.nz + 1);

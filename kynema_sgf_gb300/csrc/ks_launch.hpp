@@ -357,6 +357,10 @@ void launch_cc_resid(Ctx& c, const CCLevelT<T>& L, double beta, double* partials
 // right-hand side r32 with its solution z32 zeroed (L.res untouched)
 void launch_cc_resid32(Ctx& c, const CCLevelT<double>& L, double beta, float* r32, float* z32, double* partials, int* nparts);
 void launch_nd_resid32(Ctx& c, const NDLevelT<double>& L, double sigma, float* r32, float* z32, double* partials, int* nparts);
+// first residual of a nodal solve from phi = 0 (the right-hand side): with out, also the
+// first Jacobi sweep of the zero iterate; with r32 / z32, the FP32 cycle's right-hand side
+void launch_nd_zero_start(Ctx& c, const NDLevelT<double>& L, double sigma, double omega, double* out, float* r32, float* z32,
+                          double* partials, int* nparts);
 template <typename T>
 void launch_cc_restrict(Ctx& c, const CCLevelT<T>& F, const CCLevelT<T>& C);
 template <typename T>

@@ -908,6 +908,27 @@ __global__ void k_nd_bottom(NDLevelT<T> L, T sigma, T omega, int sweeps) {
 }
 
 // defect correction: phi64 += phi32
+// First residual of a solve that starts from phi = 0: it is the right-hand
+// side itself (rhs - A 0 = rhs exactly), so no stencil is evaluated.  With out
+// (FP64 cycles) it also writes the first Jacobi sweep, omega rhs / diag (the
+// sweep of the zero iterate: the value k_nd_col<double, 1> writes); with r32 /
+// z32 (mixed precision) the FP32 cycle's right-hand side and zero start.
+// Block maxima of |rhs| as the residual kernels return them.
+__global__ void k_nd_zero_start(const double* rhs, long long n, double oinv, double* out, float* r32, float* z32, double* parts) {
+    MaxAbs<double> mx;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const double r = rhs[t];
+        mx.add(r);
+        if (out) out[t] = oinv * r;
+        if (r32) {
+            r32[t] = (float)r;
+            z32[t] = 0.0f;
+        }
+    }
+    const double m = bred<1>(mx.get());
+    if (threadIdx.x == 0) parts[blockIdx.x] = m;
+}
+
 __global__ void k_add_f32(double* phi, const float* e, long long n) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= n) return;
@@ -1060,6 +1081,13 @@ void launch_nd_jacobi_norm(Ctx& c, const NDLevelT<double>& L, double sigma, doub
     const int n = parts_for(nd_cols(L, kc));
     *np = n;
     KS_LAUNCH(c, (k_nd_col<double, 1>), n, BS, 8.0 * 3.0 * nnd(L), L, nd_coef(L, sigma, omega), in, out, kc, parts);
+}
+void launch_nd_zero_start(Ctx& c, const NDLevelT<double>& L, double sigma, double omega, double* out, float* r32, float* z32, double* parts,
+                          int* np) {
+    const long long n = (long long)L.nx * L.ny * L.nz;
+    *np = parts_for(n);
+    KS_LAUNCH(c, k_nd_zero_start, *np, BS, 8.0 * n * (1 + (out ? 1 : 0)) + 8.0 * n * (r32 ? 1 : 0), L.rhs, n,
+              (double)nd_coef(L, sigma, omega).oinv, out, r32, z32, parts);
 }
 void launch_add_f32(Ctx& c, double* phi, const float* e, long long n) {
     KS_LAUNCH(c, k_add_f32, nblocks(n, BS), BS, 20.0 * n, phi, e, n);

@@ -306,6 +306,7 @@ class Sim {
     size_t glev_ = 0;          // first graphed level (0: none)
     int mg_graphs_ = 1;        // ks.mg_graphs
     int mg_inner_ = 2;         // ks.mixed_inner_cycles
+    bool nod_zero_ = false;    // nd_rhs zero-filled the finest nodal phi for the next solve
     template <typename F>
     void mg_graph_run(MGGraph& G, double key, F&& body);
    public:
