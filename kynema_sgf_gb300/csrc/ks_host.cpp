@@ -230,7 +230,8 @@ void Sim::setup(const Deck& D) {
     mg_graphs_ = D.flag("ks.mg_graphs", 1);  // coarse V-cycle levels as CUDA graphs (not a reference key)
     // mixed precision: FP32 V-cycles per FP64 defect-correction residual (not a reference key)
     mg_inner_ = D.flag("ks.mixed_inner_cycles", 2);
-    if (mg_inner_ < 1) throw KsError(KS_ERR_DECK, "ks.mixed_inner_cycles must be >= 1");
+    mg_inner_nd_ = D.flag("ks.mixed_inner_cycles_nodal", 4);
+    if (mg_inner_ < 1 || mg_inner_nd_ < 1) throw KsError(KS_ERR_DECK, "ks.mixed_inner_cycles(_nodal) must be >= 1");
     restart_file_ = D.str("io.restart_file", "");
     plt_prefix_ = D.str("io.plot_file", "plt");
     chk_prefix_ = D.str("io.check_file", "chk");
@@ -1111,14 +1112,26 @@ void Sim::nd_solve(double sigma) {
         target = std::max(nod_.atol, nod_.rtol * std::max(nod_bnorm_, r0));
         rn = r0;
         while (rn > target && it < nod_.maxiter) {
-            // the correction equation gets up to mg_inner_ FP32 V-cycles (each
-            // continues from the last; FP32 holds the correction to ~1e-7 of
-            // the FP64 residual, far below one cycle's 0.1 contraction)
-            const int inner = std::min(mg_inner_, nod_.maxiter - it);
+            // The correction equation gets as many FP32 V-cycles (each
+            // continuing from the last) as the contraction seen so far says
+            // are still needed, at most mg_inner_nd_: FP32 holds the correction
+            // to ~1e-7 of the FP64 residual, and 4 nodal cycles reduce it by
+            // ~1e-4.  An FP64 residual costs about one FP32 cycle, so checking
+            // only where convergence is expected saves residuals without
+            // adding cycles.  Early cycles contract faster than later ones,
+            // so the prediction gets half a cycle of margin.
+            int inner = mg_inner_nd_;
+            if (nod_rho_ > 0.0 && nod_rho_ < 1.0) {
+                const double need = std::ceil(std::log(target / rn) / std::log(nod_rho_) + 0.5);
+                inner = (int)std::max(1.0, std::min((double)mg_inner_nd_, need));
+            }
+            inner = std::min(inner, nod_.maxiter - it);
             for (int c = 0; c < inner; ++c) nd_vcycle(nd32_, 0, sigma);
             launch_add_f32(ctx_, L.phi, nd32_[0].phi, M);
             launch_nd_resid32(ctx_, L, sigma, nd32_[0].rhs, nd32_[0].phi, parts_.p, &np);
+            const double rprev = rn;
             rn = reduce(np, 1, 1, nullptr);
+            if (rn > 0.0 && rn < rprev) nod_rho_ = std::max(1e-3, std::pow(rn / rprev, 1.0 / inner));
             it += inner;
             if (!std::isfinite(rn)) throw KsError(KS_ERR_NONFINITE, "nodal projection diverged");
             if (rn > 1e20 * r0) throw KsError(KS_ERR_NOT_CONVERGED, "nodal projection diverged (residual above 1e20 times the initial one)");

@@ -305,7 +305,9 @@ class Sim {
     MGGraph gcc_[2], gnd_[2];  // [FP64, FP32] MAC and nodal tails
     size_t glev_ = 0;          // first graphed level (0: none)
     int mg_graphs_ = 1;        // ks.mg_graphs
-    int mg_inner_ = 2;         // ks.mixed_inner_cycles
+    int mg_inner_ = 2;         // ks.mixed_inner_cycles (MAC)
+    int mg_inner_nd_ = 4;      // ks.mixed_inner_cycles_nodal (at most; see nd_solve)
+    double nod_rho_ = 0.0;     // last measured FP32 nodal V-cycle contraction (0: none yet)
     bool nod_zero_ = false;    // nd_rhs zero-filled the finest nodal phi for the next solve
     template <typename F>
     void mg_graph_run(MGGraph& G, double key, F&& body);
