@@ -19,7 +19,6 @@ namespace ks {
 namespace {
 
 constexpr int BS = 256;
-constexpr double kSV = kSmallVel;
 
 __device__ inline void aadd(double* p, double v) {
     if ((dbits(v) & kMag)) atomicAdd(p, v);
@@ -454,68 +453,31 @@ __global__ void k_adj_pm_final(Grid g, int d, double dt, double c1_64, double c2
     }
 }
 
-// ---- reverse of k_adv_trans (a, b): out_n = upwind(u_a; l, h),
-// h = HI + (-cb (vp E(h1) - vm E(h0)) + cb q(c) (vp - vm)), l likewise at c - e_a
-template <typename TI>
-__global__ void k_adj_adv_trans(Grid g, int a, int b, const double* u, double rho64, double cb64, const double* ua, const double* vb, KI<TI> E,
-                                K3 Ob, A3 LOb, A3 HIb, A3 Ebb, double* vbb, double* ub) {
-    using A = TI;
-    int i, j, k;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (!face_at(g, a, t, i, j, k)) return;
-    const bool wl = (a == 2 && !g.zper && k == 0), wh = (a == 2 && !g.zper && k == g.nz);
-    const long long f = t;
-    const A uaf = (A)ua[f], rho = (A)rho64, cb = (A)cb64;
-    const int ci = i - (a == 0), cj = j - (a == 1), ck = k - (a == 2);
-    const long long h0 = fidx(g, b, i, j, k), h1 = fidx(g, b, i + (b == 0), j + (b == 1), k + (b == 2));
-    const long long l0 = fidx(g, b, ci, cj, ck), l1 = fidx(g, b, ci + (b == 0), cj + (b == 1), ck + (b == 2));
-    A vhp = A(0), vhm = A(0), vlp = A(0), vlm = A(0);
-    if (!wh) {
-        vhp = (A)vb[h1];
-        vhm = (A)vb[h0];
-    }
-    if (!wl) {
-        vlp = (A)vb[l1];
-        vlm = (A)vb[l0];
-    }
-    A gvhp = A(0), gvhm = A(0), gvlp = A(0), gvlm = A(0);
-    for (int n = 0; n < 3; ++n) {
-        const double ob64 = Ob.p[n][f];
-        if (!(dbits(ob64) & kMag)) continue;
-        const A ob = (A)ob64;
-        A lb = A(0), hb = A(0);
-        rev_upwind(uaf, ob, lb, hb);
-        if (a == 2) zbc_rev(g, k, n, lb, hb);
-        LOb.p[n][f] += (double)lb;
-        HIb.p[n][f] += (double)hb;
-        if (!wh && nonzero(hb)) {
-            const A qc = rho * Q<A>(g, u, n, i, j, k);
-            aadd(&Ebb.p[n][h1], (double)(-cb * vhp * hb));
-            aadd(&Ebb.p[n][h0], (double)(cb * vhm * hb));
-            gvhp += (-cb * E.p[n][h1] + cb * qc) * hb;
-            gvhm += (cb * E.p[n][h0] - cb * qc) * hb;
-            Qb(g, ub, n, i, j, k, (double)(rho * cb * (vhp - vhm) * hb));
-        }
-        if (!wl && nonzero(lb)) {
-            const A qc = rho * Q<A>(g, u, n, ci, cj, ck);
-            aadd(&Ebb.p[n][l1], (double)(-cb * vlp * lb));
-            aadd(&Ebb.p[n][l0], (double)(cb * vlm * lb));
-            gvlp += (-cb * E.p[n][l1] + cb * qc) * lb;
-            gvlm += (cb * E.p[n][l0] - cb * qc) * lb;
-            Qb(g, ub, n, ci, cj, ck, (double)(rho * cb * (vlp - vlm) * lb));
-        }
-    }
-    aadd(&vbb[h1], (double)gvhp);
-    aadd(&vbb[h0], (double)gvhm);
-    aadd(&vbb[l1], (double)gvlp);
-    aadd(&vbb[l0], (double)gvlm);
-}
+// ---- reverse of the post-MAC stages 2 and 3 (k_adv_trans_x/col,
+// k_adv_flux_x/col) in gather form.  The forward gives every face state its
+// cell's correction, corr(c) = hdt F(c) + q(c) r(c) - c1 x1(c) - c2 x2(c)
+// (stage 3; r = rho (c1 (v1+ - v1-) + c2 (v2+ - v2-)), x_b = T_b(+) v_b+ -
+// T_b(-) v_b- over the b faces of c) or the pair corr_b(c) = q(c) rho cb
+// (v_b+ - v_b-) - cb (v_b+ E_b(+) - v_b- E_b(-)) (stage 2).  The reverse:
+//  - per d-face, the upwind selection's adjoints of the two states (bl, bh)
+//    and of the advective velocity (k_adj_flux_faces, stage 3 only);
+//  - per cell, the adjoint of its correction, cb(c) = bl(face above) +
+//    bh(face below), and what the cell owns: the velocity and forces
+//    adjoints, the state adjoints of its low face (k_adj_*_cells); cb is kept
+//    per cell, in the pass precision;
+//  - per transverse face, the adjoints of T_b / E_b and of the MAC velocity
+//    there, gathered from cb of its two cells (k_adj_*_bfaces).
+// Every adjoint is written by the one thread that owns it: no atomics.  The
+// arithmetic is the pass precision's, and each owned value takes one FP64
+// add: FP64 issues at 1/64 of the FP32 rate, and an FP64 atomic's add runs in
+// L2, so a gather form that summed its terms in FP64 on the SM (as the
+// accumulations of a scatter form would) was slower than the atomics.
 
-// ---- reverse of k_adv_flux (d) with the flux adjoint Fb given
+// stage 3, per d-face: gum = sum_n st_n fb_n (the upwinded state), and the
+// face's LO / HI adjoints
 template <typename TI>
-__global__ void k_adj_adv_flux(Grid g, int d, const double* u, const double* forces, double rho64, double dt64, double c1_64, double c2_64,
-                               K3 Uf, KI<TI> LO, KI<TI> HI, KI<TI> T1, KI<TI> T2, K3 Fb, A3 Ufb, A3 LOb, A3 HIb, A3 T1b, A3 T2b, double* ub,
-                               double* forcesb) {
+__global__ void k_adj_flux_faces(Grid g, int d, const double* u, const double* forces, double rho64, double dt64, double c1_64, double c2_64,
+                                 K3 Uf, KI<TI> LO, KI<TI> HI, KI<TI> T1, KI<TI> T2, K3 Fb, double* Udb, A3 LOb, A3 HIb) {
     using A = TI;
     int i, j, k;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -543,18 +505,18 @@ __global__ void k_adj_adv_flux(Grid g, int d, const double* u, const double* for
         h2p = (A)Uf.p[b2][hp2];
         h2m = (A)Uf.p[b2][hm2];
     }
-    A gum = A(0), gl1p = A(0), gl1m = A(0), gl2p = A(0), gl2m = A(0), gh1p = A(0), gh1m = A(0), gh2p = A(0), gh2m = A(0);
+    A gum = A(0);
     const long long cl = wl ? 0 : cell_fo(g, li, lj, lk);
     const long long ch = wh ? 0 : cell_fo(g, i, j, k);
     for (int n = 0; n < 3; ++n) {
         const double fb64 = Fb.p[n][f];
         if (!(dbits(fb64) & kMag)) continue;
         const A fb = (A)fb64;
-        // the forward's face states in its own precision (decide the upwind branch)
-        A ql = A(0), qh = A(0), stl = A(0), sth = A(0);
+        // the forward's face states in its own precision (the upwind branch is
+        // set by um alone; the states enter gum)
+        A stl = A(0), sth = A(0);
         if (!wl) {
             const A q = rho * (A)u[n * g.N + cl];
-            ql = q;
             A s_ = LO.p[n][f];
             s_ -= c1 * (T1.p[n][lp1] * l1p - T1.p[n][lm1] * l1m);
             s_ -= c2 * (T2.p[n][lp2] * l2p - T2.p[n][lm2] * l2m);
@@ -565,7 +527,6 @@ __global__ void k_adj_adv_flux(Grid g, int d, const double* u, const double* for
         }
         if (!wh) {
             const A q = rho * (A)u[n * g.N + ch];
-            qh = q;
             A s_ = HI.p[n][f];
             s_ -= c1 * (T1.p[n][hp1] * h1p - T1.p[n][hm1] * h1m);
             s_ -= c2 * (T2.p[n][hp2] * h2p - T2.p[n][hm2] * h2m);
@@ -589,42 +550,130 @@ __global__ void k_adj_adv_flux(Grid g, int d, const double* u, const double* for
         }
         gum += st * fb;
         if (d == 2) zbc_rev(g, k, n, bl, bh);
-        if (!wl && nonzero(bl)) {
-            LOb.p[n][f] += (double)bl;
-            aadd(&T1b.p[n][lp1], (double)(-c1 * l1p * bl));
-            aadd(&T1b.p[n][lm1], (double)(c1 * l1m * bl));
-            aadd(&T2b.p[n][lp2], (double)(-c2 * l2p * bl));
-            aadd(&T2b.p[n][lm2], (double)(c2 * l2m * bl));
-            gl1p += (-c1 * T1.p[n][lp1] + c1 * ql) * bl;
-            gl1m += (c1 * T1.p[n][lm1] - c1 * ql) * bl;
-            gl2p += (-c2 * T2.p[n][lp2] + c2 * ql) * bl;
-            gl2m += (c2 * T2.p[n][lm2] - c2 * ql) * bl;
-            aadd(&ub[n * g.N + cl], (double)(rho * (c1 * (l1p - l1m) + c2 * (l2p - l2m)) * bl));
-            aadd(&forcesb[n * g.N + cl], (double)(hdt * rho * bl));
-        }
-        if (!wh && nonzero(bh)) {
-            HIb.p[n][f] += (double)bh;
-            aadd(&T1b.p[n][hp1], (double)(-c1 * h1p * bh));
-            aadd(&T1b.p[n][hm1], (double)(c1 * h1m * bh));
-            aadd(&T2b.p[n][hp2], (double)(-c2 * h2p * bh));
-            aadd(&T2b.p[n][hm2], (double)(c2 * h2m * bh));
-            gh1p += (-c1 * T1.p[n][hp1] + c1 * qh) * bh;
-            gh1m += (c1 * T1.p[n][hm1] - c1 * qh) * bh;
-            gh2p += (-c2 * T2.p[n][hp2] + c2 * qh) * bh;
-            gh2m += (c2 * T2.p[n][hm2] - c2 * qh) * bh;
-            aadd(&ub[n * g.N + ch], (double)(rho * (c1 * (h1p - h1m) + c2 * (h2p - h2m)) * bh));
-            aadd(&forcesb[n * g.N + ch], (double)(hdt * rho * bh));
+        if (!wl) LOb.p[n][f] += (double)bl;
+        if (!wh) HIb.p[n][f] += (double)bh;
+    }
+    if (nonzero(gum)) Udb[f] += (double)gum;
+}
+
+// adjoints (bl, bh) of the two states of a d-face of stage 3 (the upwind
+// selection by um, then the wall rule)
+template <typename A>
+__device__ inline void flux_state_rev(const Grid& g, int d, int k, int n, A um, A fb, A& bl, A& bh) {
+    bl = bh = A(0);
+    if (below_small_abs(um)) bl = bh = A(0.5) * um * fb;
+    else if (ge0(um)) bl = um * fb;
+    else bh = um * fb;
+    if (d == 2) zbc_rev(g, k, n, bl, bh);
+}
+
+// stage 3, per cell: cb = bl(face above) + bh(face below); the velocity and
+// forces adjoints of the cell; cb kept in CB (3 components)
+template <typename TI>
+__global__ void k_adj_flux_cells(Grid g, int d, double rho64, double dt64, double c1_64, double c2_64, K3 Uf, K3 Fb, double* ub, double* forcesb,
+                                 TI* CB) {
+    using A = TI;
+    int i, j, k;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (!face_at(g, 0, t, i, j, k)) return;  // the x-face domain is the cell domain
+    const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
+    const long long flo = fidx(g, d, i, j, k), fhi = fidx(g, d, i + (d == 0), j + (d == 1), k + (d == 2));
+    const A ulo = (A)Uf.p[d][flo], uhi = (A)Uf.p[d][fhi];
+    const long long p1 = fidx(g, b1, i + (b1 == 0), j + (b1 == 1), k + (b1 == 2)), m1 = fidx(g, b1, i, j, k);
+    const long long p2 = fidx(g, b2, i + (b2 == 0), j + (b2 == 1), k + (b2 == 2)), m2 = fidx(g, b2, i, j, k);
+    const A rho = (A)rho64, c1 = (A)c1_64, c2 = (A)c2_64, hdt = A(0.5) * (A)dt64;
+    const A r = rho * (c1 * ((A)Uf.p[b1][p1] - (A)Uf.p[b1][m1]) + c2 * ((A)Uf.p[b2][p2] - (A)Uf.p[b2][m2]));
+    for (int n = 0; n < 3; ++n) {
+        A bl, bh, dl, dh;
+        flux_state_rev(g, d, k, n, ulo, (A)Fb.p[n][flo], dl, bh);
+        flux_state_rev(g, d, k + 1, n, uhi, (A)Fb.p[n][fhi], bl, dh);
+        const A cb = bh + bl;
+        CB[n * g.N + t] = cb;
+        if (nonzero(cb)) {
+            ub[n * g.N + t] += (double)(r * cb);
+            forcesb[n * g.N + t] += (double)(hdt * rho * cb);
         }
     }
-    aadd(&Ufb.p[d][f], (double)gum);
-    aadd(&Ufb.p[b1][lp1], (double)gl1p);
-    aadd(&Ufb.p[b1][lm1], (double)gl1m);
-    aadd(&Ufb.p[b2][lp2], (double)gl2p);
-    aadd(&Ufb.p[b2][lm2], (double)gl2m);
-    aadd(&Ufb.p[b1][hp1], (double)gh1p);
-    aadd(&Ufb.p[b1][hm1], (double)gh1m);
-    aadd(&Ufb.p[b2][hp2], (double)gh2p);
-    aadd(&Ufb.p[b2][hm2], (double)gh2m);
+}
+
+// stage 3 / stage 2, per b-face: the faces' T_b (E_b) and MAC velocity
+// adjoints from cb of the cells below (c-, the face is its high b face) and
+// above (c+, its low b face):
+//   Tb_n += c v (cb_n(c+) - cb_n(c-)),
+//   vb += c sum_n (T_n (cb_n(c+) - cb_n(c-)) + rho (q_n(c-) cb_n(c-) - q_n(c+) cb_n(c+)))
+// (c = c_b of stage 3, cb of stage 2).  CB holds the cb of this b.
+template <typename TI>
+__global__ void k_adj_bfaces(Grid g, int b, const double* u, double rho64, double c64, const double* vb, KI<TI> T, const TI* CB, A3 Tb,
+                             double* vbb) {
+    using A = TI;
+    int i, j, k;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (!face_at(g, b, t, i, j, k)) return;
+    const bool walls = b == 2 && !g.zper;
+    const bool hasm = !(walls && k == 0), hasp = !(walls && k == g.nz);
+    const long long f = t;
+    const long long cp = hasp ? cidx(g, i, j, k) : 0;
+    const long long cm = hasm ? cidx(g, wrapn(i - (b == 0), g.nx), wrapn(j - (b == 1), g.ny), g.zper ? wrapn(k - (b == 2), g.nz) : k - (b == 2)) : 0;
+    const A c = (A)c64, rho = (A)rho64, v = (A)vb[f];
+    A gv = A(0);
+    for (int n = 0; n < 3; ++n) {
+        const A bp = hasp ? CB[n * g.N + cp] : A(0), bm = hasm ? CB[n * g.N + cm] : A(0);
+        if (!nonzero(bp) && !nonzero(bm)) continue;
+        const A e = T.p[n][f];
+        Tb.p[n][f] += (double)(c * v * (bp - bm));
+        const A qm = hasm ? rho * (A)u[n * g.N + cm] : A(0), qp = hasp ? rho * (A)u[n * g.N + cp] : A(0);
+        gv += (c * qm - c * e) * bm + (c * e - c * qp) * bp;
+    }
+    if (nonzero(gv)) vbb[f] += (double)gv;
+}
+
+// stage 2 for the a-faces, per cell: the adjoints of its two corrections (one
+// per transverse direction), cb_k = lb_k(face above) + hb_k(face below) from
+// the upwind selections of outputs O1 (along b1) and O2 (along b2); the
+// velocity adjoint of the cell; the LO / HI adjoints of its low a-face (and
+// of the top wall face from the cells under it).  CB holds cb_1 then cb_2.
+template <typename TI>
+__global__ void k_adj_trans_cells(Grid g, int a, double rho64, double cb1_64, double cb2_64, const double* ua, const double* v1, const double* v2,
+                                  K3 O1b, K3 O2b, A3 LOb, A3 HIb, double* ub, TI* CB) {
+    using A = TI;
+    int i, j, k;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (!face_at(g, 0, t, i, j, k)) return;
+    const int b1 = (a + 1) % 3, b2 = (a + 2) % 3;
+    const bool top = a == 2 && !g.zper && k + 1 == g.nz;  // the face above is the top wall face
+    const long long flo = fidx(g, a, i, j, k), fhi = fidx(g, a, i + (a == 0), j + (a == 1), k + (a == 2));
+    const A ulo = (A)ua[flo], uhi = (A)ua[fhi];
+    const long long p1 = fidx(g, b1, i + (b1 == 0), j + (b1 == 1), k + (b1 == 2)), m1 = fidx(g, b1, i, j, k);
+    const long long p2 = fidx(g, b2, i + (b2 == 0), j + (b2 == 1), k + (b2 == 2)), m2 = fidx(g, b2, i, j, k);
+    const A rho = (A)rho64;
+    const A w1 = rho * (A)cb1_64 * ((A)v1[p1] - (A)v1[m1]), w2 = rho * (A)cb2_64 * ((A)v2[p2] - (A)v2[m2]);
+    A ubs[3];
+    for (int n = 0; n < 3; ++n) {
+        A l1 = A(0), h1 = A(0), l2 = A(0), h2 = A(0), L1 = A(0), H1 = A(0), L2 = A(0), H2 = A(0);
+        rev_upwind(ulo, (A)O1b.p[n][flo], l1, h1);  // face below
+        rev_upwind(ulo, (A)O2b.p[n][flo], l2, h2);
+        rev_upwind(uhi, (A)O1b.p[n][fhi], L1, H1);  // face above
+        rev_upwind(uhi, (A)O2b.p[n][fhi], L2, H2);
+        if (a == 2) {
+            zbc_rev(g, k, n, l1, h1);
+            zbc_rev(g, k, n, l2, h2);
+            zbc_rev(g, k + 1, n, L1, H1);
+            zbc_rev(g, k + 1, n, L2, H2);
+        }
+        const A sl = l1 + l2, sh = h1 + h2;
+        if (nonzero(sl)) LOb.p[n][flo] += (double)sl;
+        if (nonzero(sh)) HIb.p[n][flo] += (double)sh;
+        if (top) {
+            LOb.p[n][fhi] += (double)(L1 + L2);
+            HIb.p[n][fhi] += (double)(H1 + H2);
+        }
+        const A cb1 = h1 + L1, cb2 = h2 + L2;
+        CB[n * g.N + t] = cb1;
+        CB[(3 + n) * g.N + t] = cb2;
+        ubs[n] = w1 * cb1 + w2 * cb2;
+    }
+    for (int n = 0; n < 3; ++n)
+        if (nonzero(ubs[n])) ub[n * g.N + t] += (double)ubs[n];
 }
 
 // ---- reverse of conv = -div F on d-faces: Fb(f) = (convb(cell above f) - convb(cell below f)) / h_d
@@ -1134,42 +1183,58 @@ void launch_adj_pm_final(Ctx& c, const Grid& g, int d, double dt, const GodunovB
 }
 
 template <typename TI>
-static void adj_adv_trans_t(Ctx& c, const Grid& g, int a, int b, const double* u, double rho, double dt, const double* const mac[3],
-                            const GodunovBufs& B, const AdjBufs& A) {
-    KI<TI> E{{ti<TI>(B.tedge[b][0]), ti<TI>(B.tedge[b][1]), ti<TI>(B.tedge[b][2])}};
-    K3 Ob{{A.tr[a][b][0], A.tr[a][b][1], A.tr[a][b][2]}};
+static void adj_adv_trans_t(Ctx& c, const Grid& g, int a, const double* u, double rho, double dt, const double* const mac[3],
+                            const GodunovBufs& B, const AdjBufs& A, double* CB) {
+    const int b1 = (a + 1) % 3, b2 = (a + 2) % 3;
+    const double cb1 = dt / (3.0 * hd(g, b1)), cb2 = dt / (3.0 * hd(g, b2));
+    K3 O1b{{A.tr[a][b1][0], A.tr[a][b1][1], A.tr[a][b1][2]}}, O2b{{A.tr[a][b2][0], A.tr[a][b2][1], A.tr[a][b2][2]}};
     A3 LOb{{A.lo[a][0], A.lo[a][1], A.lo[a][2]}}, HIb{{A.hi[a][0], A.hi[a][1], A.hi[a][2]}};
-    A3 Ebb{{A.tedge[b][0], A.tedge[b][1], A.tedge[b][2]}};
-    const long long na = nfaces(g, a), nb = nfaces(g, b);
-    KS_LAUNCH(c, k_adj_adv_trans<TI>, nblocks(na, BS), BS, B8 * (6.0 * g.N + 10.0 * na + 5.0 * nb) + sizeof(TI) * 3.0 * nb, g, a, b, u, rho,
-              dt / (3.0 * hd(g, b)), mac[a], mac[b], E, Ob, LOb, HIb, Ebb, A.umac[b], A.u);
+    const double na = (double)nfaces(g, a), N = (double)g.N;
+    KS_LAUNCH(c, k_adj_trans_cells<TI>, nblocks(g.N, BS), BS, B8 * (2.0 * na + 4.0 * N + 12.0 * na + 12.0 * na + 6.0 * N + 6.0 * N), g, a, rho,
+              cb1, cb2, mac[a], mac[b1], mac[b2], O1b, O2b, LOb, HIb, A.u, reinterpret_cast<TI*>(CB));
+    for (int q = 0; q < 2; ++q) {
+        const int b = q == 0 ? b1 : b2;
+        const double nb = (double)nfaces(g, b);
+        KI<TI> E{{ti<TI>(B.tedge[b][0]), ti<TI>(B.tedge[b][1]), ti<TI>(B.tedge[b][2])}};
+        A3 Eb{{A.tedge[b][0], A.tedge[b][1], A.tedge[b][2]}};
+        KS_LAUNCH(c, k_adj_bfaces<TI>, nblocks(nfaces(g, b), BS), BS, B8 * (12.0 * N + 2.0 * nb + 6.0 * nb) + sizeof(TI) * 3.0 * nb, g, b, u, rho,
+                  q == 0 ? cb1 : cb2, mac[b], E, reinterpret_cast<const TI*>(CB) + 3LL * q * g.N, Eb, A.umac[b]);
+    }
 }
-void launch_adj_adv_trans(Ctx& c, const Grid& g, int a, int b, const double* u, double rho, double dt, const double* const mac[3],
-                          const GodunovBufs& B, const AdjBufs& A, int fp32) {
-    if (fp32) adj_adv_trans_t<float>(c, g, a, b, u, rho, dt, mac, B, A);
-    else adj_adv_trans_t<double>(c, g, a, b, u, rho, dt, mac, B, A);
+void launch_adj_adv_trans(Ctx& c, const Grid& g, int a, const double* u, double rho, double dt, const double* const mac[3],
+                          const GodunovBufs& B, const AdjBufs& A, double* CB, int fp32) {
+    if (fp32) adj_adv_trans_t<float>(c, g, a, u, rho, dt, mac, B, A, CB);
+    else adj_adv_trans_t<double>(c, g, a, u, rho, dt, mac, B, A, CB);
 }
 
 template <typename TI>
 static void adj_adv_flux_t(Ctx& c, const Grid& g, int d, const double* u, const double* forces, double rho, double dt, const double* const mac[3],
-                           const GodunovBufs& B, const AdjBufs& A) {
+                           const GodunovBufs& B, const AdjBufs& A, double* CB) {
     const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
+    const double c1 = dt / (2.0 * hd(g, b1)), c2 = dt / (2.0 * hd(g, b2));
     K3 Uf{{mac[0], mac[1], mac[2]}};
     KI<TI> LO{{ti<TI>(B.lo[d][0]), ti<TI>(B.lo[d][1]), ti<TI>(B.lo[d][2])}}, HI{{ti<TI>(B.hi[d][0]), ti<TI>(B.hi[d][1]), ti<TI>(B.hi[d][2])}};
     KI<TI> T1{{ti<TI>(B.tr[b1][b2][0]), ti<TI>(B.tr[b1][b2][1]), ti<TI>(B.tr[b1][b2][2])}};
     KI<TI> T2{{ti<TI>(B.tr[b2][b1][0]), ti<TI>(B.tr[b2][b1][1]), ti<TI>(B.tr[b2][b1][2])}};
     K3 Fb{{A.flux[d][0], A.flux[d][1], A.flux[d][2]}};
-    A3 Ufb{{A.umac[0], A.umac[1], A.umac[2]}};
     A3 LOb{{A.lo[d][0], A.lo[d][1], A.lo[d][2]}}, HIb{{A.hi[d][0], A.hi[d][1], A.hi[d][2]}};
     A3 T1b{{A.tr[b1][b2][0], A.tr[b1][b2][1], A.tr[b1][b2][2]}}, T2b{{A.tr[b2][b1][0], A.tr[b2][b1][1], A.tr[b2][b1][2]}};
-    const long long nf = nfaces(g, d), nt = nfaces(g, b1) + nfaces(g, b2);
-    KS_LAUNCH(c, k_adj_adv_flux<TI>, nblocks(nf, BS), BS, B8 * (12.0 * g.N + 10.0 * nf + 8.0 * nt) + sizeof(TI) * (6.0 * nf + 6.0 * nt), g, d, u,
-              forces, rho, dt, dt / (2.0 * hd(g, b1)), dt / (2.0 * hd(g, b2)), Uf, LO, HI, T1, T2, Fb, Ufb, LOb, HIb, T1b, T2b, A.u, A.forces);
+    const double nf = (double)nfaces(g, d), nt = (double)(nfaces(g, b1) + nfaces(g, b2)), N = (double)g.N;
+    KS_LAUNCH(c, k_adj_flux_faces<TI>, nblocks(nfaces(g, d), BS), BS, B8 * (6.0 * N + 5.0 * nf + 8.0 * nt + 7.0 * nf) + sizeof(TI) * (6.0 * nf + 6.0 * nt),
+              g, d, u, forces, rho, dt, c1, c2, Uf, LO, HI, T1, T2, Fb, A.umac[d], LOb, HIb);
+    KS_LAUNCH(c, k_adj_flux_cells<TI>, nblocks(g.N, BS), BS, B8 * (2.0 * nf + 6.0 * nf + nt + 12.0 * N) + sizeof(TI) * 3.0 * N, g, d, rho, dt, c1,
+              c2, Uf, Fb, A.u, A.forces, reinterpret_cast<TI*>(CB));
+    for (int q = 0; q < 2; ++q) {
+        const int b = q == 0 ? b1 : b2;
+        const double nb = (double)nfaces(g, b);
+        KS_LAUNCH(c, k_adj_bfaces<TI>, nblocks(nfaces(g, b), BS), BS, B8 * (12.0 * N + 2.0 * nb + 6.0 * nb) + sizeof(TI) * 3.0 * nb, g, b, u, rho,
+                  q == 0 ? c1 : c2, mac[b], q == 0 ? T1 : T2, reinterpret_cast<const TI*>(CB), q == 0 ? T1b : T2b, A.umac[b]);
+    }
 }
 void launch_adj_adv_flux(Ctx& c, const Grid& g, int d, const double* u, const double* forces, double rho, double dt, const double* const mac[3],
-                         const GodunovBufs& B, const AdjBufs& A, int fp32) {
-    if (fp32) adj_adv_flux_t<float>(c, g, d, u, forces, rho, dt, mac, B, A);
-    else adj_adv_flux_t<double>(c, g, d, u, forces, rho, dt, mac, B, A);
+                         const GodunovBufs& B, const AdjBufs& A, double* CB, int fp32) {
+    if (fp32) adj_adv_flux_t<float>(c, g, d, u, forces, rho, dt, mac, B, A, CB);
+    else adj_adv_flux_t<double>(c, g, d, u, forces, rho, dt, mac, B, A, CB);
 }
 void launch_adj_div(Ctx& c, const Grid& g, const double* convb, const AdjBufs& A) {
     for (int d = 0; d < 3; ++d) {

@@ -80,6 +80,7 @@ void Sim::adj_alloc() {
     for (auto* b : {&S->w, &S->t1, &S->t2, &S->srcb, &S->doldb, &S->su, &S->sgp}) b->alloc(N3);
     S->sp.alloc(p_.n);
     S->mub.alloc(N);
+    S->cbuf.alloc(6 * N);
     S->wgb.alloc(2 * (size_t)g_.nx * g_.ny);
     // post-MAC intermediates of the recompute: lo, hi, tedge, flux per direction and tr
     size_t total2 = 0;
@@ -292,10 +293,9 @@ void Sim::adjoint_step_impl(bool seed) {
     launch_fill(ctx_, A.forces, 0.0, N3);
     const double* mac[3] = {umac_[0].p, umac_[1].p, umac_[2].p};
     launch_adj_div(ctx_, g_, S.srcb.p, A);
-    for (int d = 0; d < 3; ++d) launch_adj_adv_flux(ctx_, g_, d, vel_old_.p, forces_.p, rho_, dt, mac, S.gb2, A, fp32);
-    for (int a = 0; a < 3; ++a)
-        for (int b = 0; b < 3; ++b)
-            if (a != b) launch_adj_adv_trans(ctx_, g_, a, b, vel_old_.p, rho_, dt, mac, S.gb2, A, fp32);
+    // stage 3 first: it accumulates the adjoints of the stage-2 outputs
+    for (int d = 0; d < 3; ++d) launch_adj_adv_flux(ctx_, g_, d, vel_old_.p, forces_.p, rho_, dt, mac, S.gb2, A, S.cbuf.p, fp32);
+    for (int a = 0; a < 3; ++a) launch_adj_adv_trans(ctx_, g_, a, vel_old_.p, rho_, dt, mac, S.gb2, A, S.cbuf.p, fp32);
     for (int a = 0; a < 3; ++a) launch_adj_faces(ctx_, g_, a, 1, vel_old_.p, S.gb2, A, dt, rho_, umac_[a].p, fp32);
     // ---- MAC projection (symmetric on the faces it changes): the pre-MAC
     // output on wall faces is 0 whatever the input, so their adjoint is dropped

@@ -121,6 +121,9 @@ __device__ __forceinline__ bool igt0(double x) { return dbits(x) > 0; }   // x >
 __device__ __forceinline__ bool ile0(double x) { return dbits(x) <= 0; }  // x <= 0
 __device__ __forceinline__ bool ilt0(double x) { return okey(x) < -1; }   // x < 0 (-0 is not)
 __device__ __forceinline__ bool ige0(double x) { return okey(x) >= -1; }  // x >= 0 (-0 is)
+// ilt / imin / imax order -0 below +0 (okey(-0) = -1, okey(+0) = 0), where IEEE
+// compares them equal: a +-0 tie goes to the signed zero's order, not to the
+// first operand as fmin / fmax may
 __device__ __forceinline__ bool ilt(double a, double b) { return okey(a) < okey(b); }
 __device__ __forceinline__ double imin(double a, double b) { return okey(a) < okey(b) ? a : b; }
 __device__ __forceinline__ double imax(double a, double b) { return okey(a) > okey(b) ? a : b; }

@@ -304,10 +304,13 @@ void launch_adj_faces(Ctx& c, const Grid& g, int d, int mode, const double* u, c
                       const double* umac_d, int fp32);
 void launch_adj_pm_trans(Ctx& c, const Grid& g, int a, int b, int n, double dt, const GodunovBufs& B, const AdjBufs& A, int fp32);
 void launch_adj_pm_final(Ctx& c, const Grid& g, int d, double dt, const GodunovBufs& B, const double* forces, const AdjBufs& A, int fp32);
-void launch_adj_adv_trans(Ctx& c, const Grid& g, int a, int b, const double* u, double rho, double dt, const double* const mac[3],
-                          const GodunovBufs& B, const AdjBufs& A, int fp32);
+// reverse of the post-MAC stages 2 (both transverse directions of the a-faces)
+// and 3 (d-faces), gather form; CB: 6N doubles of scratch (the per-cell
+// correction adjoints)
+void launch_adj_adv_trans(Ctx& c, const Grid& g, int a, const double* u, double rho, double dt, const double* const mac[3],
+                          const GodunovBufs& B, const AdjBufs& A, double* CB, int fp32);
 void launch_adj_adv_flux(Ctx& c, const Grid& g, int d, const double* u, const double* forces, double rho, double dt, const double* const mac[3],
-                         const GodunovBufs& B, const AdjBufs& A, int fp32);
+                         const GodunovBufs& B, const AdjBufs& A, double* CB, int fp32);
 void launch_adj_div(Ctx& c, const Grid& g, const double* convb, const AdjBufs& A);
 // reverse of divtau(vel; mueff, wg) for the adjoint s * divtau_b: accumulates the
 // velocity (ub), cell viscosity (mub, may be null) and wall-gradient (wgb, may be null) adjoints
