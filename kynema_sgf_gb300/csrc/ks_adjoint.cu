@@ -136,17 +136,37 @@ __device__ inline A clip_rev(A e, A a, A b, A rb, A& ga, A& gb) {
     return rb;
 }
 
-// ---- reverse of the unlimited PPM edges on d-faces (k_edges).  TI is the
-// forward's precision and the arithmetic type of the reverse pass.
-template <typename TI>
-__global__ void k_adj_edges(Grid g, int d, const double* u, const double* Eb0, const double* Eb1, const double* Eb2, double* ub) {
-    using A = TI;
-    int i, j, k;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (!face_at(g, d, t, i, j, k)) return;
+// adjoints of the four cells of an interior d-face's unlimited edge
+// e = (a0 + a1) / 2 - (s1 - s0) / 6 (s the van Leer slopes), clipped to
+// [a0, a1], given the edge's adjoint eb: g[0..3] for cells am, a0, a1, a2
+template <typename A>
+__device__ inline void edge_rev(A am, A a0, A a1, A a2, A eb, A g[4]) {
+    A c1a, c1b, c1c, c0a, c0b, c0c;
+    const A s1 = vls_d(a0, a1, a2, c1a, c1b, c1c);
+    const A s0 = vls_d(am, a0, a1, c0a, c0b, c0c);
+    const A e = A(0.5) * (a0 + a1) - A(1.0 / 6.0) * (s1 - s0);
+    g[0] = g[1] = g[2] = g[3] = A(0);
+    const A ebar = clip_rev(e, a0, a1, eb, g[1], g[2]);
+    if (nonzero(ebar)) {
+        g[1] += A(0.5) * ebar;
+        g[2] += A(0.5) * ebar;
+        const A ds1 = -ebar * A(1.0 / 6.0), ds0 = ebar * A(1.0 / 6.0);
+        g[1] += ds1 * c1a;
+        g[2] += ds1 * c1b;
+        g[3] += ds1 * c1c;
+        g[0] += ds0 * c0a;
+        g[1] += ds0 * c0b;
+        g[2] += ds0 * c0c;
+    }
+}
+
+// the reverse of one d-face's edge, scattered with atomics (the wall faces and
+// the one-sided faces next to them, every face of a short wall-bounded column)
+template <typename A>
+__device__ inline void edge_rev_scatter(const Grid& g, int d, const double* u, const double* const Eb[3], int i, int j, int k, long long t,
+                                        double* ub) {
     const int di = (d == 0), dj = (d == 1), dk = (d == 2);
     const bool wall = (d == 2 && !g.zper);
-    const double* Eb[3] = {Eb0, Eb1, Eb2};
     for (int n = 0; n < 3; ++n) {
         const double eb64 = Eb[n][t];
         if (!(dbits(eb64) & kMag)) continue;
@@ -168,29 +188,80 @@ __global__ void k_adj_edges(Grid g, int d, const double* u, const double* Eb0, c
             Qb(g, ub, n, i, j, k0 + 2 * s, (double)(A(-0.05) * ebar));
             continue;
         }
-        const A am = Q<A>(g, u, n, i - 2 * di, j - 2 * dj, k - 2 * dk), a0 = Q<A>(g, u, n, i - di, j - dj, k - dk);
-        const A a1 = Q<A>(g, u, n, i, j, k), a2 = Q<A>(g, u, n, i + di, j + dj, k + dk);
-        A c1a, c1b, c1c, c0a, c0b, c0c;
-        const A s1 = vls_d(a0, a1, a2, c1a, c1b, c1c);
-        const A s0 = vls_d(am, a0, a1, c0a, c0b, c0c);
-        const A e = A(0.5) * (a0 + a1) - A(1.0 / 6.0) * (s1 - s0);
-        A gm = A(0), g0 = A(0), g1 = A(0), g2 = A(0);
-        const A ebar = clip_rev(e, a0, a1, eb, g0, g1);
-        if (nonzero(ebar)) {
-            g0 += A(0.5) * ebar;
-            g1 += A(0.5) * ebar;
-            const A ds1 = -ebar * A(1.0 / 6.0), ds0 = ebar * A(1.0 / 6.0);
-            g0 += ds1 * c1a;
-            g1 += ds1 * c1b;
-            g2 += ds1 * c1c;
-            gm += ds0 * c0a;
-            g0 += ds0 * c0b;
-            g1 += ds0 * c0c;
+        A gr[4];
+        edge_rev(Q<A>(g, u, n, i - 2 * di, j - 2 * dj, k - 2 * dk), Q<A>(g, u, n, i - di, j - dj, k - dk), Q<A>(g, u, n, i, j, k),
+                 Q<A>(g, u, n, i + di, j + dj, k + dk), eb, gr);
+        Qb(g, ub, n, i - 2 * di, j - 2 * dj, k - 2 * dk, (double)gr[0]);
+        Qb(g, ub, n, i - di, j - dj, k - dk, (double)gr[1]);
+        Qb(g, ub, n, i, j, k, (double)gr[2]);
+        Qb(g, ub, n, i + di, j + dj, k + dk, (double)gr[3]);
+    }
+}
+
+// ---- reverse of the unlimited PPM edges on d-faces (k_edges).  TI is the
+// forward's precision and the arithmetic type of the reverse pass.
+// Scatter form over all d-faces (short wall-bounded columns) ...
+template <typename TI>
+__global__ void k_adj_edges(Grid g, int d, const double* u, const double* Eb0, const double* Eb1, const double* Eb2, double* ub) {
+    int i, j, k;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (!face_at(g, d, t, i, j, k)) return;
+    const double* Eb[3] = {Eb0, Eb1, Eb2};
+    edge_rev_scatter<TI>(g, d, u, Eb, i, j, k, t, ub);
+}
+
+// ... or over the face layers 0, 1, nz - 1, nz of a wall-bounded z (nz >= 4)
+template <typename TI>
+__global__ void k_adj_edges_wall(Grid g, const double* u, const double* Eb0, const double* Eb1, const double* Eb2, double* ub) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long M = (long long)g.nx * g.ny;
+    if (t >= 4 * M) return;
+    const int layer = (int)(t / M), r = (int)(t - layer * M);
+    const int k = layer < 2 ? layer : g.nz - 3 + layer, j = r / g.nx, i = r - j * g.nx;
+    const double* Eb[3] = {Eb0, Eb1, Eb2};
+    edge_rev_scatter<TI>(g, 2, u, Eb, i, j, k, cidx(g, i, j, k), ub);
+}
+
+// ... with every other face gathered per cell: cell c is a2, a1, a0, am of the
+// d-faces c - 1, c, c + 1, c + 2 (face m reads cells m - 2 .. m + 1); the
+// thread re-evaluates those four faces' slopes and clips from the seven cells
+// c - 3 .. c + 3 (cheap in the pass precision) and owns the cell's adjoint.
+// With a wall-bounded z only the faces 2 .. nz - 2 are gathered.
+template <typename TI>
+__global__ void __launch_bounds__(256, 2) k_adj_edges_gather(Grid g, int d, const double* u, const double* Eb0, const double* Eb1, const double* Eb2, double* ub) {
+    using A = TI;
+    int i, j, k;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (!face_at(g, 0, t, i, j, k)) return;  // the x-face domain is the cell domain
+    const bool wall = (d == 2 && !g.zper);
+    const int c = d == 0 ? i : (d == 1 ? j : k), nd = d == 0 ? g.nx : (d == 1 ? g.ny : g.nz);
+    const long long st = d == 0 ? 1 : (d == 1 ? (long long)g.nx : (long long)g.nx * g.ny);
+    const long long base = t - (long long)c * st;  // the cell's column at d-index 0
+    const double* Eb[3] = {Eb0, Eb1, Eb2};
+    for (int n = 0; n < 3; ++n) {
+        const double* un = u + n * g.N;
+        A q[7];  // cells c - 3 .. c + 3 (wrapped; unused where a wall cuts the column)
+        for (int s = -3; s <= 3; ++s) {
+            int m = c + s;
+            if (wall) m = m < 0 ? 0 : (m >= nd ? nd - 1 : m);
+            else m = m < 0 ? m + nd : (m >= nd ? m - nd : m);
+            q[s + 3] = (A)un[base + m * st];
         }
-        Qb(g, ub, n, i - 2 * di, j - 2 * dj, k - 2 * dk, (double)gm);
-        Qb(g, ub, n, i - di, j - dj, k - dk, (double)g0);
-        Qb(g, ub, n, i, j, k, (double)g1);
-        Qb(g, ub, n, i + di, j + dj, k + dk, (double)g2);
+        A acc = A(0);
+        for (int o = -1; o <= 2; ++o) {  // face m = c + o; the cell is its cell m + 1 - (o + 1) ... role 2 - o
+            int m = c + o;
+            if (wall) {
+                if (m < 2 || m > nd - 2) continue;
+            } else {
+                m = m < 0 ? m + nd : (m >= nd ? m - nd : m);
+            }
+            const double eb64 = Eb[n][base + m * st];
+            if (!(dbits(eb64) & kMag)) continue;
+            A gr[4];
+            edge_rev(q[o + 1], q[o + 2], q[o + 3], q[o + 4], (A)eb64, gr);
+            acc += gr[2 - o];
+        }
+        if (nonzero(acc)) ub[n * g.N + t] += (double)acc;
     }
 }
 
@@ -1122,12 +1193,23 @@ static const TI* ti(void* p) {
     return static_cast<const TI*>(p);
 }
 
-void launch_adj_edges(Ctx& c, const Grid& g, int d, const double* u, double* const Eb[3], double* ub, int fp32) {
+template <typename TI>
+static void adj_edges_t(Ctx& c, const Grid& g, int d, const double* u, double* const Eb[3], double* ub) {
     const long long nf = nfaces(g, d);
-    if (fp32)
-        KS_LAUNCH(c, k_adj_edges<float>, nblocks(nf, BS), BS, B8 * (3.0 * nf + 6.0 * g.N), g, d, u, Eb[0], Eb[1], Eb[2], ub);
-    else
-        KS_LAUNCH(c, k_adj_edges<double>, nblocks(nf, BS), BS, B8 * (3.0 * nf + 6.0 * g.N), g, d, u, Eb[0], Eb[1], Eb[2], ub);
+    const int nd = d == 0 ? g.nx : (d == 1 ? g.ny : g.nz);
+    if (nd < 4) {  // the gather's window of 7 cells wraps more than once
+        KS_LAUNCH(c, k_adj_edges<TI>, nblocks(nf, BS), BS, B8 * (3.0 * nf + 6.0 * g.N), g, d, u, Eb[0], Eb[1], Eb[2], ub);
+        return;
+    }
+    KS_LAUNCH(c, k_adj_edges_gather<TI>, nblocks(g.N, BS), BS, B8 * (3.0 * nf + 6.0 * g.N), g, d, u, Eb[0], Eb[1], Eb[2], ub);
+    if (d == 2 && !g.zper) {
+        const long long M = 4LL * g.nx * g.ny;
+        KS_LAUNCH(c, k_adj_edges_wall<TI>, nblocks(M, BS), BS, B8 * 3.0 * (M + 4.0 * M), g, u, Eb[0], Eb[1], Eb[2], ub);
+    }
+}
+void launch_adj_edges(Ctx& c, const Grid& g, int d, const double* u, double* const Eb[3], double* ub, int fp32) {
+    if (fp32) adj_edges_t<float>(c, g, d, u, Eb, ub);
+    else adj_edges_t<double>(c, g, d, u, Eb, ub);
 }
 
 template <typename TI>
