@@ -818,17 +818,20 @@ constexpr int ANH = AHX * AHY * AHZ;
 // shared memory of the reverse diffusion tile: FP64 accumulators (4 per box
 // cell) and the staged values in the arithmetic type A (7 per box cell)
 template <typename A>
-constexpr size_t adj_tau_smem() { return sizeof(double) * 4 * (size_t)ANH + sizeof(A) * 7 * (size_t)ANH; }
+constexpr size_t adj_tau_smem() { return sizeof(A) * 11 * (size_t)ANH; }
 
-// A: arithmetic of the face terms, double, or float for the reverse of the
-// mixed-precision form's FP32 diffusion; the accumulators are FP64.
+// A: arithmetic of the face terms and of the tile's shared-memory
+// accumulators, double, or float for the reverse of the mixed-precision
+// form's FP32 diffusion (native FP32 shared-memory atomics; each tile
+// position sums a few dozen face terms); the flush adds them to the FP64
+// adjoints.
 template <typename A>
 __global__ void __launch_bounds__(ATX* ATY* ATZ) k_adj_tau_tile(Grid g, const double* vel, const double* mu, const double* wg,
                                                                 const double* db, double s, double* ub, double* mub, double* wgb) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
-    double* aU = reinterpret_cast<double*>(sm_raw);  // [3][box] accumulated velocity adjoint
-    double* aM = aU + 3 * ANH;                       // [box] accumulated viscosity adjoint
-    A* sV = reinterpret_cast<A*>(aM + ANH);          // [3][box]
+    A* aU = reinterpret_cast<A*>(sm_raw);  // [3][box] accumulated velocity adjoint
+    A* aM = aU + 3 * ANH;                  // [box] accumulated viscosity adjoint
+    A* sV = aM + ANH;                      // [3][box]
     A* sD = sV + 3 * ANH;                            // [3][box] divergence adjoint (cells in the domain, else 0)
     A* sM = sV + 6 * ANH;                            // [box]
     const int i0 = blockIdx.x * ATX, j0 = blockIdx.y * ATY, k0 = blockIdx.z * ATZ;
@@ -847,9 +850,9 @@ __global__ void __launch_bounds__(ATX* ATY* ATZ) k_adj_tau_tile(Grid g, const do
         sM[h] = (A)mu[c];
         for (int n = 0; n < 3; ++n) {
             sD[n * ANH + h] = inz ? sA * (A)db[n * g.N + c] : A(0);
-            aU[n * ANH + h] = 0.0;
+            aU[n * ANH + h] = A(0);
         }
-        aM[h] = 0.0;
+        aM[h] = A(0);
     }
     __syncthreads();
     const A ih[3] = {(A)g.idx, (A)g.idy, (A)g.idz};
@@ -919,25 +922,25 @@ __global__ void __launch_bounds__(ATX* ATY* ATZ) k_adj_tau_tile(Grid g, const do
             }
         }
         for (int m = 0; m < 3; ++m) grb[m][m] += dvb;
-        if (!has_lo) atomicAdd(&aM[hb(hx, hy, hz)], (double)mfb);
-        else if (!has_hi) atomicAdd(&aM[hb(mx, my, mz)], (double)mfb);
+        if (!has_lo) atomicAdd(&aM[hb(hx, hy, hz)], mfb);
+        else if (!has_hi) atomicAdd(&aM[hb(mx, my, mz)], mfb);
         else {
-            const double hm = (double)(A(0.5) * mfb);
+            const A hm = A(0.5) * mfb;
             atomicAdd(&aM[hb(mx, my, mz)], hm);
             atomicAdd(&aM[hb(hx, hy, hz)], hm);
         }
         for (int n = 0; n < 3; ++n) {
-            double* a = aU + n * ANH;
+            A* a = aU + n * ANH;
             for (int m = 0; m < 3; ++m) {
                 const A b = grb[m][n];
                 if (!nonzero(b)) continue;
                 if (m == d) {
-                    const double w = (double)(b * ih[m]);
+                    const A w = b * ih[m];
                     atomicAdd(&a[hb(hx, hy, hz)], w);
                     atomicAdd(&a[hb(mx, my, mz)], -w);
                 } else {
                     const int f0 = (m == 0), f1 = (m == 1), f2 = (m == 2);
-                    const double w = (double)(A(0.25) * b * ih[m]);
+                    const A w = A(0.25) * b * ih[m];
                     atomicAdd(&a[hb(hx + f0, hy + f1, hz + f2)], w);
                     atomicAdd(&a[hb(mx + f0, my + f1, mz + f2)], w);
                     atomicAdd(&a[hb(hx - f0, hy - f1, hz - f2)], -w);
@@ -952,9 +955,9 @@ __global__ void __launch_bounds__(ATX* ATY* ATZ) k_adj_tau_tile(Grid g, const do
         const int hx = h % AHX, hy = (h / AHX) % AHY, hz = h / (AHX * AHY);
         const int gi = ((i0 + hx - 1) % g.nx + g.nx) % g.nx, gj = ((j0 + hy - 1) % g.ny + g.ny) % g.ny;
         const int gk = k0 + hz - 1;
-        for (int n = 0; n < 3; ++n) Vdb(g, ub, wgb, n, gi, gj, gk, aU[n * ANH + h]);
-        if (mub && (dbits(aM[h]) & kMag)) {
-            if (g.zper || (gk >= 0 && gk < g.nz)) atomicAdd(&mub[cidx(g, gi, gj, g.zper ? (gk % g.nz + g.nz) % g.nz : gk)], aM[h]);
+        for (int n = 0; n < 3; ++n) Vdb(g, ub, wgb, n, gi, gj, gk, (double)aU[n * ANH + h]);
+        if (mub && nonzero(aM[h])) {
+            if (g.zper || (gk >= 0 && gk < g.nz)) atomicAdd(&mub[cidx(g, gi, gj, g.zper ? (gk % g.nz + g.nz) % g.nz : gk)], (double)aM[h]);
         }
     }
 }
@@ -1009,6 +1012,126 @@ __global__ void k_adj_smag(Grid g, const double* vel, const double* mub, double 
         Qb(g, ub, n, i, j, k + 1, (double)(a * iz * gzb[n]));
         Qb(g, ub, n, i, j, k, (double)(b * iz * gzb[n]));
         Qb(g, ub, n, i, j, k - 1, (double)(c * iz * gzb[n]));
+    }
+}
+
+// Gather form of k_adj_smag (nz >= 4 or a periodic z): the first pass writes
+// each cell's gradient adjoints, scaled by their stencil factors, W = (hx gxb,
+// hy gyb, iz gzb) (zeros where the cell has none); the second lets every cell
+// collect what the stencils of its neighbours give it:
+//   ub += W_x(i-1) - W_x(i+1) + W_y(j-1) - W_y(j+1)
+//       + a(k-1) W_z(k-1) + b(k) W_z(k) + c(k+1) W_z(k+1)
+// (a, b, c the z stencil of each layer, one-sided at walls), and, at a wall,
+// the ghost term of the wall layer's one-sided stencil through the ghost's
+// extrapolation (15 q0 - 10 q1 + 3 q2) / 8 onto the three layers next to it
+// (the normal component's ghost is 0).
+template <typename A>
+__device__ inline void smag_zcoef(const Grid& g, int k, A& a, A& b, A& c) {
+    a = A(0.5);
+    b = A(0);
+    c = A(-0.5);
+    if (!g.zper && k == 0) {
+        a = A(1.0 / 3.0);
+        b = A(1);
+        c = A(-4.0 / 3.0);
+    }
+    if (!g.zper && k == g.nz - 1) {
+        a = A(4.0 / 3.0);
+        b = A(-1);
+        c = A(-1.0 / 3.0);
+    }
+}
+
+template <typename A>
+__global__ void k_adj_smag_w(Grid g, const double* vel, const double* mub, double rho, double fac, A* W) {
+    int i, j, k;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (!face_at(g, 0, t, i, j, k)) return;
+    const double mb = mub[t];
+    A gxb[3] = {A(0), A(0), A(0)}, gyb[3] = {A(0), A(0), A(0)}, gzb[3] = {A(0), A(0), A(0)};
+    const A hx = A(0.5 * g.idx), hy = A(0.5 * g.idy), iz = (A)g.idz;
+    if (dbits(mb) & kMag) {
+        A a, b, c;
+        smag_zcoef(g, k, a, b, c);
+        const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+        const long long xm = t + (i == 0 ? g.nx - 1 : -1), xp = t + (i + 1 == g.nx ? 1 - g.nx : 1);
+        const long long ym = t + (j == 0 ? (long long)(g.ny - 1) * sy : -sy), yp = t + (j + 1 == g.ny ? -(long long)(g.ny - 1) * sy : sy);
+        const long long zm = t + (k == 0 ? (long long)(g.nz - 1) * sz : -sz), zp = t + (k + 1 == g.nz ? -(long long)(g.nz - 1) * sz : sz);
+        const bool glo = !g.zper && k == 0, ghi = !g.zper && k + 1 == g.nz;  // the z neighbour is a wall ghost
+        A gx[3], gy[3], gz[3];
+        for (int n = 0; n < 3; ++n) {
+            const double* v = vel + n * g.N;
+            gx[n] = hx * ((A)v[xp] - (A)v[xm]);
+            gy[n] = hy * ((A)v[yp] - (A)v[ym]);
+            // fill-patch ghost (VelFPT): the normal component 0, the others
+            // (15 q0 - 10 q1 + 3 q2) / 8 from the three cells next to the wall
+            A qm, qp;
+            if (glo) qm = n == 2 ? A(0) : A(0.125) * (A(15) * (A)v[t] - A(10) * (A)v[t + sz] + A(3) * (A)v[t + 2 * sz]);
+            else qm = (A)v[zm];
+            if (ghi) qp = n == 2 ? A(0) : A(0.125) * (A(15) * (A)v[t] - A(10) * (A)v[t - sz] + A(3) * (A)v[t - 2 * sz]);
+            else qp = (A)v[zp];
+            gz[n] = (a * qp + b * (A)v[t] + c * qm) * iz;
+        }
+        const A S = sqrt(A(2) * gx[0] * gx[0] + A(2) * gy[1] * gy[1] + A(2) * gz[2] * gz[2] + (gy[0] + gx[1]) * (gy[0] + gx[1]) +
+                         (gz[1] + gy[2]) * (gz[1] + gy[2]) + (gx[2] + gz[0]) * (gx[2] + gz[0]));
+        if (S > A(0)) {
+            const A q = (A)(rho * fac * mb) / S;
+            gxb[0] = A(2) * q * gx[0];
+            gyb[1] = A(2) * q * gy[1];
+            gzb[2] = A(2) * q * gz[2];
+            const A t1 = q * (gy[0] + gx[1]), t2 = q * (gz[1] + gy[2]), t3 = q * (gx[2] + gz[0]);
+            gyb[0] += t1;
+            gxb[1] += t1;
+            gzb[1] += t2;
+            gyb[2] += t2;
+            gxb[2] += t3;
+            gzb[0] += t3;
+        }
+    }
+    for (int n = 0; n < 3; ++n) {
+        W[n * g.N + t] = hx * gxb[n];
+        W[(3 + n) * g.N + t] = hy * gyb[n];
+        W[(6 + n) * g.N + t] = iz * gzb[n];
+    }
+}
+
+template <typename A>
+__global__ void k_adj_smag_gather(Grid g, const A* W, double* ub) {
+    int i, j, k;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (!face_at(g, 0, t, i, j, k)) return;
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    const long long xm = t + (i == 0 ? g.nx - 1 : -1), xp = t + (i + 1 == g.nx ? 1 - g.nx : 1);
+    const long long ym = t + (j == 0 ? (long long)(g.ny - 1) * sy : -sy), yp = t + (j + 1 == g.ny ? -(long long)(g.ny - 1) * sy : sy);
+    const bool hasm = g.zper || k > 0, hasp = g.zper || k + 1 < g.nz;
+    const long long zm = t + (k == 0 ? (long long)(g.nz - 1) * sz : -sz), zp = t + (k + 1 == g.nz ? -(long long)(g.nz - 1) * sz : sz);
+    A a, b, c, am, bm, cm, ap, bp, cp;
+    smag_zcoef(g, k, a, b, c);
+    smag_zcoef(g, k == 0 ? g.nz - 1 : k - 1, am, bm, cm);
+    smag_zcoef(g, k + 1 == g.nz ? 0 : k + 1, ap, bp, cp);
+    const bool walls = !g.zper;
+    const A gw[3] = {A(1.875), A(-1.25), A(0.375)};
+    for (int n = 0; n < 3; ++n) {
+        const A* Wx = W + n * g.N;
+        const A* Wy = W + (3 + n) * g.N;
+        const A* Wz = W + (6 + n) * g.N;
+        A acc = (Wx[xm] - Wx[xp]) + (Wy[ym] - Wy[yp]) + b * Wz[t];
+        if (hasm) acc += am * Wz[zm];
+        if (hasp) acc += cp * Wz[zp];
+        if (walls && n != 2) {
+            const long long col = t - (long long)k * sz;
+            if (k <= 2) {  // the bottom wall layer's ghost (its c term)
+                A a0, b0, c0;
+                smag_zcoef(g, 0, a0, b0, c0);
+                acc += gw[k] * c0 * Wz[col];
+            }
+            if (k >= g.nz - 3) {  // the top wall layer's ghost (its a term)
+                A a1, b1, c1;
+                smag_zcoef(g, g.nz - 1, a1, b1, c1);
+                acc += gw[g.nz - 1 - k] * a1 * Wz[col + (long long)(g.nz - 1) * sz];
+            }
+        }
+        if (nonzero(acc)) ub[n * g.N + t] += (double)acc;
     }
 }
 
@@ -1337,9 +1460,19 @@ void launch_adj_tau(Ctx& c, const Grid& g, const double* vel, const double* muef
                        ub, mub, wgb);
     }
 }
-void launch_adj_smag(Ctx& c, const Grid& g, const double* vel, const double* mub, const Scalars& s, double* ub, int fp32) {
-    if (fp32) KS_LAUNCH(c, k_adj_smag<float>, nblocks(g.N, BS), BS, B8 * 7.0 * g.N, g, vel, mub, s.rho, s.smag_fac, ub);
-    else KS_LAUNCH(c, k_adj_smag<double>, nblocks(g.N, BS), BS, B8 * 7.0 * g.N, g, vel, mub, s.rho, s.smag_fac, ub);
+template <typename A>
+static void adj_smag_t(Ctx& c, const Grid& g, const double* vel, const double* mub, const Scalars& s, double* ub, double* scratch) {
+    if (!scratch || (!g.zper && g.nz < 4)) {
+        KS_LAUNCH(c, k_adj_smag<A>, nblocks(g.N, BS), BS, B8 * 7.0 * g.N, g, vel, mub, s.rho, s.smag_fac, ub);
+        return;
+    }
+    A* W = reinterpret_cast<A*>(scratch);
+    KS_LAUNCH(c, k_adj_smag_w<A>, nblocks(g.N, BS), BS, B8 * 4.0 * g.N + sizeof(A) * 9.0 * g.N, g, vel, mub, s.rho, s.smag_fac, W);
+    KS_LAUNCH(c, k_adj_smag_gather<A>, nblocks(g.N, BS), BS, B8 * 6.0 * g.N + sizeof(A) * 9.0 * g.N, g, (const A*)W, ub);
+}
+void launch_adj_smag(Ctx& c, const Grid& g, const double* vel, const double* mub, const Scalars& s, double* ub, double* scratch, int fp32) {
+    if (fp32) adj_smag_t<float>(c, g, vel, mub, s, ub, scratch);
+    else adj_smag_t<double>(c, g, vel, mub, s, ub, scratch);
 }
 void launch_adj_wall_local(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wgb, double ut2, double um0, double um1,
                            double vm, double rho, double* ub, double* mub, double* parts, int* np) {

@@ -80,7 +80,7 @@ void Sim::adj_alloc() {
     for (auto* b : {&S->w, &S->t1, &S->t2, &S->srcb, &S->doldb, &S->su, &S->sgp}) b->alloc(N3);
     S->sp.alloc(p_.n);
     S->mub.alloc(N);
-    S->cbuf.alloc(6 * N);
+    S->cbuf.alloc(9 * N);  // scratch of the gather-form reverse passes
     S->wgb.alloc(2 * (size_t)g_.nx * g_.ny);
     // post-MAC intermediates of the recompute: lo, hi, tedge, flux per direction and tr
     size_t total2 = 0;
@@ -355,7 +355,7 @@ void Sim::adjoint_step_impl(bool seed) {
         launch_adj_wall_global(ctx_, g_, vel_old_.p, b[0] / M, b[1] / M, vmb / M, ub);
     }
     // ---- Smagorinsky: mu_eff(u)
-    if (S_.smag) launch_adj_smag(ctx_, g_, vel_old_.p, S.mub.p, S_, ub, fp32);
+    if (S_.smag) launch_adj_smag(ctx_, g_, vel_old_.p, S.mub.p, S_, ub, S.cbuf.p, fp32);
     // ---- back to x^n
     launch_copy(ctx_, vel_.p, S.su.p, N3);
     launch_copy(ctx_, gp_.p, S.sgp.p, N3);

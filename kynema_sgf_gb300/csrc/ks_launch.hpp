@@ -316,7 +316,8 @@ void launch_adj_div(Ctx& c, const Grid& g, const double* convb, const AdjBufs& A
 // velocity (ub), cell viscosity (mub, may be null) and wall-gradient (wgb, may be null) adjoints
 void launch_adj_tau(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wg, const double* divtau_b, double s, double* ub,
                     double* mub, double* wgb, int fp32 = 0);
-void launch_adj_smag(Ctx& c, const Grid& g, const double* vel, const double* mub, const Scalars& s, double* ub, int fp32 = 0);
+// scratch: 9N doubles for the gather form (null: the scatter form)
+void launch_adj_smag(Ctx& c, const Grid& g, const double* vel, const double* mub, const Scalars& s, double* ub, double* scratch, int fp32 = 0);
 void launch_adj_wall_local(Ctx& c, const Grid& g, const double* vel, const double* mueff, const double* wgb, double ut2, double um0, double um1,
                            double vm, double rho, double* ub, double* mub, double* parts, int* np);
 void launch_adj_wall_global(Ctx& c, const Grid& g, const double* vel, double bu, double bv, double bm, double* ub);

@@ -204,7 +204,7 @@ struct AdjState {
     DevBuf<double> ub, gpb;         // adjoints of (velocity, gp) at the current time level
     DevBuf<double> w, t1, t2, srcb, doldb, forcesb;  // 3N scratch
     DevBuf<double> mub, wgb;        // adjoints of mu_eff (N) and of the wall-model gradient (2 nx ny)
-    DevBuf<double> cbuf;            // per-cell correction adjoints of the post-MAC reverse (6N)
+    DevBuf<double> cbuf;            // 9N scratch of the gather-form reverse passes
     DevBuf<double> umacb[3];        // adjoint of the MAC velocities
     DevBuf<double> gbuf2;           // post-MAC intermediates of the recompute (the pre-MAC ones stay in gb_)
     GodunovBufs gb2{};
