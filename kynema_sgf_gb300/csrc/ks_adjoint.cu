@@ -423,6 +423,112 @@ __global__ void k_adj_faces(Grid g, int d, const double* u, KI<TI> E, double s, 
     }
 }
 
+// ---- gather form of k_adj_faces.  A cell's value and the edges of its two
+// d-faces are read by exactly two traces: its high-side trace at the face
+// above (adjoint lb of that face) and its low-side trace at the face below
+// (hb).  The per-cell pass re-forms the state adjoints of its two faces
+// (LOb / HIb with the Riemann / upwind reverse and the wall rule, as
+// k_adj_faces), reverses the two traces, owns the cell's velocity adjoint
+// (before the MAC projection also that of its advective component), and
+// keeps the edge adjoints of its lower and upper face (G[0..2], G[3..5]) and,
+// after the MAC projection, the MAC-velocity adjoints (G[6], G[7]); the
+// per-face pass gathers them.  Needs at least 2 cells along d.
+template <int MODE, typename TI>
+__device__ inline void face_state_rev(const Grid& g, int d, long long f, int kf, const KI<TI>& LO, const KI<TI>& HI, const TI* ad, const K3& LOb,
+                                      const K3& HIb, const double* adb, const K3& TEb, const double* umac_d, TI lb[3], TI hb[3]) {
+    using A = TI;
+    for (int n = 0; n < 3; ++n) {
+        lb[n] = (A)LOb.p[n][f];
+        hb[n] = (A)HIb.p[n][f];
+    }
+    if (MODE == 0) {
+        rev_riemann(LO.p[d][f], HI.p[d][f], (A)adb[f], lb[d], hb[d]);
+        const A a = ad[f];
+        for (int n = 0; n < 3; ++n)
+            if (n != d) rev_upwind(a, (A)TEb.p[n][f], lb[n], hb[n]);
+    } else {
+        const A umf = (A)umac_d[f];
+        for (int n = 0; n < 3; ++n) rev_upwind(umf, (A)TEb.p[n][f], lb[n], hb[n]);
+    }
+    if (d == 2)
+        for (int n = 0; n < 3; ++n) zbc_rev(g, kf, n, lb[n], hb[n]);
+}
+
+template <int MODE, typename TI>
+__global__ void __launch_bounds__(256, 2) k_adj_faces_cells(Grid g, int d, const double* u, KI<TI> E, double s, double rho, const double* umac_d,
+                                                            KI<TI> LO, KI<TI> HI, const TI* ad, K3 LOb, K3 HIb, const double* adb, K3 TEb,
+                                                            double* ub, TI* G) {
+    using A = TI;
+    int i, j, k;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (!face_at(g, 0, t, i, j, k)) return;  // the x-face domain is the cell domain
+    const int di = (d == 0), dj = (d == 1), dk = (d == 2);
+    const long long flo = fidx(g, d, i, j, k), fhi = fidx(g, d, i + di, j + dj, k + dk);
+    A lbH[3], hbH[3], lbL[3], hbL[3];
+    face_state_rev<MODE, TI>(g, d, fhi, k + dk, LO, HI, ad, LOb, HIb, adb, TEb, umac_d, lbH, hbH);
+    face_state_rev<MODE, TI>(g, d, flo, k, LO, HI, ad, LOb, HIb, adb, TEb, umac_d, lbL, hbL);
+    const A scale = (MODE == 1) ? (A)rho : A(1), sT = (A)s;
+    A uhi, ulo;  // the trace speeds: the cell's own advective component, or the MAC velocity of each face
+    if (MODE == 0) uhi = ulo = Q<A>(g, u, d, i, j, k);
+    else {
+        uhi = (A)umac_d[fhi];
+        ulo = (A)umac_d[flo];
+    }
+    A guh = A(0), gul = A(0);
+    for (int n = 0; n < 3; ++n) {
+        A gsm = A(0), gs0 = A(0), gsp = A(0);
+        const A s0 = Q<A>(g, u, n, i, j, k);
+        const A tl = lbH[n] * scale;  // high-side trace (at the face above)
+        if (nonzero(tl)) {
+            if (above_small(uhi)) {
+                const A bsig = rev_trace(true, E.p[n][flo], s0, E.p[n][fhi], absv(uhi) * sT, tl, gsm, gs0, gsp);
+                guh += bsig * sT * (ge0(uhi) ? A(1) : A(-1));
+            } else {
+                gs0 += tl;
+            }
+        }
+        const A th = hbL[n] * scale;  // low-side trace (at the face below)
+        if (nonzero(th)) {
+            if (below_msmall(ulo)) {
+                const A bsig = rev_trace(false, E.p[n][flo], s0, E.p[n][fhi], absv(ulo) * sT, th, gsm, gs0, gsp);
+                gul += bsig * sT * (ge0(ulo) ? A(1) : A(-1));
+            } else {
+                gs0 += th;
+            }
+        }
+        G[n * g.N + t] = gsm;
+        G[(3 + n) * g.N + t] = gsp;
+        if (nonzero(gs0)) ub[n * g.N + t] += (double)gs0;
+    }
+    if (MODE == 0) {
+        const A gu = guh + gul;
+        if (nonzero(gu)) ub[d * g.N + t] += (double)gu;
+    } else {
+        G[6 * g.N + t] = gul;
+        G[7 * g.N + t] = guh;
+    }
+}
+
+template <int MODE, typename TI>
+__global__ void k_adj_faces_gather(Grid g, int d, const TI* G, A3 Eb, double* umacb_d) {
+    using A = TI;
+    int i, j, k;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (!face_at(g, d, t, i, j, k)) return;
+    const bool walls = d == 2 && !g.zper;
+    const bool hasm = !(walls && k == 0), hasp = !(walls && k == g.nz);
+    const long long cp = hasp ? cidx(g, i, j, k) : 0;
+    const long long cm = hasm ? cidx(g, wrapn(i - (d == 0), g.nx), wrapn(j - (d == 1), g.ny), g.zper ? wrapn(k - (d == 2), g.nz) : k - (d == 2)) : 0;
+    for (int n = 0; n < 3; ++n) {  // the upper edge terms of the cell below, the lower ones of the cell above
+        const A v = (hasm ? G[(3 + n) * g.N + cm] : A(0)) + (hasp ? G[n * g.N + cp] : A(0));
+        if (nonzero(v)) Eb.p[n][t] += (double)v;
+    }
+    if (MODE == 1) {
+        const A w = (hasm ? G[7 * g.N + cm] : A(0)) + (hasp ? G[6 * g.N + cp] : A(0));
+        if (nonzero(w)) umacb_d[t] += (double)w;
+    }
+}
+
 // ---- reverse of k_pm_trans (a, b, n)
 template <typename TI>
 __global__ void k_adj_pm_trans(Grid g, int a, int b, int n, double cb64, const TI* ad_a, const TI* ad_b, const TI* edge_b, const double* outb,
@@ -1337,7 +1443,7 @@ void launch_adj_edges(Ctx& c, const Grid& g, int d, const double* u, double* con
 
 template <typename TI>
 static void adj_faces_t(Ctx& c, const Grid& g, int d, int mode, const double* u, const GodunovBufs& B, const AdjBufs& A, double dt, double rho,
-                        const double* umac_d) {
+                        const double* umac_d, double* scratch) {
     KI<TI> E{{ti<TI>(B.edge[d][0]), ti<TI>(B.edge[d][1]), ti<TI>(B.edge[d][2])}};
     KI<TI> LO{{ti<TI>(B.lo[d][0]), ti<TI>(B.lo[d][1]), ti<TI>(B.lo[d][2])}}, HI{{ti<TI>(B.hi[d][0]), ti<TI>(B.hi[d][1]), ti<TI>(B.hi[d][2])}};
     K3 LOb{{A.lo[d][0], A.lo[d][1], A.lo[d][2]}}, HIb{{A.hi[d][0], A.hi[d][1], A.hi[d][2]}};
@@ -1346,6 +1452,22 @@ static void adj_faces_t(Ctx& c, const Grid& g, int d, int mode, const double* u,
     const double s = dt * ihd(g, d);
     const long long nf = nfaces(g, d);
     const double bytes = B8 * (6.0 * g.N + 13.0 * nf) + sizeof(TI) * 9.0 * nf;
+    const int nd = d == 0 ? g.nx : (d == 1 ? g.ny : g.nz);
+    if (scratch && nd >= 2) {  // gather form
+        TI* G = reinterpret_cast<TI*>(scratch);
+        const double cb = B8 * (6.0 * g.N + 2.0 * 12.0 * nf) + sizeof(TI) * (2.0 * 9.0 * nf + 8.0 * g.N);
+        const double fb = B8 * 2.0 * 4.0 * nf + sizeof(TI) * 8.0 * g.N;
+        if (mode == 0) {
+            KS_LAUNCH(c, (k_adj_faces_cells<0, TI>), nblocks(g.N, BS), BS, cb, g, d, u, E, s, rho, nullptr, LO, HI, ti<TI>(B.ad[d]), LOb, HIb,
+                      A.ad[d], TEb, A.u, G);
+            KS_LAUNCH(c, (k_adj_faces_gather<0, TI>), nblocks(nf, BS), BS, fb, g, d, (const TI*)G, Eb, nullptr);
+        } else {
+            KS_LAUNCH(c, (k_adj_faces_cells<1, TI>), nblocks(g.N, BS), BS, cb, g, d, u, E, s, rho, umac_d, LO, HI, (const TI*)nullptr, LOb, HIb,
+                      nullptr, TEb, A.u, G);
+            KS_LAUNCH(c, (k_adj_faces_gather<1, TI>), nblocks(nf, BS), BS, fb, g, d, (const TI*)G, Eb, A.umac[d]);
+        }
+        return;
+    }
     if (mode == 0)
         KS_LAUNCH(c, (k_adj_faces<0, TI>), nblocks(nf, BS), BS, bytes, g, d, u, E, s, rho, nullptr, LO, HI, ti<TI>(B.ad[d]), LOb, HIb, A.ad[d], TEb,
                   Eb, A.u, nullptr);
@@ -1354,9 +1476,9 @@ static void adj_faces_t(Ctx& c, const Grid& g, int d, int mode, const double* u,
                   TEb, Eb, A.u, A.umac[d]);
 }
 void launch_adj_faces(Ctx& c, const Grid& g, int d, int mode, const double* u, const GodunovBufs& B, const AdjBufs& A, double dt, double rho,
-                      const double* umac_d, int fp32) {
-    if (fp32) adj_faces_t<float>(c, g, d, mode, u, B, A, dt, rho, umac_d);
-    else adj_faces_t<double>(c, g, d, mode, u, B, A, dt, rho, umac_d);
+                      const double* umac_d, double* scratch, int fp32) {
+    if (fp32) adj_faces_t<float>(c, g, d, mode, u, B, A, dt, rho, umac_d, scratch);
+    else adj_faces_t<double>(c, g, d, mode, u, B, A, dt, rho, umac_d, scratch);
 }
 
 template <typename TI>

@@ -296,7 +296,7 @@ void Sim::adjoint_step_impl(bool seed) {
     // stage 3 first: it accumulates the adjoints of the stage-2 outputs
     for (int d = 0; d < 3; ++d) launch_adj_adv_flux(ctx_, g_, d, vel_old_.p, forces_.p, rho_, dt, mac, S.gb2, A, S.cbuf.p, fp32);
     for (int a = 0; a < 3; ++a) launch_adj_adv_trans(ctx_, g_, a, vel_old_.p, rho_, dt, mac, S.gb2, A, S.cbuf.p, fp32);
-    for (int a = 0; a < 3; ++a) launch_adj_faces(ctx_, g_, a, 1, vel_old_.p, S.gb2, A, dt, rho_, umac_[a].p, fp32);
+    for (int a = 0; a < 3; ++a) launch_adj_faces(ctx_, g_, a, 1, vel_old_.p, S.gb2, A, dt, rho_, umac_[a].p, S.cbuf.p, fp32);
     // ---- MAC projection (symmetric on the faces it changes): the pre-MAC
     // output on wall faces is 0 whatever the input, so their adjoint is dropped
     if (!g_.zper) {
@@ -332,7 +332,7 @@ void Sim::adjoint_step_impl(bool seed) {
     for (int d = 0; d < 3; ++d) launch_adj_pm_final(ctx_, g_, d, dt, gb_, forces_.p, A, fp32);
     const int tpl[6][3] = {{1, 2, 0}, {2, 1, 0}, {0, 2, 1}, {2, 0, 1}, {0, 1, 2}, {1, 0, 2}};
     for (auto& t : tpl) launch_adj_pm_trans(ctx_, g_, t[0], t[1], t[2], dt, gb_, A, fp32);
-    for (int d = 0; d < 3; ++d) launch_adj_faces(ctx_, g_, d, 0, vel_old_.p, gb_, A, dt, 1.0, nullptr, fp32);
+    for (int d = 0; d < 3; ++d) launch_adj_faces(ctx_, g_, d, 0, vel_old_.p, gb_, A, dt, 1.0, nullptr, S.cbuf.p, fp32);
     // ---- unlimited edges (shared by both passes)
     for (int d = 0; d < 3; ++d) launch_adj_edges(ctx_, g_, d, vel_old_.p, A.edge[d], ub, fp32);
     // ---- forces = (src + dold)/rho

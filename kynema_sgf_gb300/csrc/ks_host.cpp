@@ -1011,6 +1011,7 @@ void Sim::mac_project() {
     const double r0 = reduce(np, 1, 1, nullptr);
     mac_r0_ = r0;
     const double target = std::max(mac_.atol, mac_.rtol * std::max(bnorm, r0));
+    mac_tgt_ = target;
     int it = 0;
     double rn = r0;
     while (rn > target && it < mac_.maxiter) {
@@ -1110,6 +1111,7 @@ void Sim::nd_solve(double sigma) {
         const double r0 = reduce(np, 1, 1, nullptr);
         nod_r0_ = r0;
         target = std::max(nod_.atol, nod_.rtol * std::max(nod_bnorm_, r0));
+        nod_tgt_ = target;
         rn = r0;
         while (rn > target && it < nod_.maxiter) {
             // The correction equation gets as many FP32 V-cycles (each
@@ -1149,6 +1151,7 @@ void Sim::nd_solve(double sigma) {
             if (it == 0) {
                 nod_r0_ = rn;
                 target = std::max(nod_.atol, nod_.rtol * std::max(nod_bnorm_, rn));
+                nod_tgt_ = target;
             }
             if (rn > 1e20 * nod_r0_) throw KsError(KS_ERR_NOT_CONVERGED, "nodal projection diverged (residual above 1e20 times the initial one)");
             if (rn <= target || it >= nod_.maxiter) break;
@@ -1672,6 +1675,8 @@ double Sim::scalar(const std::string& n) {
     if (n == "abl_forcing_x") return S_.ablf_force[0];
     if (n == "abl_forcing_y") return S_.ablf_force[1];
     if (n == "mac_res0") return mac_r0_;
+    if (n == "mac_target") return mac_tgt_;    // the last solve's stopping threshold
+    if (n == "nodal_target") return nod_tgt_;
     if (n == "mac_res") return mac_r_;
     if (n == "nodal_res0") return nod_r0_;
     if (n == "nodal_res") return nod_r_;

@@ -300,8 +300,9 @@ struct AdjBufs {
 // fp32: the forward intermediates in B are FP32 (mixed-precision Godunov passes);
 // the reverse arithmetic is FP64 either way
 void launch_adj_edges(Ctx& c, const Grid& g, int d, const double* u, double* const Eb[3], double* ub, int fp32);
+// scratch: 8N doubles for the gather form (null: the scatter form)
 void launch_adj_faces(Ctx& c, const Grid& g, int d, int mode, const double* u, const GodunovBufs& B, const AdjBufs& A, double dt, double rho,
-                      const double* umac_d, int fp32);
+                      const double* umac_d, double* scratch, int fp32);
 void launch_adj_pm_trans(Ctx& c, const Grid& g, int a, int b, int n, double dt, const GodunovBufs& B, const AdjBufs& A, int fp32);
 void launch_adj_pm_final(Ctx& c, const Grid& g, int d, double dt, const GodunovBufs& B, const double* forces, const AdjBufs& A, int fp32);
 // reverse of the post-MAC stages 2 (both transverse directions of the a-faces)

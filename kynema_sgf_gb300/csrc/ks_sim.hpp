@@ -282,6 +282,7 @@ class Sim {
     int mixed_ = 0;  // 1: FP32 advection and multigrid cycles with FP64 defect correction
     GodunovBufs* adv_bufs_ = nullptr;  // post-MAC pass scratch when not gb_ (reverse-step recompute keeps both passes)
     double mac_r0_ = 0, mac_r_ = 0, nod_r0_ = 0, nod_r_ = 0;
+    double mac_tgt_ = 0, nod_tgt_ = 0;  // stopping thresholds max(atol, rtol max(|rhs|, r0)) of the last solves
     std::string err_;
 
    private:

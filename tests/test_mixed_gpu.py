@@ -24,6 +24,17 @@ pytestmark = pytest.mark.gpu
 EPS = np.finfo(float).eps
 
 
+def assert_fp64_tolerance(sim):
+    """Both solves stopped by MLMG's rule at the FP64 tolerance: the final
+    max-norm FP64 residual is at most the solve's threshold max(atol,
+    rtol max(|rhs|, initial residual)) (mac_proj / nodal_proj rtol 1e-11 on
+    these decks; a warm-started solve measures against |rhs|, which can exceed
+    the initial residual)."""
+    for s in ("mac", "nodal"):
+        r, tgt = sim.scalar(s + "_res"), sim.scalar(s + "_target")
+        assert 0.0 < tgt and r <= tgt, (s, r, tgt)
+
+
 def rel(a, b):
     return np.abs(a - b).max() / np.abs(b).max()
 
@@ -38,8 +49,7 @@ def test_mixed_matches_fp64(cuda_dev):
     for _ in range(40):
         ref.step()
         mix.step()
-        assert mix.scalar("mac_res") <= max(1e2 * EPS, 1e5 * EPS * mix.scalar("mac_res0"))
-        assert mix.scalar("nodal_res") <= max(1e2 * EPS, 1e5 * EPS * mix.scalar("nodal_res0"))
+        assert_fp64_tolerance(mix)
         assert mix.scalar("mac_iters") <= ref.scalar("mac_iters") + 2
         assert mix.scalar("nodal_iters") <= ref.scalar("nodal_iters") + 2
         # post-projection divergence: the MAC projection is exact (its
@@ -71,8 +81,7 @@ def test_mixed_large_levels(cuda_dev):
     for _ in range(6):
         ref.step()
         mix.step()
-        assert mix.scalar("mac_res") <= max(1e2 * EPS, 1e5 * EPS * mix.scalar("mac_res0"))
-        assert mix.scalar("nodal_res") <= max(1e2 * EPS, 1e5 * EPS * mix.scalar("nodal_res0"))
+        assert_fp64_tolerance(mix)
         assert mix.scalar("mac_iters") <= ref.scalar("mac_iters") + 2
         assert mix.scalar("nodal_iters") <= ref.scalar("nodal_iters") + 2
         assert mix.scalar("mac_divu_rel") <= 1e-10
