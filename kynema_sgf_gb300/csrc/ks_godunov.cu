@@ -458,247 +458,49 @@ __global__ void __launch_bounds__(256) k_ppm_x(PpmArgs<T> A, T s, T rho, PpmOut<
     }
 }
 
-// ---- pre-MAC stage 2: a-face states of component n corrected along b
-template <typename T>
-__global__ void k_pm_trans(Grid g, int a, int b, int n, T cb, const T* lo_an, const T* hi_an, const T* ad_a, const T* ad_b, const T* edge_b,
-                           T* out) {
-    int i, j, k;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (!face_of(g, a, t, i, j, k)) return;
-    const long long f = fidx(g, a, i, j, k);
-    T l = lo_an[f], h = hi_an[f];
-    const bool wl = (a == 2 && !g.zper && k == 0), wh = (a == 2 && !g.zper && k == g.nz);
-    const int eb0 = (b == 0), eb1 = (b == 1), eb2 = (b == 2);
-    if (!wh) {
-        const long long f0 = fidx(g, b, i, j, k), f1 = fidx(g, b, i + eb0, j + eb1, k + eb2);
-        h -= cb * (ad_b[f1] + ad_b[f0]) * (edge_b[f1] - edge_b[f0]);
-    }
-    if (!wl) {
-        const int ci = i - (a == 0), cj = j - (a == 1), ck = k - (a == 2);
-        const long long f0 = fidx(g, b, ci, cj, ck), f1 = fidx(g, b, ci + eb0, cj + eb1, ck + eb2);
-        l -= cb * (ad_b[f1] + ad_b[f0]) * (edge_b[f1] - edge_b[f0]);
-    }
-    if (a == 2) zbc(g, k, n, l, h);
-    out[f] = upwind(ad_a[f], l, h);
-}
-
-// ---- pre-MAC stage 3: final normal velocity on d-faces
-template <typename T>
-__global__ void k_pm_final(Grid g, int d, const T* lo_dd, const T* hi_dd, const T* forces, T dt, T c1, T c2, C3<T> AD, const T* T1,
-                           const T* T2, double* mac) {
-    int i, j, k;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (!face_of(g, d, t, i, j, k)) return;
-    CellFOT<T, T> F{forces, g};
-    const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
-    const long long f = fidx(g, d, i, j, k);
-    const bool wl = (d == 2 && !g.zper && k == 0), wh = (d == 2 && !g.zper && k == g.nz);
-    auto side = [&](int ci, int cj, int ck, T base) {
-        const long long p1 = fidx(g, b1, ci + (b1 == 0), cj + (b1 == 1), ck + (b1 == 2)), m1 = fidx(g, b1, ci, cj, ck);
-        const long long p2 = fidx(g, b2, ci + (b2 == 0), cj + (b2 == 1), ck + (b2 == 2)), m2 = fidx(g, b2, ci, cj, ck);
-        T s = base;
-        s -= c1 * (AD.p[b1][p1] + AD.p[b1][m1]) * (T1[p1] - T1[m1]);
-        s -= c2 * (AD.p[b2][p2] + AD.p[b2][m2]) * (T2[p2] - T2[m2]);
-        s += T(0.5) * dt * F(d, ci, cj, ck);
-        return s;
-    };
-    T stl = T(0), sth = T(0);
-    if (!wl) stl = side(i - (d == 0), j - (d == 1), k - (d == 2), lo_dd[f]);
-    if (!wh) sth = side(i, j, k, hi_dd[f]);
-    if (d == 2) zbc(g, k, d, stl, sth);
-    mac[f] = (double)riemann(stl, sth);
-}
-
-// ---- post-MAC stage 2: the a-face states corrected along both transverse
-// directions b1 = a+1 and b2 = a+2 (conservative form, dt/3 corner factors).
-// Stage 2 by cells: the corrections of a face state along b1 and b2 depend only
-// on the cell the state is traced from,
-//   corr_b(c) = q(c) rho cb (v_b+ - v_b-) - cb (v_b+ E_b(+) - v_b- E_b(-))
-// over the b faces of c, so that each state is its stage-1 value plus the
-// corr of its cell; the kernels below form each cell's pair once.
-template <typename T, int NC>
-struct TransCell {
-    Grid g;
-    int a, b1, b2;
-    const T* vel;
-    T rho, cb1, cb2;
-    const T *vb1, *vb2;
-    C3<T> E1, E2;
-    __device__ inline void operator()(int i, int j, int k, T c1[NC], T c2[NC]) const {
-        const long long p1 = fidx(g, b1, i + (b1 == 0), j + (b1 == 1), k + (b1 == 2)), m1 = fidx(g, b1, i, j, k);
-        const long long p2 = fidx(g, b2, i + (b2 == 0), j + (b2 == 1), k + (b2 == 2)), m2 = fidx(g, b2, i, j, k);
-        const T v1p = (T)vb1[p1], v1m = (T)vb1[m1], v2p = (T)vb2[p2], v2m = (T)vb2[m2];
-        const T r1 = rho * cb1 * (v1p - v1m), r2 = rho * cb2 * (v2p - v2m);
-        const VelFPT<T, T> q{vel, g, T(1)};
-        for (int n = 0; n < NC; ++n) {
-            const T qc = q(n, i, j, k);
-            c1[n] = qc * r1 - cb1 * (v1p * E1.p[n][p1] - v1m * E1.p[n][m1]);
-            c2[n] = qc * r2 - cb2 * (v2p * E2.p[n][p2] - v2m * E2.p[n][m2]);
-        }
-    }
-};
-
-template <typename T, int NC>
-__device__ inline void trans_out(const Grid& g, int a, int k, long long f, T u, const C3<T>& LO, const C3<T>& HI, bool wl, bool wh,
-                                 const T* l1, const T* l2, const T* h1, const T* h2, P3<T>& out1, P3<T>& out2) {
-    const bool usmall = below_small_abs(u), upos = ge0(u);
-    auto pick = [&](T l, T h) { return usmall ? T(0.5) * (l + h) : (upos ? l : h); };
-    for (int n = 0; n < NC; ++n) {
-        const T l0 = LO.p[n][f], h0 = HI.p[n][f];
-        T l = wl ? l0 : l0 + l1[n], h = wh ? h0 : h0 + h1[n];
-        if (a == 2) zbc(g, k, n, l, h);
-        out1.p[n][f] = pick(l, h);
-        l = wl ? l0 : l0 + l2[n];
-        h = wh ? h0 : h0 + h2[n];
-        if (a == 2) zbc(g, k, n, l, h);
-        out2.p[n][f] = pick(l, h);
-    }
-}
-
-// x faces: lanes along a row, the low cell's corrections from the previous lane
-template <typename T, int NC = 3>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_adv_trans_x(TransCell<T, NC> C, const T* ua, C3<T> LO, C3<T> HI, P3<T> out1,
-                                                                             P3<T> out2) {
-    const Grid& g = C.g;
+// ---- stages 2 and 3 of both passes by cells.  In each stage a face state is
+// its stage-1 (or stage-2) value plus a correction that depends only on the
+// cell it is traced from (its value, forces, and the advective / MAC
+// velocities and states on its own transverse faces).  The low-side state of
+// face c + e_d and the high-side state of face c share it, so the kernels
+// below form each cell's corrections once: x faces take the low cell's from
+// the previous lane of the warp (lane 0 and the periodic wrap form their
+// own); y and z faces march a chunk of 16 faces along d and carry it.
+//
+// An op supplies T, K (values per cell), the grid g and face direction d,
+//   cell(i, j, k, c[K]): the cell's corrections,
+//   face(f, kf, wl, wh, cl[K], ch[K]): the face's output from the low and
+//     high cells' corrections (kf the face's z index, wl / wh a wall face
+//     without a cell below / above).
+template <typename Op>
+__global__ void __launch_bounds__(256, sizeof(typename Op::T) == 4 ? 3 : 2) k_cf_x(Op op) {
+    using T = typename Op::T;
+    constexpr int K = Op::K;
+    const Grid& g = op.g;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const bool live = t < g.N;
     int i = 0, j = 0, k = 0;
-    T h1[NC], h2[NC], l1[NC], l2[NC];
-    for (int n = 0; n < NC; ++n) h1[n] = h2[n] = T(0);
+    T ch[K], cl[K];
+    for (int n = 0; n < K; ++n) ch[n] = T(0);
     if (live) {
         const unsigned u = (unsigned)t, r = u / (unsigned)g.nx;
         i = (int)(u - r * (unsigned)g.nx);
         k = (int)(r / (unsigned)g.ny);
         j = (int)(r - (unsigned)k * (unsigned)g.ny);
-        C(i, j, k, h1, h2);
+        op.cell(i, j, k, ch);
     }
-    for (int n = 0; n < NC; ++n) {
-        l1[n] = __shfl_up_sync(0xffffffffu, h1[n], 1);
-        l2[n] = __shfl_up_sync(0xffffffffu, h2[n], 1);
-    }
+    for (int n = 0; n < K; ++n) cl[n] = __shfl_up_sync(0xffffffffu, ch[n], 1);
     if (!live) return;
-    if ((threadIdx.x & 31) == 0 || i == 0) C(i == 0 ? g.nx - 1 : i - 1, j, k, l1, l2);
-    trans_out<T, NC>(g, 0, k, t, (T)ua[t], LO, HI, false, false, l1, l2, h1, h2, out1, out2);
+    if ((threadIdx.x & 31) == 0 || i == 0) op.cell(i == 0 ? g.nx - 1 : i - 1, j, k, cl);
+    op.face(t, k, false, false, cl, ch);
 }
 
-// y and z faces: a thread per (i, other index) marches a chunk of faces along a
-template <typename T, int NC = 3>
-__global__ void __launch_bounds__(128) k_adv_trans_col(TransCell<T, NC> C, const T* ua, C3<T> LO, C3<T> HI, P3<T> out1, P3<T> out2, int chunk) {
-    const Grid& g = C.g;
-    const int a = C.a;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= g.nx) return;
-    const int nf = a == 1 ? g.ny : nzfaces(g);
-    const int no = a == 1 ? g.nz : g.ny;
-    const int o = (int)(blockIdx.y % (unsigned)no), chn = (int)(blockIdx.y / (unsigned)no);
-    const int m0 = chn * chunk, m1 = min(m0 + chunk, nf);
-    if (m0 >= m1) return;
-    const bool walls = a == 2 && !g.zper;
-    const int ncell = a == 1 ? g.ny : g.nz;
-    auto cellc = [&](int m, T c1[NC], T c2[NC]) {
-        m = m < 0 ? m + ncell : (m >= ncell ? m - ncell : m);
-        if (a == 1) C(i, m, o, c1, c2);
-        else C(i, o, m, c1, c2);
-    };
-    T l1[NC], l2[NC], h1[NC], h2[NC];
-    for (int n = 0; n < NC; ++n) l1[n] = l2[n] = h1[n] = h2[n] = T(0);
-    if (!(walls && m0 == 0)) cellc(m0 - 1, l1, l2);
-    for (int m = m0; m < m1; ++m) {
-        const bool wl = walls && m == 0, wh = walls && m == g.nz;
-        if (!wh) cellc(m, h1, h2);
-        const long long f = a == 1 ? fidx(g, 1, i, m, o) : fidx(g, 2, i, o, m);
-        trans_out<T, NC>(g, a, m, f, (T)ua[f], LO, HI, wl, wh, l1, l2, h1, h2, out1, out2);
-        for (int n = 0; n < NC; ++n) {
-            l1[n] = h1[n];
-            l2[n] = h2[n];
-        }
-    }
-}
-
-template <typename T, int NC>
-static void launch_adv_trans(Ctx& c, const Grid& g, int a, const T* vel, double rho, double dt, const T* ua, const T* vb1, const T* vb2,
-                             C3<T> LO, C3<T> HI, C3<T> E1, C3<T> E2, P3<T> O1, P3<T> O2, double bytes) {
-    const int b1 = (a + 1) % 3, b2 = (a + 2) % 3;
-    const TransCell<T, NC> C{g, a, b1, b2, vel, T(rho), T(dt / (3.0 * hd(g, b1))), T(dt / (3.0 * hd(g, b2))), vb1, vb2, E1, E2};
-    if (a == 0) {
-        KS_LAUNCH(c, (k_adv_trans_x<T, NC>), nblocks(g.N, 256), 256, bytes, C, ua, LO, HI, O1, O2);
-    } else {
-        constexpr int chunk = 16;
-        const int nf = a == 1 ? g.ny : nzfaces(g), no = a == 1 ? g.nz : g.ny;
-        const int bx = g.nx >= 128 ? 128 : 32 * ((g.nx + 31) / 32);
-        const dim3 grid((unsigned)((g.nx + bx - 1) / bx), (unsigned)(no * ((nf + chunk - 1) / chunk)));
-        KS_LAUNCH(c, (k_adv_trans_col<T, NC>), grid, bx, bytes, C, ua, LO, HI, O1, O2, chunk);
-    }
-}
-
-// ---- post-MAC stage 3: final states and fluxes on d-faces
-// The forces enter scaled by rho for the velocity (forces = (src + divtau) / rho)
-// and as they are for a scalar (NC = 1: forces = src + diff, AdvOp_Godunov.H:114-329).
-// Stage 3 by cells: the part of a face state that depends only on the cell
-// it is traced from,
-//   corr(c) = hdt forces(c) + (q(c) r(c) - c1 x1(c) - c2 x2(c)),
-//   r = rho (c1 (v1+ - v1-) + c2 (v2+ - v2-)),  x_b = T_b(+) v_b+ - T_b(-) v_b-
-// over the b1 / b2 faces of c, so that a face state is its stage-1 state plus
-// corr of its cell.  The low-side state of face c + e_d and the high-side state
-// of face c share it: the kernels below form each cell's corr once (half the
-// FP64 work of forming it per face side).
-template <typename T, int NC>
-struct FluxCell {
-    Grid g;
-    int d, b1, b2;
-    const T *vel, *forces;
-    T rho, hdt, c1, c2;
-    C3<T> U, T1, T2;
-    __device__ inline void operator()(int i, int j, int k, T corr[NC]) const {
-        const long long p1 = fidx(g, b1, i + (b1 == 0), j + (b1 == 1), k + (b1 == 2)), m1 = fidx(g, b1, i, j, k);
-        const long long p2 = fidx(g, b2, i + (b2 == 0), j + (b2 == 1), k + (b2 == 2)), m2 = fidx(g, b2, i, j, k);
-        const T v1p = (T)U.p[b1][p1], v1m = (T)U.p[b1][m1], v2p = (T)U.p[b2][p2], v2m = (T)U.p[b2][m2];
-        const T r = rho * (c1 * (v1p - v1m) + c2 * (v2p - v2m));
-        const VelFPT<T, T> q{vel, g, T(1)};
-        const CellFOT<T, T> Fo{forces, g};
-        for (int n = 0; n < NC; ++n) {
-            const T x1 = T1.p[n][p1] * v1p - T1.p[n][m1] * v1m, x2 = T2.p[n][p2] * v2p - T2.p[n][m2] * v2m;
-            corr[n] = hdt * Fo(n, i, j, k) + ((q(n, i, j, k) * r - c1 * x1) - c2 * x2);
-        }
-    }
-};
-
-// x faces: a thread per face, lanes of a warp along a row of faces; the
-// low-side cell correction of face i is the high-side one of face i - 1, taken
-// from the previous lane (lane 0 and the periodic wrap form their own).
-template <typename T, int NC = 3>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_adv_flux_x(FluxCell<T, NC> C, C3<T> LO, C3<T> HI, P3<T> Fl) {
-    const Grid& g = C.g;
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    const bool live = t < g.N;
-    int i = 0, j = 0, k = 0;
-    T ch[NC], cl[NC];
-    for (int n = 0; n < NC; ++n) ch[n] = T(0);
-    if (live) {
-        const unsigned u = (unsigned)t, r = u / (unsigned)g.nx;
-        i = (int)(u - r * (unsigned)g.nx);
-        k = (int)(r / (unsigned)g.ny);
-        j = (int)(r - (unsigned)k * (unsigned)g.ny);
-        C(i, j, k, ch);
-    }
-    for (int n = 0; n < NC; ++n) cl[n] = __shfl_up_sync(0xffffffffu, ch[n], 1);
-    if (!live) return;
-    if ((threadIdx.x & 31) == 0 || i == 0) C(i == 0 ? g.nx - 1 : i - 1, j, k, cl);
-    const T um = (T)C.U.p[0][t];
-    const bool usmall = below_small_abs(um), upos = ge0(um);
-    for (int n = 0; n < NC; ++n) {
-        const T stl = LO.p[n][t] + cl[n], sth = HI.p[n][t] + ch[n];
-        const T st = usmall ? T(0.5) * (stl + sth) : (upos ? stl : sth);
-        Fl.p[n][t] = um * st;
-    }
-}
-
-// y and z faces: a thread per (i, other index) marches a chunk of faces along d
-// and carries the cell correction from one face to the next.
-template <typename T, int NC = 3>
-__global__ void __launch_bounds__(128) k_adv_flux_col(FluxCell<T, NC> C, C3<T> LO, C3<T> HI, P3<T> Fl, int chunk) {
-    const Grid& g = C.g;
-    const int d = C.d;
+template <typename Op>
+__global__ void __launch_bounds__(128) k_cf_col(Op op, int chunk) {
+    using T = typename Op::T;
+    constexpr int K = Op::K;
+    const Grid& g = op.g;
+    const int d = op.d;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.nx) return;
     const int nf = d == 1 ? g.ny : nzfaces(g);
@@ -708,48 +510,177 @@ __global__ void __launch_bounds__(128) k_adv_flux_col(FluxCell<T, NC> C, C3<T> L
     if (m0 >= m1) return;
     const bool walls = d == 2 && !g.zper;
     const int ncell = d == 1 ? g.ny : g.nz;
-    // cell m along d (periodic wrap), as (j, k)
-    auto cellc = [&](int m, T corr[NC]) {
+    auto cellc = [&](int m, T c[K]) {  // cell m along d (periodic wrap)
         m = m < 0 ? m + ncell : (m >= ncell ? m - ncell : m);
-        if (d == 1) C(i, m, o, corr);
-        else C(i, o, m, corr);
+        if (d == 1) op.cell(i, m, o, c);
+        else op.cell(i, o, m, c);
     };
-    T cl[NC], ch[NC];
-    for (int n = 0; n < NC; ++n) cl[n] = ch[n] = T(0);
+    T cl[K], ch[K];
+    for (int n = 0; n < K; ++n) cl[n] = ch[n] = T(0);
     if (!(walls && m0 == 0)) cellc(m0 - 1, cl);
     for (int m = m0; m < m1; ++m) {
         const bool wl = walls && m == 0, wh = walls && m == g.nz;
         if (!wh) cellc(m, ch);
         const long long f = d == 1 ? fidx(g, 1, i, m, o) : fidx(g, 2, i, o, m);
-        const T um = (T)C.U.p[d][f];
+        op.face(f, m, wl, wh, cl, ch);
+        for (int n = 0; n < K; ++n) cl[n] = ch[n];
+    }
+}
+
+template <typename Op>
+static void launch_cf(Ctx& c, const char* name_x, const char* name_col, const Op& op, double bytes) {
+    const Grid& g = op.g;
+    if (op.d == 0) {
+        KS_LAUNCH_NAMED(c, name_x, k_cf_x<Op>, nblocks(g.N, 256), 256, bytes, op);
+    } else {
+        constexpr int chunk = 16;
+        const int nf = op.d == 1 ? g.ny : nzfaces(g), no = op.d == 1 ? g.nz : g.ny;
+        const int bx = g.nx >= 128 ? 128 : 32 * ((g.nx + 31) / 32);
+        const dim3 grid((unsigned)((g.nx + bx - 1) / bx), (unsigned)(no * ((nf + chunk - 1) / chunk)));
+        KS_LAUNCH_NAMED(c, name_col, k_cf_col<Op>, grid, bx, bytes, op, chunk);
+    }
+}
+
+// pre-MAC stage 2: the a-face states of component n corrected along b,
+// corr(c) = cb (ad_b+ + ad_b-) (E_b+ - E_b-) over the b faces of c (velocity
+// form, dt/6 corner factor); out = upwind(ad_a; lo - corr(c - e_a), hi - corr(c))
+template <typename T_>
+struct PmTransOp {
+    using T = T_;
+    static constexpr int K = 1;
+    Grid g;
+    int d, b, n;
+    T cb;
+    const T *lo, *hi, *ad_a, *ad_b, *edge_b;
+    T* out;
+    __device__ inline void cell(int i, int j, int k, T c[1]) const {
+        const long long f0 = fidx(g, b, i, j, k), f1 = fidx(g, b, i + (b == 0), j + (b == 1), k + (b == 2));
+        c[0] = cb * (ad_b[f1] + ad_b[f0]) * (edge_b[f1] - edge_b[f0]);
+    }
+    __device__ inline void face(long long f, int kf, bool wl, bool wh, const T cl[1], const T ch[1]) const {
+        T l = lo[f], h = hi[f];
+        if (!wl) l -= cl[0];
+        if (!wh) h -= ch[0];
+        if (d == 2) zbc(g, kf, n, l, h);
+        out[f] = upwind(ad_a[f], l, h);
+    }
+};
+
+// pre-MAC stage 3: the normal velocity on d-faces,
+// corr(c) = 0.5 dt F_d(c) - c1 (ad_b1+ + ad_b1-) (T1+ - T1-) - c2 (...)
+// over the b1 / b2 faces of c (T_b the stage-2 states of component d on the
+// b faces corrected along the other direction); mac = riemann(lo + corr(c -
+// e_d), hi + corr(c))
+template <typename T_>
+struct PmFinalOp {
+    using T = T_;
+    static constexpr int K = 1;
+    Grid g;
+    int d, b1, b2;
+    T hdt, c1, c2;
+    const T *lo, *hi, *forces;
+    C3<T> AD;
+    const T *T1, *T2;
+    double* mac;
+    __device__ inline void cell(int i, int j, int k, T c[1]) const {
+        const long long p1 = fidx(g, b1, i + (b1 == 0), j + (b1 == 1), k + (b1 == 2)), m1 = fidx(g, b1, i, j, k);
+        const long long p2 = fidx(g, b2, i + (b2 == 0), j + (b2 == 1), k + (b2 == 2)), m2 = fidx(g, b2, i, j, k);
+        const CellFOT<T, T> F{forces, g};
+        T s = hdt * F(d, i, j, k);
+        s -= c1 * (AD.p[b1][p1] + AD.p[b1][m1]) * (T1[p1] - T1[m1]);
+        s -= c2 * (AD.p[b2][p2] + AD.p[b2][m2]) * (T2[p2] - T2[m2]);
+        c[0] = s;
+    }
+    __device__ inline void face(long long f, int kf, bool wl, bool wh, const T cl[1], const T ch[1]) const {
+        T stl = wl ? T(0) : lo[f] + cl[0], sth = wh ? T(0) : hi[f] + ch[0];
+        if (d == 2) zbc(g, kf, d, stl, sth);
+        mac[f] = (double)riemann(stl, sth);
+    }
+};
+
+// post-MAC stage 2: the a-face states corrected along both transverse
+// directions b1 = a+1 and b2 = a+2 (conservative form, dt/3 corner factors),
+//   corr_b(c) = q(c) rho cb (v_b+ - v_b-) - cb (v_b+ E_b(+) - v_b- E_b(-))
+// over the b faces of c; c[0..NC) the corrections along b1, c[NC..2NC) along b2
+template <typename T_, int NC>
+struct AdvTransOp {
+    using T = T_;
+    static constexpr int K = 2 * NC;
+    Grid g;
+    int d, b1, b2;
+    const T* vel;
+    T rho, cb1, cb2;
+    const T *ua, *vb1, *vb2;
+    C3<T> LO, HI, E1, E2;
+    P3<T> O1, O2;
+    __device__ inline void cell(int i, int j, int k, T c[K]) const {
+        const long long p1 = fidx(g, b1, i + (b1 == 0), j + (b1 == 1), k + (b1 == 2)), m1 = fidx(g, b1, i, j, k);
+        const long long p2 = fidx(g, b2, i + (b2 == 0), j + (b2 == 1), k + (b2 == 2)), m2 = fidx(g, b2, i, j, k);
+        const T v1p = (T)vb1[p1], v1m = (T)vb1[m1], v2p = (T)vb2[p2], v2m = (T)vb2[m2];
+        const T r1 = rho * cb1 * (v1p - v1m), r2 = rho * cb2 * (v2p - v2m);
+        const VelFPT<T, T> q{vel, g, T(1)};
+        for (int n = 0; n < NC; ++n) {
+            const T qc = q(n, i, j, k);
+            c[n] = qc * r1 - cb1 * (v1p * E1.p[n][p1] - v1m * E1.p[n][m1]);
+            c[NC + n] = qc * r2 - cb2 * (v2p * E2.p[n][p2] - v2m * E2.p[n][m2]);
+        }
+    }
+    __device__ inline void face(long long f, int kf, bool wl, bool wh, const T cl[K], const T ch[K]) const {
+        const T u = (T)ua[f];
+        const bool usmall = below_small_abs(u), upos = ge0(u);
+        auto pick = [&](T l, T h) { return usmall ? T(0.5) * (l + h) : (upos ? l : h); };
+        for (int n = 0; n < NC; ++n) {
+            const T l0 = LO.p[n][f], h0 = HI.p[n][f];
+            T l = wl ? l0 : l0 + cl[n], h = wh ? h0 : h0 + ch[n];
+            if (d == 2) zbc(g, kf, n, l, h);
+            O1.p[n][f] = pick(l, h);
+            l = wl ? l0 : l0 + cl[NC + n];
+            h = wh ? h0 : h0 + ch[NC + n];
+            if (d == 2) zbc(g, kf, n, l, h);
+            O2.p[n][f] = pick(l, h);
+        }
+    }
+};
+
+// post-MAC stage 3: final states and fluxes on d-faces.  The forces enter
+// scaled by rho for the velocity (forces = (src + divtau) / rho) and as they
+// are for a scalar (NC = 1: forces = src + diff, AdvOp_Godunov.H:114-329):
+//   corr(c) = hdt forces(c) + (q(c) r(c) - c1 x1(c) - c2 x2(c)),
+//   r = rho (c1 (v1+ - v1-) + c2 (v2+ - v2-)),  x_b = T_b(+) v_b+ - T_b(-) v_b-
+template <typename T_, int NC>
+struct AdvFluxOp {
+    using T = T_;
+    static constexpr int K = NC;
+    Grid g;
+    int d, b1, b2;
+    const T *vel, *forces;
+    T rho, hdt, c1, c2;
+    C3<T> U, T1, T2, LO, HI;
+    P3<T> Fl;
+    __device__ inline void cell(int i, int j, int k, T c[K]) const {
+        const long long p1 = fidx(g, b1, i + (b1 == 0), j + (b1 == 1), k + (b1 == 2)), m1 = fidx(g, b1, i, j, k);
+        const long long p2 = fidx(g, b2, i + (b2 == 0), j + (b2 == 1), k + (b2 == 2)), m2 = fidx(g, b2, i, j, k);
+        const T v1p = (T)U.p[b1][p1], v1m = (T)U.p[b1][m1], v2p = (T)U.p[b2][p2], v2m = (T)U.p[b2][m2];
+        const T r = rho * (c1 * (v1p - v1m) + c2 * (v2p - v2m));
+        const VelFPT<T, T> q{vel, g, T(1)};
+        const CellFOT<T, T> Fo{forces, g};
+        for (int n = 0; n < NC; ++n) {
+            const T x1 = T1.p[n][p1] * v1p - T1.p[n][m1] * v1m, x2 = T2.p[n][p2] * v2p - T2.p[n][m2] * v2m;
+            c[n] = hdt * Fo(n, i, j, k) + ((q(n, i, j, k) * r - c1 * x1) - c2 * x2);
+        }
+    }
+    __device__ inline void face(long long f, int kf, bool wl, bool wh, const T cl[K], const T ch[K]) const {
+        const T um = (T)U.p[d][f];
         const bool usmall = below_small_abs(um), upos = ge0(um);
         for (int n = 0; n < NC; ++n) {
             T stl = wl ? T(0) : LO.p[n][f] + cl[n];
             T sth = wh ? T(0) : HI.p[n][f] + ch[n];
-            if (d == 2) zbc(g, m, n, stl, sth);
+            if (d == 2) zbc(g, kf, n, stl, sth);
             const T st = usmall ? T(0.5) * (stl + sth) : (upos ? stl : sth);
             Fl.p[n][f] = um * st;
-            cl[n] = ch[n];
         }
     }
-}
-
-template <typename T, int NC>
-static void launch_adv_flux(Ctx& c, const Grid& g, int d, const T* vel, const T* forces, double rho, double dt, C3<T> U, C3<T> LO, C3<T> HI,
-                            C3<T> T1, C3<T> T2, P3<T> F, double bytes) {
-    const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
-    const FluxCell<T, NC> C{g, d, b1, b2, vel, forces, T(rho), T(0.5) * T(dt) * (NC == 3 ? T(rho) : T(1)), T(dt / (2.0 * hd(g, b1))),
-                            T(dt / (2.0 * hd(g, b2))), U, T1, T2};
-    if (d == 0) {
-        KS_LAUNCH(c, (k_adv_flux_x<T, NC>), nblocks(g.N, 256), 256, bytes, C, LO, HI, F);
-    } else {
-        constexpr int chunk = 16;
-        const int nf = d == 1 ? g.ny : nzfaces(g), no = d == 1 ? g.nz : g.ny;
-        const int bx = g.nx >= 128 ? 128 : 32 * ((g.nx + 31) / 32);
-        const dim3 grid((unsigned)((g.nx + bx - 1) / bx), (unsigned)(no * ((nf + chunk - 1) / chunk)));
-        KS_LAUNCH(c, (k_adv_flux_col<T, NC>), grid, bx, bytes, C, LO, HI, F, chunk);
-    }
-}
+};
 
 template <typename T>
 struct FluxPtrs {
@@ -817,17 +748,17 @@ static void premac_t(Ctx& c, const Grid& g, const T* vel, const T* forces, doubl
     for (auto& p : tpl) {
         const int a = p[0], b = p[1], n = p[2];
         const double bytes = BT * (4.0 * nfaces(g, a) + 2.0 * nfaces(g, b));
-        const T cb = T(dt / (6.0 * hd(g, b)));
-        KS_LAUNCH(c, k_pm_trans<T>, nblocks(nfaces(g, a), BS), BS, bytes, g, a, b, n, cb, tp<T>(B.lo[a][n]), tp<T>(B.hi[a][n]),
-                  tp<T>(B.ad[a]), tp<T>(B.ad[b]), tp<T>(B.tedge[b][n]), tp<T>(B.tr[a][b][0]));
+        const PmTransOp<T> op{g, a, b, n, T(dt / (6.0 * hd(g, b))), tp<T>(B.lo[a][n]), tp<T>(B.hi[a][n]), tp<T>(B.ad[a]), tp<T>(B.ad[b]),
+                              tp<T>(B.tedge[b][n]), tp<T>(B.tr[a][b][0])};
+        launch_cf(c, "k_pm_trans_x", "k_pm_trans_col", op, bytes);
     }
     C3<T> AD{{tp<T>(B.ad[0]), tp<T>(B.ad[1]), tp<T>(B.ad[2])}};
     for (int d = 0; d < 3; ++d) {
         const int b1 = (d + 1) % 3, b2 = (d + 2) % 3;
         const double bytes = BT * (1.0 * g.N + 3.0 * nfaces(g, d) + 2.0 * nfaces(g, b1) + 2.0 * nfaces(g, b2)) + B8 * nfaces(g, d);
-        const T c1 = T(dt / (4.0 * hd(g, b1))), c2 = T(dt / (4.0 * hd(g, b2)));
-        KS_LAUNCH(c, k_pm_final<T>, nblocks(nfaces(g, d), BS), BS, bytes, g, d, tp<T>(B.lo[d][d]), tp<T>(B.hi[d][d]), forces, T(dt), c1, c2,
-                  AD, tp<T>(B.tr[b1][b2][0]), tp<T>(B.tr[b2][b1][0]), mac[d]);
+        const PmFinalOp<T> op{g, d, b1, b2, T(0.5) * T(dt), T(dt / (4.0 * hd(g, b1))), T(dt / (4.0 * hd(g, b2))), tp<T>(B.lo[d][d]),
+                              tp<T>(B.hi[d][d]), forces, AD, tp<T>(B.tr[b1][b2][0]), tp<T>(B.tr[b2][b1][0]), mac[d]};
+        launch_cf(c, "k_pm_final_x", "k_pm_final_col", op, bytes);
     }
 }
 
@@ -857,7 +788,9 @@ static void advection_t(Ctx& c, const Grid& g, const T* vel, const T* forces, co
         C3<T> E2{{tp<T>(B.tedge[b2][0]), tp<T>(B.tedge[b2][1]), tp<T>(B.tedge[b2][2])}};
         P3<T> O1{{tp<T>(B.tr[a][b1][0]), tp<T>(B.tr[a][b1][1]), tp<T>(B.tr[a][b1][2])}};
         P3<T> O2{{tp<T>(B.tr[a][b2][0]), tp<T>(B.tr[a][b2][1]), tp<T>(B.tr[a][b2][2])}};
-        launch_adv_trans<T, 3>(c, g, a, vel, rho, dt, mac[a], mac[b1], mac[b2], LO, HI, E1, E2, O1, O2, bytes);
+        const AdvTransOp<T, 3> op{g, a, b1, b2, vel, T(rho), T(dt / (3.0 * hd(g, b1))), T(dt / (3.0 * hd(g, b2))), mac[a], mac[b1], mac[b2],
+                                  LO, HI, E1, E2, O1, O2};
+        launch_cf(c, "k_adv_trans_x", "k_adv_trans_col", op, bytes);
     }
     C3<T> U{{mac[0], mac[1], mac[2]}};
     for (int d = 0; d < 3; ++d) {
@@ -868,7 +801,9 @@ static void advection_t(Ctx& c, const Grid& g, const T* vel, const T* forces, co
         C3<T> T1{{tp<T>(B.tr[b1][b2][0]), tp<T>(B.tr[b1][b2][1]), tp<T>(B.tr[b1][b2][2])}};
         C3<T> T2{{tp<T>(B.tr[b2][b1][0]), tp<T>(B.tr[b2][b1][1]), tp<T>(B.tr[b2][b1][2])}};
         P3<T> F{{tp<T>(B.flux[d][0]), tp<T>(B.flux[d][1]), tp<T>(B.flux[d][2])}};
-        launch_adv_flux<T, 3>(c, g, d, vel, forces, rho, dt, U, LO, HI, T1, T2, F, bytes);
+        const AdvFluxOp<T, 3> op{g, d, b1, b2, vel, forces, T(rho), T(0.5) * T(dt) * T(rho), T(dt / (2.0 * hd(g, b1))), T(dt / (2.0 * hd(g, b2))),
+                                 U, T1, T2, LO, HI, F};
+        launch_cf(c, "k_adv_flux_x", "k_adv_flux_col", op, bytes);
     }
     FluxPtrs<T> F;
     for (int d = 0; d < 3; ++d)
@@ -897,7 +832,9 @@ void launch_scalar_advection(Ctx& c, const Grid& g, const double* s, const doubl
         C3<T> LO{{tp<T>(B.lo[a][0]), nullptr, nullptr}}, HI{{tp<T>(B.hi[a][0]), nullptr, nullptr}};
         C3<T> E1{{tp<T>(B.tedge[b1][0]), nullptr, nullptr}}, E2{{tp<T>(B.tedge[b2][0]), nullptr, nullptr}};
         P3<T> O1{{tp<T>(B.tr[a][b1][0]), nullptr, nullptr}}, O2{{tp<T>(B.tr[a][b2][0]), nullptr, nullptr}};
-        launch_adv_trans<T, 1>(c, g, a, s, rho, dt, mac[a], mac[b1], mac[b2], LO, HI, E1, E2, O1, O2, B8 * (g.N + 5.0 * na + 2.0 * nt));
+        const AdvTransOp<T, 1> op{g, a, b1, b2, s, T(rho), T(dt / (3.0 * hd(g, b1))), T(dt / (3.0 * hd(g, b2))), mac[a], mac[b1], mac[b2],
+                                  LO, HI, E1, E2, O1, O2};
+        launch_cf(c, "k_scalar_trans_x", "k_scalar_trans_col", op, B8 * (g.N + 5.0 * na + 2.0 * nt));
     }
     C3<double> U{{mac[0], mac[1], mac[2]}};
     for (int d = 0; d < 3; ++d) {
@@ -906,7 +843,9 @@ void launch_scalar_advection(Ctx& c, const Grid& g, const double* s, const doubl
         C3<T> T1{{tp<T>(B.tr[b1][b2][0]), nullptr, nullptr}}, T2{{tp<T>(B.tr[b2][b1][0]), nullptr, nullptr}};
         P3<T> F{{tp<T>(B.flux[d][0]), nullptr, nullptr}};
         const double bytes = B8 * (2.0 * g.N + 4.0 * nfaces(g, d) + 2.0 * (nfaces(g, b1) + nfaces(g, b2)));
-        launch_adv_flux<T, 1>(c, g, d, s, fs, rho, dt, U, LO, HI, T1, T2, F, bytes);
+        const AdvFluxOp<T, 1> op{g, d, b1, b2, s, fs, T(rho), T(0.5) * T(dt), T(dt / (2.0 * hd(g, b1))), T(dt / (2.0 * hd(g, b2))), U, T1, T2,
+                                 LO, HI, F};
+        launch_cf(c, "k_scalar_flux_x", "k_scalar_flux_col", op, bytes);
     }
     FluxPtrs<T> F;
     for (int m = 0; m < 9; ++m) F.p[m] = nullptr;

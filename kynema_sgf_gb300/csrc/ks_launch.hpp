@@ -96,6 +96,16 @@ struct Ctx {
         ++(c).launches;                                        \
     } while (0)
 
+// the same under a given profiling name (a kernel template launched for several ops)
+#define KS_LAUNCH_NAMED(c, name, kern, grid, block, bytes, ...) \
+    do {                                                        \
+        const bool ks_p_ = (c).prof_match(name);                \
+        if (ks_p_) (c).prof_begin(name, (double)(bytes));       \
+        kern<<<(grid), (block), 0, (c).stream>>>(__VA_ARGS__);  \
+        if (ks_p_) (c).prof_end();                              \
+        ++(c).launches;                                         \
+    } while (0)
+
 // the same with dynamic shared memory
 #define KS_LAUNCH_SMEM(c, kern, grid, block, smem, bytes, ...)        \
     do {                                                               \
