@@ -1,11 +1,17 @@
-// Reverse (adjoint) kernels of the advance, FP64.
+// Reverse (adjoint) kernels of the advance.  Adjoint arrays are FP64; each
+// pass computes in its forward pass's precision (TI / A: double, or float for
+// the mixed-precision form's FP32 passes).
 //
-// Every forward pass y = K(x) gets a kernel that accumulates x_bar += (dK/dx)^T
-// y_bar at the forward linearisation point.  The PPM limiter, clipping,
-// Riemann and upwind selections are re-evaluated from the stored forward
-// values and frozen (their derivatives are the derivatives of the selected
-// branch).  Inputs that several outputs read are accumulated with atomicAdd.
-// Boundary handling mirrors the forward kernels: x/y periodic; z periodic or
+// Every forward pass y = K(x) gets a kernel (or a pair) that accumulates
+// x_bar += (dK/dx)^T y_bar at the forward linearisation point.  The PPM
+// limiter, clipping, Riemann and upwind selections are re-evaluated from the
+// stored forward values and frozen (their derivatives are the derivatives of
+// the selected branch).  Inputs that several outputs read are accumulated
+// either in gather form, each adjoint value owned by one thread that collects
+// the terms of the outputs reading it (the post-MAC stages, the PPM edges and
+// face stage, Smagorinsky; one FP64 add per owned value), or with atomicAdd
+// (the pre-MAC transverse / final stages, the wall faces, the diffusion
+// tile's flush).  Boundary handling mirrors the forward kernels: x/y periodic; z periodic or
 // walls, where the forward reads fill-patch ghosts (high-order extrapolation
 // of the tangential components, zero normal component) for Godunov, odd/even
 // reflections or the wall-model shift for diffusion, and replaces wall-face
