@@ -908,7 +908,7 @@ void Sim::cc_vcycle(std::vector<CCLevelT<T>>& Ls, size_t l, double beta, bool in
         launch_cc_gsrb(ctx_, L, beta, 0);
         launch_cc_gsrb(ctx_, L, beta, 1);
     }
-    launch_cc_resid(ctx_, L, beta, nullptr, nullptr);
+    launch_cc_resid(ctx_, L, beta, nullptr, nullptr, mac_.nu1 > 0 ? 1 : -1);  // after the colour-1 half-sweep
     launch_cc_restrict(ctx_, L, Ls[l + 1]);
     cc_vcycle(Ls, l + 1, beta, in_graph);
     launch_cc_prolong(ctx_, L, Ls[l + 1]);
@@ -1003,11 +1003,14 @@ void Sim::mac_project() {
         launch_fill(ctx_, L.phi, 0.0, g_.N);
     }
     // mixed precision: each FP64 residual is the next FP32 cycle's right-hand side
+    int zc = -1;  // the colour whose residual is zero (none for the starting iterate)
     auto resid = [&]() {
         if (mixed_) launch_cc_resid32(ctx_, L, beta, cc32_[0].rhs, cc32_[0].phi, parts_.p, &np);
-        else launch_cc_resid(ctx_, L, beta, parts_.p, &np);
+        else launch_cc_resid(ctx_, L, beta, parts_.p, &np, zc);
     };
     resid();
+    // after a V-cycle the last half-sweep was colour 1's (post-smoothing on a level above the bottom)
+    if (mac_.nu2 > 0 && cc_.size() > 1) zc = 1;
     const double r0 = reduce(np, 1, 1, nullptr);
     mac_r0_ = r0;
     const double target = std::max(mac_.atol, mac_.rtol * std::max(bnorm, r0));

@@ -367,7 +367,9 @@ using NDLevelDev = NDLevelT<double>;
 template <typename T>
 void launch_cc_gsrb(Ctx& c, const CCLevelT<T>& L, double beta, int color);
 template <typename T>
-void launch_cc_resid(Ctx& c, const CCLevelT<T>& L, double beta, double* partials, int* nparts);
+// zero_color 0 / 1: the cells of that colour were the last red-black half-sweep's (their
+// residual is zero to rounding and is written as 0 without evaluation); -1: none
+void launch_cc_resid(Ctx& c, const CCLevelT<T>& L, double beta, double* partials, int* nparts, int zero_color = -1);
 // FP64 residuals of the mixed-precision defect correction, written as the FP32 cycle's
 // right-hand side r32 with its solution z32 zeroed (L.res untouched)
 void launch_cc_resid32(Ctx& c, const CCLevelT<double>& L, double beta, float* r32, float* z32, double* partials, int* nparts);

@@ -174,11 +174,59 @@ __global__ void k_cc_gsrb(CCLevelT<T> L, CCCoef<T> w, int color, int kc) {
 // the mixed-precision form) it goes to the FP32 cycle's right-hand side r32,
 // whose solution z32 starts at zero, instead of L.res.  Grid-stride over
 // (i, j, chunk of kc layers) columns marching in k, with the class weights
-// selected from scalars (as in k_cc_gsrb).
+// selected from scalars (as in k_cc_gsrb).  zc = 0 / 1: the cells of that
+// colour, (i + j + k) & 1 == zc, were the last half-sweep's, whose update
+// solved their equations with their (other-colour) neighbours unchanged, so
+// their residual is zero to rounding: it is written as 0 without the
+// stencil.  A thread then owns the cell pair (2 i2, 2 i2 + 1) of a row, as in
+// k_cc_gsrb, so that every lane of a warp evaluates the same colour (half the
+// FP64 work); zc = -1: every cell is evaluated.
 template <typename T>
-__global__ void k_cc_resid(CCLevelT<T> L, CCCoef<T> w, int kc, double* parts, float* r32, float* z32) {
+__global__ void k_cc_resid(CCLevelT<T> L, CCCoef<T> w, int kc, double* parts, float* r32, float* z32, int zc) {
     const int sy = L.nx, sz = L.nx * L.ny;
     const int nch = (L.nz + kc - 1) / kc;
+    if (zc >= 0) {
+        const int hx = L.nx >> 1;
+        const unsigned M2 = (unsigned)(hx * L.ny * nch);
+        MaxAbs<T> mx;
+        const T* p = L.phi;
+        for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < M2; t += gridDim.x * blockDim.x) {
+            int i2, j, ch;
+            split3(t, (unsigned)hx, (unsigned)L.ny, i2, j, ch);
+            const int dyp = (j + 1 == L.ny ? -j : 1) * sy, dym = (j == 0 ? L.ny - 1 : -1) * sy;
+            const int k0 = ch * kc, k1 = min(k0 + kc, L.nz);
+            for (int k = k0; k < k1; ++k) {
+                const int o = (j + k + 1 - zc) & 1;  // the pair member of the evaluated colour 1 - zc
+                const int i = 2 * i2 + o, c = k * sz + j * sy + i;
+                const int dxp = i + 1 == L.nx ? 1 - L.nx : 1, dxm = i == 0 ? L.nx - 1 : -1;
+                const T sx = p[c + dxp] + p[c + dxm];
+                const T syv = p[c + dyp] + p[c + dym];
+                T szv;
+                if (L.zper) {
+                    const int kp = k + 1 == L.nz ? 0 : k + 1, km = k == 0 ? L.nz - 1 : k - 1;
+                    szv = p[c + (kp - k) * sz] + p[c + (km - k) * sz];
+                } else {
+                    szv = (k == 0 ? T(0) : p[c - sz]) + (k + 1 == L.nz ? T(0) : p[c + sz]);
+                }
+                T gx = w.gx0, gy = w.gy0, gz = w.gz0, dg = w.dg0;
+                if (!L.zper && (k == 0 || k + 1 == L.nz)) {
+                    const bool one = L.nz == 1;
+                    gx = one ? w.gx2 : w.gx1;
+                    gy = one ? w.gy2 : w.gy1;
+                    gz = one ? w.gz2 : w.gz1;
+                    dg = one ? w.dg2 : w.dg1;
+                }
+                const T S = gx * sx + gy * syv + gz * szv;
+                const T v = L.rhs[c] - dg * (p[c] - S);
+                L.res[c] = v;
+                L.res[c + 1 - 2 * o] = T(0);  // the other member
+                mx.add(v);
+            }
+        }
+        const double m = bred<1>(mx.get());
+        if (threadIdx.x == 0 && parts) parts[blockIdx.x] = m;
+        return;
+    }
     const unsigned M = (unsigned)(sz * nch);
     MaxAbs<T> mx;
     const T* p = L.phi;
@@ -975,7 +1023,7 @@ void launch_cc_gsrb(Ctx& c, const CCLevelT<T>& L, double beta, int color) {
     KS_LAUNCH(c, k_cc_gsrb<T>, grid, bx, sizeof(T) * 2.0 * ncc(L), L, cc_coef(L), color, kc);
 }
 template <typename T>
-void launch_cc_resid(Ctx& c, const CCLevelT<T>& L, double beta, double* parts, int* np) {
+void launch_cc_resid(Ctx& c, const CCLevelT<T>& L, double beta, double* parts, int* np, int zero_color) {
     (void)beta;
     const int kc = cc_chunk(L);
     if constexpr (sizeof(T) == 4) {
@@ -986,16 +1034,17 @@ void launch_cc_resid(Ctx& c, const CCLevelT<T>& L, double beta, double* parts, i
             return;
         }
     }
-    const int n = parts_for((long long)L.nx * L.ny * ((L.nz + kc - 1) / kc));
+    if (L.nx % 2) zero_color = -1;  // the pair form needs an even row
+    const int n = parts_for((long long)(zero_color >= 0 ? L.nx / 2 : L.nx) * L.ny * ((L.nz + kc - 1) / kc));
     if (np) *np = n;
-    KS_LAUNCH(c, k_cc_resid<T>, n, BS, sizeof(T) * 3.0 * ncc(L), L, cc_coef(L), kc, parts, (float*)nullptr, (float*)nullptr);
+    KS_LAUNCH(c, k_cc_resid<T>, n, BS, sizeof(T) * 3.0 * ncc(L), L, cc_coef(L), kc, parts, (float*)nullptr, (float*)nullptr, zero_color);
 }
 void launch_cc_resid32(Ctx& c, const CCLevelT<double>& L, double beta, float* r32, float* z32, double* parts, int* np) {
     (void)beta;
     const int kc = cc_chunk(L);
     const int n = parts_for((long long)L.nx * L.ny * ((L.nz + kc - 1) / kc));
     *np = n;
-    KS_LAUNCH(c, k_cc_resid<double>, n, BS, 8.0 * 2.0 * ncc(L) + 8.0 * ncc(L), L, cc_coef(L), kc, parts, r32, z32);
+    KS_LAUNCH(c, k_cc_resid<double>, n, BS, 8.0 * 2.0 * ncc(L) + 8.0 * ncc(L), L, cc_coef(L), kc, parts, r32, z32, -1);
 }
 void launch_nd_resid32(Ctx& c, const NDLevelT<double>& L, double sigma, float* r32, float* z32, double* parts, int* np) {
     const int kc = nd_chunk(L);
@@ -1095,7 +1144,7 @@ void launch_add_f32(Ctx& c, double* phi, const float* e, long long n) {
 
 #define KS_INST(T)                                                                                           \
     template void launch_cc_gsrb<T>(Ctx&, const CCLevelT<T>&, double, int);                                  \
-    template void launch_cc_resid<T>(Ctx&, const CCLevelT<T>&, double, double*, int*);                       \
+    template void launch_cc_resid<T>(Ctx&, const CCLevelT<T>&, double, double*, int*, int);                  \
     template void launch_cc_restrict<T>(Ctx&, const CCLevelT<T>&, const CCLevelT<T>&);                       \
     template void launch_cc_prolong<T>(Ctx&, const CCLevelT<T>&, const CCLevelT<T>&);                        \
     template void launch_cc_bottom<T>(Ctx&, const CCLevelT<T>&, double, int);                                \
