@@ -27,19 +27,6 @@ namespace {
 
 constexpr int BS = 256;
 
-// face index -> (i, j, k) in 32-bit arithmetic (a 64-bit division costs as
-// much issue as tens of FP64 operations)
-__device__ inline bool face_of(const Grid& g, int d, long long t, int& i, int& j, int& k) {
-    const int nzl = (d == 2) ? nzfaces(g) : g.nz;
-    const long long M = (long long)g.nx * g.ny * nzl;
-    if (t >= M) return false;
-    const unsigned u = (unsigned)t, r = u / (unsigned)g.nx;
-    i = (int)(u - r * (unsigned)g.nx);
-    k = (int)(r / (unsigned)g.ny);
-    j = (int)(r - (unsigned)k * (unsigned)g.ny);
-    return true;
-}
-
 inline long long nfaces(const Grid& g, int d) { return (long long)g.nx * g.ny * (d == 2 ? nzfaces(g) : g.nz); }
 
 // van Leer limited slope of the middle cell of (a, b, c):
@@ -395,7 +382,6 @@ __global__ void __launch_bounds__(256) k_ppm_x(PpmArgs<T> A, T s, T rho, PpmOut<
     else u = (T)A.umac[fc];
     const bool up = above_small(u), dn = below_msmall(u);
     const TraceCoef<T> tc(absv(u) * s);
-#pragma unroll
     T pmv[NC], ppv[NC];
     for (int n = 0; n < NC; ++n) {
         const T a0 = ld(n, c);
