@@ -2120,6 +2120,34 @@ static void rotate(const double* ax, double ang, const double* v, double* out) {
     for (int m = 0; m < 3; ++m) out[m] = v[m] * c + cr[m] * s + ax[m] * d * (1 - c);
 }
 
+// Sampling points of a disk and their area weights (ops::base::compute_disk_points,
+// src/wind_energy/actuator/disk/disk_ops.cpp:373-412, with the sampling vector as the
+// cylinder axis and diameters_to_sample as the offset; AreaComputer::weight,
+// disk_ops.cpp:105-123): the reference vector khat x axis (compute_coplanar_vector,
+// disk_ops.cpp:322-326) is rotated about the axis by 2 pi j / nt at radius
+// dr (i + 1/2) (dr i for a single radial point), radius-major; the weight of ring i is
+// ((i + 1)^2 - i^2) / (nr^2 nt).
+static void sample_points(const DiskParams& dp, std::vector<double>& x, std::vector<double>& w) {
+    const double* ax = dp.sample;
+    double refv[3] = {-ax[1], ax[0], 0.0};
+    {
+        double m = std::sqrt(refv[0] * refv[0] + refv[1] * refv[1]);
+        refv[0] /= m; refv[1] /= m;
+    }
+    const double drs = 0.5 * dp.diameter / dp.nr;
+    const double shift = dp.nr == 1 ? 0.0 : 0.5;
+    x.assign(3 * (size_t)dp.nr * dp.nt, 0.0);
+    w.assign((size_t)dp.nr * dp.nt, 0.0);
+    for (int ir = 0; ir < dp.nr; ++ir)
+        for (int it = 0; it < dp.nt; ++it) {
+            const size_t p = (size_t)ir * dp.nt + it;
+            double rp[3];
+            rotate(ax, 2 * kPi / dp.nt * it, refv, rp);
+            for (int m = 0; m < 3; ++m) x[3 * p + m] = dp.center[m] + dp.diameters_to_sample * dp.diameter * ax[m] + drs * (ir + shift) * rp[m];
+            w[p] = ((ir + 1.0) * (ir + 1.0) - (double)ir * ir) / ((double)dp.nr * dp.nr * dp.nt);
+        }
+}
+
 // Actuator::pre_advance_work (src/wind_energy/actuator/Actuator.cpp:148-158):
 // trilinear sampling (ActuatorContainer.cpp:284-360), area-weighted average
 // (disk_ops.H:144-169), Ct table (disk_ops.H:128-134), uniform-Ct force
@@ -2134,22 +2162,13 @@ void Sim::actuator_update() {
         const double R = 0.5 * dp.diameter;
         // sampling points on the upstream (sample) disk
         double ref[3] = {0, 0, 0};
-        const double* ax = dp.sample;  // the sampling disk is normal to sample_vec (compute_disk_points)
-        double refv[3] = {-ax[1], ax[0], 0.0};
-        {
-            double m = std::sqrt(refv[0] * refv[0] + refv[1] * refv[1]);
-            refv[0] /= m; refv[1] /= m;
-        }
-        const double drs = R / dp.nr;
-        const double shift = dp.nr == 1 ? 0.0 : 0.5;
+        std::vector<double> xs, ws;
+        sample_points(dp, xs, ws);
         for (int ir = 0; ir < dp.nr; ++ir) {
-            const double wgt = ((ir + 1.0) * (ir + 1.0) - (double)ir * ir) / ((double)dp.nr * dp.nr * dp.nt);
             for (int it = 0; it < dp.nt; ++it) {
-                double rp[3];
-                rotate(ax, 2 * kPi / dp.nt * it, refv, rp);
-                double x[3];
-                for (int m = 0; m < 3; ++m)
-                    x[m] = dp.center[m] + dp.diameters_to_sample * dp.diameter * ax[m] + drs * (ir + shift) * rp[m];
+                const size_t p = (size_t)ir * dp.nt + it;
+                const double wgt = ws[p];
+                const double* x = &xs[3 * p];
                 const double fx = (x[0] - g.plo[0] - 0.5 * g.dx[0]) / g.dx[0];
                 const double fy = (x[1] - g.plo[1] - 0.5 * g.dx[1]) / g.dx[1];
                 const double fz = (x[2] - g.plo[2] - 0.5 * g.dx[2]) / g.dx[2];
@@ -2171,7 +2190,7 @@ void Sim::actuator_update() {
             }
         }
         for (int n = 0; n < 3; ++n) dp.ref_vel[n] = ref[n];
-        ax = dp.normal;  // U_inf is the sampled velocity along the disk normal; the force ring lies in the disk plane
+        const double* ax = dp.normal;  // U_inf is the sampled velocity along the disk normal; the force ring lies in the disk plane
         const double un = ref[0] * ax[0] + ref[1] * ax[1] + ref[2] * ax[2];
         dp.uinf_sqr = un * un;
         // linear table with end clamping
@@ -2887,6 +2906,17 @@ double kso_get_scalar(void* h, const char* name) {
         const auto& dp = s.disks.at(std::stoi(n.substr(12, c - 12)));
         const int m = std::stoi(n.substr(c + 1));
         return n[5] == 'n' ? dp.normal[m] : dp.sample[m];
+    }
+    // "disk_point:k:p:m" / "disk_weight:k:p": sampling point p of disk k and its area weight
+    if (n.rfind("disk_point:", 0) == 0 || n.rfind("disk_weight:", 0) == 0) {
+        const bool pt = n[5] == 'p';
+        const size_t a = pt ? 11 : 12, b = n.find(':', a);
+        const auto& dp = s.disks.at(std::stoi(n.substr(a, b - a)));
+        std::vector<double> xs, ws;
+        sample_points(dp, xs, ws);
+        if (!pt) return ws.at(std::stoi(n.substr(b + 1)));
+        const size_t c = n.find(':', b + 1);
+        return xs.at(3 * std::stoul(n.substr(b + 1, c - b - 1)) + std::stoi(n.substr(c + 1)));
     }
     return NAN;
 }

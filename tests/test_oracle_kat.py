@@ -483,6 +483,71 @@ time.max_step = 2
 """
 
 
+def disk_points_deck(center, nr=2, nt=2, diameter=2.0, normal="1 0 0"):
+    """One uniform-Ct disk with its sampling disk on the rotor (diameters_to_sample 0),
+    in a box holding every centre of the known answers below."""
+    return f"""
+geometry.prob_lo = -2000 -2000 -2000
+geometry.prob_hi = 2000 2000 2000
+geometry.is_periodic = 1 1 1
+amr.n_cell = 8 8 8
+incflo.physics = FreeStream
+incflo.velocity = 8.0 0.0 0.0
+transport.viscosity = 1e-5
+turbulence.model = Laminar
+ICNS.source_terms = ActuatorForcing
+Actuator.labels = T0
+Actuator.type = UniformCtDisk
+Actuator.UniformCtDisk.rotor_diameter = {diameter}
+Actuator.UniformCtDisk.epsilon = 1
+Actuator.UniformCtDisk.thrust_coeff = 0.75
+Actuator.UniformCtDisk.num_points_r = {nr}
+Actuator.UniformCtDisk.num_points_t = {nt}
+Actuator.UniformCtDisk.spreading_type = UniformGaussian
+Actuator.UniformCtDisk.diameters_to_sample = 0
+Actuator.T0.disk_center = {center[0]} {center[1]} {center[2]}
+Actuator.T0.disk_normal = {normal}
+incflo.use_godunov = 1
+incflo.godunov_type = ppm
+time.fixed_dt = 0.1
+time.max_step = 1
+"""
+
+
+# unit_tests/wind_energy/actuator/test_disk_functions.cpp:80-116: a disk of
+# diameter 2 facing x, 2 x 2 points; the points sit at -+ 0.5 dr and -+ 1.5 dr
+# along y (dr = 0.5) from each of these centres, radius-major
+DISK_POINT_CENTERS = [(0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1), (1, 1, 1), (-1, 0, 0), (-1, -1, -1), (1000.0, 30.0, 5.0)]
+
+
+@pytest.mark.parametrize("center", DISK_POINT_CENTERS)
+def test_disk_points_known_answers(oracle_mod, center):
+    o = oracle_mod.Oracle(disk_points_deck(center))
+    dr = 2.0 * 0.5 / 2
+    gold = [(0.0, 0.5 * dr, 0.0), (0.0, -0.5 * dr, 0.0), (0.0, 1.5 * dr, 0.0), (0.0, -1.5 * dr, 0.0)]
+    eps = 3.0 * EPS
+    for p, gp in enumerate(gold):
+        for m in range(3):
+            x = o.scalar("disk_point:0:%d:%d" % (p, m))
+            assert abs(x - (gp[m] + center[m])) <= eps * max(1.0, abs(center[m])), (p, m, x)
+
+
+# test_disk_functions.cpp:47-78, 118-125 (AreaComputer): the ring sections of a
+# polar grid of nr x nt points add up to pi R^2 and their weights to 1
+@pytest.mark.parametrize("radius,nr,nt", [(1.0, 3, 1), (1.0, 3, 2), (127.0, 10, 3), (30.0, 5, 30)])
+def test_disk_area_weights_known_answers(oracle_mod, radius, nr, nt):
+    o = oracle_mod.Oracle(disk_points_deck((0, 0, 0), nr=nr, nt=nt, diameter=2.0 * radius))
+    area = math.pi * radius * radius
+    w = [o.scalar("disk_weight:0:%d" % p) for p in range(nr * nt)]
+    assert abs(sum(w) - 1.0) <= 10.0 * EPS
+    assert abs(sum(x * area for x in w) - area) <= 1.0e4 * EPS * area
+    # AreaComputer::area_section(i) = R^2 pi / (nr^2 nt) ((i + 1)^2 - i^2)
+    for i in range(nr):
+        for j in range(nt):
+            sec = radius * radius / nr / nr * math.pi / nt * ((i + 1.0) ** 2 - float(i) ** 2)
+            assert abs(w[i * nt + j] * area - sec) <= 1.0e2 * EPS * area
+
+
 DIFFERENT_NORTH = "Coriolis.Forcing.north_vector = 1 0 0\nCoriolis.Forcing.east_vector = 0 -1 0"
 _R2 = math.sqrt(0.5)
 # (disk keys, Coriolis keys, gold normal, gold sample vector): the cases of
