@@ -1,7 +1,7 @@
 #!/usr/bin/env python
 """Throughput benchmark of the single-level incompressible advance.
 
-Workload: neutral ABL LES, 256 x 256 x 128 cells on 5120 x 5120 x 1280 m,
+Workload: neutral ABL LES, 256 x 256 x 128 cells on 5120 x 5120 x 1280 m (20 x 20 x 10 m cells),
 FP64, Godunov PPM advection, MAC and nodal projections by geometric
 multigrid, Smagorinsky Cs = 0.135, geostrophic (8 m/s) + Coriolis forcing,
 wall-model bottom, slip top, CFL 0.9, log-law start with seeded +-0.5 m/s
@@ -34,7 +34,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Mcell-steps/s at 256^3 (FP64 vs mixed-precision at stated error) + adjoint/forward cost ratio"
 UNIT = "Mcell-steps/s"
-WORKLOAD = "ABL LES 256x256x128 FP64 (5120x5120x1280 m, Smagorinsky, geostrophic+Coriolis, wall model, CFL 0.9)"
+# the ABL box: 256 x 256 x 128 cells on 5120 x 5120 x 1280 m, i.e. 20 x 20 x 10 m cells
+# (other --size values keep the cell size)
+ABL_DZ = 10.0
+WORKLOAD = "ABL LES 256x256x128 FP64 (5120x5120x1280 m: 20x20x10 m cells, Smagorinsky, geostrophic+Coriolis, wall model, CFL 0.9)"
 CPU_SAMPLE = (128, 128, 64)  # same dx, physics and deck as the workload, 1/8 of the cells
 DATA = "synthetic (log-law + seeded uniform noise, SplitMix64 seed 42)"
 
@@ -103,12 +106,12 @@ def cpu_worker(spec):
     from kynema_sgf_gb300 import decks
     from oracle.oracle import Oracle
     skip_init = "\nincflo.do_initial_proj = 0\nincflo.initial_iterations = 0\n"
-    deck = decks.abl(nx, ny, nz, steps=10 ** 6) + skip_init
+    deck = decks.abl(nx, ny, nz, steps=10 ** 6, dz=ABL_DZ) + skip_init
     if case == "tgv":
         nx = ny = nz = 64
         deck = decks.tgv(64, steps=10 ** 6)
     if case == "mol":
-        deck = decks.mol(decks.abl(nx, ny, nz, steps=10 ** 6, cfl=0.45)) + skip_init
+        deck = decks.mol(decks.abl(nx, ny, nz, steps=10 ** 6, cfl=0.45, dz=ABL_DZ)) + skip_init
     runs = []
     for _ in range(repeats):
         o = Oracle(deck)
@@ -250,7 +253,7 @@ def our_arm(args, rank, world, local_rank):
         import torch.distributed as tdist
     torch.cuda.set_device(local_rank)
     nx, ny, nz = (int(x) for x in args.size.split(","))
-    sim = ks.Incflo(decks.abl(nx, ny, nz, steps=10 ** 9))
+    sim = ks.Incflo(decks.abl(nx, ny, nz, steps=10 ** 9, dz=ABL_DZ))
     sim.InitData()
     cells = sim.scalar("ncells")
     # warm-up; the last warm-up step times every kernel to pick the dominant one
@@ -375,7 +378,7 @@ def c2_bench(args, torch, ks, decks, nx, ny, nz, world, rank, fp64_ms_main):
     peak, peak_kind = peaks()
     res = {}
     for form in ("fp64", "mixed"):
-        deck = decks.abl(nx, ny, nz, steps=10 ** 9) + ("\nks.precision = mixed\n" if form == "mixed" else "")
+        deck = decks.abl(nx, ny, nz, steps=10 ** 9, dz=ABL_DZ) + ("\nks.precision = mixed\n" if form == "mixed" else "")
         sim = ks.Incflo(deck)
         sim.InitData()
         cells = sim.scalar("ncells")
@@ -501,7 +504,7 @@ def mol_bench(args, torch, ks, decks, nx, ny, nz, world, rank):
     """The ABL workload advanced with the MOL predictor-corrector
     (incflo.use_godunov = false, explicit diffusion) at CFL 0.45 (MOL requires
     <= 0.5): two MAC and two nodal projections per step."""
-    out = variant_bench(args, torch, ks, decks.mol(decks.abl(nx, ny, nz, steps=10 ** 9, cfl=0.45)),
+    out = variant_bench(args, torch, ks, decks.mol(decks.abl(nx, ny, nz, steps=10 ** 9, cfl=0.45, dz=ABL_DZ)),
                         "ABL %dx%dx%d, MOL predictor-corrector, explicit diffusion, CFL 0.45, FP64" % (nx, ny, nz), world, rank, "MOL")
     out["projections_per_step"] = {"mac": 2, "nodal": 2}
     return out
@@ -512,7 +515,7 @@ def cn_bench(args, torch, ks, decks, nx, ny, nz, world, rank):
     Crank-Nicolson (incflo.diffusion_type = 1): predictor_rhs with half the old
     diffusion term and a multigrid solve of rho u - dt/2 divtau(u) per step; no
     diffusion CFL."""
-    d = decks.abl(nx, ny, nz, steps=10 ** 9).replace("incflo.diffusion_type = 0", "incflo.diffusion_type = 1")
+    d = decks.abl(nx, ny, nz, steps=10 ** 9, dz=ABL_DZ).replace("incflo.diffusion_type = 0", "incflo.diffusion_type = 1")
     return variant_bench(args, torch, ks, d, "ABL %dx%dx%d, Godunov, Crank-Nicolson diffusion, CFL 0.9, FP64" % (nx, ny, nz), world, rank,
                          "Crank-Nicolson")
 

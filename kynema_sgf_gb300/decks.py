@@ -39,12 +39,14 @@ def mol(deck):
     return out
 
 
-def abl(nx=256, ny=256, nz=128, steps=100, dx=20.0, cfl=0.9, seed=42):
+def abl(nx=256, ny=256, nz=128, steps=100, dx=20.0, cfl=0.9, seed=42, dz=None):
     """Neutral ABL LES: periodic x/y, wall-model bottom, slip top,
-    Smagorinsky Cs = 0.135, geostrophic forcing for 8 m/s with Coriolis."""
+    Smagorinsky Cs = 0.135, geostrophic forcing for 8 m/s with Coriolis;
+    cells of dx x dx x dz (dz = dx unless given)."""
+    dz = dx if dz is None else dz
     return f"""
 geometry.prob_lo = 0 0 0
-geometry.prob_hi = {nx * dx} {ny * dx} {nz * dx}
+geometry.prob_hi = {nx * dx} {ny * dx} {nz * dz}
 geometry.is_periodic = 1 1 0
 amr.n_cell = {nx} {ny} {nz}
 amr.max_level = 0

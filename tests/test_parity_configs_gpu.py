@@ -3,8 +3,9 @@
 The CUDA path (C ABI, cuda:0) and the CPU oracle advance the same decks:
 - the Taylor-Green vortex exactly as benchmarked: 64^3, Re 1600, CFL 0.5,
   nodal rtol 1e-11, initial projection and 3 pressure iterations, 20 steps;
-- the neutral ABL on 128 x 128 x 64 cells at the benchmark's 20 m spacing
-  (wall model, slip top, Smagorinsky, geostrophic + Coriolis, CFL 0.9), 4 steps;
+- the neutral ABL on 128 x 128 x 64 cubic 20 m cells (wall model, slip top,
+  Smagorinsky, geostrophic + Coriolis, CFL 0.9), 4 steps (the benchmark box's
+  20 x 20 x 10 m cells: test_zzz_named_box_gpu.py);
 - the adjoint-check disk deck (128 x 128 x 64, 3 uniform-Ct disks, D = 16
   cells, fixed dt), 3 steps.
 
