@@ -65,6 +65,7 @@ def parse():
     p.add_argument("--c2-steps", type=int, default=100, help="steps of the FP64 / mixed-precision comparison")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint cost / gradient check (128x128x64, 3 disks)")
     p.add_argument("--no-mol", action="store_true", help="skip the MOL and Crank-Nicolson forms of the ABL workload")
+    p.add_argument("--no-semi", action="store_true", help="skip the workload with MAC semicoarsening (mac_proj.do_semicoarsening)")
     p.add_argument("--c4", action="store_true",
                    help="only the production forward + adjoint run: 512x512x256 ABL, 16 disks, mixed forward, FP64 adjoint")
     p.add_argument("--c4-steps", type=int, default=200)
@@ -342,8 +343,11 @@ def our_arm(args, rank, world, local_rank):
     tgv = {"workload": "Taylor-Green vortex 64^3, Re 1600, CFL 0.5, FP64, 20 timed steps", "value": 64 ** 3 / (tms * 1e-3) / 1e6,
            "unit": UNIT, "ms_per_step": tms}
     del tg
+    # last, so that no number above depends on it
+    semi = None if (args.no_semi or world > 1) else semi_bench(args, torch, ks, decks, nx, ny, nz, world, rank)
     return dict(value=value, ms=ms_max, cells=cells, launches=launches, dominant=dominant, dom=dom, clocks=clk, e2e=e2e, fp64_peak=fp64_peak, div=div,
-                mac=statistics.mean(mac_it), nodal=statistics.mean(nod_it), size=(nx, ny, nz), mixed=mixed, adjoint=adj, tgv=tgv, mol=mol, cn=cn, strat=strat)
+                mac=statistics.mean(mac_it), nodal=statistics.mean(nod_it), size=(nx, ny, nz), mixed=mixed, adjoint=adj, tgv=tgv, mol=mol, cn=cn, strat=strat,
+                semi=semi)
 
 
 def divergence(sim):
@@ -497,6 +501,25 @@ def variant_bench(args, torch, ks, deck, workload, world, rank, label):
            "nodal_vcycles_per_step": statistics.mean(nod_it), "diffusion_vcycles_per_solve": statistics.mean(dif_it),
            "divergence": divergence(sim)}
     del sim
+    return out
+
+
+def semi_bench(args, torch, ks, decks, nx, ny, nz, world, rank):
+    """The workload with mac_proj.do_semicoarsening = true, the reference's MLMG
+    option for cells finer in one direction: the MAC hierarchy halves z alone
+    (20 x 20 x 10 m -> 20 x 20 x 20 m cells), then all three directions.  FP64
+    and mixed precision, --steps steps after --warmup each.  A failure is
+    reported in the line instead of raised."""
+    out = {}
+    for form in ("fp64", "mixed"):
+        deck = (decks.abl(nx, ny, nz, steps=10 ** 9, dz=ABL_DZ) + "\nmac_proj.do_semicoarsening = true\n" +
+                ("ks.precision = mixed\n" if form == "mixed" else ""))
+        try:
+            out[form] = variant_bench(args, torch, ks, deck, "ABL %dx%dx%d, MAC semicoarsening, %s" % (nx, ny, nz, form), world, rank,
+                                      "semicoarsened MAC, " + form)
+        except Exception as e:  # reported, never silently replaced
+            out[form] = {"failed": str(e)[:300]}
+            break
     return out
 
 
@@ -796,7 +819,7 @@ def main():
                          "algorithmic_bytes_per_launch": by_l / n_l if n_l else None},
             "gpu_launches": r["launches"], "clocks": r["clocks"], "e2e": r["e2e"], "mixed_precision": r["mixed"],
             "adjoint": r["adjoint"], "tgv64": r["tgv"], "mol": r["mol"], "crank_nicolson": r["cn"],
-            "stratified_abl": r["strat"]}
+            "stratified_abl": r["strat"], "mac_semicoarsening": r["semi"]}
     # The FP64 path is bound by FP64 issue on this GPU (the nodal sweep's FP64 pipe is 81-83 % busy
     # under ncu): report the dominant kernel against the FMA peak measured live by ks_fma_peak as well.
     fl = FP64_FLOPS_PER_BYTE.get(r["dominant"])

@@ -214,6 +214,8 @@ void Sim::setup(const Deck& D) {
         m.nu1 = D.flag(p + ".num_pre_smooth", m.nu1);
         m.nu2 = D.flag(p + ".num_post_smooth", m.nu2);
         m.fixed_iters = D.flag(p + ".do_fixed_iters", m.fixed_iters);
+        m.semi = D.flag(p + ".do_semicoarsening", m.semi);
+        m.max_semi = D.flag(p + ".max_semicoarsening_level", m.max_semi);
     };
     mg(mac_, "mac_proj");
     mg(nod_, "nodal_proj");
@@ -419,6 +421,36 @@ static bool pinned_inverse(const std::vector<double>& A, int n, std::vector<doub
     return true;
 }
 
+// The coarsest MAC operator d p - sum w p of level C, assembled and inverted
+// with one unknown pinned (pinned_inverse); inv is left empty if that fails.
+static void cc_direct_inverse(const CCLevelDev& C, std::vector<double>& inv) {
+    const int nc = C.nx * C.ny * C.nz;
+    std::vector<double> A((size_t)nc * nc, 0.0);
+    const double d0 = 2.0 * C.ix2 + 2.0 * C.iy2;
+    auto at = [&](int ii, int jj, int kk) { return (kk * C.ny + jj) * C.nx + ii; };
+    for (int k = 0; k < C.nz; ++k)
+        for (int j = 0; j < C.ny; ++j)
+            for (int i = 0; i < C.nx; ++i) {
+                const int r = at(i, j, k);
+                const int ip = (i + 1) % C.nx, im = (i + C.nx - 1) % C.nx, jp = (j + 1) % C.ny, jm = (j + C.ny - 1) % C.ny;
+                double d = d0;
+                A[(size_t)r * nc + at(ip, j, k)] -= C.ix2;
+                A[(size_t)r * nc + at(im, j, k)] -= C.ix2;
+                A[(size_t)r * nc + at(i, jp, k)] -= C.iy2;
+                A[(size_t)r * nc + at(i, jm, k)] -= C.iy2;
+                if (C.zper) {
+                    d += 2.0 * C.iz2;
+                    A[(size_t)r * nc + at(i, j, (k + 1) % C.nz)] -= C.iz2;
+                    A[(size_t)r * nc + at(i, j, (k + C.nz - 1) % C.nz)] -= C.iz2;
+                } else {
+                    if (k > 0) { d += C.iz2; A[(size_t)r * nc + at(i, j, k - 1)] -= C.iz2; }
+                    if (k < C.nz - 1) { d += C.iz2; A[(size_t)r * nc + at(i, j, k + 1)] -= C.iz2; }
+                }
+                A[(size_t)r * nc + r] += d;
+            }
+    if (!pinned_inverse(A, nc, inv)) inv.clear();
+}
+
 // Bottom levels of up to kDirectBottom points are solved exactly: the coarsest MAC
 // operator d p - sum w p (scaled by -beta in the solve) and the coarsest nodal
 // stencil (scaled by sigma) are assembled on the host, their pinned inverses
@@ -432,32 +464,7 @@ void Sim::bottom_setup() {
     CCLevelDev& C = cc_.back();
     NDLevelDev& D = nd_.back();
     const int nc = C.nx * C.ny * C.nz, nn = D.nx * D.ny * D.nz;
-    if (nc <= kMaxDirect && cc_.size() > 1) {
-        std::vector<double> A((size_t)nc * nc, 0.0);
-        const double d0 = 2.0 * C.ix2 + 2.0 * C.iy2;
-        for (int k = 0; k < C.nz; ++k)
-            for (int j = 0; j < C.ny; ++j)
-                for (int i = 0; i < C.nx; ++i) {
-                    const int r = (k * C.ny + j) * C.nx + i;
-                    auto at = [&](int ii, int jj, int kk) { return (kk * C.ny + jj) * C.nx + ii; };
-                    const int ip = (i + 1) % C.nx, im = (i + C.nx - 1) % C.nx, jp = (j + 1) % C.ny, jm = (j + C.ny - 1) % C.ny;
-                    double d = d0;
-                    A[(size_t)r * nc + at(ip, j, k)] -= C.ix2;
-                    A[(size_t)r * nc + at(im, j, k)] -= C.ix2;
-                    A[(size_t)r * nc + at(i, jp, k)] -= C.iy2;
-                    A[(size_t)r * nc + at(i, jm, k)] -= C.iy2;
-                    if (C.zper) {
-                        d += 2.0 * C.iz2;
-                        A[(size_t)r * nc + at(i, j, (k + 1) % C.nz)] -= C.iz2;
-                        A[(size_t)r * nc + at(i, j, (k + C.nz - 1) % C.nz)] -= C.iz2;
-                    } else {
-                        if (k > 0) { d += C.iz2; A[(size_t)r * nc + at(i, j, k - 1)] -= C.iz2; }
-                        if (k < C.nz - 1) { d += C.iz2; A[(size_t)r * nc + at(i, j, k + 1)] -= C.iz2; }
-                    }
-                    A[(size_t)r * nc + r] += d;
-                }
-        if (!pinned_inverse(A, nc, binv_cc_h_)) binv_cc_h_.clear();
-    }
+    if (nc <= kMaxDirect && cc_.size() > 1) cc_direct_inverse(C, binv_cc_h_);
     if (nn <= kMaxDirect && nd_.size() > 1) {
         std::vector<double> A((size_t)nn * nn, 0.0);
         for (int k = 0; k < D.nz; ++k)
@@ -486,6 +493,115 @@ void Sim::bottom_setup() {
            "H2D bottom inverse");
     C.binv = binv_cc_h_.empty() ? nullptr : binv_.p;
     D.binv = binv_nd_h_.empty() ? nullptr : binv_.p + binv_cc_h_.size();
+}
+
+// Coarsening ratio (1 or 2 per direction) from a level of n cells of spacing
+// h to the next.  Full coarsening needs every count divisible by 4 (the
+// coarse count stays even for the red-black sweeps).  Semicoarsening
+// (MLMGOptions do_semicoarsening, src/core/MLMGOptions.cpp:24-28) halves only
+// the directions of smallest spacing while the spacings differ, each of them
+// divisible by 4; otherwise the level coarsens fully or not at all.  The
+// oracle's semi_ratio is the same rule.
+static void mg_ratio(const int n[3], const double h[3], bool semi, int r[3]) {
+    const double hmin = std::min(h[0], std::min(h[1], h[2])), hmax = std::max(h[0], std::max(h[1], h[2]));
+    bool full = true;
+    for (int d = 0; d < 3; ++d) full = full && (n[d] % 4 == 0);
+    if (semi && hmax > 1.0000001 * hmin) {
+        bool ok = true;
+        for (int d = 0; d < 3; ++d) {
+            r[d] = (h[d] <= 1.0000001 * hmin) ? 2 : 1;
+            if (r[d] == 2 && n[d] % 4 != 0) ok = false;
+        }
+        if (ok) return;
+    }
+    for (int d = 0; d < 3; ++d) r[d] = full ? 2 : 1;
+}
+
+// The MAC hierarchy under mac_proj.do_semicoarsening: levels coarsened by
+// mg_ratio until one cannot coarsen or a level below the finest holds at most
+// kDirectBottom cells (solved exactly, as in cc_).  When every coarsening is
+// full the hierarchy equals cc_ and nothing is built.
+void Sim::mac_semi_setup() {
+    std::vector<std::array<int, 3>> dims;
+    int n3[3] = {g_.nx, g_.ny, g_.nz};
+    double h[3] = {g_.dx, g_.dy, g_.dz};
+    bool partial = false;
+    while (true) {
+        dims.push_back({n3[0], n3[1], n3[2]});
+        int r[3];
+        mg_ratio(n3, h, (long long)dims.size() - 1 < (long long)mac_.max_semi, r);
+        if (r[0] * r[1] * r[2] == 1) break;
+        if (dims.size() > 1 && (long long)n3[0] * n3[1] * n3[2] <= kDirectBottom) break;
+        for (int d = 0; d < 3; ++d) {
+            if (r[d] != 1 && r[d] != 2) throw KsError(KS_ERR_UNSUPPORTED, "MAC semicoarsening ratio");
+            n3[d] /= r[d];
+            h[d] *= r[d];
+        }
+        if (r[0] * r[1] * r[2] != 8) partial = true;
+    }
+    if (!partial) return;
+    size_t tot = 0;
+    for (size_t l = 1; l < dims.size(); ++l) tot += 3 * (size_t)dims[l][0] * dims[l][1] * dims[l][2];
+    mgbufs_.alloc(tot);
+    double* q = mgbufs_.p;
+    ccs_.clear();
+    ccs_.push_back(cc_[0]);
+    ccs_[0].binv = nullptr;
+    double hl[3] = {g_.dx, g_.dy, g_.dz};
+    for (size_t l = 1; l < dims.size(); ++l) {
+        const CCLevelDev& F = ccs_.back();
+        CCLevelDev C{};
+        C.nx = dims[l][0]; C.ny = dims[l][1]; C.nz = dims[l][2]; C.zper = g_.zper;
+        // the restriction and prolongation kernels index F = r C, r in {1, 2}
+        const int fn[3] = {F.nx, F.ny, F.nz}, cn[3] = {C.nx, C.ny, C.nz};
+        for (int d = 0; d < 3; ++d) {
+            if (fn[d] != cn[d] && fn[d] != 2 * cn[d]) throw KsError(KS_ERR_UNSUPPORTED, "MAC semicoarsening level sizes");
+            hl[d] *= fn[d] / cn[d];
+        }
+        C.ix2 = 1.0 / (hl[0] * hl[0]); C.iy2 = 1.0 / (hl[1] * hl[1]); C.iz2 = 1.0 / (hl[2] * hl[2]);
+        const size_t nc = (size_t)C.nx * C.ny * C.nz;
+        C.phi = q; q += nc; C.rhs = q; q += nc; C.res = q; q += nc;
+        ccs_.push_back(C);
+    }
+    binv_ccs_h_.clear();
+    CCLevelDev& B = ccs_.back();
+    if (ccs_.size() > 1 && (long long)B.nx * B.ny * B.nz <= kDirectBottom) cc_direct_inverse(B, binv_ccs_h_);
+    binvs_.alloc(std::max<size_t>(1, binv_ccs_h_.size()));
+    if (!binv_ccs_h_.empty())
+        ck(cudaMemcpy(binvs_.p, binv_ccs_h_.data(), binv_ccs_h_.size() * sizeof(double), cudaMemcpyHostToDevice), "H2D bottom inverse");
+    B.binv = binv_ccs_h_.empty() ? nullptr : binvs_.p;
+    glev_s_ = 0;
+    for (size_t l = 1; l + 1 < ccs_.size(); ++l)
+        if ((long long)ccs_[l].nx * ccs_[l].ny * ccs_[l].nz <= (1LL << 18)) {
+            glev_s_ = l;
+            break;
+        }
+    mac_semi_ = true;
+}
+
+// FP32 copies of the semicoarsened MAC levels (mixed precision); level 0 is
+// cc32_[0].
+void Sim::mac_semi_mixed() {
+    size_t tot = 0;
+    for (size_t l = 1; l < ccs_.size(); ++l) tot += 3 * (size_t)ccs_[l].nx * ccs_[l].ny * ccs_[l].nz;
+    mgbufs32_.alloc(tot);
+    float* q = mgbufs32_.p;
+    ccs32_.clear();
+    ccs32_.push_back(cc32_[0]);
+    ccs32_[0].binv = nullptr;
+    for (size_t l = 1; l < ccs_.size(); ++l) {
+        CCLevelT<float> C{};
+        C.nx = ccs_[l].nx; C.ny = ccs_[l].ny; C.nz = ccs_[l].nz; C.zper = ccs_[l].zper;
+        C.ix2 = (float)ccs_[l].ix2; C.iy2 = (float)ccs_[l].iy2; C.iz2 = (float)ccs_[l].iz2;
+        const size_t nc = (size_t)C.nx * C.ny * C.nz;
+        C.phi = q; q += nc; C.rhs = q; q += nc; C.res = q; q += nc;
+        ccs32_.push_back(C);
+    }
+    std::vector<float> b32(binv_ccs_h_.size());
+    for (size_t m = 0; m < binv_ccs_h_.size(); ++m) b32[m] = (float)binv_ccs_h_[m];
+    binvs32_.alloc(std::max<size_t>(1, b32.size()));
+    if (!b32.empty()) ck(cudaMemcpy(binvs32_.p, b32.data(), b32.size() * sizeof(float), cudaMemcpyHostToDevice), "H2D bottom inverse");
+    ccs32_.back().binv = b32.empty() ? nullptr : binvs32_.p;
 }
 
 // ---------------------------------------------------------------- allocation
@@ -603,6 +719,7 @@ void Sim::alloc() {
             glev_ = l;
             break;
         }
+    if (mac_.semi) mac_semi_setup();
     parts_.alloc(4 * 1216);
     red_.alloc(8);
     if (temp_ || S_.ablf) layer_.alloc(3 * (size_t)g_.nz);
@@ -896,7 +1013,8 @@ void Sim::mg_graph_run(MGGraph& G, double key, F&& body) {
 template <typename T>
 void Sim::cc_vcycle(std::vector<CCLevelT<T>>& Ls, size_t l, double beta, bool in_graph) {
     CCLevelT<T>& L = Ls[l];
-    if (!in_graph && mg_graphs_ && glev_ > 0 && l == glev_) {
+    const size_t gl = mac_semi_ ? glev_s_ : glev_;  // the MAC solve uses one hierarchy for the life of the handle
+    if (!in_graph && mg_graphs_ && gl > 0 && l == gl) {
         mg_graph_run(gcc_[sizeof(T) == 4 ? 1 : 0], beta, [&]() { cc_vcycle(Ls, l, beta, true); });
         return;
     }
@@ -966,11 +1084,14 @@ void Sim::set_mixed(int on) {
     if (!b32.empty()) ck(cudaMemcpy(binv32_.p, b32.data(), b32.size() * sizeof(float), cudaMemcpyHostToDevice), "H2D bottom inverse");
     cc32_.back().binv = binv_cc_h_.empty() ? nullptr : binv32_.p;
     nd32_.back().binv = binv_nd_h_.empty() ? nullptr : binv32_.p + binv_cc_h_.size();
+    if (mac_semi_) mac_semi_mixed();
 }
 
 void Sim::mac_project() {
     const double beta = 1.0 / rho_;
-    for (auto& L : cc_) {
+    std::vector<CCLevelDev>& M = mac_semi_ ? ccs_ : cc_;
+    std::vector<CCLevelT<float>>& M32 = mac_semi_ ? ccs32_ : cc32_;
+    for (auto& L : M) {
         const double d0 = 2.0 * L.ix2 + 2.0 * L.iy2;
         L.inv_diag[0] = 1.0 / (-beta * (d0 + 2.0 * L.iz2));
         L.inv_diag[1] = 1.0 / (-beta * (d0 + L.iz2));
@@ -983,13 +1104,13 @@ void Sim::mac_project() {
             L.gs[m][2] = L.iz2 / dc[m];
         }
     }
-    for (size_t l = 0; l < cc32_.size(); ++l)
+    for (size_t l = 0; l < M32.size(); ++l)
         for (int m = 0; m < 3; ++m) {
-            cc32_[l].inv_diag[m] = (float)cc_[l].inv_diag[m];
-            cc32_[l].dg[m] = (float)cc_[l].dg[m];
-            for (int q = 0; q < 3; ++q) cc32_[l].gs[m][q] = (float)cc_[l].gs[m][q];
+            M32[l].inv_diag[m] = (float)M[l].inv_diag[m];
+            M32[l].dg[m] = (float)M[l].dg[m];
+            for (int q = 0; q < 3; ++q) M32[l].gs[m][q] = (float)M[l].gs[m][q];
         }
-    CCLevelDev& L = cc_[0];
+    CCLevelDev& L = M[0];
     int np = 0;
     launch_mac_rhs(ctx_, g_, umac_[0].p, umac_[1].p, umac_[2].p, L.rhs, parts_.p, &np);
     launch_reduce(ctx_, parts_.p, np, 1, 0, red_.p);
@@ -1005,12 +1126,12 @@ void Sim::mac_project() {
     // mixed precision: each FP64 residual is the next FP32 cycle's right-hand side
     int zc = -1;  // the colour whose residual is zero (none for the starting iterate)
     auto resid = [&]() {
-        if (mixed_) launch_cc_resid32(ctx_, L, beta, cc32_[0].rhs, cc32_[0].phi, parts_.p, &np);
+        if (mixed_) launch_cc_resid32(ctx_, L, beta, M32[0].rhs, M32[0].phi, parts_.p, &np);
         else launch_cc_resid(ctx_, L, beta, parts_.p, &np, zc);
     };
     resid();
     // after a V-cycle the last half-sweep was colour 1's (post-smoothing on a level above the bottom)
-    if (mac_.nu2 > 0 && cc_.size() > 1) zc = 1;
+    if (mac_.nu2 > 0 && M.size() > 1) zc = 1;
     const double r0 = reduce(np, 1, 1, nullptr);
     mac_r0_ = r0;
     const double target = std::max(mac_.atol, mac_.rtol * std::max(bnorm, r0));
@@ -1021,10 +1142,10 @@ void Sim::mac_project() {
         int inner = 1;
         if (mixed_) {  // up to mg_inner_ FP32 V-cycles on the correction equation (as the nodal solve)
             inner = std::min(mg_inner_, mac_.maxiter - it);
-            for (int c = 0; c < inner; ++c) cc_vcycle(cc32_, 0, beta);
-            launch_add_f32(ctx_, L.phi, cc32_[0].phi, g_.N);
+            for (int c = 0; c < inner; ++c) cc_vcycle(M32, 0, beta);
+            launch_add_f32(ctx_, L.phi, M32[0].phi, g_.N);
         } else {
-            cc_vcycle(cc_, 0, beta);
+            cc_vcycle(M, 0, beta);
         }
         resid();
         rn = reduce(np, 1, 1, nullptr);
@@ -1669,6 +1790,16 @@ double Sim::scalar(const std::string& n) {
     if (n == "step") return t_.step;
     if (n == "mac_iters") return mac_it_;
     if (n == "nodal_iters") return nod_it_;
+    if (n == "mac_levels") return (double)(mac_semi_ ? ccs_ : cc_).size();
+    if (n.rfind("mac_level:", 0) == 0) {  // mac_level:l:d, cells of MAC level l in direction d
+        const std::vector<CCLevelDev>& M = mac_semi_ ? ccs_ : cc_;
+        const size_t c = n.find(':', 10);
+        if (c == std::string::npos) throw KsError(KS_ERR_ARG, "scalar " + n);
+        const size_t l = (size_t)std::stoul(n.substr(10, c - 10));
+        const int d = std::stoi(n.substr(c + 1));
+        if (l >= M.size() || d < 0 || d > 2) throw KsError(KS_ERR_ARG, "scalar " + n);
+        return d == 0 ? M[l].nx : (d == 1 ? M[l].ny : M[l].nz);
+    }
     if (n == "diff_iters") return dif_it_;
     if (n == "diff_res0") return dif_r0_;
     if (n == "diff_res") return dif_r_;

@@ -3,7 +3,8 @@
 // MAC projection (cell-centred, 7-point, beta = 1/rho0): red-black
 // Gauss-Seidel with the exact local solve at Neumann z walls, residual with a
 // max-norm partial, 8-cell average restriction, piecewise-constant
-// prolongation, single-CTA bottom sweeps.
+// prolongation (2- or 4-cell averages where the hierarchy is semicoarsened),
+// single-CTA bottom sweeps.
 //
 // Nodal projection (node-centred, 27-point Q1 finite-element Laplacian times
 // sigma = dt/rho0): weighted Jacobi, residual, full-weighting restriction
@@ -313,6 +314,35 @@ __global__ void k_cc_prolong(CCLevelT<T> F, CCLevelT<T> C) {
     int i, j, k;
     split3(t, (unsigned)F.nx, (unsigned)F.ny, i, j, k);
     F.phi[t] += C.phi[ci3(C, i / 2, j / 2, k / 2)];
+}
+
+// The same pair between levels of a semicoarsened hierarchy: ratio rx, ry, rz
+// (1 or 2 each) per direction, F.n = r C.n in every direction (checked where
+// the hierarchy is built), w = 1 / (rx ry rz).  The fine cells of a coarse
+// cell are summed z-, y-, x-outermost-first, as the oracle sums them.
+template <typename T>
+__global__ void k_cc_restrict_r(CCLevelT<T> F, CCLevelT<T> C, int rx, int ry, int rz, T w) {
+    const unsigned N = (unsigned)(C.nx * C.ny * C.nz);
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N) return;
+    int i, j, k;
+    split3(t, (unsigned)C.nx, (unsigned)C.ny, i, j, k);
+    T s = T(0);
+    for (int c = 0; c < rz; ++c)
+        for (int b = 0; b < ry; ++b)
+            for (int a = 0; a < rx; ++a) s += F.res[ci3(F, rx * i + a, ry * j + b, rz * k + c)];
+    C.rhs[t] = w * s;
+    C.phi[t] = T(0);
+}
+
+template <typename T>
+__global__ void k_cc_prolong_r(CCLevelT<T> F, CCLevelT<T> C, int rx, int ry, int rz) {
+    const unsigned N = (unsigned)(F.nx * F.ny * F.nz);
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N) return;
+    int i, j, k;
+    split3(t, (unsigned)F.nx, (unsigned)F.ny, i, j, k);
+    F.phi[t] += C.phi[ci3(C, i / rx, j / ry, k / rz)];
 }
 
 // Bottom solve: red-black sweeps by one CTA.  Levels of up to BOTTOM_SMEM
@@ -1053,13 +1083,30 @@ void launch_nd_resid32(Ctx& c, const NDLevelT<double>& L, double sigma, float* r
     KS_LAUNCH(c, (k_nd_col<double, 2>), n, BS, 8.0 * 2.0 * nnd(L) + 8.0 * nnd(L), L, nd_coef(L, sigma, 0.0), (const double*)L.phi,
               (double*)nullptr, kc, parts, r32, z32);
 }
+// full coarsening (2 in every direction) or a semicoarsened pair, whose
+// ratios the hierarchy's construction has checked to be 1 or 2 with F.n = r C.n
+template <typename T>
+inline bool cc_full_ratio(const CCLevelT<T>& F, const CCLevelT<T>& C) {
+    return F.nx == 2 * C.nx && F.ny == 2 * C.ny && F.nz == 2 * C.nz;
+}
 template <typename T>
 void launch_cc_restrict(Ctx& c, const CCLevelT<T>& F, const CCLevelT<T>& C) {
-    KS_LAUNCH(c, k_cc_restrict<T>, nblocks((long long)C.nx * C.ny * C.nz, BS), BS, sizeof(T) * (ncc(F) + 2.0 * ncc(C)), F, C);
+    if (cc_full_ratio(F, C)) {
+        KS_LAUNCH(c, k_cc_restrict<T>, nblocks((long long)C.nx * C.ny * C.nz, BS), BS, sizeof(T) * (ncc(F) + 2.0 * ncc(C)), F, C);
+        return;
+    }
+    const int rx = F.nx / C.nx, ry = F.ny / C.ny, rz = F.nz / C.nz;
+    KS_LAUNCH(c, k_cc_restrict_r<T>, nblocks((long long)C.nx * C.ny * C.nz, BS), BS, sizeof(T) * (ncc(F) + 2.0 * ncc(C)), F, C, rx, ry,
+              rz, T(1.0 / (rx * ry * rz)));
 }
 template <typename T>
 void launch_cc_prolong(Ctx& c, const CCLevelT<T>& F, const CCLevelT<T>& C) {
-    KS_LAUNCH(c, k_cc_prolong<T>, nblocks((long long)F.nx * F.ny * F.nz, BS), BS, sizeof(T) * (2.0 * ncc(F) + ncc(C)), F, C);
+    if (cc_full_ratio(F, C)) {
+        KS_LAUNCH(c, k_cc_prolong<T>, nblocks((long long)F.nx * F.ny * F.nz, BS), BS, sizeof(T) * (2.0 * ncc(F) + ncc(C)), F, C);
+        return;
+    }
+    KS_LAUNCH(c, k_cc_prolong_r<T>, nblocks((long long)F.nx * F.ny * F.nz, BS), BS, sizeof(T) * (2.0 * ncc(F) + ncc(C)), F, C,
+              F.nx / C.nx, F.ny / C.ny, F.nz / C.nz);
 }
 template <typename T>
 void launch_cc_bottom(Ctx& c, const CCLevelT<T>& L, double beta, int sweeps) {

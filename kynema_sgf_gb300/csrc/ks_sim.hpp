@@ -170,6 +170,8 @@ struct MGParams {
     double rtol = 1.0e5 * 2.220446049250313e-16, atol = 1.0e2 * 2.220446049250313e-16;
     int maxiter = 200, nu1 = 2, nu2 = 2, bottom = 100;
     int fixed_iters = 1;  // MLMGOptions do_fixed_iters: stop at maxiter without an error
+    int semi = 0;         // MLMGOptions do_semicoarsening (honoured by the MAC solve)
+    int max_semi = 1 << 30;  // max_semicoarsening_level: coarsenings that may be partial
     double omega = 0.9;
 };
 
@@ -395,6 +397,19 @@ class Sim {
     DevBuf<float> g32_;  // mixed precision: FP32 copies of the advection inputs
     GodunovIn32 in32_{};
     void bottom_setup();
+    // MAC semicoarsening (mac_proj.do_semicoarsening): the MAC solve's own
+    // hierarchy, used in place of cc_ / cc32_ when some coarsening is partial.
+    // Its level 0 shares cc_[0]'s (and cc32_[0]'s) arrays; cc_ keeps the full
+    // coarsening the diffusion solve and the nodal sizes follow.
+    void mac_semi_setup();
+    void mac_semi_mixed();
+    bool mac_semi_ = false;
+    size_t glev_s_ = 0;  // first graphed level of ccs_ (0: none)
+    std::vector<CCLevelDev> ccs_;
+    std::vector<CCLevelT<float>> ccs32_;
+    std::vector<double> binv_ccs_h_;
+    DevBuf<double> mgbufs_, binvs_;
+    DevBuf<float> mgbufs32_, binvs32_;
     int mg_warm_ = 1;          // ks.mg_warm_start
     bool mac_prev_ok_ = false; // mac_phi_prev_ holds the last MAC potential
     DevBuf<double> mac_phi_prev_;

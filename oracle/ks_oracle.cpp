@@ -29,6 +29,7 @@
 #include "ks_oracle.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -196,6 +197,7 @@ struct MGOpts {
     int maxiter = 200, nu1 = 2, nu2 = 2, bottom = 100;
     double omega = 0.9;  // nodal Jacobi weight
     int fixed_iters = 1;  // MLMGOptions do_fixed_iters: stop at maxiter without an error
+    int semicoarsening = 0, max_semi = 1 << 30;  // do_semicoarsening, max_semicoarsening_level
 };
 
 struct SimTime {
@@ -294,6 +296,7 @@ struct Sim {
     Arr theta, theta_old, theta_nph, alpha, tsrc, tdiff, tdiff_new, tconv, tconv_old;
     Arr umac, vmac, wmac;
     int mac_iters = 0, nodal_iters = 0;
+    std::vector<std::array<int, 3>> mac_dims;  // cells per level of the last MAC hierarchy
     double mac_res0 = 0, mac_res = 0, nodal_res0 = 0, nodal_res = 0;
     int diff_iters = 0;
     double diff_res0 = 0, diff_res = 0, diff_bnorm = 0;
@@ -484,6 +487,8 @@ void Sim::setup(const std::string& text) {
         o.nu1 = D.i(pfx + ".num_pre_smooth", o.nu1);
         o.nu2 = D.i(pfx + ".num_post_smooth", o.nu2);
         o.fixed_iters = D.i(pfx + ".do_fixed_iters", o.fixed_iters);
+        o.semicoarsening = D.i(pfx + ".do_semicoarsening", o.semicoarsening);
+        o.max_semi = D.i(pfx + ".max_semicoarsening_level", o.max_semi);
     };
     rd(mac, "mac_proj");
     rd(nod, "nodal_proj");
@@ -1301,9 +1306,31 @@ void Sim::premac(double dt) {
 }
 
 // ---- multigrid: cell-centred 7-point Poisson -----------------------------------------------------
+// Coarsening ratio of one level to the next (1 or 2 per direction).  Full
+// coarsening needs every count divisible by 4 (the coarse count stays even).
+// Semicoarsening (MLMGOptions do_semicoarsening, src/core/MLMGOptions.cpp:24-28)
+// halves only the directions of smallest spacing while the spacings differ,
+// each of them divisible by 4; with equal spacings, or when one of them is not
+// divisible, the level coarsens fully or not at all as without it.
+static void semi_ratio(const int n[3], const double h[3], bool semi, int r[3]) {
+    const double hmin = std::min(h[0], std::min(h[1], h[2])), hmax = std::max(h[0], std::max(h[1], h[2]));
+    bool full = true;
+    for (int d = 0; d < 3; ++d) full = full && (n[d] % 4 == 0);
+    if (semi && hmax > 1.0000001 * hmin) {
+        bool ok = true;
+        for (int d = 0; d < 3; ++d) {
+            r[d] = (h[d] <= 1.0000001 * hmin) ? 2 : 1;
+            if (r[d] == 2 && n[d] % 4 != 0) ok = false;
+        }
+        if (ok) return;
+    }
+    for (int d = 0; d < 3; ++d) r[d] = full ? 2 : 1;
+}
+
 struct CCLevel {
     int n[3];
     double h[3];
+    int r[3] = {2, 2, 2};  // coarsening ratio to the next level
     Arr phi, rhs, res;
 };
 
@@ -1374,26 +1401,28 @@ static void cc_vcycle(std::vector<CCLevel>& Ls, size_t l, double beta, bool zper
     cc_smooth(L, beta, zper, o.nu1);
     cc_residual(L, beta, zper);
     CCLevel& C = Ls[l + 1];
+    const int rx = L.r[0], ry = L.r[1], rz = L.r[2];
+    const double w = 1.0 / (rx * ry * rz);
 #pragma omp parallel for collapse(2)
     for (int k = 0; k < C.n[2]; ++k)
         for (int j = 0; j < C.n[1]; ++j)
             for (int i = 0; i < C.n[0]; ++i) {
                 double s = 0;
-                for (int c = 0; c < 2; ++c)
-                    for (int b = 0; b < 2; ++b)
-                        for (int a = 0; a < 2; ++a) s += L.res(2 * i + a, 2 * j + b, 2 * k + c);
-                C.rhs(i, j, k) = 0.125 * s;
+                for (int c = 0; c < rz; ++c)
+                    for (int b = 0; b < ry; ++b)
+                        for (int a = 0; a < rx; ++a) s += L.res(rx * i + a, ry * j + b, rz * k + c);
+                C.rhs(i, j, k) = w * s;
                 C.phi(i, j, k) = 0.0;
             }
     cc_vcycle(Ls, l + 1, beta, zper, o);
 #pragma omp parallel for collapse(2)
     for (int k = 0; k < L.n[2]; ++k)
         for (int j = 0; j < L.n[1]; ++j)
-            for (int i = 0; i < L.n[0]; ++i) L.phi(i, j, k) += C.phi(i / 2, j / 2, k / 2);
+            for (int i = 0; i < L.n[0]; ++i) L.phi(i, j, k) += C.phi(i / rx, j / ry, k / rz);
     cc_smooth(L, beta, zper, o.nu2);
 }
 
-static std::vector<CCLevel> cc_levels(const Geo& g) {
+static std::vector<CCLevel> cc_levels(const Geo& g, const MGOpts& o) {
     std::vector<CCLevel> Ls;
     int n[3] = {g.n[0], g.n[1], g.n[2]};
     double h[3] = {g.dx[0], g.dx[1], g.dx[2]};
@@ -1403,11 +1432,11 @@ static std::vector<CCLevel> cc_levels(const Geo& g) {
         L.phi.define(-1, -1, -1, n[0], n[1], n[2], 1);
         L.rhs.define(0, 0, 0, n[0] - 1, n[1] - 1, n[2] - 1, 1);
         L.res.define(0, 0, 0, n[0] - 1, n[1] - 1, n[2] - 1, 1);
+        semi_ratio(n, h, o.semicoarsening && (int)Ls.size() < o.max_semi, L.r);
+        const bool can = L.r[0] + L.r[1] + L.r[2] > 3;
         Ls.push_back(std::move(L));
-        bool can = true;
-        for (int d = 0; d < 3; ++d) can = can && (n[d] % 4 == 0);
         if (!can) break;
-        for (int d = 0; d < 3; ++d) { n[d] /= 2; h[d] *= 2; }
+        for (int d = 0; d < 3; ++d) { n[d] /= Ls.back().r[d]; h[d] *= Ls.back().r[d]; }
     }
     return Ls;
 }
@@ -1418,7 +1447,9 @@ void Sim::mac_project() {
     const int nx = g.n[0], ny = g.n[1], nz = g.n[2];
     const bool zper = g.per[2];
     const double beta = 1.0 / rho;
-    std::vector<CCLevel> Ls = cc_levels(g);
+    std::vector<CCLevel> Ls = cc_levels(g, mac);
+    mac_dims.clear();
+    for (const CCLevel& C : Ls) mac_dims.push_back({C.n[0], C.n[1], C.n[2]});
     CCLevel& L = Ls[0];
     double sum = 0;
 #pragma omp parallel for collapse(2) reduction(+ : sum)
@@ -2871,6 +2902,12 @@ double kso_get_scalar(void* h, const char* name) {
     if (n == "dt_nm1") return s.t.dt[1];
     if (n == "step") return s.t.step;
     if (n == "mac_iters") return s.mac_iters;
+    if (n == "mac_levels") return (double)s.mac_dims.size();
+    if (n.rfind("mac_level:", 0) == 0) {  // mac_level:l:d, cells of MAC level l in direction d
+        const size_t c = n.find(':', 10);
+        if (c == std::string::npos) throw kso::Error(kso::ERR_ARG, "scalar " + n);
+        return s.mac_dims.at((size_t)std::stoul(n.substr(10, c - 10))).at((size_t)std::stoul(n.substr(c + 1)));
+    }
     if (n == "nodal_iters") return s.nodal_iters;
     if (n == "mac_res0") return s.mac_res0;
     if (n == "mac_res") return s.mac_res;
