@@ -35,17 +35,21 @@ sys.path.insert(0, ROOT)
 METRIC = "Mcell-steps/s at 256^3 (FP64 vs mixed-precision at stated error) + adjoint/forward cost ratio"
 UNIT = "Mcell-steps/s"
 # the ABL box: 256 x 256 x 128 cells on 5120 x 5120 x 1280 m, i.e. 20 x 20 x 10 m cells
-# (other --size values keep the cell size)
+# (other --size values keep the cell size; --dz changes the vertical one)
 ABL_DZ = 10.0
-WORKLOAD = "ABL LES 256x256x128 FP64 (5120x5120x1280 m: 20x20x10 m cells, Smagorinsky, geostrophic+Coriolis, wall model, CFL 0.9)"
 CPU_SAMPLE = (128, 128, 64)  # same dx, physics and deck as the workload, 1/8 of the cells
 DATA = "synthetic (log-law + seeded uniform noise, SplitMix64 seed 42)"
 
 
-def workload_config(size, world=1):
+def workload(dz):
+    return ("ABL LES 256x256x128 FP64 (5120x5120x%g m: 20x20x%g m cells, Smagorinsky, geostrophic+Coriolis, wall model, CFL 0.9)"
+            % (128 * dz, dz))
+
+
+def workload_config(size, dz, world=1):
     """The `config` object both arms print (the workload, not a measurement)."""
-    return {"workload": WORKLOAD, "cells": list(size), "parallelism": "replicas" if world > 1 else "single GPU",
-            "l2": "state larger than L2 (no flush)"}
+    return {"workload": workload(dz), "cells": list(size), "cell_size_m": [20.0, 20.0, dz],
+            "parallelism": "replicas" if world > 1 else "single GPU", "l2": "state larger than L2 (no flush)"}
 # FP64 flops per algorithmic byte (an FMA counts 2) of the kernels that can dominate the FP64 step:
 # nodal column sweep 20 flops per node (5 plane sums, 3 pair sums, 5 FMAs from the right-hand side,
 # 1 FMA update) over 24 bytes; residual form 18; red-black update 10 flops over 16 bytes
@@ -73,6 +77,7 @@ def parse():
     p.add_argument("--c4-fd-h", default="1e-6,1e-8", help="finite-difference steps for the 2-disk gradient check")
     p.add_argument("--profile-all", action="store_true", help="print the per-kernel breakdown to stderr")
     p.add_argument("--size", default="256,256,128")
+    p.add_argument("--dz", type=float, default=ABL_DZ, help="vertical cell size of the ABL workloads in m (20 m horizontal)")
     p.add_argument("--cpu-worker", default="", help=argparse.SUPPRESS)
     return p.parse_args()
 
@@ -96,23 +101,24 @@ def replica_throughput(cells, steps, world, seconds):
 
 # ---------------------------------------------------------------- CPU side
 def cpu_worker(spec):
-    """Runs in a child process: times the oracle.  spec = "warm,steps,repeats,nx,ny,nz[,case]":
-    `repeats` fresh runs of the ABL deck on nx x ny x nz cells (or the 64^3
+    """Runs in a child process: times the oracle.  spec = "warm,steps,repeats,nx,ny,nz,dz[,case]":
+    `repeats` fresh runs of the ABL deck on nx x ny x nz cells of 20 x 20 x dz m (or the 64^3
     Taylor-Green case, or the MOL form of the ABL deck), each timing `steps`
     Evolve steps after `warm` untimed ones, initialisation skipped."""
     parts = spec.split(",")
     warm, steps, repeats = int(parts[0]), int(parts[1]), int(parts[2])
     nx, ny, nz = int(parts[3]), int(parts[4]), int(parts[5])
-    case = parts[6] if len(parts) > 6 else ""
+    dz = float(parts[6])
+    case = parts[7] if len(parts) > 7 else ""
     from kynema_sgf_gb300 import decks
     from oracle.oracle import Oracle
     skip_init = "\nincflo.do_initial_proj = 0\nincflo.initial_iterations = 0\n"
-    deck = decks.abl(nx, ny, nz, steps=10 ** 6, dz=ABL_DZ) + skip_init
+    deck = decks.abl(nx, ny, nz, steps=10 ** 6, dz=dz) + skip_init
     if case == "tgv":
         nx = ny = nz = 64
         deck = decks.tgv(64, steps=10 ** 6)
     if case == "mol":
-        deck = decks.mol(decks.abl(nx, ny, nz, steps=10 ** 6, cfl=0.45, dz=ABL_DZ)) + skip_init
+        deck = decks.mol(decks.abl(nx, ny, nz, steps=10 ** 6, cfl=0.45, dz=dz)) + skip_init
     runs = []
     for _ in range(repeats):
         o = Oracle(deck)
@@ -151,14 +157,14 @@ def cpu_model():
     return {"model": name, "logical_cores": os.cpu_count(), "machine": platform.machine()}
 
 
-def run_cpu(warm, steps, repeats=1, size=CPU_SAMPLE, case=""):
+def run_cpu(warm, steps, repeats=1, size=CPU_SAMPLE, case="", dz=ABL_DZ):
     """Time the oracle on all host cores in a child process; returns (cells,
     per-run Mcell-steps/s list, per-run step times, cores)."""
     from oracle import oracle as orc
     orc.build()
     cores = os.cpu_count() or 1
     env = dict(os.environ, OMP_NUM_THREADS=str(cores), OMP_PROC_BIND="spread", OMP_PLACES="cores")
-    spec = "%d,%d,%d,%d,%d,%d" % ((warm, steps, repeats) + tuple(size)) + ("," + case if case else "")
+    spec = "%d,%d,%d,%d,%d,%d,%r" % ((warm, steps, repeats) + tuple(size) + (float(dz),)) + ("," + case if case else "")
     r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-worker", spec],
                        capture_output=True, text=True, env=env, cwd=ROOT)
     if r.returncode != 0:
@@ -169,12 +175,12 @@ def run_cpu(warm, steps, repeats=1, size=CPU_SAMPLE, case=""):
     return cells, rates, out["runs"], cores
 
 
-def cpu_baseline_entry(warm, steps, repeats, size=CPU_SAMPLE, case="", what=None):
+def cpu_baseline_entry(warm, steps, repeats, size=CPU_SAMPLE, case="", what=None, dz=ABL_DZ):
     """The median over `repeats` fresh runs of the oracle's rate."""
-    cells, rates, runs, cores = run_cpu(warm, steps, repeats, size, case)
+    cells, rates, runs, cores = run_cpu(warm, steps, repeats, size, case, dz)
     nx, ny, nz = size if case != "tgv" else (64, 64, 64)
-    what = what or ("CPU restatement (oracle/ks_oracle.cpp, g++ -O3 -fopenmp) on %dx%dx%d cells of the same ABL deck (same dx and "
-                    "physics%s)" % (nx, ny, nz, ", 1/8 of the cells" if (nx, ny, nz) == CPU_SAMPLE else ""))
+    what = what or ("CPU restatement (oracle/ks_oracle.cpp, g++ -O3 -fopenmp) on %dx%dx%d cells of the same ABL deck (same cell size "
+                    "20x20x%g m and physics%s)" % (nx, ny, nz, dz, ", 1/8 of the cells" if (nx, ny, nz) == CPU_SAMPLE else ""))
     return {"value": statistics.median(rates), "unit": UNIT, "cores": cores, "kind": "port",
             "sample": "%s; median of %d fresh runs, each %d timed Evolve steps after %d untimed, initialisation skipped"
                       % (what, repeats, steps, warm),
@@ -254,7 +260,7 @@ def our_arm(args, rank, world, local_rank):
         import torch.distributed as tdist
     torch.cuda.set_device(local_rank)
     nx, ny, nz = (int(x) for x in args.size.split(","))
-    sim = ks.Incflo(decks.abl(nx, ny, nz, steps=10 ** 9, dz=ABL_DZ))
+    sim = ks.Incflo(decks.abl(nx, ny, nz, steps=10 ** 9, dz=args.dz))
     sim.InitData()
     cells = sim.scalar("ncells")
     # warm-up; the last warm-up step times every kernel to pick the dominant one
@@ -382,7 +388,7 @@ def c2_bench(args, torch, ks, decks, nx, ny, nz, world, rank, fp64_ms_main):
     peak, peak_kind = peaks()
     res = {}
     for form in ("fp64", "mixed"):
-        deck = decks.abl(nx, ny, nz, steps=10 ** 9, dz=ABL_DZ) + ("\nks.precision = mixed\n" if form == "mixed" else "")
+        deck = decks.abl(nx, ny, nz, steps=10 ** 9, dz=args.dz) + ("\nks.precision = mixed\n" if form == "mixed" else "")
         sim = ks.Incflo(deck)
         sim.InitData()
         cells = sim.scalar("ncells")
@@ -512,7 +518,7 @@ def semi_bench(args, torch, ks, decks, nx, ny, nz, world, rank):
     reported in the line instead of raised."""
     out = {}
     for form in ("fp64", "mixed"):
-        deck = (decks.abl(nx, ny, nz, steps=10 ** 9, dz=ABL_DZ) + "\nmac_proj.do_semicoarsening = true\n" +
+        deck = (decks.abl(nx, ny, nz, steps=10 ** 9, dz=args.dz) + "\nmac_proj.do_semicoarsening = true\n" +
                 ("ks.precision = mixed\n" if form == "mixed" else ""))
         try:
             out[form] = variant_bench(args, torch, ks, deck, "ABL %dx%dx%d, MAC semicoarsening, %s" % (nx, ny, nz, form), world, rank,
@@ -527,7 +533,7 @@ def mol_bench(args, torch, ks, decks, nx, ny, nz, world, rank):
     """The ABL workload advanced with the MOL predictor-corrector
     (incflo.use_godunov = false, explicit diffusion) at CFL 0.45 (MOL requires
     <= 0.5): two MAC and two nodal projections per step."""
-    out = variant_bench(args, torch, ks, decks.mol(decks.abl(nx, ny, nz, steps=10 ** 9, cfl=0.45, dz=ABL_DZ)),
+    out = variant_bench(args, torch, ks, decks.mol(decks.abl(nx, ny, nz, steps=10 ** 9, cfl=0.45, dz=args.dz)),
                         "ABL %dx%dx%d, MOL predictor-corrector, explicit diffusion, CFL 0.45, FP64" % (nx, ny, nz), world, rank, "MOL")
     out["projections_per_step"] = {"mac": 2, "nodal": 2}
     return out
@@ -538,7 +544,7 @@ def cn_bench(args, torch, ks, decks, nx, ny, nz, world, rank):
     Crank-Nicolson (incflo.diffusion_type = 1): predictor_rhs with half the old
     diffusion term and a multigrid solve of rho u - dt/2 divtau(u) per step; no
     diffusion CFL."""
-    d = decks.abl(nx, ny, nz, steps=10 ** 9, dz=ABL_DZ).replace("incflo.diffusion_type = 0", "incflo.diffusion_type = 1")
+    d = decks.abl(nx, ny, nz, steps=10 ** 9, dz=args.dz).replace("incflo.diffusion_type = 0", "incflo.diffusion_type = 1")
     return variant_bench(args, torch, ks, d, "ABL %dx%dx%d, Godunov, Crank-Nicolson diffusion, CFL 0.9, FP64" % (nx, ny, nz), world, rank,
                          "Crank-Nicolson")
 
@@ -778,7 +784,7 @@ def main():
             return
         # the full workload (not a sample): every Evolve step of the 256x256x128 deck on all host cores
         size = tuple(int(x) for x in args.size.split(","))
-        cells, rates, runs, cores = run_cpu(args.warmup, args.steps, 1, size)
+        cells, rates, runs, cores = run_cpu(args.warmup, args.steps, 1, size, dz=args.dz)
         per = runs[0]
         v = rates[0]
         what = ("CPU restatement (oracle/ks_oracle.cpp, g++ -O3 -fopenmp; the reference's own build cannot be compiled: its "
@@ -786,7 +792,7 @@ def main():
                 "initialisation skipped" % (size + (len(per), args.warmup)))
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * sum(per) / len(per), "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": DATA, "config": workload_config(size, world),
+                "vs_baseline": None, "dtype": "f64", "data": DATA, "config": workload_config(size, args.dz, world),
                 "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": what, "cpu": cpu_model()},
                 "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
@@ -810,7 +816,7 @@ def main():
     nx, ny, nz = r["size"]
     line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": DATA, "config": workload_config((nx, ny, nz), world),
+            "data": DATA, "config": workload_config((nx, ny, nz), args.dz, world),
             "solver": {"mac_vcycles_per_step": r["mac"], "nodal_vcycles_per_step": r["nodal"]},
             "divergence": r["div"],
             "roofline": {"bound": "hbm", "kernel": r["dominant"], "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -833,7 +839,7 @@ def main():
                              "frac": bstep / (r["ms"] / args.steps * 1e-3) / 1e9 / peak}
     if world == 1 and not args.no_cpu_baseline:
         try:
-            line["cpu_baseline"] = cpu_baseline_entry(1, 5, 5)
+            line["cpu_baseline"] = cpu_baseline_entry(1, 5, 5, dz=args.dz)
         except Exception as e:  # reported, never silently replaced
             line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": "failed: %s" % e}
         try:
@@ -843,7 +849,7 @@ def main():
         if r["mol"]:
             try:
                 r["mol"]["cpu"] = cpu_baseline_entry(1, 3, 3, case="mol", what="CPU restatement, MOL form of the %dx%dx%d ABL sample"
-                                                     % CPU_SAMPLE)
+                                                     % CPU_SAMPLE, dz=args.dz)
             except Exception as e:
                 r["mol"]["cpu"] = {"value": None, "sample": "failed: %s" % e}
     print(json.dumps(line))
