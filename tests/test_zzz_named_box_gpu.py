@@ -6,9 +6,12 @@ same neutral ABL deck on 128 x 128 x 64 cells of that shape (wall model,
 slip top, Smagorinsky, geostrophic + Coriolis, CFL 0.9), both solves started
 from zero, for 3 steps.
 
-On 2:1 cells the multigrid contracts slowly (the oracle takes 64 MAC and
-25-27 nodal V-cycles per step here), so a small difference in the
-contraction per cycle moves the count by more than one: the counts must
+On 2:1 cells the multigrid contracts slowly.  The oracle takes 64 MAC and
+25-27 nodal V-cycles per step here; the GPU takes about 48 MAC V-cycles
+(measured on a GB300), because it solves its coarsest MAC level (8x8x4
+cells) exactly where the oracle keeps smoothing down to 4x4x2 cells, and
+on 2:1 cells that raises the contraction per cycle.  So the GPU's MAC count
+may only be lower (at most 2 above the oracle's), and the nodal counts must
 agree to 10 % (at least 2).  The fields are insensitive to where the solves
 stop (a 100-fold tighter rtol moves the oracle's pressure by 1.3e-10 and its
 velocity by 1.8e-12 relative), so they must agree to the same 1e-9 relative
@@ -39,8 +42,9 @@ def test_abl_named_cell_shape_128x128x64(cuda_dev, oracle_mod):
     for _ in range(3):
         assert g.step() and o.step()
         assert abs(g.scalar("dt") - o.scalar("dt")) <= 1e-12 * o.scalar("dt")
-        for s in ("mac_iters", "nodal_iters"):
-            assert abs(g.scalar(s) - o.scalar(s)) <= max(2.0, 0.1 * o.scalar(s)), (s, g.scalar(s), o.scalar(s))
+        assert g.scalar("mac_iters") <= o.scalar("mac_iters") + 2, (g.scalar("mac_iters"), o.scalar("mac_iters"))
+        assert abs(g.scalar("nodal_iters") - o.scalar("nodal_iters")) <= max(2.0, 0.1 * o.scalar("nodal_iters"))
+        assert g.scalar("mac_res") <= g.scalar("mac_target") and g.scalar("nodal_res") <= g.scalar("nodal_target")
         for side in (g, o):
             assert side.scalar("mac_divu_rel") <= DIV_TOL, side.scalar("mac_divu_rel")
         dg, do = g.scalar("divu"), o.scalar("divu")
