@@ -78,6 +78,8 @@ def parse():
     p.add_argument("--profile-all", action="store_true", help="print the per-kernel breakdown to stderr")
     p.add_argument("--size", default="256,256,128")
     p.add_argument("--dz", type=float, default=ABL_DZ, help="vertical cell size of the ABL workloads in m (20 m horizontal)")
+    p.add_argument("--ref-budget", type=float, default=150.0,
+                   help="reference arm: seconds of timed CPU steps after which it stops (at least one step; 0: no limit)")
     p.add_argument("--cpu-worker", default="", help=argparse.SUPPRESS)
     return p.parse_args()
 
@@ -101,15 +103,17 @@ def replica_throughput(cells, steps, world, seconds):
 
 # ---------------------------------------------------------------- CPU side
 def cpu_worker(spec):
-    """Runs in a child process: times the oracle.  spec = "warm,steps,repeats,nx,ny,nz,dz[,case]":
+    """Runs in a child process: times the oracle.  spec = "warm,steps,repeats,nx,ny,nz,dz,budget[,case]":
     `repeats` fresh runs of the ABL deck on nx x ny x nz cells of 20 x 20 x dz m (or the 64^3
     Taylor-Green case, or the MOL form of the ABL deck), each timing `steps`
-    Evolve steps after `warm` untimed ones, initialisation skipped."""
+    Evolve steps after `warm` untimed ones, initialisation skipped.  A budget
+    above 0 (seconds) ends a run's warm-up after a quarter of it and its timed
+    steps once they have used it, after at least one."""
     parts = spec.split(",")
     warm, steps, repeats = int(parts[0]), int(parts[1]), int(parts[2])
     nx, ny, nz = int(parts[3]), int(parts[4]), int(parts[5])
-    dz = float(parts[6])
-    case = parts[7] if len(parts) > 7 else ""
+    dz, budget = float(parts[6]), float(parts[7])
+    case = parts[8] if len(parts) > 8 else ""
     from kynema_sgf_gb300 import decks
     from oracle.oracle import Oracle
     skip_init = "\nincflo.do_initial_proj = 0\nincflo.initial_iterations = 0\n"
@@ -122,13 +126,18 @@ def cpu_worker(spec):
     runs = []
     for _ in range(repeats):
         o = Oracle(deck)
+        t0 = time.perf_counter()
         for _ in range(warm):
             o.step()
+            if budget > 0 and time.perf_counter() - t0 > 0.25 * budget:
+                break
         per = []
         for _ in range(steps):
             t0 = time.perf_counter()
             o.step()
             per.append(time.perf_counter() - t0)
+            if budget > 0 and sum(per) > budget:
+                break
         runs.append(per)
         del o
     print(json.dumps({"runs": runs, "cells": nx * ny * nz}))
@@ -157,14 +166,14 @@ def cpu_model():
     return {"model": name, "logical_cores": os.cpu_count(), "machine": platform.machine()}
 
 
-def run_cpu(warm, steps, repeats=1, size=CPU_SAMPLE, case="", dz=ABL_DZ):
+def run_cpu(warm, steps, repeats=1, size=CPU_SAMPLE, case="", dz=ABL_DZ, budget=0.0):
     """Time the oracle on all host cores in a child process; returns (cells,
     per-run Mcell-steps/s list, per-run step times, cores)."""
     from oracle import oracle as orc
     orc.build()
     cores = os.cpu_count() or 1
     env = dict(os.environ, OMP_NUM_THREADS=str(cores), OMP_PROC_BIND="spread", OMP_PLACES="cores")
-    spec = "%d,%d,%d,%d,%d,%d,%r" % ((warm, steps, repeats) + tuple(size) + (float(dz),)) + ("," + case if case else "")
+    spec = "%d,%d,%d,%d,%d,%d,%r,%r" % ((warm, steps, repeats) + tuple(size) + (float(dz), float(budget))) + ("," + case if case else "")
     r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-worker", spec],
                        capture_output=True, text=True, env=env, cwd=ROOT)
     if r.returncode != 0:
@@ -782,15 +791,18 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        # the full workload (not a sample): every Evolve step of the 256x256x128 deck on all host cores
+        # the full workload (not a sample): Evolve steps of the 256x256x128 deck on all host cores, as
+        # many of --steps as fit in --ref-budget seconds (a warm-up cut short after a quarter of it)
         size = tuple(int(x) for x in args.size.split(","))
-        cells, rates, runs, cores = run_cpu(args.warmup, args.steps, 1, size, dz=args.dz)
+        cells, rates, runs, cores = run_cpu(args.warmup, args.steps, 1, size, dz=args.dz, budget=args.ref_budget)
         per = runs[0]
         v = rates[0]
         what = ("CPU restatement (oracle/ks_oracle.cpp, g++ -O3 -fopenmp; the reference's own build cannot be compiled: its "
-                "AMReX / AMReX-Hydro submodules are absent) on the full %dx%dx%d workload, %d timed Evolve steps after %d untimed, "
-                "initialisation skipped" % (size + (len(per), args.warmup)))
+                "AMReX / AMReX-Hydro submodules are absent) on the full %dx%dx%d workload, %d timed Evolve steps of the %d asked "
+                "(budget %g s) after up to %d untimed, initialisation skipped" % (size + (len(per), args.steps, args.ref_budget,
+                                                                                  args.warmup)))
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "steps_timed": len(per),
                 "warmup": args.warmup, "ms_per_step": 1e3 * sum(per) / len(per), "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": DATA, "config": workload_config(size, args.dz, world),
                 "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": what, "cpu": cpu_model()},
