@@ -334,14 +334,16 @@ def our_arm(args, rank, world, local_rank):
         hin = sum(host[f].numel() * 8 for f in host)
         e2e = {"value": replica_throughput(cells, args.steps, world, el), "unit": UNIT, "h2d_bytes_per_step": hin,
                "d2h_bytes_per_step": host["velocity"].numel() * 8}
+    # the other forms of the workload: a failure of one is reported in its entry, and the
+    # headline numbers above stand
     mixed = None
     if not args.no_mixed:
         del sim
-        mixed = c2_bench(args, torch, ks, decks, nx, ny, nz, world, rank, ms_max / args.steps)
-    mol = None if args.no_mol else mol_bench(args, torch, ks, decks, nx, ny, nz, world, rank)
-    cn = None if args.no_mol else cn_bench(args, torch, ks, decks, nx, ny, nz, world, rank)
-    strat = None if args.no_mol else stratified_bench(args, torch, ks, decks, nx, ny, nz, world, rank)
-    adj = None if args.no_adjoint else adjoint_bench(args, torch, ks, decks)
+        mixed = leg(c2_bench, args, torch, ks, decks, nx, ny, nz, world, rank, ms_max / args.steps)
+    mol = None if args.no_mol else leg(mol_bench, args, torch, ks, decks, nx, ny, nz, world, rank)
+    cn = None if args.no_mol else leg(cn_bench, args, torch, ks, decks, nx, ny, nz, world, rank)
+    strat = None if args.no_mol else leg(stratified_bench, args, torch, ks, decks, nx, ny, nz, world, rank)
+    adj = None if args.no_adjoint else leg(adjoint_bench, args, torch, ks, decks)
     # the reference's own CPU-runnable case: Taylor-Green vortex 64^3, Re 1600, CFL 0.5, 20 steps
     tg = ks.Incflo(decks.tgv(64, steps=10 ** 6))
     tg.InitData()
@@ -363,6 +365,14 @@ def our_arm(args, rank, world, local_rank):
     return dict(value=value, ms=ms_max, cells=cells, launches=launches, dominant=dominant, dom=dom, clocks=clk, e2e=e2e, fp64_peak=fp64_peak, div=div,
                 mac=statistics.mean(mac_it), nodal=statistics.mean(nod_it), size=(nx, ny, nz), mixed=mixed, adjoint=adj, tgv=tgv, mol=mol, cn=cn, strat=strat,
                 semi=semi)
+
+
+def leg(fn, *a):
+    """Run one secondary leg of the bench; an exception becomes its entry."""
+    try:
+        return fn(*a)
+    except Exception as e:  # reported in the line, never silently replaced
+        return {"failed": "%s: %s" % (type(e).__name__, str(e)[:300])}
 
 
 def divergence(sim):
